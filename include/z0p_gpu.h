@@ -1,0 +1,223 @@
+/*
+ * z0p_gpu.h — C ABI of the GB300 (sm_103a) proving backend for z0p.
+ *
+ * The backend replaces the CPU prove path of z0p (FutureProofsTech/z0p,
+ * a pure-Rust crate) behind its own API: the same parameter structs and
+ * validation rules, the same Fiat-Shamir transcript and the same VERSION=6
+ * proof bytes. Every declaration below names the reference item it stands in
+ * for (paths inside the z0p repository). All structs are plain C with fixed
+ * widths, so a `z0p-gpu-sys` crate can mirror them with #[repr(C)].
+ *
+ * Conventions
+ *  - Field elements are canonical BabyBear values (< 2013265921) as uint32_t.
+ *  - Status codes: 0 = Ok; 1..9 mirror the variants of z0p::Error in
+ *    declaration order (src/error.rs:7-40); >= 100 are backend errors.
+ *    z0p_gpu_last_reason() returns a static, thread-local message.
+ *  - Proof-producing calls write into a caller-owned host buffer. When `cap`
+ *    is too small they write the required size to *len and return
+ *    Z0P_ERR_BUFFER_TOO_SMALL before any device work.
+ *  - A context owns one CUDA stream and the device workspace; calls on one
+ *    context are serialised by an internal mutex. Outputs are deterministic.
+ */
+#ifndef Z0P_GPU_H
+#define Z0P_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define Z0P_GPU_ABI_VERSION 1
+
+/* Status codes. 1..9 follow z0p::Error (src/error.rs:7-40) in order. */
+enum {
+    Z0P_OK = 0,
+    Z0P_ERR_EMPTY_INPUT = 1,             /* Error::EmptyInput */
+    Z0P_ERR_INDEX_OUT_OF_BOUNDS = 2,     /* Error::IndexOutOfBounds */
+    Z0P_ERR_INVALID_DOMAIN_SIZE = 3,     /* Error::InvalidDomainSize */
+    Z0P_ERR_INVALID_BLOWUP = 4,          /* Error::InvalidBlowup */
+    Z0P_ERR_NO_QUERIES = 5,              /* Error::NoQueries */
+    Z0P_ERR_BAD_MERKLE_PATH = 6,         /* Error::BadMerklePath */
+    Z0P_ERR_FRI_VERIFICATION_FAILED = 7, /* Error::FriVerificationFailed */
+    Z0P_ERR_MALFORMED_INPUT = 8,         /* Error::MalformedInput */
+    Z0P_ERR_RNG_UNAVAILABLE = 9,         /* Error::RngUnavailable */
+    Z0P_ERR_BUFFER_TOO_SMALL = 100,
+    Z0P_ERR_CUDA = 101,
+    Z0P_ERR_OUT_OF_MEMORY = 102,
+    Z0P_ERR_UNSUPPORTED = 103,
+    Z0P_ERR_DEVICE_TIMEOUT = 104,        /* a bounded device wait gave up */
+    Z0P_ERR_ADMISSION = 105,             /* job larger than the HBM budget */
+    Z0P_ERR_INVALID_ARGUMENT = 106,
+    Z0P_ERR_CANCELLED = 107
+};
+
+/* air::Params (src/air.rs:31-54). usize fields are widened to uint64_t. */
+typedef struct {
+    uint64_t n_steps;
+    uint64_t blowup;
+    uint64_t num_queries;
+    uint64_t final_size;
+    uint32_t grinding_bits;
+    uint64_t cap_height;
+    uint32_t a0;
+    uint32_t b0;
+    uint32_t b_last;
+} z0p_air_params;
+
+/* range::Params (src/range.rs:30-51). */
+typedef struct {
+    uint64_t n_rows;
+    uint64_t n_bits;
+    uint64_t blowup;
+    uint64_t num_queries;
+    uint64_t final_size;
+    uint32_t grinding_bits;
+    uint64_t cap_height;
+    uint32_t value;
+} z0p_range_params;
+
+/*
+ * Transcript state (src/transcript.rs:54-57: Transcript{history: Hasher,
+ * counter}; src/hash.rs:233-240: Hasher{buf[start..], stack, stack_len,
+ * next_index, total_len}). `tail` holds the unprocessed history bytes
+ * (always < 2048 after an absorb). Exporting a z0p Transcript into this POD
+ * and importing it back after a prove call leaves it exactly where the CPU
+ * prover would have left it, so proofs can be chained on one transcript.
+ */
+typedef struct {
+    uint8_t tail[2048];
+    uint32_t tail_len;
+    uint8_t stack[54][32];
+    uint32_t stack_len;
+    uint64_t next_index;
+    uint64_t total_len;
+    uint64_t counter;
+} z0p_transcript_state;
+
+typedef struct z0p_gpu_ctx z0p_gpu_ctx;
+
+/* ------------------------------------------------------------ misc ---- */
+int z0p_gpu_abi_version(void);
+const char *z0p_gpu_last_reason(void);
+
+/* ------------------------------------------------- transcript (host) ---- */
+/* Transcript::new (src/transcript.rs:62-69). */
+int z0p_transcript_init(z0p_transcript_state *st, const uint8_t *label, size_t label_len);
+/* Transcript::absorb (src/transcript.rs:72-77). */
+int z0p_transcript_absorb(z0p_transcript_state *st, const uint8_t *label, size_t label_len,
+                          const uint8_t *data, size_t data_len);
+/* Transcript::challenge_bytes (src/transcript.rs:95-97 via squeeze_raw :162-171). */
+int z0p_transcript_challenge_bytes(z0p_transcript_state *st, const uint8_t *label,
+                                   size_t label_len, uint8_t out[32]);
+/* Transcript::challenge_ext (src/transcript.rs:136-141): 4 canonical coordinates. */
+int z0p_transcript_challenge_ext(z0p_transcript_state *st, const uint8_t *label,
+                                 size_t label_len, uint32_t out[4]);
+/* Transcript::challenge_index (src/transcript.rs:148-160); MALFORMED_INPUT
+ * where the reference returns None. */
+int z0p_transcript_challenge_index(z0p_transcript_state *st, const uint8_t *label,
+                                   size_t label_len, uint64_t domain, uint64_t *out);
+
+/* ------------------------------------------------------ params (host) ---- */
+/* air::Params::new (src/air.rs:62-102). */
+int z0p_air_params_new(uint64_t n_steps, uint64_t blowup, uint64_t num_queries,
+                       uint64_t final_size, uint32_t a0, uint32_t b0, uint32_t b_last,
+                       z0p_air_params *out);
+/* air::Params::for_security (src/air.rs:127-158). */
+int z0p_air_params_for_security(uint64_t n_steps, uint32_t a0, uint32_t b0, uint32_t b_last,
+                                uint32_t target_bits, z0p_air_params *out);
+/* range::Params::new (src/range.rs:57-99). */
+int z0p_range_params_new(uint64_t n_rows, uint64_t n_bits, uint64_t blowup,
+                         uint64_t num_queries, uint64_t final_size, uint32_t value,
+                         z0p_range_params *out);
+/* range::Params::for_security (src/range.rs:124-161). */
+int z0p_range_params_for_security(uint64_t n_rows, uint64_t n_bits, uint32_t value,
+                                  uint32_t target_bits, z0p_range_params *out);
+/* Exact length of air::Proof::to_bytes (src/air.rs:262-281) for `params`. */
+int z0p_air_proof_size(const z0p_air_params *params, size_t *len);
+/* Exact length of range::Proof::to_bytes (src/range.rs:253-269) for `params`. */
+int z0p_range_proof_size(const z0p_range_params *params, size_t *len);
+
+/* ---------------------------------------------------------- contexts ---- */
+/* Creates a prover context on CUDA device `device` (one stream, lazily grown
+ * device workspace). */
+int z0p_gpu_ctx_create(int device, z0p_gpu_ctx **out);
+void z0p_gpu_ctx_destroy(z0p_gpu_ctx *ctx);
+/* The context's cudaStream_t (as void*), for callers that time or order work. */
+void *z0p_gpu_ctx_stream(z0p_gpu_ctx *ctx);
+/* Bytes of device memory currently held by the context. */
+size_t z0p_gpu_ctx_device_bytes(z0p_gpu_ctx *ctx);
+/* Cumulative counters of a context (launches are process-wide). */
+typedef struct {
+    uint64_t launches;   /* kernels launched by this library in this process */
+    uint64_t h2d_bytes;  /* host-to-device bytes copied by this context */
+    uint64_t d2h_bytes;  /* device-to-host bytes copied by this context */
+    uint64_t syncs;      /* stream synchronisations (host round trips) */
+    uint64_t proofs;     /* proofs completed */
+} z0p_gpu_stats;
+int z0p_gpu_ctx_stats(z0p_gpu_ctx *ctx, z0p_gpu_stats *out);
+/* Diagnostic per-stage timing: while on, every kernel stage is bracketed by
+ * CUDA events on the context stream. z0p_gpu_ctx_profile writes a JSON
+ * object {"stage": {"ms": total, "calls": n}, ...} covering the stages since
+ * the previous call, then clears it. Profiling uses a process-wide hook, so
+ * only one context should profile at a time. */
+int z0p_gpu_ctx_set_profiling(z0p_gpu_ctx *ctx, int on);
+int z0p_gpu_ctx_profile(z0p_gpu_ctx *ctx, char *json, size_t cap, size_t *len);
+/* Device bytes a proof of `params` needs (the admission footprint). */
+int z0p_gpu_air_footprint(const z0p_air_params *params, size_t *bytes);
+int z0p_gpu_range_footprint(const z0p_range_params *params, size_t *bytes);
+
+/* ------------------------------------------------------------ prove ---- */
+/*
+ * air::prove (src/air.rs:365-372) followed by Proof::to_bytes
+ * (src/air.rs:262-281). `transcript` is read and advanced exactly as the
+ * reference advances its &mut Transcript.
+ */
+int z0p_gpu_air_prove(z0p_gpu_ctx *ctx, const z0p_air_params *params,
+                      z0p_transcript_state *transcript, uint8_t *out, size_t cap,
+                      size_t *len);
+/* range::prove (src/range.rs:337-343) followed by Proof::to_bytes
+ * (src/range.rs:253-269). */
+int z0p_gpu_range_prove(z0p_gpu_ctx *ctx, const z0p_range_params *params,
+                        z0p_transcript_state *transcript, uint8_t *out, size_t cap,
+                        size_t *len);
+
+/* ------------------------------------------ per-stage kernels (device) ---- */
+/*
+ * ntt::reed_solomon_extend (src/ntt.rs:436-439) over `batch` columns of
+ * length n (power of two): d_out[c*n*blowup + k] = LDE of column c at the
+ * natural-order point GENERATOR * omega_{n*blowup}^k. Device pointers; runs on
+ * the context stream and synchronises before returning.
+ */
+int z0p_gpu_rs_extend(z0p_gpu_ctx *ctx, const uint32_t *d_values, uint64_t n, uint64_t batch,
+                      uint64_t blowup, uint32_t *d_out);
+/*
+ * MerkleTree::from_flat64 (src/merkle.rs:93-110) + cap (src/merkle.rs:229-232):
+ * builds the BLAKE3 tree over len/64 64-byte leaves of the device buffer
+ * d_flat and copies cap level min(cap_height, depth) to the host buffer
+ * h_cap (2^drop * 32 bytes; *cap_count receives the digest count).
+ */
+int z0p_gpu_merkle_flat64_cap(z0p_gpu_ctx *ctx, const uint8_t *d_flat, uint64_t len,
+                              uint64_t cap_height, uint8_t *h_cap, uint64_t *cap_count);
+/*
+ * fri::fold_layer (src/fri.rs:1273-1302) for layer `depth` of an FRI stack
+ * over an LDE of length lde_len: folds n bit-reversed Ext4 values (d_in,
+ * 4*n uint32) with challenges ch[12] into n/4 values (d_out). The quad
+ * leader points are derived from (lde_len, depth) exactly as fri::point_at
+ * (src/fri.rs:1108-1115) defines them.
+ */
+int z0p_gpu_fri_fold(z0p_gpu_ctx *ctx, const uint32_t *d_in, uint64_t n, uint64_t lde_len,
+                     uint64_t depth, const uint32_t ch[12], uint32_t *d_out);
+/*
+ * Transcript::grind core (src/transcript.rs:263-281): the smallest nonce
+ * whose BLAKE3(head || LE64(nonce)) has >= bits leading zero bits, MSB first.
+ * head_len + 8 must fit one BLAKE3 block (head_len <= 56); bits <= 32.
+ */
+int z0p_gpu_grind(z0p_gpu_ctx *ctx, const uint8_t *head, size_t head_len, uint32_t bits,
+                  uint64_t *nonce);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,174 @@
+"""C-ABI host logic, checked on the CPU against the oracle (no GPU calls).
+
+Covers: the library loads and exports every symbol include/z0p_gpu.h
+declares; transcript streaming state, parameter constructors/tuners and
+proof-size arithmetic match the oracle; hostile parameters fail with the
+reference's error codes before any device work (tests/hardening.rs:21-66).
+"""
+import ctypes as C
+import os
+import random
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    src = open(os.path.join(ROOT, "include", "z0p_gpu.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(z0p_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_library_exports_every_declared_symbol(z0p):
+    L = z0p.lib()
+    names = declared_symbols()
+    assert len(names) >= 25
+    for name in names:
+        assert hasattr(L, name), name
+    assert L.z0p_gpu_abi_version() == 1
+
+
+def test_struct_layouts_match_header(z0p):
+    from z0p_gb300._lib import AirParams, RangeParams, TranscriptState
+
+    assert C.sizeof(AirParams) == 64
+    assert AirParams.cap_height.offset == 40 and AirParams.a0.offset == 48 and AirParams.b_last.offset == 56
+    assert C.sizeof(RangeParams) == 64
+    assert C.sizeof(TranscriptState) == 2048 + 4 + 54 * 32 + 4 + 24
+
+
+def test_transcript_matches_oracle(z0p, oracle):
+    for trial in range(40):
+        rnd = random.Random(trial)
+        a = oracle.Transcript(b"t%d" % trial)
+        b = z0p.Transcript(b"t%d" % trial)
+        for _ in range(rnd.randint(1, 30)):
+            op = rnd.random()
+            if op < 0.55:
+                n = rnd.choice([0, 1, 7, 8, 63, 64, 65, 1000, 1023, 1024, 1025, 2047, 2048, 4100])
+                d = bytes(rnd.getrandbits(8) for _ in range(n))
+                a.absorb(b"lbl", d)
+                b.absorb(b"lbl", d)
+            elif op < 0.75:
+                assert a.challenge_ext(b"c") == b.challenge_ext(b"c")
+            elif op < 0.9:
+                assert a.challenge_bytes(b"cb") == b.challenge_bytes(b"cb")
+            else:
+                assert a.challenge_index(b"q", 1 << 24) == b.challenge_index(b"q", 1 << 24)
+        assert a.export() == b.export()
+    t = z0p.Transcript(b"x")
+    assert t.challenge_index(b"q", 0) is None and t.challenge_index(b"q", 3) is None
+
+
+def test_streaming_equals_concatenation(z0p, oracle):
+    # src/transcript.rs:358-381
+    def frame(label, data):
+        return len(label).to_bytes(8, "little") + label + len(data).to_bytes(8, "little") + data
+
+    log = frame(b"domain", b"test") + frame(b"stmt", b"hello")
+    expected = oracle.blake3(log + (9).to_bytes(8, "little") + b"challenge" + (0).to_bytes(8, "little"))
+    t = z0p.Transcript(b"test")
+    t.absorb(b"stmt", b"hello")
+    assert t.challenge_bytes(b"challenge") == expected
+
+
+@pytest.mark.parametrize("n", [2, 4, 8, 16, 64, 1024, 8192, 1 << 16, 1 << 20, 1 << 22, 1 << 23])
+def test_air_for_security_matches_oracle(z0p, oracle, n):
+    po = oracle.air_for_security(n, 1, 2, 3, 100)
+    pz = z0p.air.Params.for_security(n, 1, 2, 3, 100)
+    for f in ("n_steps", "blowup", "num_queries", "final_size", "grinding_bits", "cap_height"):
+        assert getattr(po, f) == getattr(pz, f), f
+    po12 = oracle.air_for_security(n, 1, 1, 1, 12)
+    pz12 = z0p.air.Params.for_security(n, 1, 1, 1, 12)
+    assert (po12.num_queries, po12.grinding_bits, po12.final_size, po12.cap_height) == (
+        pz12.num_queries, pz12.grinding_bits, pz12.final_size, pz12.cap_height)
+
+
+@pytest.mark.parametrize("n,bits", [(8, 16), (1 << 12, 16), (1 << 16, 16), (1 << 18, 16), (64, 1), (64, 24)])
+def test_range_for_security_matches_oracle(z0p, oracle, n, bits):
+    po = oracle.range_for_security(n, bits, 5, 100)
+    pz = z0p.range.Params.for_security(n, bits, 5, 100)
+    for f in ("n_rows", "n_bits", "blowup", "num_queries", "final_size", "grinding_bits", "cap_height"):
+        assert getattr(po, f) == getattr(pz, f), f
+
+
+def test_proof_sizes_match_oracle_and_pins(z0p, oracle):
+    import json
+
+    gold = json.load(open(os.path.join(ROOT, "tests", "golden", "proofs.json")))
+    for case in gold["cases"]:
+        if case["kind"] == "air":
+            p = z0p.air.Params.new(case["n"], case["blowup"], case["queries"], case["final"],
+                                   case["a0"], case["b0"], case["b_last"])
+        else:
+            p = z0p.range.Params.new(case["n"], case["n_bits"], case["blowup"], case["queries"],
+                                     case["final"], case["value"])
+        p.grinding_bits = case["grinding"]
+        p.cap_height = case["cap"]
+        assert p.proof_size() == case["len"], case["name"]
+    assert z0p.air.Params.for_security(1 << 20, 1, 1, 1, 100).proof_size() == 203553
+
+
+# Hostile parameters (tests/hardening.rs:21-66): each must fail with the
+# reference's error variant, never crash.
+HOSTILE_AIR = [
+    (dict(n_steps=3), 3), (dict(n_steps=1), 3), (dict(n_steps=0), 3),
+    (dict(blowup=2), 4), (dict(blowup=6), 4), (dict(num_queries=0), 5),
+    (dict(final_size=1), 3), (dict(final_size=3), 3), (dict(cap_height=9), 8),
+    (dict(n_steps=1 << 63, blowup=4), 3), (dict(n_steps=1 << 26, blowup=4), 3),
+    (dict(final_size=2048), 3), (dict(grinding_bits=33), 8), (dict(num_queries=(1 << 20) + 1), 8),
+]
+
+
+@pytest.mark.parametrize("override,code", HOSTILE_AIR)
+def test_hostile_air_params(z0p, override, code):
+    from z0p_gb300._lib import AirParams
+
+    p = AirParams(n_steps=16, blowup=8, num_queries=8, final_size=8, grinding_bits=0,
+                  cap_height=0, a0=1, b0=1, b_last=610)
+    for k, v in override.items():
+        setattr(p, k, v)
+    n = C.c_size_t()
+    assert z0p.lib().z0p_air_proof_size(C.byref(p), C.byref(n)) == code, override
+
+
+def test_hostile_air_rate_and_final(z0p):
+    from z0p_gb300._lib import AirParams
+
+    n = C.c_size_t()
+    # a power-of-four ratio with blowup >= 4 always passes the residual check
+    p = AirParams(n_steps=64, blowup=4, num_queries=8, final_size=4, a0=1, b0=1, b_last=1)
+    assert z0p.lib().z0p_air_proof_size(C.byref(p), C.byref(n)) == 0
+    # an odd power-of-two ratio cannot quarter down to the final layer
+    p = AirParams(n_steps=64, blowup=4, num_queries=8, final_size=8, a0=1, b0=1, b_last=1)
+    assert z0p.lib().z0p_air_proof_size(C.byref(p), C.byref(n)) == 3
+    # final size equal to the LDE (no fold) is rejected (src/fri.rs:1130-1140)
+    p = AirParams(n_steps=4, blowup=4, num_queries=8, final_size=16, a0=1, b0=1, b_last=1)
+    assert z0p.lib().z0p_air_proof_size(C.byref(p), C.byref(n)) == 3
+    # non-canonical field element at the boundary
+    p = AirParams(n_steps=16, blowup=8, num_queries=8, final_size=8, a0=2013265921, b0=1, b_last=1)
+    assert z0p.lib().z0p_air_proof_size(C.byref(p), C.byref(n)) == 8
+
+
+def test_hostile_range_params(z0p):
+    from z0p_gb300._lib import RangeParams
+
+    n = C.c_size_t()
+    base = dict(n_rows=8, n_bits=16, blowup=8, num_queries=8, final_size=4, value=5)
+    for override, code in [
+        (dict(n_bits=0), 8), (dict(n_bits=25), 8), (dict(n_rows=3), 3), (dict(blowup=1), 4),
+        (dict(num_queries=0), 5), (dict(final_size=1), 3), (dict(cap_height=9), 8),
+        (dict(value=2013265921), 8), (dict(final_size=8), 3),
+    ]:
+        p = RangeParams(**{**base, **override})
+        assert z0p.lib().z0p_range_proof_size(C.byref(p), C.byref(n)) == code, override
+
+
+def test_buffer_too_small_reports_size_without_device(z0p):
+    # BUFFER_TOO_SMALL is decided before any device work: with a NULL context
+    # the call fails on the argument check instead, so probe with the size API.
+    p = z0p.air.Params.for_security(1024, 1, 1, 1, 100)
+    assert p.proof_size() == 68573
+    assert z0p.lib().z0p_gpu_air_prove(None, C.byref(p), None, None, 0, None) == 106

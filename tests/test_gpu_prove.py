@@ -1,0 +1,220 @@
+"""GPU parity: the device prover against the oracle, byte for byte.
+
+Every case proves on the GB300 through the C ABI and compares the proof with
+(a) a live oracle proof on the same parameters, seed and transcript label and
+(b) the committed golden digest; the oracle verifier must accept the GPU
+proof, and the transcript must be left in the oracle's post-state.
+"""
+import hashlib
+import json
+import os
+
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+GOLD = json.load(open(os.path.join(ROOT, "tests", "golden", "proofs.json")))["cases"]
+
+
+def _air_pair(z0p, oracle, case):
+    po = oracle.air_params_new(case["n"], case["blowup"], case["queries"], case["final"], case["a0"],
+                               case["b0"], case["b_last"], case["grinding"], case["cap"])
+    pz = z0p.air.Params.new(case["n"], case["blowup"], case["queries"], case["final"], case["a0"],
+                            case["b0"], case["b_last"])
+    pz.grinding_bits = case["grinding"]
+    pz.cap_height = case["cap"]
+    return po, pz
+
+
+def _range_pair(z0p, oracle, case):
+    po = oracle.range_params_new(case["n"], case["n_bits"], case["blowup"], case["queries"], case["final"],
+                                 case["value"], case["grinding"], case["cap"])
+    pz = z0p.range.Params.new(case["n"], case["n_bits"], case["blowup"], case["queries"], case["final"],
+                              case["value"])
+    pz.grinding_bits = case["grinding"]
+    pz.cap_height = case["cap"]
+    return po, pz
+
+
+@pytest.mark.parametrize("case", GOLD, ids=[c["name"] for c in GOLD])
+def test_golden_case_byte_identical(z0p, oracle, gpu_ctx, case):
+    label = case["label"].encode()
+    if case["kind"] == "air":
+        po, pz = _air_pair(z0p, oracle, case)
+        tz = z0p.Transcript(label)
+        proof = z0p.air.prove(pz, tz, gpu_ctx)
+        to = oracle.Transcript(label)
+        ref = oracle.air_prove(po, to)
+        assert oracle.air_verify(po, proof, oracle.Transcript(label)) == 0
+    else:
+        po, pz = _range_pair(z0p, oracle, case)
+        tz = z0p.Transcript(label)
+        proof = z0p.range.prove(pz, tz, gpu_ctx)
+        to = oracle.Transcript(label)
+        ref = oracle.range_prove(po, to)
+        ok = oracle.range_verify(po, proof, oracle.Transcript(label)) == 0
+        assert ok == case["verifies"]
+    assert len(proof) == case["len"]
+    assert proof == ref
+    assert hashlib.sha256(proof).hexdigest() == case["sha256"]
+    assert tz.export() == to.export()
+
+
+def test_air_prod_1m_byte_identical(z0p, oracle, gpu_ctx):
+    """Fibonacci 2^20 steps, production schedule, seeded initial pair."""
+    n = 1 << 20
+    P = oracle.P
+    z1, s = oracle.splitmix64(0x5EED000000000001)
+    z2, _ = oracle.splitmix64(s)
+    a0, b0 = z1 % P, z2 % P
+    _, b = oracle.build_trace(a0, b0, n)
+    po = oracle.air_for_security(n, a0, b0, int(b[-1]), 100)
+    pz = z0p.air.Params.for_security(n, a0, b0, int(b[-1]), 100)
+    proof = z0p.air.prove(pz, z0p.Transcript(b"bench/air-scale"), gpu_ctx)
+    assert len(proof) == 203553
+    ref = oracle.air_prove(po, oracle.Transcript(b"bench/air-scale"))
+    assert proof == ref
+    assert oracle.air_verify(po, proof, oracle.Transcript(b"bench/air-scale")) == 0
+
+
+def test_chained_proofs_on_one_transcript(z0p, oracle, gpu_ctx):
+    """Proofs chained on one transcript (src/transcript.rs:37-40)."""
+    _, b = oracle.build_trace(1, 1, 64)
+    po = oracle.air_params_new(64, 8, 12, 8, 1, 1, int(b[-1]), 6, 2)
+    pz = z0p.air.Params.new(64, 8, 12, 8, 1, 1, int(b[-1])).with_grinding_bits(6).with_cap_height(2)
+    ro = oracle.range_params_new(16, 8, 8, 6, 8, 200, 4, 1)
+    rz = z0p.range.Params.new(16, 8, 8, 6, 8, 200).with_grinding_bits(4).with_cap_height(1)
+    to, tz = oracle.Transcript(b"chain"), z0p.Transcript(b"chain")
+    to.absorb(b"prefix", b"x" * 3000)
+    tz.absorb(b"prefix", b"x" * 3000)
+    for _ in range(2):
+        assert z0p.air.prove(pz, tz, gpu_ctx) == oracle.air_prove(po, to)
+        assert z0p.range.prove(rz, tz, gpu_ctx) == oracle.range_prove(ro, to)
+        assert tz.export() == to.export()
+
+
+def test_forged_and_dishonest_statements_prove_structurally(z0p, oracle, gpu_ctx):
+    """False claims still prove (src/air.rs:356-364) and fail verification."""
+    _, b = oracle.build_trace(1, 1, 32)
+    lie = (int(b[-1]) + 5) % oracle.P
+    po = oracle.air_params_new(32, 8, 8, 16, 1, 1, lie)
+    pz = z0p.air.Params.new(32, 8, 8, 16, 1, 1, lie)
+    proof = z0p.air.prove(pz, z0p.Transcript(b"lie"), gpu_ctx)
+    assert proof == oracle.air_prove(po, oracle.Transcript(b"lie"))
+    assert oracle.air_verify(po, proof, oracle.Transcript(b"lie")) != 0
+
+
+def test_buffer_too_small_and_errors(z0p, gpu_ctx):
+    import ctypes as C
+
+    p = z0p.air.Params.for_security(1024, 1, 1, 1, 100)
+    buf = (C.c_uint8 * 100)()
+    n = C.c_size_t()
+    t = z0p.Transcript(b"x")
+    before = t.export()
+    rc = z0p.lib().z0p_gpu_air_prove(gpu_ctx.handle, C.byref(p), C.byref(t.state), buf, 100, C.byref(n))
+    assert rc == 100 and n.value == 68573
+    assert t.export() == before  # no transcript mutation on failure
+    bad = z0p.air.Params.for_security(1024, 1, 1, 1, 100)
+    bad.num_queries = 0
+    with pytest.raises(z0p.Z0pError) as e:
+        z0p.air.prove(bad, z0p.Transcript(b"x"), gpu_ctx)
+    assert e.value.code == 5
+
+
+# ------------------------------------------------------- per-stage kernels --
+
+
+def _torch():
+    return pytest.importorskip("torch")
+
+
+def test_rs_extend_matches_oracle(z0p, oracle, gpu_ctx):
+    torch = _torch()
+    import ctypes as C
+    import numpy as np
+
+    rng = np.random.default_rng(7)
+    for logn, batch, blowup in [(4, 3, 16), (10, 2, 16), (13, 4, 16), (16, 2, 8), (17, 1, 4)]:
+        n = 1 << logn
+        vals = rng.integers(0, oracle.P, size=(batch, n), dtype=np.uint64).astype(np.uint32)
+        d_in = torch.from_numpy(vals.astype(np.int64)).to(torch.int32).cuda()
+        d_out = torch.empty(batch * n * blowup, dtype=torch.int32, device="cuda")
+        torch.cuda.synchronize()
+        rc = z0p.lib().z0p_gpu_rs_extend(gpu_ctx.handle, C.c_void_p(d_in.data_ptr()), n, batch, blowup,
+                                         C.c_void_p(d_out.data_ptr()))
+        assert rc == 0, z0p.lib().z0p_gpu_last_reason()
+        got = d_out.cpu().numpy().view(np.uint32).reshape(batch, n * blowup)
+        for c in range(batch):
+            assert np.array_equal(got[c], oracle.reed_solomon_extend(vals[c], blowup)), (logn, c)
+
+
+def test_merkle_cap_matches_oracle(z0p, oracle, gpu_ctx):
+    torch = _torch()
+    import ctypes as C
+    import numpy as np
+
+    rng = np.random.default_rng(11)
+    for leaves, cap_h in [(1, 0), (2, 1), (64, 4), (1 << 12, 4), (1 << 15, 8), (1 << 18, 2)]:
+        flat = rng.integers(0, 256, size=leaves * 64, dtype=np.uint8)
+        d = torch.from_numpy(flat).cuda()
+        out = (C.c_uint8 * (32 * 256))()
+        cnt = C.c_uint64()
+        torch.cuda.synchronize()
+        rc = z0p.lib().z0p_gpu_merkle_flat64_cap(gpu_ctx.handle, C.c_void_p(d.data_ptr()), leaves * 64,
+                                                 cap_h, out, C.byref(cnt))
+        assert rc == 0
+        assert bytes(out)[: 32 * cnt.value] == oracle.merkle_flat64_cap(flat.tobytes(), cap_h), leaves
+
+
+def test_fri_fold_matches_oracle(z0p, oracle, gpu_ctx):
+    torch = _torch()
+    import ctypes as C
+    import numpy as np
+
+    P = oracle.P
+    rng = np.random.default_rng(3)
+    for logm, depth in [(6, 0), (10, 0), (12, 1), (16, 0), (18, 2), (20, 1)]:
+        m = 1 << logm
+        n = m >> (2 * depth)
+        vals = rng.integers(0, P, size=4 * n, dtype=np.uint64).astype(np.uint32)
+        ch = rng.integers(0, P, size=12, dtype=np.uint64).astype(np.uint32)
+        # quad leaders of layer `depth` (fri::point_at, src/fri.rs:1108-1115)
+        omega = oracle.f_pow(31, (P - 1) >> logm)
+        bits = logm - 2 * depth
+        pts = []
+        for i in range(n // 4):
+            e = int(format(4 * i, f"0{bits}b")[::-1], 2)
+            pts.append(oracle.f_pow(oracle.f_mul(31, oracle.f_pow(omega, e)), 4 ** depth))
+        ref, _ = oracle.fold_layer(vals, pts, ch)
+        d_in = torch.from_numpy(vals.astype(np.int64)).to(torch.int32).cuda()
+        d_out = torch.empty(n, dtype=torch.int32, device="cuda")
+        torch.cuda.synchronize()
+        rc = z0p.lib().z0p_gpu_fri_fold(gpu_ctx.handle, C.c_void_p(d_in.data_ptr()), n, m, depth,
+                                        (C.c_uint32 * 12)(*ch.tolist()), C.c_void_p(d_out.data_ptr()))
+        assert rc == 0
+        assert np.array_equal(d_out.cpu().numpy().view(np.uint32), ref), (logm, depth)
+
+
+def test_grind_matches_oracle(z0p, oracle, gpu_ctx):
+    """Minimum nonce equals the reference's sequential scan (src/transcript.rs:263-281)."""
+    import ctypes as C
+
+    for bits, label in [(1, b"a"), (8, b"b"), (13, b"c"), (18, b"d"), (20, b"fri-pow")]:
+        t = oracle.Transcript(b"grind-" + label)
+        t.absorb(b"stmt", b"hello")
+        # head = H(history) || LE64(|"fri-pow"|) || "fri-pow" (src/transcript.rs:182-189)
+        head = _history_digest(oracle, b"grind-" + label) + (7).to_bytes(8, "little") + b"fri-pow"
+        nonce = C.c_uint64()
+        rc = z0p.lib().z0p_gpu_grind(gpu_ctx.handle, head, len(head), bits, C.byref(nonce))
+        assert rc == 0
+        assert nonce.value == t.grind(b"fri-pow", bits), bits
+
+
+def _history_digest(oracle, label):
+    # BLAKE3 of the framed history Transcript::new(label); absorb("stmt","hello")
+    def frame(l, d):
+        return len(l).to_bytes(8, "little") + l + len(d).to_bytes(8, "little") + d
+
+    return oracle.blake3(frame(b"domain", label) + frame(b"stmt", b"hello"))

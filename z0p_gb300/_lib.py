@@ -1,0 +1,113 @@
+"""ctypes binding of libz0p_gpu.so (include/z0p_gpu.h).
+
+Loading fails loudly: there is no CPU fallback anywhere in this package.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+from . import build as _build
+
+ERRORS = {
+    0: "Ok", 1: "EmptyInput", 2: "IndexOutOfBounds", 3: "InvalidDomainSize",
+    4: "InvalidBlowup", 5: "NoQueries", 6: "BadMerklePath", 7: "FriVerificationFailed",
+    8: "MalformedInput", 9: "RngUnavailable", 100: "BufferTooSmall", 101: "Cuda",
+    102: "OutOfMemory", 103: "Unsupported", 104: "DeviceTimeout", 105: "Admission",
+    106: "InvalidArgument", 107: "Cancelled",
+}
+
+
+class Z0pError(Exception):
+    """A non-zero status from the C ABI (code mirrors z0p::Error for 1..9)."""
+
+    def __init__(self, code: int, reason: str = ""):
+        self.code = code
+        self.name = ERRORS.get(code, f"Status{code}")
+        super().__init__(f"{self.name} ({code})" + (f": {reason}" if reason else ""))
+
+
+class AirParams(C.Structure):
+    _fields_ = [
+        ("n_steps", C.c_uint64), ("blowup", C.c_uint64), ("num_queries", C.c_uint64),
+        ("final_size", C.c_uint64), ("grinding_bits", C.c_uint32), ("cap_height", C.c_uint64),
+        ("a0", C.c_uint32), ("b0", C.c_uint32), ("b_last", C.c_uint32),
+    ]
+
+
+class RangeParams(C.Structure):
+    _fields_ = [
+        ("n_rows", C.c_uint64), ("n_bits", C.c_uint64), ("blowup", C.c_uint64),
+        ("num_queries", C.c_uint64), ("final_size", C.c_uint64),
+        ("grinding_bits", C.c_uint32), ("cap_height", C.c_uint64), ("value", C.c_uint32),
+    ]
+
+
+class Stats(C.Structure):
+    _fields_ = [("launches", C.c_uint64), ("h2d_bytes", C.c_uint64), ("d2h_bytes", C.c_uint64),
+                ("syncs", C.c_uint64), ("proofs", C.c_uint64)]
+
+
+class TranscriptState(C.Structure):
+    _fields_ = [
+        ("tail", C.c_uint8 * 2048), ("tail_len", C.c_uint32),
+        ("stack", (C.c_uint8 * 32) * 54), ("stack_len", C.c_uint32),
+        ("next_index", C.c_uint64), ("total_len", C.c_uint64), ("counter", C.c_uint64),
+    ]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _build.LIB_PATH
+        if not os.path.exists(path):
+            path = _build.build()
+        L = C.CDLL(path)
+        P = C.POINTER
+        u8p, u32p, u64p, sz = P(C.c_uint8), P(C.c_uint32), P(C.c_uint64), C.c_size_t
+        vp = C.c_void_p
+        sig = {
+            "z0p_gpu_abi_version": (C.c_int, []),
+            "z0p_gpu_last_reason": (C.c_char_p, []),
+            "z0p_transcript_init": (C.c_int, [P(TranscriptState), C.c_char_p, sz]),
+            "z0p_transcript_absorb": (C.c_int, [P(TranscriptState), C.c_char_p, sz, C.c_char_p, sz]),
+            "z0p_transcript_challenge_bytes": (C.c_int, [P(TranscriptState), C.c_char_p, sz, u8p]),
+            "z0p_transcript_challenge_ext": (C.c_int, [P(TranscriptState), C.c_char_p, sz, u32p]),
+            "z0p_transcript_challenge_index": (C.c_int, [P(TranscriptState), C.c_char_p, sz, C.c_uint64, u64p]),
+            "z0p_air_params_new": (C.c_int, [C.c_uint64] * 4 + [C.c_uint32] * 3 + [P(AirParams)]),
+            "z0p_air_params_for_security": (C.c_int, [C.c_uint64] + [C.c_uint32] * 4 + [P(AirParams)]),
+            "z0p_range_params_new": (C.c_int, [C.c_uint64] * 5 + [C.c_uint32, P(RangeParams)]),
+            "z0p_range_params_for_security": (C.c_int, [C.c_uint64, C.c_uint64, C.c_uint32, C.c_uint32, P(RangeParams)]),
+            "z0p_air_proof_size": (C.c_int, [P(AirParams), P(sz)]),
+            "z0p_range_proof_size": (C.c_int, [P(RangeParams), P(sz)]),
+            "z0p_gpu_air_footprint": (C.c_int, [P(AirParams), P(sz)]),
+            "z0p_gpu_range_footprint": (C.c_int, [P(RangeParams), P(sz)]),
+            "z0p_gpu_ctx_create": (C.c_int, [C.c_int, P(vp)]),
+            "z0p_gpu_ctx_destroy": (None, [vp]),
+            "z0p_gpu_ctx_stream": (vp, [vp]),
+            "z0p_gpu_ctx_device_bytes": (sz, [vp]),
+            "z0p_gpu_ctx_stats": (C.c_int, [vp, P(Stats)]),
+            "z0p_gpu_ctx_set_profiling": (C.c_int, [vp, C.c_int]),
+            "z0p_gpu_ctx_profile": (C.c_int, [vp, C.c_char_p, sz, P(sz)]),
+            "z0p_gpu_air_prove": (C.c_int, [vp, P(AirParams), P(TranscriptState), u8p, sz, P(sz)]),
+            "z0p_gpu_range_prove": (C.c_int, [vp, P(RangeParams), P(TranscriptState), u8p, sz, P(sz)]),
+            "z0p_gpu_rs_extend": (C.c_int, [vp, vp, C.c_uint64, C.c_uint64, C.c_uint64, vp]),
+            "z0p_gpu_merkle_flat64_cap": (C.c_int, [vp, vp, C.c_uint64, C.c_uint64, u8p, u64p]),
+            "z0p_gpu_fri_fold": (C.c_int, [vp, vp, C.c_uint64, C.c_uint64, C.c_uint64, u32p, vp]),
+            "z0p_gpu_grind": (C.c_int, [vp, C.c_char_p, sz, C.c_uint32, u64p]),
+        }
+        for name, (res, args) in sig.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def check(rc: int):
+    if rc != 0:
+        reason = lib().z0p_gpu_last_reason()
+        raise Z0pError(rc, reason.decode(errors="replace") if reason else "")

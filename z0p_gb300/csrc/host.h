@@ -1,0 +1,79 @@
+// Host-side pieces of the z0p GB300 prover: BabyBear scalar arithmetic, the
+// streaming BLAKE3 hasher and Fiat-Shamir transcript over the C-ABI state,
+// parameter rules and tuners, and the proof shape/size arithmetic.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/z0p_gpu.h"
+
+namespace z0p {
+namespace host {
+
+constexpr uint32_t P = 2013265921u;
+constexpr uint32_t GENERATOR = 31u;
+constexpr uint32_t TWO_ADICITY = 27u;
+constexpr uint64_t MAX_DOMAIN = 1ull << 27;
+
+inline uint32_t fadd(uint32_t a, uint32_t b) { uint32_t s = a + b; return s >= P ? s - P : s; }
+inline uint32_t fsub(uint32_t a, uint32_t b) { return a >= b ? a - b : P - (b - a); }
+inline uint32_t fmul(uint32_t a, uint32_t b) { return (uint32_t)((uint64_t)a * b % P); }
+uint32_t fpow(uint32_t a, uint64_t e);
+inline uint32_t finv(uint32_t a) { return fpow(a, P - 2); }
+inline uint32_t to_mont(uint32_t a) { return (uint32_t)(((uint64_t)a << 32) % P); }
+inline bool is_pow2(uint64_t x) { return x && !(x & (x - 1)); }
+inline uint32_t log2u(uint64_t x) { return (uint32_t)__builtin_ctzll(x); }
+uint32_t two_adic_generator(uint32_t bits);  // bits <= 27
+uint64_t brev(uint64_t x, uint32_t bits);
+
+// BLAKE3 (unkeyed, 32-byte output) and the streaming hasher semantics of
+// src/hash.rs:233-324 over the C-ABI transcript state.
+void blake3(const uint8_t* data, size_t len, uint8_t out[32]);
+void hasher_update(z0p_transcript_state* st, const uint8_t* data, size_t len);
+void hasher_finalize(const z0p_transcript_state* st, uint8_t out[32]);
+
+void transcript_init(z0p_transcript_state* st, const uint8_t* label, size_t len);
+void transcript_absorb(z0p_transcript_state* st, const char* label, const uint8_t* data,
+                       size_t len);
+void transcript_absorb_raw(z0p_transcript_state* st, const uint8_t* label, size_t llen,
+                           const uint8_t* data, size_t len);
+void squeeze_raw(z0p_transcript_state* st, const uint8_t* label, size_t llen, uint8_t out[32]);
+void challenge_ext(z0p_transcript_state* st, const char* label, uint32_t out[4]);
+uint64_t challenge_index(z0p_transcript_state* st, const char* label, uint64_t domain);
+// pow_head (src/transcript.rs:182-189): H(history) || LE64(|label|) || label.
+std::vector<uint8_t> pow_head(const z0p_transcript_state* st, const char* label);
+
+// FRI parameter rules (src/fri.rs:105-196) and tuners (src/fri.rs:945-1074).
+struct FriParams {
+  uint64_t blowup, num_queries, final_size;
+  uint32_t grinding_bits;
+  uint64_t cap_height;
+};
+int fri_params_new(uint64_t blowup, uint64_t q, uint64_t final_size, FriParams* out);
+int fri_params_validate(const FriParams& p);
+void tune_shape(uint64_t lde_len, uint64_t q, uint64_t col_lde, uint64_t col_vb,
+                uint64_t* final_size, uint64_t* cap_height);
+void tune_strength(uint32_t target, uint32_t millibits, uint64_t* q, uint32_t* g);
+uint32_t composition_millibits(uint64_t lde_len, uint64_t degree_bound);
+
+int air_validate(const z0p_air_params& p);
+int range_validate(const z0p_range_params& p);
+
+// Shape of the FRI layer stack and trees for an LDE of length m.
+struct FriShape {
+  uint64_t m;
+  std::vector<uint64_t> len;      // layer lengths, m down to final_size
+  std::vector<uint64_t> leaves;   // Merkle leaves per layer
+  std::vector<uint32_t> depth;    // log2(leaves)
+  std::vector<uint32_t> drop;     // cap level drop = min(cap_height, depth)
+};
+// Checks commit_inner's preconditions (src/fri.rs:551-575) and builds the shape.
+int fri_shape(uint64_t m, uint64_t degree_bound, const FriParams& fp, FriShape* out);
+uint64_t fri_bytes(const FriShape& s, uint64_t q);  // commitment + proof bodies
+
+void set_reason(const std::string& r);
+
+}  // namespace host
+}  // namespace z0p

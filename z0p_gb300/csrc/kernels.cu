@@ -1,0 +1,934 @@
+// sm_103a kernels of the z0p GB300 prover.
+//
+// Layout conventions shared by all kernels:
+//  * An LDE of blowup B = 2^logB over N = 2^logN trace rows is stored
+//    coset-major: row k = B*q + j (natural order, src/air.rs:520-531) lives at
+//    [j][q] = j*N + q. Coset j is the N-point NTT of the coefficients twisted
+//    by (31 * omega_m^j)^i, so each coset is one contiguous, coalesced stream;
+//    the next-row shift k -> k + B (src/air.rs:519) becomes q -> q + 1.
+//  * FRI layer 0 is bitrev(composition) (src/fri.rs:584-586). Its quad P
+//    holds rows k0 + s*m/4 (s = 0..3) with k0 = brev_{log m - 2}(P), i.e.
+//    rows q0 + s*N/4 of a single coset, so a thread that owns one quad reads
+//    four coalesced streams and writes its 64-byte leaf contiguously.
+//  * Merkle trees are stored level-contiguous: level l of a tree with L
+//    leaves starts at digest 2L - 2(L >> l); a digest is 8 little-endian
+//    words, byte-identical to the reference's [u8; 32].
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cstdint>
+
+#include "device.cuh"
+#include "kernels.h"
+
+namespace z0p {
+
+namespace {
+
+constexpr int kThreads = 256;
+
+inline unsigned grid_for(uint64_t n, int threads = kThreads) {
+  return (unsigned)((n + threads - 1) / threads);
+}
+
+__device__ __forceinline__ uint32_t tw_exp(uint32_t e, uint32_t shift, uint32_t inverse) {
+  uint32_t x = e << shift;
+  return inverse ? 0u - x : x;
+}
+
+__device__ __forceinline__ void load_digest(const uint32_t* p, uint32_t d[8]) {
+  uint4 a = *reinterpret_cast<const uint4*>(p);
+  uint4 b = *reinterpret_cast<const uint4*>(p + 4);
+  d[0] = a.x; d[1] = a.y; d[2] = a.z; d[3] = a.w;
+  d[4] = b.x; d[5] = b.y; d[6] = b.z; d[7] = b.w;
+}
+__device__ __forceinline__ void store_digest(uint32_t* p, const uint32_t d[8]) {
+  *reinterpret_cast<uint4*>(p) = make_uint4(d[0], d[1], d[2], d[3]);
+  *reinterpret_cast<uint4*>(p + 4) = make_uint4(d[4], d[5], d[6], d[7]);
+}
+
+// ------------------------------------------------------------ trace gen ----
+// (A_i, B_i) = M^i (a0, b0) with M = [[0,1],[1,1]] (src/air.rs:341-354): each
+// thread jumps to its chunk start with the binary powers of M, then steps.
+struct FibMats {
+  uint32_t m[32][4];
+};
+
+__global__ void fib_trace_kernel(uint32_t* __restrict__ col_a, uint32_t* __restrict__ col_b,
+                                 uint32_t n, uint32_t a0, uint32_t b0, FibMats mats,
+                                 uint32_t per_thread) {
+  uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  uint64_t start = t * per_thread;
+  if (start >= n) return;
+  uint32_t r00 = 1, r01 = 0, r10 = 0, r11 = 1;
+  for (int k = 0; k < 32; k++) {
+    if ((start >> k) & 1u) {
+      const uint32_t* q = mats.m[k];
+      uint32_t n00 = fadd(fmul(r00, q[0]), fmul(r01, q[2]));
+      uint32_t n01 = fadd(fmul(r00, q[1]), fmul(r01, q[3]));
+      uint32_t n10 = fadd(fmul(r10, q[0]), fmul(r11, q[2]));
+      uint32_t n11 = fadd(fmul(r10, q[1]), fmul(r11, q[3]));
+      r00 = n00; r01 = n01; r10 = n10; r11 = n11;
+    }
+  }
+  uint32_t a = fadd(fmul(r00, a0), fmul(r01, b0));
+  uint32_t b = fadd(fmul(r10, a0), fmul(r11, b0));
+  uint64_t end = start + per_thread < n ? start + per_thread : n;
+  for (uint64_t i = start; i < end; i++) {
+    col_a[i] = a;
+    col_b[i] = b;
+    uint32_t nb = fadd(a, b);
+    a = b;
+    b = nb;
+  }
+}
+
+__global__ void fill_columns_kernel(uint32_t* cols, uint32_t n, uint32_t ncols,
+                                    const uint32_t* __restrict__ values) {
+  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (uint64_t)n * ncols) return;
+  cols[i] = values[i / n];
+}
+
+// ----------------------------------------------------------------- NTT ----
+// Exact arithmetic: any transform order gives the reference's values
+// (src/ntt.rs:116-177 is radix-2 DIT; these kernels are DIF in shared memory
+// with a bit-reversed read-out).
+struct NttArgs {
+  uint32_t logn, inverse, in_div, twist_mod, twist_shift, post_gamma, ninv_m;
+  Tables tb;
+};
+
+// In-place DIF over `cols` independent columns of length 2^logl held in
+// shared memory at s[c * cstride + i * istride]; tw[t] = w^t for t < len/2.
+__device__ __forceinline__ void smem_dif(uint32_t* s, const uint32_t* tw, uint32_t logl,
+                                         uint32_t logcols, uint32_t cstride, uint32_t istride,
+                                         bool col_fast) {
+  uint32_t half = 1u << (logl - 1);
+  uint32_t total = half << logcols;
+  for (uint32_t h = half; h >= 1; h >>= 1) {
+    uint32_t tshift = __ffs(half / h) - 1;  // log2(half / h)
+    for (uint32_t idx = threadIdx.x; idx < total; idx += blockDim.x) {
+      uint32_t c, bj;
+      if (col_fast) {
+        c = idx & ((1u << logcols) - 1u);
+        bj = idx >> logcols;
+      } else {
+        c = idx >> (logl - 1);
+        bj = idx & (half - 1u);
+      }
+      uint32_t jj = bj & (h - 1u);
+      uint32_t i0 = ((bj - jj) << 1) + jj;
+      uint32_t p0 = c * cstride + i0 * istride;
+      uint32_t p1 = p0 + h * istride;
+      uint32_t u = s[p0], v = s[p1];
+      s[p0] = fadd(u, v);
+      s[p1] = mmul(fsub(u, v), tw[jj << tshift]);
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void ntt_small_kernel(const uint32_t* __restrict__ in, uint32_t* __restrict__ out,
+                                 NttArgs a) {
+  extern __shared__ uint32_t sm[];
+  const uint32_t n = 1u << a.logn, half = n >> 1;
+  uint32_t* s = sm;
+  uint32_t* tw = sm + n;
+  const uint32_t b = blockIdx.x;
+  const uint32_t* src = in + (size_t)(b / a.in_div) * n;
+  const uint32_t j = b % a.twist_mod;
+  const uint32_t shift = kRootBits - a.logn;
+  for (uint32_t i = threadIdx.x; i < half; i += blockDim.x)
+    tw[i] = root_pow(a.tb, tw_exp(i, shift, a.inverse));
+  for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+    uint32_t v = src[i];
+    if (j) v = mmul(v, root_pow(a.tb, (j * i) << a.twist_shift));
+    s[i] = v;
+  }
+  __syncthreads();
+  if (a.logn > 0) smem_dif(s, tw, a.logn, 0, 0, 1, true);
+  uint32_t* dst = out + (size_t)b * n;
+  for (uint32_t k = threadIdx.x; k < n; k += blockDim.x) {
+    uint32_t v = s[brev_bits(k, a.logn)];
+    if (a.post_gamma) v = mmul(mmul(v, gamma_pow(a.tb, k)), a.ninv_m);
+    dst[k] = v;
+  }
+}
+
+// Four-step pass 1: for C columns i2 of x viewed as [n1][n2], n1-point
+// transforms over i1, times omega_n^(i2 k1); written transposed as yt[k1][i2].
+template <int LOGC>
+__global__ void ntt_pass1_kernel(const uint32_t* __restrict__ in, uint32_t* __restrict__ yt,
+                                 NttArgs a, uint32_t logn1) {
+  constexpr uint32_t C = 1u << LOGC;
+  extern __shared__ uint32_t sm[];
+  const uint32_t logn2 = a.logn - logn1;
+  const uint32_t n1 = 1u << logn1;
+  const uint32_t n = 1u << a.logn;
+  uint32_t* s = sm;
+  uint32_t* tw = sm + (n1 << LOGC);
+  const uint32_t b = blockIdx.y;
+  const uint32_t c0 = blockIdx.x * C;
+  const uint32_t* src = in + (size_t)(b / a.in_div) * n;
+  const uint32_t j = b % a.twist_mod;
+  for (uint32_t i = threadIdx.x; i < n1 / 2; i += blockDim.x)
+    tw[i] = root_pow(a.tb, tw_exp(i, kRootBits - logn1, a.inverse));
+  for (uint32_t e = threadIdx.x; e < (n1 << LOGC); e += blockDim.x) {
+    uint32_t i1 = e >> LOGC, c = e & (C - 1);
+    uint32_t i = (i1 << logn2) + c0 + c;
+    uint32_t v = src[i];
+    if (j) v = mmul(v, root_pow(a.tb, (j * i) << a.twist_shift));
+    s[e] = v;
+  }
+  __syncthreads();
+  smem_dif(s, tw, logn1, LOGC, 1, C, true);
+  uint32_t* dst = yt + (size_t)b * n;
+  const uint32_t shift = kRootBits - a.logn;
+  for (uint32_t e = threadIdx.x; e < (n1 << LOGC); e += blockDim.x) {
+    uint32_t k1 = e >> LOGC, c = e & (C - 1);
+    uint32_t i2 = c0 + c;
+    uint32_t v = s[(brev_bits(k1, logn1) << LOGC) + c];
+    v = mmul(v, root_pow(a.tb, tw_exp(i2 * k1, shift, a.inverse)));
+    dst[((size_t)k1 << logn2) + i2] = v;
+  }
+}
+
+// Four-step pass 2: for R rows k1 of yt, n2-point transforms over i2; output
+// k = k1 + n1 k2 (natural order), optionally scaled by 31^k / n.
+template <int LOGR>
+__global__ void ntt_pass2_kernel(const uint32_t* __restrict__ yt, uint32_t* __restrict__ out,
+                                 NttArgs a, uint32_t logn1) {
+  constexpr uint32_t R = 1u << LOGR;
+  extern __shared__ uint32_t sm[];
+  const uint32_t logn2 = a.logn - logn1;
+  const uint32_t n2 = 1u << logn2;
+  const uint32_t n = 1u << a.logn;
+  const uint32_t stride = n2 + 1;  // padding against bank conflicts on the read-out
+  uint32_t* s = sm;
+  uint32_t* tw = sm + R * stride;
+  const uint32_t b = blockIdx.y;
+  const uint32_t r0 = blockIdx.x * R;
+  for (uint32_t i = threadIdx.x; i < n2 / 2; i += blockDim.x)
+    tw[i] = root_pow(a.tb, tw_exp(i, kRootBits - logn2, a.inverse));
+  const uint32_t* src = yt + (size_t)b * n + ((size_t)r0 << logn2);
+  for (uint32_t e = threadIdx.x; e < (R << logn2); e += blockDim.x) {
+    uint32_t r = e >> logn2, i2 = e & (n2 - 1);
+    s[r * stride + i2] = src[e];
+  }
+  __syncthreads();
+  smem_dif(s, tw, logn2, LOGR, stride, 1, false);
+  uint32_t* dst = out + (size_t)b * n;
+  for (uint32_t e = threadIdx.x; e < (R << logn2); e += blockDim.x) {
+    uint32_t k2 = e >> LOGR, r = e & (R - 1);
+    uint32_t k = r0 + r + (k2 << logn1);
+    uint32_t v = s[r * stride + brev_bits(k2, logn2)];
+    if (a.post_gamma) v = mmul(mmul(v, gamma_pow(a.tb, k)), a.ninv_m);
+    dst[k] = v;
+  }
+}
+
+// Per coset j: 1 / (x^N - 1) with x^N = 31^N * omega_B^j (constant on the
+// coset), in Montgomery form, and the same value times 2^32 once more.
+__global__ void coset_zinv_kernel(uint32_t* zinv, uint32_t* zinv2, uint32_t logB,
+                                  uint32_t gamma_n_m, Tables tb) {
+  uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= (1u << logB)) return;
+  uint32_t xn = mmul(gamma_n_m, root_pow(tb, j << (kRootBits - logB)));
+  uint32_t inv = minv(fsub(xn, kR));
+  zinv[j] = inv;
+  zinv2[j] = mmul(inv, kR2);
+}
+
+// --------------------------------------------------------------- Merkle ----
+// Trace tree leaf L = rows 8L..8L+7 packed A||B (src/air.rs:520-531), hashed
+// as one 64-byte block (src/merkle.rs:93-110).
+__global__ void air_trace_leaves_kernel(const uint32_t* __restrict__ lde_a,
+                                        const uint32_t* __restrict__ lde_b,
+                                        uint32_t* __restrict__ leaves, uint32_t logN,
+                                        uint32_t logB, uint32_t nleaves) {
+  uint32_t L = blockIdx.x * blockDim.x + threadIdx.x;
+  if (L >= nleaves) return;
+  uint32_t m[16];
+#pragma unroll
+  for (int r = 0; r < 8; r++) {
+    uint32_t k = 8u * L + r;
+    uint32_t j = k & ((1u << logB) - 1u), q = k >> logB;
+    size_t off = ((size_t)j << logN) + q;
+    m[2 * r] = __ldg(lde_a + off);
+    m[2 * r + 1] = __ldg(lde_b + off);
+  }
+  uint32_t d[8];
+  blake3_leaf64(m, d);
+  store_digest(leaves + 8 * (size_t)L, d);
+}
+
+// Range tree leaf k = BLAKE3(0x00 || row k) with the row = ncols LE words
+// (src/range.rs:452-460, src/hash.rs:351-381). Threads walk rows in
+// coset-major order so column reads coalesce; digests land at index k.
+__global__ void range_trace_leaves_kernel(const uint32_t* __restrict__ lde,
+                                          uint32_t* __restrict__ leaves, uint32_t logN,
+                                          uint32_t logB, uint32_t ncols) {
+  uint32_t u = blockIdx.x * blockDim.x + threadIdx.x;
+  uint32_t m = 1u << (logN + logB);
+  if (u >= m) return;
+  uint32_t j = u >> logN, q = u & ((1u << logN) - 1u);
+  uint32_t k = (q << logB) | j;
+  uint32_t w[32];
+#pragma unroll
+  for (int c = 0; c < 32; c++) w[c] = 0u;
+#pragma unroll
+  for (int c = 0; c < 25; c++)
+    if ((uint32_t)c < ncols) w[c] = __ldg(lde + ((size_t)c << (logN + logB)) + u);
+  // 0x00 || row: word i = (w[i-1] >> 24) | (w[i] << 8); one or two blocks.
+  uint32_t len = 4u * ncols + 1u;
+  uint32_t cv[8];
+  iv_words(cv);
+  uint32_t blk[16];
+#pragma unroll
+  for (int i = 0; i < 16; i++) blk[i] = __funnelshift_l(i ? w[i - 1] : 0u, w[i], 8);
+  bool one = len <= 64u;
+  uint32_t o[8];
+  blake3_compress(cv, blk, 0u, 0u, one ? len : 64u,
+                  one ? (kChunkStart | kChunkEnd | kRoot) : kChunkStart, o);
+  if (!one) {
+#pragma unroll
+    for (int i = 0; i < 16; i++) blk[i] = __funnelshift_l(w[15 + i], w[16 + i], 8);
+    uint32_t o2[8];
+    blake3_compress(o, blk, 0u, 0u, len - 64u, kChunkEnd | kRoot, o2);
+#pragma unroll
+    for (int i = 0; i < 8; i++) o[i] = o2[i];
+  }
+  store_digest(leaves + 8 * (size_t)k, o);
+}
+
+__global__ void merkle_level_kernel(const uint32_t* __restrict__ prev, uint32_t* __restrict__ next,
+                                    uint64_t count) {
+  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  uint32_t l[8], r[8], d[8];
+  load_digest(prev + 16 * i, l);
+  load_digest(prev + 16 * i + 8, r);
+  blake3_node(l, r, d);
+  store_digest(next + 8 * i, d);
+}
+
+__device__ __forceinline__ uint64_t level_offset(uint64_t leaves, uint32_t level) {
+  return 2 * leaves - 2 * (leaves >> level);
+}
+
+// Remaining levels of a tree once a level has <= 2 * blockDim nodes: one CTA.
+__global__ void merkle_tail_kernel(uint32_t* tree, uint64_t leaves, uint32_t start_level) {
+  for (uint32_t l = start_level; (leaves >> l) > 1; l++) {
+    const uint32_t* prev = tree + 8 * level_offset(leaves, l);
+    uint32_t* next = tree + 8 * level_offset(leaves, l + 1);
+    uint64_t cnt = leaves >> (l + 1);
+    for (uint64_t i = threadIdx.x; i < cnt; i += blockDim.x) {
+      uint32_t a[8], b[8], d[8];
+      load_digest(prev + 16 * i, a);
+      load_digest(prev + 16 * i + 8, b);
+      blake3_node(a, b, d);
+      store_digest(next + 8 * i, d);
+    }
+    __syncthreads();
+  }
+}
+
+// 64-byte leaves (four Ext4 values) of an in-memory FRI layer
+// (src/fri.rs:1408-1414) or of any flat buffer.
+__global__ void leaf64_kernel(const uint32_t* __restrict__ flat, uint32_t* __restrict__ leaves,
+                              uint64_t nleaves) {
+  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nleaves) return;
+  uint32_t m[16];
+  const uint4* p = reinterpret_cast<const uint4*>(flat + 16 * i);
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    uint4 v = p[k];
+    m[4 * k] = v.x; m[4 * k + 1] = v.y; m[4 * k + 2] = v.z; m[4 * k + 3] = v.w;
+  }
+  uint32_t d[8];
+  blake3_leaf64(m, d);
+  store_digest(leaves + 8 * i, d);
+}
+
+// 0x00-prefixed 16-byte leaves for layers whose length is not a multiple of
+// four (src/fri.rs:1422-1428).
+__global__ void leaf16_kernel(const uint32_t* __restrict__ values, uint32_t* __restrict__ leaves,
+                              uint64_t n) {
+  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  uint32_t w[4] = {values[4 * i], values[4 * i + 1], values[4 * i + 2], values[4 * i + 3]};
+  uint32_t d[8];
+  blake3_prefixed_leaf<4>(w, d);
+  store_digest(leaves + 8 * i, d);
+}
+
+// -------------------------------------------------------------- compose ----
+// AIR composition (src/air.rs:847-929 == composition_at :938-962) on the four
+// rows of layer-0 quad P, written bit-reversed as one 64-byte leaf and hashed.
+__global__ void __launch_bounds__(kThreads) air_compose_leaves_kernel(AirComposeArgs a, Tables tb) {
+  const uint32_t logm = a.logN + a.logB;
+  const uint32_t quarter = 1u << (logm - 2);
+  uint32_t u = blockIdx.x * blockDim.x + threadIdx.x;
+  if (u >= quarter) return;
+  const uint32_t N = 1u << a.logN, B = 1u << a.logB;
+  uint32_t k0;
+  if (a.logN >= 2) {
+    uint32_t j = u >> (a.logN - 2), q0 = u & ((N >> 2) - 1u);
+    k0 = (q0 << a.logB) | j;
+  } else {
+    k0 = u;
+  }
+  const uint32_t P = brev_bits(k0, logm - 2);
+  uint32_t va[4], vb[4], van[4], vbn[4], zt[4];
+  uint32_t den[8];
+  const uint32_t gamma_m = to_mont(31u);
+#pragma unroll
+  for (int s = 0; s < 4; s++) {
+    uint32_t k = k0 + (uint32_t)s * quarter;
+    uint32_t j = k & (B - 1u), q = k >> a.logB;
+    uint32_t qn = (q + 1u) & (N - 1u);
+    size_t base = (size_t)j << a.logN;
+    va[s] = __ldg(a.lde_a + base + q);
+    vb[s] = __ldg(a.lde_b + base + q);
+    van[s] = __ldg(a.lde_a + base + qn);
+    vbn[s] = __ldg(a.lde_b + base + qn);
+    uint32_t x = mmul(gamma_m, root_pow(tb, k << (kRootBits - logm)));
+    den[2 * s] = fsub(x, a.w_last_m);
+    den[2 * s + 1] = fsub(x, kR);
+    zt[s] = mmul(den[2 * s], __ldg(a.zinv + j));  // 1 / Z_t = (x - w_last) / (x^N - 1)
+  }
+  batch_minv(den);
+  uint32_t leaf[16];
+#pragma unroll
+  for (int s = 0; s < 4; s++) {
+    uint32_t av = va[s], bv = vb[s];
+    uint32_t t1 = mmul(fsub(van[s], bv), zt[s]);
+    uint32_t t2 = mmul(fsub(vbn[s], fadd(av, bv)), zt[s]);
+    uint32_t ba = mmul(fsub(av, a.a0), den[2 * s + 1]);
+    uint32_t bb = mmul(fsub(bv, a.b0), den[2 * s + 1]);
+    uint32_t bo = mmul(fsub(bv, a.b_last), den[2 * s]);
+    const int t = (s == 1) ? 2 : (s == 2) ? 1 : s;  // position 4P + brev2(s)
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+      uint32_t acc = mmul(t1, a.alpha[0][c]);
+      acc = fadd(acc, mmul(t2, a.alpha[1][c]));
+      acc = fadd(acc, mmul(ba, a.alpha[2][c]));
+      acc = fadd(acc, mmul(bb, a.alpha[3][c]));
+      acc = fadd(acc, mmul(bo, a.alpha[4][c]));
+      leaf[4 * t + c] = acc;
+    }
+  }
+  uint4* dst = reinterpret_cast<uint4*>(a.layer0 + 16 * (size_t)P);
+#pragma unroll
+  for (int t = 0; t < 4; t++)
+    dst[t] = make_uint4(leaf[4 * t], leaf[4 * t + 1], leaf[4 * t + 2], leaf[4 * t + 3]);
+  uint32_t d[8];
+  blake3_leaf64(leaf, d);
+  store_digest(a.leaves + 8 * (size_t)P, d);
+}
+
+// Range-check composition (src/range.rs:678-741 == composition_at :746-774).
+__global__ void __launch_bounds__(kThreads) range_compose_leaves_kernel(RangeComposeArgs a,
+                                                                        Tables tb) {
+  const uint32_t logm = a.logN + a.logB;
+  const uint32_t quarter = 1u << (logm - 2);
+  uint32_t u = blockIdx.x * blockDim.x + threadIdx.x;
+  if (u >= quarter) return;
+  const uint32_t N = 1u << a.logN, B = 1u << a.logB;
+  uint32_t k0;
+  if (a.logN >= 2) {
+    uint32_t j = u >> (a.logN - 2), q0 = u & ((N >> 2) - 1u);
+    k0 = (q0 << a.logB) | j;
+  } else {
+    k0 = u;
+  }
+  const uint32_t P = brev_bits(k0, logm - 2);
+  const uint32_t gamma_m = to_mont(31u);
+  uint32_t den[4], kk[4];
+#pragma unroll
+  for (int s = 0; s < 4; s++) {
+    uint32_t k = k0 + (uint32_t)s * quarter;
+    kk[s] = k;
+    uint32_t x = mmul(gamma_m, root_pow(tb, k << (kRootBits - logm)));
+    den[s] = fsub(x, kR);
+  }
+  batch_minv(den);
+  const uint32_t nb = a.n_bits;
+  uint32_t leaf[16];
+#pragma unroll
+  for (int s = 0; s < 4; s++) {
+    uint32_t k = kk[s];
+    uint32_t j = k & (B - 1u), q = k >> a.logB;
+    size_t row = ((size_t)j << a.logN) + q;
+    size_t colstride = (size_t)1 << logm;
+    uint32_t v = __ldg(a.lde + row);
+    uint32_t zi = __ldg(a.zinv + j), zi2 = __ldg(a.zinv2 + j);
+    uint32_t rec = 0u, pow2 = kR;  // 2^i in Montgomery form
+    E4 acc = {{0u, 0u, 0u, 0u}};
+    for (uint32_t c = 0; c < nb; c++) {
+      uint32_t bit = __ldg(a.lde + (c + 1) * colstride + row);
+      rec = fadd(rec, mmul(bit, pow2));
+      pow2 = fadd(pow2, pow2);
+      // bit * (bit - 1) * zinv: mmul(bit, bit-1) carries 2^-32, zinv2 restores it.
+      uint32_t bterm = mmul(mmul(bit, fsub(bit, 1u)), zi2);
+      const uint32_t* al = a.alphas + 4 * (1 + c);
+#pragma unroll
+      for (int e = 0; e < 4; e++) acc.c[e] = fadd(acc.c[e], mmul(bterm, __ldg(al + e)));
+    }
+    uint32_t dterm = mmul(fsub(v, rec), zi);
+    uint32_t bound = mmul(fsub(v, a.value), den[s]);
+    const uint32_t* ad = a.alphas;
+    const uint32_t* ab = a.alphas + 4 * (1 + nb);
+    const int t = (s == 1) ? 2 : (s == 2) ? 1 : s;
+#pragma unroll
+    for (int e = 0; e < 4; e++) {
+      uint32_t x = mmul(dterm, __ldg(ad + e));
+      x = fadd(x, acc.c[e]);
+      x = fadd(x, mmul(bound, __ldg(ab + e)));
+      leaf[4 * t + e] = x;
+    }
+  }
+  uint4* dst = reinterpret_cast<uint4*>(a.layer0 + 16 * (size_t)P);
+#pragma unroll
+  for (int t = 0; t < 4; t++)
+    dst[t] = make_uint4(leaf[4 * t], leaf[4 * t + 1], leaf[4 * t + 2], leaf[4 * t + 3]);
+  uint32_t d[8];
+  blake3_leaf64(leaf, d);
+  store_digest(a.leaves + 8 * (size_t)P, d);
+}
+
+// ----------------------------------------------------------------- FRI ----
+// fold_values (src/fri.rs:1311-1331): A + x^-1 (r0 B + x^-1 (r1 C + x^-1 r2 D)).
+__device__ __forceinline__ E4 fold_quad(const E4& q0, const E4& q1, const E4& q2, const E4& q3,
+                                        uint32_t xinv_m, const FoldArgs& a) {
+  E4 s01 = e4_add(q0, q1), s23 = e4_add(q2, q3);
+  E4 odd_diff = e4_sub(q0, q1);
+  E4 skew_u = e4_mul_base(e4_sub(q2, q3), a.unit_m);
+  E4 mean = e4_quarter(e4_add(s01, s23));
+  E4 odd = e4_quarter(e4_sub(odd_diff, skew_u));
+  E4 even = e4_quarter(e4_sub(s01, s23));
+  E4 skew = e4_quarter(e4_add(odd_diff, skew_u));
+  E4 r0, r1, r2;
+#pragma unroll
+  for (int c = 0; c < 4; c++) { r0.c[c] = a.ch[0][c]; r1.c[c] = a.ch[1][c]; r2.c[c] = a.ch[2][c]; }
+  E4 acc = e4_add(e4_mul_base(e4_mul_cm(skew, r2), xinv_m), e4_mul_cm(even, r1));
+  acc = e4_add(e4_mul_base(acc, xinv_m), e4_mul_cm(odd, r0));
+  return e4_add(mean, e4_mul_base(acc, xinv_m));
+}
+
+// x^-1 of quad P's leader on a layer of length 2^logn: the layer domain is
+// 31^(4^depth) <omega_n> in bit-reversed order (src/fri.rs:1108-1115), so no
+// field inversion is needed.
+__device__ __forceinline__ uint32_t quad_xinv(const Tables& tb, const FoldArgs& a, uint32_t P) {
+  uint32_t e = brev_bits(P, a.logn - 2);
+  return mmul(a.ginv_m, root_pow(tb, 0u - (e << (kRootBits - a.logn))));
+}
+
+// Thread per next-layer leaf: folds four quads (256 contiguous input bytes,
+// staged through shared memory), writes the 64-byte next leaf and its digest.
+constexpr int kFoldThreads = 128;
+__global__ void __launch_bounds__(kFoldThreads) fri_fold_leaf_kernel(FoldArgs a, Tables tb) {
+  __shared__ uint4 sm[kFoldThreads * 17];
+  const uint64_t nleaf = 1ull << (a.logn - 4);
+  const uint64_t first = (uint64_t)blockIdx.x * kFoldThreads;
+  const uint4* src = reinterpret_cast<const uint4*>(a.in) + first * 16;
+  uint64_t avail = nleaf - first < (uint64_t)kFoldThreads ? nleaf - first : kFoldThreads;
+  for (uint32_t e = threadIdx.x; e < avail * 16; e += kFoldThreads)
+    sm[(e >> 4) * 17 + (e & 15)] = src[e];
+  __syncthreads();
+  uint64_t Pn = first + threadIdx.x;
+  if (threadIdx.x >= avail) return;
+  uint32_t leaf[16];
+#pragma unroll
+  for (int t = 0; t < 4; t++) {
+    E4 q[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+      uint4 v = sm[threadIdx.x * 17 + 4 * t + i];
+      q[i].c[0] = v.x; q[i].c[1] = v.y; q[i].c[2] = v.z; q[i].c[3] = v.w;
+    }
+    uint32_t P = (uint32_t)(4 * Pn + t);
+    E4 r = fold_quad(q[0], q[1], q[2], q[3], quad_xinv(tb, a, P), a);
+#pragma unroll
+    for (int c = 0; c < 4; c++) leaf[4 * t + c] = r.c[c];
+  }
+  uint4* dst = reinterpret_cast<uint4*>(a.out + 16 * Pn);
+#pragma unroll
+  for (int t = 0; t < 4; t++)
+    dst[t] = make_uint4(leaf[4 * t], leaf[4 * t + 1], leaf[4 * t + 2], leaf[4 * t + 3]);
+  uint32_t d[8];
+  blake3_leaf64(leaf, d);
+  store_digest(a.leaves + 8 * Pn, d);
+}
+
+// Thread per next-layer value (small layers; leaves hashed separately).
+__global__ void fri_fold_plain_kernel(FoldArgs a, Tables tb) {
+  uint32_t P = blockIdx.x * blockDim.x + threadIdx.x;
+  if (P >= (1u << (a.logn - 2))) return;
+  E4 q[4];
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    uint4 v = reinterpret_cast<const uint4*>(a.in)[4 * P + i];
+    q[i].c[0] = v.x; q[i].c[1] = v.y; q[i].c[2] = v.z; q[i].c[3] = v.w;
+  }
+  E4 r = fold_quad(q[0], q[1], q[2], q[3], quad_xinv(tb, a, P), a);
+  reinterpret_cast<uint4*>(a.out)[P] = make_uint4(r.c[0], r.c[1], r.c[2], r.c[3]);
+}
+
+// ------------------------------------------------------------------ PoW ----
+// Transcript::grind (src/transcript.rs:206-228): smallest nonce n with
+// BLAKE3(head || LE64(n)) having >= bits leading zero bits (MSB first). CTAs
+// take nonce chunks in increasing order from a counter and stop once a chunk
+// starts above the best nonce found: every chunk below the final minimum was
+// taken and finished, so the result equals the sequential scan. The chunk
+// counter is capped (max_chunks), after which the kernel sets status and
+// returns instead of spinning.
+constexpr int kGrindThreads = 256;
+constexpr int kGrindPerThread = 4;
+constexpr uint64_t kGrindChunk = (uint64_t)kGrindThreads * kGrindPerThread;
+
+struct GrindArgs {
+  uint32_t head[16];
+  uint32_t bits;
+  unsigned long long* best;
+  unsigned long long* next_chunk;
+  unsigned int* status;
+  unsigned long long max_chunks;
+};
+
+template <int H>
+__global__ void __launch_bounds__(kGrindThreads) grind_kernel(GrindArgs a) {
+  static_assert(H + 8 <= 64, "head and nonce must fit one block");
+  constexpr int W = H / 4, SH = (H % 4) * 8;
+  __shared__ unsigned long long s_chunk;
+  __shared__ int s_stop;
+  for (;;) {
+    if (threadIdx.x == 0) {
+      unsigned long long c = atomicAdd(a.next_chunk, 1ull);
+      s_chunk = c;
+      unsigned long long best = *reinterpret_cast<volatile unsigned long long*>(a.best);
+      s_stop = (c >= a.max_chunks) ? 2 : (c * kGrindChunk > best ? 1 : 0);
+      if (s_stop == 2) atomicOr(a.status, 1u);
+    }
+    __syncthreads();
+    unsigned long long c = s_chunk;
+    int stop = s_stop;
+    __syncthreads();
+    if (stop) return;
+#pragma unroll 1
+    for (int k = 0; k < kGrindPerThread; k++) {
+      unsigned long long nonce = c * kGrindChunk + (unsigned long long)k * kGrindThreads + threadIdx.x;
+      uint32_t lo = (uint32_t)nonce, hi = (uint32_t)(nonce >> 32);
+      uint32_t m[16];
+#pragma unroll
+      for (int i = 0; i < 16; i++) m[i] = i < W ? a.head[i] : 0u;
+      if (SH == 0) {
+        m[W] = lo;
+        m[W + 1] = hi;
+      } else {
+        m[W] = a.head[W] | (lo << SH);
+        m[W + 1] = (lo >> (32 - SH)) | (hi << SH);
+        m[W + 2] = hi >> (32 - SH);
+      }
+      uint32_t cv[8], o[8];
+      iv_words(cv);
+      blake3_compress(cv, m, 0u, 0u, (uint32_t)(H + 8), kChunkStart | kChunkEnd | kRoot, o);
+      uint32_t lz = __clz(__byte_perm(o[0], 0, 0x0123));
+      if (lz >= a.bits) atomicMin(a.best, nonce);
+    }
+  }
+}
+
+// Coset-major [c][j][q] -> natural [c][k], k = B q + j (for callers that
+// want reed_solomon_extend's natural order, src/ntt.rs:436-439).
+__global__ void coset_to_natural_kernel(const uint32_t* __restrict__ in, uint32_t* __restrict__ out,
+                                        uint32_t logN, uint32_t logB, uint64_t total) {
+  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= total) return;
+  const uint32_t logm = logN + logB;
+  uint64_t col = i >> logm;
+  uint32_t k = (uint32_t)(i & ((1ull << logm) - 1));
+  uint32_t j = k & ((1u << logB) - 1u), q = k >> logB;
+  out[i] = in[(col << logm) + ((uint64_t)j << logN) + q];
+}
+
+// --------------------------------------------------------------- gather ----
+__global__ void gather16_kernel(const uint64_t* __restrict__ addr, uint4* __restrict__ out,
+                                uint32_t n) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  out[i] = *reinterpret_cast<const uint4*>(addr[i]);
+}
+__global__ void gather4_kernel(const uint64_t* __restrict__ addr, uint32_t* __restrict__ out,
+                               uint32_t n) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  out[i] = *reinterpret_cast<const uint32_t*>(addr[i]);
+}
+
+}  // namespace
+
+// ============================================================= launchers ====
+namespace launch {
+
+static std::atomic<uint64_t> g_launches{0};
+static StageRecorder* g_recorder = nullptr;
+uint64_t launch_count() { return g_launches.load(); }
+void set_recorder(StageRecorder* r) { g_recorder = r; }
+
+// Counts the launches of one stage and brackets them with the recorder.
+struct Stage {
+  const char* name;
+  cudaStream_t st;
+  Stage(const char* n, cudaStream_t s) : name(n), st(s) {
+    if (g_recorder) g_recorder->begin(name, st);
+  }
+  ~Stage() {
+    if (g_recorder) g_recorder->end(name, st);
+  }
+  void launched(int k = 1) { g_launches += k; }
+};
+
+cudaError_t fib_trace(cudaStream_t st, uint32_t* col_a, uint32_t* col_b, uint32_t n, uint32_t a0,
+                      uint32_t b0, const uint32_t mats[32][4]) {
+  FibMats fm;
+  for (int k = 0; k < 32; k++)
+    for (int i = 0; i < 4; i++) fm.m[k][i] = mats[k][i];
+  uint32_t per = 64;
+  uint64_t threads = (n + per - 1) / per;
+  Stage stg("trace", st);
+  stg.launched();
+  fib_trace_kernel<<<grid_for(threads), kThreads, 0, st>>>(col_a, col_b, n, a0, b0, fm, per);
+  return cudaGetLastError();
+}
+
+cudaError_t fill_constant_columns(cudaStream_t st, uint32_t* cols, uint32_t n, uint32_t ncols,
+                                  const uint32_t* d_values) {
+  Stage stg("fill_columns", st);
+  stg.launched();
+  fill_columns_kernel<<<grid_for((uint64_t)n * ncols), kThreads, 0, st>>>(cols, n, ncols, d_values);
+  return cudaGetLastError();
+}
+
+cudaError_t ntt(cudaStream_t st, const Tables& tb, const NttPlan& plan, const uint32_t* in,
+                uint32_t* out, uint32_t* scratch) {
+  NttArgs a;
+  a.logn = plan.logn;
+  a.inverse = plan.inverse;
+  a.in_div = plan.in_div ? plan.in_div : 1;
+  a.twist_mod = plan.twist_mod ? plan.twist_mod : 1;
+  a.twist_shift = plan.twist_shift;
+  a.post_gamma = plan.post_gamma;
+  // n^-1 in Montgomery form: (2^-logn) * 2^32 mod p.
+  {
+    uint64_t inv2 = (kP + 1) / 2;  // 2^-1 mod p
+    uint64_t v = 1;
+    for (uint32_t i = 0; i < plan.logn; i++) v = v * inv2 % kP;
+    a.ninv_m = (uint32_t)((v << 32) % kP);
+  }
+  a.tb = tb;
+  const uint32_t n = 1u << plan.logn;
+  if (plan.logn <= 12) {
+    size_t smem = (size_t)(n + n / 2 + 1) * 4;
+    static bool attr_set = false;
+    if (!attr_set) {
+      cudaFuncSetAttribute(ntt_small_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 48 * 1024);
+      attr_set = true;
+    }
+    Stage stg(plan.inverse ? "intt" : "ntt", st);
+    stg.launched();
+    ntt_small_kernel<<<plan.batch, 256, smem, st>>>(in, out, a);
+    return cudaGetLastError();
+  }
+  const uint32_t logn1 = (plan.logn + 1) / 2;
+  const uint32_t logn2 = plan.logn - logn1;
+  const uint32_t n1 = 1u << logn1, n2 = 1u << logn2;
+  static bool attrs = false;
+  if (!attrs) {
+    const int maxs = 200 * 1024;
+    cudaFuncSetAttribute(ntt_pass1_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxs);
+    cudaFuncSetAttribute(ntt_pass1_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxs);
+    cudaFuncSetAttribute(ntt_pass2_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxs);
+    cudaFuncSetAttribute(ntt_pass2_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxs);
+    attrs = true;
+  }
+  // C = R = 8 columns per CTA (32-byte segments), 4 for the largest halves.
+  const int logc = logn1 > 12 ? 2 : 3;
+  size_t smem1 = ((size_t)(n1 << logc) + n1 / 2) * 4;
+  dim3 g1(n2 >> logc, plan.batch);
+  Stage stg(plan.inverse ? "intt" : "ntt", st);
+  stg.launched(2);
+  if (logc == 3)
+    ntt_pass1_kernel<3><<<g1, 512, smem1, st>>>(in, scratch, a, logn1);
+  else
+    ntt_pass1_kernel<2><<<g1, 512, smem1, st>>>(in, scratch, a, logn1);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  const int logr = logn2 > 12 ? 2 : 3;
+  size_t smem2 = ((size_t)(n2 + 1) * (1u << logr) + n2 / 2) * 4;
+  dim3 g2(n1 >> logr, plan.batch);
+  if (logr == 3)
+    ntt_pass2_kernel<3><<<g2, 512, smem2, st>>>(scratch, out, a, logn1);
+  else
+    ntt_pass2_kernel<2><<<g2, 512, smem2, st>>>(scratch, out, a, logn1);
+  (void)n;
+  return cudaGetLastError();
+}
+
+cudaError_t coset_zinv(cudaStream_t st, const Tables& tb, uint32_t* zinv, uint32_t* zinv2,
+                       uint32_t logB, uint32_t gamma_n_m) {
+  Stage stg("coset_zinv", st);
+  stg.launched();
+  coset_zinv_kernel<<<grid_for(1ull << logB), kThreads, 0, st>>>(zinv, zinv2, logB, gamma_n_m, tb);
+  return cudaGetLastError();
+}
+
+cudaError_t air_trace_leaves(cudaStream_t st, const uint32_t* lde_a, const uint32_t* lde_b,
+                             uint32_t* leaves, uint32_t logN, uint32_t logB) {
+  uint32_t nleaves = 1u << (logN + logB - 3);
+  Stage stg("trace_leaves", st);
+  stg.launched();
+  air_trace_leaves_kernel<<<grid_for(nleaves), kThreads, 0, st>>>(lde_a, lde_b, leaves, logN, logB,
+                                                                  nleaves);
+  return cudaGetLastError();
+}
+
+cudaError_t range_trace_leaves(cudaStream_t st, const uint32_t* lde, uint32_t* leaves,
+                               uint32_t logN, uint32_t logB, uint32_t ncols) {
+  if (ncols < 1 || ncols > 25) return cudaErrorInvalidValue;
+  Stage stg("trace_leaves", st);
+  stg.launched();
+  range_trace_leaves_kernel<<<grid_for(1ull << (logN + logB)), kThreads, 0, st>>>(lde, leaves, logN,
+                                                                                logB, ncols);
+  return cudaGetLastError();
+}
+
+cudaError_t merkle_build(cudaStream_t st, uint32_t* tree, uint64_t leaves) {
+  Stage stg("merkle_levels", st);
+  uint32_t level = 0;
+  while ((leaves >> level) > 2048) {
+    uint64_t cnt = leaves >> (level + 1);
+    const uint32_t* prev = tree + 8 * (2 * leaves - 2 * (leaves >> level));
+    uint32_t* next = tree + 8 * (2 * leaves - 2 * (leaves >> (level + 1)));
+    stg.launched();
+    merkle_level_kernel<<<grid_for(cnt), kThreads, 0, st>>>(prev, next, cnt);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    level++;
+  }
+  if ((leaves >> level) > 1) {
+    stg.launched();
+    merkle_tail_kernel<<<1, 1024, 0, st>>>(tree, leaves, level);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t air_compose_leaves(cudaStream_t st, const Tables& tb, const AirComposeArgs& a) {
+  uint32_t quarter = 1u << (a.logN + a.logB - 2);
+  Stage stg("air_compose_leaves", st);
+  stg.launched();
+  air_compose_leaves_kernel<<<grid_for(quarter), kThreads, 0, st>>>(a, tb);
+  return cudaGetLastError();
+}
+
+cudaError_t range_compose_leaves(cudaStream_t st, const Tables& tb, const RangeComposeArgs& a) {
+  uint32_t quarter = 1u << (a.logN + a.logB - 2);
+  Stage stg("range_compose_leaves", st);
+  stg.launched();
+  range_compose_leaves_kernel<<<grid_for(quarter), kThreads, 0, st>>>(a, tb);
+  return cudaGetLastError();
+}
+
+cudaError_t fri_fold(cudaStream_t st, const Tables& tb, const FoldArgs& a) {
+  if (a.logn < 2) return cudaErrorInvalidValue;
+  if (a.logn >= 4) {
+    uint64_t nleaf = 1ull << (a.logn - 4);
+    Stage stg("fri_fold_leaves", st);
+    stg.launched();
+    fri_fold_leaf_kernel<<<grid_for(nleaf, kFoldThreads), kFoldThreads, 0, st>>>(a, tb);
+    return cudaGetLastError();
+  }
+  {
+    Stage stg("fri_fold_small", st);
+    stg.launched();
+    fri_fold_plain_kernel<<<1, 32, 0, st>>>(a, tb);
+  }
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  return layer_leaves(st, a.out, 1ull << (a.logn - 2), a.leaves);
+}
+
+cudaError_t layer_leaves(cudaStream_t st, const uint32_t* values, uint64_t len, uint32_t* leaves) {
+  Stage stg("layer_leaves", st);
+  stg.launched();
+  if (len % 4 == 0) {
+    leaf64_kernel<<<grid_for(len / 4), kThreads, 0, st>>>(values, leaves, len / 4);
+  } else {
+    leaf16_kernel<<<grid_for(len), kThreads, 0, st>>>(values, leaves, len);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t merkle_flat64_leaves(cudaStream_t st, const uint32_t* flat, uint64_t nleaves,
+                                 uint32_t* leaves) {
+  Stage stg("leaf64", st);
+  stg.launched();
+  leaf64_kernel<<<grid_for(nleaves), kThreads, 0, st>>>(flat, leaves, nleaves);
+  return cudaGetLastError();
+}
+
+bool grind_supports(uint32_t head_len) { return head_len == 47; }
+
+cudaError_t grind(cudaStream_t st, const uint8_t* head, uint32_t head_len, uint32_t bits,
+                  unsigned long long* state, uint64_t max_nonces) {
+  if (!grind_supports(head_len) || bits > 32) return cudaErrorInvalidValue;
+  GrindArgs a;
+  for (int i = 0; i < 16; i++) a.head[i] = 0;
+  for (uint32_t i = 0; i < head_len; i++) a.head[i / 4] |= (uint32_t)head[i] << (8 * (i % 4));
+  a.bits = bits;
+  a.best = state;
+  a.next_chunk = state + 1;
+  a.status = reinterpret_cast<unsigned int*>(state + 2);
+  a.max_chunks = (max_nonces + kGrindChunk - 1) / kGrindChunk;
+  static int ctas = 0;
+  if (!ctas) {
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, grind_kernel<47>, kGrindThreads, 0);
+    ctas = sms * (per > 0 ? per : 1);
+  }
+  Stage stg("grind", st);
+  stg.launched();
+  grind_kernel<47><<<ctas, kGrindThreads, 0, st>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t coset_to_natural(cudaStream_t st, const uint32_t* in, uint32_t* out, uint32_t logN,
+                             uint32_t logB, uint64_t batch) {
+  uint64_t total = batch << (logN + logB);
+  Stage stg("coset_to_natural", st);
+  stg.launched();
+  coset_to_natural_kernel<<<grid_for(total), kThreads, 0, st>>>(in, out, logN, logB, total);
+  return cudaGetLastError();
+}
+
+cudaError_t gather16(cudaStream_t st, const uint64_t* addr, void* out, uint32_t n) {
+  if (!n) return cudaSuccess;
+  Stage stg("gather", st);
+  stg.launched();
+  gather16_kernel<<<grid_for(n), kThreads, 0, st>>>(addr, reinterpret_cast<uint4*>(out), n);
+  return cudaGetLastError();
+}
+cudaError_t gather4(cudaStream_t st, const uint64_t* addr, uint32_t* out, uint32_t n) {
+  if (!n) return cudaSuccess;
+  Stage stg("gather", st);
+  stg.launched();
+  gather4_kernel<<<grid_for(n), kThreads, 0, st>>>(addr, out, n);
+  return cudaGetLastError();
+}
+
+}  // namespace launch
+}  // namespace z0p

@@ -1,0 +1,1093 @@
+// GB300 prove path for z0p: device workspace, the Fibonacci-AIR and
+// range-check provers, and the C ABI declared in include/z0p_gpu.h.
+//
+// Dataflow of one AIR proof (src/air.rs:485-599), all stages on one stream:
+//   trace (parallel 2x2 matrix powers) -> iNTT of both columns, outputs
+//   pre-multiplied by 31^i / N -> 2B coset NTTs written coset-major ->
+//   trace leaves + tree -> [host: cap, alphas] -> composition written as
+//   bit-reversed FRI layer 0 with its leaf digests -> tree -> [host: cap,
+//   fold challenges] -> fold + next-layer leaves -> tree -> ... -> final
+//   layer -> [host: head] -> PoW grind -> [host: query indices] -> one
+//   gather of every opened value and path -> proof bytes on the host.
+// The host holds the transcript; each bracket is one stream synchronisation.
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/z0p_gpu.h"
+#include "host.h"
+#include "kernels.h"
+
+using namespace z0p;
+using namespace z0p::host;
+
+namespace z0p {
+namespace host {
+const char* reason();
+}
+}  // namespace z0p
+
+#define CK(expr)                                                              \
+  do {                                                                        \
+    cudaError_t _e = (expr);                                                  \
+    if (_e != cudaSuccess) {                                                  \
+      set_reason(std::string(#expr) + ": " + cudaGetErrorString(_e));         \
+      return _e == cudaErrorMemoryAllocation ? Z0P_ERR_OUT_OF_MEMORY : Z0P_ERR_CUDA; \
+    }                                                                         \
+  } while (0)
+
+#define RC(expr)              \
+  do {                        \
+    int _r = (expr);          \
+    if (_r != Z0P_OK) return _r; \
+  } while (0)
+
+namespace {
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+};
+
+// Little-endian byte writer (src/codec.rs:38-114).
+struct Writer {
+  std::vector<uint8_t> b;
+  void byte(uint8_t v) { b.push_back(v); }
+  void u32(uint32_t v) { for (int i = 0; i < 4; i++) b.push_back((uint8_t)(v >> (8 * i))); }
+  void u64(uint64_t v) { for (int i = 0; i < 8; i++) b.push_back((uint8_t)(v >> (8 * i))); }
+  void bytes(const void* p, size_t n) { b.insert(b.end(), (const uint8_t*)p, (const uint8_t*)p + n); }
+};
+
+// Host-built list of device addresses to fetch in one gather.
+struct Gather {
+  std::vector<uint64_t> a16;  // 16-byte granules
+  std::vector<uint64_t> a4;   // 4-byte words
+  size_t add16(const void* p, size_t granules) {
+    size_t at = a16.size();
+    for (size_t i = 0; i < granules; i++) a16.push_back((uint64_t)p + 16 * i);
+    return at;
+  }
+  size_t add4(const void* p) {
+    a4.push_back((uint64_t)p);
+    return a4.size() - 1;
+  }
+};
+
+}  // namespace
+
+// Per-stage CUDA-event timing on the launching stream (diagnostic mode).
+struct EventRecorder final : launch::StageRecorder {
+  struct Mark {
+    std::string stage;
+    cudaEvent_t a, b;
+  };
+  std::vector<Mark> marks;
+  std::vector<cudaEvent_t> pool;
+  cudaEvent_t take() {
+    if (!pool.empty()) {
+      cudaEvent_t e = pool.back();
+      pool.pop_back();
+      return e;
+    }
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    return e;
+  }
+  void begin(const char* stage, cudaStream_t st) override {
+    Mark m{stage, take(), take()};
+    cudaEventRecord(m.a, st);
+    marks.push_back(m);
+  }
+  void end(const char* stage, cudaStream_t st) override {
+    for (size_t i = marks.size(); i-- > 0;)
+      if (marks[i].stage == stage) {
+        cudaEventRecord(marks[i].b, st);
+        return;
+      }
+  }
+  ~EventRecorder() override {
+    for (auto& m : marks) { cudaEventDestroy(m.a); cudaEventDestroy(m.b); }
+    for (auto e : pool) cudaEventDestroy(e);
+  }
+};
+
+struct z0p_gpu_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::mutex mu;
+  Tables tb{};
+  DevBuf tables, cols, coeffs, scratch, lde, ttree, layers, ftrees, misc, gaddr, gout;
+  uint8_t* pinned = nullptr;
+  size_t pinned_bytes = 0;
+  size_t held = 0;
+  uint64_t h2d = 0, d2h = 0, syncs = 0, proofs = 0;
+  bool profiling = false;
+  EventRecorder rec;
+};
+
+namespace {
+
+cudaError_t h2d(z0p_gpu_ctx* c, void* dst, const void* src, size_t n) {
+  c->h2d += n;
+  return cudaMemcpyAsync(dst, src, n, cudaMemcpyHostToDevice, c->stream);
+}
+cudaError_t d2h(z0p_gpu_ctx* c, void* dst, const void* src, size_t n) {
+  c->d2h += n;
+  return cudaMemcpyAsync(dst, src, n, cudaMemcpyDeviceToHost, c->stream);
+}
+cudaError_t sync(z0p_gpu_ctx* c) {
+  c->syncs++;
+  return cudaStreamSynchronize(c->stream);
+}
+
+int ensure(z0p_gpu_ctx* c, DevBuf& b, size_t bytes) {
+  if (bytes <= b.bytes) return Z0P_OK;
+  if (b.p) {
+    CK(sync(c));
+    CK(cudaFree(b.p));
+    c->held -= b.bytes;
+    b.p = nullptr;
+    b.bytes = 0;
+  }
+  size_t want = bytes + bytes / 8;  // headroom so near sizes reuse the buffer
+  CK(cudaMalloc(&b.p, want));
+  b.bytes = want;
+  c->held += want;
+  return Z0P_OK;
+}
+
+int ensure_pinned(z0p_gpu_ctx* c, size_t bytes) {
+  if (bytes <= c->pinned_bytes) return Z0P_OK;
+  if (c->pinned) {
+    CK(sync(c));
+    CK(cudaFreeHost(c->pinned));
+  }
+  size_t want = bytes + bytes / 4 + 4096;
+  CK(cudaMallocHost((void**)&c->pinned, want));
+  c->pinned_bytes = want;
+  return Z0P_OK;
+}
+
+int build_tables(z0p_gpu_ctx* c) {
+  const int lo_w = 1 << 14, hi_w = 1 << 13, lo_g = 1 << 12, hi_g = 1 << 15;
+  std::vector<uint32_t> t(lo_w + hi_w + lo_g + hi_g);
+  uint32_t omega = two_adic_generator(27);
+  uint32_t* w_lo = t.data();
+  uint32_t* w_hi = w_lo + lo_w;
+  uint32_t* g_lo = w_hi + hi_w;
+  uint32_t* g_hi = g_lo + lo_g;
+  uint32_t x = 1;
+  for (int i = 0; i < lo_w; i++) { w_lo[i] = to_mont(x); x = fmul(x, omega); }
+  uint32_t step = fpow(omega, lo_w);
+  x = 1;
+  for (int i = 0; i < hi_w; i++) { w_hi[i] = to_mont(x); x = fmul(x, step); }
+  x = 1;
+  for (int i = 0; i < lo_g; i++) { g_lo[i] = to_mont(x); x = fmul(x, GENERATOR); }
+  step = fpow(GENERATOR, lo_g);
+  x = 1;
+  for (int i = 0; i < hi_g; i++) { g_hi[i] = to_mont(x); x = fmul(x, step); }
+  RC(ensure(c, c->tables, t.size() * 4));
+  CK(cudaMemcpy(c->tables.p, t.data(), t.size() * 4, cudaMemcpyHostToDevice));
+  const uint32_t* d = (const uint32_t*)c->tables.p;
+  c->tb.w_lo = d;
+  c->tb.w_hi = d + lo_w;
+  c->tb.g_lo = d + lo_w + hi_w;
+  c->tb.g_hi = d + lo_w + hi_w + lo_g;
+  return Z0P_OK;
+}
+
+inline uint64_t tree_digests(uint64_t leaves) { return 2 * leaves - 1; }
+inline uint64_t level_off(uint64_t leaves, uint32_t l) { return 2 * leaves - 2 * (leaves >> l); }
+
+// One FRI commitment + opening over layer 0 (already written with its leaf
+// digests) — src/fri.rs:551-666 from the first layer-root absorb onward.
+struct FriOut {
+  std::vector<std::vector<uint8_t>> caps;
+  std::vector<uint32_t> final_vals;
+  uint64_t nonce = 0;
+  std::vector<uint64_t> indices;
+};
+
+struct FriBufs {
+  std::vector<uint32_t*> layer;  // device values per layer (layer 0 included)
+  std::vector<uint32_t*> tree;   // device trees per layer
+};
+
+int plan_fri_buffers(z0p_gpu_ctx* c, const FriShape& s, FriBufs* fb) {
+  size_t vals = 0, digs = 0;
+  for (size_t i = 0; i < s.len.size(); i++) {
+    vals += 4 * s.len[i];
+    digs += 8 * tree_digests(s.leaves[i]);
+  }
+  RC(ensure(c, c->layers, vals * 4));
+  RC(ensure(c, c->ftrees, digs * 4));
+  uint32_t* v = (uint32_t*)c->layers.p;
+  uint32_t* d = (uint32_t*)c->ftrees.p;
+  fb->layer.clear();
+  fb->tree.clear();
+  for (size_t i = 0; i < s.len.size(); i++) {
+    fb->layer.push_back(v);
+    fb->tree.push_back(d);
+    v += 4 * s.len[i];
+    d += 8 * tree_digests(s.leaves[i]);
+  }
+  return Z0P_OK;
+}
+
+int fetch_cap(z0p_gpu_ctx* c, const uint32_t* tree, uint64_t leaves, uint32_t drop,
+              std::vector<uint8_t>* out) {
+  uint32_t depth = log2u(leaves);
+  uint64_t n = 1ull << drop;
+  out->resize(32 * n);
+  RC(ensure_pinned(c, 32 * n));
+  CK(d2h(c, c->pinned, tree + 8 * level_off(leaves, depth - drop), 32 * n));
+  CK(sync(c));
+  std::memcpy(out->data(), c->pinned, 32 * n);
+  return Z0P_OK;
+}
+
+int run_fri(z0p_gpu_ctx* c, const FriShape& s, const FriParams& fp, const FriBufs& fb,
+            uint64_t poly_len, uint64_t degree_bound, z0p_transcript_state* ts, FriOut* out,
+            bool dims_absorbed) {
+  if (!dims_absorbed) {
+    uint8_t dims[24];  // src/fri.rs:1450-1456
+    for (int i = 0; i < 8; i++) {
+      dims[i] = (uint8_t)(s.m >> (8 * i));
+      dims[8 + i] = (uint8_t)(poly_len >> (8 * i));
+      dims[16 + i] = (uint8_t)(degree_bound >> (8 * i));
+    }
+    transcript_absorb(ts, "fri-dims", dims, 24);
+  }
+  const uint32_t unit_m = to_mont(two_adic_generator(2));
+  out->caps.assign(s.len.size(), {});
+  for (size_t l = 0;; l++) {
+    RC(fetch_cap(c, fb.tree[l], s.leaves[l], s.drop[l], &out->caps[l]));
+    for (size_t k = 0; k < out->caps[l].size() / 32; k++)
+      transcript_absorb(ts, "fri-layer-root", out->caps[l].data() + 32 * k, 32);
+    if (l + 1 == s.len.size()) break;
+    FoldArgs fa;
+    uint32_t ch[3][4];
+    for (int k = 0; k < 3; k++) challenge_ext(ts, "fri-fold", ch[k]);
+    for (int k = 0; k < 3; k++)
+      for (int e = 0; e < 4; e++) fa.ch[k][e] = to_mont(ch[k][e]);
+    fa.in = fb.layer[l];
+    fa.out = fb.layer[l + 1];
+    fa.leaves = fb.tree[l + 1];
+    fa.logn = log2u(s.len[l]);
+    // layer-l domain is 31^(4^l) <omega_len>; its inverse shift:
+    uint32_t g = GENERATOR;
+    for (size_t i = 0; i < l; i++) g = fpow(g, 4);
+    fa.ginv_m = to_mont(finv(g));
+    fa.unit_m = unit_m;
+    CK(launch::fri_fold(c->stream, c->tb, fa));
+    if (s.leaves[l + 1] > 1) CK(launch::merkle_build(c->stream, fb.tree[l + 1], s.leaves[l + 1]));
+  }
+  // Final layer in the clear (src/fri.rs:620-621).
+  uint64_t fl = s.len.back();
+  out->final_vals.resize(4 * fl);
+  RC(ensure_pinned(c, 16 * fl));
+  CK(d2h(c, c->pinned, fb.layer.back(), 16 * fl));
+  CK(sync(c));
+  std::memcpy(out->final_vals.data(), c->pinned, 16 * fl);
+  transcript_absorb(ts, "fri-final", (const uint8_t*)out->final_vals.data(), 16 * fl);
+  // Proof of work (src/fri.rs:645-650, src/transcript.rs:206-228).
+  out->nonce = 0;
+  if (fp.grinding_bits > 0) {
+    std::vector<uint8_t> head = pow_head(ts, "fri-pow");
+    RC(ensure(c, c->misc, 64));
+    unsigned long long init[3] = {~0ull, 0ull, 0ull};
+    CK(h2d(c, c->misc.p, init, sizeof init));
+    CK(launch::grind(c->stream, head.data(), (uint32_t)head.size(), fp.grinding_bits,
+                     (unsigned long long*)c->misc.p, 1ull << 40));
+    RC(ensure_pinned(c, 24));
+    CK(d2h(c, c->pinned, c->misc.p, 24));
+    CK(sync(c));
+    unsigned long long res[3];
+    std::memcpy(res, c->pinned, 24);
+    if ((res[2] & 0xffffffffull) != 0 || res[0] == ~0ull) {
+      set_reason("proof-of-work search reached its nonce cap without a solution");
+      return Z0P_ERR_DEVICE_TIMEOUT;
+    }
+    out->nonce = res[0];
+    uint8_t nb[8];
+    for (int i = 0; i < 8; i++) nb[i] = (uint8_t)(out->nonce >> (8 * i));
+    transcript_absorb(ts, "fri-pow", nb, 8);
+  }
+  out->indices.resize(fp.num_queries);
+  for (uint64_t i = 0; i < fp.num_queries; i++) out->indices[i] = challenge_index(ts, "fri-query", s.m);
+  return Z0P_OK;
+}
+
+// Queues the FRI openings (src/fri.rs:1229-1260) of every query: the four
+// quad values and the capped path of each non-final layer.
+struct FriOpenRefs {
+  std::vector<size_t> vals;   // per (query, depth): gather16 offset of 4 granules
+  std::vector<size_t> paths;  // per (query, depth): gather16 offset of path digests
+};
+
+void queue_fri_openings(const FriShape& s, const FriBufs& fb, const FriOut& fo, Gather* g,
+                        FriOpenRefs* r) {
+  size_t L = s.len.size() - 1;
+  for (size_t qi = 0; qi < fo.indices.size(); qi++) {
+    uint64_t index = fo.indices[qi];
+    for (size_t d = 0; d < L; d++) {
+      uint64_t base = index / 4 * 4;
+      r->vals.push_back(g->add16(fb.layer[d] + 4 * base, 4));
+      uint64_t Q = base / 4;
+      r->paths.push_back(g->a16.size());
+      uint32_t steps = s.depth[d] - s.drop[d];
+      for (uint32_t st = 0; st < steps; st++) {
+        uint64_t sib = (Q >> st) ^ 1;
+        g->add16(fb.tree[d] + 8 * (level_off(s.leaves[d], st) + sib), 2);
+      }
+      index /= 4;
+    }
+  }
+}
+
+int run_gather(z0p_gpu_ctx* c, const Gather& g, std::vector<uint8_t>* out16,
+               std::vector<uint32_t>* out4) {
+  size_t n16 = g.a16.size(), n4 = g.a4.size();
+  RC(ensure(c, c->gaddr, 8 * (n16 + n4) + 16));
+  RC(ensure(c, c->gout, 16 * n16 + 4 * n4 + 16));
+  size_t addr_bytes = 8 * (n16 + n4), out_bytes = 16 * n16 + 4 * n4;
+  RC(ensure_pinned(c, addr_bytes > out_bytes ? addr_bytes : out_bytes));
+  std::memcpy(c->pinned, g.a16.data(), 8 * n16);
+  std::memcpy(c->pinned + 8 * n16, g.a4.data(), 8 * n4);
+  CK(h2d(c, c->gaddr.p, c->pinned, addr_bytes));
+  uint64_t* da = (uint64_t*)c->gaddr.p;
+  uint8_t* dout = (uint8_t*)c->gout.p;
+  CK(launch::gather16(c->stream, da, dout, (uint32_t)n16));
+  CK(launch::gather4(c->stream, da + n16, (uint32_t*)(dout + 16 * n16), (uint32_t)n4));
+  CK(d2h(c, c->pinned, dout, out_bytes));
+  CK(sync(c));
+  out16->assign(c->pinned, c->pinned + 16 * n16);
+  out4->resize(n4);
+  std::memcpy(out4->data(), c->pinned + 16 * n16, 4 * n4);
+  return Z0P_OK;
+}
+
+void write_path(Writer& w, const uint8_t* digests, uint64_t leaf, uint32_t steps) {
+  w.u32(steps);  // src/codec.rs:95-101: digest then direction byte (1 = left)
+  for (uint32_t s = 0; s < steps; s++) {
+    w.bytes(digests + 32 * s, 32);
+    w.byte(((leaf >> s) & 1) == 0 ? 1 : 0);
+  }
+}
+
+void write_fri(Writer& w, const FriShape& s, const FriOut& fo, uint64_t poly_len,
+               uint64_t degree_bound, const std::vector<uint8_t>& g16, const FriOpenRefs& r) {
+  w.u64(s.m);  // Commitment::write_body (src/fri.rs:896-904)
+  w.u64(poly_len);
+  w.u64(degree_bound);
+  w.u32((uint32_t)fo.caps.size());
+  for (auto& cap : fo.caps) {
+    w.u32((uint32_t)(cap.size() / 32));
+    w.bytes(cap.data(), cap.size());
+  }
+  w.u32((uint32_t)(fo.final_vals.size() / 4));  // Proof::write_body (src/fri.rs:352-368)
+  w.bytes(fo.final_vals.data(), 4 * fo.final_vals.size());
+  w.u64(fo.nonce);
+  w.u32((uint32_t)fo.indices.size());
+  size_t L = s.len.size() - 1, k = 0;
+  for (size_t qi = 0; qi < fo.indices.size(); qi++) {
+    w.u32((uint32_t)L);
+    uint64_t index = fo.indices[qi];
+    for (size_t d = 0; d < L; d++, k++) {
+      w.bytes(g16.data() + 16 * r.vals[k], 64);
+      write_path(w, g16.data() + 16 * r.paths[k], index / 4, s.depth[d] - s.drop[d]);
+      index /= 4;
+    }
+  }
+}
+
+int air_shape(const z0p_air_params& p, FriParams* fp, FriShape* s) {
+  RC(air_validate(p));
+  // fri_params (src/air.rs:163-169) then commit_ext_evals_owned's checks.
+  RC(fri_params_new(p.blowup, p.num_queries, p.final_size, fp));
+  fp->grinding_bits = p.grinding_bits;
+  fp->cap_height = p.cap_height;
+  return fri_shape(p.n_steps * p.blowup, p.n_steps - 1, *fp, s);
+}
+
+int range_shape(const z0p_range_params& p, FriParams* fp, FriShape* s) {
+  RC(range_validate(p));
+  RC(fri_params_new(p.blowup, p.num_queries, p.final_size, fp));
+  fp->grinding_bits = p.grinding_bits;
+  fp->cap_height = p.cap_height;
+  return fri_shape(p.n_rows * p.blowup, p.n_rows - 1, *fp, s);
+}
+
+uint64_t air_size(const z0p_air_params& p, const FriShape& s) {
+  uint64_t m = s.m, leaves = m / 8;
+  uint32_t depth = log2u(leaves), drop = p.cap_height < depth ? (uint32_t)p.cap_height : depth;
+  uint64_t st = depth - drop;  // src/air.rs:262-281
+  return 1 + 4 + 32 * (1ull << drop) + fri_bytes(s, p.num_queries) + 4 +
+         p.num_queries * (8 + 16 + 4 + 33 * st + 4 + 33 * st + 128);
+}
+
+uint64_t range_size(const z0p_range_params& p, const FriShape& s) {
+  uint32_t depth = log2u(s.m), drop = p.cap_height < depth ? (uint32_t)p.cap_height : depth;
+  uint64_t st = depth - drop;  // src/range.rs:253-269
+  return 1 + 4 + 32 * (1ull << drop) + fri_bytes(s, p.num_queries) + 4 +
+         p.num_queries * (8 + 4 + 4 + 4 * p.n_bits + 4 + 33 * st);
+}
+
+void fib_mats(uint32_t mats[32][4]) {
+  uint32_t m00 = 0, m01 = 1, m10 = 1, m11 = 1;  // M = [[0,1],[1,1]]
+  for (int k = 0; k < 32; k++) {
+    mats[k][0] = m00; mats[k][1] = m01; mats[k][2] = m10; mats[k][3] = m11;
+    uint32_t n00 = fadd(fmul(m00, m00), fmul(m01, m10));
+    uint32_t n01 = fadd(fmul(m00, m01), fmul(m01, m11));
+    uint32_t n10 = fadd(fmul(m10, m00), fmul(m11, m10));
+    uint32_t n11 = fadd(fmul(m10, m01), fmul(m11, m11));
+    m00 = n00; m01 = n01; m10 = n10; m11 = n11;
+  }
+}
+
+// src/air.rs:365-372 -> 485-599 on the device.
+int air_prove(z0p_gpu_ctx* c, const z0p_air_params& p, z0p_transcript_state* ts, uint8_t* out,
+              size_t cap, size_t* len) {
+  FriParams fp;
+  FriShape s;
+  RC(air_shape(p, &fp, &s));
+  uint64_t need = air_size(p, s);
+  if (len) *len = need;
+  if (!out || cap < need) {
+    set_reason("output buffer too small for the proof");
+    return Z0P_ERR_BUFFER_TOO_SMALL;
+  }
+  const uint64_t N = p.n_steps, B = p.blowup, m = N * B;
+  const uint32_t logN = log2u(N), logB = log2u(B), logm = logN + logB;
+  cudaStream_t st = c->stream;
+
+  RC(ensure(c, c->cols, 8 * N));
+  RC(ensure(c, c->coeffs, 8 * N));
+  RC(ensure(c, c->scratch, 8 * m));
+  RC(ensure(c, c->lde, 8 * m));
+  RC(ensure(c, c->ttree, 32 * tree_digests(m / 8)));
+  RC(ensure(c, c->misc, 64 + 8 * B));
+  FriBufs fb;
+  RC(plan_fri_buffers(c, s, &fb));
+  uint32_t* cols = (uint32_t*)c->cols.p;
+  uint32_t* coeffs = (uint32_t*)c->coeffs.p;
+  uint32_t* lde = (uint32_t*)c->lde.p;
+  uint32_t* ttree = (uint32_t*)c->ttree.p;
+  uint32_t* zinv = (uint32_t*)c->misc.p + 16;
+  uint32_t* zinv2 = zinv + B;
+
+  // absorb_params (src/air.rs:754-766)
+  uint8_t pb[56];
+  auto p64 = [&](int off, uint64_t v) { for (int i = 0; i < 8; i++) pb[off + i] = (uint8_t)(v >> (8 * i)); };
+  auto p32 = [&](int off, uint32_t v) { for (int i = 0; i < 4; i++) pb[off + i] = (uint8_t)(v >> (8 * i)); };
+  p64(0, p.n_steps); p64(8, p.blowup); p64(16, p.num_queries); p64(24, p.final_size);
+  p32(32, p.grinding_bits); p64(36, p.cap_height); p32(44, p.a0); p32(48, p.b0); p32(52, p.b_last);
+  transcript_absorb(ts, "fib/params", pb, 56);
+
+  // Trace, interpolation (times 31^i / N), coset LDE of both columns.
+  uint32_t mats[32][4];
+  fib_mats(mats);
+  CK(launch::fib_trace(st, cols, cols + N, (uint32_t)N, p.a0, p.b0, mats));
+  NttPlan ip;
+  ip.logn = logN; ip.batch = 2; ip.inverse = 1; ip.post_gamma = 1;
+  CK(launch::ntt(st, c->tb, ip, cols, coeffs, (uint32_t*)c->scratch.p));
+  NttPlan lp;
+  lp.logn = logN; lp.batch = 2 * (uint32_t)B; lp.in_div = (uint32_t)B; lp.twist_mod = (uint32_t)B;
+  lp.twist_shift = 27 - logm;
+  CK(launch::ntt(st, c->tb, lp, coeffs, lde, (uint32_t*)c->scratch.p));
+  const uint32_t* lde_a = lde;
+  const uint32_t* lde_b = lde + m;
+
+  // Joint trace tree over 8-row 64-byte leaves (src/air.rs:520-537).
+  uint64_t tleaves = m / 8;
+  uint32_t tdepth = log2u(tleaves), tdrop = p.cap_height < tdepth ? (uint32_t)p.cap_height : tdepth;
+  CK(launch::air_trace_leaves(st, lde_a, lde_b, ttree, logN, logB));
+  if (tleaves > 1) CK(launch::merkle_build(st, ttree, tleaves));
+  uint32_t gamma_n = fpow(GENERATOR, N);
+  CK(launch::coset_zinv(st, c->tb, zinv, zinv2, logB, to_mont(gamma_n)));
+  std::vector<uint8_t> column_cap;
+  RC(fetch_cap(c, ttree, tleaves, tdrop, &column_cap));
+  transcript_absorb(ts, "fib/trace", column_cap.data(), column_cap.size());
+  uint32_t alpha[5][4];
+  for (int k = 0; k < 5; k++) challenge_ext(ts, "fib/alpha", alpha[k]);
+
+  // Composition as bit-reversed FRI layer 0 with its leaves (src/air.rs:847-929).
+  AirComposeArgs ca;
+  ca.lde_a = lde_a; ca.lde_b = lde_b; ca.zinv = zinv;
+  ca.layer0 = fb.layer[0]; ca.leaves = fb.tree[0];
+  ca.logN = logN; ca.logB = logB;
+  ca.a0 = p.a0; ca.b0 = p.b0; ca.b_last = p.b_last;
+  uint32_t omega_n = two_adic_generator(logN);
+  ca.w_last_m = to_mont(fpow(omega_n, N - 1));
+  for (int k = 0; k < 5; k++)
+    for (int e = 0; e < 4; e++) ca.alpha[k][e] = to_mont(alpha[k][e]);
+  CK(launch::air_compose_leaves(st, c->tb, ca));
+  if (s.leaves[0] > 1) CK(launch::merkle_build(st, fb.tree[0], s.leaves[0]));
+
+  FriOut fo;
+  RC(run_fri(c, s, fp, fb, m, N - 1, ts, &fo, false));
+
+  // Openings: FRI queries plus the two trace leaves per query (src/air.rs:565-591).
+  Gather g;
+  FriOpenRefs fr;
+  queue_fri_openings(s, fb, fo, &g, &fr);
+  std::vector<size_t> trow, tpath;
+  uint32_t tsteps = tdepth - tdrop;
+  for (uint64_t leaf : fo.indices) {
+    uint64_t index = brev(leaf, logm);
+    uint64_t shifted = (index + B) % m;
+    for (uint64_t at : {index, shifted}) {
+      uint64_t base = at & ~7ull;
+      trow.push_back(g.a4.size());
+      for (uint64_t r = 0; r < 8; r++) {
+        uint64_t k = base + r, j = k & (B - 1), q = k >> logB;
+        g.add4(lde_a + j * N + q);
+        g.add4(lde_b + j * N + q);
+      }
+      tpath.push_back(g.a16.size());
+      uint64_t L = base / 8;
+      for (uint32_t sx = 0; sx < tsteps; sx++)
+        g.add16(ttree + 8 * (level_off(tleaves, sx) + ((L >> sx) ^ 1)), 2);
+    }
+  }
+  std::vector<uint8_t> g16;
+  std::vector<uint32_t> g4;
+  RC(run_gather(c, g, &g16, &g4));
+
+  Writer w;  // air::Proof::to_bytes (src/air.rs:262-281)
+  w.b.reserve(need);
+  w.byte(6);
+  w.u32((uint32_t)(column_cap.size() / 32));
+  w.bytes(column_cap.data(), column_cap.size());
+  write_fri(w, s, fo, m, N - 1, g16, fr);
+  w.u32((uint32_t)fo.indices.size());
+  for (size_t qi = 0; qi < fo.indices.size(); qi++) {
+    uint64_t index = brev(fo.indices[qi], logm);
+    uint64_t shifted = (index + B) % m;
+    const uint32_t* rows = g4.data() + trow[2 * qi];
+    const uint32_t* srows = g4.data() + trow[2 * qi + 1];
+    w.u64(index);
+    w.u32(rows[2 * (index & 7)]);
+    w.u32(rows[2 * (index & 7) + 1]);
+    w.u32(srows[2 * (shifted & 7)]);
+    w.u32(srows[2 * (shifted & 7) + 1]);
+    write_path(w, g16.data() + 16 * tpath[2 * qi], index / 8, tsteps);
+    write_path(w, g16.data() + 16 * tpath[2 * qi + 1], shifted / 8, tsteps);
+    w.bytes(rows, 64);
+    w.bytes(srows, 64);
+  }
+  if (w.b.size() != need) {
+    set_reason("internal error: proof length differs from its shape");
+    return Z0P_ERR_CUDA;
+  }
+  std::memcpy(out, w.b.data(), need);
+  return Z0P_OK;
+}
+
+// src/range.rs:337-343 -> 353-375 -> 425-514 on the device.
+int range_prove(z0p_gpu_ctx* c, const z0p_range_params& p, z0p_transcript_state* ts, uint8_t* out,
+                size_t cap, size_t* len) {
+  FriParams fp;
+  FriShape s;
+  RC(range_shape(p, &fp, &s));
+  uint64_t need = range_size(p, s);
+  if (len) *len = need;
+  if (!out || cap < need) {
+    set_reason("output buffer too small for the proof");
+    return Z0P_ERR_BUFFER_TOO_SMALL;
+  }
+  const uint64_t N = p.n_rows, B = p.blowup, m = N * B, ncol = p.n_bits + 1;
+  const uint32_t logN = log2u(N), logB = log2u(B), logm = logN + logB;
+  cudaStream_t st = c->stream;
+  RC(ensure(c, c->cols, 4 * N * ncol));
+  RC(ensure(c, c->coeffs, 4 * N * ncol));
+  RC(ensure(c, c->scratch, 4 * m * ncol));
+  RC(ensure(c, c->lde, 4 * m * ncol));
+  RC(ensure(c, c->ttree, 32 * tree_digests(m)));
+  RC(ensure(c, c->misc, 64 + 8 * B + 4 * ncol + 16 * (ncol + 1)));
+  FriBufs fb;
+  RC(plan_fri_buffers(c, s, &fb));
+  uint32_t* cols = (uint32_t*)c->cols.p;
+  uint32_t* coeffs = (uint32_t*)c->coeffs.p;
+  uint32_t* lde = (uint32_t*)c->lde.p;
+  uint32_t* ttree = (uint32_t*)c->ttree.p;
+  uint32_t* zinv = (uint32_t*)c->misc.p + 16;
+  uint32_t* zinv2 = zinv + B;
+  uint32_t* dvals = zinv2 + B;
+  uint32_t* dalpha = dvals + ncol;
+
+  // build_columns (src/range.rs:316-330): V = value, C_j = bit j of value.
+  std::vector<uint32_t> vals(ncol);
+  vals[0] = p.value;
+  for (uint64_t j = 0; j < p.n_bits; j++) vals[1 + j] = j < 32 ? (p.value >> j) & 1 : 0;
+  RC(ensure_pinned(c, 4 * ncol));
+  std::memcpy(c->pinned, vals.data(), 4 * ncol);
+  CK(h2d(c, dvals, c->pinned, 4 * ncol));
+  CK(launch::fill_constant_columns(st, cols, (uint32_t)N, (uint32_t)ncol, dvals));
+  NttPlan ip;
+  ip.logn = logN; ip.batch = (uint32_t)ncol; ip.inverse = 1; ip.post_gamma = 1;
+  CK(launch::ntt(st, c->tb, ip, cols, coeffs, (uint32_t*)c->scratch.p));
+
+  uint8_t pb[56];  // absorb_params (src/range.rs:634-645)
+  auto p64 = [&](int off, uint64_t v) { for (int i = 0; i < 8; i++) pb[off + i] = (uint8_t)(v >> (8 * i)); };
+  auto p32 = [&](int off, uint32_t v) { for (int i = 0; i < 4; i++) pb[off + i] = (uint8_t)(v >> (8 * i)); };
+  p64(0, p.n_rows); p64(8, p.n_bits); p64(16, p.blowup); p64(24, p.num_queries);
+  p64(32, p.final_size); p32(40, p.grinding_bits); p64(44, p.cap_height); p32(52, p.value);
+  transcript_absorb(ts, "range/params", pb, 56);
+
+  NttPlan lp;
+  lp.logn = logN; lp.batch = (uint32_t)(ncol * B); lp.in_div = (uint32_t)B; lp.twist_mod = (uint32_t)B;
+  lp.twist_shift = 27 - logm;
+  CK(launch::ntt(st, c->tb, lp, coeffs, lde, (uint32_t*)c->scratch.p));
+  uint32_t tdepth = logm, tdrop = p.cap_height < tdepth ? (uint32_t)p.cap_height : tdepth;
+  CK(launch::range_trace_leaves(st, lde, ttree, logN, logB, (uint32_t)ncol));
+  if (m > 1) CK(launch::merkle_build(st, ttree, m));
+  CK(launch::coset_zinv(st, c->tb, zinv, zinv2, logB, to_mont(fpow(GENERATOR, N))));
+  std::vector<uint8_t> column_cap;
+  RC(fetch_cap(c, ttree, m, tdrop, &column_cap));
+  transcript_absorb(ts, "range/column", column_cap.data(), column_cap.size());
+  std::vector<uint32_t> alphas(4 * (ncol + 1));
+  for (uint64_t k = 0; k < ncol + 1; k++) {  // decomposition, n_bits booleans, boundary
+    uint32_t a[4];
+    challenge_ext(ts, "range/alpha", a);
+    for (int e = 0; e < 4; e++) alphas[4 * k + e] = to_mont(a[e]);
+  }
+  RC(ensure_pinned(c, 4 * alphas.size()));
+  std::memcpy(c->pinned, alphas.data(), 4 * alphas.size());
+  CK(h2d(c, dalpha, c->pinned, 4 * alphas.size()));
+
+  RangeComposeArgs ca;
+  ca.lde = lde; ca.zinv = zinv; ca.zinv2 = zinv2; ca.alphas = dalpha;
+  ca.layer0 = fb.layer[0]; ca.leaves = fb.tree[0];
+  ca.logN = logN; ca.logB = logB; ca.n_bits = (uint32_t)p.n_bits; ca.value = p.value;
+  CK(launch::range_compose_leaves(st, c->tb, ca));
+  if (s.leaves[0] > 1) CK(launch::merkle_build(st, fb.tree[0], s.leaves[0]));
+
+  FriOut fo;
+  RC(run_fri(c, s, fp, fb, m, N - 1, ts, &fo, false));
+
+  Gather g;
+  FriOpenRefs fr;
+  queue_fri_openings(s, fb, fo, &g, &fr);
+  std::vector<size_t> trow, tpath;
+  uint32_t tsteps = tdepth - tdrop;
+  for (uint64_t leaf : fo.indices) {
+    uint64_t index = brev(leaf, logm), j = index & (B - 1), q = index >> logB;
+    trow.push_back(g.a4.size());
+    for (uint64_t col = 0; col < ncol; col++) g.add4(lde + col * m + j * N + q);
+    tpath.push_back(g.a16.size());
+    for (uint32_t sx = 0; sx < tsteps; sx++)
+      g.add16(ttree + 8 * (level_off(m, sx) + ((index >> sx) ^ 1)), 2);
+  }
+  std::vector<uint8_t> g16;
+  std::vector<uint32_t> g4;
+  RC(run_gather(c, g, &g16, &g4));
+
+  Writer w;  // range::Proof::to_bytes (src/range.rs:253-269)
+  w.b.reserve(need);
+  w.byte(6);
+  w.u32((uint32_t)(column_cap.size() / 32));
+  w.bytes(column_cap.data(), column_cap.size());
+  write_fri(w, s, fo, m, N - 1, g16, fr);
+  w.u32((uint32_t)fo.indices.size());
+  for (size_t qi = 0; qi < fo.indices.size(); qi++) {
+    uint64_t index = brev(fo.indices[qi], logm);
+    const uint32_t* row = g4.data() + trow[qi];
+    w.u64(index);
+    w.u32(row[0]);
+    w.u32((uint32_t)p.n_bits);
+    for (uint64_t b = 0; b < p.n_bits; b++) w.u32(row[1 + b]);
+    write_path(w, g16.data() + 16 * tpath[qi], index, tsteps);
+  }
+  if (w.b.size() != need) {
+    set_reason("internal error: proof length differs from its shape");
+    return Z0P_ERR_CUDA;
+  }
+  std::memcpy(out, w.b.data(), need);
+  return Z0P_OK;
+}
+
+int with_device(z0p_gpu_ctx* c) {
+  CK(cudaSetDevice(c->device));
+  return Z0P_OK;
+}
+
+}  // namespace
+
+// ================================================================ C ABI ====
+extern "C" {
+
+int z0p_gpu_abi_version(void) { return Z0P_GPU_ABI_VERSION; }
+const char* z0p_gpu_last_reason(void) { return z0p::host::reason(); }
+
+int z0p_transcript_init(z0p_transcript_state* st, const uint8_t* label, size_t len) {
+  if (!st || (!label && len)) return Z0P_ERR_INVALID_ARGUMENT;
+  transcript_init(st, label, len);
+  return Z0P_OK;
+}
+int z0p_transcript_absorb(z0p_transcript_state* st, const uint8_t* label, size_t llen,
+                          const uint8_t* data, size_t dlen) {
+  if (!st || (!label && llen) || (!data && dlen)) return Z0P_ERR_INVALID_ARGUMENT;
+  transcript_absorb_raw(st, label, llen, data, dlen);
+  return Z0P_OK;
+}
+int z0p_transcript_challenge_bytes(z0p_transcript_state* st, const uint8_t* label, size_t llen,
+                                   uint8_t out[32]) {
+  if (!st || !out || (!label && llen)) return Z0P_ERR_INVALID_ARGUMENT;
+  squeeze_raw(st, label, llen, out);
+  return Z0P_OK;
+}
+int z0p_transcript_challenge_ext(z0p_transcript_state* st, const uint8_t* label, size_t llen,
+                                 uint32_t out[4]) {
+  if (!st || !out || (!label && llen)) return Z0P_ERR_INVALID_ARGUMENT;
+  uint8_t b[32];
+  squeeze_raw(st, label, llen, b);
+  for (int i = 0; i < 4; i++)
+    out[i] = ((uint32_t)b[4 * i] | ((uint32_t)b[4 * i + 1] << 8) | ((uint32_t)b[4 * i + 2] << 16) |
+              ((uint32_t)b[4 * i + 3] << 24)) % P;
+  return Z0P_OK;
+}
+int z0p_transcript_challenge_index(z0p_transcript_state* st, const uint8_t* label, size_t llen,
+                                   uint64_t domain, uint64_t* out) {
+  if (!st || !out || (!label && llen)) return Z0P_ERR_INVALID_ARGUMENT;
+  if (!is_pow2(domain)) {
+    set_reason("challenge_index domain must be a nonzero power of two");
+    return Z0P_ERR_MALFORMED_INPUT;
+  }
+  uint8_t b[32];
+  squeeze_raw(st, label, llen, b);
+  uint64_t v = 0;
+  for (int i = 0; i < 8; i++) v |= (uint64_t)b[i] << (8 * i);
+  *out = v & (domain - 1);
+  return Z0P_OK;
+}
+
+int z0p_air_params_new(uint64_t n, uint64_t blowup, uint64_t q, uint64_t final_size, uint32_t a0,
+                       uint32_t b0, uint32_t b_last, z0p_air_params* o) {
+  if (!o) return Z0P_ERR_INVALID_ARGUMENT;  // src/air.rs:62-102
+  if (n < 2 || !is_pow2(n)) return Z0P_ERR_INVALID_DOMAIN_SIZE;
+  if (blowup < 4 || !is_pow2(blowup)) return Z0P_ERR_INVALID_BLOWUP;
+  if (q == 0) return Z0P_ERR_NO_QUERIES;
+  if (final_size < 2 || !is_pow2(final_size)) return Z0P_ERR_INVALID_DOMAIN_SIZE;
+  if (n > UINT64_MAX / blowup || n * blowup > MAX_DOMAIN) return Z0P_ERR_INVALID_DOMAIN_SIZE;
+  *o = z0p_air_params{n, blowup, q, final_size, 0, 0, a0 % P, b0 % P, b_last % P};
+  return Z0P_OK;
+}
+int z0p_air_params_for_security(uint64_t n, uint32_t a0, uint32_t b0, uint32_t b_last,
+                                uint32_t target, z0p_air_params* o) {
+  if (!o) return Z0P_ERR_INVALID_ARGUMENT;  // src/air.rs:127-158
+  if (n < 2 || !is_pow2(n)) return Z0P_ERR_INVALID_DOMAIN_SIZE;
+  if (n > UINT64_MAX / 16 || n * 16 > MAX_DOMAIN) return Z0P_ERR_INVALID_DOMAIN_SIZE;
+  uint64_t lde = n * 16, q, fs, ch;
+  uint32_t g;
+  tune_strength(target, composition_millibits(lde, n - 1), &q, &g);
+  tune_shape(lde, q, lde, 24, &fs, &ch);
+  *o = z0p_air_params{n, 16, q, fs, g, ch, a0 % P, b0 % P, b_last % P};
+  return Z0P_OK;
+}
+int z0p_range_params_new(uint64_t n_rows, uint64_t n_bits, uint64_t blowup, uint64_t q,
+                         uint64_t final_size, uint32_t value, z0p_range_params* o) {
+  if (!o) return Z0P_ERR_INVALID_ARGUMENT;  // src/range.rs:57-99
+  if (n_rows < 2 || !is_pow2(n_rows)) return Z0P_ERR_INVALID_DOMAIN_SIZE;
+  if (n_bits == 0 || n_bits > 24) { set_reason("n_bits must be within 1..=24"); return Z0P_ERR_MALFORMED_INPUT; }
+  if (blowup < 2 || !is_pow2(blowup)) return Z0P_ERR_INVALID_BLOWUP;
+  if (q == 0) return Z0P_ERR_NO_QUERIES;
+  if (final_size < 2 || !is_pow2(final_size)) return Z0P_ERR_INVALID_DOMAIN_SIZE;
+  if (n_rows > UINT64_MAX / blowup || n_rows * blowup > MAX_DOMAIN) return Z0P_ERR_INVALID_DOMAIN_SIZE;
+  *o = z0p_range_params{n_rows, n_bits, blowup, q, final_size, 0, 0, value % P};
+  return Z0P_OK;
+}
+int z0p_range_params_for_security(uint64_t n_rows, uint64_t n_bits, uint32_t value,
+                                  uint32_t target, z0p_range_params* o) {
+  if (!o) return Z0P_ERR_INVALID_ARGUMENT;  // src/range.rs:124-161
+  if (n_rows < 2 || !is_pow2(n_rows)) return Z0P_ERR_INVALID_DOMAIN_SIZE;
+  if (n_bits == 0 || n_bits > 24) { set_reason("n_bits must be within 1..=24"); return Z0P_ERR_MALFORMED_INPUT; }
+  if (n_rows > UINT64_MAX / 16 || n_rows * 16 > MAX_DOMAIN) return Z0P_ERR_INVALID_DOMAIN_SIZE;
+  uint64_t lde = n_rows * 16, q, fs, ch;
+  uint32_t g;
+  tune_strength(target, composition_millibits(lde, n_rows - 1), &q, &g);
+  tune_shape(lde, q, lde, 8 + 4 * (n_bits + 1), &fs, &ch);
+  *o = z0p_range_params{n_rows, n_bits, 16, q, fs, g, ch, value % P};
+  return Z0P_OK;
+}
+
+int z0p_air_proof_size(const z0p_air_params* p, size_t* len) {
+  if (!p || !len) return Z0P_ERR_INVALID_ARGUMENT;
+  FriParams fp;
+  FriShape s;
+  RC(air_shape(*p, &fp, &s));
+  *len = air_size(*p, s);
+  return Z0P_OK;
+}
+int z0p_range_proof_size(const z0p_range_params* p, size_t* len) {
+  if (!p || !len) return Z0P_ERR_INVALID_ARGUMENT;
+  FriParams fp;
+  FriShape s;
+  RC(range_shape(*p, &fp, &s));
+  *len = range_size(*p, s);
+  return Z0P_OK;
+}
+
+int z0p_gpu_air_footprint(const z0p_air_params* p, size_t* bytes) {
+  if (!p || !bytes) return Z0P_ERR_INVALID_ARGUMENT;
+  FriParams fp;
+  FriShape s;
+  RC(air_shape(*p, &fp, &s));
+  uint64_t N = p->n_steps, m = s.m, total = 16 * N + 16 * m + 32 * tree_digests(m / 8);
+  for (size_t i = 0; i < s.len.size(); i++) total += 16 * s.len[i] + 32 * tree_digests(s.leaves[i]);
+  *bytes = total;
+  return Z0P_OK;
+}
+int z0p_gpu_range_footprint(const z0p_range_params* p, size_t* bytes) {
+  if (!p || !bytes) return Z0P_ERR_INVALID_ARGUMENT;
+  FriParams fp;
+  FriShape s;
+  RC(range_shape(*p, &fp, &s));
+  uint64_t ncol = p->n_bits + 1, N = p->n_rows, m = s.m;
+  uint64_t total = 8 * N * ncol + 8 * m * ncol + 32 * tree_digests(m);
+  for (size_t i = 0; i < s.len.size(); i++) total += 16 * s.len[i] + 32 * tree_digests(s.leaves[i]);
+  *bytes = total;
+  return Z0P_OK;
+}
+
+int z0p_gpu_ctx_create(int device, z0p_gpu_ctx** out) {
+  if (!out) return Z0P_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  int count = 0;
+  CK(cudaGetDeviceCount(&count));
+  if (device < 0 || device >= count) {
+    set_reason("no such CUDA device");
+    return Z0P_ERR_INVALID_ARGUMENT;
+  }
+  z0p_gpu_ctx* c = new z0p_gpu_ctx();
+  c->device = device;
+  cudaError_t e = cudaSetDevice(device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    set_reason(std::string("context creation: ") + cudaGetErrorString(e));
+    delete c;
+    return Z0P_ERR_CUDA;
+  }
+  int rc = build_tables(c);
+  if (rc) {
+    z0p_gpu_ctx_destroy(c);
+    return rc;
+  }
+  *out = c;
+  return Z0P_OK;
+}
+
+void z0p_gpu_ctx_destroy(z0p_gpu_ctx* c) {
+  if (!c) return;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  for (DevBuf* b : {&c->tables, &c->cols, &c->coeffs, &c->scratch, &c->lde, &c->ttree, &c->layers,
+                    &c->ftrees, &c->misc, &c->gaddr, &c->gout})
+    if (b->p) cudaFree(b->p);
+  if (c->pinned) cudaFreeHost(c->pinned);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+void* z0p_gpu_ctx_stream(z0p_gpu_ctx* c) { return c ? (void*)c->stream : nullptr; }
+size_t z0p_gpu_ctx_device_bytes(z0p_gpu_ctx* c) { return c ? c->held : 0; }
+
+struct ProfileScope {
+  bool on;
+  explicit ProfileScope(z0p_gpu_ctx* c) : on(c->profiling) {
+    if (on) launch::set_recorder(&c->rec);
+  }
+  ~ProfileScope() {
+    if (on) launch::set_recorder(nullptr);
+  }
+};
+
+int z0p_gpu_air_prove(z0p_gpu_ctx* c, const z0p_air_params* p, z0p_transcript_state* ts,
+                      uint8_t* out, size_t cap, size_t* len) {
+  if (!c || !p || !ts) return Z0P_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lk(c->mu);
+  RC(with_device(c));
+  ProfileScope ps(c);
+  z0p_transcript_state work = *ts;
+  int rc = air_prove(c, *p, &work, out, cap, len);
+  if (rc == Z0P_OK) {
+    *ts = work;
+    c->proofs++;
+  }
+  return rc;
+}
+
+int z0p_gpu_ctx_stats(z0p_gpu_ctx* c, z0p_gpu_stats* out) {
+  if (!c || !out) return Z0P_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lk(c->mu);
+  *out = z0p_gpu_stats{launch::launch_count(), c->h2d, c->d2h, c->syncs, c->proofs};
+  return Z0P_OK;
+}
+
+int z0p_gpu_ctx_set_profiling(z0p_gpu_ctx* c, int on) {
+  if (!c) return Z0P_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lk(c->mu);
+  c->profiling = on != 0;
+  return Z0P_OK;
+}
+
+int z0p_gpu_ctx_profile(z0p_gpu_ctx* c, char* json, size_t cap, size_t* len) {
+  if (!c || !len) return Z0P_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lk(c->mu);
+  RC(with_device(c));
+  CK(sync(c));
+  std::vector<std::pair<std::string, std::pair<double, uint64_t>>> agg;
+  for (auto& m : c->rec.marks) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, m.a, m.b) != cudaSuccess) ms = 0.f;
+    size_t i = 0;
+    while (i < agg.size() && agg[i].first != m.stage) i++;
+    if (i == agg.size()) agg.push_back({m.stage, {0.0, 0}});
+    agg[i].second.first += ms;
+    agg[i].second.second += 1;
+  }
+  std::string s = "{";
+  for (size_t i = 0; i < agg.size(); i++) {
+    char buf[160];
+    snprintf(buf, sizeof buf, "%s\"%s\": {\"ms\": %.6f, \"calls\": %llu}", i ? ", " : "",
+             agg[i].first.c_str(), agg[i].second.first, (unsigned long long)agg[i].second.second);
+    s += buf;
+  }
+  s += "}";
+  *len = s.size() + 1;
+  if (!json || cap < s.size() + 1) return Z0P_ERR_BUFFER_TOO_SMALL;
+  std::memcpy(json, s.c_str(), s.size() + 1);
+  for (auto& m : c->rec.marks) {
+    c->rec.pool.push_back(m.a);
+    c->rec.pool.push_back(m.b);
+  }
+  c->rec.marks.clear();
+  return Z0P_OK;
+}
+
+int z0p_gpu_range_prove(z0p_gpu_ctx* c, const z0p_range_params* p, z0p_transcript_state* ts,
+                        uint8_t* out, size_t cap, size_t* len) {
+  if (!c || !p || !ts) return Z0P_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lk(c->mu);
+  RC(with_device(c));
+  ProfileScope ps(c);
+  z0p_transcript_state work = *ts;
+  int rc = range_prove(c, *p, &work, out, cap, len);
+  if (rc == Z0P_OK) {
+    *ts = work;
+    c->proofs++;
+  }
+  return rc;
+}
+
+int z0p_gpu_rs_extend(z0p_gpu_ctx* c, const uint32_t* d_values, uint64_t n, uint64_t batch,
+                      uint64_t blowup, uint32_t* d_out) {
+  if (!c || !d_values || !d_out || batch == 0 || batch > 65535) return Z0P_ERR_INVALID_ARGUMENT;
+  if (!is_pow2(n) || n > MAX_DOMAIN) return Z0P_ERR_INVALID_DOMAIN_SIZE;  // src/ntt.rs:441-446
+  if (!is_pow2(blowup)) return Z0P_ERR_INVALID_BLOWUP;
+  if (n * blowup > MAX_DOMAIN || batch * blowup > 65535) return Z0P_ERR_INVALID_DOMAIN_SIZE;
+  std::lock_guard<std::mutex> lk(c->mu);
+  RC(with_device(c));
+  uint32_t logn = log2u(n), logm = logn + log2u(blowup);
+  RC(ensure(c, c->coeffs, 4 * n * batch));
+  RC(ensure(c, c->scratch, 4 * n * batch * blowup));
+  NttPlan ip;
+  ip.logn = logn; ip.batch = (uint32_t)batch; ip.inverse = 1; ip.post_gamma = 1;
+  CK(launch::ntt(c->stream, c->tb, ip, d_values, (uint32_t*)c->coeffs.p, (uint32_t*)c->scratch.p));
+  // The LDE kernels write coset-major [c][j][q]; this entry returns the
+  // natural order [c][k], k = B q + j.
+  RC(ensure(c, c->lde, 4 * n * batch * blowup));
+  NttPlan lp;
+  lp.logn = logn; lp.batch = (uint32_t)(batch * blowup); lp.in_div = (uint32_t)blowup;
+  lp.twist_mod = (uint32_t)blowup; lp.twist_shift = 27 - logm;
+  CK(launch::ntt(c->stream, c->tb, lp, (uint32_t*)c->coeffs.p, (uint32_t*)c->lde.p,
+                 (uint32_t*)c->scratch.p));
+  CK(launch::coset_to_natural(c->stream, (const uint32_t*)c->lde.p, d_out, logn, log2u(blowup),
+                              batch));
+  CK(sync(c));
+  return Z0P_OK;
+}
+
+int z0p_gpu_merkle_flat64_cap(z0p_gpu_ctx* c, const uint8_t* d_flat, uint64_t len,
+                              uint64_t cap_height, uint8_t* h_cap, uint64_t* cap_count) {
+  if (!c || !d_flat || !h_cap || !cap_count) return Z0P_ERR_INVALID_ARGUMENT;
+  if (len == 0) return Z0P_ERR_EMPTY_INPUT;  // src/merkle.rs:93-110
+  if (len % 64) return Z0P_ERR_MALFORMED_INPUT;
+  uint64_t leaves = len / 64;
+  if (!is_pow2(leaves)) {
+    set_reason("leaf count must be a power of two on the device path");
+    return Z0P_ERR_UNSUPPORTED;
+  }
+  std::lock_guard<std::mutex> lk(c->mu);
+  RC(with_device(c));
+  RC(ensure(c, c->ttree, 32 * tree_digests(leaves)));
+  uint32_t* tree = (uint32_t*)c->ttree.p;
+  CK(launch::merkle_flat64_leaves(c->stream, (const uint32_t*)d_flat, leaves, tree));
+  if (leaves > 1) CK(launch::merkle_build(c->stream, tree, leaves));
+  uint32_t depth = log2u(leaves), drop = cap_height < depth ? (uint32_t)cap_height : depth;
+  std::vector<uint8_t> cap;
+  RC(fetch_cap(c, tree, leaves, drop, &cap));
+  std::memcpy(h_cap, cap.data(), cap.size());
+  *cap_count = cap.size() / 32;
+  return Z0P_OK;
+}
+
+int z0p_gpu_fri_fold(z0p_gpu_ctx* c, const uint32_t* d_in, uint64_t n, uint64_t lde_len,
+                     uint64_t depth, const uint32_t ch[12], uint32_t* d_out) {
+  if (!c || !d_in || !d_out || !ch) return Z0P_ERR_INVALID_ARGUMENT;
+  if (!is_pow2(n) || n < 4 || !is_pow2(lde_len) || lde_len > MAX_DOMAIN || depth > 13 ||
+      (lde_len >> (2 * depth)) != n)
+    return Z0P_ERR_INVALID_DOMAIN_SIZE;
+  std::lock_guard<std::mutex> lk(c->mu);
+  RC(with_device(c));
+  RC(ensure(c, c->ftrees, 32 * (n / 4 + 4)));
+  FoldArgs fa;
+  fa.in = d_in;
+  fa.out = d_out;
+  fa.leaves = (uint32_t*)c->ftrees.p;
+  fa.logn = log2u(n);
+  uint32_t g = GENERATOR;
+  for (uint64_t i = 0; i < depth; i++) g = fpow(g, 4);
+  fa.ginv_m = to_mont(finv(g));
+  fa.unit_m = to_mont(two_adic_generator(2));
+  for (int k = 0; k < 3; k++)
+    for (int e = 0; e < 4; e++) fa.ch[k][e] = to_mont(ch[4 * k + e] % P);
+  CK(launch::fri_fold(c->stream, c->tb, fa));
+  CK(sync(c));
+  return Z0P_OK;
+}
+
+int z0p_gpu_grind(z0p_gpu_ctx* c, const uint8_t* head, size_t head_len, uint32_t bits,
+                  uint64_t* nonce) {
+  if (!c || !head || !nonce) return Z0P_ERR_INVALID_ARGUMENT;
+  if (bits > 32) {
+    set_reason("grinding difficulty above 32 bits");
+    return Z0P_ERR_MALFORMED_INPUT;
+  }
+  if (!launch::grind_supports((uint32_t)head_len)) {
+    set_reason("grind head length not supported by the device kernel");
+    return Z0P_ERR_UNSUPPORTED;
+  }
+  std::lock_guard<std::mutex> lk(c->mu);
+  RC(with_device(c));
+  RC(ensure(c, c->misc, 64));
+  unsigned long long init[3] = {~0ull, 0ull, 0ull};
+  CK(h2d(c, c->misc.p, init, sizeof init));
+  CK(launch::grind(c->stream, head, (uint32_t)head_len, bits, (unsigned long long*)c->misc.p,
+                   1ull << 40));
+  unsigned long long res[3];
+  CK(d2h(c, res, c->misc.p, 24));
+  CK(sync(c));
+  if ((res[2] & 0xffffffffull) != 0 || res[0] == ~0ull) {
+    set_reason("proof-of-work search reached its nonce cap without a solution");
+    return Z0P_ERR_DEVICE_TIMEOUT;
+  }
+  *nonce = res[0];
+  return Z0P_OK;
+}
+
+}  // extern "C"

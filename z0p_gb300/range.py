@@ -1,0 +1,63 @@
+"""Range-check AIR on the GB300 backend — mirrors z0p::range (src/range.rs)."""
+from __future__ import annotations
+
+import ctypes as C
+
+from ._lib import RangeParams, check, lib
+from .context import default_context
+from .transcript import Transcript
+
+P = 2013265921
+
+
+class Params(RangeParams):
+    """range::Params (src/range.rs:30-51)."""
+
+    @classmethod
+    def new(cls, n_rows, n_bits, blowup, num_queries, final_size, value) -> "Params":
+        p = cls()
+        check(lib().z0p_range_params_new(n_rows, n_bits, blowup, num_queries, final_size,
+                                         value % P, C.byref(p)))
+        return p
+
+    @classmethod
+    def for_security(cls, n_rows, n_bits, value, target_bits) -> "Params":
+        p = cls()
+        check(lib().z0p_range_params_for_security(n_rows, n_bits, value % P, target_bits,
+                                                  C.byref(p)))
+        return p
+
+    def with_grinding_bits(self, bits: int) -> "Params":
+        self.grinding_bits = bits
+        return self
+
+    def with_cap_height(self, height: int) -> "Params":
+        self.cap_height = height
+        return self
+
+    def lde_len(self) -> int:
+        return self.n_rows * self.blowup
+
+    def n_columns(self) -> int:
+        return self.n_bits + 1
+
+    def proof_size(self) -> int:
+        n = C.c_size_t()
+        check(lib().z0p_range_proof_size(C.byref(self), C.byref(n)))
+        return n.value
+
+    def footprint(self) -> int:
+        n = C.c_size_t()
+        check(lib().z0p_gpu_range_footprint(C.byref(self), C.byref(n)))
+        return n.value
+
+
+def prove(params: Params, transcript: Transcript, ctx=None) -> bytes:
+    """range::prove + Proof::to_bytes (src/range.rs:337-343, 253-269) on the GPU."""
+    ctx = ctx or default_context()
+    size = params.proof_size()
+    buf = (C.c_uint8 * size)()
+    n = C.c_size_t()
+    check(lib().z0p_gpu_range_prove(ctx.handle, C.byref(params), C.byref(transcript.state), buf,
+                                    size, C.byref(n)))
+    return bytes(buf)[: n.value]
