@@ -268,12 +268,14 @@ def run_gpu(args):
         dev_ms, wall_s = float(t[0]), float(t[1])
 
     # --- per-stage timing (CUDA events on the context stream) ---------------
-    ctx.set_profiling(True)
-    prof_steps = 2
-    for _ in range(prof_steps):
-        prove_once()
-    prof = ctx.profile()
-    ctx.set_profiling(False)
+    prof_steps = 0 if args.quick else 2
+    prof = {}
+    if prof_steps:
+        ctx.set_profiling(True)
+        for _ in range(prof_steps):
+            prove_once()
+        prof = ctx.profile()
+        ctx.set_profiling(False)
 
     if rank != 0:
         if dist is not None:
@@ -281,8 +283,12 @@ def run_gpu(args):
         return 0
 
     # --- parity of the measured proof (outside every timed region) ----------
-    cpu_proof, cpu = cpu_baseline_sample()
-    parity = proof0 == cpu_proof
+    if args.quick:
+        cpu_proof, cpu = None, None
+        parity = None
+    else:
+        cpu_proof, cpu = cpu_baseline_sample()
+        parity = proof0 == cpu_proof
 
     peak, peak_kind = measured_peaks()
     work = stage_work(N_STEPS, params)
@@ -344,6 +350,8 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--quick", action="store_true",
+                    help="skip the CPU baseline, parity check and per-stage pass (for profilers)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
