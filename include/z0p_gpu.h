@@ -193,6 +193,31 @@ int z0p_gpu_range_prove(z0p_gpu_ctx *ctx, const z0p_range_params *params,
 int z0p_gpu_rs_extend(z0p_gpu_ctx *ctx, const uint32_t *d_values, uint64_t n, uint64_t batch,
                       uint64_t blowup, uint32_t *d_out);
 /*
+ * Allocation-free variant of z0p_gpu_rs_extend. It has no counterpart in the
+ * reference. It serves callers that may not allocate device memory: a process
+ * whose device heap is owned by another allocator that must see every byte, a
+ * latency-critical loop where cudaMalloc/cudaFree would synchronise the
+ * device, or a deployment whose memory budget is fixed when the library loads.
+ * It needs no context. It allocates nothing, and it calls no allocating
+ * library routine.
+ *
+ * Its working memory is static device arrays inside this library: 12 MiB of
+ * scratch plus 240 KiB of power tables, held on every device that loads the
+ * library until the process exits.
+ * - Limit: n * batch * blowup <= 1048576 output elements, and
+ *   batch * blowup <= 65535. Larger sizes return Z0P_ERR_UNSUPPORTED.
+ * - Set-up: the first call on a device, with that device current, resolves
+ *   the arrays' device addresses and uploads the tables through the legacy
+ *   default stream. Make that first call before any stream capture.
+ * - Semantics: the same output as z0p_gpu_rs_extend. The work is enqueued on
+ *   `stream` (NULL = legacy default stream) and the call returns without
+ *   waiting.
+ * - Concurrency: every call shares the one scratch area, so calls whose work
+ *   overlaps on the GPU race. Serialise them on one stream.
+ */
+int z0p_gpu_rs_extend_noalloc(const uint32_t *d_values, uint64_t n, uint64_t batch,
+                              uint64_t blowup, uint32_t *d_out, void *stream);
+/*
  * MerkleTree::from_flat64 (src/merkle.rs:93-110) + cap (src/merkle.rs:229-232):
  * builds the BLAKE3 tree over len/64 64-byte leaves of the device buffer
  * d_flat and copies cap level min(cap_height, depth) to the host buffer

@@ -932,3 +932,142 @@ cudaError_t gather4(cudaStream_t st, const uint64_t* addr, uint32_t* out, uint32
 
 }  // namespace launch
 }  // namespace z0p
+
+// ====================================================== allocation-free LDE ====
+// z0p_gpu_rs_extend_noalloc: the Reed-Solomon extension of z0p_gpu_rs_extend
+// for callers that may not allocate device memory. Such callers include a
+// process whose device heap is owned by another allocator (a framework's
+// caching pool that must see every byte), a latency-critical loop in which
+// cudaMalloc/cudaFree would synchronise the device, and a deployment with a
+// fixed memory budget that must be fully accounted when the library loads.
+// Its working memory is the static arrays below. They are sized for at most
+// kNoAllocMaxElems output elements and stay resident on every device that
+// loads this library until the process exits.
+#include <mutex>
+#include <vector>
+
+#include "../../include/z0p_gpu.h"
+#include "host.h"
+
+namespace {
+
+// Largest n * batch * blowup the allocation-free entry accepts (4 MiB per region).
+constexpr uint64_t kNoAllocMaxElems = 1ull << 20;
+constexpr size_t kNoAllocTableWords = (1u << 14) + (1u << 13) + (1u << 12) + (1u << 15);
+
+// Three regions of kNoAllocMaxElems words: coefficients, four-step
+// intermediate, coset-major LDE (12 MiB in total).
+static __device__ __align__(256) uint32_t g_noalloc_scratch[3 * kNoAllocMaxElems];
+// omega_{2^27} and 31 power tables (same contents as a context's tables).
+static __device__ __align__(256) uint32_t g_noalloc_tables[kNoAllocTableWords];
+
+struct NoAllocDevice {
+  bool ready = false;
+  uint32_t* scratch = nullptr;
+  uint32_t* tables = nullptr;
+};
+std::mutex g_noalloc_mu;
+NoAllocDevice g_noalloc_dev[64];
+
+// Once per device, with that device current: resolve the device addresses of
+// the static arrays (host code cannot use their names as pointers) and fill
+// the power tables. The copy goes through the legacy default stream.
+int noalloc_setup(int dev, NoAllocDevice** out) {
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  NoAllocDevice& d = g_noalloc_dev[dev];
+  if (!d.ready) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) {
+      z0p::host::set_reason(std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e));
+      return Z0P_ERR_CUDA;
+    }
+    d.scratch = static_cast<uint32_t*>(p);
+    e = cudaGetSymbolAddress(&p, g_noalloc_tables);
+    if (e != cudaSuccess) {
+      z0p::host::set_reason(std::string("cudaGetSymbolAddress(tables): ") + cudaGetErrorString(e));
+      return Z0P_ERR_CUDA;
+    }
+    d.tables = static_cast<uint32_t*>(p);
+    using namespace z0p::host;
+    std::vector<uint32_t> t(kNoAllocTableWords);
+    uint32_t* w_lo = t.data();
+    uint32_t* w_hi = w_lo + (1u << 14);
+    uint32_t* g_lo = w_hi + (1u << 13);
+    uint32_t* g_hi = g_lo + (1u << 12);
+    const uint32_t omega = two_adic_generator(27);
+    uint32_t x = 1;
+    for (uint32_t i = 0; i < (1u << 14); i++) { w_lo[i] = to_mont(x); x = fmul(x, omega); }
+    const uint32_t wstep = fpow(omega, 1u << 14);
+    x = 1;
+    for (uint32_t i = 0; i < (1u << 13); i++) { w_hi[i] = to_mont(x); x = fmul(x, wstep); }
+    x = 1;
+    for (uint32_t i = 0; i < (1u << 12); i++) { g_lo[i] = to_mont(x); x = fmul(x, GENERATOR); }
+    const uint32_t gstep = fpow(GENERATOR, 1u << 12);
+    x = 1;
+    for (uint32_t i = 0; i < (1u << 15); i++) { g_hi[i] = to_mont(x); x = fmul(x, gstep); }
+    e = cudaMemcpyToSymbol(g_noalloc_tables, t.data(), t.size() * sizeof(uint32_t));
+    if (e != cudaSuccess) {
+      z0p::host::set_reason(std::string("cudaMemcpyToSymbol(tables): ") + cudaGetErrorString(e));
+      return Z0P_ERR_CUDA;
+    }
+    d.ready = true;
+  }
+  *out = &d;
+  return Z0P_OK;
+}
+
+}  // namespace
+
+extern "C" int z0p_gpu_rs_extend_noalloc(const uint32_t* d_values, uint64_t n, uint64_t batch,
+                                         uint64_t blowup, uint32_t* d_out, void* stream) {
+  using namespace z0p;
+  if (!d_values || !d_out || batch == 0) return Z0P_ERR_INVALID_ARGUMENT;
+  if (!host::is_pow2(n) || n > host::MAX_DOMAIN) return Z0P_ERR_INVALID_DOMAIN_SIZE;
+  if (!host::is_pow2(blowup)) return Z0P_ERR_INVALID_BLOWUP;
+  if (n * blowup > host::MAX_DOMAIN) return Z0P_ERR_INVALID_DOMAIN_SIZE;
+  if (batch > kNoAllocMaxElems || n * blowup > kNoAllocMaxElems ||
+      n * batch * blowup > kNoAllocMaxElems || batch * blowup > 65535) {
+    host::set_reason("z0p_gpu_rs_extend_noalloc: n * batch * blowup exceeds the static scratch "
+                     "limit of 1048576 elements");
+    return Z0P_ERR_UNSUPPORTED;
+  }
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess || dev < 0 || dev >= 64) {
+    host::set_reason("z0p_gpu_rs_extend_noalloc: no usable current CUDA device");
+    return Z0P_ERR_CUDA;
+  }
+  NoAllocDevice* d = nullptr;
+  int rc = noalloc_setup(dev, &d);
+  if (rc != Z0P_OK) return rc;
+  Tables tb;
+  tb.w_lo = d->tables;
+  tb.w_hi = d->tables + (1u << 14);
+  tb.g_lo = d->tables + (1u << 14) + (1u << 13);
+  tb.g_hi = d->tables + (1u << 14) + (1u << 13) + (1u << 12);
+  uint32_t* coeffs = d->scratch;
+  uint32_t* four_step = d->scratch + kNoAllocMaxElems;
+  uint32_t* coset_major = d->scratch + 2 * kNoAllocMaxElems;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const uint32_t logn = host::log2u(n), logb = host::log2u(blowup);
+  NttPlan ip;
+  ip.logn = logn;
+  ip.batch = (uint32_t)batch;
+  ip.inverse = 1;
+  ip.post_gamma = 1;
+  e = launch::ntt(st, tb, ip, d_values, coeffs, four_step);
+  NttPlan lp;
+  lp.logn = logn;
+  lp.batch = (uint32_t)(batch * blowup);
+  lp.in_div = (uint32_t)blowup;
+  lp.twist_mod = (uint32_t)blowup;
+  lp.twist_shift = 27 - (logn + logb);
+  if (e == cudaSuccess) e = launch::ntt(st, tb, lp, coeffs, coset_major, four_step);
+  if (e == cudaSuccess) e = launch::coset_to_natural(st, coset_major, d_out, logn, logb, batch);
+  if (e != cudaSuccess) {
+    host::set_reason(std::string("z0p_gpu_rs_extend_noalloc: ") + cudaGetErrorString(e));
+    return Z0P_ERR_CUDA;
+  }
+  return Z0P_OK;
+}
