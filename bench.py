@@ -151,6 +151,125 @@ def stage_work(n, params):
     return work
 
 
+# ------------------------------------------------- batched / served configs --
+def _mix_params(Z, seed, n_air, n_range, air_logs, range_logs):
+    """Seeded job mix: Fibonacci AIRs (log2 steps uniform in air_logs) and
+    16-bit range checks (log2 rows uniform in range_logs), for_security(100)."""
+    state = seed
+    specs = []
+    for i in range(n_air + n_range):
+        z, state = splitmix64(state)
+        if i < n_air:
+            logn = air_logs[z % len(air_logs)]
+            z1, state = splitmix64(state)
+            z2, state = splitmix64(state)
+            a0, b0 = z1 % P, z2 % P
+            _, b_last = Z.air.trace_last(a0, b0, 1 << logn)
+            specs.append((Z.air.Params.for_security(1 << logn, a0, b0, b_last, 100), 1 << logn,
+                          b"bench/air-scale"))
+        else:
+            logn = range_logs[z % len(range_logs)]
+            z1, state = splitmix64(state)
+            specs.append((Z.range.Params.for_security(1 << logn, 16, z1 % (1 << 16), 100),
+                          1 << logn, b"bench/range"))
+    return specs
+
+
+def _prove_plain(Z, ctx, specs):
+    out, lat = [], []
+    for params, _, label in specs:
+        t0 = time.perf_counter()
+        mod = Z.air if isinstance(params, Z.air.Params) else Z.range
+        out.append(mod.prove(params, Z.Transcript(label), ctx))
+        lat.append(time.perf_counter() - t0)
+    return out, lat
+
+
+def _pct(xs, q):
+    xs = sorted(xs)
+    return xs[min(len(xs) - 1, int(q * len(xs)))]
+
+
+def run_batched(Z, ctx, workers=16):
+    """256 proofs: 192 Fibonacci (2^10..2^18 steps) + 64 range (2^12..2^16 rows)."""
+    from z0p_gb300.pool import Pool
+
+    specs = _mix_params(Z, 0x5EED000000000003, 192, 64, list(range(10, 19)), list(range(12, 17)))
+    steps = sum(n for _, n, _ in specs)
+    _prove_plain(Z, ctx, specs[:8])  # warm the plain context
+    t0 = time.perf_counter()
+    plain, plain_lat = _prove_plain(Z, ctx, specs)
+    t_plain = time.perf_counter() - t0
+    pool = Pool(ctx.device, workers=workers)
+    warm = [pool.make_job(p, Z.Transcript(l)) for p, _, l in specs[:2 * workers]]
+    pool.prove_all(warm)
+    jobs = [pool.make_job(p, Z.Transcript(l)) for p, _, l in specs]
+    t0 = time.perf_counter()
+    batched = pool.prove_all(jobs)
+    t_batch = time.perf_counter() - t0
+    lat = [j.end_s - j.submit_s for j in jobs]
+    pool.close()
+    return {
+        "workload": "192 fibonacci (2^10..2^18 steps) + 64 range-16 (2^12..2^16 rows), for_security(100)",
+        "proofs": len(specs), "steps": steps, "workers": workers,
+        "plain_serial_s": t_plain, "batched_s": t_batch,
+        "plain_steps_per_s": steps / t_plain, "batched_steps_per_s": steps / t_batch,
+        "speedup_vs_plain": t_plain / t_batch,
+        "byte_identical_to_plain": all(a == b for a, b in zip(plain, batched)),
+        "plain_latency_ms": {"p50": 1e3 * _pct(plain_lat, 0.5), "p99": 1e3 * _pct(plain_lat, 0.99)},
+        "batched_latency_ms": {"p50": 1e3 * _pct(lat, 0.5), "p99": 1e3 * _pct(lat, 0.99)},
+    }
+
+
+def run_served(Z, ctx, rates=(100, 200, 400), requests=120, workers=16, budget=180 << 30):
+    """Poisson arrivals of mixed Fibonacci (2^10..2^22) / range (2^12..2^18) requests."""
+    import random
+    import threading
+
+    from z0p_gb300.pool import Pool
+
+    free, _ = __import__("torch").cuda.mem_get_info(ctx.device)
+    budget = min(budget, int(free * 0.9))
+    pool = Pool(ctx.device, workers=workers, hbm_budget=budget)
+    out = []
+    for ri, rate in enumerate(rates):
+        specs = _mix_params(Z, 0x5EED000000000004 + 977 * ri, (3 * requests) // 4,
+                            requests - (3 * requests) // 4, list(range(10, 23)), list(range(12, 19)))
+        rng = random.Random(0x5EED0005 + ri)
+        steps = sum(n for _, n, _ in specs)
+        jobs = [pool.make_job(p, Z.Transcript(l)) for p, _, l in specs]
+        tickets = [None] * len(jobs)
+
+        def arrive():
+            for i, j in enumerate(jobs):
+                tickets[i] = pool.submit(j)
+                time.sleep(rng.expovariate(rate))
+
+        t0 = pool.clock()
+        th = threading.Thread(target=arrive)
+        th.start()
+        th.join()
+        for t in tickets:
+            pool.wait(t)
+        t1 = max(j.end_s for j in jobs)
+        lat = [j.end_s - j.submit_s for j in jobs]
+        out.append({"rate_per_s": rate, "requests": len(jobs), "steps": steps,
+                    "steps_per_s": steps / (t1 - t0),
+                    "latency_ms": {"p50": 1e3 * _pct(lat, 0.5), "p99": 1e3 * _pct(lat, 0.99)}})
+    pool.close()
+    # the same request set proved one at a time on the plain path
+    specs = _mix_params(Z, 0x5EED000000000004, (3 * requests) // 4, requests - (3 * requests) // 4,
+                        list(range(10, 23)), list(range(12, 19)))
+    t0 = time.perf_counter()
+    _, lat = _prove_plain(Z, ctx, specs)
+    t_plain = time.perf_counter() - t0
+    steps = sum(n for _, n, _ in specs)
+    return {"workload": "poisson arrivals; 75% fibonacci 2^10..2^22, 25% range-16 2^12..2^18",
+            "workers": workers, "hbm_budget_gb": budget / 2**30, "by_rate": out,
+            "plain_one_at_a_time": {"steps_per_s": steps / t_plain,
+                                    "latency_ms": {"p50": 1e3 * _pct(lat, 0.5), "p99": 1e3 * _pct(lat, 0.99)}}}
+
+
 # -------------------------------------------------------------------- arms --
 def run_reference(args):
     ws, rank, _ = dist_env()
@@ -277,6 +396,11 @@ def run_gpu(args):
         prof = ctx.profile()
         ctx.set_profiling(False)
 
+    batched = served = None
+    if not args.quick and ws == 1:
+        batched = run_batched(Z, ctx)
+        served = run_served(Z, ctx)
+
     if rank != 0:
         if dist is not None:
             dist.destroy_process_group()
@@ -333,10 +457,15 @@ def run_gpu(args):
         "latency_ms": {"p50": 1000 * statistics.median(lat),
                        "p99": 1000 * sorted(lat)[min(len(lat) - 1, int(0.99 * len(lat)))]},
         "host_syncs_per_step": (st1["syncs"] - st0["syncs"]) / args.steps,
+        "host_ms_per_step": {
+            "prove_wall": (st1["prove_ns"] - st0["prove_ns"]) / 1e6 / args.steps,
+            "blocked_in_sync": (st1["sync_wait_ns"] - st0["sync_wait_ns"]) / 1e6 / args.steps},
         "clocks": clocks,
         "roofline": roof,
         "stages": stages,
         "cpu_baseline": cpu,
+        "batched": batched,
+        "served": served,
     }
     print(json.dumps(line), flush=True)
     if dist is not None:

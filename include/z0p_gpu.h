@@ -155,6 +155,8 @@ typedef struct {
     uint64_t d2h_bytes;  /* device-to-host bytes copied by this context */
     uint64_t syncs;      /* stream synchronisations (host round trips) */
     uint64_t proofs;     /* proofs completed */
+    uint64_t sync_wait_ns; /* host time blocked in those synchronisations */
+    uint64_t prove_ns;     /* host wall time inside prove calls */
 } z0p_gpu_stats;
 int z0p_gpu_ctx_stats(z0p_gpu_ctx *ctx, z0p_gpu_stats *out);
 /* Diagnostic per-stage timing: while on, every kernel stage is bracketed by
@@ -182,6 +184,43 @@ int z0p_gpu_air_prove(z0p_gpu_ctx *ctx, const z0p_air_params *params,
 int z0p_gpu_range_prove(z0p_gpu_ctx *ctx, const z0p_range_params *params,
                         z0p_transcript_state *transcript, uint8_t *out, size_t cap,
                         size_t *len);
+
+/* ------------------------------------------------- batching / serving ---- */
+/*
+ * Many independent proofs (the batched and served configurations). A pool
+ * owns `workers` contexts, each with its own stream and host thread, and a
+ * FIFO job queue. A job starts once its device footprint
+ * (z0p_gpu_*_footprint) fits the pool's HBM budget next to the jobs already
+ * running. Jobs whose footprint exceeds the whole budget are rejected with
+ * Z0P_ERR_ADMISSION. Proofs are deterministic: a job's bytes and transcript
+ * post-state are the same alone and in any mix. The reference has no
+ * counterpart: it proves one statement per call (air::prove / range::prove).
+ */
+enum { Z0P_JOB_AIR = 0, Z0P_JOB_RANGE = 1 };
+typedef struct {
+    int kind;                          /* Z0P_JOB_AIR or Z0P_JOB_RANGE */
+    z0p_air_params air;                /* used when kind == Z0P_JOB_AIR */
+    z0p_range_params range;            /* used when kind == Z0P_JOB_RANGE */
+    z0p_transcript_state *transcript;  /* in/out, owned by the caller */
+    uint8_t *out;                      /* proof bytes (caller-owned) */
+    size_t cap;
+    size_t len;                        /* written: proof length */
+    int status;                        /* written: the prove call's status */
+    double submit_s, start_s, end_s;   /* written: pool clock, seconds */
+} z0p_job;
+typedef struct z0p_gpu_pool z0p_gpu_pool;
+/* hbm_budget = 0 means 90% of the device's free memory at creation. */
+int z0p_gpu_pool_create(int device, int workers, size_t hbm_budget, z0p_gpu_pool **out);
+void z0p_gpu_pool_destroy(z0p_gpu_pool *pool);
+/* Queues a job (it must stay valid until it completes); *ticket identifies it. */
+int z0p_gpu_pool_submit(z0p_gpu_pool *pool, z0p_job *job, uint64_t *ticket);
+/* Waits up to timeout_ms (< 0: forever) for a ticket; Z0P_ERR_DEVICE_TIMEOUT
+ * if it is still pending. Returns the job's status once done. */
+int z0p_gpu_pool_wait(z0p_gpu_pool *pool, uint64_t ticket, int timeout_ms);
+/* Proves all jobs (largest footprint first) and waits; 0 if every job returned 0. */
+int z0p_gpu_pool_prove_all(z0p_gpu_pool *pool, z0p_job *jobs, size_t n);
+/* Seconds on the pool's clock (the clock of the job timestamps). */
+double z0p_gpu_pool_clock(z0p_gpu_pool *pool);
 
 /* ------------------------------------------ per-stage kernels (device) ---- */
 /*

@@ -45,7 +45,8 @@ class RangeParams(C.Structure):
 
 class Stats(C.Structure):
     _fields_ = [("launches", C.c_uint64), ("h2d_bytes", C.c_uint64), ("d2h_bytes", C.c_uint64),
-                ("syncs", C.c_uint64), ("proofs", C.c_uint64)]
+                ("syncs", C.c_uint64), ("proofs", C.c_uint64), ("sync_wait_ns", C.c_uint64),
+                ("prove_ns", C.c_uint64)]
 
 
 class TranscriptState(C.Structure):
@@ -53,6 +54,15 @@ class TranscriptState(C.Structure):
         ("tail", C.c_uint8 * 2048), ("tail_len", C.c_uint32),
         ("stack", (C.c_uint8 * 32) * 54), ("stack_len", C.c_uint32),
         ("next_index", C.c_uint64), ("total_len", C.c_uint64), ("counter", C.c_uint64),
+    ]
+
+
+class Job(C.Structure):
+    _fields_ = [
+        ("kind", C.c_int), ("air", AirParams), ("range", RangeParams),
+        ("transcript", C.POINTER(TranscriptState)), ("out", C.POINTER(C.c_uint8)),
+        ("cap", C.c_size_t), ("len", C.c_size_t), ("status", C.c_int),
+        ("submit_s", C.c_double), ("start_s", C.c_double), ("end_s", C.c_double),
     ]
 
 
@@ -95,6 +105,13 @@ def lib():
             "z0p_gpu_air_prove": (C.c_int, [vp, P(AirParams), P(TranscriptState), u8p, sz, P(sz)]),
             "z0p_gpu_range_prove": (C.c_int, [vp, P(RangeParams), P(TranscriptState), u8p, sz, P(sz)]),
             "z0p_gpu_rs_extend": (C.c_int, [vp, vp, C.c_uint64, C.c_uint64, C.c_uint64, vp]),
+            "z0p_gpu_rs_extend_noalloc": (C.c_int, [vp, C.c_uint64, C.c_uint64, C.c_uint64, vp, vp]),
+            "z0p_gpu_pool_create": (C.c_int, [C.c_int, C.c_int, sz, P(vp)]),
+            "z0p_gpu_pool_destroy": (None, [vp]),
+            "z0p_gpu_pool_submit": (C.c_int, [vp, P(Job), u64p]),
+            "z0p_gpu_pool_wait": (C.c_int, [vp, C.c_uint64, C.c_int]),
+            "z0p_gpu_pool_prove_all": (C.c_int, [vp, P(Job), sz]),
+            "z0p_gpu_pool_clock": (C.c_double, [vp]),
             "z0p_gpu_merkle_flat64_cap": (C.c_int, [vp, vp, C.c_uint64, C.c_uint64, u8p, u64p]),
             "z0p_gpu_fri_fold": (C.c_int, [vp, vp, C.c_uint64, C.c_uint64, C.c_uint64, u32p, vp]),
             "z0p_gpu_grind": (C.c_int, [vp, C.c_char_p, sz, C.c_uint32, u64p]),

@@ -54,7 +54,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     jobs.append([nvcc, *ARCH, "-lineinfo", *common, "-Xcompiler", "-fPIC", "-c",
                  os.path.join(CSRC, "kernels.cu"), "-o", obj_k])
     objs = [obj_k]
-    for name in ("host.cpp", "prover.cpp"):
+    for name in ("host.cpp", "prover.cpp", "pool.cpp"):
         obj = os.path.join(BUILD_DIR, name.replace(".cpp", ".o"))
         jobs.append(["g++", *common, "-fPIC", "-Wall", "-Wextra", "-Wno-unused-parameter",
                      "-I" + os.path.join(cuda, "include"), "-c", os.path.join(CSRC, name), "-o", obj])

@@ -47,6 +47,17 @@ __device__ __forceinline__ uint32_t mmul(uint32_t a, uint32_t b) {
   uint32_t r = hi - mp;
   return hi < mp ? r + kP : r;
 }
+// (a0 b0 + a1 b1) * 2^-32 mod p for canonical a_i and b_i < p: the sum of
+// the two products is below 2p^2 < p * 2^32, so one signed Montgomery
+// reduction covers both (lazy reduction of a two-term dot product).
+__device__ __forceinline__ uint32_t mdot2(uint32_t a0, uint32_t b0, uint32_t a1, uint32_t b1) {
+  uint64_t t = (uint64_t)a0 * b0 + (uint64_t)a1 * b1;
+  uint32_t lo = (uint32_t)t, hi = (uint32_t)(t >> 32);
+  uint32_t m = lo * kPInv;
+  uint32_t mp = __umulhi(m, kP);
+  uint32_t r = hi - mp;
+  return hi < mp ? r + kP : r;
+}
 // Canonical x canonical -> canonical.
 __device__ __forceinline__ uint32_t fmul(uint32_t a, uint32_t b) { return mmul(mmul(a, b), kR2); }
 __device__ __forceinline__ uint32_t to_mont(uint32_t a) { return mmul(a, kR2); }
@@ -159,6 +170,20 @@ __device__ __forceinline__ E4 e4_mul_cm(const E4& v, const E4& rM) {
   r.c[1] = fadd(ac1, bd0);
   r.c[2] = fsub(fsub(t0, ac0), bd0);
   r.c[3] = fsub(fsub(t1, ac1), bd1);
+  return r;
+}
+
+// Canonical Fp4 times a constant r, given r's product table T (Montgomery
+// form): coordinate c of v*r is sum_i v_i T[c][i] with
+//   T[0] = (r0, 11 r1, 11 r3, 11 r2)   T[1] = (r1, r0, r2, 11 r3)
+//   T[2] = (r2, 11 r3, r0, 11 r1)      T[3] = (r3, r2, r1, r0)
+// (the tower product of src/ext4.rs:106-117 written out), i.e. two lazy
+// two-term reductions per coordinate.
+__device__ __forceinline__ E4 e4_mul_tab(const E4& v, const uint32_t (&T)[4][4]) {
+  E4 r;
+#pragma unroll
+  for (int c = 0; c < 4; c++)
+    r.c[c] = fadd(mdot2(v.c[0], T[c][0], v.c[1], T[c][1]), mdot2(v.c[2], T[c][2], v.c[3], T[c][3]));
   return r;
 }
 

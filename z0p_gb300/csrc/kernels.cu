@@ -92,175 +92,299 @@ __global__ void fill_columns_kernel(uint32_t* cols, uint32_t n, uint32_t ncols,
 
 // ----------------------------------------------------------------- NTT ----
 // Exact arithmetic: any transform order gives the reference's values
-// (src/ntt.rs:116-177 is radix-2 DIT; these kernels are DIF in shared memory
-// with a bit-reversed read-out).
+// (src/ntt.rs:116-177 is radix-2 DIT). These kernels run decimation in
+// frequency with a bit-reversed read-out. Each column of 2^L values sits in
+// shared memory at the skewed index i + i/32 (no bank conflicts for unit or
+// power-of-two strides); its stages are done four at a time in registers, one
+// 16-element group per thread per pass. L is a template parameter, so every
+// shared-memory offset inside a group is a compile-time immediate: for a
+// group base i0 whose bits [s_lo, s_lo + K) are zero,
+// spos(i0 + (t << s_lo)) = spos(i0) + (t << s_lo) + ((t << s_lo) >> 5).
 struct NttArgs {
   uint32_t logn, inverse, in_div, twist_mod, twist_shift, post_gamma, ninv_m;
   Tables tb;
 };
 
-// In-place DIF over `cols` independent columns of length 2^logl held in
-// shared memory at s[c * cstride + i * istride]; tw[t] = w^t for t < len/2.
-__device__ __forceinline__ void smem_dif(uint32_t* s, const uint32_t* tw, uint32_t logl,
-                                         uint32_t logcols, uint32_t cstride, uint32_t istride,
-                                         bool col_fast) {
-  uint32_t half = 1u << (logl - 1);
-  uint32_t total = half << logcols;
-  for (uint32_t h = half; h >= 1; h >>= 1) {
-    uint32_t tshift = __ffs(half / h) - 1;  // log2(half / h)
-    for (uint32_t idx = threadIdx.x; idx < total; idx += blockDim.x) {
-      uint32_t c, bj;
-      if (col_fast) {
-        c = idx & ((1u << logcols) - 1u);
-        bj = idx >> logcols;
-      } else {
-        c = idx >> (logl - 1);
-        bj = idx & (half - 1u);
-      }
-      uint32_t jj = bj & (h - 1u);
-      uint32_t i0 = ((bj - jj) << 1) + jj;
-      uint32_t p0 = c * cstride + i0 * istride;
-      uint32_t p1 = p0 + h * istride;
-      uint32_t u = s[p0], v = s[p1];
-      s[p0] = fadd(u, v);
-      s[p1] = mmul(fsub(u, v), tw[jj << tshift]);
+__device__ __forceinline__ uint32_t spos(uint32_t i) { return i + (i >> 5); }
+__host__ __device__ constexpr uint32_t skewed_len(uint32_t n) { return n + (n >> 5); }
+
+// K DIF stages (distances 2^S_HI .. 2^(S_HI-K+1)) on group g of a column at
+// col (skewed); tw[e] = w^e (Montgomery) for the column root w of order 2^L.
+// Butterfly (u + v, (u - v) w): u - v + p < 2^32 and w < p keep the
+// Montgomery product exact without a prior reduction.
+template <int L, int S_HI, int K>
+__device__ __forceinline__ void dif_group_t(uint32_t* col, const uint32_t* tw, uint32_t g) {
+  constexpr int S_LO = S_HI + 1 - K;
+  const uint32_t g_lo = g & ((1u << S_LO) - 1u);
+  const uint32_t i0 = g_lo | ((g >> S_LO) << (S_HI + 1));
+  uint32_t* base = col + spos(i0);
+  uint32_t x[1 << K];
+#pragma unroll
+  for (int t = 0; t < (1 << K); t++) x[t] = base[(t << S_LO) + ((t << S_LO) >> 5)];
+#pragma unroll
+  for (int st = K - 1; st >= 0; st--) {
+    const int d = 1 << st;
+    const uint32_t tshift = L - (S_LO + st) - 1;
+    const uint32_t* twb = tw + (g_lo << tshift);
+#pragma unroll
+    for (int t = 0; t < (1 << K); t++) {
+      if (t & d) continue;
+      const uint32_t w = twb[(t & (d - 1)) << (S_LO + tshift)];
+      const uint32_t u = x[t], v = x[t + d];
+      x[t] = fadd(u, v);
+      x[t + d] = mmul(u + kP - v, w);
     }
-    __syncthreads();
   }
+#pragma unroll
+  for (int t = 0; t < (1 << K); t++) base[(t << S_LO) + ((t << S_LO) >> 5)] = x[t];
 }
 
-__global__ void ntt_small_kernel(const uint32_t* __restrict__ in, uint32_t* __restrict__ out,
-                                 NttArgs a) {
+template <int L, int S_HI>
+__device__ __forceinline__ void dif_passes_t(uint32_t* s, const uint32_t* tw, uint32_t ncols,
+                                             uint32_t cstride) {
+  constexpr int K = S_HI + 1 < 4 ? S_HI + 1 : 4;
+  constexpr uint32_t groups = 1u << (L - K);
+  const uint32_t total = groups * ncols;
+  for (uint32_t idx = threadIdx.x; idx < total; idx += blockDim.x)
+    dif_group_t<L, S_HI, K>(s + (idx >> (L - K)) * cstride, tw, idx & (groups - 1u));
+  __syncthreads();
+  if constexpr (S_HI - K >= 0) dif_passes_t<L, S_HI - K>(s, tw, ncols, cstride);
+}
+
+template <int L>
+__device__ __forceinline__ void smem_dif_t(uint32_t* s, const uint32_t* tw, uint32_t ncols,
+                                           uint32_t cstride) {
+  if constexpr (L > 0) dif_passes_t<L, L - 1>(s, tw, ncols, cstride);
+}
+
+// One transform of length 2^L per CTA (L <= 12).
+template <int L>
+__global__ void __launch_bounds__(512) ntt_small_kernel(const uint32_t* __restrict__ in,
+                                                        uint32_t* __restrict__ out, NttArgs a) {
   extern __shared__ uint32_t sm[];
-  const uint32_t n = 1u << a.logn, half = n >> 1;
+  constexpr uint32_t n = 1u << L;
   uint32_t* s = sm;
-  uint32_t* tw = sm + n;
+  uint32_t* tw = sm + skewed_len(n);
   const uint32_t b = blockIdx.x;
   const uint32_t* src = in + (size_t)(b / a.in_div) * n;
   const uint32_t j = b % a.twist_mod;
-  const uint32_t shift = kRootBits - a.logn;
-  for (uint32_t i = threadIdx.x; i < half; i += blockDim.x)
-    tw[i] = root_pow(a.tb, tw_exp(i, shift, a.inverse));
+  for (uint32_t i = threadIdx.x; i < n / 2; i += blockDim.x)
+    tw[i] = root_pow(a.tb, tw_exp(i, kRootBits - L, a.inverse));
+  // twist w^(j i): a geometric chain per thread (stride blockDim)
+  uint32_t tw_cur = 0, tw_step = 0;
+  if (j) {
+    tw_cur = root_pow(a.tb, (j * threadIdx.x) << a.twist_shift);
+    tw_step = root_pow(a.tb, (j * blockDim.x) << a.twist_shift);
+  }
   for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
     uint32_t v = src[i];
-    if (j) v = mmul(v, root_pow(a.tb, (j * i) << a.twist_shift));
-    s[i] = v;
+    if (j) {
+      v = mmul(v, tw_cur);
+      tw_cur = mmul(tw_cur, tw_step);
+    }
+    s[spos(i)] = v;
   }
   __syncthreads();
-  if (a.logn > 0) smem_dif(s, tw, a.logn, 0, 0, 1, true);
+  smem_dif_t<L>(s, tw, 1, 0);
   uint32_t* dst = out + (size_t)b * n;
+  uint32_t g_cur = 0, g_step = 0;
+  if (a.post_gamma) {
+    g_cur = mmul(gamma_pow(a.tb, threadIdx.x), a.ninv_m);
+    g_step = gamma_pow(a.tb, blockDim.x);
+  }
   for (uint32_t k = threadIdx.x; k < n; k += blockDim.x) {
-    uint32_t v = s[brev_bits(k, a.logn)];
-    if (a.post_gamma) v = mmul(mmul(v, gamma_pow(a.tb, k)), a.ninv_m);
+    uint32_t v = s[spos(brev_bits(k, L))];
+    if (a.post_gamma) {
+      v = mmul(v, g_cur);
+      g_cur = mmul(g_cur, g_step);
+    }
     dst[k] = v;
   }
 }
 
-// Four-step pass 1: for C columns i2 of x viewed as [n1][n2], n1-point
-// transforms over i1, times omega_n^(i2 k1); written transposed as yt[k1][i2].
-template <int LOGC>
-__global__ void ntt_pass1_kernel(const uint32_t* __restrict__ in, uint32_t* __restrict__ yt,
-                                 NttArgs a, uint32_t logn1) {
+// Column stride (words) of C skewed columns of length 2^L: congruent to 32/C
+// mod 32 so the transposing store of a C-wide row hits distinct banks.
+__host__ __device__ constexpr uint32_t col_stride(uint32_t L, uint32_t C) {
+  return skewed_len(1u << L) + ((32u / C - (skewed_len(1u << L) & 31u)) & 31u);
+}
+
+// Four-step pass 1: for C columns i2 of x viewed as [n1][n2] (n1 = 2^L1),
+// n1-point transforms over i1. The coset twist w^(j i), i = n2 i1 + i2,
+// splits into a per-CTA table over i1 (applied on load) and a per-column
+// factor folded into the four-step twiddle on the way out; each thread then
+// writes C consecutive words of row k1 of yt (32 bytes for C = 8), with the
+// twiddles w_k1(i2) a geometric chain in i2.
+template <int L1, int LOGC>
+__global__ void __launch_bounds__(512) ntt_pass1_kernel(const uint32_t* __restrict__ in,
+                                                        uint32_t* __restrict__ yt, NttArgs a) {
   constexpr uint32_t C = 1u << LOGC;
+  constexpr uint32_t n1 = 1u << L1;
+  constexpr uint32_t cstride = col_stride(L1, C);
   extern __shared__ uint32_t sm[];
-  const uint32_t logn2 = a.logn - logn1;
-  const uint32_t n1 = 1u << logn1;
+  const uint32_t logn2 = a.logn - L1;
   const uint32_t n = 1u << a.logn;
   uint32_t* s = sm;
-  uint32_t* tw = sm + (n1 << LOGC);
+  uint32_t* tw = sm + C * cstride;
+  uint32_t* twist = tw + n1 / 2;
   const uint32_t b = blockIdx.y;
   const uint32_t c0 = blockIdx.x * C;
   const uint32_t* src = in + (size_t)(b / a.in_div) * n;
   const uint32_t j = b % a.twist_mod;
   for (uint32_t i = threadIdx.x; i < n1 / 2; i += blockDim.x)
-    tw[i] = root_pow(a.tb, tw_exp(i, kRootBits - logn1, a.inverse));
+    tw[i] = root_pow(a.tb, tw_exp(i, kRootBits - L1, a.inverse));
+  if (j)
+    for (uint32_t i1 = threadIdx.x; i1 < n1; i1 += blockDim.x)
+      twist[i1] = root_pow(a.tb, ((j * i1) << logn2) << a.twist_shift);
+  __syncthreads();
   for (uint32_t e = threadIdx.x; e < (n1 << LOGC); e += blockDim.x) {
-    uint32_t i1 = e >> LOGC, c = e & (C - 1);
-    uint32_t i = (i1 << logn2) + c0 + c;
-    uint32_t v = src[i];
-    if (j) v = mmul(v, root_pow(a.tb, (j * i) << a.twist_shift));
-    s[e] = v;
+    const uint32_t i1 = e >> LOGC, c = e & (C - 1);
+    uint32_t v = src[(i1 << logn2) + c0 + c];
+    if (j) v = mmul(v, twist[i1]);
+    s[c * cstride + spos(i1)] = v;
   }
   __syncthreads();
-  smem_dif(s, tw, logn1, LOGC, 1, C, true);
+  smem_dif_t<L1>(s, tw, C, cstride);
   uint32_t* dst = yt + (size_t)b * n;
   const uint32_t shift = kRootBits - a.logn;
-  for (uint32_t e = threadIdx.x; e < (n1 << LOGC); e += blockDim.x) {
-    uint32_t k1 = e >> LOGC, c = e & (C - 1);
-    uint32_t i2 = c0 + c;
-    uint32_t v = s[(brev_bits(k1, logn1) << LOGC) + c];
-    v = mmul(v, root_pow(a.tb, tw_exp(i2 * k1, shift, a.inverse)));
-    dst[((size_t)k1 << logn2) + i2] = v;
+  for (uint32_t k1 = threadIdx.x; k1 < n1; k1 += blockDim.x) {
+    const uint32_t p = spos(brev_bits(k1, L1));
+    // exponent of the twiddle for column i2: tw_exp(i2 k1) + (j i2 << twist_shift)
+    const uint32_t step = tw_exp(k1, shift, a.inverse) + (j << a.twist_shift);
+    uint32_t w = root_pow(a.tb, step * c0);
+    const uint32_t wstep = root_pow(a.tb, step);
+    uint32_t v[C];
+#pragma unroll
+    for (uint32_t c = 0; c < C; c++) {
+      v[c] = mmul(s[c * cstride + p], w);
+      w = mmul(w, wstep);
+    }
+    uint32_t* row = dst + ((size_t)k1 << logn2) + c0;
+#pragma unroll
+    for (uint32_t c = 0; c < C; c += 4)
+      *reinterpret_cast<uint4*>(row + c) = make_uint4(v[c], v[c + 1], v[c + 2], v[c + 3]);
   }
 }
 
-// Four-step pass 2: for R rows k1 of yt, n2-point transforms over i2; output
-// k = k1 + n1 k2 (natural order), optionally scaled by 31^k / n.
-template <int LOGR>
-__global__ void ntt_pass2_kernel(const uint32_t* __restrict__ yt, uint32_t* __restrict__ out,
-                                 NttArgs a, uint32_t logn1) {
+// Four-step pass 2: for R rows k1 of yt, n2-point transforms over i2 (n2 =
+// 2^L2); output k = k1 + n1 k2 (natural order). Each thread writes R
+// consecutive words of out, optionally scaled by 31^k / n (a chain in k).
+template <int L2, int LOGR>
+__global__ void __launch_bounds__(512) ntt_pass2_kernel(const uint32_t* __restrict__ yt,
+                                                        uint32_t* __restrict__ out, NttArgs a) {
   constexpr uint32_t R = 1u << LOGR;
+  constexpr uint32_t n2 = 1u << L2;
+  constexpr uint32_t rstride = col_stride(L2, R);
   extern __shared__ uint32_t sm[];
-  const uint32_t logn2 = a.logn - logn1;
-  const uint32_t n2 = 1u << logn2;
+  const uint32_t logn1 = a.logn - L2;
   const uint32_t n = 1u << a.logn;
-  const uint32_t stride = n2 + 1;  // padding against bank conflicts on the read-out
   uint32_t* s = sm;
-  uint32_t* tw = sm + R * stride;
+  uint32_t* tw = sm + R * rstride;
   const uint32_t b = blockIdx.y;
   const uint32_t r0 = blockIdx.x * R;
   for (uint32_t i = threadIdx.x; i < n2 / 2; i += blockDim.x)
-    tw[i] = root_pow(a.tb, tw_exp(i, kRootBits - logn2, a.inverse));
-  const uint32_t* src = yt + (size_t)b * n + ((size_t)r0 << logn2);
-  for (uint32_t e = threadIdx.x; e < (R << logn2); e += blockDim.x) {
-    uint32_t r = e >> logn2, i2 = e & (n2 - 1);
-    s[r * stride + i2] = src[e];
+    tw[i] = root_pow(a.tb, tw_exp(i, kRootBits - L2, a.inverse));
+  const uint4* src = reinterpret_cast<const uint4*>(yt + (size_t)b * n + ((size_t)r0 << L2));
+  for (uint32_t e = threadIdx.x; e < (R << L2) / 4; e += blockDim.x) {
+    const uint32_t r = (4 * e) >> L2, i2 = (4 * e) & (n2 - 1);
+    const uint4 v = src[e];
+    uint32_t* dstrow = s + r * rstride + spos(i2);  // i2 % 4 == 0: no skew step inside
+    dstrow[0] = v.x;
+    dstrow[1] = v.y;
+    dstrow[2] = v.z;
+    dstrow[3] = v.w;
   }
   __syncthreads();
-  smem_dif(s, tw, logn2, LOGR, stride, 1, false);
+  smem_dif_t<L2>(s, tw, R, rstride);
   uint32_t* dst = out + (size_t)b * n;
-  for (uint32_t e = threadIdx.x; e < (R << logn2); e += blockDim.x) {
-    uint32_t k2 = e >> LOGR, r = e & (R - 1);
-    uint32_t k = r0 + r + (k2 << logn1);
-    uint32_t v = s[r * stride + brev_bits(k2, logn2)];
-    if (a.post_gamma) v = mmul(mmul(v, gamma_pow(a.tb, k)), a.ninv_m);
-    dst[k] = v;
+  for (uint32_t k2 = threadIdx.x; k2 < n2; k2 += blockDim.x) {
+    const uint32_t p = spos(brev_bits(k2, L2));
+    const uint32_t k0 = r0 + (k2 << logn1);
+    uint32_t v[R];
+    if (a.post_gamma) {
+      uint32_t g = mmul(gamma_pow(a.tb, k0), a.ninv_m);
+      const uint32_t gamma_m = to_mont(31u);
+#pragma unroll
+      for (uint32_t r = 0; r < R; r++) {
+        v[r] = mmul(s[r * rstride + p], g);
+        g = mmul(g, gamma_m);
+      }
+    } else {
+#pragma unroll
+      for (uint32_t r = 0; r < R; r++) v[r] = s[r * rstride + p];
+    }
+    uint32_t* o = dst + k0;
+#pragma unroll
+    for (uint32_t r = 0; r < R; r += 4)
+      *reinterpret_cast<uint4*>(o + r) = make_uint4(v[r], v[r + 1], v[r + 2], v[r + 3]);
   }
 }
 
 // Per coset j: 1 / (x^N - 1) with x^N = 31^N * omega_B^j (constant on the
-// coset), in Montgomery form, and the same value times 2^32 once more.
+// coset), in Montgomery form, the same value times 2^32 once more, and the
+// linked-column constant C_j = coeff * (x^N - 1) (canonical).
 __global__ void coset_zinv_kernel(uint32_t* zinv, uint32_t* zinv2, uint32_t logB,
-                                  uint32_t gamma_n_m, Tables tb) {
+                                  uint32_t gamma_n_m, uint32_t* cb, uint32_t coeff, Tables tb) {
   uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= (1u << logB)) return;
   uint32_t xn = mmul(gamma_n_m, root_pow(tb, j << (kRootBits - logB)));
-  uint32_t inv = minv(fsub(xn, kR));
+  uint32_t xn1 = fsub(xn, kR);
+  uint32_t inv = minv(xn1);
   zinv[j] = inv;
   zinv2[j] = mmul(inv, kR2);
+  if (cb) cb[j] = mmul(coeff, xn1);
+}
+
+// B at row k = B q + j of the LDE from A: A[j][q+1] + C_j / (x_k - w_last),
+// given the Montgomery-form inverse of (x_k - w_last).
+__device__ __forceinline__ uint32_t linked_b(const uint32_t* lde_a, uint32_t logN, uint32_t j,
+                                             uint32_t q, uint32_t cbj, uint32_t inv_den_m) {
+  const uint32_t N = 1u << logN;
+  return fadd(__ldg(lde_a + ((size_t)j << logN) + ((q + 1u) & (N - 1u))), mmul(cbj, inv_den_m));
 }
 
 // --------------------------------------------------------------- Merkle ----
 // Trace tree leaf L = rows 8L..8L+7 packed A||B (src/air.rs:520-531), hashed
-// as one 64-byte block (src/merkle.rs:93-110).
-__global__ void air_trace_leaves_kernel(const uint32_t* __restrict__ lde_a,
-                                        const uint32_t* __restrict__ lde_b,
-                                        uint32_t* __restrict__ leaves, uint32_t logN,
-                                        uint32_t logB, uint32_t nleaves) {
+// as one 64-byte block (src/merkle.rs:93-110). B comes from A (linked_b):
+// eight (x - w_last) inverses per thread in one batch.
+__global__ void __launch_bounds__(256) air_trace_leaves_kernel(
+    const uint32_t* __restrict__ lde_a, const uint32_t* __restrict__ cb, uint32_t w_last_m,
+    uint32_t* __restrict__ leaves, uint32_t logN, uint32_t logB, uint32_t nleaves, Tables tb) {
   uint32_t L = blockIdx.x * blockDim.x + threadIdx.x;
   if (L >= nleaves) return;
+  const uint32_t logm = logN + logB;
+  const uint32_t gamma_m = to_mont(31u);
+  uint32_t den[8];
+#pragma unroll
+  for (int r = 0; r < 8; r++) {
+    uint32_t k = 8u * L + r;
+    den[r] = fsub(mmul(gamma_m, root_pow(tb, k << (kRootBits - logm))), w_last_m);
+  }
+  batch_minv(den);
   uint32_t m[16];
 #pragma unroll
   for (int r = 0; r < 8; r++) {
     uint32_t k = 8u * L + r;
     uint32_t j = k & ((1u << logB) - 1u), q = k >> logB;
-    size_t off = ((size_t)j << logN) + q;
-    m[2 * r] = __ldg(lde_a + off);
-    m[2 * r + 1] = __ldg(lde_b + off);
+    m[2 * r] = __ldg(lde_a + ((size_t)j << logN) + q);
+    m[2 * r + 1] = linked_b(lde_a, logN, j, q, __ldg(cb + j), den[r]);
   }
   uint32_t d[8];
   blake3_leaf64(m, d);
   store_digest(leaves + 8 * (size_t)L, d);
+}
+
+// (A, B) at arbitrary natural rows, for the trace openings.
+__global__ void air_rows_kernel(const uint32_t* __restrict__ lde_a, const uint32_t* __restrict__ cb,
+                                uint32_t w_last_m, uint32_t logN, uint32_t logB,
+                                const uint32_t* __restrict__ rows, uint32_t n,
+                                uint32_t* __restrict__ out, Tables tb) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint32_t k = rows[i], logm = logN + logB;
+  const uint32_t j = k & ((1u << logB) - 1u), q = k >> logB;
+  uint32_t x = mmul(to_mont(31u), root_pow(tb, k << (kRootBits - logm)));
+  out[2 * i] = __ldg(lde_a + ((size_t)j << logN) + q);
+  out[2 * i + 1] = linked_b(lde_a, logN, j, q, __ldg(cb + j), minv(fsub(x, w_last_m)));
 }
 
 // Range tree leaf k = BLAKE3(0x00 || row k) with the row = ncols LE words
@@ -317,16 +441,76 @@ __device__ __forceinline__ uint64_t level_offset(uint64_t leaves, uint32_t level
   return 2 * leaves - 2 * (leaves >> level);
 }
 
-// Remaining levels of a tree once a level has <= 2 * blockDim nodes: one CTA.
-__global__ void merkle_tail_kernel(uint32_t* tree, uint64_t leaves, uint32_t start_level) {
-  for (uint32_t l = start_level; (leaves >> l) > 1; l++) {
+// Upper levels of a tree without a grid barrier: CTA b hashes the 2T nodes
+// [2T b, 2T b + 2T) of level l0 up to one node at level l0 + log2(2T) (or
+// up to `top`), keeping each level in shared memory and writing it to
+// global. The CTA that finishes last (one atomic per CTA on `counter`, after a
+// release fence) then hashes the remaining levels from the other CTAs' roots.
+// Nobody waits for anybody: the last CTA simply continues.
+constexpr int kTopThreads = 256;
+
+__device__ __forceinline__ void hash_pair_to(const uint32_t* l, const uint32_t* r, uint32_t* out) {
+  uint32_t a[8], b[8], d[8];
+#pragma unroll
+  for (int i = 0; i < 8; i++) { a[i] = l[i]; b[i] = r[i]; }
+  blake3_node(a, b, d);
+#pragma unroll
+  for (int i = 0; i < 8; i++) out[i] = d[i];
+}
+
+__global__ void __launch_bounds__(kTopThreads) merkle_top_kernel(uint32_t* tree, uint64_t leaves,
+                                                                 uint32_t l0, uint32_t top,
+                                                                 unsigned int* counter) {
+  __shared__ uint32_t sm[2][kTopThreads * 8];
+  __shared__ int last;
+  const uint32_t lsub = l0 + 9 < top ? l0 + 9 : top;  // last level done per CTA
+  // level l0+1: thread t hashes children 2(base+t), 2(base+t)+1
+  uint64_t cnt = leaves >> (l0 + 1);                    // nodes at level l0+1
+  uint64_t per = 1ull << (lsub - l0 - 1);               // nodes per CTA at level l0+1
+  uint64_t node = (uint64_t)blockIdx.x * per + threadIdx.x;
+  int cur = 0;
+  if (threadIdx.x < per && node < cnt) {
+    const uint32_t* prev = tree + 8 * level_offset(leaves, l0);
+    uint32_t d[8];
+    uint32_t a[8], b[8];
+    load_digest(prev + 16 * node, a);
+    load_digest(prev + 16 * node + 8, b);
+    blake3_node(a, b, d);
+    store_digest(tree + 8 * (level_offset(leaves, l0 + 1) + node), d);
+#pragma unroll
+    for (int i = 0; i < 8; i++) sm[cur][8 * threadIdx.x + i] = d[i];
+  }
+  __syncthreads();
+  for (uint32_t l = l0 + 1; l < lsub; l++) {
+    per >>= 1;
+    if (threadIdx.x < per) {
+      uint32_t* out = sm[cur ^ 1] + 8 * threadIdx.x;
+      hash_pair_to(sm[cur] + 16 * threadIdx.x, sm[cur] + 16 * threadIdx.x + 8, out);
+      uint64_t n = (uint64_t)blockIdx.x * per + threadIdx.x;
+      uint32_t* g = tree + 8 * (level_offset(leaves, l + 1) + n);
+#pragma unroll
+      for (int i = 0; i < 8; i++) g[i] = out[i];
+    }
+    cur ^= 1;
+    __syncthreads();
+  }
+  if (lsub == top) return;
+  // Publish this CTA's root, then let the last CTA finish the tree.
+  __threadfence();
+  if (threadIdx.x == 0) last = (atomicAdd(counter, 1u) == gridDim.x - 1);
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  for (uint32_t l = lsub; l < top; l++) {
+    const uint64_t n = leaves >> (l + 1);
     const uint32_t* prev = tree + 8 * level_offset(leaves, l);
     uint32_t* next = tree + 8 * level_offset(leaves, l + 1);
-    uint64_t cnt = leaves >> (l + 1);
-    for (uint64_t i = threadIdx.x; i < cnt; i += blockDim.x) {
-      uint32_t a[8], b[8], d[8];
-      load_digest(prev + 16 * i, a);
-      load_digest(prev + 16 * i + 8, b);
+    for (uint64_t i = threadIdx.x; i < n; i += blockDim.x) {
+      const uint4* p = reinterpret_cast<const uint4*>(prev + 16 * i);
+      uint4 a0 = __ldcg(p), a1 = __ldcg(p + 1), b0 = __ldcg(p + 2), b1 = __ldcg(p + 3);
+      uint32_t a[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+      uint32_t b[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+      uint32_t d[8];
       blake3_node(a, b, d);
       store_digest(next + 8 * i, d);
     }
@@ -367,6 +551,8 @@ __global__ void leaf16_kernel(const uint32_t* __restrict__ values, uint32_t* __r
 // -------------------------------------------------------------- compose ----
 // AIR composition (src/air.rs:847-929 == composition_at :938-962) on the four
 // rows of layer-0 quad P, written bit-reversed as one 64-byte leaf and hashed.
+// B at rows q and q+1 comes from A (linked_b); the inverses of (x - 1),
+// (x - w_last) and (x omega_N - w_last) for the four rows share one batch.
 __global__ void __launch_bounds__(kThreads) air_compose_leaves_kernel(AirComposeArgs a, Tables tb) {
   const uint32_t logm = a.logN + a.logB;
   const uint32_t quarter = 1u << (logm - 2);
@@ -381,43 +567,42 @@ __global__ void __launch_bounds__(kThreads) air_compose_leaves_kernel(AirCompose
     k0 = u;
   }
   const uint32_t P = brev_bits(k0, logm - 2);
-  uint32_t va[4], vb[4], van[4], vbn[4], zt[4];
-  uint32_t den[8];
   const uint32_t gamma_m = to_mont(31u);
+  uint32_t den[12], zt[4];
 #pragma unroll
   for (int s = 0; s < 4; s++) {
     uint32_t k = k0 + (uint32_t)s * quarter;
-    uint32_t j = k & (B - 1u), q = k >> a.logB;
-    uint32_t qn = (q + 1u) & (N - 1u);
-    size_t base = (size_t)j << a.logN;
-    va[s] = __ldg(a.lde_a + base + q);
-    vb[s] = __ldg(a.lde_b + base + q);
-    van[s] = __ldg(a.lde_a + base + qn);
-    vbn[s] = __ldg(a.lde_b + base + qn);
+    uint32_t j = k & (B - 1u);
     uint32_t x = mmul(gamma_m, root_pow(tb, k << (kRootBits - logm)));
-    den[2 * s] = fsub(x, a.w_last_m);
-    den[2 * s + 1] = fsub(x, kR);
-    zt[s] = mmul(den[2 * s], __ldg(a.zinv + j));  // 1 / Z_t = (x - w_last) / (x^N - 1)
+    den[3 * s] = fsub(x, a.w_last_m);                              // row q
+    den[3 * s + 1] = fsub(x, kR);                                  // x - 1
+    den[3 * s + 2] = fsub(mmul(x, a.omega_n_m), a.w_last_m);       // row q + 1
+    zt[s] = mmul(den[3 * s], __ldg(a.zinv + j));  // 1 / Z_t = (x - w_last) / (x^N - 1)
   }
   batch_minv(den);
   uint32_t leaf[16];
 #pragma unroll
   for (int s = 0; s < 4; s++) {
-    uint32_t av = va[s], bv = vb[s];
-    uint32_t t1 = mmul(fsub(van[s], bv), zt[s]);
-    uint32_t t2 = mmul(fsub(vbn[s], fadd(av, bv)), zt[s]);
-    uint32_t ba = mmul(fsub(av, a.a0), den[2 * s + 1]);
-    uint32_t bb = mmul(fsub(bv, a.b0), den[2 * s + 1]);
-    uint32_t bo = mmul(fsub(bv, a.b_last), den[2 * s]);
+    uint32_t k = k0 + (uint32_t)s * quarter;
+    uint32_t j = k & (B - 1u), q = k >> a.logB;
+    uint32_t qn = (q + 1u) & (N - 1u);
+    const uint32_t cbj = __ldg(a.cb + j);
+    const size_t base = (size_t)j << a.logN;
+    uint32_t av = __ldg(a.lde_a + base + q);
+    uint32_t avn = __ldg(a.lde_a + base + qn);
+    uint32_t bv = linked_b(a.lde_a, a.logN, j, q, cbj, den[3 * s]);
+    uint32_t bvn = linked_b(a.lde_a, a.logN, j, qn, cbj, den[3 * s + 2]);
+    uint32_t t1 = mmul(fsub(avn, bv), zt[s]);
+    uint32_t t2 = mmul(fsub(bvn, fadd(av, bv)), zt[s]);
+    uint32_t ba = mmul(fsub(av, a.a0), den[3 * s + 1]);
+    uint32_t bb = mmul(fsub(bv, a.b0), den[3 * s + 1]);
+    uint32_t bo = mmul(fsub(bv, a.b_last), den[3 * s]);
     const int t = (s == 1) ? 2 : (s == 2) ? 1 : s;  // position 4P + brev2(s)
 #pragma unroll
     for (int c = 0; c < 4; c++) {
-      uint32_t acc = mmul(t1, a.alpha[0][c]);
-      acc = fadd(acc, mmul(t2, a.alpha[1][c]));
-      acc = fadd(acc, mmul(ba, a.alpha[2][c]));
-      acc = fadd(acc, mmul(bb, a.alpha[3][c]));
-      acc = fadd(acc, mmul(bo, a.alpha[4][c]));
-      leaf[4 * t + c] = acc;
+      const uint32_t* al = a.alpha[c];
+      uint32_t acc = fadd(mdot2(t1, al[0], t2, al[1]), mdot2(ba, al[2], bb, al[3]));
+      leaf[4 * t + c] = fadd(acc, mmul(bo, al[4]));
     }
   }
   uint4* dst = reinterpret_cast<uint4*>(a.layer0 + 16 * (size_t)P);
@@ -500,21 +685,20 @@ __global__ void __launch_bounds__(kThreads) range_compose_leaves_kernel(RangeCom
 }
 
 // ----------------------------------------------------------------- FRI ----
-// fold_values (src/fri.rs:1311-1331): A + x^-1 (r0 B + x^-1 (r1 C + x^-1 r2 D)).
+// fold_values (src/fri.rs:1311-1331): A + x^-1 (r0 B + x^-1 (r1 C + x^-1 r2 D))
+// with B, C, D the quarter-scaled differences; the 1/4 is folded into the
+// challenge tables (r_k / 4), so only the mean is halved twice here.
 __device__ __forceinline__ E4 fold_quad(const E4& q0, const E4& q1, const E4& q2, const E4& q3,
                                         uint32_t xinv_m, const FoldArgs& a) {
   E4 s01 = e4_add(q0, q1), s23 = e4_add(q2, q3);
   E4 odd_diff = e4_sub(q0, q1);
   E4 skew_u = e4_mul_base(e4_sub(q2, q3), a.unit_m);
   E4 mean = e4_quarter(e4_add(s01, s23));
-  E4 odd = e4_quarter(e4_sub(odd_diff, skew_u));
-  E4 even = e4_quarter(e4_sub(s01, s23));
-  E4 skew = e4_quarter(e4_add(odd_diff, skew_u));
-  E4 r0, r1, r2;
-#pragma unroll
-  for (int c = 0; c < 4; c++) { r0.c[c] = a.ch[0][c]; r1.c[c] = a.ch[1][c]; r2.c[c] = a.ch[2][c]; }
-  E4 acc = e4_add(e4_mul_base(e4_mul_cm(skew, r2), xinv_m), e4_mul_cm(even, r1));
-  acc = e4_add(e4_mul_base(acc, xinv_m), e4_mul_cm(odd, r0));
+  E4 odd4 = e4_sub(odd_diff, skew_u);
+  E4 even4 = e4_sub(s01, s23);
+  E4 skew4 = e4_add(odd_diff, skew_u);
+  E4 acc = e4_add(e4_mul_base(e4_mul_tab(skew4, a.tab[2]), xinv_m), e4_mul_tab(even4, a.tab[1]));
+  acc = e4_add(e4_mul_base(acc, xinv_m), e4_mul_tab(odd4, a.tab[0]));
   return e4_add(mean, e4_mul_base(acc, xinv_m));
 }
 
@@ -671,6 +855,15 @@ __global__ void gather4_kernel(const uint64_t* __restrict__ addr, uint32_t* __re
 }  // namespace
 
 // ============================================================= launchers ====
+void e4_table(const uint32_t r[4], uint32_t T[4][4]) {
+  auto m = [](uint64_t x) { return (uint32_t)(((x % kP) << 32) % kP); };
+  const uint64_t r0 = r[0], r1 = r[1], r2 = r[2], r3 = r[3];
+  const uint64_t e1 = 11 * r1, e2 = 11 * r2, e3 = 11 * r3;
+  const uint64_t rows[4][4] = {{r0, e1, e3, e2}, {r1, r0, r2, e3}, {r2, e3, r0, e1}, {r3, r2, r1, r0}};
+  for (int c = 0; c < 4; c++)
+    for (int i = 0; i < 4; i++) T[c][i] = m(rows[c][i]);
+}
+
 namespace launch {
 
 static std::atomic<uint64_t> g_launches{0};
@@ -731,67 +924,87 @@ cudaError_t ntt(cudaStream_t st, const Tables& tb, const NttPlan& plan, const ui
   a.tb = tb;
   const uint32_t n = 1u << plan.logn;
   if (plan.logn <= 12) {
-    size_t smem = (size_t)(n + n / 2 + 1) * 4;
-    static bool attr_set = false;
-    if (!attr_set) {
-      cudaFuncSetAttribute(ntt_small_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 48 * 1024);
-      attr_set = true;
-    }
+    size_t smem = (size_t)(skewed_len(n) + n / 2 + 1) * 4;
+    int threads = n >= 2048 ? 512 : (n >= 256 ? 256 : 128);
     Stage stg(plan.inverse ? "intt" : "ntt", st);
     stg.launched();
-    ntt_small_kernel<<<plan.batch, 256, smem, st>>>(in, out, a);
+    switch (plan.logn) {
+#define Z0P_SMALL(Lv) \
+  case Lv: ntt_small_kernel<Lv><<<plan.batch, threads, smem, st>>>(in, out, a); break;
+      Z0P_SMALL(0) Z0P_SMALL(1) Z0P_SMALL(2) Z0P_SMALL(3) Z0P_SMALL(4) Z0P_SMALL(5)
+      Z0P_SMALL(6) Z0P_SMALL(7) Z0P_SMALL(8) Z0P_SMALL(9) Z0P_SMALL(10) Z0P_SMALL(11)
+      Z0P_SMALL(12)
+#undef Z0P_SMALL
+    }
     return cudaGetLastError();
   }
   const uint32_t logn1 = (plan.logn + 1) / 2;
   const uint32_t logn2 = plan.logn - logn1;
   const uint32_t n1 = 1u << logn1, n2 = 1u << logn2;
-  static bool attrs = false;
-  if (!attrs) {
-    const int maxs = 200 * 1024;
-    cudaFuncSetAttribute(ntt_pass1_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxs);
-    cudaFuncSetAttribute(ntt_pass1_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxs);
-    cudaFuncSetAttribute(ntt_pass2_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxs);
-    cudaFuncSetAttribute(ntt_pass2_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxs);
-    attrs = true;
-  }
-  // C = R = 8 columns per CTA (32-byte segments), 4 for the largest halves.
+  // C = R = 8 columns per CTA (32-byte global segments), 4 for the largest halves.
   const int logc = logn1 > 12 ? 2 : 3;
-  size_t smem1 = ((size_t)(n1 << logc) + n1 / 2) * 4;
-  dim3 g1(n2 >> logc, plan.batch);
+  const int logr = logn2 > 12 ? 2 : 3;
+  size_t smem1 = ((size_t)(col_stride(logn1, 1u << logc) << logc) + n1 / 2 + n1) * 4;
+  size_t smem2 = ((size_t)(col_stride(logn2, 1u << logr) << logr) + n2 / 2) * 4;
+  dim3 g1(n2 >> logc, plan.batch), g2(n1 >> logr, plan.batch);
   Stage stg(plan.inverse ? "intt" : "ntt", st);
   stg.launched(2);
-  if (logc == 3)
-    ntt_pass1_kernel<3><<<g1, 512, smem1, st>>>(in, scratch, a, logn1);
-  else
-    ntt_pass1_kernel<2><<<g1, 512, smem1, st>>>(in, scratch, a, logn1);
+  switch (logn1) {
+#define Z0P_P1(Lv, LC)                                                                          \
+  case Lv:                                                                                      \
+    cudaFuncSetAttribute(ntt_pass1_kernel<Lv, LC>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                         (int)smem1);                                                           \
+    ntt_pass1_kernel<Lv, LC><<<g1, 512, smem1, st>>>(in, scratch, a);                           \
+    break;
+    Z0P_P1(7, 3) Z0P_P1(8, 3) Z0P_P1(9, 3) Z0P_P1(10, 3) Z0P_P1(11, 3) Z0P_P1(12, 3) Z0P_P1(13, 2)
+#undef Z0P_P1
+    default: return cudaErrorInvalidValue;
+  }
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  const int logr = logn2 > 12 ? 2 : 3;
-  size_t smem2 = ((size_t)(n2 + 1) * (1u << logr) + n2 / 2) * 4;
-  dim3 g2(n1 >> logr, plan.batch);
-  if (logr == 3)
-    ntt_pass2_kernel<3><<<g2, 512, smem2, st>>>(scratch, out, a, logn1);
-  else
-    ntt_pass2_kernel<2><<<g2, 512, smem2, st>>>(scratch, out, a, logn1);
+  switch (logn2) {
+#define Z0P_P2(Lv, LR)                                                                          \
+  case Lv:                                                                                      \
+    cudaFuncSetAttribute(ntt_pass2_kernel<Lv, LR>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                         (int)smem2);                                                           \
+    ntt_pass2_kernel<Lv, LR><<<g2, 512, smem2, st>>>(scratch, out, a);                          \
+    break;
+    Z0P_P2(6, 3) Z0P_P2(7, 3) Z0P_P2(8, 3) Z0P_P2(9, 3) Z0P_P2(10, 3) Z0P_P2(11, 3) Z0P_P2(12, 3)
+    Z0P_P2(13, 2)
+#undef Z0P_P2
+    default: return cudaErrorInvalidValue;
+  }
   (void)n;
   return cudaGetLastError();
 }
 
 cudaError_t coset_zinv(cudaStream_t st, const Tables& tb, uint32_t* zinv, uint32_t* zinv2,
-                       uint32_t logB, uint32_t gamma_n_m) {
+                       uint32_t logB, uint32_t gamma_n_m, uint32_t* cb, uint32_t coeff) {
   Stage stg("coset_zinv", st);
   stg.launched();
-  coset_zinv_kernel<<<grid_for(1ull << logB), kThreads, 0, st>>>(zinv, zinv2, logB, gamma_n_m, tb);
+  coset_zinv_kernel<<<grid_for(1ull << logB), kThreads, 0, st>>>(zinv, zinv2, logB, gamma_n_m, cb,
+                                                                 coeff, tb);
   return cudaGetLastError();
 }
 
-cudaError_t air_trace_leaves(cudaStream_t st, const uint32_t* lde_a, const uint32_t* lde_b,
-                             uint32_t* leaves, uint32_t logN, uint32_t logB) {
+cudaError_t air_trace_leaves(cudaStream_t st, const Tables& tb, const uint32_t* lde_a,
+                             const uint32_t* cb, uint32_t w_last_m, uint32_t* leaves,
+                             uint32_t logN, uint32_t logB) {
   uint32_t nleaves = 1u << (logN + logB - 3);
   Stage stg("trace_leaves", st);
   stg.launched();
-  air_trace_leaves_kernel<<<grid_for(nleaves), kThreads, 0, st>>>(lde_a, lde_b, leaves, logN, logB,
-                                                                  nleaves);
+  air_trace_leaves_kernel<<<grid_for(nleaves), kThreads, 0, st>>>(lde_a, cb, w_last_m, leaves, logN,
+                                                                  logB, nleaves, tb);
+  return cudaGetLastError();
+}
+
+cudaError_t air_rows(cudaStream_t st, const Tables& tb, const uint32_t* lde_a, const uint32_t* cb,
+                     uint32_t w_last_m, uint32_t logN, uint32_t logB, const uint32_t* rows,
+                     uint32_t n, uint32_t* out) {
+  if (!n) return cudaSuccess;
+  Stage stg("gather", st);
+  stg.launched();
+  air_rows_kernel<<<grid_for(n), kThreads, 0, st>>>(lde_a, cb, w_last_m, logN, logB, rows, n, out, tb);
   return cudaGetLastError();
 }
 
@@ -805,10 +1018,14 @@ cudaError_t range_trace_leaves(cudaStream_t st, const uint32_t* lde, uint32_t* l
   return cudaGetLastError();
 }
 
-cudaError_t merkle_build(cudaStream_t st, uint32_t* tree, uint64_t leaves) {
+cudaError_t merkle_build(cudaStream_t st, uint32_t* tree, uint64_t leaves, uint32_t top,
+                         unsigned int* counter) {
   Stage stg("merkle_levels", st);
+  // Levels with more than 2^16 nodes fill the GPU on their own: one launch
+  // each. The rest (at most 2^16 nodes at l0, so at most 128 CTAs of 512
+  // children) go to one launch of merkle_top_kernel.
   uint32_t level = 0;
-  while ((leaves >> level) > 2048) {
+  while (level < top && (leaves >> level) > (1ull << 16)) {
     uint64_t cnt = leaves >> (level + 1);
     const uint32_t* prev = tree + 8 * (2 * leaves - 2 * (leaves >> level));
     uint32_t* next = tree + 8 * (2 * leaves - 2 * (leaves >> (level + 1)));
@@ -818,10 +1035,14 @@ cudaError_t merkle_build(cudaStream_t st, uint32_t* tree, uint64_t leaves) {
     if (e != cudaSuccess) return e;
     level++;
   }
-  if ((leaves >> level) > 1) {
-    stg.launched();
-    merkle_tail_kernel<<<1, 1024, 0, st>>>(tree, leaves, level);
-  }
+  if (level >= top) return cudaSuccess;
+  const uint32_t lsub = level + 9 < top ? level + 9 : top;
+  const uint64_t per_cta_children = 2ull << (lsub - level - 1);  // level-l0 nodes per CTA
+  const uint64_t blocks = ((leaves >> level) + per_cta_children - 1) / per_cta_children;
+  cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(unsigned int), st);
+  if (e != cudaSuccess) return e;
+  stg.launched();
+  merkle_top_kernel<<<(unsigned)blocks, kTopThreads, 0, st>>>(tree, leaves, level, top, counter);
   return cudaGetLastError();
 }
 

@@ -29,16 +29,20 @@ struct NttPlan {
   uint32_t post_gamma = 0;
 };
 
+// Column B of the Fibonacci trace is never transformed: on the LDE,
+// B(x) = A(omega_N x) + C_j / (x - w_last) with C_j constant on coset j
+// (src/air.rs:806-844, linked_lde), so kernels that need B derive it from A.
 struct AirComposeArgs {
   const uint32_t* lde_a;  // coset-major [j][q]
-  const uint32_t* lde_b;
+  const uint32_t* cb;     // per coset C_j (canonical)
   const uint32_t* zinv;   // per coset 1 / (x^N - 1) (Montgomery)
   uint32_t* layer0;       // FRI layer 0, bit-reversed Ext4 values
   uint32_t* leaves;       // layer-0 tree, leaf digests
   uint32_t logN, logB;
   uint32_t a0, b0, b_last;  // canonical
   uint32_t w_last_m;        // omega_N^(N-1) (Montgomery)
-  uint32_t alpha[5][4];     // Montgomery
+  uint32_t omega_n_m;       // omega_N (Montgomery): x of row k + B is x * omega_N
+  uint32_t alpha[4][5];     // alpha_k coordinate c at [c][k] (Montgomery)
 };
 
 struct RangeComposeArgs {
@@ -59,8 +63,13 @@ struct FoldArgs {
   uint32_t logn;
   uint32_t ginv_m;     // (31^(4^depth))^-1 (Montgomery)
   uint32_t unit_m;     // two_adic_generator(2) (Montgomery)
-  uint32_t ch[3][4];   // fold challenges (Montgomery)
+  // Product tables (e4_mul_tab) of r_k / 4 for the three fold challenges.
+  uint32_t tab[3][4][4];
 };
+
+// Product table of the Fp4 constant r (canonical coordinates) in the layout
+// e4_mul_tab expects, in Montgomery form.
+void e4_table(const uint32_t r[4], uint32_t T[4][4]);
 
 namespace launch {
 
@@ -81,15 +90,29 @@ cudaError_t fill_constant_columns(cudaStream_t st, uint32_t* cols, uint32_t n, u
                                   const uint32_t* h_values);
 cudaError_t ntt(cudaStream_t st, const Tables& tb, const NttPlan& plan, const uint32_t* in,
                 uint32_t* out, uint32_t* scratch);
+// Per coset j (x^N = 31^N omega_B^j): zinv = 1/(x^N - 1) (Montgomery),
+// zinv2 = zinv * 2^32, and, when cb is non-null, cb = coeff * (x^N - 1)
+// (canonical; coeff canonical), the linked-column constant.
 cudaError_t coset_zinv(cudaStream_t st, const Tables& tb, uint32_t* zinv, uint32_t* zinv2,
-                       uint32_t logB, uint32_t gamma_n_m);
-cudaError_t air_trace_leaves(cudaStream_t st, const uint32_t* lde_a, const uint32_t* lde_b,
-                             uint32_t* leaves, uint32_t logN, uint32_t logB);
+                       uint32_t logB, uint32_t gamma_n_m, uint32_t* cb, uint32_t coeff);
+// Trace leaves of the AIR: rows 8L..8L+7 as A || B with B derived from A.
+cudaError_t air_trace_leaves(cudaStream_t st, const Tables& tb, const uint32_t* lde_a,
+                             const uint32_t* cb, uint32_t w_last_m, uint32_t* leaves,
+                             uint32_t logN, uint32_t logB);
+// (A, B) of the AIR trace LDE at natural rows rows[0..n): out[2i], out[2i+1].
+cudaError_t air_rows(cudaStream_t st, const Tables& tb, const uint32_t* lde_a, const uint32_t* cb,
+                     uint32_t w_last_m, uint32_t logN, uint32_t logB, const uint32_t* rows,
+                     uint32_t n, uint32_t* out);
 cudaError_t range_trace_leaves(cudaStream_t st, const uint32_t* lde, uint32_t* leaves,
                                uint32_t logN, uint32_t logB, uint32_t ncols);
-// Builds every level above the leaves of a tree stored level-contiguous
-// (level l at digest offset 2L - 2(L >> l), L = leaves, power of two).
-cudaError_t merkle_build(cudaStream_t st, uint32_t* tree, uint64_t leaves);
+// Builds levels 1..top of a tree stored level-contiguous (level l at digest
+// offset 2L - 2(L >> l), L = leaves, power of two). Levels above the cap
+// level are never read (caps and capped paths stop there), so callers pass
+// top = depth - drop.
+// `counter` is one device word of scratch (the upper levels are finished by
+// the last CTA to arrive; nothing waits).
+cudaError_t merkle_build(cudaStream_t st, uint32_t* tree, uint64_t leaves, uint32_t top,
+                         unsigned int* counter);
 cudaError_t air_compose_leaves(cudaStream_t st, const Tables& tb, const AirComposeArgs& a);
 cudaError_t range_compose_leaves(cudaStream_t st, const Tables& tb, const RangeComposeArgs& a);
 // Folds one FRI layer; hashes the next layer's 64-byte leaves when it has a

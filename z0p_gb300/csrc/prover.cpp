@@ -12,6 +12,7 @@
 // The host holds the transcript; each bracket is one stream synchronisation.
 #include <cuda_runtime.h>
 
+#include <chrono>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -124,7 +125,7 @@ struct z0p_gpu_ctx {
   uint8_t* pinned = nullptr;
   size_t pinned_bytes = 0;
   size_t held = 0;
-  uint64_t h2d = 0, d2h = 0, syncs = 0, proofs = 0;
+  uint64_t h2d = 0, d2h = 0, syncs = 0, proofs = 0, sync_ns = 0, prove_ns = 0;
   bool profiling = false;
   EventRecorder rec;
 };
@@ -139,9 +140,17 @@ cudaError_t d2h(z0p_gpu_ctx* c, void* dst, const void* src, size_t n) {
   c->d2h += n;
   return cudaMemcpyAsync(dst, src, n, cudaMemcpyDeviceToHost, c->stream);
 }
+uint64_t now_ns() {
+  return (uint64_t)std::chrono::duration_cast<std::chrono::nanoseconds>(
+             std::chrono::steady_clock::now().time_since_epoch())
+      .count();
+}
 cudaError_t sync(z0p_gpu_ctx* c) {
   c->syncs++;
-  return cudaStreamSynchronize(c->stream);
+  uint64_t t0 = now_ns();
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  c->sync_ns += now_ns() - t0;
+  return e;
 }
 
 int ensure(z0p_gpu_ctx* c, DevBuf& b, size_t bytes) {
@@ -201,6 +210,12 @@ int build_tables(z0p_gpu_ctx* c) {
 }
 
 inline uint64_t tree_digests(uint64_t leaves) { return 2 * leaves - 1; }
+
+// Device word counting finished CTAs in the Merkle top-level kernel (bytes
+// 32..35 of the context's misc buffer; the PoW state uses bytes 0..23).
+inline unsigned int* sync_words(z0p_gpu_ctx* c) { return (unsigned int*)c->misc.p + 8; }
+
+
 inline uint64_t level_off(uint64_t leaves, uint32_t l) { return 2 * leaves - 2 * (leaves >> l); }
 
 // One FRI commitment + opening over layer 0 (already written with its leaf
@@ -238,6 +253,7 @@ int plan_fri_buffers(z0p_gpu_ctx* c, const FriShape& s, FriBufs* fb) {
   return Z0P_OK;
 }
 
+// Copies a tree's cap level to the host.
 int fetch_cap(z0p_gpu_ctx* c, const uint32_t* tree, uint64_t leaves, uint32_t drop,
               std::vector<uint8_t>* out) {
   uint32_t depth = log2u(leaves);
@@ -272,8 +288,12 @@ int run_fri(z0p_gpu_ctx* c, const FriShape& s, const FriParams& fp, const FriBuf
     FoldArgs fa;
     uint32_t ch[3][4];
     for (int k = 0; k < 3; k++) challenge_ext(ts, "fri-fold", ch[k]);
-    for (int k = 0; k < 3; k++)
-      for (int e = 0; e < 4; e++) fa.ch[k][e] = to_mont(ch[k][e]);
+    const uint32_t inv4 = finv(4);
+    for (int k = 0; k < 3; k++) {
+      uint32_t q[4];
+      for (int e = 0; e < 4; e++) q[e] = fmul(ch[k][e], inv4);
+      e4_table(q, fa.tab[k]);
+    }
     fa.in = fb.layer[l];
     fa.out = fb.layer[l + 1];
     fa.leaves = fb.tree[l + 1];
@@ -284,7 +304,8 @@ int run_fri(z0p_gpu_ctx* c, const FriShape& s, const FriParams& fp, const FriBuf
     fa.ginv_m = to_mont(finv(g));
     fa.unit_m = unit_m;
     CK(launch::fri_fold(c->stream, c->tb, fa));
-    if (s.leaves[l + 1] > 1) CK(launch::merkle_build(c->stream, fb.tree[l + 1], s.leaves[l + 1]));
+    CK(launch::merkle_build(c->stream, fb.tree[l + 1], s.leaves[l + 1], s.depth[l + 1] - s.drop[l + 1],
+                            sync_words(c)));
   }
   // Final layer in the clear (src/fri.rs:620-621).
   uint64_t fl = s.len.back();
@@ -349,26 +370,41 @@ void queue_fri_openings(const FriShape& s, const FriBufs& fb, const FriOut& fo, 
   }
 }
 
+// Fetches every queued granule/word in one round trip. With `rows`, a row
+// kernel also runs (rows in, 2 words per row out) and its output is appended
+// to out4 after the gathered words.
+template <typename RowFn>
 int run_gather(z0p_gpu_ctx* c, const Gather& g, std::vector<uint8_t>* out16,
-               std::vector<uint32_t>* out4) {
-  size_t n16 = g.a16.size(), n4 = g.a4.size();
-  RC(ensure(c, c->gaddr, 8 * (n16 + n4) + 16));
-  RC(ensure(c, c->gout, 16 * n16 + 4 * n4 + 16));
-  size_t addr_bytes = 8 * (n16 + n4), out_bytes = 16 * n16 + 4 * n4;
+               std::vector<uint32_t>* out4, const std::vector<uint32_t>* rows, RowFn row_fn) {
+  size_t n16 = g.a16.size(), n4 = g.a4.size(), nr = rows ? rows->size() : 0;
+  size_t addr_bytes = 8 * (n16 + n4) + 4 * nr;
+  size_t out_bytes = 16 * n16 + 4 * n4 + 8 * nr;
+  RC(ensure(c, c->gaddr, addr_bytes + 16));
+  RC(ensure(c, c->gout, out_bytes + 16));
   RC(ensure_pinned(c, addr_bytes > out_bytes ? addr_bytes : out_bytes));
   std::memcpy(c->pinned, g.a16.data(), 8 * n16);
   std::memcpy(c->pinned + 8 * n16, g.a4.data(), 8 * n4);
+  if (nr) std::memcpy(c->pinned + 8 * (n16 + n4), rows->data(), 4 * nr);
   CK(h2d(c, c->gaddr.p, c->pinned, addr_bytes));
   uint64_t* da = (uint64_t*)c->gaddr.p;
   uint8_t* dout = (uint8_t*)c->gout.p;
   CK(launch::gather16(c->stream, da, dout, (uint32_t)n16));
   CK(launch::gather4(c->stream, da + n16, (uint32_t*)(dout + 16 * n16), (uint32_t)n4));
+  if (nr)
+    CK(row_fn((const uint32_t*)(da + n16 + n4), (uint32_t)nr,
+              (uint32_t*)(dout + 16 * n16 + 4 * n4)));
   CK(d2h(c, c->pinned, dout, out_bytes));
   CK(sync(c));
   out16->assign(c->pinned, c->pinned + 16 * n16);
-  out4->resize(n4);
-  std::memcpy(out4->data(), c->pinned + 16 * n16, 4 * n4);
+  out4->resize(n4 + 2 * nr);
+  std::memcpy(out4->data(), c->pinned + 16 * n16, 4 * n4 + 8 * nr);
   return Z0P_OK;
+}
+
+int run_gather(z0p_gpu_ctx* c, const Gather& g, std::vector<uint8_t>* out16,
+               std::vector<uint32_t>* out4) {
+  return run_gather(c, g, out16, out4, nullptr,
+                    [](const uint32_t*, uint32_t, uint32_t*) { return cudaSuccess; });
 }
 
 void write_path(Writer& w, const uint8_t* digests, uint64_t leaf, uint32_t steps) {
@@ -467,10 +503,10 @@ int air_prove(z0p_gpu_ctx* c, const z0p_air_params& p, z0p_transcript_state* ts,
 
   RC(ensure(c, c->cols, 8 * N));
   RC(ensure(c, c->coeffs, 8 * N));
-  RC(ensure(c, c->scratch, 8 * m));
-  RC(ensure(c, c->lde, 8 * m));
+  RC(ensure(c, c->scratch, 4 * m));
+  RC(ensure(c, c->lde, 4 * m));
   RC(ensure(c, c->ttree, 32 * tree_digests(m / 8)));
-  RC(ensure(c, c->misc, 64 + 8 * B));
+  RC(ensure(c, c->misc, 64 + 12 * B));
   FriBufs fb;
   RC(plan_fri_buffers(c, s, &fb));
   uint32_t* cols = (uint32_t*)c->cols.p;
@@ -488,27 +524,49 @@ int air_prove(z0p_gpu_ctx* c, const z0p_air_params& p, z0p_transcript_state* ts,
   p32(32, p.grinding_bits); p64(36, p.cap_height); p32(44, p.a0); p32(48, p.b0); p32(52, p.b_last);
   transcript_absorb(ts, "fib/params", pb, 56);
 
-  // Trace, interpolation (times 31^i / N), coset LDE of both columns.
+  // Trace, interpolation of column A (times 31^i / N) and its coset LDE.
+  // Column B is derived from A wherever it is needed (linked_lde,
+  // src/air.rs:806-844): B(x) = A(omega_N x) + C_j / (x - w_last).
   uint32_t mats[32][4];
   fib_mats(mats);
   CK(launch::fib_trace(st, cols, cols + N, (uint32_t)N, p.a0, p.b0, mats));
   NttPlan ip;
-  ip.logn = logN; ip.batch = 2; ip.inverse = 1; ip.post_gamma = 1;
+  ip.logn = logN; ip.batch = 1; ip.inverse = 1; ip.post_gamma = 1;
   CK(launch::ntt(st, c->tb, ip, cols, coeffs, (uint32_t*)c->scratch.p));
   NttPlan lp;
-  lp.logn = logN; lp.batch = 2 * (uint32_t)B; lp.in_div = (uint32_t)B; lp.twist_mod = (uint32_t)B;
+  lp.logn = logN; lp.batch = (uint32_t)B; lp.in_div = (uint32_t)B; lp.twist_mod = (uint32_t)B;
   lp.twist_shift = 27 - logm;
   CK(launch::ntt(st, c->tb, lp, coeffs, lde, (uint32_t*)c->scratch.p));
   const uint32_t* lde_a = lde;
-  const uint32_t* lde_b = lde + m;
+
+  // C_j = coeff * (x^N - 1) with coeff = (B[N-1] - a0) w_last / N, where
+  // B[N-1] is the actual last trace value (src/air.rs:366-371, 817-821).
+  uint32_t omega_n = two_adic_generator(logN);
+  uint32_t w_last = fpow(omega_n, N - 1);
+  uint32_t b_actual = 0;
+  {
+    // (A[N-1], B[N-1]) = M^(N-1) (a0, b0) from the binary powers of M.
+    uint32_t r00 = 1, r01 = 0, r10 = 0, r11 = 1;
+    for (int k = 0; k < 32; k++)
+      if (((N - 1) >> k) & 1) {
+        const uint32_t* q = mats[k];
+        uint32_t n00 = fadd(fmul(r00, q[0]), fmul(r01, q[2])), n01 = fadd(fmul(r00, q[1]), fmul(r01, q[3]));
+        uint32_t n10 = fadd(fmul(r10, q[0]), fmul(r11, q[2])), n11 = fadd(fmul(r10, q[1]), fmul(r11, q[3]));
+        r00 = n00; r01 = n01; r10 = n10; r11 = n11;
+      }
+    b_actual = fadd(fmul(r10, p.a0), fmul(r11, p.b0));
+  }
+  uint32_t coeff = fmul(fmul(fsub(b_actual, p.a0), w_last), finv((uint32_t)(N % P)));
+  uint32_t* cb = zinv2 + B;
+  uint32_t gamma_n = fpow(GENERATOR, N);
+  CK(launch::coset_zinv(st, c->tb, zinv, zinv2, logB, to_mont(gamma_n), cb, coeff));
+  const uint32_t w_last_m = to_mont(w_last);
 
   // Joint trace tree over 8-row 64-byte leaves (src/air.rs:520-537).
   uint64_t tleaves = m / 8;
   uint32_t tdepth = log2u(tleaves), tdrop = p.cap_height < tdepth ? (uint32_t)p.cap_height : tdepth;
-  CK(launch::air_trace_leaves(st, lde_a, lde_b, ttree, logN, logB));
-  if (tleaves > 1) CK(launch::merkle_build(st, ttree, tleaves));
-  uint32_t gamma_n = fpow(GENERATOR, N);
-  CK(launch::coset_zinv(st, c->tb, zinv, zinv2, logB, to_mont(gamma_n)));
+  CK(launch::air_trace_leaves(st, c->tb, lde_a, cb, w_last_m, ttree, logN, logB));
+  CK(launch::merkle_build(st, ttree, tleaves, tdepth - tdrop, sync_words(c)));
   std::vector<uint8_t> column_cap;
   RC(fetch_cap(c, ttree, tleaves, tdrop, &column_cap));
   transcript_absorb(ts, "fib/trace", column_cap.data(), column_cap.size());
@@ -517,16 +575,16 @@ int air_prove(z0p_gpu_ctx* c, const z0p_air_params& p, z0p_transcript_state* ts,
 
   // Composition as bit-reversed FRI layer 0 with its leaves (src/air.rs:847-929).
   AirComposeArgs ca;
-  ca.lde_a = lde_a; ca.lde_b = lde_b; ca.zinv = zinv;
+  ca.lde_a = lde_a; ca.cb = cb; ca.zinv = zinv;
   ca.layer0 = fb.layer[0]; ca.leaves = fb.tree[0];
   ca.logN = logN; ca.logB = logB;
   ca.a0 = p.a0; ca.b0 = p.b0; ca.b_last = p.b_last;
-  uint32_t omega_n = two_adic_generator(logN);
-  ca.w_last_m = to_mont(fpow(omega_n, N - 1));
+  ca.w_last_m = w_last_m;
+  ca.omega_n_m = to_mont(omega_n);
   for (int k = 0; k < 5; k++)
-    for (int e = 0; e < 4; e++) ca.alpha[k][e] = to_mont(alpha[k][e]);
+    for (int e = 0; e < 4; e++) ca.alpha[e][k] = to_mont(alpha[k][e]);
   CK(launch::air_compose_leaves(st, c->tb, ca));
-  if (s.leaves[0] > 1) CK(launch::merkle_build(st, fb.tree[0], s.leaves[0]));
+  CK(launch::merkle_build(st, fb.tree[0], s.leaves[0], s.depth[0] - s.drop[0], sync_words(c)));
 
   FriOut fo;
   RC(run_fri(c, s, fp, fb, m, N - 1, ts, &fo, false));
@@ -535,19 +593,15 @@ int air_prove(z0p_gpu_ctx* c, const z0p_air_params& p, z0p_transcript_state* ts,
   Gather g;
   FriOpenRefs fr;
   queue_fri_openings(s, fb, fo, &g, &fr);
-  std::vector<size_t> trow, tpath;
+  std::vector<uint32_t> rows;  // 8 rows per opened trace leaf, (A, B) computed on the device
+  std::vector<size_t> tpath;
   uint32_t tsteps = tdepth - tdrop;
   for (uint64_t leaf : fo.indices) {
     uint64_t index = brev(leaf, logm);
     uint64_t shifted = (index + B) % m;
     for (uint64_t at : {index, shifted}) {
       uint64_t base = at & ~7ull;
-      trow.push_back(g.a4.size());
-      for (uint64_t r = 0; r < 8; r++) {
-        uint64_t k = base + r, j = k & (B - 1), q = k >> logB;
-        g.add4(lde_a + j * N + q);
-        g.add4(lde_b + j * N + q);
-      }
+      for (uint64_t r = 0; r < 8; r++) rows.push_back((uint32_t)(base + r));
       tpath.push_back(g.a16.size());
       uint64_t L = base / 8;
       for (uint32_t sx = 0; sx < tsteps; sx++)
@@ -556,7 +610,11 @@ int air_prove(z0p_gpu_ctx* c, const z0p_air_params& p, z0p_transcript_state* ts,
   }
   std::vector<uint8_t> g16;
   std::vector<uint32_t> g4;
-  RC(run_gather(c, g, &g16, &g4));
+  RC(run_gather(c, g, &g16, &g4, &rows, [&](const uint32_t* d_rows, uint32_t n, uint32_t* d_out) {
+    return launch::air_rows(st, c->tb, lde_a, cb, w_last_m, logN, logB, d_rows, n, d_out);
+  }));
+  std::vector<size_t> trow;
+  for (size_t i = 0; i < 2 * fo.indices.size(); i++) trow.push_back(g.a4.size() + 16 * i);
 
   Writer w;  // air::Proof::to_bytes (src/air.rs:262-281)
   w.b.reserve(need);
@@ -645,8 +703,8 @@ int range_prove(z0p_gpu_ctx* c, const z0p_range_params& p, z0p_transcript_state*
   CK(launch::ntt(st, c->tb, lp, coeffs, lde, (uint32_t*)c->scratch.p));
   uint32_t tdepth = logm, tdrop = p.cap_height < tdepth ? (uint32_t)p.cap_height : tdepth;
   CK(launch::range_trace_leaves(st, lde, ttree, logN, logB, (uint32_t)ncol));
-  if (m > 1) CK(launch::merkle_build(st, ttree, m));
-  CK(launch::coset_zinv(st, c->tb, zinv, zinv2, logB, to_mont(fpow(GENERATOR, N))));
+  CK(launch::merkle_build(st, ttree, m, tdepth - tdrop, sync_words(c)));
+  CK(launch::coset_zinv(st, c->tb, zinv, zinv2, logB, to_mont(fpow(GENERATOR, N)), nullptr, 0));
   std::vector<uint8_t> column_cap;
   RC(fetch_cap(c, ttree, m, tdrop, &column_cap));
   transcript_absorb(ts, "range/column", column_cap.data(), column_cap.size());
@@ -665,7 +723,7 @@ int range_prove(z0p_gpu_ctx* c, const z0p_range_params& p, z0p_transcript_state*
   ca.layer0 = fb.layer[0]; ca.leaves = fb.tree[0];
   ca.logN = logN; ca.logB = logB; ca.n_bits = (uint32_t)p.n_bits; ca.value = p.value;
   CK(launch::range_compose_leaves(st, c->tb, ca));
-  if (s.leaves[0] > 1) CK(launch::merkle_build(st, fb.tree[0], s.leaves[0]));
+  CK(launch::merkle_build(st, fb.tree[0], s.leaves[0], s.depth[0] - s.drop[0], sync_words(c)));
 
   FriOut fo;
   RC(run_fri(c, s, fp, fb, m, N - 1, ts, &fo, false));
@@ -837,7 +895,7 @@ int z0p_gpu_air_footprint(const z0p_air_params* p, size_t* bytes) {
   FriParams fp;
   FriShape s;
   RC(air_shape(*p, &fp, &s));
-  uint64_t N = p->n_steps, m = s.m, total = 16 * N + 16 * m + 32 * tree_digests(m / 8);
+  uint64_t N = p->n_steps, m = s.m, total = 16 * N + 8 * m + 32 * tree_digests(m / 8);
   for (size_t i = 0; i < s.len.size(); i++) total += 16 * s.len[i] + 32 * tree_digests(s.leaves[i]);
   *bytes = total;
   return Z0P_OK;
@@ -912,8 +970,10 @@ int z0p_gpu_air_prove(z0p_gpu_ctx* c, const z0p_air_params* p, z0p_transcript_st
   std::lock_guard<std::mutex> lk(c->mu);
   RC(with_device(c));
   ProfileScope ps(c);
+  uint64_t t0 = now_ns();
   z0p_transcript_state work = *ts;
   int rc = air_prove(c, *p, &work, out, cap, len);
+  c->prove_ns += now_ns() - t0;
   if (rc == Z0P_OK) {
     *ts = work;
     c->proofs++;
@@ -924,7 +984,8 @@ int z0p_gpu_air_prove(z0p_gpu_ctx* c, const z0p_air_params* p, z0p_transcript_st
 int z0p_gpu_ctx_stats(z0p_gpu_ctx* c, z0p_gpu_stats* out) {
   if (!c || !out) return Z0P_ERR_INVALID_ARGUMENT;
   std::lock_guard<std::mutex> lk(c->mu);
-  *out = z0p_gpu_stats{launch::launch_count(), c->h2d, c->d2h, c->syncs, c->proofs};
+  *out = z0p_gpu_stats{launch::launch_count(), c->h2d, c->d2h, c->syncs, c->proofs, c->sync_ns,
+                       c->prove_ns};
   return Z0P_OK;
 }
 
@@ -975,8 +1036,10 @@ int z0p_gpu_range_prove(z0p_gpu_ctx* c, const z0p_range_params* p, z0p_transcrip
   std::lock_guard<std::mutex> lk(c->mu);
   RC(with_device(c));
   ProfileScope ps(c);
+  uint64_t t0 = now_ns();
   z0p_transcript_state work = *ts;
   int rc = range_prove(c, *p, &work, out, cap, len);
+  c->prove_ns += now_ns() - t0;
   if (rc == Z0P_OK) {
     *ts = work;
     c->proofs++;
@@ -1024,11 +1087,12 @@ int z0p_gpu_merkle_flat64_cap(z0p_gpu_ctx* c, const uint8_t* d_flat, uint64_t le
   }
   std::lock_guard<std::mutex> lk(c->mu);
   RC(with_device(c));
+  RC(ensure(c, c->misc, 64));
   RC(ensure(c, c->ttree, 32 * tree_digests(leaves)));
   uint32_t* tree = (uint32_t*)c->ttree.p;
   CK(launch::merkle_flat64_leaves(c->stream, (const uint32_t*)d_flat, leaves, tree));
-  if (leaves > 1) CK(launch::merkle_build(c->stream, tree, leaves));
   uint32_t depth = log2u(leaves), drop = cap_height < depth ? (uint32_t)cap_height : depth;
+  CK(launch::merkle_build(c->stream, tree, leaves, depth - drop, sync_words(c)));
   std::vector<uint8_t> cap;
   RC(fetch_cap(c, tree, leaves, drop, &cap));
   std::memcpy(h_cap, cap.data(), cap.size());
@@ -1054,8 +1118,12 @@ int z0p_gpu_fri_fold(z0p_gpu_ctx* c, const uint32_t* d_in, uint64_t n, uint64_t 
   for (uint64_t i = 0; i < depth; i++) g = fpow(g, 4);
   fa.ginv_m = to_mont(finv(g));
   fa.unit_m = to_mont(two_adic_generator(2));
-  for (int k = 0; k < 3; k++)
-    for (int e = 0; e < 4; e++) fa.ch[k][e] = to_mont(ch[4 * k + e] % P);
+  const uint32_t inv4 = finv(4);
+  for (int k = 0; k < 3; k++) {
+    uint32_t q[4];
+    for (int e = 0; e < 4; e++) q[e] = fmul(ch[4 * k + e] % P, inv4);
+    e4_table(q, fa.tab[k]);
+  }
   CK(launch::fri_fold(c->stream, c->tb, fa));
   CK(sync(c));
   return Z0P_OK;
