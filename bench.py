@@ -416,6 +416,15 @@ def run_gpu(args):
 
     peak, peak_kind = measured_peaks()
     work = stage_work(N_STEPS, params)
+    host = prof.pop("host", {})
+    host_sites = {}
+    for name, v in host.items():
+        if "calls" in v:
+            host_sites[name] = {"calls_per_proof": v["calls"] / prof_steps,
+                                "blocked_ms": round(v["wait_ms"] / prof_steps, 4),
+                                "host_before_ms": round(v["before_ms"] / prof_steps, 4)}
+        else:
+            host_sites[name] = {"host_ms": round(v["ms"] / prof_steps, 4)}
     stages = {}
     for name, v in prof.items():
         per = v["ms"] / prof_steps
@@ -459,7 +468,8 @@ def run_gpu(args):
         "host_syncs_per_step": (st1["syncs"] - st0["syncs"]) / args.steps,
         "host_ms_per_step": {
             "prove_wall": (st1["prove_ns"] - st0["prove_ns"]) / 1e6 / args.steps,
-            "blocked_in_sync": (st1["sync_wait_ns"] - st0["sync_wait_ns"]) / 1e6 / args.steps},
+            "blocked_in_sync": (st1["sync_wait_ns"] - st0["sync_wait_ns"]) / 1e6 / args.steps,
+            "by_sync_site": host_sites},
         "clocks": clocks,
         "roofline": roof,
         "stages": stages,

@@ -51,57 +51,50 @@ static inline void put64(uint8_t* p, uint64_t v) {
   for (int i = 0; i < 8; i++) p[i] = (uint8_t)(v >> (8 * i));
 }
 
-static inline void gmix(uint32_t s[16], int a, int b, int c, int d, uint32_t x, uint32_t y) {
-  s[a] += s[b] + x; s[d] = rotr(s[d] ^ s[a], 16);
-  s[c] += s[d];     s[b] = rotr(s[b] ^ s[c], 12);
-  s[a] += s[b] + y; s[d] = rotr(s[d] ^ s[a], 8);
-  s[c] += s[d];     s[b] = rotr(s[b] ^ s[c], 7);
-}
+#define Z0P_HG(a, b, c, d, x, y)  \
+  do {                            \
+    a = a + b + (x);              \
+    d = rotr(d ^ a, 16);          \
+    c = c + d;                    \
+    b = rotr(b ^ c, 12);          \
+    a = a + b + (y);              \
+    d = rotr(d ^ a, 8);           \
+    c = c + d;                    \
+    b = rotr(b ^ c, 7);           \
+  } while (0)
 
 // BLAKE3 compression (specification; src/hash.rs:93-133). Returns the
-// chaining value (first 8 output words).
+// chaining value (first 8 output words). The state lives in locals so the
+// compiler keeps it in registers; the message schedule is applied by index.
 static void compress_cv(const uint32_t cv[8], const uint32_t block[16], uint64_t counter,
                         uint32_t len, uint32_t flags, uint32_t out[8]) {
-  uint32_t s[16], m[16], t[16];
-  std::memcpy(s, cv, 32);
-  std::memcpy(s + 8, IV, 16);
-  s[12] = (uint32_t)counter; s[13] = (uint32_t)(counter >> 32); s[14] = len; s[15] = flags;
+  uint32_t s0 = cv[0], s1 = cv[1], s2 = cv[2], s3 = cv[3];
+  uint32_t s4 = cv[4], s5 = cv[5], s6 = cv[6], s7 = cv[7];
+  uint32_t s8 = IV[0], s9 = IV[1], s10 = IV[2], s11 = IV[3];
+  uint32_t s12 = (uint32_t)counter, s13 = (uint32_t)(counter >> 32), s14 = len, s15 = flags;
+  uint32_t m[16], t[16];
   std::memcpy(m, block, 64);
   for (int r = 0; r < 7; r++) {
-    gmix(s, 0, 4, 8, 12, m[0], m[1]);
-    gmix(s, 1, 5, 9, 13, m[2], m[3]);
-    gmix(s, 2, 6, 10, 14, m[4], m[5]);
-    gmix(s, 3, 7, 11, 15, m[6], m[7]);
-    gmix(s, 0, 5, 10, 15, m[8], m[9]);
-    gmix(s, 1, 6, 11, 12, m[10], m[11]);
-    gmix(s, 2, 7, 8, 13, m[12], m[13]);
-    gmix(s, 3, 4, 9, 14, m[14], m[15]);
+    Z0P_HG(s0, s4, s8, s12, m[0], m[1]);
+    Z0P_HG(s1, s5, s9, s13, m[2], m[3]);
+    Z0P_HG(s2, s6, s10, s14, m[4], m[5]);
+    Z0P_HG(s3, s7, s11, s15, m[6], m[7]);
+    Z0P_HG(s0, s5, s10, s15, m[8], m[9]);
+    Z0P_HG(s1, s6, s11, s12, m[10], m[11]);
+    Z0P_HG(s2, s7, s8, s13, m[12], m[13]);
+    Z0P_HG(s3, s4, s9, s14, m[14], m[15]);
     for (int i = 0; i < 16; i++) t[i] = m[MSG_PERM[i]];
     std::memcpy(m, t, 64);
   }
-  for (int i = 0; i < 8; i++) out[i] = s[i] ^ s[i + 8];
+  out[0] = s0 ^ s8; out[1] = s1 ^ s9; out[2] = s2 ^ s10; out[3] = s3 ^ s11;
+  out[4] = s4 ^ s12; out[5] = s5 ^ s13; out[6] = s6 ^ s14; out[7] = s7 ^ s15;
 }
+#undef Z0P_HG
 
 static void block_words(const uint8_t* p, size_t len, uint32_t w[16]) {
   uint8_t b[64] = {0};
   std::memcpy(b, p, len);
   for (int i = 0; i < 16; i++) w[i] = le32(b + 4 * i);
-}
-
-// Output of one chunk of 1..1024 bytes (src/hash.rs:186-225).
-static void chunk_output(const uint8_t* data, size_t len, uint64_t counter, bool root,
-                         uint8_t out[32]) {
-  uint32_t cv[8], w[16];
-  std::memcpy(cv, IV, 32);
-  size_t blocks = (len + 63) / 64;
-  for (size_t i = 0; i < blocks; i++) {
-    size_t bl = i + 1 == blocks ? len - 64 * i : 64;
-    block_words(data + 64 * i, bl, w);
-    uint32_t flags = (i == 0 ? (uint32_t)CHUNK_START : 0u) |
-                     (i + 1 == blocks ? ((uint32_t)CHUNK_END | (root ? (uint32_t)ROOT : 0u)) : 0u);
-    compress_cv(cv, w, counter, (uint32_t)bl, flags, cv);
-  }
-  for (int i = 0; i < 8; i++) put32(out + 4 * i, cv[i]);
 }
 
 static void parent(const uint8_t l[32], const uint8_t r[32], uint32_t flags, uint8_t out[32]) {
@@ -128,10 +121,42 @@ static void push_merged(z0p_transcript_state* st, const uint8_t cv[32]) {
   }
 }
 
+// Block i of a chunk whose first `len` bytes are at p, zero-padded.
+static void chunk_block(const uint8_t* p, size_t len, uint32_t i, uint32_t w[16]) {
+  size_t off = 64 * (size_t)i;
+  block_words(p + off, len - off < 64 ? len - off : 64, w);
+}
+
+Hasher::Hasher(z0p_transcript_state* s) : st(s) {
+  for (int h = 0; h < 2; h++) {
+    std::memcpy(cv[h], IV, 32);
+    nblk[h] = 0;
+  }
+  advance();
+}
+
+// Folds into cv[h] every block of tail chunk h that has at least one byte
+// after it inside the chunk: such a block is never its chunk's last block, so
+// its compression (flags CHUNK_START or none, counter = chunk index) is final.
+void Hasher::advance() {
+  for (uint32_t h = 0; h < 2; h++) {
+    size_t base = CHUNK_LEN * h;
+    if (st->tail_len <= base) break;
+    size_t len = st->tail_len - base < CHUNK_LEN ? st->tail_len - base : CHUNK_LEN;
+    while (64 * ((size_t)nblk[h] + 1) < len) {
+      uint32_t w[16];
+      chunk_block(st->tail + base, len, nblk[h], w);
+      compress_cv(cv[h], w, st->next_index + h, 64, nblk[h] == 0 ? (uint32_t)CHUNK_START : 0u,
+                  cv[h]);
+      nblk[h]++;
+    }
+  }
+}
+
 // Hasher::update (src/hash.rs:256-272). The tail never reaches 2048 bytes
 // between calls: whenever it does, its first chunk is known not to be the
 // last one and is compressed, exactly as the reference's loop does.
-void hasher_update(z0p_transcript_state* st, const uint8_t* data, size_t len) {
+void Hasher::update(const uint8_t* data, size_t len) {
   st->total_len += len;
   while (len) {
     size_t room = 2 * CHUNK_LEN - st->tail_len;
@@ -140,105 +165,133 @@ void hasher_update(z0p_transcript_state* st, const uint8_t* data, size_t len) {
     st->tail_len += (uint32_t)take;
     data += take;
     len -= take;
+    advance();
     if (st->tail_len == 2 * CHUNK_LEN) {
-      uint8_t cv[32];
-      chunk_output(st->tail, CHUNK_LEN, st->next_index, false, cv);
-      push_merged(st, cv);
+      // Blocks 0..14 of the first chunk are folded; its last block ends it.
+      uint32_t w[16], out[8];
+      chunk_block(st->tail, CHUNK_LEN, 15, w);
+      compress_cv(cv[0], w, st->next_index, 64, CHUNK_END, out);
+      uint8_t cvb[32];
+      for (int i = 0; i < 8; i++) put32(cvb + 4 * i, out[i]);
+      push_merged(st, cvb);
       std::memmove(st->tail, st->tail + CHUNK_LEN, CHUNK_LEN);
       st->tail_len = CHUNK_LEN;
+      std::memcpy(cv[0], cv[1], 32);
+      nblk[0] = nblk[1];
+      std::memcpy(cv[1], IV, 32);
+      nblk[1] = 0;
     }
   }
 }
 
-// Hasher::finalize (src/hash.rs:276-302) on a copy of the state.
-void hasher_finalize(const z0p_transcript_state* src, uint8_t out[32]) {
-  if (src->total_len == 0) {
-    uint32_t w[16] = {0}, cv[8];
-    compress_cv(IV, w, 0, 0, CHUNK_START | CHUNK_END | ROOT, cv);
-    for (int i = 0; i < 8; i++) put32(out + 4 * i, cv[i]);
+// Hasher::finalize (src/hash.rs:276-302) without touching the state: the
+// first chunk's output, when the tail holds two, is merged into a virtual
+// copy of the stack top; the last chunk needs only its last block.
+void Hasher::finalize(uint8_t out[32]) const {
+  if (st->total_len == 0) {
+    uint32_t w[16] = {0}, o[8];
+    compress_cv(IV, w, 0, 0, CHUNK_START | CHUNK_END | ROOT, o);
+    for (int i = 0; i < 8; i++) put32(out + 4 * i, o[i]);
     return;
   }
-  z0p_transcript_state st = *src;
-  const uint8_t* tail = st.tail;
-  size_t tl = st.tail_len;
+  size_t tl = st->tail_len;
+  uint32_t sl = st->stack_len;
+  uint8_t top[32];
+  bool have_top = false;  // virtual stack = stack[0..sl) (+ top)
+  uint32_t h = 0;
   if (tl > CHUNK_LEN) {
-    uint8_t cv[32];
-    chunk_output(tail, CHUNK_LEN, st.next_index, false, cv);
-    push_merged(&st, cv);
-    tail += CHUNK_LEN;
-    tl -= CHUNK_LEN;
+    uint32_t w[16], o[8];
+    chunk_block(st->tail, CHUNK_LEN, 15, w);
+    compress_cv(cv[0], w, st->next_index, 64, CHUNK_END, o);
+    for (int i = 0; i < 8; i++) put32(top + 4 * i, o[i]);
+    uint64_t total = st->next_index + 1;  // push_merged on the virtual stack
+    while (total % 2 == 0) {
+      parent(st->stack[sl - 1], top, PARENT, top);
+      sl--;
+      total /= 2;
+    }
+    have_top = true;
+    h = 1;
   }
-  if (st.stack_len == 0) {
-    chunk_output(tail, tl, st.next_index, true, out);
+  const uint8_t* chunk = st->tail + CHUNK_LEN * h;
+  size_t len = tl - CHUNK_LEN * h;
+  uint32_t last = (uint32_t)((len + 63) / 64) - 1;  // == nblk[h]
+  size_t depth = sl + (have_top ? 1 : 0);
+  uint32_t w[16], o[8];
+  chunk_block(chunk, len, last, w);
+  uint32_t flags = (last == 0 ? (uint32_t)CHUNK_START : 0u) | CHUNK_END | (depth == 0 ? ROOT : 0u);
+  compress_cv(cv[h], w, st->next_index + h, (uint32_t)(len - 64 * (size_t)last), flags, o);
+  uint8_t cur[32];
+  for (int i = 0; i < 8; i++) put32(cur + 4 * i, o[i]);
+  if (depth == 0) {
+    std::memcpy(out, cur, 32);
     return;
   }
-  uint8_t cur[32];
-  chunk_output(tail, tl, st.next_index, false, cur);
-  for (uint32_t i = st.stack_len - 1; i >= 1; i--) {
-    uint8_t nx[32];
-    parent(st.stack[i], cur, PARENT, nx);
-    std::memcpy(cur, nx, 32);
-  }
-  parent(st.stack[0], cur, PARENT | ROOT, out);
+  auto entry = [&](size_t i) -> const uint8_t* { return i < sl ? st->stack[i] : top; };
+  for (size_t i = depth - 1; i >= 1; i--) parent(entry(i), cur, PARENT, cur);
+  parent(entry(0), cur, PARENT | ROOT, out);
 }
 
 void blake3(const uint8_t* data, size_t len, uint8_t out[32]) {
   z0p_transcript_state st;
   std::memset(&st, 0, sizeof st);
-  hasher_update(&st, data, len);
-  hasher_finalize(&st, out);
+  Hasher hs(&st);
+  hs.update(data, len);
+  hs.finalize(out);
 }
 
 // ------------------------------------------------------------- transcript ----
-void transcript_absorb_raw(z0p_transcript_state* st, const uint8_t* label, size_t llen,
-                           const uint8_t* data, size_t len) {  // src/transcript.rs:72-77
+void Transcript::absorb_raw(const uint8_t* label, size_t llen, const uint8_t* data,
+                            size_t len) {  // src/transcript.rs:72-77
   uint8_t b[8];
   put64(b, llen);
-  hasher_update(st, b, 8);
-  hasher_update(st, label, llen);
+  h_.update(b, 8);
+  h_.update(label, llen);
   put64(b, len);
-  hasher_update(st, b, 8);
-  hasher_update(st, data, len);
+  h_.update(b, 8);
+  h_.update(data, len);
 }
-void transcript_absorb(z0p_transcript_state* st, const char* label, const uint8_t* data,
-                       size_t len) {
-  transcript_absorb_raw(st, (const uint8_t*)label, std::strlen(label), data, len);
+void Transcript::absorb(const char* label, const uint8_t* data, size_t len) {
+  absorb_raw((const uint8_t*)label, std::strlen(label), data, len);
 }
-void transcript_init(z0p_transcript_state* st, const uint8_t* label, size_t len) {
-  std::memset(st, 0, sizeof *st);  // src/transcript.rs:62-69
-  transcript_absorb(st, "domain", label, len);
-}
-void squeeze_raw(z0p_transcript_state* st, const uint8_t* label, size_t llen, uint8_t out[32]) {
-  z0p_transcript_state h = *st;  // src/transcript.rs:162-171
+void Transcript::squeeze(const uint8_t* label, size_t llen, uint8_t out[32]) {
+  z0p_transcript_state copy = *h_.st;  // src/transcript.rs:162-171
+  Hasher hc = h_;
+  hc.st = &copy;
   uint8_t b[8];
   put64(b, llen);
-  hasher_update(&h, b, 8);
-  hasher_update(&h, label, llen);
-  put64(b, st->counter);
-  hasher_update(&h, b, 8);
-  st->counter++;
-  hasher_finalize(&h, out);
-  transcript_absorb_raw(st, label, llen, out, 32);
+  hc.update(b, 8);
+  hc.update(label, llen);
+  put64(b, h_.st->counter);
+  hc.update(b, 8);
+  h_.st->counter++;
+  hc.finalize(out);
+  absorb_raw(label, llen, out, 32);
 }
-void challenge_ext(z0p_transcript_state* st, const char* label, uint32_t out[4]) {
+void Transcript::challenge_ext(const char* label, uint32_t out[4]) {
   uint8_t b[32];  // src/transcript.rs:136-141, src/ext4.rs:179-187
-  squeeze_raw(st, (const uint8_t*)label, std::strlen(label), b);
+  squeeze((const uint8_t*)label, std::strlen(label), b);
   for (int i = 0; i < 4; i++) out[i] = le32(b + 4 * i) % P;
 }
-uint64_t challenge_index(z0p_transcript_state* st, const char* label, uint64_t domain) {
+uint64_t Transcript::challenge_index(const char* label, uint64_t domain) {
   uint8_t b[32];  // src/transcript.rs:148-160 (domain checked by the caller)
-  squeeze_raw(st, (const uint8_t*)label, std::strlen(label), b);
+  squeeze((const uint8_t*)label, std::strlen(label), b);
   uint64_t v = 0;
   for (int i = 0; i < 8; i++) v |= (uint64_t)b[i] << (8 * i);
   return v & (domain - 1);
 }
-std::vector<uint8_t> pow_head(const z0p_transcript_state* st, const char* label) {
-  size_t ll = std::strlen(label);
+std::vector<uint8_t> Transcript::pow_head(const char* label) const {
+  size_t ll = std::strlen(label);  // src/transcript.rs:182-189
   std::vector<uint8_t> head(40 + ll);
-  hasher_finalize(st, head.data());
+  h_.finalize(head.data());
   put64(head.data() + 32, ll);
   std::memcpy(head.data() + 40, label, ll);
   return head;
+}
+
+void transcript_init(z0p_transcript_state* st, const uint8_t* label, size_t len) {
+  std::memset(st, 0, sizeof *st);  // src/transcript.rs:62-69
+  Transcript(st).absorb("domain", label, len);
 }
 
 // ----------------------------------------------------------------- params ----

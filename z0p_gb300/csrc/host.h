@@ -28,22 +28,55 @@ inline uint32_t log2u(uint64_t x) { return (uint32_t)__builtin_ctzll(x); }
 uint32_t two_adic_generator(uint32_t bits);  // bits <= 27
 uint64_t brev(uint64_t x, uint32_t bits);
 
-// BLAKE3 (unkeyed, 32-byte output) and the streaming hasher semantics of
-// src/hash.rs:233-324 over the C-ABI transcript state.
+// BLAKE3 (unkeyed, 32-byte output).
 void blake3(const uint8_t* data, size_t len, uint8_t out[32]);
-void hasher_update(z0p_transcript_state* st, const uint8_t* data, size_t len);
-void hasher_finalize(const z0p_transcript_state* st, uint8_t out[32]);
+
+// Streaming BLAKE3 hasher of src/hash.rs:233-324 over the C-ABI state. The
+// state bytes evolve exactly as the reference's do; beside them, cv[h] holds
+// tail chunk h (tail bytes 1024h..) after its first nblk[h] blocks — every
+// block known not to be its chunk's last — so finalize compresses only the
+// last block of each open chunk instead of re-hashing the whole tail.
+struct Hasher {
+  z0p_transcript_state* st;
+  uint32_t cv[2][8];
+  uint32_t nblk[2];
+  explicit Hasher(z0p_transcript_state* s);  // builds the cache from the state
+  void update(const uint8_t* data, size_t len);
+  void finalize(uint8_t out[32]) const;
+
+ private:
+  void advance();
+};
+
+// Fiat-Shamir transcript (src/transcript.rs:54-189) over the C-ABI state.
+class Transcript {
+ public:
+  explicit Transcript(z0p_transcript_state* st) : h_(st) {}
+  void absorb_raw(const uint8_t* label, size_t llen, const uint8_t* data, size_t len);
+  void absorb(const char* label, const uint8_t* data, size_t len);
+  void squeeze(const uint8_t* label, size_t llen, uint8_t out[32]);
+  void challenge_ext(const char* label, uint32_t out[4]);
+  uint64_t challenge_index(const char* label, uint64_t domain);
+  // pow_head (src/transcript.rs:182-189): H(history) || LE64(|label|) || label.
+  std::vector<uint8_t> pow_head(const char* label) const;
+
+ private:
+  Hasher h_;
+};
 
 void transcript_init(z0p_transcript_state* st, const uint8_t* label, size_t len);
-void transcript_absorb(z0p_transcript_state* st, const char* label, const uint8_t* data,
-                       size_t len);
-void transcript_absorb_raw(z0p_transcript_state* st, const uint8_t* label, size_t llen,
-                           const uint8_t* data, size_t len);
-void squeeze_raw(z0p_transcript_state* st, const uint8_t* label, size_t llen, uint8_t out[32]);
-void challenge_ext(z0p_transcript_state* st, const char* label, uint32_t out[4]);
-uint64_t challenge_index(z0p_transcript_state* st, const char* label, uint64_t domain);
-// pow_head (src/transcript.rs:182-189): H(history) || LE64(|label|) || label.
-std::vector<uint8_t> pow_head(const z0p_transcript_state* st, const char* label);
+inline void transcript_absorb(Transcript& t, const char* label, const uint8_t* data, size_t len) {
+  t.absorb(label, data, len);
+}
+inline void challenge_ext(Transcript& t, const char* label, uint32_t out[4]) {
+  t.challenge_ext(label, out);
+}
+inline uint64_t challenge_index(Transcript& t, const char* label, uint64_t domain) {
+  return t.challenge_index(label, domain);
+}
+inline std::vector<uint8_t> pow_head(const Transcript& t, const char* label) {
+  return t.pow_head(label);
+}
 
 // FRI parameter rules (src/fri.rs:105-196) and tuners (src/fri.rs:945-1074).
 struct FriParams {

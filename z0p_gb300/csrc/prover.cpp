@@ -13,6 +13,7 @@
 #include <cuda_runtime.h>
 
 #include <chrono>
+#include <map>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -54,13 +55,29 @@ struct DevBuf {
   size_t bytes = 0;
 };
 
-// Little-endian byte writer (src/codec.rs:38-114).
+// Little-endian byte writer (src/codec.rs:38-114) straight into the caller's
+// buffer; the proof length is known from its shape before the first byte.
 struct Writer {
-  std::vector<uint8_t> b;
-  void byte(uint8_t v) { b.push_back(v); }
-  void u32(uint32_t v) { for (int i = 0; i < 4; i++) b.push_back((uint8_t)(v >> (8 * i))); }
-  void u64(uint64_t v) { for (int i = 0; i < 8; i++) b.push_back((uint8_t)(v >> (8 * i))); }
-  void bytes(const void* p, size_t n) { b.insert(b.end(), (const uint8_t*)p, (const uint8_t*)p + n); }
+  uint8_t* p;
+  size_t n = 0, cap;
+  Writer(uint8_t* out, size_t c) : p(out), cap(c) {}
+  bool ok() const { return n <= cap; }
+  void byte(uint8_t v) {
+    if (n < cap) p[n] = v;
+    n++;
+  }
+  void u32(uint32_t v) {
+    if (n + 4 <= cap) for (int i = 0; i < 4; i++) p[n + i] = (uint8_t)(v >> (8 * i));
+    n += 4;
+  }
+  void u64(uint64_t v) {
+    if (n + 8 <= cap) for (int i = 0; i < 8; i++) p[n + i] = (uint8_t)(v >> (8 * i));
+    n += 8;
+  }
+  void bytes(const void* src, size_t k) {
+    if (n + k <= cap) std::memcpy(p + n, src, k);
+    n += k;
+  }
 };
 
 // Host-built list of device addresses to fetch in one gather.
@@ -128,7 +145,14 @@ struct z0p_gpu_ctx {
   uint64_t h2d = 0, d2h = 0, syncs = 0, proofs = 0, sync_ns = 0, prove_ns = 0;
   bool profiling = false;
   EventRecorder rec;
+  struct HostSite {
+    uint64_t calls = 0, wait_ns = 0, before_ns = 0;
+  };
+  std::map<std::string, HostSite> sites;
+  uint64_t last_sync_ns = 0;  // 0 = no prove call in progress
+  uint64_t tail_ns = 0;       // host time after a prove call's last synchronisation
 };
+using HostSite = z0p_gpu_ctx::HostSite;
 
 namespace {
 
@@ -145,11 +169,23 @@ uint64_t now_ns() {
              std::chrono::steady_clock::now().time_since_epoch())
       .count();
 }
-cudaError_t sync(z0p_gpu_ctx* c) {
+// Every stream synchronisation of a prove call goes through here. With
+// profiling on, it also records, per call site, the time blocked and the host
+// time since the previous synchronisation returned (the GPU is idle for part
+// of the latter, from the moment its queue drains until the next launch).
+cudaError_t sync(z0p_gpu_ctx* c, const char* site = "other") {
   c->syncs++;
   uint64_t t0 = now_ns();
   cudaError_t e = cudaStreamSynchronize(c->stream);
-  c->sync_ns += now_ns() - t0;
+  uint64_t t1 = now_ns();
+  c->sync_ns += t1 - t0;
+  if (c->profiling) {
+    HostSite& h = c->sites[site];
+    h.calls++;
+    h.wait_ns += t1 - t0;
+    if (c->last_sync_ns) h.before_ns += t0 - c->last_sync_ns;
+  }
+  c->last_sync_ns = t1;
   return e;
 }
 
@@ -261,13 +297,13 @@ int fetch_cap(z0p_gpu_ctx* c, const uint32_t* tree, uint64_t leaves, uint32_t dr
   out->resize(32 * n);
   RC(ensure_pinned(c, 32 * n));
   CK(d2h(c, c->pinned, tree + 8 * level_off(leaves, depth - drop), 32 * n));
-  CK(sync(c));
+  CK(sync(c, "cap"));
   std::memcpy(out->data(), c->pinned, 32 * n);
   return Z0P_OK;
 }
 
 int run_fri(z0p_gpu_ctx* c, const FriShape& s, const FriParams& fp, const FriBufs& fb,
-            uint64_t poly_len, uint64_t degree_bound, z0p_transcript_state* ts, FriOut* out,
+            uint64_t poly_len, uint64_t degree_bound, Transcript& ts, FriOut* out,
             bool dims_absorbed) {
   if (!dims_absorbed) {
     uint8_t dims[24];  // src/fri.rs:1450-1456
@@ -280,8 +316,23 @@ int run_fri(z0p_gpu_ctx* c, const FriShape& s, const FriParams& fp, const FriBuf
   }
   const uint32_t unit_m = to_mont(two_adic_generator(2));
   out->caps.assign(s.len.size(), {});
+  const uint64_t fl = s.len.back();
+  out->final_vals.resize(4 * fl);
   for (size_t l = 0;; l++) {
-    RC(fetch_cap(c, fb.tree[l], s.leaves[l], s.drop[l], &out->caps[l]));
+    if (l + 1 == s.len.size()) {
+      // Last layer: its cap and its values (sent in the clear) in one trip.
+      uint32_t depth = log2u(s.leaves[l]);
+      uint64_t n = 1ull << s.drop[l];
+      out->caps[l].resize(32 * n);
+      RC(ensure_pinned(c, 32 * n + 16 * fl));
+      CK(d2h(c, c->pinned, fb.tree[l] + 8 * level_off(s.leaves[l], depth - s.drop[l]), 32 * n));
+      CK(d2h(c, c->pinned + 32 * n, fb.layer.back(), 16 * fl));
+      CK(sync(c, "cap+final"));
+      std::memcpy(out->caps[l].data(), c->pinned, 32 * n);
+      std::memcpy(out->final_vals.data(), c->pinned + 32 * n, 16 * fl);
+    } else {
+      RC(fetch_cap(c, fb.tree[l], s.leaves[l], s.drop[l], &out->caps[l]));
+    }
     for (size_t k = 0; k < out->caps[l].size() / 32; k++)
       transcript_absorb(ts, "fri-layer-root", out->caps[l].data() + 32 * k, 32);
     if (l + 1 == s.len.size()) break;
@@ -308,12 +359,6 @@ int run_fri(z0p_gpu_ctx* c, const FriShape& s, const FriParams& fp, const FriBuf
                             sync_words(c)));
   }
   // Final layer in the clear (src/fri.rs:620-621).
-  uint64_t fl = s.len.back();
-  out->final_vals.resize(4 * fl);
-  RC(ensure_pinned(c, 16 * fl));
-  CK(d2h(c, c->pinned, fb.layer.back(), 16 * fl));
-  CK(sync(c));
-  std::memcpy(out->final_vals.data(), c->pinned, 16 * fl);
   transcript_absorb(ts, "fri-final", (const uint8_t*)out->final_vals.data(), 16 * fl);
   // Proof of work (src/fri.rs:645-650, src/transcript.rs:206-228).
   out->nonce = 0;
@@ -326,7 +371,7 @@ int run_fri(z0p_gpu_ctx* c, const FriShape& s, const FriParams& fp, const FriBuf
                      (unsigned long long*)c->misc.p, 1ull << 40));
     RC(ensure_pinned(c, 24));
     CK(d2h(c, c->pinned, c->misc.p, 24));
-    CK(sync(c));
+    CK(sync(c, "grind"));
     unsigned long long res[3];
     std::memcpy(res, c->pinned, 24);
     if ((res[2] & 0xffffffffull) != 0 || res[0] == ~0ull) {
@@ -394,7 +439,7 @@ int run_gather(z0p_gpu_ctx* c, const Gather& g, std::vector<uint8_t>* out16,
     CK(row_fn((const uint32_t*)(da + n16 + n4), (uint32_t)nr,
               (uint32_t*)(dout + 16 * n16 + 4 * n4)));
   CK(d2h(c, c->pinned, dout, out_bytes));
-  CK(sync(c));
+  CK(sync(c, "openings"));
   out16->assign(c->pinned, c->pinned + 16 * n16);
   out4->resize(n4 + 2 * nr);
   std::memcpy(out4->data(), c->pinned + 16 * n16, 4 * n4 + 8 * nr);
@@ -486,7 +531,7 @@ void fib_mats(uint32_t mats[32][4]) {
 }
 
 // src/air.rs:365-372 -> 485-599 on the device.
-int air_prove(z0p_gpu_ctx* c, const z0p_air_params& p, z0p_transcript_state* ts, uint8_t* out,
+int air_prove(z0p_gpu_ctx* c, const z0p_air_params& p, Transcript& ts, uint8_t* out,
               size_t cap, size_t* len) {
   FriParams fp;
   FriShape s;
@@ -616,8 +661,7 @@ int air_prove(z0p_gpu_ctx* c, const z0p_air_params& p, z0p_transcript_state* ts,
   std::vector<size_t> trow;
   for (size_t i = 0; i < 2 * fo.indices.size(); i++) trow.push_back(g.a4.size() + 16 * i);
 
-  Writer w;  // air::Proof::to_bytes (src/air.rs:262-281)
-  w.b.reserve(need);
+  Writer w(out, need);  // air::Proof::to_bytes (src/air.rs:262-281)
   w.byte(6);
   w.u32((uint32_t)(column_cap.size() / 32));
   w.bytes(column_cap.data(), column_cap.size());
@@ -638,16 +682,15 @@ int air_prove(z0p_gpu_ctx* c, const z0p_air_params& p, z0p_transcript_state* ts,
     w.bytes(rows, 64);
     w.bytes(srows, 64);
   }
-  if (w.b.size() != need) {
+  if (w.n != need) {
     set_reason("internal error: proof length differs from its shape");
     return Z0P_ERR_CUDA;
   }
-  std::memcpy(out, w.b.data(), need);
   return Z0P_OK;
 }
 
 // src/range.rs:337-343 -> 353-375 -> 425-514 on the device.
-int range_prove(z0p_gpu_ctx* c, const z0p_range_params& p, z0p_transcript_state* ts, uint8_t* out,
+int range_prove(z0p_gpu_ctx* c, const z0p_range_params& p, Transcript& ts, uint8_t* out,
                 size_t cap, size_t* len) {
   FriParams fp;
   FriShape s;
@@ -745,8 +788,7 @@ int range_prove(z0p_gpu_ctx* c, const z0p_range_params& p, z0p_transcript_state*
   std::vector<uint32_t> g4;
   RC(run_gather(c, g, &g16, &g4));
 
-  Writer w;  // range::Proof::to_bytes (src/range.rs:253-269)
-  w.b.reserve(need);
+  Writer w(out, need);  // range::Proof::to_bytes (src/range.rs:253-269)
   w.byte(6);
   w.u32((uint32_t)(column_cap.size() / 32));
   w.bytes(column_cap.data(), column_cap.size());
@@ -761,11 +803,10 @@ int range_prove(z0p_gpu_ctx* c, const z0p_range_params& p, z0p_transcript_state*
     for (uint64_t b = 0; b < p.n_bits; b++) w.u32(row[1 + b]);
     write_path(w, g16.data() + 16 * tpath[qi], index, tsteps);
   }
-  if (w.b.size() != need) {
+  if (w.n != need) {
     set_reason("internal error: proof length differs from its shape");
     return Z0P_ERR_CUDA;
   }
-  std::memcpy(out, w.b.data(), need);
   return Z0P_OK;
 }
 
@@ -790,20 +831,20 @@ int z0p_transcript_init(z0p_transcript_state* st, const uint8_t* label, size_t l
 int z0p_transcript_absorb(z0p_transcript_state* st, const uint8_t* label, size_t llen,
                           const uint8_t* data, size_t dlen) {
   if (!st || (!label && llen) || (!data && dlen)) return Z0P_ERR_INVALID_ARGUMENT;
-  transcript_absorb_raw(st, label, llen, data, dlen);
+  Transcript(st).absorb_raw(label, llen, data, dlen);
   return Z0P_OK;
 }
 int z0p_transcript_challenge_bytes(z0p_transcript_state* st, const uint8_t* label, size_t llen,
                                    uint8_t out[32]) {
   if (!st || !out || (!label && llen)) return Z0P_ERR_INVALID_ARGUMENT;
-  squeeze_raw(st, label, llen, out);
+  Transcript(st).squeeze(label, llen, out);
   return Z0P_OK;
 }
 int z0p_transcript_challenge_ext(z0p_transcript_state* st, const uint8_t* label, size_t llen,
                                  uint32_t out[4]) {
   if (!st || !out || (!label && llen)) return Z0P_ERR_INVALID_ARGUMENT;
   uint8_t b[32];
-  squeeze_raw(st, label, llen, b);
+  Transcript(st).squeeze(label, llen, b);
   for (int i = 0; i < 4; i++)
     out[i] = ((uint32_t)b[4 * i] | ((uint32_t)b[4 * i + 1] << 8) | ((uint32_t)b[4 * i + 2] << 16) |
               ((uint32_t)b[4 * i + 3] << 24)) % P;
@@ -817,7 +858,7 @@ int z0p_transcript_challenge_index(z0p_transcript_state* st, const uint8_t* labe
     return Z0P_ERR_MALFORMED_INPUT;
   }
   uint8_t b[32];
-  squeeze_raw(st, label, llen, b);
+  Transcript(st).squeeze(label, llen, b);
   uint64_t v = 0;
   for (int i = 0; i < 8; i++) v |= (uint64_t)b[i] << (8 * i);
   *out = v & (domain - 1);
@@ -972,7 +1013,11 @@ int z0p_gpu_air_prove(z0p_gpu_ctx* c, const z0p_air_params* p, z0p_transcript_st
   ProfileScope ps(c);
   uint64_t t0 = now_ns();
   z0p_transcript_state work = *ts;
-  int rc = air_prove(c, *p, &work, out, cap, len);
+  Transcript t(&work);
+  c->last_sync_ns = t0;
+  int rc = air_prove(c, *p, t, out, cap, len);
+  if (c->profiling && c->last_sync_ns) c->tail_ns += now_ns() - c->last_sync_ns;
+  c->last_sync_ns = 0;
   c->prove_ns += now_ns() - t0;
   if (rc == Z0P_OK) {
     *ts = work;
@@ -1018,7 +1063,20 @@ int z0p_gpu_ctx_profile(z0p_gpu_ctx* c, char* json, size_t cap, size_t* len) {
              agg[i].first.c_str(), agg[i].second.first, (unsigned long long)agg[i].second.second);
     s += buf;
   }
-  s += "}";
+  s += agg.empty() ? "\"host\": {" : ", \"host\": {";
+  bool first = true;
+  for (auto& kv : c->sites) {
+    char buf[200];
+    snprintf(buf, sizeof buf, "%s\"%s\": {\"calls\": %llu, \"wait_ms\": %.6f, \"before_ms\": %.6f}",
+             first ? "" : ", ", kv.first.c_str(), (unsigned long long)kv.second.calls,
+             kv.second.wait_ns * 1e-6, kv.second.before_ns * 1e-6);
+    s += buf;
+    first = false;
+  }
+  char tb[80];
+  snprintf(tb, sizeof tb, "%s\"tail\": {\"ms\": %.6f}", first ? "" : ", ", c->tail_ns * 1e-6);
+  s += tb;
+  s += "}}";
   *len = s.size() + 1;
   if (!json || cap < s.size() + 1) return Z0P_ERR_BUFFER_TOO_SMALL;
   std::memcpy(json, s.c_str(), s.size() + 1);
@@ -1027,6 +1085,8 @@ int z0p_gpu_ctx_profile(z0p_gpu_ctx* c, char* json, size_t cap, size_t* len) {
     c->rec.pool.push_back(m.b);
   }
   c->rec.marks.clear();
+  c->sites.clear();
+  c->tail_ns = 0;
   return Z0P_OK;
 }
 
@@ -1038,7 +1098,11 @@ int z0p_gpu_range_prove(z0p_gpu_ctx* c, const z0p_range_params* p, z0p_transcrip
   ProfileScope ps(c);
   uint64_t t0 = now_ns();
   z0p_transcript_state work = *ts;
-  int rc = range_prove(c, *p, &work, out, cap, len);
+  Transcript t(&work);
+  c->last_sync_ns = t0;
+  int rc = range_prove(c, *p, t, out, cap, len);
+  if (c->profiling && c->last_sync_ns) c->tail_ns += now_ns() - c->last_sync_ns;
+  c->last_sync_ns = 0;
   c->prove_ns += now_ns() - t0;
   if (rc == Z0P_OK) {
     *ts = work;
