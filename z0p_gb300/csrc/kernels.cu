@@ -345,10 +345,12 @@ __device__ __forceinline__ uint32_t linked_b(const uint32_t* lde_a, uint32_t log
 // --------------------------------------------------------------- Merkle ----
 // Trace tree leaf L = rows 8L..8L+7 packed A||B (src/air.rs:520-531), hashed
 // as one 64-byte block (src/merkle.rs:93-110). B comes from A (linked_b):
-// eight (x - w_last) inverses per thread in one batch.
+// eight (x - w_last) inverses per thread in one batch, also stored coset-major
+// in tinv for the composition.
 __global__ void __launch_bounds__(256) air_trace_leaves_kernel(
     const uint32_t* __restrict__ lde_a, const uint32_t* __restrict__ cb, uint32_t w_last_m,
-    uint32_t* __restrict__ leaves, uint32_t logN, uint32_t logB, uint32_t nleaves, Tables tb) {
+    uint32_t* __restrict__ leaves, uint32_t* __restrict__ tinv, uint32_t logN, uint32_t logB,
+    uint32_t nleaves, Tables tb) {
   uint32_t L = blockIdx.x * blockDim.x + threadIdx.x;
   if (L >= nleaves) return;
   const uint32_t logm = logN + logB;
@@ -367,6 +369,7 @@ __global__ void __launch_bounds__(256) air_trace_leaves_kernel(
     uint32_t j = k & ((1u << logB) - 1u), q = k >> logB;
     m[2 * r] = __ldg(lde_a + ((size_t)j << logN) + q);
     m[2 * r + 1] = linked_b(lde_a, logN, j, q, __ldg(cb + j), den[r]);
+    tinv[((size_t)j << logN) + q] = den[r];
   }
   uint32_t d[8];
   blake3_leaf64(m, d);
@@ -551,8 +554,16 @@ __global__ void leaf16_kernel(const uint32_t* __restrict__ values, uint32_t* __r
 // -------------------------------------------------------------- compose ----
 // AIR composition (src/air.rs:847-929 == composition_at :938-962) on the four
 // rows of layer-0 quad P, written bit-reversed as one 64-byte leaf and hashed.
-// B at rows q and q+1 comes from A (linked_b); the inverses of (x - 1),
-// (x - w_last) and (x omega_N - w_last) for the four rows share one batch.
+//
+// No inversion here. With T(q) = 1/(x_q - w_last) from the trace-leaf pass and
+// w_last = omega_N^-1, x_{q+1} = omega_N x_q on a coset:
+//   1/(x - w_last)          = T(q)
+//   1/(omega_N x - w_last)  = T(q+1)        (B at the next row)
+//   1/(x - 1)               = omega_N^-1 T(q-1)   (folded into alpha_2, alpha_3)
+// and with B(x) = A(omega_N x) + C_j/(x - w_last) the first transition term
+// (A(omega_N x) - B(x)) (x - w_last)/Z(x) is the constant -coeff, so
+// alpha_0 times it is the per-proof constant kc. All arithmetic is exact, so
+// the values equal the reference's term by term.
 __global__ void __launch_bounds__(kThreads) air_compose_leaves_kernel(AirComposeArgs a, Tables tb) {
   const uint32_t logm = a.logN + a.logB;
   const uint32_t quarter = 1u << (logm - 2);
@@ -568,41 +579,34 @@ __global__ void __launch_bounds__(kThreads) air_compose_leaves_kernel(AirCompose
   }
   const uint32_t P = brev_bits(k0, logm - 2);
   const uint32_t gamma_m = to_mont(31u);
-  uint32_t den[12], zt[4];
-#pragma unroll
-  for (int s = 0; s < 4; s++) {
-    uint32_t k = k0 + (uint32_t)s * quarter;
-    uint32_t j = k & (B - 1u);
-    uint32_t x = mmul(gamma_m, root_pow(tb, k << (kRootBits - logm)));
-    den[3 * s] = fsub(x, a.w_last_m);                              // row q
-    den[3 * s + 1] = fsub(x, kR);                                  // x - 1
-    den[3 * s + 2] = fsub(mmul(x, a.omega_n_m), a.w_last_m);       // row q + 1
-    zt[s] = mmul(den[3 * s], __ldg(a.zinv + j));  // 1 / Z_t = (x - w_last) / (x^N - 1)
-  }
-  batch_minv(den);
   uint32_t leaf[16];
 #pragma unroll
   for (int s = 0; s < 4; s++) {
-    uint32_t k = k0 + (uint32_t)s * quarter;
-    uint32_t j = k & (B - 1u), q = k >> a.logB;
-    uint32_t qn = (q + 1u) & (N - 1u);
-    const uint32_t cbj = __ldg(a.cb + j);
+    const uint32_t k = k0 + (uint32_t)s * quarter;
+    const uint32_t j = k & (B - 1u), q = k >> a.logB;
+    const uint32_t qm = (q - 1u) & (N - 1u), qn = (q + 1u) & (N - 1u), qnn = (q + 2u) & (N - 1u);
     const size_t base = (size_t)j << a.logN;
-    uint32_t av = __ldg(a.lde_a + base + q);
-    uint32_t avn = __ldg(a.lde_a + base + qn);
-    uint32_t bv = linked_b(a.lde_a, a.logN, j, q, cbj, den[3 * s]);
-    uint32_t bvn = linked_b(a.lde_a, a.logN, j, qn, cbj, den[3 * s + 2]);
-    uint32_t t1 = mmul(fsub(avn, bv), zt[s]);
-    uint32_t t2 = mmul(fsub(bvn, fadd(av, bv)), zt[s]);
-    uint32_t ba = mmul(fsub(av, a.a0), den[3 * s + 1]);
-    uint32_t bb = mmul(fsub(bv, a.b0), den[3 * s + 1]);
-    uint32_t bo = mmul(fsub(bv, a.b_last), den[3 * s]);
+    const uint32_t av = __ldg(a.lde_a + base + q);
+    const uint32_t avn = __ldg(a.lde_a + base + qn);
+    const uint32_t avnn = __ldg(a.lde_a + base + qnn);
+    const uint32_t tm = __ldg(a.tinv + base + qm);
+    const uint32_t t0 = __ldg(a.tinv + base + q);
+    const uint32_t tn = __ldg(a.tinv + base + qn);
+    const uint32_t cbj = __ldg(a.cb + j);
+    const uint32_t x = mmul(gamma_m, root_pow(tb, k << (kRootBits - logm)));
+    const uint32_t zt = mmul(fsub(x, a.w_last_m), __ldg(a.zinv + j));  // (x - w_last)/Z
+    const uint32_t bv = fadd(avn, mmul(cbj, t0));
+    const uint32_t bvn = fadd(avnn, mmul(cbj, tn));
+    const uint32_t t2 = mmul(fsub(bvn, fadd(av, bv)), zt);
+    const uint32_t ba = mmul(fsub(av, a.a0), tm);
+    const uint32_t bb = mmul(fsub(bv, a.b0), tm);
+    const uint32_t bo = mmul(fsub(bv, a.b_last), t0);
     const int t = (s == 1) ? 2 : (s == 2) ? 1 : s;  // position 4P + brev2(s)
 #pragma unroll
     for (int c = 0; c < 4; c++) {
       const uint32_t* al = a.alpha[c];
-      uint32_t acc = fadd(mdot2(t1, al[0], t2, al[1]), mdot2(ba, al[2], bb, al[3]));
-      leaf[4 * t + c] = fadd(acc, mmul(bo, al[4]));
+      uint32_t acc = fadd(mdot2(t2, al[1], ba, al[2]), mdot2(bb, al[3], bo, al[4]));
+      leaf[4 * t + c] = fadd(acc, a.kc[c]);
     }
   }
   uint4* dst = reinterpret_cast<uint4*>(a.layer0 + 16 * (size_t)P);
@@ -989,12 +993,12 @@ cudaError_t coset_zinv(cudaStream_t st, const Tables& tb, uint32_t* zinv, uint32
 
 cudaError_t air_trace_leaves(cudaStream_t st, const Tables& tb, const uint32_t* lde_a,
                              const uint32_t* cb, uint32_t w_last_m, uint32_t* leaves,
-                             uint32_t logN, uint32_t logB) {
+                             uint32_t* tinv, uint32_t logN, uint32_t logB) {
   uint32_t nleaves = 1u << (logN + logB - 3);
   Stage stg("trace_leaves", st);
   stg.launched();
-  air_trace_leaves_kernel<<<grid_for(nleaves), kThreads, 0, st>>>(lde_a, cb, w_last_m, leaves, logN,
-                                                                  logB, nleaves, tb);
+  air_trace_leaves_kernel<<<grid_for(nleaves), kThreads, 0, st>>>(lde_a, cb, w_last_m, leaves, tinv,
+                                                                  logN, logB, nleaves, tb);
   return cudaGetLastError();
 }
 

@@ -36,13 +36,16 @@ struct AirComposeArgs {
   const uint32_t* lde_a;  // coset-major [j][q]
   const uint32_t* cb;     // per coset C_j (canonical)
   const uint32_t* zinv;   // per coset 1 / (x^N - 1) (Montgomery)
+  const uint32_t* tinv;   // coset-major 1 / (x - w_last) (Montgomery), from air_trace_leaves
   uint32_t* layer0;       // FRI layer 0, bit-reversed Ext4 values
   uint32_t* leaves;       // layer-0 tree, leaf digests
   uint32_t logN, logB;
   uint32_t a0, b0, b_last;  // canonical
   uint32_t w_last_m;        // omega_N^(N-1) (Montgomery)
-  uint32_t omega_n_m;       // omega_N (Montgomery): x of row k + B is x * omega_N
-  uint32_t alpha[4][5];     // alpha_k coordinate c at [c][k] (Montgomery)
+  // Coordinate c of the weights at [c][k] (Montgomery): alpha_1, alpha_2 and
+  // alpha_3 times omega_N^-1, alpha_4 ([c][0] unused).
+  uint32_t alpha[4][5];
+  uint32_t kc[4];  // alpha_0 * (-coeff), canonical: the constant first term
 };
 
 struct RangeComposeArgs {
@@ -96,9 +99,10 @@ cudaError_t ntt(cudaStream_t st, const Tables& tb, const NttPlan& plan, const ui
 cudaError_t coset_zinv(cudaStream_t st, const Tables& tb, uint32_t* zinv, uint32_t* zinv2,
                        uint32_t logB, uint32_t gamma_n_m, uint32_t* cb, uint32_t coeff);
 // Trace leaves of the AIR: rows 8L..8L+7 as A || B with B derived from A.
+// Also writes tinv (m words, coset-major): 1 / (x - w_last) per LDE row.
 cudaError_t air_trace_leaves(cudaStream_t st, const Tables& tb, const uint32_t* lde_a,
                              const uint32_t* cb, uint32_t w_last_m, uint32_t* leaves,
-                             uint32_t logN, uint32_t logB);
+                             uint32_t* tinv, uint32_t logN, uint32_t logB);
 // (A, B) of the AIR trace LDE at natural rows rows[0..n): out[2i], out[2i+1].
 cudaError_t air_rows(cudaStream_t st, const Tables& tb, const uint32_t* lde_a, const uint32_t* cb,
                      uint32_t w_last_m, uint32_t logN, uint32_t logB, const uint32_t* rows,

@@ -610,7 +610,8 @@ int air_prove(z0p_gpu_ctx* c, const z0p_air_params& p, Transcript& ts, uint8_t* 
   // Joint trace tree over 8-row 64-byte leaves (src/air.rs:520-537).
   uint64_t tleaves = m / 8;
   uint32_t tdepth = log2u(tleaves), tdrop = p.cap_height < tdepth ? (uint32_t)p.cap_height : tdepth;
-  CK(launch::air_trace_leaves(st, c->tb, lde_a, cb, w_last_m, ttree, logN, logB));
+  uint32_t* tinv = (uint32_t*)c->scratch.p;  // the NTT's scratch is free from here on
+  CK(launch::air_trace_leaves(st, c->tb, lde_a, cb, w_last_m, ttree, tinv, logN, logB));
   CK(launch::merkle_build(st, ttree, tleaves, tdepth - tdrop, sync_words(c)));
   std::vector<uint8_t> column_cap;
   RC(fetch_cap(c, ttree, tleaves, tdrop, &column_cap));
@@ -620,14 +621,20 @@ int air_prove(z0p_gpu_ctx* c, const z0p_air_params& p, Transcript& ts, uint8_t* 
 
   // Composition as bit-reversed FRI layer 0 with its leaves (src/air.rs:847-929).
   AirComposeArgs ca;
-  ca.lde_a = lde_a; ca.cb = cb; ca.zinv = zinv;
+  ca.lde_a = lde_a; ca.cb = cb; ca.zinv = zinv; ca.tinv = tinv;
   ca.layer0 = fb.layer[0]; ca.leaves = fb.tree[0];
   ca.logN = logN; ca.logB = logB;
   ca.a0 = p.a0; ca.b0 = p.b0; ca.b_last = p.b_last;
   ca.w_last_m = w_last_m;
-  ca.omega_n_m = to_mont(omega_n);
-  for (int k = 0; k < 5; k++)
-    for (int e = 0; e < 4; e++) ca.alpha[e][k] = to_mont(alpha[k][e]);
+  const uint32_t omega_inv = finv(omega_n), neg_coeff = fsub(0, coeff);
+  for (int e = 0; e < 4; e++) {
+    ca.alpha[e][0] = 0;
+    ca.alpha[e][1] = to_mont(alpha[1][e]);
+    ca.alpha[e][2] = to_mont(fmul(alpha[2][e], omega_inv));
+    ca.alpha[e][3] = to_mont(fmul(alpha[3][e], omega_inv));
+    ca.alpha[e][4] = to_mont(alpha[4][e]);
+    ca.kc[e] = fmul(alpha[0][e], neg_coeff);
+  }
   CK(launch::air_compose_leaves(st, c->tb, ca));
   CK(launch::merkle_build(st, fb.tree[0], s.leaves[0], s.depth[0] - s.drop[0], sync_words(c)));
 
