@@ -148,6 +148,12 @@ void z0p_gpu_ctx_destroy(z0p_gpu_ctx *ctx);
 void *z0p_gpu_ctx_stream(z0p_gpu_ctx *ctx);
 /* Bytes of device memory currently held by the context. */
 size_t z0p_gpu_ctx_device_bytes(z0p_gpu_ctx *ctx);
+/* Hands the context's proof workspace (trace, LDE, trees, FRI layers) back to
+ * the library's device memory pool, queued on the context's stream; the next
+ * prove call takes it again. No counterpart in the reference (its buffers are
+ * per-call Vecs); a serving loop uses it to keep held memory near the sum of
+ * the running jobs' footprints. */
+int z0p_gpu_ctx_trim(z0p_gpu_ctx *ctx);
 /* Cumulative counters of a context (launches are process-wide). */
 typedef struct {
     uint64_t launches;   /* kernels launched by this library in this process */

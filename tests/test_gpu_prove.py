@@ -94,6 +94,25 @@ def test_chained_proofs_on_one_transcript(z0p, oracle, gpu_ctx):
         assert tz.export() == to.export()
 
 
+def test_trim_and_regrow_workspace(z0p, oracle):
+    """Proofs after the workspace went back to the pool (and grew again) are unchanged."""
+    from z0p_gb300.context import Context
+
+    ctx = Context(0)
+    shapes = [(256, 1, 2), (1 << 12, 3, 4), (64, 5, 6)]
+    for n, a0, b0 in shapes:
+        _, b = oracle.build_trace(a0, b0, n)
+        pz = z0p.air.Params.for_security(n, a0, b0, int(b[-1]), 100)
+        po = oracle.air_for_security(n, a0, b0, int(b[-1]), 100)
+        ref = oracle.air_prove(po, oracle.Transcript(b"trim"))
+        assert z0p.air.prove(pz, z0p.Transcript(b"trim"), ctx) == ref
+        held = ctx.device_bytes
+        ctx.trim()
+        assert ctx.device_bytes < min(held, 1 << 20)  # twiddle tables and counters stay
+        assert z0p.air.prove(pz, z0p.Transcript(b"trim"), ctx) == ref
+    ctx.close()
+
+
 def test_forged_and_dishonest_statements_prove_structurally(z0p, oracle, gpu_ctx):
     """False claims still prove (src/air.rs:356-364) and fail verification."""
     _, b = oracle.build_trace(1, 1, 32)

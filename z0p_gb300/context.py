@@ -36,6 +36,10 @@ class Context:
     def device_bytes(self) -> int:
         return lib().z0p_gpu_ctx_device_bytes(self.handle)
 
+    def trim(self) -> None:
+        """Hand the proof workspace back to the library's device memory pool."""
+        check(lib().z0p_gpu_ctx_trim(self.handle))
+
     def stats(self) -> dict:
         s = Stats()
         check(lib().z0p_gpu_ctx_stats(self.handle, C.byref(s)))

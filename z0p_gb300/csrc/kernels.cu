@@ -17,6 +17,7 @@
 
 #include <atomic>
 #include <cstdint>
+#include <mutex>
 
 #include "device.cuh"
 #include "kernels.h"
@@ -168,8 +169,9 @@ __global__ void __launch_bounds__(512) ntt_small_kernel(const uint32_t* __restri
   const uint32_t b = blockIdx.x;
   const uint32_t* src = in + (size_t)(b / a.in_div) * n;
   const uint32_t j = b % a.twist_mod;
-  for (uint32_t i = threadIdx.x; i < n / 2; i += blockDim.x)
-    tw[i] = root_pow(a.tb, tw_exp(i, kRootBits - L, a.inverse));
+  if constexpr (L > 0)
+    for (uint32_t i = threadIdx.x; i < n / 2; i += blockDim.x)
+      tw[i] = root_pow(a.tb, tw_exp(i, kRootBits - L, a.inverse));
   // twist w^(j i): a geometric chain per thread (stride blockDim)
   uint32_t tw_cur = 0, tw_step = 0;
   if (j) {
@@ -376,20 +378,6 @@ __global__ void __launch_bounds__(256) air_trace_leaves_kernel(
   store_digest(leaves + 8 * (size_t)L, d);
 }
 
-// (A, B) at arbitrary natural rows, for the trace openings.
-__global__ void air_rows_kernel(const uint32_t* __restrict__ lde_a, const uint32_t* __restrict__ cb,
-                                uint32_t w_last_m, uint32_t logN, uint32_t logB,
-                                const uint32_t* __restrict__ rows, uint32_t n,
-                                uint32_t* __restrict__ out, Tables tb) {
-  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const uint32_t k = rows[i], logm = logN + logB;
-  const uint32_t j = k & ((1u << logB) - 1u), q = k >> logB;
-  uint32_t x = mmul(to_mont(31u), root_pow(tb, k << (kRootBits - logm)));
-  out[2 * i] = __ldg(lde_a + ((size_t)j << logN) + q);
-  out[2 * i + 1] = linked_b(lde_a, logN, j, q, __ldg(cb + j), minv(fsub(x, w_last_m)));
-}
-
 // Range tree leaf k = BLAKE3(0x00 || row k) with the row = ncols LE words
 // (src/range.rs:452-460, src/hash.rs:351-381). Threads walk rows in
 // coset-major order so column reads coalesce; digests land at index k.
@@ -429,8 +417,10 @@ __global__ void range_trace_leaves_kernel(const uint32_t* __restrict__ lde,
   store_digest(leaves + 8 * (size_t)k, o);
 }
 
+// One tree level; `cap` (may be null) receives a second copy of the level
+// when it is the tree's cap level.
 __global__ void merkle_level_kernel(const uint32_t* __restrict__ prev, uint32_t* __restrict__ next,
-                                    uint64_t count) {
+                                    uint64_t count, uint32_t* __restrict__ cap) {
   uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= count) return;
   uint32_t l[8], r[8], d[8];
@@ -438,6 +428,13 @@ __global__ void merkle_level_kernel(const uint32_t* __restrict__ prev, uint32_t*
   load_digest(prev + 16 * i + 8, r);
   blake3_node(l, r, d);
   store_digest(next + 8 * i, d);
+  if (cap) store_digest(cap + 8 * i, d);
+}
+
+__global__ void copy_words_kernel(const uint32_t* __restrict__ src, uint32_t* __restrict__ dst,
+                                  uint64_t n) {
+  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) dst[i] = src[i];
 }
 
 __device__ __forceinline__ uint64_t level_offset(uint64_t leaves, uint32_t level) {
@@ -448,23 +445,33 @@ __device__ __forceinline__ uint64_t level_offset(uint64_t leaves, uint32_t level
 // [2T b, 2T b + 2T) of level l0 up to one node at level l0 + log2(2T) (or
 // up to `top`), keeping each level in shared memory and writing it to
 // global. The CTA that finishes last (one atomic per CTA on `counter`, after a
-// release fence) then hashes the remaining levels from the other CTAs' roots.
-// Nobody waits for anybody: the last CTA simply continues.
+// release fence) loads the CTAs' roots into shared memory and hashes the
+// remaining levels there. Nobody waits for anybody: the last CTA continues.
+// Digests sit in shared memory at a stride of 9 words (2-way bank conflicts
+// at most when a thread reads its two children).
 constexpr int kTopThreads = 256;
+constexpr int kTopStride = 9;
+constexpr int kTopMaxRoots = 512;  // level-l0 nodes <= 2^18, 512 per CTA
 
-__device__ __forceinline__ void hash_pair_to(const uint32_t* l, const uint32_t* r, uint32_t* out) {
+__device__ __forceinline__ void hash_pair_smem(const uint32_t* pair, uint32_t* out_s,
+                                               uint32_t* out_g, uint32_t* out_cap) {
   uint32_t a[8], b[8], d[8];
 #pragma unroll
-  for (int i = 0; i < 8; i++) { a[i] = l[i]; b[i] = r[i]; }
+  for (int i = 0; i < 8; i++) { a[i] = pair[i]; b[i] = pair[kTopStride + i]; }
   blake3_node(a, b, d);
 #pragma unroll
-  for (int i = 0; i < 8; i++) out[i] = d[i];
+  for (int i = 0; i < 8; i++) out_s[i] = d[i];
+  store_digest(out_g, d);
+  if (out_cap) store_digest(out_cap, d);
 }
 
+// `cap` (may be null) receives a copy of level `top`. The CTA that finishes
+// the tree puts `counter` back to zero for the next launch.
 __global__ void __launch_bounds__(kTopThreads) merkle_top_kernel(uint32_t* tree, uint64_t leaves,
                                                                  uint32_t l0, uint32_t top,
-                                                                 unsigned int* counter) {
-  __shared__ uint32_t sm[2][kTopThreads * 8];
+                                                                 unsigned int* counter,
+                                                                 uint32_t* cap) {
+  __shared__ uint32_t sm[2][kTopMaxRoots * kTopStride];
   __shared__ int last;
   const uint32_t lsub = l0 + 9 < top ? l0 + 9 : top;  // last level done per CTA
   // level l0+1: thread t hashes children 2(base+t), 2(base+t)+1
@@ -480,19 +487,18 @@ __global__ void __launch_bounds__(kTopThreads) merkle_top_kernel(uint32_t* tree,
     load_digest(prev + 16 * node + 8, b);
     blake3_node(a, b, d);
     store_digest(tree + 8 * (level_offset(leaves, l0 + 1) + node), d);
+    if (cap && l0 + 1 == top) store_digest(cap + 8 * node, d);
 #pragma unroll
-    for (int i = 0; i < 8; i++) sm[cur][8 * threadIdx.x + i] = d[i];
+    for (int i = 0; i < 8; i++) sm[cur][kTopStride * threadIdx.x + i] = d[i];
   }
   __syncthreads();
   for (uint32_t l = l0 + 1; l < lsub; l++) {
     per >>= 1;
     if (threadIdx.x < per) {
-      uint32_t* out = sm[cur ^ 1] + 8 * threadIdx.x;
-      hash_pair_to(sm[cur] + 16 * threadIdx.x, sm[cur] + 16 * threadIdx.x + 8, out);
       uint64_t n = (uint64_t)blockIdx.x * per + threadIdx.x;
-      uint32_t* g = tree + 8 * (level_offset(leaves, l + 1) + n);
-#pragma unroll
-      for (int i = 0; i < 8; i++) g[i] = out[i];
+      hash_pair_smem(sm[cur] + 2 * kTopStride * threadIdx.x, sm[cur ^ 1] + kTopStride * threadIdx.x,
+                     tree + 8 * (level_offset(leaves, l + 1) + n),
+                     (cap && l + 1 == top) ? cap + 8 * n : nullptr);
     }
     cur ^= 1;
     __syncthreads();
@@ -504,21 +510,27 @@ __global__ void __launch_bounds__(kTopThreads) merkle_top_kernel(uint32_t* tree,
   __syncthreads();
   if (!last) return;
   __threadfence();
+  uint64_t n = leaves >> lsub;  // == gridDim.x <= kTopMaxRoots
+  const uint32_t* roots = tree + 8 * level_offset(leaves, lsub);
+  for (uint64_t i = threadIdx.x; i < n; i += blockDim.x) {
+    const uint4* p = reinterpret_cast<const uint4*>(roots + 8 * i);
+    uint4 v0 = __ldcg(p), v1 = __ldcg(p + 1);
+    uint32_t* o = sm[0] + kTopStride * i;
+    o[0] = v0.x; o[1] = v0.y; o[2] = v0.z; o[3] = v0.w;
+    o[4] = v1.x; o[5] = v1.y; o[6] = v1.z; o[7] = v1.w;
+  }
+  cur = 0;
+  __syncthreads();
   for (uint32_t l = lsub; l < top; l++) {
-    const uint64_t n = leaves >> (l + 1);
-    const uint32_t* prev = tree + 8 * level_offset(leaves, l);
+    n >>= 1;
     uint32_t* next = tree + 8 * level_offset(leaves, l + 1);
-    for (uint64_t i = threadIdx.x; i < n; i += blockDim.x) {
-      const uint4* p = reinterpret_cast<const uint4*>(prev + 16 * i);
-      uint4 a0 = __ldcg(p), a1 = __ldcg(p + 1), b0 = __ldcg(p + 2), b1 = __ldcg(p + 3);
-      uint32_t a[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
-      uint32_t b[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
-      uint32_t d[8];
-      blake3_node(a, b, d);
-      store_digest(next + 8 * i, d);
-    }
+    for (uint64_t i = threadIdx.x; i < n; i += blockDim.x)
+      hash_pair_smem(sm[cur] + 2 * kTopStride * i, sm[cur ^ 1] + kTopStride * i, next + 8 * i,
+                     (cap && l + 1 == top) ? cap + 8 * i : nullptr);
+    cur ^= 1;
     __syncthreads();
   }
+  if (threadIdx.x == 0) *counter = 0u;
 }
 
 // 64-byte leaves (four Ext4 values) of an in-memory FRI layer
@@ -777,14 +789,30 @@ constexpr int kGrindThreads = 256;
 constexpr int kGrindPerThread = 4;
 constexpr uint64_t kGrindChunk = (uint64_t)kGrindThreads * kGrindPerThread;
 
+// state: [0] best nonce, [1] next chunk, [2] status (1 = chunk cap reached),
+// [3] CTAs finished. The last CTA to finish copies {best, status} to `out`
+// and puts the state back to {~0, 0, 0, 0} for the next launch.
 struct GrindArgs {
   uint32_t head[16];
   uint32_t bits;
-  unsigned long long* best;
-  unsigned long long* next_chunk;
-  unsigned int* status;
+  unsigned long long* state;
+  unsigned long long* out;
   unsigned long long max_chunks;
 };
+
+__device__ __forceinline__ void grind_finish(const GrindArgs& a) {
+  if (threadIdx.x != 0) return;
+  __threadfence();
+  if (atomicAdd(a.state + 3, 1ull) != gridDim.x - 1) return;
+  __threadfence();
+  a.out[0] = atomicAdd(a.state + 0, 0ull);
+  a.out[1] = atomicAdd(a.state + 2, 0ull);
+  a.state[0] = ~0ull;
+  a.state[1] = 0ull;
+  a.state[2] = 0ull;
+  a.state[3] = 0ull;
+  __threadfence();
+}
 
 template <int H>
 __global__ void __launch_bounds__(kGrindThreads) grind_kernel(GrindArgs a) {
@@ -794,17 +822,20 @@ __global__ void __launch_bounds__(kGrindThreads) grind_kernel(GrindArgs a) {
   __shared__ int s_stop;
   for (;;) {
     if (threadIdx.x == 0) {
-      unsigned long long c = atomicAdd(a.next_chunk, 1ull);
+      unsigned long long c = atomicAdd(a.state + 1, 1ull);
       s_chunk = c;
-      unsigned long long best = *reinterpret_cast<volatile unsigned long long*>(a.best);
+      unsigned long long best = *reinterpret_cast<volatile unsigned long long*>(a.state);
       s_stop = (c >= a.max_chunks) ? 2 : (c * kGrindChunk > best ? 1 : 0);
-      if (s_stop == 2) atomicOr(a.status, 1u);
+      if (s_stop == 2) atomicOr(a.state + 2, 1ull);
     }
     __syncthreads();
     unsigned long long c = s_chunk;
     int stop = s_stop;
     __syncthreads();
-    if (stop) return;
+    if (stop) {
+      grind_finish(a);
+      return;
+    }
 #pragma unroll 1
     for (int k = 0; k < kGrindPerThread; k++) {
       unsigned long long nonce = c * kGrindChunk + (unsigned long long)k * kGrindThreads + threadIdx.x;
@@ -824,7 +855,7 @@ __global__ void __launch_bounds__(kGrindThreads) grind_kernel(GrindArgs a) {
       iv_words(cv);
       blake3_compress(cv, m, 0u, 0u, (uint32_t)(H + 8), kChunkStart | kChunkEnd | kRoot, o);
       uint32_t lz = __clz(__byte_perm(o[0], 0, 0x0123));
-      if (lz >= a.bits) atomicMin(a.best, nonce);
+      if (lz >= a.bits) atomicMin(a.state, nonce);
     }
   }
 }
@@ -842,19 +873,74 @@ __global__ void coset_to_natural_kernel(const uint32_t* __restrict__ in, uint32_
   out[i] = in[(col << logm) + ((uint64_t)j << logN) + q];
 }
 
-// --------------------------------------------------------------- gather ----
-__global__ void gather16_kernel(const uint64_t* __restrict__ addr, uint4* __restrict__ out,
-                                uint32_t n) {
-  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  out[i] = *reinterpret_cast<const uint4*>(addr[i]);
+// ------------------------------------------------------------- openings ----
+// Every opened value and Merkle path of one proof, gathered straight from the
+// device-resident layers and trees into the proof-order block of each query
+// (src/fri.rs:1229-1260 for FRI, src/air.rs:565-591 and src/range.rs:483-500
+// for the trace). One CTA per query; the block layout is OpenArgs'.
+__global__ void __launch_bounds__(128) openings_kernel(OpenArgs a) {
+  const uint32_t qi = blockIdx.x;
+  uint32_t* out = a.out + (size_t)qi * a.stride;
+  const uint64_t leaf = a.indices[qi];
+  // FRI layers: 16 words of values, then steps x 8 words of siblings.
+  for (uint32_t d = 0; d < a.nlayers; d++) {
+    const OpenLayer& L = a.layer[d];
+    const uint64_t base = (leaf >> (2 * d)) & ~3ull;
+    const uint64_t Q = base >> 2;
+    uint32_t* o = out + L.off;
+    for (uint32_t t = threadIdx.x; t < 16 + 8 * L.steps; t += blockDim.x) {
+      if (t < 16) {
+        o[t] = L.values[4 * base + t];
+      } else {
+        const uint32_t st = (t - 16) >> 3, w = (t - 16) & 7u;
+        const uint64_t sib = (Q >> st) ^ 1ull;
+        o[t] = L.tree[8 * (2 * L.leaves - 2 * (L.leaves >> st) + sib) + w];
+      }
+    }
+  }
+  // Trace openings.
+  const uint32_t logm = a.logN + a.logB;
+  const uint32_t N = 1u << a.logN, B = 1u << a.logB;
+  const uint64_t m = 1ull << logm;
+  const uint64_t index = brev_bits((uint32_t)leaf, logm);
+  uint32_t* o = out + a.trace_off;
+  if (a.ncol == 0) {
+    // AIR: rows base..base+7 of `index` and of `index + B`, A || B each, with
+    // B = A(q+1) + C_j * tinv[j][q] (the linked column).
+    for (uint32_t h = 0; h < 2; h++) {
+      const uint64_t at = h ? (index + B) % m : index;
+      const uint64_t base = at & ~7ull;
+      uint32_t* oh = o + h * (16 + 8 * a.tsteps);
+      for (uint32_t t = threadIdx.x; t < 16 + 8 * a.tsteps; t += blockDim.x) {
+        if (t < 16) {
+          const uint32_t k = (uint32_t)base + (t >> 1);
+          const uint32_t j = k & (B - 1u), q = k >> a.logB;
+          const size_t cj = (size_t)j << a.logN;
+          uint32_t v = a.lde[cj + q];
+          if (t & 1u) v = fadd(a.lde[cj + ((q + 1u) & (N - 1u))], mmul(a.cb[j], a.tinv[cj + q]));
+          oh[t] = v;
+        } else {
+          const uint32_t st = (t - 16) >> 3, w = (t - 16) & 7u;
+          const uint64_t sib = ((base >> 3) >> st) ^ 1ull;
+          oh[t] = a.ttree[8 * (2 * a.tleaves - 2 * (a.tleaves >> st) + sib) + w];
+        }
+      }
+    }
+  } else {
+    // Range: the ncol column values at `index`, then its path.
+    const uint32_t j = (uint32_t)index & (B - 1u), q = (uint32_t)(index >> a.logB);
+    for (uint32_t t = threadIdx.x; t < a.ncol + 8 * a.tsteps; t += blockDim.x) {
+      if (t < a.ncol) {
+        o[t] = a.lde[(size_t)t * m + ((size_t)j << a.logN) + q];
+      } else {
+        const uint32_t st = (t - a.ncol) >> 3, w = (t - a.ncol) & 7u;
+        const uint64_t sib = (index >> st) ^ 1ull;
+        o[t] = a.ttree[8 * (2 * a.tleaves - 2 * (a.tleaves >> st) + sib) + w];
+      }
+    }
+  }
 }
-__global__ void gather4_kernel(const uint64_t* __restrict__ addr, uint32_t* __restrict__ out,
-                               uint32_t n) {
-  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  out[i] = *reinterpret_cast<const uint32_t*>(addr[i]);
-}
+
 
 }  // namespace
 
@@ -909,6 +995,18 @@ cudaError_t fill_constant_columns(cudaStream_t st, uint32_t* cols, uint32_t n, u
   return cudaGetLastError();
 }
 
+// True when the pass-`pass` kernel for half-length 2^L has already been
+// allowed `smem` bytes of dynamic shared memory in this process (each kernel's
+// need is fixed by L, so the attribute is set once per kernel, not per launch).
+bool smem_raised(int pass, uint32_t L, size_t smem) {
+  static std::mutex mu;
+  static size_t done[3][32] = {};
+  std::lock_guard<std::mutex> lk(mu);
+  if (done[pass][L] >= smem) return true;
+  done[pass][L] = smem;
+  return false;
+}
+
 cudaError_t ntt(cudaStream_t st, const Tables& tb, const NttPlan& plan, const uint32_t* in,
                 uint32_t* out, uint32_t* scratch) {
   NttArgs a;
@@ -956,8 +1054,9 @@ cudaError_t ntt(cudaStream_t st, const Tables& tb, const NttPlan& plan, const ui
   switch (logn1) {
 #define Z0P_P1(Lv, LC)                                                                          \
   case Lv:                                                                                      \
-    cudaFuncSetAttribute(ntt_pass1_kernel<Lv, LC>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
-                         (int)smem1);                                                           \
+    if (!smem_raised(1, Lv, smem1))                                                             \
+      cudaFuncSetAttribute(ntt_pass1_kernel<Lv, LC>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                           (int)smem1);                                                         \
     ntt_pass1_kernel<Lv, LC><<<g1, 512, smem1, st>>>(in, scratch, a);                           \
     break;
     Z0P_P1(7, 3) Z0P_P1(8, 3) Z0P_P1(9, 3) Z0P_P1(10, 3) Z0P_P1(11, 3) Z0P_P1(12, 3) Z0P_P1(13, 2)
@@ -969,8 +1068,9 @@ cudaError_t ntt(cudaStream_t st, const Tables& tb, const NttPlan& plan, const ui
   switch (logn2) {
 #define Z0P_P2(Lv, LR)                                                                          \
   case Lv:                                                                                      \
-    cudaFuncSetAttribute(ntt_pass2_kernel<Lv, LR>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
-                         (int)smem2);                                                           \
+    if (!smem_raised(2, Lv, smem2))                                                             \
+      cudaFuncSetAttribute(ntt_pass2_kernel<Lv, LR>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                           (int)smem2);                                                         \
     ntt_pass2_kernel<Lv, LR><<<g2, 512, smem2, st>>>(scratch, out, a);                          \
     break;
     Z0P_P2(6, 3) Z0P_P2(7, 3) Z0P_P2(8, 3) Z0P_P2(9, 3) Z0P_P2(10, 3) Z0P_P2(11, 3) Z0P_P2(12, 3)
@@ -1002,16 +1102,6 @@ cudaError_t air_trace_leaves(cudaStream_t st, const Tables& tb, const uint32_t* 
   return cudaGetLastError();
 }
 
-cudaError_t air_rows(cudaStream_t st, const Tables& tb, const uint32_t* lde_a, const uint32_t* cb,
-                     uint32_t w_last_m, uint32_t logN, uint32_t logB, const uint32_t* rows,
-                     uint32_t n, uint32_t* out) {
-  if (!n) return cudaSuccess;
-  Stage stg("gather", st);
-  stg.launched();
-  air_rows_kernel<<<grid_for(n), kThreads, 0, st>>>(lde_a, cb, w_last_m, logN, logB, rows, n, out, tb);
-  return cudaGetLastError();
-}
-
 cudaError_t range_trace_leaves(cudaStream_t st, const uint32_t* lde, uint32_t* leaves,
                                uint32_t logN, uint32_t logB, uint32_t ncols) {
   if (ncols < 1 || ncols > 25) return cudaErrorInvalidValue;
@@ -1023,18 +1113,26 @@ cudaError_t range_trace_leaves(cudaStream_t st, const uint32_t* lde, uint32_t* l
 }
 
 cudaError_t merkle_build(cudaStream_t st, uint32_t* tree, uint64_t leaves, uint32_t top,
-                         unsigned int* counter) {
+                         unsigned int* counter, uint32_t* cap) {
   Stage stg("merkle_levels", st);
-  // Levels with more than 2^16 nodes fill the GPU on their own: one launch
-  // each. The rest (at most 2^16 nodes at l0, so at most 128 CTAs of 512
-  // children) go to one launch of merkle_top_kernel.
+  if (top == 0) {  // the cap is the leaf level itself
+    if (!cap) return cudaSuccess;
+    stg.launched();
+    copy_words_kernel<<<grid_for(8 * leaves), kThreads, 0, st>>>(tree, cap, 8 * leaves);
+    return cudaGetLastError();
+  }
+  // Levels with more than 2^18 nodes fill the GPU on their own: one launch
+  // each. The rest (at most 2^18 nodes at l0, so at most 512 CTAs of 512
+  // children, whose roots fit the last CTA's shared memory) go to one launch
+  // of merkle_top_kernel.
   uint32_t level = 0;
-  while (level < top && (leaves >> level) > (1ull << 16)) {
+  while (level < top && (leaves >> level) > (1ull << 18)) {
     uint64_t cnt = leaves >> (level + 1);
     const uint32_t* prev = tree + 8 * (2 * leaves - 2 * (leaves >> level));
     uint32_t* next = tree + 8 * (2 * leaves - 2 * (leaves >> (level + 1)));
     stg.launched();
-    merkle_level_kernel<<<grid_for(cnt), kThreads, 0, st>>>(prev, next, cnt);
+    merkle_level_kernel<<<grid_for(cnt), kThreads, 0, st>>>(prev, next, cnt,
+                                                            level + 1 == top ? cap : nullptr);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     level++;
@@ -1043,10 +1141,8 @@ cudaError_t merkle_build(cudaStream_t st, uint32_t* tree, uint64_t leaves, uint3
   const uint32_t lsub = level + 9 < top ? level + 9 : top;
   const uint64_t per_cta_children = 2ull << (lsub - level - 1);  // level-l0 nodes per CTA
   const uint64_t blocks = ((leaves >> level) + per_cta_children - 1) / per_cta_children;
-  cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(unsigned int), st);
-  if (e != cudaSuccess) return e;
   stg.launched();
-  merkle_top_kernel<<<(unsigned)blocks, kTopThreads, 0, st>>>(tree, leaves, level, top, counter);
+  merkle_top_kernel<<<(unsigned)blocks, kTopThreads, 0, st>>>(tree, leaves, level, top, counter, cap);
   return cudaGetLastError();
 }
 
@@ -1107,15 +1203,14 @@ cudaError_t merkle_flat64_leaves(cudaStream_t st, const uint32_t* flat, uint64_t
 bool grind_supports(uint32_t head_len) { return head_len == 47; }
 
 cudaError_t grind(cudaStream_t st, const uint8_t* head, uint32_t head_len, uint32_t bits,
-                  unsigned long long* state, uint64_t max_nonces) {
+                  unsigned long long* state, unsigned long long* out, uint64_t max_nonces) {
   if (!grind_supports(head_len) || bits > 32) return cudaErrorInvalidValue;
   GrindArgs a;
   for (int i = 0; i < 16; i++) a.head[i] = 0;
   for (uint32_t i = 0; i < head_len; i++) a.head[i / 4] |= (uint32_t)head[i] << (8 * (i % 4));
   a.bits = bits;
-  a.best = state;
-  a.next_chunk = state + 1;
-  a.status = reinterpret_cast<unsigned int*>(state + 2);
+  a.state = state;
+  a.out = out;
   a.max_chunks = (max_nonces + kGrindChunk - 1) / kGrindChunk;
   static int ctas = 0;
   if (!ctas) {
@@ -1131,6 +1226,15 @@ cudaError_t grind(cudaStream_t st, const uint8_t* head, uint32_t head_len, uint3
   return cudaGetLastError();
 }
 
+cudaError_t openings(cudaStream_t st, const OpenArgs& a) {
+  if (a.nlayers > kMaxOpenLayers) return cudaErrorInvalidValue;
+  if (!a.nq) return cudaSuccess;
+  Stage stg("gather", st);
+  stg.launched();
+  openings_kernel<<<a.nq, 128, 0, st>>>(a);
+  return cudaGetLastError();
+}
+
 cudaError_t coset_to_natural(cudaStream_t st, const uint32_t* in, uint32_t* out, uint32_t logN,
                              uint32_t logB, uint64_t batch) {
   uint64_t total = batch << (logN + logB);
@@ -1140,20 +1244,6 @@ cudaError_t coset_to_natural(cudaStream_t st, const uint32_t* in, uint32_t* out,
   return cudaGetLastError();
 }
 
-cudaError_t gather16(cudaStream_t st, const uint64_t* addr, void* out, uint32_t n) {
-  if (!n) return cudaSuccess;
-  Stage stg("gather", st);
-  stg.launched();
-  gather16_kernel<<<grid_for(n), kThreads, 0, st>>>(addr, reinterpret_cast<uint4*>(out), n);
-  return cudaGetLastError();
-}
-cudaError_t gather4(cudaStream_t st, const uint64_t* addr, uint32_t* out, uint32_t n) {
-  if (!n) return cudaSuccess;
-  Stage stg("gather", st);
-  stg.launched();
-  gather4_kernel<<<grid_for(n), kThreads, 0, st>>>(addr, out, n);
-  return cudaGetLastError();
-}
 
 }  // namespace launch
 }  // namespace z0p

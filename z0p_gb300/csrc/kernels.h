@@ -70,6 +70,35 @@ struct FoldArgs {
   uint32_t tab[3][4][4];
 };
 
+// Openings of one proof, gathered on the device into one block per query.
+// Block layout (32-bit words): for each non-final FRI layer d, at layer[d].off,
+// the 16 words of the opened quad then steps x 8 words of sibling digests
+// (leaf upward); at trace_off, the trace part: for the AIR, twice (row index,
+// then row index + B) the 16 words A0 B0 .. A7 B7 of the 8-row leaf and
+// tsteps x 8 words of siblings; for the range AIR, the ncol column values of
+// the row then tsteps x 8 words of siblings.
+constexpr uint32_t kMaxOpenLayers = 16;
+struct OpenLayer {
+  const uint32_t* values;  // layer values (Ext4, 4 words each)
+  const uint32_t* tree;    // level-contiguous tree
+  uint64_t leaves;
+  uint32_t steps;          // path length (depth - cap drop)
+  uint32_t off;            // word offset of this layer inside a query block
+};
+struct OpenArgs {
+  const uint64_t* indices;  // nq FRI query indices (layer-0 positions)
+  uint32_t* out;            // nq blocks of `stride` words
+  uint32_t nq, nlayers, stride, trace_off;
+  OpenLayer layer[kMaxOpenLayers];
+  const uint32_t* lde;      // AIR: column A coset-major; range: ncol columns
+  const uint32_t* cb;       // AIR: per-coset linked-column constant
+  const uint32_t* tinv;     // AIR: 1 / (x - w_last), coset-major
+  const uint32_t* ttree;    // trace tree
+  uint64_t tleaves;
+  uint32_t tsteps, logN, logB;
+  uint32_t ncol;            // 0 for the AIR, else the range AIR's column count
+};
+
 // Product table of the Fp4 constant r (canonical coordinates) in the layout
 // e4_mul_tab expects, in Montgomery form.
 void e4_table(const uint32_t r[4], uint32_t T[4][4]);
@@ -103,20 +132,18 @@ cudaError_t coset_zinv(cudaStream_t st, const Tables& tb, uint32_t* zinv, uint32
 cudaError_t air_trace_leaves(cudaStream_t st, const Tables& tb, const uint32_t* lde_a,
                              const uint32_t* cb, uint32_t w_last_m, uint32_t* leaves,
                              uint32_t* tinv, uint32_t logN, uint32_t logB);
-// (A, B) of the AIR trace LDE at natural rows rows[0..n): out[2i], out[2i+1].
-cudaError_t air_rows(cudaStream_t st, const Tables& tb, const uint32_t* lde_a, const uint32_t* cb,
-                     uint32_t w_last_m, uint32_t logN, uint32_t logB, const uint32_t* rows,
-                     uint32_t n, uint32_t* out);
 cudaError_t range_trace_leaves(cudaStream_t st, const uint32_t* lde, uint32_t* leaves,
                                uint32_t logN, uint32_t logB, uint32_t ncols);
 // Builds levels 1..top of a tree stored level-contiguous (level l at digest
 // offset 2L - 2(L >> l), L = leaves, power of two). Levels above the cap
 // level are never read (caps and capped paths stop there), so callers pass
 // top = depth - drop.
-// `counter` is one device word of scratch (the upper levels are finished by
-// the last CTA to arrive; nothing waits).
+// `counter` is one device word, zero before the call and zero again after it
+// (the upper levels are finished by the last CTA to arrive; nothing waits).
+// `cap` (may be null; device-visible, e.g. mapped host memory) receives a copy
+// of level `top`, 32 bytes per node.
 cudaError_t merkle_build(cudaStream_t st, uint32_t* tree, uint64_t leaves, uint32_t top,
-                         unsigned int* counter);
+                         unsigned int* counter, uint32_t* cap);
 cudaError_t air_compose_leaves(cudaStream_t st, const Tables& tb, const AirComposeArgs& a);
 cudaError_t range_compose_leaves(cudaStream_t st, const Tables& tb, const RangeComposeArgs& a);
 // Folds one FRI layer; hashes the next layer's 64-byte leaves when it has a
@@ -126,18 +153,16 @@ cudaError_t fri_fold(cudaStream_t st, const Tables& tb, const FoldArgs& a);
 cudaError_t layer_leaves(cudaStream_t st, const uint32_t* values, uint64_t len, uint32_t* leaves);
 cudaError_t merkle_flat64_leaves(cudaStream_t st, const uint32_t* flat, uint64_t nleaves,
                                  uint32_t* leaves);
-// Minimum-nonce proof-of-work search; `state` is 3 device words of scratch:
-// best (u64), next chunk (u64), status (u32, 1 = iteration cap reached).
+// Minimum-nonce proof-of-work search. `state` is 4 device u64s holding
+// {~0, 0, 0, 0} before the call and again after it; `out` (device-visible)
+// receives {best nonce, status}, status 1 when the nonce cap was reached.
 cudaError_t grind(cudaStream_t st, const uint8_t* head, uint32_t head_len, uint32_t bits,
-                  unsigned long long* state, uint64_t max_nonces);
+                  unsigned long long* state, unsigned long long* out, uint64_t max_nonces);
 bool grind_supports(uint32_t head_len);
 // Reorders `batch` coset-major LDEs ([j][q]) into natural order ([B q + j]).
 cudaError_t coset_to_natural(cudaStream_t st, const uint32_t* in, uint32_t* out, uint32_t logN,
                              uint32_t logB, uint64_t batch);
-// out[i] = 16 bytes at device address addr[i].
-cudaError_t gather16(cudaStream_t st, const uint64_t* addr, void* out, uint32_t n);
-// out[i] = 4 bytes at device address addr[i].
-cudaError_t gather4(cudaStream_t st, const uint64_t* addr, uint32_t* out, uint32_t n);
+cudaError_t openings(cudaStream_t st, const OpenArgs& a);
 
 }  // namespace launch
 }  // namespace z0p

@@ -22,6 +22,8 @@
 
 namespace {
 
+constexpr size_t kKeepBytes = 512ull << 20;  // workspace an idle worker may keep
+
 struct Pending {
   z0p_job* job;
   uint64_t ticket;
@@ -81,6 +83,10 @@ void worker(z0p_gpu_pool* p, z0p_gpu_ctx* ctx) {
       rc = z0p_gpu_air_prove(ctx, &j->air, j->transcript, j->out, j->cap, &j->len);
     else
       rc = z0p_gpu_range_prove(ctx, &j->range, j->transcript, j->out, j->cap, &j->len);
+    // A context that just held a large job gives its workspace back to the
+    // device pool, so memory held by idle workers stays small next to the
+    // admission budget.
+    if (z0p_gpu_ctx_device_bytes(ctx) > kKeepBytes) z0p_gpu_ctx_trim(ctx);
     {
       std::lock_guard<std::mutex> lk(p->mu);
       j->status = rc;

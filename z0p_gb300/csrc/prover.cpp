@@ -80,21 +80,6 @@ struct Writer {
   }
 };
 
-// Host-built list of device addresses to fetch in one gather.
-struct Gather {
-  std::vector<uint64_t> a16;  // 16-byte granules
-  std::vector<uint64_t> a4;   // 4-byte words
-  size_t add16(const void* p, size_t granules) {
-    size_t at = a16.size();
-    for (size_t i = 0; i < granules; i++) a16.push_back((uint64_t)p + 16 * i);
-    return at;
-  }
-  size_t add4(const void* p) {
-    a4.push_back((uint64_t)p);
-    return a4.size() - 1;
-  }
-};
-
 }  // namespace
 
 // Per-stage CUDA-event timing on the launching stream (diagnostic mode).
@@ -138,9 +123,13 @@ struct z0p_gpu_ctx {
   cudaStream_t stream = nullptr;
   std::mutex mu;
   Tables tb{};
-  DevBuf tables, cols, coeffs, scratch, lde, ttree, layers, ftrees, misc, gaddr, gout;
-  uint8_t* pinned = nullptr;
-  size_t pinned_bytes = 0;
+  DevBuf tables, cols, coeffs, scratch, lde, ttree, layers, ftrees, misc, state;
+  // Mapped pinned buffer for what a proof hands to the host (caps, final
+  // layer, PoW result, query indices, openings): kernels write it directly,
+  // so no copy operation is queued for them.
+  uint8_t* hio = nullptr;
+  uint8_t* hio_d = nullptr;  // its device address
+  size_t hio_bytes = 0;
   size_t held = 0;
   uint64_t h2d = 0, d2h = 0, syncs = 0, proofs = 0, sync_ns = 0, prove_ns = 0;
   bool profiling = false;
@@ -156,10 +145,6 @@ using HostSite = z0p_gpu_ctx::HostSite;
 
 namespace {
 
-cudaError_t h2d(z0p_gpu_ctx* c, void* dst, const void* src, size_t n) {
-  c->h2d += n;
-  return cudaMemcpyAsync(dst, src, n, cudaMemcpyHostToDevice, c->stream);
-}
 cudaError_t d2h(z0p_gpu_ctx* c, void* dst, const void* src, size_t n) {
   c->d2h += n;
   return cudaMemcpyAsync(dst, src, n, cudaMemcpyDeviceToHost, c->stream);
@@ -189,32 +174,72 @@ cudaError_t sync(z0p_gpu_ctx* c, const char* site = "other") {
   return e;
 }
 
+// Workspace comes from one stream-ordered memory pool per device that keeps
+// freed memory for reuse: growing or releasing a context's buffers is queued
+// on its own stream and never synchronises the device, so contexts proving
+// side by side do not stall one another.
+cudaError_t device_pool(int device, cudaMemPool_t* out) {
+  static std::mutex mu;
+  static std::map<int, cudaMemPool_t> pools;
+  std::lock_guard<std::mutex> lk(mu);
+  auto it = pools.find(device);
+  if (it != pools.end()) {
+    *out = it->second;
+    return cudaSuccess;
+  }
+  cudaMemPoolProps props{};
+  props.allocType = cudaMemAllocationTypePinned;
+  props.handleTypes = cudaMemHandleTypeNone;
+  props.location.type = cudaMemLocationTypeDevice;
+  props.location.id = device;
+  cudaMemPool_t pool;
+  cudaError_t e = cudaMemPoolCreate(&pool, &props);
+  if (e != cudaSuccess) return e;
+  uint64_t keep = UINT64_MAX;
+  e = cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  if (e != cudaSuccess) return e;
+  pools[device] = pool;
+  *out = pool;
+  return cudaSuccess;
+}
+
+void release(z0p_gpu_ctx* c, DevBuf& b) {
+  if (!b.p) return;
+  cudaFreeAsync(b.p, c->stream);
+  c->held -= b.bytes;
+  b.p = nullptr;
+  b.bytes = 0;
+}
+
 int ensure(z0p_gpu_ctx* c, DevBuf& b, size_t bytes) {
   if (bytes <= b.bytes) return Z0P_OK;
-  if (b.p) {
-    CK(sync(c));
-    CK(cudaFree(b.p));
-    c->held -= b.bytes;
-    b.p = nullptr;
-    b.bytes = 0;
-  }
+  release(c, b);
   size_t want = bytes + bytes / 8;  // headroom so near sizes reuse the buffer
-  CK(cudaMalloc(&b.p, want));
+  cudaMemPool_t pool;
+  CK(device_pool(c->device, &pool));
+  CK(cudaMallocFromPoolAsync(&b.p, want, pool, c->stream));
   b.bytes = want;
   c->held += want;
   return Z0P_OK;
 }
 
-int ensure_pinned(z0p_gpu_ctx* c, size_t bytes) {
-  if (bytes <= c->pinned_bytes) return Z0P_OK;
-  if (c->pinned) {
+int ensure_hio(z0p_gpu_ctx* c, size_t bytes) {
+  if (bytes <= c->hio_bytes) return Z0P_OK;
+  if (c->hio) {
     CK(sync(c));
-    CK(cudaFreeHost(c->pinned));
+    CK(cudaFreeHost(c->hio));
+    c->hio = c->hio_d = nullptr;
+    c->hio_bytes = 0;
   }
-  size_t want = bytes + bytes / 4 + 4096;
-  CK(cudaMallocHost((void**)&c->pinned, want));
-  c->pinned_bytes = want;
+  size_t want = bytes + bytes / 4 < (4u << 20) ? (4u << 20) : bytes + bytes / 4;
+  CK(cudaHostAlloc((void**)&c->hio, want, cudaHostAllocMapped));
+  CK(cudaHostGetDevicePointer((void**)&c->hio_d, c->hio, 0));
+  c->hio_bytes = want;
   return Z0P_OK;
+}
+template <class T>
+T* hio_dev(z0p_gpu_ctx* c, size_t off) {
+  return reinterpret_cast<T*>(c->hio_d + off);
 }
 
 int build_tables(z0p_gpu_ctx* c) {
@@ -236,7 +261,8 @@ int build_tables(z0p_gpu_ctx* c) {
   x = 1;
   for (int i = 0; i < hi_g; i++) { g_hi[i] = to_mont(x); x = fmul(x, step); }
   RC(ensure(c, c->tables, t.size() * 4));
-  CK(cudaMemcpy(c->tables.p, t.data(), t.size() * 4, cudaMemcpyHostToDevice));
+  CK(cudaMemcpyAsync(c->tables.p, t.data(), t.size() * 4, cudaMemcpyHostToDevice, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
   const uint32_t* d = (const uint32_t*)c->tables.p;
   c->tb.w_lo = d;
   c->tb.w_hi = d + lo_w;
@@ -247,9 +273,11 @@ int build_tables(z0p_gpu_ctx* c) {
 
 inline uint64_t tree_digests(uint64_t leaves) { return 2 * leaves - 1; }
 
-// Device word counting finished CTAs in the Merkle top-level kernel (bytes
-// 32..35 of the context's misc buffer; the PoW state uses bytes 0..23).
-inline unsigned int* sync_words(z0p_gpu_ctx* c) { return (unsigned int*)c->misc.p + 8; }
+// Device counters that kernels leave as they found them, set once when the
+// context is created: the Merkle last-CTA counter (bytes 0..3) and the PoW
+// search state (bytes 8..39).
+inline unsigned int* merkle_counter(z0p_gpu_ctx* c) { return (unsigned int*)c->state.p; }
+inline unsigned long long* grind_state(z0p_gpu_ctx* c) { return (unsigned long long*)c->state.p + 1; }
 
 
 inline uint64_t level_off(uint64_t leaves, uint32_t l) { return 2 * leaves - 2 * (leaves >> l); }
@@ -289,53 +317,76 @@ int plan_fri_buffers(z0p_gpu_ctx* c, const FriShape& s, FriBufs* fb) {
   return Z0P_OK;
 }
 
-// Copies a tree's cap level to the host.
-int fetch_cap(z0p_gpu_ctx* c, const uint32_t* tree, uint64_t leaves, uint32_t drop,
-              std::vector<uint8_t>* out) {
-  uint32_t depth = log2u(leaves);
-  uint64_t n = 1ull << drop;
-  out->resize(32 * n);
-  RC(ensure_pinned(c, 32 * n));
-  CK(d2h(c, c->pinned, tree + 8 * level_off(leaves, depth - drop), 32 * n));
-  CK(sync(c, "cap"));
-  std::memcpy(out->data(), c->pinned, 32 * n);
-  return Z0P_OK;
+// Where a proof's host-visible pieces land in the context's mapped buffer:
+// the trace cap and each FRI layer's cap (written by the tree kernels), the
+// final layer, the PoW result, the query indices (written by the host) and
+// one opening block per query (written by the openings kernel; layout in
+// kernels.h, OpenArgs).
+struct HioPlan {
+  size_t trace_cap = 0;
+  std::vector<size_t> fri_cap;
+  size_t final_vals = 0, grind = 0, indices = 0, open = 0, extra = 0;
+  uint32_t stride = 0, trace_off = 0;  // opening block, in words
+  std::vector<uint32_t> layer_off;     // per non-final FRI layer, in words
+};
+
+int plan_hio(z0p_gpu_ctx* c, const FriShape& s, uint64_t queries, uint32_t tdrop,
+             uint32_t trace_words, HioPlan* h, size_t extra_bytes = 0) {
+  size_t at = 0;
+  auto take = [&](size_t bytes) {
+    size_t r = at;
+    at += (bytes + 15) & ~(size_t)15;
+    return r;
+  };
+  h->trace_cap = take(32ull << tdrop);
+  h->fri_cap.clear();
+  for (size_t l = 0; l < s.len.size(); l++) h->fri_cap.push_back(take(32ull << s.drop[l]));
+  h->final_vals = take(16 * s.len.back());
+  h->grind = take(16);
+  h->indices = take(8 * queries);
+  size_t L = s.len.size() - 1;
+  if (L > kMaxOpenLayers) {
+    set_reason("more FRI layers than the openings kernel supports");
+    return Z0P_ERR_UNSUPPORTED;
+  }
+  h->layer_off.clear();
+  uint32_t w = 0;
+  for (size_t d = 0; d < L; d++) {
+    h->layer_off.push_back(w);
+    w += 16 + 8 * (s.depth[d] - s.drop[d]);
+  }
+  h->trace_off = w;
+  h->stride = (w + trace_words + 3) & ~3u;
+  h->open = take(4ull * h->stride * queries);
+  h->extra = take(extra_bytes);  // small per-proof inputs read by kernels in place
+  return ensure_hio(c, at);
 }
 
 int run_fri(z0p_gpu_ctx* c, const FriShape& s, const FriParams& fp, const FriBufs& fb,
-            uint64_t poly_len, uint64_t degree_bound, Transcript& ts, FriOut* out,
-            bool dims_absorbed) {
-  if (!dims_absorbed) {
-    uint8_t dims[24];  // src/fri.rs:1450-1456
-    for (int i = 0; i < 8; i++) {
-      dims[i] = (uint8_t)(s.m >> (8 * i));
-      dims[8 + i] = (uint8_t)(poly_len >> (8 * i));
-      dims[16 + i] = (uint8_t)(degree_bound >> (8 * i));
-    }
-    transcript_absorb(ts, "fri-dims", dims, 24);
+            uint64_t poly_len, uint64_t degree_bound, Transcript& ts, const HioPlan& h,
+            FriOut* out) {
+  uint8_t dims[24];  // src/fri.rs:1450-1456
+  for (int i = 0; i < 8; i++) {
+    dims[i] = (uint8_t)(s.m >> (8 * i));
+    dims[8 + i] = (uint8_t)(poly_len >> (8 * i));
+    dims[16 + i] = (uint8_t)(degree_bound >> (8 * i));
   }
+  transcript_absorb(ts, "fri-dims", dims, 24);
   const uint32_t unit_m = to_mont(two_adic_generator(2));
   out->caps.assign(s.len.size(), {});
   const uint64_t fl = s.len.back();
-  out->final_vals.resize(4 * fl);
   for (size_t l = 0;; l++) {
-    if (l + 1 == s.len.size()) {
-      // Last layer: its cap and its values (sent in the clear) in one trip.
-      uint32_t depth = log2u(s.leaves[l]);
-      uint64_t n = 1ull << s.drop[l];
-      out->caps[l].resize(32 * n);
-      RC(ensure_pinned(c, 32 * n + 16 * fl));
-      CK(d2h(c, c->pinned, fb.tree[l] + 8 * level_off(s.leaves[l], depth - s.drop[l]), 32 * n));
-      CK(d2h(c, c->pinned + 32 * n, fb.layer.back(), 16 * fl));
-      CK(sync(c, "cap+final"));
-      std::memcpy(out->caps[l].data(), c->pinned, 32 * n);
-      std::memcpy(out->final_vals.data(), c->pinned + 32 * n, 16 * fl);
-    } else {
-      RC(fetch_cap(c, fb.tree[l], s.leaves[l], s.drop[l], &out->caps[l]));
-    }
+    const bool last = l + 1 == s.len.size();
+    // The layer's cap is already in the mapped buffer once its tree is done;
+    // the last layer's values (sent in the clear) come back in the same trip.
+    if (last) CK(d2h(c, c->hio + h.final_vals, fb.layer.back(), 16 * fl));
+    CK(sync(c, last ? "cap+final" : "cap"));
+    const uint8_t* cap = c->hio + h.fri_cap[l];
+    out->caps[l].assign(cap, cap + (32ull << s.drop[l]));
+    c->d2h += 32ull << s.drop[l];  // written by the tree kernel into the mapped buffer
     for (size_t k = 0; k < out->caps[l].size() / 32; k++)
       transcript_absorb(ts, "fri-layer-root", out->caps[l].data() + 32 * k, 32);
-    if (l + 1 == s.len.size()) break;
+    if (last) break;
     FoldArgs fa;
     uint32_t ch[3][4];
     for (int k = 0; k < 3; k++) challenge_ext(ts, "fri-fold", ch[k]);
@@ -356,25 +407,23 @@ int run_fri(z0p_gpu_ctx* c, const FriShape& s, const FriParams& fp, const FriBuf
     fa.unit_m = unit_m;
     CK(launch::fri_fold(c->stream, c->tb, fa));
     CK(launch::merkle_build(c->stream, fb.tree[l + 1], s.leaves[l + 1], s.depth[l + 1] - s.drop[l + 1],
-                            sync_words(c)));
+                            merkle_counter(c), hio_dev<uint32_t>(c, h.fri_cap[l + 1])));
   }
   // Final layer in the clear (src/fri.rs:620-621).
+  out->final_vals.resize(4 * fl);
+  std::memcpy(out->final_vals.data(), c->hio + h.final_vals, 16 * fl);
   transcript_absorb(ts, "fri-final", (const uint8_t*)out->final_vals.data(), 16 * fl);
   // Proof of work (src/fri.rs:645-650, src/transcript.rs:206-228).
   out->nonce = 0;
   if (fp.grinding_bits > 0) {
     std::vector<uint8_t> head = pow_head(ts, "fri-pow");
-    RC(ensure(c, c->misc, 64));
-    unsigned long long init[3] = {~0ull, 0ull, 0ull};
-    CK(h2d(c, c->misc.p, init, sizeof init));
     CK(launch::grind(c->stream, head.data(), (uint32_t)head.size(), fp.grinding_bits,
-                     (unsigned long long*)c->misc.p, 1ull << 40));
-    RC(ensure_pinned(c, 24));
-    CK(d2h(c, c->pinned, c->misc.p, 24));
+                     grind_state(c), hio_dev<unsigned long long>(c, h.grind), 1ull << 40));
     CK(sync(c, "grind"));
-    unsigned long long res[3];
-    std::memcpy(res, c->pinned, 24);
-    if ((res[2] & 0xffffffffull) != 0 || res[0] == ~0ull) {
+    unsigned long long res[2];
+    std::memcpy(res, c->hio + h.grind, 16);
+    c->d2h += 16;
+    if (res[1] != 0 || res[0] == ~0ull) {
       set_reason("proof-of-work search reached its nonce cap without a solution");
       return Z0P_ERR_DEVICE_TIMEOUT;
     }
@@ -388,68 +437,25 @@ int run_fri(z0p_gpu_ctx* c, const FriShape& s, const FriParams& fp, const FriBuf
   return Z0P_OK;
 }
 
-// Queues the FRI openings (src/fri.rs:1229-1260) of every query: the four
-// quad values and the capped path of each non-final layer.
-struct FriOpenRefs {
-  std::vector<size_t> vals;   // per (query, depth): gather16 offset of 4 granules
-  std::vector<size_t> paths;  // per (query, depth): gather16 offset of path digests
-};
-
-void queue_fri_openings(const FriShape& s, const FriBufs& fb, const FriOut& fo, Gather* g,
-                        FriOpenRefs* r) {
-  size_t L = s.len.size() - 1;
-  for (size_t qi = 0; qi < fo.indices.size(); qi++) {
-    uint64_t index = fo.indices[qi];
-    for (size_t d = 0; d < L; d++) {
-      uint64_t base = index / 4 * 4;
-      r->vals.push_back(g->add16(fb.layer[d] + 4 * base, 4));
-      uint64_t Q = base / 4;
-      r->paths.push_back(g->a16.size());
-      uint32_t steps = s.depth[d] - s.drop[d];
-      for (uint32_t st = 0; st < steps; st++) {
-        uint64_t sib = (Q >> st) ^ 1;
-        g->add16(fb.tree[d] + 8 * (level_off(s.leaves[d], st) + sib), 2);
-      }
-      index /= 4;
-    }
-  }
-}
-
-// Fetches every queued granule/word in one round trip. With `rows`, a row
-// kernel also runs (rows in, 2 words per row out) and its output is appended
-// to out4 after the gathered words.
-template <typename RowFn>
-int run_gather(z0p_gpu_ctx* c, const Gather& g, std::vector<uint8_t>* out16,
-               std::vector<uint32_t>* out4, const std::vector<uint32_t>* rows, RowFn row_fn) {
-  size_t n16 = g.a16.size(), n4 = g.a4.size(), nr = rows ? rows->size() : 0;
-  size_t addr_bytes = 8 * (n16 + n4) + 4 * nr;
-  size_t out_bytes = 16 * n16 + 4 * n4 + 8 * nr;
-  RC(ensure(c, c->gaddr, addr_bytes + 16));
-  RC(ensure(c, c->gout, out_bytes + 16));
-  RC(ensure_pinned(c, addr_bytes > out_bytes ? addr_bytes : out_bytes));
-  std::memcpy(c->pinned, g.a16.data(), 8 * n16);
-  std::memcpy(c->pinned + 8 * n16, g.a4.data(), 8 * n4);
-  if (nr) std::memcpy(c->pinned + 8 * (n16 + n4), rows->data(), 4 * nr);
-  CK(h2d(c, c->gaddr.p, c->pinned, addr_bytes));
-  uint64_t* da = (uint64_t*)c->gaddr.p;
-  uint8_t* dout = (uint8_t*)c->gout.p;
-  CK(launch::gather16(c->stream, da, dout, (uint32_t)n16));
-  CK(launch::gather4(c->stream, da + n16, (uint32_t*)(dout + 16 * n16), (uint32_t)n4));
-  if (nr)
-    CK(row_fn((const uint32_t*)(da + n16 + n4), (uint32_t)nr,
-              (uint32_t*)(dout + 16 * n16 + 4 * n4)));
-  CK(d2h(c, c->pinned, dout, out_bytes));
+// Gathers every opening of the proof on the device (kernels.h, OpenArgs)
+// into the mapped buffer; `oa` arrives with its trace fields set.
+int run_openings(z0p_gpu_ctx* c, const FriShape& s, const FriBufs& fb, const HioPlan& h,
+                 const FriOut& fo, OpenArgs& oa) {
+  std::memcpy(c->hio + h.indices, fo.indices.data(), 8 * fo.indices.size());
+  oa.indices = hio_dev<uint64_t>(c, h.indices);
+  oa.out = hio_dev<uint32_t>(c, h.open);
+  oa.nq = (uint32_t)fo.indices.size();
+  oa.nlayers = (uint32_t)(s.len.size() - 1);
+  oa.stride = h.stride;
+  oa.trace_off = h.trace_off;
+  for (uint32_t d = 0; d < oa.nlayers; d++)
+    oa.layer[d] = OpenLayer{fb.layer[d], fb.tree[d], s.leaves[d], s.depth[d] - s.drop[d],
+                            h.layer_off[d]};
+  CK(launch::openings(c->stream, oa));
   CK(sync(c, "openings"));
-  out16->assign(c->pinned, c->pinned + 16 * n16);
-  out4->resize(n4 + 2 * nr);
-  std::memcpy(out4->data(), c->pinned + 16 * n16, 4 * n4 + 8 * nr);
+  c->h2d += 8 * fo.indices.size();                      // indices read in place
+  c->d2h += 4ull * h.stride * fo.indices.size();        // opening blocks
   return Z0P_OK;
-}
-
-int run_gather(z0p_gpu_ctx* c, const Gather& g, std::vector<uint8_t>* out16,
-               std::vector<uint32_t>* out4) {
-  return run_gather(c, g, out16, out4, nullptr,
-                    [](const uint32_t*, uint32_t, uint32_t*) { return cudaSuccess; });
 }
 
 void write_path(Writer& w, const uint8_t* digests, uint64_t leaf, uint32_t steps) {
@@ -460,8 +466,12 @@ void write_path(Writer& w, const uint8_t* digests, uint64_t leaf, uint32_t steps
   }
 }
 
-void write_fri(Writer& w, const FriShape& s, const FriOut& fo, uint64_t poly_len,
-               uint64_t degree_bound, const std::vector<uint8_t>& g16, const FriOpenRefs& r) {
+const uint32_t* open_block(z0p_gpu_ctx* c, const HioPlan& h, size_t qi) {
+  return reinterpret_cast<const uint32_t*>(c->hio + h.open) + (size_t)h.stride * qi;
+}
+
+void write_fri(Writer& w, z0p_gpu_ctx* c, const FriShape& s, const FriOut& fo, uint64_t poly_len,
+               uint64_t degree_bound, const HioPlan& h) {
   w.u64(s.m);  // Commitment::write_body (src/fri.rs:896-904)
   w.u64(poly_len);
   w.u64(degree_bound);
@@ -474,13 +484,15 @@ void write_fri(Writer& w, const FriShape& s, const FriOut& fo, uint64_t poly_len
   w.bytes(fo.final_vals.data(), 4 * fo.final_vals.size());
   w.u64(fo.nonce);
   w.u32((uint32_t)fo.indices.size());
-  size_t L = s.len.size() - 1, k = 0;
+  size_t L = s.len.size() - 1;
   for (size_t qi = 0; qi < fo.indices.size(); qi++) {
+    const uint32_t* blk = open_block(c, h, qi);
     w.u32((uint32_t)L);
     uint64_t index = fo.indices[qi];
-    for (size_t d = 0; d < L; d++, k++) {
-      w.bytes(g16.data() + 16 * r.vals[k], 64);
-      write_path(w, g16.data() + 16 * r.paths[k], index / 4, s.depth[d] - s.drop[d]);
+    for (size_t d = 0; d < L; d++) {
+      const uint32_t* at = blk + h.layer_off[d];
+      w.bytes(at, 64);
+      write_path(w, (const uint8_t*)(at + 16), index / 4, s.depth[d] - s.drop[d]);
       index /= 4;
     }
   }
@@ -610,11 +622,16 @@ int air_prove(z0p_gpu_ctx* c, const z0p_air_params& p, Transcript& ts, uint8_t* 
   // Joint trace tree over 8-row 64-byte leaves (src/air.rs:520-537).
   uint64_t tleaves = m / 8;
   uint32_t tdepth = log2u(tleaves), tdrop = p.cap_height < tdepth ? (uint32_t)p.cap_height : tdepth;
+  const uint32_t tsteps = tdepth - tdrop;
+  HioPlan h;
+  RC(plan_hio(c, s, p.num_queries, tdrop, 2 * (16 + 8 * tsteps), &h));
   uint32_t* tinv = (uint32_t*)c->scratch.p;  // the NTT's scratch is free from here on
   CK(launch::air_trace_leaves(st, c->tb, lde_a, cb, w_last_m, ttree, tinv, logN, logB));
-  CK(launch::merkle_build(st, ttree, tleaves, tdepth - tdrop, sync_words(c)));
-  std::vector<uint8_t> column_cap;
-  RC(fetch_cap(c, ttree, tleaves, tdrop, &column_cap));
+  CK(launch::merkle_build(st, ttree, tleaves, tsteps, merkle_counter(c),
+                          hio_dev<uint32_t>(c, h.trace_cap)));
+  CK(sync(c, "cap"));
+  std::vector<uint8_t> column_cap(c->hio + h.trace_cap, c->hio + h.trace_cap + (32ull << tdrop));
+  c->d2h += column_cap.size();
   transcript_absorb(ts, "fib/trace", column_cap.data(), column_cap.size());
   uint32_t alpha[5][4];
   for (int k = 0; k < 5; k++) challenge_ext(ts, "fib/alpha", alpha[k]);
@@ -636,56 +653,37 @@ int air_prove(z0p_gpu_ctx* c, const z0p_air_params& p, Transcript& ts, uint8_t* 
     ca.kc[e] = fmul(alpha[0][e], neg_coeff);
   }
   CK(launch::air_compose_leaves(st, c->tb, ca));
-  CK(launch::merkle_build(st, fb.tree[0], s.leaves[0], s.depth[0] - s.drop[0], sync_words(c)));
+  CK(launch::merkle_build(st, fb.tree[0], s.leaves[0], s.depth[0] - s.drop[0], merkle_counter(c),
+                          hio_dev<uint32_t>(c, h.fri_cap[0])));
 
   FriOut fo;
-  RC(run_fri(c, s, fp, fb, m, N - 1, ts, &fo, false));
+  RC(run_fri(c, s, fp, fb, m, N - 1, ts, h, &fo));
 
   // Openings: FRI queries plus the two trace leaves per query (src/air.rs:565-591).
-  Gather g;
-  FriOpenRefs fr;
-  queue_fri_openings(s, fb, fo, &g, &fr);
-  std::vector<uint32_t> rows;  // 8 rows per opened trace leaf, (A, B) computed on the device
-  std::vector<size_t> tpath;
-  uint32_t tsteps = tdepth - tdrop;
-  for (uint64_t leaf : fo.indices) {
-    uint64_t index = brev(leaf, logm);
-    uint64_t shifted = (index + B) % m;
-    for (uint64_t at : {index, shifted}) {
-      uint64_t base = at & ~7ull;
-      for (uint64_t r = 0; r < 8; r++) rows.push_back((uint32_t)(base + r));
-      tpath.push_back(g.a16.size());
-      uint64_t L = base / 8;
-      for (uint32_t sx = 0; sx < tsteps; sx++)
-        g.add16(ttree + 8 * (level_off(tleaves, sx) + ((L >> sx) ^ 1)), 2);
-    }
-  }
-  std::vector<uint8_t> g16;
-  std::vector<uint32_t> g4;
-  RC(run_gather(c, g, &g16, &g4, &rows, [&](const uint32_t* d_rows, uint32_t n, uint32_t* d_out) {
-    return launch::air_rows(st, c->tb, lde_a, cb, w_last_m, logN, logB, d_rows, n, d_out);
-  }));
-  std::vector<size_t> trow;
-  for (size_t i = 0; i < 2 * fo.indices.size(); i++) trow.push_back(g.a4.size() + 16 * i);
+  OpenArgs oa{};
+  oa.lde = lde_a; oa.cb = cb; oa.tinv = tinv;
+  oa.ttree = ttree; oa.tleaves = tleaves; oa.tsteps = tsteps;
+  oa.logN = logN; oa.logB = logB; oa.ncol = 0;
+  RC(run_openings(c, s, fb, h, fo, oa));
 
   Writer w(out, need);  // air::Proof::to_bytes (src/air.rs:262-281)
   w.byte(6);
   w.u32((uint32_t)(column_cap.size() / 32));
   w.bytes(column_cap.data(), column_cap.size());
-  write_fri(w, s, fo, m, N - 1, g16, fr);
+  write_fri(w, c, s, fo, m, N - 1, h);
   w.u32((uint32_t)fo.indices.size());
   for (size_t qi = 0; qi < fo.indices.size(); qi++) {
     uint64_t index = brev(fo.indices[qi], logm);
     uint64_t shifted = (index + B) % m;
-    const uint32_t* rows = g4.data() + trow[2 * qi];
-    const uint32_t* srows = g4.data() + trow[2 * qi + 1];
+    const uint32_t* rows = open_block(c, h, qi) + h.trace_off;  // A0 B0 .. A7 B7, path
+    const uint32_t* srows = rows + 16 + 8 * tsteps;
     w.u64(index);
     w.u32(rows[2 * (index & 7)]);
     w.u32(rows[2 * (index & 7) + 1]);
     w.u32(srows[2 * (shifted & 7)]);
     w.u32(srows[2 * (shifted & 7) + 1]);
-    write_path(w, g16.data() + 16 * tpath[2 * qi], index / 8, tsteps);
-    write_path(w, g16.data() + 16 * tpath[2 * qi + 1], shifted / 8, tsteps);
+    write_path(w, (const uint8_t*)(rows + 16), index / 8, tsteps);
+    write_path(w, (const uint8_t*)(srows + 16), shifted / 8, tsteps);
     w.bytes(rows, 64);
     w.bytes(srows, 64);
   }
@@ -716,7 +714,7 @@ int range_prove(z0p_gpu_ctx* c, const z0p_range_params& p, Transcript& ts, uint8
   RC(ensure(c, c->scratch, 4 * m * ncol));
   RC(ensure(c, c->lde, 4 * m * ncol));
   RC(ensure(c, c->ttree, 32 * tree_digests(m)));
-  RC(ensure(c, c->misc, 64 + 8 * B + 4 * ncol + 16 * (ncol + 1)));
+  RC(ensure(c, c->misc, 64 + 8 * B));
   FriBufs fb;
   RC(plan_fri_buffers(c, s, &fb));
   uint32_t* cols = (uint32_t*)c->cols.p;
@@ -725,17 +723,20 @@ int range_prove(z0p_gpu_ctx* c, const z0p_range_params& p, Transcript& ts, uint8
   uint32_t* ttree = (uint32_t*)c->ttree.p;
   uint32_t* zinv = (uint32_t*)c->misc.p + 16;
   uint32_t* zinv2 = zinv + B;
-  uint32_t* dvals = zinv2 + B;
-  uint32_t* dalpha = dvals + ncol;
+  uint32_t tdepth = logm, tdrop = p.cap_height < tdepth ? (uint32_t)p.cap_height : tdepth;
+  const uint32_t tsteps = tdepth - tdrop;
+  HioPlan h;
+  RC(plan_hio(c, s, p.num_queries, tdrop, (uint32_t)ncol + 8 * tsteps, &h,
+              4 * ncol + 16 * (ncol + 1)));
+  uint32_t* hvals = reinterpret_cast<uint32_t*>(c->hio + h.extra);
+  uint32_t* halpha = hvals + ncol;
+  c->h2d += 4 * ncol + 16 * (ncol + 1);  // column values and alphas, read in place
 
   // build_columns (src/range.rs:316-330): V = value, C_j = bit j of value.
-  std::vector<uint32_t> vals(ncol);
-  vals[0] = p.value;
-  for (uint64_t j = 0; j < p.n_bits; j++) vals[1 + j] = j < 32 ? (p.value >> j) & 1 : 0;
-  RC(ensure_pinned(c, 4 * ncol));
-  std::memcpy(c->pinned, vals.data(), 4 * ncol);
-  CK(h2d(c, dvals, c->pinned, 4 * ncol));
-  CK(launch::fill_constant_columns(st, cols, (uint32_t)N, (uint32_t)ncol, dvals));
+  hvals[0] = p.value;
+  for (uint64_t j = 0; j < p.n_bits; j++) hvals[1 + j] = j < 32 ? (p.value >> j) & 1 : 0;
+  CK(launch::fill_constant_columns(st, cols, (uint32_t)N, (uint32_t)ncol,
+                                   hio_dev<uint32_t>(c, h.extra)));
   NttPlan ip;
   ip.logn = logN; ip.batch = (uint32_t)ncol; ip.inverse = 1; ip.post_gamma = 1;
   CK(launch::ntt(st, c->tb, ip, cols, coeffs, (uint32_t*)c->scratch.p));
@@ -751,64 +752,50 @@ int range_prove(z0p_gpu_ctx* c, const z0p_range_params& p, Transcript& ts, uint8
   lp.logn = logN; lp.batch = (uint32_t)(ncol * B); lp.in_div = (uint32_t)B; lp.twist_mod = (uint32_t)B;
   lp.twist_shift = 27 - logm;
   CK(launch::ntt(st, c->tb, lp, coeffs, lde, (uint32_t*)c->scratch.p));
-  uint32_t tdepth = logm, tdrop = p.cap_height < tdepth ? (uint32_t)p.cap_height : tdepth;
   CK(launch::range_trace_leaves(st, lde, ttree, logN, logB, (uint32_t)ncol));
-  CK(launch::merkle_build(st, ttree, m, tdepth - tdrop, sync_words(c)));
+  CK(launch::merkle_build(st, ttree, m, tsteps, merkle_counter(c), hio_dev<uint32_t>(c, h.trace_cap)));
   CK(launch::coset_zinv(st, c->tb, zinv, zinv2, logB, to_mont(fpow(GENERATOR, N)), nullptr, 0));
-  std::vector<uint8_t> column_cap;
-  RC(fetch_cap(c, ttree, m, tdrop, &column_cap));
+  CK(sync(c, "cap"));
+  std::vector<uint8_t> column_cap(c->hio + h.trace_cap, c->hio + h.trace_cap + (32ull << tdrop));
+  c->d2h += column_cap.size();
   transcript_absorb(ts, "range/column", column_cap.data(), column_cap.size());
-  std::vector<uint32_t> alphas(4 * (ncol + 1));
   for (uint64_t k = 0; k < ncol + 1; k++) {  // decomposition, n_bits booleans, boundary
     uint32_t a[4];
     challenge_ext(ts, "range/alpha", a);
-    for (int e = 0; e < 4; e++) alphas[4 * k + e] = to_mont(a[e]);
+    for (int e = 0; e < 4; e++) halpha[4 * k + e] = to_mont(a[e]);
   }
-  RC(ensure_pinned(c, 4 * alphas.size()));
-  std::memcpy(c->pinned, alphas.data(), 4 * alphas.size());
-  CK(h2d(c, dalpha, c->pinned, 4 * alphas.size()));
 
   RangeComposeArgs ca;
-  ca.lde = lde; ca.zinv = zinv; ca.zinv2 = zinv2; ca.alphas = dalpha;
+  ca.lde = lde; ca.zinv = zinv; ca.zinv2 = zinv2;
+  ca.alphas = hio_dev<uint32_t>(c, h.extra) + ncol;
   ca.layer0 = fb.layer[0]; ca.leaves = fb.tree[0];
   ca.logN = logN; ca.logB = logB; ca.n_bits = (uint32_t)p.n_bits; ca.value = p.value;
   CK(launch::range_compose_leaves(st, c->tb, ca));
-  CK(launch::merkle_build(st, fb.tree[0], s.leaves[0], s.depth[0] - s.drop[0], sync_words(c)));
+  CK(launch::merkle_build(st, fb.tree[0], s.leaves[0], s.depth[0] - s.drop[0], merkle_counter(c),
+                          hio_dev<uint32_t>(c, h.fri_cap[0])));
 
   FriOut fo;
-  RC(run_fri(c, s, fp, fb, m, N - 1, ts, &fo, false));
+  RC(run_fri(c, s, fp, fb, m, N - 1, ts, h, &fo));
 
-  Gather g;
-  FriOpenRefs fr;
-  queue_fri_openings(s, fb, fo, &g, &fr);
-  std::vector<size_t> trow, tpath;
-  uint32_t tsteps = tdepth - tdrop;
-  for (uint64_t leaf : fo.indices) {
-    uint64_t index = brev(leaf, logm), j = index & (B - 1), q = index >> logB;
-    trow.push_back(g.a4.size());
-    for (uint64_t col = 0; col < ncol; col++) g.add4(lde + col * m + j * N + q);
-    tpath.push_back(g.a16.size());
-    for (uint32_t sx = 0; sx < tsteps; sx++)
-      g.add16(ttree + 8 * (level_off(m, sx) + ((index >> sx) ^ 1)), 2);
-  }
-  std::vector<uint8_t> g16;
-  std::vector<uint32_t> g4;
-  RC(run_gather(c, g, &g16, &g4));
+  OpenArgs oa{};  // src/range.rs:483-500
+  oa.lde = lde; oa.ttree = ttree; oa.tleaves = m; oa.tsteps = tsteps;
+  oa.logN = logN; oa.logB = logB; oa.ncol = (uint32_t)ncol;
+  RC(run_openings(c, s, fb, h, fo, oa));
 
   Writer w(out, need);  // range::Proof::to_bytes (src/range.rs:253-269)
   w.byte(6);
   w.u32((uint32_t)(column_cap.size() / 32));
   w.bytes(column_cap.data(), column_cap.size());
-  write_fri(w, s, fo, m, N - 1, g16, fr);
+  write_fri(w, c, s, fo, m, N - 1, h);
   w.u32((uint32_t)fo.indices.size());
   for (size_t qi = 0; qi < fo.indices.size(); qi++) {
     uint64_t index = brev(fo.indices[qi], logm);
-    const uint32_t* row = g4.data() + trow[qi];
+    const uint32_t* row = open_block(c, h, qi) + h.trace_off;
     w.u64(index);
     w.u32(row[0]);
     w.u32((uint32_t)p.n_bits);
     for (uint64_t b = 0; b < p.n_bits; b++) w.u32(row[1 + b]);
-    write_path(w, g16.data() + 16 * tpath[qi], index, tsteps);
+    write_path(w, (const uint8_t*)(row + ncol), index, tsteps);
   }
   if (w.n != need) {
     set_reason("internal error: proof length differs from its shape");
@@ -979,6 +966,17 @@ int z0p_gpu_ctx_create(int device, z0p_gpu_ctx** out) {
     return Z0P_ERR_CUDA;
   }
   int rc = build_tables(c);
+  if (rc == Z0P_OK) rc = ensure(c, c->state, 64);
+  if (rc == Z0P_OK) {
+    // Merkle counter 0; PoW state {best = ~0, next chunk 0, status 0, done 0}.
+    uint64_t init[8] = {0, ~0ull, 0, 0, 0, 0, 0, 0};
+    if (cudaMemcpyAsync(c->state.p, init, sizeof init, cudaMemcpyHostToDevice, c->stream) !=
+            cudaSuccess ||
+        cudaStreamSynchronize(c->stream) != cudaSuccess) {
+      set_reason("context creation: state upload failed");
+      rc = Z0P_ERR_CUDA;
+    }
+  }
   if (rc) {
     z0p_gpu_ctx_destroy(c);
     return rc;
@@ -992,11 +990,22 @@ void z0p_gpu_ctx_destroy(z0p_gpu_ctx* c) {
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
   for (DevBuf* b : {&c->tables, &c->cols, &c->coeffs, &c->scratch, &c->lde, &c->ttree, &c->layers,
-                    &c->ftrees, &c->misc, &c->gaddr, &c->gout})
-    if (b->p) cudaFree(b->p);
-  if (c->pinned) cudaFreeHost(c->pinned);
+                    &c->ftrees, &c->misc, &c->state})
+    release(c, *b);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  if (c->hio) cudaFreeHost(c->hio);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
+}
+
+int z0p_gpu_ctx_trim(z0p_gpu_ctx* c) {
+  if (!c) return Z0P_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lk(c->mu);
+  RC(with_device(c));
+  for (DevBuf* b : {&c->cols, &c->coeffs, &c->scratch, &c->lde, &c->ttree, &c->layers, &c->ftrees,
+                    &c->misc})
+    release(c, *b);
+  return Z0P_OK;
 }
 
 void* z0p_gpu_ctx_stream(z0p_gpu_ctx* c) { return c ? (void*)c->stream : nullptr; }
@@ -1158,16 +1167,16 @@ int z0p_gpu_merkle_flat64_cap(z0p_gpu_ctx* c, const uint8_t* d_flat, uint64_t le
   }
   std::lock_guard<std::mutex> lk(c->mu);
   RC(with_device(c));
-  RC(ensure(c, c->misc, 64));
   RC(ensure(c, c->ttree, 32 * tree_digests(leaves)));
   uint32_t* tree = (uint32_t*)c->ttree.p;
-  CK(launch::merkle_flat64_leaves(c->stream, (const uint32_t*)d_flat, leaves, tree));
   uint32_t depth = log2u(leaves), drop = cap_height < depth ? (uint32_t)cap_height : depth;
-  CK(launch::merkle_build(c->stream, tree, leaves, depth - drop, sync_words(c)));
-  std::vector<uint8_t> cap;
-  RC(fetch_cap(c, tree, leaves, drop, &cap));
-  std::memcpy(h_cap, cap.data(), cap.size());
-  *cap_count = cap.size() / 32;
+  RC(ensure_hio(c, 32ull << drop));
+  CK(launch::merkle_flat64_leaves(c->stream, (const uint32_t*)d_flat, leaves, tree));
+  CK(launch::merkle_build(c->stream, tree, leaves, depth - drop, merkle_counter(c),
+                          hio_dev<uint32_t>(c, 0)));
+  CK(sync(c));
+  std::memcpy(h_cap, c->hio, 32ull << drop);
+  *cap_count = 1ull << drop;
   return Z0P_OK;
 }
 
@@ -1213,15 +1222,13 @@ int z0p_gpu_grind(z0p_gpu_ctx* c, const uint8_t* head, size_t head_len, uint32_t
   }
   std::lock_guard<std::mutex> lk(c->mu);
   RC(with_device(c));
-  RC(ensure(c, c->misc, 64));
-  unsigned long long init[3] = {~0ull, 0ull, 0ull};
-  CK(h2d(c, c->misc.p, init, sizeof init));
-  CK(launch::grind(c->stream, head, (uint32_t)head_len, bits, (unsigned long long*)c->misc.p,
-                   1ull << 40));
-  unsigned long long res[3];
-  CK(d2h(c, res, c->misc.p, 24));
+  RC(ensure_hio(c, 16));
+  CK(launch::grind(c->stream, head, (uint32_t)head_len, bits, grind_state(c),
+                   hio_dev<unsigned long long>(c, 0), 1ull << 40));
   CK(sync(c));
-  if ((res[2] & 0xffffffffull) != 0 || res[0] == ~0ull) {
+  unsigned long long res[2];
+  std::memcpy(res, c->hio, 16);
+  if (res[1] != 0 || res[0] == ~0ull) {
     set_reason("proof-of-work search reached its nonce cap without a solution");
     return Z0P_ERR_DEVICE_TIMEOUT;
   }
