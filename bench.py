@@ -221,8 +221,9 @@ def run_batched(Z, ctx, workers=16):
     }
 
 
-def run_served(Z, ctx, rates=(100, 200, 400), requests=120, workers=16, budget=180 << 30):
-    """Poisson arrivals of mixed Fibonacci (2^10..2^22) / range (2^12..2^18) requests."""
+def run_served(Z, ctx, rates=(100, 200, 400, None), requests=120, workers=16, budget=180 << 30):
+    """Poisson arrivals of mixed Fibonacci (2^10..2^22) / range (2^12..2^18) requests.
+    A rate of None submits the whole set at once (saturation)."""
     import random
     import threading
 
@@ -233,7 +234,8 @@ def run_served(Z, ctx, rates=(100, 200, 400), requests=120, workers=16, budget=1
     pool = Pool(ctx.device, workers=workers, hbm_budget=budget)
     out = []
     for ri, rate in enumerate(rates):
-        specs = _mix_params(Z, 0x5EED000000000004 + 977 * ri, (3 * requests) // 4,
+        seed = 0x5EED000000000004 + (977 * ri if rate else 0)  # saturation: the plain run's set
+        specs = _mix_params(Z, seed, (3 * requests) // 4,
                             requests - (3 * requests) // 4, list(range(10, 23)), list(range(12, 19)))
         rng = random.Random(0x5EED0005 + ri)
         steps = sum(n for _, n, _ in specs)
@@ -243,7 +245,8 @@ def run_served(Z, ctx, rates=(100, 200, 400), requests=120, workers=16, budget=1
         def arrive():
             for i, j in enumerate(jobs):
                 tickets[i] = pool.submit(j)
-                time.sleep(rng.expovariate(rate))
+                if rate:
+                    time.sleep(rng.expovariate(rate))
 
         t0 = pool.clock()
         th = threading.Thread(target=arrive)
@@ -253,7 +256,7 @@ def run_served(Z, ctx, rates=(100, 200, 400), requests=120, workers=16, budget=1
             pool.wait(t)
         t1 = max(j.end_s for j in jobs)
         lat = [j.end_s - j.submit_s for j in jobs]
-        out.append({"rate_per_s": rate, "requests": len(jobs), "steps": steps,
+        out.append({"rate_per_s": rate if rate else "saturate", "requests": len(jobs), "steps": steps,
                     "steps_per_s": steps / (t1 - t0),
                     "latency_ms": {"p50": 1e3 * _pct(lat, 0.5), "p99": 1e3 * _pct(lat, 0.99)}})
     pool.close()
@@ -264,10 +267,12 @@ def run_served(Z, ctx, rates=(100, 200, 400), requests=120, workers=16, budget=1
     _, lat = _prove_plain(Z, ctx, specs)
     t_plain = time.perf_counter() - t0
     steps = sum(n for _, n, _ in specs)
+    sat = [r for r in out if r["rate_per_s"] == "saturate"]
     return {"workload": "poisson arrivals; 75% fibonacci 2^10..2^22, 25% range-16 2^12..2^18",
             "workers": workers, "hbm_budget_gb": budget / 2**30, "by_rate": out,
             "plain_one_at_a_time": {"steps_per_s": steps / t_plain,
-                                    "latency_ms": {"p50": 1e3 * _pct(lat, 0.5), "p99": 1e3 * _pct(lat, 0.99)}}}
+                                    "latency_ms": {"p50": 1e3 * _pct(lat, 0.5), "p99": 1e3 * _pct(lat, 0.99)}},
+            "saturated_vs_plain": (sat[0]["steps_per_s"] / (steps / t_plain)) if sat else None}
 
 
 # -------------------------------------------------------------------- arms --

@@ -1212,14 +1212,21 @@ cudaError_t grind(cudaStream_t st, const uint8_t* head, uint32_t head_len, uint3
   a.state = state;
   a.out = out;
   a.max_chunks = (max_nonces + kGrindChunk - 1) / kGrindChunk;
-  static int ctas = 0;
-  if (!ctas) {
-    int dev = 0, sms = 0, per = 0;
+  static int max_ctas = 0, sms = 0;
+  if (!max_ctas) {
+    int dev = 0, per = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, grind_kernel<47>, kGrindThreads, 0);
-    ctas = sms * (per > 0 ? per : 1);
+    max_ctas = sms * (per > 0 ? per : 1);
   }
+  // The search expects 2^bits nonces. Every CTA in flight finishes the chunk
+  // it holds when the minimum is found, so the grid keeps about a quarter of
+  // the expected search in flight (at least one CTA per SM): less work past
+  // the answer, and room for other streams' kernels beside it.
+  uint64_t want = (1ull << bits) / (4 * kGrindChunk);
+  int ctas = want > (uint64_t)max_ctas ? max_ctas : (int)want;
+  if (ctas < sms) ctas = sms;
   Stage stg("grind", st);
   stg.launched();
   grind_kernel<47><<<ctas, kGrindThreads, 0, st>>>(a);
