@@ -279,6 +279,12 @@ int z0p_gpu_merkle_flat64_cap(z0p_gpu_ctx *ctx, const uint8_t *d_flat, uint64_t 
  */
 int z0p_gpu_fri_fold(z0p_gpu_ctx *ctx, const uint32_t *d_in, uint64_t n, uint64_t lde_len,
                      uint64_t depth, const uint32_t ch[12], uint32_t *d_out);
+/* Diagnostic, no counterpart in the reference: the device's BLAKE3
+ * throughput ceiling in G compressions/s, measured with register-resident
+ * chains of Merkle-node hashes (no memory traffic). The hashing stages'
+ * roofline fraction is taken against it. */
+int z0p_gpu_blake3_ceiling(z0p_gpu_ctx *ctx, double *gcompress_per_s);
+
 /*
  * Transcript::grind core (src/transcript.rs:263-281): the smallest nonce
  * whose BLAKE3(head || LE64(nonce)) has >= bits leading zero bits, MSB first.

@@ -36,6 +36,12 @@ class Context:
     def device_bytes(self) -> int:
         return lib().z0p_gpu_ctx_device_bytes(self.handle)
 
+    def blake3_ceiling(self) -> float:
+        """Measured BLAKE3 throughput ceiling of the device, G compressions/s."""
+        g = C.c_double()
+        check(lib().z0p_gpu_blake3_ceiling(self.handle, C.byref(g)))
+        return g.value
+
     def trim(self) -> None:
         """Hand the proof workspace back to the library's device memory pool."""
         check(lib().z0p_gpu_ctx_trim(self.handle))

@@ -344,17 +344,68 @@ __device__ __forceinline__ uint32_t linked_b(const uint32_t* lde_a, uint32_t log
   return fadd(__ldg(lde_a + ((size_t)j << logN) + ((q + 1u) & (N - 1u))), mmul(cbj, inv_den_m));
 }
 
+// ------------------------------------------------------------- subtrees ----
+// Level-contiguous tree offset (level l at digest 2L - 2(L >> l), L leaves).
+__device__ __forceinline__ uint64_t level_offset(uint64_t leaves, uint32_t level) {
+  return 2 * leaves - 2 * (leaves >> level);
+}
+
+// Levels 1..min(log2(nt), top) of the subtree over one CTA's nt consecutive
+// leaves (leaf first + t holds thread t's digest d), hashed in shared memory
+// right where the leaves are made: each node goes to the tree and, at level
+// `top`, to `cap` (as does the leaf itself when top == 0). Every thread of
+// the CTA calls it; nt is a power of two no larger than the CTA, and buf
+// holds 2 * nt * 9 words. Returns the number of levels built.
+__device__ __forceinline__ uint32_t cta_subtree(const uint32_t d[8], uint32_t* buf, uint32_t nt,
+                                                uint64_t first, uint32_t* tree, uint64_t leaves,
+                                                uint32_t top, uint32_t* cap) {
+  const uint32_t t = threadIdx.x;
+  if (t < nt) {
+    if (cap && top == 0) store_digest(cap + 8 * (first + t), d);
+#pragma unroll
+    for (int i = 0; i < 8; i++) buf[9 * t + i] = d[i];
+  }
+  uint32_t levels = 0;
+  while ((2u << levels) <= nt && levels < top) levels++;
+  uint32_t* cur = buf;
+  uint32_t* nxt = buf + 9 * nt;
+  __syncthreads();
+  for (uint32_t l = 1; l <= levels; l++) {
+    const uint32_t per = nt >> l;
+    if (t < per) {
+      uint32_t a[8], b[8], o[8];
+#pragma unroll
+      for (int i = 0; i < 8; i++) { a[i] = cur[18 * t + i]; b[i] = cur[18 * t + 9 + i]; }
+      blake3_node(a, b, o);
+#pragma unroll
+      for (int i = 0; i < 8; i++) nxt[9 * t + i] = o[i];
+      const uint64_t n = (first >> l) + t;
+      store_digest(tree + 8 * (level_offset(leaves, l) + n), o);
+      if (cap && l == top) store_digest(cap + 8 * n, o);
+    }
+    uint32_t* tmp = cur;
+    cur = nxt;
+    nxt = tmp;
+    __syncthreads();
+  }
+  return levels;
+}
+
 // --------------------------------------------------------------- Merkle ----
 // Trace tree leaf L = rows 8L..8L+7 packed A||B (src/air.rs:520-531), hashed
 // as one 64-byte block (src/merkle.rs:93-110). B comes from A (linked_b):
 // eight (x - w_last) inverses per thread in one batch, also stored coset-major
 // in tinv for the composition.
-__global__ void __launch_bounds__(256) air_trace_leaves_kernel(
+constexpr uint32_t kTraceLeafThreads = 256;
+__global__ void __launch_bounds__(kTraceLeafThreads) air_trace_leaves_kernel(
     const uint32_t* __restrict__ lde_a, const uint32_t* __restrict__ cb, uint32_t w_last_m,
     uint32_t* __restrict__ leaves, uint32_t* __restrict__ tinv, uint32_t logN, uint32_t logB,
-    uint32_t nleaves, Tables tb) {
-  uint32_t L = blockIdx.x * blockDim.x + threadIdx.x;
-  if (L >= nleaves) return;
+    uint32_t nleaves, uint32_t top, uint32_t* cap, Tables tb) {
+  __shared__ uint32_t buf[2 * kTraceLeafThreads * 9];
+  const uint32_t nt = nleaves < kTraceLeafThreads ? nleaves : kTraceLeafThreads;
+  const uint32_t L = blockIdx.x * kTraceLeafThreads + threadIdx.x;
+  uint32_t d[8];
+  if (threadIdx.x < nt) {
   const uint32_t logm = logN + logB;
   const uint32_t gamma_m = to_mont(31u);
   uint32_t den[8];
@@ -373,9 +424,10 @@ __global__ void __launch_bounds__(256) air_trace_leaves_kernel(
     m[2 * r + 1] = linked_b(lde_a, logN, j, q, __ldg(cb + j), den[r]);
     tinv[((size_t)j << logN) + q] = den[r];
   }
-  uint32_t d[8];
   blake3_leaf64(m, d);
   store_digest(leaves + 8 * (size_t)L, d);
+  }
+  cta_subtree(d, buf, nt, (uint64_t)blockIdx.x * kTraceLeafThreads, leaves, nleaves, top, cap);
 }
 
 // Range tree leaf k = BLAKE3(0x00 || row k) with the row = ncols LE words
@@ -435,10 +487,6 @@ __global__ void copy_words_kernel(const uint32_t* __restrict__ src, uint32_t* __
                                   uint64_t n) {
   uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) dst[i] = src[i];
-}
-
-__device__ __forceinline__ uint64_t level_offset(uint64_t leaves, uint32_t level) {
-  return 2 * leaves - 2 * (leaves >> level);
 }
 
 // Upper levels of a tree without a grid barrier: CTA b hashes the 2T nodes
@@ -734,12 +782,13 @@ __global__ void __launch_bounds__(kFoldThreads) fri_fold_leaf_kernel(FoldArgs a,
   const uint64_t nleaf = 1ull << (a.logn - 4);
   const uint64_t first = (uint64_t)blockIdx.x * kFoldThreads;
   const uint4* src = reinterpret_cast<const uint4*>(a.in) + first * 16;
-  uint64_t avail = nleaf - first < (uint64_t)kFoldThreads ? nleaf - first : kFoldThreads;
+  const uint32_t avail = nleaf < (uint64_t)kFoldThreads ? (uint32_t)nleaf : (uint32_t)kFoldThreads;
   for (uint32_t e = threadIdx.x; e < avail * 16; e += kFoldThreads)
     sm[(e >> 4) * 17 + (e & 15)] = src[e];
   __syncthreads();
   uint64_t Pn = first + threadIdx.x;
-  if (threadIdx.x >= avail) return;
+  uint32_t d[8];
+  if (threadIdx.x < avail) {
   uint32_t leaf[16];
 #pragma unroll
   for (int t = 0; t < 4; t++) {
@@ -758,9 +807,13 @@ __global__ void __launch_bounds__(kFoldThreads) fri_fold_leaf_kernel(FoldArgs a,
 #pragma unroll
   for (int t = 0; t < 4; t++)
     dst[t] = make_uint4(leaf[4 * t], leaf[4 * t + 1], leaf[4 * t + 2], leaf[4 * t + 3]);
-  uint32_t d[8];
   blake3_leaf64(leaf, d);
   store_digest(a.leaves + 8 * Pn, d);
+  }
+  // The staging buffer is free again: the next layer's subtree over these
+  // leaves is hashed in it (2 * 128 * 9 words fit in 128 * 17 uint4).
+  __syncthreads();
+  cta_subtree(d, reinterpret_cast<uint32_t*>(sm), avail, first, a.leaves, nleaf, a.top, a.cap);
 }
 
 // Thread per next-layer value (small layers; leaves hashed separately).
@@ -871,6 +924,26 @@ __global__ void coset_to_natural_kernel(const uint32_t* __restrict__ in, uint32_
   uint32_t k = (uint32_t)(i & ((1ull << logm) - 1));
   uint32_t j = k & ((1u << logB) - 1u), q = k >> logB;
   out[i] = in[(col << logm) + ((uint64_t)j << logN) + q];
+}
+
+// ------------------------------------------------------- hash ceiling ----
+// Throughput reference for the hashing stages: each thread chains `iters`
+// Merkle-node hashes (two compressions each) in registers, so the kernel is
+// bound by the BLAKE3 arithmetic alone, with no memory traffic.
+__global__ void __launch_bounds__(256) hash_ceiling_kernel(const uint32_t* __restrict__ in,
+                                                           uint32_t* __restrict__ out, int iters) {
+  const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  uint32_t l[8], r[8];
+  load_digest(in + 16 * t, l);
+  load_digest(in + 16 * t + 8, r);
+#pragma unroll 1
+  for (int it = 0; it < iters; it++) {
+    uint32_t o[8];
+    blake3_node(l, r, o);
+#pragma unroll
+    for (int i = 0; i < 8; i++) { l[i] = r[i]; r[i] = o[i]; }
+  }
+  store_digest(out + 8 * t, r);
 }
 
 // ------------------------------------------------------------- openings ----
@@ -998,6 +1071,13 @@ cudaError_t fill_constant_columns(cudaStream_t st, uint32_t* cols, uint32_t n, u
 // True when the pass-`pass` kernel for half-length 2^L has already been
 // allowed `smem` bytes of dynamic shared memory in this process (each kernel's
 // need is fixed by L, so the attribute is set once per kernel, not per launch).
+// Levels cta_subtree builds for a CTA of nt leaves under a tree capped at `top`.
+uint32_t subtree_levels(uint32_t nt, uint32_t top) {
+  uint32_t l = 0;
+  while ((2u << l) <= nt && l < top) l++;
+  return l;
+}
+
 bool smem_raised(int pass, uint32_t L, size_t smem) {
   static std::mutex mu;
   static size_t done[3][32] = {};
@@ -1093,12 +1173,18 @@ cudaError_t coset_zinv(cudaStream_t st, const Tables& tb, uint32_t* zinv, uint32
 
 cudaError_t air_trace_leaves(cudaStream_t st, const Tables& tb, const uint32_t* lde_a,
                              const uint32_t* cb, uint32_t w_last_m, uint32_t* leaves,
-                             uint32_t* tinv, uint32_t logN, uint32_t logB) {
+                             uint32_t* tinv, uint32_t logN, uint32_t logB, uint32_t top,
+                             uint32_t* cap, uint32_t* levels) {
   uint32_t nleaves = 1u << (logN + logB - 3);
+  if (nleaves > kFuseMaxLeaves) {
+    top = 0;  // no subtree; merkle_build does every level
+    cap = nullptr;
+  }
+  *levels = subtree_levels(nleaves < kTraceLeafThreads ? nleaves : kTraceLeafThreads, top);
   Stage stg("trace_leaves", st);
   stg.launched();
-  air_trace_leaves_kernel<<<grid_for(nleaves), kThreads, 0, st>>>(lde_a, cb, w_last_m, leaves, tinv,
-                                                                  logN, logB, nleaves, tb);
+  air_trace_leaves_kernel<<<grid_for(nleaves, kTraceLeafThreads), kTraceLeafThreads, 0, st>>>(
+      lde_a, cb, w_last_m, leaves, tinv, logN, logB, nleaves, top, cap, tb);
   return cudaGetLastError();
 }
 
@@ -1113,7 +1199,8 @@ cudaError_t range_trace_leaves(cudaStream_t st, const uint32_t* lde, uint32_t* l
 }
 
 cudaError_t merkle_build(cudaStream_t st, uint32_t* tree, uint64_t leaves, uint32_t top,
-                         unsigned int* counter, uint32_t* cap) {
+                         unsigned int* counter, uint32_t* cap, uint32_t from) {
+  if (from > 0 && from >= top) return cudaSuccess;  // the leaf kernel built up to the cap
   Stage stg("merkle_levels", st);
   if (top == 0) {  // the cap is the leaf level itself
     if (!cap) return cudaSuccess;
@@ -1125,7 +1212,7 @@ cudaError_t merkle_build(cudaStream_t st, uint32_t* tree, uint64_t leaves, uint3
   // each. The rest (at most 2^18 nodes at l0, so at most 512 CTAs of 512
   // children, whose roots fit the last CTA's shared memory) go to one launch
   // of merkle_top_kernel.
-  uint32_t level = 0;
+  uint32_t level = from;
   while (level < top && (leaves >> level) > (1ull << 18)) {
     uint64_t cnt = leaves >> (level + 1);
     const uint32_t* prev = tree + 8 * (2 * leaves - 2 * (leaves >> level));
@@ -1162,13 +1249,20 @@ cudaError_t range_compose_leaves(cudaStream_t st, const Tables& tb, const RangeC
   return cudaGetLastError();
 }
 
-cudaError_t fri_fold(cudaStream_t st, const Tables& tb, const FoldArgs& a) {
+cudaError_t fri_fold(cudaStream_t st, const Tables& tb, const FoldArgs& a, uint32_t* levels) {
+  *levels = 0;
   if (a.logn < 2) return cudaErrorInvalidValue;
   if (a.logn >= 4) {
     uint64_t nleaf = 1ull << (a.logn - 4);
+    FoldArgs f = a;
+    if (nleaf > kFuseMaxLeaves) {
+      f.top = 0;  // no subtree; merkle_build does every level
+      f.cap = nullptr;
+    }
+    *levels = subtree_levels(nleaf < (uint64_t)kFoldThreads ? (uint32_t)nleaf : kFoldThreads, f.top);
     Stage stg("fri_fold_leaves", st);
     stg.launched();
-    fri_fold_leaf_kernel<<<grid_for(nleaf, kFoldThreads), kFoldThreads, 0, st>>>(a, tb);
+    fri_fold_leaf_kernel<<<grid_for(nleaf, kFoldThreads), kFoldThreads, 0, st>>>(f, tb);
     return cudaGetLastError();
   }
   {
@@ -1230,6 +1324,12 @@ cudaError_t grind(cudaStream_t st, const uint8_t* head, uint32_t head_len, uint3
   Stage stg("grind", st);
   stg.launched();
   grind_kernel<47><<<ctas, kGrindThreads, 0, st>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t hash_ceiling(cudaStream_t st, const uint32_t* in, uint32_t* out, uint32_t blocks,
+                         int iters) {
+  hash_ceiling_kernel<<<blocks, 256, 0, st>>>(in, out, iters);
   return cudaGetLastError();
 }
 

@@ -62,7 +62,9 @@ struct RangeComposeArgs {
 struct FoldArgs {
   const uint32_t* in;  // layer values (4 words each), bit-reversed, length 2^logn
   uint32_t* out;       // next layer, length 2^(logn-2)
-  uint32_t* leaves;    // next layer's leaf digests (fused variant only)
+  uint32_t* leaves;    // next layer's tree (level-contiguous; leaf digests first)
+  uint32_t top = 0;    // the next tree's cap level: subtree levels stop there
+  uint32_t* cap = nullptr;  // receives the cap level when the fold reaches it
   uint32_t logn;
   uint32_t ginv_m;     // (31^(4^depth))^-1 (Montgomery)
   uint32_t unit_m;     // two_adic_generator(2) (Montgomery)
@@ -103,6 +105,13 @@ struct OpenArgs {
 // e4_mul_tab expects, in Montgomery form.
 void e4_table(const uint32_t r[4], uint32_t T[4][4]);
 
+// Leaf kernels (trace leaves, FRI fold) hash their CTA's Merkle subtree only
+// for trees of at most kFuseMaxLeaves leaves: such launches do not fill the
+// GPU, so the shrinking levels' latency is paid either way and the separate
+// level launches are saved. Larger trees keep the flat level kernels, which
+// run the hash at the ALU ceiling where fused levels would leave warps idle.
+constexpr uint64_t kFuseMaxLeaves = 1ull << 15;
+
 namespace launch {
 
 // Number of kernel launches issued by this library in this process.
@@ -129,9 +138,13 @@ cudaError_t coset_zinv(cudaStream_t st, const Tables& tb, uint32_t* zinv, uint32
                        uint32_t logB, uint32_t gamma_n_m, uint32_t* cb, uint32_t coeff);
 // Trace leaves of the AIR: rows 8L..8L+7 as A || B with B derived from A.
 // Also writes tinv (m words, coset-major): 1 / (x - w_last) per LDE row.
+// The kernel also hashes each CTA's subtree (up to the cap level `top`;
+// nodes to the tree, the cap level to `cap`); *levels receives how many
+// levels above the leaves are done, the start level for merkle_build.
 cudaError_t air_trace_leaves(cudaStream_t st, const Tables& tb, const uint32_t* lde_a,
                              const uint32_t* cb, uint32_t w_last_m, uint32_t* leaves,
-                             uint32_t* tinv, uint32_t logN, uint32_t logB);
+                             uint32_t* tinv, uint32_t logN, uint32_t logB, uint32_t top,
+                             uint32_t* cap, uint32_t* levels);
 cudaError_t range_trace_leaves(cudaStream_t st, const uint32_t* lde, uint32_t* leaves,
                                uint32_t logN, uint32_t logB, uint32_t ncols);
 // Builds levels 1..top of a tree stored level-contiguous (level l at digest
@@ -142,13 +155,16 @@ cudaError_t range_trace_leaves(cudaStream_t st, const uint32_t* lde, uint32_t* l
 // (the upper levels are finished by the last CTA to arrive; nothing waits).
 // `cap` (may be null; device-visible, e.g. mapped host memory) receives a copy
 // of level `top`, 32 bytes per node.
+// Levels below `from` must already be built (0: from the leaves).
 cudaError_t merkle_build(cudaStream_t st, uint32_t* tree, uint64_t leaves, uint32_t top,
-                         unsigned int* counter, uint32_t* cap);
+                         unsigned int* counter, uint32_t* cap, uint32_t from = 0);
 cudaError_t air_compose_leaves(cudaStream_t st, const Tables& tb, const AirComposeArgs& a);
 cudaError_t range_compose_leaves(cudaStream_t st, const Tables& tb, const RangeComposeArgs& a);
 // Folds one FRI layer; hashes the next layer's 64-byte leaves when it has a
-// multiple of four values, its 0x00-prefixed 16-byte leaves otherwise.
-cudaError_t fri_fold(cudaStream_t st, const Tables& tb, const FoldArgs& a);
+// multiple of four values, its 0x00-prefixed 16-byte leaves otherwise. With
+// 64-byte leaves it also hashes each CTA's subtree up to a.top (writing the
+// cap level to a.cap); *levels receives the levels done above the leaves.
+cudaError_t fri_fold(cudaStream_t st, const Tables& tb, const FoldArgs& a, uint32_t* levels);
 // Leaf digests of an FRI layer held in memory (64-byte quads or 16-byte values).
 cudaError_t layer_leaves(cudaStream_t st, const uint32_t* values, uint64_t len, uint32_t* leaves);
 cudaError_t merkle_flat64_leaves(cudaStream_t st, const uint32_t* flat, uint64_t nleaves,
@@ -163,6 +179,10 @@ bool grind_supports(uint32_t head_len);
 cudaError_t coset_to_natural(cudaStream_t st, const uint32_t* in, uint32_t* out, uint32_t logN,
                              uint32_t logB, uint64_t batch);
 cudaError_t openings(cudaStream_t st, const OpenArgs& a);
+// blocks x 256 threads, each chaining `iters` node hashes from 16 words of
+// `in` (blocks * 256 * 64 bytes) and writing 8 words of `out`.
+cudaError_t hash_ceiling(cudaStream_t st, const uint32_t* in, uint32_t* out, uint32_t blocks,
+                         int iters);
 
 }  // namespace launch
 }  // namespace z0p

@@ -405,9 +405,18 @@ int run_fri(z0p_gpu_ctx* c, const FriShape& s, const FriParams& fp, const FriBuf
     for (size_t i = 0; i < l; i++) g = fpow(g, 4);
     fa.ginv_m = to_mont(finv(g));
     fa.unit_m = unit_m;
-    CK(launch::fri_fold(c->stream, c->tb, fa));
-    CK(launch::merkle_build(c->stream, fb.tree[l + 1], s.leaves[l + 1], s.depth[l + 1] - s.drop[l + 1],
-                            merkle_counter(c), hio_dev<uint32_t>(c, h.fri_cap[l + 1])));
+    const uint32_t top = s.depth[l + 1] - s.drop[l + 1];
+    fa.top = top;
+    fa.cap = hio_dev<uint32_t>(c, h.fri_cap[l + 1]);
+    uint32_t built = 0;  // subtree levels the fold kernel hashed itself
+    CK(launch::fri_fold(c->stream, c->tb, fa, &built));
+    // Levels above `built` remain, if any. A tree capped at its leaves has
+    // its cap written by the fold only when the fold hashed its subtree (64-
+    // byte leaves, small tree); otherwise merkle_build copies it.
+    const bool fused = s.len[l] >= 16 && s.leaves[l + 1] <= kFuseMaxLeaves;
+    if (built < top || (top == 0 && !fused))
+      CK(launch::merkle_build(c->stream, fb.tree[l + 1], s.leaves[l + 1], top, merkle_counter(c),
+                              fa.cap, built));
   }
   // Final layer in the clear (src/fri.rs:620-621).
   out->final_vals.resize(4 * fl);
@@ -626,9 +635,12 @@ int air_prove(z0p_gpu_ctx* c, const z0p_air_params& p, Transcript& ts, uint8_t* 
   HioPlan h;
   RC(plan_hio(c, s, p.num_queries, tdrop, 2 * (16 + 8 * tsteps), &h));
   uint32_t* tinv = (uint32_t*)c->scratch.p;  // the NTT's scratch is free from here on
-  CK(launch::air_trace_leaves(st, c->tb, lde_a, cb, w_last_m, ttree, tinv, logN, logB));
-  CK(launch::merkle_build(st, ttree, tleaves, tsteps, merkle_counter(c),
-                          hio_dev<uint32_t>(c, h.trace_cap)));
+  uint32_t built = 0;  // subtree levels the leaf kernel hashed itself
+  CK(launch::air_trace_leaves(st, c->tb, lde_a, cb, w_last_m, ttree, tinv, logN, logB, tsteps,
+                              hio_dev<uint32_t>(c, h.trace_cap), &built));
+  if (built < tsteps || (tsteps == 0 && tleaves > kFuseMaxLeaves))
+    CK(launch::merkle_build(st, ttree, tleaves, tsteps, merkle_counter(c),
+                            hio_dev<uint32_t>(c, h.trace_cap), built));
   CK(sync(c, "cap"));
   std::vector<uint8_t> column_cap(c->hio + h.trace_cap, c->hio + h.trace_cap + (32ull << tdrop));
   c->d2h += column_cap.size();
@@ -1204,8 +1216,46 @@ int z0p_gpu_fri_fold(z0p_gpu_ctx* c, const uint32_t* d_in, uint64_t n, uint64_t 
     for (int e = 0; e < 4; e++) q[e] = fmul(ch[4 * k + e] % P, inv4);
     e4_table(q, fa.tab[k]);
   }
-  CK(launch::fri_fold(c->stream, c->tb, fa));
+  uint32_t built = 0;
+  CK(launch::fri_fold(c->stream, c->tb, fa, &built));  // top 0, no cap: leaves only
   CK(sync(c));
+  return Z0P_OK;
+}
+
+int z0p_gpu_blake3_ceiling(z0p_gpu_ctx* c, double* gcompress_per_s) {
+  if (!c || !gcompress_per_s) return Z0P_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lk(c->mu);
+  RC(with_device(c));
+  int sms = 0;
+  CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device));
+  const uint32_t blocks = 8u * (uint32_t)sms;
+  const size_t threads = 256ull * blocks;
+  const int iters = 256;
+  RC(ensure(c, c->scratch, threads * 64 + threads * 32));
+  uint32_t* in = (uint32_t*)c->scratch.p;
+  uint32_t* outp = in + 16 * threads;
+  CK(cudaMemsetAsync(in, 0x5a, threads * 64, c->stream));
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  cudaError_t e = launch::hash_ceiling(c->stream, in, outp, blocks, iters);  // warm-up
+  float best = 0.f;
+  for (int rep = 0; rep < 3 && e == cudaSuccess; rep++) {
+    e = cudaEventRecord(e0, c->stream);
+    if (e == cudaSuccess) e = launch::hash_ceiling(c->stream, in, outp, blocks, iters);
+    if (e == cudaSuccess) e = cudaEventRecord(e1, c->stream);
+    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+    float ms = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+    if (e == cudaSuccess && ms > 0.f) {
+      float g = (float)(2.0 * threads * iters / (ms * 1e-3) / 1e9);
+      if (g > best) best = g;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  CK(e);
+  *gcompress_per_s = best;
   return Z0P_OK;
 }
 
