@@ -29,6 +29,9 @@ P = 2013265921
 LOG_N = 20
 N_STEPS = 1 << LOG_N
 SEED = 0x5EED000000000001
+# The reference's published 2^20-step Fibonacci prove on its 16-core machine:
+# 1,733.55 ms, i.e. 604,872 steps/s (docs/benchmarks.md:30-36).
+PUBLISHED_STEPS_PER_S = 604872.0
 LABEL = b"bench/air-scale"
 METRIC = "proved AIR steps/s (batched vs plain, byte-exact proofs); p50/p99 prove latency"
 
@@ -124,6 +127,16 @@ def measured_peaks():
         return float(d["hbm_gbs"]), "measured"
     except (OSError, KeyError, ValueError):
         return 6800.0, "fallback"
+
+
+def measured_traffic():
+    """Per-stage DRAM bytes per proof from the committed ncu capture of this
+    workload (profiles/dram_traffic_air_prove_2p20.json), or {}."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "dram_traffic_air_prove_2p20.json")) as f:
+            return json.load(f)["stages"]
+    except (OSError, KeyError, ValueError):
+        return {}
 
 
 def stage_work(n, params):
@@ -306,7 +319,8 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": value, "unit": "steps/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1000 * total / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "u32 (BabyBear mod p, BLAKE3 ARX)", "data": "synthetic (seeded)",
+        "vs_baseline": value / PUBLISHED_STEPS_PER_S, "dtype": "u32 (BabyBear mod p, BLAKE3 ARX)",
+        "data": "synthetic (seeded)",
         "config": {"workload": "fibonacci-air prove, 2^20 steps, for_security(100): B16 Q40 G20 C4 F16",
                    "n_steps": N_STEPS, "lde_len": N_STEPS * 16, "proof_bytes": 203553},
         "cpu_baseline": {"value": value, "unit": "steps/s", "cores": cores, "kind": "port",
@@ -457,8 +471,12 @@ def run_gpu(args):
         per_launch_ms = d["ms_per_proof"] / max(d["launches_per_proof"], 1)
         alg = d.get("alg_bytes", 0) / max(d["launches_per_proof"], 1)
         achieved = alg / (per_launch_ms / 1e3) / 1e9 if per_launch_ms > 0 else 0.0
+        traffic = measured_traffic().get(dominant, {}).get("dram_bytes_per_proof")
         roof = {"kernel": dominant, "bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
-                "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": None,
+                "unit": "GB/s", "frac": round(achieved / peak, 4),
+                # ncu dram__bytes_read.sum + dram__bytes_write.sum, per launch like achieved
+                "traffic": (round(traffic / max(d["launches_per_proof"], 1)) if traffic else None),
+                "alg_bytes_per_launch": round(alg),
                 "peak_source": peak_kind}
         if "blake3_compressions" in d:
             # BLAKE3 stages are bound by integer issue, not HBM: their fraction
@@ -473,7 +491,8 @@ def run_gpu(args):
     line = {
         "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "u32 (BabyBear mod p, BLAKE3 ARX)",
+        "scaling": "weak", "vs_baseline": value / PUBLISHED_STEPS_PER_S,
+        "dtype": "u32 (BabyBear mod p, BLAKE3 ARX)",
         "data": "synthetic (seeded splitmix64 initial pair)",
         "config": {"workload": "fibonacci-air prove, 2^20 steps, for_security(100): B16 Q40 G20 C4 F16",
                    "n_steps": N_STEPS, "lde_len": N_STEPS * 16, "proof_bytes": size,
