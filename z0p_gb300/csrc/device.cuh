@@ -20,19 +20,22 @@ constexpr uint32_t kR = 0x0FFFFFFEu;      // 2^32 mod p  (Montgomery one)
 constexpr uint32_t kR2 = 0x45DDDDE3u;     // 2^64 mod p
 constexpr uint32_t k11R = 939524073u;     // 11 * 2^32 mod p (Fp2 non-residue)
 constexpr int kRootBits = 27;             // omega = 31^((p-1)/2^27)
+constexpr uint32_t kOmega4M = 473486609u; // omega_4 = 31^((p-1)/4) = 1728404513, Montgomery form
 constexpr int kWLoBits = 14;
 constexpr int kWHiBits = kRootBits - kWLoBits;
 constexpr int kGLoBits = 12;
 constexpr int kGHiBits = kRootBits - kGLoBits;
 
 
+// Final corrections as an unsigned min: with x < 2p < 2^32, exactly one of
+// x and x - p (or x + p) lies in [0, p), and the other wraps above 2^32 - p.
 __device__ __forceinline__ uint32_t fadd(uint32_t a, uint32_t b) {
   uint32_t s = a + b;
-  return s >= kP ? s - kP : s;
+  return min(s, s - kP);
 }
 __device__ __forceinline__ uint32_t fsub(uint32_t a, uint32_t b) {
   uint32_t d = a - b;
-  return a >= b ? d : d + kP;
+  return min(d, d + kP);
 }
 __device__ __forceinline__ uint32_t fneg(uint32_t a) { return a ? kP - a : 0u; }
 __device__ __forceinline__ uint32_t fhalve(uint32_t a) { return (a + ((a & 1u) ? kP : 0u)) >> 1; }
@@ -44,8 +47,8 @@ __device__ __forceinline__ uint32_t mmul(uint32_t a, uint32_t b) {
   uint32_t hi = __umulhi(a, b);
   uint32_t m = lo * kPInv;
   uint32_t mp = __umulhi(m, kP);
-  uint32_t r = hi - mp;
-  return hi < mp ? r + kP : r;
+  uint32_t r = hi - mp;  // hi, mp < p: r in (-p, p)
+  return min(r, r + kP);
 }
 // (a0 b0 + a1 b1) * 2^-32 mod p for canonical a_i and b_i < p: the sum of
 // the two products is below 2p^2 < p * 2^32, so one signed Montgomery
@@ -56,7 +59,7 @@ __device__ __forceinline__ uint32_t mdot2(uint32_t a0, uint32_t b0, uint32_t a1,
   uint32_t m = lo * kPInv;
   uint32_t mp = __umulhi(m, kP);
   uint32_t r = hi - mp;
-  return hi < mp ? r + kP : r;
+  return min(r, r + kP);
 }
 // Canonical x canonical -> canonical.
 __device__ __forceinline__ uint32_t fmul(uint32_t a, uint32_t b) { return mmul(mmul(a, b), kR2); }

@@ -611,6 +611,17 @@ __global__ void leaf16_kernel(const uint32_t* __restrict__ values, uint32_t* __r
   store_digest(leaves + 8 * i, d);
 }
 
+// The four rows k0 + s m/4 of a layer-0 quad share a coset and sit at
+// x0 omega_4^s: x1 = x0 omega_4, x2 = -x0, x3 = -x1 (omega_4^2 = -1), all in
+// Montgomery form.
+__device__ __forceinline__ void quad_points(const Tables& tb, uint32_t k0, uint32_t logm,
+                                            uint32_t x[4]) {
+  x[0] = mmul(to_mont(31u), root_pow(tb, k0 << (kRootBits - logm)));
+  x[1] = mmul(x[0], kOmega4M);
+  x[2] = fneg(x[0]);
+  x[3] = fneg(x[1]);
+}
+
 // -------------------------------------------------------------- compose ----
 // AIR composition (src/air.rs:847-929 == composition_at :938-962) on the four
 // rows of layer-0 quad P, written bit-reversed as one 64-byte leaf and hashed.
@@ -638,7 +649,8 @@ __global__ void __launch_bounds__(kThreads) air_compose_leaves_kernel(AirCompose
     k0 = u;
   }
   const uint32_t P = brev_bits(k0, logm - 2);
-  const uint32_t gamma_m = to_mont(31u);
+  uint32_t xs[4];
+  quad_points(tb, k0, logm, xs);
   uint32_t leaf[16];
 #pragma unroll
   for (int s = 0; s < 4; s++) {
@@ -653,8 +665,7 @@ __global__ void __launch_bounds__(kThreads) air_compose_leaves_kernel(AirCompose
     const uint32_t t0 = __ldg(a.tinv + base + q);
     const uint32_t tn = __ldg(a.tinv + base + qn);
     const uint32_t cbj = __ldg(a.cb + j);
-    const uint32_t x = mmul(gamma_m, root_pow(tb, k << (kRootBits - logm)));
-    const uint32_t zt = mmul(fsub(x, a.w_last_m), __ldg(a.zinv + j));  // (x - w_last)/Z
+    const uint32_t zt = mmul(fsub(xs[s], a.w_last_m), __ldg(a.zinv + j));  // (x - w_last)/Z
     const uint32_t bv = fadd(avn, mmul(cbj, t0));
     const uint32_t bvn = fadd(avnn, mmul(cbj, tn));
     const uint32_t t2 = mmul(fsub(bvn, fadd(av, bv)), zt);
@@ -694,14 +705,12 @@ __global__ void __launch_bounds__(kThreads) range_compose_leaves_kernel(RangeCom
     k0 = u;
   }
   const uint32_t P = brev_bits(k0, logm - 2);
-  const uint32_t gamma_m = to_mont(31u);
-  uint32_t den[4], kk[4];
+  uint32_t den[4], kk[4], xs[4];
+  quad_points(tb, k0, logm, xs);
 #pragma unroll
   for (int s = 0; s < 4; s++) {
-    uint32_t k = k0 + (uint32_t)s * quarter;
-    kk[s] = k;
-    uint32_t x = mmul(gamma_m, root_pow(tb, k << (kRootBits - logm)));
-    den[s] = fsub(x, kR);
+    kk[s] = k0 + (uint32_t)s * quarter;
+    den[s] = fsub(xs[s], kR);
   }
   batch_minv(den);
   const uint32_t nb = a.n_bits;
@@ -1208,12 +1217,13 @@ cudaError_t merkle_build(cudaStream_t st, uint32_t* tree, uint64_t leaves, uint3
     copy_words_kernel<<<grid_for(8 * leaves), kThreads, 0, st>>>(tree, cap, 8 * leaves);
     return cudaGetLastError();
   }
-  // Levels with more than 2^18 nodes fill the GPU on their own: one launch
-  // each. The rest (at most 2^18 nodes at l0, so at most 512 CTAs of 512
+  // Levels with more than 2^16 nodes fill the GPU on their own: one launch
+  // each. The rest (at most 2^16 nodes at l0, so at most 128 CTAs of 512
   // children, whose roots fit the last CTA's shared memory) go to one launch
-  // of merkle_top_kernel.
+  // of merkle_top_kernel. (Starting the top kernel anywhere from 2^12 to 2^18
+  // nodes measured within 7% on a 2^21-leaf tree; 2^16 was the fastest.)
   uint32_t level = from;
-  while (level < top && (leaves >> level) > (1ull << 18)) {
+  while (level < top && (leaves >> level) > (1ull << 16)) {
     uint64_t cnt = leaves >> (level + 1);
     const uint32_t* prev = tree + 8 * (2 * leaves - 2 * (leaves >> level));
     uint32_t* next = tree + 8 * (2 * leaves - 2 * (leaves >> (level + 1)));
