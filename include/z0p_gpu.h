@@ -265,8 +265,9 @@ int z0p_gpu_rs_extend_noalloc(const uint32_t *d_values, uint64_t n, uint64_t bat
 /*
  * MerkleTree::from_flat64 (src/merkle.rs:93-110) + cap (src/merkle.rs:229-232):
  * builds the BLAKE3 tree over len/64 64-byte leaves of the device buffer
- * d_flat and copies cap level min(cap_height, depth) to the host buffer
- * h_cap (2^drop * 32 bytes; *cap_count receives the digest count).
+ * d_flat, padded to a power of two by duplicating the last leaf
+ * (src/merkle.rs:350-360), and copies cap level min(cap_height, depth) to
+ * the host buffer h_cap (2^drop * 32 bytes; *cap_count receives the count).
  */
 int z0p_gpu_merkle_flat64_cap(z0p_gpu_ctx *ctx, const uint8_t *d_flat, uint64_t len,
                               uint64_t cap_height, uint8_t *h_cap, uint64_t *cap_count);

@@ -175,7 +175,9 @@ def test_merkle_cap_matches_oracle(z0p, oracle, gpu_ctx):
     import numpy as np
 
     rng = np.random.default_rng(11)
-    for leaves, cap_h in [(1, 0), (2, 1), (64, 4), (1 << 12, 4), (1 << 15, 8), (1 << 18, 2)]:
+    # power-of-two and padded (duplicate-last, src/merkle.rs:350-360) leaf counts
+    for leaves, cap_h in [(1, 0), (2, 1), (64, 4), (1 << 12, 4), (1 << 15, 8), (1 << 18, 2),
+                          (3, 1), (5, 4), (1000, 3), (4097, 8), (3 * (1 << 14), 4)]:
         flat = rng.integers(0, 256, size=leaves * 64, dtype=np.uint8)
         d = torch.from_numpy(flat).cuda()
         out = (C.c_uint8 * (32 * 256))()
@@ -185,6 +187,78 @@ def test_merkle_cap_matches_oracle(z0p, oracle, gpu_ctx):
                                                  cap_h, out, C.byref(cnt))
         assert rc == 0
         assert bytes(out)[: 32 * cnt.value] == oracle.merkle_flat64_cap(flat.tobytes(), cap_h), leaves
+
+
+def test_kernel_sweep_shape_matches_oracle(z0p, oracle, gpu_ctx):
+    """The kernel-sweep configuration at reduced n: 64 seeded columns with
+    log2 n uniform in {8..12}; each column's LDE at blowup 16
+    (reed_solomon_extend, src/ntt.rs:436-439); a Merkle cap over each
+    equal-n group's row-major flat buffer (leaf = 16 consecutive limbs,
+    src/merkle.rs:93-110); then the FRI fold chain on each LDE lifted to Fp4
+    and bit-reversed, with seeded challenges, while the degree bound
+    (n - 1) >> 2f is at least 8 (src/fri.rs:1273-1331)."""
+    torch = _torch()
+    import ctypes as C
+    import numpy as np
+
+    P, B = oracle.P, 16
+    state = 0x5EED000000000003
+    groups = {}
+    for _ in range(64):
+        z, state = oracle.splitmix64(state)
+        logn = 8 + z % 5
+        col = np.empty(1 << logn, dtype=np.uint32)
+        for i in range(col.size):
+            z, state = oracle.splitmix64(state)
+            col[i] = z % P
+        groups.setdefault(logn, []).append(col)
+    for logn, cols in sorted(groups.items()):
+        n, k = 1 << logn, len(cols)
+        m = n * B
+        d_in = torch.from_numpy(np.stack(cols).astype(np.int64)).to(torch.int32).cuda()
+        d_lde = torch.empty(k * m, dtype=torch.int32, device="cuda")
+        torch.cuda.synchronize()
+        assert z0p.lib().z0p_gpu_rs_extend(gpu_ctx.handle, C.c_void_p(d_in.data_ptr()), n, k, B,
+                                           C.c_void_p(d_lde.data_ptr())) == 0
+        lde = d_lde.cpu().numpy().view(np.uint32).reshape(k, m)
+        for c in range(k):
+            assert np.array_equal(lde[c], oracle.reed_solomon_extend(cols[c], B)), (logn, c)
+        # Merkle over the row-major flat buffer of the group (k may not be a power of two).
+        flat = np.ascontiguousarray(lde.T).reshape(-1)
+        d_flat = torch.from_numpy(flat.view(np.int32).copy()).cuda()
+        out = (C.c_uint8 * (32 * 256))()
+        cnt = C.c_uint64()
+        torch.cuda.synchronize()
+        assert z0p.lib().z0p_gpu_merkle_flat64_cap(gpu_ctx.handle, C.c_void_p(d_flat.data_ptr()),
+                                                   flat.size * 4, 4, out, C.byref(cnt)) == 0
+        assert bytes(out)[: 32 * cnt.value] == oracle.merkle_flat64_cap(flat.tobytes(), 4), logn
+        # FRI fold chain on the first column of the group.
+        logm = logn + 4
+        omega = oracle.f_pow(31, (P - 1) >> logm)
+        lifted = np.zeros(4 * m, dtype=np.uint32)
+        br = [int(format(i, f"0{logm}b")[::-1], 2) for i in range(m)]
+        lifted[0::4] = lde[0][br]
+        pts = [oracle.f_mul(31, oracle.f_pow(omega, int(format(4 * i, f"0{logm}b")[::-1], 2)))
+               for i in range(m // 4)]
+        cur = lifted
+        d_cur = torch.from_numpy(cur.astype(np.int64)).to(torch.int32).cuda()
+        depth = 0
+        while ((n - 1) >> (2 * depth)) >= 8:
+            ch = []
+            for _ in range(12):
+                z, state = oracle.splitmix64(state)
+                ch.append(z % P)
+            ref, pts = oracle.fold_layer(cur, pts, np.array(ch, dtype=np.uint32))
+            nl = cur.size // 4
+            d_next = torch.empty(nl // 4 * 4, dtype=torch.int32, device="cuda")
+            torch.cuda.synchronize()
+            rc = z0p.lib().z0p_gpu_fri_fold(gpu_ctx.handle, C.c_void_p(d_cur.data_ptr()), nl, m, depth,
+                                            (C.c_uint32 * 12)(*ch), C.c_void_p(d_next.data_ptr()))
+            assert rc == 0
+            got = d_next.cpu().numpy().view(np.uint32)
+            assert np.array_equal(got, ref), (logn, depth)
+            cur, d_cur = ref, d_next
+            depth += 1
 
 
 def test_fri_fold_matches_oracle(z0p, oracle, gpu_ctx):

@@ -61,6 +61,20 @@ __device__ __forceinline__ uint32_t mdot2(uint32_t a0, uint32_t b0, uint32_t a1,
   uint32_t r = hi - mp;
   return min(r, r + kP);
 }
+// (a0 b0 + a1 b1 + a2 b2 + a3 b3) * 2^-32 mod p for a_i, b_i < p: the sum is
+// below 4p^2 < 2^64, so one Montgomery reduction covers the four products.
+// Its high word is below 1.9p; reducing it once first keeps the signed
+// reduction in (-p, p).
+__device__ __forceinline__ uint32_t mdot4(uint32_t a0, uint32_t b0, uint32_t a1, uint32_t b1,
+                                          uint32_t a2, uint32_t b2, uint32_t a3, uint32_t b3) {
+  uint64_t t = (uint64_t)a0 * b0 + (uint64_t)a1 * b1 + (uint64_t)a2 * b2 + (uint64_t)a3 * b3;
+  uint32_t lo = (uint32_t)t, hi = (uint32_t)(t >> 32);
+  hi = min(hi, hi - kP);
+  uint32_t m = lo * kPInv;
+  uint32_t mp = __umulhi(m, kP);
+  uint32_t r = hi - mp;
+  return min(r, r + kP);
+}
 // Canonical x canonical -> canonical.
 __device__ __forceinline__ uint32_t fmul(uint32_t a, uint32_t b) { return mmul(mmul(a, b), kR2); }
 __device__ __forceinline__ uint32_t to_mont(uint32_t a) { return mmul(a, kR2); }
@@ -186,7 +200,7 @@ __device__ __forceinline__ E4 e4_mul_tab(const E4& v, const uint32_t (&T)[4][4])
   E4 r;
 #pragma unroll
   for (int c = 0; c < 4; c++)
-    r.c[c] = fadd(mdot2(v.c[0], T[c][0], v.c[1], T[c][1]), mdot2(v.c[2], T[c][2], v.c[3], T[c][3]));
+    r.c[c] = mdot4(v.c[0], T[c][0], v.c[1], T[c][1], v.c[2], T[c][2], v.c[3], T[c][3]);
   return r;
 }
 

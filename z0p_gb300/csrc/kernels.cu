@@ -583,12 +583,14 @@ __global__ void __launch_bounds__(kTopThreads) merkle_top_kernel(uint32_t* tree,
 
 // 64-byte leaves (four Ext4 values) of an in-memory FRI layer
 // (src/fri.rs:1408-1414) or of any flat buffer.
+// Leaf digests i < npad of `count` 64-byte leaves; i >= count repeats the
+// last leaf (power-of-two padding, src/merkle.rs:350-360).
 __global__ void leaf64_kernel(const uint32_t* __restrict__ flat, uint32_t* __restrict__ leaves,
-                              uint64_t nleaves) {
+                              uint64_t count, uint64_t npad) {
   uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= nleaves) return;
+  if (i >= npad) return;
   uint32_t m[16];
-  const uint4* p = reinterpret_cast<const uint4*>(flat + 16 * i);
+  const uint4* p = reinterpret_cast<const uint4*>(flat + 16 * (i < count ? i : count - 1));
 #pragma unroll
   for (int k = 0; k < 4; k++) {
     uint4 v = p[k];
@@ -676,8 +678,7 @@ __global__ void __launch_bounds__(kThreads) air_compose_leaves_kernel(AirCompose
 #pragma unroll
     for (int c = 0; c < 4; c++) {
       const uint32_t* al = a.alpha[c];
-      uint32_t acc = fadd(mdot2(t2, al[1], ba, al[2]), mdot2(bb, al[3], bo, al[4]));
-      leaf[4 * t + c] = fadd(acc, a.kc[c]);
+      leaf[4 * t + c] = fadd(mdot4(t2, al[1], ba, al[2], bb, al[3], bo, al[4]), a.kc[c]);
     }
   }
   uint4* dst = reinterpret_cast<uint4*>(a.layer0 + 16 * (size_t)P);
@@ -1289,18 +1290,19 @@ cudaError_t layer_leaves(cudaStream_t st, const uint32_t* values, uint64_t len, 
   Stage stg("layer_leaves", st);
   stg.launched();
   if (len % 4 == 0) {
-    leaf64_kernel<<<grid_for(len / 4), kThreads, 0, st>>>(values, leaves, len / 4);
+    leaf64_kernel<<<grid_for(len / 4), kThreads, 0, st>>>(values, leaves, len / 4, len / 4);
   } else {
     leaf16_kernel<<<grid_for(len), kThreads, 0, st>>>(values, leaves, len);
   }
   return cudaGetLastError();
 }
 
-cudaError_t merkle_flat64_leaves(cudaStream_t st, const uint32_t* flat, uint64_t nleaves,
-                                 uint32_t* leaves) {
+cudaError_t merkle_flat64_leaves(cudaStream_t st, const uint32_t* flat, uint64_t count,
+                                 uint64_t npad, uint32_t* leaves) {
+  if (!count || npad < count) return cudaErrorInvalidValue;
   Stage stg("leaf64", st);
   stg.launched();
-  leaf64_kernel<<<grid_for(nleaves), kThreads, 0, st>>>(flat, leaves, nleaves);
+  leaf64_kernel<<<grid_for(npad), kThreads, 0, st>>>(flat, leaves, count, npad);
   return cudaGetLastError();
 }
 

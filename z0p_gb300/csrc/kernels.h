@@ -167,8 +167,10 @@ cudaError_t range_compose_leaves(cudaStream_t st, const Tables& tb, const RangeC
 cudaError_t fri_fold(cudaStream_t st, const Tables& tb, const FoldArgs& a, uint32_t* levels);
 // Leaf digests of an FRI layer held in memory (64-byte quads or 16-byte values).
 cudaError_t layer_leaves(cudaStream_t st, const uint32_t* values, uint64_t len, uint32_t* leaves);
-cudaError_t merkle_flat64_leaves(cudaStream_t st, const uint32_t* flat, uint64_t nleaves,
-                                 uint32_t* leaves);
+// Digests of `count` 64-byte leaves, padded to npad (a power of two) by
+// repeating the last leaf.
+cudaError_t merkle_flat64_leaves(cudaStream_t st, const uint32_t* flat, uint64_t count,
+                                 uint64_t npad, uint32_t* leaves);
 // Minimum-nonce proof-of-work search. `state` is 4 device u64s holding
 // {~0, 0, 0, 0} before the call and again after it; `out` (device-visible)
 // receives {best nonce, status}, status 1 when the nonce cap was reached.

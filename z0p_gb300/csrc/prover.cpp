@@ -1172,18 +1172,16 @@ int z0p_gpu_merkle_flat64_cap(z0p_gpu_ctx* c, const uint8_t* d_flat, uint64_t le
   if (!c || !d_flat || !h_cap || !cap_count) return Z0P_ERR_INVALID_ARGUMENT;
   if (len == 0) return Z0P_ERR_EMPTY_INPUT;  // src/merkle.rs:93-110
   if (len % 64) return Z0P_ERR_MALFORMED_INPUT;
-  uint64_t leaves = len / 64;
-  if (!is_pow2(leaves)) {
-    set_reason("leaf count must be a power of two on the device path");
-    return Z0P_ERR_UNSUPPORTED;
-  }
+  const uint64_t count = len / 64;
+  uint64_t leaves = 1;  // padded by duplicating the last leaf (src/merkle.rs:350-360)
+  while (leaves < count) leaves <<= 1;
   std::lock_guard<std::mutex> lk(c->mu);
   RC(with_device(c));
   RC(ensure(c, c->ttree, 32 * tree_digests(leaves)));
   uint32_t* tree = (uint32_t*)c->ttree.p;
   uint32_t depth = log2u(leaves), drop = cap_height < depth ? (uint32_t)cap_height : depth;
   RC(ensure_hio(c, 32ull << drop));
-  CK(launch::merkle_flat64_leaves(c->stream, (const uint32_t*)d_flat, leaves, tree));
+  CK(launch::merkle_flat64_leaves(c->stream, (const uint32_t*)d_flat, count, leaves, tree));
   CK(launch::merkle_build(c->stream, tree, leaves, depth - drop, merkle_counter(c),
                           hio_dev<uint32_t>(c, 0)));
   CK(sync(c));
