@@ -75,6 +75,18 @@ __device__ __forceinline__ uint32_t mdot4(uint32_t a0, uint32_t b0, uint32_t a1,
   uint32_t r = hi - mp;
   return min(r, r + kP);
 }
+// a * w mod p for any a < 2^32 and canonical w, with wq = floor(w 2^32 / p)
+// precomputed (Shoup's product): q = floor(a wq / 2^32) leaves a w - q p in
+// [0, 2p), so one correction gives the canonical product.
+__device__ __forceinline__ uint32_t shoup_mul(uint32_t a, uint32_t w, uint32_t wq) {
+  uint32_t q = __umulhi(a, wq);
+  uint32_t r = a * w - q * kP;
+  return min(r, r - kP);
+}
+// (w, floor(w 2^32 / p)) for canonical w.
+__device__ __forceinline__ uint2 shoup_pair(uint32_t w) {
+  return make_uint2(w, (uint32_t)(((uint64_t)w << 32) / kP));
+}
 // Canonical x canonical -> canonical.
 __device__ __forceinline__ uint32_t fmul(uint32_t a, uint32_t b) { return mmul(mmul(a, b), kR2); }
 __device__ __forceinline__ uint32_t to_mont(uint32_t a) { return mmul(a, kR2); }

@@ -110,11 +110,13 @@ __device__ __forceinline__ uint32_t spos(uint32_t i) { return i + (i >> 5); }
 __host__ __device__ constexpr uint32_t skewed_len(uint32_t n) { return n + (n >> 5); }
 
 // K DIF stages (distances 2^S_HI .. 2^(S_HI-K+1)) on group g of a column at
-// col (skewed); tw[e] = w^e (Montgomery) for the column root w of order 2^L.
-// Butterfly (u + v, (u - v) w): u - v + p < 2^32 and w < p keep the
-// Montgomery product exact without a prior reduction.
+// col (skewed); tw[e] = (w^e, quotient) for the column root w of order 2^L,
+// canonical with its Shoup quotient. Butterfly (u + v, (u - v) w): u - v + p
+// < 2^32 is a valid Shoup operand without a prior reduction. In the last
+// pass (S_LO = 0) the butterflies whose twiddle index is 0 multiply by 1,
+// known at compile time, and reduce to a subtraction.
 template <int L, int S_HI, int K>
-__device__ __forceinline__ void dif_group_t(uint32_t* col, const uint32_t* tw, uint32_t g) {
+__device__ __forceinline__ void dif_group_t(uint32_t* col, const uint2* tw, uint32_t g) {
   constexpr int S_LO = S_HI + 1 - K;
   const uint32_t g_lo = g & ((1u << S_LO) - 1u);
   const uint32_t i0 = g_lo | ((g >> S_LO) << (S_HI + 1));
@@ -126,14 +128,18 @@ __device__ __forceinline__ void dif_group_t(uint32_t* col, const uint32_t* tw, u
   for (int st = K - 1; st >= 0; st--) {
     const int d = 1 << st;
     const uint32_t tshift = L - (S_LO + st) - 1;
-    const uint32_t* twb = tw + (g_lo << tshift);
+    const uint2* twb = tw + (g_lo << tshift);
 #pragma unroll
     for (int t = 0; t < (1 << K); t++) {
       if (t & d) continue;
-      const uint32_t w = twb[(t & (d - 1)) << (S_LO + tshift)];
       const uint32_t u = x[t], v = x[t + d];
       x[t] = fadd(u, v);
-      x[t + d] = mmul(u + kP - v, w);
+      if (S_LO == 0 && (t & (d - 1)) == 0) {
+        x[t + d] = fsub(u, v);
+      } else {
+        const uint2 w = twb[(t & (d - 1)) << (S_LO + tshift)];
+        x[t + d] = shoup_mul(u + kP - v, w.x, w.y);
+      }
     }
   }
 #pragma unroll
@@ -141,7 +147,7 @@ __device__ __forceinline__ void dif_group_t(uint32_t* col, const uint32_t* tw, u
 }
 
 template <int L, int S_HI>
-__device__ __forceinline__ void dif_passes_t(uint32_t* s, const uint32_t* tw, uint32_t ncols,
+__device__ __forceinline__ void dif_passes_t(uint32_t* s, const uint2* tw, uint32_t ncols,
                                              uint32_t cstride) {
   constexpr int K = S_HI + 1 < 4 ? S_HI + 1 : 4;
   constexpr uint32_t groups = 1u << (L - K);
@@ -153,10 +159,23 @@ __device__ __forceinline__ void dif_passes_t(uint32_t* s, const uint32_t* tw, ui
 }
 
 template <int L>
-__device__ __forceinline__ void smem_dif_t(uint32_t* s, const uint32_t* tw, uint32_t ncols,
+__device__ __forceinline__ void smem_dif_t(uint32_t* s, const uint2* tw, uint32_t ncols,
                                            uint32_t cstride) {
   if constexpr (L > 0) dif_passes_t<L, L - 1>(s, tw, ncols, cstride);
 }
+
+// Stage twiddles of a 2^L-point transform: tw[i] = (w^i, Shoup quotient),
+// canonical, for i < 2^(L-1); w^-1 for the inverse transform.
+template <int L>
+__device__ __forceinline__ void stage_twiddles(uint2* tw, const NttArgs& a) {
+  if constexpr (L > 0)
+    for (uint32_t i = threadIdx.x; i < (1u << (L - 1)); i += blockDim.x)
+      tw[i] = shoup_pair(from_mont(root_pow(a.tb, tw_exp(i, kRootBits - L, a.inverse))));
+}
+
+// Word offset of the stage-twiddle table after `words` of shared memory
+// (8-byte aligned for the uint2 entries).
+__host__ __device__ constexpr uint32_t tw_offset(uint32_t words) { return (words + 1u) & ~1u; }
 
 // One transform of length 2^L per CTA (L <= 12).
 template <int L>
@@ -165,13 +184,11 @@ __global__ void __launch_bounds__(512) ntt_small_kernel(const uint32_t* __restri
   extern __shared__ uint32_t sm[];
   constexpr uint32_t n = 1u << L;
   uint32_t* s = sm;
-  uint32_t* tw = sm + skewed_len(n);
+  uint2* tw = reinterpret_cast<uint2*>(sm + tw_offset(skewed_len(n)));
   const uint32_t b = blockIdx.x;
   const uint32_t* src = in + (size_t)(b / a.in_div) * n;
   const uint32_t j = b % a.twist_mod;
-  if constexpr (L > 0)
-    for (uint32_t i = threadIdx.x; i < n / 2; i += blockDim.x)
-      tw[i] = root_pow(a.tb, tw_exp(i, kRootBits - L, a.inverse));
+  stage_twiddles<L>(tw, a);
   // twist w^(j i): a geometric chain per thread (stride blockDim)
   uint32_t tw_cur = 0, tw_step = 0;
   if (j) {
@@ -226,14 +243,13 @@ __global__ void __launch_bounds__(512) ntt_pass1_kernel(const uint32_t* __restri
   const uint32_t logn2 = a.logn - L1;
   const uint32_t n = 1u << a.logn;
   uint32_t* s = sm;
-  uint32_t* tw = sm + C * cstride;
-  uint32_t* twist = tw + n1 / 2;
+  uint2* tw = reinterpret_cast<uint2*>(sm + tw_offset(C * cstride));
+  uint32_t* twist = reinterpret_cast<uint32_t*>(tw + n1 / 2);
   const uint32_t b = blockIdx.y;
   const uint32_t c0 = blockIdx.x * C;
   const uint32_t* src = in + (size_t)(b / a.in_div) * n;
   const uint32_t j = b % a.twist_mod;
-  for (uint32_t i = threadIdx.x; i < n1 / 2; i += blockDim.x)
-    tw[i] = root_pow(a.tb, tw_exp(i, kRootBits - L1, a.inverse));
+  stage_twiddles<L1>(tw, a);
   if (j)
     for (uint32_t i1 = threadIdx.x; i1 < n1; i1 += blockDim.x)
       twist[i1] = root_pow(a.tb, ((j * i1) << logn2) << a.twist_shift);
@@ -280,11 +296,10 @@ __global__ void __launch_bounds__(512) ntt_pass2_kernel(const uint32_t* __restri
   const uint32_t logn1 = a.logn - L2;
   const uint32_t n = 1u << a.logn;
   uint32_t* s = sm;
-  uint32_t* tw = sm + R * rstride;
+  uint2* tw = reinterpret_cast<uint2*>(sm + tw_offset(R * rstride));
   const uint32_t b = blockIdx.y;
   const uint32_t r0 = blockIdx.x * R;
-  for (uint32_t i = threadIdx.x; i < n2 / 2; i += blockDim.x)
-    tw[i] = root_pow(a.tb, tw_exp(i, kRootBits - L2, a.inverse));
+  stage_twiddles<L2>(tw, a);
   const uint4* src = reinterpret_cast<const uint4*>(yt + (size_t)b * n + ((size_t)r0 << L2));
   for (uint32_t e = threadIdx.x; e < (R << L2) / 4; e += blockDim.x) {
     const uint32_t r = (4 * e) >> L2, i2 = (4 * e) & (n2 - 1);
@@ -1116,7 +1131,7 @@ cudaError_t ntt(cudaStream_t st, const Tables& tb, const NttPlan& plan, const ui
   a.tb = tb;
   const uint32_t n = 1u << plan.logn;
   if (plan.logn <= 12) {
-    size_t smem = (size_t)(skewed_len(n) + n / 2 + 1) * 4;
+    size_t smem = (size_t)(tw_offset(skewed_len(n)) + n + 2) * 4;
     int threads = n >= 2048 ? 512 : (n >= 256 ? 256 : 128);
     Stage stg(plan.inverse ? "intt" : "ntt", st);
     stg.launched();
@@ -1136,8 +1151,8 @@ cudaError_t ntt(cudaStream_t st, const Tables& tb, const NttPlan& plan, const ui
   // C = R = 8 columns per CTA (32-byte global segments), 4 for the largest halves.
   const int logc = logn1 > 12 ? 2 : 3;
   const int logr = logn2 > 12 ? 2 : 3;
-  size_t smem1 = ((size_t)(col_stride(logn1, 1u << logc) << logc) + n1 / 2 + n1) * 4;
-  size_t smem2 = ((size_t)(col_stride(logn2, 1u << logr) << logr) + n2 / 2) * 4;
+  size_t smem1 = ((size_t)tw_offset(col_stride(logn1, 1u << logc) << logc) + n1 + n1) * 4;
+  size_t smem2 = ((size_t)tw_offset(col_stride(logn2, 1u << logr) << logr) + n2) * 4;
   dim3 g1(n2 >> logc, plan.batch), g2(n1 >> logr, plan.batch);
   Stage stg(plan.inverse ? "intt" : "ntt", st);
   stg.launched(2);
