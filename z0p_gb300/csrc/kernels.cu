@@ -107,6 +107,12 @@ struct NttArgs {
 };
 
 __device__ __forceinline__ uint32_t spos(uint32_t i) { return i + (i >> 5); }
+// Stage-twiddle table position: one padding entry per 16 spreads the
+// power-of-two strides at which a warp's threads read twiddles over the banks.
+__host__ __device__ constexpr uint32_t tpos(uint32_t i) { return i + (i >> 4); }
+__host__ __device__ constexpr uint32_t tw_entries(uint32_t L) {
+  return L ? tpos(1u << (L - 1)) : 0u;
+}
 __host__ __device__ constexpr uint32_t skewed_len(uint32_t n) { return n + (n >> 5); }
 
 // K DIF stages (distances 2^S_HI .. 2^(S_HI-K+1)) on group g of a column at
@@ -128,7 +134,7 @@ __device__ __forceinline__ void dif_group_t(uint32_t* col, const uint2* tw, uint
   for (int st = K - 1; st >= 0; st--) {
     const int d = 1 << st;
     const uint32_t tshift = L - (S_LO + st) - 1;
-    const uint2* twb = tw + (g_lo << tshift);
+    const uint32_t tbase = g_lo << tshift;
 #pragma unroll
     for (int t = 0; t < (1 << K); t++) {
       if (t & d) continue;
@@ -137,7 +143,7 @@ __device__ __forceinline__ void dif_group_t(uint32_t* col, const uint2* tw, uint
       if (S_LO == 0 && (t & (d - 1)) == 0) {
         x[t + d] = fsub(u, v);
       } else {
-        const uint2 w = twb[(t & (d - 1)) << (S_LO + tshift)];
+        const uint2 w = tw[tpos(tbase + ((uint32_t)(t & (d - 1)) << (S_LO + tshift)))];
         x[t + d] = shoup_mul(u + kP - v, w.x, w.y);
       }
     }
@@ -164,13 +170,13 @@ __device__ __forceinline__ void smem_dif_t(uint32_t* s, const uint2* tw, uint32_
   if constexpr (L > 0) dif_passes_t<L, L - 1>(s, tw, ncols, cstride);
 }
 
-// Stage twiddles of a 2^L-point transform: tw[i] = (w^i, Shoup quotient),
-// canonical, for i < 2^(L-1); w^-1 for the inverse transform.
+// Stage twiddles of a 2^L-point transform: (w^i, Shoup quotient), canonical,
+// for i < 2^(L-1) (w^-1 for the inverse transform), entry i at tpos(i).
 template <int L>
 __device__ __forceinline__ void stage_twiddles(uint2* tw, const NttArgs& a) {
   if constexpr (L > 0)
     for (uint32_t i = threadIdx.x; i < (1u << (L - 1)); i += blockDim.x)
-      tw[i] = shoup_pair(from_mont(root_pow(a.tb, tw_exp(i, kRootBits - L, a.inverse))));
+      tw[tpos(i)] = shoup_pair(from_mont(root_pow(a.tb, tw_exp(i, kRootBits - L, a.inverse))));
 }
 
 // Word offset of the stage-twiddle table after `words` of shared memory
@@ -244,7 +250,7 @@ __global__ void __launch_bounds__(512) ntt_pass1_kernel(const uint32_t* __restri
   const uint32_t n = 1u << a.logn;
   uint32_t* s = sm;
   uint2* tw = reinterpret_cast<uint2*>(sm + tw_offset(C * cstride));
-  uint32_t* twist = reinterpret_cast<uint32_t*>(tw + n1 / 2);
+  uint32_t* twist = reinterpret_cast<uint32_t*>(tw + tw_entries(L1));
   const uint32_t b = blockIdx.y;
   const uint32_t c0 = blockIdx.x * C;
   const uint32_t* src = in + (size_t)(b / a.in_div) * n;
@@ -422,12 +428,14 @@ __global__ void __launch_bounds__(kTraceLeafThreads) air_trace_leaves_kernel(
   uint32_t d[8];
   if (threadIdx.x < nt) {
   const uint32_t logm = logN + logB;
-  const uint32_t gamma_m = to_mont(31u);
+  // Rows 8L..8L+7 are consecutive powers of omega_m: x_{k+1} = x_k omega_m.
+  const uint32_t step = root_pow(tb, 1u << (kRootBits - logm));
+  uint32_t x = mmul(to_mont(31u), root_pow(tb, (8u * L) << (kRootBits - logm)));
   uint32_t den[8];
 #pragma unroll
   for (int r = 0; r < 8; r++) {
-    uint32_t k = 8u * L + r;
-    den[r] = fsub(mmul(gamma_m, root_pow(tb, k << (kRootBits - logm))), w_last_m);
+    den[r] = fsub(x, w_last_m);
+    x = mmul(x, step);
   }
   batch_minv(den);
   uint32_t m[16];
@@ -1131,7 +1139,7 @@ cudaError_t ntt(cudaStream_t st, const Tables& tb, const NttPlan& plan, const ui
   a.tb = tb;
   const uint32_t n = 1u << plan.logn;
   if (plan.logn <= 12) {
-    size_t smem = (size_t)(tw_offset(skewed_len(n)) + n + 2) * 4;
+    size_t smem = (size_t)(tw_offset(skewed_len(n)) + 2 * tw_entries(plan.logn) + 2) * 4;
     int threads = n >= 2048 ? 512 : (n >= 256 ? 256 : 128);
     Stage stg(plan.inverse ? "intt" : "ntt", st);
     stg.launched();
@@ -1151,8 +1159,9 @@ cudaError_t ntt(cudaStream_t st, const Tables& tb, const NttPlan& plan, const ui
   // C = R = 8 columns per CTA (32-byte global segments), 4 for the largest halves.
   const int logc = logn1 > 12 ? 2 : 3;
   const int logr = logn2 > 12 ? 2 : 3;
-  size_t smem1 = ((size_t)tw_offset(col_stride(logn1, 1u << logc) << logc) + n1 + n1) * 4;
-  size_t smem2 = ((size_t)tw_offset(col_stride(logn2, 1u << logr) << logr) + n2) * 4;
+  size_t smem1 =
+      ((size_t)tw_offset(col_stride(logn1, 1u << logc) << logc) + 2 * tw_entries(logn1) + n1) * 4;
+  size_t smem2 = ((size_t)tw_offset(col_stride(logn2, 1u << logr) << logr) + 2 * tw_entries(logn2)) * 4;
   dim3 g1(n2 >> logc, plan.batch), g2(n1 >> logr, plan.batch);
   Stage stg(plan.inverse ? "intt" : "ntt", st);
   stg.launched(2);
