@@ -811,24 +811,23 @@ __device__ __forceinline__ uint32_t quad_xinv(const Tables& tb, const FoldArgs& 
 // staged through shared memory), writes the 64-byte next leaf and its digest.
 constexpr int kFoldThreads = 128;
 __global__ void __launch_bounds__(kFoldThreads) fri_fold_leaf_kernel(FoldArgs a, Tables tb) {
-  __shared__ uint4 sm[kFoldThreads * 17];
+  __shared__ uint32_t sm[2 * kFoldThreads * 9];  // the next layer's subtree (small trees)
   const uint64_t nleaf = 1ull << (a.logn - 4);
   const uint64_t first = (uint64_t)blockIdx.x * kFoldThreads;
-  const uint4* src = reinterpret_cast<const uint4*>(a.in) + first * 16;
   const uint32_t avail = nleaf < (uint64_t)kFoldThreads ? (uint32_t)nleaf : (uint32_t)kFoldThreads;
-  for (uint32_t e = threadIdx.x; e < avail * 16; e += kFoldThreads)
-    sm[(e >> 4) * 17 + (e & 15)] = src[e];
-  __syncthreads();
   uint64_t Pn = first + threadIdx.x;
   uint32_t d[8];
   if (threadIdx.x < avail) {
+  // The thread's 256 input bytes are contiguous; each 16-byte load of a warp
+  // touches 32 lines that its next loads reuse from L1.
+  const uint4* src = reinterpret_cast<const uint4*>(a.in) + Pn * 16;
   uint32_t leaf[16];
 #pragma unroll
   for (int t = 0; t < 4; t++) {
     E4 q[4];
 #pragma unroll
     for (int i = 0; i < 4; i++) {
-      uint4 v = sm[threadIdx.x * 17 + 4 * t + i];
+      uint4 v = __ldcs(src + 4 * t + i);
       q[i].c[0] = v.x; q[i].c[1] = v.y; q[i].c[2] = v.z; q[i].c[3] = v.w;
     }
     uint32_t P = (uint32_t)(4 * Pn + t);
@@ -843,10 +842,7 @@ __global__ void __launch_bounds__(kFoldThreads) fri_fold_leaf_kernel(FoldArgs a,
   blake3_leaf64(leaf, d);
   store_digest(a.leaves + 8 * Pn, d);
   }
-  // The staging buffer is free again: the next layer's subtree over these
-  // leaves is hashed in it (2 * 128 * 9 words fit in 128 * 17 uint4).
-  __syncthreads();
-  cta_subtree(d, reinterpret_cast<uint32_t*>(sm), avail, first, a.leaves, nleaf, a.top, a.cap);
+  cta_subtree(d, sm, avail, first, a.leaves, nleaf, a.top, a.cap);
 }
 
 // Thread per next-layer value (small layers; leaves hashed separately).
