@@ -57,6 +57,19 @@ def dist_env():
     return ws, rank, local
 
 
+def aggregate_replicas(dist, dev_ms, wall_s, device):
+    """Replicas: every rank proves its own proofs; the job's time is the
+    slowest rank's (device-event and wall clock), so value = all ranks'
+    steps / that time. No data crosses ranks but these two numbers."""
+    if dist is None:
+        return dev_ms, wall_s
+    import torch
+
+    t = torch.tensor([dev_ms, wall_s], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t[0]), float(t[1])
+
+
 # ------------------------------------------------------------------ clocks --
 REASONS = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
 
@@ -404,10 +417,7 @@ def run_gpu(args):
     clocks = sampler.stop()
     dev_ms = ev0.elapsed_time(ev1)
     wall_s = w1 - w0
-    if dist is not None:
-        t = torch.tensor([dev_ms, wall_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        dev_ms, wall_s = float(t[0]), float(t[1])
+    dev_ms, wall_s = aggregate_replicas(dist, dev_ms, wall_s, "cuda")
 
     # --- per-stage timing (CUDA events on the context stream) ---------------
     prof_steps = 0 if args.quick else 2
