@@ -51,13 +51,16 @@ __device__ __forceinline__ void store_digest(uint32_t* p, const uint32_t d[8]) {
 // ------------------------------------------------------------ trace gen ----
 // (A_i, B_i) = M^i (a0, b0) with M = [[0,1],[1,1]] (src/air.rs:341-354): each
 // thread jumps to its chunk start with the binary powers of M, then steps.
+__constant__ ProofConsts g_consts[kConstSlots];
+
 struct FibMats {
   uint32_t m[32][4];
 };
 
 __global__ void fib_trace_kernel(uint32_t* __restrict__ col_a, uint32_t* __restrict__ col_b,
-                                 uint32_t n, uint32_t a0, uint32_t b0, FibMats mats,
+                                 uint32_t n, uint32_t slot, FibMats mats,
                                  uint32_t per_thread) {
+  const uint32_t a0 = g_consts[slot].a0, b0 = g_consts[slot].b0;
   uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   uint64_t start = t * per_thread;
   if (start >= n) return;
@@ -346,7 +349,7 @@ __global__ void __launch_bounds__(512) ntt_pass2_kernel(const uint32_t* __restri
 // coset), in Montgomery form, the same value times 2^32 once more, and the
 // linked-column constant C_j = coeff * (x^N - 1) (canonical).
 __global__ void coset_zinv_kernel(uint32_t* zinv, uint32_t* zinv2, uint32_t logB,
-                                  uint32_t gamma_n_m, uint32_t* cb, uint32_t coeff, Tables tb) {
+                                  uint32_t gamma_n_m, uint32_t* cb, uint32_t slot, Tables tb) {
   uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= (1u << logB)) return;
   uint32_t xn = mmul(gamma_n_m, root_pow(tb, j << (kRootBits - logB)));
@@ -354,7 +357,7 @@ __global__ void coset_zinv_kernel(uint32_t* zinv, uint32_t* zinv2, uint32_t logB
   uint32_t inv = minv(xn1);
   zinv[j] = inv;
   zinv2[j] = mmul(inv, kR2);
-  if (cb) cb[j] = mmul(coeff, xn1);
+  if (cb) cb[j] = mmul(g_consts[slot].coeff, xn1);
 }
 
 // B at row k = B q + j of the LDE from A: A[j][q+1] + C_j / (x_k - w_last),
@@ -694,14 +697,16 @@ __global__ void __launch_bounds__(kThreads) air_compose_leaves_kernel(AirCompose
     const uint32_t bv = fadd(avn, mmul(cbj, t0));
     const uint32_t bvn = fadd(avnn, mmul(cbj, tn));
     const uint32_t t2 = mmul(fsub(bvn, fadd(av, bv)), zt);
-    const uint32_t ba = mmul(fsub(av, a.a0), tm);
-    const uint32_t bb = mmul(fsub(bv, a.b0), tm);
-    const uint32_t bo = mmul(fsub(bv, a.b_last), t0);
+    const ProofConsts& pc = g_consts[a.slot];
+    const uint32_t ba = mmul(fsub(av, pc.a0), tm);
+    const uint32_t bb = mmul(fsub(bv, pc.b0), tm);
+    const uint32_t bo = mmul(fsub(bv, pc.b_last), t0);
     const int t = (s == 1) ? 2 : (s == 2) ? 1 : s;  // position 4P + brev2(s)
 #pragma unroll
     for (int c = 0; c < 4; c++) {
-      const uint32_t* al = a.alpha[c];
-      leaf[4 * t + c] = fadd(mdot4(t2, al[1], ba, al[2], bb, al[3], bo, al[4]), a.kc[c]);
+      leaf[4 * t + c] = fadd(mdot4(t2, pc.alpha[c][1], ba, pc.alpha[c][2], bb, pc.alpha[c][3], bo,
+                                   pc.alpha[c][4]),
+                             pc.kc[c]);
     }
   }
   uint4* dst = reinterpret_cast<uint4*>(a.layer0 + 16 * (size_t)P);
@@ -760,7 +765,7 @@ __global__ void __launch_bounds__(kThreads) range_compose_leaves_kernel(RangeCom
       for (int e = 0; e < 4; e++) acc.c[e] = fadd(acc.c[e], mmul(bterm, __ldg(al + e)));
     }
     uint32_t dterm = mmul(fsub(v, rec), zi);
-    uint32_t bound = mmul(fsub(v, a.value), den[s]);
+    uint32_t bound = mmul(fsub(v, g_consts[a.slot].value), den[s]);
     const uint32_t* ad = a.alphas;
     const uint32_t* ab = a.alphas + 4 * (1 + nb);
     const int t = (s == 1) ? 2 : (s == 2) ? 1 : s;
@@ -794,8 +799,9 @@ __device__ __forceinline__ E4 fold_quad(const E4& q0, const E4& q1, const E4& q2
   E4 odd4 = e4_sub(odd_diff, skew_u);
   E4 even4 = e4_sub(s01, s23);
   E4 skew4 = e4_add(odd_diff, skew_u);
-  E4 acc = e4_add(e4_mul_base(e4_mul_tab(skew4, a.tab[2]), xinv_m), e4_mul_tab(even4, a.tab[1]));
-  acc = e4_add(e4_mul_base(acc, xinv_m), e4_mul_tab(odd4, a.tab[0]));
+  const ProofConsts& pc = g_consts[a.slot];
+  E4 acc = e4_add(e4_mul_base(e4_mul_tab(skew4, pc.tab[2]), xinv_m), e4_mul_tab(even4, pc.tab[1]));
+  acc = e4_add(e4_mul_base(acc, xinv_m), e4_mul_tab(odd4, pc.tab[0]));
   return e4_add(mean, e4_mul_base(acc, xinv_m));
 }
 
@@ -875,7 +881,7 @@ constexpr uint64_t kGrindChunk = (uint64_t)kGrindThreads * kGrindPerThread;
 // [3] CTAs finished. The last CTA to finish copies {best, status} to `out`
 // and puts the state back to {~0, 0, 0, 0} for the next launch.
 struct GrindArgs {
-  uint32_t head[16];
+  uint32_t slot;  // ProofConsts slot: the head
   uint32_t bits;
   unsigned long long* state;
   unsigned long long* out;
@@ -924,12 +930,12 @@ __global__ void __launch_bounds__(kGrindThreads) grind_kernel(GrindArgs a) {
       uint32_t lo = (uint32_t)nonce, hi = (uint32_t)(nonce >> 32);
       uint32_t m[16];
 #pragma unroll
-      for (int i = 0; i < 16; i++) m[i] = i < W ? a.head[i] : 0u;
+      for (int i = 0; i < 16; i++) m[i] = i < W ? g_consts[a.slot].head[i] : 0u;
       if (SH == 0) {
         m[W] = lo;
         m[W + 1] = hi;
       } else {
-        m[W] = a.head[W] | (lo << SH);
+        m[W] = g_consts[a.slot].head[W] | (lo << SH);
         m[W + 1] = (lo >> (32 - SH)) | (hi << SH);
         m[W + 2] = hi >> (32 - SH);
       }
@@ -1076,8 +1082,17 @@ struct Stage {
   void launched(int k = 1) { g_launches += k; }
 };
 
-cudaError_t fib_trace(cudaStream_t st, uint32_t* col_a, uint32_t* col_b, uint32_t n, uint32_t a0,
-                      uint32_t b0, const uint32_t mats[32][4]) {
+cudaError_t const_slot_address(int slot, void** ptr) {
+  if (slot < 0 || slot >= kConstSlots) return cudaErrorInvalidValue;
+  void* base = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&base, g_consts);
+  if (e != cudaSuccess) return e;
+  *ptr = static_cast<char*>(base) + (size_t)slot * sizeof(ProofConsts);
+  return cudaSuccess;
+}
+
+cudaError_t fib_trace(cudaStream_t st, uint32_t* col_a, uint32_t* col_b, uint32_t n, uint32_t slot,
+                      const uint32_t mats[32][4]) {
   FibMats fm;
   for (int k = 0; k < 32; k++)
     for (int i = 0; i < 4; i++) fm.m[k][i] = mats[k][i];
@@ -1085,7 +1100,7 @@ cudaError_t fib_trace(cudaStream_t st, uint32_t* col_a, uint32_t* col_b, uint32_
   uint64_t threads = (n + per - 1) / per;
   Stage stg("trace", st);
   stg.launched();
-  fib_trace_kernel<<<grid_for(threads), kThreads, 0, st>>>(col_a, col_b, n, a0, b0, fm, per);
+  fib_trace_kernel<<<grid_for(threads), kThreads, 0, st>>>(col_a, col_b, n, slot, fm, per);
   return cudaGetLastError();
 }
 
@@ -1097,9 +1112,6 @@ cudaError_t fill_constant_columns(cudaStream_t st, uint32_t* cols, uint32_t n, u
   return cudaGetLastError();
 }
 
-// True when the pass-`pass` kernel for half-length 2^L has already been
-// allowed `smem` bytes of dynamic shared memory in this process (each kernel's
-// need is fixed by L, so the attribute is set once per kernel, not per launch).
 // Levels cta_subtree builds for a CTA of nt leaves under a tree capped at `top`.
 uint32_t subtree_levels(uint32_t nt, uint32_t top) {
   uint32_t l = 0;
@@ -1107,6 +1119,9 @@ uint32_t subtree_levels(uint32_t nt, uint32_t top) {
   return l;
 }
 
+// True when the pass-`pass` kernel for half-length 2^L has already been
+// allowed `smem` bytes of dynamic shared memory in this process (each kernel's
+// need is fixed by L, so the attribute is set once per kernel, not per launch).
 bool smem_raised(int pass, uint32_t L, size_t smem) {
   static std::mutex mu;
   static size_t done[3][32] = {};
@@ -1193,11 +1208,11 @@ cudaError_t ntt(cudaStream_t st, const Tables& tb, const NttPlan& plan, const ui
 }
 
 cudaError_t coset_zinv(cudaStream_t st, const Tables& tb, uint32_t* zinv, uint32_t* zinv2,
-                       uint32_t logB, uint32_t gamma_n_m, uint32_t* cb, uint32_t coeff) {
+                       uint32_t logB, uint32_t gamma_n_m, uint32_t* cb, uint32_t slot) {
   Stage stg("coset_zinv", st);
   stg.launched();
   coset_zinv_kernel<<<grid_for(1ull << logB), kThreads, 0, st>>>(zinv, zinv2, logB, gamma_n_m, cb,
-                                                                 coeff, tb);
+                                                                 slot, tb);
   return cudaGetLastError();
 }
 
@@ -1328,12 +1343,12 @@ cudaError_t merkle_flat64_leaves(cudaStream_t st, const uint32_t* flat, uint64_t
 
 bool grind_supports(uint32_t head_len) { return head_len == 47; }
 
-cudaError_t grind(cudaStream_t st, const uint8_t* head, uint32_t head_len, uint32_t bits,
+cudaError_t grind(cudaStream_t st, uint32_t slot, uint32_t head_len, uint32_t bits,
                   unsigned long long* state, unsigned long long* out, uint64_t max_nonces) {
-  if (!grind_supports(head_len) || bits > 32) return cudaErrorInvalidValue;
+  if (!grind_supports(head_len) || bits > 32 || slot >= (uint32_t)kConstSlots)
+    return cudaErrorInvalidValue;
   GrindArgs a;
-  for (int i = 0; i < 16; i++) a.head[i] = 0;
-  for (uint32_t i = 0; i < head_len; i++) a.head[i / 4] |= (uint32_t)head[i] << (8 * (i % 4));
+  a.slot = slot;
   a.bits = bits;
   a.state = state;
   a.out = out;

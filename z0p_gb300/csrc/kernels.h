@@ -32,6 +32,24 @@ struct NttPlan {
 // Column B of the Fibonacci trace is never transformed: on the LDE,
 // B(x) = A(omega_N x) + C_j / (x - w_last) with C_j constant on coset j
 // (src/air.rs:806-844, linked_lde), so kernels that need B derive it from A.
+// Values that change from one proof to the next on the same shape: the
+// statement, the Fiat-Shamir challenges in the forms the kernels use and the
+// PoW head. Each context owns one slot of them in constant memory, filled by a
+// stream-ordered copy before the kernels that read it, so a captured launch
+// sequence replays unchanged for every proof of its shape.
+struct ProofConsts {
+  uint32_t a0, b0, b_last;  // AIR statement (canonical)
+  uint32_t coeff;           // linked-column coefficient (B[N-1] - a0) w_last / N
+  uint32_t value;           // range statement
+  uint32_t kc[4];           // alpha_0 * (-coeff): the composition's constant term
+  // Composition weights, coordinate c at [c][k] (Montgomery): alpha_1,
+  // alpha_2 and alpha_3 times omega_N^-1, alpha_4 ([c][0] unused).
+  uint32_t alpha[4][5];
+  uint32_t head[16];        // PoW head (47 bytes, little-endian words, zero padded)
+  uint32_t tab[3][4][4];    // the current fold's e4_mul_tab tables of r_k / 4
+};
+constexpr int kConstSlots = 128;
+
 struct AirComposeArgs {
   const uint32_t* lde_a;  // coset-major [j][q]
   const uint32_t* cb;     // per coset C_j (canonical)
@@ -40,12 +58,8 @@ struct AirComposeArgs {
   uint32_t* layer0;       // FRI layer 0, bit-reversed Ext4 values
   uint32_t* leaves;       // layer-0 tree, leaf digests
   uint32_t logN, logB;
-  uint32_t a0, b0, b_last;  // canonical
-  uint32_t w_last_m;        // omega_N^(N-1) (Montgomery)
-  // Coordinate c of the weights at [c][k] (Montgomery): alpha_1, alpha_2 and
-  // alpha_3 times omega_N^-1, alpha_4 ([c][0] unused).
-  uint32_t alpha[4][5];
-  uint32_t kc[4];  // alpha_0 * (-coeff), canonical: the constant first term
+  uint32_t w_last_m;      // omega_N^(N-1) (Montgomery)
+  uint32_t slot;          // ProofConsts slot: statement, alphas, kc
 };
 
 struct RangeComposeArgs {
@@ -56,7 +70,7 @@ struct RangeComposeArgs {
   uint32_t* layer0;
   uint32_t* leaves;
   uint32_t logN, logB, n_bits;
-  uint32_t value;  // canonical
+  uint32_t slot;  // ProofConsts slot: the claimed value
 };
 
 struct FoldArgs {
@@ -68,8 +82,7 @@ struct FoldArgs {
   uint32_t logn;
   uint32_t ginv_m;     // (31^(4^depth))^-1 (Montgomery)
   uint32_t unit_m;     // two_adic_generator(2) (Montgomery)
-  // Product tables (e4_mul_tab) of r_k / 4 for the three fold challenges.
-  uint32_t tab[3][4][4];
+  uint32_t slot = 0;   // ProofConsts slot: the fold's challenge tables
 };
 
 // Openings of one proof, gathered on the device into one block per query.
@@ -125,17 +138,21 @@ struct StageRecorder {
 };
 void set_recorder(StageRecorder* r);
 
-cudaError_t fib_trace(cudaStream_t st, uint32_t* col_a, uint32_t* col_b, uint32_t n, uint32_t a0,
-                      uint32_t b0, const uint32_t mats[32][4]);
+// Device address of constant slot `slot` (a ProofConsts).
+cudaError_t const_slot_address(int slot, void** ptr);
+
+// (a0, b0) from the slot.
+cudaError_t fib_trace(cudaStream_t st, uint32_t* col_a, uint32_t* col_b, uint32_t n, uint32_t slot,
+                      const uint32_t mats[32][4]);
 cudaError_t fill_constant_columns(cudaStream_t st, uint32_t* cols, uint32_t n, uint32_t ncols,
                                   const uint32_t* h_values);
 cudaError_t ntt(cudaStream_t st, const Tables& tb, const NttPlan& plan, const uint32_t* in,
                 uint32_t* out, uint32_t* scratch);
 // Per coset j (x^N = 31^N omega_B^j): zinv = 1/(x^N - 1) (Montgomery),
 // zinv2 = zinv * 2^32, and, when cb is non-null, cb = coeff * (x^N - 1)
-// (canonical; coeff canonical), the linked-column constant.
+// (canonical; coeff from the slot), the linked-column constant.
 cudaError_t coset_zinv(cudaStream_t st, const Tables& tb, uint32_t* zinv, uint32_t* zinv2,
-                       uint32_t logB, uint32_t gamma_n_m, uint32_t* cb, uint32_t coeff);
+                       uint32_t logB, uint32_t gamma_n_m, uint32_t* cb, uint32_t slot);
 // Trace leaves of the AIR: rows 8L..8L+7 as A || B with B derived from A.
 // Also writes tinv (m words, coset-major): 1 / (x - w_last) per LDE row.
 // The kernel also hashes each CTA's subtree (up to the cap level `top`;
@@ -174,7 +191,8 @@ cudaError_t merkle_flat64_leaves(cudaStream_t st, const uint32_t* flat, uint64_t
 // Minimum-nonce proof-of-work search. `state` is 4 device u64s holding
 // {~0, 0, 0, 0} before the call and again after it; `out` (device-visible)
 // receives {best nonce, status}, status 1 when the nonce cap was reached.
-cudaError_t grind(cudaStream_t st, const uint8_t* head, uint32_t head_len, uint32_t bits,
+// The head comes from the slot (head_len bytes).
+cudaError_t grind(cudaStream_t st, uint32_t slot, uint32_t head_len, uint32_t bits,
                   unsigned long long* state, unsigned long long* out, uint64_t max_nonces);
 bool grind_supports(uint32_t head_len);
 // Reorders `batch` coset-major LDEs ([j][q]) into natural order ([B q + j]).

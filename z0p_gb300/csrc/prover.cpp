@@ -130,6 +130,11 @@ struct z0p_gpu_ctx {
   uint8_t* hio = nullptr;
   uint8_t* hio_d = nullptr;  // its device address
   size_t hio_bytes = 0;
+  // The context's constant slot of per-proof values, and its pinned staging
+  // copy: the host fills `consts`, push_consts queues the copy into the slot.
+  int slot = -1;
+  void* slot_dev = nullptr;
+  ProofConsts* consts = nullptr;
   size_t held = 0;
   uint64_t h2d = 0, d2h = 0, syncs = 0, proofs = 0, sync_ns = 0, prove_ns = 0;
   bool profiling = false;
@@ -221,6 +226,39 @@ int ensure(z0p_gpu_ctx* c, DevBuf& b, size_t bytes) {
   b.bytes = want;
   c->held += want;
   return Z0P_OK;
+}
+
+// Constant slots are handed out to contexts for their lifetime.
+std::mutex g_slot_mu;
+bool g_slot_used[kConstSlots] = {};
+
+int take_slot() {
+  std::lock_guard<std::mutex> lk(g_slot_mu);
+  for (int i = 0; i < kConstSlots; i++)
+    if (!g_slot_used[i]) {
+      g_slot_used[i] = true;
+      return i;
+    }
+  return -1;
+}
+void give_slot(int i) {
+  std::lock_guard<std::mutex> lk(g_slot_mu);
+  if (i >= 0 && i < kConstSlots) g_slot_used[i] = false;
+}
+
+// Queues the copy of the context's per-proof values into its constant slot.
+// The host changes c->consts only after the stream has synchronised past the
+// previous copy.
+cudaError_t push_consts(z0p_gpu_ctx* c) {
+  c->h2d += sizeof(ProofConsts);
+  return cudaMemcpyAsync(c->slot_dev, c->consts, sizeof(ProofConsts), cudaMemcpyHostToDevice,
+                         c->stream);
+}
+
+// PoW head bytes as little-endian words, zero padded.
+void set_head(ProofConsts* pc, const uint8_t* head, size_t len) {
+  for (int i = 0; i < 16; i++) pc->head[i] = 0;
+  for (size_t i = 0; i < len && i < 64; i++) pc->head[i / 4] |= (uint32_t)head[i] << (8 * (i % 4));
 }
 
 int ensure_hio(z0p_gpu_ctx* c, size_t bytes) {
@@ -388,14 +426,16 @@ int run_fri(z0p_gpu_ctx* c, const FriShape& s, const FriParams& fp, const FriBuf
       transcript_absorb(ts, "fri-layer-root", out->caps[l].data() + 32 * k, 32);
     if (last) break;
     FoldArgs fa;
+    fa.slot = (uint32_t)c->slot;
     uint32_t ch[3][4];
     for (int k = 0; k < 3; k++) challenge_ext(ts, "fri-fold", ch[k]);
     const uint32_t inv4 = finv(4);
     for (int k = 0; k < 3; k++) {
       uint32_t q[4];
       for (int e = 0; e < 4; e++) q[e] = fmul(ch[k][e], inv4);
-      e4_table(q, fa.tab[k]);
+      e4_table(q, c->consts->tab[k]);
     }
+    CK(push_consts(c));
     fa.in = fb.layer[l];
     fa.out = fb.layer[l + 1];
     fa.leaves = fb.tree[l + 1];
@@ -426,7 +466,9 @@ int run_fri(z0p_gpu_ctx* c, const FriShape& s, const FriParams& fp, const FriBuf
   out->nonce = 0;
   if (fp.grinding_bits > 0) {
     std::vector<uint8_t> head = pow_head(ts, "fri-pow");
-    CK(launch::grind(c->stream, head.data(), (uint32_t)head.size(), fp.grinding_bits,
+    set_head(c->consts, head.data(), head.size());
+    CK(push_consts(c));
+    CK(launch::grind(c->stream, (uint32_t)c->slot, (uint32_t)head.size(), fp.grinding_bits,
                      grind_state(c), hio_dev<unsigned long long>(c, h.grind), 1ull << 40));
     CK(sync(c, "grind"));
     unsigned long long res[2];
@@ -595,16 +637,6 @@ int air_prove(z0p_gpu_ctx* c, const z0p_air_params& p, Transcript& ts, uint8_t* 
   // src/air.rs:806-844): B(x) = A(omega_N x) + C_j / (x - w_last).
   uint32_t mats[32][4];
   fib_mats(mats);
-  CK(launch::fib_trace(st, cols, cols + N, (uint32_t)N, p.a0, p.b0, mats));
-  NttPlan ip;
-  ip.logn = logN; ip.batch = 1; ip.inverse = 1; ip.post_gamma = 1;
-  CK(launch::ntt(st, c->tb, ip, cols, coeffs, (uint32_t*)c->scratch.p));
-  NttPlan lp;
-  lp.logn = logN; lp.batch = (uint32_t)B; lp.in_div = (uint32_t)B; lp.twist_mod = (uint32_t)B;
-  lp.twist_shift = 27 - logm;
-  CK(launch::ntt(st, c->tb, lp, coeffs, lde, (uint32_t*)c->scratch.p));
-  const uint32_t* lde_a = lde;
-
   // C_j = coeff * (x^N - 1) with coeff = (B[N-1] - a0) w_last / N, where
   // B[N-1] is the actual last trace value (src/air.rs:366-371, 817-821).
   uint32_t omega_n = two_adic_generator(logN);
@@ -623,9 +655,22 @@ int air_prove(z0p_gpu_ctx* c, const z0p_air_params& p, Transcript& ts, uint8_t* 
     b_actual = fadd(fmul(r10, p.a0), fmul(r11, p.b0));
   }
   uint32_t coeff = fmul(fmul(fsub(b_actual, p.a0), w_last), finv((uint32_t)(N % P)));
+  ProofConsts* pc = c->consts;
+  pc->a0 = p.a0; pc->b0 = p.b0; pc->b_last = p.b_last;
+  pc->coeff = coeff;
+  CK(push_consts(c));
+  CK(launch::fib_trace(st, cols, cols + N, (uint32_t)N, (uint32_t)c->slot, mats));
+  NttPlan ip;
+  ip.logn = logN; ip.batch = 1; ip.inverse = 1; ip.post_gamma = 1;
+  CK(launch::ntt(st, c->tb, ip, cols, coeffs, (uint32_t*)c->scratch.p));
+  NttPlan lp;
+  lp.logn = logN; lp.batch = (uint32_t)B; lp.in_div = (uint32_t)B; lp.twist_mod = (uint32_t)B;
+  lp.twist_shift = 27 - logm;
+  CK(launch::ntt(st, c->tb, lp, coeffs, lde, (uint32_t*)c->scratch.p));
+  const uint32_t* lde_a = lde;
   uint32_t* cb = zinv2 + B;
   uint32_t gamma_n = fpow(GENERATOR, N);
-  CK(launch::coset_zinv(st, c->tb, zinv, zinv2, logB, to_mont(gamma_n), cb, coeff));
+  CK(launch::coset_zinv(st, c->tb, zinv, zinv2, logB, to_mont(gamma_n), cb, (uint32_t)c->slot));
   const uint32_t w_last_m = to_mont(w_last);
 
   // Joint trace tree over 8-row 64-byte leaves (src/air.rs:520-537).
@@ -653,17 +698,18 @@ int air_prove(z0p_gpu_ctx* c, const z0p_air_params& p, Transcript& ts, uint8_t* 
   ca.lde_a = lde_a; ca.cb = cb; ca.zinv = zinv; ca.tinv = tinv;
   ca.layer0 = fb.layer[0]; ca.leaves = fb.tree[0];
   ca.logN = logN; ca.logB = logB;
-  ca.a0 = p.a0; ca.b0 = p.b0; ca.b_last = p.b_last;
   ca.w_last_m = w_last_m;
+  ca.slot = (uint32_t)c->slot;
   const uint32_t omega_inv = finv(omega_n), neg_coeff = fsub(0, coeff);
   for (int e = 0; e < 4; e++) {
-    ca.alpha[e][0] = 0;
-    ca.alpha[e][1] = to_mont(alpha[1][e]);
-    ca.alpha[e][2] = to_mont(fmul(alpha[2][e], omega_inv));
-    ca.alpha[e][3] = to_mont(fmul(alpha[3][e], omega_inv));
-    ca.alpha[e][4] = to_mont(alpha[4][e]);
-    ca.kc[e] = fmul(alpha[0][e], neg_coeff);
+    pc->alpha[e][0] = 0;
+    pc->alpha[e][1] = to_mont(alpha[1][e]);
+    pc->alpha[e][2] = to_mont(fmul(alpha[2][e], omega_inv));
+    pc->alpha[e][3] = to_mont(fmul(alpha[3][e], omega_inv));
+    pc->alpha[e][4] = to_mont(alpha[4][e]);
+    pc->kc[e] = fmul(alpha[0][e], neg_coeff);
   }
+  CK(push_consts(c));
   CK(launch::air_compose_leaves(st, c->tb, ca));
   CK(launch::merkle_build(st, fb.tree[0], s.leaves[0], s.depth[0] - s.drop[0], merkle_counter(c),
                           hio_dev<uint32_t>(c, h.fri_cap[0])));
@@ -766,7 +812,8 @@ int range_prove(z0p_gpu_ctx* c, const z0p_range_params& p, Transcript& ts, uint8
   CK(launch::ntt(st, c->tb, lp, coeffs, lde, (uint32_t*)c->scratch.p));
   CK(launch::range_trace_leaves(st, lde, ttree, logN, logB, (uint32_t)ncol));
   CK(launch::merkle_build(st, ttree, m, tsteps, merkle_counter(c), hio_dev<uint32_t>(c, h.trace_cap)));
-  CK(launch::coset_zinv(st, c->tb, zinv, zinv2, logB, to_mont(fpow(GENERATOR, N)), nullptr, 0));
+  CK(launch::coset_zinv(st, c->tb, zinv, zinv2, logB, to_mont(fpow(GENERATOR, N)), nullptr,
+                        (uint32_t)c->slot));
   CK(sync(c, "cap"));
   std::vector<uint8_t> column_cap(c->hio + h.trace_cap, c->hio + h.trace_cap + (32ull << tdrop));
   c->d2h += column_cap.size();
@@ -781,7 +828,9 @@ int range_prove(z0p_gpu_ctx* c, const z0p_range_params& p, Transcript& ts, uint8
   ca.lde = lde; ca.zinv = zinv; ca.zinv2 = zinv2;
   ca.alphas = hio_dev<uint32_t>(c, h.extra) + ncol;
   ca.layer0 = fb.layer[0]; ca.leaves = fb.tree[0];
-  ca.logN = logN; ca.logB = logB; ca.n_bits = (uint32_t)p.n_bits; ca.value = p.value;
+  ca.logN = logN; ca.logB = logB; ca.n_bits = (uint32_t)p.n_bits; ca.slot = (uint32_t)c->slot;
+  c->consts->value = p.value;
+  CK(push_consts(c));
   CK(launch::range_compose_leaves(st, c->tb, ca));
   CK(launch::merkle_build(st, fb.tree[0], s.leaves[0], s.depth[0] - s.drop[0], merkle_counter(c),
                           hio_dev<uint32_t>(c, h.fri_cap[0])));
@@ -978,6 +1027,20 @@ int z0p_gpu_ctx_create(int device, z0p_gpu_ctx** out) {
     return Z0P_ERR_CUDA;
   }
   int rc = build_tables(c);
+  if (rc == Z0P_OK) {
+    c->slot = take_slot();
+    if (c->slot < 0) {
+      set_reason("context creation: every constant slot is taken (too many contexts)");
+      rc = Z0P_ERR_OUT_OF_MEMORY;
+    } else if (launch::const_slot_address(c->slot, &c->slot_dev) != cudaSuccess ||
+               cudaHostAlloc((void**)&c->consts, sizeof(ProofConsts), cudaHostAllocDefault) !=
+                   cudaSuccess) {
+      set_reason("context creation: constant slot setup failed");
+      rc = Z0P_ERR_CUDA;
+    } else {
+      std::memset(c->consts, 0, sizeof(ProofConsts));
+    }
+  }
   if (rc == Z0P_OK) rc = ensure(c, c->state, 64);
   if (rc == Z0P_OK) {
     // Merkle counter 0; PoW state {best = ~0, next chunk 0, status 0, done 0}.
@@ -1006,6 +1069,8 @@ void z0p_gpu_ctx_destroy(z0p_gpu_ctx* c) {
     release(c, *b);
   if (c->stream) cudaStreamSynchronize(c->stream);
   if (c->hio) cudaFreeHost(c->hio);
+  if (c->consts) cudaFreeHost(c->consts);
+  give_slot(c->slot);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }
@@ -1212,8 +1277,10 @@ int z0p_gpu_fri_fold(z0p_gpu_ctx* c, const uint32_t* d_in, uint64_t n, uint64_t 
   for (int k = 0; k < 3; k++) {
     uint32_t q[4];
     for (int e = 0; e < 4; e++) q[e] = fmul(ch[4 * k + e] % P, inv4);
-    e4_table(q, fa.tab[k]);
+    e4_table(q, c->consts->tab[k]);
   }
+  fa.slot = (uint32_t)c->slot;
+  CK(push_consts(c));
   uint32_t built = 0;
   CK(launch::fri_fold(c->stream, c->tb, fa, &built));  // top 0, no cap: leaves only
   CK(sync(c));
@@ -1271,7 +1338,9 @@ int z0p_gpu_grind(z0p_gpu_ctx* c, const uint8_t* head, size_t head_len, uint32_t
   std::lock_guard<std::mutex> lk(c->mu);
   RC(with_device(c));
   RC(ensure_hio(c, 16));
-  CK(launch::grind(c->stream, head, (uint32_t)head_len, bits, grind_state(c),
+  set_head(c->consts, head, head_len);
+  CK(push_consts(c));
+  CK(launch::grind(c->stream, (uint32_t)c->slot, (uint32_t)head_len, bits, grind_state(c),
                    hio_dev<unsigned long long>(c, 0), 1ull << 40));
   CK(sync(c));
   unsigned long long res[2];
