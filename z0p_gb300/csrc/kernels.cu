@@ -60,7 +60,10 @@ struct FibMats {
 __global__ void fib_trace_kernel(uint32_t* __restrict__ col_a, uint32_t* __restrict__ col_b,
                                  uint32_t n, uint32_t slot, FibMats mats,
                                  uint32_t per_thread) {
-  const uint32_t a0 = g_consts[slot].a0, b0 = g_consts[slot].b0;
+  const uint32_t pk = blockIdx.y;  // proof of the group
+  col_a += (size_t)pk * n;
+  col_b += (size_t)pk * n;
+  const uint32_t a0 = g_consts[slot + pk].a0, b0 = g_consts[slot + pk].b0;
   uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   uint64_t start = t * per_thread;
   if (start >= n) return;
@@ -89,9 +92,10 @@ __global__ void fib_trace_kernel(uint32_t* __restrict__ col_a, uint32_t* __restr
 
 __global__ void fill_columns_kernel(uint32_t* cols, uint32_t n, uint32_t ncols,
                                     const uint32_t* __restrict__ values) {
+  const uint32_t pk = blockIdx.y;
   uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= (uint64_t)n * ncols) return;
-  cols[i] = values[i / n];
+  cols[(uint64_t)pk * n * ncols + i] = values[(size_t)pk * ncols + i / n];
 }
 
 // ----------------------------------------------------------------- NTT ----
@@ -350,14 +354,17 @@ __global__ void __launch_bounds__(512) ntt_pass2_kernel(const uint32_t* __restri
 // linked-column constant C_j = coeff * (x^N - 1) (canonical).
 __global__ void coset_zinv_kernel(uint32_t* zinv, uint32_t* zinv2, uint32_t logB,
                                   uint32_t gamma_n_m, uint32_t* cb, uint32_t slot, Tables tb) {
+  const uint32_t pk = blockIdx.y;  // zinv is shared by the group; cb is per proof
   uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= (1u << logB)) return;
   uint32_t xn = mmul(gamma_n_m, root_pow(tb, j << (kRootBits - logB)));
   uint32_t xn1 = fsub(xn, kR);
-  uint32_t inv = minv(xn1);
-  zinv[j] = inv;
-  zinv2[j] = mmul(inv, kR2);
-  if (cb) cb[j] = mmul(g_consts[slot].coeff, xn1);
+  if (pk == 0) {
+    uint32_t inv = minv(xn1);
+    zinv[j] = inv;
+    zinv2[j] = mmul(inv, kR2);
+  }
+  if (cb) cb[((size_t)pk << logB) + j] = mmul(g_consts[slot + pk].coeff, xn1);
 }
 
 // B at row k = B q + j of the LDE from A: A[j][q+1] + C_j / (x_k - w_last),
@@ -424,8 +431,18 @@ constexpr uint32_t kTraceLeafThreads = 256;
 __global__ void __launch_bounds__(kTraceLeafThreads) air_trace_leaves_kernel(
     const uint32_t* __restrict__ lde_a, const uint32_t* __restrict__ cb, uint32_t w_last_m,
     uint32_t* __restrict__ leaves, uint32_t* __restrict__ tinv, uint32_t logN, uint32_t logB,
-    uint32_t nleaves, uint32_t top, uint32_t* cap, Tables tb) {
+    uint32_t nleaves, uint32_t top, uint32_t* cap, uint64_t tree_stride, uint64_t cap_stride,
+    Tables tb) {
   __shared__ uint32_t buf[2 * kTraceLeafThreads * 9];
+  {
+    const uint32_t pk = blockIdx.y;  // proof of the group
+    const size_t m = (size_t)nleaves * 8;
+    lde_a += pk * m;
+    cb += (size_t)pk << logB;
+    tinv += pk * m;
+    leaves += pk * tree_stride;
+    if (cap) cap += pk * cap_stride;
+  }
   const uint32_t nt = nleaves < kTraceLeafThreads ? nleaves : kTraceLeafThreads;
   const uint32_t L = blockIdx.x * kTraceLeafThreads + threadIdx.x;
   uint32_t d[8];
@@ -461,10 +478,12 @@ __global__ void __launch_bounds__(kTraceLeafThreads) air_trace_leaves_kernel(
 // coset-major order so column reads coalesce; digests land at index k.
 __global__ void range_trace_leaves_kernel(const uint32_t* __restrict__ lde,
                                           uint32_t* __restrict__ leaves, uint32_t logN,
-                                          uint32_t logB, uint32_t ncols) {
+                                          uint32_t logB, uint32_t ncols, uint64_t tree_stride) {
   uint32_t u = blockIdx.x * blockDim.x + threadIdx.x;
   uint32_t m = 1u << (logN + logB);
   if (u >= m) return;
+  lde += (size_t)blockIdx.y * ncols * m;
+  leaves += blockIdx.y * tree_stride;
   uint32_t j = u >> logN, q = u & ((1u << logN) - 1u);
   uint32_t k = (q << logB) | j;
   uint32_t w[32];
@@ -498,9 +517,13 @@ __global__ void range_trace_leaves_kernel(const uint32_t* __restrict__ lde,
 // One tree level; `cap` (may be null) receives a second copy of the level
 // when it is the tree's cap level.
 __global__ void merkle_level_kernel(const uint32_t* __restrict__ prev, uint32_t* __restrict__ next,
-                                    uint64_t count, uint32_t* __restrict__ cap) {
+                                    uint64_t count, uint32_t* __restrict__ cap, uint64_t stride,
+                                    uint64_t cap_stride) {
   uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= count) return;
+  prev += blockIdx.y * stride;
+  next += blockIdx.y * stride;
+  if (cap) cap += blockIdx.y * cap_stride;
   uint32_t l[8], r[8], d[8];
   load_digest(prev + 16 * i, l);
   load_digest(prev + 16 * i + 8, r);
@@ -510,9 +533,9 @@ __global__ void merkle_level_kernel(const uint32_t* __restrict__ prev, uint32_t*
 }
 
 __global__ void copy_words_kernel(const uint32_t* __restrict__ src, uint32_t* __restrict__ dst,
-                                  uint64_t n) {
+                                  uint64_t n, uint64_t src_stride, uint64_t dst_stride) {
   uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) dst[i] = src[i];
+  if (i < n) dst[blockIdx.y * dst_stride + i] = src[blockIdx.y * src_stride + i];
 }
 
 // Upper levels of a tree without a grid barrier: CTA b hashes the 2T nodes
@@ -544,9 +567,13 @@ __device__ __forceinline__ void hash_pair_smem(const uint32_t* pair, uint32_t* o
 __global__ void __launch_bounds__(kTopThreads) merkle_top_kernel(uint32_t* tree, uint64_t leaves,
                                                                  uint32_t l0, uint32_t top,
                                                                  unsigned int* counter,
-                                                                 uint32_t* cap) {
+                                                                 uint32_t* cap, uint64_t stride,
+                                                                 uint64_t cap_stride) {
   __shared__ uint32_t sm[2][kTopMaxRoots * kTopStride];
   __shared__ int last;
+  tree += blockIdx.y * stride;  // proof of the group: its tree, counter and cap
+  counter += blockIdx.y;
+  if (cap) cap += blockIdx.y * cap_stride;
   const uint32_t lsub = l0 + 9 < top ? l0 + 9 : top;  // last level done per CTA
   // level l0+1: thread t hashes children 2(base+t), 2(base+t)+1
   uint64_t cnt = leaves >> (l0 + 1);                    // nodes at level l0+1
@@ -612,9 +639,12 @@ __global__ void __launch_bounds__(kTopThreads) merkle_top_kernel(uint32_t* tree,
 // Leaf digests i < npad of `count` 64-byte leaves; i >= count repeats the
 // last leaf (power-of-two padding, src/merkle.rs:350-360).
 __global__ void leaf64_kernel(const uint32_t* __restrict__ flat, uint32_t* __restrict__ leaves,
-                              uint64_t count, uint64_t npad) {
+                              uint64_t count, uint64_t npad, uint64_t in_stride,
+                              uint64_t out_stride) {
   uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= npad) return;
+  flat += blockIdx.y * in_stride;
+  leaves += blockIdx.y * out_stride;
   uint32_t m[16];
   const uint4* p = reinterpret_cast<const uint4*>(flat + 16 * (i < count ? i : count - 1));
 #pragma unroll
@@ -630,9 +660,11 @@ __global__ void leaf64_kernel(const uint32_t* __restrict__ flat, uint32_t* __res
 // 0x00-prefixed 16-byte leaves for layers whose length is not a multiple of
 // four (src/fri.rs:1422-1428).
 __global__ void leaf16_kernel(const uint32_t* __restrict__ values, uint32_t* __restrict__ leaves,
-                              uint64_t n) {
+                              uint64_t n, uint64_t in_stride, uint64_t out_stride) {
   uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
+  values += blockIdx.y * in_stride;
+  leaves += blockIdx.y * out_stride;
   uint32_t w[4] = {values[4 * i], values[4 * i + 1], values[4 * i + 2], values[4 * i + 3]};
   uint32_t d[8];
   blake3_prefixed_leaf<4>(w, d);
@@ -668,6 +700,15 @@ __global__ void __launch_bounds__(kThreads) air_compose_leaves_kernel(AirCompose
   const uint32_t quarter = 1u << (logm - 2);
   uint32_t u = blockIdx.x * blockDim.x + threadIdx.x;
   if (u >= quarter) return;
+  {
+    const uint32_t pk = blockIdx.y;  // proof of the group
+    a.lde_a += (size_t)pk << logm;
+    a.tinv += (size_t)pk << logm;
+    a.cb += (size_t)pk << a.logB;
+    a.layer0 += pk * a.layer_stride;
+    a.leaves += pk * a.tree_stride;
+    a.slot += pk;
+  }
   const uint32_t N = 1u << a.logN, B = 1u << a.logB;
   uint32_t k0;
   if (a.logN >= 2) {
@@ -725,6 +766,14 @@ __global__ void __launch_bounds__(kThreads) range_compose_leaves_kernel(RangeCom
   const uint32_t quarter = 1u << (logm - 2);
   uint32_t u = blockIdx.x * blockDim.x + threadIdx.x;
   if (u >= quarter) return;
+  {
+    const uint32_t pk = blockIdx.y;  // proof of the group
+    a.lde += ((size_t)pk * (a.n_bits + 1)) << logm;
+    a.alphas += (size_t)pk * 4 * (a.n_bits + 2);
+    a.layer0 += pk * a.layer_stride;
+    a.leaves += pk * a.tree_stride;
+    a.slot += pk;
+  }
   const uint32_t N = 1u << a.logN, B = 1u << a.logB;
   uint32_t k0;
   if (a.logN >= 2) {
@@ -816,8 +865,18 @@ __device__ __forceinline__ uint32_t quad_xinv(const Tables& tb, const FoldArgs& 
 // Thread per next-layer leaf: folds four quads (256 contiguous input bytes,
 // staged through shared memory), writes the 64-byte next leaf and its digest.
 constexpr int kFoldThreads = 128;
+__device__ __forceinline__ void fold_for_proof(FoldArgs& a) {
+  const uint32_t pk = blockIdx.y;  // proof of the group
+  a.in += pk * a.in_stride;
+  a.out += pk * a.out_stride;
+  a.leaves += pk * a.tree_stride;
+  if (a.cap) a.cap += pk * a.cap_stride;
+  a.slot += pk;
+}
+
 __global__ void __launch_bounds__(kFoldThreads) fri_fold_leaf_kernel(FoldArgs a, Tables tb) {
   __shared__ uint32_t sm[2 * kFoldThreads * 9];  // the next layer's subtree (small trees)
+  fold_for_proof(a);
   const uint64_t nleaf = 1ull << (a.logn - 4);
   const uint64_t first = (uint64_t)blockIdx.x * kFoldThreads;
   const uint32_t avail = nleaf < (uint64_t)kFoldThreads ? (uint32_t)nleaf : (uint32_t)kFoldThreads;
@@ -853,6 +912,7 @@ __global__ void __launch_bounds__(kFoldThreads) fri_fold_leaf_kernel(FoldArgs a,
 
 // Thread per next-layer value (small layers; leaves hashed separately).
 __global__ void fri_fold_plain_kernel(FoldArgs a, Tables tb) {
+  fold_for_proof(a);
   uint32_t P = blockIdx.x * blockDim.x + threadIdx.x;
   if (P >= (1u << (a.logn - 2))) return;
   E4 q[4];
@@ -904,6 +964,9 @@ __device__ __forceinline__ void grind_finish(const GrindArgs& a) {
 
 template <int H>
 __global__ void __launch_bounds__(kGrindThreads) grind_kernel(GrindArgs a) {
+  a.slot += blockIdx.y;  // proof of the group: its head, search state and result
+  a.state += 4 * blockIdx.y;
+  a.out += 2 * blockIdx.y;
   static_assert(H + 8 <= 64, "head and nonce must fit one block");
   constexpr int W = H / 4, SH = (H % 4) * 8;
   __shared__ unsigned long long s_chunk;
@@ -987,22 +1050,29 @@ __global__ void __launch_bounds__(256) hash_ceiling_kernel(const uint32_t* __res
 // (src/fri.rs:1229-1260 for FRI, src/air.rs:565-591 and src/range.rs:483-500
 // for the trace). One CTA per query; the block layout is OpenArgs'.
 __global__ void __launch_bounds__(128) openings_kernel(OpenArgs a) {
-  const uint32_t qi = blockIdx.x;
-  uint32_t* out = a.out + (size_t)qi * a.stride;
-  const uint64_t leaf = a.indices[qi];
+  const uint32_t qi = blockIdx.x, pk = blockIdx.y;  // query, proof of the group
+  uint32_t* out = a.out + ((size_t)pk * a.nq + qi) * a.stride;
+  const uint64_t leaf = a.indices[(size_t)pk * a.nq + qi];
+  const uint64_t vo = pk * a.fri_val_stride, to = pk * a.fri_tree_stride;
+  a.lde += pk * a.lde_stride;
+  a.ttree += pk * a.ttree_stride;
+  if (a.cb) a.cb += (size_t)pk << a.logB;
+  if (a.tinv) a.tinv += (size_t)pk << (a.logN + a.logB);
   // FRI layers: 16 words of values, then steps x 8 words of siblings.
   for (uint32_t d = 0; d < a.nlayers; d++) {
     const OpenLayer& L = a.layer[d];
     const uint64_t base = (leaf >> (2 * d)) & ~3ull;
     const uint64_t Q = base >> 2;
     uint32_t* o = out + L.off;
+    const uint32_t* values = L.values + vo;
+    const uint32_t* tree = L.tree + to;
     for (uint32_t t = threadIdx.x; t < 16 + 8 * L.steps; t += blockDim.x) {
       if (t < 16) {
-        o[t] = L.values[4 * base + t];
+        o[t] = values[4 * base + t];
       } else {
         const uint32_t st = (t - 16) >> 3, w = (t - 16) & 7u;
         const uint64_t sib = (Q >> st) ^ 1ull;
-        o[t] = L.tree[8 * (2 * L.leaves - 2 * (L.leaves >> st) + sib) + w];
+        o[t] = tree[8 * (2 * L.leaves - 2 * (L.leaves >> st) + sib) + w];
       }
     }
   }
@@ -1092,7 +1162,7 @@ cudaError_t const_slot_address(int slot, void** ptr) {
 }
 
 cudaError_t fib_trace(cudaStream_t st, uint32_t* col_a, uint32_t* col_b, uint32_t n, uint32_t slot,
-                      const uint32_t mats[32][4]) {
+                      const uint32_t mats[32][4], uint32_t nproofs) {
   FibMats fm;
   for (int k = 0; k < 32; k++)
     for (int i = 0; i < 4; i++) fm.m[k][i] = mats[k][i];
@@ -1100,15 +1170,17 @@ cudaError_t fib_trace(cudaStream_t st, uint32_t* col_a, uint32_t* col_b, uint32_
   uint64_t threads = (n + per - 1) / per;
   Stage stg("trace", st);
   stg.launched();
-  fib_trace_kernel<<<grid_for(threads), kThreads, 0, st>>>(col_a, col_b, n, slot, fm, per);
+  fib_trace_kernel<<<dim3(grid_for(threads), nproofs), kThreads, 0, st>>>(col_a, col_b, n, slot, fm,
+                                                                          per);
   return cudaGetLastError();
 }
 
 cudaError_t fill_constant_columns(cudaStream_t st, uint32_t* cols, uint32_t n, uint32_t ncols,
-                                  const uint32_t* d_values) {
+                                  const uint32_t* d_values, uint32_t nproofs) {
   Stage stg("fill_columns", st);
   stg.launched();
-  fill_columns_kernel<<<grid_for((uint64_t)n * ncols), kThreads, 0, st>>>(cols, n, ncols, d_values);
+  fill_columns_kernel<<<dim3(grid_for((uint64_t)n * ncols), nproofs), kThreads, 0, st>>>(cols, n, ncols,
+                                                                                       d_values);
   return cudaGetLastError();
 }
 
@@ -1208,18 +1280,20 @@ cudaError_t ntt(cudaStream_t st, const Tables& tb, const NttPlan& plan, const ui
 }
 
 cudaError_t coset_zinv(cudaStream_t st, const Tables& tb, uint32_t* zinv, uint32_t* zinv2,
-                       uint32_t logB, uint32_t gamma_n_m, uint32_t* cb, uint32_t slot) {
+                       uint32_t logB, uint32_t gamma_n_m, uint32_t* cb, uint32_t slot,
+                       uint32_t nproofs) {
   Stage stg("coset_zinv", st);
   stg.launched();
-  coset_zinv_kernel<<<grid_for(1ull << logB), kThreads, 0, st>>>(zinv, zinv2, logB, gamma_n_m, cb,
-                                                                 slot, tb);
+  coset_zinv_kernel<<<dim3(grid_for(1ull << logB), nproofs), kThreads, 0, st>>>(
+      zinv, zinv2, logB, gamma_n_m, cb, slot, tb);
   return cudaGetLastError();
 }
 
 cudaError_t air_trace_leaves(cudaStream_t st, const Tables& tb, const uint32_t* lde_a,
                              const uint32_t* cb, uint32_t w_last_m, uint32_t* leaves,
                              uint32_t* tinv, uint32_t logN, uint32_t logB, uint32_t top,
-                             uint32_t* cap, uint32_t* levels) {
+                             uint32_t* cap, uint32_t* levels, uint32_t nproofs,
+                             uint64_t tree_stride, uint64_t cap_stride) {
   uint32_t nleaves = 1u << (logN + logB - 3);
   if (nleaves > kFuseMaxLeaves) {
     top = 0;  // no subtree; merkle_build does every level
@@ -1228,29 +1302,33 @@ cudaError_t air_trace_leaves(cudaStream_t st, const Tables& tb, const uint32_t* 
   *levels = subtree_levels(nleaves < kTraceLeafThreads ? nleaves : kTraceLeafThreads, top);
   Stage stg("trace_leaves", st);
   stg.launched();
-  air_trace_leaves_kernel<<<grid_for(nleaves, kTraceLeafThreads), kTraceLeafThreads, 0, st>>>(
-      lde_a, cb, w_last_m, leaves, tinv, logN, logB, nleaves, top, cap, tb);
+  air_trace_leaves_kernel<<<dim3(grid_for(nleaves, kTraceLeafThreads), nproofs), kTraceLeafThreads,
+                            0, st>>>(lde_a, cb, w_last_m, leaves, tinv, logN, logB, nleaves, top, cap,
+                                     tree_stride, cap_stride, tb);
   return cudaGetLastError();
 }
 
 cudaError_t range_trace_leaves(cudaStream_t st, const uint32_t* lde, uint32_t* leaves,
-                               uint32_t logN, uint32_t logB, uint32_t ncols) {
+                               uint32_t logN, uint32_t logB, uint32_t ncols, uint32_t nproofs,
+                               uint64_t tree_stride) {
   if (ncols < 1 || ncols > 25) return cudaErrorInvalidValue;
   Stage stg("trace_leaves", st);
   stg.launched();
-  range_trace_leaves_kernel<<<grid_for(1ull << (logN + logB)), kThreads, 0, st>>>(lde, leaves, logN,
-                                                                                logB, ncols);
+  range_trace_leaves_kernel<<<dim3(grid_for(1ull << (logN + logB)), nproofs), kThreads, 0, st>>>(
+      lde, leaves, logN, logB, ncols, tree_stride);
   return cudaGetLastError();
 }
 
 cudaError_t merkle_build(cudaStream_t st, uint32_t* tree, uint64_t leaves, uint32_t top,
-                         unsigned int* counter, uint32_t* cap, uint32_t from) {
+                         unsigned int* counter, uint32_t* cap, uint32_t from, uint32_t nproofs,
+                         uint64_t stride, uint64_t cap_stride) {
   if (from > 0 && from >= top) return cudaSuccess;  // the leaf kernel built up to the cap
   Stage stg("merkle_levels", st);
   if (top == 0) {  // the cap is the leaf level itself
     if (!cap) return cudaSuccess;
     stg.launched();
-    copy_words_kernel<<<grid_for(8 * leaves), kThreads, 0, st>>>(tree, cap, 8 * leaves);
+    copy_words_kernel<<<dim3(grid_for(8 * leaves), nproofs), kThreads, 0, st>>>(tree, cap, 8 * leaves,
+                                                                               stride, cap_stride);
     return cudaGetLastError();
   }
   // Levels with more than 2^16 nodes fill the GPU on their own: one launch
@@ -1264,8 +1342,8 @@ cudaError_t merkle_build(cudaStream_t st, uint32_t* tree, uint64_t leaves, uint3
     const uint32_t* prev = tree + 8 * (2 * leaves - 2 * (leaves >> level));
     uint32_t* next = tree + 8 * (2 * leaves - 2 * (leaves >> (level + 1)));
     stg.launched();
-    merkle_level_kernel<<<grid_for(cnt), kThreads, 0, st>>>(prev, next, cnt,
-                                                            level + 1 == top ? cap : nullptr);
+    merkle_level_kernel<<<dim3(grid_for(cnt), nproofs), kThreads, 0, st>>>(
+        prev, next, cnt, level + 1 == top ? cap : nullptr, stride, cap_stride);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     level++;
@@ -1275,27 +1353,31 @@ cudaError_t merkle_build(cudaStream_t st, uint32_t* tree, uint64_t leaves, uint3
   const uint64_t per_cta_children = 2ull << (lsub - level - 1);  // level-l0 nodes per CTA
   const uint64_t blocks = ((leaves >> level) + per_cta_children - 1) / per_cta_children;
   stg.launched();
-  merkle_top_kernel<<<(unsigned)blocks, kTopThreads, 0, st>>>(tree, leaves, level, top, counter, cap);
+  merkle_top_kernel<<<dim3((unsigned)blocks, nproofs), kTopThreads, 0, st>>>(
+      tree, leaves, level, top, counter, cap, stride, cap_stride);
   return cudaGetLastError();
 }
 
-cudaError_t air_compose_leaves(cudaStream_t st, const Tables& tb, const AirComposeArgs& a) {
+cudaError_t air_compose_leaves(cudaStream_t st, const Tables& tb, const AirComposeArgs& a,
+                               uint32_t nproofs) {
   uint32_t quarter = 1u << (a.logN + a.logB - 2);
   Stage stg("air_compose_leaves", st);
   stg.launched();
-  air_compose_leaves_kernel<<<grid_for(quarter), kThreads, 0, st>>>(a, tb);
+  air_compose_leaves_kernel<<<dim3(grid_for(quarter), nproofs), kThreads, 0, st>>>(a, tb);
   return cudaGetLastError();
 }
 
-cudaError_t range_compose_leaves(cudaStream_t st, const Tables& tb, const RangeComposeArgs& a) {
+cudaError_t range_compose_leaves(cudaStream_t st, const Tables& tb, const RangeComposeArgs& a,
+                                 uint32_t nproofs) {
   uint32_t quarter = 1u << (a.logN + a.logB - 2);
   Stage stg("range_compose_leaves", st);
   stg.launched();
-  range_compose_leaves_kernel<<<grid_for(quarter), kThreads, 0, st>>>(a, tb);
+  range_compose_leaves_kernel<<<dim3(grid_for(quarter), nproofs), kThreads, 0, st>>>(a, tb);
   return cudaGetLastError();
 }
 
-cudaError_t fri_fold(cudaStream_t st, const Tables& tb, const FoldArgs& a, uint32_t* levels) {
+cudaError_t fri_fold(cudaStream_t st, const Tables& tb, const FoldArgs& a, uint32_t* levels,
+                     uint32_t nproofs) {
   *levels = 0;
   if (a.logn < 2) return cudaErrorInvalidValue;
   if (a.logn >= 4) {
@@ -1308,26 +1390,31 @@ cudaError_t fri_fold(cudaStream_t st, const Tables& tb, const FoldArgs& a, uint3
     *levels = subtree_levels(nleaf < (uint64_t)kFoldThreads ? (uint32_t)nleaf : kFoldThreads, f.top);
     Stage stg("fri_fold_leaves", st);
     stg.launched();
-    fri_fold_leaf_kernel<<<grid_for(nleaf, kFoldThreads), kFoldThreads, 0, st>>>(f, tb);
+    fri_fold_leaf_kernel<<<dim3(grid_for(nleaf, kFoldThreads), nproofs), kFoldThreads, 0, st>>>(f, tb);
     return cudaGetLastError();
   }
   {
     Stage stg("fri_fold_small", st);
     stg.launched();
-    fri_fold_plain_kernel<<<1, 32, 0, st>>>(a, tb);
+    fri_fold_plain_kernel<<<dim3(1, nproofs), 32, 0, st>>>(a, tb);
   }
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  return layer_leaves(st, a.out, 1ull << (a.logn - 2), a.leaves);
+  return layer_leaves(st, a.out, 1ull << (a.logn - 2), a.leaves, nproofs, a.out_stride,
+                      a.tree_stride);
 }
 
-cudaError_t layer_leaves(cudaStream_t st, const uint32_t* values, uint64_t len, uint32_t* leaves) {
+cudaError_t layer_leaves(cudaStream_t st, const uint32_t* values, uint64_t len, uint32_t* leaves,
+                         uint32_t nproofs, uint64_t in_stride, uint64_t out_stride) {
   Stage stg("layer_leaves", st);
   stg.launched();
   if (len % 4 == 0) {
-    leaf64_kernel<<<grid_for(len / 4), kThreads, 0, st>>>(values, leaves, len / 4, len / 4);
+    leaf64_kernel<<<dim3(grid_for(len / 4), nproofs), kThreads, 0, st>>>(values, leaves, len / 4,
+                                                                        len / 4, in_stride,
+                                                                        out_stride);
   } else {
-    leaf16_kernel<<<grid_for(len), kThreads, 0, st>>>(values, leaves, len);
+    leaf16_kernel<<<dim3(grid_for(len), nproofs), kThreads, 0, st>>>(values, leaves, len, in_stride,
+                                                                    out_stride);
   }
   return cudaGetLastError();
 }
@@ -1337,15 +1424,16 @@ cudaError_t merkle_flat64_leaves(cudaStream_t st, const uint32_t* flat, uint64_t
   if (!count || npad < count) return cudaErrorInvalidValue;
   Stage stg("leaf64", st);
   stg.launched();
-  leaf64_kernel<<<grid_for(npad), kThreads, 0, st>>>(flat, leaves, count, npad);
+  leaf64_kernel<<<grid_for(npad), kThreads, 0, st>>>(flat, leaves, count, npad, 0, 0);
   return cudaGetLastError();
 }
 
 bool grind_supports(uint32_t head_len) { return head_len == 47; }
 
 cudaError_t grind(cudaStream_t st, uint32_t slot, uint32_t head_len, uint32_t bits,
-                  unsigned long long* state, unsigned long long* out, uint64_t max_nonces) {
-  if (!grind_supports(head_len) || bits > 32 || slot >= (uint32_t)kConstSlots)
+                  unsigned long long* state, unsigned long long* out, uint64_t max_nonces,
+                  uint32_t nproofs) {
+  if (!grind_supports(head_len) || bits > 32 || slot + nproofs > (uint32_t)kConstSlots)
     return cudaErrorInvalidValue;
   GrindArgs a;
   a.slot = slot;
@@ -1370,7 +1458,7 @@ cudaError_t grind(cudaStream_t st, uint32_t slot, uint32_t head_len, uint32_t bi
   if (ctas < sms) ctas = sms;
   Stage stg("grind", st);
   stg.launched();
-  grind_kernel<47><<<ctas, kGrindThreads, 0, st>>>(a);
+  grind_kernel<47><<<dim3(ctas, nproofs), kGrindThreads, 0, st>>>(a);
   return cudaGetLastError();
 }
 
@@ -1380,12 +1468,12 @@ cudaError_t hash_ceiling(cudaStream_t st, const uint32_t* in, uint32_t* out, uin
   return cudaGetLastError();
 }
 
-cudaError_t openings(cudaStream_t st, const OpenArgs& a) {
+cudaError_t openings(cudaStream_t st, const OpenArgs& a, uint32_t nproofs) {
   if (a.nlayers > kMaxOpenLayers) return cudaErrorInvalidValue;
   if (!a.nq) return cudaSuccess;
   Stage stg("gather", st);
   stg.launched();
-  openings_kernel<<<a.nq, 128, 0, st>>>(a);
+  openings_kernel<<<dim3(a.nq, nproofs), 128, 0, st>>>(a);
   return cudaGetLastError();
 }
 

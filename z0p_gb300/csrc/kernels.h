@@ -59,7 +59,8 @@ struct AirComposeArgs {
   uint32_t* leaves;       // layer-0 tree, leaf digests
   uint32_t logN, logB;
   uint32_t w_last_m;      // omega_N^(N-1) (Montgomery)
-  uint32_t slot;          // ProofConsts slot: statement, alphas, kc
+  uint32_t slot;          // ProofConsts slot of the first proof: statement, alphas, kc
+  uint64_t layer_stride = 0, tree_stride = 0;  // per-proof strides (words) of layer0 / leaves
 };
 
 struct RangeComposeArgs {
@@ -70,7 +71,8 @@ struct RangeComposeArgs {
   uint32_t* layer0;
   uint32_t* leaves;
   uint32_t logN, logB, n_bits;
-  uint32_t slot;  // ProofConsts slot: the claimed value
+  uint32_t slot;  // ProofConsts slot of the first proof: the claimed value
+  uint64_t layer_stride = 0, tree_stride = 0;  // per-proof strides (words) of layer0 / leaves
 };
 
 struct FoldArgs {
@@ -82,7 +84,9 @@ struct FoldArgs {
   uint32_t logn;
   uint32_t ginv_m;     // (31^(4^depth))^-1 (Montgomery)
   uint32_t unit_m;     // two_adic_generator(2) (Montgomery)
-  uint32_t slot = 0;   // ProofConsts slot: the fold's challenge tables
+  uint32_t slot = 0;   // ProofConsts slot of the first proof: the fold's challenge tables
+  // Per-proof strides (words) of in, out, leaves and cap for a proof group.
+  uint64_t in_stride = 0, out_stride = 0, tree_stride = 0, cap_stride = 0;
 };
 
 // Openings of one proof, gathered on the device into one block per query.
@@ -101,8 +105,8 @@ struct OpenLayer {
   uint32_t off;            // word offset of this layer inside a query block
 };
 struct OpenArgs {
-  const uint64_t* indices;  // nq FRI query indices (layer-0 positions)
-  uint32_t* out;            // nq blocks of `stride` words
+  const uint64_t* indices;  // nq FRI query indices (layer-0 positions) per proof
+  uint32_t* out;            // nq blocks of `stride` words per proof
   uint32_t nq, nlayers, stride, trace_off;
   OpenLayer layer[kMaxOpenLayers];
   const uint32_t* lde;      // AIR: column A coset-major; range: ncol columns
@@ -112,6 +116,9 @@ struct OpenArgs {
   uint64_t tleaves;
   uint32_t tsteps, logN, logB;
   uint32_t ncol;            // 0 for the AIR, else the range AIR's column count
+  // Per-proof strides (words) for a proof group: FRI layer values and trees,
+  // trace LDE and trace tree (cb and tinv follow from B and m).
+  uint64_t fri_val_stride = 0, fri_tree_stride = 0, lde_stride = 0, ttree_stride = 0;
 };
 
 // Product table of the Fp4 constant r (canonical coordinates) in the layout
@@ -142,17 +149,24 @@ void set_recorder(StageRecorder* r);
 cudaError_t const_slot_address(int slot, void** ptr);
 
 // (a0, b0) from the slot.
+//
+// Proof groups: the launchers below take `nproofs` proofs of one shape at
+// once (grid y = proof). Proof k's buffers sit at the given per-proof strides
+// from proof 0's, its ProofConsts in slot + k, and its counters and search
+// state at index k.
 cudaError_t fib_trace(cudaStream_t st, uint32_t* col_a, uint32_t* col_b, uint32_t n, uint32_t slot,
-                      const uint32_t mats[32][4]);
+                      const uint32_t mats[32][4], uint32_t nproofs = 1);
+// Proof k: cols + k n ncols, values + k ncols.
 cudaError_t fill_constant_columns(cudaStream_t st, uint32_t* cols, uint32_t n, uint32_t ncols,
-                                  const uint32_t* h_values);
+                                  const uint32_t* d_values, uint32_t nproofs = 1);
 cudaError_t ntt(cudaStream_t st, const Tables& tb, const NttPlan& plan, const uint32_t* in,
                 uint32_t* out, uint32_t* scratch);
 // Per coset j (x^N = 31^N omega_B^j): zinv = 1/(x^N - 1) (Montgomery),
 // zinv2 = zinv * 2^32, and, when cb is non-null, cb = coeff * (x^N - 1)
 // (canonical; coeff from the slot), the linked-column constant.
 cudaError_t coset_zinv(cudaStream_t st, const Tables& tb, uint32_t* zinv, uint32_t* zinv2,
-                       uint32_t logB, uint32_t gamma_n_m, uint32_t* cb, uint32_t slot);
+                       uint32_t logB, uint32_t gamma_n_m, uint32_t* cb, uint32_t slot,
+                       uint32_t nproofs = 1);
 // Trace leaves of the AIR: rows 8L..8L+7 as A || B with B derived from A.
 // Also writes tinv (m words, coset-major): 1 / (x - w_last) per LDE row.
 // The kernel also hashes each CTA's subtree (up to the cap level `top`;
@@ -161,9 +175,11 @@ cudaError_t coset_zinv(cudaStream_t st, const Tables& tb, uint32_t* zinv, uint32
 cudaError_t air_trace_leaves(cudaStream_t st, const Tables& tb, const uint32_t* lde_a,
                              const uint32_t* cb, uint32_t w_last_m, uint32_t* leaves,
                              uint32_t* tinv, uint32_t logN, uint32_t logB, uint32_t top,
-                             uint32_t* cap, uint32_t* levels);
+                             uint32_t* cap, uint32_t* levels, uint32_t nproofs = 1,
+                             uint64_t tree_stride = 0, uint64_t cap_stride = 0);
 cudaError_t range_trace_leaves(cudaStream_t st, const uint32_t* lde, uint32_t* leaves,
-                               uint32_t logN, uint32_t logB, uint32_t ncols);
+                               uint32_t logN, uint32_t logB, uint32_t ncols, uint32_t nproofs = 1,
+                               uint64_t tree_stride = 0);
 // Builds levels 1..top of a tree stored level-contiguous (level l at digest
 // offset 2L - 2(L >> l), L = leaves, power of two). Levels above the cap
 // level are never read (caps and capped paths stop there), so callers pass
@@ -174,16 +190,21 @@ cudaError_t range_trace_leaves(cudaStream_t st, const uint32_t* lde, uint32_t* l
 // of level `top`, 32 bytes per node.
 // Levels below `from` must already be built (0: from the leaves).
 cudaError_t merkle_build(cudaStream_t st, uint32_t* tree, uint64_t leaves, uint32_t top,
-                         unsigned int* counter, uint32_t* cap, uint32_t from = 0);
-cudaError_t air_compose_leaves(cudaStream_t st, const Tables& tb, const AirComposeArgs& a);
-cudaError_t range_compose_leaves(cudaStream_t st, const Tables& tb, const RangeComposeArgs& a);
+                         unsigned int* counter, uint32_t* cap, uint32_t from = 0,
+                         uint32_t nproofs = 1, uint64_t stride = 0, uint64_t cap_stride = 0);
+cudaError_t air_compose_leaves(cudaStream_t st, const Tables& tb, const AirComposeArgs& a,
+                               uint32_t nproofs = 1);
+cudaError_t range_compose_leaves(cudaStream_t st, const Tables& tb, const RangeComposeArgs& a,
+                                 uint32_t nproofs = 1);
 // Folds one FRI layer; hashes the next layer's 64-byte leaves when it has a
 // multiple of four values, its 0x00-prefixed 16-byte leaves otherwise. With
 // 64-byte leaves it also hashes each CTA's subtree up to a.top (writing the
 // cap level to a.cap); *levels receives the levels done above the leaves.
-cudaError_t fri_fold(cudaStream_t st, const Tables& tb, const FoldArgs& a, uint32_t* levels);
+cudaError_t fri_fold(cudaStream_t st, const Tables& tb, const FoldArgs& a, uint32_t* levels,
+                     uint32_t nproofs = 1);
 // Leaf digests of an FRI layer held in memory (64-byte quads or 16-byte values).
-cudaError_t layer_leaves(cudaStream_t st, const uint32_t* values, uint64_t len, uint32_t* leaves);
+cudaError_t layer_leaves(cudaStream_t st, const uint32_t* values, uint64_t len, uint32_t* leaves,
+                         uint32_t nproofs = 1, uint64_t in_stride = 0, uint64_t out_stride = 0);
 // Digests of `count` 64-byte leaves, padded to npad (a power of two) by
 // repeating the last leaf.
 cudaError_t merkle_flat64_leaves(cudaStream_t st, const uint32_t* flat, uint64_t count,
@@ -193,12 +214,13 @@ cudaError_t merkle_flat64_leaves(cudaStream_t st, const uint32_t* flat, uint64_t
 // receives {best nonce, status}, status 1 when the nonce cap was reached.
 // The head comes from the slot (head_len bytes).
 cudaError_t grind(cudaStream_t st, uint32_t slot, uint32_t head_len, uint32_t bits,
-                  unsigned long long* state, unsigned long long* out, uint64_t max_nonces);
+                  unsigned long long* state, unsigned long long* out, uint64_t max_nonces,
+                  uint32_t nproofs = 1);
 bool grind_supports(uint32_t head_len);
 // Reorders `batch` coset-major LDEs ([j][q]) into natural order ([B q + j]).
 cudaError_t coset_to_natural(cudaStream_t st, const uint32_t* in, uint32_t* out, uint32_t logN,
                              uint32_t logB, uint64_t batch);
-cudaError_t openings(cudaStream_t st, const OpenArgs& a);
+cudaError_t openings(cudaStream_t st, const OpenArgs& a, uint32_t nproofs = 1);
 // blocks x 256 threads, each chaining `iters` node hashes from 16 words of
 // `in` (blocks * 256 * 64 bytes) and writing 8 words of `out`.
 cudaError_t hash_ceiling(cudaStream_t st, const uint32_t* in, uint32_t* out, uint32_t blocks,
