@@ -191,6 +191,22 @@ int z0p_gpu_range_prove(z0p_gpu_ctx *ctx, const z0p_range_params *params,
                         z0p_transcript_state *transcript, uint8_t *out, size_t cap,
                         size_t *len);
 
+/* Proof groups (no counterpart in the reference): n statements of one shape
+ * -- the same n_steps / n_rows (and n_bits), blowup, num_queries,
+ * final_size, grinding_bits and cap_height -- proved in lockstep, so each
+ * kernel launch and each host round trip serves the whole group. Proof i
+ * lands in outs[i] (caps[i] bytes; lens[i] receives its length when lens is
+ * non-null) with transcripts[i] advanced exactly as z0p_gpu_air_prove /
+ * z0p_gpu_range_prove would leave it for that statement alone; on any error
+ * no transcript is changed. Groups larger than the library's group limit are
+ * proved in consecutive groups. */
+int z0p_gpu_air_prove_group(z0p_gpu_ctx *ctx, size_t n, const z0p_air_params *params,
+                            z0p_transcript_state *const *transcripts, uint8_t *const *outs,
+                            const size_t *caps, size_t *lens);
+int z0p_gpu_range_prove_group(z0p_gpu_ctx *ctx, size_t n, const z0p_range_params *params,
+                              z0p_transcript_state *const *transcripts, uint8_t *const *outs,
+                              const size_t *caps, size_t *lens);
+
 /* ------------------------------------------------- batching / serving ---- */
 /*
  * Many independent proofs (the batched and served configurations). A pool

@@ -106,6 +106,10 @@ def lib():
             "z0p_gpu_ctx_profile": (C.c_int, [vp, C.c_char_p, sz, P(sz)]),
             "z0p_gpu_air_prove": (C.c_int, [vp, P(AirParams), P(TranscriptState), u8p, sz, P(sz)]),
             "z0p_gpu_range_prove": (C.c_int, [vp, P(RangeParams), P(TranscriptState), u8p, sz, P(sz)]),
+            "z0p_gpu_air_prove_group": (C.c_int, [vp, sz, P(AirParams), P(P(TranscriptState)),
+                                                  P(u8p), P(sz), P(sz)]),
+            "z0p_gpu_range_prove_group": (C.c_int, [vp, sz, P(RangeParams), P(P(TranscriptState)),
+                                                    P(u8p), P(sz), P(sz)]),
             "z0p_gpu_rs_extend": (C.c_int, [vp, vp, C.c_uint64, C.c_uint64, C.c_uint64, vp]),
             "z0p_gpu_rs_extend_noalloc": (C.c_int, [vp, C.c_uint64, C.c_uint64, C.c_uint64, vp, vp]),
             "z0p_gpu_pool_create": (C.c_int, [C.c_int, C.c_int, sz, P(vp)]),

@@ -7,7 +7,7 @@ from __future__ import annotations
 
 import ctypes as C
 
-from ._lib import AirParams, check, lib
+from ._lib import AirParams, TranscriptState, check, lib
 from .context import default_context
 from .transcript import Transcript
 
@@ -92,3 +92,22 @@ def prove_into(params: Params, transcript: Transcript, buf, ctx=None) -> int:
     check(lib().z0p_gpu_air_prove(ctx.handle, C.byref(params), C.byref(transcript.state), buf,
                                   len(buf), C.byref(n)))
     return n.value
+
+
+def prove_group(params_list, transcripts, ctx=None):
+    """Proves statements of one shape in lockstep (one launch sequence and one
+    set of host round trips for the group); proof i equals prove(params_list[i],
+    transcripts[i]) alone, and each transcript advances the same way."""
+    ctx = ctx or default_context()
+    n = len(params_list)
+    if n != len(transcripts) or n == 0:
+        raise ValueError("one transcript per statement, at least one statement")
+    arr = (Params * n)(*params_list)
+    size = params_list[0].proof_size()
+    bufs = [(C.c_uint8 * size)() for _ in range(n)]
+    outs = (C.POINTER(C.c_uint8) * n)(*[C.cast(b, C.POINTER(C.c_uint8)) for b in bufs])
+    caps = (C.c_size_t * n)(*([size] * n))
+    lens = (C.c_size_t * n)()
+    states = (C.POINTER(TranscriptState) * n)(*[C.pointer(t.state) for t in transcripts])
+    check(lib().z0p_gpu_air_prove_group(ctx.handle, n, arr, states, outs, caps, lens))
+    return [bytes(b)[: lens[i]] for i, b in enumerate(bufs)]

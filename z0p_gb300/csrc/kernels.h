@@ -48,7 +48,10 @@ struct ProofConsts {
   uint32_t head[16];        // PoW head (47 bytes, little-endian words, zero padded)
   uint32_t tab[3][4][4];    // the current fold's e4_mul_tab tables of r_k / 4
 };
-constexpr int kConstSlots = 128;
+constexpr int kConstSlots = 168;  // 168 x 372 bytes of the 64 KiB constant bank
+// Largest proof group one launch sequence covers (per-proof counters and PoW
+// states are sized for it).
+constexpr int kMaxGroup = 64;
 
 struct AirComposeArgs {
   const uint32_t* lde_a;  // coset-major [j][q]

@@ -130,11 +130,12 @@ struct z0p_gpu_ctx {
   uint8_t* hio = nullptr;
   uint8_t* hio_d = nullptr;  // its device address
   size_t hio_bytes = 0;
-  // The context's constant slot of per-proof values, and its pinned staging
-  // copy: the host fills `consts`, push_consts queues the copy into the slot.
-  int slot = -1;
+  // The context's constant slots of per-proof values (slot .. slot+nslots-1,
+  // one per proof of a group) and their pinned staging copies: the host
+  // fills `consts`, push_consts queues the copy into the slots.
+  int slot = -1, nslots = 0;
   void* slot_dev = nullptr;
-  ProofConsts* consts = nullptr;
+  ProofConsts* consts = nullptr;  // kMaxGroup entries
   size_t held = 0;
   uint64_t h2d = 0, d2h = 0, syncs = 0, proofs = 0, sync_ns = 0, prove_ns = 0;
   bool profiling = false;
@@ -150,10 +151,6 @@ using HostSite = z0p_gpu_ctx::HostSite;
 
 namespace {
 
-cudaError_t d2h(z0p_gpu_ctx* c, void* dst, const void* src, size_t n) {
-  c->d2h += n;
-  return cudaMemcpyAsync(dst, src, n, cudaMemcpyDeviceToHost, c->stream);
-}
 uint64_t now_ns() {
   return (uint64_t)std::chrono::duration_cast<std::chrono::nanoseconds>(
              std::chrono::steady_clock::now().time_since_epoch())
@@ -228,31 +225,54 @@ int ensure(z0p_gpu_ctx* c, DevBuf& b, size_t bytes) {
   return Z0P_OK;
 }
 
-// Constant slots are handed out to contexts for their lifetime.
+// Constant slots are handed to contexts as contiguous ranges (one slot per
+// proof of a group), first fit.
 std::mutex g_slot_mu;
 bool g_slot_used[kConstSlots] = {};
 
-int take_slot() {
+int take_slots(int n) {
   std::lock_guard<std::mutex> lk(g_slot_mu);
-  for (int i = 0; i < kConstSlots; i++)
-    if (!g_slot_used[i]) {
-      g_slot_used[i] = true;
+  for (int i = 0; i + n <= kConstSlots; i++) {
+    int j = 0;
+    while (j < n && !g_slot_used[i + j]) j++;
+    if (j == n) {
+      for (j = 0; j < n; j++) g_slot_used[i + j] = true;
       return i;
     }
+    i += j;
+  }
   return -1;
 }
-void give_slot(int i) {
+void give_slots(int first, int n) {
   std::lock_guard<std::mutex> lk(g_slot_mu);
-  if (i >= 0 && i < kConstSlots) g_slot_used[i] = false;
+  for (int i = first; i >= 0 && i < first + n && i < kConstSlots; i++) g_slot_used[i] = false;
 }
 
-// Queues the copy of the context's per-proof values into its constant slot.
+// The context holds at least K contiguous slots. A context only grows its
+// range between prove calls, after its stream has drained.
+int ensure_slots(z0p_gpu_ctx* c, uint32_t K) {
+  if ((int)K <= c->nslots) return Z0P_OK;
+  CK(cudaStreamSynchronize(c->stream));
+  give_slots(c->slot, c->nslots);
+  c->slot = take_slots((int)K);
+  c->nslots = c->slot < 0 ? 0 : (int)K;
+  if (c->slot < 0) {
+    c->slot = take_slots(1);  // keep single proofs working
+    c->nslots = c->slot < 0 ? 0 : 1;
+    set_reason("no free constant slots for a group of this size");
+    return Z0P_ERR_OUT_OF_MEMORY;
+  }
+  CK(launch::const_slot_address(c->slot, &c->slot_dev));
+  return Z0P_OK;
+}
+
+// Queues the copy of the first K proofs' values into the context's slots.
 // The host changes c->consts only after the stream has synchronised past the
 // previous copy.
-cudaError_t push_consts(z0p_gpu_ctx* c) {
-  c->h2d += sizeof(ProofConsts);
-  return cudaMemcpyAsync(c->slot_dev, c->consts, sizeof(ProofConsts), cudaMemcpyHostToDevice,
-                         c->stream);
+cudaError_t push_consts(z0p_gpu_ctx* c, uint32_t K) {
+  c->h2d += (uint64_t)K * sizeof(ProofConsts);
+  return cudaMemcpyAsync(c->slot_dev, c->consts, (size_t)K * sizeof(ProofConsts),
+                         cudaMemcpyHostToDevice, c->stream);
 }
 
 // PoW head bytes as little-endian words, zero padded.
@@ -312,16 +332,18 @@ int build_tables(z0p_gpu_ctx* c) {
 inline uint64_t tree_digests(uint64_t leaves) { return 2 * leaves - 1; }
 
 // Device counters that kernels leave as they found them, set once when the
-// context is created: the Merkle last-CTA counter (bytes 0..3) and the PoW
-// search state (bytes 8..39).
+// context is created, one per proof of a group: the Merkle last-CTA counters
+// (kMaxGroup words) and the PoW search states (kMaxGroup x 4 u64).
 inline unsigned int* merkle_counter(z0p_gpu_ctx* c) { return (unsigned int*)c->state.p; }
-inline unsigned long long* grind_state(z0p_gpu_ctx* c) { return (unsigned long long*)c->state.p + 1; }
+inline unsigned long long* grind_state(z0p_gpu_ctx* c) {
+  return reinterpret_cast<unsigned long long*>((char*)c->state.p + 4 * kMaxGroup);
+}
 
 
 inline uint64_t level_off(uint64_t leaves, uint32_t l) { return 2 * leaves - 2 * (leaves >> l); }
 
-// One FRI commitment + opening over layer 0 (already written with its leaf
-// digests) — src/fri.rs:551-666 from the first layer-root absorb onward.
+// One FRI commitment + opening of one proof (src/fri.rs:551-666 from the
+// first layer-root absorb onward).
 struct FriOut {
   std::vector<std::vector<uint8_t>> caps;
   std::vector<uint32_t> final_vals;
@@ -329,19 +351,25 @@ struct FriOut {
   std::vector<uint64_t> indices;
 };
 
+// Device FRI layers and trees of a proof group: proof k's layer l values at
+// layer[l] + k * val_stride and its layer-l tree at tree[l] + k * tree_stride
+// (words).
 struct FriBufs {
-  std::vector<uint32_t*> layer;  // device values per layer (layer 0 included)
-  std::vector<uint32_t*> tree;   // device trees per layer
+  std::vector<uint32_t*> layer;  // proof 0's values per layer (layer 0 included)
+  std::vector<uint32_t*> tree;   // proof 0's trees per layer
+  uint64_t val_stride = 0, tree_stride = 0;
 };
 
-int plan_fri_buffers(z0p_gpu_ctx* c, const FriShape& s, FriBufs* fb) {
+int plan_fri_buffers(z0p_gpu_ctx* c, const FriShape& s, uint32_t K, FriBufs* fb) {
   size_t vals = 0, digs = 0;
   for (size_t i = 0; i < s.len.size(); i++) {
     vals += 4 * s.len[i];
     digs += 8 * tree_digests(s.leaves[i]);
   }
-  RC(ensure(c, c->layers, vals * 4));
-  RC(ensure(c, c->ftrees, digs * 4));
+  RC(ensure(c, c->layers, (size_t)K * vals * 4));
+  RC(ensure(c, c->ftrees, (size_t)K * digs * 4));
+  fb->val_stride = vals;
+  fb->tree_stride = digs;
   uint32_t* v = (uint32_t*)c->layers.p;
   uint32_t* d = (uint32_t*)c->ftrees.p;
   fb->layer.clear();
@@ -355,31 +383,43 @@ int plan_fri_buffers(z0p_gpu_ctx* c, const FriShape& s, FriBufs* fb) {
   return Z0P_OK;
 }
 
-// Where a proof's host-visible pieces land in the context's mapped buffer:
-// the trace cap and each FRI layer's cap (written by the tree kernels), the
-// final layer, the PoW result, the query indices (written by the host) and
-// one opening block per query (written by the openings kernel; layout in
-// kernels.h, OpenArgs).
+// Where a group's host-visible pieces land in the mapped buffer. Each piece
+// is one region holding the K proofs' copies back to back, so kernels reach
+// proof k's at a fixed stride: the trace cap and each FRI layer's cap (tree
+// kernels), the final layers, the PoW results, the query indices (host),
+// the opening blocks (openings kernel; layout in kernels.h, OpenArgs) and
+// small per-proof inputs read by kernels in place.
 struct HioPlan {
-  size_t trace_cap = 0;
-  std::vector<size_t> fri_cap;
-  size_t final_vals = 0, grind = 0, indices = 0, open = 0, extra = 0;
-  uint32_t stride = 0, trace_off = 0;  // opening block, in words
+  uint32_t K = 1;
+  uint64_t queries = 0;
+  size_t trace_cap = 0, trace_cap_bytes = 0;
+  std::vector<size_t> fri_cap, fri_cap_bytes;
+  size_t final_vals = 0, final_bytes = 0, grind = 0, indices = 0, open = 0;
+  size_t extra = 0, extra_bytes = 0;
+  uint32_t stride = 0, trace_off = 0;  // one opening block, in words
   std::vector<uint32_t> layer_off;     // per non-final FRI layer, in words
 };
 
 int plan_hio(z0p_gpu_ctx* c, const FriShape& s, uint64_t queries, uint32_t tdrop,
-             uint32_t trace_words, HioPlan* h, size_t extra_bytes = 0) {
+             uint32_t trace_words, uint32_t K, HioPlan* h, size_t extra_bytes = 0) {
   size_t at = 0;
-  auto take = [&](size_t bytes) {
+  auto take = [&](size_t bytes) {  // a region of K copies, 16-byte aligned
     size_t r = at;
-    at += (bytes + 15) & ~(size_t)15;
+    at += ((size_t)K * bytes + 15) & ~(size_t)15;
     return r;
   };
-  h->trace_cap = take(32ull << tdrop);
+  h->K = K;
+  h->queries = queries;
+  h->trace_cap_bytes = 32ull << tdrop;
+  h->trace_cap = take(h->trace_cap_bytes);
   h->fri_cap.clear();
-  for (size_t l = 0; l < s.len.size(); l++) h->fri_cap.push_back(take(32ull << s.drop[l]));
-  h->final_vals = take(16 * s.len.back());
+  h->fri_cap_bytes.clear();
+  for (size_t l = 0; l < s.len.size(); l++) {
+    h->fri_cap_bytes.push_back(32ull << s.drop[l]);
+    h->fri_cap.push_back(take(h->fri_cap_bytes.back()));
+  }
+  h->final_bytes = 16 * s.len.back();
+  h->final_vals = take(h->final_bytes);
   h->grind = take(16);
   h->indices = take(8 * queries);
   size_t L = s.len.size() - 1;
@@ -396,46 +436,59 @@ int plan_hio(z0p_gpu_ctx* c, const FriShape& s, uint64_t queries, uint32_t tdrop
   h->trace_off = w;
   h->stride = (w + trace_words + 3) & ~3u;
   h->open = take(4ull * h->stride * queries);
-  h->extra = take(extra_bytes);  // small per-proof inputs read by kernels in place
+  h->extra_bytes = extra_bytes;
+  h->extra = take(extra_bytes);
   return ensure_hio(c, at);
 }
 
+// Fold tables, PoW heads and query indices of one group, proof by proof on
+// the host; the device work of each round serves the whole group.
 int run_fri(z0p_gpu_ctx* c, const FriShape& s, const FriParams& fp, const FriBufs& fb,
-            uint64_t poly_len, uint64_t degree_bound, Transcript& ts, const HioPlan& h,
-            FriOut* out) {
+            uint64_t poly_len, uint64_t degree_bound, Transcript* const* ts, uint32_t K,
+            const HioPlan& h, FriOut* outs) {
   uint8_t dims[24];  // src/fri.rs:1450-1456
   for (int i = 0; i < 8; i++) {
     dims[i] = (uint8_t)(s.m >> (8 * i));
     dims[8 + i] = (uint8_t)(poly_len >> (8 * i));
     dims[16 + i] = (uint8_t)(degree_bound >> (8 * i));
   }
-  transcript_absorb(ts, "fri-dims", dims, 24);
+  for (uint32_t k = 0; k < K; k++) {
+    transcript_absorb(*ts[k], "fri-dims", dims, 24);
+    outs[k].caps.assign(s.len.size(), {});
+  }
   const uint32_t unit_m = to_mont(two_adic_generator(2));
-  out->caps.assign(s.len.size(), {});
   const uint64_t fl = s.len.back();
   for (size_t l = 0;; l++) {
     const bool last = l + 1 == s.len.size();
-    // The layer's cap is already in the mapped buffer once its tree is done;
-    // the last layer's values (sent in the clear) come back in the same trip.
-    if (last) CK(d2h(c, c->hio + h.final_vals, fb.layer.back(), 16 * fl));
+    // A layer's caps are in the mapped buffer once its trees are done; the
+    // last layer's values (sent in the clear) come back in the same trip.
+    if (last) {
+      c->d2h += (uint64_t)K * h.final_bytes;
+      CK(cudaMemcpy2DAsync(c->hio + h.final_vals, h.final_bytes, fb.layer.back(),
+                           4 * fb.val_stride, h.final_bytes, K, cudaMemcpyDeviceToHost, c->stream));
+    }
     CK(sync(c, last ? "cap+final" : "cap"));
-    const uint8_t* cap = c->hio + h.fri_cap[l];
-    out->caps[l].assign(cap, cap + (32ull << s.drop[l]));
-    c->d2h += 32ull << s.drop[l];  // written by the tree kernel into the mapped buffer
-    for (size_t k = 0; k < out->caps[l].size() / 32; k++)
-      transcript_absorb(ts, "fri-layer-root", out->caps[l].data() + 32 * k, 32);
+    for (uint32_t k = 0; k < K; k++) {
+      const uint8_t* cap = c->hio + h.fri_cap[l] + k * h.fri_cap_bytes[l];
+      outs[k].caps[l].assign(cap, cap + h.fri_cap_bytes[l]);
+      c->d2h += h.fri_cap_bytes[l];  // written by the tree kernel into the mapped buffer
+      for (size_t i = 0; i < h.fri_cap_bytes[l] / 32; i++)
+        transcript_absorb(*ts[k], "fri-layer-root", cap + 32 * i, 32);
+    }
     if (last) break;
+    const uint32_t inv4 = finv(4);
+    for (uint32_t k = 0; k < K; k++) {
+      uint32_t ch[3][4];
+      for (int r = 0; r < 3; r++) challenge_ext(*ts[k], "fri-fold", ch[r]);
+      for (int r = 0; r < 3; r++) {
+        uint32_t q[4];
+        for (int e = 0; e < 4; e++) q[e] = fmul(ch[r][e], inv4);
+        e4_table(q, c->consts[k].tab[r]);
+      }
+    }
+    CK(push_consts(c, K));
     FoldArgs fa;
     fa.slot = (uint32_t)c->slot;
-    uint32_t ch[3][4];
-    for (int k = 0; k < 3; k++) challenge_ext(ts, "fri-fold", ch[k]);
-    const uint32_t inv4 = finv(4);
-    for (int k = 0; k < 3; k++) {
-      uint32_t q[4];
-      for (int e = 0; e < 4; e++) q[e] = fmul(ch[k][e], inv4);
-      e4_table(q, c->consts->tab[k]);
-    }
-    CK(push_consts(c));
     fa.in = fb.layer[l];
     fa.out = fb.layer[l + 1];
     fa.leaves = fb.tree[l + 1];
@@ -448,64 +501,82 @@ int run_fri(z0p_gpu_ctx* c, const FriShape& s, const FriParams& fp, const FriBuf
     const uint32_t top = s.depth[l + 1] - s.drop[l + 1];
     fa.top = top;
     fa.cap = hio_dev<uint32_t>(c, h.fri_cap[l + 1]);
+    fa.in_stride = fa.out_stride = fb.val_stride;
+    fa.tree_stride = fb.tree_stride;
+    fa.cap_stride = h.fri_cap_bytes[l + 1] / 4;
     uint32_t built = 0;  // subtree levels the fold kernel hashed itself
-    CK(launch::fri_fold(c->stream, c->tb, fa, &built));
+    CK(launch::fri_fold(c->stream, c->tb, fa, &built, K));
     // Levels above `built` remain, if any. A tree capped at its leaves has
     // its cap written by the fold only when the fold hashed its subtree (64-
     // byte leaves, small tree); otherwise merkle_build copies it.
     const bool fused = s.len[l] >= 16 && s.leaves[l + 1] <= kFuseMaxLeaves;
     if (built < top || (top == 0 && !fused))
       CK(launch::merkle_build(c->stream, fb.tree[l + 1], s.leaves[l + 1], top, merkle_counter(c),
-                              fa.cap, built));
+                              fa.cap, built, K, fb.tree_stride, fa.cap_stride));
   }
   // Final layer in the clear (src/fri.rs:620-621).
-  out->final_vals.resize(4 * fl);
-  std::memcpy(out->final_vals.data(), c->hio + h.final_vals, 16 * fl);
-  transcript_absorb(ts, "fri-final", (const uint8_t*)out->final_vals.data(), 16 * fl);
-  // Proof of work (src/fri.rs:645-650, src/transcript.rs:206-228).
-  out->nonce = 0;
-  if (fp.grinding_bits > 0) {
-    std::vector<uint8_t> head = pow_head(ts, "fri-pow");
-    set_head(c->consts, head.data(), head.size());
-    CK(push_consts(c));
-    CK(launch::grind(c->stream, (uint32_t)c->slot, (uint32_t)head.size(), fp.grinding_bits,
-                     grind_state(c), hio_dev<unsigned long long>(c, h.grind), 1ull << 40));
-    CK(sync(c, "grind"));
-    unsigned long long res[2];
-    std::memcpy(res, c->hio + h.grind, 16);
-    c->d2h += 16;
-    if (res[1] != 0 || res[0] == ~0ull) {
-      set_reason("proof-of-work search reached its nonce cap without a solution");
-      return Z0P_ERR_DEVICE_TIMEOUT;
-    }
-    out->nonce = res[0];
-    uint8_t nb[8];
-    for (int i = 0; i < 8; i++) nb[i] = (uint8_t)(out->nonce >> (8 * i));
-    transcript_absorb(ts, "fri-pow", nb, 8);
+  for (uint32_t k = 0; k < K; k++) {
+    outs[k].final_vals.resize(4 * fl);
+    std::memcpy(outs[k].final_vals.data(), c->hio + h.final_vals + k * h.final_bytes, 16 * fl);
+    transcript_absorb(*ts[k], "fri-final", (const uint8_t*)outs[k].final_vals.data(), 16 * fl);
+    outs[k].nonce = 0;
   }
-  out->indices.resize(fp.num_queries);
-  for (uint64_t i = 0; i < fp.num_queries; i++) out->indices[i] = challenge_index(ts, "fri-query", s.m);
+  // Proof of work (src/fri.rs:645-650, src/transcript.rs:206-228).
+  if (fp.grinding_bits > 0) {
+    size_t head_len = 0;
+    for (uint32_t k = 0; k < K; k++) {
+      std::vector<uint8_t> head = pow_head(*ts[k], "fri-pow");
+      set_head(&c->consts[k], head.data(), head.size());
+      head_len = head.size();
+    }
+    CK(push_consts(c, K));
+    CK(launch::grind(c->stream, (uint32_t)c->slot, (uint32_t)head_len, fp.grinding_bits,
+                     grind_state(c), hio_dev<unsigned long long>(c, h.grind), 1ull << 40, K));
+    CK(sync(c, "grind"));
+    for (uint32_t k = 0; k < K; k++) {
+      unsigned long long res[2];
+      std::memcpy(res, c->hio + h.grind + 16 * k, 16);
+      c->d2h += 16;
+      if (res[1] != 0 || res[0] == ~0ull) {
+        set_reason("proof-of-work search reached its nonce cap without a solution");
+        return Z0P_ERR_DEVICE_TIMEOUT;
+      }
+      outs[k].nonce = res[0];
+      uint8_t nb[8];
+      for (int i = 0; i < 8; i++) nb[i] = (uint8_t)(outs[k].nonce >> (8 * i));
+      transcript_absorb(*ts[k], "fri-pow", nb, 8);
+    }
+  }
+  for (uint32_t k = 0; k < K; k++) {
+    outs[k].indices.resize(fp.num_queries);
+    for (uint64_t i = 0; i < fp.num_queries; i++)
+      outs[k].indices[i] = challenge_index(*ts[k], "fri-query", s.m);
+  }
   return Z0P_OK;
 }
 
-// Gathers every opening of the proof on the device (kernels.h, OpenArgs)
-// into the mapped buffer; `oa` arrives with its trace fields set.
+// Gathers every opening of the group on the device (kernels.h, OpenArgs)
+// into the mapped buffer; `oa` arrives with its trace fields and strides set.
 int run_openings(z0p_gpu_ctx* c, const FriShape& s, const FriBufs& fb, const HioPlan& h,
-                 const FriOut& fo, OpenArgs& oa) {
-  std::memcpy(c->hio + h.indices, fo.indices.data(), 8 * fo.indices.size());
+                 const FriOut* outs, uint32_t K, OpenArgs& oa) {
+  const uint64_t Q = h.queries;
+  for (uint32_t k = 0; k < K; k++)
+    std::memcpy(c->hio + h.indices + 8 * Q * k, outs[k].indices.data(), 8 * Q);
   oa.indices = hio_dev<uint64_t>(c, h.indices);
   oa.out = hio_dev<uint32_t>(c, h.open);
-  oa.nq = (uint32_t)fo.indices.size();
+  oa.nq = (uint32_t)Q;
   oa.nlayers = (uint32_t)(s.len.size() - 1);
   oa.stride = h.stride;
   oa.trace_off = h.trace_off;
+  oa.fri_val_stride = fb.val_stride;
+  oa.fri_tree_stride = fb.tree_stride;
   for (uint32_t d = 0; d < oa.nlayers; d++)
     oa.layer[d] = OpenLayer{fb.layer[d], fb.tree[d], s.leaves[d], s.depth[d] - s.drop[d],
                             h.layer_off[d]};
-  CK(launch::openings(c->stream, oa));
+  CK(launch::openings(c->stream, oa, K));
   CK(sync(c, "openings"));
-  c->h2d += 8 * fo.indices.size();                      // indices read in place
-  c->d2h += 4ull * h.stride * fo.indices.size();        // opening blocks
+  c->h2d += 8 * Q * K;                      // indices read in place
+  c->d2h += 4ull * h.stride * Q * K;        // opening blocks
   return Z0P_OK;
 }
 
@@ -517,12 +588,14 @@ void write_path(Writer& w, const uint8_t* digests, uint64_t leaf, uint32_t steps
   }
 }
 
-const uint32_t* open_block(z0p_gpu_ctx* c, const HioPlan& h, size_t qi) {
-  return reinterpret_cast<const uint32_t*>(c->hio + h.open) + (size_t)h.stride * qi;
+// Opening block of query qi of proof k.
+const uint32_t* open_block(z0p_gpu_ctx* c, const HioPlan& h, uint32_t k, size_t qi) {
+  return reinterpret_cast<const uint32_t*>(c->hio + h.open) +
+         (size_t)h.stride * ((size_t)k * h.queries + qi);
 }
 
 void write_fri(Writer& w, z0p_gpu_ctx* c, const FriShape& s, const FriOut& fo, uint64_t poly_len,
-               uint64_t degree_bound, const HioPlan& h) {
+               uint64_t degree_bound, const HioPlan& h, uint32_t k) {
   w.u64(s.m);  // Commitment::write_body (src/fri.rs:896-904)
   w.u64(poly_len);
   w.u64(degree_bound);
@@ -537,7 +610,7 @@ void write_fri(Writer& w, z0p_gpu_ctx* c, const FriShape& s, const FriOut& fo, u
   w.u32((uint32_t)fo.indices.size());
   size_t L = s.len.size() - 1;
   for (size_t qi = 0; qi < fo.indices.size(); qi++) {
-    const uint32_t* blk = open_block(c, h, qi);
+    const uint32_t* blk = open_block(c, h, k, qi);
     w.u32((uint32_t)L);
     uint64_t index = fo.indices[qi];
     for (size_t d = 0; d < L; d++) {
@@ -593,105 +666,172 @@ void fib_mats(uint32_t mats[32][4]) {
   }
 }
 
-// src/air.rs:365-372 -> 485-599 on the device.
-int air_prove(z0p_gpu_ctx* c, const z0p_air_params& p, Transcript& ts, uint8_t* out,
-              size_t cap, size_t* len) {
+// One proof of a group: its statement, transcript and output buffer.
+template <class Params>
+struct Task {
+  const Params* p;
+  Transcript* ts;
+  uint8_t* out;
+  size_t cap;
+  size_t* len;
+};
+using AirTask = Task<z0p_air_params>;
+using RangeTask = Task<z0p_range_params>;
+
+bool same_air_shape(const z0p_air_params& a, const z0p_air_params& b) {
+  return a.n_steps == b.n_steps && a.blowup == b.blowup && a.num_queries == b.num_queries &&
+         a.final_size == b.final_size && a.grinding_bits == b.grinding_bits &&
+         a.cap_height == b.cap_height;
+}
+bool same_range_shape(const z0p_range_params& a, const z0p_range_params& b) {
+  return a.n_rows == b.n_rows && a.n_bits == b.n_bits && a.blowup == b.blowup &&
+         a.num_queries == b.num_queries && a.final_size == b.final_size &&
+         a.grinding_bits == b.grinding_bits && a.cap_height == b.cap_height;
+}
+
+// Validation, sizes and output buffers of a group, before any device work.
+template <class T, class Shape, class Size, class Same>
+int check_group(const T* tasks, uint32_t K, Shape shape, Size size, Same same, FriParams* fp,
+                FriShape* s, uint64_t* need) {
+  if (!K || K > (uint32_t)kMaxGroup) return Z0P_ERR_INVALID_ARGUMENT;
+  RC(shape(*tasks[0].p, fp, s));
+  *need = size(*tasks[0].p, *s);
+  for (uint32_t k = 0; k < K; k++) {
+    if (k) {
+      if (!same(*tasks[0].p, *tasks[k].p)) {
+        set_reason("proofs of a group must share their shape (sizes and schedule)");
+        return Z0P_ERR_INVALID_ARGUMENT;
+      }
+      FriParams f2;
+      FriShape s2;
+      RC(shape(*tasks[k].p, &f2, &s2));  // statement checks (canonical values)
+    }
+    if (tasks[k].len) *tasks[k].len = *need;
+  }
+  for (uint32_t k = 0; k < K; k++)
+    if (!tasks[k].out || tasks[k].cap < *need) {
+      set_reason("output buffer too small for the proof");
+      return Z0P_ERR_BUFFER_TOO_SMALL;
+    }
+  return Z0P_OK;
+}
+
+// src/air.rs:365-372 -> 485-599 on the device, for K proofs of one shape in
+// lockstep: every launch covers the group (grid y = proof) and every
+// Fiat-Shamir round trip serves it.
+int air_prove(z0p_gpu_ctx* c, const AirTask* tasks, uint32_t K) {
   FriParams fp;
   FriShape s;
-  RC(air_shape(p, &fp, &s));
-  uint64_t need = air_size(p, s);
-  if (len) *len = need;
-  if (!out || cap < need) {
-    set_reason("output buffer too small for the proof");
-    return Z0P_ERR_BUFFER_TOO_SMALL;
-  }
-  const uint64_t N = p.n_steps, B = p.blowup, m = N * B;
+  uint64_t need = 0;
+  RC(check_group(tasks, K, air_shape, air_size, same_air_shape, &fp, &s, &need));
+  const z0p_air_params& p0 = *tasks[0].p;
+  const uint64_t N = p0.n_steps, B = p0.blowup, m = N * B;
   const uint32_t logN = log2u(N), logB = log2u(B), logm = logN + logB;
   cudaStream_t st = c->stream;
 
-  RC(ensure(c, c->cols, 8 * N));
-  RC(ensure(c, c->coeffs, 8 * N));
-  RC(ensure(c, c->scratch, 4 * m));
-  RC(ensure(c, c->lde, 4 * m));
-  RC(ensure(c, c->ttree, 32 * tree_digests(m / 8)));
-  RC(ensure(c, c->misc, 64 + 12 * B));
+  RC(ensure_slots(c, K));
+  RC(ensure(c, c->cols, 8 * N * K));
+  RC(ensure(c, c->coeffs, 4 * N * K));
+  RC(ensure(c, c->scratch, 4 * m * K));
+  RC(ensure(c, c->lde, 4 * m * K));
+  const uint64_t tleaves = m / 8, ttree_words = 8 * tree_digests(tleaves);
+  RC(ensure(c, c->ttree, 4 * ttree_words * K));
+  RC(ensure(c, c->misc, 64 + 8 * B + 4 * B * K));
   FriBufs fb;
-  RC(plan_fri_buffers(c, s, &fb));
+  RC(plan_fri_buffers(c, s, K, &fb));
+  const uint32_t tdepth = log2u(tleaves);
+  const uint32_t tdrop = p0.cap_height < tdepth ? (uint32_t)p0.cap_height : tdepth;
+  const uint32_t tsteps = tdepth - tdrop;
+  HioPlan h;
+  RC(plan_hio(c, s, p0.num_queries, tdrop, 2 * (16 + 8 * tsteps), K, &h));
   uint32_t* cols = (uint32_t*)c->cols.p;
   uint32_t* coeffs = (uint32_t*)c->coeffs.p;
   uint32_t* lde = (uint32_t*)c->lde.p;
   uint32_t* ttree = (uint32_t*)c->ttree.p;
   uint32_t* zinv = (uint32_t*)c->misc.p + 16;
   uint32_t* zinv2 = zinv + B;
+  uint32_t* cb = zinv2 + B;  // K x B: per-proof linked-column constants
 
-  // absorb_params (src/air.rs:754-766)
-  uint8_t pb[56];
-  auto p64 = [&](int off, uint64_t v) { for (int i = 0; i < 8; i++) pb[off + i] = (uint8_t)(v >> (8 * i)); };
-  auto p32 = [&](int off, uint32_t v) { for (int i = 0; i < 4; i++) pb[off + i] = (uint8_t)(v >> (8 * i)); };
-  p64(0, p.n_steps); p64(8, p.blowup); p64(16, p.num_queries); p64(24, p.final_size);
-  p32(32, p.grinding_bits); p64(36, p.cap_height); p32(44, p.a0); p32(48, p.b0); p32(52, p.b_last);
-  transcript_absorb(ts, "fib/params", pb, 56);
-
-  // Trace, interpolation of column A (times 31^i / N) and its coset LDE.
-  // Column B is derived from A wherever it is needed (linked_lde,
-  // src/air.rs:806-844): B(x) = A(omega_N x) + C_j / (x - w_last).
   uint32_t mats[32][4];
   fib_mats(mats);
   // C_j = coeff * (x^N - 1) with coeff = (B[N-1] - a0) w_last / N, where
   // B[N-1] is the actual last trace value (src/air.rs:366-371, 817-821).
-  uint32_t omega_n = two_adic_generator(logN);
-  uint32_t w_last = fpow(omega_n, N - 1);
-  uint32_t b_actual = 0;
-  {
-    // (A[N-1], B[N-1]) = M^(N-1) (a0, b0) from the binary powers of M.
-    uint32_t r00 = 1, r01 = 0, r10 = 0, r11 = 1;
-    for (int k = 0; k < 32; k++)
-      if (((N - 1) >> k) & 1) {
-        const uint32_t* q = mats[k];
-        uint32_t n00 = fadd(fmul(r00, q[0]), fmul(r01, q[2])), n01 = fadd(fmul(r00, q[1]), fmul(r01, q[3]));
-        uint32_t n10 = fadd(fmul(r10, q[0]), fmul(r11, q[2])), n11 = fadd(fmul(r10, q[1]), fmul(r11, q[3]));
-        r00 = n00; r01 = n01; r10 = n10; r11 = n11;
-      }
-    b_actual = fadd(fmul(r10, p.a0), fmul(r11, p.b0));
+  const uint32_t omega_n = two_adic_generator(logN);
+  const uint32_t w_last = fpow(omega_n, N - 1);
+  const uint32_t n_inv = finv((uint32_t)(N % P));
+  // (A[N-1], B[N-1]) = M^(N-1) (a0, b0) from the binary powers of M.
+  uint32_t r00 = 1, r01 = 0, r10 = 0, r11 = 1;
+  for (int k = 0; k < 32; k++)
+    if (((N - 1) >> k) & 1) {
+      const uint32_t* q = mats[k];
+      uint32_t n00 = fadd(fmul(r00, q[0]), fmul(r01, q[2])), n01 = fadd(fmul(r00, q[1]), fmul(r01, q[3]));
+      uint32_t n10 = fadd(fmul(r10, q[0]), fmul(r11, q[2])), n11 = fadd(fmul(r10, q[1]), fmul(r11, q[3]));
+      r00 = n00; r01 = n01; r10 = n10; r11 = n11;
+    }
+  std::vector<uint32_t> coeff(K);
+  for (uint32_t k = 0; k < K; k++) {
+    const z0p_air_params& p = *tasks[k].p;
+    // absorb_params (src/air.rs:754-766)
+    uint8_t pb[56];
+    auto p64 = [&](int off, uint64_t v) { for (int i = 0; i < 8; i++) pb[off + i] = (uint8_t)(v >> (8 * i)); };
+    auto p32 = [&](int off, uint32_t v) { for (int i = 0; i < 4; i++) pb[off + i] = (uint8_t)(v >> (8 * i)); };
+    p64(0, p.n_steps); p64(8, p.blowup); p64(16, p.num_queries); p64(24, p.final_size);
+    p32(32, p.grinding_bits); p64(36, p.cap_height); p32(44, p.a0); p32(48, p.b0); p32(52, p.b_last);
+    transcript_absorb(*tasks[k].ts, "fib/params", pb, 56);
+    const uint32_t b_actual = fadd(fmul(r10, p.a0), fmul(r11, p.b0));
+    coeff[k] = fmul(fmul(fsub(b_actual, p.a0), w_last), n_inv);
+    ProofConsts& pc = c->consts[k];
+    pc.a0 = p.a0; pc.b0 = p.b0; pc.b_last = p.b_last;
+    pc.coeff = coeff[k];
   }
-  uint32_t coeff = fmul(fmul(fsub(b_actual, p.a0), w_last), finv((uint32_t)(N % P)));
-  ProofConsts* pc = c->consts;
-  pc->a0 = p.a0; pc->b0 = p.b0; pc->b_last = p.b_last;
-  pc->coeff = coeff;
-  CK(push_consts(c));
-  CK(launch::fib_trace(st, cols, cols + N, (uint32_t)N, (uint32_t)c->slot, mats));
+  const uint32_t slot = (uint32_t)c->slot;
+  // Trace, interpolation of column A (times 31^i / N) and its coset LDE.
+  // Column B is derived from A wherever it is needed (linked_lde,
+  // src/air.rs:806-844): B(x) = A(omega_N x) + C_j / (x - w_last).
+  CK(push_consts(c, K));
+  CK(launch::fib_trace(st, cols, cols + N * K, (uint32_t)N, slot, mats, K));
   NttPlan ip;
-  ip.logn = logN; ip.batch = 1; ip.inverse = 1; ip.post_gamma = 1;
+  ip.logn = logN; ip.batch = K; ip.inverse = 1; ip.post_gamma = 1;
   CK(launch::ntt(st, c->tb, ip, cols, coeffs, (uint32_t*)c->scratch.p));
   NttPlan lp;
-  lp.logn = logN; lp.batch = (uint32_t)B; lp.in_div = (uint32_t)B; lp.twist_mod = (uint32_t)B;
+  lp.logn = logN; lp.batch = (uint32_t)(B * K); lp.in_div = (uint32_t)B; lp.twist_mod = (uint32_t)B;
   lp.twist_shift = 27 - logm;
   CK(launch::ntt(st, c->tb, lp, coeffs, lde, (uint32_t*)c->scratch.p));
   const uint32_t* lde_a = lde;
-  uint32_t* cb = zinv2 + B;
-  uint32_t gamma_n = fpow(GENERATOR, N);
-  CK(launch::coset_zinv(st, c->tb, zinv, zinv2, logB, to_mont(gamma_n), cb, (uint32_t)c->slot));
+  CK(launch::coset_zinv(st, c->tb, zinv, zinv2, logB, to_mont(fpow(GENERATOR, N)), cb, slot, K));
   const uint32_t w_last_m = to_mont(w_last);
 
   // Joint trace tree over 8-row 64-byte leaves (src/air.rs:520-537).
-  uint64_t tleaves = m / 8;
-  uint32_t tdepth = log2u(tleaves), tdrop = p.cap_height < tdepth ? (uint32_t)p.cap_height : tdepth;
-  const uint32_t tsteps = tdepth - tdrop;
-  HioPlan h;
-  RC(plan_hio(c, s, p.num_queries, tdrop, 2 * (16 + 8 * tsteps), &h));
   uint32_t* tinv = (uint32_t*)c->scratch.p;  // the NTT's scratch is free from here on
   uint32_t built = 0;  // subtree levels the leaf kernel hashed itself
+  const uint64_t tcap_stride = h.trace_cap_bytes / 4;
   CK(launch::air_trace_leaves(st, c->tb, lde_a, cb, w_last_m, ttree, tinv, logN, logB, tsteps,
-                              hio_dev<uint32_t>(c, h.trace_cap), &built));
+                              hio_dev<uint32_t>(c, h.trace_cap), &built, K, ttree_words,
+                              tcap_stride));
   if (built < tsteps || (tsteps == 0 && tleaves > kFuseMaxLeaves))
     CK(launch::merkle_build(st, ttree, tleaves, tsteps, merkle_counter(c),
-                            hio_dev<uint32_t>(c, h.trace_cap), built));
+                            hio_dev<uint32_t>(c, h.trace_cap), built, K, ttree_words, tcap_stride));
   CK(sync(c, "cap"));
-  std::vector<uint8_t> column_cap(c->hio + h.trace_cap, c->hio + h.trace_cap + (32ull << tdrop));
-  c->d2h += column_cap.size();
-  transcript_absorb(ts, "fib/trace", column_cap.data(), column_cap.size());
-  uint32_t alpha[5][4];
-  for (int k = 0; k < 5; k++) challenge_ext(ts, "fib/alpha", alpha[k]);
+  std::vector<std::vector<uint8_t>> column_cap(K);
+  const uint32_t omega_inv = finv(omega_n);
+  for (uint32_t k = 0; k < K; k++) {
+    const uint8_t* cap = c->hio + h.trace_cap + k * h.trace_cap_bytes;
+    column_cap[k].assign(cap, cap + h.trace_cap_bytes);
+    c->d2h += h.trace_cap_bytes;
+    transcript_absorb(*tasks[k].ts, "fib/trace", cap, h.trace_cap_bytes);
+    uint32_t alpha[5][4];
+    for (int i = 0; i < 5; i++) challenge_ext(*tasks[k].ts, "fib/alpha", alpha[i]);
+    ProofConsts& pc = c->consts[k];
+    const uint32_t neg_coeff = fsub(0, coeff[k]);
+    for (int e = 0; e < 4; e++) {
+      pc.alpha[e][0] = 0;
+      pc.alpha[e][1] = to_mont(alpha[1][e]);
+      pc.alpha[e][2] = to_mont(fmul(alpha[2][e], omega_inv));
+      pc.alpha[e][3] = to_mont(fmul(alpha[3][e], omega_inv));
+      pc.alpha[e][4] = to_mont(alpha[4][e]);
+      pc.kc[e] = fmul(alpha[0][e], neg_coeff);
+    }
+  }
 
   // Composition as bit-reversed FRI layer 0 with its leaves (src/air.rs:847-929).
   AirComposeArgs ca;
@@ -699,168 +839,189 @@ int air_prove(z0p_gpu_ctx* c, const z0p_air_params& p, Transcript& ts, uint8_t* 
   ca.layer0 = fb.layer[0]; ca.leaves = fb.tree[0];
   ca.logN = logN; ca.logB = logB;
   ca.w_last_m = w_last_m;
-  ca.slot = (uint32_t)c->slot;
-  const uint32_t omega_inv = finv(omega_n), neg_coeff = fsub(0, coeff);
-  for (int e = 0; e < 4; e++) {
-    pc->alpha[e][0] = 0;
-    pc->alpha[e][1] = to_mont(alpha[1][e]);
-    pc->alpha[e][2] = to_mont(fmul(alpha[2][e], omega_inv));
-    pc->alpha[e][3] = to_mont(fmul(alpha[3][e], omega_inv));
-    pc->alpha[e][4] = to_mont(alpha[4][e]);
-    pc->kc[e] = fmul(alpha[0][e], neg_coeff);
-  }
-  CK(push_consts(c));
-  CK(launch::air_compose_leaves(st, c->tb, ca));
+  ca.slot = slot;
+  ca.layer_stride = fb.val_stride;
+  ca.tree_stride = fb.tree_stride;
+  CK(push_consts(c, K));
+  CK(launch::air_compose_leaves(st, c->tb, ca, K));
   CK(launch::merkle_build(st, fb.tree[0], s.leaves[0], s.depth[0] - s.drop[0], merkle_counter(c),
-                          hio_dev<uint32_t>(c, h.fri_cap[0])));
+                          hio_dev<uint32_t>(c, h.fri_cap[0]), 0, K, fb.tree_stride,
+                          h.fri_cap_bytes[0] / 4));
 
-  FriOut fo;
-  RC(run_fri(c, s, fp, fb, m, N - 1, ts, h, &fo));
+  std::vector<Transcript*> ts(K);
+  for (uint32_t k = 0; k < K; k++) ts[k] = tasks[k].ts;
+  std::vector<FriOut> fo(K);
+  RC(run_fri(c, s, fp, fb, m, N - 1, ts.data(), K, h, fo.data()));
 
   // Openings: FRI queries plus the two trace leaves per query (src/air.rs:565-591).
   OpenArgs oa{};
   oa.lde = lde_a; oa.cb = cb; oa.tinv = tinv;
   oa.ttree = ttree; oa.tleaves = tleaves; oa.tsteps = tsteps;
   oa.logN = logN; oa.logB = logB; oa.ncol = 0;
-  RC(run_openings(c, s, fb, h, fo, oa));
+  oa.lde_stride = m;
+  oa.ttree_stride = ttree_words;
+  RC(run_openings(c, s, fb, h, fo.data(), K, oa));
 
-  Writer w(out, need);  // air::Proof::to_bytes (src/air.rs:262-281)
-  w.byte(6);
-  w.u32((uint32_t)(column_cap.size() / 32));
-  w.bytes(column_cap.data(), column_cap.size());
-  write_fri(w, c, s, fo, m, N - 1, h);
-  w.u32((uint32_t)fo.indices.size());
-  for (size_t qi = 0; qi < fo.indices.size(); qi++) {
-    uint64_t index = brev(fo.indices[qi], logm);
-    uint64_t shifted = (index + B) % m;
-    const uint32_t* rows = open_block(c, h, qi) + h.trace_off;  // A0 B0 .. A7 B7, path
-    const uint32_t* srows = rows + 16 + 8 * tsteps;
-    w.u64(index);
-    w.u32(rows[2 * (index & 7)]);
-    w.u32(rows[2 * (index & 7) + 1]);
-    w.u32(srows[2 * (shifted & 7)]);
-    w.u32(srows[2 * (shifted & 7) + 1]);
-    write_path(w, (const uint8_t*)(rows + 16), index / 8, tsteps);
-    write_path(w, (const uint8_t*)(srows + 16), shifted / 8, tsteps);
-    w.bytes(rows, 64);
-    w.bytes(srows, 64);
-  }
-  if (w.n != need) {
-    set_reason("internal error: proof length differs from its shape");
-    return Z0P_ERR_CUDA;
+  for (uint32_t k = 0; k < K; k++) {
+    Writer w(tasks[k].out, need);  // air::Proof::to_bytes (src/air.rs:262-281)
+    w.byte(6);
+    w.u32((uint32_t)(column_cap[k].size() / 32));
+    w.bytes(column_cap[k].data(), column_cap[k].size());
+    write_fri(w, c, s, fo[k], m, N - 1, h, k);
+    w.u32((uint32_t)fo[k].indices.size());
+    for (size_t qi = 0; qi < fo[k].indices.size(); qi++) {
+      uint64_t index = brev(fo[k].indices[qi], logm);
+      uint64_t shifted = (index + B) % m;
+      const uint32_t* rows = open_block(c, h, k, qi) + h.trace_off;  // A0 B0 .. A7 B7, path
+      const uint32_t* srows = rows + 16 + 8 * tsteps;
+      w.u64(index);
+      w.u32(rows[2 * (index & 7)]);
+      w.u32(rows[2 * (index & 7) + 1]);
+      w.u32(srows[2 * (shifted & 7)]);
+      w.u32(srows[2 * (shifted & 7) + 1]);
+      write_path(w, (const uint8_t*)(rows + 16), index / 8, tsteps);
+      write_path(w, (const uint8_t*)(srows + 16), shifted / 8, tsteps);
+      w.bytes(rows, 64);
+      w.bytes(srows, 64);
+    }
+    if (w.n != need) {
+      set_reason("internal error: proof length differs from its shape");
+      return Z0P_ERR_CUDA;
+    }
   }
   return Z0P_OK;
 }
 
-// src/range.rs:337-343 -> 353-375 -> 425-514 on the device.
-int range_prove(z0p_gpu_ctx* c, const z0p_range_params& p, Transcript& ts, uint8_t* out,
-                size_t cap, size_t* len) {
+// src/range.rs:337-343 -> 353-375 -> 425-514 on the device, for K proofs of
+// one shape in lockstep.
+int range_prove(z0p_gpu_ctx* c, const RangeTask* tasks, uint32_t K) {
   FriParams fp;
   FriShape s;
-  RC(range_shape(p, &fp, &s));
-  uint64_t need = range_size(p, s);
-  if (len) *len = need;
-  if (!out || cap < need) {
-    set_reason("output buffer too small for the proof");
-    return Z0P_ERR_BUFFER_TOO_SMALL;
-  }
-  const uint64_t N = p.n_rows, B = p.blowup, m = N * B, ncol = p.n_bits + 1;
+  uint64_t need = 0;
+  RC(check_group(tasks, K, range_shape, range_size, same_range_shape, &fp, &s, &need));
+  const z0p_range_params& p0 = *tasks[0].p;
+  const uint64_t N = p0.n_rows, B = p0.blowup, m = N * B, ncol = p0.n_bits + 1;
   const uint32_t logN = log2u(N), logB = log2u(B), logm = logN + logB;
   cudaStream_t st = c->stream;
-  RC(ensure(c, c->cols, 4 * N * ncol));
-  RC(ensure(c, c->coeffs, 4 * N * ncol));
-  RC(ensure(c, c->scratch, 4 * m * ncol));
-  RC(ensure(c, c->lde, 4 * m * ncol));
-  RC(ensure(c, c->ttree, 32 * tree_digests(m)));
+  RC(ensure_slots(c, K));
+  RC(ensure(c, c->cols, 4 * N * ncol * K));
+  RC(ensure(c, c->coeffs, 4 * N * ncol * K));
+  RC(ensure(c, c->scratch, 4 * m * ncol * K));
+  RC(ensure(c, c->lde, 4 * m * ncol * K));
+  const uint64_t ttree_words = 8 * tree_digests(m);
+  RC(ensure(c, c->ttree, 4 * ttree_words * K));
   RC(ensure(c, c->misc, 64 + 8 * B));
   FriBufs fb;
-  RC(plan_fri_buffers(c, s, &fb));
+  RC(plan_fri_buffers(c, s, K, &fb));
   uint32_t* cols = (uint32_t*)c->cols.p;
   uint32_t* coeffs = (uint32_t*)c->coeffs.p;
   uint32_t* lde = (uint32_t*)c->lde.p;
   uint32_t* ttree = (uint32_t*)c->ttree.p;
   uint32_t* zinv = (uint32_t*)c->misc.p + 16;
   uint32_t* zinv2 = zinv + B;
-  uint32_t tdepth = logm, tdrop = p.cap_height < tdepth ? (uint32_t)p.cap_height : tdepth;
+  const uint32_t tdepth = logm;
+  const uint32_t tdrop = p0.cap_height < tdepth ? (uint32_t)p0.cap_height : tdepth;
   const uint32_t tsteps = tdepth - tdrop;
+  // Per-proof inputs read in place: the column values (ncol words, all proofs
+  // first) then the alphas (ncol + 1 Ext4 per proof).
   HioPlan h;
-  RC(plan_hio(c, s, p.num_queries, tdrop, (uint32_t)ncol + 8 * tsteps, &h,
+  RC(plan_hio(c, s, p0.num_queries, tdrop, (uint32_t)ncol + 8 * tsteps, K, &h,
               4 * ncol + 16 * (ncol + 1)));
   uint32_t* hvals = reinterpret_cast<uint32_t*>(c->hio + h.extra);
-  uint32_t* halpha = hvals + ncol;
-  c->h2d += 4 * ncol + 16 * (ncol + 1);  // column values and alphas, read in place
+  uint32_t* halpha = hvals + ncol * K;
+  const uint32_t* dvals = hio_dev<uint32_t>(c, h.extra);
+  const uint32_t* dalpha = dvals + ncol * K;
+  c->h2d += (4 * ncol + 16 * (ncol + 1)) * K;
 
-  // build_columns (src/range.rs:316-330): V = value, C_j = bit j of value.
-  hvals[0] = p.value;
-  for (uint64_t j = 0; j < p.n_bits; j++) hvals[1 + j] = j < 32 ? (p.value >> j) & 1 : 0;
-  CK(launch::fill_constant_columns(st, cols, (uint32_t)N, (uint32_t)ncol,
-                                   hio_dev<uint32_t>(c, h.extra)));
+  const uint32_t slot = (uint32_t)c->slot;
+  for (uint32_t k = 0; k < K; k++) {
+    const z0p_range_params& p = *tasks[k].p;
+    // build_columns (src/range.rs:316-330): V = value, C_j = bit j of value.
+    uint32_t* v = hvals + ncol * k;
+    v[0] = p.value;
+    for (uint64_t j = 0; j < p.n_bits; j++) v[1 + j] = j < 32 ? (p.value >> j) & 1 : 0;
+    uint8_t pb[56];  // absorb_params (src/range.rs:634-645)
+    auto p64 = [&](int off, uint64_t x) { for (int i = 0; i < 8; i++) pb[off + i] = (uint8_t)(x >> (8 * i)); };
+    auto p32 = [&](int off, uint32_t x) { for (int i = 0; i < 4; i++) pb[off + i] = (uint8_t)(x >> (8 * i)); };
+    p64(0, p.n_rows); p64(8, p.n_bits); p64(16, p.blowup); p64(24, p.num_queries);
+    p64(32, p.final_size); p32(40, p.grinding_bits); p64(44, p.cap_height); p32(52, p.value);
+    transcript_absorb(*tasks[k].ts, "range/params", pb, 56);
+    c->consts[k].value = p.value;
+  }
+  CK(push_consts(c, K));
+  CK(launch::fill_constant_columns(st, cols, (uint32_t)N, (uint32_t)ncol, dvals, K));
   NttPlan ip;
-  ip.logn = logN; ip.batch = (uint32_t)ncol; ip.inverse = 1; ip.post_gamma = 1;
+  ip.logn = logN; ip.batch = (uint32_t)(ncol * K); ip.inverse = 1; ip.post_gamma = 1;
   CK(launch::ntt(st, c->tb, ip, cols, coeffs, (uint32_t*)c->scratch.p));
-
-  uint8_t pb[56];  // absorb_params (src/range.rs:634-645)
-  auto p64 = [&](int off, uint64_t v) { for (int i = 0; i < 8; i++) pb[off + i] = (uint8_t)(v >> (8 * i)); };
-  auto p32 = [&](int off, uint32_t v) { for (int i = 0; i < 4; i++) pb[off + i] = (uint8_t)(v >> (8 * i)); };
-  p64(0, p.n_rows); p64(8, p.n_bits); p64(16, p.blowup); p64(24, p.num_queries);
-  p64(32, p.final_size); p32(40, p.grinding_bits); p64(44, p.cap_height); p32(52, p.value);
-  transcript_absorb(ts, "range/params", pb, 56);
-
   NttPlan lp;
-  lp.logn = logN; lp.batch = (uint32_t)(ncol * B); lp.in_div = (uint32_t)B; lp.twist_mod = (uint32_t)B;
+  lp.logn = logN; lp.batch = (uint32_t)(ncol * B * K); lp.in_div = (uint32_t)B;
+  lp.twist_mod = (uint32_t)B;
   lp.twist_shift = 27 - logm;
   CK(launch::ntt(st, c->tb, lp, coeffs, lde, (uint32_t*)c->scratch.p));
-  CK(launch::range_trace_leaves(st, lde, ttree, logN, logB, (uint32_t)ncol));
-  CK(launch::merkle_build(st, ttree, m, tsteps, merkle_counter(c), hio_dev<uint32_t>(c, h.trace_cap)));
-  CK(launch::coset_zinv(st, c->tb, zinv, zinv2, logB, to_mont(fpow(GENERATOR, N)), nullptr,
-                        (uint32_t)c->slot));
+  const uint64_t tcap_stride = h.trace_cap_bytes / 4;
+  CK(launch::range_trace_leaves(st, lde, ttree, logN, logB, (uint32_t)ncol, K, ttree_words));
+  CK(launch::merkle_build(st, ttree, m, tsteps, merkle_counter(c), hio_dev<uint32_t>(c, h.trace_cap),
+                          0, K, ttree_words, tcap_stride));
+  CK(launch::coset_zinv(st, c->tb, zinv, zinv2, logB, to_mont(fpow(GENERATOR, N)), nullptr, slot));
   CK(sync(c, "cap"));
-  std::vector<uint8_t> column_cap(c->hio + h.trace_cap, c->hio + h.trace_cap + (32ull << tdrop));
-  c->d2h += column_cap.size();
-  transcript_absorb(ts, "range/column", column_cap.data(), column_cap.size());
-  for (uint64_t k = 0; k < ncol + 1; k++) {  // decomposition, n_bits booleans, boundary
-    uint32_t a[4];
-    challenge_ext(ts, "range/alpha", a);
-    for (int e = 0; e < 4; e++) halpha[4 * k + e] = to_mont(a[e]);
+  std::vector<std::vector<uint8_t>> column_cap(K);
+  for (uint32_t k = 0; k < K; k++) {
+    const uint8_t* cap = c->hio + h.trace_cap + k * h.trace_cap_bytes;
+    column_cap[k].assign(cap, cap + h.trace_cap_bytes);
+    c->d2h += h.trace_cap_bytes;
+    transcript_absorb(*tasks[k].ts, "range/column", cap, h.trace_cap_bytes);
+    for (uint64_t i = 0; i < ncol + 1; i++) {  // decomposition, n_bits booleans, boundary
+      uint32_t a[4];
+      challenge_ext(*tasks[k].ts, "range/alpha", a);
+      for (int e = 0; e < 4; e++) halpha[4 * (ncol + 1) * k + 4 * i + e] = to_mont(a[e]);
+    }
   }
 
   RangeComposeArgs ca;
   ca.lde = lde; ca.zinv = zinv; ca.zinv2 = zinv2;
-  ca.alphas = hio_dev<uint32_t>(c, h.extra) + ncol;
+  ca.alphas = dalpha;
   ca.layer0 = fb.layer[0]; ca.leaves = fb.tree[0];
-  ca.logN = logN; ca.logB = logB; ca.n_bits = (uint32_t)p.n_bits; ca.slot = (uint32_t)c->slot;
-  c->consts->value = p.value;
-  CK(push_consts(c));
-  CK(launch::range_compose_leaves(st, c->tb, ca));
+  ca.logN = logN; ca.logB = logB; ca.n_bits = (uint32_t)p0.n_bits; ca.slot = slot;
+  ca.layer_stride = fb.val_stride;
+  ca.tree_stride = fb.tree_stride;
+  CK(launch::range_compose_leaves(st, c->tb, ca, K));
   CK(launch::merkle_build(st, fb.tree[0], s.leaves[0], s.depth[0] - s.drop[0], merkle_counter(c),
-                          hio_dev<uint32_t>(c, h.fri_cap[0])));
+                          hio_dev<uint32_t>(c, h.fri_cap[0]), 0, K, fb.tree_stride,
+                          h.fri_cap_bytes[0] / 4));
 
-  FriOut fo;
-  RC(run_fri(c, s, fp, fb, m, N - 1, ts, h, &fo));
+  std::vector<Transcript*> ts(K);
+  for (uint32_t k = 0; k < K; k++) ts[k] = tasks[k].ts;
+  std::vector<FriOut> fo(K);
+  RC(run_fri(c, s, fp, fb, m, N - 1, ts.data(), K, h, fo.data()));
 
   OpenArgs oa{};  // src/range.rs:483-500
   oa.lde = lde; oa.ttree = ttree; oa.tleaves = m; oa.tsteps = tsteps;
   oa.logN = logN; oa.logB = logB; oa.ncol = (uint32_t)ncol;
-  RC(run_openings(c, s, fb, h, fo, oa));
+  oa.lde_stride = m * ncol;
+  oa.ttree_stride = ttree_words;
+  RC(run_openings(c, s, fb, h, fo.data(), K, oa));
 
-  Writer w(out, need);  // range::Proof::to_bytes (src/range.rs:253-269)
-  w.byte(6);
-  w.u32((uint32_t)(column_cap.size() / 32));
-  w.bytes(column_cap.data(), column_cap.size());
-  write_fri(w, c, s, fo, m, N - 1, h);
-  w.u32((uint32_t)fo.indices.size());
-  for (size_t qi = 0; qi < fo.indices.size(); qi++) {
-    uint64_t index = brev(fo.indices[qi], logm);
-    const uint32_t* row = open_block(c, h, qi) + h.trace_off;
-    w.u64(index);
-    w.u32(row[0]);
-    w.u32((uint32_t)p.n_bits);
-    for (uint64_t b = 0; b < p.n_bits; b++) w.u32(row[1 + b]);
-    write_path(w, (const uint8_t*)(row + ncol), index, tsteps);
-  }
-  if (w.n != need) {
-    set_reason("internal error: proof length differs from its shape");
-    return Z0P_ERR_CUDA;
+  for (uint32_t k = 0; k < K; k++) {
+    const z0p_range_params& p = *tasks[k].p;
+    Writer w(tasks[k].out, need);  // range::Proof::to_bytes (src/range.rs:253-269)
+    w.byte(6);
+    w.u32((uint32_t)(column_cap[k].size() / 32));
+    w.bytes(column_cap[k].data(), column_cap[k].size());
+    write_fri(w, c, s, fo[k], m, N - 1, h, k);
+    w.u32((uint32_t)fo[k].indices.size());
+    for (size_t qi = 0; qi < fo[k].indices.size(); qi++) {
+      uint64_t index = brev(fo[k].indices[qi], logm);
+      const uint32_t* row = open_block(c, h, k, qi) + h.trace_off;
+      w.u64(index);
+      w.u32(row[0]);
+      w.u32((uint32_t)p.n_bits);
+      for (uint64_t b = 0; b < p.n_bits; b++) w.u32(row[1 + b]);
+      write_path(w, (const uint8_t*)(row + ncol), index, tsteps);
+    }
+    if (w.n != need) {
+      set_reason("internal error: proof length differs from its shape");
+      return Z0P_ERR_CUDA;
+    }
   }
   return Z0P_OK;
 }
@@ -871,6 +1032,55 @@ int with_device(z0p_gpu_ctx* c) {
 }
 
 }  // namespace
+
+struct ProfileScope {
+  bool on;
+  explicit ProfileScope(z0p_gpu_ctx* c) : on(c->profiling) {
+    if (on) launch::set_recorder(&c->rec);
+  }
+  ~ProfileScope() {
+    if (on) launch::set_recorder(nullptr);
+  }
+};
+
+// Proves n statements of one shape in groups of at most kMaxGroup, each on
+// working copies of the transcripts; the copies are written back only when
+// every proof succeeded, so a failing call leaves every transcript untouched.
+template <class Params, class Fn>
+int prove_group_abi(z0p_gpu_ctx* c, size_t n, const Params* params,
+                    z0p_transcript_state* const* transcripts, uint8_t* const* outs,
+                    const size_t* caps, size_t* lens, Fn prove) {
+  if (!c || !n || !params || !transcripts || !outs || !caps) return Z0P_ERR_INVALID_ARGUMENT;
+  for (size_t i = 0; i < n; i++)
+    if (!transcripts[i]) return Z0P_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lk(c->mu);
+  RC(with_device(c));
+  ProfileScope ps(c);
+  const uint64_t t0 = now_ns();
+  std::vector<z0p_transcript_state> work(n);
+  for (size_t i = 0; i < n; i++) work[i] = *transcripts[i];
+  int rc = Z0P_OK;
+  for (size_t at = 0; at < n && rc == Z0P_OK; at += kMaxGroup) {
+    const uint32_t K = (uint32_t)(n - at < (size_t)kMaxGroup ? n - at : (size_t)kMaxGroup);
+    std::vector<Transcript> tr;
+    tr.reserve(K);
+    std::vector<Task<Params>> tasks(K);
+    for (uint32_t k = 0; k < K; k++) {
+      tr.emplace_back(&work[at + k]);
+      tasks[k] = Task<Params>{&params[at + k], &tr[k], outs[at + k], caps[at + k],
+                              lens ? &lens[at + k] : nullptr};
+    }
+    c->last_sync_ns = now_ns();
+    rc = prove(c, tasks.data(), K);
+    if (c->profiling && c->last_sync_ns) c->tail_ns += now_ns() - c->last_sync_ns;
+    c->last_sync_ns = 0;
+  }
+  c->prove_ns += now_ns() - t0;
+  if (rc != Z0P_OK) return rc;
+  for (size_t i = 0; i < n; i++) *transcripts[i] = work[i];
+  c->proofs += n;
+  return Z0P_OK;
+}
 
 // ================================================================ C ABI ====
 extern "C" {
@@ -1028,24 +1238,27 @@ int z0p_gpu_ctx_create(int device, z0p_gpu_ctx** out) {
   }
   int rc = build_tables(c);
   if (rc == Z0P_OK) {
-    c->slot = take_slot();
+    c->slot = take_slots(1);
+    c->nslots = c->slot < 0 ? 0 : 1;
     if (c->slot < 0) {
       set_reason("context creation: every constant slot is taken (too many contexts)");
       rc = Z0P_ERR_OUT_OF_MEMORY;
     } else if (launch::const_slot_address(c->slot, &c->slot_dev) != cudaSuccess ||
-               cudaHostAlloc((void**)&c->consts, sizeof(ProofConsts), cudaHostAllocDefault) !=
-                   cudaSuccess) {
+               cudaHostAlloc((void**)&c->consts, kMaxGroup * sizeof(ProofConsts),
+                             cudaHostAllocDefault) != cudaSuccess) {
       set_reason("context creation: constant slot setup failed");
       rc = Z0P_ERR_CUDA;
     } else {
-      std::memset(c->consts, 0, sizeof(ProofConsts));
+      std::memset(c->consts, 0, kMaxGroup * sizeof(ProofConsts));
     }
   }
-  if (rc == Z0P_OK) rc = ensure(c, c->state, 64);
+  const size_t state_bytes = 4 * kMaxGroup + 32 * kMaxGroup;
+  if (rc == Z0P_OK) rc = ensure(c, c->state, state_bytes);
   if (rc == Z0P_OK) {
-    // Merkle counter 0; PoW state {best = ~0, next chunk 0, status 0, done 0}.
-    uint64_t init[8] = {0, ~0ull, 0, 0, 0, 0, 0, 0};
-    if (cudaMemcpyAsync(c->state.p, init, sizeof init, cudaMemcpyHostToDevice, c->stream) !=
+    // Merkle counters 0; PoW states {best = ~0, next chunk 0, status 0, done 0}.
+    std::vector<uint64_t> init(state_bytes / 8, 0);
+    for (int k = 0; k < kMaxGroup; k++) init[kMaxGroup / 2 + 4 * k] = ~0ull;
+    if (cudaMemcpyAsync(c->state.p, init.data(), state_bytes, cudaMemcpyHostToDevice, c->stream) !=
             cudaSuccess ||
         cudaStreamSynchronize(c->stream) != cudaSuccess) {
       set_reason("context creation: state upload failed");
@@ -1070,7 +1283,7 @@ void z0p_gpu_ctx_destroy(z0p_gpu_ctx* c) {
   if (c->stream) cudaStreamSynchronize(c->stream);
   if (c->hio) cudaFreeHost(c->hio);
   if (c->consts) cudaFreeHost(c->consts);
-  give_slot(c->slot);
+  give_slots(c->slot, c->nslots);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }
@@ -1088,35 +1301,17 @@ int z0p_gpu_ctx_trim(z0p_gpu_ctx* c) {
 void* z0p_gpu_ctx_stream(z0p_gpu_ctx* c) { return c ? (void*)c->stream : nullptr; }
 size_t z0p_gpu_ctx_device_bytes(z0p_gpu_ctx* c) { return c ? c->held : 0; }
 
-struct ProfileScope {
-  bool on;
-  explicit ProfileScope(z0p_gpu_ctx* c) : on(c->profiling) {
-    if (on) launch::set_recorder(&c->rec);
-  }
-  ~ProfileScope() {
-    if (on) launch::set_recorder(nullptr);
-  }
-};
 
 int z0p_gpu_air_prove(z0p_gpu_ctx* c, const z0p_air_params* p, z0p_transcript_state* ts,
                       uint8_t* out, size_t cap, size_t* len) {
   if (!c || !p || !ts) return Z0P_ERR_INVALID_ARGUMENT;
-  std::lock_guard<std::mutex> lk(c->mu);
-  RC(with_device(c));
-  ProfileScope ps(c);
-  uint64_t t0 = now_ns();
-  z0p_transcript_state work = *ts;
-  Transcript t(&work);
-  c->last_sync_ns = t0;
-  int rc = air_prove(c, *p, t, out, cap, len);
-  if (c->profiling && c->last_sync_ns) c->tail_ns += now_ns() - c->last_sync_ns;
-  c->last_sync_ns = 0;
-  c->prove_ns += now_ns() - t0;
-  if (rc == Z0P_OK) {
-    *ts = work;
-    c->proofs++;
-  }
-  return rc;
+  return prove_group_abi(c, 1, p, &ts, &out, &cap, len, air_prove);
+}
+
+int z0p_gpu_air_prove_group(z0p_gpu_ctx* c, size_t n, const z0p_air_params* params,
+                            z0p_transcript_state* const* transcripts, uint8_t* const* outs,
+                            const size_t* caps, size_t* lens) {
+  return prove_group_abi(c, n, params, transcripts, outs, caps, lens, air_prove);
 }
 
 int z0p_gpu_ctx_stats(z0p_gpu_ctx* c, z0p_gpu_stats* out) {
@@ -1186,22 +1381,13 @@ int z0p_gpu_ctx_profile(z0p_gpu_ctx* c, char* json, size_t cap, size_t* len) {
 int z0p_gpu_range_prove(z0p_gpu_ctx* c, const z0p_range_params* p, z0p_transcript_state* ts,
                         uint8_t* out, size_t cap, size_t* len) {
   if (!c || !p || !ts) return Z0P_ERR_INVALID_ARGUMENT;
-  std::lock_guard<std::mutex> lk(c->mu);
-  RC(with_device(c));
-  ProfileScope ps(c);
-  uint64_t t0 = now_ns();
-  z0p_transcript_state work = *ts;
-  Transcript t(&work);
-  c->last_sync_ns = t0;
-  int rc = range_prove(c, *p, t, out, cap, len);
-  if (c->profiling && c->last_sync_ns) c->tail_ns += now_ns() - c->last_sync_ns;
-  c->last_sync_ns = 0;
-  c->prove_ns += now_ns() - t0;
-  if (rc == Z0P_OK) {
-    *ts = work;
-    c->proofs++;
-  }
-  return rc;
+  return prove_group_abi(c, 1, p, &ts, &out, &cap, len, range_prove);
+}
+
+int z0p_gpu_range_prove_group(z0p_gpu_ctx* c, size_t n, const z0p_range_params* params,
+                              z0p_transcript_state* const* transcripts, uint8_t* const* outs,
+                              const size_t* caps, size_t* lens) {
+  return prove_group_abi(c, n, params, transcripts, outs, caps, lens, range_prove);
 }
 
 int z0p_gpu_rs_extend(z0p_gpu_ctx* c, const uint32_t* d_values, uint64_t n, uint64_t batch,
@@ -1280,7 +1466,7 @@ int z0p_gpu_fri_fold(z0p_gpu_ctx* c, const uint32_t* d_in, uint64_t n, uint64_t 
     e4_table(q, c->consts->tab[k]);
   }
   fa.slot = (uint32_t)c->slot;
-  CK(push_consts(c));
+  CK(push_consts(c, 1));
   uint32_t built = 0;
   CK(launch::fri_fold(c->stream, c->tb, fa, &built));  // top 0, no cap: leaves only
   CK(sync(c));
@@ -1339,7 +1525,7 @@ int z0p_gpu_grind(z0p_gpu_ctx* c, const uint8_t* head, size_t head_len, uint32_t
   RC(with_device(c));
   RC(ensure_hio(c, 16));
   set_head(c->consts, head, head_len);
-  CK(push_consts(c));
+  CK(push_consts(c, 1));
   CK(launch::grind(c->stream, (uint32_t)c->slot, (uint32_t)head_len, bits, grind_state(c),
                    hio_dev<unsigned long long>(c, 0), 1ull << 40));
   CK(sync(c));
