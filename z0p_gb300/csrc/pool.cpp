@@ -3,9 +3,13 @@
 //
 // Each worker thread owns one context (its own CUDA stream and workspace),
 // so independent proofs overlap on the GPU: one proof's kernels fill the
-// SMs while another waits on its Fiat-Shamir round trip. Admission keeps the
-// sum of running jobs' device footprints within the budget; the queue is
-// strictly FIFO so a large job is never starved by smaller ones behind it.
+// SMs while another waits on its Fiat-Shamir round trip. A worker that
+// takes the queue head also takes the queued jobs of the same shape behind
+// it that fit the budget, up to a group limit, and proves them as one
+// lockstep group (one launch sequence and one set of round trips): requests
+// that arrive while others run are batched as they come. Admission keeps the
+// sum of running jobs' device footprints within the budget; the head is
+// always served first, so a large job is never starved by smaller ones.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -23,12 +27,37 @@
 namespace {
 
 constexpr size_t kKeepBytes = 512ull << 20;  // workspace an idle worker may keep
+// A group holds at most kGroupMax proofs and about kGroupRows LDE rows in all:
+// small proofs group widely (their kernels and round trips are mostly fixed
+// cost), a proof whose LDE alone fills the GPU stays alone.
+constexpr uint32_t kGroupMax = 16;
+constexpr uint64_t kGroupRows = 1ull << 22;
 
 struct Pending {
   z0p_job* job;
   uint64_t ticket;
   size_t footprint;
 };
+
+bool same_shape(const z0p_job* a, const z0p_job* b) {
+  if (a->kind != b->kind) return false;
+  if (a->kind == Z0P_JOB_AIR)
+    return a->air.n_steps == b->air.n_steps && a->air.blowup == b->air.blowup &&
+           a->air.num_queries == b->air.num_queries && a->air.final_size == b->air.final_size &&
+           a->air.grinding_bits == b->air.grinding_bits && a->air.cap_height == b->air.cap_height;
+  return a->range.n_rows == b->range.n_rows && a->range.n_bits == b->range.n_bits &&
+         a->range.blowup == b->range.blowup && a->range.num_queries == b->range.num_queries &&
+         a->range.final_size == b->range.final_size &&
+         a->range.grinding_bits == b->range.grinding_bits &&
+         a->range.cap_height == b->range.cap_height;
+}
+
+uint32_t group_limit(const z0p_job* j) {
+  uint64_t rows = j->kind == Z0P_JOB_AIR ? j->air.n_steps * j->air.blowup
+                                         : j->range.n_rows * j->range.blowup * (j->range.n_bits + 1);
+  uint64_t g = rows ? kGroupRows / rows : 1;
+  return g < 1 ? 1u : (g > kGroupMax ? kGroupMax : (uint32_t)g);
+}
 
 }  // namespace
 
@@ -58,41 +87,80 @@ int footprint(const z0p_job* j, size_t* bytes) {
   return Z0P_ERR_INVALID_ARGUMENT;
 }
 
+// Proves one group of same-shape jobs on the worker's context.
+int prove_group(z0p_gpu_ctx* ctx, const std::vector<Pending>& group) {
+  const size_t n = group.size();
+  std::vector<z0p_transcript_state*> ts(n);
+  std::vector<uint8_t*> outs(n);
+  std::vector<size_t> caps(n), lens(n, 0);
+  for (size_t i = 0; i < n; i++) {
+    ts[i] = group[i].job->transcript;
+    outs[i] = group[i].job->out;
+    caps[i] = group[i].job->cap;
+  }
+  int rc;
+  if (group[0].job->kind == Z0P_JOB_AIR) {
+    std::vector<z0p_air_params> ps(n);
+    for (size_t i = 0; i < n; i++) ps[i] = group[i].job->air;
+    rc = z0p_gpu_air_prove_group(ctx, n, ps.data(), ts.data(), outs.data(), caps.data(), lens.data());
+  } else {
+    std::vector<z0p_range_params> ps(n);
+    for (size_t i = 0; i < n; i++) ps[i] = group[i].job->range;
+    rc = z0p_gpu_range_prove_group(ctx, n, ps.data(), ts.data(), outs.data(), caps.data(),
+                                   lens.data());
+  }
+  for (size_t i = 0; i < n; i++) group[i].job->len = lens[i];
+  return rc;
+}
+
 void worker(z0p_gpu_pool* p, z0p_gpu_ctx* ctx) {
   cudaSetDevice(p->device);
   for (;;) {
-    Pending item;
+    std::vector<Pending> group;
+    size_t group_fp = 0;
     {
       std::unique_lock<std::mutex> lk(p->mu);
-      // FIFO head only, admitted when it fits next to the running jobs.
+      // FIFO head first, admitted when it fits next to the running jobs.
       p->work_cv.wait(lk, [&] {
         return p->stop ||
                (!p->queue.empty() && p->inflight + p->queue.front().footprint <= p->budget);
       });
       if (p->stop) return;
-      item = p->queue.front();
+      group.push_back(p->queue.front());
       p->queue.pop_front();
-      p->inflight += item.footprint;
-      item.job->start_s = p->now();
+      group_fp = group[0].footprint;
+      // Then the queued jobs of the same shape, while they fit.
+      const uint32_t limit = group_limit(group[0].job);
+      for (auto it = p->queue.begin(); it != p->queue.end() && group.size() < limit;) {
+        if (same_shape(it->job, group[0].job) &&
+            p->inflight + group_fp + it->footprint <= p->budget) {
+          group_fp += it->footprint;
+          group.push_back(*it);
+          it = p->queue.erase(it);
+        } else {
+          ++it;
+        }
+      }
+      p->inflight += group_fp;
+      const double t = p->now();
+      for (auto& g : group) g.job->start_s = t;
     }
     // The next head may fit too.
     p->work_cv.notify_all();
-    z0p_job* j = item.job;
-    int rc;
-    if (j->kind == Z0P_JOB_AIR)
-      rc = z0p_gpu_air_prove(ctx, &j->air, j->transcript, j->out, j->cap, &j->len);
-    else
-      rc = z0p_gpu_range_prove(ctx, &j->range, j->transcript, j->out, j->cap, &j->len);
+    int rc = prove_group(ctx, group);
     // A context that just held a large job gives its workspace back to the
     // device pool, so memory held by idle workers stays small next to the
     // admission budget.
     if (z0p_gpu_ctx_device_bytes(ctx) > kKeepBytes) z0p_gpu_ctx_trim(ctx);
     {
       std::lock_guard<std::mutex> lk(p->mu);
-      j->status = rc;
-      j->end_s = p->now();
-      p->inflight -= item.footprint;
-      p->done[item.ticket] = rc;
+      const double t = p->now();
+      for (auto& g : group) {
+        g.job->status = rc;
+        g.job->end_s = t;
+        p->done[g.ticket] = rc;
+      }
+      p->inflight -= group_fp;
     }
     p->done_cv.notify_all();
     p->work_cv.notify_all();
