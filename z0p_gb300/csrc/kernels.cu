@@ -49,23 +49,25 @@ __device__ __forceinline__ void store_digest(uint32_t* p, const uint32_t d[8]) {
 }
 
 // ------------------------------------------------------------ trace gen ----
-// (A_i, B_i) = M^i (a0, b0) with M = [[0,1],[1,1]] (src/air.rs:341-354): each
-// thread jumps to its chunk start with the binary powers of M, then steps.
+// (A_i, B_i) = M^i (a0, b0) with M = [[0,1],[1,1]] (src/air.rs:341-354).
+// Lane l of a warp owns rows base + l + 32 j (j < per_lane): it jumps to its
+// first row with the binary powers of M, then steps by M^32, so every store
+// of the warp covers 32 consecutive rows.
 __constant__ ProofConsts g_consts[kConstSlots];
 
 struct FibMats {
-  uint32_t m[32][4];
+  uint32_t m[32][4];  // M^(2^k), canonical
 };
 
 __global__ void fib_trace_kernel(uint32_t* __restrict__ col_a, uint32_t* __restrict__ col_b,
                                  uint32_t n, uint32_t slot, FibMats mats,
-                                 uint32_t per_thread) {
+                                 uint32_t per_lane) {
   const uint32_t pk = blockIdx.y;  // proof of the group
   col_a += (size_t)pk * n;
   col_b += (size_t)pk * n;
   const uint32_t a0 = g_consts[slot + pk].a0, b0 = g_consts[slot + pk].b0;
-  uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  uint64_t start = t * per_thread;
+  const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const uint64_t start = (t >> 5) * 32 * per_lane + (t & 31);
   if (start >= n) return;
   uint32_t r00 = 1, r01 = 0, r10 = 0, r11 = 1;
   for (int k = 0; k < 32; k++) {
@@ -80,13 +82,16 @@ __global__ void fib_trace_kernel(uint32_t* __restrict__ col_a, uint32_t* __restr
   }
   uint32_t a = fadd(fmul(r00, a0), fmul(r01, b0));
   uint32_t b = fadd(fmul(r10, a0), fmul(r11, b0));
-  uint64_t end = start + per_thread < n ? start + per_thread : n;
-  for (uint64_t i = start; i < end; i++) {
+  const uint32_t s00 = to_mont(mats.m[5][0]), s01 = to_mont(mats.m[5][1]);
+  const uint32_t s10 = to_mont(mats.m[5][2]), s11 = to_mont(mats.m[5][3]);
+  for (uint32_t j = 0; j < per_lane; j++) {
+    const uint64_t i = start + 32ull * j;
+    if (i >= n) break;
     col_a[i] = a;
     col_b[i] = b;
-    uint32_t nb = fadd(a, b);
-    a = b;
-    b = nb;
+    const uint32_t na = mdot2(a, s00, b, s01);
+    b = mdot2(a, s10, b, s11);
+    a = na;
   }
 }
 
@@ -381,15 +386,77 @@ __device__ __forceinline__ uint64_t level_offset(uint64_t leaves, uint32_t level
   return 2 * leaves - 2 * (leaves >> level);
 }
 
+// Digests sit in shared memory at a stride of 9 words (2-way bank conflicts
+// at most when a thread reads its two children).
+constexpr int kTopStride = 9;
+
+__device__ __forceinline__ void hash_pair_smem(const uint32_t* pair, uint32_t* out_s,
+                                               uint32_t* out_g, uint32_t* out_cap) {
+  uint32_t a[8], b[8], d[8];
+#pragma unroll
+  for (int i = 0; i < 8; i++) { a[i] = pair[i]; b[i] = pair[kTopStride + i]; }
+  blake3_node(a, b, d);
+#pragma unroll
+  for (int i = 0; i < 8; i++) out_s[i] = d[i];
+  store_digest(out_g, d);
+  if (out_cap) store_digest(out_cap, d);
+}
+
+// Levels lsub+1..top of a tree whose CTAs have each written one root at
+// level lsub (leaves >> lsub == gridDim.x; thread 0 wrote the CTA's root).
+// Without a grid barrier: the CTA that arrives last (one atomic per CTA on
+// `counter`, after a release fence; nobody waits) loads the roots into
+// shared memory (buf: 2 * 9 * gridDim.x words) and hashes the remaining
+// levels there, each node to the tree and level `top` also to `cap`. It puts
+// the counter back to zero for the next launch. Every thread calls it.
+__device__ __forceinline__ void last_cta_levels(uint32_t* tree, uint64_t leaves, uint32_t lsub,
+                                                uint32_t top, unsigned int* counter,
+                                                uint32_t* cap, uint32_t* buf) {
+  __shared__ int s_last;
+  if (threadIdx.x == 0) {
+    __threadfence();
+    s_last = (atomicAdd(counter, 1u) == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  uint64_t n = leaves >> lsub;
+  const uint32_t* roots = tree + 8 * level_offset(leaves, lsub);
+  for (uint64_t i = threadIdx.x; i < n; i += blockDim.x) {
+    const uint4* p = reinterpret_cast<const uint4*>(roots + 8 * i);
+    uint4 v0 = __ldcg(p), v1 = __ldcg(p + 1);
+    uint32_t* o = buf + kTopStride * i;
+    o[0] = v0.x; o[1] = v0.y; o[2] = v0.z; o[3] = v0.w;
+    o[4] = v1.x; o[5] = v1.y; o[6] = v1.z; o[7] = v1.w;
+  }
+  uint32_t* cur = buf;
+  uint32_t* nxt = buf + kTopStride * n;
+  __syncthreads();
+  for (uint32_t l = lsub; l < top; l++) {
+    n >>= 1;
+    uint32_t* next = tree + 8 * level_offset(leaves, l + 1);
+    for (uint64_t i = threadIdx.x; i < n; i += blockDim.x)
+      hash_pair_smem(cur + 2 * kTopStride * i, nxt + kTopStride * i, next + 8 * i,
+                     (cap && l + 1 == top) ? cap + 8 * i : nullptr);
+    uint32_t* tmp = cur;
+    cur = nxt;
+    nxt = tmp;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *counter = 0u;
+}
+
 // Levels 1..min(log2(nt), top) of the subtree over one CTA's nt consecutive
 // leaves (leaf first + t holds thread t's digest d), hashed in shared memory
 // right where the leaves are made: each node goes to the tree and, at level
 // `top`, to `cap` (as does the leaf itself when top == 0). Every thread of
 // the CTA calls it; nt is a power of two no larger than the CTA, and buf
-// holds 2 * nt * 9 words. Returns the number of levels built.
-__device__ __forceinline__ uint32_t cta_subtree(const uint32_t d[8], uint32_t* buf, uint32_t nt,
-                                                uint64_t first, uint32_t* tree, uint64_t leaves,
-                                                uint32_t top, uint32_t* cap) {
+// holds 2 * nt * 9 words. With a `counter` (every CTA full, so one root per
+// CTA) the last CTA to finish also hashes the levels above the roots up to
+// `top` (last_cta_levels; buf then holds 2 * 9 * max(nt, gridDim.x) words).
+__device__ __forceinline__ void cta_subtree(const uint32_t d[8], uint32_t* buf, uint32_t nt,
+                                            uint64_t first, uint32_t* tree, uint64_t leaves,
+                                            uint32_t top, uint32_t* cap, unsigned int* counter) {
   const uint32_t t = threadIdx.x;
   if (t < nt) {
     if (cap && top == 0) store_digest(cap + 8 * (first + t), d);
@@ -419,7 +486,7 @@ __device__ __forceinline__ uint32_t cta_subtree(const uint32_t d[8], uint32_t* b
     nxt = tmp;
     __syncthreads();
   }
-  return levels;
+  if (counter && levels < top) last_cta_levels(tree, leaves, levels, top, counter, cap, buf);
 }
 
 // --------------------------------------------------------------- Merkle ----
@@ -431,9 +498,9 @@ constexpr uint32_t kTraceLeafThreads = 256;
 __global__ void __launch_bounds__(kTraceLeafThreads) air_trace_leaves_kernel(
     const uint32_t* __restrict__ lde_a, const uint32_t* __restrict__ cb, uint32_t w_last_m,
     uint32_t* __restrict__ leaves, uint32_t* __restrict__ tinv, uint32_t logN, uint32_t logB,
-    uint32_t nleaves, uint32_t top, uint32_t* cap, uint64_t tree_stride, uint64_t cap_stride,
-    Tables tb) {
-  __shared__ uint32_t buf[2 * kTraceLeafThreads * 9];
+    uint32_t nleaves, uint32_t top, uint32_t* cap, unsigned int* counter, uint64_t tree_stride,
+    uint64_t cap_stride, Tables tb) {
+  __shared__ uint32_t buf[2 * kTraceLeafThreads * 9];  // >= 2 * 9 * (kFuseMaxLeaves / 256) roots
   {
     const uint32_t pk = blockIdx.y;  // proof of the group
     const size_t m = (size_t)nleaves * 8;
@@ -442,6 +509,7 @@ __global__ void __launch_bounds__(kTraceLeafThreads) air_trace_leaves_kernel(
     tinv += pk * m;
     leaves += pk * tree_stride;
     if (cap) cap += pk * cap_stride;
+    if (counter) counter += pk;
   }
   const uint32_t nt = nleaves < kTraceLeafThreads ? nleaves : kTraceLeafThreads;
   const uint32_t L = blockIdx.x * kTraceLeafThreads + threadIdx.x;
@@ -470,7 +538,8 @@ __global__ void __launch_bounds__(kTraceLeafThreads) air_trace_leaves_kernel(
   blake3_leaf64(m, d);
   store_digest(leaves + 8 * (size_t)L, d);
   }
-  cta_subtree(d, buf, nt, (uint64_t)blockIdx.x * kTraceLeafThreads, leaves, nleaves, top, cap);
+  cta_subtree(d, buf, nt, (uint64_t)blockIdx.x * kTraceLeafThreads, leaves, nleaves, top, cap,
+              counter);
 }
 
 // Range tree leaf k = BLAKE3(0x00 || row k) with the row = ncols LE words
@@ -541,26 +610,9 @@ __global__ void copy_words_kernel(const uint32_t* __restrict__ src, uint32_t* __
 // Upper levels of a tree without a grid barrier: CTA b hashes the 2T nodes
 // [2T b, 2T b + 2T) of level l0 up to one node at level l0 + log2(2T) (or
 // up to `top`), keeping each level in shared memory and writing it to
-// global. The CTA that finishes last (one atomic per CTA on `counter`, after a
-// release fence) loads the CTAs' roots into shared memory and hashes the
-// remaining levels there. Nobody waits for anybody: the last CTA continues.
-// Digests sit in shared memory at a stride of 9 words (2-way bank conflicts
-// at most when a thread reads its two children).
+// global; the last CTA to finish hashes the rest (last_cta_levels).
 constexpr int kTopThreads = 256;
-constexpr int kTopStride = 9;
 constexpr int kTopMaxRoots = 512;  // level-l0 nodes <= 2^18, 512 per CTA
-
-__device__ __forceinline__ void hash_pair_smem(const uint32_t* pair, uint32_t* out_s,
-                                               uint32_t* out_g, uint32_t* out_cap) {
-  uint32_t a[8], b[8], d[8];
-#pragma unroll
-  for (int i = 0; i < 8; i++) { a[i] = pair[i]; b[i] = pair[kTopStride + i]; }
-  blake3_node(a, b, d);
-#pragma unroll
-  for (int i = 0; i < 8; i++) out_s[i] = d[i];
-  store_digest(out_g, d);
-  if (out_cap) store_digest(out_cap, d);
-}
 
 // `cap` (may be null) receives a copy of level `top`. The CTA that finishes
 // the tree puts `counter` back to zero for the next launch.
@@ -570,7 +622,6 @@ __global__ void __launch_bounds__(kTopThreads) merkle_top_kernel(uint32_t* tree,
                                                                  uint32_t* cap, uint64_t stride,
                                                                  uint64_t cap_stride) {
   __shared__ uint32_t sm[2][kTopMaxRoots * kTopStride];
-  __shared__ int last;
   tree += blockIdx.y * stride;  // proof of the group: its tree, counter and cap
   counter += blockIdx.y;
   if (cap) cap += blockIdx.y * cap_stride;
@@ -605,33 +656,7 @@ __global__ void __launch_bounds__(kTopThreads) merkle_top_kernel(uint32_t* tree,
     __syncthreads();
   }
   if (lsub == top) return;
-  // Publish this CTA's root, then let the last CTA finish the tree.
-  __threadfence();
-  if (threadIdx.x == 0) last = (atomicAdd(counter, 1u) == gridDim.x - 1);
-  __syncthreads();
-  if (!last) return;
-  __threadfence();
-  uint64_t n = leaves >> lsub;  // == gridDim.x <= kTopMaxRoots
-  const uint32_t* roots = tree + 8 * level_offset(leaves, lsub);
-  for (uint64_t i = threadIdx.x; i < n; i += blockDim.x) {
-    const uint4* p = reinterpret_cast<const uint4*>(roots + 8 * i);
-    uint4 v0 = __ldcg(p), v1 = __ldcg(p + 1);
-    uint32_t* o = sm[0] + kTopStride * i;
-    o[0] = v0.x; o[1] = v0.y; o[2] = v0.z; o[3] = v0.w;
-    o[4] = v1.x; o[5] = v1.y; o[6] = v1.z; o[7] = v1.w;
-  }
-  cur = 0;
-  __syncthreads();
-  for (uint32_t l = lsub; l < top; l++) {
-    n >>= 1;
-    uint32_t* next = tree + 8 * level_offset(leaves, l + 1);
-    for (uint64_t i = threadIdx.x; i < n; i += blockDim.x)
-      hash_pair_smem(sm[cur] + 2 * kTopStride * i, sm[cur ^ 1] + kTopStride * i, next + 8 * i,
-                     (cap && l + 1 == top) ? cap + 8 * i : nullptr);
-    cur ^= 1;
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) *counter = 0u;
+  last_cta_levels(tree, leaves, lsub, top, counter, cap, &sm[0][0]);
 }
 
 // 64-byte leaves (four Ext4 values) of an in-memory FRI layer
@@ -871,12 +896,20 @@ __device__ __forceinline__ void fold_for_proof(FoldArgs& a) {
   a.out += pk * a.out_stride;
   a.leaves += pk * a.tree_stride;
   if (a.cap) a.cap += pk * a.cap_stride;
+  if (a.counter) a.counter += pk;
+  if (a.final_vals) a.final_vals += pk * a.final_stride;
   a.slot += pk;
 }
 
+// kFinish: the launch may finish a small tree in its last CTA (a.counter);
+// a separate instantiation keeps the large layers' kernel at its own
+// register count.
+template <bool kFinish>
 __global__ void __launch_bounds__(kFoldThreads) fri_fold_leaf_kernel(FoldArgs a, Tables tb) {
-  __shared__ uint32_t sm[2 * kFoldThreads * 9];  // the next layer's subtree (small trees)
+  // The next layer's subtree (small trees), then the roots of all CTAs.
+  __shared__ uint32_t sm[2 * kTopStride * (kFinish ? kFuseMaxLeaves / kFoldThreads : kFoldThreads)];
   fold_for_proof(a);
+  if (!kFinish) a.counter = nullptr;
   const uint64_t nleaf = 1ull << (a.logn - 4);
   const uint64_t first = (uint64_t)blockIdx.x * kFoldThreads;
   const uint32_t avail = nleaf < (uint64_t)kFoldThreads ? (uint32_t)nleaf : (uint32_t)kFoldThreads;
@@ -904,10 +937,16 @@ __global__ void __launch_bounds__(kFoldThreads) fri_fold_leaf_kernel(FoldArgs a,
 #pragma unroll
   for (int t = 0; t < 4; t++)
     dst[t] = make_uint4(leaf[4 * t], leaf[4 * t + 1], leaf[4 * t + 2], leaf[4 * t + 3]);
+  if (a.final_vals) {
+    uint4* fin = reinterpret_cast<uint4*>(a.final_vals + 16 * Pn);
+#pragma unroll
+    for (int t = 0; t < 4; t++)
+      fin[t] = make_uint4(leaf[4 * t], leaf[4 * t + 1], leaf[4 * t + 2], leaf[4 * t + 3]);
+  }
   blake3_leaf64(leaf, d);
   store_digest(a.leaves + 8 * Pn, d);
   }
-  cta_subtree(d, sm, avail, first, a.leaves, nleaf, a.top, a.cap);
+  cta_subtree(d, sm, avail, first, a.leaves, nleaf, a.top, a.cap, a.counter);
 }
 
 // Thread per next-layer value (small layers; leaves hashed separately).
@@ -923,6 +962,8 @@ __global__ void fri_fold_plain_kernel(FoldArgs a, Tables tb) {
   }
   E4 r = fold_quad(q[0], q[1], q[2], q[3], quad_xinv(tb, a, P), a);
   reinterpret_cast<uint4*>(a.out)[P] = make_uint4(r.c[0], r.c[1], r.c[2], r.c[3]);
+  if (a.final_vals)
+    reinterpret_cast<uint4*>(a.final_vals)[P] = make_uint4(r.c[0], r.c[1], r.c[2], r.c[3]);
 }
 
 // ------------------------------------------------------------------ PoW ----
@@ -962,20 +1003,23 @@ __device__ __forceinline__ void grind_finish(const GrindArgs& a) {
   __threadfence();
 }
 
-template <int H>
+// The preimage is head (47 bytes) || LE64(nonce): one 55-byte block.
+constexpr uint32_t kPowHeadLen = 47;
+
 __global__ void __launch_bounds__(kGrindThreads) grind_kernel(GrindArgs a) {
   a.slot += blockIdx.y;  // proof of the group: its head, search state and result
   a.state += 4 * blockIdx.y;
   a.out += 2 * blockIdx.y;
-  static_assert(H + 8 <= 64, "head and nonce must fit one block");
-  constexpr int W = H / 4, SH = (H % 4) * 8;
+  constexpr int W = kPowHeadLen / 4, SH = (kPowHeadLen % 4) * 8;
+  static_assert(kPowHeadLen + 8 <= 64 && SH != 0, "head and nonce must fit one block");
   __shared__ unsigned long long s_chunk;
   __shared__ int s_stop;
+  const volatile unsigned long long* best_p = a.state;
   for (;;) {
     if (threadIdx.x == 0) {
       unsigned long long c = atomicAdd(a.state + 1, 1ull);
       s_chunk = c;
-      unsigned long long best = *reinterpret_cast<volatile unsigned long long*>(a.state);
+      unsigned long long best = *best_p;
       s_stop = (c >= a.max_chunks) ? 2 : (c * kGrindChunk > best ? 1 : 0);
       if (s_stop == 2) atomicOr(a.state + 2, 1ull);
     }
@@ -987,24 +1031,24 @@ __global__ void __launch_bounds__(kGrindThreads) grind_kernel(GrindArgs a) {
       grind_finish(a);
       return;
     }
+    // Nonces above the best hit so far cannot be the minimum: a thread
+    // leaves the chunk once its next nonce passes the best it last read.
+    unsigned long long best = ~0ull;
 #pragma unroll 1
     for (int k = 0; k < kGrindPerThread; k++) {
       unsigned long long nonce = c * kGrindChunk + (unsigned long long)k * kGrindThreads + threadIdx.x;
-      uint32_t lo = (uint32_t)nonce, hi = (uint32_t)(nonce >> 32);
+      if (nonce > best) break;
+      best = *best_p;
+      const uint32_t lo = (uint32_t)nonce, hi = (uint32_t)(nonce >> 32);
       uint32_t m[16];
 #pragma unroll
       for (int i = 0; i < 16; i++) m[i] = i < W ? g_consts[a.slot].head[i] : 0u;
-      if (SH == 0) {
-        m[W] = lo;
-        m[W + 1] = hi;
-      } else {
-        m[W] = g_consts[a.slot].head[W] | (lo << SH);
-        m[W + 1] = (lo >> (32 - SH)) | (hi << SH);
-        m[W + 2] = hi >> (32 - SH);
-      }
+      m[W] = g_consts[a.slot].head[W] | (lo << SH);
+      m[W + 1] = (lo >> (32 - SH)) | (hi << SH);
+      m[W + 2] = hi >> (32 - SH);
       uint32_t cv[8], o[8];
       iv_words(cv);
-      blake3_compress(cv, m, 0u, 0u, (uint32_t)(H + 8), kChunkStart | kChunkEnd | kRoot, o);
+      blake3_compress(cv, m, 0u, 0u, kPowHeadLen + 8u, kChunkStart | kChunkEnd | kRoot, o);
       uint32_t lz = __clz(__byte_perm(o[0], 0, 0x0123));
       if (lz >= a.bits) atomicMin(a.state, nonce);
     }
@@ -1166,12 +1210,12 @@ cudaError_t fib_trace(cudaStream_t st, uint32_t* col_a, uint32_t* col_b, uint32_
   FibMats fm;
   for (int k = 0; k < 32; k++)
     for (int i = 0; i < 4; i++) fm.m[k][i] = mats[k][i];
-  uint32_t per = 64;
-  uint64_t threads = (n + per - 1) / per;
+  const uint32_t per_lane = 16;  // rows per lane; a warp covers 512 consecutive rows
+  const uint64_t threads = 32 * ((n + 32 * per_lane - 1) / (32 * per_lane));
   Stage stg("trace", st);
   stg.launched();
   fib_trace_kernel<<<dim3(grid_for(threads), nproofs), kThreads, 0, st>>>(col_a, col_b, n, slot, fm,
-                                                                          per);
+                                                                          per_lane);
   return cudaGetLastError();
 }
 
@@ -1292,19 +1336,21 @@ cudaError_t coset_zinv(cudaStream_t st, const Tables& tb, uint32_t* zinv, uint32
 cudaError_t air_trace_leaves(cudaStream_t st, const Tables& tb, const uint32_t* lde_a,
                              const uint32_t* cb, uint32_t w_last_m, uint32_t* leaves,
                              uint32_t* tinv, uint32_t logN, uint32_t logB, uint32_t top,
-                             uint32_t* cap, uint32_t* levels, uint32_t nproofs,
-                             uint64_t tree_stride, uint64_t cap_stride) {
+                             uint32_t* cap, unsigned int* counter, uint32_t* levels,
+                             uint32_t nproofs, uint64_t tree_stride, uint64_t cap_stride) {
   uint32_t nleaves = 1u << (logN + logB - 3);
   if (nleaves > kFuseMaxLeaves) {
     top = 0;  // no subtree; merkle_build does every level
     cap = nullptr;
+    counter = nullptr;
   }
-  *levels = subtree_levels(nleaves < kTraceLeafThreads ? nleaves : kTraceLeafThreads, top);
+  *levels = counter ? top
+                    : subtree_levels(nleaves < kTraceLeafThreads ? nleaves : kTraceLeafThreads, top);
   Stage stg("trace_leaves", st);
   stg.launched();
   air_trace_leaves_kernel<<<dim3(grid_for(nleaves, kTraceLeafThreads), nproofs), kTraceLeafThreads,
                             0, st>>>(lde_a, cb, w_last_m, leaves, tinv, logN, logB, nleaves, top, cap,
-                                     tree_stride, cap_stride, tb);
+                                     counter, tree_stride, cap_stride, tb);
   return cudaGetLastError();
 }
 
@@ -1386,11 +1432,19 @@ cudaError_t fri_fold(cudaStream_t st, const Tables& tb, const FoldArgs& a, uint3
     if (nleaf > kFuseMaxLeaves) {
       f.top = 0;  // no subtree; merkle_build does every level
       f.cap = nullptr;
+      f.counter = nullptr;
     }
-    *levels = subtree_levels(nleaf < (uint64_t)kFoldThreads ? (uint32_t)nleaf : kFoldThreads, f.top);
+    *levels = f.counter ? f.top
+                        : subtree_levels(nleaf < (uint64_t)kFoldThreads ? (uint32_t)nleaf
+                                                                        : kFoldThreads,
+                                         f.top);
     Stage stg("fri_fold_leaves", st);
     stg.launched();
-    fri_fold_leaf_kernel<<<dim3(grid_for(nleaf, kFoldThreads), nproofs), kFoldThreads, 0, st>>>(f, tb);
+    const dim3 grid(grid_for(nleaf, kFoldThreads), nproofs);
+    if (f.counter)
+      fri_fold_leaf_kernel<true><<<grid, kFoldThreads, 0, st>>>(f, tb);
+    else
+      fri_fold_leaf_kernel<false><<<grid, kFoldThreads, 0, st>>>(f, tb);
     return cudaGetLastError();
   }
   {
@@ -1428,7 +1482,7 @@ cudaError_t merkle_flat64_leaves(cudaStream_t st, const uint32_t* flat, uint64_t
   return cudaGetLastError();
 }
 
-bool grind_supports(uint32_t head_len) { return head_len == 47; }
+bool grind_supports(uint32_t head_len) { return head_len == kPowHeadLen; }
 
 cudaError_t grind(cudaStream_t st, uint32_t slot, uint32_t head_len, uint32_t bits,
                   unsigned long long* state, unsigned long long* out, uint64_t max_nonces,
@@ -1446,19 +1500,20 @@ cudaError_t grind(cudaStream_t st, uint32_t slot, uint32_t head_len, uint32_t bi
     int dev = 0, per = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, grind_kernel<47>, kGrindThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, grind_kernel, kGrindThreads, 0);
     max_ctas = sms * (per > 0 ? per : 1);
   }
-  // The search expects 2^bits nonces. Every CTA in flight finishes the chunk
-  // it holds when the minimum is found, so the grid keeps about a quarter of
-  // the expected search in flight (at least one CTA per SM): less work past
-  // the answer, and room for other streams' kernels beside it.
-  uint64_t want = (1ull << bits) / (4 * kGrindChunk);
-  int ctas = want > (uint64_t)max_ctas ? max_ctas : (int)want;
+  // The search expects 2^bits nonces. A thread stops at its next nonce once
+  // that passes the best hit, so at most one nonce per thread is hashed past
+  // the answer: the grid can fill the GPU (four CTAs per SM reach the hash
+  // ceiling) without wasting much, but stays below the expected search.
+  uint64_t want = (1ull << bits) / kGrindChunk;
+  int ctas = want > (uint64_t)(4 * sms) ? 4 * sms : (int)want;
+  if (ctas > max_ctas) ctas = max_ctas;
   if (ctas < sms) ctas = sms;
   Stage stg("grind", st);
   stg.launched();
-  grind_kernel<47><<<dim3(ctas, nproofs), kGrindThreads, 0, st>>>(a);
+  grind_kernel<<<dim3(ctas, nproofs), kGrindThreads, 0, st>>>(a);
   return cudaGetLastError();
 }
 

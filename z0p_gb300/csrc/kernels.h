@@ -88,8 +88,15 @@ struct FoldArgs {
   uint32_t ginv_m;     // (31^(4^depth))^-1 (Montgomery)
   uint32_t unit_m;     // two_adic_generator(2) (Montgomery)
   uint32_t slot = 0;   // ProofConsts slot of the first proof: the fold's challenge tables
-  // Per-proof strides (words) of in, out, leaves and cap for a proof group.
-  uint64_t in_stride = 0, out_stride = 0, tree_stride = 0, cap_stride = 0;
+  // One zero device word per proof: with it, a small tree is finished up to
+  // `top` by the fold's last CTA (nullptr: the fold stops at its subtrees).
+  unsigned int* counter = nullptr;
+  // Receives a second copy of the output values when the output is the final
+  // layer (device-visible, e.g. mapped host memory; nullptr: none).
+  uint32_t* final_vals = nullptr;
+  // Per-proof strides (words) of in, out, leaves, cap and final_vals for a
+  // proof group.
+  uint64_t in_stride = 0, out_stride = 0, tree_stride = 0, cap_stride = 0, final_stride = 0;
 };
 
 // Openings of one proof, gathered on the device into one block per query.
@@ -172,14 +179,17 @@ cudaError_t coset_zinv(cudaStream_t st, const Tables& tb, uint32_t* zinv, uint32
                        uint32_t nproofs = 1);
 // Trace leaves of the AIR: rows 8L..8L+7 as A || B with B derived from A.
 // Also writes tinv (m words, coset-major): 1 / (x - w_last) per LDE row.
-// The kernel also hashes each CTA's subtree (up to the cap level `top`;
-// nodes to the tree, the cap level to `cap`); *levels receives how many
-// levels above the leaves are done, the start level for merkle_build.
+// For trees of at most kFuseMaxLeaves leaves the kernel also hashes each
+// CTA's subtree (up to the cap level `top`; nodes to the tree, the cap level
+// to `cap`), and with `counter` (one zero device word per proof) its last CTA
+// finishes the tree up to `top`. *levels receives how many levels above the
+// leaves are done, the start level for merkle_build.
 cudaError_t air_trace_leaves(cudaStream_t st, const Tables& tb, const uint32_t* lde_a,
                              const uint32_t* cb, uint32_t w_last_m, uint32_t* leaves,
                              uint32_t* tinv, uint32_t logN, uint32_t logB, uint32_t top,
-                             uint32_t* cap, uint32_t* levels, uint32_t nproofs = 1,
-                             uint64_t tree_stride = 0, uint64_t cap_stride = 0);
+                             uint32_t* cap, unsigned int* counter, uint32_t* levels,
+                             uint32_t nproofs = 1, uint64_t tree_stride = 0,
+                             uint64_t cap_stride = 0);
 cudaError_t range_trace_leaves(cudaStream_t st, const uint32_t* lde, uint32_t* leaves,
                                uint32_t logN, uint32_t logB, uint32_t ncols, uint32_t nproofs = 1,
                                uint64_t tree_stride = 0);
@@ -202,7 +212,8 @@ cudaError_t range_compose_leaves(cudaStream_t st, const Tables& tb, const RangeC
 // Folds one FRI layer; hashes the next layer's 64-byte leaves when it has a
 // multiple of four values, its 0x00-prefixed 16-byte leaves otherwise. With
 // 64-byte leaves it also hashes each CTA's subtree up to a.top (writing the
-// cap level to a.cap); *levels receives the levels done above the leaves.
+// cap level to a.cap), and the last CTA finishes the tree when a.counter is
+// set; *levels receives the levels done above the leaves.
 cudaError_t fri_fold(cudaStream_t st, const Tables& tb, const FoldArgs& a, uint32_t* levels,
                      uint32_t nproofs = 1);
 // Leaf digests of an FRI layer held in memory (64-byte quads or 16-byte values).

@@ -461,11 +461,14 @@ int run_fri(z0p_gpu_ctx* c, const FriShape& s, const FriParams& fp, const FriBuf
   for (size_t l = 0;; l++) {
     const bool last = l + 1 == s.len.size();
     // A layer's caps are in the mapped buffer once its trees are done; the
-    // last layer's values (sent in the clear) come back in the same trip.
+    // last layer's values (sent in the clear) come back in the same trip,
+    // written there by the last fold (or copied, when there is no fold).
     if (last) {
       c->d2h += (uint64_t)K * h.final_bytes;
-      CK(cudaMemcpy2DAsync(c->hio + h.final_vals, h.final_bytes, fb.layer.back(),
-                           4 * fb.val_stride, h.final_bytes, K, cudaMemcpyDeviceToHost, c->stream));
+      if (l == 0)
+        CK(cudaMemcpy2DAsync(c->hio + h.final_vals, h.final_bytes, fb.layer.back(),
+                             4 * fb.val_stride, h.final_bytes, K, cudaMemcpyDeviceToHost,
+                             c->stream));
     }
     CK(sync(c, last ? "cap+final" : "cap"));
     for (uint32_t k = 0; k < K; k++) {
@@ -504,7 +507,12 @@ int run_fri(z0p_gpu_ctx* c, const FriShape& s, const FriParams& fp, const FriBuf
     fa.in_stride = fa.out_stride = fb.val_stride;
     fa.tree_stride = fb.tree_stride;
     fa.cap_stride = h.fri_cap_bytes[l + 1] / 4;
-    uint32_t built = 0;  // subtree levels the fold kernel hashed itself
+    fa.counter = merkle_counter(c);
+    if (l + 2 == s.len.size()) {  // this fold makes the final layer
+      fa.final_vals = hio_dev<uint32_t>(c, h.final_vals);
+      fa.final_stride = h.final_bytes / 4;
+    }
+    uint32_t built = 0;  // tree levels the fold kernel hashed itself
     CK(launch::fri_fold(c->stream, c->tb, fa, &built, K));
     // Levels above `built` remain, if any. A tree capped at its leaves has
     // its cap written by the fold only when the fold hashed its subtree (64-
@@ -806,8 +814,8 @@ int air_prove(z0p_gpu_ctx* c, const AirTask* tasks, uint32_t K) {
   uint32_t built = 0;  // subtree levels the leaf kernel hashed itself
   const uint64_t tcap_stride = h.trace_cap_bytes / 4;
   CK(launch::air_trace_leaves(st, c->tb, lde_a, cb, w_last_m, ttree, tinv, logN, logB, tsteps,
-                              hio_dev<uint32_t>(c, h.trace_cap), &built, K, ttree_words,
-                              tcap_stride));
+                              hio_dev<uint32_t>(c, h.trace_cap), merkle_counter(c), &built, K,
+                              ttree_words, tcap_stride));
   if (built < tsteps || (tsteps == 0 && tleaves > kFuseMaxLeaves))
     CK(launch::merkle_build(st, ttree, tleaves, tsteps, merkle_counter(c),
                             hio_dev<uint32_t>(c, h.trace_cap), built, K, ttree_words, tcap_stride));
