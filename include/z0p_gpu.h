@@ -154,6 +154,14 @@ size_t z0p_gpu_ctx_device_bytes(z0p_gpu_ctx *ctx);
  * per-call Vecs); a serving loop uses it to keep held memory near the sum of
  * the running jobs' footprints. */
 int z0p_gpu_ctx_trim(z0p_gpu_ctx *ctx);
+/* Reserves the context's per-proof constant slots for proof groups of up to
+ * max_group (1..64) statements, so that later group calls neither wait for
+ * nor compete for them. The process has 168 slots in all (64 KiB of constant
+ * memory); every context holds at least one. Returns Z0P_ERR_OUT_OF_MEMORY
+ * when no max_group free slots are contiguous: the context then keeps its
+ * previous reservation, and a group call larger than the reservation is
+ * proved as consecutive smaller groups. No counterpart in the reference. */
+int z0p_gpu_ctx_reserve_group(z0p_gpu_ctx *ctx, uint32_t max_group);
 /* Cumulative counters of a context (launches are process-wide). */
 typedef struct {
     uint64_t launches;   /* kernels launched by this library in this process */

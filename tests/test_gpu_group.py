@@ -76,3 +76,30 @@ def test_mixed_shapes_are_refused_untouched(z0p, oracle, gpu_ctx):
         z0p.air.prove_group([a, b], ts, gpu_ctx)
     assert e.value.code == 106
     assert [t.export() for t in ts] == before
+
+
+def test_group_on_a_context_short_of_constant_slots(z0p, oracle):
+    """When the process's constant slots run short, reserve_group reports
+    OutOfMemory and keeps the old reservation, and a group call on that
+    context is proved as smaller consecutive groups, byte for byte."""
+    held = []
+    short = None
+    try:
+        for _ in range(4):  # 168 slots: at most two ranges of 64 fit
+            c = z0p.Context(0)
+            held.append(c)
+            try:
+                c.reserve_group(64)
+            except z0p.Z0pError as e:
+                assert e.code == 102
+                short = c
+                break
+        assert short is not None
+        stmts = _air_statements(z0p, oracle, 64, 9, 0x5EED000000000030)
+        ts = [z0p.Transcript(b"short-%d" % i) for i in range(len(stmts))]
+        proofs = z0p.air.prove_group([pz for pz, _ in stmts], ts, short)
+        for i, ((_, po), proof) in enumerate(zip(stmts, proofs)):
+            assert proof == oracle.air_prove(po, oracle.Transcript(b"short-%d" % i)), i
+    finally:
+        for c in held:
+            c.close()

@@ -100,6 +100,7 @@ def lib():
             "z0p_gpu_ctx_stream": (vp, [vp]),
             "z0p_gpu_ctx_device_bytes": (sz, [vp]),
             "z0p_gpu_ctx_trim": (C.c_int, [vp]),
+            "z0p_gpu_ctx_reserve_group": (C.c_int, [vp, C.c_uint32]),
             "z0p_gpu_blake3_ceiling": (C.c_int, [vp, P(C.c_double)]),
             "z0p_gpu_ctx_stats": (C.c_int, [vp, P(Stats)]),
             "z0p_gpu_ctx_set_profiling": (C.c_int, [vp, C.c_int]),

@@ -46,6 +46,10 @@ class Context:
         """Hand the proof workspace back to the library's device memory pool."""
         check(lib().z0p_gpu_ctx_trim(self.handle))
 
+    def reserve_group(self, max_group: int) -> None:
+        """Reserve constant slots for proof groups of up to max_group statements."""
+        check(lib().z0p_gpu_ctx_reserve_group(self.handle, max_group))
+
     def stats(self) -> dict:
         s = Stats()
         check(lib().z0p_gpu_ctx_stats(self.handle, C.byref(s)))

@@ -23,6 +23,7 @@
 
 #include "../../include/z0p_gpu.h"
 #include "host.h"
+#include "kernels.h"
 
 namespace {
 
@@ -52,11 +53,13 @@ bool same_shape(const z0p_job* a, const z0p_job* b) {
          a->range.cap_height == b->range.cap_height;
 }
 
-uint32_t group_limit(const z0p_job* j) {
+// `slots`: the worker's reserved group size (constant slots).
+uint32_t group_limit(const z0p_job* j, uint32_t slots) {
   uint64_t rows = j->kind == Z0P_JOB_AIR ? j->air.n_steps * j->air.blowup
                                          : j->range.n_rows * j->range.blowup * (j->range.n_bits + 1);
   uint64_t g = rows ? kGroupRows / rows : 1;
-  return g < 1 ? 1u : (g > kGroupMax ? kGroupMax : (uint32_t)g);
+  const uint32_t most = kGroupMax < slots ? kGroupMax : slots;
+  return g < 1 ? 1u : (g > most ? most : (uint32_t)g);
 }
 
 }  // namespace
@@ -64,6 +67,7 @@ uint32_t group_limit(const z0p_job* j) {
 struct z0p_gpu_pool {
   int device = 0;
   std::vector<z0p_gpu_ctx*> ctxs;
+  std::vector<uint32_t> slots;  // per worker: the group size its context reserved
   std::vector<std::thread> threads;
   std::mutex mu;
   std::condition_variable work_cv, done_cv;
@@ -113,7 +117,7 @@ int prove_group(z0p_gpu_ctx* ctx, const std::vector<Pending>& group) {
   return rc;
 }
 
-void worker(z0p_gpu_pool* p, z0p_gpu_ctx* ctx) {
+void worker(z0p_gpu_pool* p, z0p_gpu_ctx* ctx, uint32_t slots) {
   cudaSetDevice(p->device);
   for (;;) {
     std::vector<Pending> group;
@@ -130,7 +134,7 @@ void worker(z0p_gpu_pool* p, z0p_gpu_ctx* ctx) {
       p->queue.pop_front();
       group_fp = group[0].footprint;
       // Then the queued jobs of the same shape, while they fit.
-      const uint32_t limit = group_limit(group[0].job);
+      const uint32_t limit = group_limit(group[0].job, slots);
       for (auto it = p->queue.begin(); it != p->queue.end() && group.size() < limit;) {
         if (same_shape(it->job, group[0].job) &&
             p->inflight + group_fp + it->footprint <= p->budget) {
@@ -197,7 +201,19 @@ int z0p_gpu_pool_create(int device, int workers, size_t hbm_budget, z0p_gpu_pool
     }
     p->ctxs.push_back(c);
   }
-  for (auto* c : p->ctxs) p->threads.emplace_back(worker, p, c);
+  // Each worker reserves constant slots for its groups: an equal share of
+  // the process's slots (a few kept for other contexts), at most kGroupMax,
+  // or less when other contexts already hold slots.
+  const int spare = z0p::kConstSlots - 8 - workers;
+  uint32_t share = spare > 0 ? 1u + (uint32_t)(spare / workers) : 1u;
+  if (share > kGroupMax) share = kGroupMax;
+  for (auto* c : p->ctxs) {
+    uint32_t g = share;
+    while (g > 1 && z0p_gpu_ctx_reserve_group(c, g) != Z0P_OK) g--;
+    p->slots.push_back(g);
+  }
+  for (size_t i = 0; i < p->ctxs.size(); i++)
+    p->threads.emplace_back(worker, p, p->ctxs[i], p->slots[i]);
   *out = p;
   return Z0P_OK;
 }

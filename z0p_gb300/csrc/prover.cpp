@@ -230,8 +230,7 @@ int ensure(z0p_gpu_ctx* c, DevBuf& b, size_t bytes) {
 std::mutex g_slot_mu;
 bool g_slot_used[kConstSlots] = {};
 
-int take_slots(int n) {
-  std::lock_guard<std::mutex> lk(g_slot_mu);
+int take_slots_locked(int n) {
   for (int i = 0; i + n <= kConstSlots; i++) {
     int j = 0;
     while (j < n && !g_slot_used[i + j]) j++;
@@ -243,26 +242,46 @@ int take_slots(int n) {
   }
   return -1;
 }
+int take_slots(int n) {
+  std::lock_guard<std::mutex> lk(g_slot_mu);
+  return take_slots_locked(n);
+}
+void give_slots_locked(int first, int n) {
+  for (int i = first; i >= 0 && i < first + n && i < kConstSlots; i++) g_slot_used[i] = false;
+}
 void give_slots(int first, int n) {
   std::lock_guard<std::mutex> lk(g_slot_mu);
-  for (int i = first; i >= 0 && i < first + n && i < kConstSlots; i++) g_slot_used[i] = false;
+  give_slots_locked(first, n);
 }
 
 // The context holds at least K contiguous slots. A context only grows its
-// range between prove calls, after its stream has drained.
+// range between prove calls, after its stream has drained. When no K free
+// slots are contiguous, the context keeps a range of its previous size
+// (which always fits again: the exchange holds the lock throughout) and the
+// call reports Z0P_ERR_OUT_OF_MEMORY; callers then prove smaller groups.
 int ensure_slots(z0p_gpu_ctx* c, uint32_t K) {
   if ((int)K <= c->nslots) return Z0P_OK;
   CK(cudaStreamSynchronize(c->stream));
-  give_slots(c->slot, c->nslots);
-  c->slot = take_slots((int)K);
-  c->nslots = c->slot < 0 ? 0 : (int)K;
-  if (c->slot < 0) {
-    c->slot = take_slots(1);  // keep single proofs working
-    c->nslots = c->slot < 0 ? 0 : 1;
+  bool grown;
+  {
+    std::lock_guard<std::mutex> lk(g_slot_mu);
+    const int old = c->nslots;
+    give_slots_locked(c->slot, old);
+    int first = take_slots_locked((int)K);
+    grown = first >= 0;
+    if (grown) {
+      c->nslots = (int)K;
+    } else {
+      first = take_slots_locked(old > 0 ? old : 1);
+      c->nslots = first < 0 ? 0 : (old > 0 ? old : 1);
+    }
+    c->slot = first;
+  }
+  if (c->nslots > 0) CK(launch::const_slot_address(c->slot, &c->slot_dev));
+  if (!grown) {
     set_reason("no free constant slots for a group of this size");
     return Z0P_ERR_OUT_OF_MEMORY;
   }
-  CK(launch::const_slot_address(c->slot, &c->slot_dev));
   return Z0P_OK;
 }
 
@@ -1067,9 +1086,17 @@ int prove_group_abi(z0p_gpu_ctx* c, size_t n, const Params* params,
   const uint64_t t0 = now_ns();
   std::vector<z0p_transcript_state> work(n);
   for (size_t i = 0; i < n; i++) work[i] = *transcripts[i];
+  // Group size: up to kMaxGroup proofs, but no more than the context's
+  // constant slots. When the process-wide slots are short (many contexts),
+  // the group is proved in smaller consecutive groups instead of failing.
+  size_t G = n < (size_t)kMaxGroup ? n : (size_t)kMaxGroup;
+  if (ensure_slots(c, (uint32_t)G) != Z0P_OK) {
+    if (c->nslots < 1) return Z0P_ERR_OUT_OF_MEMORY;  // reason already set
+    G = (size_t)c->nslots;
+  }
   int rc = Z0P_OK;
-  for (size_t at = 0; at < n && rc == Z0P_OK; at += kMaxGroup) {
-    const uint32_t K = (uint32_t)(n - at < (size_t)kMaxGroup ? n - at : (size_t)kMaxGroup);
+  for (size_t at = 0; at < n && rc == Z0P_OK; at += G) {
+    const uint32_t K = (uint32_t)(n - at < G ? n - at : G);
     std::vector<Transcript> tr;
     tr.reserve(K);
     std::vector<Task<Params>> tasks(K);
@@ -1304,6 +1331,13 @@ int z0p_gpu_ctx_trim(z0p_gpu_ctx* c) {
                     &c->misc})
     release(c, *b);
   return Z0P_OK;
+}
+
+int z0p_gpu_ctx_reserve_group(z0p_gpu_ctx* c, uint32_t max_group) {
+  if (!c || max_group < 1 || max_group > (uint32_t)kMaxGroup) return Z0P_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lk(c->mu);
+  RC(with_device(c));
+  return ensure_slots(c, max_group);
 }
 
 void* z0p_gpu_ctx_stream(z0p_gpu_ctx* c) { return c ? (void*)c->stream : nullptr; }
