@@ -38,10 +38,14 @@ __device__ __forceinline__ uint32_t fsub(uint32_t a, uint32_t b) {
   return min(d, d + kP);
 }
 __device__ __forceinline__ uint32_t fneg(uint32_t a) { return a ? kP - a : 0u; }
+// a - b + p for a, b < p: in (0, 2p), not reduced. Valid only as an operand
+// of mmul beside an operand below p (the product stays below p * 2^32).
+__device__ __forceinline__ uint32_t fsub_lazy(uint32_t a, uint32_t b) { return a + kP - b; }
 __device__ __forceinline__ uint32_t fhalve(uint32_t a) { return (a + ((a & 1u) ? kP : 0u)) >> 1; }
 
-// Montgomery product a*b*2^-32 mod p for a, b < p (Montgomery 1985, with the
-// signed "hi - hi(m p)" reduction so no 64-bit addition is needed).
+// Montgomery product a*b*2^-32 mod p for a*b < p * 2^32, e.g. a, b < p or
+// a < 2p and b < p (Montgomery 1985, with the signed "hi - hi(m p)"
+// reduction so no 64-bit addition is needed).
 __device__ __forceinline__ uint32_t mmul(uint32_t a, uint32_t b) {
   uint32_t lo = a * b;
   uint32_t hi = __umulhi(a, b);
@@ -165,13 +169,27 @@ __device__ __forceinline__ E4 e4_sub(const E4& a, const E4& b) {
   for (int i = 0; i < 4; i++) r.c[i] = fsub(a.c[i], b.c[i]);
   return r;
 }
+// Unreduced sums and differences (components below 2p), for operands of
+// e4_mul_base only (see fsub_lazy).
+__device__ __forceinline__ E4 e4_add_lazy(const E4& a, const E4& b) {
+  E4 r;
+#pragma unroll
+  for (int i = 0; i < 4; i++) r.c[i] = a.c[i] + b.c[i];
+  return r;
+}
+__device__ __forceinline__ E4 e4_sub_lazy(const E4& a, const E4& b) {
+  E4 r;
+#pragma unroll
+  for (int i = 0; i < 4; i++) r.c[i] = fsub_lazy(a.c[i], b.c[i]);
+  return r;
+}
 __device__ __forceinline__ E4 e4_quarter(const E4& a) {
   E4 r;
 #pragma unroll
   for (int i = 0; i < 4; i++) r.c[i] = fhalve(fhalve(a.c[i]));
   return r;
 }
-// canonical Fp4 times a Montgomery-form base scalar -> canonical.
+// Fp4 (components below 2p) times a Montgomery-form base scalar -> canonical.
 __device__ __forceinline__ E4 e4_mul_base(const E4& a, uint32_t sM) {
   E4 r;
 #pragma unroll

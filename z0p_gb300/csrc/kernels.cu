@@ -759,14 +759,15 @@ __global__ void __launch_bounds__(kThreads) air_compose_leaves_kernel(AirCompose
     const uint32_t t0 = __ldg(a.tinv + base + q);
     const uint32_t tn = __ldg(a.tinv + base + qn);
     const uint32_t cbj = __ldg(a.cb + j);
-    const uint32_t zt = mmul(fsub(xs[s], a.w_last_m), __ldg(a.zinv + j));  // (x - w_last)/Z
+    // Differences that only feed a Montgomery product stay unreduced.
+    const uint32_t zt = mmul(fsub_lazy(xs[s], a.w_last_m), __ldg(a.zinv + j));  // (x - w_last)/Z
     const uint32_t bv = fadd(avn, mmul(cbj, t0));
     const uint32_t bvn = fadd(avnn, mmul(cbj, tn));
-    const uint32_t t2 = mmul(fsub(bvn, fadd(av, bv)), zt);
+    const uint32_t t2 = mmul(fsub_lazy(bvn, fadd(av, bv)), zt);
     const ProofConsts& pc = g_consts[a.slot];
-    const uint32_t ba = mmul(fsub(av, pc.a0), tm);
-    const uint32_t bb = mmul(fsub(bv, pc.b0), tm);
-    const uint32_t bo = mmul(fsub(bv, pc.b_last), t0);
+    const uint32_t ba = mmul(fsub_lazy(av, pc.a0), tm);
+    const uint32_t bb = mmul(fsub_lazy(bv, pc.b0), tm);
+    const uint32_t bo = mmul(fsub_lazy(bv, pc.b_last), t0);
     const int t = (s == 1) ? 2 : (s == 2) ? 1 : s;  // position 4P + brev2(s)
 #pragma unroll
     for (int c = 0; c < 4; c++) {
@@ -868,14 +869,16 @@ __device__ __forceinline__ E4 fold_quad(const E4& q0, const E4& q1, const E4& q2
                                         uint32_t xinv_m, const FoldArgs& a) {
   E4 s01 = e4_add(q0, q1), s23 = e4_add(q2, q3);
   E4 odd_diff = e4_sub(q0, q1);
-  E4 skew_u = e4_mul_base(e4_sub(q2, q3), a.unit_m);
+  E4 skew_u = e4_mul_base(e4_sub_lazy(q2, q3), a.unit_m);
   E4 mean = e4_quarter(e4_add(s01, s23));
   E4 odd4 = e4_sub(odd_diff, skew_u);
   E4 even4 = e4_sub(s01, s23);
   E4 skew4 = e4_add(odd_diff, skew_u);
   const ProofConsts& pc = g_consts[a.slot];
-  E4 acc = e4_add(e4_mul_base(e4_mul_tab(skew4, pc.tab[2]), xinv_m), e4_mul_tab(even4, pc.tab[1]));
-  acc = e4_add(e4_mul_base(acc, xinv_m), e4_mul_tab(odd4, pc.tab[0]));
+  // The Horner sums only feed the next product by x^-1: left unreduced.
+  E4 acc = e4_add_lazy(e4_mul_base(e4_mul_tab(skew4, pc.tab[2]), xinv_m),
+                       e4_mul_tab(even4, pc.tab[1]));
+  acc = e4_add_lazy(e4_mul_base(acc, xinv_m), e4_mul_tab(odd4, pc.tab[0]));
   return e4_add(mean, e4_mul_base(acc, xinv_m));
 }
 
