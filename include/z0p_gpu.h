@@ -215,6 +215,48 @@ int z0p_gpu_range_prove_group(z0p_gpu_ctx *ctx, size_t n, const z0p_range_params
                               z0p_transcript_state *const *transcripts, uint8_t *const *outs,
                               const size_t *caps, size_t *lens);
 
+/* --------------------------------------- FRI as a polynomial commitment ---- */
+/* fri::Params (src/fri.rs:103-126): fields and validation as the reference. */
+typedef struct {
+    uint64_t blowup;
+    uint64_t num_queries;
+    uint64_t final_size;
+    uint32_t grinding_bits;
+    uint64_t cap_height;
+} z0p_fri_params;
+/* Input forms of the commit call:
+ *   Z0P_FRI_COEFFS      fri::commit            (src/fri.rs:407-433), n coefficients
+ *   Z0P_FRI_COEFFS_EXT  fri::commit_ext        (src/fri.rs:443-460), n Ext4 coefficients
+ *   Z0P_FRI_EVALS       fri::commit_evals      (src/fri.rs:473-499), n LDE values
+ *   Z0P_FRI_EVALS_EXT   fri::commit_ext_evals  (src/fri.rs:508-549), n Ext4 LDE values
+ * Ext4 values are 4 words each (coordinates a, b, c, d of a + bu + cv + duv);
+ * the evaluation forms take natural-order values on the 31-coset and a
+ * degree_bound (ignored by the coefficient forms, whose bound is n - 1). */
+enum { Z0P_FRI_COEFFS = 0, Z0P_FRI_COEFFS_EXT = 1, Z0P_FRI_EVALS = 2, Z0P_FRI_EVALS_EXT = 3 };
+/* fri::Params::for_security (src/fri.rs:232-255): blowup 16, queries and
+ * grinding from the target, size-optimal final layer and cap height. */
+int z0p_fri_params_for_security(uint64_t poly_len, uint32_t target_bits, z0p_fri_params *out);
+/* Byte lengths of Commitment::to_bytes and Proof::to_bytes for these inputs
+ * (src/fri.rs:331-336, 875-880), after the same checks as the commit call. */
+int z0p_fri_sizes(const z0p_fri_params *params, int form, size_t n, uint64_t degree_bound,
+                  size_t *commitment_len, size_t *proof_len);
+/* Commits to host `values` and writes Commitment::to_bytes to `out` (cap
+ * bytes; *len receives the length, also when cap is too small). The
+ * transcript advances as the reference's commit call leaves it. Checks run
+ * in the reference's order before any device work; a word >= p gives
+ * Z0P_ERR_MALFORMED_INPUT. The committed layers and trees (ProverState,
+ * src/fri.rs:276-295) stay on the device for z0p_gpu_fri_open until any
+ * other call on this context uses its workspace. */
+int z0p_gpu_fri_commit(z0p_gpu_ctx *ctx, const z0p_fri_params *params, int form,
+                       const uint32_t *values, size_t n, uint64_t degree_bound,
+                       z0p_transcript_state *transcript, uint8_t *out, size_t cap, size_t *len);
+/* fri::open (src/fri.rs:645-666) of the context's last commitment: grinds,
+ * draws the query indices (num_queries entries into `indices`, may be null)
+ * and writes Proof::to_bytes. Z0P_ERR_INVALID_ARGUMENT when there is no
+ * commitment to open. On error the transcript is left untouched. */
+int z0p_gpu_fri_open(z0p_gpu_ctx *ctx, z0p_transcript_state *transcript, uint8_t *out, size_t cap,
+                     size_t *len, uint64_t *indices);
+
 /* ------------------------------------------------- batching / serving ---- */
 /*
  * Many independent proofs (the batched and served configurations). A pool

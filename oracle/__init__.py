@@ -46,6 +46,30 @@ class AirParams(C.Structure):
     ]
 
 
+class FriParams(C.Structure):
+    """fri::Params (src/fri.rs:103-126)."""
+    _fields_ = [
+        ("blowup", C.c_uint64), ("num_queries", C.c_uint64), ("final_size", C.c_uint64),
+        ("grinding_bits", C.c_uint32), ("cap_height", C.c_uint64),
+    ]
+
+
+FRI_COEFFS, FRI_COEFFS_EXT, FRI_EVALS, FRI_EVALS_EXT = 0, 1, 2, 3
+
+
+def fri_for_security(poly_len: int, target_bits: int) -> FriParams:
+    """fri::Params::for_security (src/fri.rs:232-255), from the oracle's tuners."""
+    if poly_len == 0:
+        raise ValueError("EmptyInput")
+    if poly_len & (poly_len - 1) or poly_len * 16 > 1 << 27:
+        raise ValueError("InvalidDomainSize")
+    q, g = C.c_size_t(), C.c_uint32()
+    lib().zo_fri_tune_strength(target_bits, 2000, C.byref(q), C.byref(g))
+    fs, ch = C.c_size_t(), C.c_size_t()
+    lib().zo_fri_tune_shape(poly_len * 16, q.value, 0, 0, 0, C.byref(fs), C.byref(ch))
+    return FriParams(16, q.value, fs.value, g.value, ch.value)
+
+
 class RangeParams(C.Structure):
     _fields_ = [
         ("n_rows", C.c_uint64), ("n_bits", C.c_uint64), ("blowup", C.c_uint64),
@@ -108,6 +132,11 @@ def lib():
             "zo_range_for_security": (C.c_int, [C.c_uint64, C.c_uint64, C.c_uint32, C.c_uint32, C.POINTER(RangeParams)]),
             "zo_range_prove": (C.c_int, [C.POINTER(RangeParams), vp, C.POINTER(u8p), C.POINTER(sz)]),
             "zo_range_verify": (C.c_int, [C.POINTER(RangeParams), C.c_char_p, sz, vp]),
+            "zo_fri_commit": (C.c_int, [C.POINTER(FriParams), C.c_int, u32p, sz, C.c_uint64, vp,
+                                        C.POINTER(vp), C.POINTER(u8p), C.POINTER(sz)]),
+            "zo_fri_open": (C.c_int, [vp, vp, C.POINTER(u8p), C.POINTER(sz), u64p]),
+            "zo_fri_state_free": (None, [vp]),
+            "zo_fri_verify": (C.c_int, [C.POINTER(FriParams), C.c_char_p, sz, C.c_char_p, sz, vp, u64p]),
             "zo_free": (None, [vp]),
             "zo_set_max_workers": (None, [sz]),
             "zo_max_workers": (sz, []),
@@ -317,6 +346,46 @@ def range_prove(params: RangeParams, t: Transcript) -> bytes:
 
 def range_verify(params: RangeParams, proof: bytes, t: Transcript) -> int:
     return lib().zo_range_verify(C.byref(params), proof, len(proof), t.h)
+
+
+class FriState:
+    """fri::ProverState (src/fri.rs:276-295): the committed layers and trees."""
+
+    def __init__(self, handle, commitment: bytes, num_queries: int):
+        self.h = handle
+        self.commitment = commitment
+        self.num_queries = num_queries
+
+    def __del__(self):
+        if self.h:
+            lib().zo_fri_state_free(self.h)
+            self.h = None
+
+
+def fri_commit(params: FriParams, form: int, values, t: Transcript, degree_bound: int = 0) -> FriState:
+    """fri::commit / commit_ext / commit_evals / commit_ext_evals (src/fri.rs:400-549).
+    Ext4 values are 4 coordinates each; `values` is the flat coordinate list."""
+    a, ap = u32arr(values)
+    n = len(a) // 4 if form in (FRI_COEFFS_EXT, FRI_EVALS_EXT) else len(a)
+    st, buf, ln = C.c_void_p(), C.POINTER(C.c_uint8)(), C.c_size_t()
+    rc = lib().zo_fri_commit(C.byref(params), form, ap, n, degree_bound, t.h, C.byref(st),
+                             C.byref(buf), C.byref(ln))
+    return FriState(st, _take_proof(rc, buf, ln), params.num_queries)
+
+
+def fri_open(state: FriState, t: Transcript):
+    """fri::open (src/fri.rs:645-666): (proof bytes, query indices)."""
+    idx = (C.c_uint64 * state.num_queries)()
+    buf, ln = C.POINTER(C.c_uint8)(), C.c_size_t()
+    rc = lib().zo_fri_open(state.h, t.h, C.byref(buf), C.byref(ln), idx)
+    return _take_proof(rc, buf, ln), list(idx)
+
+
+def fri_verify(params: FriParams, commitment: bytes, proof: bytes, t: Transcript):
+    """fri::verify (src/fri.rs:694-858): (status, query indices)."""
+    idx = (C.c_uint64 * max(1, params.num_queries))()
+    rc = lib().zo_fri_verify(C.byref(params), commitment, len(commitment), proof, len(proof), t.h, idx)
+    return rc, list(idx)[: params.num_queries]
 
 
 # ------------------------------------------------------------ kernel pieces

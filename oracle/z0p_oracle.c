@@ -1456,7 +1456,8 @@ static void fri_decoded_free(fri_decoded *d) {
 }
 
 /* fri.rs:908-925 Commitment::read_body + fri.rs:370-397 Proof::read_body */
-static void fri_read(reader *r, fri_decoded *d) {
+/* fri.rs:906-925 Commitment::read_body */
+static void fri_read_commitment(reader *r, fri_decoded *d) {
     memset(d, 0, sizeof *d);
     d->lde_len = r_u64(r); d->poly_len = r_u64(r); d->degree_bound = r_u64(r);
     size_t nc = r_count(r, MAX_FOLDS);
@@ -1464,6 +1465,10 @@ static void fri_read(reader *r, fri_decoded *d) {
     d->caps = calloc(nc ? nc : 1, sizeof(digest *));
     d->cap_n = calloc(nc ? nc : 1, sizeof(size_t));
     for (size_t i = 0; i < nc && !r->err; i++) { d->caps[i] = r_cap(r, &d->cap_n[i]); d->n_caps = i + 1; }
+}
+
+/* fri.rs:370-397 Proof::read_body, into the same decoded record */
+static void fri_read_proof(reader *r, fri_decoded *d) {
     size_t fn = r_count(r, MAX_ELEMS);
     if (r->err) return;
     if (fn * 16 > r->n - r->pos) { r->err = 1; return; }
@@ -1486,6 +1491,11 @@ static void fri_read(reader *r, fri_decoded *d) {
             r_path(r, &d->q[i].f[k].path);
         }
     }
+}
+
+static void fri_read(reader *r, fri_decoded *d) {
+    fri_read_commitment(r, d);
+    if (!r->err) fri_read_proof(r, d);
 }
 
 /* fri.rs:1153-1227 */
@@ -1606,6 +1616,101 @@ static int fri_verify(const fri_decoded *d, const fri_params *params, zo_transcr
         rc = verify_one(d, (const ext4 (*)[3])fold_ch, &d->q[i], indices[i], unit, params->cap_height);
     }
     free(fold_ch);
+    return rc;
+}
+
+/* ------------------------------------------------------------------------ */
+/* fri.rs public commit / open / verify (the PCS entry points)               */
+/* ------------------------------------------------------------------------ */
+
+static fri_params fri_from_public(const zo_fri_params *p) {
+    fri_params f;
+    f.blowup = p->blowup; f.num_queries = p->num_queries; f.final_size = p->final_size;
+    f.grinding_bits = p->grinding_bits; f.cap_height = p->cap_height;
+    return f;
+}
+
+/* fri.rs:407-433 commit, :443-460 commit_ext, :473-499 commit_evals,
+ * :508-549 commit_ext_evals(_owned): entry checks, encoding, then
+ * commit_inner (fri_commit_inner). Ext4 input is 4 coordinates per value. */
+int zo_fri_commit(const zo_fri_params *params, int form, const uint32_t *values, size_t n,
+                  uint64_t degree_bound, zo_transcript *t, void **state, uint8_t **commitment,
+                  size_t *commitment_len) {
+    fri_params fp = fri_from_public(params);
+    int rc = fri_params_validate(&fp);
+    if (rc) return rc;
+    if (form < ZO_FRI_COEFFS || form > ZO_FRI_EVALS_EXT) return ZO_MALFORMED_INPUT;
+    const int ext = form == ZO_FRI_COEFFS_EXT || form == ZO_FRI_EVALS_EXT;
+    const int evals = form >= ZO_FRI_EVALS;
+    if (n == 0) return ZO_EMPTY_INPUT;
+    if (!is_pow2(n)) return ZO_INVALID_DOMAIN_SIZE;
+    size_t lde_len, poly_len, bound;
+    ext4 *current;
+    if (!evals) {
+        /* ntt.rs:341-363 (per coordinate for ext, ntt.rs:394-403) */
+        if (n > SIZE_MAX / fp.blowup || n * fp.blowup > ((size_t)1 << TWO_ADICITY))
+            return ZO_INVALID_DOMAIN_SIZE;
+        lde_len = n * fp.blowup; poly_len = n; bound = n - 1;
+        current = calloc(lde_len, sizeof(ext4));
+        uint32_t *coord = malloc(n * 4), *lde = malloc(lde_len * 4);
+        for (int c = 0; c < (ext ? 4 : 1); c++) {
+            for (size_t i = 0; i < n; i++) coord[i] = values[ext ? 4 * i + c : i];
+            zo_evaluate_on_coset(coord, n, fp.blowup, LDE_SHIFT, lde);
+            for (size_t k = 0; k < lde_len; k++) current[k].c[c] = lde[k];
+        }
+        free(coord); free(lde);
+    } else {
+        if (n > ((size_t)1 << TWO_ADICITY)) return ZO_INVALID_DOMAIN_SIZE;
+        if (degree_bound >= n) return ZO_MALFORMED_INPUT;
+        lde_len = n; poly_len = n; bound = degree_bound;
+        current = calloc(lde_len, sizeof(ext4));
+        for (size_t k = 0; k < n; k++)
+            for (int c = 0; c < (ext ? 4 : 1); c++) current[k].c[c] = values[ext ? 4 * k + c : k];
+    }
+    fri_state *st = calloc(1, sizeof(fri_state));
+    rc = fri_commit_inner(current, lde_len, bound, poly_len, &fp, t, st);
+    if (rc) { free(st); return rc; }
+    writer w = {0};
+    w_byte(&w, VERSION);
+    fri_write_commitment(&w, st);
+    *state = st;
+    *commitment = w.b; *commitment_len = w.n;
+    return ZO_OK;
+}
+
+/* fri.rs:645-666 open, bytes per fri.rs:331-336 Proof::to_bytes */
+int zo_fri_open(void *state, zo_transcript *t, uint8_t **proof, size_t *proof_len,
+                uint64_t *indices) {
+    fri_state *st = state;
+    writer w = {0};
+    w_byte(&w, VERSION);
+    int rc = fri_open_write(st, t, &w, indices);
+    if (rc) { free(w.b); return rc; }
+    *proof = w.b; *proof_len = w.n;
+    return ZO_OK;
+}
+
+void zo_fri_state_free(void *state) {
+    if (!state) return;
+    fri_state_free(state);
+    free(state);
+}
+
+/* fri.rs:694-858 verify over Commitment::from_bytes / Proof::from_bytes */
+int zo_fri_verify(const zo_fri_params *params, const uint8_t *commitment, size_t commitment_len,
+                  const uint8_t *proof, size_t proof_len, zo_transcript *t, uint64_t *indices) {
+    fri_params fp = fri_from_public(params);
+    reader rc_ = {commitment, commitment_len, 0, 0}, rp = {proof, proof_len, 0, 0};
+    fri_decoded d;
+    memset(&d, 0, sizeof d);
+    int bad = r_byte(&rc_) != VERSION;
+    if (!bad) fri_read_commitment(&rc_, &d);
+    bad = bad || rc_.err || rc_.pos != rc_.n;
+    if (!bad) bad = r_byte(&rp) != VERSION;
+    if (!bad) fri_read_proof(&rp, &d);
+    bad = bad || rp.err || rp.pos != rp.n;
+    int rc = bad ? ZO_MALFORMED_INPUT : fri_verify(&d, &fp, t, indices);
+    fri_decoded_free(&d);
     return rc;
 }
 

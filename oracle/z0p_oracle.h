@@ -152,6 +152,24 @@ int zo_reed_solomon_extend(const uint32_t *values, size_t n, size_t blowup, uint
 void zo_fold_layer(const uint32_t *values, size_t n, const uint32_t *first_points,
                    const uint32_t ch[12], uint32_t *out_values, uint32_t *out_points);
 
+/* FRI as a polynomial commitment (src/fri.rs:400-858): commit to
+ * coefficients or LDE evaluations (base field, or Ext4 as 4 coordinates per
+ * value), open, verify. The state handle holds the layers and trees. */
+typedef struct {
+    uint64_t blowup, num_queries, final_size;
+    uint32_t grinding_bits;
+    uint64_t cap_height;
+} zo_fri_params;
+enum { ZO_FRI_COEFFS = 0, ZO_FRI_COEFFS_EXT = 1, ZO_FRI_EVALS = 2, ZO_FRI_EVALS_EXT = 3 };
+int zo_fri_commit(const zo_fri_params *params, int form, const uint32_t *values, size_t n,
+                  uint64_t degree_bound, zo_transcript *t, void **state, uint8_t **commitment,
+                  size_t *commitment_len);
+int zo_fri_open(void *state, zo_transcript *t, uint8_t **proof, size_t *proof_len,
+                uint64_t *indices);
+void zo_fri_state_free(void *state);
+int zo_fri_verify(const zo_fri_params *params, const uint8_t *commitment, size_t commitment_len,
+                  const uint8_t *proof, size_t proof_len, zo_transcript *t, uint64_t *indices);
+
 void zo_free(void *p);
 /* Worker-thread cap for the parallel paths (0 = all online cores). */
 void zo_set_max_workers(size_t workers);

@@ -35,6 +35,13 @@ class AirParams(C.Structure):
     ]
 
 
+class FriParams(C.Structure):
+    _fields_ = [
+        ("blowup", C.c_uint64), ("num_queries", C.c_uint64), ("final_size", C.c_uint64),
+        ("grinding_bits", C.c_uint32), ("cap_height", C.c_uint64),
+    ]
+
+
 class RangeParams(C.Structure):
     _fields_ = [
         ("n_rows", C.c_uint64), ("n_bits", C.c_uint64), ("blowup", C.c_uint64),
@@ -107,6 +114,12 @@ def lib():
             "z0p_gpu_ctx_profile": (C.c_int, [vp, C.c_char_p, sz, P(sz)]),
             "z0p_gpu_air_prove": (C.c_int, [vp, P(AirParams), P(TranscriptState), u8p, sz, P(sz)]),
             "z0p_gpu_range_prove": (C.c_int, [vp, P(RangeParams), P(TranscriptState), u8p, sz, P(sz)]),
+            "z0p_fri_params_for_security": (C.c_int, [C.c_uint64, C.c_uint32, P(FriParams)]),
+            "z0p_fri_sizes": (C.c_int, [P(FriParams), C.c_int, sz, C.c_uint64, P(sz), P(sz)]),
+            "z0p_gpu_fri_commit": (C.c_int, [vp, P(FriParams), C.c_int, P(C.c_uint32), sz, C.c_uint64,
+                                             P(TranscriptState), P(C.c_uint8), sz, P(sz)]),
+            "z0p_gpu_fri_open": (C.c_int, [vp, P(TranscriptState), P(C.c_uint8), sz, P(sz),
+                                           P(C.c_uint64)]),
             "z0p_gpu_air_prove_group": (C.c_int, [vp, sz, P(AirParams), P(P(TranscriptState)),
                                                   P(u8p), P(sz), P(sz)]),
             "z0p_gpu_range_prove_group": (C.c_int, [vp, sz, P(RangeParams), P(P(TranscriptState)),

@@ -346,7 +346,8 @@ void tune_shape(uint64_t lde_len, uint64_t q, uint64_t col_lde, uint64_t col_vb,
   for (;;) {
     auto layers = layer_sizes(lde_len, shifted);
     for (uint64_t h = 0; h <= 4; h++) {
-      uint64_t total = sat_add(est_fri(layers, q, h), est_col(col_lde, q, col_vb, h));
+      uint64_t total = est_fri(layers, q, h);
+      if (col_lde) total = sat_add(total, est_col(col_lde, q, col_vb, h));  // 0: no column
       if (total < best) { best = total; best_f = shifted; best_h = h; }
     }
     if (shifted <= 1) break;

@@ -86,6 +86,7 @@ struct FriParams {
 };
 int fri_params_new(uint64_t blowup, uint64_t q, uint64_t final_size, FriParams* out);
 int fri_params_validate(const FriParams& p);
+// col_lde = 0: no opened column beside the FRI layers (fri::Params::for_security).
 void tune_shape(uint64_t lde_len, uint64_t q, uint64_t col_lde, uint64_t col_vb,
                 uint64_t* final_size, uint64_t* cap_height);
 void tune_strength(uint32_t target, uint32_t millibits, uint64_t* q, uint32_t* g);

@@ -861,6 +861,72 @@ __global__ void __launch_bounds__(kThreads) range_compose_leaves_kernel(RangeCom
   store_digest(a.leaves + 8 * (size_t)P, d);
 }
 
+// ------------------------------------------------- FRI commitment input ----
+// fri::commit on coefficients (src/fri.rs:407-433, 443-460): evaluate_on_coset
+// scales c_i by 31^i before the forward transform (src/ntt.rs:353-358). One
+// launch per coordinate (grid y); Ext4 input is interleaved, 4 words per
+// value. Values >= p raise *bad (the C boundary takes canonical elements).
+__global__ void gamma_scale_kernel(const uint32_t* __restrict__ in, uint32_t* __restrict__ out,
+                                   uint32_t n, uint32_t ext, unsigned int* bad, Tables tb) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x, c = blockIdx.y;
+  if (i >= n) return;
+  const uint32_t v = in[ext ? 4 * (size_t)i + c : i];
+  if (v >= kP) atomicOr(bad, 1u);
+  out[(size_t)c * n + i] = mmul(v < kP ? v : 0u, gamma_pow(tb, i));
+}
+
+// FRI layer 0 of a commitment (src/fri.rs:584-586): the LDE bit-reversed as
+// Ext4 values, written as 64-byte quad leaves and hashed, as in the AIR
+// composition kernel (quad P holds rows k0 + s m/4, k0 = brev(P)). The LDE is
+// either coset-major per coordinate (fri::commit: `coset_major`, ncomp 1 or
+// 4 coordinate planes of m words) or the caller's natural-order evaluations
+// (fri::commit_evals: 1 or 4 words per value, checked canonical into *bad).
+struct Layer0Args {
+  const uint32_t* src;
+  uint32_t* layer0;
+  uint32_t* leaves;
+  unsigned int* bad;
+  uint32_t logm, logB, ncomp, coset_major;
+};
+__global__ void __launch_bounds__(kThreads) layer0_leaves_kernel(Layer0Args a) {
+  const uint32_t quarter = 1u << (a.logm - 2);
+  const uint32_t u = blockIdx.x * blockDim.x + threadIdx.x;
+  if (u >= quarter) return;
+  const uint32_t logN = a.logm - a.logB;
+  uint32_t k0 = u;
+  if (a.coset_major && logN >= 2) {  // consecutive threads read consecutive q
+    const uint32_t j = u >> (logN - 2), q0 = u & ((1u << (logN - 2)) - 1u);
+    k0 = (q0 << a.logB) | j;
+  }
+  const uint32_t P = brev_bits(k0, a.logm - 2);
+  const size_t m = (size_t)1 << a.logm;
+  uint32_t leaf[16];
+  unsigned int over = 0;
+#pragma unroll
+  for (int s = 0; s < 4; s++) {
+    const uint32_t k = k0 + (uint32_t)s * quarter;
+    const int t = (s == 1) ? 2 : (s == 2) ? 1 : s;  // position 4P + brev2(s)
+    size_t idx = k;
+    if (a.coset_major) idx = ((size_t)(k & ((1u << a.logB) - 1u)) << logN) + (k >> a.logB);
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+      uint32_t v = 0u;
+      if ((uint32_t)c < a.ncomp)
+        v = a.coset_major ? a.src[(size_t)c * m + idx] : a.src[idx * a.ncomp + c];
+      over |= v >= kP;
+      leaf[4 * t + c] = v;
+    }
+  }
+  if (over) atomicOr(a.bad, 1u);
+  uint4* dst = reinterpret_cast<uint4*>(a.layer0 + 16 * (size_t)P);
+#pragma unroll
+  for (int t = 0; t < 4; t++)
+    dst[t] = make_uint4(leaf[4 * t], leaf[4 * t + 1], leaf[4 * t + 2], leaf[4 * t + 3]);
+  uint32_t d[8];
+  blake3_leaf64(leaf, d);
+  store_digest(a.leaves + 8 * (size_t)P, d);
+}
+
 // ----------------------------------------------------------------- FRI ----
 // fold_values (src/fri.rs:1311-1331): A + x^-1 (r0 B + x^-1 (r1 C + x^-1 r2 D))
 // with B, C, D the quarter-scaled differences; the 1/4 is folded into the
@@ -1123,6 +1189,7 @@ __global__ void __launch_bounds__(128) openings_kernel(OpenArgs a) {
       }
     }
   }
+  if (a.no_trace) return;
   // Trace openings.
   const uint32_t logm = a.logN + a.logB;
   const uint32_t N = 1u << a.logN, B = 1u << a.logB;
@@ -1517,6 +1584,26 @@ cudaError_t grind(cudaStream_t st, uint32_t slot, uint32_t head_len, uint32_t bi
   Stage stg("grind", st);
   stg.launched();
   grind_kernel<<<dim3(ctas, nproofs), kGrindThreads, 0, st>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t gamma_scale(cudaStream_t st, const Tables& tb, const uint32_t* in, uint32_t* out,
+                        uint32_t n, uint32_t ext, unsigned int* bad) {
+  Stage stg("fri_input", st);
+  stg.launched();
+  gamma_scale_kernel<<<dim3(grid_for(n), ext ? 4 : 1), kThreads, 0, st>>>(in, out, n, ext, bad, tb);
+  return cudaGetLastError();
+}
+
+cudaError_t layer0_leaves(cudaStream_t st, const uint32_t* src, uint32_t* layer0, uint32_t* leaves,
+                          unsigned int* bad, uint32_t logm, uint32_t logB, uint32_t ncomp,
+                          bool coset_major) {
+  if (logm < 2) return cudaErrorInvalidValue;
+  Layer0Args a{src, layer0, leaves, bad, logm, coset_major ? logB : 0u, ncomp,
+               coset_major ? 1u : 0u};
+  Stage stg("layer0_leaves", st);
+  stg.launched();
+  layer0_leaves_kernel<<<grid_for(1ull << (logm - 2)), kThreads, 0, st>>>(a);
   return cudaGetLastError();
 }
 

@@ -126,6 +126,7 @@ struct OpenArgs {
   uint64_t tleaves;
   uint32_t tsteps, logN, logB;
   uint32_t ncol;            // 0 for the AIR, else the range AIR's column count
+  uint32_t no_trace = 0;    // 1: FRI openings only (a FRI commitment on its own)
   // Per-proof strides (words) for a proof group: FRI layer values and trees,
   // trace LDE and trace tree (cb and tinv follow from B and m).
   uint64_t fri_val_stride = 0, fri_tree_stride = 0, lde_stride = 0, ttree_stride = 0;
@@ -216,6 +217,18 @@ cudaError_t range_compose_leaves(cudaStream_t st, const Tables& tb, const RangeC
 // set; *levels receives the levels done above the leaves.
 cudaError_t fri_fold(cudaStream_t st, const Tables& tb, const FoldArgs& a, uint32_t* levels,
                      uint32_t nproofs = 1);
+// fri::commit input: out[c][i] = in[c-th coordinate of value i] * 31^i (one
+// coordinate, or four for Ext4 input interleaved 4 words per value); *bad
+// receives 1 when an input word is not a canonical field element.
+cudaError_t gamma_scale(cudaStream_t st, const Tables& tb, const uint32_t* in, uint32_t* out,
+                        uint32_t n, uint32_t ext, unsigned int* bad);
+// FRI layer 0 of a commitment and its leaf digests, from coset-major
+// coordinate LDEs (coset_major; ncomp planes of m = 2^logm words, 2^logB
+// cosets) or from natural-order evaluations (ncomp words per value, checked
+// canonical into *bad).
+cudaError_t layer0_leaves(cudaStream_t st, const uint32_t* src, uint32_t* layer0, uint32_t* leaves,
+                          unsigned int* bad, uint32_t logm, uint32_t logB, uint32_t ncomp,
+                          bool coset_major);
 // Leaf digests of an FRI layer held in memory (64-byte quads or 16-byte values).
 cudaError_t layer_leaves(cudaStream_t st, const uint32_t* values, uint64_t len, uint32_t* leaves,
                          uint32_t nproofs = 1, uint64_t in_stride = 0, uint64_t out_stride = 0);

@@ -118,6 +118,10 @@ struct EventRecorder final : launch::StageRecorder {
   }
 };
 
+namespace z0p {
+struct FriPending;
+}
+
 struct z0p_gpu_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -146,6 +150,10 @@ struct z0p_gpu_ctx {
   std::map<std::string, HostSite> sites;
   uint64_t last_sync_ns = 0;  // 0 = no prove call in progress
   uint64_t tail_ns = 0;       // host time after a prove call's last synchronisation
+  // Every call that uses the workspace or the mapped buffer counts here; a
+  // FRI commitment stays openable only while no other such call came after it.
+  uint64_t work_serial = 0;
+  z0p::FriPending* fri = nullptr;
 };
 using HostSite = z0p_gpu_ctx::HostSite;
 
@@ -460,11 +468,12 @@ int plan_hio(z0p_gpu_ctx* c, const FriShape& s, uint64_t queries, uint32_t tdrop
   return ensure_hio(c, at);
 }
 
-// Fold tables, PoW heads and query indices of one group, proof by proof on
-// the host; the device work of each round serves the whole group.
-int run_fri(z0p_gpu_ctx* c, const FriShape& s, const FriParams& fp, const FriBufs& fb,
-            uint64_t poly_len, uint64_t degree_bound, Transcript* const* ts, uint32_t K,
-            const HioPlan& h, FriOut* outs) {
+// FRI commit of one group (src/fri.rs:551-633), layer 0 and its tree
+// already queued: fold tables proof by proof on the host, the device work
+// of each round for the whole group.
+int run_fri_commit(z0p_gpu_ctx* c, const FriShape& s, const FriParams& fp, const FriBufs& fb,
+                   uint64_t poly_len, uint64_t degree_bound, Transcript* const* ts, uint32_t K,
+                   const HioPlan& h, FriOut* outs) {
   uint8_t dims[24];  // src/fri.rs:1450-1456
   for (int i = 0; i < 8; i++) {
     dims[i] = (uint8_t)(s.m >> (8 * i));
@@ -548,6 +557,13 @@ int run_fri(z0p_gpu_ctx* c, const FriShape& s, const FriParams& fp, const FriBuf
     transcript_absorb(*ts[k], "fri-final", (const uint8_t*)outs[k].final_vals.data(), 16 * fl);
     outs[k].nonce = 0;
   }
+  return Z0P_OK;
+}
+
+// FRI open of one group up to the openings (src/fri.rs:645-666): the PoW
+// nonce, then the query indices.
+int run_fri_open(z0p_gpu_ctx* c, const FriShape& s, const FriParams& fp, Transcript* const* ts,
+                 uint32_t K, const HioPlan& h, FriOut* outs) {
   // Proof of work (src/fri.rs:645-650, src/transcript.rs:206-228).
   if (fp.grinding_bits > 0) {
     size_t head_len = 0;
@@ -580,6 +596,13 @@ int run_fri(z0p_gpu_ctx* c, const FriShape& s, const FriParams& fp, const FriBuf
       outs[k].indices[i] = challenge_index(*ts[k], "fri-query", s.m);
   }
   return Z0P_OK;
+}
+
+int run_fri(z0p_gpu_ctx* c, const FriShape& s, const FriParams& fp, const FriBufs& fb,
+            uint64_t poly_len, uint64_t degree_bound, Transcript* const* ts, uint32_t K,
+            const HioPlan& h, FriOut* outs) {
+  RC(run_fri_commit(c, s, fp, fb, poly_len, degree_bound, ts, K, h, outs));
+  return run_fri_open(c, s, fp, ts, K, h, outs);
 }
 
 // Gathers every opening of the group on the device (kernels.h, OpenArgs)
@@ -621,9 +644,10 @@ const uint32_t* open_block(z0p_gpu_ctx* c, const HioPlan& h, uint32_t k, size_t 
          (size_t)h.stride * ((size_t)k * h.queries + qi);
 }
 
-void write_fri(Writer& w, z0p_gpu_ctx* c, const FriShape& s, const FriOut& fo, uint64_t poly_len,
-               uint64_t degree_bound, const HioPlan& h, uint32_t k) {
-  w.u64(s.m);  // Commitment::write_body (src/fri.rs:896-904)
+// Commitment::write_body (src/fri.rs:896-904).
+void write_fri_commitment(Writer& w, const FriShape& s, const FriOut& fo, uint64_t poly_len,
+                          uint64_t degree_bound) {
+  w.u64(s.m);
   w.u64(poly_len);
   w.u64(degree_bound);
   w.u32((uint32_t)fo.caps.size());
@@ -631,7 +655,12 @@ void write_fri(Writer& w, z0p_gpu_ctx* c, const FriShape& s, const FriOut& fo, u
     w.u32((uint32_t)(cap.size() / 32));
     w.bytes(cap.data(), cap.size());
   }
-  w.u32((uint32_t)(fo.final_vals.size() / 4));  // Proof::write_body (src/fri.rs:352-368)
+}
+
+// Proof::write_body (src/fri.rs:352-368), openings from proof k's blocks.
+void write_fri_proof(Writer& w, z0p_gpu_ctx* c, const FriShape& s, const FriOut& fo,
+                     const HioPlan& h, uint32_t k) {
+  w.u32((uint32_t)(fo.final_vals.size() / 4));
   w.bytes(fo.final_vals.data(), 4 * fo.final_vals.size());
   w.u64(fo.nonce);
   w.u32((uint32_t)fo.indices.size());
@@ -647,6 +676,12 @@ void write_fri(Writer& w, z0p_gpu_ctx* c, const FriShape& s, const FriOut& fo, u
       index /= 4;
     }
   }
+}
+
+void write_fri(Writer& w, z0p_gpu_ctx* c, const FriShape& s, const FriOut& fo, uint64_t poly_len,
+               uint64_t degree_bound, const HioPlan& h, uint32_t k) {
+  write_fri_commitment(w, s, fo, poly_len, degree_bound);
+  write_fri_proof(w, c, s, fo, h, k);
 }
 
 int air_shape(const z0p_air_params& p, FriParams* fp, FriShape* s) {
@@ -1058,6 +1093,151 @@ int with_device(z0p_gpu_ctx* c) {
   return Z0P_OK;
 }
 
+
+// ====================================================== FRI as a PCS ====
+// fri::commit* and fri::open (src/fri.rs:400-666) on the device. Between the
+// two calls the committed layers and trees (ProverState, src/fri.rs:276-295)
+// stay in the context's workspace; fri.serial pins them to the workspace
+// state they were made in.
+struct FriInput {
+  FriParams fp{};
+  FriShape s;
+  bool ext = false, evals = false;
+  uint64_t n = 0, m = 0, poly_len = 0, bound = 0;
+  uint64_t commitment_bytes = 0, proof_bytes = 0;
+};
+
+// The entry checks of src/fri.rs:407-549 in the reference's order, then
+// commit_inner's (fri_shape), and the byte lengths of both outputs.
+int fri_input(const z0p_fri_params* p, int form, size_t n, uint64_t degree_bound, FriInput* in) {
+  if (!p || form < Z0P_FRI_COEFFS || form > Z0P_FRI_EVALS_EXT) return Z0P_ERR_INVALID_ARGUMENT;
+  in->fp = FriParams{p->blowup, p->num_queries, p->final_size, p->grinding_bits, p->cap_height};
+  RC(fri_params_validate(in->fp));
+  in->ext = form == Z0P_FRI_COEFFS_EXT || form == Z0P_FRI_EVALS_EXT;
+  in->evals = form >= Z0P_FRI_EVALS;
+  if (n == 0) return Z0P_ERR_EMPTY_INPUT;
+  if (!is_pow2(n)) return Z0P_ERR_INVALID_DOMAIN_SIZE;
+  const uint64_t max_domain = 1ull << 27;  // Field::TWO_ADICITY
+  in->n = n;
+  if (!in->evals) {  // src/ntt.rs:341-352
+    if (n > max_domain / in->fp.blowup) return Z0P_ERR_INVALID_DOMAIN_SIZE;
+    in->m = n * in->fp.blowup;
+    in->bound = n - 1;
+  } else {
+    if (n > max_domain) return Z0P_ERR_INVALID_DOMAIN_SIZE;
+    if (degree_bound >= n) {
+      set_reason("degree bound must be below LDE size (rate < 1)");
+      return Z0P_ERR_MALFORMED_INPUT;
+    }
+    in->m = n;
+    in->bound = degree_bound;
+  }
+  in->poly_len = n;
+  RC(fri_shape(in->m, in->bound, in->fp, &in->s));
+  const FriShape& s = in->s;
+  uint64_t cb = 1 + 24 + 4;  // Commitment::to_bytes
+  for (size_t i = 0; i < s.len.size(); i++) cb += 4 + 32ull * (1ull << s.drop[i]);
+  uint64_t per_query = 4;  // Proof::to_bytes
+  for (size_t d = 0; d + 1 < s.len.size(); d++) per_query += 64 + 4 + 33ull * (s.depth[d] - s.drop[d]);
+  in->commitment_bytes = cb;
+  in->proof_bytes = 1 + 4 + 16 * s.len.back() + 8 + 4 + in->fp.num_queries * per_query;
+  return Z0P_OK;
+}
+
+}  // namespace
+
+namespace z0p {
+struct FriPending {
+  bool valid = false;
+  uint64_t serial = 0;
+  FriInput in;
+  FriBufs fb;
+  HioPlan h;
+  FriOut out;
+};
+}  // namespace z0p
+
+namespace {
+
+int fri_commit(z0p_gpu_ctx* c, const FriInput& in, const uint32_t* values,
+               z0p_transcript_state* t, uint8_t* out) {
+  const FriShape& s = in.s;
+  const uint32_t ncomp = in.ext ? 4 : 1;
+  const uint32_t logm = log2u(in.m), logn = log2u(in.n), logB = log2u(in.fp.blowup);
+  cudaStream_t st = c->stream;
+  const uint64_t in_words = in.n * ncomp;
+  RC(ensure(c, c->cols, 4 * in_words));
+  if (!in.evals) {
+    RC(ensure(c, c->coeffs, 4ull * ncomp * in.n));
+    RC(ensure(c, c->lde, 4ull * ncomp * in.m));
+    RC(ensure(c, c->scratch, 4ull * ncomp * in.m));
+  }
+  if (!c->fri) c->fri = new FriPending();
+  FriPending& f = *c->fri;
+  f.valid = false;
+  f.in = in;
+  RC(plan_fri_buffers(c, s, 1, &f.fb));
+  RC(plan_hio(c, s, in.fp.num_queries, 0, 0, 1, &f.h, 16));
+  unsigned int* bad_h = reinterpret_cast<unsigned int*>(c->hio + f.h.extra);
+  unsigned int* bad = hio_dev<unsigned int>(c, f.h.extra);
+  *bad_h = 0;
+  uint32_t* src = (uint32_t*)c->cols.p;
+  CK(cudaMemcpyAsync(src, values, 4 * in_words, cudaMemcpyHostToDevice, st));
+  c->h2d += 4 * in_words;
+  if (!in.evals) {
+    uint32_t* coeffs = (uint32_t*)c->coeffs.p;
+    uint32_t* lde = (uint32_t*)c->lde.p;
+    CK(launch::gamma_scale(st, c->tb, src, coeffs, (uint32_t)in.n, in.ext ? 1u : 0u, bad));
+    NttPlan lp;
+    lp.logn = logn;
+    lp.batch = ncomp << logB;
+    lp.in_div = 1u << logB;
+    lp.twist_mod = 1u << logB;
+    lp.twist_shift = 27 - logm;
+    CK(launch::ntt(st, c->tb, lp, coeffs, lde, (uint32_t*)c->scratch.p));
+    CK(launch::layer0_leaves(st, lde, f.fb.layer[0], f.fb.tree[0], bad, logm, logB, ncomp, true));
+  } else {
+    CK(launch::layer0_leaves(st, src, f.fb.layer[0], f.fb.tree[0], bad, logm, 0, ncomp, false));
+  }
+  CK(launch::merkle_build(st, f.fb.tree[0], s.leaves[0], s.depth[0] - s.drop[0], merkle_counter(c),
+                          hio_dev<uint32_t>(c, f.h.fri_cap[0]), 0, 1, f.fb.tree_stride,
+                          f.h.fri_cap_bytes[0] / 4));
+  z0p_transcript_state work = *t;
+  Transcript tr(&work);
+  Transcript* ts[1] = {&tr};
+  RC(run_fri_commit(c, s, in.fp, f.fb, in.poly_len, in.bound, ts, 1, f.h, &f.out));
+  if (*reinterpret_cast<volatile unsigned int*>(bad_h)) {  // read after the stream drained
+    set_reason("field elements must be canonical (< p)");
+    return Z0P_ERR_MALFORMED_INPUT;
+  }
+  Writer w(out, in.commitment_bytes);
+  w.byte(6);  // VERSION (src/codec.rs:21)
+  write_fri_commitment(w, s, f.out, in.poly_len, in.bound);
+  *t = work;
+  f.valid = true;
+  f.serial = c->work_serial;
+  return Z0P_OK;
+}
+
+int fri_open(z0p_gpu_ctx* c, z0p_transcript_state* t, uint8_t* out, uint64_t* indices) {
+  FriPending& f = *c->fri;
+  const FriShape& s = f.in.s;
+  z0p_transcript_state work = *t;
+  Transcript tr(&work);
+  Transcript* ts[1] = {&tr};
+  RC(run_fri_open(c, s, f.in.fp, ts, 1, f.h, &f.out));
+  OpenArgs oa{};
+  oa.no_trace = 1;
+  RC(run_openings(c, s, f.fb, f.h, &f.out, 1, oa));
+  Writer w(out, f.in.proof_bytes);
+  w.byte(6);  // VERSION (src/codec.rs:21)
+  write_fri_proof(w, c, s, f.out, f.h, 0);
+  if (indices)
+    for (size_t i = 0; i < f.out.indices.size(); i++) indices[i] = f.out.indices[i];
+  *t = work;
+  f.valid = false;
+  return Z0P_OK;
+}
 }  // namespace
 
 struct ProfileScope {
@@ -1081,6 +1261,7 @@ int prove_group_abi(z0p_gpu_ctx* c, size_t n, const Params* params,
   for (size_t i = 0; i < n; i++)
     if (!transcripts[i]) return Z0P_ERR_INVALID_ARGUMENT;
   std::lock_guard<std::mutex> lk(c->mu);
+  c->work_serial++;
   RC(with_device(c));
   ProfileScope ps(c);
   const uint64_t t0 = now_ns();
@@ -1320,17 +1501,78 @@ void z0p_gpu_ctx_destroy(z0p_gpu_ctx* c) {
   if (c->consts) cudaFreeHost(c->consts);
   give_slots(c->slot, c->nslots);
   if (c->stream) cudaStreamDestroy(c->stream);
+  delete c->fri;
   delete c;
 }
 
 int z0p_gpu_ctx_trim(z0p_gpu_ctx* c) {
   if (!c) return Z0P_ERR_INVALID_ARGUMENT;
   std::lock_guard<std::mutex> lk(c->mu);
+  c->work_serial++;
   RC(with_device(c));
   for (DevBuf* b : {&c->cols, &c->coeffs, &c->scratch, &c->lde, &c->ttree, &c->layers, &c->ftrees,
                     &c->misc})
     release(c, *b);
   return Z0P_OK;
+}
+
+int z0p_fri_params_for_security(uint64_t poly_len, uint32_t target_bits, z0p_fri_params* out) {
+  if (!out) return Z0P_ERR_INVALID_ARGUMENT;  // src/fri.rs:232-255
+  if (poly_len == 0) return Z0P_ERR_EMPTY_INPUT;
+  if (!is_pow2(poly_len)) return Z0P_ERR_INVALID_DOMAIN_SIZE;
+  const uint64_t blowup = 16;
+  if (poly_len > (1ull << 27) / blowup) return Z0P_ERR_INVALID_DOMAIN_SIZE;
+  uint64_t q = 0, fs = 0, ch = 0;
+  uint32_t g = 0;
+  tune_strength(target_bits, 2000, &q, &g);
+  tune_shape(poly_len * blowup, q, 0, 0, &fs, &ch);
+  *out = z0p_fri_params{blowup, q, fs, g, ch};
+  return Z0P_OK;
+}
+
+int z0p_fri_sizes(const z0p_fri_params* p, int form, size_t n, uint64_t degree_bound,
+                  size_t* commitment_len, size_t* proof_len) {
+  FriInput in;
+  RC(fri_input(p, form, n, degree_bound, &in));
+  if (commitment_len) *commitment_len = in.commitment_bytes;
+  if (proof_len) *proof_len = in.proof_bytes;
+  return Z0P_OK;
+}
+
+int z0p_gpu_fri_commit(z0p_gpu_ctx* c, const z0p_fri_params* p, int form, const uint32_t* values,
+                       size_t n, uint64_t degree_bound, z0p_transcript_state* t, uint8_t* out,
+                       size_t cap, size_t* len) {
+  if (!c || !t || (!values && n)) return Z0P_ERR_INVALID_ARGUMENT;
+  FriInput in;
+  RC(fri_input(p, form, n, degree_bound, &in));
+  if (len) *len = in.commitment_bytes;
+  if (!out || cap < in.commitment_bytes) {
+    set_reason("output buffer too small for the commitment");
+    return Z0P_ERR_BUFFER_TOO_SMALL;
+  }
+  std::lock_guard<std::mutex> lk(c->mu);
+  c->work_serial++;
+  RC(with_device(c));
+  ProfileScope ps(c);
+  return fri_commit(c, in, values, t, out);
+}
+
+int z0p_gpu_fri_open(z0p_gpu_ctx* c, z0p_transcript_state* t, uint8_t* out, size_t cap,
+                     size_t* len, uint64_t* indices) {
+  if (!c || !t) return Z0P_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lk(c->mu);
+  if (!c->fri || !c->fri->valid || c->fri->serial != c->work_serial) {
+    set_reason("no FRI commitment to open on this context");
+    return Z0P_ERR_INVALID_ARGUMENT;
+  }
+  if (len) *len = c->fri->in.proof_bytes;
+  if (!out || cap < c->fri->in.proof_bytes) {
+    set_reason("output buffer too small for the proof");
+    return Z0P_ERR_BUFFER_TOO_SMALL;
+  }
+  RC(with_device(c));
+  ProfileScope ps(c);
+  return fri_open(c, t, out, indices);
 }
 
 int z0p_gpu_ctx_reserve_group(z0p_gpu_ctx* c, uint32_t max_group) {
@@ -1439,6 +1681,7 @@ int z0p_gpu_rs_extend(z0p_gpu_ctx* c, const uint32_t* d_values, uint64_t n, uint
   if (!is_pow2(blowup)) return Z0P_ERR_INVALID_BLOWUP;
   if (n * blowup > MAX_DOMAIN || batch * blowup > 65535) return Z0P_ERR_INVALID_DOMAIN_SIZE;
   std::lock_guard<std::mutex> lk(c->mu);
+  c->work_serial++;
   RC(with_device(c));
   uint32_t logn = log2u(n), logm = logn + log2u(blowup);
   RC(ensure(c, c->coeffs, 4 * n * batch));
@@ -1469,6 +1712,7 @@ int z0p_gpu_merkle_flat64_cap(z0p_gpu_ctx* c, const uint8_t* d_flat, uint64_t le
   uint64_t leaves = 1;  // padded by duplicating the last leaf (src/merkle.rs:350-360)
   while (leaves < count) leaves <<= 1;
   std::lock_guard<std::mutex> lk(c->mu);
+  c->work_serial++;
   RC(with_device(c));
   RC(ensure(c, c->ttree, 32 * tree_digests(leaves)));
   uint32_t* tree = (uint32_t*)c->ttree.p;
@@ -1490,6 +1734,7 @@ int z0p_gpu_fri_fold(z0p_gpu_ctx* c, const uint32_t* d_in, uint64_t n, uint64_t 
       (lde_len >> (2 * depth)) != n)
     return Z0P_ERR_INVALID_DOMAIN_SIZE;
   std::lock_guard<std::mutex> lk(c->mu);
+  c->work_serial++;
   RC(with_device(c));
   RC(ensure(c, c->ftrees, 32 * (n / 4 + 4)));
   FoldArgs fa;
@@ -1518,6 +1763,7 @@ int z0p_gpu_fri_fold(z0p_gpu_ctx* c, const uint32_t* d_in, uint64_t n, uint64_t 
 int z0p_gpu_blake3_ceiling(z0p_gpu_ctx* c, double* gcompress_per_s) {
   if (!c || !gcompress_per_s) return Z0P_ERR_INVALID_ARGUMENT;
   std::lock_guard<std::mutex> lk(c->mu);
+  c->work_serial++;
   RC(with_device(c));
   int sms = 0;
   CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device));
@@ -1564,6 +1810,7 @@ int z0p_gpu_grind(z0p_gpu_ctx* c, const uint8_t* head, size_t head_len, uint32_t
     return Z0P_ERR_UNSUPPORTED;
   }
   std::lock_guard<std::mutex> lk(c->mu);
+  c->work_serial++;
   RC(with_device(c));
   RC(ensure_hio(c, 16));
   set_head(c->consts, head, head_len);
