@@ -251,6 +251,85 @@ def run_batched(Z, ctx, workers=16):
     }
 
 
+def run_fri_pcs(Z, ctx, reps=5):
+    """FRI as a polynomial commitment (fri::commit + fri::open): the reference's
+    `fri prod` rows (docs/benchmarks.md:24,26; coefficients and labels of
+    benches/speed_size.rs:607-647, 756-795) and a 2^20-coefficient commitment.
+    Host coefficients in, commitment and proof bytes out, per call."""
+    import numpy as np
+
+    P = 2013265921
+    rows = []
+    for n, label, ref_ms, ref_bytes in [(256, b"bench/fri-prod", 10.59, 29378),
+                                        (1024, b"bench/fri-prod-big", 21.50, 43174),
+                                        (1 << 20, b"bench/fri-pcs-2p20", None, None)]:
+        i = np.arange(n, dtype=np.uint64)
+        coeffs = (((i * 0x9E3779B9) + 17) % 2**32 % P).astype(np.uint32)
+        params = Z.fri.Params.for_security(n, 100)
+        times, size = [], 0
+        for _ in range(reps + 1):
+            t = Z.Transcript(label)
+            t0 = time.perf_counter()
+            st = Z.fri.commit(coeffs, params, t, ctx)
+            proof, _ = Z.fri.open(st, t)
+            times.append(time.perf_counter() - t0)
+            size = len(st.commitment) + len(proof)
+        ms = 1e3 * sorted(times[1:])[len(times[1:]) // 2]
+        rows.append({"poly_len": n, "lde_len": 16 * n, "ms": round(ms, 4), "bytes": size,
+                     "reference_ms_16_cores": ref_ms, "reference_bytes": ref_bytes,
+                     "bytes_match_reference": None if ref_bytes is None else size == ref_bytes})
+    return {"workload": "fri::Params::for_security(n, 100): B16 Q40 G20 C4 F16; commit + open",
+            "rows": rows}
+
+
+def run_fold_ivc(Z, ctx, reps=3):
+    """Folded IVC (fold::Accumulator): the reference's `fold 4x8 fib` row
+    (docs/benchmarks.md:127; workload of benches/speed_size.rs:432-449) and
+    16 segments of 2^16 rows at for_security(100). Host columns in, proof
+    bytes out; a step is add_segment for every segment plus finalize."""
+    import numpy as np
+
+    P = 2013265921
+
+    def chain(seg, count):
+        out, a, b = [], 1, 1
+        for _ in range(count):
+            ca, cb = np.empty(seg, np.uint32), np.empty(seg, np.uint32)
+            for i in range(seg):
+                ca[i], cb[i] = a, b
+                a, b = b, (a + b) % P
+            a, b = int(ca[-1]), int(cb[-1])  # the next segment restarts at the last row
+            out.append((ca, cb))
+        return out
+
+    rows = []
+    for seg, count, label, ref_ms, ref_bytes in [(8, 4, b"bench/fold", 0.19, 16845),
+                                                 (1 << 16, 16, b"bench/fold-2p16x16", None, None)]:
+        traces = chain(seg, count)
+        out_b = int(traces[-1][1][-1])
+        if seg == 8:
+            params = Z.fold.Params.new(8, 8, 8, 4, 1, 1, out_b)
+        else:
+            params = Z.fold.Params.for_security(seg, 1, 1, out_b, 100)
+        times, size = [], 0
+        for _ in range(reps + 1):
+            t = Z.Transcript(label)
+            t0 = time.perf_counter()
+            acc = Z.fold.Accumulator(params, ctx)
+            for ca, cb in traces:
+                acc.add_segment(ca, cb, t)
+            proof = acc.finalize(t)
+            times.append(time.perf_counter() - t0)
+            acc.close()
+            size = len(proof)
+        ms = 1e3 * sorted(times[1:])[len(times[1:]) // 2]
+        rows.append({"segments": count, "seg_steps": seg, "steps": count * seg, "ms": round(ms, 4),
+                     "steps_per_s": round(count * seg / (ms / 1e3)), "bytes": size,
+                     "reference_ms_16_cores": ref_ms, "reference_bytes": ref_bytes,
+                     "bytes_match_reference": None if ref_bytes is None else size == ref_bytes})
+    return {"workload": "Fibonacci segments chained from (1, 1), one batched FRI", "rows": rows}
+
+
 def run_served(Z, ctx, rates=(100, 200, 400, None), requests=120, workers=16, budget=180 << 30):
     """Poisson arrivals of mixed Fibonacci (2^10..2^22) / range (2^12..2^18) requests.
     A rate of None submits the whole set at once (saturation)."""
@@ -429,10 +508,12 @@ def run_gpu(args):
         prof = ctx.profile()
         ctx.set_profiling(False)
 
-    batched = served = None
+    batched = served = fri_pcs = fold_ivc = None
     if not args.quick and ws == 1:
         batched = run_batched(Z, ctx)
         served = run_served(Z, ctx)
+        fri_pcs = run_fri_pcs(Z, ctx)
+        fold_ivc = run_fold_ivc(Z, ctx)
 
     if rank != 0:
         if dist is not None:
@@ -525,6 +606,8 @@ def run_gpu(args):
         "cpu_baseline": cpu,
         "batched": batched,
         "served": served,
+        "fri_pcs": fri_pcs,
+        "fold_ivc": fold_ivc,
     }
     print(json.dumps(line), flush=True)
     if dist is not None:

@@ -257,6 +257,44 @@ int z0p_gpu_fri_commit(z0p_gpu_ctx *ctx, const z0p_fri_params *params, int form,
 int z0p_gpu_fri_open(z0p_gpu_ctx *ctx, z0p_transcript_state *transcript, uint8_t *out, size_t cap,
                      size_t *len, uint64_t *indices);
 
+/* -------------------------------------------------------- folded IVC ---- */
+/* fold::Params (src/fold.rs:42-64): rows per segment, FRI shape, and the
+ * global claims (input A, B; output B). */
+typedef struct {
+    uint64_t seg_steps;
+    uint64_t blowup;
+    uint64_t num_queries;
+    uint64_t final_size;
+    uint32_t grinding_bits;
+    uint64_t cap_height;
+    uint32_t in_a;
+    uint32_t in_b;
+    uint32_t out_b;
+} z0p_fold_params;
+/* fold::Params::new (src/fold.rs:72-111) and ::for_security (:136-171). */
+int z0p_fold_params_new(uint64_t seg_steps, uint64_t blowup, uint64_t num_queries,
+                        uint64_t final_size, uint32_t in_a, uint32_t in_b, uint32_t out_b,
+                        z0p_fold_params *out);
+int z0p_fold_params_for_security(uint64_t seg_steps, uint32_t in_a, uint32_t in_b, uint32_t out_b,
+                                 uint32_t target_bits, z0p_fold_params *out);
+/* fold::Accumulator (src/fold.rs:362-561) on a context: every segment's column
+ * LDEs and row tree stay on the device until finalize. Calls on an
+ * accumulator are serialised by its context's mutex. */
+typedef struct z0p_gpu_fold z0p_gpu_fold;
+int z0p_gpu_fold_create(z0p_gpu_ctx *ctx, const z0p_fold_params *params, z0p_gpu_fold **out);
+void z0p_gpu_fold_destroy(z0p_gpu_fold *acc);
+size_t z0p_gpu_fold_len(const z0p_gpu_fold *acc);
+/* Accumulator::add_segment (src/fold.rs:407-488): columns of seg_steps
+ * canonical words each; on error the transcript is left untouched. */
+int z0p_gpu_fold_add_segment(z0p_gpu_fold *acc, const uint32_t *col_a, const uint32_t *col_b,
+                             size_t len, z0p_transcript_state *transcript);
+/* Exact length of IvcProof::to_bytes (src/fold.rs:281-309) for the segments so far. */
+int z0p_gpu_fold_proof_size(const z0p_gpu_fold *acc, size_t *len);
+/* Accumulator::finalize (src/fold.rs:494-561): writes IvcProof::to_bytes; the
+ * accumulator accepts no further segment afterwards. */
+int z0p_gpu_fold_finalize(z0p_gpu_fold *acc, z0p_transcript_state *transcript, uint8_t *out,
+                          size_t cap, size_t *len);
+
 /* ------------------------------------------------- batching / serving ---- */
 /*
  * Many independent proofs (the batched and served configurations). A pool

@@ -57,6 +57,15 @@ class FriParams(C.Structure):
 FRI_COEFFS, FRI_COEFFS_EXT, FRI_EVALS, FRI_EVALS_EXT = 0, 1, 2, 3
 
 
+class FoldParams(C.Structure):
+    """fold::Params (src/fold.rs:42-64)."""
+    _fields_ = [
+        ("seg_steps", C.c_uint64), ("blowup", C.c_uint64), ("num_queries", C.c_uint64),
+        ("final_size", C.c_uint64), ("grinding_bits", C.c_uint32), ("cap_height", C.c_uint64),
+        ("in_a", C.c_uint32), ("in_b", C.c_uint32), ("out_b", C.c_uint32),
+    ]
+
+
 def fri_for_security(poly_len: int, target_bits: int) -> FriParams:
     """fri::Params::for_security (src/fri.rs:232-255), from the oracle's tuners."""
     if poly_len == 0:
@@ -137,6 +146,13 @@ def lib():
             "zo_fri_open": (C.c_int, [vp, vp, C.POINTER(u8p), C.POINTER(sz), u64p]),
             "zo_fri_state_free": (None, [vp]),
             "zo_fri_verify": (C.c_int, [C.POINTER(FriParams), C.c_char_p, sz, C.c_char_p, sz, vp, u64p]),
+            "zo_fold_params_new": (C.c_int, [C.c_uint64] * 4 + [C.c_uint32] * 3 + [C.POINTER(FoldParams)]),
+            "zo_fold_for_security": (C.c_int, [C.c_uint64] + [C.c_uint32] * 4 + [C.POINTER(FoldParams)]),
+            "zo_fold_new": (vp, [C.POINTER(FoldParams)]),
+            "zo_fold_add_segment": (C.c_int, [vp, u32p, u32p, sz, vp]),
+            "zo_fold_finalize": (C.c_int, [vp, vp, C.POINTER(u8p), C.POINTER(sz)]),
+            "zo_fold_free": (None, [vp]),
+            "zo_fold_verify": (C.c_int, [C.POINTER(FoldParams), C.c_char_p, sz, vp]),
             "zo_free": (None, [vp]),
             "zo_set_max_workers": (None, [sz]),
             "zo_max_workers": (sz, []),
@@ -386,6 +402,56 @@ def fri_verify(params: FriParams, commitment: bytes, proof: bytes, t: Transcript
     idx = (C.c_uint64 * max(1, params.num_queries))()
     rc = lib().zo_fri_verify(C.byref(params), commitment, len(commitment), proof, len(proof), t.h, idx)
     return rc, list(idx)[: params.num_queries]
+
+
+def fold_params_new(seg_steps, blowup, num_queries, final_size, in_a, in_b, out_b) -> FoldParams:
+    p = FoldParams()
+    rc = lib().zo_fold_params_new(seg_steps, blowup, num_queries, final_size, in_a, in_b, out_b,
+                                  C.byref(p))
+    if rc:
+        raise ValueError(ERRORS[rc])
+    return p
+
+
+def fold_for_security(seg_steps, in_a, in_b, out_b, target_bits) -> FoldParams:
+    p = FoldParams()
+    rc = lib().zo_fold_for_security(seg_steps, in_a, in_b, out_b, target_bits, C.byref(p))
+    if rc:
+        raise ValueError(ERRORS[rc])
+    return p
+
+
+class Accumulator:
+    """fold::Accumulator (src/fold.rs:362-561)."""
+
+    def __init__(self, params: FoldParams):
+        self.params = params
+        self.h = lib().zo_fold_new(C.byref(params))
+        self.n = 0
+
+    def __del__(self):
+        if self.h:
+            lib().zo_fold_free(self.h)
+            self.h = None
+
+    def add_segment(self, col_a, col_b, t: Transcript) -> None:
+        a, ap = u32arr(col_a)
+        b, bp = u32arr(col_b)
+        if len(a) != len(b):
+            raise ValueError("MalformedInput")
+        rc = lib().zo_fold_add_segment(self.h, ap, bp, len(a), t.h)
+        if rc:
+            raise ValueError(ERRORS[rc])
+        self.n += 1
+
+    def finalize(self, t: Transcript) -> bytes:
+        buf, n = C.POINTER(C.c_uint8)(), C.c_size_t()
+        rc = lib().zo_fold_finalize(self.h, t.h, C.byref(buf), C.byref(n))
+        return _take_proof(rc, buf, n)
+
+
+def fold_verify(params: FoldParams, proof: bytes, t: Transcript) -> int:
+    return lib().zo_fold_verify(C.byref(params), proof, len(proof), t.h)
 
 
 # ------------------------------------------------------------ kernel pieces

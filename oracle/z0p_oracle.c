@@ -2104,6 +2104,382 @@ out:
 }
 
 /* ------------------------------------------------------------------------ */
+/* fold.rs — hash-chained Fibonacci segments with one batched FRI (IVC)     */
+/* ------------------------------------------------------------------------ */
+
+/* fold.rs:72-111 Params::new */
+int zo_fold_params_new(uint64_t seg, uint64_t blowup, uint64_t q, uint64_t final_size,
+                       uint32_t in_a, uint32_t in_b, uint32_t out_b, zo_fold_params *o) {
+    if (seg < 2 || !is_pow2(seg)) return ZO_INVALID_DOMAIN_SIZE;
+    if (blowup < 4 || !is_pow2(blowup)) return ZO_INVALID_BLOWUP;
+    if (q == 0) return ZO_NO_QUERIES;
+    if (final_size < 2 || !is_pow2(final_size)) return ZO_INVALID_DOMAIN_SIZE;
+    if (seg > UINT64_MAX / blowup || seg * blowup > MAX_DOMAIN) return ZO_INVALID_DOMAIN_SIZE;
+    o->seg_steps = seg; o->blowup = blowup; o->num_queries = q; o->final_size = final_size;
+    o->grinding_bits = 0; o->cap_height = 0;
+    o->in_a = in_a % P; o->in_b = in_b % P; o->out_b = out_b % P;
+    return ZO_OK;
+}
+
+/* fold.rs:136-171 Params::for_security */
+int zo_fold_for_security(uint64_t seg, uint32_t in_a, uint32_t in_b, uint32_t out_b,
+                         uint32_t target, zo_fold_params *o) {
+    if (seg < 2 || !is_pow2(seg)) return ZO_INVALID_DOMAIN_SIZE;
+    uint64_t blowup = 16;
+    if (seg > UINT64_MAX / blowup || seg * blowup > MAX_DOMAIN) return ZO_INVALID_DOMAIN_SIZE;
+    size_t lde = seg * blowup;
+    uint32_t mb = zo_fri_composition_millibits(lde, seg - 1);
+    size_t q; uint32_t g;
+    zo_fri_tune_strength(target, mb, &q, &g);
+    size_t fs, ch;
+    zo_fri_tune_shape(lde, q, lde, 24, 1, &fs, &ch);
+    o->seg_steps = seg; o->blowup = blowup; o->num_queries = q; o->final_size = fs;
+    o->grinding_bits = g; o->cap_height = ch;
+    o->in_a = in_a % P; o->in_b = in_b % P; o->out_b = out_b % P;
+    return ZO_OK;
+}
+
+/* fold.rs:186-222 validate */
+static int fold_validate(const zo_fold_params *p) {
+    if (p->seg_steps < 2 || !is_pow2(p->seg_steps)) return ZO_INVALID_DOMAIN_SIZE;
+    if (p->blowup < 4 || !is_pow2(p->blowup)) return ZO_INVALID_BLOWUP;
+    if (p->num_queries == 0) return ZO_NO_QUERIES;
+    if (p->final_size < 2 || !is_pow2(p->final_size)) return ZO_INVALID_DOMAIN_SIZE;
+    if (p->cap_height > 8) return ZO_MALFORMED_INPUT;
+    if (p->seg_steps > UINT64_MAX / p->blowup || p->seg_steps * p->blowup > MAX_DOMAIN)
+        return ZO_INVALID_DOMAIN_SIZE;
+    return ZO_OK;
+}
+
+/* fold.rs:177-184 fri_params */
+static int fold_fri_params(const zo_fold_params *p, fri_params *f) {
+    int rc = fri_params_new(p->blowup, p->num_queries, p->final_size, f);
+    if (rc) return rc;
+    f->grinding_bits = p->grinding_bits; f->cap_height = p->cap_height;
+    return ZO_OK;
+}
+
+/* fold.rs:729-741 */
+static void fold_absorb_params(const zo_fold_params *p, zo_transcript *t) {
+    uint8_t b[64];
+    put_u64(b, p->seg_steps); put_u64(b + 8, p->blowup); put_u64(b + 16, p->num_queries);
+    put_u64(b + 24, p->final_size); put_u32(b + 32, p->grinding_bits);
+    put_u64(b + 36, p->cap_height); put_u32(b + 44, p->in_a); put_u32(b + 48, p->in_b);
+    put_u32(b + 52, p->out_b);
+    absorb_s(t, "fold/params", b, 56);
+}
+
+typedef struct { uint32_t in_a, in_b, out_a, out_b; } fold_claims;
+
+/* fold.rs:743-751 */
+static void fold_absorb_step(const fold_claims *c, zo_transcript *t) {
+    uint8_t b[16];
+    put_u32(b, c->in_a); put_u32(b + 4, c->in_b); put_u32(b + 8, c->out_a); put_u32(b + 12, c->out_b);
+    absorb_s(t, "fold/step", b, 16);
+}
+
+typedef struct {
+    fold_claims claims;
+    uint32_t *lde[2];
+    mtree tree;
+    ext4 *composition;
+} fold_step;
+
+typedef struct {
+    zo_fold_params params;
+    fold_step *steps;
+    size_t n, cap;
+} fold_acc;
+
+void *zo_fold_new(const zo_fold_params *p) {  /* fold.rs:379-384 */
+    fold_acc *a = calloc(1, sizeof *a);
+    a->params = *p;
+    return a;
+}
+
+void zo_fold_free(void *acc) {
+    fold_acc *a = acc;
+    if (!a) return;
+    for (size_t i = 0; i < a->n; i++) {
+        free(a->steps[i].lde[0]); free(a->steps[i].lde[1]);
+        mtree_free(&a->steps[i].tree); free(a->steps[i].composition);
+    }
+    free(a->steps);
+    free(a);
+}
+
+/* fold.rs:856-879 composition_at (quotient form) */
+static ext4 fold_composition_at(uint32_t a, uint32_t b, uint32_t an, uint32_t bn, uint32_t x,
+                                uint32_t w_last, const fold_claims *c, size_t s,
+                                const ext4 alpha[6]) {
+    uint32_t vanishing = f_sub(f_pow(x, s), 1);
+    uint32_t z_trans = f_mul(vanishing, f_inv(f_sub(x, w_last)));
+    uint32_t inv_z = f_inv(z_trans);
+    uint32_t inv_b = f_inv(f_sub(x, 1)), inv_a = f_inv(f_sub(x, w_last));
+    uint32_t t[6] = {
+        f_mul(f_sub(an, b), inv_z), f_mul(f_sub(bn, f_add(a, b)), inv_z),
+        f_mul(f_sub(a, c->in_a), inv_b), f_mul(f_sub(b, c->in_b), inv_b),
+        f_mul(f_sub(a, c->out_a), inv_a), f_mul(f_sub(b, c->out_b), inv_a),
+    };
+    ext4 acc = e_mul_base(alpha[0], t[0]);
+    for (int k = 1; k < 6; k++) acc = e_add(acc, e_mul_base(alpha[k], t[k]));
+    return acc;
+}
+
+/* fold.rs:407-488 add_segment */
+int zo_fold_add_segment(void *acc, const uint32_t *col_a, const uint32_t *col_b, size_t len,
+                        zo_transcript *t) {
+    fold_acc *a = acc;
+    int rc = fold_validate(&a->params);
+    if (rc) return rc;
+    size_t s = a->params.seg_steps;
+    if (len != s) return ZO_MALFORMED_INPUT;
+    fold_claims c = {col_a[0] % P, col_b[0] % P, col_a[s - 1] % P, col_b[s - 1] % P};
+    if (a->n == 0) fold_absorb_params(&a->params, t);
+    fold_absorb_step(&c, t);
+    size_t m = s * a->params.blowup;
+    fold_step st;
+    memset(&st, 0, sizeof st);
+    st.claims = c;
+    for (int k = 0; k < 2; k++) {
+        uint32_t *coeffs = malloc(s * 4);
+        for (size_t i = 0; i < s; i++) coeffs[i] = (k ? col_b : col_a)[i] % P;
+        zo_ntt_inverse(coeffs, s);
+        st.lde[k] = malloc(m * 4);
+        zo_evaluate_on_coset(coeffs, s, a->params.blowup, LDE_SHIFT, st.lde[k]);
+        free(coeffs);
+    }
+    size_t offset = m / s;
+    uint8_t *flat = malloc(m * 8);
+    for (size_t i = 0; i < m; i++) { put_u32(flat + 8 * i, st.lde[0][i]); put_u32(flat + 8 * i + 4, st.lde[1][i]); }
+    mtree_from_flat(flat, m * 8, 8, &st.tree);
+    free(flat);
+    size_t drop, depth;
+    capped_shape(m, a->params.cap_height, &drop, &depth);
+    size_t ncap;
+    const digest *cap = mtree_cap(&st.tree, drop, &ncap);
+    absorb_s(t, "fold/trace", (const uint8_t *)cap, 32 * ncap);
+    ext4 alpha[6];
+    for (int k = 0; k < 6; k++) alpha[k] = challenge_ext(t, "fold/alpha");
+    /* compose_step (fold.rs:785-850): batched inverses over the whole domain */
+    uint32_t omega_m, omega_s;
+    primitive_root(m, &omega_m);
+    primitive_root(s, &omega_s);
+    uint32_t w_last = f_pow(omega_s, s - 1);
+    uint32_t *da = malloc(m * 4), *db = malloc(m * 4), *zt = malloc(m * 4), *xs = malloc(m * 4);
+    uint32_t x = LDE_SHIFT;
+    for (size_t i = 0; i < m; i++) {
+        xs[i] = x;
+        da[i] = f_sub(x, w_last);
+        db[i] = f_sub(x, 1);
+        x = f_mul(x, omega_m);
+    }
+    zo_batch_invert(da, m);
+    zo_batch_invert(db, m);
+    for (size_t i = 0; i < m; i++) zt[i] = f_mul(f_sub(f_pow(xs[i], s), 1), da[i]);
+    zo_batch_invert(zt, m);
+    st.composition = malloc(m * sizeof(ext4));
+    for (size_t i = 0; i < m; i++) {
+        uint32_t av = st.lde[0][i], bv = st.lde[1][i];
+        uint32_t an = st.lde[0][(i + offset) % m], bn = st.lde[1][(i + offset) % m];
+        uint32_t tv[6] = {
+            f_mul(f_sub(an, bv), zt[i]), f_mul(f_sub(bn, f_add(av, bv)), zt[i]),
+            f_mul(f_sub(av, c.in_a), db[i]), f_mul(f_sub(bv, c.in_b), db[i]),
+            f_mul(f_sub(av, c.out_a), da[i]), f_mul(f_sub(bv, c.out_b), da[i]),
+        };
+        ext4 accv = e_mul_base(alpha[0], tv[0]);
+        for (int k = 1; k < 6; k++) accv = e_add(accv, e_mul_base(alpha[k], tv[k]));
+        st.composition[i] = accv;
+    }
+    free(da); free(db); free(zt); free(xs);
+    if (a->n == a->cap) {
+        a->cap = a->cap ? 2 * a->cap : 4;
+        a->steps = realloc(a->steps, a->cap * sizeof(fold_step));
+    }
+    a->steps[a->n++] = st;
+    return ZO_OK;
+}
+
+static size_t bit_reverse_index(size_t x, uint32_t bits) {  /* fold.rs:881-888 */
+    size_t out = 0;
+    for (uint32_t i = 0; i < bits; i++) { out = (out << 1) | (x & 1); x >>= 1; }
+    return out;
+}
+
+/* fold.rs:494-560 finalize, bytes per fold.rs:281-309 */
+int zo_fold_finalize(void *acc, zo_transcript *t, uint8_t **proof, size_t *proof_len) {
+    fold_acc *a = acc;
+    if (a->n == 0) return ZO_EMPTY_INPUT;
+    const zo_fold_params *p = &a->params;
+    size_t s = p->seg_steps, m = s * p->blowup;
+    ext4 *gamma = malloc(a->n * sizeof(ext4));
+    for (size_t k = 0; k < a->n; k++) gamma[k] = challenge_ext(t, "fold/gamma");
+    ext4 *combined = calloc(m, sizeof(ext4));
+    for (size_t i = 0; i < m; i++)
+        for (size_t k = 0; k < a->n; k++)
+            combined[i] = e_add(combined[i], e_mul(gamma[k], a->steps[k].composition[i]));
+    free(gamma);
+    fri_params fp;
+    int rc = fold_fri_params(p, &fp);
+    if (rc) { free(combined); return rc; }
+    /* fri::commit_ext_evals (fri.rs:508-549): the bound check, then commit_inner */
+    rc = fri_params_validate(&fp);
+    if (!rc && s - 1 >= m) rc = ZO_MALFORMED_INPUT;
+    if (rc) { free(combined); return rc; }
+    fri_state st;
+    rc = fri_commit_inner(combined, m, s - 1, m, &fp, t, &st);
+    if (rc) return rc;
+    writer fc = {0}, fo = {0};
+    fri_write_commitment(&fc, &st);
+    uint64_t *idx = malloc(p->num_queries * sizeof(uint64_t));
+    rc = fri_open_write(&st, t, &fo, idx);
+    if (rc) { fri_state_free(&st); free(fc.b); free(fo.b); free(idx); return rc; }
+    uint32_t log_m = log2u(m);
+    size_t offset = m / s, drop, depth;
+    capped_shape(m, p->cap_height, &drop, &depth);
+    writer w = {0};
+    w_byte(&w, VERSION);
+    w_u32(&w, (uint32_t)a->n);
+    for (size_t k = 0; k < a->n && !rc; k++) {
+        fold_step *sp = &a->steps[k];
+        w_u32(&w, sp->claims.in_a); w_u32(&w, sp->claims.in_b);
+        w_u32(&w, sp->claims.out_a); w_u32(&w, sp->claims.out_b);
+        size_t ncap;
+        const digest *cap = mtree_cap(&sp->tree, drop, &ncap);
+        w_cap(&w, cap, ncap);
+        w_u32(&w, (uint32_t)p->num_queries);
+        for (size_t qi = 0; qi < p->num_queries && !rc; qi++) {
+            size_t index = bit_reverse_index(idx[qi], log_m);
+            size_t shifted = (index + offset) % m;
+            w_u64(&w, index);
+            w_u32(&w, sp->lde[0][index]); w_u32(&w, sp->lde[1][index]);
+            w_u32(&w, sp->lde[0][shifted]); w_u32(&w, sp->lde[1][shifted]);
+            path_t pa, pb;
+            rc = mtree_prove_capped(&sp->tree, index, drop, &pa);
+            if (rc) break;
+            rc = mtree_prove_capped(&sp->tree, shifted, drop, &pb);
+            if (rc) { free(pa.s); break; }
+            w_path(&w, &pa); w_path(&w, &pb);
+            free(pa.s); free(pb.s);
+        }
+    }
+    if (!rc) { w_bytes(&w, fc.b, fc.n); w_bytes(&w, fo.b, fo.n); }
+    fri_state_free(&st);
+    free(fc.b); free(fo.b); free(idx);
+    if (rc) { free(w.b); return rc; }
+    *proof = w.b; *proof_len = w.n;
+    return ZO_OK;
+}
+
+typedef struct { size_t index; uint32_t cols[4]; path_t path, spath; } fold_open_t;
+typedef struct { fold_claims claims; digest *cap; size_t ncap; fold_open_t *op; size_t nop; } fold_step_t;
+
+/* fold.rs:572-667 verify (decoding per fold.rs:312-355) */
+int zo_fold_verify(const zo_fold_params *p, const uint8_t *proof, size_t proof_len,
+                   zo_transcript *t) {
+    int rc = fold_validate(p);
+    if (rc) return rc;
+    reader r = {proof, proof_len, 0, 0};
+    if (r_byte(&r) != VERSION) return ZO_MALFORMED_INPUT;
+    size_t nsteps = r_count(&r, 1u << 20);
+    if (r.err) return ZO_MALFORMED_INPUT;
+    if (nsteps * 20 > r.n - r.pos) return ZO_MALFORMED_INPUT;
+    fold_step_t *st = calloc(nsteps ? nsteps : 1, sizeof(fold_step_t));
+    size_t got = 0;
+    fri_decoded d;
+    memset(&d, 0, sizeof d);
+    for (size_t k = 0; k < nsteps && !r.err; k++) {
+        got = k + 1;
+        st[k].claims.in_a = r_field(&r); st[k].claims.in_b = r_field(&r);
+        st[k].claims.out_a = r_field(&r); st[k].claims.out_b = r_field(&r);
+        st[k].cap = r_cap(&r, &st[k].ncap);
+        size_t no = r_count(&r, MAX_QUERIES);
+        if (r.err || no * 24 > r.n - r.pos) { r.err = 1; break; }
+        st[k].op = calloc(no ? no : 1, sizeof(fold_open_t));
+        for (size_t i = 0; i < no && !r.err; i++) {
+            st[k].nop = i + 1;
+            st[k].op[i].index = r_u64(&r);
+            for (int c = 0; c < 4; c++) st[k].op[i].cols[c] = r_field(&r);
+            r_path(&r, &st[k].op[i].path);
+            r_path(&r, &st[k].op[i].spath);
+        }
+    }
+    if (!r.err) fri_read(&r, &d);
+    if (r.err || r.pos != r.n) { rc = ZO_MALFORMED_INPUT; goto out; }
+    if (nsteps == 0) { rc = ZO_EMPTY_INPUT; goto out; }
+    size_t s = p->seg_steps, m = s * p->blowup, offset = m / s;
+    if (d.lde_len != m || d.poly_len != m || d.degree_bound != s - 1) { rc = ZO_FRI_VERIFICATION_FAILED; goto out; }
+    fold_absorb_params(p, t);
+    /* check_chain (fold.rs:710-727) */
+    if (st[0].claims.in_a != p->in_a || st[0].claims.in_b != p->in_b) { rc = ZO_FRI_VERIFICATION_FAILED; goto out; }
+    for (size_t k = 0; k + 1 < nsteps; k++)
+        if (st[k].claims.out_a != st[k + 1].claims.in_a || st[k].claims.out_b != st[k + 1].claims.in_b)
+            { rc = ZO_FRI_VERIFICATION_FAILED; goto out; }
+    if (st[nsteps - 1].claims.out_b != p->out_b) { rc = ZO_FRI_VERIFICATION_FAILED; goto out; }
+    uint32_t omega_s, omega_m;
+    primitive_root(s, &omega_s);
+    primitive_root(m, &omega_m);
+    uint32_t w_last = f_pow(omega_s, s - 1);
+    ext4 (*alpha)[6] = malloc(nsteps * sizeof(ext4[6]));
+    for (size_t k = 0; k < nsteps && !rc; k++) {
+        fold_absorb_step(&st[k].claims, t);
+        absorb_s(t, "fold/trace", (const uint8_t *)st[k].cap, 32 * st[k].ncap);
+        for (int j = 0; j < 6; j++) alpha[k][j] = challenge_ext(t, "fold/alpha");
+        if (st[k].nop != p->num_queries) rc = ZO_FRI_VERIFICATION_FAILED;
+    }
+    ext4 *gamma = malloc(nsteps * sizeof(ext4));
+    for (size_t k = 0; k < nsteps && !rc; k++) gamma[k] = challenge_ext(t, "fold/gamma");
+    fri_params fp;
+    uint64_t *idx = NULL;
+    if (!rc) rc = fold_fri_params(p, &fp);
+    if (!rc) {
+        idx = malloc((d.nq ? d.nq : 1) * sizeof(uint64_t));
+        rc = fri_verify(&d, &fp, t, idx);
+    }
+    size_t drop, depth;
+    capped_shape(m, p->cap_height, &drop, &depth);
+    uint32_t log_m = log2u(m);
+    for (size_t qi = 0; !rc && qi < d.nq; qi++) {
+        size_t index = bit_reverse_index(idx[qi], log_m);
+        uint32_t x = f_mul(LDE_SHIFT, f_pow(omega_m, index));
+        ext4 combined = {{0, 0, 0, 0}};
+        for (size_t k = 0; k < nsteps && !rc; k++) {
+            fold_open_t *o = &st[k].op[qi];
+            if (o->index != index) { rc = ZO_FRI_VERIFICATION_FAILED; break; }
+            /* check_step_openings (fold.rs:669-708) */
+            if (st[k].ncap != ((size_t)1 << drop) || o->path.n != depth - drop ||
+                o->spath.n != depth - drop) { rc = ZO_BAD_MERKLE_PATH; break; }
+            uint8_t row[8];
+            put_u32(row, o->cols[0]); put_u32(row + 4, o->cols[1]);
+            size_t e = index >> (depth - drop);
+            if (e >= st[k].ncap || !verify_capped(st[k].cap[e], row, 8, index, depth, &o->path))
+                { rc = ZO_BAD_MERKLE_PATH; break; }
+            size_t sh = (index + offset) % m;
+            put_u32(row, o->cols[2]); put_u32(row + 4, o->cols[3]);
+            e = sh >> (depth - drop);
+            if (e >= st[k].ncap || !verify_capped(st[k].cap[e], row, 8, sh, depth, &o->spath))
+                { rc = ZO_BAD_MERKLE_PATH; break; }
+            combined = e_add(combined, e_mul(gamma[k],
+                fold_composition_at(o->cols[0], o->cols[1], o->cols[2], o->cols[3], x, w_last,
+                                    &st[k].claims, s, alpha[k])));
+        }
+        if (rc) break;
+        if (d.q[qi].n == 0) { rc = ZO_FRI_VERIFICATION_FAILED; break; }
+        if (!e_eq(d.q[qi].f[0].v[idx[qi] % 4], combined)) rc = ZO_FRI_VERIFICATION_FAILED;
+    }
+    free(idx); free(alpha); free(gamma);
+out:
+    for (size_t k = 0; k < got; k++) {
+        free(st[k].cap);
+        for (size_t i = 0; i < st[k].nop; i++) { free(st[k].op[i].path.s); free(st[k].op[i].spath.s); }
+        free(st[k].op);
+    }
+    free(st);
+    fri_decoded_free(&d);
+    return rc;
+}
+
+/* ------------------------------------------------------------------------ */
 /* range.rs — range-check AIR                                                */
 /* ------------------------------------------------------------------------ */
 

@@ -170,6 +170,27 @@ void zo_fri_state_free(void *state);
 int zo_fri_verify(const zo_fri_params *params, const uint8_t *commitment, size_t commitment_len,
                   const uint8_t *proof, size_t proof_len, zo_transcript *t, uint64_t *indices);
 
+/* fold.rs: hash-chained Fibonacci segments plus one batched FRI (IVC).
+ * The accumulator handle holds every segment's LDEs, tree and composition. */
+typedef struct {
+    uint64_t seg_steps, blowup, num_queries, final_size;
+    uint32_t grinding_bits;
+    uint64_t cap_height;
+    uint32_t in_a, in_b, out_b;
+} zo_fold_params;
+int zo_fold_params_new(uint64_t seg_steps, uint64_t blowup, uint64_t num_queries,
+                       uint64_t final_size, uint32_t in_a, uint32_t in_b, uint32_t out_b,
+                       zo_fold_params *out);
+int zo_fold_for_security(uint64_t seg_steps, uint32_t in_a, uint32_t in_b, uint32_t out_b,
+                         uint32_t target_bits, zo_fold_params *out);
+void *zo_fold_new(const zo_fold_params *params);
+int zo_fold_add_segment(void *acc, const uint32_t *col_a, const uint32_t *col_b, size_t len,
+                        zo_transcript *t);
+int zo_fold_finalize(void *acc, zo_transcript *t, uint8_t **proof, size_t *proof_len);
+void zo_fold_free(void *acc);
+int zo_fold_verify(const zo_fold_params *params, const uint8_t *proof, size_t proof_len,
+                   zo_transcript *t);
+
 void zo_free(void *p);
 /* Worker-thread cap for the parallel paths (0 = all online cores). */
 void zo_set_max_workers(size_t workers);

@@ -42,6 +42,14 @@ class FriParams(C.Structure):
     ]
 
 
+class FoldParams(C.Structure):
+    _fields_ = [
+        ("seg_steps", C.c_uint64), ("blowup", C.c_uint64), ("num_queries", C.c_uint64),
+        ("final_size", C.c_uint64), ("grinding_bits", C.c_uint32), ("cap_height", C.c_uint64),
+        ("in_a", C.c_uint32), ("in_b", C.c_uint32), ("out_b", C.c_uint32),
+    ]
+
+
 class RangeParams(C.Structure):
     _fields_ = [
         ("n_rows", C.c_uint64), ("n_bits", C.c_uint64), ("blowup", C.c_uint64),
@@ -114,6 +122,15 @@ def lib():
             "z0p_gpu_ctx_profile": (C.c_int, [vp, C.c_char_p, sz, P(sz)]),
             "z0p_gpu_air_prove": (C.c_int, [vp, P(AirParams), P(TranscriptState), u8p, sz, P(sz)]),
             "z0p_gpu_range_prove": (C.c_int, [vp, P(RangeParams), P(TranscriptState), u8p, sz, P(sz)]),
+            "z0p_fold_params_new": (C.c_int, [C.c_uint64] * 4 + [C.c_uint32] * 3 + [P(FoldParams)]),
+            "z0p_fold_params_for_security": (C.c_int, [C.c_uint64] + [C.c_uint32] * 4 + [P(FoldParams)]),
+            "z0p_gpu_fold_create": (C.c_int, [vp, P(FoldParams), P(vp)]),
+            "z0p_gpu_fold_destroy": (None, [vp]),
+            "z0p_gpu_fold_len": (sz, [vp]),
+            "z0p_gpu_fold_add_segment": (C.c_int, [vp, P(C.c_uint32), P(C.c_uint32), sz,
+                                                   P(TranscriptState)]),
+            "z0p_gpu_fold_proof_size": (C.c_int, [vp, P(sz)]),
+            "z0p_gpu_fold_finalize": (C.c_int, [vp, P(TranscriptState), P(C.c_uint8), sz, P(sz)]),
             "z0p_fri_params_for_security": (C.c_int, [C.c_uint64, C.c_uint32, P(FriParams)]),
             "z0p_fri_sizes": (C.c_int, [P(FriParams), C.c_int, sz, C.c_uint64, P(sz), P(sz)]),
             "z0p_gpu_fri_commit": (C.c_int, [vp, P(FriParams), C.c_int, P(C.c_uint32), sz, C.c_uint64,

@@ -927,6 +927,124 @@ __global__ void __launch_bounds__(kThreads) layer0_leaves_kernel(Layer0Args a) {
   store_digest(a.leaves + 8 * (size_t)P, d);
 }
 
+// ---------------------------------------------------------- folded IVC ----
+__global__ void check_canonical_kernel(const uint32_t* __restrict__ in, uint64_t n,
+                                       unsigned int* bad) {
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n && in[i] >= kP) atomicOr(bad, 1u);
+}
+
+// 1/(x_k - w_last) for rows k = 8L..8L+7 (consecutive powers of omega_m), one
+// batched inversion per thread, stored coset-major at [j][q], k = B q + j.
+__global__ void row_inverses_kernel(uint32_t* __restrict__ tinv, uint32_t w_last_m, uint32_t logN,
+                                    uint32_t logB, Tables tb) {
+  const uint32_t logm = logN + logB;
+  const uint32_t L = blockIdx.x * blockDim.x + threadIdx.x;
+  if (L >= (1u << (logm - 3))) return;
+  const uint32_t step = root_pow(tb, 1u << (kRootBits - logm));
+  uint32_t x = mmul(to_mont(31u), root_pow(tb, (8u * L) << (kRootBits - logm)));
+  uint32_t den[8];
+#pragma unroll
+  for (int r = 0; r < 8; r++) {
+    den[r] = fsub(x, w_last_m);
+    x = mmul(x, step);
+  }
+  batch_minv(den);
+#pragma unroll
+  for (int r = 0; r < 8; r++) {
+    const uint32_t k = 8u * L + r;
+    tinv[((size_t)(k & ((1u << logB) - 1u)) << logN) + (k >> logB)] = den[r];
+  }
+}
+
+// One thread per layer-0 quad (the composition kernel's mapping): for each of
+// its four rows, the six quotient terms of every segment (src/fold.rs:833-847)
+// times gamma_k alpha_t, summed over the segments; then the 64-byte leaf.
+//   1/z_trans = (x - w_last) / (x^s - 1)     (x^s constant on a coset)
+//   1/(x - w_last) = T(q),  1/(x - 1) = omega_s^-1 T(q-1)  (folded into ga[2], ga[3])
+// All arithmetic is exact, so the sum equals sum_k gamma_k C_k term by term.
+__global__ void __launch_bounds__(kThreads) fold_combine_kernel(FoldCombineArgs a, Tables tb) {
+  const uint32_t logm = a.logN + a.logB;
+  const uint32_t quarter = 1u << (logm - 2);
+  const uint32_t u = blockIdx.x * blockDim.x + threadIdx.x;
+  if (u >= quarter) return;
+  const uint32_t N = 1u << a.logN, B = 1u << a.logB;
+  uint32_t k0 = u;
+  if (a.logN >= 2) {
+    const uint32_t j = u >> (a.logN - 2), q0 = u & ((N >> 2) - 1u);
+    k0 = (q0 << a.logB) | j;
+  }
+  const uint32_t P = brev_bits(k0, logm - 2);
+  uint32_t xs[4];
+  quad_points(tb, k0, logm, xs);
+  uint32_t leaf[16];
+#pragma unroll
+  for (int s = 0; s < 4; s++) {
+    const uint32_t k = k0 + (uint32_t)s * quarter;
+    const uint32_t j = k & (B - 1u), q = k >> a.logB;
+    const size_t base = (size_t)j << a.logN;
+    const size_t at = base + q, atn = base + ((q + 1u) & (N - 1u));
+    const uint32_t tm = __ldg(a.tinv + base + ((q - 1u) & (N - 1u)));
+    const uint32_t t0 = __ldg(a.tinv + at);
+    const uint32_t iz = mmul(fsub_lazy(xs[s], a.w_last_m), __ldg(a.zinv + j));
+    uint32_t acc[4] = {0u, 0u, 0u, 0u};
+    for (uint32_t st = 0; st < a.nsteps; st++) {
+      const FoldStepDev& S = a.steps[st];
+      const uint32_t av = __ldg(S.a + at), bv = __ldg(S.b + at);
+      const uint32_t an = __ldg(S.a + atn), bn = __ldg(S.b + atn);
+      const uint32_t tr1 = mmul(fsub_lazy(an, bv), iz);
+      const uint32_t tr2 = mmul(fsub_lazy(bn, fadd(av, bv)), iz);
+      const uint32_t ia = mmul(fsub_lazy(av, S.in_a), tm);
+      const uint32_t ib = mmul(fsub_lazy(bv, S.in_b), tm);
+      const uint32_t oa = mmul(fsub_lazy(av, S.out_a), t0);
+      const uint32_t ob = mmul(fsub_lazy(bv, S.out_b), t0);
+#pragma unroll
+      for (int c = 0; c < 4; c++) {
+        const uint32_t v = fadd(mdot4(tr1, S.ga[0][c], tr2, S.ga[1][c], ia, S.ga[2][c], ib, S.ga[3][c]),
+                                mdot2(oa, S.ga[4][c], ob, S.ga[5][c]));
+        acc[c] = fadd(acc[c], v);
+      }
+    }
+    const int t = (s == 1) ? 2 : (s == 2) ? 1 : s;  // position 4P + brev2(s)
+#pragma unroll
+    for (int c = 0; c < 4; c++) leaf[4 * t + c] = acc[c];
+  }
+  uint4* dst = reinterpret_cast<uint4*>(a.layer0 + 16 * (size_t)P);
+#pragma unroll
+  for (int t = 0; t < 4; t++)
+    dst[t] = make_uint4(leaf[4 * t], leaf[4 * t + 1], leaf[4 * t + 2], leaf[4 * t + 3]);
+  uint32_t d[8];
+  blake3_leaf64(leaf, d);
+  store_digest(a.leaves + 8 * (size_t)P, d);
+}
+
+// CTA (query i, step k): 4 column words, then the two capped row paths.
+__global__ void __launch_bounds__(64) fold_openings_kernel(const FoldStepDev* steps,
+                                                          const uint64_t* leaves, uint32_t nq,
+                                                          uint32_t logN, uint32_t logB,
+                                                          uint32_t path_steps, uint32_t* out,
+                                                          uint32_t stride) {
+  const uint32_t qi = blockIdx.x, k = blockIdx.y;
+  const FoldStepDev& S = steps[k];
+  const uint32_t logm = logN + logB;
+  const uint64_t m = 1ull << logm;
+  const uint64_t index = brev_bits((uint32_t)leaves[qi], logm);
+  const uint64_t shifted = (index + (1ull << logB)) & (m - 1);
+  uint32_t* o = out + ((size_t)k * nq + qi) * stride;
+  for (uint32_t t = threadIdx.x; t < 4 + 16 * path_steps; t += blockDim.x) {
+    if (t < 4) {
+      const uint64_t idx = t < 2 ? index : shifted;
+      const size_t at = ((size_t)(idx & ((1u << logB) - 1u)) << logN) + (idx >> logB);
+      o[t] = (t & 1u) ? S.b[at] : S.a[at];
+    } else {
+      const uint32_t h = (t - 4) / (8 * path_steps), r = (t - 4) % (8 * path_steps);
+      const uint32_t lv = r >> 3, w = r & 7u;
+      const uint64_t sib = ((h ? shifted : index) >> lv) ^ 1ull;
+      o[t] = S.tree[8 * (2 * m - 2 * (m >> lv) + sib) + w];
+    }
+  }
+}
+
 // ----------------------------------------------------------------- FRI ----
 // fold_values (src/fri.rs:1311-1331): A + x^-1 (r0 B + x^-1 (r1 C + x^-1 r2 D))
 // with B, C, D the quarter-scaled differences; the 1/4 is folded into the
@@ -1604,6 +1722,41 @@ cudaError_t layer0_leaves(cudaStream_t st, const uint32_t* src, uint32_t* layer0
   Stage stg("layer0_leaves", st);
   stg.launched();
   layer0_leaves_kernel<<<grid_for(1ull << (logm - 2)), kThreads, 0, st>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t row_inverses(cudaStream_t st, const Tables& tb, uint32_t* tinv, uint32_t w_last_m,
+                         uint32_t logN, uint32_t logB) {
+  if (logN + logB < 3) return cudaErrorInvalidValue;
+  Stage stg("row_inverses", st);
+  stg.launched();
+  row_inverses_kernel<<<grid_for(1ull << (logN + logB - 3)), kThreads, 0, st>>>(tinv, w_last_m, logN,
+                                                                             logB, tb);
+  return cudaGetLastError();
+}
+
+cudaError_t check_canonical(cudaStream_t st, const uint32_t* in, uint64_t n, unsigned int* bad) {
+  Stage stg("check_canonical", st);
+  stg.launched();
+  check_canonical_kernel<<<grid_for(n), kThreads, 0, st>>>(in, n, bad);
+  return cudaGetLastError();
+}
+
+cudaError_t fold_combine(cudaStream_t st, const Tables& tb, const FoldCombineArgs& a) {
+  if (a.logN + a.logB < 3) return cudaErrorInvalidValue;
+  Stage stg("fold_combine", st);
+  stg.launched();
+  fold_combine_kernel<<<grid_for(1ull << (a.logN + a.logB - 2)), kThreads, 0, st>>>(a, tb);
+  return cudaGetLastError();
+}
+
+cudaError_t fold_openings(cudaStream_t st, const FoldStepDev* steps, uint32_t nsteps,
+                          const uint64_t* leaves, uint32_t nq, uint32_t logN, uint32_t logB,
+                          uint32_t path_steps, uint32_t* out, uint32_t stride) {
+  Stage stg("fold_openings", st);
+  stg.launched();
+  fold_openings_kernel<<<dim3(nq, nsteps), 64, 0, st>>>(steps, leaves, nq, logN, logB, path_steps,
+                                                       out, stride);
   return cudaGetLastError();
 }
 

@@ -143,6 +143,28 @@ void e4_table(const uint32_t r[4], uint32_t T[4][4]);
 // run the hash at the ALU ceiling where fused levels would leave warps idle.
 constexpr uint64_t kFuseMaxLeaves = 1ull << 15;
 
+// Folded IVC (src/fold.rs): one accumulated segment as the combination
+// kernel reads it. `a`/`b` are the segment's column LDEs, coset-major
+// [j][q]; `ga[t]` is gamma_k * alpha_t (Montgomery form, canonical
+// coordinates), with the boundary-at-1 terms (t = 2, 3) also carrying
+// omega_s^-1 (1/(x - 1) = omega_s^-1 T(q-1)); `tree` is the segment's row tree.
+struct FoldStepDev {
+  const uint32_t* a;
+  const uint32_t* b;
+  const uint32_t* tree;
+  uint32_t in_a, in_b, out_a, out_b;
+  uint32_t ga[6][4];
+};
+struct FoldCombineArgs {
+  const FoldStepDev* steps;
+  uint32_t nsteps;
+  const uint32_t* tinv;  // coset-major 1/(x - w_last) (Montgomery)
+  const uint32_t* zinv;  // per coset 1/(x^s - 1) (Montgomery)
+  uint32_t* layer0;      // FRI layer 0 (bit-reversed Ext4 values)
+  uint32_t* leaves;      // its leaf digests
+  uint32_t logN, logB;   // segment rows s = 2^logN, blowup 2^logB
+  uint32_t w_last_m;     // omega_s^(s-1) (Montgomery)
+};
 namespace launch {
 
 // Number of kernel launches issued by this library in this process.
@@ -229,6 +251,20 @@ cudaError_t gamma_scale(cudaStream_t st, const Tables& tb, const uint32_t* in, u
 cudaError_t layer0_leaves(cudaStream_t st, const uint32_t* src, uint32_t* layer0, uint32_t* leaves,
                           unsigned int* bad, uint32_t logm, uint32_t logB, uint32_t ncomp,
                           bool coset_major);
+// Words of 1 / (x_k - w_last) for every LDE row, stored coset-major.
+cudaError_t row_inverses(cudaStream_t st, const Tables& tb, uint32_t* tinv, uint32_t w_last_m,
+                         uint32_t logN, uint32_t logB);
+// *bad = 1 when any of the n words is not a canonical field element.
+cudaError_t check_canonical(cudaStream_t st, const uint32_t* in, uint64_t n, unsigned int* bad);
+// combined(x) = sum_k gamma_k C_k(x) over the accumulated segments, written
+// as FRI layer 0 with its leaf digests (src/fold.rs:494-517, 785-850).
+cudaError_t fold_combine(cudaStream_t st, const Tables& tb, const FoldCombineArgs& a);
+// Step openings (src/fold.rs:527-552): for step k and query i, at
+// out + (k nq + i) stride: A, B at index = brev(leaf) and at index + B
+// (mod m), then the capped paths of both rows (steps x 8 words each).
+cudaError_t fold_openings(cudaStream_t st, const FoldStepDev* steps, uint32_t nsteps,
+                          const uint64_t* leaves, uint32_t nq, uint32_t logN, uint32_t logB,
+                          uint32_t path_steps, uint32_t* out, uint32_t stride);
 // Leaf digests of an FRI layer held in memory (64-byte quads or 16-byte values).
 cudaError_t layer_leaves(cudaStream_t st, const uint32_t* values, uint64_t len, uint32_t* leaves,
                          uint32_t nproofs = 1, uint64_t in_stride = 0, uint64_t out_stride = 0);

@@ -1238,6 +1238,252 @@ int fri_open(z0p_gpu_ctx* c, z0p_transcript_state* t, uint8_t* out, uint64_t* in
   f.valid = false;
   return Z0P_OK;
 }
+
+// ====================================================== folded IVC ====
+// fold::Accumulator (src/fold.rs:362-561) on the device: each segment's two
+// column LDEs and row tree stay resident; finalize combines every segment's
+// composition into FRI layer 0 in one pass, commits it with the FRI engine
+// and gathers the step openings.
+// Ext4 product on the host (src/ext4.rs:106-117): with x = x0 + x1 v over
+// Fp2 = Fp[u]/(u^2 - 11) and v^2 = u, xy = (x0 y0 + u x1 y1) + (x0 y1 + x1 y0) v.
+void e4_mul_host(const uint32_t x[4], const uint32_t y[4], uint32_t out[4]) {
+  auto fp2 = [](uint32_t a0, uint32_t a1, uint32_t b0, uint32_t b1, uint32_t o[2]) {
+    o[0] = fadd(fmul(a0, b0), fmul(11, fmul(a1, b1)));
+    o[1] = fadd(fmul(a0, b1), fmul(a1, b0));
+  };
+  uint32_t p00[2], p11[2], p01[2], p10[2];
+  fp2(x[0], x[1], y[0], y[1], p00);
+  fp2(x[2], x[3], y[2], y[3], p11);
+  fp2(x[0], x[1], y[2], y[3], p01);
+  fp2(x[2], x[3], y[0], y[1], p10);
+  out[0] = fadd(p00[0], fmul(11, p11[1]));  // u (a + b u) = 11 b + a u
+  out[1] = fadd(p00[1], p11[0]);
+  out[2] = fadd(p01[0], p10[0]);
+  out[3] = fadd(p01[1], p10[1]);
+}
+
+int fold_validate(const z0p_fold_params& p) {  // src/fold.rs:186-222
+  if (p.seg_steps < 2 || !is_pow2(p.seg_steps)) return Z0P_ERR_INVALID_DOMAIN_SIZE;
+  if (p.blowup < 4 || !is_pow2(p.blowup)) return Z0P_ERR_INVALID_BLOWUP;
+  if (p.num_queries == 0) return Z0P_ERR_NO_QUERIES;
+  if (p.final_size < 2 || !is_pow2(p.final_size)) return Z0P_ERR_INVALID_DOMAIN_SIZE;
+  if (p.cap_height > 8) { set_reason("cap_height above 8"); return Z0P_ERR_MALFORMED_INPUT; }
+  if (p.seg_steps > (1ull << 27) / p.blowup) return Z0P_ERR_INVALID_DOMAIN_SIZE;
+  if (p.in_a >= P || p.in_b >= P || p.out_b >= P) {
+    set_reason("field elements must be canonical (< p)");
+    return Z0P_ERR_MALFORMED_INPUT;
+  }
+  return Z0P_OK;
+}
+
+int fold_fri(const z0p_fold_params& p, FriParams* fp, FriShape* s) {  // src/fold.rs:177-184
+  RC(fri_params_new(p.blowup, p.num_queries, p.final_size, fp));
+  fp->grinding_bits = p.grinding_bits;
+  fp->cap_height = p.cap_height;
+  const uint64_t m = p.seg_steps * p.blowup;
+  if (p.seg_steps - 1 >= m) return Z0P_ERR_MALFORMED_INPUT;  // fri::commit_ext_evals
+  return fri_shape(m, p.seg_steps - 1, *fp, s);
+}
+
+struct FoldStepHost {
+  uint32_t claims[4];  // in_a, in_b, out_a, out_b
+  uint32_t alpha[6][4];
+  std::vector<uint8_t> cap;
+  DevBuf lde, tree;  // [A planes | B planes] coset-major; level-contiguous row tree
+};
+
+}  // namespace
+
+struct z0p_gpu_fold {
+  z0p_gpu_ctx* ctx = nullptr;
+  z0p_fold_params p{};
+  std::vector<FoldStepHost> steps;
+  DevBuf tinv, table;  // row inverses; FoldStepDev table + per-coset 1/(x^s - 1)
+  bool finalized = false;
+};
+
+namespace {
+
+uint64_t fold_proof_bytes(const z0p_fold_params& p, size_t nsteps, const FriShape& s) {
+  const uint64_t m = p.seg_steps * p.blowup;
+  const uint32_t depth = log2u(m), drop = p.cap_height < depth ? (uint32_t)p.cap_height : depth;
+  const uint64_t path = 4 + 33ull * (depth - drop);
+  const uint64_t per_step = 16 + 4 + 32ull * (1ull << drop) + 4 + p.num_queries * (8 + 16 + 2 * path);
+  return 1 + 4 + nsteps * per_step + fri_bytes(s, p.num_queries);
+}
+
+void fold_absorb_params(const z0p_fold_params& p, Transcript& t) {  // src/fold.rs:729-741
+  uint8_t b[56];
+  auto u64 = [&](int at, uint64_t v) { for (int i = 0; i < 8; i++) b[at + i] = (uint8_t)(v >> (8 * i)); };
+  auto u32 = [&](int at, uint32_t v) { for (int i = 0; i < 4; i++) b[at + i] = (uint8_t)(v >> (8 * i)); };
+  u64(0, p.seg_steps); u64(8, p.blowup); u64(16, p.num_queries); u64(24, p.final_size);
+  u32(32, p.grinding_bits); u64(36, p.cap_height); u32(44, p.in_a); u32(48, p.in_b); u32(52, p.out_b);
+  transcript_absorb(t, "fold/params", b, 56);
+}
+
+int fold_add(z0p_gpu_fold* f, const uint32_t* col_a, const uint32_t* col_b,
+             z0p_transcript_state* ts) {
+  z0p_gpu_ctx* c = f->ctx;
+  const z0p_fold_params& p = f->p;
+  const uint64_t S = p.seg_steps, B = p.blowup, m = S * B;
+  const uint32_t logN = log2u(S), logB = log2u(B), logm = logN + logB;
+  cudaStream_t st = c->stream;
+  RC(ensure(c, c->cols, 8 * S));
+  RC(ensure(c, c->coeffs, 8 * S));
+  RC(ensure(c, c->scratch, 8 * m));
+  FoldStepHost step;
+  RC(ensure(c, step.lde, 8 * m));
+  RC(ensure(c, step.tree, 32 * tree_digests(m)));
+  const uint32_t depth = logm, drop = p.cap_height < depth ? (uint32_t)p.cap_height : depth;
+  const size_t cap_bytes = 32ull << drop;
+  RC(ensure_hio(c, 64 + cap_bytes));
+  unsigned int* bad_h = reinterpret_cast<unsigned int*>(c->hio);
+  *bad_h = 0;
+  uint32_t* cols = (uint32_t*)c->cols.p;
+  CK(cudaMemcpyAsync(cols, col_a, 4 * S, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(cols + S, col_b, 4 * S, cudaMemcpyHostToDevice, st));
+  c->h2d += 8 * S;
+  CK(launch::check_canonical(st, cols, 2 * S, hio_dev<unsigned int>(c, 0)));
+  NttPlan ip;  // interpolate (src/ntt.rs:316-321), outputs times 31^i / S
+  ip.logn = logN; ip.batch = 2; ip.inverse = 1; ip.post_gamma = 1;
+  CK(launch::ntt(st, c->tb, ip, cols, (uint32_t*)c->coeffs.p, (uint32_t*)c->scratch.p));
+  NttPlan lp;  // evaluate_on_coset (src/ntt.rs:341-363), coset-major per column
+  lp.logn = logN; lp.batch = (uint32_t)(2 * B); lp.in_div = (uint32_t)B; lp.twist_mod = (uint32_t)B;
+  lp.twist_shift = 27 - logm;
+  uint32_t* lde = (uint32_t*)step.lde.p;
+  CK(launch::ntt(st, c->tb, lp, (uint32_t*)c->coeffs.p, lde, (uint32_t*)c->scratch.p));
+  // Row tree over A || B (src/fold.rs:448-458: MerkleTree::from_flat, 8-byte rows).
+  uint32_t* tree = (uint32_t*)step.tree.p;
+  CK(launch::range_trace_leaves(st, lde, tree, logN, logB, 2));
+  CK(launch::merkle_build(st, tree, m, depth - drop, merkle_counter(c), hio_dev<uint32_t>(c, 64)));
+  CK(sync(c, "cap"));
+  if (*reinterpret_cast<volatile unsigned int*>(bad_h)) {
+    set_reason("field elements must be canonical (< p)");
+    return Z0P_ERR_MALFORMED_INPUT;
+  }
+  step.claims[0] = col_a[0]; step.claims[1] = col_b[0];
+  step.claims[2] = col_a[S - 1]; step.claims[3] = col_b[S - 1];
+  step.cap.assign(c->hio + 64, c->hio + 64 + cap_bytes);
+  c->d2h += cap_bytes;
+  z0p_transcript_state work = *ts;
+  Transcript t(&work);
+  if (f->steps.empty()) fold_absorb_params(p, t);
+  uint8_t cl[16];
+  for (int i = 0; i < 16; i++) cl[i] = (uint8_t)(step.claims[i / 4] >> (8 * (i % 4)));
+  transcript_absorb(t, "fold/step", cl, 16);
+  transcript_absorb(t, "fold/trace", step.cap.data(), cap_bytes);
+  for (int k = 0; k < 6; k++) challenge_ext(t, "fold/alpha", step.alpha[k]);
+  *ts = work;
+  f->steps.push_back(std::move(step));
+  return Z0P_OK;
+}
+
+int fold_finalize(z0p_gpu_fold* f, z0p_transcript_state* ts, uint8_t* out) {
+  z0p_gpu_ctx* c = f->ctx;
+  const z0p_fold_params& p = f->p;
+  const uint64_t S = p.seg_steps, B = p.blowup, m = S * B;
+  const uint32_t logN = log2u(S), logB = log2u(B), logm = logN + logB;
+  const uint32_t K = (uint32_t)f->steps.size();
+  cudaStream_t st = c->stream;
+  FriParams fp;
+  FriShape s;
+  RC(fold_fri(p, &fp, &s));
+  const uint32_t depth = logm, drop = p.cap_height < depth ? (uint32_t)p.cap_height : depth;
+  const uint32_t psteps = depth - drop;
+  z0p_transcript_state work = *ts;
+  Transcript t(&work);
+  // Combination challenges (src/fold.rs:500-504), folded with each step's alphas.
+  const uint32_t omega_s = two_adic_generator(logN);
+  const uint32_t omega_inv = finv(omega_s);
+  const uint32_t w_last = fpow(omega_s, S - 1);
+  std::vector<FoldStepDev> table(K);
+  for (uint32_t k = 0; k < K; k++) {
+    uint32_t g[4];
+    challenge_ext(t, "fold/gamma", g);
+    FoldStepHost& h = f->steps[k];
+    FoldStepDev& d = table[k];
+    d.a = (const uint32_t*)h.lde.p;
+    d.b = d.a + m;
+    d.tree = (const uint32_t*)h.tree.p;
+    d.in_a = h.claims[0]; d.in_b = h.claims[1]; d.out_a = h.claims[2]; d.out_b = h.claims[3];
+    for (int j = 0; j < 6; j++) {
+      uint32_t ga[4];
+      e4_mul_host(g, h.alpha[j], ga);
+      for (int e = 0; e < 4; e++)
+        d.ga[j][e] = to_mont(j == 2 || j == 3 ? fmul(ga[e], omega_inv) : ga[e]);
+    }
+  }
+  // Per-coset 1/(x^S - 1), x^S = 31^S omega_m^(j S) (src/fold.rs:818-825).
+  std::vector<uint32_t> zinv(B);
+  const uint32_t omega_m = two_adic_generator(logm);
+  const uint32_t g_s = fpow(GENERATOR, S);
+  for (uint64_t j = 0; j < B; j++)
+    zinv[j] = to_mont(finv(fsub(fmul(g_s, fpow(omega_m, j * S)), 1)));
+  const size_t tbytes = (size_t)K * sizeof(FoldStepDev), zoff = (tbytes + 15) & ~(size_t)15;
+  RC(ensure(c, f->table, zoff + 4 * B));
+  CK(cudaMemcpyAsync(f->table.p, table.data(), tbytes, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync((char*)f->table.p + zoff, zinv.data(), 4 * B, cudaMemcpyHostToDevice, st));
+  c->h2d += tbytes + 4 * B;
+  RC(ensure(c, f->tinv, 4 * m));
+  CK(launch::row_inverses(st, c->tb, (uint32_t*)f->tinv.p, to_mont(w_last), logN, logB));
+  FriBufs fb;
+  RC(plan_fri_buffers(c, s, 1, &fb));
+  const uint32_t stride = (4 + 16 * psteps + 3) & ~3u;
+  HioPlan h;
+  RC(plan_hio(c, s, fp.num_queries, 0, 0, 1, &h, 4ull * stride * fp.num_queries * K));
+  FoldCombineArgs ca;
+  ca.steps = (const FoldStepDev*)f->table.p;
+  ca.nsteps = K;
+  ca.tinv = (const uint32_t*)f->tinv.p;
+  ca.zinv = (const uint32_t*)((const char*)f->table.p + zoff);
+  ca.layer0 = fb.layer[0];
+  ca.leaves = fb.tree[0];
+  ca.logN = logN; ca.logB = logB;
+  ca.w_last_m = to_mont(w_last);
+  CK(launch::fold_combine(st, c->tb, ca));
+  CK(launch::merkle_build(st, fb.tree[0], s.leaves[0], s.depth[0] - s.drop[0], merkle_counter(c),
+                          hio_dev<uint32_t>(c, h.fri_cap[0]), 0, 1, fb.tree_stride,
+                          h.fri_cap_bytes[0] / 4));
+  // fri::commit_ext_evals(combined, S - 1) and fri::open (src/fold.rs:517-520).
+  Transcript* tp[1] = {&t};
+  FriOut fo;
+  RC(run_fri_commit(c, s, fp, fb, m, S - 1, tp, 1, h, &fo));
+  RC(run_fri_open(c, s, fp, tp, 1, h, &fo));
+  OpenArgs oa{};
+  oa.no_trace = 1;
+  RC(run_openings(c, s, fb, h, &fo, 1, oa));  // also leaves the indices in the mapped buffer
+  CK(launch::fold_openings(st, ca.steps, K, hio_dev<uint64_t>(c, h.indices),
+                           (uint32_t)fp.num_queries, logN, logB, psteps,
+                           hio_dev<uint32_t>(c, h.extra), stride));
+  CK(sync(c, "openings"));
+  // IvcProof::to_bytes (src/fold.rs:281-309).
+  Writer w(out, fold_proof_bytes(p, K, s));
+  w.byte(6);
+  w.u32(K);
+  const uint32_t* blocks = reinterpret_cast<const uint32_t*>(c->hio + h.extra);
+  for (uint32_t k = 0; k < K; k++) {
+    const FoldStepHost& sh = f->steps[k];
+    for (int i = 0; i < 4; i++) w.u32(sh.claims[i]);
+    w.u32((uint32_t)(sh.cap.size() / 32));
+    w.bytes(sh.cap.data(), sh.cap.size());
+    w.u32((uint32_t)fp.num_queries);
+    for (uint64_t qi = 0; qi < fp.num_queries; qi++) {
+      const uint32_t* blk = blocks + ((size_t)k * fp.num_queries + qi) * stride;
+      const uint64_t index = brev(fo.indices[qi], logm);
+      const uint64_t shifted = (index + B) % m;
+      w.u64(index);
+      for (int i = 0; i < 4; i++) w.u32(blk[i]);
+      write_path(w, (const uint8_t*)(blk + 4), index, psteps);
+      write_path(w, (const uint8_t*)(blk + 4 + 8 * psteps), shifted, psteps);
+    }
+  }
+  c->d2h += 4ull * stride * fp.num_queries * K;
+  write_fri_commitment(w, s, fo, m, S - 1);
+  write_fri_proof(w, c, s, fo, h, 0);
+  *ts = work;
+  f->finalized = true;
+  return Z0P_OK;
+}
 }  // namespace
 
 struct ProfileScope {
@@ -1573,6 +1819,120 @@ int z0p_gpu_fri_open(z0p_gpu_ctx* c, z0p_transcript_state* t, uint8_t* out, size
   RC(with_device(c));
   ProfileScope ps(c);
   return fri_open(c, t, out, indices);
+}
+
+int z0p_fold_params_new(uint64_t seg_steps, uint64_t blowup, uint64_t num_queries,
+                        uint64_t final_size, uint32_t in_a, uint32_t in_b, uint32_t out_b,
+                        z0p_fold_params* out) {
+  if (!out) return Z0P_ERR_INVALID_ARGUMENT;  // src/fold.rs:72-111
+  if (seg_steps < 2 || !is_pow2(seg_steps)) return Z0P_ERR_INVALID_DOMAIN_SIZE;
+  if (blowup < 4 || !is_pow2(blowup)) return Z0P_ERR_INVALID_BLOWUP;
+  if (num_queries == 0) return Z0P_ERR_NO_QUERIES;
+  if (final_size < 2 || !is_pow2(final_size)) return Z0P_ERR_INVALID_DOMAIN_SIZE;
+  if (seg_steps > (1ull << 27) / blowup) return Z0P_ERR_INVALID_DOMAIN_SIZE;
+  if (in_a >= P || in_b >= P || out_b >= P) {
+    set_reason("field elements must be canonical (< p)");
+    return Z0P_ERR_MALFORMED_INPUT;
+  }
+  *out = z0p_fold_params{seg_steps, blowup, num_queries, final_size, 0, 0, in_a, in_b, out_b};
+  return Z0P_OK;
+}
+
+int z0p_fold_params_for_security(uint64_t seg_steps, uint32_t in_a, uint32_t in_b, uint32_t out_b,
+                                 uint32_t target_bits, z0p_fold_params* out) {
+  if (!out) return Z0P_ERR_INVALID_ARGUMENT;  // src/fold.rs:136-171
+  if (seg_steps < 2 || !is_pow2(seg_steps)) return Z0P_ERR_INVALID_DOMAIN_SIZE;
+  const uint64_t blowup = 16;
+  if (seg_steps > (1ull << 27) / blowup) return Z0P_ERR_INVALID_DOMAIN_SIZE;
+  if (in_a >= P || in_b >= P || out_b >= P) {
+    set_reason("field elements must be canonical (< p)");
+    return Z0P_ERR_MALFORMED_INPUT;
+  }
+  const uint64_t lde = seg_steps * blowup;
+  uint64_t q = 0, fs = 0, ch = 0;
+  uint32_t g = 0;
+  tune_strength(target_bits, composition_millibits(lde, seg_steps - 1), &q, &g);
+  tune_shape(lde, q, lde, 24, &fs, &ch);
+  *out = z0p_fold_params{seg_steps, blowup, q, fs, g, ch, in_a, in_b, out_b};
+  return Z0P_OK;
+}
+
+int z0p_gpu_fold_create(z0p_gpu_ctx* c, const z0p_fold_params* p, z0p_gpu_fold** out) {
+  if (!c || !p || !out) return Z0P_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  z0p_gpu_fold* f = new z0p_gpu_fold();
+  f->ctx = c;
+  f->p = *p;
+  *out = f;
+  return Z0P_OK;
+}
+
+void z0p_gpu_fold_destroy(z0p_gpu_fold* f) {
+  if (!f) return;
+  {
+    std::lock_guard<std::mutex> lk(f->ctx->mu);
+    cudaSetDevice(f->ctx->device);
+    for (auto& s : f->steps) {
+      release(f->ctx, s.lde);
+      release(f->ctx, s.tree);
+    }
+    release(f->ctx, f->tinv);
+    release(f->ctx, f->table);
+  }
+  delete f;
+}
+
+size_t z0p_gpu_fold_len(const z0p_gpu_fold* f) { return f ? f->steps.size() : 0; }
+
+int z0p_gpu_fold_add_segment(z0p_gpu_fold* f, const uint32_t* col_a, const uint32_t* col_b,
+                             size_t len, z0p_transcript_state* t) {
+  if (!f || !t || !col_a || !col_b) return Z0P_ERR_INVALID_ARGUMENT;
+  if (f->finalized) {
+    set_reason("the accumulator was finalized");
+    return Z0P_ERR_INVALID_ARGUMENT;
+  }
+  RC(fold_validate(f->p));
+  if (len != f->p.seg_steps) {
+    set_reason("segment columns must match seg_steps");
+    return Z0P_ERR_MALFORMED_INPUT;
+  }
+  std::lock_guard<std::mutex> lk(f->ctx->mu);
+  f->ctx->work_serial++;
+  RC(with_device(f->ctx));
+  ProfileScope ps(f->ctx);
+  return fold_add(f, col_a, col_b, t);
+}
+
+int z0p_gpu_fold_proof_size(const z0p_gpu_fold* f, size_t* len) {
+  if (!f || !len) return Z0P_ERR_INVALID_ARGUMENT;
+  if (f->steps.empty()) return Z0P_ERR_EMPTY_INPUT;
+  FriParams fp;
+  FriShape s;
+  RC(fold_fri(f->p, &fp, &s));
+  *len = fold_proof_bytes(f->p, f->steps.size(), s);
+  return Z0P_OK;
+}
+
+int z0p_gpu_fold_finalize(z0p_gpu_fold* f, z0p_transcript_state* t, uint8_t* out, size_t cap,
+                          size_t* len) {
+  if (!f || !t) return Z0P_ERR_INVALID_ARGUMENT;
+  if (f->finalized) {
+    set_reason("the accumulator was finalized");
+    return Z0P_ERR_INVALID_ARGUMENT;
+  }
+  if (f->steps.empty()) return Z0P_ERR_EMPTY_INPUT;  // src/fold.rs:495-497
+  size_t need = 0;
+  RC(z0p_gpu_fold_proof_size(f, &need));
+  if (len) *len = need;
+  if (!out || cap < need) {
+    set_reason("output buffer too small for the proof");
+    return Z0P_ERR_BUFFER_TOO_SMALL;
+  }
+  std::lock_guard<std::mutex> lk(f->ctx->mu);
+  f->ctx->work_serial++;
+  RC(with_device(f->ctx));
+  ProfileScope ps(f->ctx);
+  return fold_finalize(f, t, out);
 }
 
 int z0p_gpu_ctx_reserve_group(z0p_gpu_ctx* c, uint32_t max_group) {
