@@ -98,6 +98,21 @@ typedef struct {
 
 typedef struct z0p_gpu_ctx z0p_gpu_ctx;
 
+/*
+ * ChaCha20 stream state (src/rng.rs:81-87: key, nonce, block counter, the
+ * buffered 64-byte block and how much of it is used), for the masking
+ * randomness of zero-knowledge proofs. ChaCha20::new(key, nonce) is
+ * {key, nonce, 0, zeros, 64}. A prove call advances it exactly as the
+ * reference's prove_zk advances its `&mut ChaCha20`.
+ */
+typedef struct {
+    uint8_t key[32];
+    uint8_t nonce[12];
+    uint32_t counter;
+    uint8_t block[64];
+    uint32_t used;
+} z0p_chacha20_state;
+
 /* ------------------------------------------------------------ misc ---- */
 int z0p_gpu_abi_version(void);
 const char *z0p_gpu_last_reason(void);
@@ -198,6 +213,22 @@ int z0p_gpu_air_prove(z0p_gpu_ctx *ctx, const z0p_air_params *params,
 int z0p_gpu_range_prove(z0p_gpu_ctx *ctx, const z0p_range_params *params,
                         z0p_transcript_state *transcript, uint8_t *out, size_t cap,
                         size_t *len);
+
+/* air::prove_with_trace (src/air.rs:381-399): the caller's two columns of
+ * n_steps canonical words, each interpolated and extended (no linked
+ * column). Same proof length as z0p_gpu_air_prove. */
+int z0p_gpu_air_prove_with_trace(z0p_gpu_ctx *ctx, const z0p_air_params *params,
+                                 const uint32_t *col_a, const uint32_t *col_b, size_t len,
+                                 z0p_transcript_state *transcript, uint8_t *out, size_t cap,
+                                 size_t *out_len);
+/* air::prove_zk (src/air.rs:439-464, masking of src/blind.rs:40-78): both
+ * columns masked with n_rand values each drawn from `rng` (n_rand >= 16 *
+ * num_queries); the LDE grows to the next power of two of n_steps + n_rand
+ * times blowup. On error neither the transcript nor the stream changes. */
+int z0p_air_proof_size_zk(const z0p_air_params *params, size_t n_rand, size_t *len);
+int z0p_gpu_air_prove_zk(z0p_gpu_ctx *ctx, const z0p_air_params *params, size_t n_rand,
+                         z0p_chacha20_state *rng, z0p_transcript_state *transcript, uint8_t *out,
+                         size_t cap, size_t *out_len);
 
 /* Proof groups (no counterpart in the reference): n statements of one shape
  * -- the same n_steps / n_rows (and n_bits), blowup, num_queries,

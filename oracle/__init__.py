@@ -57,6 +57,32 @@ class FriParams(C.Structure):
 FRI_COEFFS, FRI_COEFFS_EXT, FRI_EVALS, FRI_EVALS_EXT = 0, 1, 2, 3
 
 
+class ChaCha20(C.Structure):
+    """rng::ChaCha20 (src/rng.rs:81-112): key, nonce, block counter, buffered block."""
+    _fields_ = [("key", C.c_uint8 * 32), ("nonce", C.c_uint8 * 12), ("counter", C.c_uint32),
+                ("block", C.c_uint8 * 64), ("used", C.c_uint32)]
+
+    @classmethod
+    def new(cls, key: bytes, nonce: bytes) -> "ChaCha20":
+        s = cls()
+        lib().zo_chacha20_init(C.byref(s), key, nonce)
+        return s
+
+    def fill_bytes(self, n: int) -> bytes:
+        out = (C.c_uint8 * n)()
+        lib().zo_chacha20_fill(C.byref(self), out, n)
+        return bytes(out)
+
+    def next_field(self) -> int:
+        return lib().zo_chacha20_next_field(C.byref(self))
+
+
+def chacha20_block(key: bytes, counter: int, nonce: bytes) -> bytes:
+    out = (C.c_uint8 * 64)()
+    lib().zo_chacha20_block(key, counter, nonce, out)
+    return bytes(out)
+
+
 class FoldParams(C.Structure):
     """fold::Params (src/fold.rs:42-64)."""
     _fields_ = [
@@ -146,6 +172,12 @@ def lib():
             "zo_fri_open": (C.c_int, [vp, vp, C.POINTER(u8p), C.POINTER(sz), u64p]),
             "zo_fri_state_free": (None, [vp]),
             "zo_fri_verify": (C.c_int, [C.POINTER(FriParams), C.c_char_p, sz, C.c_char_p, sz, vp, u64p]),
+            "zo_chacha20_block": (None, [C.c_char_p, C.c_uint32, C.c_char_p, u8p]),
+            "zo_chacha20_init": (None, [C.POINTER(ChaCha20), C.c_char_p, C.c_char_p]),
+            "zo_chacha20_fill": (None, [C.POINTER(ChaCha20), u8p, sz]),
+            "zo_chacha20_next_field": (C.c_uint32, [C.POINTER(ChaCha20)]),
+            "zo_air_prove_zk": (C.c_int, [C.POINTER(AirParams), sz, C.POINTER(ChaCha20), vp,
+                                          C.POINTER(u8p), C.POINTER(sz)]),
             "zo_fold_params_new": (C.c_int, [C.c_uint64] * 4 + [C.c_uint32] * 3 + [C.POINTER(FoldParams)]),
             "zo_fold_for_security": (C.c_int, [C.c_uint64] + [C.c_uint32] * 4 + [C.POINTER(FoldParams)]),
             "zo_fold_new": (vp, [C.POINTER(FoldParams)]),
@@ -347,6 +379,13 @@ def air_prove_with_trace(params: AirParams, col_a, col_b, t: Transcript) -> byte
     b, bp = u32arr(col_b)
     buf, n = C.POINTER(C.c_uint8)(), C.c_size_t()
     rc = lib().zo_air_prove_with_trace(C.byref(params), ap, bp, t.h, C.byref(buf), C.byref(n))
+    return _take_proof(rc, buf, n)
+
+
+def air_prove_zk(params: AirParams, n_rand: int, rng: ChaCha20, t: Transcript) -> bytes:
+    """air::prove_zk (src/air.rs:439-464): advances rng and t."""
+    buf, n = C.POINTER(C.c_uint8)(), C.c_size_t()
+    rc = lib().zo_air_prove_zk(C.byref(params), n_rand, C.byref(rng), t.h, C.byref(buf), C.byref(n))
     return _take_proof(rc, buf, n)
 
 

@@ -1897,9 +1897,10 @@ static ext4 air_composition_at(uint32_t a, uint32_t b, uint32_t an, uint32_t bn,
 
 /* air.rs:485-599 prove_inner; lde_b given (from linked_lde or a second NTT) */
 static int air_prove_inner(const zo_air_params *params, uint32_t *lde_a, uint32_t *lde_b,
-                           size_t degree_bound, zo_transcript *t, uint8_t **proof,
+                           size_t m, size_t degree_bound, zo_transcript *t, uint8_t **proof,
                            size_t *proof_len) {
-    size_t n = params->n_steps, m = n * params->blowup, offset = m / n;
+    /* m = LDE length: n * blowup, or the padded masked length (air.rs:505-513) */
+    size_t n = params->n_steps, offset = m / n;
     uint32_t omega_base = 0;
     primitive_root(n, &omega_base);
     /* Joint rows A || B, 8 bytes each; 64-byte leaves of 8 rows (air.rs:520-531). */
@@ -1983,7 +1984,7 @@ int zo_air_prove(const zo_air_params *params, zo_transcript *t, uint8_t **proof,
     uint32_t *lde_a = malloc(m * 4), *lde_b = malloc(m * 4);
     zo_evaluate_on_coset(a, n, params->blowup, LDE_SHIFT, lde_a);
     linked_lde(lde_a, m, n, actual_b_last, params->a0, lde_b);
-    rc = air_prove_inner(params, lde_a, lde_b, n - 1, t, proof, proof_len);
+    rc = air_prove_inner(params, lde_a, lde_b, m, n - 1, t, proof, proof_len);
     free(a); free(b); free(lde_a); free(lde_b);
     return rc;
 }
@@ -2002,8 +2003,115 @@ int zo_air_prove_with_trace(const zo_air_params *params, const uint32_t *col_a,
     uint32_t *lde_a = malloc(m * 4), *lde_b = malloc(m * 4);
     zo_evaluate_on_coset(ca, n, params->blowup, LDE_SHIFT, lde_a);
     zo_evaluate_on_coset(cb, n, params->blowup, LDE_SHIFT, lde_b);
-    rc = air_prove_inner(params, lde_a, lde_b, n - 1, t, proof, proof_len);
+    rc = air_prove_inner(params, lde_a, lde_b, m, n - 1, t, proof, proof_len);
     free(ca); free(cb); free(lde_a); free(lde_b);
+    return rc;
+}
+
+/* rng.rs:22-35 quarter round, :40-73 block (RFC 8439 section 2.3) */
+static void chacha_qr(uint32_t *x, int a, int b, int c, int d) {
+    x[a] += x[b]; x[d] ^= x[a]; x[d] = (x[d] << 16) | (x[d] >> 16);
+    x[c] += x[d]; x[b] ^= x[c]; x[b] = (x[b] << 12) | (x[b] >> 20);
+    x[a] += x[b]; x[d] ^= x[a]; x[d] = (x[d] << 8) | (x[d] >> 24);
+    x[c] += x[d]; x[b] ^= x[c]; x[b] = (x[b] << 7) | (x[b] >> 25);
+}
+void zo_chacha20_block(const uint8_t key[32], uint32_t counter, const uint8_t nonce[12],
+                       uint8_t out[64]) {
+    uint32_t x[16], in[16];
+    in[0] = 0x61707865u; in[1] = 0x3320646eu; in[2] = 0x79622d32u; in[3] = 0x6b206574u;
+    for (int i = 0; i < 8; i++) in[4 + i] = get_u32(key + 4 * i);
+    in[12] = counter;
+    for (int i = 0; i < 3; i++) in[13 + i] = get_u32(nonce + 4 * i);
+    memcpy(x, in, sizeof x);
+    for (int r = 0; r < 10; r++) {
+        chacha_qr(x, 0, 4, 8, 12); chacha_qr(x, 1, 5, 9, 13);
+        chacha_qr(x, 2, 6, 10, 14); chacha_qr(x, 3, 7, 11, 15);
+        chacha_qr(x, 0, 5, 10, 15); chacha_qr(x, 1, 6, 11, 12);
+        chacha_qr(x, 2, 7, 8, 13); chacha_qr(x, 3, 4, 9, 14);
+    }
+    for (int i = 0; i < 16; i++) put_u32(out + 4 * i, x[i] + in[i]);
+}
+
+/* rng.rs:101-112 ChaCha20::new */
+void zo_chacha20_init(zo_chacha20 *s, const uint8_t key[32], const uint8_t nonce[12]) {
+    memcpy(s->key, key, 32); memcpy(s->nonce, nonce, 12);
+    s->counter = 0; memset(s->block, 0, 64); s->used = 64;
+}
+/* rng.rs:115-131 fill_bytes */
+void zo_chacha20_fill(zo_chacha20 *s, uint8_t *out, size_t n) {
+    size_t done = 0;
+    while (done < n) {
+        if (s->used == 64) {
+            zo_chacha20_block(s->key, s->counter, s->nonce, s->block);
+            s->counter += 1;
+            s->used = 0;
+        }
+        size_t take = 64 - s->used < n - done ? 64 - s->used : n - done;
+        memcpy(out + done, s->block + s->used, take);
+        s->used += (uint32_t)take;
+        done += take;
+    }
+}
+/* rng.rs:157-167 next_field: rejection above 2p */
+uint32_t zo_chacha20_next_field(zo_chacha20 *s) {
+    const uint64_t limit = (((uint64_t)1 << 32) / P) * P;
+    for (;;) {
+        uint8_t w[4];
+        zo_chacha20_fill(s, w, 4);
+        uint64_t v = get_u32(w);
+        if (v < limit) return (uint32_t)(v % P);
+    }
+}
+
+/* blind.rs:40-78 mask_coeffs: T + (x^n - 1) R, padded to a power of two */
+static uint32_t *mask_coeffs(const uint32_t *coeffs, size_t n, size_t n_rand, zo_chacha20 *rng,
+                             size_t *padded_out) {
+    size_t total = n + n_rand, padded = 1;
+    while (padded < total) padded <<= 1;
+    uint32_t *r = malloc((n_rand ? n_rand : 1) * 4);
+    for (size_t i = 0; i < n_rand; i++) r[i] = zo_chacha20_next_field(rng);
+    uint32_t *out = calloc(padded, 4);
+    for (size_t i = 0; i < n; i++) out[i] = f_add(out[i], coeffs[i]);
+    for (size_t i = 0; i < n_rand; i++) {
+        out[i + n] = f_add(out[i + n], r[i]);
+        out[i] = f_sub(out[i], r[i]);
+    }
+    free(r);
+    *padded_out = padded;
+    return out;
+}
+
+/* air.rs:439-464 prove_zk: both columns masked, then prove_from_coeffs */
+int zo_air_prove_zk(const zo_air_params *params, size_t n_rand, zo_chacha20 *rng,
+                    zo_transcript *t, uint8_t **proof, size_t *proof_len) {
+    int rc = air_validate(params);
+    if (rc) return rc;
+    if (params->num_queries > SIZE_MAX / 16) return ZO_MALFORMED_INPUT;
+    if (n_rand < 16 * params->num_queries) return ZO_MALFORMED_INPUT;
+    size_t n = params->n_steps;
+    uint32_t *a = malloc(n * 4), *b = malloc(n * 4);
+    zo_air_build_trace(params->a0, params->b0, n, a, b);
+    zo_ntt_inverse(a, n);
+    zo_ntt_inverse(b, n);
+    size_t pa = 0, pb = 0;
+    if (n + n_rand < n) { free(a); free(b); return ZO_INVALID_DOMAIN_SIZE; }
+    size_t total = n + n_rand, padded = 1;
+    while (padded < total) padded <<= 1;
+    if (padded > ((size_t)1 << TWO_ADICITY)) { free(a); free(b); return ZO_INVALID_DOMAIN_SIZE; }
+    uint32_t *ma = mask_coeffs(a, n, n_rand, rng, &pa);
+    uint32_t *mb = mask_coeffs(b, n, n_rand, rng, &pb);
+    free(a); free(b);
+    size_t m = pa * params->blowup;
+    if (pa > SIZE_MAX / params->blowup || m > ((size_t)1 << TWO_ADICITY)) {
+        free(ma); free(mb); return ZO_INVALID_DOMAIN_SIZE;
+    }
+    air_absorb_params(params, t);
+    uint32_t *lde_a = malloc(m * 4), *lde_b = malloc(m * 4);
+    zo_evaluate_on_coset(ma, pa, params->blowup, LDE_SHIFT, lde_a);
+    zo_evaluate_on_coset(mb, pb, params->blowup, LDE_SHIFT, lde_b);
+    free(ma); free(mb);
+    rc = air_prove_inner(params, lde_a, lde_b, m, n + n_rand - 1, t, proof, proof_len);
+    free(lde_a); free(lde_b);
     return rc;
 }
 

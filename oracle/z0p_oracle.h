@@ -191,6 +191,24 @@ void zo_fold_free(void *acc);
 int zo_fold_verify(const zo_fold_params *params, const uint8_t *proof, size_t proof_len,
                    zo_transcript *t);
 
+/* ChaCha20 stream (src/rng.rs, RFC 8439) and the zero-knowledge AIR prover
+ * (src/air.rs:439-464 with src/blind.rs:40-78). The state layout is the
+ * reference's fields, in order. */
+typedef struct {
+    uint8_t key[32];
+    uint8_t nonce[12];
+    uint32_t counter;
+    uint8_t block[64];
+    uint32_t used;
+} zo_chacha20;
+void zo_chacha20_block(const uint8_t key[32], uint32_t counter, const uint8_t nonce[12],
+                       uint8_t out[64]);
+void zo_chacha20_init(zo_chacha20 *s, const uint8_t key[32], const uint8_t nonce[12]);
+void zo_chacha20_fill(zo_chacha20 *s, uint8_t *out, size_t n);
+uint32_t zo_chacha20_next_field(zo_chacha20 *s);
+int zo_air_prove_zk(const zo_air_params *params, size_t n_rand, zo_chacha20 *rng,
+                    zo_transcript *t, uint8_t **proof, size_t *proof_len);
+
 void zo_free(void *p);
 /* Worker-thread cap for the parallel paths (0 = all online cores). */
 void zo_set_max_workers(size_t workers);

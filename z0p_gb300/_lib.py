@@ -35,6 +35,11 @@ class AirParams(C.Structure):
     ]
 
 
+class ChaChaState(C.Structure):
+    _fields_ = [("key", C.c_uint8 * 32), ("nonce", C.c_uint8 * 12), ("counter", C.c_uint32),
+                ("block", C.c_uint8 * 64), ("used", C.c_uint32)]
+
+
 class FriParams(C.Structure):
     _fields_ = [
         ("blowup", C.c_uint64), ("num_queries", C.c_uint64), ("final_size", C.c_uint64),
@@ -122,6 +127,12 @@ def lib():
             "z0p_gpu_ctx_profile": (C.c_int, [vp, C.c_char_p, sz, P(sz)]),
             "z0p_gpu_air_prove": (C.c_int, [vp, P(AirParams), P(TranscriptState), u8p, sz, P(sz)]),
             "z0p_gpu_range_prove": (C.c_int, [vp, P(RangeParams), P(TranscriptState), u8p, sz, P(sz)]),
+            "z0p_gpu_air_prove_with_trace": (C.c_int, [vp, P(AirParams), P(C.c_uint32), P(C.c_uint32),
+                                                       sz, P(TranscriptState), P(C.c_uint8), sz,
+                                                       P(sz)]),
+            "z0p_air_proof_size_zk": (C.c_int, [P(AirParams), sz, P(sz)]),
+            "z0p_gpu_air_prove_zk": (C.c_int, [vp, P(AirParams), sz, P(ChaChaState),
+                                               P(TranscriptState), P(C.c_uint8), sz, P(sz)]),
             "z0p_fold_params_new": (C.c_int, [C.c_uint64] * 4 + [C.c_uint32] * 3 + [P(FoldParams)]),
             "z0p_fold_params_for_security": (C.c_int, [C.c_uint64] + [C.c_uint32] * 4 + [P(FoldParams)]),
             "z0p_gpu_fold_create": (C.c_int, [vp, P(FoldParams), P(vp)]),

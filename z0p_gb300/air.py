@@ -94,6 +94,37 @@ def prove_into(params: Params, transcript: Transcript, buf, ctx=None) -> int:
     return n.value
 
 
+def prove_with_trace(params: Params, col_a, col_b, transcript: Transcript, ctx=None) -> bytes:
+    """air::prove_with_trace (src/air.rs:381-399): the caller's two columns."""
+    import numpy as np
+
+    ctx = ctx or default_context()
+    a = np.ascontiguousarray(np.asarray(col_a, dtype=np.uint32))
+    b = np.ascontiguousarray(np.asarray(col_b, dtype=np.uint32))
+    if len(a) != len(b):
+        raise ValueError("trace columns must have one length")
+    size = params.proof_size()
+    out = (C.c_uint8 * size)()
+    n = C.c_size_t()
+    u32p = C.POINTER(C.c_uint32)
+    check(lib().z0p_gpu_air_prove_with_trace(ctx.handle, C.byref(params), a.ctypes.data_as(u32p),
+                                             b.ctypes.data_as(u32p), len(a),
+                                             C.byref(transcript.state), out, size, C.byref(n)))
+    return bytes(out)[: n.value]
+
+
+def prove_zk(params: Params, n_rand: int, rng, transcript: Transcript, ctx=None) -> bytes:
+    """air::prove_zk (src/air.rs:439-464): `rng` is a z0p_gb300.rng.ChaCha20."""
+    ctx = ctx or default_context()
+    n = C.c_size_t()
+    check(lib().z0p_air_proof_size_zk(C.byref(params), n_rand, C.byref(n)))
+    size = n.value
+    out = (C.c_uint8 * size)()
+    check(lib().z0p_gpu_air_prove_zk(ctx.handle, C.byref(params), n_rand, C.byref(rng),
+                                     C.byref(transcript.state), out, size, C.byref(n)))
+    return bytes(out)[: n.value]
+
+
 def prove_group(params_list, transcripts, ctx=None):
     """Proves statements of one shape in lockstep (one launch sequence and one
     set of host round trips for the group); proof i equals prove(params_list[i],

@@ -438,5 +438,58 @@ uint64_t fri_bytes(const FriShape& s, uint64_t q) {
   return total + q * per_query;
 }
 
+// ---------------------------------------------------------------- ChaCha20 ----
+// RFC 8439 section 2.3: 20 rounds (10 column/diagonal double rounds) over the
+// constant, key, counter and nonce words, plus the input (src/rng.rs:22-73).
+static inline uint32_t rotl32(uint32_t x, int n) { return (x << n) | (x >> (32 - n)); }
+static inline void chacha_qr(uint32_t* x, int a, int b, int c, int d) {
+  x[a] += x[b]; x[d] = rotl32(x[d] ^ x[a], 16);
+  x[c] += x[d]; x[b] = rotl32(x[b] ^ x[c], 12);
+  x[a] += x[b]; x[d] = rotl32(x[d] ^ x[a], 8);
+  x[c] += x[d]; x[b] = rotl32(x[b] ^ x[c], 7);
+}
+void chacha20_block(const uint8_t key[32], uint32_t counter, const uint8_t nonce[12],
+                    uint8_t out[64]) {
+  uint32_t in[16] = {0x61707865u, 0x3320646eu, 0x79622d32u, 0x6b206574u};
+  for (int i = 0; i < 8; i++) in[4 + i] = le32(key + 4 * i);
+  in[12] = counter;
+  for (int i = 0; i < 3; i++) in[13 + i] = le32(nonce + 4 * i);
+  uint32_t x[16];
+  for (int i = 0; i < 16; i++) x[i] = in[i];
+  for (int r = 0; r < 10; r++) {
+    chacha_qr(x, 0, 4, 8, 12); chacha_qr(x, 1, 5, 9, 13);
+    chacha_qr(x, 2, 6, 10, 14); chacha_qr(x, 3, 7, 11, 15);
+    chacha_qr(x, 0, 5, 10, 15); chacha_qr(x, 1, 6, 11, 12);
+    chacha_qr(x, 2, 7, 8, 13); chacha_qr(x, 3, 4, 9, 14);
+  }
+  for (int i = 0; i < 16; i++) {
+    const uint32_t v = x[i] + in[i];
+    for (int b = 0; b < 4; b++) out[4 * i + b] = (uint8_t)(v >> (8 * b));
+  }
+}
+void chacha20_fill(z0p_chacha20_state* s, uint8_t* out, size_t n) {  // src/rng.rs:115-131
+  size_t done = 0;
+  while (done < n) {
+    if (s->used >= 64) {
+      chacha20_block(s->key, s->counter, s->nonce, s->block);
+      s->counter += 1;
+      s->used = 0;
+    }
+    size_t take = 64 - s->used < n - done ? 64 - s->used : n - done;
+    for (size_t i = 0; i < take; i++) out[done + i] = s->block[s->used + i];
+    s->used += (uint32_t)take;
+    done += take;
+  }
+}
+uint32_t chacha20_next_field(z0p_chacha20_state* s) {  // src/rng.rs:157-167
+  const uint64_t limit = ((1ull << 32) / P) * P;
+  for (;;) {
+    uint8_t w[4];
+    chacha20_fill(s, w, 4);
+    const uint64_t v = le32(w);
+    if (v < limit) return (uint32_t)(v % P);
+  }
+}
+
 }  // namespace host
 }  // namespace z0p

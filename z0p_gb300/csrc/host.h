@@ -109,5 +109,11 @@ uint64_t fri_bytes(const FriShape& s, uint64_t q);  // commitment + proof bodies
 
 void set_reason(const std::string& r);
 
+// ChaCha20 (RFC 8439) stream over the C-ABI state (src/rng.rs:40-167).
+void chacha20_block(const uint8_t key[32], uint32_t counter, const uint8_t nonce[12],
+                    uint8_t out[64]);
+void chacha20_fill(z0p_chacha20_state* s, uint8_t* out, size_t n);
+uint32_t chacha20_next_field(z0p_chacha20_state* s);  // rejection above 2p
+
 }  // namespace host
 }  // namespace z0p

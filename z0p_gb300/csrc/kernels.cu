@@ -499,7 +499,7 @@ __global__ void __launch_bounds__(kTraceLeafThreads) air_trace_leaves_kernel(
     const uint32_t* __restrict__ lde_a, const uint32_t* __restrict__ cb, uint32_t w_last_m,
     uint32_t* __restrict__ leaves, uint32_t* __restrict__ tinv, uint32_t logN, uint32_t logB,
     uint32_t nleaves, uint32_t top, uint32_t* cap, unsigned int* counter, uint64_t tree_stride,
-    uint64_t cap_stride, Tables tb) {
+    uint64_t cap_stride, const uint32_t* __restrict__ lde_b, Tables tb) {
   __shared__ uint32_t buf[2 * kTraceLeafThreads * 9];  // >= 2 * 9 * (kFuseMaxLeaves / 256) roots
   {
     const uint32_t pk = blockIdx.y;  // proof of the group
@@ -532,7 +532,8 @@ __global__ void __launch_bounds__(kTraceLeafThreads) air_trace_leaves_kernel(
     uint32_t k = 8u * L + r;
     uint32_t j = k & ((1u << logB) - 1u), q = k >> logB;
     m[2 * r] = __ldg(lde_a + ((size_t)j << logN) + q);
-    m[2 * r + 1] = linked_b(lde_a, logN, j, q, __ldg(cb + j), den[r]);
+    m[2 * r + 1] = lde_b ? __ldg(lde_b + ((size_t)j << logN) + q)
+                         : linked_b(lde_a, logN, j, q, __ldg(cb + j), den[r]);
     tinv[((size_t)j << logN) + q] = den[r];
   }
   blake3_leaf64(m, d);
@@ -851,6 +852,78 @@ __global__ void __launch_bounds__(kThreads) range_compose_leaves_kernel(RangeCom
       x = fadd(x, mmul(bound, __ldg(ab + e)));
       leaf[4 * t + e] = x;
     }
+  }
+  uint4* dst = reinterpret_cast<uint4*>(a.layer0 + 16 * (size_t)P);
+#pragma unroll
+  for (int t = 0; t < 4; t++)
+    dst[t] = make_uint4(leaf[4 * t], leaf[4 * t + 1], leaf[4 * t + 2], leaf[4 * t + 3]);
+  uint32_t d[8];
+  blake3_leaf64(leaf, d);
+  store_digest(a.leaves + 8 * (size_t)P, d);
+}
+
+// -------------------------------------------- general two-column AIR ----
+// air::prove_zk's masking (src/blind.rs:40-78) on coefficients that already
+// carry the coset twist 31^k: plane c of `out` (padded words) is
+//   c_k 31^k - r_k 31^k [k < n_rand] + r_(k-n) 31^k [n <= k < n + n_rand],
+// zero beyond, i.e. T + (x^n - 1) R with R = r[c] (canonical, n_rand words).
+__global__ void mask_pad_kernel(const uint32_t* __restrict__ coeffs, const uint32_t* __restrict__ r,
+                                uint32_t* __restrict__ out, uint32_t n, uint32_t n_rand,
+                                uint32_t padded, Tables tb) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x, c = blockIdx.y;
+  if (k >= padded) return;
+  uint32_t v = k < n ? coeffs[(size_t)c * n + k] : 0u;
+  const uint32_t g = gamma_pow(tb, k);
+  if (k < n_rand) v = fsub(v, mmul(r[(size_t)c * n_rand + k], g));
+  if (k >= n && k - n < n_rand) v = fadd(v, mmul(r[(size_t)c * n_rand + (k - n)], g));
+  out[(size_t)c * padded + k] = v;
+}
+
+// AIR composition on two committed columns (src/air.rs:847-929 with
+// cols[1] its own LDE, the prove_with_trace / prove_zk path): quad P as in
+// air_compose_leaves_kernel, over an LDE of B cosets of N' = 2^logN rows whose
+// next trace row is r = N' / n rows further in a coset (r = 1 unpadded).
+//   1/z_trans = (x - w_last) / (x^n - 1),  x^n periodic in q with period r
+//   1/(x - w_last) = T(q),  1/(x - 1) = omega_n^-1 T(q - r)  (in alpha_2, alpha_3)
+__global__ void __launch_bounds__(kThreads) air_compose_general_kernel(AirComposeArgs a,
+                                                                       const uint32_t* lde_b,
+                                                                       uint32_t r, Tables tb) {
+  const uint32_t logm = a.logN + a.logB;
+  const uint32_t quarter = 1u << (logm - 2);
+  const uint32_t u = blockIdx.x * blockDim.x + threadIdx.x;
+  if (u >= quarter) return;
+  const uint32_t N = 1u << a.logN, B = 1u << a.logB;
+  uint32_t k0 = u;
+  if (a.logN >= 2) {
+    const uint32_t j = u >> (a.logN - 2), q0 = u & ((N >> 2) - 1u);
+    k0 = (q0 << a.logB) | j;
+  }
+  const uint32_t P = brev_bits(k0, logm - 2);
+  uint32_t xs[4];
+  quad_points(tb, k0, logm, xs);
+  const ProofConsts& pc = g_consts[a.slot];
+  uint32_t leaf[16];
+#pragma unroll
+  for (int s = 0; s < 4; s++) {
+    const uint32_t k = k0 + (uint32_t)s * quarter;
+    const uint32_t j = k & (B - 1u), q = k >> a.logB;
+    const size_t base = (size_t)j << a.logN;
+    const uint32_t qn = (q + r) & (N - 1u), qm = (q - r) & (N - 1u);
+    const uint32_t av = __ldg(a.lde_a + base + q), bv = __ldg(lde_b + base + q);
+    const uint32_t an = __ldg(a.lde_a + base + qn), bn = __ldg(lde_b + base + qn);
+    const uint32_t tm = __ldg(a.tinv + base + qm), t0 = __ldg(a.tinv + base + q);
+    const uint32_t iz = mmul(fsub_lazy(xs[s], a.w_last_m), __ldg(a.zinv + j * r + (q & (r - 1u))));
+    const uint32_t t1 = mmul(fsub_lazy(an, bv), iz);
+    const uint32_t t2 = mmul(fsub_lazy(bn, fadd(av, bv)), iz);
+    const uint32_t ba = mmul(fsub_lazy(av, pc.a0), tm);
+    const uint32_t bb = mmul(fsub_lazy(bv, pc.b0), tm);
+    const uint32_t bo = mmul(fsub_lazy(bv, pc.b_last), t0);
+    const int t = (s == 1) ? 2 : (s == 2) ? 1 : s;  // position 4P + brev2(s)
+#pragma unroll
+    for (int c = 0; c < 4; c++)
+      leaf[4 * t + c] = fadd(mdot4(t1, pc.alpha[c][0], t2, pc.alpha[c][1], ba, pc.alpha[c][2], bb,
+                                   pc.alpha[c][3]),
+                             mmul(bo, pc.alpha[c][4]));
   }
   uint4* dst = reinterpret_cast<uint4*>(a.layer0 + 16 * (size_t)P);
 #pragma unroll
@@ -1317,8 +1390,9 @@ __global__ void __launch_bounds__(128) openings_kernel(OpenArgs a) {
   if (a.ncol == 0) {
     // AIR: rows base..base+7 of `index` and of `index + B`, A || B each, with
     // B = A(q+1) + C_j * tinv[j][q] (the linked column).
+    const uint64_t shift = a.shift ? a.shift : B;
     for (uint32_t h = 0; h < 2; h++) {
-      const uint64_t at = h ? (index + B) % m : index;
+      const uint64_t at = h ? (index + shift) % m : index;
       const uint64_t base = at & ~7ull;
       uint32_t* oh = o + h * (16 + 8 * a.tsteps);
       for (uint32_t t = threadIdx.x; t < 16 + 8 * a.tsteps; t += blockDim.x) {
@@ -1327,7 +1401,9 @@ __global__ void __launch_bounds__(128) openings_kernel(OpenArgs a) {
           const uint32_t j = k & (B - 1u), q = k >> a.logB;
           const size_t cj = (size_t)j << a.logN;
           uint32_t v = a.lde[cj + q];
-          if (t & 1u) v = fadd(a.lde[cj + ((q + 1u) & (N - 1u))], mmul(a.cb[j], a.tinv[cj + q]));
+          if (t & 1u)
+            v = a.lde_b ? a.lde_b[cj + q]
+                        : fadd(a.lde[cj + ((q + 1u) & (N - 1u))], mmul(a.cb[j], a.tinv[cj + q]));
           oh[t] = v;
         } else {
           const uint32_t st = (t - 16) >> 3, w = (t - 16) & 7u;
@@ -1525,7 +1601,8 @@ cudaError_t air_trace_leaves(cudaStream_t st, const Tables& tb, const uint32_t* 
                              const uint32_t* cb, uint32_t w_last_m, uint32_t* leaves,
                              uint32_t* tinv, uint32_t logN, uint32_t logB, uint32_t top,
                              uint32_t* cap, unsigned int* counter, uint32_t* levels,
-                             uint32_t nproofs, uint64_t tree_stride, uint64_t cap_stride) {
+                             uint32_t nproofs, uint64_t tree_stride, uint64_t cap_stride,
+                             const uint32_t* lde_b) {
   uint32_t nleaves = 1u << (logN + logB - 3);
   if (nleaves > kFuseMaxLeaves) {
     top = 0;  // no subtree; merkle_build does every level
@@ -1538,7 +1615,7 @@ cudaError_t air_trace_leaves(cudaStream_t st, const Tables& tb, const uint32_t* 
   stg.launched();
   air_trace_leaves_kernel<<<dim3(grid_for(nleaves, kTraceLeafThreads), nproofs), kTraceLeafThreads,
                             0, st>>>(lde_a, cb, w_last_m, leaves, tinv, logN, logB, nleaves, top, cap,
-                                     counter, tree_stride, cap_stride, tb);
+                                     counter, tree_stride, cap_stride, lde_b, tb);
   return cudaGetLastError();
 }
 
@@ -1702,6 +1779,23 @@ cudaError_t grind(cudaStream_t st, uint32_t slot, uint32_t head_len, uint32_t bi
   Stage stg("grind", st);
   stg.launched();
   grind_kernel<<<dim3(ctas, nproofs), kGrindThreads, 0, st>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t mask_pad(cudaStream_t st, const Tables& tb, const uint32_t* coeffs, const uint32_t* r,
+                     uint32_t* out, uint32_t n, uint32_t n_rand, uint32_t padded) {
+  Stage stg("mask_pad", st);
+  stg.launched();
+  mask_pad_kernel<<<dim3(grid_for(padded), 2), kThreads, 0, st>>>(coeffs, r, out, n, n_rand, padded, tb);
+  return cudaGetLastError();
+}
+
+cudaError_t air_compose_general(cudaStream_t st, const Tables& tb, const AirComposeArgs& a,
+                                const uint32_t* lde_b, uint32_t r) {
+  Stage stg("air_compose_leaves", st);
+  stg.launched();
+  air_compose_general_kernel<<<grid_for(1ull << (a.logN + a.logB - 2)), kThreads, 0, st>>>(a, lde_b, r,
+                                                                                        tb);
   return cudaGetLastError();
 }
 

@@ -127,6 +127,10 @@ struct OpenArgs {
   uint32_t tsteps, logN, logB;
   uint32_t ncol;            // 0 for the AIR, else the range AIR's column count
   uint32_t no_trace = 0;    // 1: FRI openings only (a FRI commitment on its own)
+  // AIR with two committed columns: column B's own LDE (nullptr: linked B)
+  // and the next-row distance in LDE index units (0: B).
+  const uint32_t* lde_b = nullptr;
+  uint64_t shift = 0;
   // Per-proof strides (words) for a proof group: FRI layer values and trees,
   // trace LDE and trace tree (cb and tinv follow from B and m).
   uint64_t fri_val_stride = 0, fri_tree_stride = 0, lde_stride = 0, ttree_stride = 0;
@@ -207,12 +211,23 @@ cudaError_t coset_zinv(cudaStream_t st, const Tables& tb, uint32_t* zinv, uint32
 // to `cap`), and with `counter` (one zero device word per proof) its last CTA
 // finishes the tree up to `top`. *levels receives how many levels above the
 // leaves are done, the start level for merkle_build.
+// With `lde_b`, column B is read from its own LDE (same layout) instead of
+// being derived from A.
 cudaError_t air_trace_leaves(cudaStream_t st, const Tables& tb, const uint32_t* lde_a,
                              const uint32_t* cb, uint32_t w_last_m, uint32_t* leaves,
                              uint32_t* tinv, uint32_t logN, uint32_t logB, uint32_t top,
                              uint32_t* cap, unsigned int* counter, uint32_t* levels,
                              uint32_t nproofs = 1, uint64_t tree_stride = 0,
-                             uint64_t cap_stride = 0);
+                             uint64_t cap_stride = 0, const uint32_t* lde_b = nullptr);
+// air::prove_zk masking of both columns' twisted coefficients into planes of
+// `padded` words (r: 2 x n_rand canonical masking values).
+cudaError_t mask_pad(cudaStream_t st, const Tables& tb, const uint32_t* coeffs, const uint32_t* r,
+                     uint32_t* out, uint32_t n, uint32_t n_rand, uint32_t padded);
+// Composition with column B from its own LDE (next row r rows further in a
+// coset; a.zinv holds B x r values 1/(x^n - 1)); the slot's alpha[.][0..4]
+// are alpha_0..alpha_4 with alpha_2, alpha_3 times omega_n^-1.
+cudaError_t air_compose_general(cudaStream_t st, const Tables& tb, const AirComposeArgs& a,
+                                const uint32_t* lde_b, uint32_t r);
 cudaError_t range_trace_leaves(cudaStream_t st, const uint32_t* lde, uint32_t* leaves,
                                uint32_t logN, uint32_t logB, uint32_t ncols, uint32_t nproofs = 1,
                                uint64_t tree_stride = 0);

@@ -778,6 +778,201 @@ int check_group(const T* tasks, uint32_t K, Shape shape, Size size, Same same, F
   return Z0P_OK;
 }
 
+// air::prove_with_trace / prove_zk (src/air.rs:381-399, 439-464) through
+// prove_inner (:485-599) with column B committed on its own: both columns
+// interpolated (caller's columns, or the Fibonacci trace), masked and padded
+// to Lp = 2^ceil(log2(n + n_rand)) coefficients when n_rand > 0, extended to
+// m = Lp * blowup, tree over 8-row A || B leaves, the general composition
+// (next row m / n further), the FRI and the openings at index and index + m/n.
+struct GeneralAir {
+  const uint32_t* host_a = nullptr;  // caller's columns (prove_with_trace), else the trace
+  const uint32_t* host_b = nullptr;
+  uint64_t n_rand = 0;
+  const uint32_t* rand = nullptr;    // 2 x n_rand canonical masking values
+};
+
+uint64_t padded_len(uint64_t n, uint64_t n_rand) {
+  uint64_t total = n + n_rand, lp = 1;
+  while (lp < total) lp <<= 1;
+  return lp;
+}
+
+int general_shape(const z0p_air_params& p, uint64_t n_rand, FriParams* fp, FriShape* s) {
+  RC(air_validate(p));
+  if (n_rand > (1ull << 27)) return Z0P_ERR_INVALID_DOMAIN_SIZE;
+  const uint64_t lp = padded_len(p.n_steps, n_rand);
+  if (lp > (1ull << 27)) return Z0P_ERR_INVALID_DOMAIN_SIZE;   // src/blind.rs:62-64
+  if (lp > (1ull << 27) / p.blowup) return Z0P_ERR_INVALID_DOMAIN_SIZE;  // src/ntt.rs:347-352
+  RC(fri_params_new(p.blowup, p.num_queries, p.final_size, fp));
+  fp->grinding_bits = p.grinding_bits;
+  fp->cap_height = p.cap_height;
+  return fri_shape(lp * p.blowup, p.n_steps + n_rand - 1, *fp, s);
+}
+
+int air_prove_general(z0p_gpu_ctx* c, const z0p_air_params& p, const GeneralAir& g,
+                      z0p_transcript_state* tsp, uint8_t* out) {
+  FriParams fp;
+  FriShape s;
+  RC(general_shape(p, g.n_rand, &fp, &s));
+  const uint64_t N = p.n_steps, B = p.blowup, Lp = padded_len(N, g.n_rand), m = Lp * B;
+  const uint32_t logN = log2u(N), logL = log2u(Lp), logB = log2u(B), logm = logL + logB;
+  const uint32_t r = (uint32_t)(Lp / N);
+  const uint64_t need = air_size(p, s);
+  cudaStream_t st = c->stream;
+  RC(ensure(c, c->cols, 8 * N));
+  RC(ensure(c, c->coeffs, 8 * (N + Lp)));
+  RC(ensure(c, c->scratch, 8 * m));
+  RC(ensure(c, c->lde, 8 * m));
+  const uint64_t tleaves = m / 8, ttree_words = 8 * tree_digests(tleaves);
+  RC(ensure(c, c->ttree, 4 * ttree_words));
+  RC(ensure(c, c->misc, 64 + 4 * B * r + 8 * g.n_rand));
+  FriBufs fb;
+  RC(plan_fri_buffers(c, s, 1, &fb));
+  const uint32_t tdepth = log2u(tleaves);
+  const uint32_t tdrop = p.cap_height < tdepth ? (uint32_t)p.cap_height : tdepth;
+  const uint32_t tsteps = tdepth - tdrop;
+  HioPlan h;
+  RC(plan_hio(c, s, p.num_queries, tdrop, 2 * (16 + 8 * tsteps), 1, &h, 16));
+  uint32_t* cols = (uint32_t*)c->cols.p;
+  uint32_t* coeffs = (uint32_t*)c->coeffs.p;
+  uint32_t* padded = coeffs + 2 * N;
+  uint32_t* lde_a = (uint32_t*)c->lde.p;
+  uint32_t* lde_b = lde_a + m;
+  uint32_t* ttree = (uint32_t*)c->ttree.p;
+  uint32_t* zinv = (uint32_t*)c->misc.p + 16;
+  uint32_t* rdev = zinv + B * r;
+  unsigned int* bad_h = reinterpret_cast<unsigned int*>(c->hio + h.extra);
+  *bad_h = 0;
+  z0p_transcript_state work = *tsp;
+  Transcript t(&work);
+  {  // absorb_params (src/air.rs:754-766)
+    uint8_t pb[56];
+    auto p64 = [&](int off, uint64_t v) { for (int i = 0; i < 8; i++) pb[off + i] = (uint8_t)(v >> (8 * i)); };
+    auto p32 = [&](int off, uint32_t v) { for (int i = 0; i < 4; i++) pb[off + i] = (uint8_t)(v >> (8 * i)); };
+    p64(0, p.n_steps); p64(8, p.blowup); p64(16, p.num_queries); p64(24, p.final_size);
+    p32(32, p.grinding_bits); p64(36, p.cap_height); p32(44, p.a0); p32(48, p.b0); p32(52, p.b_last);
+    transcript_absorb(t, "fib/params", pb, 56);
+  }
+  ProofConsts& pc = c->consts[0];
+  pc.a0 = p.a0; pc.b0 = p.b0; pc.b_last = p.b_last;
+  CK(push_consts(c, 1));
+  if (g.host_a) {
+    CK(cudaMemcpyAsync(cols, g.host_a, 4 * N, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(cols + N, g.host_b, 4 * N, cudaMemcpyHostToDevice, st));
+    c->h2d += 8 * N;
+    CK(launch::check_canonical(st, cols, 2 * N, hio_dev<unsigned int>(c, h.extra)));
+  } else {
+    uint32_t mats[32][4];
+    fib_mats(mats);
+    CK(launch::fib_trace(st, cols, cols + N, (uint32_t)N, (uint32_t)c->slot, mats, 1));
+  }
+  NttPlan ip;  // interpolate both columns; outputs times 31^i / ... (coset twist included)
+  ip.logn = logN; ip.batch = 2; ip.inverse = 1; ip.post_gamma = 1;
+  CK(launch::ntt(st, c->tb, ip, cols, coeffs, (uint32_t*)c->scratch.p));
+  const uint32_t* lde_in = coeffs;
+  if (Lp != N || g.n_rand) {  // T + (x^n - 1) R, zero-padded (src/blind.rs:40-78)
+    if (g.n_rand) {
+      CK(cudaMemcpyAsync(rdev, g.rand, 8 * g.n_rand, cudaMemcpyHostToDevice, st));
+      c->h2d += 8 * g.n_rand;
+    }
+    CK(launch::mask_pad(st, c->tb, coeffs, rdev, padded, (uint32_t)N, (uint32_t)g.n_rand,
+                        (uint32_t)Lp));
+    lde_in = padded;
+  }
+  NttPlan lp;
+  lp.logn = logL; lp.batch = (uint32_t)(2 * B); lp.in_div = (uint32_t)B; lp.twist_mod = (uint32_t)B;
+  lp.twist_shift = 27 - logm;
+  CK(launch::ntt(st, c->tb, lp, lde_in, lde_a, (uint32_t*)c->scratch.p));
+  // 1/(x^n - 1) per coset j and q mod r: x^n = (31 omega_m^j omega_Lp^q)^n.
+  const uint32_t omega_n = two_adic_generator(logN);
+  const uint32_t w_last = fpow(omega_n, N - 1);
+  {
+    std::vector<uint32_t> zt(B * r);
+    const uint32_t omega_m = two_adic_generator(logm), omega_l = two_adic_generator(logL);
+    for (uint64_t j = 0; j < B; j++)
+      for (uint32_t q = 0; q < r; q++) {
+        const uint32_t x = fmul(fmul(GENERATOR, fpow(omega_m, j)), fpow(omega_l, q));
+        zt[j * r + q] = to_mont(finv(fsub(fpow(x, N), 1)));
+      }
+    CK(cudaMemcpyAsync(zinv, zt.data(), 4 * B * r, cudaMemcpyHostToDevice, st));
+  }
+  // Joint trace tree over 8-row A || B leaves (src/air.rs:520-537) and T.
+  uint32_t* tinv = (uint32_t*)c->scratch.p;
+  uint32_t built = 0;
+  CK(launch::air_trace_leaves(st, c->tb, lde_a, nullptr, to_mont(w_last), ttree, tinv, logL, logB,
+                              tsteps, hio_dev<uint32_t>(c, h.trace_cap), merkle_counter(c), &built,
+                              1, ttree_words, h.trace_cap_bytes / 4, lde_b));
+  if (built < tsteps || (tsteps == 0 && tleaves > kFuseMaxLeaves))
+    CK(launch::merkle_build(st, ttree, tleaves, tsteps, merkle_counter(c),
+                            hio_dev<uint32_t>(c, h.trace_cap), built, 1, ttree_words,
+                            h.trace_cap_bytes / 4));
+  CK(sync(c, "cap"));
+  if (*reinterpret_cast<volatile unsigned int*>(bad_h)) {
+    set_reason("field elements must be canonical (< p)");
+    return Z0P_ERR_MALFORMED_INPUT;
+  }
+  std::vector<uint8_t> column_cap(c->hio + h.trace_cap, c->hio + h.trace_cap + h.trace_cap_bytes);
+  c->d2h += h.trace_cap_bytes;
+  transcript_absorb(t, "fib/trace", column_cap.data(), column_cap.size());
+  uint32_t alpha[5][4];
+  for (int i = 0; i < 5; i++) challenge_ext(t, "fib/alpha", alpha[i]);
+  const uint32_t omega_inv = finv(omega_n);
+  for (int e = 0; e < 4; e++) {
+    pc.alpha[e][0] = to_mont(alpha[0][e]);
+    pc.alpha[e][1] = to_mont(alpha[1][e]);
+    pc.alpha[e][2] = to_mont(fmul(alpha[2][e], omega_inv));
+    pc.alpha[e][3] = to_mont(fmul(alpha[3][e], omega_inv));
+    pc.alpha[e][4] = to_mont(alpha[4][e]);
+  }
+  CK(push_consts(c, 1));
+  AirComposeArgs ca;
+  ca.lde_a = lde_a; ca.cb = nullptr; ca.zinv = zinv; ca.tinv = tinv;
+  ca.layer0 = fb.layer[0]; ca.leaves = fb.tree[0];
+  ca.logN = logL; ca.logB = logB;
+  ca.w_last_m = to_mont(w_last);
+  ca.slot = (uint32_t)c->slot;
+  CK(launch::air_compose_general(st, c->tb, ca, lde_b, r));
+  CK(launch::merkle_build(st, fb.tree[0], s.leaves[0], s.depth[0] - s.drop[0], merkle_counter(c),
+                          hio_dev<uint32_t>(c, h.fri_cap[0]), 0, 1, fb.tree_stride,
+                          h.fri_cap_bytes[0] / 4));
+  Transcript* ts[1] = {&t};
+  FriOut fo;
+  RC(run_fri(c, s, fp, fb, m, N + g.n_rand - 1, ts, 1, h, &fo));
+  const uint64_t offset = m / N;
+  OpenArgs oa{};
+  oa.lde = lde_a; oa.lde_b = lde_b; oa.shift = offset;
+  oa.ttree = ttree; oa.tleaves = tleaves; oa.tsteps = tsteps;
+  oa.logN = logL; oa.logB = logB; oa.ncol = 0;
+  RC(run_openings(c, s, fb, h, &fo, 1, oa));
+  Writer w(out, need);  // air::Proof::to_bytes (src/air.rs:262-281)
+  w.byte(6);
+  w.u32((uint32_t)(column_cap.size() / 32));
+  w.bytes(column_cap.data(), column_cap.size());
+  write_fri(w, c, s, fo, m, N + g.n_rand - 1, h, 0);
+  w.u32((uint32_t)fo.indices.size());
+  for (size_t qi = 0; qi < fo.indices.size(); qi++) {
+    const uint64_t index = brev(fo.indices[qi], logm);
+    const uint64_t shifted = (index + offset) % m;
+    const uint32_t* rows = open_block(c, h, 0, qi) + h.trace_off;
+    const uint32_t* srows = rows + 16 + 8 * tsteps;
+    w.u64(index);
+    w.u32(rows[2 * (index & 7)]);
+    w.u32(rows[2 * (index & 7) + 1]);
+    w.u32(srows[2 * (shifted & 7)]);
+    w.u32(srows[2 * (shifted & 7) + 1]);
+    write_path(w, (const uint8_t*)(rows + 16), index / 8, tsteps);
+    write_path(w, (const uint8_t*)(srows + 16), shifted / 8, tsteps);
+    w.bytes(rows, 64);
+    w.bytes(srows, 64);
+  }
+  if (w.n != need) {
+    set_reason("internal error: proof length differs from its shape");
+    return Z0P_ERR_CUDA;
+  }
+  *tsp = work;
+  return Z0P_OK;
+}
+
 // src/air.rs:365-372 -> 485-599 on the device, for K proofs of one shape in
 // lockstep: every launch covers the group (grid y = proof) and every
 // Fiat-Shamir round trip serves it.
@@ -1819,6 +2014,81 @@ int z0p_gpu_fri_open(z0p_gpu_ctx* c, z0p_transcript_state* t, uint8_t* out, size
   RC(with_device(c));
   ProfileScope ps(c);
   return fri_open(c, t, out, indices);
+}
+
+int z0p_gpu_air_prove_with_trace(z0p_gpu_ctx* c, const z0p_air_params* p, const uint32_t* col_a,
+                                 const uint32_t* col_b, size_t len, z0p_transcript_state* t,
+                                 uint8_t* out, size_t cap, size_t* out_len) {
+  if (!c || !p || !t || !col_a || !col_b) return Z0P_ERR_INVALID_ARGUMENT;
+  FriParams fp;
+  FriShape s;
+  RC(general_shape(*p, 0, &fp, &s));
+  if (len != p->n_steps) {  // src/air.rs:389-394
+    set_reason("trace columns must match n_steps");
+    return Z0P_ERR_MALFORMED_INPUT;
+  }
+  const uint64_t need = air_size(*p, s);
+  if (out_len) *out_len = need;
+  if (!out || cap < need) {
+    set_reason("output buffer too small for the proof");
+    return Z0P_ERR_BUFFER_TOO_SMALL;
+  }
+  std::lock_guard<std::mutex> lk(c->mu);
+  c->work_serial++;
+  RC(with_device(c));
+  ProfileScope ps(c);
+  GeneralAir g;
+  g.host_a = col_a;
+  g.host_b = col_b;
+  return air_prove_general(c, *p, g, t, out);
+}
+
+int z0p_air_proof_size_zk(const z0p_air_params* p, size_t n_rand, size_t* len) {
+  if (!p || !len) return Z0P_ERR_INVALID_ARGUMENT;
+  FriParams fp;
+  FriShape s;
+  RC(general_shape(*p, n_rand, &fp, &s));
+  *len = air_size(*p, s);
+  return Z0P_OK;
+}
+
+int z0p_gpu_air_prove_zk(z0p_gpu_ctx* c, const z0p_air_params* p, size_t n_rand,
+                         z0p_chacha20_state* rng, z0p_transcript_state* t, uint8_t* out,
+                         size_t cap, size_t* out_len) {
+  if (!c || !p || !t || !rng || rng->used > 64) return Z0P_ERR_INVALID_ARGUMENT;
+  RC(air_validate(*p));  // src/air.rs:445-458: the hiding budget first
+  if (p->num_queries > SIZE_MAX / 16) {
+    set_reason("query budget overflows the hiding requirement");
+    return Z0P_ERR_MALFORMED_INPUT;
+  }
+  if (n_rand < 16 * p->num_queries) {
+    set_reason("n_rand must cover every revealed leaf row for hiding");
+    return Z0P_ERR_MALFORMED_INPUT;
+  }
+  FriParams fp;
+  FriShape s;
+  RC(general_shape(*p, n_rand, &fp, &s));
+  const uint64_t need = air_size(*p, s);
+  if (out_len) *out_len = need;
+  if (!out || cap < need) {
+    set_reason("output buffer too small for the proof");
+    return Z0P_ERR_BUFFER_TOO_SMALL;
+  }
+  // Masking values: n_rand for column A, then n_rand for column B
+  // (src/air.rs:461-462, src/blind.rs:65), on a copy of the stream.
+  z0p_chacha20_state r = *rng;
+  std::vector<uint32_t> rand(2 * n_rand);
+  for (auto& v : rand) v = chacha20_next_field(&r);
+  std::lock_guard<std::mutex> lk(c->mu);
+  c->work_serial++;
+  RC(with_device(c));
+  ProfileScope ps(c);
+  GeneralAir g;
+  g.n_rand = n_rand;
+  g.rand = rand.data();
+  RC(air_prove_general(c, *p, g, t, out));
+  *rng = r;
+  return Z0P_OK;
 }
 
 int z0p_fold_params_new(uint64_t seg_steps, uint64_t blowup, uint64_t num_queries,
