@@ -282,6 +282,33 @@ def run_fri_pcs(Z, ctx, reps=5):
             "rows": rows}
 
 
+def run_table(Z, ctx, reps=5):
+    """Table membership (table::prove): the reference's `table 4-entry` row
+    (docs/benchmarks.md:125; workload of benches/speed_size.rs:301-305) and a
+    2^20-row column against a 4-entry table at for_security(100). Host table in,
+    proof bytes out, per call."""
+    rows = []
+    table = [10, 20, 30, 40]
+    for n, label, ref_ms, ref_bytes in [(8, b"bench/table", 0.04, 4673),
+                                        (1 << 20, b"bench/table-2p20", None, None)]:
+        if n == 8:
+            params = Z.table.Params.new(8, 8, 8, 4, 30)
+        else:
+            params = Z.table.Params.for_security(n, len(table), 30, 100)
+        times, size = [], 0
+        for _ in range(reps + 1):
+            t = Z.Transcript(label)
+            t0 = time.perf_counter()
+            proof = Z.table.prove(params, table, t, ctx)
+            times.append(time.perf_counter() - t0)
+            size = len(proof)
+        ms = 1e3 * sorted(times[1:])[len(times[1:]) // 2]
+        rows.append({"n_rows": n, "lde_len": n * params.blowup, "ms": round(ms, 4), "bytes": size,
+                     "reference_ms_16_cores": ref_ms, "reference_bytes": ref_bytes,
+                     "bytes_match_reference": None if ref_bytes is None else size == ref_bytes})
+    return {"workload": "constant column in a 4-entry table [10, 20, 30, 40], value 30", "rows": rows}
+
+
 def run_fold_ivc(Z, ctx, reps=3):
     """Folded IVC (fold::Accumulator): the reference's `fold 4x8 fib` row
     (docs/benchmarks.md:127; workload of benches/speed_size.rs:432-449) and
@@ -508,12 +535,13 @@ def run_gpu(args):
         prof = ctx.profile()
         ctx.set_profiling(False)
 
-    batched = served = fri_pcs = fold_ivc = None
+    batched = served = fri_pcs = fold_ivc = table_row = None
     if not args.quick and ws == 1:
         batched = run_batched(Z, ctx)
         served = run_served(Z, ctx)
         fri_pcs = run_fri_pcs(Z, ctx)
         fold_ivc = run_fold_ivc(Z, ctx)
+        table_row = run_table(Z, ctx)
 
     if rank != 0:
         if dist is not None:
@@ -608,6 +636,7 @@ def run_gpu(args):
         "served": served,
         "fri_pcs": fri_pcs,
         "fold_ivc": fold_ivc,
+        "table": table_row,
     }
     print(json.dumps(line), flush=True)
     if dist is not None:

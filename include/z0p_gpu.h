@@ -12,7 +12,9 @@
  *  - Field elements are canonical BabyBear values (< 2013265921) as uint32_t.
  *  - Status codes: 0 = Ok; 1..9 mirror the variants of z0p::Error in
  *    declaration order (src/error.rs:7-40); >= 100 are backend errors.
- *    z0p_gpu_last_reason() returns a static, thread-local message.
+ *    z0p_gpu_last_reason() returns the thread-local message of the last
+ *    failure on this thread and consumes it (a second read returns ""); the
+ *    pointer stays valid until the next read on the same thread.
  *  - Proof-producing calls write into a caller-owned host buffer. When `cap`
  *    is too small they write the required size to *len and return
  *    Z0P_ERR_BUFFER_TOO_SMALL before any device work.
@@ -229,6 +231,36 @@ int z0p_air_proof_size_zk(const z0p_air_params *params, size_t n_rand, size_t *l
 int z0p_gpu_air_prove_zk(z0p_gpu_ctx *ctx, const z0p_air_params *params, size_t n_rand,
                          z0p_chacha20_state *rng, z0p_transcript_state *transcript, uint8_t *out,
                          size_t cap, size_t *out_len);
+
+/* table::Params (src/table.rs:27-45): a constant column `value` proved to lie
+ * in a public table of canonical entries. */
+typedef struct {
+    uint64_t n_rows;
+    uint64_t blowup;
+    uint64_t num_queries;
+    uint64_t final_size;
+    uint32_t grinding_bits;
+    uint64_t cap_height;
+    uint32_t value;
+} z0p_table_params;
+/* table::Params::new (src/table.rs:55-88) and ::for_security (:114-170). */
+int z0p_table_params_new(uint64_t n_rows, uint64_t blowup, uint64_t num_queries,
+                         uint64_t final_size, uint32_t value, z0p_table_params *out);
+int z0p_table_params_for_security(uint64_t n_rows, uint64_t table_len, uint32_t value,
+                                  uint32_t target_bits, z0p_table_params *out);
+/* Exact length of table::Proof::to_bytes (src/table.rs:244-262); n_rand = 0
+ * for table::prove. */
+int z0p_table_proof_size(const z0p_table_params *params, size_t table_len, size_t n_rand,
+                         size_t *len);
+/* table::prove (src/table.rs:305-317) and table::prove_zk (:329-356, n_rand
+ * >= num_queries maskers drawn from `rng`). */
+int z0p_gpu_table_prove(z0p_gpu_ctx *ctx, const z0p_table_params *params, const uint32_t *table,
+                        size_t table_len, z0p_transcript_state *transcript, uint8_t *out,
+                        size_t cap, size_t *out_len);
+int z0p_gpu_table_prove_zk(z0p_gpu_ctx *ctx, const z0p_table_params *params,
+                           const uint32_t *table, size_t table_len, size_t n_rand,
+                           z0p_chacha20_state *rng, z0p_transcript_state *transcript,
+                           uint8_t *out, size_t cap, size_t *out_len);
 
 /* Proof groups (no counterpart in the reference): n statements of one shape
  * -- the same n_steps / n_rows (and n_bits), blowup, num_queries,

@@ -83,6 +83,15 @@ def chacha20_block(key: bytes, counter: int, nonce: bytes) -> bytes:
     return bytes(out)
 
 
+class TableParams(C.Structure):
+    """table::Params (src/table.rs:27-45)."""
+    _fields_ = [
+        ("n_rows", C.c_uint64), ("blowup", C.c_uint64), ("num_queries", C.c_uint64),
+        ("final_size", C.c_uint64), ("grinding_bits", C.c_uint32), ("cap_height", C.c_uint64),
+        ("value", C.c_uint32),
+    ]
+
+
 class FoldParams(C.Structure):
     """fold::Params (src/fold.rs:42-64)."""
     _fields_ = [
@@ -178,6 +187,14 @@ def lib():
             "zo_chacha20_next_field": (C.c_uint32, [C.POINTER(ChaCha20)]),
             "zo_air_prove_zk": (C.c_int, [C.POINTER(AirParams), sz, C.POINTER(ChaCha20), vp,
                                           C.POINTER(u8p), C.POINTER(sz)]),
+            "zo_table_params_new": (C.c_int, [C.c_uint64] * 4 + [C.c_uint32, C.POINTER(TableParams)]),
+            "zo_table_for_security": (C.c_int, [C.c_uint64, C.c_uint64, C.c_uint32, C.c_uint32,
+                                                 C.POINTER(TableParams)]),
+            "zo_table_prove": (C.c_int, [C.POINTER(TableParams), u32p, sz, vp, C.POINTER(u8p),
+                                         C.POINTER(sz)]),
+            "zo_table_prove_zk": (C.c_int, [C.POINTER(TableParams), u32p, sz, sz, C.POINTER(ChaCha20),
+                                            vp, C.POINTER(u8p), C.POINTER(sz)]),
+            "zo_table_verify": (C.c_int, [C.POINTER(TableParams), u32p, sz, C.c_char_p, sz, vp]),
             "zo_fold_params_new": (C.c_int, [C.c_uint64] * 4 + [C.c_uint32] * 3 + [C.POINTER(FoldParams)]),
             "zo_fold_for_security": (C.c_int, [C.c_uint64] + [C.c_uint32] * 4 + [C.POINTER(FoldParams)]),
             "zo_fold_new": (vp, [C.POINTER(FoldParams)]),
@@ -387,6 +404,44 @@ def air_prove_zk(params: AirParams, n_rand: int, rng: ChaCha20, t: Transcript) -
     buf, n = C.POINTER(C.c_uint8)(), C.c_size_t()
     rc = lib().zo_air_prove_zk(C.byref(params), n_rand, C.byref(rng), t.h, C.byref(buf), C.byref(n))
     return _take_proof(rc, buf, n)
+
+
+def table_params_new(n_rows, blowup, num_queries, final_size, value) -> TableParams:
+    p = TableParams()
+    rc = lib().zo_table_params_new(n_rows, blowup, num_queries, final_size, value, C.byref(p))
+    if rc:
+        raise ValueError(ERRORS[rc])
+    return p
+
+
+def table_for_security(n_rows, table_len, value, target_bits) -> TableParams:
+    p = TableParams()
+    rc = lib().zo_table_for_security(n_rows, table_len, value, target_bits, C.byref(p))
+    if rc:
+        raise ValueError(ERRORS[rc])
+    return p
+
+
+def table_prove(params: TableParams, table, t: Transcript) -> bytes:
+    """table::prove (src/table.rs:305-317)."""
+    a, ap = u32arr(table)
+    buf, n = C.POINTER(C.c_uint8)(), C.c_size_t()
+    rc = lib().zo_table_prove(C.byref(params), ap, len(a), t.h, C.byref(buf), C.byref(n))
+    return _take_proof(rc, buf, n)
+
+
+def table_prove_zk(params: TableParams, table, n_rand: int, rng: "ChaCha20", t: Transcript) -> bytes:
+    """table::prove_zk (src/table.rs:329-356)."""
+    a, ap = u32arr(table)
+    buf, n = C.POINTER(C.c_uint8)(), C.c_size_t()
+    rc = lib().zo_table_prove_zk(C.byref(params), ap, len(a), n_rand, C.byref(rng), t.h,
+                                 C.byref(buf), C.byref(n))
+    return _take_proof(rc, buf, n)
+
+
+def table_verify(params: TableParams, table, proof: bytes, t: Transcript) -> int:
+    a, ap = u32arr(table)
+    return lib().zo_table_verify(C.byref(params), ap, len(a), proof, len(proof), t.h)
 
 
 def air_verify(params: AirParams, proof: bytes, t: Transcript) -> int:

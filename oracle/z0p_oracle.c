@@ -2588,6 +2588,276 @@ out:
 }
 
 /* ------------------------------------------------------------------------ */
+/* table.rs — membership of a committed value in a public table              */
+/* ------------------------------------------------------------------------ */
+
+/* table.rs:55-88 Params::new */
+int zo_table_params_new(uint64_t n_rows, uint64_t blowup, uint64_t q, uint64_t final_size,
+                        uint32_t value, zo_table_params *o) {
+    if (n_rows < 2 || !is_pow2(n_rows)) return ZO_INVALID_DOMAIN_SIZE;
+    if (blowup < 2 || !is_pow2(blowup)) return ZO_INVALID_BLOWUP;
+    if (q == 0) return ZO_NO_QUERIES;
+    if (final_size < 2 || !is_pow2(final_size)) return ZO_INVALID_DOMAIN_SIZE;
+    if (n_rows > UINT64_MAX / blowup || n_rows * blowup > MAX_DOMAIN) return ZO_INVALID_DOMAIN_SIZE;
+    o->n_rows = n_rows; o->blowup = blowup; o->num_queries = q; o->final_size = final_size;
+    o->grinding_bits = 0; o->cap_height = 0; o->value = value % P;
+    return ZO_OK;
+}
+
+/* table.rs:114-170 Params::for_security */
+int zo_table_for_security(uint64_t n_rows, uint64_t table_len, uint32_t value, uint32_t target,
+                          zo_table_params *o) {
+    if (n_rows < 2 || !is_pow2(n_rows)) return ZO_INVALID_DOMAIN_SIZE;
+    if (table_len < 2) return ZO_MALFORMED_INPUT;
+    if (n_rows - 1 > UINT64_MAX / table_len || table_len * (n_rows - 1) < n_rows) return ZO_MALFORMED_INPUT;
+    uint64_t bound = table_len * (n_rows - 1) - n_rows;
+    uint64_t need = bound + 1, blowup = 4, lde;
+    for (;;) {
+        if (n_rows > UINT64_MAX / blowup) return ZO_INVALID_DOMAIN_SIZE;
+        lde = n_rows * blowup;
+        if (need <= lde / 4 || blowup >= ((uint64_t)1 << 27)) break;
+        blowup *= 2;
+    }
+    if (lde > MAX_DOMAIN || need > lde / 4) return ZO_INVALID_DOMAIN_SIZE;
+    uint32_t mb = zo_fri_composition_millibits(lde, bound);
+    size_t q; uint32_t g;
+    zo_fri_tune_strength(target, mb, &q, &g);
+    size_t fs, ch;
+    zo_fri_tune_shape(lde, q, lde, 12, 1, &fs, &ch);
+    o->n_rows = n_rows; o->blowup = blowup; o->num_queries = q; o->final_size = fs;
+    o->grinding_bits = g; o->cap_height = ch; o->value = value % P;
+    return ZO_OK;
+}
+
+/* table.rs:220-250 validate */
+static int table_validate(const zo_table_params *p) {
+    if (p->n_rows < 2 || !is_pow2(p->n_rows)) return ZO_INVALID_DOMAIN_SIZE;
+    if (p->blowup < 2 || !is_pow2(p->blowup)) return ZO_INVALID_BLOWUP;
+    if (p->num_queries == 0) return ZO_NO_QUERIES;
+    if (p->final_size < 2 || !is_pow2(p->final_size)) return ZO_INVALID_DOMAIN_SIZE;
+    if (p->cap_height > 8) return ZO_MALFORMED_INPUT;
+    if (p->n_rows > UINT64_MAX / p->blowup || p->n_rows * p->blowup > MAX_DOMAIN) return ZO_INVALID_DOMAIN_SIZE;
+    return ZO_OK;
+}
+
+/* table.rs:364-374 membership_bound (saturating) */
+static uint64_t membership_bound(uint64_t tlen, uint64_t n, uint64_t n_rand) {
+    uint64_t a = n + n_rand < n ? UINT64_MAX : n + n_rand;
+    a = a ? a - 1 : 0;
+    uint64_t prod = (a && tlen > UINT64_MAX / a) ? UINT64_MAX : tlen * a;
+    return prod > n ? prod - n : 0;
+}
+
+/* table.rs:540-554 absorb_params */
+static void table_absorb_params(const zo_table_params *p, const uint32_t *table, size_t tlen,
+                                zo_transcript *t) {
+    size_t len = 56 + 4 * tlen;
+    uint8_t *b = malloc(len);
+    put_u64(b, p->n_rows); put_u64(b + 8, p->blowup); put_u64(b + 16, p->num_queries);
+    put_u64(b + 24, p->final_size); put_u32(b + 32, p->grinding_bits); put_u64(b + 36, p->cap_height);
+    put_u32(b + 44, p->value); put_u64(b + 48, tlen);
+    for (size_t i = 0; i < tlen; i++) put_u32(b + 56 + 4 * i, table[i]);
+    absorb_s(t, "table/params", b, len);
+    free(b);
+}
+
+/* table.rs:646-660 composition_at */
+static ext4 table_composition_at(uint32_t v, uint32_t x, const uint32_t *table, size_t tlen,
+                                 uint32_t value, size_t n, ext4 am, ext4 ab) {
+    uint32_t z_inv = f_inv(f_sub(f_pow(x, n), 1));
+    uint32_t prod = 1;
+    for (size_t i = 0; i < tlen; i++) prod = f_mul(prod, f_sub(v, table[i]));
+    return e_add(e_mul_base(am, f_mul(prod, z_inv)),
+                 e_mul_base(ab, f_mul(f_sub(v, value), f_inv(f_sub(x, 1)))));
+}
+
+/* table.rs:376-424 prove_from_coeffs; bytes per table.rs:244-262 */
+static int table_prove_coeffs(const zo_table_params *p, const uint32_t *table, size_t tlen,
+                              const uint32_t *coeffs, size_t len, uint64_t degree_bound,
+                              zo_transcript *t, uint8_t **proof, size_t *proof_len) {
+    size_t n = p->n_rows, m = len * p->blowup;
+    if (len > SIZE_MAX / p->blowup || m > MAX_DOMAIN) return ZO_INVALID_DOMAIN_SIZE;
+    table_absorb_params(p, table, tlen, t);
+    uint32_t *lde = malloc(m * 4);
+    zo_evaluate_on_coset(coeffs, len, p->blowup, LDE_SHIFT, lde);
+    uint8_t *flat = malloc(m * 4);
+    for (size_t i = 0; i < m; i++) put_u32(flat + 4 * i, lde[i]);
+    mtree tree;
+    mtree_from_flat(flat, m * 4, 4, &tree);
+    free(flat);
+    size_t drop, depth;
+    capped_shape(m, p->cap_height, &drop, &depth);
+    size_t ncap;
+    const digest *cap = mtree_cap(&tree, drop, &ncap);
+    absorb_s(t, "table/column", (const uint8_t *)cap, 32 * ncap);
+    ext4 am = challenge_ext(t, "table/alpha"), ab = challenge_ext(t, "table/alpha");
+    uint32_t omega;
+    primitive_root(m, &omega);
+    ext4 *comp = malloc(m * sizeof(ext4));
+    uint32_t *dz = malloc(m * 4), *db = malloc(m * 4);
+    uint32_t x = LDE_SHIFT;
+    for (size_t i = 0; i < m; i++) {
+        dz[i] = f_sub(f_pow(x, n), 1);
+        db[i] = f_sub(x, 1);
+        x = f_mul(x, omega);
+    }
+    zo_batch_invert(dz, m);
+    zo_batch_invert(db, m);
+    for (size_t i = 0; i < m; i++) {
+        uint32_t prod = 1;
+        for (size_t k = 0; k < tlen; k++) prod = f_mul(prod, f_sub(lde[i], table[k]));
+        comp[i] = e_add(e_mul_base(am, f_mul(prod, dz[i])),
+                        e_mul_base(ab, f_mul(f_sub(lde[i], p->value), db[i])));
+    }
+    free(dz); free(db);
+    fri_params fp;
+    int rc = fri_params_new(p->blowup, p->num_queries, p->final_size, &fp);
+    if (!rc) { fp.grinding_bits = p->grinding_bits; fp.cap_height = p->cap_height; rc = fri_params_validate(&fp); }
+    if (!rc && degree_bound >= m) rc = ZO_MALFORMED_INPUT;
+    if (rc) { free(comp); free(lde); mtree_free(&tree); return rc; }
+    fri_state st;
+    rc = fri_commit_inner(comp, m, degree_bound, m, &fp, t, &st);
+    if (rc) { free(lde); mtree_free(&tree); return rc; }
+    writer w = {0};
+    w_byte(&w, VERSION);
+    w_cap(&w, cap, ncap);
+    fri_write_commitment(&w, &st);
+    uint64_t *idx = malloc(p->num_queries * sizeof(uint64_t));
+    rc = fri_open_write(&st, t, &w, idx);
+    if (!rc) {
+        w_u32(&w, (uint32_t)p->num_queries);
+        uint32_t log_m = log2u(m);
+        for (size_t k = 0; k < p->num_queries && !rc; k++) {
+            size_t index = brev(idx[k], log_m);
+            path_t pa;
+            rc = mtree_prove_capped(&tree, index, drop, &pa);
+            if (rc) break;
+            w_u64(&w, index);
+            w_u32(&w, lde[index]);
+            w_path(&w, &pa);
+            free(pa.s);
+        }
+    }
+    free(idx); free(lde);
+    fri_state_free(&st);
+    mtree_free(&tree);
+    if (rc) { free(w.b); return rc; }
+    *proof = w.b; *proof_len = w.n;
+    return ZO_OK;
+}
+
+/* table.rs:305-317 prove */
+int zo_table_prove(const zo_table_params *p, const uint32_t *table, size_t tlen, zo_transcript *t,
+                   uint8_t **proof, size_t *proof_len) {
+    int rc = table_validate(p);
+    if (rc) return rc;
+    if (tlen < 2) return ZO_MALFORMED_INPUT;  /* table.rs:291-298 */
+    size_t n = p->n_rows;
+    uint32_t *c = calloc(n, 4);
+    for (size_t i = 0; i < n; i++) c[i] = p->value;
+    zo_ntt_inverse(c, n);
+    rc = table_prove_coeffs(p, table, tlen, c, n, membership_bound(tlen, n, 0), t, proof, proof_len);
+    free(c);
+    return rc;
+}
+
+/* table.rs:329-356 prove_zk */
+int zo_table_prove_zk(const zo_table_params *p, const uint32_t *table, size_t tlen, size_t n_rand,
+                      zo_chacha20 *rng, zo_transcript *t, uint8_t **proof, size_t *proof_len) {
+    int rc = table_validate(p);
+    if (rc) return rc;
+    if (tlen < 2) return ZO_MALFORMED_INPUT;
+    if (n_rand < p->num_queries) return ZO_MALFORMED_INPUT;
+    size_t n = p->n_rows;
+    uint32_t *c = calloc(n, 4);
+    for (size_t i = 0; i < n; i++) c[i] = p->value;
+    zo_ntt_inverse(c, n);
+    size_t total = n + n_rand, padded = 1;
+    while (padded < total) padded <<= 1;
+    if (padded > MAX_DOMAIN) { free(c); return ZO_INVALID_DOMAIN_SIZE; }
+    size_t pl;
+    uint32_t *masked = mask_coeffs(c, n, n_rand, rng, &pl);
+    free(c);
+    rc = table_prove_coeffs(p, table, tlen, masked, pl, membership_bound(tlen, n, n_rand), t, proof,
+                            proof_len);
+    free(masked);
+    return rc;
+}
+
+/* table.rs:430-538 verify (decoding per table.rs:265-289) */
+int zo_table_verify(const zo_table_params *p, const uint32_t *table, size_t tlen,
+                    const uint8_t *proof, size_t proof_len, zo_transcript *t) {
+    int rc = table_validate(p);
+    if (rc) return rc;
+    if (tlen < 2) return ZO_MALFORMED_INPUT;
+    reader r = {proof, proof_len, 0, 0};
+    if (r_byte(&r) != VERSION) return ZO_MALFORMED_INPUT;
+    size_t ncap;
+    digest *cap = r_cap(&r, &ncap);
+    fri_decoded d;
+    memset(&d, 0, sizeof d);
+    if (!r.err) fri_read(&r, &d);
+    size_t no = r.err ? 0 : r_count(&r, MAX_QUERIES);
+    typedef struct { size_t index; uint32_t v; path_t path; } top_t;
+    top_t *op = NULL;
+    size_t got = 0;
+    if (!r.err && no * 12 <= r.n - r.pos) {
+        op = calloc(no ? no : 1, sizeof(top_t));
+        for (size_t k = 0; k < no && !r.err; k++) {
+            got = k + 1;
+            op[k].index = r_u64(&r);
+            op[k].v = r_field(&r);
+            r_path(&r, &op[k].path);
+        }
+    } else r.err = 1;
+    if (r.err || r.pos != r.n) { rc = ZO_MALFORMED_INPUT; goto out; }
+    size_t n = p->n_rows, m = d.lde_len, expected = n * p->blowup;
+    if (m < expected || m % expected) { rc = ZO_FRI_VERIFICATION_FAILED; goto out; }
+    if (m == expected) {
+        if (d.degree_bound != membership_bound(tlen, n, 0)) { rc = ZO_FRI_VERIFICATION_FAILED; goto out; }
+    } else {
+        size_t padded = m / p->blowup;
+        if (padded - 1 > UINT64_MAX / tlen || tlen * (padded - 1) < n) { rc = ZO_FRI_VERIFICATION_FAILED; goto out; }
+        if (d.degree_bound > tlen * (padded - 1) - n) { rc = ZO_FRI_VERIFICATION_FAILED; goto out; }
+    }
+    if (d.poly_len != m) { rc = ZO_FRI_VERIFICATION_FAILED; goto out; }
+    table_absorb_params(p, table, tlen, t);
+    if (no != p->num_queries) { rc = ZO_FRI_VERIFICATION_FAILED; goto out; }
+    absorb_s(t, "table/column", (const uint8_t *)cap, 32 * ncap);
+    ext4 am = challenge_ext(t, "table/alpha"), ab = challenge_ext(t, "table/alpha");
+    fri_params fp;
+    rc = fri_params_new(p->blowup, p->num_queries, p->final_size, &fp);
+    if (rc) goto out;
+    fp.grinding_bits = p->grinding_bits; fp.cap_height = p->cap_height;
+    uint64_t *idx = malloc((d.nq ? d.nq : 1) * sizeof(uint64_t));
+    rc = fri_verify(&d, &fp, t, idx);
+    uint32_t log_m = log2u(m), omega;
+    primitive_root(m, &omega);
+    size_t drop, depth;
+    capped_shape(m, p->cap_height, &drop, &depth);
+    for (size_t k = 0; !rc && k < d.nq; k++) {
+        size_t index = brev(idx[k], log_m);
+        if (op[k].index != index) { rc = ZO_FRI_VERIFICATION_FAILED; break; }
+        if (ncap != ((size_t)1 << drop) || op[k].path.n != depth - drop) { rc = ZO_BAD_MERKLE_PATH; break; }
+        uint8_t vb[4];
+        put_u32(vb, op[k].v);
+        size_t e = index >> (depth - drop);
+        if (e >= ncap || !verify_capped(cap[e], vb, 4, index, depth, &op[k].path)) { rc = ZO_BAD_MERKLE_PATH; break; }
+        uint32_t x = f_mul(LDE_SHIFT, f_pow(omega, index));
+        ext4 want = table_composition_at(op[k].v, x, table, tlen, p->value, n, am, ab);
+        if (d.q[k].n == 0) { rc = ZO_FRI_VERIFICATION_FAILED; break; }
+        if (!e_eq(d.q[k].f[0].v[idx[k] % 4], want)) rc = ZO_FRI_VERIFICATION_FAILED;
+    }
+    free(idx);
+out:
+    for (size_t k = 0; k < got; k++) free(op[k].path.s);
+    free(op);
+    free(cap);
+    fri_decoded_free(&d);
+    return rc;
+}
+
+/* ------------------------------------------------------------------------ */
 /* range.rs — range-check AIR                                                */
 /* ------------------------------------------------------------------------ */
 

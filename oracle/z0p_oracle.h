@@ -209,6 +209,25 @@ uint32_t zo_chacha20_next_field(zo_chacha20 *s);
 int zo_air_prove_zk(const zo_air_params *params, size_t n_rand, zo_chacha20 *rng,
                     zo_transcript *t, uint8_t **proof, size_t *proof_len);
 
+/* table.rs: membership of a committed constant value in a public table. */
+typedef struct {
+    uint64_t n_rows, blowup, num_queries, final_size;
+    uint32_t grinding_bits;
+    uint64_t cap_height;
+    uint32_t value;
+} zo_table_params;
+int zo_table_params_new(uint64_t n_rows, uint64_t blowup, uint64_t num_queries,
+                        uint64_t final_size, uint32_t value, zo_table_params *out);
+int zo_table_for_security(uint64_t n_rows, uint64_t table_len, uint32_t value,
+                          uint32_t target_bits, zo_table_params *out);
+int zo_table_prove(const zo_table_params *params, const uint32_t *table, size_t table_len,
+                   zo_transcript *t, uint8_t **proof, size_t *proof_len);
+int zo_table_prove_zk(const zo_table_params *params, const uint32_t *table, size_t table_len,
+                      size_t n_rand, zo_chacha20 *rng, zo_transcript *t, uint8_t **proof,
+                      size_t *proof_len);
+int zo_table_verify(const zo_table_params *params, const uint32_t *table, size_t table_len,
+                    const uint8_t *proof, size_t proof_len, zo_transcript *t);
+
 void zo_free(void *p);
 /* Worker-thread cap for the parallel paths (0 = all online cores). */
 void zo_set_max_workers(size_t workers);

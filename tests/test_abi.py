@@ -172,3 +172,30 @@ def test_buffer_too_small_reports_size_without_device(z0p):
     p = z0p.air.Params.for_security(1024, 1, 1, 1, 100)
     assert p.proof_size() == 68573
     assert z0p.lib().z0p_gpu_air_prove(None, C.byref(p), None, None, 0, None) == 106
+
+
+def test_table_sizes_match_oracle_and_errors_carry_their_own_reason(z0p, oracle):
+    # Sizes from the shape alone (no device) equal the oracle's proofs, and a
+    # failure without a message of its own does not report an older one.
+    for n, b, q, f, tl, n_rand in [(8, 8, 8, 4, 4, 0), (64, 32, 12, 8, 7, 0), (8, 8, 8, 4, 4, 24)]:
+        n_out = C.c_size_t()
+        pz = z0p.table.Params.new(n, b, q, f, 10)
+        assert z0p.lib().z0p_table_proof_size(C.byref(pz), tl, n_rand, C.byref(n_out)) == 0
+        table = [10 + i for i in range(tl)]
+        po = oracle.table_params_new(n, b, q, f, 10)
+        if n_rand:
+            proof = oracle.table_prove_zk(po, table, n_rand, oracle.ChaCha20.new(bytes(32), bytes(12)),
+                                          oracle.Transcript(b"s"))
+        else:
+            proof = oracle.table_prove(po, table, oracle.Transcript(b"s"))
+        assert n_out.value == len(proof)
+    L = z0p.lib()
+    pz = z0p.table.Params.new(8, 8, 8, 4, 10)
+    n_out = C.c_size_t()
+    assert L.z0p_table_proof_size(C.byref(pz), 1, 0, C.byref(n_out)) == 8
+    assert b"two entries" in L.z0p_gpu_last_reason()
+    assert L.z0p_gpu_last_reason() == b""
+    assert L.z0p_table_proof_size(C.byref(pz), 4, 7, C.byref(n_out)) == 8  # n_rand < queries
+    assert b"n_rand" in L.z0p_gpu_last_reason()
+    assert L.z0p_table_proof_size(C.byref(pz), 4, 8, C.byref(n_out)) == 3  # 16 rows: LDE 128 / 4
+    assert L.z0p_gpu_last_reason() == b""

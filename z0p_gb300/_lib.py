@@ -47,6 +47,14 @@ class FriParams(C.Structure):
     ]
 
 
+class TableParams(C.Structure):
+    _fields_ = [
+        ("n_rows", C.c_uint64), ("blowup", C.c_uint64), ("num_queries", C.c_uint64),
+        ("final_size", C.c_uint64), ("grinding_bits", C.c_uint32), ("cap_height", C.c_uint64),
+        ("value", C.c_uint32),
+    ]
+
+
 class FoldParams(C.Structure):
     _fields_ = [
         ("seg_steps", C.c_uint64), ("blowup", C.c_uint64), ("num_queries", C.c_uint64),
@@ -133,6 +141,15 @@ def lib():
             "z0p_air_proof_size_zk": (C.c_int, [P(AirParams), sz, P(sz)]),
             "z0p_gpu_air_prove_zk": (C.c_int, [vp, P(AirParams), sz, P(ChaChaState),
                                                P(TranscriptState), P(C.c_uint8), sz, P(sz)]),
+            "z0p_table_params_new": (C.c_int, [C.c_uint64] * 4 + [C.c_uint32, P(TableParams)]),
+            "z0p_table_params_for_security": (C.c_int, [C.c_uint64, C.c_uint64, C.c_uint32, C.c_uint32,
+                                                        P(TableParams)]),
+            "z0p_table_proof_size": (C.c_int, [P(TableParams), sz, sz, P(sz)]),
+            "z0p_gpu_table_prove": (C.c_int, [vp, P(TableParams), P(C.c_uint32), sz, P(TranscriptState),
+                                              P(C.c_uint8), sz, P(sz)]),
+            "z0p_gpu_table_prove_zk": (C.c_int, [vp, P(TableParams), P(C.c_uint32), sz, sz,
+                                                 P(ChaChaState), P(TranscriptState), P(C.c_uint8), sz,
+                                                 P(sz)]),
             "z0p_fold_params_new": (C.c_int, [C.c_uint64] * 4 + [C.c_uint32] * 3 + [P(FoldParams)]),
             "z0p_fold_params_for_security": (C.c_int, [C.c_uint64] + [C.c_uint32] * 4 + [P(FoldParams)]),
             "z0p_gpu_fold_create": (C.c_int, [vp, P(FoldParams), P(vp)]),

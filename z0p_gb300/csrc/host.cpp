@@ -9,9 +9,16 @@
 namespace z0p {
 namespace host {
 
-static thread_local std::string g_reason;
+// The message of the last failure on this thread. Reading it consumes it, so
+// a later failure that sets no message of its own reports none rather than
+// an older one.
+static thread_local std::string g_reason, g_read;
 void set_reason(const std::string& r) { g_reason = r; }
-const char* reason() { return g_reason.c_str(); }
+const char* reason() {
+  g_read.swap(g_reason);
+  g_reason.clear();
+  return g_read.c_str();
+}
 
 uint32_t fpow(uint32_t a, uint64_t e) {  // src/babybear.rs:147-158
   uint32_t acc = 1;

@@ -934,6 +934,51 @@ __global__ void __launch_bounds__(kThreads) air_compose_general_kernel(AirCompos
   store_digest(a.leaves + 8 * (size_t)P, d);
 }
 
+// Table membership composition (src/table.rs:597-644 == composition_at
+// :646-660) on layer-0 quads, as the AIR kernels lay them out:
+//   alpha_m prod_t (v - t) / (x^n - 1) + alpha_b (v - value) / (x - 1)
+// with 1/(x^n - 1) periodic in q (period r = N'/n) and 1/(x - 1) =
+// omega_n^-1 T(q - r), omega_n^-1 folded into alpha_b. The product runs as a
+// chain of Montgomery products of canonical factors and is brought back to
+// canonical by one product with R^len.
+__global__ void __launch_bounds__(kThreads) table_compose_kernel(TableComposeArgs a, Tables tb) {
+  const uint32_t logm = a.logN + a.logB;
+  const uint32_t quarter = 1u << (logm - 2);
+  const uint32_t u = blockIdx.x * blockDim.x + threadIdx.x;
+  if (u >= quarter) return;
+  const uint32_t N = 1u << a.logN, B = 1u << a.logB;
+  uint32_t k0 = u;
+  if (a.logN >= 2) {
+    const uint32_t j = u >> (a.logN - 2), q0 = u & ((N >> 2) - 1u);
+    k0 = (q0 << a.logB) | j;
+  }
+  const uint32_t P = brev_bits(k0, logm - 2);
+  uint32_t leaf[16];
+#pragma unroll
+  for (int s = 0; s < 4; s++) {
+    const uint32_t k = k0 + (uint32_t)s * quarter;
+    const uint32_t j = k & (B - 1u), q = k >> a.logB;
+    const size_t base = (size_t)j << a.logN;
+    const uint32_t v = __ldg(a.lde + base + q);
+    const uint32_t tm = __ldg(a.tinv + base + ((q - a.r) & (N - 1u)));
+    const uint32_t iz = __ldg(a.zinv + j * a.r + (q & (a.r - 1u)));
+    uint32_t prod = fsub(v, __ldg(a.table));
+    for (uint32_t i = 1; i < a.table_len; i++) prod = mmul(prod, fsub(v, __ldg(a.table + i)));
+    prod = mmul(mmul(prod, a.corr_m), iz);
+    const uint32_t bd = mmul(fsub_lazy(v, a.value), tm);
+    const int t = (s == 1) ? 2 : (s == 2) ? 1 : s;  // position 4P + brev2(s)
+#pragma unroll
+    for (int c = 0; c < 4; c++) leaf[4 * t + c] = mdot2(prod, a.alpha_m[c], bd, a.alpha_b[c]);
+  }
+  uint4* dst = reinterpret_cast<uint4*>(a.layer0 + 16 * (size_t)P);
+#pragma unroll
+  for (int t = 0; t < 4; t++)
+    dst[t] = make_uint4(leaf[4 * t], leaf[4 * t + 1], leaf[4 * t + 2], leaf[4 * t + 3]);
+  uint32_t d[8];
+  blake3_leaf64(leaf, d);
+  store_digest(a.leaves + 8 * (size_t)P, d);
+}
+
 // ------------------------------------------------- FRI commitment input ----
 // fri::commit on coefficients (src/fri.rs:407-433, 443-460): evaluate_on_coset
 // scales c_i by 31^i before the forward transform (src/ntt.rs:353-358). One
@@ -1783,10 +1828,18 @@ cudaError_t grind(cudaStream_t st, uint32_t slot, uint32_t head_len, uint32_t bi
 }
 
 cudaError_t mask_pad(cudaStream_t st, const Tables& tb, const uint32_t* coeffs, const uint32_t* r,
-                     uint32_t* out, uint32_t n, uint32_t n_rand, uint32_t padded) {
+                     uint32_t* out, uint32_t n, uint32_t n_rand, uint32_t padded, uint32_t ncols) {
   Stage stg("mask_pad", st);
   stg.launched();
-  mask_pad_kernel<<<dim3(grid_for(padded), 2), kThreads, 0, st>>>(coeffs, r, out, n, n_rand, padded, tb);
+  mask_pad_kernel<<<dim3(grid_for(padded), ncols), kThreads, 0, st>>>(coeffs, r, out, n, n_rand, padded,
+                                                                      tb);
+  return cudaGetLastError();
+}
+
+cudaError_t table_compose(cudaStream_t st, const Tables& tb, const TableComposeArgs& a) {
+  Stage stg("table_compose", st);
+  stg.launched();
+  table_compose_kernel<<<grid_for(1ull << (a.logN + a.logB - 2)), kThreads, 0, st>>>(a, tb);
   return cudaGetLastError();
 }
 

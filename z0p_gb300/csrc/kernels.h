@@ -169,6 +169,21 @@ struct FoldCombineArgs {
   uint32_t logN, logB;   // segment rows s = 2^logN, blowup 2^logB
   uint32_t w_last_m;     // omega_s^(s-1) (Montgomery)
 };
+// Table membership composition inputs (src/table.rs:597-644).
+struct TableComposeArgs {
+  const uint32_t* lde;    // the value column's LDE, coset-major [j][q]
+  const uint32_t* tinv;   // 1/(x - omega_n^-1) per row, coset-major (Montgomery)
+  const uint32_t* zinv;   // B x r values 1/(x^n - 1) (Montgomery)
+  const uint32_t* table;  // public table entries (canonical)
+  uint32_t table_len;
+  uint32_t corr_m;        // R^table_len mod p: restores the product chain to canonical
+  uint32_t value;         // claimed member (canonical)
+  uint32_t alpha_m[4];    // alpha_member (Montgomery)
+  uint32_t alpha_b[4];    // alpha_bound * omega_n^-1 (Montgomery)
+  uint32_t* layer0;
+  uint32_t* leaves;
+  uint32_t logN, logB, r;
+};
 namespace launch {
 
 // Number of kernel launches issued by this library in this process.
@@ -222,7 +237,8 @@ cudaError_t air_trace_leaves(cudaStream_t st, const Tables& tb, const uint32_t* 
 // air::prove_zk masking of both columns' twisted coefficients into planes of
 // `padded` words (r: 2 x n_rand canonical masking values).
 cudaError_t mask_pad(cudaStream_t st, const Tables& tb, const uint32_t* coeffs, const uint32_t* r,
-                     uint32_t* out, uint32_t n, uint32_t n_rand, uint32_t padded);
+                     uint32_t* out, uint32_t n, uint32_t n_rand, uint32_t padded, uint32_t ncols = 2);
+cudaError_t table_compose(cudaStream_t st, const Tables& tb, const TableComposeArgs& a);
 // Composition with column B from its own LDE (next row r rows further in a
 // coset; a.zinv holds B x r values 1/(x^n - 1)); the slot's alpha[.][0..4]
 // are alpha_0..alpha_4 with alpha_2, alpha_3 times omega_n^-1.

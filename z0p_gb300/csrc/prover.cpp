@@ -973,6 +973,190 @@ int air_prove_general(z0p_gpu_ctx* c, const z0p_air_params& p, const GeneralAir&
   return Z0P_OK;
 }
 
+// table::prove / prove_zk (src/table.rs:305-424) on the device: the value
+// column is the constant polynomial [v, 0, ..] (interpolate of a constant),
+// masked and padded for prove_zk, extended, hashed as 4-byte row leaves; the
+// membership composition, the FRI, and one opening per query.
+int table_validate(const z0p_table_params& p) {  // src/table.rs:220-250
+  if (p.n_rows < 2 || !is_pow2(p.n_rows)) return Z0P_ERR_INVALID_DOMAIN_SIZE;
+  if (p.blowup < 2 || !is_pow2(p.blowup)) return Z0P_ERR_INVALID_BLOWUP;
+  if (p.num_queries == 0) return Z0P_ERR_NO_QUERIES;
+  if (p.final_size < 2 || !is_pow2(p.final_size)) return Z0P_ERR_INVALID_DOMAIN_SIZE;
+  if (p.cap_height > 8) { set_reason("cap_height above 8"); return Z0P_ERR_MALFORMED_INPUT; }
+  if (p.n_rows > (1ull << 27) / p.blowup) return Z0P_ERR_INVALID_DOMAIN_SIZE;
+  if (p.value >= P) { set_reason("field elements must be canonical (< p)"); return Z0P_ERR_MALFORMED_INPUT; }
+  return Z0P_OK;
+}
+
+uint64_t membership_bound(uint64_t tlen, uint64_t n, uint64_t n_rand) {  // src/table.rs:364-374
+  uint64_t a = n + n_rand < n ? UINT64_MAX : n + n_rand;
+  a = a ? a - 1 : 0;
+  const uint64_t prod = (a && tlen > UINT64_MAX / a) ? UINT64_MAX : tlen * a;
+  return prod > n ? prod - n : 0;
+}
+
+int table_shape(const z0p_table_params& p, const uint32_t* table, size_t tlen, uint64_t n_rand,
+                FriParams* fp, FriShape* s, uint64_t* bytes) {
+  RC(table_validate(p));
+  if (tlen < 2) {  // src/table.rs:291-298
+    set_reason("table needs at least two entries");
+    return Z0P_ERR_MALFORMED_INPUT;
+  }
+  if (n_rand && n_rand < p.num_queries) {  // src/table.rs:338-342
+    set_reason("n_rand must cover num_queries for hiding");
+    return Z0P_ERR_MALFORMED_INPUT;
+  }
+  if (table)
+    for (size_t i = 0; i < tlen; i++)
+      if (table[i] >= P) {
+        set_reason("field elements must be canonical (< p)");
+        return Z0P_ERR_MALFORMED_INPUT;
+      }
+  const uint64_t lp = padded_len(p.n_rows, n_rand);
+  if (lp > (1ull << 27) || lp > (1ull << 27) / p.blowup) return Z0P_ERR_INVALID_DOMAIN_SIZE;
+  RC(fri_params_new(p.blowup, p.num_queries, p.final_size, fp));
+  fp->grinding_bits = p.grinding_bits;
+  fp->cap_height = p.cap_height;
+  const uint64_t m = lp * p.blowup;
+  const uint64_t bound = membership_bound(tlen, p.n_rows, n_rand);
+  if (bound >= m) {
+    set_reason("degree bound must be below LDE size (rate < 1)");
+    return Z0P_ERR_MALFORMED_INPUT;
+  }
+  RC(fri_shape(m, bound, *fp, s));
+  const uint32_t depth = log2u(m), drop = p.cap_height < depth ? (uint32_t)p.cap_height : depth;
+  *bytes = 1 + 4 + 32ull * (1ull << drop) + fri_bytes(*s, p.num_queries) + 4 +
+           p.num_queries * (8 + 4 + 4 + 33ull * (depth - drop));  // src/table.rs:244-262
+  return Z0P_OK;
+}
+
+int table_prove_dev(z0p_gpu_ctx* c, const z0p_table_params& p, const uint32_t* table, size_t tlen,
+                    uint64_t n_rand, const uint32_t* rand, z0p_transcript_state* tsp,
+                    uint8_t* out) {
+  FriParams fp;
+  FriShape s;
+  uint64_t need = 0;
+  RC(table_shape(p, table, tlen, n_rand, &fp, &s, &need));
+  const uint64_t N = p.n_rows, B = p.blowup, Lp = padded_len(N, n_rand), m = Lp * B;
+  const uint32_t logN = log2u(N), logL = log2u(Lp), logB = log2u(B), logm = logL + logB;
+  const uint32_t r = (uint32_t)(Lp / N);
+  cudaStream_t st = c->stream;
+  RC(ensure(c, c->coeffs, 4 * (N + Lp)));
+  RC(ensure(c, c->scratch, 4 * m));
+  RC(ensure(c, c->lde, 4 * m));
+  const uint64_t ttree_words = 8 * tree_digests(m);
+  RC(ensure(c, c->ttree, 4 * ttree_words));
+  RC(ensure(c, c->misc, 64 + 4 * B * r + 4 * n_rand + 4 * tlen + 4 * m));
+  FriBufs fb;
+  RC(plan_fri_buffers(c, s, 1, &fb));
+  const uint32_t tdrop = p.cap_height < logm ? (uint32_t)p.cap_height : logm;
+  const uint32_t tsteps = logm - tdrop;
+  HioPlan h;
+  RC(plan_hio(c, s, p.num_queries, tdrop, 1 + 8 * tsteps, 1, &h));
+  uint32_t* coeffs = (uint32_t*)c->coeffs.p;
+  uint32_t* lde = (uint32_t*)c->lde.p;
+  uint32_t* ttree = (uint32_t*)c->ttree.p;
+  uint32_t* zinv = (uint32_t*)c->misc.p + 16;
+  uint32_t* rdev = zinv + B * r;
+  uint32_t* tdev = rdev + n_rand;
+  uint32_t* tinv = tdev + tlen;
+  z0p_transcript_state work = *tsp;
+  Transcript t(&work);
+  {  // absorb_params (src/table.rs:540-554)
+    std::vector<uint8_t> pb(56 + 4 * tlen);
+    auto p64 = [&](size_t off, uint64_t v) { for (int i = 0; i < 8; i++) pb[off + i] = (uint8_t)(v >> (8 * i)); };
+    auto p32 = [&](size_t off, uint32_t v) { for (int i = 0; i < 4; i++) pb[off + i] = (uint8_t)(v >> (8 * i)); };
+    p64(0, p.n_rows); p64(8, p.blowup); p64(16, p.num_queries); p64(24, p.final_size);
+    p32(32, p.grinding_bits); p64(36, p.cap_height); p32(44, p.value); p64(48, tlen);
+    for (size_t i = 0; i < tlen; i++) p32(56 + 4 * i, table[i]);
+    transcript_absorb(t, "table/params", pb.data(), pb.size());
+  }
+  // interpolate(vec![value; n]) = [value, 0, ..] (src/table.rs:307-309).
+  CK(cudaMemsetAsync(coeffs, 0, 4 * N, st));
+  CK(cudaMemcpyAsync(coeffs, &p.value, 4, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(tdev, table, 4 * tlen, cudaMemcpyHostToDevice, st));
+  c->h2d += 4 + 4 * tlen;
+  const uint32_t* lde_in = coeffs;
+  if (Lp != N || n_rand) {
+    if (n_rand) {
+      CK(cudaMemcpyAsync(rdev, rand, 4 * n_rand, cudaMemcpyHostToDevice, st));
+      c->h2d += 4 * n_rand;
+    }
+    CK(launch::mask_pad(st, c->tb, coeffs, rdev, coeffs + N, (uint32_t)N, (uint32_t)n_rand,
+                        (uint32_t)Lp, 1));
+    lde_in = coeffs + N;
+  }
+  // The twisted coefficients: [value, 0, ..] already equal c_k 31^k.
+  NttPlan lp;
+  lp.logn = logL; lp.batch = (uint32_t)B; lp.in_div = (uint32_t)B; lp.twist_mod = (uint32_t)B;
+  lp.twist_shift = 27 - logm;
+  CK(launch::ntt(st, c->tb, lp, lde_in, lde, (uint32_t*)c->scratch.p));
+  CK(launch::range_trace_leaves(st, lde, ttree, logL, logB, 1));  // from_flat(.., 4) leaves
+  CK(launch::merkle_build(st, ttree, m, tsteps, merkle_counter(c), hio_dev<uint32_t>(c, h.trace_cap)));
+  const uint32_t omega_n = two_adic_generator(logN);
+  const uint32_t omega_inv = finv(omega_n);
+  CK(launch::row_inverses(st, c->tb, tinv, to_mont(omega_inv), logL, logB));
+  {
+    std::vector<uint32_t> zt(B * r);
+    const uint32_t omega_m = two_adic_generator(logm), omega_l = two_adic_generator(logL);
+    for (uint64_t j = 0; j < B; j++)
+      for (uint32_t q = 0; q < r; q++) {
+        const uint32_t x = fmul(fmul(GENERATOR, fpow(omega_m, j)), fpow(omega_l, q));
+        zt[j * r + q] = to_mont(finv(fsub(fpow(x, N), 1)));
+      }
+    CK(cudaMemcpyAsync(zinv, zt.data(), 4 * B * r, cudaMemcpyHostToDevice, st));
+  }
+  CK(sync(c, "cap"));
+  std::vector<uint8_t> column_cap(c->hio + h.trace_cap, c->hio + h.trace_cap + h.trace_cap_bytes);
+  c->d2h += h.trace_cap_bytes;
+  transcript_absorb(t, "table/column", column_cap.data(), column_cap.size());
+  uint32_t am[4], ab[4];
+  challenge_ext(t, "table/alpha", am);
+  challenge_ext(t, "table/alpha", ab);
+  TableComposeArgs ca;
+  ca.lde = lde; ca.tinv = tinv; ca.zinv = zinv; ca.table = tdev;
+  ca.table_len = (uint32_t)tlen;
+  ca.corr_m = fpow((uint32_t)((1ull << 32) % P), tlen);
+  ca.value = p.value;
+  for (int e = 0; e < 4; e++) {
+    ca.alpha_m[e] = to_mont(am[e]);
+    ca.alpha_b[e] = to_mont(fmul(ab[e], omega_inv));
+  }
+  ca.layer0 = fb.layer[0]; ca.leaves = fb.tree[0];
+  ca.logN = logL; ca.logB = logB; ca.r = r;
+  CK(launch::table_compose(st, c->tb, ca));
+  CK(launch::merkle_build(st, fb.tree[0], s.leaves[0], s.depth[0] - s.drop[0], merkle_counter(c),
+                          hio_dev<uint32_t>(c, h.fri_cap[0]), 0, 1, fb.tree_stride,
+                          h.fri_cap_bytes[0] / 4));
+  Transcript* ts[1] = {&t};
+  FriOut fo;
+  const uint64_t bound = membership_bound(tlen, N, n_rand);
+  RC(run_fri(c, s, fp, fb, m, bound, ts, 1, h, &fo));
+  OpenArgs oa{};  // src/table.rs:412-420
+  oa.lde = lde; oa.ttree = ttree; oa.tleaves = m; oa.tsteps = tsteps;
+  oa.logN = logL; oa.logB = logB; oa.ncol = 1;
+  RC(run_openings(c, s, fb, h, &fo, 1, oa));
+  Writer w(out, need);  // table::Proof::to_bytes (src/table.rs:244-262)
+  w.byte(6);
+  w.u32((uint32_t)(column_cap.size() / 32));
+  w.bytes(column_cap.data(), column_cap.size());
+  write_fri(w, c, s, fo, m, bound, h, 0);
+  w.u32((uint32_t)fo.indices.size());
+  for (size_t qi = 0; qi < fo.indices.size(); qi++) {
+    const uint64_t index = brev(fo.indices[qi], logm);
+    const uint32_t* row = open_block(c, h, 0, qi) + h.trace_off;
+    w.u64(index);
+    w.u32(row[0]);
+    write_path(w, (const uint8_t*)(row + 1), index, tsteps);
+  }
+  if (w.n != need) {
+    set_reason("internal error: proof length differs from its shape");
+    return Z0P_ERR_CUDA;
+  }
+  *tsp = work;
+  return Z0P_OK;
+}
+
 // src/air.rs:365-372 -> 485-599 on the device, for K proofs of one shape in
 // lockstep: every launch covers the group (grid y = proof) and every
 // Fiat-Shamir round trip serves it.
@@ -2087,6 +2271,101 @@ int z0p_gpu_air_prove_zk(z0p_gpu_ctx* c, const z0p_air_params* p, size_t n_rand,
   g.n_rand = n_rand;
   g.rand = rand.data();
   RC(air_prove_general(c, *p, g, t, out));
+  *rng = r;
+  return Z0P_OK;
+}
+
+int z0p_table_params_new(uint64_t n_rows, uint64_t blowup, uint64_t num_queries,
+                         uint64_t final_size, uint32_t value, z0p_table_params* out) {
+  if (!out) return Z0P_ERR_INVALID_ARGUMENT;  // src/table.rs:55-88
+  if (n_rows < 2 || !is_pow2(n_rows)) return Z0P_ERR_INVALID_DOMAIN_SIZE;
+  if (blowup < 2 || !is_pow2(blowup)) return Z0P_ERR_INVALID_BLOWUP;
+  if (num_queries == 0) return Z0P_ERR_NO_QUERIES;
+  if (final_size < 2 || !is_pow2(final_size)) return Z0P_ERR_INVALID_DOMAIN_SIZE;
+  if (n_rows > (1ull << 27) / blowup) return Z0P_ERR_INVALID_DOMAIN_SIZE;
+  if (value >= P) { set_reason("field elements must be canonical (< p)"); return Z0P_ERR_MALFORMED_INPUT; }
+  *out = z0p_table_params{n_rows, blowup, num_queries, final_size, 0, 0, value};
+  return Z0P_OK;
+}
+
+int z0p_table_params_for_security(uint64_t n_rows, uint64_t table_len, uint32_t value,
+                                  uint32_t target_bits, z0p_table_params* out) {
+  if (!out) return Z0P_ERR_INVALID_ARGUMENT;  // src/table.rs:114-170
+  if (n_rows < 2 || !is_pow2(n_rows)) return Z0P_ERR_INVALID_DOMAIN_SIZE;
+  if (table_len < 2) { set_reason("table needs at least two entries"); return Z0P_ERR_MALFORMED_INPUT; }
+  if (n_rows - 1 > UINT64_MAX / table_len || table_len * (n_rows - 1) < n_rows) {
+    set_reason("table length overflows composition bound");
+    return Z0P_ERR_MALFORMED_INPUT;
+  }
+  if (value >= P) { set_reason("field elements must be canonical (< p)"); return Z0P_ERR_MALFORMED_INPUT; }
+  const uint64_t bound = table_len * (n_rows - 1) - n_rows, need = bound + 1;
+  uint64_t blowup = 4, lde = 0;
+  for (;;) {
+    if (n_rows > UINT64_MAX / blowup) return Z0P_ERR_INVALID_DOMAIN_SIZE;
+    lde = n_rows * blowup;
+    if (need <= lde / 4 || blowup >= (1ull << 27)) break;
+    blowup *= 2;
+  }
+  if (lde > (1ull << 27) || need > lde / 4) return Z0P_ERR_INVALID_DOMAIN_SIZE;
+  uint64_t q = 0, fs = 0, ch = 0;
+  uint32_t g = 0;
+  tune_strength(target_bits, composition_millibits(lde, bound), &q, &g);
+  tune_shape(lde, q, lde, 12, &fs, &ch);
+  *out = z0p_table_params{n_rows, blowup, q, fs, g, ch, value};
+  return Z0P_OK;
+}
+
+int z0p_table_proof_size(const z0p_table_params* p, size_t table_len, size_t n_rand, size_t* len) {
+  if (!p || !len) return Z0P_ERR_INVALID_ARGUMENT;
+  FriParams fp;
+  FriShape s;
+  uint64_t bytes = 0;
+  RC(table_shape(*p, nullptr, table_len, n_rand, &fp, &s, &bytes));
+  *len = bytes;
+  return Z0P_OK;
+}
+
+int z0p_gpu_table_prove(z0p_gpu_ctx* c, const z0p_table_params* p, const uint32_t* table,
+                        size_t table_len, z0p_transcript_state* t, uint8_t* out, size_t cap,
+                        size_t* out_len) {
+  if (!c || !p || !t || (!table && table_len)) return Z0P_ERR_INVALID_ARGUMENT;
+  FriParams fp;
+  FriShape s;
+  uint64_t need = 0;
+  RC(table_shape(*p, table, table_len, 0, &fp, &s, &need));
+  if (out_len) *out_len = need;
+  if (!out || cap < need) { set_reason("output buffer too small for the proof"); return Z0P_ERR_BUFFER_TOO_SMALL; }
+  std::lock_guard<std::mutex> lk(c->mu);
+  c->work_serial++;
+  RC(with_device(c));
+  ProfileScope ps(c);
+  return table_prove_dev(c, *p, table, table_len, 0, nullptr, t, out);
+}
+
+int z0p_gpu_table_prove_zk(z0p_gpu_ctx* c, const z0p_table_params* p, const uint32_t* table,
+                           size_t table_len, size_t n_rand, z0p_chacha20_state* rng,
+                           z0p_transcript_state* t, uint8_t* out, size_t cap, size_t* out_len) {
+  if (!c || !p || !t || !rng || rng->used > 64 || (!table && table_len)) return Z0P_ERR_INVALID_ARGUMENT;
+  RC(table_validate(*p));  // src/table.rs:336-343
+  if (table_len < 2) { set_reason("table needs at least two entries"); return Z0P_ERR_MALFORMED_INPUT; }
+  if (n_rand < p->num_queries) {
+    set_reason("n_rand must cover num_queries for hiding");
+    return Z0P_ERR_MALFORMED_INPUT;
+  }
+  FriParams fp;
+  FriShape s;
+  uint64_t need = 0;
+  RC(table_shape(*p, table, table_len, n_rand, &fp, &s, &need));
+  if (out_len) *out_len = need;
+  if (!out || cap < need) { set_reason("output buffer too small for the proof"); return Z0P_ERR_BUFFER_TOO_SMALL; }
+  z0p_chacha20_state r = *rng;
+  std::vector<uint32_t> rand(n_rand);
+  for (auto& v : rand) v = chacha20_next_field(&r);
+  std::lock_guard<std::mutex> lk(c->mu);
+  c->work_serial++;
+  RC(with_device(c));
+  ProfileScope ps(c);
+  RC(table_prove_dev(c, *p, table, table_len, n_rand, rand.data(), t, out));
   *rng = r;
   return Z0P_OK;
 }
