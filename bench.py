@@ -256,15 +256,11 @@ def run_fri_pcs(Z, ctx, reps=5):
     `fri prod` rows (docs/benchmarks.md:24,26; coefficients and labels of
     benches/speed_size.rs:607-647, 756-795) and a 2^20-coefficient commitment.
     Host coefficients in, commitment and proof bytes out, per call."""
-    import numpy as np
-
-    P = 2013265921
     rows = []
     for n, label, ref_ms, ref_bytes in [(256, b"bench/fri-prod", 10.59, 29378),
                                         (1024, b"bench/fri-prod-big", 21.50, 43174),
                                         (1 << 20, b"bench/fri-pcs-2p20", None, None)]:
-        i = np.arange(n, dtype=np.uint64)
-        coeffs = (((i * 0x9E3779B9) + 17) % 2**32 % P).astype(np.uint32)
+        coeffs = bench_coeffs(n)
         params = Z.fri.Params.for_security(n, 100)
         times, size = [], 0
         for _ in range(reps + 1):
@@ -280,6 +276,150 @@ def run_fri_pcs(Z, ctx, reps=5):
                      "bytes_match_reference": None if ref_bytes is None else size == ref_bytes})
     return {"workload": "fri::Params::for_security(n, 100): B16 Q40 G20 C4 F16; commit + open",
             "rows": rows}
+
+
+def bench_coeffs(n):
+    """benches/speed_size.rs:203-205, 609-611: Field::new(i.wrapping_mul(0x9e37_79b9) + 17)."""
+    import numpy as np
+
+    i = np.arange(n, dtype=np.uint64)
+    return (((i * 0x9E3779B9) + 17) % 2**32 % P).astype(np.uint32)
+
+
+def run_published(Z, ctx):
+    """Every published prove row of the reference that this backend covers
+    (docs/benchmarks.md:21-27, 119-127), on the reference's own workloads,
+    parameters and labels (benches/speed_size.rs:201-483, 607-795): the
+    median wall-clock of the public call (host inputs in, proof bytes in host
+    memory out) beside the reference's published 16-core time, and the proof
+    size beside its published size."""
+    def fib_params(n, new_args=None):
+        _, b_last = Z.air.trace_last(1, 1, n)
+        if new_args:
+            return Z.air.Params.new(n, *new_args, 1, 1, b_last)
+        return Z.air.Params.for_security(n, 1, 1, b_last, 100)
+
+    def fri_row(params, n, label):
+        coeffs = bench_coeffs(n)
+
+        def run():
+            t = Z.Transcript(label)
+            st = Z.fri.commit(coeffs, params, t, ctx)
+            proof, _ = Z.fri.open(st, t)
+            return len(st.commitment) + len(proof)
+        return run
+
+    def air_row(params, label):
+        return lambda: len(Z.air.prove(params, Z.Transcript(label), ctx))
+
+    def range_row():
+        params = Z.range.Params.new(8, 16, 8, 8, 4, 12345)
+        return lambda: len(Z.range.prove(params, Z.Transcript(b"bench/range"), ctx))
+
+    def table_row():
+        params = Z.table.Params.new(8, 8, 8, 4, 30)
+        return lambda: len(Z.table.prove(params, [10, 20, 30, 40], Z.Transcript(b"bench/table"), ctx))
+
+    def fold_row():
+        segs, a, b = [], 1, 1
+        for _ in range(4):
+            ca, cb = [], []
+            for _ in range(8):
+                ca.append(a)
+                cb.append(b)
+                a, b = b, (a + b) % P
+            a, b = ca[-1], cb[-1]
+            segs.append((ca, cb))
+        params = Z.fold.Params.new(8, 8, 8, 4, 1, 1, segs[-1][1][-1])
+
+        def run():
+            t = Z.Transcript(b"bench/fold")
+            acc = Z.fold.Accumulator(params, ctx)
+            for ca, cb in segs:
+                acc.add_segment(ca, cb, t)
+            n = len(acc.finalize(t))
+            acc.close()
+            return n
+        return run
+
+    rows = [
+        ("fri poly256 B4 Q12", fri_row(Z.fri.Params.new(4, 12, 4), 256, b"bench/fri"), 0.15, 11522),
+        ("air fib64", air_row(fib_params(64, (8, 12, 8)), b"bench/air"), 0.17, 15465),
+        ("range 16-bit", range_row(), 0.10, 5217),
+        ("table 4-entry", table_row(), 0.04, 4673),
+        ("fold 4x8 fib", fold_row(), 0.19, 16845),
+        ("air fib1024", air_row(fib_params(1024, (8, 12, 8)), b"bench/air1024"), 2.01, 28257),
+        ("fri prod B16Q40G20C4F16 (poly-256)",
+         fri_row(Z.fri.Params.for_security(256, 100), 256, b"bench/fri-prod"), 10.59, 29378),
+        ("air prod B16Q40G20C4F16 (fib-64)", air_row(fib_params(64), b"bench/air-prod"), 11.99, 33061),
+        ("fri prod P1024 B16Q40G20C4F16",
+         fri_row(Z.fri.Params.for_security(1024, 100), 1024, b"bench/fri-prod-big"), 21.50, 43174),
+        ("air prod N1024", air_row(fib_params(1024), b"bench/air-scale"), 37.05, 68573),
+        ("air prod N8192", air_row(fib_params(8192), b"bench/air-scale"), 49.81, 101233),
+        ("air prod N65536", air_row(fib_params(65536), b"bench/air-scale"), 115.49, 141641),
+        ("air prod N1048576", air_row(fib_params(1 << 20), b"bench/air-scale"), 1733.55, 203553),
+    ]
+    out = []
+    for name, run, ref_ms, ref_bytes in rows:
+        size = run()  # warm-up (first use of a shape allocates its workspace)
+        times = []
+        for _ in range(21):
+            t0 = time.perf_counter()
+            run()
+            times.append(time.perf_counter() - t0)
+        ms = 1e3 * statistics.median(times)
+        out.append({"row": name, "ms": round(ms, 4), "reference_ms_16_cores": ref_ms,
+                    "speedup": round(ref_ms / ms, 2), "bytes": size, "reference_bytes": ref_bytes,
+                    "bytes_match_reference": size == ref_bytes})
+    return {"timing": "median of 21 calls after one warm-up; host inputs in, proof bytes in host memory",
+            "rows": out}
+
+
+def run_scale(Z, ctx, reps=5):
+    """The other prove entry points at 2^20 rows, production schedule
+    (for_security(100)): range::prove (16-bit, value 12,345; the batched and
+    served mixes use the same shape at smaller n), air::prove_zk with the
+    minimum hiding budget n_rand = 16 * num_queries (src/air.rs:445-458;
+    padded trace 2^21, LDE 2^25, final layer 32) and air::prove_with_trace on
+    host columns."""
+    import numpy as np
+
+    n = 1 << 20
+    a0, b0 = workload(0)
+    _, b_last = Z.air.trace_last(a0, b0, n)
+    air_p = Z.air.Params.for_security(n, a0, b0, b_last, 100)
+    range_p = Z.range.Params.for_security(n, 16, 12345, 100)
+    n_rand = 16 * air_p.num_queries
+    # The masked LDE is 2^25 rows; its FRI ends in a 32-value layer (the
+    # fold chain divides m / final_size by 4).
+    zk_p = Z.air.Params.new(n, 16, air_p.num_queries, 32, a0, b0, b_last) \
+        .with_grinding_bits(air_p.grinding_bits).with_cap_height(air_p.cap_height)
+    ca = np.empty(n, np.uint32)
+    cb = np.empty(n, np.uint32)
+    a, b = a0, b0
+    for i in range(n):  # the Fibonacci trace, built once on the host
+        ca[i], cb[i] = a, b
+        a, b = b, (a + b) % P
+    cases = [
+        ("range::prove 16-bit, 2^20 rows", n, lambda: Z.range.prove(range_p, Z.Transcript(b"bench/range"), ctx)),
+        ("air::prove_zk, 2^20 steps, n_rand %d" % n_rand, n,
+         lambda: Z.air.prove_zk(zk_p, n_rand, Z.rng.ChaCha20.new(bytes(32), bytes(12)),
+                                Z.Transcript(b"bench/air-zk"), ctx)),
+        ("air::prove_with_trace, 2^20 steps (host columns)", n,
+         lambda: Z.air.prove_with_trace(air_p, ca, cb, Z.Transcript(b"bench/air-scale"), ctx)),
+    ]
+    rows = []
+    for name, steps, run in cases:
+        size = len(run())
+        times = []
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            run()
+            times.append(time.perf_counter() - t0)
+        ms = 1e3 * statistics.median(times)
+        rows.append({"row": name, "ms": round(ms, 4), "rows_per_s": round(steps / (ms / 1e3)),
+                     "bytes": size})
+    return {"workload": "for_security(100): B16 Q40 G20 C4 F16", "rows": rows}
 
 
 def run_table(Z, ctx, reps=5):
@@ -480,6 +620,23 @@ def run_gpu(args):
 
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     ctx = Z.Context(local)
+    # Launch schedule: read from a file the autotuner wrote (--schedule), or
+    # measured here by the autotuner, outside every timed region (sections
+    # run alone keep the default unless given a file).
+    if args.schedule:
+        sched = Z.tune.load(args.schedule)
+        Z.tune.set(sched, local)
+        tune_info = {"source": args.schedule, "schedule": Z.tune.to_dict(sched)}
+    elif not args.only:
+        sched, report = Z.tune.autotune(ctx, max_log_n=22)
+        tune_info = {"source": "autotune (live)", "schedule": Z.tune.to_dict(sched), "report": report}
+    if args.only:
+        # One section alone (for profilers and quick checks): no headline line.
+        fn = {"published": run_published, "scale": run_scale, "fri_pcs": run_fri_pcs,
+              "fold_ivc": run_fold_ivc,
+              "table": run_table, "batched": run_batched, "served": run_served}[args.only]
+        print(json.dumps({"section": args.only, "result": fn(Z, ctx)}), flush=True)
+        return 0
     stream = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", local))
     a0, b0 = workload(rank)
     _, b_last = Z.air.trace_last(a0, b0, N_STEPS)
@@ -535,13 +692,15 @@ def run_gpu(args):
         prof = ctx.profile()
         ctx.set_profiling(False)
 
-    batched = served = fri_pcs = fold_ivc = table_row = None
+    batched = served = fri_pcs = fold_ivc = table_row = published = scale = None
     if not args.quick and ws == 1:
         batched = run_batched(Z, ctx)
         served = run_served(Z, ctx)
         fri_pcs = run_fri_pcs(Z, ctx)
         fold_ivc = run_fold_ivc(Z, ctx)
         table_row = run_table(Z, ctx)
+        published = run_published(Z, ctx)
+        scale = run_scale(Z, ctx)
 
     if rank != 0:
         if dist is not None:
@@ -629,6 +788,7 @@ def run_gpu(args):
             "blocked_in_sync": (st1["sync_wait_ns"] - st0["sync_wait_ns"]) / 1e6 / args.steps,
             "by_sync_site": host_sites},
         "clocks": clocks,
+        "launch_schedule": tune_info,
         "roofline": roof,
         "stages": stages,
         "cpu_baseline": cpu,
@@ -637,6 +797,8 @@ def run_gpu(args):
         "fri_pcs": fri_pcs,
         "fold_ivc": fold_ivc,
         "table": table_row,
+        "published_rows": published,
+        "scale_rows": scale,
     }
     print(json.dumps(line), flush=True)
     if dist is not None:
@@ -652,6 +814,11 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--quick", action="store_true",
                     help="skip the CPU baseline, parity check and per-stage pass (for profilers)")
+    ap.add_argument("--schedule", default=None,
+                    help="launch schedule file written by z0p_gb300.tune.save (default: autotune live)")
+    ap.add_argument("--only", default=None,
+                    choices=["published", "scale", "fri_pcs", "fold_ivc", "table", "batched", "served"],
+                    help="run one secondary section alone and print its JSON (no headline line)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

@@ -447,6 +447,49 @@ int z0p_gpu_merkle_flat64_cap(z0p_gpu_ctx *ctx, const uint8_t *d_flat, uint64_t 
  */
 int z0p_gpu_fri_fold(z0p_gpu_ctx *ctx, const uint32_t *d_in, uint64_t n, uint64_t lde_len,
                      uint64_t depth, const uint32_t ch[12], uint32_t *d_out);
+/* ------------------------------------------- launch schedule autotuning ---- */
+/* No counterpart in the reference (its prover has no device schedule).
+ * Launch choices the kernels read, one schedule per device, process-wide.
+ * Every schedule gives byte-identical proofs; only the time changes.
+ *  - ntt_log_n1[l]: for a four-step NTT of length 2^l (13 <= l <= 26),
+ *    log2 of the first pass's transform length, within
+ *    [max(7, l - 13), min(13, l - 6)]; 0 = the balanced split ceil(l / 2).
+ *    Other entries must be 0.
+ *  - merkle_top_log: a Merkle tree's levels are one launch each while they
+ *    hold more than 2^merkle_top_log nodes; one top kernel hashes the rest
+ *    (10..18).
+ *  - grind_ctas_per_sm: proof-of-work grid, CTAs per SM (1..16, clamped to
+ *    the occupancy limit). */
+typedef struct {
+    uint8_t ntt_log_n1[32];
+    uint32_t merkle_top_log;
+    uint32_t grind_ctas_per_sm;
+} z0p_schedule;
+/* What z0p_gpu_autotune measured, device time per candidate set (µs):
+ * the default and the chosen schedule for each LDE transform size (16
+ * cosets of 2^l; 0 where not tuned), for a 2^21-leaf Merkle tree above its
+ * leaves, and for eight single 20-bit proof-of-work searches. */
+typedef struct {
+    float ntt_default_us[32];
+    float ntt_best_us[32];
+    float merkle_default_us, merkle_best_us;
+    float grind_default_us, grind_best_us;
+    float wall_ms;  /* tuning time, host clock */
+} z0p_tune_report;
+int z0p_schedule_default(z0p_schedule *out);
+/* Read or replace a device's schedule; set validates every field first
+ * (Z0P_ERR_INVALID_ARGUMENT, schedule unchanged). Neither touches the GPU. */
+int z0p_gpu_schedule_get(int device, z0p_schedule *out);
+int z0p_gpu_schedule_set(int device, const z0p_schedule *schedule);
+/* Times the candidates of every field on the context's device (LDE
+ * transforms up to 16 x 2^min(max_log_n, 22) points, in the context's
+ * workspace), keeps a candidate only when it beats the default by 3% or
+ * more, installs the result as the device's schedule and writes it to *out.
+ * The proof-of-work candidates must agree on the nonce (else
+ * Z0P_ERR_UNSUPPORTED). `report` may be NULL. */
+int z0p_gpu_autotune(z0p_gpu_ctx *ctx, uint32_t max_log_n, z0p_schedule *out,
+                     z0p_tune_report *report);
+
 /* Diagnostic, no counterpart in the reference: the device's BLAKE3
  * throughput ceiling in G compressions/s, measured with register-resident
  * chains of Merkle-node hashes (no memory traffic). The hashing stages'

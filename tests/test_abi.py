@@ -199,3 +199,28 @@ def test_table_sizes_match_oracle_and_errors_carry_their_own_reason(z0p, oracle)
     assert b"n_rand" in L.z0p_gpu_last_reason()
     assert L.z0p_table_proof_size(C.byref(pz), 4, 8, C.byref(n_out)) == 3  # 16 rows: LDE 128 / 4
     assert L.z0p_gpu_last_reason() == b""
+
+
+def test_schedule_get_set_validation(z0p):
+    # Host-only state: no device needed. Every field is range-checked and a
+    # rejected schedule leaves the installed one unchanged.
+    t = z0p.tune
+    d = t.default()
+    assert (d.merkle_top_log, d.grind_ctas_per_sm) == (16, 4)
+    assert all(v == 0 for v in d.ntt_log_n1)
+    dev = 5
+    before = t.to_dict(t.get(dev))
+    good = t.from_dict({"ntt_log_n1": {"20": 9, "26": 13, "13": 7}, "merkle_top_log": 12,
+                        "grind_ctas_per_sm": 8})
+    t.set(good, dev)
+    assert t.to_dict(t.get(dev)) == t.to_dict(good)
+    for bad in [{"ntt_log_n1": {"20": 14}}, {"ntt_log_n1": {"20": 6}}, {"ntt_log_n1": {"12": 6}},
+                {"ntt_log_n1": {"27": 13}}, {"ntt_log_n1": {"14": 9}}, {"merkle_top_log": 9},
+                {"merkle_top_log": 19}, {"grind_ctas_per_sm": 0}, {"grind_ctas_per_sm": 17}]:
+        with pytest.raises(z0p.Z0pError) as e:
+            t.set(t.from_dict(bad), dev)
+        assert e.value.code == 106, bad
+        assert t.to_dict(t.get(dev)) == t.to_dict(good)
+    with pytest.raises(z0p.Z0pError):
+        t.get(64)
+    t.set(t.from_dict(before), dev)

@@ -35,6 +35,18 @@ class AirParams(C.Structure):
     ]
 
 
+class Schedule(C.Structure):
+    _fields_ = [("ntt_log_n1", C.c_uint8 * 32), ("merkle_top_log", C.c_uint32),
+                ("grind_ctas_per_sm", C.c_uint32)]
+
+
+class TuneReport(C.Structure):
+    _fields_ = [("ntt_default_us", C.c_float * 32), ("ntt_best_us", C.c_float * 32),
+                ("merkle_default_us", C.c_float), ("merkle_best_us", C.c_float),
+                ("grind_default_us", C.c_float), ("grind_best_us", C.c_float),
+                ("wall_ms", C.c_float)]
+
+
 class ChaChaState(C.Structure):
     _fields_ = [("key", C.c_uint8 * 32), ("nonce", C.c_uint8 * 12), ("counter", C.c_uint32),
                 ("block", C.c_uint8 * 64), ("used", C.c_uint32)]
@@ -130,6 +142,10 @@ def lib():
             "z0p_gpu_ctx_trim": (C.c_int, [vp]),
             "z0p_gpu_ctx_reserve_group": (C.c_int, [vp, C.c_uint32]),
             "z0p_gpu_blake3_ceiling": (C.c_int, [vp, P(C.c_double)]),
+            "z0p_schedule_default": (C.c_int, [P(Schedule)]),
+            "z0p_gpu_schedule_get": (C.c_int, [C.c_int, P(Schedule)]),
+            "z0p_gpu_schedule_set": (C.c_int, [C.c_int, P(Schedule)]),
+            "z0p_gpu_autotune": (C.c_int, [vp, C.c_uint32, P(Schedule), P(TuneReport)]),
             "z0p_gpu_ctx_stats": (C.c_int, [vp, P(Stats)]),
             "z0p_gpu_ctx_set_profiling": (C.c_int, [vp, C.c_int]),
             "z0p_gpu_ctx_profile": (C.c_int, [vp, C.c_char_p, sz, P(sz)]),

@@ -828,18 +828,33 @@ __global__ void __launch_bounds__(kThreads) range_compose_leaves_kernel(RangeCom
     size_t colstride = (size_t)1 << logm;
     uint32_t v = __ldg(a.lde + row);
     uint32_t zi = __ldg(a.zinv + j), zi2 = __ldg(a.zinv2 + j);
-    uint32_t rec = 0u, pow2 = kR;  // 2^i in Montgomery form
+    // Bit columns four at a time, highest first (columns past nb read as 0):
+    // rec = sum bit_c 2^c by Horner, and per coordinate
+    // sum_c alpha_c bit_c (bit_c - 1) as one lazy four-term dot product per
+    // group (mmul(bit, bit - 1) carries 2^-32 and so does the dot product;
+    // zinv2 = zinv 2^64 restores both at the end).
+    uint32_t rec = 0u;
     E4 acc = {{0u, 0u, 0u, 0u}};
-    for (uint32_t c = 0; c < nb; c++) {
-      uint32_t bit = __ldg(a.lde + (c + 1) * colstride + row);
-      rec = fadd(rec, mmul(bit, pow2));
-      pow2 = fadd(pow2, pow2);
-      // bit * (bit - 1) * zinv: mmul(bit, bit-1) carries 2^-32, zinv2 restores it.
-      uint32_t bterm = mmul(mmul(bit, fsub(bit, 1u)), zi2);
-      const uint32_t* al = a.alphas + 4 * (1 + c);
+    const uint32_t groups = (nb + 3u) >> 2;
+#pragma unroll 2
+    for (uint32_t g = groups; g-- > 0;) {
+      uint32_t b2[4];
+      const uint32_t* al[4];
 #pragma unroll
-      for (int e = 0; e < 4; e++) acc.c[e] = fadd(acc.c[e], mmul(bterm, __ldg(al + e)));
+      for (int i = 3; i >= 0; i--) {
+        const uint32_t c = 4u * g + (uint32_t)i;
+        const uint32_t bit = c < nb ? __ldg(a.lde + (c + 1) * colstride + row) : 0u;
+        rec = fadd(fadd(rec, rec), bit);
+        b2[i] = mmul(bit, fsub_lazy(bit, 1u));
+        al[i] = a.alphas + 4 * (1 + (c < nb ? c : nb - 1u));
+      }
+#pragma unroll
+      for (int e = 0; e < 4; e++)
+        acc.c[e] = fadd(acc.c[e], mdot4(b2[0], __ldg(al[0] + e), b2[1], __ldg(al[1] + e), b2[2],
+                                        __ldg(al[2] + e), b2[3], __ldg(al[3] + e)));
     }
+#pragma unroll
+    for (int e = 0; e < 4; e++) acc.c[e] = mmul(acc.c[e], zi2);
     uint32_t dterm = mmul(fsub(v, rec), zi);
     uint32_t bound = mmul(fsub(v, g_consts[a.slot].value), den[s]);
     const uint32_t* ad = a.alphas;
@@ -1556,6 +1571,55 @@ bool smem_raised(int pass, uint32_t L, size_t smem) {
   return false;
 }
 
+// ------------------------------------------------------------ schedule ----
+namespace {
+constexpr int kMaxDevices = 64;
+std::mutex g_sched_mu;
+Schedule g_sched[kMaxDevices];
+
+Schedule current_schedule() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) dev = 0;
+  std::lock_guard<std::mutex> lk(g_sched_mu);
+  return g_sched[dev];
+}
+}  // namespace
+
+// Pass 1 is instantiated for 2^7..2^13 points and pass 2 for 2^6..2^13.
+void ntt_split_range(uint32_t logn, uint32_t* lo, uint32_t* hi) {
+  if (logn <= 12 || logn > 26) {
+    *lo = 1;
+    *hi = 0;
+    return;
+  }
+  *lo = logn >= 20 ? logn - 13 : 7;
+  *hi = logn - 6 < 13 ? logn - 6 : 13;
+}
+
+uint32_t ntt_default_split(uint32_t logn) { return (logn + 1) / 2; }
+
+bool schedule_valid(const Schedule& s) {
+  for (uint32_t l = 0; l < 32; l++) {
+    if (!s.ntt_log_n1[l]) continue;
+    uint32_t lo, hi;
+    ntt_split_range(l, &lo, &hi);
+    if (s.ntt_log_n1[l] < lo || s.ntt_log_n1[l] > hi) return false;
+  }
+  return s.merkle_top_log >= 10 && s.merkle_top_log <= 18 && s.grind_ctas_per_sm >= 1 &&
+         s.grind_ctas_per_sm <= 16;
+}
+
+Schedule get_schedule(int device) {
+  std::lock_guard<std::mutex> lk(g_sched_mu);
+  return g_sched[device >= 0 && device < kMaxDevices ? device : 0];
+}
+
+void set_schedule(int device, const Schedule& s) {
+  if (device < 0 || device >= kMaxDevices) return;
+  std::lock_guard<std::mutex> lk(g_sched_mu);
+  g_sched[device] = s;
+}
+
 cudaError_t ntt(cudaStream_t st, const Tables& tb, const NttPlan& plan, const uint32_t* in,
                 uint32_t* out, uint32_t* scratch) {
   NttArgs a;
@@ -1589,7 +1653,14 @@ cudaError_t ntt(cudaStream_t st, const Tables& tb, const NttPlan& plan, const ui
     }
     return cudaGetLastError();
   }
-  const uint32_t logn1 = (plan.logn + 1) / 2;
+  const Schedule sched = current_schedule();
+  uint32_t logn1 = ntt_default_split(plan.logn);
+  if (plan.logn < 32 && sched.ntt_log_n1[plan.logn]) {
+    uint32_t lo, hi;
+    ntt_split_range(plan.logn, &lo, &hi);
+    if (sched.ntt_log_n1[plan.logn] >= lo && sched.ntt_log_n1[plan.logn] <= hi)
+      logn1 = sched.ntt_log_n1[plan.logn];
+  }
   const uint32_t logn2 = plan.logn - logn1;
   const uint32_t n1 = 1u << logn1, n2 = 1u << logn2;
   // C = R = 8 columns per CTA (32-byte global segments), 4 for the largest halves.
@@ -1693,7 +1764,8 @@ cudaError_t merkle_build(cudaStream_t st, uint32_t* tree, uint64_t leaves, uint3
   // of merkle_top_kernel. (Starting the top kernel anywhere from 2^12 to 2^18
   // nodes measured within 7% on a 2^21-leaf tree; 2^16 was the fastest.)
   uint32_t level = from;
-  while (level < top && (leaves >> level) > (1ull << 16)) {
+  const uint32_t top_log = current_schedule().merkle_top_log;
+  while (level < top && (leaves >> level) > (1ull << top_log)) {
     uint64_t cnt = leaves >> (level + 1);
     const uint32_t* prev = tree + 8 * (2 * leaves - 2 * (leaves >> level));
     uint32_t* next = tree + 8 * (2 * leaves - 2 * (leaves >> (level + 1)));
@@ -1818,7 +1890,8 @@ cudaError_t grind(cudaStream_t st, uint32_t slot, uint32_t head_len, uint32_t bi
   // the answer: the grid can fill the GPU (four CTAs per SM reach the hash
   // ceiling) without wasting much, but stays below the expected search.
   uint64_t want = (1ull << bits) / kGrindChunk;
-  int ctas = want > (uint64_t)(4 * sms) ? 4 * sms : (int)want;
+  const int per_sm = (int)current_schedule().grind_ctas_per_sm;
+  int ctas = want > (uint64_t)(per_sm * sms) ? per_sm * sms : (int)want;
   if (ctas > max_ctas) ctas = max_ctas;
   if (ctas < sms) ctas = sms;
   Stage stg("grind", st);

@@ -186,6 +186,28 @@ struct TableComposeArgs {
 };
 namespace launch {
 
+// Launch schedule: choices that change how work is split across launches,
+// CTAs and passes but never a result. One per device, process-wide; the
+// launchers read the current device's on every call.
+struct Schedule {
+  // Four-step NTT of length 2^logn (13 <= logn <= 26): log2 of the pass-1
+  // transform length; 0 = the balanced default ceil(logn / 2).
+  uint8_t ntt_log_n1[32] = {};
+  // A Merkle tree's levels go one launch each while they have more than
+  // 2^merkle_top_log nodes; the rest go to one top kernel (10..18).
+  uint32_t merkle_top_log = 16;
+  // Proof-of-work grid: CTAs per SM (1..16, clamped to the occupancy limit).
+  uint32_t grind_ctas_per_sm = 4;
+};
+// Valid pass-1 lengths for an NTT of length 2^logn: [lo, hi] (empty if
+// logn is served by the one-kernel path).
+void ntt_split_range(uint32_t logn, uint32_t* lo, uint32_t* hi);
+uint32_t ntt_default_split(uint32_t logn);
+// Range checks of every field; false names no field (the caller reports).
+bool schedule_valid(const Schedule& s);
+Schedule get_schedule(int device);
+void set_schedule(int device, const Schedule& s);
+
 // Number of kernel launches issued by this library in this process.
 uint64_t launch_count();
 // Optional per-stage timing: when a recorder is installed, every launcher

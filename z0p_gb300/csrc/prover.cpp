@@ -13,6 +13,7 @@
 #include <cuda_runtime.h>
 
 #include <chrono>
+#include <functional>
 #include <map>
 #include <cstdio>
 #include <cstring>
@@ -2704,6 +2705,239 @@ int z0p_gpu_blake3_ceiling(z0p_gpu_ctx* c, double* gcompress_per_s) {
   cudaEventDestroy(e1);
   CK(e);
   *gcompress_per_s = best;
+  return Z0P_OK;
+}
+
+static launch::Schedule from_abi(const z0p_schedule& s) {
+  launch::Schedule o;
+  std::memcpy(o.ntt_log_n1, s.ntt_log_n1, sizeof o.ntt_log_n1);
+  o.merkle_top_log = s.merkle_top_log;
+  o.grind_ctas_per_sm = s.grind_ctas_per_sm;
+  return o;
+}
+
+static z0p_schedule to_abi(const launch::Schedule& s) {
+  z0p_schedule o;
+  std::memcpy(o.ntt_log_n1, s.ntt_log_n1, sizeof o.ntt_log_n1);
+  o.merkle_top_log = s.merkle_top_log;
+  o.grind_ctas_per_sm = s.grind_ctas_per_sm;
+  return o;
+}
+
+int z0p_schedule_default(z0p_schedule* out) {
+  if (!out) return Z0P_ERR_INVALID_ARGUMENT;
+  *out = to_abi(launch::Schedule{});
+  return Z0P_OK;
+}
+
+int z0p_gpu_schedule_get(int device, z0p_schedule* out) {
+  if (!out || device < 0 || device >= 64) return Z0P_ERR_INVALID_ARGUMENT;
+  *out = to_abi(launch::get_schedule(device));
+  return Z0P_OK;
+}
+
+int z0p_gpu_schedule_set(int device, const z0p_schedule* s) {
+  if (!s || device < 0 || device >= 64) return Z0P_ERR_INVALID_ARGUMENT;
+  const launch::Schedule v = from_abi(*s);
+  if (!launch::schedule_valid(v)) {
+    set_reason("schedule field out of range");
+    return Z0P_ERR_INVALID_ARGUMENT;
+  }
+  launch::set_schedule(device, v);
+  return Z0P_OK;
+}
+
+// Device time of `run` (ms): the fastest of `reps` event-timed calls after
+// one untimed call.
+static cudaError_t time_best(z0p_gpu_ctx* c, cudaEvent_t e0, cudaEvent_t e1, int reps,
+                             const std::function<cudaError_t()>& run, float* ms) {
+  cudaError_t e = run();
+  *ms = 0.f;
+  for (int r = 0; r < reps && e == cudaSuccess; r++) {
+    e = cudaEventRecord(e0, c->stream);
+    if (e == cudaSuccess) e = run();
+    if (e == cudaSuccess) e = cudaEventRecord(e1, c->stream);
+    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+    float t = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&t, e0, e1);
+    if (e == cudaSuccess && (r == 0 || t < *ms)) *ms = t;
+  }
+  return e;
+}
+
+static int autotune_locked(z0p_gpu_ctx* c, uint32_t max_log_n, launch::Schedule* best,
+                           z0p_tune_report* rep, cudaEvent_t e0, cudaEvent_t e1) {
+  constexpr float kKeep = 0.97f;  // a candidate must beat the default by 3%
+  constexpr uint32_t B = 16;      // LDE cosets: the production blowup
+  const launch::Schedule base{};
+  *best = base;
+  auto use = [&](const launch::Schedule& s) { launch::set_schedule(c->device, s); };
+
+  // Four-step NTT splits, one LDE of 16 cosets of 2^l per run.
+  const uint32_t top_l = max_log_n < 22 ? max_log_n : 22;
+  if (top_l >= 13) {
+    const size_t n_max = 1ull << top_l;
+    RC(ensure(c, c->coeffs, 4 * n_max));
+    RC(ensure(c, c->lde, 4 * B * n_max));
+    RC(ensure(c, c->scratch, 4 * B * n_max));
+    CK(cudaMemsetAsync(c->coeffs.p, 0x11, 4 * n_max, c->stream));
+  }
+  for (uint32_t l = 13; l <= top_l; l++) {
+    NttPlan plan;
+    plan.logn = l;
+    plan.batch = B;
+    plan.in_div = B;
+    plan.twist_mod = B;
+    plan.twist_shift = 27 - (l + log2u(B));
+    auto run = [&]() {
+      return launch::ntt(c->stream, c->tb, plan, (const uint32_t*)c->coeffs.p, (uint32_t*)c->lde.p,
+                         (uint32_t*)c->scratch.p);
+    };
+    uint32_t lo, hi;
+    launch::ntt_split_range(l, &lo, &hi);
+    const uint32_t def = launch::ntt_default_split(l);
+    float t_def = 0.f, t_best = 0.f;
+    uint32_t pick = 0;
+    for (uint32_t s1 = (def > lo + 2 ? def - 2 : lo); s1 <= hi && s1 <= def + 2; s1++) {
+      launch::Schedule s = base;
+      s.ntt_log_n1[l] = (uint8_t)s1;
+      use(s);
+      float t = 0.f;
+      CK(time_best(c, e0, e1, 3, run, &t));
+      if (s1 == def) t_def = t;
+      if (pick == 0 || t < t_best) {
+        t_best = t;
+        pick = s1;
+      }
+    }
+    if (pick != def && t_best > kKeep * t_def) {
+      pick = def;
+      t_best = t_def;
+    }
+    best->ntt_log_n1[l] = pick == def ? 0 : (uint8_t)pick;
+    if (rep) {
+      rep->ntt_default_us[l] = 1e3f * t_def;
+      rep->ntt_best_us[l] = 1e3f * t_best;
+    }
+  }
+
+  // Merkle top level, on a 2^21-leaf tree (the trace tree of a 2^20-step
+  // proof), every level above the leaves.
+  {
+    const uint64_t leaves = 1ull << 21;
+    RC(ensure(c, c->ttree, 32 * tree_digests(leaves)));
+    uint32_t* tree = (uint32_t*)c->ttree.p;
+    CK(cudaMemsetAsync(tree, 0x5a, 32 * leaves, c->stream));
+    const uint32_t top = 21 - 4;
+    auto run = [&]() {
+      return launch::merkle_build(c->stream, tree, leaves, top, merkle_counter(c), nullptr, 0, 1, 0, 0);
+    };
+    float t_def = 0.f, t_best = 0.f;
+    uint32_t pick = 0;
+    for (uint32_t tl = 12; tl <= 18; tl++) {
+      launch::Schedule s = base;
+      s.merkle_top_log = tl;
+      use(s);
+      float t = 0.f;
+      CK(time_best(c, e0, e1, 3, run, &t));
+      if (tl == base.merkle_top_log) t_def = t;
+      if (pick == 0 || t < t_best) {
+        t_best = t;
+        pick = tl;
+      }
+    }
+    if (t_best > kKeep * t_def) {
+      pick = base.merkle_top_log;
+      t_best = t_def;
+    }
+    best->merkle_top_log = pick;
+    if (rep) {
+      rep->merkle_default_us = 1e3f * t_def;
+      rep->merkle_best_us = 1e3f * t_best;
+    }
+  }
+
+  // Proof-of-work grid: 20-bit searches on eight fixed heads, timed together
+  // (a search's time depends on where its first hit lies); every grid must
+  // find the same nonces.
+  {
+    constexpr int kHeads = 8;
+    RC(ensure_slots(c, kHeads));
+    RC(ensure_hio(c, 16 * kHeads));
+    for (int h = 0; h < kHeads; h++) {
+      uint8_t head[47];
+      for (int i = 0; i < 47; i++) head[i] = (uint8_t)(0x3c ^ (7 * i) ^ (29 * h));
+      set_head(&c->consts[h], head, sizeof head);
+    }
+    CK(push_consts(c, kHeads));
+    auto run = [&]() {  // eight single searches, one after the other, as proofs run them
+      cudaError_t e = cudaSuccess;
+      for (int h = 0; h < kHeads && e == cudaSuccess; h++)
+        e = launch::grind(c->stream, (uint32_t)c->slot + h, 47, 20, grind_state(c),
+                          hio_dev<unsigned long long>(c, 16 * h), 1ull << 40, 1);
+      return e;
+    };
+    float t_def = 0.f, t_best = 0.f;
+    uint32_t pick = 0;
+    unsigned long long nonce0[kHeads] = {};
+    for (uint32_t per : {1u, 2u, 3u, 4u, 6u, 8u}) {
+      launch::Schedule s = base;
+      s.grind_ctas_per_sm = per;
+      use(s);
+      float t = 0.f;
+      CK(time_best(c, e0, e1, 3, run, &t));
+      for (int h = 0; h < kHeads; h++) {
+        unsigned long long res[2];
+        std::memcpy(res, c->hio + 16 * h, 16);  // the last run's result; the stream is idle
+        if (res[1] != 0 || res[0] == ~0ull || (pick != 0 && res[0] != nonce0[h])) {
+          set_reason("autotune: proof-of-work grids disagree on the nonce");
+          return Z0P_ERR_UNSUPPORTED;
+        }
+        nonce0[h] = res[0];
+      }
+      if (per == base.grind_ctas_per_sm) t_def = t;
+      if (pick == 0 || t < t_best) {
+        t_best = t;
+        pick = per;
+      }
+    }
+    if (t_best > kKeep * t_def) {
+      pick = base.grind_ctas_per_sm;
+      t_best = t_def;
+    }
+    best->grind_ctas_per_sm = pick;
+    if (rep) {
+      rep->grind_default_us = 1e3f * t_def;
+      rep->grind_best_us = 1e3f * t_best;
+    }
+  }
+  return Z0P_OK;
+}
+
+int z0p_gpu_autotune(z0p_gpu_ctx* c, uint32_t max_log_n, z0p_schedule* out, z0p_tune_report* rep) {
+  if (!c || !out || max_log_n > 26) return Z0P_ERR_INVALID_ARGUMENT;
+  const auto w0 = std::chrono::steady_clock::now();
+  std::lock_guard<std::mutex> lk(c->mu);
+  c->work_serial++;
+  RC(with_device(c));
+  if (rep) std::memset(rep, 0, sizeof *rep);
+  const launch::Schedule before = launch::get_schedule(c->device);
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  if (cudaEventCreate(&e1) != cudaSuccess) {
+    cudaEventDestroy(e0);
+    set_reason("cudaEventCreate failed");
+    return Z0P_ERR_CUDA;
+  }
+  launch::Schedule best;
+  const int rc = autotune_locked(c, max_log_n, &best, rep, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  launch::set_schedule(c->device, rc == Z0P_OK ? best : before);
+  if (rc != Z0P_OK) return rc;
+  *out = to_abi(best);
+  if (rep)
+    rep->wall_ms = (float)std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - w0).count();
   return Z0P_OK;
 }
 
