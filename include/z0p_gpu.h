@@ -211,10 +211,24 @@ int z0p_gpu_air_prove(z0p_gpu_ctx *ctx, const z0p_air_params *params,
                       z0p_transcript_state *transcript, uint8_t *out, size_t cap,
                       size_t *len);
 /* range::prove (src/range.rs:337-343) followed by Proof::to_bytes
- * (src/range.rs:253-269). */
+ * (src/range.rs:253-269). range::prove's columns each repeat one value, so
+ * the device builds every tree as runs of equal leaves (one chain of node
+ * hashes per run) and every FRI layer as per-coset constants, with the same
+ * bytes as transforming and hashing every row; shapes outside that form
+ * (final layers below 4 values, or an out-of-range value with final layers
+ * below the blowup or fewer than 4 rows) take the row-by-row path. */
 int z0p_gpu_range_prove(z0p_gpu_ctx *ctx, const z0p_range_params *params,
                         z0p_transcript_state *transcript, uint8_t *out, size_t cap,
                         size_t *len);
+/* range::prove_with_columns (src/range.rs:353-375): the caller's value column
+ * and n_bits bit columns, n_rows canonical words each. Any values prove
+ * structurally (invalid columns fail verify). Shapes that differ from the
+ * params are Z0P_ERR_MALFORMED_INPUT (after the params' own checks). */
+int z0p_gpu_range_prove_with_columns(z0p_gpu_ctx *ctx, const z0p_range_params *params,
+                                     const uint32_t *v_col, size_t v_len,
+                                     const uint32_t *const *bit_cols, const size_t *bit_lens,
+                                     size_t n_bit_cols, z0p_transcript_state *transcript,
+                                     uint8_t *out, size_t cap, size_t *out_len);
 
 /* air::prove_with_trace (src/air.rs:381-399): the caller's two columns of
  * n_steps canonical words, each interpolated and extended (no linked

@@ -175,6 +175,8 @@ def lib():
             "zo_range_params_new": (C.c_int, [C.c_uint64] * 5 + [C.c_uint32, C.POINTER(RangeParams)]),
             "zo_range_for_security": (C.c_int, [C.c_uint64, C.c_uint64, C.c_uint32, C.c_uint32, C.POINTER(RangeParams)]),
             "zo_range_prove": (C.c_int, [C.POINTER(RangeParams), vp, C.POINTER(u8p), C.POINTER(sz)]),
+            "zo_range_prove_with_columns": (C.c_int, [C.POINTER(RangeParams), u32p, vp, C.POINTER(u8p),
+                                                      C.POINTER(sz)]),
             "zo_range_verify": (C.c_int, [C.POINTER(RangeParams), C.c_char_p, sz, vp]),
             "zo_fri_commit": (C.c_int, [C.POINTER(FriParams), C.c_int, u32p, sz, C.c_uint64, vp,
                                         C.POINTER(vp), C.POINTER(u8p), C.POINTER(sz)]),
@@ -451,6 +453,20 @@ def air_verify(params: AirParams, proof: bytes, t: Transcript) -> int:
 def range_prove(params: RangeParams, t: Transcript) -> bytes:
     buf, n = C.POINTER(C.c_uint8)(), C.c_size_t()
     rc = lib().zo_range_prove(C.byref(params), t.h, C.byref(buf), C.byref(n))
+    return _take_proof(rc, buf, n)
+
+
+def range_prove_with_columns(params: RangeParams, v_col, bit_cols, t: Transcript) -> bytes:
+    """range.rs:353-375: the caller's columns (value column, then n_bits bit columns)."""
+    import numpy as np
+
+    cols = np.ascontiguousarray(np.concatenate([np.asarray(v_col, dtype=np.uint32)] +
+                                               [np.asarray(b, dtype=np.uint32) for b in bit_cols]))
+    if len(bit_cols) != params.n_bits or cols.size != (params.n_bits + 1) * params.n_rows:
+        raise ValueError("MalformedInput")
+    buf, n = C.POINTER(C.c_uint8)(), C.c_size_t()
+    rc = lib().zo_range_prove_with_columns(C.byref(params), cols.ctypes.data_as(C.POINTER(C.c_uint32)),
+                                           t.h, C.byref(buf), C.byref(n))
     return _take_proof(rc, buf, n)
 
 

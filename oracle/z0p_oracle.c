@@ -2963,18 +2963,43 @@ static ext4 range_composition_at(uint32_t v, const uint32_t *bits, size_t nbits,
 }
 
 /* range.rs:337-343 prove -> 353-375 prove_with_columns -> 425-514 prove_from_columns */
+static int range_prove_cols(const zo_range_params *params, const uint32_t *cols, zo_transcript *t,
+                            uint8_t **proof, size_t *proof_len);
+
 int zo_range_prove(const zo_range_params *params, zo_transcript *t, uint8_t **proof,
                    size_t *proof_len) {
     int rc = range_validate(params);
     if (rc) return rc;
+    size_t n = params->n_rows, ncol = params->n_bits + 1;
+    uint32_t *cols = malloc(ncol * n * 4);
+    for (size_t k = 0; k < ncol; k++) {  /* range.rs:316-330 build_columns */
+        uint32_t v = k == 0 ? params->value
+                            : ((k - 1) < 32 ? (params->value >> (k - 1)) & 1 : 0);
+        for (size_t i = 0; i < n; i++) cols[k * n + i] = v;
+    }
+    rc = range_prove_cols(params, cols, t, proof, proof_len);
+    free(cols);
+    return rc;
+}
+
+/* range.rs:353-375 prove_with_columns: ncol x n_rows words, column-major,
+ * value column first (lengths are the caller's to check). */
+int zo_range_prove_with_columns(const zo_range_params *params, const uint32_t *cols,
+                                zo_transcript *t, uint8_t **proof, size_t *proof_len) {
+    int rc = range_validate(params);
+    if (rc) return rc;
+    return range_prove_cols(params, cols, t, proof, proof_len);
+}
+
+static int range_prove_cols(const zo_range_params *params, const uint32_t *cols, zo_transcript *t,
+                            uint8_t **proof, size_t *proof_len) {
+    int rc;
     size_t n = params->n_rows, m = n * params->blowup, ncol = params->n_bits + 1;
     uint32_t **ldes = malloc(ncol * sizeof(uint32_t *));
     uint32_t **coeffs = malloc(ncol * sizeof(uint32_t *));
-    for (size_t k = 0; k < ncol; k++) {  /* range.rs:316-330 build_columns, :370-374 */
-        uint32_t v = k == 0 ? params->value
-                            : ((k - 1) < 32 ? (params->value >> (k - 1)) & 1 : 0);
+    for (size_t k = 0; k < ncol; k++) {  /* range.rs:370-374 interpolate */
         coeffs[k] = malloc(n * 4);
-        for (size_t i = 0; i < n; i++) coeffs[k][i] = v;
+        memcpy(coeffs[k], cols + k * n, n * 4);
         zo_ntt_inverse(coeffs[k], n);
     }
     range_absorb_params(params, t);  /* range.rs:437 */

@@ -141,6 +141,8 @@ int zo_range_params_new(uint64_t n_rows, uint64_t n_bits, uint64_t blowup,
                         zo_range_params *out);
 int zo_range_for_security(uint64_t n_rows, uint64_t n_bits, uint32_t value,
                           uint32_t target_bits, zo_range_params *out);
+int zo_range_prove_with_columns(const zo_range_params *params, const uint32_t *cols,
+                                zo_transcript *t, uint8_t **proof, size_t *proof_len);
 int zo_range_prove(const zo_range_params *params, zo_transcript *t, uint8_t **proof,
                    size_t *proof_len);
 int zo_range_verify(const zo_range_params *params, const uint8_t *proof, size_t proof_len,

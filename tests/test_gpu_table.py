@@ -80,3 +80,22 @@ def test_table_errors(z0p, gpu_ctx):
         z0p.table.prove_zk(pz, TABLE, 7, z0p.rng.ChaCha20.new(bytes(32), bytes(12)), t, gpu_ctx)
     assert e.value.code == 8
     assert t.export() == before
+
+
+@pytest.mark.parametrize("n,blowup,final,tlen,member", [
+    (8, 8, 4, 4, True), (16, 8, 8, 4, False), (1 << 10, 16, 16, 5, False), (1 << 10, 16, 4, 5, False),
+    (2, 8, 4, 3, True), (1 << 12, 8, 32, 2, False)])
+def test_constant_column_paths_match_oracle(z0p, oracle, gpu_ctx, n, blowup, final, tlen, member):
+    # Members and non-members on the compact path (final >= blowup or a
+    # member), and a non-member with final < blowup on the row-by-row path.
+    rng = random.Random(n + tlen)
+    table = [rng.randrange(P) for _ in range(tlen)]
+    value = table[1] if member else rng.randrange(P)
+    pz = z0p.table.Params.new(n, blowup, 8, final, value).with_cap_height(3)
+    po = oracle.table_params_new(n, blowup, 8, final, value)
+    po.cap_height = 3
+    tg, to = z0p.Transcript(b"tab-c"), oracle.Transcript(b"tab-c")
+    proof = z0p.table.prove(pz, table, tg, gpu_ctx)
+    assert proof == oracle.table_prove(po, table, to)
+    assert tg.export() == to.export()
+    assert (oracle.table_verify(po, table, proof, oracle.Transcript(b"tab-c")) == 0) == member

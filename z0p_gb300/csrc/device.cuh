@@ -356,4 +356,29 @@ __device__ __forceinline__ void blake3_prefixed_leaf(const uint32_t (&d)[NW], ui
   for (int i = 0; i < 8; i++) out[i] = cv[i];
 }
 
+// BLAKE3 of 0x00 || ncols little-endian words (a Merkle leaf over one row,
+// src/merkle.rs:93-110; ncols <= 25, so one or two blocks). w[ncols..32)
+// must be zero.
+__device__ __forceinline__ void row_leaf_digest(const uint32_t (&w)[32], uint32_t ncols,
+                                                uint32_t o[8]) {
+  // 0x00 || row: word i = (w[i-1] >> 24) | (w[i] << 8).
+  const uint32_t len = 4u * ncols + 1u;
+  uint32_t cv[8];
+  iv_words(cv);
+  uint32_t blk[16];
+#pragma unroll
+  for (int i = 0; i < 16; i++) blk[i] = __funnelshift_l(i ? w[i - 1] : 0u, w[i], 8);
+  const bool one = len <= 64u;
+  blake3_compress(cv, blk, 0u, 0u, one ? len : 64u,
+                  one ? (kChunkStart | kChunkEnd | kRoot) : kChunkStart, o);
+  if (!one) {
+#pragma unroll
+    for (int i = 0; i < 16; i++) blk[i] = __funnelshift_l(w[15 + i], w[16 + i], 8);
+    uint32_t o2[8];
+    blake3_compress(o, blk, 0u, 0u, len - 64u, kChunkEnd | kRoot, o2);
+#pragma unroll
+    for (int i = 0; i < 8; i++) o[i] = o2[i];
+  }
+}
+
 }  // namespace z0p

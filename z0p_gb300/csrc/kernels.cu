@@ -562,26 +562,70 @@ __global__ void range_trace_leaves_kernel(const uint32_t* __restrict__ lde,
 #pragma unroll
   for (int c = 0; c < 25; c++)
     if ((uint32_t)c < ncols) w[c] = __ldg(lde + ((size_t)c << (logN + logB)) + u);
-  // 0x00 || row: word i = (w[i-1] >> 24) | (w[i] << 8); one or two blocks.
-  uint32_t len = 4u * ncols + 1u;
-  uint32_t cv[8];
-  iv_words(cv);
-  uint32_t blk[16];
-#pragma unroll
-  for (int i = 0; i < 16; i++) blk[i] = __funnelshift_l(i ? w[i - 1] : 0u, w[i], 8);
-  bool one = len <= 64u;
   uint32_t o[8];
-  blake3_compress(cv, blk, 0u, 0u, one ? len : 64u,
-                  one ? (kChunkStart | kChunkEnd | kRoot) : kChunkStart, o);
-  if (!one) {
-#pragma unroll
-    for (int i = 0; i < 16; i++) blk[i] = __funnelshift_l(w[15 + i], w[16 + i], 8);
-    uint32_t o2[8];
-    blake3_compress(o, blk, 0u, 0u, len - 64u, kChunkEnd | kRoot, o2);
-#pragma unroll
-    for (int i = 0; i < 8; i++) o[i] = o2[i];
-  }
+  row_leaf_digest(w, ncols, o);
   store_digest(leaves + 8 * (size_t)k, o);
+}
+
+// Merkle trees whose leaves repeat in runs (kernels.h, UniformTree): one CTA
+// per tree. Each group's chain is one thread's sequence of node hashes of a
+// digest with itself; the group roots then go up as an ordinary tree in
+// shared memory.
+constexpr uint32_t kUniformMaxGroups = 512;
+__global__ void __launch_bounds__(128) uniform_trees_kernel(const UniformTree* trees) {
+  __shared__ uint32_t top[2 * kUniformMaxGroups * 8];
+  const UniformTree t = trees[blockIdx.x];
+  if (t.G == 0 || t.G > kUniformMaxGroups || (t.G & (t.G - 1u)) || t.logS > 31 ||
+      (t.row ? (t.seed_words == 0 || t.seed_words > 25) : t.seed_words != 16))
+    return;  // the launcher's caller validates; never index past the buffers
+  const uint32_t L = t.logS + 1;
+  for (uint32_t g = threadIdx.x; g < t.G; g += blockDim.x) {
+    const uint32_t* sd = t.seeds + (size_t)g * t.seed_words;
+    uint32_t d[8];
+    if (!t.row) {
+      uint32_t m[16];
+#pragma unroll
+      for (int i = 0; i < 16; i++) m[i] = sd[i];
+      blake3_leaf64(m, d);
+    } else {
+      uint32_t w[32];
+#pragma unroll
+      for (int c = 0; c < 32; c++) w[c] = (uint32_t)c < t.seed_words ? sd[c] : 0u;
+      row_leaf_digest(w, t.seed_words, d);
+    }
+    uint32_t* o = t.out + 8 * ((size_t)g * L);
+    store_digest(o, d);
+    for (uint32_t l = 1; l < L; l++) {
+      uint32_t n[8];
+      blake3_node(d, d, n);
+#pragma unroll
+      for (int i = 0; i < 8; i++) d[i] = n[i];
+      store_digest(o + 8 * l, d);
+    }
+#pragma unroll
+    for (int i = 0; i < 8; i++) top[8 * g + i] = d[i];
+  }
+  __syncthreads();
+  uint32_t* dst = t.out + 8 * ((size_t)t.G * L);
+  for (uint32_t g = threadIdx.x; g < t.G; g += blockDim.x) store_digest(dst + 8 * g, top + 8 * g);
+  uint32_t off = 0, cnt = t.G;
+  while (cnt > 1) {
+    for (uint32_t i = threadIdx.x; i < cnt / 2; i += blockDim.x) {
+      uint32_t a[8], b[8], n[8];
+#pragma unroll
+      for (int w = 0; w < 8; w++) {
+        a[w] = top[8 * (off + 2 * i) + w];
+        b[w] = top[8 * (off + 2 * i + 1) + w];
+      }
+      blake3_node(a, b, n);
+#pragma unroll
+      for (int w = 0; w < 8; w++) top[8 * (off + cnt + i) + w] = n[w];
+      store_digest(dst + 8 * (off + cnt + i), n);
+    }
+    off += cnt;
+    cnt >>= 1;
+    __syncthreads();
+  }
 }
 
 // One tree level; `cap` (may be null) receives a second copy of the level
@@ -1897,6 +1941,14 @@ cudaError_t grind(cudaStream_t st, uint32_t slot, uint32_t head_len, uint32_t bi
   Stage stg("grind", st);
   stg.launched();
   grind_kernel<<<dim3(ctas, nproofs), kGrindThreads, 0, st>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t uniform_trees(cudaStream_t st, const UniformTree* trees, uint32_t ntrees) {
+  if (ntrees == 0) return cudaSuccess;
+  Stage stg("uniform_trees", st);
+  stg.launched();
+  uniform_trees_kernel<<<ntrees, 128, 0, st>>>(trees);
   return cudaGetLastError();
 }
 

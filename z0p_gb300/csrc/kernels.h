@@ -184,6 +184,21 @@ struct TableComposeArgs {
   uint32_t* leaves;
   uint32_t logN, logB, r;
 };
+// A Merkle tree whose leaves repeat in runs (a constant trace, or an FRI
+// layer of per-coset constants): G groups of 2^logS equal consecutive leaves,
+// group g's leaf hashed from seed g. Every node of a group's subtree at level
+// l is one digest, chain[g][l]; the G group roots then form an ordinary
+// tree. `out` (16-byte aligned) receives chain[g][l] at digest g * (logS + 1)
+// + l, then the tree over the roots, level-contiguous (2G - 1 digests).
+struct UniformTree {
+  const uint32_t* seeds;  // G seeds of seed_words words each
+  uint32_t* out;
+  uint32_t G;             // power of two, <= 512
+  uint32_t logS;
+  uint32_t row;           // 0: a 64-byte block leaf (16 words); 1: a 0x00-prefixed row
+  uint32_t seed_words;    // 16 for a block; 1..25 for a row
+};
+
 namespace launch {
 
 // Launch schedule: choices that change how work is split across launches,
@@ -207,6 +222,9 @@ uint32_t ntt_default_split(uint32_t logn);
 bool schedule_valid(const Schedule& s);
 Schedule get_schedule(int device);
 void set_schedule(int device, const Schedule& s);
+
+// One CTA per tree (kernels.h, UniformTree); `trees` is device-readable.
+cudaError_t uniform_trees(cudaStream_t st, const UniformTree* trees, uint32_t ntrees);
 
 // Number of kernel launches issued by this library in this process.
 uint64_t launch_count();

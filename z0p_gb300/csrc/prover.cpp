@@ -12,6 +12,7 @@
 // The host holds the transcript; each bracket is one stream synchronisation.
 #include <cuda_runtime.h>
 
+#include <array>
 #include <chrono>
 #include <functional>
 #include <map>
@@ -1031,6 +1032,334 @@ int table_shape(const z0p_table_params& p, const uint32_t* table, size_t tlen, u
   return Z0P_OK;
 }
 
+// ------------------------------------------------- constant traces ----
+// range::prove builds every column as one repeated value (src/range.rs:
+// 316-330), and table::prove one column of one value (src/table.rs:305-317).
+// The coset LDE of a constant is that constant, so:
+//  - every trace row is the same, and each level of the trace tree is one
+//    repeated digest;
+//  - the composition is one Ext4 constant K_j per coset j: for range
+//    (src/range.rs:678-774), (v - sum 2^c b_c) zinv_j alpha_d, since the
+//    boolean terms vanish (bits are 0 or 1) and so does the boundary term
+//    (v = value); for table (src/table.rs:646-660), alpha_m prod_k (v - T_k)
+//    zinv_j. K is zero for an in-range value or a table member;
+//  - an arity-4 fold of four equal values returns that value (the three
+//    non-constant components of the quad are zero), and the four rows of a
+//    quad share their coset while the layer holds at least 4B values. So
+//    FRI layer l, of length L >= B, holds K_j at position x with
+//    j = brev(x >> (log L - log B), log B): runs of L / B equal values, in
+//    every layer, whatever the fold challenges.
+// Each tree is then G groups of equal leaves (UniformTree): one chain of
+// node hashes per group and a tree over the group roots. The proof bytes are
+// the generic path's (tests compare both against the oracle).
+struct CompactTree {
+  const uint8_t* out;  // UniformTree::out, as the host holds it
+  uint32_t G, logS;
+  const uint8_t* node(uint32_t l, uint64_t i) const {
+    if (l <= logS) return out + 32 * ((i >> (logS - l)) * (logS + 1) + l);
+    const uint32_t tl = l - logS;
+    return out + 32 * ((uint64_t)G * (logS + 1) + (2ull * G - 2ull * (G >> tl)) + i);
+  }
+  // Siblings from the leaf up to the cap (`steps` levels) into buf.
+  const uint8_t* path(uint64_t leaf, uint32_t steps, std::vector<uint8_t>& buf) const {
+    buf.resize(32 * (size_t)steps);
+    for (uint32_t l = 0; l < steps; l++) std::memcpy(&buf[32 * l], node(l, (leaf >> l) ^ 1), 32);
+    return buf.data();
+  }
+};
+
+// A compact tree as one launch of uniform_trees builds it: its seeds go in,
+// its digests come back into `bytes`.
+struct ConstTree {
+  uint32_t G = 1, logS = 0, row = 0, words = 16;
+  std::vector<uint32_t> seeds;  // G x words
+  std::vector<uint8_t> bytes;   // G (logS + 1) + 2G - 1 digests
+  CompactTree view() const { return CompactTree{bytes.data(), G, logS}; }
+};
+
+// Builds every tree in one launch through the mapped buffer and waits.
+int build_const_trees(z0p_gpu_ctx* c, std::vector<ConstTree*>& trees, const char* site) {
+  size_t at = 0;
+  auto take = [&](size_t bytes) {
+    size_t r = at;
+    at += (bytes + 15) & ~(size_t)15;
+    return r;
+  };
+  const size_t n = trees.size();
+  const size_t desc = take(sizeof(UniformTree) * n);
+  std::vector<size_t> sd(n), od(n);
+  for (size_t i = 0; i < n; i++) {
+    const ConstTree& t = *trees[i];
+    if (t.G == 0 || t.G > 512 || (t.G & (t.G - 1)) || t.seeds.size() != (size_t)t.G * t.words) {
+      set_reason("internal error: compact tree shape");
+      return Z0P_ERR_CUDA;
+    }
+    sd[i] = take(4 * t.seeds.size());
+    od[i] = take(32ull * ((uint64_t)t.G * (t.logS + 1) + 2 * t.G - 1));
+  }
+  RC(ensure_hio(c, at));
+  UniformTree* u = reinterpret_cast<UniformTree*>(c->hio + desc);
+  for (size_t i = 0; i < n; i++) {
+    const ConstTree& t = *trees[i];
+    std::memcpy(c->hio + sd[i], t.seeds.data(), 4 * t.seeds.size());
+    u[i] = UniformTree{hio_dev<uint32_t>(c, sd[i]), hio_dev<uint32_t>(c, od[i]), t.G, t.logS, t.row,
+                       t.words};
+    c->h2d += 4 * t.seeds.size() + sizeof(UniformTree);
+  }
+  CK(launch::uniform_trees(c->stream, hio_dev<UniformTree>(c, desc), (uint32_t)n));
+  CK(sync(c, site));
+  for (size_t i = 0; i < n; i++) {
+    ConstTree& t = *trees[i];
+    t.bytes.assign(c->hio + od[i], c->hio + od[i] + 32ull * ((uint64_t)t.G * (t.logS + 1) + 2 * t.G - 1));
+    c->d2h += t.bytes.size();
+  }
+  return Z0P_OK;
+}
+
+// FRI over a composition that is one Ext4 constant per coset (kc: 4B words,
+// canonical; null: zero), as fri::commit_ext_evals then fri::open
+// (src/fri.rs:551-666) drive the transcript, from compact trees. Layer l of
+// length 2^logL >= B holds K_j at x, j = brev(x >> (logL - logB), logB).
+struct ConstFri {
+  const uint32_t* kc = nullptr;
+  uint32_t logB = 0;
+  std::vector<ConstTree> trees;  // per layer
+  FriOut fo;
+  const uint32_t* val(uint32_t logL, uint64_t x) const {
+    static const uint32_t z4[4] = {0, 0, 0, 0};
+    return kc ? kc + 4 * brev(x >> (logL - logB), logB) : z4;
+  }
+};
+
+bool const_fri_ok(const FriShape& s, bool zero, uint64_t rows, uint64_t blowup) {
+  if (s.len.back() < 4) return false;  // quad leaves in every layer
+  for (size_t l = 0; l < s.len.size(); l++)
+    if (s.leaves[l] * 4 != s.len[l]) return false;
+  if (zero) return true;
+  return rows >= 4 && s.len.back() >= blowup && blowup <= 512;
+}
+
+int const_fri(z0p_gpu_ctx* c, const FriShape& s, const FriParams& fp, uint64_t poly_len,
+              uint64_t degree_bound, Transcript* const* ts, uint32_t K, ConstFri* fr) {
+  const size_t nl = s.len.size();
+  std::vector<ConstTree*> all;
+  for (uint32_t k = 0; k < K; k++) {
+    ConstFri& f = fr[k];
+    const uint32_t logB = f.logB;
+    f.trees.assign(nl, ConstTree{});
+    for (size_t l = 0; l < nl; l++) {
+      ConstTree& t = f.trees[l];
+      const uint32_t logL = log2u(s.len[l]), logNL = logL - 2;
+      if (!f.kc) {
+        t.G = 1;
+        t.logS = logNL;
+      } else if (logL >= logB + 2) {
+        t.G = 1u << logB;
+        t.logS = logNL - logB;
+      } else {
+        t.G = 1u << logNL;
+        t.logS = 0;
+      }
+      t.seeds.resize(16ull * t.G);
+      for (uint32_t g = 0; g < t.G; g++) {
+        const uint64_t leaf = (uint64_t)g << t.logS;  // any leaf of the group
+        for (int q = 0; q < 4; q++) std::memcpy(&t.seeds[16 * g + 4 * q], f.val(logL, 4 * leaf + q), 16);
+      }
+      all.push_back(&t);
+    }
+  }
+  RC(build_const_trees(c, all, "cap"));
+  uint8_t dims[24];  // src/fri.rs:1450-1456
+  for (int i = 0; i < 8; i++) {
+    dims[i] = (uint8_t)(s.m >> (8 * i));
+    dims[8 + i] = (uint8_t)(poly_len >> (8 * i));
+    dims[16 + i] = (uint8_t)(degree_bound >> (8 * i));
+  }
+  const uint64_t F = s.len.back();
+  for (uint32_t k = 0; k < K; k++) {
+    Transcript& t = *ts[k];
+    ConstFri& f = fr[k];
+    transcript_absorb(t, "fri-dims", dims, 24);
+    f.fo.caps.assign(nl, {});
+    for (size_t l = 0; l < nl; l++) {
+      const CompactTree tr = f.trees[l].view();
+      const uint32_t steps = s.depth[l] - s.drop[l];
+      std::vector<uint8_t>& cap = f.fo.caps[l];
+      cap.resize(32ull << s.drop[l]);
+      for (uint64_t i = 0; i < (1ull << s.drop[l]); i++) std::memcpy(&cap[32 * i], tr.node(steps, i), 32);
+      for (size_t i = 0; i < cap.size() / 32; i++) transcript_absorb(t, "fri-layer-root", &cap[32 * i], 32);
+      if (l + 1 == nl) break;
+      uint32_t ch[4];
+      for (int r = 0; r < 3; r++) challenge_ext(t, "fri-fold", ch);  // the values do not depend on them
+    }
+    f.fo.final_vals.resize(4 * F);
+    const uint32_t logF = log2u(F);
+    for (uint64_t x = 0; x < F; x++) std::memcpy(&f.fo.final_vals[4 * x], f.val(logF, x), 16);
+    transcript_absorb(t, "fri-final", (const uint8_t*)f.fo.final_vals.data(), 16 * F);
+    f.fo.nonce = 0;
+  }
+  if (fp.grinding_bits > 0) {  // src/fri.rs:645-650
+    RC(ensure_slots(c, K));
+    RC(ensure_hio(c, 16ull * K));
+    size_t head_len = 0;
+    for (uint32_t k = 0; k < K; k++) {
+      std::vector<uint8_t> head = pow_head(*ts[k], "fri-pow");
+      set_head(&c->consts[k], head.data(), head.size());
+      head_len = head.size();
+    }
+    CK(push_consts(c, K));
+    CK(launch::grind(c->stream, (uint32_t)c->slot, (uint32_t)head_len, fp.grinding_bits, grind_state(c),
+                     hio_dev<unsigned long long>(c, 0), 1ull << 40, K));
+    CK(sync(c, "grind"));
+    for (uint32_t k = 0; k < K; k++) {
+      unsigned long long res[2];
+      std::memcpy(res, c->hio + 16 * k, 16);
+      c->d2h += 16;
+      if (res[1] != 0 || res[0] == ~0ull) {
+        set_reason("proof-of-work search reached its nonce cap without a solution");
+        return Z0P_ERR_DEVICE_TIMEOUT;
+      }
+      fr[k].fo.nonce = res[0];
+      uint8_t nb[8];
+      for (int i = 0; i < 8; i++) nb[i] = (uint8_t)(res[0] >> (8 * i));
+      transcript_absorb(*ts[k], "fri-pow", nb, 8);
+    }
+  }
+  for (uint32_t k = 0; k < K; k++) {
+    fr[k].fo.indices.resize(fp.num_queries);
+    for (uint64_t i = 0; i < fp.num_queries; i++)
+      fr[k].fo.indices[i] = challenge_index(*ts[k], "fri-query", s.m);
+  }
+  return Z0P_OK;
+}
+
+// Commitment::to_bytes and Proof::to_bytes (src/fri.rs:352-368, 896-904)
+// of a ConstFri.
+void write_const_fri(Writer& w, const FriShape& s, const ConstFri& f, uint64_t poly_len,
+                     uint64_t degree_bound) {
+  write_fri_commitment(w, s, f.fo, poly_len, degree_bound);
+  const uint64_t F = s.len.back();
+  const size_t nl = s.len.size();
+  w.u32((uint32_t)F);
+  w.bytes(f.fo.final_vals.data(), 16 * F);
+  w.u64(f.fo.nonce);
+  w.u32((uint32_t)f.fo.indices.size());
+  std::vector<uint8_t> pbuf;
+  for (size_t qi = 0; qi < f.fo.indices.size(); qi++) {
+    w.u32((uint32_t)(nl - 1));
+    uint64_t index = f.fo.indices[qi];
+    for (size_t d = 0; d + 1 < nl; d++) {
+      const uint32_t logL = log2u(s.len[d]);
+      const uint64_t leaf = index / 4;
+      for (int q = 0; q < 4; q++) {
+        const uint32_t* v = f.val(logL, 4 * leaf + q);
+        for (int e = 0; e < 4; e++) w.u32(v[e]);
+      }
+      const uint32_t steps = s.depth[d] - s.drop[d];
+      write_path(w, f.trees[d].view().path(leaf, steps, pbuf), leaf, steps);
+      index /= 4;
+    }
+  }
+}
+
+// The trace trees of constant rows: K rows of `words` words, one tree of m
+// equal leaves each; returns the trees (digest chains) and their caps.
+int const_trace_trees(z0p_gpu_ctx* c, const std::vector<std::vector<uint32_t>>& rows,
+                      uint32_t logm, uint32_t tdrop, std::vector<ConstTree>* trees,
+                      std::vector<std::vector<uint8_t>>* caps) {
+  const size_t K = rows.size();
+  trees->assign(K, ConstTree{});
+  std::vector<ConstTree*> all;
+  for (size_t k = 0; k < K; k++) {
+    ConstTree& t = (*trees)[k];
+    t.G = 1;
+    t.logS = logm;
+    t.row = 1;
+    t.words = (uint32_t)rows[k].size();
+    t.seeds = rows[k];
+    all.push_back(&t);
+  }
+  RC(build_const_trees(c, all, "cap"));
+  caps->assign(K, {});
+  for (size_t k = 0; k < K; k++) {
+    const CompactTree tt = (*trees)[k].view();
+    (*caps)[k].resize(32ull << tdrop);
+    for (uint64_t i = 0; i < (1ull << tdrop); i++)
+      std::memcpy(&(*caps)[k][32 * i], tt.node(logm - tdrop, i), 32);
+  }
+  return Z0P_OK;
+}
+
+// table::prove on its constant column (src/table.rs:305-317 proves
+// vec![value; n]): the trace tree is one chain of equal leaves and the
+// composition (src/table.rs:646-660) is alpha_m prod_k (value - T_k) zinv_j
+// per coset (the boundary term vanishes, v = value); see range_prove_const.
+int table_prove_const(z0p_gpu_ctx* c, const z0p_table_params& p, const uint32_t* table, size_t tlen,
+                      const FriParams& fp, const FriShape& s, uint64_t need,
+                      z0p_transcript_state* tsp, uint8_t* out) {
+  const uint64_t N = p.n_rows, B = p.blowup, m = N * B;
+  const uint32_t logB = log2u(B), logm = log2u(m);
+  const uint32_t tdrop = p.cap_height < logm ? (uint32_t)p.cap_height : logm;
+  const uint32_t tsteps = logm - tdrop;
+  z0p_transcript_state work = *tsp;
+  Transcript t(&work);
+  {  // absorb_params (src/table.rs:540-554)
+    std::vector<uint8_t> pb(56 + 4 * tlen);
+    auto p64 = [&](size_t off, uint64_t v) { for (int i = 0; i < 8; i++) pb[off + i] = (uint8_t)(v >> (8 * i)); };
+    auto p32 = [&](size_t off, uint32_t v) { for (int i = 0; i < 4; i++) pb[off + i] = (uint8_t)(v >> (8 * i)); };
+    p64(0, p.n_rows); p64(8, p.blowup); p64(16, p.num_queries); p64(24, p.final_size);
+    p32(32, p.grinding_bits); p64(36, p.cap_height); p32(44, p.value); p64(48, tlen);
+    for (size_t i = 0; i < tlen; i++) p32(56 + 4 * i, table[i]);
+    transcript_absorb(t, "table/params", pb.data(), pb.size());
+  }
+  std::vector<ConstTree> ttrees;
+  std::vector<std::vector<uint8_t>> tcap;
+  RC(const_trace_trees(c, {{p.value}}, logm, tdrop, &ttrees, &tcap));  // from_flat(.., 4) leaves
+  transcript_absorb(t, "table/column", tcap[0].data(), tcap[0].size());
+  uint32_t am[4], ab[4];
+  challenge_ext(t, "table/alpha", am);
+  challenge_ext(t, "table/alpha", ab);
+  uint32_t prod = 1;
+  for (size_t i = 0; i < tlen; i++) prod = fmul(prod, fsub(p.value, table[i]));
+  std::vector<uint32_t> kc;
+  ConstFri fr;
+  fr.logB = logB;
+  if (prod) {
+    kc.assign(4 * B, 0u);
+    const uint32_t wB = two_adic_generator(logB);
+    uint32_t xn = fpow(GENERATOR, N);  // x^N on coset j: 31^N omega_B^j
+    for (uint64_t j = 0; j < B; j++) {
+      const uint32_t base = fmul(prod, finv(fsub(xn, 1)));
+      for (int e = 0; e < 4; e++) kc[4 * j + e] = fmul(base, am[e]);
+      xn = fmul(xn, wB);
+    }
+    fr.kc = kc.data();
+  }
+  const uint64_t bound = membership_bound(tlen, N, 0);
+  Transcript* ts[1] = {&t};
+  RC(const_fri(c, s, fp, m, bound, ts, 1, &fr));
+  Writer w(out, need);  // table::Proof::to_bytes (src/table.rs:244-262)
+  w.byte(6);
+  w.u32((uint32_t)(tcap[0].size() / 32));
+  w.bytes(tcap[0].data(), tcap[0].size());
+  write_const_fri(w, s, fr, m, bound);
+  w.u32((uint32_t)fr.fo.indices.size());
+  const CompactTree tt = ttrees[0].view();
+  std::vector<uint8_t> pbuf;
+  for (size_t qi = 0; qi < fr.fo.indices.size(); qi++) {
+    const uint64_t index = brev(fr.fo.indices[qi], logm);
+    w.u64(index);
+    w.u32(p.value);
+    write_path(w, tt.path(index, tsteps, pbuf), index, tsteps);
+  }
+  if (w.n != need) {
+    set_reason("internal error: proof length differs from its shape");
+    return Z0P_ERR_CUDA;
+  }
+  *tsp = work;
+  return Z0P_OK;
+}
+
 int table_prove_dev(z0p_gpu_ctx* c, const z0p_table_params& p, const uint32_t* table, size_t tlen,
                     uint64_t n_rand, const uint32_t* rand, z0p_transcript_state* tsp,
                     uint8_t* out) {
@@ -1038,6 +1367,12 @@ int table_prove_dev(z0p_gpu_ctx* c, const z0p_table_params& p, const uint32_t* t
   FriShape s;
   uint64_t need = 0;
   RC(table_shape(p, table, tlen, n_rand, &fp, &s, &need));
+  if (n_rand == 0) {
+    uint32_t prod = 1;
+    for (size_t i = 0; i < tlen; i++) prod = fmul(prod, fsub(p.value, table[i]));
+    if (const_fri_ok(s, prod == 0, p.n_rows, p.blowup))
+      return table_prove_const(c, p, table, tlen, fp, s, need, tsp, out);
+  }
   const uint64_t N = p.n_rows, B = p.blowup, Lp = padded_len(N, n_rand), m = Lp * B;
   const uint32_t logN = log2u(N), logL = log2u(Lp), logB = log2u(B), logm = logL + logB;
   const uint32_t r = (uint32_t)(Lp / N);
@@ -1334,13 +1669,93 @@ int air_prove(z0p_gpu_ctx* c, const AirTask* tasks, uint32_t K) {
   return Z0P_OK;
 }
 
-// src/range.rs:337-343 -> 353-375 -> 425-514 on the device, for K proofs of
-// one shape in lockstep.
-int range_prove(z0p_gpu_ctx* c, const RangeTask* tasks, uint32_t K) {
-  FriParams fp;
-  FriShape s;
-  uint64_t need = 0;
-  RC(check_group(tasks, K, range_shape, range_size, same_range_shape, &fp, &s, &need));
+bool range_const_ok(const z0p_range_params& p, const FriShape& s) {
+  return const_fri_ok(s, p.value < (1u << p.n_bits), p.n_rows, p.blowup);
+}
+
+int range_prove_const(z0p_gpu_ctx* c, const RangeTask* tasks, uint32_t K, const FriParams& fp,
+                      const FriShape& s, uint64_t need) {
+  const z0p_range_params& p0 = *tasks[0].p;
+  const uint64_t N = p0.n_rows, B = p0.blowup, m = N * B, ncol = p0.n_bits + 1;
+  const uint32_t logB = log2u(B), logm = log2u(m);
+  const uint32_t tdrop = p0.cap_height < logm ? (uint32_t)p0.cap_height : logm;
+  const uint32_t tsteps = logm - tdrop;
+  std::vector<std::vector<uint32_t>> rows(K);
+  for (uint32_t k = 0; k < K; k++) {
+    const z0p_range_params& p = *tasks[k].p;
+    rows[k].assign(ncol, 0u);
+    rows[k][0] = p.value;  // build_columns (src/range.rs:316-330)
+    for (uint64_t j = 0; j < p.n_bits; j++) rows[k][1 + j] = (p.value >> j) & 1u;
+    uint8_t pb[56];  // absorb_params (src/range.rs:634-645)
+    auto p64 = [&](int off, uint64_t x) { for (int i = 0; i < 8; i++) pb[off + i] = (uint8_t)(x >> (8 * i)); };
+    auto p32 = [&](int off, uint32_t x) { for (int i = 0; i < 4; i++) pb[off + i] = (uint8_t)(x >> (8 * i)); };
+    p64(0, p.n_rows); p64(8, p.n_bits); p64(16, p.blowup); p64(24, p.num_queries);
+    p64(32, p.final_size); p32(40, p.grinding_bits); p64(44, p.cap_height); p32(52, p.value);
+    transcript_absorb(*tasks[k].ts, "range/params", pb, 56);
+  }
+  std::vector<ConstTree> ttrees;
+  std::vector<std::vector<uint8_t>> tcap;
+  RC(const_trace_trees(c, rows, logm, tdrop, &ttrees, &tcap));
+  // Composition (src/range.rs:678-774) on coset j: (value - rec) zinv_j alpha_d.
+  const uint32_t gN = fpow(GENERATOR, N), wB = two_adic_generator(logB);
+  std::vector<std::vector<uint32_t>> kc(K);
+  std::vector<ConstFri> fr(K);
+  std::vector<Transcript*> ts(K);
+  for (uint32_t k = 0; k < K; k++) {
+    ts[k] = tasks[k].ts;
+    transcript_absorb(*ts[k], "range/column", tcap[k].data(), tcap[k].size());
+    uint32_t alpha_d[4];
+    for (uint64_t i = 0; i < ncol + 1; i++) {  // decomposition, n_bits booleans, boundary
+      uint32_t a[4];
+      challenge_ext(*ts[k], "range/alpha", a);
+      if (i == 0) std::memcpy(alpha_d, a, 16);
+    }
+    const uint32_t value = tasks[k].p->value, rec = value & ((1u << p0.n_bits) - 1u);
+    fr[k].logB = logB;
+    if (value != rec) {
+      kc[k].assign(4 * B, 0u);
+      uint32_t xn = gN;  // x^N on coset j: 31^N omega_B^j
+      for (uint64_t j = 0; j < B; j++) {
+        const uint32_t base = fmul(fsub(value, rec), finv(fsub(xn, 1)));
+        for (int e = 0; e < 4; e++) kc[k][4 * j + e] = fmul(base, alpha_d[e]);
+        xn = fmul(xn, wB);
+      }
+      fr[k].kc = kc[k].data();
+    }
+  }
+  RC(const_fri(c, s, fp, m, N - 1, ts.data(), K, fr.data()));
+  std::vector<uint8_t> pbuf;
+  for (uint32_t k = 0; k < K; k++) {
+    const z0p_range_params& p = *tasks[k].p;
+    Writer w(tasks[k].out, need);  // range::Proof::to_bytes (src/range.rs:253-269)
+    w.byte(6);
+    w.u32((uint32_t)(tcap[k].size() / 32));
+    w.bytes(tcap[k].data(), tcap[k].size());
+    write_const_fri(w, s, fr[k], m, N - 1);
+    w.u32((uint32_t)fr[k].fo.indices.size());
+    const CompactTree tt = ttrees[k].view();
+    for (size_t qi = 0; qi < fr[k].fo.indices.size(); qi++) {
+      const uint64_t index = brev(fr[k].fo.indices[qi], logm);
+      w.u64(index);
+      w.u32(rows[k][0]);
+      w.u32((uint32_t)p.n_bits);
+      for (uint64_t b = 0; b < p.n_bits; b++) w.u32(rows[k][1 + b]);
+      write_path(w, tt.path(index, tsteps, pbuf), index, tsteps);
+    }
+    if (w.n != need) {
+      set_reason("internal error: proof length differs from its shape");
+      return Z0P_ERR_CUDA;
+    }
+  }
+  return Z0P_OK;
+}
+
+// src/range.rs:353-375 -> 425-514 on the device for any columns, for K
+// proofs of one shape in lockstep: the columns of range::prove (host_cols
+// null: value and its bits, filled on the device) or, for K = 1, the
+// caller's (n_bits + 1) x n_rows words, column-major, value column first.
+int range_prove_columns(z0p_gpu_ctx* c, const RangeTask* tasks, uint32_t K, const FriParams& fp,
+                        const FriShape& s, uint64_t need, const uint32_t* host_cols) {
   const z0p_range_params& p0 = *tasks[0].p;
   const uint64_t N = p0.n_rows, B = p0.blowup, m = N * B, ncol = p0.n_bits + 1;
   const uint32_t logN = log2u(N), logB = log2u(B), logm = logN + logB;
@@ -1368,9 +1783,10 @@ int range_prove(z0p_gpu_ctx* c, const RangeTask* tasks, uint32_t K) {
   // first) then the alphas (ncol + 1 Ext4 per proof).
   HioPlan h;
   RC(plan_hio(c, s, p0.num_queries, tdrop, (uint32_t)ncol + 8 * tsteps, K, &h,
-              4 * ncol + 16 * (ncol + 1)));
+              4 * ncol + 16 * (ncol + 1) + 16));
   uint32_t* hvals = reinterpret_cast<uint32_t*>(c->hio + h.extra);
   uint32_t* halpha = hvals + ncol * K;
+  const size_t bad_at = h.extra + (4 * ncol + 16 * (ncol + 1)) * K;  // caller's columns: a non-canonical value
   const uint32_t* dvals = hio_dev<uint32_t>(c, h.extra);
   const uint32_t* dalpha = dvals + ncol * K;
   c->h2d += (4 * ncol + 16 * (ncol + 1)) * K;
@@ -1391,7 +1807,14 @@ int range_prove(z0p_gpu_ctx* c, const RangeTask* tasks, uint32_t K) {
     c->consts[k].value = p.value;
   }
   CK(push_consts(c, K));
-  CK(launch::fill_constant_columns(st, cols, (uint32_t)N, (uint32_t)ncol, dvals, K));
+  if (host_cols) {
+    CK(cudaMemcpyAsync(cols, host_cols, 4 * N * ncol, cudaMemcpyHostToDevice, st));
+    c->h2d += 4 * N * ncol;
+    *reinterpret_cast<unsigned int*>(c->hio + bad_at) = 0u;
+    CK(launch::check_canonical(st, cols, N * ncol, hio_dev<unsigned int>(c, bad_at)));
+  } else {
+    CK(launch::fill_constant_columns(st, cols, (uint32_t)N, (uint32_t)ncol, dvals, K));
+  }
   NttPlan ip;
   ip.logn = logN; ip.batch = (uint32_t)(ncol * K); ip.inverse = 1; ip.post_gamma = 1;
   CK(launch::ntt(st, c->tb, ip, cols, coeffs, (uint32_t*)c->scratch.p));
@@ -1406,6 +1829,10 @@ int range_prove(z0p_gpu_ctx* c, const RangeTask* tasks, uint32_t K) {
                           0, K, ttree_words, tcap_stride));
   CK(launch::coset_zinv(st, c->tb, zinv, zinv2, logB, to_mont(fpow(GENERATOR, N)), nullptr, slot));
   CK(sync(c, "cap"));
+  if (host_cols && *reinterpret_cast<volatile unsigned int*>(c->hio + bad_at)) {
+    set_reason("field elements must be canonical (< p)");
+    return Z0P_ERR_MALFORMED_INPUT;
+  }
   std::vector<std::vector<uint8_t>> column_cap(K);
   for (uint32_t k = 0; k < K; k++) {
     const uint8_t* cap = c->hio + h.trace_cap + k * h.trace_cap_bytes;
@@ -1466,6 +1893,19 @@ int range_prove(z0p_gpu_ctx* c, const RangeTask* tasks, uint32_t K) {
     }
   }
   return Z0P_OK;
+}
+
+// src/range.rs:337-343 (range::prove) for K proofs of one shape in lockstep:
+// the constant-trace path whenever its conditions hold, else the columns path.
+int range_prove(z0p_gpu_ctx* c, const RangeTask* tasks, uint32_t K) {
+  FriParams fp;
+  FriShape s;
+  uint64_t need = 0;
+  RC(check_group(tasks, K, range_shape, range_size, same_range_shape, &fp, &s, &need));
+  bool constant_ok = true;
+  for (uint32_t k = 0; k < K && constant_ok; k++) constant_ok = range_const_ok(*tasks[k].p, s);
+  if (constant_ok) return range_prove_const(c, tasks, K, fp, s, need);
+  return range_prove_columns(c, tasks, K, fp, s, need, nullptr);
 }
 
 int with_device(z0p_gpu_ctx* c) {
@@ -2576,6 +3016,51 @@ int z0p_gpu_range_prove(z0p_gpu_ctx* c, const z0p_range_params* p, z0p_transcrip
                         uint8_t* out, size_t cap, size_t* len) {
   if (!c || !p || !ts) return Z0P_ERR_INVALID_ARGUMENT;
   return prove_group_abi(c, 1, p, &ts, &out, &cap, len, range_prove);
+}
+
+int z0p_gpu_range_prove_with_columns(z0p_gpu_ctx* c, const z0p_range_params* p,
+                                     const uint32_t* v_col, size_t v_len,
+                                     const uint32_t* const* bit_cols, const size_t* bit_lens,
+                                     size_t n_bit_cols, z0p_transcript_state* t, uint8_t* out,
+                                     size_t cap, size_t* out_len) {
+  if (!c || !p || !t || (!v_col && v_len) || (n_bit_cols && (!bit_cols || !bit_lens)))
+    return Z0P_ERR_INVALID_ARGUMENT;
+  RC(range_validate(*p));  // src/range.rs:359-366: params, then the column shapes
+  bool shape_ok = v_len == p->n_rows && n_bit_cols == p->n_bits;
+  for (size_t i = 0; shape_ok && i < n_bit_cols; i++)
+    shape_ok = bit_cols[i] && bit_lens[i] == p->n_rows;
+  if (!shape_ok) {
+    set_reason("range columns must match n_rows/n_bits");
+    return Z0P_ERR_MALFORMED_INPUT;
+  }
+  FriParams fp;
+  FriShape s;
+  RC(range_shape(*p, &fp, &s));
+  const uint64_t need = range_size(*p, s);
+  if (out_len) *out_len = need;
+  if (!out || cap < need) {
+    set_reason("output buffer too small for the proof");
+    return Z0P_ERR_BUFFER_TOO_SMALL;
+  }
+  const size_t N = p->n_rows;
+  std::vector<uint32_t> cols((n_bit_cols + 1) * N);
+  std::memcpy(cols.data(), v_col, 4 * N);
+  for (size_t i = 0; i < n_bit_cols; i++) std::memcpy(cols.data() + (i + 1) * N, bit_cols[i], 4 * N);
+  std::lock_guard<std::mutex> lk(c->mu);
+  c->work_serial++;
+  RC(with_device(c));
+  RC(ensure_slots(c, 1));
+  ProfileScope ps(c);
+  z0p_transcript_state work = *t;
+  Transcript tr(&work);
+  RangeTask task{p, &tr, out, cap, out_len};
+  c->last_sync_ns = now_ns();
+  const int rc = range_prove_columns(c, &task, 1, fp, s, need, cols.data());
+  c->last_sync_ns = 0;
+  if (rc != Z0P_OK) return rc;
+  *t = work;
+  c->proofs++;
+  return Z0P_OK;
 }
 
 int z0p_gpu_range_prove_group(z0p_gpu_ctx* c, size_t n, const z0p_range_params* params,

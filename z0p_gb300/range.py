@@ -63,6 +63,33 @@ def prove(params: Params, transcript: Transcript, ctx=None) -> bytes:
     return bytes(buf)[: n.value]
 
 
+def prove_with_columns(params: Params, v_col, bit_cols, transcript: Transcript, ctx=None) -> bytes:
+    """range::prove_with_columns (src/range.rs:353-375): the caller's value
+    column and n_bits bit columns, proved row by row on the device."""
+    import numpy as np
+
+    ctx = ctx or default_context()
+    v = np.ascontiguousarray(np.asarray(v_col, dtype=np.uint32))
+    bits = [np.ascontiguousarray(np.asarray(b, dtype=np.uint32)) for b in bit_cols]
+    ptrs = (C.POINTER(C.c_uint32) * max(1, len(bits)))(
+        *[b.ctypes.data_as(C.POINTER(C.c_uint32)) for b in bits])
+    lens = (C.c_size_t * max(1, len(bits)))(*[b.size for b in bits])
+    n = C.c_size_t()
+    rc = lib().z0p_gpu_range_prove_with_columns(ctx.handle, C.byref(params),
+                                                v.ctypes.data_as(C.POINTER(C.c_uint32)), v.size, ptrs,
+                                                lens, len(bits), C.byref(transcript.state), None, 0,
+                                                C.byref(n))
+    if rc != 100:  # Z0P_ERR_BUFFER_TOO_SMALL reports the size; anything else is the answer
+        check(rc)
+    size = n.value
+    buf = (C.c_uint8 * size)()
+    check(lib().z0p_gpu_range_prove_with_columns(ctx.handle, C.byref(params),
+                                                 v.ctypes.data_as(C.POINTER(C.c_uint32)), v.size,
+                                                 ptrs, lens, len(bits), C.byref(transcript.state),
+                                                 buf, size, C.byref(n)))
+    return bytes(buf)[: n.value]
+
+
 def prove_group(params_list, transcripts, ctx=None):
     """Proves statements of one shape in lockstep (one launch sequence and one
     set of host round trips for the group); proof i equals prove(params_list[i],
