@@ -378,10 +378,11 @@ def run_published(Z, ctx):
 def run_scale(Z, ctx, reps=5):
     """The other prove entry points at 2^20 rows, production schedule
     (for_security(100)): range::prove (16-bit, value 12,345; the batched and
-    served mixes use the same shape at smaller n), air::prove_zk with the
-    minimum hiding budget n_rand = 16 * num_queries (src/air.rs:445-458;
-    padded trace 2^21, LDE 2^25, final layer 32) and air::prove_with_trace on
-    host columns."""
+    served mixes use the same shape at smaller n) and the same columns
+    through range::prove_with_columns (row by row), table::prove_zk and
+    air::prove_zk with n_rand = 16 * num_queries (src/air.rs:445-458; padded
+    trace 2^21, LDE 2^25, final layer 32), and air::prove_with_trace on host
+    columns."""
     import numpy as np
 
     n = 1 << 20
@@ -400,8 +401,18 @@ def run_scale(Z, ctx, reps=5):
     for i in range(n):  # the Fibonacci trace, built once on the host
         ca[i], cb[i] = a, b
         a, b = b, (a + b) % P
+    rv = np.full(n, 12345, np.uint32)
+    rbits = [np.full(n, (12345 >> c) & 1, np.uint32) for c in range(16)]
+    table = [10, 20, 30, 12345]
+    table_p = Z.table.Params.new(n, 16, air_p.num_queries, 32, 12345) \
+        .with_grinding_bits(air_p.grinding_bits).with_cap_height(air_p.cap_height)
     cases = [
         ("range::prove 16-bit, 2^20 rows", n, lambda: Z.range.prove(range_p, Z.Transcript(b"bench/range"), ctx)),
+        ("range::prove_with_columns, the same columns row by row", n,
+         lambda: Z.range.prove_with_columns(range_p, rv, rbits, Z.Transcript(b"bench/range"), ctx)),
+        ("table::prove_zk, 2^20 rows, 4 entries, n_rand %d" % n_rand, n,
+         lambda: Z.table.prove_zk(table_p, table, n_rand, Z.rng.ChaCha20.new(bytes(32), bytes(12)),
+                                  Z.Transcript(b"bench/table-zk"), ctx)),
         ("air::prove_zk, 2^20 steps, n_rand %d" % n_rand, n,
          lambda: Z.air.prove_zk(zk_p, n_rand, Z.rng.ChaCha20.new(bytes(32), bytes(12)),
                                 Z.Transcript(b"bench/air-zk"), ctx)),

@@ -1753,9 +1753,9 @@ int range_prove_const(z0p_gpu_ctx* c, const RangeTask* tasks, uint32_t K, const 
 // src/range.rs:353-375 -> 425-514 on the device for any columns, for K
 // proofs of one shape in lockstep: the columns of range::prove (host_cols
 // null: value and its bits, filled on the device) or, for K = 1, the
-// caller's (n_bits + 1) x n_rows words, column-major, value column first.
+// caller's n_bits + 1 columns of n_rows words, value column first.
 int range_prove_columns(z0p_gpu_ctx* c, const RangeTask* tasks, uint32_t K, const FriParams& fp,
-                        const FriShape& s, uint64_t need, const uint32_t* host_cols) {
+                        const FriShape& s, uint64_t need, const uint32_t* const* host_cols) {
   const z0p_range_params& p0 = *tasks[0].p;
   const uint64_t N = p0.n_rows, B = p0.blowup, m = N * B, ncol = p0.n_bits + 1;
   const uint32_t logN = log2u(N), logB = log2u(B), logm = logN + logB;
@@ -1808,7 +1808,8 @@ int range_prove_columns(z0p_gpu_ctx* c, const RangeTask* tasks, uint32_t K, cons
   }
   CK(push_consts(c, K));
   if (host_cols) {
-    CK(cudaMemcpyAsync(cols, host_cols, 4 * N * ncol, cudaMemcpyHostToDevice, st));
+    for (uint64_t j = 0; j < ncol; j++)
+      CK(cudaMemcpyAsync(cols + j * N, host_cols[j], 4 * N, cudaMemcpyHostToDevice, st));
     c->h2d += 4 * N * ncol;
     *reinterpret_cast<unsigned int*>(c->hio + bad_at) = 0u;
     CK(launch::check_canonical(st, cols, N * ncol, hio_dev<unsigned int>(c, bad_at)));
@@ -3042,10 +3043,9 @@ int z0p_gpu_range_prove_with_columns(z0p_gpu_ctx* c, const z0p_range_params* p,
     set_reason("output buffer too small for the proof");
     return Z0P_ERR_BUFFER_TOO_SMALL;
   }
-  const size_t N = p->n_rows;
-  std::vector<uint32_t> cols((n_bit_cols + 1) * N);
-  std::memcpy(cols.data(), v_col, 4 * N);
-  for (size_t i = 0; i < n_bit_cols; i++) std::memcpy(cols.data() + (i + 1) * N, bit_cols[i], 4 * N);
+  std::vector<const uint32_t*> cols(n_bit_cols + 1);
+  cols[0] = v_col;
+  for (size_t i = 0; i < n_bit_cols; i++) cols[i + 1] = bit_cols[i];
   std::lock_guard<std::mutex> lk(c->mu);
   c->work_serial++;
   RC(with_device(c));
