@@ -433,6 +433,145 @@ def run_scale(Z, ctx, reps=5):
     return {"workload": "for_security(100): B16 Q40 G20 C4 F16", "rows": rows}
 
 
+def sweep_values(start, count):
+    """Elements start..start+count of the kernel-sweep stream:
+    Field::from_u64(splitmix64) with the state advanced once per element
+    (gf2.rs:425-431, babybear.rs:66-69), vectorised."""
+    import numpy as np
+
+    s = (np.uint64(SWEEP_SEED) + (np.arange(start + 1, start + count + 1, dtype=np.uint64)
+                                  * np.uint64(0x9E3779B97F4A7C15)))
+    z = (s ^ (s >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+    z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+    z = z ^ (z >> np.uint64(31))
+    return (z % np.uint64(P)).astype(np.uint32)
+
+
+SWEEP_SEED = 0x5EED000000000003
+
+
+def sweep_columns():
+    """The kernel-sweep configuration: 64 columns, log2 n uniform in {16..22}
+    (one splitmix64 draw each), grouped by n; column values follow in one
+    stream, column after column."""
+    state = SWEEP_SEED ^ 0xC0FFEE
+    logs = []
+    for _ in range(64):
+        z, state = splitmix64(state)
+        logs.append(16 + z % 7)
+    cols, at = [], 0
+    for logn in logs:
+        cols.append((logn, at))
+        at += 1 << logn
+    return cols
+
+
+def run_sweep(Z, ctx):
+    """The kernel-sweep configuration at full size: per equal-n group, the
+    coset LDE at blowup 16 (reed_solomon_extend, ntt.rs:436-439), a Merkle
+    cap over the group's row-major flat buffer (from_flat64, merkle.rs:93-110)
+    and, per column, the arity-4 fold chain (fri.rs:1273-1331) on the LDE
+    lifted to Fp4 and bit-reversed, with seeded challenges, while the degree
+    bound (n - 1) >> 2f is at least 8. Device inputs; every call is
+    synchronous, timed by the host clock after an untimed call of the same
+    size (which sizes the workspace); layouts between stages (transpose,
+    lift, bit reversal) are untimed."""
+    import ctypes as C
+
+    import numpy as np
+    import torch
+
+    from z0p_gb300._lib import check
+
+    peak, peak_kind = measured_peaks()
+    L = Z.lib()
+    groups = {}
+    for logn, at in sweep_columns():
+        groups.setdefault(logn, []).append(at)
+    B = 16
+    t_lde = t_merkle = t_fold = 0.0
+    by_lde = by_merkle = by_fold = 0
+    compressions = 0
+    rows = []
+    state = SWEEP_SEED ^ 0xF01D
+    for logn in sorted(groups):
+        n, k = 1 << logn, len(groups[logn])
+        m = n * B
+        vals = np.concatenate([sweep_values(at, n) for at in groups[logn]])
+        d_in = torch.from_numpy(vals.view(np.int32)).cuda()
+        d_lde = torch.empty(k * m, dtype=torch.int32, device="cuda")
+        torch.cuda.synchronize()
+        dt_lde = 1e9
+        for _ in range(2):  # the first call sizes the workspace for this n
+            t0 = time.perf_counter()
+            check(L.z0p_gpu_rs_extend(ctx.handle, C.c_void_p(d_in.data_ptr()), n, k, B,
+                                      C.c_void_p(d_lde.data_ptr())))
+            dt_lde = min(dt_lde, time.perf_counter() - t0)
+        flat = d_lde.view(k, m).t().contiguous()  # row-major: leaf = 16 consecutive limbs
+        torch.cuda.synchronize()
+        out = (C.c_uint8 * (32 * 16))()
+        cnt = C.c_uint64()
+        dt_merkle = 1e9
+        for _ in range(2):
+            t0 = time.perf_counter()
+            check(L.z0p_gpu_merkle_flat64_cap(ctx.handle, C.c_void_p(flat.data_ptr()), 4 * k * m, 4, out,
+                                              C.byref(cnt)))
+            dt_merkle = min(dt_merkle, time.perf_counter() - t0)
+        del flat
+        leaves = k * m // 16
+        npad = 1 << (leaves - 1).bit_length()
+        dt_fold, fold_bytes = 0.0, 0
+        logm = logn + 4
+        br = torch.arange(m, device="cuda", dtype=torch.int64)
+        rev = torch.zeros_like(br)
+        for b in range(logm):
+            rev |= ((br >> b) & 1) << (logm - 1 - b)
+        for c in range(-1, k):  # column -1: an untimed pass over column 0 sizes the workspace
+            lifted = torch.zeros(4 * m, dtype=torch.int32, device="cuda")
+            lifted[0::4] = d_lde[max(c, 0) * m:(max(c, 0) + 1) * m][rev]
+            cur, depth = lifted, 0
+            while ((n - 1) >> (2 * depth)) >= 8:
+                ch = []
+                for _ in range(12):
+                    z, state = splitmix64(state)
+                    ch.append(z % P)
+                nl = cur.numel() // 16
+                nxt = torch.empty(4 * nl, dtype=torch.int32, device="cuda")
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                check(L.z0p_gpu_fri_fold(ctx.handle, C.c_void_p(cur.data_ptr()), cur.numel() // 4, m,
+                                         depth, (C.c_uint32 * 12)(*ch), C.c_void_p(nxt.data_ptr())))
+                if c >= 0:
+                    dt_fold += time.perf_counter() - t0
+                    fold_bytes += 16 * (cur.numel() // 4) + 4 * (cur.numel() // 4) + 32 * (nl // 4)
+                    compressions += nl // 4
+                cur, depth = nxt, depth + 1
+            del lifted, cur
+        del d_lde, d_in, br, rev
+        torch.cuda.empty_cache()
+        b_lde = k * (4 * n + 4 * m)
+        b_merkle = 4 * k * m + 32 * (2 * npad - 1)
+        compressions += npad + 2 * (npad - 1)
+        t_lde += dt_lde
+        t_merkle += dt_merkle
+        t_fold += dt_fold
+        by_lde += b_lde
+        by_merkle += b_merkle
+        by_fold += fold_bytes
+        rows.append({"log2_n": logn, "columns": k, "lde_ms": round(1e3 * dt_lde, 3),
+                     "lde_gbs": round(b_lde / dt_lde / 1e9, 1), "merkle_ms": round(1e3 * dt_merkle, 3),
+                     "fold_ms": round(1e3 * dt_fold, 3), "cap": bytes(out)[:32 * cnt.value].hex()[:16]})
+
+    def stage(t, by):
+        return {"ms": round(1e3 * t, 3), "alg_bytes": by, "gbs": round(by / t / 1e9, 1),
+                "frac_hbm": round(by / t / 1e9 / peak, 4)}
+    return {"workload": "64 columns, log2 n uniform in {16..22}, blowup 16; splitmix64 values",
+            "timing": "host clock around each synchronous call (launch and sync included), after a warm call",
+            "peak_gbs": peak, "peak_source": peak_kind,
+            "lde": stage(t_lde, by_lde), "merkle": dict(stage(t_merkle, by_merkle)),
+            "fold": stage(t_fold, by_fold), "blake3_compressions": compressions, "groups": rows}
+
+
 def run_table(Z, ctx, reps=5):
     """Table membership (table::prove): the reference's `table 4-entry` row
     (docs/benchmarks.md:125; workload of benches/speed_size.rs:301-305) and a
@@ -643,7 +782,7 @@ def run_gpu(args):
         tune_info = {"source": "autotune (live)", "schedule": Z.tune.to_dict(sched), "report": report}
     if args.only:
         # One section alone (for profilers and quick checks): no headline line.
-        fn = {"published": run_published, "scale": run_scale, "fri_pcs": run_fri_pcs,
+        fn = {"published": run_published, "scale": run_scale, "sweep": run_sweep, "fri_pcs": run_fri_pcs,
               "fold_ivc": run_fold_ivc,
               "table": run_table, "batched": run_batched, "served": run_served}[args.only]
         print(json.dumps({"section": args.only, "result": fn(Z, ctx)}), flush=True)
@@ -703,7 +842,7 @@ def run_gpu(args):
         prof = ctx.profile()
         ctx.set_profiling(False)
 
-    batched = served = fri_pcs = fold_ivc = table_row = published = scale = None
+    batched = served = fri_pcs = fold_ivc = table_row = published = scale = sweep = None
     if not args.quick and ws == 1:
         batched = run_batched(Z, ctx)
         served = run_served(Z, ctx)
@@ -712,6 +851,7 @@ def run_gpu(args):
         table_row = run_table(Z, ctx)
         published = run_published(Z, ctx)
         scale = run_scale(Z, ctx)
+        sweep = run_sweep(Z, ctx)
 
     if rank != 0:
         if dist is not None:
@@ -810,6 +950,7 @@ def run_gpu(args):
         "table": table_row,
         "published_rows": published,
         "scale_rows": scale,
+        "kernel_sweep": sweep,
     }
     print(json.dumps(line), flush=True)
     if dist is not None:
@@ -828,7 +969,8 @@ def main():
     ap.add_argument("--schedule", default=None,
                     help="launch schedule file written by z0p_gb300.tune.save (default: autotune live)")
     ap.add_argument("--only", default=None,
-                    choices=["published", "scale", "fri_pcs", "fold_ivc", "table", "batched", "served"],
+                    choices=["published", "scale", "sweep", "fri_pcs", "fold_ivc", "table", "batched",
+                             "served"],
                     help="run one secondary section alone and print its JSON (no headline line)")
     args = ap.parse_args()
     if args.impl == "reference":

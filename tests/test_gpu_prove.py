@@ -155,7 +155,8 @@ def test_rs_extend_matches_oracle(z0p, oracle, gpu_ctx):
     import numpy as np
 
     rng = np.random.default_rng(7)
-    for logn, batch, blowup in [(4, 3, 16), (10, 2, 16), (13, 4, 16), (16, 2, 8), (17, 1, 4)]:
+    for logn, batch, blowup in [(4, 3, 16), (10, 2, 16), (13, 4, 16), (16, 2, 8), (17, 1, 4), (10, 2, 64),
+                                (3, 1, 128)]:
         n = 1 << logn
         vals = rng.integers(0, oracle.P, size=(batch, n), dtype=np.uint64).astype(np.uint32)
         d_in = torch.from_numpy(vals.astype(np.int64)).to(torch.int32).cuda()

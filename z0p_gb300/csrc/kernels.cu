@@ -1421,15 +1421,30 @@ __global__ void __launch_bounds__(kGrindThreads) grind_kernel(GrindArgs a) {
 
 // Coset-major [c][j][q] -> natural [c][k], k = B q + j (for callers that
 // want reed_solomon_extend's natural order, src/ntt.rs:436-439).
-__global__ void coset_to_natural_kernel(const uint32_t* __restrict__ in, uint32_t* __restrict__ out,
-                                        uint32_t logN, uint32_t logB, uint64_t total) {
-  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= total) return;
-  const uint32_t logm = logN + logB;
-  uint64_t col = i >> logm;
-  uint32_t k = (uint32_t)(i & ((1ull << logm) - 1));
-  uint32_t j = k & ((1u << logB) - 1u), q = k >> logB;
-  out[i] = in[(col << logm) + ((uint64_t)j << logN) + q];
+// Coset-major [j][q] to natural k = B q + j: per column a transpose of the
+// B x n matrix, through shared memory in tiles of up to 32 cosets x 64 rows,
+// so the loads read 256 contiguous bytes per coset and the stores write
+// 64 B contiguous words (B <= 32) or 128-byte runs.
+constexpr uint32_t kNatTileQ = 64;
+__global__ void __launch_bounds__(256) coset_to_natural_kernel(const uint32_t* __restrict__ in,
+                                                               uint32_t* __restrict__ out,
+                                                               uint32_t logN, uint32_t logB) {
+  __shared__ uint32_t tile[32][kNatTileQ + 1];
+  const uint64_t n = 1ull << logN, B = 1ull << logB, m = n << logB;
+  const uint64_t q0 = (uint64_t)blockIdx.x * kNatTileQ, j0 = (uint64_t)blockIdx.y * 32;
+  const uint32_t tj = (uint32_t)(B - j0 < 32 ? B - j0 : 32);
+  const uint32_t tq = (uint32_t)(n - q0 < kNatTileQ ? n - q0 : kNatTileQ);
+  in += (uint64_t)blockIdx.z * m;
+  out += (uint64_t)blockIdx.z * m;
+  for (uint32_t i = threadIdx.x; i < tj * kNatTileQ; i += blockDim.x) {
+    const uint32_t jj = i / kNatTileQ, qq = i % kNatTileQ;
+    if (qq < tq) tile[jj][qq] = in[((j0 + jj) << logN) + q0 + qq];
+  }
+  __syncthreads();
+  for (uint32_t i = threadIdx.x; i < tj * kNatTileQ; i += blockDim.x) {
+    const uint32_t qq = i / tj, jj = i % tj;
+    if (qq < tq) out[((q0 + qq) << logB) + j0 + jj] = tile[jj][qq];
+  }
 }
 
 // ------------------------------------------------------- hash ceiling ----
@@ -2049,10 +2064,14 @@ cudaError_t openings(cudaStream_t st, const OpenArgs& a, uint32_t nproofs) {
 
 cudaError_t coset_to_natural(cudaStream_t st, const uint32_t* in, uint32_t* out, uint32_t logN,
                              uint32_t logB, uint64_t batch) {
-  uint64_t total = batch << (logN + logB);
+  if (batch == 0) return cudaSuccess;
+  if (batch > 65535 || (logB > 5 && (1ull << (logB - 5)) > 65535)) return cudaErrorInvalidValue;
+  const uint64_t qt = ((1ull << logN) + kNatTileQ - 1) / kNatTileQ;
+  const uint32_t jt = logB > 5 ? 1u << (logB - 5) : 1u;
+  if (qt > 0x7fffffffull) return cudaErrorInvalidValue;
   Stage stg("coset_to_natural", st);
   stg.launched();
-  coset_to_natural_kernel<<<grid_for(total), kThreads, 0, st>>>(in, out, logN, logB, total);
+  coset_to_natural_kernel<<<dim3((unsigned)qt, jt, (unsigned)batch), 256, 0, st>>>(in, out, logN, logB);
   return cudaGetLastError();
 }
 
