@@ -224,3 +224,10 @@ def test_schedule_get_set_validation(z0p):
     with pytest.raises(z0p.Z0pError):
         t.get(64)
     t.set(t.from_dict(before), dev)
+
+
+def test_shipped_schedule_is_valid(z0p):
+    s = z0p.tune.shipped("gb300")
+    z0p.tune.set(s, 6)  # validates every field
+    assert z0p.tune.to_dict(z0p.tune.get(6)) == z0p.tune.to_dict(s)
+    z0p.tune.set(z0p.tune.default(), 6)

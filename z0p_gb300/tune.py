@@ -55,6 +55,14 @@ def load(path: str) -> Schedule:
         return from_dict(json.load(f))
 
 
+def shipped(name: str = "gb300") -> Schedule:
+    """A schedule the autotuner wrote on that hardware, shipped with the
+    package (schedules/<name>.json)."""
+    import os
+
+    return load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "schedules", name + ".json"))
+
+
 def autotune(ctx, max_log_n: int = 22):
     """Times every field's candidates on ctx's device, installs the winners
     (a candidate must beat the default by 3%) and returns (schedule, report)
