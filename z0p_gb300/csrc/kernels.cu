@@ -1936,13 +1936,22 @@ cudaError_t grind(cudaStream_t st, uint32_t slot, uint32_t head_len, uint32_t bi
   a.state = state;
   a.out = out;
   a.max_chunks = (max_nonces + kGrindChunk - 1) / kGrindChunk;
-  static int max_ctas = 0, sms = 0;
-  if (!max_ctas) {
-    int dev = 0, per = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, grind_kernel, kGrindThreads, 0);
-    max_ctas = sms * (per > 0 ? per : 1);
+  // Per device: SM count and the grind kernel's resident CTAs.
+  static std::mutex mu;
+  static int cached_sms[kMaxDevices] = {}, cached_max[kMaxDevices] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) dev = 0;
+  int sms, max_ctas;
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    if (!cached_max[dev]) {
+      int per = 0;
+      cudaDeviceGetAttribute(&cached_sms[dev], cudaDevAttrMultiProcessorCount, dev);
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, grind_kernel, kGrindThreads, 0);
+      cached_max[dev] = cached_sms[dev] * (per > 0 ? per : 1);
+    }
+    sms = cached_sms[dev];
+    max_ctas = cached_max[dev];
   }
   // The search expects 2^bits nonces. A thread stops at its next nonce once
   // that passes the best hit, so at most one nonce per thread is hashed past
