@@ -1432,7 +1432,7 @@ __global__ void __launch_bounds__(256) coset_to_natural_kernel(const uint32_t* _
   __shared__ uint32_t tile[32][kNatTileQ + 1];
   const uint64_t n = 1ull << logN, B = 1ull << logB, m = n << logB;
   const uint64_t q0 = (uint64_t)blockIdx.x * kNatTileQ, j0 = (uint64_t)blockIdx.y * 32;
-  const uint32_t tj = (uint32_t)(B - j0 < 32 ? B - j0 : 32);
+  const uint32_t ltj = logB < 5 ? logB : 5, tj = 1u << ltj;  // B - j0 >= 32 whenever B > 32
   const uint32_t tq = (uint32_t)(n - q0 < kNatTileQ ? n - q0 : kNatTileQ);
   in += (uint64_t)blockIdx.z * m;
   out += (uint64_t)blockIdx.z * m;
@@ -1442,7 +1442,7 @@ __global__ void __launch_bounds__(256) coset_to_natural_kernel(const uint32_t* _
   }
   __syncthreads();
   for (uint32_t i = threadIdx.x; i < tj * kNatTileQ; i += blockDim.x) {
-    const uint32_t qq = i / tj, jj = i % tj;
+    const uint32_t qq = i >> ltj, jj = i & (tj - 1u);
     if (qq < tq) out[((q0 + qq) << logB) + j0 + jj] = tile[jj][qq];
   }
 }
