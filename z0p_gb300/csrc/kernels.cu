@@ -186,9 +186,15 @@ __device__ __forceinline__ void smem_dif_t(uint32_t* s, const uint2* tw, uint32_
 // for i < 2^(L-1) (w^-1 for the inverse transform), entry i at tpos(i).
 template <int L>
 __device__ __forceinline__ void stage_twiddles(uint2* tw, const NttArgs& a) {
-  if constexpr (L > 0)
-    for (uint32_t i = threadIdx.x; i < (1u << (L - 1)); i += blockDim.x)
-      tw[tpos(i)] = shoup_pair(from_mont(root_pow(a.tb, tw_exp(i, kRootBits - L, a.inverse))));
+  if constexpr (L > 0) {
+    if (a.tb.stw) {
+      const uint2* src = a.tb.stw + (a.inverse ? kStwInverse : 0u) + ((1u << (L - 1)) - 1u);
+      for (uint32_t i = threadIdx.x; i < (1u << (L - 1)); i += blockDim.x) tw[tpos(i)] = __ldg(src + i);
+    } else {
+      for (uint32_t i = threadIdx.x; i < (1u << (L - 1)); i += blockDim.x)
+        tw[tpos(i)] = shoup_pair(from_mont(root_pow(a.tb, tw_exp(i, kRootBits - L, a.inverse))));
+    }
+  }
 }
 
 // Word offset of the stage-twiddle table after `words` of shared memory

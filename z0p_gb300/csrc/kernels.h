@@ -13,7 +13,13 @@ struct Tables {
   const uint32_t* w_hi;  // omega_{2^27}^(i * 2^14), i < 2^13
   const uint32_t* g_lo;  // 31^i,                    i < 2^12
   const uint32_t* g_hi;  // 31^(i * 2^12),           i < 2^15
+  // NTT stage twiddles (w, floor(w 2^32 / p)), w = omega_{2^L}^(+-i)
+  // canonical, i < 2^(L-1), for L = 1..13: the forward table at
+  // stw + 2^(L-1) - 1, the inverse one kStwInverse entries further. Null:
+  // the transforms compute them.
+  const uint2* stw = nullptr;
 };
+constexpr uint32_t kStwInverse = 1u << 13;
 
 // Batched NTT of length 2^logn. Transform b reads in + (b / in_div) * n,
 // multiplies input i by omega_{2^27}^((j*i) << twist_shift) with

@@ -347,6 +347,21 @@ int build_tables(z0p_gpu_ctx* c) {
   step = fpow(GENERATOR, lo_g);
   x = 1;
   for (int i = 0; i < hi_g; i++) { g_hi[i] = to_mont(x); x = fmul(x, step); }
+  // NTT stage twiddles with their Shoup quotients (kernels.h, Tables::stw).
+  const size_t stw_at = t.size();  // in words; t.size() is even
+  t.resize(stw_at + 4 * (size_t)kStwInverse, 0u);
+  for (uint32_t inv = 0; inv < 2; inv++)
+    for (uint32_t L = 1; L <= 13; L++) {
+      const uint32_t root = two_adic_generator(L);
+      uint32_t w = 1;
+      const uint32_t step = inv ? finv(root) : root;
+      uint32_t* dst = t.data() + stw_at + 2 * ((size_t)inv * kStwInverse + (1u << (L - 1)) - 1);
+      for (uint32_t i = 0; i < (1u << (L - 1)); i++) {
+        dst[2 * i] = w;
+        dst[2 * i + 1] = (uint32_t)(((uint64_t)w << 32) / P);
+        w = fmul(w, step);
+      }
+    }
   RC(ensure(c, c->tables, t.size() * 4));
   CK(cudaMemcpyAsync(c->tables.p, t.data(), t.size() * 4, cudaMemcpyHostToDevice, c->stream));
   CK(cudaStreamSynchronize(c->stream));
@@ -355,6 +370,7 @@ int build_tables(z0p_gpu_ctx* c) {
   c->tb.w_hi = d + lo_w;
   c->tb.g_lo = d + lo_w + hi_w;
   c->tb.g_hi = d + lo_w + hi_w + lo_g;
+  c->tb.stw = reinterpret_cast<const uint2*>(d + stw_at);
   return Z0P_OK;
 }
 
