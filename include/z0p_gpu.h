@@ -469,6 +469,9 @@ int z0p_gpu_fri_fold(z0p_gpu_ctx *ctx, const uint32_t *d_in, uint64_t n, uint64_
  *    log2 of the first pass's transform length, within
  *    [max(7, l - 13), min(13, l - 6)]; 0 = the balanced split ceil(l / 2).
  *    Other entries must be 0.
+ *  - ntt_radix32[l]: nonzero for the same transforms: the passes work in
+ *    register groups of 32 elements (256 threads a CTA) instead of 16 (512
+ *    threads); 0 or 1, and 0 outside 13 <= l <= 26.
  *  - merkle_top_log: a Merkle tree's levels are one launch each while they
  *    hold more than 2^merkle_top_log nodes; one top kernel hashes the rest
  *    (10..18).
@@ -476,6 +479,7 @@ int z0p_gpu_fri_fold(z0p_gpu_ctx *ctx, const uint32_t *d_in, uint64_t n, uint64_
  *    the occupancy limit). */
 typedef struct {
     uint8_t ntt_log_n1[32];
+    uint8_t ntt_radix32[32];
     uint32_t merkle_top_log;
     uint32_t grind_ctas_per_sm;
 } z0p_schedule;

@@ -36,7 +36,7 @@ class AirParams(C.Structure):
 
 
 class Schedule(C.Structure):
-    _fields_ = [("ntt_log_n1", C.c_uint8 * 32), ("merkle_top_log", C.c_uint32),
+    _fields_ = [("ntt_log_n1", C.c_uint8 * 32), ("ntt_radix32", C.c_uint8 * 32), ("merkle_top_log", C.c_uint32),
                 ("grind_ctas_per_sm", C.c_uint32)]
 
 

@@ -164,22 +164,23 @@ __device__ __forceinline__ void dif_group_t(uint32_t* col, const uint2* tw, uint
   for (int t = 0; t < (1 << K); t++) base[(t << S_LO) + ((t << S_LO) >> 5)] = x[t];
 }
 
-template <int L, int S_HI>
+template <int L, int S_HI, int KM = 4>
 __device__ __forceinline__ void dif_passes_t(uint32_t* s, const uint2* tw, uint32_t ncols,
                                              uint32_t cstride) {
-  constexpr int K = S_HI + 1 < 4 ? S_HI + 1 : 4;
+  constexpr int K = S_HI + 1 < KM ? S_HI + 1 : KM;
   constexpr uint32_t groups = 1u << (L - K);
   const uint32_t total = groups * ncols;
   for (uint32_t idx = threadIdx.x; idx < total; idx += blockDim.x)
     dif_group_t<L, S_HI, K>(s + (idx >> (L - K)) * cstride, tw, idx & (groups - 1u));
   __syncthreads();
-  if constexpr (S_HI - K >= 0) dif_passes_t<L, S_HI - K>(s, tw, ncols, cstride);
+  if constexpr (S_HI - K >= 0) dif_passes_t<L, S_HI - K, KM>(s, tw, ncols, cstride);
 }
 
-template <int L>
+// KM: register group of 2^KM elements per thread and pass (16 or 32).
+template <int L, int KM = 4>
 __device__ __forceinline__ void smem_dif_t(uint32_t* s, const uint2* tw, uint32_t ncols,
                                            uint32_t cstride) {
-  if constexpr (L > 0) dif_passes_t<L, L - 1>(s, tw, ncols, cstride);
+  if constexpr (L > 0) dif_passes_t<L, L - 1, KM>(s, tw, ncols, cstride);
 }
 
 // Stage twiddles of a 2^L-point transform: (w^i, Shoup quotient), canonical,
@@ -257,7 +258,7 @@ __host__ __device__ constexpr uint32_t col_stride(uint32_t L, uint32_t C) {
 // factor folded into the four-step twiddle on the way out; each thread then
 // writes C consecutive words of row k1 of yt (32 bytes for C = 8), with the
 // twiddles w_k1(i2) a geometric chain in i2.
-template <int L1, int LOGC>
+template <int L1, int LOGC, int KM>
 __global__ void __launch_bounds__(512) ntt_pass1_kernel(const uint32_t* __restrict__ in,
                                                         uint32_t* __restrict__ yt, NttArgs a) {
   constexpr uint32_t C = 1u << LOGC;
@@ -285,7 +286,7 @@ __global__ void __launch_bounds__(512) ntt_pass1_kernel(const uint32_t* __restri
     s[c * cstride + spos(i1)] = v;
   }
   __syncthreads();
-  smem_dif_t<L1>(s, tw, C, cstride);
+  smem_dif_t<L1, KM>(s, tw, C, cstride);
   uint32_t* dst = yt + (size_t)b * n;
   const uint32_t shift = kRootBits - a.logn;
   for (uint32_t k1 = threadIdx.x; k1 < n1; k1 += blockDim.x) {
@@ -310,7 +311,7 @@ __global__ void __launch_bounds__(512) ntt_pass1_kernel(const uint32_t* __restri
 // Four-step pass 2: for R rows k1 of yt, n2-point transforms over i2 (n2 =
 // 2^L2); output k = k1 + n1 k2 (natural order). Each thread writes R
 // consecutive words of out, optionally scaled by 31^k / n (a chain in k).
-template <int L2, int LOGR>
+template <int L2, int LOGR, int KM>
 __global__ void __launch_bounds__(512) ntt_pass2_kernel(const uint32_t* __restrict__ yt,
                                                         uint32_t* __restrict__ out, NttArgs a) {
   constexpr uint32_t R = 1u << LOGR;
@@ -335,7 +336,7 @@ __global__ void __launch_bounds__(512) ntt_pass2_kernel(const uint32_t* __restri
     dstrow[3] = v.w;
   }
   __syncthreads();
-  smem_dif_t<L2>(s, tw, R, rstride);
+  smem_dif_t<L2, KM>(s, tw, R, rstride);
   uint32_t* dst = out + (size_t)b * n;
   for (uint32_t k2 = threadIdx.x; k2 < n2; k2 += blockDim.x) {
     const uint32_t p = spos(brev_bits(k2, L2));
@@ -1629,7 +1630,7 @@ uint32_t subtree_levels(uint32_t nt, uint32_t top) {
 // need is fixed by L, so the attribute is set once per kernel, not per launch).
 bool smem_raised(int pass, uint32_t L, size_t smem) {
   static std::mutex mu;
-  static size_t done[3][32] = {};
+  static size_t done[6][32] = {};
   std::lock_guard<std::mutex> lk(mu);
   if (done[pass][L] >= smem) return true;
   done[pass][L] = smem;
@@ -1665,9 +1666,10 @@ uint32_t ntt_default_split(uint32_t logn) { return (logn + 1) / 2; }
 
 bool schedule_valid(const Schedule& s) {
   for (uint32_t l = 0; l < 32; l++) {
-    if (!s.ntt_log_n1[l]) continue;
     uint32_t lo, hi;
     ntt_split_range(l, &lo, &hi);
+    if (s.ntt_radix32[l] > 1 || (s.ntt_radix32[l] && lo > hi)) return false;
+    if (!s.ntt_log_n1[l]) continue;
     if (s.ntt_log_n1[l] < lo || s.ntt_log_n1[l] > hi) return false;
   }
   return s.merkle_top_log >= 10 && s.merkle_top_log <= 18 && s.grind_ctas_per_sm >= 1 &&
@@ -1735,33 +1737,43 @@ cudaError_t ntt(cudaStream_t st, const Tables& tb, const NttPlan& plan, const ui
       ((size_t)tw_offset(col_stride(logn1, 1u << logc) << logc) + 2 * tw_entries(logn1) + n1) * 4;
   size_t smem2 = ((size_t)tw_offset(col_stride(logn2, 1u << logr) << logr) + 2 * tw_entries(logn2)) * 4;
   dim3 g1(n2 >> logc, plan.batch), g2(n1 >> logr, plan.batch);
+  // Register groups of 32 (two shared-memory passes for a 2^10 half) run
+  // 256 threads a CTA; groups of 16 run 512.
+  const bool r32 = plan.logn < 32 && sched.ntt_radix32[plan.logn];
+  const int threads = r32 ? 256 : 512, slot = r32 ? 3 : 0;
   Stage stg(plan.inverse ? "intt" : "ntt", st);
   stg.launched(2);
   switch (logn1) {
-#define Z0P_P1(Lv, LC)                                                                          \
-  case Lv:                                                                                      \
-    if (!smem_raised(1, Lv, smem1))                                                             \
-      cudaFuncSetAttribute(ntt_pass1_kernel<Lv, LC>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
-                           (int)smem1);                                                         \
-    ntt_pass1_kernel<Lv, LC><<<g1, 512, smem1, st>>>(in, scratch, a);                           \
+#define Z0P_P1K(Lv, LC, KM)                                                                      \
+    if (!smem_raised(1 + slot, Lv, smem1))                                                       \
+      cudaFuncSetAttribute(ntt_pass1_kernel<Lv, LC, KM>,                                         \
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1);             \
+    ntt_pass1_kernel<Lv, LC, KM><<<g1, threads, smem1, st>>>(in, scratch, a);
+#define Z0P_P1(Lv, LC)                                                                           \
+  case Lv:                                                                                       \
+    if (r32) { Z0P_P1K(Lv, LC, 5) } else { Z0P_P1K(Lv, LC, 4) }                                  \
     break;
     Z0P_P1(7, 3) Z0P_P1(8, 3) Z0P_P1(9, 3) Z0P_P1(10, 3) Z0P_P1(11, 3) Z0P_P1(12, 3) Z0P_P1(13, 2)
 #undef Z0P_P1
+#undef Z0P_P1K
     default: return cudaErrorInvalidValue;
   }
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   switch (logn2) {
-#define Z0P_P2(Lv, LR)                                                                          \
-  case Lv:                                                                                      \
-    if (!smem_raised(2, Lv, smem2))                                                             \
-      cudaFuncSetAttribute(ntt_pass2_kernel<Lv, LR>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
-                           (int)smem2);                                                         \
-    ntt_pass2_kernel<Lv, LR><<<g2, 512, smem2, st>>>(scratch, out, a);                          \
+#define Z0P_P2K(Lv, LR, KM)                                                                      \
+    if (!smem_raised(2 + slot, Lv, smem2))                                                       \
+      cudaFuncSetAttribute(ntt_pass2_kernel<Lv, LR, KM>,                                         \
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2);             \
+    ntt_pass2_kernel<Lv, LR, KM><<<g2, threads, smem2, st>>>(scratch, out, a);
+#define Z0P_P2(Lv, LR)                                                                           \
+  case Lv:                                                                                       \
+    if (r32) { Z0P_P2K(Lv, LR, 5) } else { Z0P_P2K(Lv, LR, 4) }                                  \
     break;
     Z0P_P2(6, 3) Z0P_P2(7, 3) Z0P_P2(8, 3) Z0P_P2(9, 3) Z0P_P2(10, 3) Z0P_P2(11, 3) Z0P_P2(12, 3)
     Z0P_P2(13, 2)
 #undef Z0P_P2
+#undef Z0P_P2K
     default: return cudaErrorInvalidValue;
   }
   (void)n;

@@ -214,6 +214,9 @@ struct Schedule {
   // Four-step NTT of length 2^logn (13 <= logn <= 26): log2 of the pass-1
   // transform length; 0 = the balanced default ceil(logn / 2).
   uint8_t ntt_log_n1[32] = {};
+  // Nonzero: the passes of a 2^logn transform work in register groups of 32
+  // elements (256 threads a CTA) instead of 16 (512 threads).
+  uint8_t ntt_radix32[32] = {};
   // A Merkle tree's levels go one launch each while they have more than
   // 2^merkle_top_log nodes; the rest go to one top kernel (10..18).
   uint32_t merkle_top_log = 16;

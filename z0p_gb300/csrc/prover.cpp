@@ -3212,6 +3212,7 @@ int z0p_gpu_blake3_ceiling(z0p_gpu_ctx* c, double* gcompress_per_s) {
 static launch::Schedule from_abi(const z0p_schedule& s) {
   launch::Schedule o;
   std::memcpy(o.ntt_log_n1, s.ntt_log_n1, sizeof o.ntt_log_n1);
+  std::memcpy(o.ntt_radix32, s.ntt_radix32, sizeof o.ntt_radix32);
   o.merkle_top_log = s.merkle_top_log;
   o.grind_ctas_per_sm = s.grind_ctas_per_sm;
   return o;
@@ -3220,6 +3221,7 @@ static launch::Schedule from_abi(const z0p_schedule& s) {
 static z0p_schedule to_abi(const launch::Schedule& s) {
   z0p_schedule o;
   std::memcpy(o.ntt_log_n1, s.ntt_log_n1, sizeof o.ntt_log_n1);
+  std::memcpy(o.ntt_radix32, s.ntt_radix32, sizeof o.ntt_radix32);
   o.merkle_top_log = s.merkle_top_log;
   o.grind_ctas_per_sm = s.grind_ctas_per_sm;
   return o;
@@ -3274,7 +3276,8 @@ static int autotune_locked(z0p_gpu_ctx* c, uint32_t max_log_n, launch::Schedule*
   *best = base;
   auto use = [&](const launch::Schedule& s) { launch::set_schedule(c->device, s); };
 
-  // Four-step NTT splits, one LDE of 16 cosets of 2^l per run.
+  // Four-step NTT splits and register-group radix, one LDE of 16 cosets of
+  // 2^l per run.
   const uint32_t top_l = max_log_n < 22 ? max_log_n : 22;
   if (top_l >= 13) {
     const size_t n_max = 1ull << top_l;
@@ -3298,24 +3301,29 @@ static int autotune_locked(z0p_gpu_ctx* c, uint32_t max_log_n, launch::Schedule*
     launch::ntt_split_range(l, &lo, &hi);
     const uint32_t def = launch::ntt_default_split(l);
     float t_def = 0.f, t_best = 0.f;
-    uint32_t pick = 0;
-    for (uint32_t s1 = (def > lo + 2 ? def - 2 : lo); s1 <= hi && s1 <= def + 2; s1++) {
-      launch::Schedule s = base;
-      s.ntt_log_n1[l] = (uint8_t)s1;
-      use(s);
-      float t = 0.f;
-      CK(time_best(c, e0, e1, 3, run, &t));
-      if (s1 == def) t_def = t;
-      if (pick == 0 || t < t_best) {
-        t_best = t;
-        pick = s1;
+    uint32_t pick = 0, pick_r32 = 0;
+    for (uint32_t s1 = (def > lo + 2 ? def - 2 : lo); s1 <= hi && s1 <= def + 2; s1++)
+      for (uint32_t r32 = 0; r32 < 2; r32++) {
+        launch::Schedule s = base;
+        s.ntt_log_n1[l] = (uint8_t)s1;
+        s.ntt_radix32[l] = (uint8_t)r32;
+        use(s);
+        float t = 0.f;
+        CK(time_best(c, e0, e1, 3, run, &t));
+        if (s1 == def && !r32) t_def = t;
+        if (pick == 0 || t < t_best) {
+          t_best = t;
+          pick = s1;
+          pick_r32 = r32;
+        }
       }
-    }
-    if (pick != def && t_best > kKeep * t_def) {
+    if ((pick != def || pick_r32) && t_best > kKeep * t_def) {
       pick = def;
+      pick_r32 = 0;
       t_best = t_def;
     }
     best->ntt_log_n1[l] = pick == def ? 0 : (uint8_t)pick;
+    best->ntt_radix32[l] = (uint8_t)pick_r32;
     if (rep) {
       rep->ntt_default_us[l] = 1e3f * t_def;
       rep->ntt_best_us[l] = 1e3f * t_best;

@@ -1,8 +1,8 @@
 """Launch schedules and their autotuner (no counterpart in the reference).
 
-A schedule picks, per device, the four-step NTT split for each transform
-size, the Merkle level where one top kernel takes over, and the
-proof-of-work grid. Every schedule gives byte-identical proofs.
+A schedule picks, per device, the four-step NTT split and register-group
+radix (16 or 32) for each transform size, the Merkle level where one top
+kernel takes over, and the proof-of-work grid. Every schedule gives byte-identical proofs.
 
     sched, report = tune.autotune(ctx)        # measure and install
     tune.save("gb300.schedule.json", sched)   # later: tune.set(tune.load(...))
@@ -33,6 +33,7 @@ def set(schedule: Schedule, device: int = 0) -> None:  # noqa: A001 - module-lev
 
 def to_dict(s: Schedule) -> dict:
     return {"ntt_log_n1": {str(l): int(s.ntt_log_n1[l]) for l in range(32) if s.ntt_log_n1[l]},
+            "ntt_radix32": sorted(l for l in range(32) if s.ntt_radix32[l]),
             "merkle_top_log": int(s.merkle_top_log), "grind_ctas_per_sm": int(s.grind_ctas_per_sm)}
 
 
@@ -40,6 +41,8 @@ def from_dict(d: dict) -> Schedule:
     s = default()
     for l, v in d.get("ntt_log_n1", {}).items():
         s.ntt_log_n1[int(l)] = int(v)
+    for l in d.get("ntt_radix32", []):
+        s.ntt_radix32[int(l)] = 1
     s.merkle_top_log = int(d.get("merkle_top_log", s.merkle_top_log))
     s.grind_ctas_per_sm = int(d.get("grind_ctas_per_sm", s.grind_ctas_per_sm))
     return s
