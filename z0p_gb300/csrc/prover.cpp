@@ -1155,10 +1155,10 @@ bool const_fri_ok(const FriShape& s, bool zero, uint64_t rows, uint64_t blowup) 
   return rows >= 4 && s.len.back() >= blowup && blowup <= 512;
 }
 
-int const_fri(z0p_gpu_ctx* c, const FriShape& s, const FriParams& fp, uint64_t poly_len,
-              uint64_t degree_bound, Transcript* const* ts, uint32_t K, ConstFri* fr) {
+// The seeds of every FRI tree of K proofs (their K_j known); `all`
+// receives the trees to build.
+void prepare_const_fri(const FriShape& s, uint32_t K, ConstFri* fr, std::vector<ConstTree*>* all) {
   const size_t nl = s.len.size();
-  std::vector<ConstTree*> all;
   for (uint32_t k = 0; k < K; k++) {
     ConstFri& f = fr[k];
     const uint32_t logB = f.logB;
@@ -1181,10 +1181,22 @@ int const_fri(z0p_gpu_ctx* c, const FriShape& s, const FriParams& fp, uint64_t p
         const uint64_t leaf = (uint64_t)g << t.logS;  // any leaf of the group
         for (int q = 0; q < 4; q++) std::memcpy(&t.seeds[16 * g + 4 * q], f.val(logL, 4 * leaf + q), 16);
       }
-      all.push_back(&t);
+      all->push_back(&t);
     }
   }
-  RC(build_const_trees(c, all, "cap"));
+}
+
+// With `built`, the trees are already there (a zero composition's trees
+// depend on the shape alone and go with the trace tree's launch).
+int const_fri(z0p_gpu_ctx* c, const FriShape& s, const FriParams& fp, uint64_t poly_len,
+              uint64_t degree_bound, Transcript* const* ts, uint32_t K, ConstFri* fr,
+              bool built = false) {
+  const size_t nl = s.len.size();
+  if (!built) {
+    std::vector<ConstTree*> all;
+    prepare_const_fri(s, K, fr, &all);
+    RC(build_const_trees(c, all, "cap"));
+  }
   uint8_t dims[24];  // src/fri.rs:1450-1456
   for (int i = 0; i < 8; i++) {
     dims[i] = (uint8_t)(s.m >> (8 * i));
@@ -1282,10 +1294,10 @@ void write_const_fri(Writer& w, const FriShape& s, const ConstFri& f, uint64_t p
 // equal leaves each; returns the trees (digest chains) and their caps.
 int const_trace_trees(z0p_gpu_ctx* c, const std::vector<std::vector<uint32_t>>& rows,
                       uint32_t logm, uint32_t tdrop, std::vector<ConstTree>* trees,
-                      std::vector<std::vector<uint8_t>>* caps) {
+                      std::vector<std::vector<uint8_t>>* caps,
+                      std::vector<ConstTree*> all = {}) {  // `all`: more trees for the same launch
   const size_t K = rows.size();
   trees->assign(K, ConstTree{});
-  std::vector<ConstTree*> all;
   for (size_t k = 0; k < K; k++) {
     ConstTree& t = (*trees)[k];
     t.G = 1;
@@ -1328,18 +1340,20 @@ int table_prove_const(z0p_gpu_ctx* c, const z0p_table_params& p, const uint32_t*
     for (size_t i = 0; i < tlen; i++) p32(56 + 4 * i, table[i]);
     transcript_absorb(t, "table/params", pb.data(), pb.size());
   }
+  uint32_t prod = 1;
+  for (size_t i = 0; i < tlen; i++) prod = fmul(prod, fsub(p.value, table[i]));
+  ConstFri fr;
+  fr.logB = logB;
+  std::vector<ConstTree*> early;  // a member's FRI trees: all-zero layers
+  if (!prod) prepare_const_fri(s, 1, &fr, &early);
   std::vector<ConstTree> ttrees;
   std::vector<std::vector<uint8_t>> tcap;
-  RC(const_trace_trees(c, {{p.value}}, logm, tdrop, &ttrees, &tcap));  // from_flat(.., 4) leaves
+  RC(const_trace_trees(c, {{p.value}}, logm, tdrop, &ttrees, &tcap, early));  // from_flat(.., 4) leaves
   transcript_absorb(t, "table/column", tcap[0].data(), tcap[0].size());
   uint32_t am[4], ab[4];
   challenge_ext(t, "table/alpha", am);
   challenge_ext(t, "table/alpha", ab);
-  uint32_t prod = 1;
-  for (size_t i = 0; i < tlen; i++) prod = fmul(prod, fsub(p.value, table[i]));
   std::vector<uint32_t> kc;
-  ConstFri fr;
-  fr.logB = logB;
   if (prod) {
     kc.assign(4 * B, 0u);
     const uint32_t wB = two_adic_generator(logB);
@@ -1353,7 +1367,7 @@ int table_prove_const(z0p_gpu_ctx* c, const z0p_table_params& p, const uint32_t*
   }
   const uint64_t bound = membership_bound(tlen, N, 0);
   Transcript* ts[1] = {&t};
-  RC(const_fri(c, s, fp, m, bound, ts, 1, &fr));
+  RC(const_fri(c, s, fp, m, bound, ts, 1, &fr, !prod));
   Writer w(out, need);  // table::Proof::to_bytes (src/table.rs:244-262)
   w.byte(6);
   w.u32((uint32_t)(tcap[0].size() / 32));
@@ -1709,13 +1723,22 @@ int range_prove_const(z0p_gpu_ctx* c, const RangeTask* tasks, uint32_t K, const 
     p64(32, p.final_size); p32(40, p.grinding_bits); p64(44, p.cap_height); p32(52, p.value);
     transcript_absorb(*tasks[k].ts, "range/params", pb, 56);
   }
+  // In-range values only: every FRI layer is zero, and its trees go with
+  // the trace trees' launch.
+  std::vector<ConstFri> fr(K);
+  bool all_zero = true;
+  for (uint32_t k = 0; k < K; k++) {
+    fr[k].logB = logB;
+    all_zero &= tasks[k].p->value < (1u << p0.n_bits);
+  }
+  std::vector<ConstTree*> early;
+  if (all_zero) prepare_const_fri(s, K, fr.data(), &early);
   std::vector<ConstTree> ttrees;
   std::vector<std::vector<uint8_t>> tcap;
-  RC(const_trace_trees(c, rows, logm, tdrop, &ttrees, &tcap));
+  RC(const_trace_trees(c, rows, logm, tdrop, &ttrees, &tcap, early));
   // Composition (src/range.rs:678-774) on coset j: (value - rec) zinv_j alpha_d.
   const uint32_t gN = fpow(GENERATOR, N), wB = two_adic_generator(logB);
   std::vector<std::vector<uint32_t>> kc(K);
-  std::vector<ConstFri> fr(K);
   std::vector<Transcript*> ts(K);
   for (uint32_t k = 0; k < K; k++) {
     ts[k] = tasks[k].ts;
@@ -1727,7 +1750,6 @@ int range_prove_const(z0p_gpu_ctx* c, const RangeTask* tasks, uint32_t K, const 
       if (i == 0) std::memcpy(alpha_d, a, 16);
     }
     const uint32_t value = tasks[k].p->value, rec = value & ((1u << p0.n_bits) - 1u);
-    fr[k].logB = logB;
     if (value != rec) {
       kc[k].assign(4 * B, 0u);
       uint32_t xn = gN;  // x^N on coset j: 31^N omega_B^j
@@ -1739,7 +1761,7 @@ int range_prove_const(z0p_gpu_ctx* c, const RangeTask* tasks, uint32_t K, const 
       fr[k].kc = kc[k].data();
     }
   }
-  RC(const_fri(c, s, fp, m, N - 1, ts.data(), K, fr.data()));
+  RC(const_fri(c, s, fp, m, N - 1, ts.data(), K, fr.data(), all_zero));
   std::vector<uint8_t> pbuf;
   for (uint32_t k = 0; k < K; k++) {
     const z0p_range_params& p = *tasks[k].p;
