@@ -772,11 +772,17 @@ __device__ __forceinline__ void quad_points(const Tables& tb, uint32_t k0, uint3
 // (A(omega_N x) - B(x)) (x - w_last)/Z(x) is the constant -coeff, so
 // alpha_0 times it is the per-proof constant kc. All arithmetic is exact, so
 // the values equal the reference's term by term.
+// With a.counter (small trees), thread u makes leaf P = u, so a CTA's leaves
+// are consecutive and it hashes their subtree (cta_subtree); otherwise
+// consecutive threads read consecutive LDE rows and leaf P is bit-reversed.
+template <bool kFused>
 __global__ void __launch_bounds__(kThreads) air_compose_leaves_kernel(AirComposeArgs a, Tables tb) {
+  // >= 2 * 9 * (kFuseMaxLeaves / 256) roots when fused
+  __shared__ uint32_t buf[kFused ? 2 * kThreads * kTopStride : 1];
+  if (!kFused) a.counter = nullptr;
   const uint32_t logm = a.logN + a.logB;
   const uint32_t quarter = 1u << (logm - 2);
-  uint32_t u = blockIdx.x * blockDim.x + threadIdx.x;
-  if (u >= quarter) return;
+  const uint32_t u = blockIdx.x * blockDim.x + threadIdx.x;
   {
     const uint32_t pk = blockIdx.y;  // proof of the group
     a.lde_a += (size_t)pk << logm;
@@ -785,16 +791,26 @@ __global__ void __launch_bounds__(kThreads) air_compose_leaves_kernel(AirCompose
     a.layer0 += pk * a.layer_stride;
     a.leaves += pk * a.tree_stride;
     a.slot += pk;
+    if (a.counter) a.counter += pk;
+    if (a.cap) a.cap += pk * a.cap_stride;
   }
+  const uint32_t nt = quarter < kThreads ? quarter : kThreads;
+  uint32_t d[8];
+  if (u < quarter) {
   const uint32_t N = 1u << a.logN, B = 1u << a.logB;
-  uint32_t k0;
-  if (a.logN >= 2) {
-    uint32_t j = u >> (a.logN - 2), q0 = u & ((N >> 2) - 1u);
-    k0 = (q0 << a.logB) | j;
+  uint32_t k0, P;
+  if (a.counter) {
+    P = u;
+    k0 = brev_bits(u, logm - 2);
   } else {
-    k0 = u;
+    if (a.logN >= 2) {
+      uint32_t j = u >> (a.logN - 2), q0 = u & ((N >> 2) - 1u);
+      k0 = (q0 << a.logB) | j;
+    } else {
+      k0 = u;
+    }
+    P = brev_bits(k0, logm - 2);
   }
-  const uint32_t P = brev_bits(k0, logm - 2);
   uint32_t xs[4];
   quad_points(tb, k0, logm, xs);
   uint32_t leaf[16];
@@ -832,9 +848,12 @@ __global__ void __launch_bounds__(kThreads) air_compose_leaves_kernel(AirCompose
 #pragma unroll
   for (int t = 0; t < 4; t++)
     dst[t] = make_uint4(leaf[4 * t], leaf[4 * t + 1], leaf[4 * t + 2], leaf[4 * t + 3]);
-  uint32_t d[8];
   blake3_leaf64(leaf, d);
   store_digest(a.leaves + 8 * (size_t)P, d);
+  }
+  if constexpr (kFused)
+    cta_subtree(d, buf, nt, (uint64_t)blockIdx.x * kThreads, a.leaves, quarter, a.top, a.cap,
+                a.counter);
 }
 
 // Range-check composition (src/range.rs:678-741 == composition_at :746-774).
@@ -1864,11 +1883,21 @@ cudaError_t merkle_build(cudaStream_t st, uint32_t* tree, uint64_t leaves, uint3
 }
 
 cudaError_t air_compose_leaves(cudaStream_t st, const Tables& tb, const AirComposeArgs& a,
-                               uint32_t nproofs) {
+                               uint32_t nproofs, uint32_t* levels) {
   uint32_t quarter = 1u << (a.logN + a.logB - 2);
+  AirComposeArgs f = a;
+  if (quarter > kFuseMaxLeaves || !f.counter) {
+    f.counter = nullptr;  // merkle_build does every level
+    f.top = 0;
+    f.cap = nullptr;
+  }
+  if (levels) *levels = f.counter ? f.top : 0;
   Stage stg("air_compose_leaves", st);
   stg.launched();
-  air_compose_leaves_kernel<<<dim3(grid_for(quarter), nproofs), kThreads, 0, st>>>(a, tb);
+  if (f.counter)
+    air_compose_leaves_kernel<true><<<dim3(grid_for(quarter), nproofs), kThreads, 0, st>>>(f, tb);
+  else
+    air_compose_leaves_kernel<false><<<dim3(grid_for(quarter), nproofs), kThreads, 0, st>>>(f, tb);
   return cudaGetLastError();
 }
 

@@ -70,6 +70,13 @@ struct AirComposeArgs {
   uint32_t w_last_m;      // omega_N^(N-1) (Montgomery)
   uint32_t slot;          // ProofConsts slot of the first proof: statement, alphas, kc
   uint64_t layer_stride = 0, tree_stride = 0;  // per-proof strides (words) of layer0 / leaves
+  // Fused layer-0 tree (air_compose_leaves, trees of <= kFuseMaxLeaves
+  // leaves): one zero counter per proof; the launch then hashes the tree up
+  // to level `top` and writes that level to cap (proof k at k * cap_stride).
+  unsigned int* counter = nullptr;
+  uint32_t top = 0;
+  uint32_t* cap = nullptr;
+  uint64_t cap_stride = 0;
 };
 
 struct RangeComposeArgs {
@@ -308,8 +315,11 @@ cudaError_t range_trace_leaves(cudaStream_t st, const uint32_t* lde, uint32_t* l
 cudaError_t merkle_build(cudaStream_t st, uint32_t* tree, uint64_t leaves, uint32_t top,
                          unsigned int* counter, uint32_t* cap, uint32_t from = 0,
                          uint32_t nproofs = 1, uint64_t stride = 0, uint64_t cap_stride = 0);
+// With a.counter set and a tree of at most kFuseMaxLeaves leaves, the
+// launch also builds the tree up to a.top; *levels receives the levels it
+// built (0: merkle_build does them all).
 cudaError_t air_compose_leaves(cudaStream_t st, const Tables& tb, const AirComposeArgs& a,
-                               uint32_t nproofs = 1);
+                               uint32_t nproofs = 1, uint32_t* levels = nullptr);
 cudaError_t range_compose_leaves(cudaStream_t st, const Tables& tb, const RangeComposeArgs& a,
                                  uint32_t nproofs = 1);
 // Folds one FRI layer; hashes the next layer's 64-byte leaves when it has a

@@ -1650,10 +1650,16 @@ int air_prove(z0p_gpu_ctx* c, const AirTask* tasks, uint32_t K) {
   ca.layer_stride = fb.val_stride;
   ca.tree_stride = fb.tree_stride;
   CK(push_consts(c, K));
-  CK(launch::air_compose_leaves(st, c->tb, ca, K));
-  CK(launch::merkle_build(st, fb.tree[0], s.leaves[0], s.depth[0] - s.drop[0], merkle_counter(c),
-                          hio_dev<uint32_t>(c, h.fri_cap[0]), 0, K, fb.tree_stride,
-                          h.fri_cap_bytes[0] / 4));
+  ca.counter = merkle_counter(c);  // small layer-0 trees are finished inside the launch
+  ca.top = s.depth[0] - s.drop[0];
+  ca.cap = hio_dev<uint32_t>(c, h.fri_cap[0]);
+  ca.cap_stride = h.fri_cap_bytes[0] / 4;
+  uint32_t built0 = 0;
+  CK(launch::air_compose_leaves(st, c->tb, ca, K, &built0));
+  if (built0 == 0)
+    CK(launch::merkle_build(st, fb.tree[0], s.leaves[0], s.depth[0] - s.drop[0], merkle_counter(c),
+                            hio_dev<uint32_t>(c, h.fri_cap[0]), 0, K, fb.tree_stride,
+                            h.fri_cap_bytes[0] / 4));
 
   std::vector<Transcript*> ts(K);
   for (uint32_t k = 0; k < K; k++) ts[k] = tasks[k].ts;
