@@ -1090,18 +1090,32 @@ struct Layer0Args {
   uint32_t* leaves;
   unsigned int* bad;
   uint32_t logm, logB, ncomp, coset_major;
+  unsigned int* counter;  // fused tree (kFused): zero counter, cap level and cap
+  uint32_t top;
+  uint32_t* cap;
 };
+// kFused (trees of <= kFuseMaxLeaves leaves): thread u makes leaf P = u and
+// the launch hashes the tree up to `top`, as air_compose_leaves does.
+template <bool kFused>
 __global__ void __launch_bounds__(kThreads) layer0_leaves_kernel(Layer0Args a) {
+  __shared__ uint32_t buf[kFused ? 2 * kThreads * kTopStride : 1];
   const uint32_t quarter = 1u << (a.logm - 2);
   const uint32_t u = blockIdx.x * blockDim.x + threadIdx.x;
-  if (u >= quarter) return;
+  const uint32_t nt = quarter < kThreads ? quarter : kThreads;
+  uint32_t d[8];
+  if (u < quarter) {
   const uint32_t logN = a.logm - a.logB;
-  uint32_t k0 = u;
-  if (a.coset_major && logN >= 2) {  // consecutive threads read consecutive q
-    const uint32_t j = u >> (logN - 2), q0 = u & ((1u << (logN - 2)) - 1u);
-    k0 = (q0 << a.logB) | j;
+  uint32_t k0 = u, P;
+  if (kFused) {
+    P = u;
+    k0 = brev_bits(u, a.logm - 2);
+  } else {
+    if (a.coset_major && logN >= 2) {  // consecutive threads read consecutive q
+      const uint32_t j = u >> (logN - 2), q0 = u & ((1u << (logN - 2)) - 1u);
+      k0 = (q0 << a.logB) | j;
+    }
+    P = brev_bits(k0, a.logm - 2);
   }
-  const uint32_t P = brev_bits(k0, a.logm - 2);
   const size_t m = (size_t)1 << a.logm;
   uint32_t leaf[16];
   unsigned int over = 0;
@@ -1125,9 +1139,12 @@ __global__ void __launch_bounds__(kThreads) layer0_leaves_kernel(Layer0Args a) {
 #pragma unroll
   for (int t = 0; t < 4; t++)
     dst[t] = make_uint4(leaf[4 * t], leaf[4 * t + 1], leaf[4 * t + 2], leaf[4 * t + 3]);
-  uint32_t d[8];
   blake3_leaf64(leaf, d);
   store_digest(a.leaves + 8 * (size_t)P, d);
+  }
+  if constexpr (kFused)
+    cta_subtree(d, buf, nt, (uint64_t)blockIdx.x * kThreads, a.leaves, quarter, a.top, a.cap,
+                a.counter);
 }
 
 // ---------------------------------------------------------- folded IVC ----
@@ -2058,13 +2075,21 @@ cudaError_t gamma_scale(cudaStream_t st, const Tables& tb, const uint32_t* in, u
 
 cudaError_t layer0_leaves(cudaStream_t st, const uint32_t* src, uint32_t* layer0, uint32_t* leaves,
                           unsigned int* bad, uint32_t logm, uint32_t logB, uint32_t ncomp,
-                          bool coset_major) {
+                          bool coset_major, unsigned int* counter, uint32_t top, uint32_t* cap,
+                          uint32_t* levels) {
   if (logm < 2) return cudaErrorInvalidValue;
+  const uint64_t quarter = 1ull << (logm - 2);
+  const bool fused = counter && quarter <= kFuseMaxLeaves;
   Layer0Args a{src, layer0, leaves, bad, logm, coset_major ? logB : 0u, ncomp,
-               coset_major ? 1u : 0u};
+               coset_major ? 1u : 0u, fused ? counter : nullptr, fused ? top : 0u,
+               fused ? cap : nullptr};
+  if (levels) *levels = fused ? top : 0u;
   Stage stg("layer0_leaves", st);
   stg.launched();
-  layer0_leaves_kernel<<<grid_for(1ull << (logm - 2)), kThreads, 0, st>>>(a);
+  if (fused)
+    layer0_leaves_kernel<true><<<grid_for(quarter), kThreads, 0, st>>>(a);
+  else
+    layer0_leaves_kernel<false><<<grid_for(quarter), kThreads, 0, st>>>(a);
   return cudaGetLastError();
 }
 

@@ -338,9 +338,13 @@ cudaError_t gamma_scale(cudaStream_t st, const Tables& tb, const uint32_t* in, u
 // coordinate LDEs (coset_major; ncomp planes of m = 2^logm words, 2^logB
 // cosets) or from natural-order evaluations (ncomp words per value, checked
 // canonical into *bad).
+// With a counter and a tree of at most kFuseMaxLeaves leaves, the launch
+// also builds the tree up to `top` and writes that level to cap; *levels
+// receives the levels built (0: merkle_build does them all).
 cudaError_t layer0_leaves(cudaStream_t st, const uint32_t* src, uint32_t* layer0, uint32_t* leaves,
                           unsigned int* bad, uint32_t logm, uint32_t logB, uint32_t ncomp,
-                          bool coset_major);
+                          bool coset_major, unsigned int* counter = nullptr, uint32_t top = 0,
+                          uint32_t* cap = nullptr, uint32_t* levels = nullptr);
 // Words of 1 / (x_k - w_last) for every LDE row, stored coset-major.
 cudaError_t row_inverses(cudaStream_t st, const Tables& tb, uint32_t* tinv, uint32_t w_last_m,
                          uint32_t logN, uint32_t logB);

@@ -2060,13 +2060,18 @@ int fri_commit(z0p_gpu_ctx* c, const FriInput& in, const uint32_t* values,
     lp.twist_mod = 1u << logB;
     lp.twist_shift = 27 - logm;
     CK(launch::ntt(st, c->tb, lp, coeffs, lde, (uint32_t*)c->scratch.p));
-    CK(launch::layer0_leaves(st, lde, f.fb.layer[0], f.fb.tree[0], bad, logm, logB, ncomp, true));
-  } else {
-    CK(launch::layer0_leaves(st, src, f.fb.layer[0], f.fb.tree[0], bad, logm, 0, ncomp, false));
   }
-  CK(launch::merkle_build(st, f.fb.tree[0], s.leaves[0], s.depth[0] - s.drop[0], merkle_counter(c),
-                          hio_dev<uint32_t>(c, f.h.fri_cap[0]), 0, 1, f.fb.tree_stride,
-                          f.h.fri_cap_bytes[0] / 4));
+  // Small layer-0 trees are finished inside the leaf launch.
+  const uint32_t top0 = s.depth[0] - s.drop[0];
+  uint32_t* cap0 = hio_dev<uint32_t>(c, f.h.fri_cap[0]);
+  uint32_t built0 = 0;
+  const bool from_lde = !in.evals;  // coefficients were extended (coset-major LDE)
+  CK(launch::layer0_leaves(st, from_lde ? (const uint32_t*)c->lde.p : src, f.fb.layer[0],
+                           f.fb.tree[0], bad, logm, from_lde ? logB : 0, ncomp, from_lde,
+                           merkle_counter(c), top0, cap0, &built0));
+  if (built0 == 0)
+    CK(launch::merkle_build(st, f.fb.tree[0], s.leaves[0], top0, merkle_counter(c), cap0, 0, 1,
+                            f.fb.tree_stride, f.h.fri_cap_bytes[0] / 4));
   z0p_transcript_state work = *t;
   Transcript tr(&work);
   Transcript* ts[1] = {&tr};
