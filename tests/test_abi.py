@@ -232,3 +232,15 @@ def test_shipped_schedule_is_valid(z0p):
     z0p.tune.set(s, 6)  # validates every field
     assert z0p.tune.to_dict(z0p.tune.get(6)) == z0p.tune.to_dict(s)
     z0p.tune.set(z0p.tune.default(), 6)
+
+
+def test_range_footprint_follows_the_proving_path(z0p):
+    # In-range values (constant-trace path) hold no device arrays; an
+    # out-of-range value whose final layer is below the blowup goes row by row.
+    n = C.c_size_t()
+    honest = z0p.range.Params.for_security(1 << 16, 16, 12345, 100)
+    assert z0p.lib().z0p_gpu_range_footprint(C.byref(honest), C.byref(n)) == 0
+    assert n.value <= 1 << 16
+    rows = z0p.range.Params.new(1 << 10, 4, 16, 8, 4, 300)
+    assert z0p.lib().z0p_gpu_range_footprint(C.byref(rows), C.byref(n)) == 0
+    assert n.value > 5 * 16 * (1 << 10) * 8

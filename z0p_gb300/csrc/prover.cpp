@@ -2544,6 +2544,12 @@ int z0p_gpu_range_footprint(const z0p_range_params* p, size_t* bytes) {
   FriShape s;
   RC(range_shape(*p, &fp, &s));
   uint64_t ncol = p->n_bits + 1, N = p->n_rows, m = s.m;
+  if (range_const_ok(*p, s)) {
+    // The constant-trace path keeps its compact trees in the mapped buffer
+    // and no device arrays: its device footprint is the PoW search state.
+    *bytes = 1ull << 16;
+    return Z0P_OK;
+  }
   uint64_t total = 8 * N * ncol + 8 * m * ncol + 32 * tree_digests(m);
   for (size_t i = 0; i < s.len.size(); i++) total += 16 * s.len[i] + 32 * tree_digests(s.leaves[i]);
   *bytes = total;
