@@ -553,25 +553,48 @@ __global__ void __launch_bounds__(kTraceLeafThreads) air_trace_leaves_kernel(
 // Range tree leaf k = BLAKE3(0x00 || row k) with the row = ncols LE words
 // (src/range.rs:452-460, src/hash.rs:351-381). Threads walk rows in
 // coset-major order so column reads coalesce; digests land at index k.
-__global__ void range_trace_leaves_kernel(const uint32_t* __restrict__ lde,
-                                          uint32_t* __restrict__ leaves, uint32_t logN,
-                                          uint32_t logB, uint32_t ncols, uint64_t tree_stride) {
-  uint32_t u = blockIdx.x * blockDim.x + threadIdx.x;
-  uint32_t m = 1u << (logN + logB);
-  if (u >= m) return;
+// kFused (trees of <= kFuseMaxLeaves leaves): thread u makes leaf k = u and
+// the launch hashes the tree up to `top` (cta_subtree); otherwise
+// consecutive threads read consecutive LDE rows of a coset.
+template <bool kFused>
+__global__ void __launch_bounds__(kThreads) range_trace_leaves_kernel(
+    const uint32_t* __restrict__ lde, uint32_t* __restrict__ leaves, uint32_t logN, uint32_t logB,
+    uint32_t ncols, uint64_t tree_stride, unsigned int* counter, uint32_t top, uint32_t* cap,
+    uint64_t cap_stride) {
+  __shared__ uint32_t buf[kFused ? 2 * kThreads * kTopStride : 1];
+  const uint32_t u = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t m = 1u << (logN + logB);
   lde += (size_t)blockIdx.y * ncols * m;
   leaves += blockIdx.y * tree_stride;
-  uint32_t j = u >> logN, q = u & ((1u << logN) - 1u);
-  uint32_t k = (q << logB) | j;
-  uint32_t w[32];
-#pragma unroll
-  for (int c = 0; c < 32; c++) w[c] = 0u;
-#pragma unroll
-  for (int c = 0; c < 25; c++)
-    if ((uint32_t)c < ncols) w[c] = __ldg(lde + ((size_t)c << (logN + logB)) + u);
+  if (kFused) {
+    counter += blockIdx.y;
+    if (cap) cap += blockIdx.y * cap_stride;
+  }
   uint32_t o[8];
-  row_leaf_digest(w, ncols, o);
-  store_digest(leaves + 8 * (size_t)k, o);
+  if (u < m) {
+    uint32_t j, q, k;
+    if (kFused) {
+      k = u;
+      j = k & ((1u << logB) - 1u);
+      q = k >> logB;
+    } else {
+      j = u >> logN;
+      q = u & ((1u << logN) - 1u);
+      k = (q << logB) | j;
+    }
+    const size_t at = ((size_t)j << logN) + q;
+    uint32_t w[32];
+#pragma unroll
+    for (int c = 0; c < 32; c++) w[c] = 0u;
+#pragma unroll
+    for (int c = 0; c < 25; c++)
+      if ((uint32_t)c < ncols) w[c] = __ldg(lde + ((size_t)c << (logN + logB)) + at);
+    row_leaf_digest(w, ncols, o);
+    store_digest(leaves + 8 * (size_t)k, o);
+  }
+  if constexpr (kFused)
+    cta_subtree(o, buf, m < kThreads ? m : kThreads, (uint64_t)blockIdx.x * kThreads, leaves, m,
+                top, cap, counter);
 }
 
 // Merkle trees whose leaves repeat in runs (kernels.h, UniformTree): one CTA
@@ -1850,12 +1873,23 @@ cudaError_t air_trace_leaves(cudaStream_t st, const Tables& tb, const uint32_t* 
 
 cudaError_t range_trace_leaves(cudaStream_t st, const uint32_t* lde, uint32_t* leaves,
                                uint32_t logN, uint32_t logB, uint32_t ncols, uint32_t nproofs,
-                               uint64_t tree_stride) {
+                               uint64_t tree_stride, unsigned int* counter, uint32_t top,
+                               uint32_t* cap, uint64_t cap_stride, uint32_t* levels) {
   if (ncols < 1 || ncols > 25) return cudaErrorInvalidValue;
+  const uint64_t m = 1ull << (logN + logB);
+  const bool fused = counter && m <= kFuseMaxLeaves;
+  if (levels) *levels = fused ? top : 0u;
   Stage stg("trace_leaves", st);
   stg.launched();
-  range_trace_leaves_kernel<<<dim3(grid_for(1ull << (logN + logB)), nproofs), kThreads, 0, st>>>(
-      lde, leaves, logN, logB, ncols, tree_stride);
+  const dim3 grid(grid_for(m), nproofs);
+  if (fused)
+    range_trace_leaves_kernel<true><<<grid, kThreads, 0, st>>>(lde, leaves, logN, logB, ncols,
+                                                               tree_stride, counter, top, cap,
+                                                               cap_stride);
+  else
+    range_trace_leaves_kernel<false><<<grid, kThreads, 0, st>>>(lde, leaves, logN, logB, ncols,
+                                                                tree_stride, nullptr, 0, nullptr,
+                                                                0);
   return cudaGetLastError();
 }
 

@@ -300,9 +300,15 @@ cudaError_t table_compose(cudaStream_t st, const Tables& tb, const TableComposeA
 // are alpha_0..alpha_4 with alpha_2, alpha_3 times omega_n^-1.
 cudaError_t air_compose_general(cudaStream_t st, const Tables& tb, const AirComposeArgs& a,
                                 const uint32_t* lde_b, uint32_t r);
+// With a counter (one zero word per proof) and at most kFuseMaxLeaves rows,
+// the launch also builds the tree up to `top` and writes that level to cap
+// (proof k at k * cap_stride); *levels receives the levels built (0:
+// merkle_build does them all).
 cudaError_t range_trace_leaves(cudaStream_t st, const uint32_t* lde, uint32_t* leaves,
                                uint32_t logN, uint32_t logB, uint32_t ncols, uint32_t nproofs = 1,
-                               uint64_t tree_stride = 0);
+                               uint64_t tree_stride = 0, unsigned int* counter = nullptr,
+                               uint32_t top = 0, uint32_t* cap = nullptr, uint64_t cap_stride = 0,
+                               uint32_t* levels = nullptr);
 // Builds levels 1..top of a tree stored level-contiguous (level l at digest
 // offset 2L - 2(L >> l), L = leaves, power of two). Levels above the cap
 // level are never read (caps and capped paths stop there), so callers pass

@@ -1457,8 +1457,11 @@ int table_prove_dev(z0p_gpu_ctx* c, const z0p_table_params& p, const uint32_t* t
   lp.logn = logL; lp.batch = (uint32_t)B; lp.in_div = (uint32_t)B; lp.twist_mod = (uint32_t)B;
   lp.twist_shift = 27 - logm;
   CK(launch::ntt(st, c->tb, lp, lde_in, lde, (uint32_t*)c->scratch.p));
-  CK(launch::range_trace_leaves(st, lde, ttree, logL, logB, 1));  // from_flat(.., 4) leaves
-  CK(launch::merkle_build(st, ttree, m, tsteps, merkle_counter(c), hio_dev<uint32_t>(c, h.trace_cap)));
+  uint32_t tbuilt = 0;  // from_flat(.., 4) leaves; small trees finished in the launch
+  CK(launch::range_trace_leaves(st, lde, ttree, logL, logB, 1, 1, 0, merkle_counter(c), tsteps,
+                                hio_dev<uint32_t>(c, h.trace_cap), 0, &tbuilt));
+  if (tbuilt == 0)
+    CK(launch::merkle_build(st, ttree, m, tsteps, merkle_counter(c), hio_dev<uint32_t>(c, h.trace_cap)));
   const uint32_t omega_n = two_adic_generator(logN);
   const uint32_t omega_inv = finv(omega_n);
   CK(launch::row_inverses(st, c->tb, tinv, to_mont(omega_inv), logL, logB));
@@ -1869,9 +1872,13 @@ int range_prove_columns(z0p_gpu_ctx* c, const RangeTask* tasks, uint32_t K, cons
   lp.twist_shift = 27 - logm;
   CK(launch::ntt(st, c->tb, lp, coeffs, lde, (uint32_t*)c->scratch.p));
   const uint64_t tcap_stride = h.trace_cap_bytes / 4;
-  CK(launch::range_trace_leaves(st, lde, ttree, logN, logB, (uint32_t)ncol, K, ttree_words));
-  CK(launch::merkle_build(st, ttree, m, tsteps, merkle_counter(c), hio_dev<uint32_t>(c, h.trace_cap),
-                          0, K, ttree_words, tcap_stride));
+  uint32_t tbuilt = 0;  // small trees finished in the launch
+  CK(launch::range_trace_leaves(st, lde, ttree, logN, logB, (uint32_t)ncol, K, ttree_words,
+                                merkle_counter(c), tsteps, hio_dev<uint32_t>(c, h.trace_cap),
+                                tcap_stride, &tbuilt));
+  if (tbuilt == 0)
+    CK(launch::merkle_build(st, ttree, m, tsteps, merkle_counter(c),
+                            hio_dev<uint32_t>(c, h.trace_cap), 0, K, ttree_words, tcap_stride));
   CK(launch::coset_zinv(st, c->tb, zinv, zinv2, logB, to_mont(fpow(GENERATOR, N)), nullptr, slot));
   CK(sync(c, "cap"));
   if (host_cols && *reinterpret_cast<volatile unsigned int*>(c->hio + bad_at)) {
@@ -2224,8 +2231,11 @@ int fold_add(z0p_gpu_fold* f, const uint32_t* col_a, const uint32_t* col_b,
   CK(launch::ntt(st, c->tb, lp, (uint32_t*)c->coeffs.p, lde, (uint32_t*)c->scratch.p));
   // Row tree over A || B (src/fold.rs:448-458: MerkleTree::from_flat, 8-byte rows).
   uint32_t* tree = (uint32_t*)step.tree.p;
-  CK(launch::range_trace_leaves(st, lde, tree, logN, logB, 2));
-  CK(launch::merkle_build(st, tree, m, depth - drop, merkle_counter(c), hio_dev<uint32_t>(c, 64)));
+  uint32_t built = 0;  // small segment trees finished in the launch
+  CK(launch::range_trace_leaves(st, lde, tree, logN, logB, 2, 1, 0, merkle_counter(c), depth - drop,
+                                hio_dev<uint32_t>(c, 64), 0, &built));
+  if (built == 0)
+    CK(launch::merkle_build(st, tree, m, depth - drop, merkle_counter(c), hio_dev<uint32_t>(c, 64)));
   CK(sync(c, "cap"));
   if (*reinterpret_cast<volatile unsigned int*>(bad_h)) {
     set_reason("field elements must be canonical (< p)");
