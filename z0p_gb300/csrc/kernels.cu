@@ -116,6 +116,7 @@ __global__ void fill_columns_kernel(uint32_t* cols, uint32_t n, uint32_t ncols,
 struct NttArgs {
   uint32_t logn, inverse, in_div, twist_mod, twist_shift, post_gamma, ninv_m;
   Tables tb;
+  unsigned int* bad;  // see NttPlan::bad
 };
 
 __device__ __forceinline__ uint32_t spos(uint32_t i) { return i + (i >> 5); }
@@ -222,6 +223,7 @@ __global__ void __launch_bounds__(512) ntt_small_kernel(const uint32_t* __restri
   }
   for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
     uint32_t v = src[i];
+    if (a.bad && v >= kP) atomicOr(a.bad, 1u);
     if (j) {
       v = mmul(v, tw_cur);
       tw_cur = mmul(tw_cur, tw_step);
@@ -282,6 +284,7 @@ __global__ void __launch_bounds__(512) ntt_pass1_kernel(const uint32_t* __restri
   for (uint32_t e = threadIdx.x; e < (n1 << LOGC); e += blockDim.x) {
     const uint32_t i1 = e >> LOGC, c = e & (C - 1);
     uint32_t v = src[(i1 << logn2) + c0 + c];
+    if (a.bad && v >= kP) atomicOr(a.bad, 1u);
     if (j) v = mmul(v, twist[i1]);
     s[c * cstride + spos(i1)] = v;
   }
@@ -1171,11 +1174,6 @@ __global__ void __launch_bounds__(kThreads) layer0_leaves_kernel(Layer0Args a) {
 }
 
 // ---------------------------------------------------------- folded IVC ----
-__global__ void check_canonical_kernel(const uint32_t* __restrict__ in, uint64_t n,
-                                       unsigned int* bad) {
-  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n && in[i] >= kP) atomicOr(bad, 1u);
-}
 
 // 1/(x_k - w_last) for rows k = 8L..8L+7 (consecutive powers of omega_m), one
 // batched inversion per thread, stored coset-major at [j][q], k = B q + j.
@@ -1755,6 +1753,7 @@ cudaError_t ntt(cudaStream_t st, const Tables& tb, const NttPlan& plan, const ui
   a.twist_mod = plan.twist_mod ? plan.twist_mod : 1;
   a.twist_shift = plan.twist_shift;
   a.post_gamma = plan.post_gamma;
+  a.bad = plan.in_div > 1 ? nullptr : plan.bad;  // each input word loaded once
   // n^-1 in Montgomery form: (2^-logn) * 2^32 mod p.
   {
     uint64_t inv2 = (kP + 1) / 2;  // 2^-1 mod p
@@ -2137,12 +2136,6 @@ cudaError_t row_inverses(cudaStream_t st, const Tables& tb, uint32_t* tinv, uint
   return cudaGetLastError();
 }
 
-cudaError_t check_canonical(cudaStream_t st, const uint32_t* in, uint64_t n, unsigned int* bad) {
-  Stage stg("check_canonical", st);
-  stg.launched();
-  check_canonical_kernel<<<grid_for(n), kThreads, 0, st>>>(in, n, bad);
-  return cudaGetLastError();
-}
 
 cudaError_t fold_combine(cudaStream_t st, const Tables& tb, const FoldCombineArgs& a) {
   if (a.logN + a.logB < 3) return cudaErrorInvalidValue;

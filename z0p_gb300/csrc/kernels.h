@@ -33,6 +33,9 @@ struct NttPlan {
   uint32_t twist_mod = 1;
   uint32_t twist_shift = 0;
   uint32_t post_gamma = 0;
+  // Non-null: every input word is checked on load, and a value >= p sets
+  // *bad (a caller's columns; the C boundary takes canonical elements).
+  unsigned int* bad = nullptr;
 };
 
 // Column B of the Fibonacci trace is never transformed: on the LDE,
@@ -354,8 +357,6 @@ cudaError_t layer0_leaves(cudaStream_t st, const uint32_t* src, uint32_t* layer0
 // Words of 1 / (x_k - w_last) for every LDE row, stored coset-major.
 cudaError_t row_inverses(cudaStream_t st, const Tables& tb, uint32_t* tinv, uint32_t w_last_m,
                          uint32_t logN, uint32_t logB);
-// *bad = 1 when any of the n words is not a canonical field element.
-cudaError_t check_canonical(cudaStream_t st, const uint32_t* in, uint64_t n, unsigned int* bad);
 // combined(x) = sum_k gamma_k C_k(x) over the accumulated segments, written
 // as FRI layer 0 with its leaf digests (src/fold.rs:494-517, 785-850).
 cudaError_t fold_combine(cudaStream_t st, const Tables& tb, const FoldCombineArgs& a);

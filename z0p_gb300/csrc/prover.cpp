@@ -877,8 +877,7 @@ int air_prove_general(z0p_gpu_ctx* c, const z0p_air_params& p, const GeneralAir&
   if (g.host_a) {
     CK(cudaMemcpyAsync(cols, g.host_a, 4 * N, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(cols + N, g.host_b, 4 * N, cudaMemcpyHostToDevice, st));
-    c->h2d += 8 * N;
-    CK(launch::check_canonical(st, cols, 2 * N, hio_dev<unsigned int>(c, h.extra)));
+    c->h2d += 8 * N;  // checked as the interpolation loads them (NttPlan::bad)
   } else {
     uint32_t mats[32][4];
     fib_mats(mats);
@@ -886,6 +885,7 @@ int air_prove_general(z0p_gpu_ctx* c, const z0p_air_params& p, const GeneralAir&
   }
   NttPlan ip;  // interpolate both columns; outputs times 31^i / ... (coset twist included)
   ip.logn = logN; ip.batch = 2; ip.inverse = 1; ip.post_gamma = 1;
+  if (g.host_a) ip.bad = hio_dev<unsigned int>(c, h.extra);
   CK(launch::ntt(st, c->tb, ip, cols, coeffs, (uint32_t*)c->scratch.p));
   const uint32_t* lde_in = coeffs;
   if (Lp != N || g.n_rand) {  // T + (x^n - 1) R, zero-padded (src/blind.rs:40-78)
@@ -1858,13 +1858,13 @@ int range_prove_columns(z0p_gpu_ctx* c, const RangeTask* tasks, uint32_t K, cons
     for (uint64_t j = 0; j < ncol; j++)
       CK(cudaMemcpyAsync(cols + j * N, host_cols[j], 4 * N, cudaMemcpyHostToDevice, st));
     c->h2d += 4 * N * ncol;
-    *reinterpret_cast<unsigned int*>(c->hio + bad_at) = 0u;
-    CK(launch::check_canonical(st, cols, N * ncol, hio_dev<unsigned int>(c, bad_at)));
+    *reinterpret_cast<unsigned int*>(c->hio + bad_at) = 0u;  // checked by the interpolation
   } else {
     CK(launch::fill_constant_columns(st, cols, (uint32_t)N, (uint32_t)ncol, dvals, K));
   }
   NttPlan ip;
   ip.logn = logN; ip.batch = (uint32_t)(ncol * K); ip.inverse = 1; ip.post_gamma = 1;
+  if (host_cols) ip.bad = hio_dev<unsigned int>(c, bad_at);
   CK(launch::ntt(st, c->tb, ip, cols, coeffs, (uint32_t*)c->scratch.p));
   NttPlan lp;
   lp.logn = logN; lp.batch = (uint32_t)(ncol * B * K); lp.in_div = (uint32_t)B;
@@ -2220,9 +2220,9 @@ int fold_add(z0p_gpu_fold* f, const uint32_t* col_a, const uint32_t* col_b,
   CK(cudaMemcpyAsync(cols, col_a, 4 * S, cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(cols + S, col_b, 4 * S, cudaMemcpyHostToDevice, st));
   c->h2d += 8 * S;
-  CK(launch::check_canonical(st, cols, 2 * S, hio_dev<unsigned int>(c, 0)));
   NttPlan ip;  // interpolate (src/ntt.rs:316-321), outputs times 31^i / S
   ip.logn = logN; ip.batch = 2; ip.inverse = 1; ip.post_gamma = 1;
+  ip.bad = hio_dev<unsigned int>(c, 0);  // the columns are checked as they load
   CK(launch::ntt(st, c->tb, ip, cols, (uint32_t*)c->coeffs.p, (uint32_t*)c->scratch.p));
   NttPlan lp;  // evaluate_on_coset (src/ntt.rs:341-363), coset-major per column
   lp.logn = logN; lp.batch = (uint32_t)(2 * B); lp.in_div = (uint32_t)B; lp.twist_mod = (uint32_t)B;
