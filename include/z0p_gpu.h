@@ -220,6 +220,15 @@ int z0p_gpu_air_prove(z0p_gpu_ctx *ctx, const z0p_air_params *params,
 int z0p_gpu_range_prove(z0p_gpu_ctx *ctx, const z0p_range_params *params,
                         z0p_transcript_state *transcript, uint8_t *out, size_t cap,
                         size_t *len);
+/* range::prove_zk (src/range.rs:393-418): every column masked with n_rand
+ * maskers drawn from `rng`, column after column (value first); the LDE runs
+ * over 2^ceil(log2(n_rows + n_rand)) rows. n_rand < num_queries is
+ * Z0P_ERR_MALFORMED_INPUT. On error neither the transcript nor the stream
+ * moves. */
+int z0p_range_proof_size_zk(const z0p_range_params *params, size_t n_rand, size_t *len);
+int z0p_gpu_range_prove_zk(z0p_gpu_ctx *ctx, const z0p_range_params *params, size_t n_rand,
+                           z0p_chacha20_state *rng, z0p_transcript_state *transcript,
+                           uint8_t *out, size_t cap, size_t *out_len);
 /* range::prove_with_columns (src/range.rs:353-375): the caller's value column
  * and n_bits bit columns, n_rows canonical words each. Any values prove
  * structurally (invalid columns fail verify). Shapes that differ from the

@@ -175,6 +175,8 @@ def lib():
             "zo_range_params_new": (C.c_int, [C.c_uint64] * 5 + [C.c_uint32, C.POINTER(RangeParams)]),
             "zo_range_for_security": (C.c_int, [C.c_uint64, C.c_uint64, C.c_uint32, C.c_uint32, C.POINTER(RangeParams)]),
             "zo_range_prove": (C.c_int, [C.POINTER(RangeParams), vp, C.POINTER(u8p), C.POINTER(sz)]),
+            "zo_range_prove_zk": (C.c_int, [C.POINTER(RangeParams), sz, C.POINTER(ChaCha20), vp,
+                                            C.POINTER(u8p), C.POINTER(sz)]),
             "zo_range_prove_with_columns": (C.c_int, [C.POINTER(RangeParams), u32p, vp, C.POINTER(u8p),
                                                       C.POINTER(sz)]),
             "zo_range_verify": (C.c_int, [C.POINTER(RangeParams), C.c_char_p, sz, vp]),
@@ -467,6 +469,13 @@ def range_prove_with_columns(params: RangeParams, v_col, bit_cols, t: Transcript
     buf, n = C.POINTER(C.c_uint8)(), C.c_size_t()
     rc = lib().zo_range_prove_with_columns(C.byref(params), cols.ctypes.data_as(C.POINTER(C.c_uint32)),
                                            t.h, C.byref(buf), C.byref(n))
+    return _take_proof(rc, buf, n)
+
+
+def range_prove_zk(params: RangeParams, n_rand: int, rng, t: Transcript) -> bytes:
+    """range.rs:393-418: every column masked from the ChaCha20 stream `rng`."""
+    buf, n = C.POINTER(C.c_uint8)(), C.c_size_t()
+    rc = lib().zo_range_prove_zk(C.byref(params), n_rand, C.byref(rng), t.h, C.byref(buf), C.byref(n))
     return _take_proof(rc, buf, n)
 
 

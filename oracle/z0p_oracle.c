@@ -2991,21 +2991,66 @@ int zo_range_prove_with_columns(const zo_range_params *params, const uint32_t *c
     return range_prove_cols(params, cols, t, proof, proof_len);
 }
 
+/* range.rs:425-514 prove_from_columns over coefficient columns of length L
+ * (power of two; takes ownership of coeffs). */
+static int range_prove_coeffs(const zo_range_params *params, uint32_t **coeffs, size_t L,
+                              uint64_t degree_bound, zo_transcript *t, uint8_t **proof,
+                              size_t *proof_len);
+
 static int range_prove_cols(const zo_range_params *params, const uint32_t *cols, zo_transcript *t,
                             uint8_t **proof, size_t *proof_len) {
-    int rc;
-    size_t n = params->n_rows, m = n * params->blowup, ncol = params->n_bits + 1;
-    uint32_t **ldes = malloc(ncol * sizeof(uint32_t *));
+    size_t n = params->n_rows, ncol = params->n_bits + 1;
     uint32_t **coeffs = malloc(ncol * sizeof(uint32_t *));
     for (size_t k = 0; k < ncol; k++) {  /* range.rs:370-374 interpolate */
         coeffs[k] = malloc(n * 4);
         memcpy(coeffs[k], cols + k * n, n * 4);
         zo_ntt_inverse(coeffs[k], n);
     }
+    return range_prove_coeffs(params, coeffs, n, n - 1, t, proof, proof_len);
+}
+
+/* range.rs:393-418 prove_zk: every column masked with n_rand maskers from the
+ * stream, column after column (value first). */
+int zo_range_prove_zk(const zo_range_params *params, size_t n_rand, zo_chacha20 *rng,
+                      zo_transcript *t, uint8_t **proof, size_t *proof_len) {
+    int rc = range_validate(params);
+    if (rc) return rc;
+    if (n_rand < params->num_queries) return ZO_MALFORMED_INPUT;
+    size_t n = params->n_rows, ncol = params->n_bits + 1, pl = 0;
+    uint32_t **coeffs = malloc(ncol * sizeof(uint32_t *));
+    uint32_t *c = malloc(n * 4);
+    for (size_t k = 0; k < ncol; k++) {
+        uint32_t v = k == 0 ? params->value
+                            : ((k - 1) < 32 ? (params->value >> (k - 1)) & 1 : 0);
+        for (size_t i = 0; i < n; i++) c[i] = v;
+        zo_ntt_inverse(c, n);
+        coeffs[k] = mask_coeffs(c, n, n_rand, rng, &pl);
+    }
+    free(c);
+    if (pl > MAX_DOMAIN) {
+        for (size_t k = 0; k < ncol; k++) free(coeffs[k]);
+        free(coeffs);
+        return ZO_INVALID_DOMAIN_SIZE;
+    }
+    return range_prove_coeffs(params, coeffs, pl, n + 2 * n_rand - 2, t, proof, proof_len);
+}
+
+static int range_prove_coeffs(const zo_range_params *params, uint32_t **coeffs, size_t L,
+                              uint64_t degree_bound, zo_transcript *t, uint8_t **proof,
+                              size_t *proof_len) {
+    int rc;
+    size_t n = params->n_rows, ncol = params->n_bits + 1;
+    if (L > SIZE_MAX / params->blowup || L * params->blowup > MAX_DOMAIN) {
+        for (size_t k = 0; k < ncol; k++) free(coeffs[k]);
+        free(coeffs);
+        return ZO_INVALID_DOMAIN_SIZE;
+    }
+    size_t m = L * params->blowup;
+    uint32_t **ldes = malloc(ncol * sizeof(uint32_t *));
     range_absorb_params(params, t);  /* range.rs:437 */
     for (size_t k = 0; k < ncol; k++) {  /* range.rs:441-448 */
         ldes[k] = malloc(m * 4);
-        zo_evaluate_on_coset(coeffs[k], n, params->blowup, LDE_SHIFT, ldes[k]);
+        zo_evaluate_on_coset(coeffs[k], L, params->blowup, LDE_SHIFT, ldes[k]);
         free(coeffs[k]);
     }
     free(coeffs);
@@ -3038,7 +3083,10 @@ static int range_prove_cols(const zo_range_params *params, const uint32_t *cols,
     fri_params_new(params->blowup, params->num_queries, params->final_size, &fp);
     fp.grinding_bits = params->grinding_bits; fp.cap_height = params->cap_height;
     fri_state st;
-    rc = fri_commit_inner(c.out, m, n - 1, m, &fp, t, &st);
+    rc = fri_params_validate(&fp);
+    if (!rc && degree_bound >= m) rc = ZO_MALFORMED_INPUT;
+    if (!rc) rc = fri_commit_inner(c.out, m, degree_bound, m, &fp, t, &st);
+    else free(c.out);
     if (!rc) {
         writer w = {0};
         w_byte(&w, VERSION);

@@ -207,6 +207,8 @@ void zo_chacha20_block(const uint8_t key[32], uint32_t counter, const uint8_t no
                        uint8_t out[64]);
 void zo_chacha20_init(zo_chacha20 *s, const uint8_t key[32], const uint8_t nonce[12]);
 void zo_chacha20_fill(zo_chacha20 *s, uint8_t *out, size_t n);
+int zo_range_prove_zk(const zo_range_params *params, size_t n_rand, zo_chacha20 *rng,
+                      zo_transcript *t, uint8_t **proof, size_t *proof_len);
 uint32_t zo_chacha20_next_field(zo_chacha20 *s);
 int zo_air_prove_zk(const zo_air_params *params, size_t n_rand, zo_chacha20 *rng,
                     zo_transcript *t, uint8_t **proof, size_t *proof_len);

@@ -96,3 +96,29 @@ def test_groups_mix_in_and_out_of_range_values(z0p, oracle, gpu_ctx):
         po = oracle.range_for_security(n, 16, v, 100)
         assert group[i] == oracle.range_prove(po, oracle.Transcript(b"grp%d" % i)), v
         assert group[i] == z0p.range.prove(params[i], z0p.Transcript(b"grp%d" % i), gpu_ctx)
+
+
+@pytest.mark.parametrize("n,bits,blowup,final,n_rand,value", [
+    (8, 4, 8, 8, 8, 5), (64, 8, 16, 32, 40, 200), (256, 16, 8, 16, 100, 300), (1 << 12, 16, 16, 32, 1 << 12, 1234)])
+def test_range_prove_zk_matches_oracle(z0p, oracle, gpu_ctx, n, bits, blowup, final, n_rand, value):
+    pz = z0p.range.Params.new(n, bits, blowup, 8, final, value).with_cap_height(2)
+    po = oracle.range_params_new(n, bits, blowup, 8, final, value, 0, 2)
+    key, nonce = bytes([n % 251]) * 32, bytes([3]) * 12
+    rz, ro = z0p.rng.ChaCha20.new(key, nonce), oracle.ChaCha20.new(key, nonce)
+    tg, to = z0p.Transcript(b"rzk"), oracle.Transcript(b"rzk")
+    proof = z0p.range.prove_zk(pz, n_rand, rz, tg, gpu_ctx)
+    assert proof == oracle.range_prove_zk(po, n_rand, ro, to)
+    assert tg.export() == to.export()
+    assert (bytes(rz.block), rz.counter, rz.used) == (bytes(ro.block), ro.counter, ro.used)
+    assert (oracle.range_verify(po, proof, oracle.Transcript(b"rzk")) == 0) == (value < (1 << bits))
+
+
+def test_range_prove_zk_errors_leave_state(z0p, gpu_ctx):
+    pz = z0p.range.Params.new(64, 8, 16, 8, 32, 5)
+    rz = z0p.rng.ChaCha20.new(bytes(32), bytes(12))
+    t = z0p.Transcript(b"rzk-err")
+    before_t, before_r = t.export(), rz.export()
+    with pytest.raises(z0p.Z0pError) as e:
+        z0p.range.prove_zk(pz, 7, rz, t, gpu_ctx)
+    assert e.value.code == 8
+    assert t.export() == before_t and rz.export() == before_r

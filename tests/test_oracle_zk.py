@@ -71,3 +71,21 @@ def test_tampered_masked_proof_fails(oracle):
     bad = bytearray(p)
     bad[-70] ^= 1
     assert oracle.air_verify(params, bytes(bad), oracle.Transcript(b"zk")) != 0
+
+
+def test_range_prove_zk_verifies_and_depends_on_the_stream(oracle):
+    # range.rs:393-418: masked columns verify with the plain verifier; the
+    # hiding budget n_rand >= num_queries is enforced.
+    p = oracle.range_params_new(64, 8, 16, 8, 32, 200)
+    a = oracle.range_prove_zk(p, 40, oracle.ChaCha20.new(bytes(32), bytes(12)), oracle.Transcript(b"rz"))
+    b = oracle.range_prove_zk(p, 40, oracle.ChaCha20.new(bytes([1]) * 32, bytes(12)),
+                              oracle.Transcript(b"rz"))
+    assert a != b
+    assert oracle.range_verify(p, a, oracle.Transcript(b"rz")) == 0
+    assert oracle.range_verify(p, b, oracle.Transcript(b"rz")) == 0
+    bad = oracle.range_params_new(64, 8, 16, 8, 32, 300)  # 300 needs 9 bits
+    c = oracle.range_prove_zk(bad, 40, oracle.ChaCha20.new(bytes(32), bytes(12)), oracle.Transcript(b"rz"))
+    assert oracle.range_verify(bad, c, oracle.Transcript(b"rz")) != 0
+    with pytest.raises(ValueError) as e:
+        oracle.range_prove_zk(p, 7, oracle.ChaCha20.new(bytes(32), bytes(12)), oracle.Transcript(b"rz"))
+    assert str(e.value) == "MalformedInput"

@@ -142,6 +142,9 @@ def lib():
             "z0p_gpu_ctx_trim": (C.c_int, [vp]),
             "z0p_gpu_ctx_reserve_group": (C.c_int, [vp, C.c_uint32]),
             "z0p_gpu_blake3_ceiling": (C.c_int, [vp, P(C.c_double)]),
+            "z0p_range_proof_size_zk": (C.c_int, [P(RangeParams), sz, P(sz)]),
+            "z0p_gpu_range_prove_zk": (C.c_int, [vp, P(RangeParams), sz, P(ChaChaState),
+                                                 P(TranscriptState), P(C.c_uint8), sz, P(sz)]),
             "z0p_gpu_range_prove_with_columns": (C.c_int, [vp, P(RangeParams), P(C.c_uint32), sz,
                                                            P(P(C.c_uint32)), P(sz), sz,
                                                            P(TranscriptState), P(C.c_uint8), sz, P(sz)]),

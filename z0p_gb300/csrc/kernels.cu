@@ -923,7 +923,8 @@ __global__ void __launch_bounds__(kThreads) range_compose_leaves_kernel(RangeCom
     size_t row = ((size_t)j << a.logN) + q;
     size_t colstride = (size_t)1 << logm;
     uint32_t v = __ldg(a.lde + row);
-    uint32_t zi = __ldg(a.zinv + j), zi2 = __ldg(a.zinv2 + j);
+    const uint32_t zrow = j * a.r + (q & (a.r - 1u));
+    uint32_t zi = __ldg(a.zinv + zrow), zi2 = __ldg(a.zinv2 + zrow);
     // Bit columns four at a time, highest first (columns past nb read as 0):
     // rec = sum bit_c 2^c by Horner, and per coordinate
     // sum_c alpha_c bit_c (bit_c - 1) as one lazy four-term dot product per

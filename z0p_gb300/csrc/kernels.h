@@ -89,9 +89,12 @@ struct RangeComposeArgs {
   const uint32_t* alphas;  // (n_bits + 2) Ext4 in Montgomery form: decomp, bits..., bound
   uint32_t* layer0;
   uint32_t* leaves;
-  uint32_t logN, logB, n_bits;
+  uint32_t logN, logB, n_bits;  // logN: rows per coset of the LDE (padded when masked)
   uint32_t slot;  // ProofConsts slot of the first proof: the claimed value
   uint64_t layer_stride = 0, tree_stride = 0;  // per-proof strides (words) of layer0 / leaves
+  // zinv / zinv2 hold B x r values, [j][q mod r]: x^n is periodic in q with
+  // period r = padded rows / n (1 unpadded).
+  uint32_t r = 1;
 };
 
 struct FoldArgs {

@@ -719,6 +719,29 @@ int range_shape(const z0p_range_params& p, FriParams* fp, FriShape* s) {
   return fri_shape(p.n_rows * p.blowup, p.n_rows - 1, *fp, s);
 }
 
+// range::prove_zk's shape (src/range.rs:393-418): rows padded to
+// 2^ceil(log2(n + n_rand)), composition bound n + 2 n_rand - 2.
+int range_zk_shape(const z0p_range_params& p, uint64_t n_rand, FriParams* fp, FriShape* s) {
+  RC(range_validate(p));
+  if (n_rand < p.num_queries) {
+    set_reason("n_rand must cover num_queries for hiding");
+    return Z0P_ERR_MALFORMED_INPUT;
+  }
+  if (n_rand > MAX_DOMAIN) return Z0P_ERR_INVALID_DOMAIN_SIZE;
+  uint64_t lp = 1;
+  while (lp < p.n_rows + n_rand) lp <<= 1;
+  if (lp > MAX_DOMAIN / p.blowup) return Z0P_ERR_INVALID_DOMAIN_SIZE;
+  RC(fri_params_new(p.blowup, p.num_queries, p.final_size, fp));
+  fp->grinding_bits = p.grinding_bits;
+  fp->cap_height = p.cap_height;
+  const uint64_t bound = p.n_rows + 2 * n_rand - 2;
+  if (bound >= lp * p.blowup) {
+    set_reason("degree bound must be below LDE size (rate < 1)");
+    return Z0P_ERR_MALFORMED_INPUT;
+  }
+  return fri_shape(lp * p.blowup, bound, *fp, s);
+}
+
 uint64_t air_size(const z0p_air_params& p, const FriShape& s) {
   uint64_t m = s.m, leaves = m / 8;
   uint32_t depth = log2u(leaves), drop = p.cap_height < depth ? (uint32_t)p.cap_height : depth;
@@ -1801,20 +1824,28 @@ int range_prove_const(z0p_gpu_ctx* c, const RangeTask* tasks, uint32_t K, const 
 // proofs of one shape in lockstep: the columns of range::prove (host_cols
 // null: value and its bits, filled on the device) or, for K = 1, the
 // caller's n_bits + 1 columns of n_rows words, value column first.
+// With n_rand (K = 1), every column is masked as range::prove_zk does
+// (src/range.rs:393-418) with rand[c * n_rand + k] and the LDE runs over the
+// padded rows.
 int range_prove_columns(z0p_gpu_ctx* c, const RangeTask* tasks, uint32_t K, const FriParams& fp,
-                        const FriShape& s, uint64_t need, const uint32_t* const* host_cols) {
+                        const FriShape& s, uint64_t need, const uint32_t* const* host_cols,
+                        uint64_t n_rand = 0, const uint32_t* rand = nullptr) {
   const z0p_range_params& p0 = *tasks[0].p;
-  const uint64_t N = p0.n_rows, B = p0.blowup, m = N * B, ncol = p0.n_bits + 1;
-  const uint32_t logN = log2u(N), logB = log2u(B), logm = logN + logB;
+  const uint64_t N = p0.n_rows, B = p0.blowup, ncol = p0.n_bits + 1;
+  uint64_t Lp = N;  // rows per coset of the LDE: padded to 2^ceil(log2(n + n_rand)) when masked
+  while (n_rand && Lp < N + n_rand) Lp <<= 1;
+  const uint64_t m = Lp * B, r = Lp / N;
+  const uint32_t logN = log2u(N), logL = log2u(Lp), logB = log2u(B), logm = logL + logB;
+  const uint64_t bound = n_rand ? N + 2 * n_rand - 2 : N - 1;  // src/range.rs:417
   cudaStream_t st = c->stream;
   RC(ensure_slots(c, K));
   RC(ensure(c, c->cols, 4 * N * ncol * K));
-  RC(ensure(c, c->coeffs, 4 * N * ncol * K));
+  RC(ensure(c, c->coeffs, 4 * (N * ncol * K + (n_rand ? Lp * ncol : 0))));
   RC(ensure(c, c->scratch, 4 * m * ncol * K));
   RC(ensure(c, c->lde, 4 * m * ncol * K));
   const uint64_t ttree_words = 8 * tree_digests(m);
   RC(ensure(c, c->ttree, 4 * ttree_words * K));
-  RC(ensure(c, c->misc, 64 + 8 * B));
+  RC(ensure(c, c->misc, 4 * (16 + 2 * B * r + ncol * n_rand)));
   FriBufs fb;
   RC(plan_fri_buffers(c, s, K, &fb));
   uint32_t* cols = (uint32_t*)c->cols.p;
@@ -1822,7 +1853,8 @@ int range_prove_columns(z0p_gpu_ctx* c, const RangeTask* tasks, uint32_t K, cons
   uint32_t* lde = (uint32_t*)c->lde.p;
   uint32_t* ttree = (uint32_t*)c->ttree.p;
   uint32_t* zinv = (uint32_t*)c->misc.p + 16;
-  uint32_t* zinv2 = zinv + B;
+  uint32_t* zinv2 = zinv + B * r;
+  uint32_t* rdev = zinv2 + B * r;
   const uint32_t tdepth = logm;
   const uint32_t tdrop = p0.cap_height < tdepth ? (uint32_t)p0.cap_height : tdepth;
   const uint32_t tsteps = tdepth - tdrop;
@@ -1866,20 +1898,42 @@ int range_prove_columns(z0p_gpu_ctx* c, const RangeTask* tasks, uint32_t K, cons
   ip.logn = logN; ip.batch = (uint32_t)(ncol * K); ip.inverse = 1; ip.post_gamma = 1;
   if (host_cols) ip.bad = hio_dev<unsigned int>(c, bad_at);
   CK(launch::ntt(st, c->tb, ip, cols, coeffs, (uint32_t*)c->scratch.p));
+  const uint32_t* lde_in = coeffs;
+  if (n_rand) {  // T + (x^n - 1) R per column, zero-padded (src/blind.rs:40-78)
+    CK(cudaMemcpyAsync(rdev, rand, 4 * ncol * n_rand, cudaMemcpyHostToDevice, st));
+    c->h2d += 4 * ncol * n_rand;
+    CK(launch::mask_pad(st, c->tb, coeffs, rdev, coeffs + N * ncol, (uint32_t)N, (uint32_t)n_rand,
+                        (uint32_t)Lp, (uint32_t)ncol));
+    lde_in = coeffs + N * ncol;
+  }
   NttPlan lp;
-  lp.logn = logN; lp.batch = (uint32_t)(ncol * B * K); lp.in_div = (uint32_t)B;
+  lp.logn = logL; lp.batch = (uint32_t)(ncol * B * K); lp.in_div = (uint32_t)B;
   lp.twist_mod = (uint32_t)B;
   lp.twist_shift = 27 - logm;
-  CK(launch::ntt(st, c->tb, lp, coeffs, lde, (uint32_t*)c->scratch.p));
+  CK(launch::ntt(st, c->tb, lp, lde_in, lde, (uint32_t*)c->scratch.p));
   const uint64_t tcap_stride = h.trace_cap_bytes / 4;
   uint32_t tbuilt = 0;  // small trees finished in the launch
-  CK(launch::range_trace_leaves(st, lde, ttree, logN, logB, (uint32_t)ncol, K, ttree_words,
+  CK(launch::range_trace_leaves(st, lde, ttree, logL, logB, (uint32_t)ncol, K, ttree_words,
                                 merkle_counter(c), tsteps, hio_dev<uint32_t>(c, h.trace_cap),
                                 tcap_stride, &tbuilt));
   if (tbuilt == 0)
     CK(launch::merkle_build(st, ttree, m, tsteps, merkle_counter(c),
                             hio_dev<uint32_t>(c, h.trace_cap), 0, K, ttree_words, tcap_stride));
-  CK(launch::coset_zinv(st, c->tb, zinv, zinv2, logB, to_mont(fpow(GENERATOR, N)), nullptr, slot));
+  if (r == 1) {
+    CK(launch::coset_zinv(st, c->tb, zinv, zinv2, logB, to_mont(fpow(GENERATOR, N)), nullptr, slot));
+  } else {  // 1/(x^n - 1) for coset j and q mod r, x = 31 omega_m^j omega_Lp^q
+    std::vector<uint32_t> zt(2 * B * r);
+    const uint32_t omega_m = two_adic_generator(logm), omega_l = two_adic_generator(logL);
+    for (uint64_t j = 0; j < B; j++)
+      for (uint64_t q = 0; q < r; q++) {
+        const uint32_t x = fmul(fmul(GENERATOR, fpow(omega_m, j)), fpow(omega_l, q));
+        const uint32_t zm = to_mont(finv(fsub(fpow(x, N), 1)));
+        zt[j * r + q] = zm;
+        zt[B * r + j * r + q] = to_mont(zm);  // times 2^64
+      }
+    CK(cudaMemcpyAsync(zinv, zt.data(), 8 * B * r, cudaMemcpyHostToDevice, st));
+    c->h2d += 8 * B * r;
+  }
   CK(sync(c, "cap"));
   if (host_cols && *reinterpret_cast<volatile unsigned int*>(c->hio + bad_at)) {
     set_reason("field elements must be canonical (< p)");
@@ -1902,7 +1956,8 @@ int range_prove_columns(z0p_gpu_ctx* c, const RangeTask* tasks, uint32_t K, cons
   ca.lde = lde; ca.zinv = zinv; ca.zinv2 = zinv2;
   ca.alphas = dalpha;
   ca.layer0 = fb.layer[0]; ca.leaves = fb.tree[0];
-  ca.logN = logN; ca.logB = logB; ca.n_bits = (uint32_t)p0.n_bits; ca.slot = slot;
+  ca.logN = logL; ca.logB = logB; ca.n_bits = (uint32_t)p0.n_bits; ca.slot = slot;
+  ca.r = (uint32_t)r;
   ca.layer_stride = fb.val_stride;
   ca.tree_stride = fb.tree_stride;
   CK(launch::range_compose_leaves(st, c->tb, ca, K));
@@ -1913,11 +1968,11 @@ int range_prove_columns(z0p_gpu_ctx* c, const RangeTask* tasks, uint32_t K, cons
   std::vector<Transcript*> ts(K);
   for (uint32_t k = 0; k < K; k++) ts[k] = tasks[k].ts;
   std::vector<FriOut> fo(K);
-  RC(run_fri(c, s, fp, fb, m, N - 1, ts.data(), K, h, fo.data()));
+  RC(run_fri(c, s, fp, fb, m, bound, ts.data(), K, h, fo.data()));
 
   OpenArgs oa{};  // src/range.rs:483-500
   oa.lde = lde; oa.ttree = ttree; oa.tleaves = m; oa.tsteps = tsteps;
-  oa.logN = logN; oa.logB = logB; oa.ncol = (uint32_t)ncol;
+  oa.logN = logL; oa.logB = logB; oa.ncol = (uint32_t)ncol;
   oa.lde_stride = m * ncol;
   oa.ttree_stride = ttree_words;
   RC(run_openings(c, s, fb, h, fo.data(), K, oa));
@@ -1928,7 +1983,7 @@ int range_prove_columns(z0p_gpu_ctx* c, const RangeTask* tasks, uint32_t K, cons
     w.byte(6);
     w.u32((uint32_t)(column_cap[k].size() / 32));
     w.bytes(column_cap[k].data(), column_cap[k].size());
-    write_fri(w, c, s, fo[k], m, N - 1, h, k);
+    write_fri(w, c, s, fo[k], m, bound, h, k);
     w.u32((uint32_t)fo[k].indices.size());
     for (size_t qi = 0; qi < fo[k].indices.size(); qi++) {
       uint64_t index = brev(fo[k].indices[qi], logm);
@@ -3082,6 +3137,52 @@ int z0p_gpu_range_prove(z0p_gpu_ctx* c, const z0p_range_params* p, z0p_transcrip
                         uint8_t* out, size_t cap, size_t* len) {
   if (!c || !p || !ts) return Z0P_ERR_INVALID_ARGUMENT;
   return prove_group_abi(c, 1, p, &ts, &out, &cap, len, range_prove);
+}
+
+int z0p_range_proof_size_zk(const z0p_range_params* p, size_t n_rand, size_t* len) {
+  if (!p || !len) return Z0P_ERR_INVALID_ARGUMENT;
+  FriParams fp;
+  FriShape s;
+  RC(range_zk_shape(*p, n_rand, &fp, &s));
+  *len = range_size(*p, s);
+  return Z0P_OK;
+}
+
+int z0p_gpu_range_prove_zk(z0p_gpu_ctx* c, const z0p_range_params* p, size_t n_rand,
+                           z0p_chacha20_state* rng, z0p_transcript_state* t, uint8_t* out,
+                           size_t cap, size_t* out_len) {
+  if (!c || !p || !t || !rng || rng->used > 64) return Z0P_ERR_INVALID_ARGUMENT;
+  FriParams fp;
+  FriShape s;
+  RC(range_zk_shape(*p, n_rand, &fp, &s));  // src/range.rs:399-404, then the shape
+  const uint64_t need = range_size(*p, s);
+  if (out_len) *out_len = need;
+  if (!out || cap < need) {
+    set_reason("output buffer too small for the proof");
+    return Z0P_ERR_BUFFER_TOO_SMALL;
+  }
+  // Masking values, column after column (value first), n_rand each
+  // (src/range.rs:411-414, src/blind.rs:65), on a copy of the stream.
+  const uint64_t ncol = p->n_bits + 1;
+  z0p_chacha20_state r = *rng;
+  std::vector<uint32_t> rand(ncol * n_rand);
+  for (auto& v : rand) v = chacha20_next_field(&r);
+  std::lock_guard<std::mutex> lk(c->mu);
+  c->work_serial++;
+  RC(with_device(c));
+  RC(ensure_slots(c, 1));
+  ProfileScope ps(c);
+  z0p_transcript_state work = *t;
+  Transcript tr(&work);
+  RangeTask task{p, &tr, out, cap, out_len};
+  c->last_sync_ns = now_ns();
+  const int rc = range_prove_columns(c, &task, 1, fp, s, need, nullptr, n_rand, rand.data());
+  c->last_sync_ns = 0;
+  if (rc != Z0P_OK) return rc;
+  *t = work;
+  *rng = r;
+  c->proofs++;
+  return Z0P_OK;
 }
 
 int z0p_gpu_range_prove_with_columns(z0p_gpu_ctx* c, const z0p_range_params* p,

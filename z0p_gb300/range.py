@@ -63,6 +63,17 @@ def prove(params: Params, transcript: Transcript, ctx=None) -> bytes:
     return bytes(buf)[: n.value]
 
 
+def prove_zk(params: Params, n_rand: int, rng, transcript: Transcript, ctx=None) -> bytes:
+    """range::prove_zk (src/range.rs:393-418): `rng` is a z0p_gb300.rng.ChaCha20."""
+    ctx = ctx or default_context()
+    n = C.c_size_t()
+    check(lib().z0p_range_proof_size_zk(C.byref(params), n_rand, C.byref(n)))
+    out = (C.c_uint8 * n.value)()
+    check(lib().z0p_gpu_range_prove_zk(ctx.handle, C.byref(params), n_rand, C.byref(rng),
+                                       C.byref(transcript.state), out, n.value, C.byref(n)))
+    return bytes(out)[: n.value]
+
+
 def prove_with_columns(params: Params, v_col, bit_cols, transcript: Transcript, ctx=None) -> bytes:
     """range::prove_with_columns (src/range.rs:353-375): the caller's value
     column and n_bits bit columns, proved row by row on the device."""
