@@ -379,8 +379,9 @@ def run_scale(Z, ctx, reps=5):
     """The other prove entry points at 2^20 rows, production schedule
     (for_security(100)): range::prove (16-bit, value 12,345; the batched and
     served mixes use the same shape at smaller n) and the same columns
-    through range::prove_with_columns (row by row), table::prove_zk and
-    air::prove_zk with n_rand = 16 * num_queries (src/air.rs:445-458; padded
+    through range::prove_with_columns (row by row), range::prove_zk
+    (n_rand = num_queries), table::prove_zk and air::prove_zk with
+    n_rand = 16 * num_queries (src/air.rs:445-458; padded
     trace 2^21, LDE 2^25, final layer 32), and air::prove_with_trace on host
     columns."""
     import numpy as np
@@ -404,6 +405,8 @@ def run_scale(Z, ctx, reps=5):
     rv = np.full(n, 12345, np.uint32)
     rbits = [np.full(n, (12345 >> c) & 1, np.uint32) for c in range(16)]
     table = [10, 20, 30, 12345]
+    range_zk_p = Z.range.Params.new(n, 16, 16, air_p.num_queries, 32, 12345) \
+        .with_grinding_bits(air_p.grinding_bits).with_cap_height(air_p.cap_height)
     table_p = Z.table.Params.new(n, 16, air_p.num_queries, 32, 12345) \
         .with_grinding_bits(air_p.grinding_bits).with_cap_height(air_p.cap_height)
     cases = [
@@ -416,6 +419,9 @@ def run_scale(Z, ctx, reps=5):
         ("air::prove_zk, 2^20 steps, n_rand %d" % n_rand, n,
          lambda: Z.air.prove_zk(zk_p, n_rand, Z.rng.ChaCha20.new(bytes(32), bytes(12)),
                                 Z.Transcript(b"bench/air-zk"), ctx)),
+        ("range::prove_zk 16-bit, 2^20 rows, n_rand %d (LDE 2^25, final 32)" % air_p.num_queries, n,
+         lambda: Z.range.prove_zk(range_zk_p, air_p.num_queries, Z.rng.ChaCha20.new(bytes(32), bytes(12)),
+                                  Z.Transcript(b"bench/range-zk"), ctx)),
         ("air::prove_with_trace, 2^20 steps (host columns)", n,
          lambda: Z.air.prove_with_trace(air_p, ca, cb, Z.Transcript(b"bench/air-scale"), ctx)),
     ]
