@@ -116,7 +116,8 @@ __global__ void fill_columns_kernel(uint32_t* cols, uint32_t n, uint32_t ncols,
 struct NttArgs {
   uint32_t logn, inverse, in_div, twist_mod, twist_shift, post_gamma, ninv_m;
   Tables tb;
-  unsigned int* bad;  // see NttPlan::bad
+  unsigned int* bad;    // see NttPlan::bad
+  uint32_t pre_gamma;   // see NttPlan::pre_gamma
 };
 
 __device__ __forceinline__ uint32_t spos(uint32_t i) { return i + (i >> 5); }
@@ -224,6 +225,7 @@ __global__ void __launch_bounds__(512) ntt_small_kernel(const uint32_t* __restri
   for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
     uint32_t v = src[i];
     if (a.bad && v >= kP) atomicOr(a.bad, 1u);
+    if (a.pre_gamma) v = mmul(v < kP ? v : 0u, gamma_pow(a.tb, i));
     if (j) {
       v = mmul(v, tw_cur);
       tw_cur = mmul(tw_cur, tw_step);
@@ -285,6 +287,7 @@ __global__ void __launch_bounds__(512) ntt_pass1_kernel(const uint32_t* __restri
     const uint32_t i1 = e >> LOGC, c = e & (C - 1);
     uint32_t v = src[(i1 << logn2) + c0 + c];
     if (a.bad && v >= kP) atomicOr(a.bad, 1u);
+    if (a.pre_gamma) v = mmul(v < kP ? v : 0u, gamma_pow(a.tb, (i1 << logn2) + c0 + c));
     if (j) v = mmul(v, twist[i1]);
     s[c * cstride + spos(i1)] = v;
   }
@@ -1754,7 +1757,8 @@ cudaError_t ntt(cudaStream_t st, const Tables& tb, const NttPlan& plan, const ui
   a.twist_mod = plan.twist_mod ? plan.twist_mod : 1;
   a.twist_shift = plan.twist_shift;
   a.post_gamma = plan.post_gamma;
-  a.bad = plan.in_div > 1 ? nullptr : plan.bad;  // each input word loaded once
+  a.bad = plan.bad;  // with in_div > 1 a word is checked once per reader: the flag is idempotent
+  a.pre_gamma = plan.pre_gamma;
   // n^-1 in Montgomery form: (2^-logn) * 2^32 mod p.
   {
     uint64_t inv2 = (kP + 1) / 2;  // 2^-1 mod p

@@ -36,6 +36,9 @@ struct NttPlan {
   // Non-null: every input word is checked on load, and a value >= p sets
   // *bad (a caller's columns; the C boundary takes canonical elements).
   unsigned int* bad = nullptr;
+  // Nonzero: input i is multiplied by 31^i on load (coefficients of
+  // fri::commit, src/ntt.rs:353-358); non-canonical inputs read as 0.
+  uint32_t pre_gamma = 0;
 };
 
 // Column B of the Fibonacci trace is never transformed: on the LDE,

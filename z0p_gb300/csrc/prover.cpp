@@ -2114,14 +2114,20 @@ int fri_commit(z0p_gpu_ctx* c, const FriInput& in, const uint32_t* values,
   if (!in.evals) {
     uint32_t* coeffs = (uint32_t*)c->coeffs.p;
     uint32_t* lde = (uint32_t*)c->lde.p;
-    CK(launch::gamma_scale(st, c->tb, src, coeffs, (uint32_t)in.n, in.ext ? 1u : 0u, bad));
     NttPlan lp;
     lp.logn = logn;
     lp.batch = ncomp << logB;
     lp.in_div = 1u << logB;
     lp.twist_mod = 1u << logB;
     lp.twist_shift = 27 - logm;
-    CK(launch::ntt(st, c->tb, lp, coeffs, lde, (uint32_t*)c->scratch.p));
+    if (in.ext) {  // de-interleave the Ext4 coordinates, scaled by 31^i
+      CK(launch::gamma_scale(st, c->tb, src, coeffs, (uint32_t)in.n, 1u, bad));
+      CK(launch::ntt(st, c->tb, lp, coeffs, lde, (uint32_t*)c->scratch.p));
+    } else {  // base coefficients: the transform scales and checks them as it loads
+      lp.pre_gamma = 1;
+      lp.bad = bad;
+      CK(launch::ntt(st, c->tb, lp, src, lde, (uint32_t*)c->scratch.p));
+    }
   }
   // Small layer-0 trees are finished inside the leaf launch.
   const uint32_t top0 = s.depth[0] - s.drop[0];
