@@ -192,8 +192,9 @@ typedef struct {
 int z0p_gpu_ctx_stats(z0p_gpu_ctx *ctx, z0p_gpu_stats *out);
 /* Diagnostic per-stage timing: while on, every kernel stage is bracketed by
  * CUDA events on the context stream. z0p_gpu_ctx_profile writes a JSON
- * object {"stage": {"ms": total, "calls": n}, ...} covering the stages since
- * the previous call, then clears it. Profiling uses a process-wide hook, so
+ * object {"stage": {"ms": total, "calls": n, "kernels": k}, ...} covering
+ * the stages since the previous call (calls: bracketed stage calls; kernels:
+ * kernel launches inside them), then clears it. Profiling uses a process-wide hook, so
  * only one context should profile at a time. */
 int z0p_gpu_ctx_set_profiling(z0p_gpu_ctx *ctx, int on);
 int z0p_gpu_ctx_profile(z0p_gpu_ctx *ctx, char *json, size_t cap, size_t *len);
@@ -439,11 +440,15 @@ int z0p_gpu_rs_extend(z0p_gpu_ctx *ctx, const uint32_t *d_values, uint64_t n, ui
  * Its working memory is static device arrays inside this library: 12 MiB of
  * scratch plus 240 KiB of power tables, held on every device that loads the
  * library until the process exits.
- * - Limit: n * batch * blowup <= 1048576 output elements, and
- *   batch * blowup <= 65535. Larger sizes return Z0P_ERR_UNSUPPORTED.
+ * - Limit: n * batch * blowup <= 1048576 output elements; larger sizes
+ *   return Z0P_ERR_UNSUPPORTED. The other checks and their codes are
+ *   z0p_gpu_rs_extend's (batch * blowup > 65535 is
+ *   Z0P_ERR_INVALID_DOMAIN_SIZE there and here).
  * - Set-up: the first call on a device, with that device current, resolves
- *   the arrays' device addresses and uploads the tables through the legacy
- *   default stream. Make that first call before any stream capture.
+ *   the arrays' device addresses, uploads the tables through the legacy
+ *   default stream and waits for that upload, so the first call's work is
+ *   correct on any stream, non-blocking ones included. Make that first call
+ *   before any stream capture.
  * - Semantics: the same output as z0p_gpu_rs_extend. The work is enqueued on
  *   `stream` (NULL = legacy default stream) and the call returns without
  *   waiting.
@@ -452,6 +457,20 @@ int z0p_gpu_rs_extend(z0p_gpu_ctx *ctx, const uint32_t *d_values, uint64_t n, ui
  */
 int z0p_gpu_rs_extend_noalloc(const uint32_t *d_values, uint64_t n, uint64_t batch,
                               uint64_t blowup, uint32_t *d_out, void *stream);
+/*
+ * air::compose (src/air.rs:847-929) as one device stage, the composition
+ * evaluation of z0p_gpu_air_prove with the caller's alphas in place of the
+ * transcript's "fib/alpha" draws: the Fibonacci trace of *p (n_steps, a0, b0;
+ * b_last enters the boundary term), its LDE at p->blowup and the composition
+ * (src/air.rs:938-962 value by value). alphas: 5 Ext4 as 20 canonical words
+ * (non-canonical: Z0P_ERR_MALFORMED_INPUT). d_out (device, 4 * m words for
+ * m = n_steps * blowup) receives FRI layer 0: position P holds the value at
+ * LDE row brev_{log m}(P), the point 31 * omega_m^row (src/fri.rs:584-586).
+ * Parameter checks are z0p_gpu_air_prove's. Runs on the context stream and
+ * synchronises before returning.
+ */
+int z0p_gpu_air_compose(z0p_gpu_ctx *ctx, const z0p_air_params *p, const uint32_t alphas[20],
+                        uint32_t *d_out);
 /*
  * MerkleTree::from_flat64 (src/merkle.rs:93-110) + cap (src/merkle.rs:229-232):
  * builds the BLAKE3 tree over len/64 64-byte leaves of the device buffer

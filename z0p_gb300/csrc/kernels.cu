@@ -1644,7 +1644,10 @@ struct Stage {
   ~Stage() {
     if (g_recorder) g_recorder->end(name, st);
   }
-  void launched(int k = 1) { g_launches += k; }
+  void launched(int k = 1) {
+    g_launches += k;
+    if (g_recorder) g_recorder->launched(name, k);
+  }
 };
 
 cudaError_t const_slot_address(int slot, void** ptr) {
@@ -1686,23 +1689,32 @@ uint32_t subtree_levels(uint32_t nt, uint32_t top) {
   return l;
 }
 
-// True when the pass-`pass` kernel for half-length 2^L has already been
-// allowed `smem` bytes of dynamic shared memory in this process (each kernel's
-// need is fixed by L, so the attribute is set once per kernel, not per launch).
-bool smem_raised(int pass, uint32_t L, size_t smem) {
-  static std::mutex mu;
-  static size_t done[6][32] = {};
-  std::lock_guard<std::mutex> lk(mu);
-  if (done[pass][L] >= smem) return true;
-  done[pass][L] = smem;
-  return false;
-}
-
 // ------------------------------------------------------------ schedule ----
 namespace {
 constexpr int kMaxDevices = 64;
 std::mutex g_sched_mu;
 Schedule g_sched[kMaxDevices];
+
+// Allows the pass-`pass` kernel `func` for half-length 2^L `smem` bytes of
+// dynamic shared memory on the current device. Each kernel's need is fixed by
+// L, so the attribute is set once per kernel and device, not per launch.
+// cudaFuncSetAttribute acts on the current device only, so what has been
+// raised is recorded per device, and only after the call has succeeded (a
+// failed raise is returned and retried on the next launch).
+template <typename K>
+cudaError_t raise_smem(K* func, int pass, uint32_t L, size_t smem) {
+  static std::mutex mu;
+  static size_t done[kMaxDevices][6][32] = {};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lk(mu);
+  if (done[dev][pass][L] >= smem) return cudaSuccess;
+  e = cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e == cudaSuccess) done[dev][pass][L] = smem;
+  return e;
+}
 
 Schedule current_schedule() {
   int dev = 0;
@@ -1808,9 +1820,8 @@ cudaError_t ntt(cudaStream_t st, const Tables& tb, const NttPlan& plan, const ui
   stg.launched(2);
   switch (logn1) {
 #define Z0P_P1K(Lv, LC, KM)                                                                      \
-    if (!smem_raised(1 + slot, Lv, smem1))                                                       \
-      cudaFuncSetAttribute(ntt_pass1_kernel<Lv, LC, KM>,                                         \
-                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1);             \
+    if (cudaError_t re = raise_smem(ntt_pass1_kernel<Lv, LC, KM>, 1 + slot, Lv, smem1))          \
+      return re;                                                                                 \
     ntt_pass1_kernel<Lv, LC, KM><<<g1, threads, smem1, st>>>(in, scratch, a);
 #define Z0P_P1(Lv, LC)                                                                           \
   case Lv:                                                                                       \
@@ -1825,9 +1836,8 @@ cudaError_t ntt(cudaStream_t st, const Tables& tb, const NttPlan& plan, const ui
   if (e != cudaSuccess) return e;
   switch (logn2) {
 #define Z0P_P2K(Lv, LR, KM)                                                                      \
-    if (!smem_raised(2 + slot, Lv, smem2))                                                       \
-      cudaFuncSetAttribute(ntt_pass2_kernel<Lv, LR, KM>,                                         \
-                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2);             \
+    if (cudaError_t re = raise_smem(ntt_pass2_kernel<Lv, LR, KM>, 2 + slot, Lv, smem2))          \
+      return re;                                                                                 \
     ntt_pass2_kernel<Lv, LR, KM><<<g2, threads, smem2, st>>>(scratch, out, a);
 #define Z0P_P2(Lv, LR)                                                                           \
   case Lv:                                                                                       \
@@ -2230,7 +2240,8 @@ NoAllocDevice g_noalloc_dev[64];
 
 // Once per device, with that device current: resolve the device addresses of
 // the static arrays (host code cannot use their names as pointers) and fill
-// the power tables. The copy goes through the legacy default stream.
+// the power tables. The copy goes through the legacy default stream, and the
+// set-up waits for it to finish before any call uses the tables.
 int noalloc_setup(int dev, NoAllocDevice** out) {
   std::lock_guard<std::mutex> lk(g_noalloc_mu);
   NoAllocDevice& d = g_noalloc_dev[dev];
@@ -2266,6 +2277,10 @@ int noalloc_setup(int dev, NoAllocDevice** out) {
     x = 1;
     for (uint32_t i = 0; i < (1u << 15); i++) { g_hi[i] = to_mont(x); x = fmul(x, gstep); }
     e = cudaMemcpyToSymbol(g_noalloc_tables, t.data(), t.size() * sizeof(uint32_t));
+    // A copy from pageable memory may return before its DMA has landed, and a
+    // caller's non-blocking stream is not ordered after the legacy stream: wait
+    // for the tables here, before any call can enqueue work that reads them.
+    if (e == cudaSuccess) e = cudaStreamSynchronize(0);
     if (e != cudaSuccess) {
       z0p::host::set_reason(std::string("cudaMemcpyToSymbol(tables): ") + cudaGetErrorString(e));
       return Z0P_ERR_CUDA;
@@ -2281,14 +2296,19 @@ int noalloc_setup(int dev, NoAllocDevice** out) {
 extern "C" int z0p_gpu_rs_extend_noalloc(const uint32_t* d_values, uint64_t n, uint64_t batch,
                                          uint64_t blowup, uint32_t* d_out, void* stream) {
   using namespace z0p;
-  if (!d_values || !d_out || batch == 0) return Z0P_ERR_INVALID_ARGUMENT;
+  // The argument, domain and blowup checks are z0p_gpu_rs_extend's, with its codes.
+  if (!d_values || !d_out || batch == 0 || batch > 65535) return Z0P_ERR_INVALID_ARGUMENT;
   if (!host::is_pow2(n) || n > host::MAX_DOMAIN) return Z0P_ERR_INVALID_DOMAIN_SIZE;
   if (!host::is_pow2(blowup)) return Z0P_ERR_INVALID_BLOWUP;
-  if (n * blowup > host::MAX_DOMAIN) return Z0P_ERR_INVALID_DOMAIN_SIZE;
-  if (batch > kNoAllocMaxElems || n * blowup > kNoAllocMaxElems ||
-      n * batch * blowup > kNoAllocMaxElems || batch * blowup > 65535) {
+  if (n * blowup > host::MAX_DOMAIN || batch * blowup > 65535) {
+    host::set_reason("z0p_gpu_rs_extend_noalloc: batch * blowup exceeds the 65535 transforms "
+                     "of one launch, or n * blowup exceeds the largest domain");
+    return Z0P_ERR_INVALID_DOMAIN_SIZE;
+  }
+  // Only this limit is particular to the static scratch.
+  if (n * blowup > kNoAllocMaxElems || n * batch * blowup > kNoAllocMaxElems) {
     host::set_reason("z0p_gpu_rs_extend_noalloc: n * batch * blowup exceeds the static scratch "
-                     "limit of 1048576 elements");
+                     "limit of 1048576 output elements");
     return Z0P_ERR_UNSUPPORTED;
   }
   int dev = 0;
