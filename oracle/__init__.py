@@ -171,6 +171,9 @@ def lib():
             "zo_air_build_trace": (None, [C.c_uint32, C.c_uint32, sz, u32p, u32p]),
             "zo_air_prove": (C.c_int, [C.POINTER(AirParams), vp, C.POINTER(u8p), C.POINTER(sz)]),
             "zo_air_prove_with_trace": (C.c_int, [C.POINTER(AirParams), u32p, u32p, vp, C.POINTER(u8p), C.POINTER(sz)]),
+            "zo_air_compose": (C.c_int, [u32p, u32p, u32p, sz, C.c_uint32, C.c_uint32, C.c_uint32,
+                                         C.c_uint32, sz, sz, u32p, u32p]),
+            "zo_air_composition_at": (None, [C.c_uint32] * 7 + [C.c_uint32, C.c_uint32, sz, u32p, u32p]),
             "zo_air_verify": (C.c_int, [C.POINTER(AirParams), C.c_char_p, sz, vp]),
             "zo_range_params_new": (C.c_int, [C.c_uint64] * 5 + [C.c_uint32, C.POINTER(RangeParams)]),
             "zo_range_for_security": (C.c_int, [C.c_uint64, C.c_uint64, C.c_uint32, C.c_uint32, C.POINTER(RangeParams)]),
@@ -273,6 +276,15 @@ def f_inv(a):
 
 def f_pow(a, e):
     return lib().zo_f_pow(a, e)
+
+
+def e_mul(x, y):
+    """ext4.rs:106-117 product of two Ext4 given as 4 coordinates."""
+    a = (C.c_uint32 * 4)(*x)
+    b = (C.c_uint32 * 4)(*y)
+    out = (C.c_uint32 * 4)()
+    lib().zo_e_mul(a, b, out)
+    return list(out)
 
 
 class Transcript:
@@ -647,6 +659,32 @@ def fold_layer(values, first_points, challenges):
     lib().zo_fold_layer(vp, n, fpp, chp, out.ctypes.data_as(C.POINTER(C.c_uint32)),
                         outp.ctypes.data_as(C.POINTER(C.c_uint32)))
     return out, outp[: n // 16]
+
+
+def air_compose(col_a, col_b, points, w_last, a0, b0, b_last, n, offset, alphas):
+    """air::compose over caller points; alphas (5, 4); returns (m, 4) uint32."""
+    import numpy as np
+
+    a, ap = u32arr(col_a)
+    b, bp = u32arr(col_b)
+    pt, ptp = u32arr(points)
+    al, alp = u32arr(np.asarray(alphas).reshape(-1))
+    out = np.zeros((len(a), 4), dtype=np.uint32)
+    rc = lib().zo_air_compose(ap, bp, ptp, len(a), w_last, a0, b0, b_last, n, offset, alp,
+                              out.ctypes.data_as(C.POINTER(C.c_uint32)))
+    if rc:
+        raise ValueError(ERRORS[rc])
+    return out
+
+
+def air_composition_at(a, b, an, bn, x, w_last, a0, b0, b_last, n, alphas):
+    import numpy as np
+
+    al, alp = u32arr(np.asarray(alphas).reshape(-1))
+    out = np.zeros(4, dtype=np.uint32)
+    lib().zo_air_composition_at(a, b, an, bn, x, w_last, a0, b0, b_last, n, alp,
+                                out.ctypes.data_as(C.POINTER(C.c_uint32)))
+    return out
 
 
 def set_max_workers(n: int):

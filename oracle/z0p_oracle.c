@@ -1895,6 +1895,50 @@ static ext4 air_composition_at(uint32_t a, uint32_t b, uint32_t an, uint32_t bn,
     return e_add(acc, e_mul_base(alpha[4], bo));
 }
 
+/* air.rs:847-929 compose over caller-chosen points, as the reference's own
+ * batched-vs-scalar test calls it (air.rs:1155-1242): LDE points and the unit
+ * domain, whose singular rows map zero denominators to zero. Fewer than two
+ * points take the scalar fallback (air.rs:863-882). */
+int zo_air_compose(const uint32_t *ca, const uint32_t *cb, const uint32_t *pts, size_t m,
+                   uint32_t w_last, uint32_t a0, uint32_t b0, uint32_t b_last, size_t n,
+                   size_t offset, const uint32_t *alphas, uint32_t *out) {
+    ext4 alpha[5];
+    for (int k = 0; k < 5; k++)
+        for (int e = 0; e < 4; e++) alpha[k].c[e] = alphas[4 * k + e];
+    if (m < 2) {
+        zo_air_params p = {0};
+        p.a0 = a0; p.b0 = b0; p.b_last = b_last;
+        for (size_t i = 0; i < m; i++) {
+            size_t nx = (i + offset) % m;
+            ext4 v = air_composition_at(ca[i], cb[i], ca[nx], cb[nx], pts[i], w_last, &p, n, alpha);
+            memcpy(out + 4 * i, v.c, 16);
+        }
+        return ZO_OK;
+    }
+    compose_ctx c;
+    c.ca = ca; c.cb = cb; c.pts = pts; c.m = m; c.offset = offset;
+    c.w_last = w_last; c.a0 = a0; c.b0 = b0; c.b_last = b_last;
+    c.p0 = f_pow(pts[0], n);
+    c.ratio = f_pow(f_mul(pts[1], f_inv(pts[0])), n);
+    c.alpha = alpha;
+    c.out = (ext4 *)out;
+    for_each_indexed(m, 2048, compose_worker, &c);
+    return ZO_OK;
+}
+
+/* air.rs:938-962 composition_at at one point */
+void zo_air_composition_at(uint32_t a, uint32_t b, uint32_t an, uint32_t bn, uint32_t x,
+                           uint32_t w_last, uint32_t a0, uint32_t b0, uint32_t b_last, size_t n,
+                           const uint32_t *alphas, uint32_t *out) {
+    ext4 alpha[5];
+    for (int k = 0; k < 5; k++)
+        for (int e = 0; e < 4; e++) alpha[k].c[e] = alphas[4 * k + e];
+    zo_air_params p = {0};
+    p.a0 = a0; p.b0 = b0; p.b_last = b_last;
+    ext4 v = air_composition_at(a, b, an, bn, x, w_last, &p, n, alpha);
+    memcpy(out, v.c, 16);
+}
+
 /* air.rs:485-599 prove_inner; lde_b given (from linked_lde or a second NTT) */
 static int air_prove_inner(const zo_air_params *params, uint32_t *lde_a, uint32_t *lde_b,
                            size_t m, size_t degree_bound, zo_transcript *t, uint8_t **proof,

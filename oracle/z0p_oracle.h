@@ -123,6 +123,14 @@ int zo_air_prove_with_trace(const zo_air_params *params, const uint32_t *col_a,
                             size_t *proof_len);
 int zo_air_verify(const zo_air_params *params, const uint8_t *proof, size_t proof_len,
                   zo_transcript *t);
+/* air::compose over caller-chosen points (alphas: 5 Ext4 as 20 words; out:
+ * m Ext4) and air::composition_at at one point (out: 4 words). */
+int zo_air_compose(const uint32_t *ca, const uint32_t *cb, const uint32_t *pts, size_t m,
+                   uint32_t w_last, uint32_t a0, uint32_t b0, uint32_t b_last, size_t n,
+                   size_t offset, const uint32_t *alphas, uint32_t *out);
+void zo_air_composition_at(uint32_t a, uint32_t b, uint32_t an, uint32_t bn, uint32_t x,
+                           uint32_t w_last, uint32_t a0, uint32_t b0, uint32_t b_last, size_t n,
+                           const uint32_t *alphas, uint32_t *out);
 
 /* Range AIR (src/range.rs) */
 typedef struct {

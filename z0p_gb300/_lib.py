@@ -192,6 +192,7 @@ def lib():
             "z0p_gpu_range_prove_group": (C.c_int, [vp, sz, P(RangeParams), P(P(TranscriptState)),
                                                     P(u8p), P(sz), P(sz)]),
             "z0p_gpu_rs_extend": (C.c_int, [vp, vp, C.c_uint64, C.c_uint64, C.c_uint64, vp]),
+            "z0p_gpu_air_compose": (C.c_int, [vp, P(AirParams), u32p, vp]),
             "z0p_gpu_rs_extend_noalloc": (C.c_int, [vp, C.c_uint64, C.c_uint64, C.c_uint64, vp, vp]),
             "z0p_gpu_pool_create": (C.c_int, [C.c_int, C.c_int, sz, P(vp)]),
             "z0p_gpu_pool_destroy": (None, [vp]),

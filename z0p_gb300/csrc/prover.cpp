@@ -89,6 +89,7 @@ struct EventRecorder final : launch::StageRecorder {
   struct Mark {
     std::string stage;
     cudaEvent_t a, b;
+    uint64_t kernels = 0;
   };
   std::vector<Mark> marks;
   std::vector<cudaEvent_t> pool;
@@ -111,6 +112,13 @@ struct EventRecorder final : launch::StageRecorder {
     for (size_t i = marks.size(); i-- > 0;)
       if (marks[i].stage == stage) {
         cudaEventRecord(marks[i].b, st);
+        return;
+      }
+  }
+  void launched(const char* stage, int kernels) override {
+    for (size_t i = marks.size(); i-- > 0;)
+      if (marks[i].stage == stage) {
+        marks[i].kernels += (uint64_t)kernels;
         return;
       }
   }
@@ -777,6 +785,11 @@ struct Task {
   uint8_t* out;
   size_t cap;
   size_t* len;
+  // Composition stage only (z0p_gpu_air_compose): alphas chosen by the
+  // caller instead of drawn, and FRI layer 0 copied to this device buffer
+  // before the call returns, with no FRI, openings or proof bytes.
+  const uint32_t* fixed_alpha = nullptr;
+  uint32_t* layer0_out = nullptr;
 };
 using AirTask = Task<z0p_air_params>;
 using RangeTask = Task<z0p_range_params>;
@@ -1654,6 +1667,9 @@ int air_prove(z0p_gpu_ctx* c, const AirTask* tasks, uint32_t K) {
     transcript_absorb(*tasks[k].ts, "fib/trace", cap, h.trace_cap_bytes);
     uint32_t alpha[5][4];
     for (int i = 0; i < 5; i++) challenge_ext(*tasks[k].ts, "fib/alpha", alpha[i]);
+    if (tasks[k].fixed_alpha)
+      for (int i = 0; i < 5; i++)
+        for (int e = 0; e < 4; e++) alpha[i][e] = tasks[k].fixed_alpha[4 * i + e];
     ProofConsts& pc = c->consts[k];
     const uint32_t neg_coeff = fsub(0, coeff[k]);
     for (int e = 0; e < 4; e++) {
@@ -1686,6 +1702,11 @@ int air_prove(z0p_gpu_ctx* c, const AirTask* tasks, uint32_t K) {
     CK(launch::merkle_build(st, fb.tree[0], s.leaves[0], s.depth[0] - s.drop[0], merkle_counter(c),
                             hio_dev<uint32_t>(c, h.fri_cap[0]), 0, K, fb.tree_stride,
                             h.fri_cap_bytes[0] / 4));
+  if (tasks[0].layer0_out) {  // composition stage: layer 0 out, nothing further
+    CK(cudaMemcpyAsync(tasks[0].layer0_out, fb.layer[0], 16 * m, cudaMemcpyDeviceToDevice, st));
+    CK(sync(c));
+    return Z0P_OK;
+  }
 
   std::vector<Transcript*> ts(K);
   for (uint32_t k = 0; k < K; k++) ts[k] = tasks[k].ts;
@@ -3069,6 +3090,30 @@ int z0p_gpu_air_prove(z0p_gpu_ctx* c, const z0p_air_params* p, z0p_transcript_st
   return prove_group_abi(c, 1, p, &ts, &out, &cap, len, air_prove);
 }
 
+int z0p_gpu_air_compose(z0p_gpu_ctx* c, const z0p_air_params* p, const uint32_t* alphas,
+                        uint32_t* d_out) {
+  if (!c || !p || !alphas || !d_out) return Z0P_ERR_INVALID_ARGUMENT;
+  for (int i = 0; i < 20; i++)
+    if (alphas[i] >= P) {
+      set_reason("alphas must be canonical field elements");
+      return Z0P_ERR_MALFORMED_INPUT;
+    }
+  size_t need = 0;
+  RC(z0p_air_proof_size(p, &need));
+  std::vector<uint8_t> unused(need);
+  z0p_transcript_state work;
+  RC(z0p_transcript_init(&work, (const uint8_t*)"compose", 7));
+  std::lock_guard<std::mutex> lk(c->mu);
+  c->work_serial++;
+  RC(with_device(c));
+  RC(ensure_slots(c, 1));
+  Transcript tr(&work);
+  AirTask task{p, &tr, unused.data(), need, nullptr};
+  task.fixed_alpha = alphas;
+  task.layer0_out = d_out;
+  return air_prove(c, &task, 1);
+}
+
 int z0p_gpu_air_prove_group(z0p_gpu_ctx* c, size_t n, const z0p_air_params* params,
                             z0p_transcript_state* const* transcripts, uint8_t* const* outs,
                             const size_t* caps, size_t* lens) {
@@ -3095,21 +3140,28 @@ int z0p_gpu_ctx_profile(z0p_gpu_ctx* c, char* json, size_t cap, size_t* len) {
   std::lock_guard<std::mutex> lk(c->mu);
   RC(with_device(c));
   CK(sync(c));
-  std::vector<std::pair<std::string, std::pair<double, uint64_t>>> agg;
+  struct Agg {
+    std::string stage;
+    double ms = 0;
+    uint64_t calls = 0, kernels = 0;
+  };
+  std::vector<Agg> agg;
   for (auto& m : c->rec.marks) {
     float ms = 0.f;
     if (cudaEventElapsedTime(&ms, m.a, m.b) != cudaSuccess) ms = 0.f;
     size_t i = 0;
-    while (i < agg.size() && agg[i].first != m.stage) i++;
-    if (i == agg.size()) agg.push_back({m.stage, {0.0, 0}});
-    agg[i].second.first += ms;
-    agg[i].second.second += 1;
+    while (i < agg.size() && agg[i].stage != m.stage) i++;
+    if (i == agg.size()) agg.push_back({m.stage});
+    agg[i].ms += ms;
+    agg[i].calls += 1;
+    agg[i].kernels += m.kernels;
   }
   std::string s = "{";
   for (size_t i = 0; i < agg.size(); i++) {
-    char buf[160];
-    snprintf(buf, sizeof buf, "%s\"%s\": {\"ms\": %.6f, \"calls\": %llu}", i ? ", " : "",
-             agg[i].first.c_str(), agg[i].second.first, (unsigned long long)agg[i].second.second);
+    char buf[200];
+    snprintf(buf, sizeof buf, "%s\"%s\": {\"ms\": %.6f, \"calls\": %llu, \"kernels\": %llu}",
+             i ? ", " : "", agg[i].stage.c_str(), agg[i].ms, (unsigned long long)agg[i].calls,
+             (unsigned long long)agg[i].kernels);
     s += buf;
   }
   s += agg.empty() ? "\"host\": {" : ", \"host\": {";
@@ -3250,6 +3302,7 @@ int z0p_gpu_rs_extend(z0p_gpu_ctx* c, const uint32_t* d_values, uint64_t n, uint
   std::lock_guard<std::mutex> lk(c->mu);
   c->work_serial++;
   RC(with_device(c));
+  ProfileScope ps(c);
   uint32_t logn = log2u(n), logm = logn + log2u(blowup);
   RC(ensure(c, c->coeffs, 4 * n * batch));
   RC(ensure(c, c->scratch, 4 * n * batch * blowup));
@@ -3281,6 +3334,7 @@ int z0p_gpu_merkle_flat64_cap(z0p_gpu_ctx* c, const uint8_t* d_flat, uint64_t le
   std::lock_guard<std::mutex> lk(c->mu);
   c->work_serial++;
   RC(with_device(c));
+  ProfileScope ps(c);
   RC(ensure(c, c->ttree, 32 * tree_digests(leaves)));
   uint32_t* tree = (uint32_t*)c->ttree.p;
   uint32_t depth = log2u(leaves), drop = cap_height < depth ? (uint32_t)cap_height : depth;
@@ -3303,6 +3357,7 @@ int z0p_gpu_fri_fold(z0p_gpu_ctx* c, const uint32_t* d_in, uint64_t n, uint64_t 
   std::lock_guard<std::mutex> lk(c->mu);
   c->work_serial++;
   RC(with_device(c));
+  ProfileScope ps(c);
   RC(ensure(c, c->ftrees, 32 * (n / 4 + 4)));
   FoldArgs fa;
   fa.in = d_in;
@@ -3620,6 +3675,7 @@ int z0p_gpu_grind(z0p_gpu_ctx* c, const uint8_t* head, size_t head_len, uint32_t
   std::lock_guard<std::mutex> lk(c->mu);
   c->work_serial++;
   RC(with_device(c));
+  ProfileScope ps(c);
   RC(ensure_hio(c, 16));
   set_head(c->consts, head, head_len);
   CK(push_consts(c, 1));
