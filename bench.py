@@ -36,6 +36,13 @@ LABEL = b"bench/air-scale"
 METRIC = "proved AIR steps/s (batched vs plain, byte-exact proofs); p50/p99 prove latency"
 
 
+def bench_config():
+    """The workload's config, identical in the GB300 and reference lines."""
+    return {"workload": "fibonacci-air prove, 2^20 steps, for_security(100): B16 Q40 G20 C4 F16",
+            "n_steps": N_STEPS, "lde_len": N_STEPS * 16, "proof_bytes": 203553,
+            "l2": "inputs larger than L2: per-proof working set ~0.9 GB > 129 MB L2"}
+
+
 def splitmix64(state):
     state = (state + 0x9E3779B97F4A7C15) & (2**64 - 1)
     z = state
@@ -150,6 +157,12 @@ def measured_traffic():
             return json.load(f)["stages"]
     except (OSError, KeyError, ValueError):
         return {}
+
+
+def measured_alu():
+    """Per-stage ALU-pipe % of the dominant kernel from the same committed
+    ncu captures, or {}."""
+    return {k: v["alu_pipe_pct"] for k, v in measured_traffic().items() if "alu_pipe_pct" in v}
 
 
 def stage_work(n, params):
@@ -472,16 +485,31 @@ def sweep_columns():
     return cols
 
 
+def device_seconds(ctx, fn):
+    """Device time of the kernel stages fn runs on ctx's stream: the
+    library's CUDA events around every stage (profiling mode), summed."""
+    ctx.set_profiling(True)
+    try:
+        fn()
+        prof = ctx.profile()
+    finally:
+        ctx.set_profiling(False)
+    prof.pop("host", None)
+    return sum(v["ms"] for v in prof.values()) / 1e3
+
+
 def run_sweep(Z, ctx):
     """The kernel-sweep configuration at full size: per equal-n group, the
     coset LDE at blowup 16 (reed_solomon_extend, ntt.rs:436-439), a Merkle
     cap over the group's row-major flat buffer (from_flat64, merkle.rs:93-110)
     and, per column, the arity-4 fold chain (fri.rs:1273-1331) on the LDE
     lifted to Fp4 and bit-reversed, with seeded challenges, while the degree
-    bound (n - 1) >> 2f is at least 8. Device inputs; every call is
-    synchronous, timed by the host clock after an untimed call of the same
-    size (which sizes the workspace); layouts between stages (transpose,
-    lift, bit reversal) are untimed."""
+    bound (n - 1) >> 2f is at least 8. Device inputs. Each stage is timed
+    on the device: the library's CUDA events on the context stream around
+    every kernel stage of the call (profiling mode), summed, after an
+    untimed call of the same size (which sizes the workspace); host launch
+    and synchronisation gaps are excluded, and layouts between stages
+    (transpose, lift, bit reversal) are untimed."""
     import ctypes as C
 
     import numpy as np
@@ -507,22 +535,20 @@ def run_sweep(Z, ctx):
         d_in = torch.from_numpy(vals.view(np.int32)).cuda()
         d_lde = torch.empty(k * m, dtype=torch.int32, device="cuda")
         torch.cuda.synchronize()
-        dt_lde = 1e9
-        for _ in range(2):  # the first call sizes the workspace for this n
-            t0 = time.perf_counter()
+        def lde():
             check(L.z0p_gpu_rs_extend(ctx.handle, C.c_void_p(d_in.data_ptr()), n, k, B,
                                       C.c_void_p(d_lde.data_ptr())))
-            dt_lde = min(dt_lde, time.perf_counter() - t0)
+        lde()  # sizes the workspace for this n
+        dt_lde = device_seconds(ctx, lde)
         flat = d_lde.view(k, m).t().contiguous()  # row-major: leaf = 16 consecutive limbs
         torch.cuda.synchronize()
         out = (C.c_uint8 * (32 * 16))()
         cnt = C.c_uint64()
-        dt_merkle = 1e9
-        for _ in range(2):
-            t0 = time.perf_counter()
+        def merkle():
             check(L.z0p_gpu_merkle_flat64_cap(ctx.handle, C.c_void_p(flat.data_ptr()), 4 * k * m, 4, out,
                                               C.byref(cnt)))
-            dt_merkle = min(dt_merkle, time.perf_counter() - t0)
+        merkle()
+        dt_merkle = device_seconds(ctx, merkle)
         del flat
         leaves = k * m // 16
         npad = 1 << (leaves - 1).bit_length()
@@ -544,11 +570,11 @@ def run_sweep(Z, ctx):
                 nl = cur.numel() // 16
                 nxt = torch.empty(4 * nl, dtype=torch.int32, device="cuda")
                 torch.cuda.synchronize()
-                t0 = time.perf_counter()
-                check(L.z0p_gpu_fri_fold(ctx.handle, C.c_void_p(cur.data_ptr()), cur.numel() // 4, m,
-                                         depth, (C.c_uint32 * 12)(*ch), C.c_void_p(nxt.data_ptr())))
+                dt = device_seconds(ctx, lambda: check(L.z0p_gpu_fri_fold(
+                    ctx.handle, C.c_void_p(cur.data_ptr()), cur.numel() // 4, m, depth,
+                    (C.c_uint32 * 12)(*ch), C.c_void_p(nxt.data_ptr()))))
                 if c >= 0:
-                    dt_fold += time.perf_counter() - t0
+                    dt_fold += dt
                     fold_bytes += 16 * (cur.numel() // 4) + 4 * (cur.numel() // 4) + 32 * (nl // 4)
                     compressions += nl // 4
                 cur, depth = nxt, depth + 1
@@ -572,7 +598,7 @@ def run_sweep(Z, ctx):
         return {"ms": round(1e3 * t, 3), "alg_bytes": by, "gbs": round(by / t / 1e9, 1),
                 "frac_hbm": round(by / t / 1e9 / peak, 4)}
     return {"workload": "64 columns, log2 n uniform in {16..22}, blowup 16; splitmix64 values",
-            "timing": "host clock around each synchronous call (launch and sync included), after a warm call",
+            "timing": "device time: CUDA events on the context stream around each kernel stage, after a warm call",
             "peak_gbs": peak, "peak_source": peak_kind,
             "lde": stage(t_lde, by_lde), "merkle": dict(stage(t_merkle, by_merkle)),
             "fold": stage(t_fold, by_fold), "blake3_compressions": compressions, "groups": rows}
@@ -736,8 +762,7 @@ def run_reference(args):
         "ms_per_step": 1000 * total / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": value / PUBLISHED_STEPS_PER_S, "dtype": "u32 (BabyBear mod p, BLAKE3 ARX)",
         "data": "synthetic (seeded)",
-        "config": {"workload": "fibonacci-air prove, 2^20 steps, for_security(100): B16 Q40 G20 C4 F16",
-                   "n_steps": N_STEPS, "lde_len": N_STEPS * 16, "proof_bytes": 203553},
+        "config": bench_config(),
         "cpu_baseline": {"value": value, "unit": "steps/s", "cores": cores, "kind": "port",
                          "sample": f"{args.steps} full 2^20-step proofs after {args.warmup} warm-up"},
         "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -888,7 +913,9 @@ def run_gpu(args):
     for name, v in prof.items():
         per = v["ms"] / prof_steps
         w = work.get(name, {})
-        ent = {"ms_per_proof": round(per, 4), "launches_per_proof": v["calls"] / prof_steps}
+        ent = {"ms_per_proof": round(per, 4),
+               "launches_per_proof": v.get("kernels", v["calls"]) / prof_steps,
+               "stage_calls_per_proof": v["calls"] / prof_steps}
         if "bytes" in w:
             ent["alg_bytes"] = w["bytes"]
             ent["gbs"] = round(w["bytes"] / (per / 1e3) / 1e9, 1) if per > 0 else None
@@ -907,7 +934,9 @@ def run_gpu(args):
         alg = d.get("alg_bytes", 0) / max(d["launches_per_proof"], 1)
         achieved = alg / (per_launch_ms / 1e3) / 1e9 if per_launch_ms > 0 else 0.0
         traffic = measured_traffic().get(dominant, {}).get("dram_bytes_per_proof")
-        roof = {"kernel": dominant, "bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
+        # BLAKE3 stages are bound by integer issue (ALU pipe), not by HBM.
+        bound = "int32" if "blake3_compressions" in d else "hbm"
+        roof = {"kernel": dominant, "bound": bound, "achieved": round(achieved, 1), "peak": peak,
                 "unit": "GB/s", "frac": round(achieved / peak, 4),
                 # ncu dram__bytes_read.sum + dram__bytes_write.sum, per launch like achieved
                 "traffic": (round(traffic / max(d["launches_per_proof"], 1)) if traffic else None),
@@ -919,7 +948,8 @@ def run_gpu(args):
             roof["int32"] = {"achieved_gcompress_per_s": d["gcompress_per_s"],
                              "ceiling_gcompress_per_s": round(hash_ceiling, 2),
                              "frac": d["frac_hash_ceiling"],
-                             "ceiling_source": "z0p_gpu_blake3_ceiling (register-resident node hashes)"}
+                             "ceiling_source": "z0p_gpu_blake3_ceiling (register-resident node hashes)",
+                             "alu_pipe_pct": measured_alu().get(dominant)}
     steps_total = args.steps * ws * N_STEPS
     value = steps_total / (dev_ms / 1e3)
     e2e = steps_total / wall_s
@@ -929,10 +959,9 @@ def run_gpu(args):
         "scaling": "weak", "vs_baseline": value / PUBLISHED_STEPS_PER_S,
         "dtype": "u32 (BabyBear mod p, BLAKE3 ARX)",
         "data": "synthetic (seeded splitmix64 initial pair)",
-        "config": {"workload": "fibonacci-air prove, 2^20 steps, for_security(100): B16 Q40 G20 C4 F16",
-                   "n_steps": N_STEPS, "lde_len": N_STEPS * 16, "proof_bytes": size,
-                   "parallelism": f"replicas x{ws}", "l2": "per-proof working set ~0.9 GB > 129 MB L2",
-                   "byte_identical_to_oracle": parity},
+        "config": bench_config(),
+        "parallelism": f"replicas x{ws}",
+        "byte_identical_to_oracle": parity,
         "e2e": {"value": e2e, "unit": "steps/s",
                 "h2d_bytes_per_step": (st1["h2d_bytes"] - st0["h2d_bytes"]) // args.steps,
                 "d2h_bytes_per_step": (st1["d2h_bytes"] - st0["d2h_bytes"]) // args.steps},
@@ -945,23 +974,57 @@ def run_gpu(args):
             "blocked_in_sync": (st1["sync_wait_ns"] - st0["sync_wait_ns"]) / 1e6 / args.steps,
             "by_sync_site": host_sites},
         "clocks": clocks,
-        "launch_schedule": tune_info,
         "roofline": roof,
-        "stages": stages,
         "cpu_baseline": cpu,
-        "batched": batched,
-        "served": served,
-        "fri_pcs": fri_pcs,
-        "fold_ivc": fold_ivc,
-        "table": table_row,
+        # secondary sections, the bulky ones first ...
+        "kernel_sweep": sweep,
         "published_rows": published,
         "scale_rows": scale,
-        "kernel_sweep": sweep,
+        "fold_ivc": fold_ivc,
+        "table": table_row,
+        "fri_pcs": fri_pcs,
+        "launch_schedule": tune_info,
+        "served": served,
+        "batched": batched,
+        "stages": stages,
     }
+    # ... and a compact summary last, so that a reader keeping only the end
+    # of the line still sees the batched / served ratios and the stage times.
+    line["summary"] = summary(line)
     print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
     return 0
+
+
+def summary(line):
+    """The evidence a short tail of the JSON line must carry."""
+    r2 = lambda x: None if x is None else round(x, 2)  # noqa: E731
+    out = {"value_msteps_per_s": r2(line["value"] / 1e6), "e2e_msteps_per_s": r2(line["e2e"]["value"] / 1e6),
+           "ms_per_step": round(line["ms_per_step"], 4)}
+    b = line.get("batched")
+    if b:
+        out["batched"] = {"speedup_vs_plain": r2(b["speedup_vs_plain"]),
+                          "msteps_per_s": r2(b["batched_steps_per_s"] / 1e6),
+                          "plain_msteps_per_s": r2(b["plain_steps_per_s"] / 1e6),
+                          "byte_identical": b["byte_identical_to_plain"],
+                          "p50_p99_ms": [r2(b["batched_latency_ms"]["p50"]), r2(b["batched_latency_ms"]["p99"])]}
+    sv = line.get("served")
+    if sv:
+        out["served"] = {"saturated_vs_plain": r2(sv["saturated_vs_plain"]),
+                         "by_rate": {str(r["rate_per_s"]): [r2(r["steps_per_s"] / 1e6), r2(r["latency_ms"]["p50"]),
+                                                            r2(r["latency_ms"]["p99"])] for r in sv["by_rate"]},
+                         "by_rate_fields": "M steps/s, p50 ms, p99 ms"}
+        if "device_busy" in sv:
+            out["served"]["device_busy_pct"] = sv["device_busy"]
+    st = line.get("stages")
+    if st:
+        out["stages_ms_frac"] = {k: [v["ms_per_proof"], v.get("frac_hbm"), v.get("frac_hash_ceiling")]
+                                 for k, v in st.items() if v["ms_per_proof"] >= 0.005}
+    ks = line.get("kernel_sweep")
+    if ks:
+        out["kernel_sweep_frac_hbm"] = {k: ks[k]["frac_hbm"] for k in ("lde", "merkle", "fold")}
+    return out
 
 
 def main():

@@ -59,7 +59,7 @@ class Context:
         check(lib().z0p_gpu_ctx_set_profiling(self.handle, 1 if on else 0))
 
     def profile(self) -> dict:
-        """Per-stage {name: {"ms", "calls"}} since the last call (profiling mode)."""
+        """Per-stage {name: {"ms", "calls", "kernels"}} since the last call (profiling mode)."""
         n = C.c_size_t()
         lib().z0p_gpu_ctx_profile(self.handle, None, 0, C.byref(n))
         buf = C.create_string_buffer(n.value + 64)

@@ -259,6 +259,8 @@ struct StageRecorder {
   virtual ~StageRecorder() = default;
   virtual void begin(const char* stage, cudaStream_t st) = 0;
   virtual void end(const char* stage, cudaStream_t st) = 0;
+  // `kernels` kernel launches issued inside the open stage `stage`.
+  virtual void launched(const char* stage, int kernels) { (void)stage; (void)kernels; }
 };
 void set_recorder(StageRecorder* r);
 
