@@ -497,9 +497,13 @@ int z0p_gpu_fri_fold(z0p_gpu_ctx *ctx, const uint32_t *d_in, uint64_t n, uint64_
  *    log2 of the first pass's transform length, within
  *    [max(7, l - 13), min(13, l - 6)]; 0 = the balanced split ceil(l / 2).
  *    Other entries must be 0.
- *  - ntt_radix32[l]: nonzero for the same transforms: the passes work in
- *    register groups of 32 elements (256 threads a CTA) instead of 16 (512
- *    threads); 0 or 1, and 0 outside 13 <= l <= 26.
+ *  - ntt_radix32[l]: the pass variant of the same transforms, 0 outside
+ *    13 <= l <= 26. 0: shared-memory passes in register groups of 16
+ *    elements (512 threads a CTA); 1: the same in groups of 32 (256
+ *    threads); 2: register passes (each half of 2^L points as two register
+ *    passes of radix 2^(L/2) with one shared-memory transpose, tiles loaded
+ *    by TMA), used when both halves are even and within 2^6..2^12 and the
+ *    input is 16-byte aligned, variant 0 otherwise.
  *  - merkle_top_log: a Merkle tree's levels are one launch each while they
  *    hold more than 2^merkle_top_log nodes; one top kernel hashes the rest
  *    (10..18).

@@ -42,15 +42,19 @@ def test_every_ntt_split_matches_oracle(z0p, oracle, gpu_ctx, restore_schedule, 
     ref = oracle.reed_solomon_extend(vals, 16)
     lo, hi = max(7, logn - 13), min(13, logn - 6)
     for split in range(lo, hi + 1):
-        for r32 in ([], [logn]):  # register groups of 16 and of 32
-            z0p.tune.set(z0p.tune.from_dict({"ntt_log_n1": {str(logn): split}, "ntt_radix32": r32}), 0)
-            assert np.array_equal(_lde(z0p, gpu_ctx, vals, 16), ref), (logn, split, r32)
+        variants = [{}, {"ntt_radix32": [logn]}]  # register groups of 16 and of 32
+        if split % 2 == 0 and (logn - split) % 2 == 0 and 6 <= logn - split <= 12 and split <= 12:
+            variants.append({"ntt_regpass": [logn]})  # register passes
+        for v in variants:
+            z0p.tune.set(z0p.tune.from_dict({"ntt_log_n1": {str(logn): split}, **v}), 0)
+            assert np.array_equal(_lde(z0p, gpu_ctx, vals, 16), ref), (logn, split, v)
 
 
 SCHEDULES = [
     {"ntt_log_n1": {"16": 7, "14": 8, "13": 7}, "merkle_top_log": 10, "grind_ctas_per_sm": 1},
     {"ntt_log_n1": {"16": 10, "14": 7}, "ntt_radix32": [14, 16, 20], "merkle_top_log": 18,
      "grind_ctas_per_sm": 8},
+    {"ntt_log_n1": {"16": 8, "14": 8}, "ntt_regpass": [14, 16], "merkle_top_log": 14},
     {"merkle_top_log": 12, "grind_ctas_per_sm": 16},
 ]
 

@@ -13,11 +13,14 @@
 //  * Merkle trees are stored level-contiguous: level l of a tree with L
 //    leaves starts at digest 2L - 2(L >> l); a digest is 8 little-endian
 //    words, byte-identical to the reference's [u8; 32].
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
 #include <atomic>
 #include <cstdint>
 #include <mutex>
+#include <utility>
 
 #include "device.cuh"
 #include "kernels.h"
@@ -366,6 +369,8 @@ __global__ void __launch_bounds__(512) ntt_pass2_kernel(const uint32_t* __restri
       *reinterpret_cast<uint4*>(o + r) = make_uint4(v[r], v[r + 1], v[r + 2], v[r + 3]);
   }
 }
+
+#include "ntt_reg.cuh"
 
 // Per coset j: 1 / (x^N - 1) with x^N = 31^N * omega_B^j (constant on the
 // coset), in Montgomery form, the same value times 2^32 once more, and the
@@ -1704,7 +1709,7 @@ Schedule g_sched[kMaxDevices];
 template <typename K>
 cudaError_t raise_smem(K* func, int pass, uint32_t L, size_t smem) {
   static std::mutex mu;
-  static size_t done[kMaxDevices][6][32] = {};
+  static size_t done[kMaxDevices][10][32] = {};
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
@@ -1741,7 +1746,7 @@ bool schedule_valid(const Schedule& s) {
   for (uint32_t l = 0; l < 32; l++) {
     uint32_t lo, hi;
     ntt_split_range(l, &lo, &hi);
-    if (s.ntt_radix32[l] > 1 || (s.ntt_radix32[l] && lo > hi)) return false;
+    if (s.ntt_radix32[l] > 2 || (s.ntt_radix32[l] && lo > hi)) return false;
     if (!s.ntt_log_n1[l]) continue;
     if (s.ntt_log_n1[l] < lo || s.ntt_log_n1[l] > hi) return false;
   }
@@ -1758,6 +1763,77 @@ void set_schedule(int device, const Schedule& s) {
   if (device < 0 || device >= kMaxDevices) return;
   std::lock_guard<std::mutex> lk(g_sched_mu);
   g_sched[device] = s;
+}
+
+// Halves the register passes cover: 2^6..2^12 points, L even.
+bool reg_split_ok(uint32_t L) { return L >= 6 && L <= 12 && (L & 1u) == 0; }
+
+namespace {
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      p = nullptr;
+    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }();
+  return fn;
+}
+
+template <int L, bool INV>
+cudaError_t reg_pass1(cudaStream_t st, const CUtensorMap& map, uint32_t* yt, const NttArgs& a, dim3 g) {
+  constexpr size_t smem = reg_ntt::pass1_smem(L);
+  if (cudaError_t e = raise_smem(ntt_reg1_kernel<L, INV>, 6 + INV, L, smem)) return e;
+  ntt_reg1_kernel<L, INV><<<g, reg_ntt::kC << (L / 2), smem, st>>>(map, yt, a);
+  return cudaGetLastError();
+}
+template <int L, bool INV>
+cudaError_t reg_pass2(cudaStream_t st, const uint32_t* yt, uint32_t* out, const NttArgs& a, dim3 g) {
+  constexpr size_t smem = reg_ntt::pass2_smem(L);
+  if (cudaError_t e = raise_smem(ntt_reg2_kernel<L, INV>, 8 + INV, L, smem)) return e;
+  ntt_reg2_kernel<L, INV><<<g, reg_ntt::kC << (L / 2), smem, st>>>(yt, out, a);
+  return cudaGetLastError();
+}
+}  // namespace
+
+// Register-pass four-step transform (ntt_reg.cuh): pass 1 reads its column
+// tiles through a tensor map over `in`, viewed as [in blocks][n1][n2] words.
+cudaError_t ntt_reg(cudaStream_t st, const NttArgs& a, const NttPlan& plan, const uint32_t* in,
+                    uint32_t* out, uint32_t* scratch, uint32_t logn1, uint32_t logn2) {
+  PFN_cuTensorMapEncodeTiled_v12000 encode = tensor_map_encoder();
+  if (!encode) return cudaErrorNotSupported;
+  const uint32_t in_div = plan.in_div ? plan.in_div : 1;
+  CUtensorMap map;
+  const cuuint64_t dims[3] = {1ull << logn2, 1ull << logn1, (plan.batch + in_div - 1) / in_div};
+  const cuuint64_t strides[2] = {4ull << logn2, 4ull << plan.logn};
+  const cuuint32_t box[3] = {reg_ntt::kC, logn1 < 8 ? (1u << logn1) : 256u, 1u};
+  const cuuint32_t elem[3] = {1u, 1u, 1u};
+  if (encode(&map, CU_TENSOR_MAP_DATA_TYPE_UINT32, 3, const_cast<uint32_t*>(in), dims, strides, box, elem,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+    return cudaErrorInvalidValue;
+  const dim3 g1((1u << logn2) / reg_ntt::kC, plan.batch), g2((1u << logn1) / reg_ntt::kC, plan.batch);
+  Stage stg(plan.inverse ? "intt" : "ntt", st);
+  stg.launched(2);
+  cudaError_t e = cudaErrorInvalidValue;
+  const bool inv = plan.inverse != 0;
+  switch (logn1) {
+#define Z0P_R1(Lv) \
+  case Lv: e = inv ? reg_pass1<Lv, true>(st, map, scratch, a, g1) : reg_pass1<Lv, false>(st, map, scratch, a, g1); break;
+    Z0P_R1(8) Z0P_R1(10) Z0P_R1(12)  // pass 1 is at least 2^7 points
+#undef Z0P_R1
+  }
+  if (e != cudaSuccess) return e;
+  e = cudaErrorInvalidValue;
+  switch (logn2) {
+#define Z0P_R2(Lv) \
+  case Lv: e = inv ? reg_pass2<Lv, true>(st, scratch, out, a, g2) : reg_pass2<Lv, false>(st, scratch, out, a, g2); break;
+    Z0P_R2(6) Z0P_R2(8) Z0P_R2(10) Z0P_R2(12)
+#undef Z0P_R2
+  }
+  return e;
 }
 
 cudaError_t ntt(cudaStream_t st, const Tables& tb, const NttPlan& plan, const uint32_t* in,
@@ -1805,6 +1881,9 @@ cudaError_t ntt(cudaStream_t st, const Tables& tb, const NttPlan& plan, const ui
   }
   const uint32_t logn2 = plan.logn - logn1;
   const uint32_t n1 = 1u << logn1, n2 = 1u << logn2;
+  if (plan.logn < 32 && sched.ntt_radix32[plan.logn] == 2 && reg_split_ok(logn1) &&
+      reg_split_ok(logn2) && tb.stw && (reinterpret_cast<uintptr_t>(in) & 15u) == 0)
+    return ntt_reg(st, a, plan, in, out, scratch, logn1, logn2);
   // C = R = 8 columns per CTA (32-byte global segments), 4 for the largest halves.
   const int logc = logn1 > 12 ? 2 : 3;
   const int logr = logn2 > 12 ? 2 : 3;
@@ -1814,7 +1893,7 @@ cudaError_t ntt(cudaStream_t st, const Tables& tb, const NttPlan& plan, const ui
   dim3 g1(n2 >> logc, plan.batch), g2(n1 >> logr, plan.batch);
   // Register groups of 32 (two shared-memory passes for a 2^10 half) run
   // 256 threads a CTA; groups of 16 run 512.
-  const bool r32 = plan.logn < 32 && sched.ntt_radix32[plan.logn];
+  const bool r32 = plan.logn < 32 && sched.ntt_radix32[plan.logn] == 1;
   const int threads = r32 ? 256 : 512, slot = r32 ? 3 : 0;
   Stage stg(plan.inverse ? "intt" : "ntt", st);
   stg.launched(2);

@@ -18,6 +18,10 @@ struct Tables {
   // stw + 2^(L-1) - 1, the inverse one kStwInverse entries further. Null:
   // the transforms compute them.
   const uint2* stw = nullptr;
+  // Device-mapped status word: a kernel whose bounded wait gave up sets it
+  // (nonzero) and returns; the host checks it after synchronising. Null: no
+  // report.
+  unsigned int* fault = nullptr;
 };
 constexpr uint32_t kStwInverse = 1u << 13;
 
@@ -230,8 +234,11 @@ struct Schedule {
   // Four-step NTT of length 2^logn (13 <= logn <= 26): log2 of the pass-1
   // transform length; 0 = the balanced default ceil(logn / 2).
   uint8_t ntt_log_n1[32] = {};
-  // Nonzero: the passes of a 2^logn transform work in register groups of 32
-  // elements (256 threads a CTA) instead of 16 (512 threads).
+  // Pass variant of a 2^logn transform: 0 = shared-memory passes in register
+  // groups of 16 elements (512 threads a CTA), 1 = the same in groups of 32
+  // (256 threads), 2 = register passes (two register passes of radix
+  // 2^(L/2) per half of 2^L points, one shared-memory transpose, the tiles
+  // loaded by TMA; both halves even and within 2^6..2^12, else variant 0).
   uint8_t ntt_radix32[32] = {};
   // A Merkle tree's levels go one launch each while they have more than
   // 2^merkle_top_log nodes; the rest go to one top kernel (10..18).
@@ -245,6 +252,8 @@ void ntt_split_range(uint32_t logn, uint32_t* lo, uint32_t* hi);
 uint32_t ntt_default_split(uint32_t logn);
 // Range checks of every field; false names no field (the caller reports).
 bool schedule_valid(const Schedule& s);
+// True when a half of 2^L points can take the register passes (variant 2).
+bool reg_split_ok(uint32_t L);
 Schedule get_schedule(int device);
 void set_schedule(int device, const Schedule& s);
 

@@ -144,6 +144,9 @@ struct z0p_gpu_ctx {
   uint8_t* hio = nullptr;
   uint8_t* hio_d = nullptr;  // its device address
   size_t hio_bytes = 0;
+  // Mapped status word of the bounded device waits (Tables::fault): nonzero
+  // once a kernel of this context gave up waiting.
+  unsigned int* fault = nullptr;
   // The context's constant slots of per-proof values (slot .. slot+nslots-1,
   // one per proof of a group) and their pinned staging copies: the host
   // fills `consts`, push_consts queues the copy into the slots.
@@ -183,6 +186,10 @@ cudaError_t sync(z0p_gpu_ctx* c, const char* site = "other") {
   uint64_t t0 = now_ns();
   cudaError_t e = cudaStreamSynchronize(c->stream);
   uint64_t t1 = now_ns();
+  if (e == cudaSuccess && c->fault && *reinterpret_cast<volatile unsigned int*>(c->fault)) {
+    *c->fault = 0u;  // reported once; the context stays usable
+    e = cudaErrorLaunchTimeout;
+  }
   c->sync_ns += t1 - t0;
   if (c->profiling) {
     HostSite& h = c->sites[site];
@@ -2668,6 +2675,17 @@ int z0p_gpu_ctx_create(int device, z0p_gpu_ctx** out) {
   }
   int rc = build_tables(c);
   if (rc == Z0P_OK) {
+    unsigned int* fault_d = nullptr;
+    if (cudaHostAlloc((void**)&c->fault, 64, cudaHostAllocMapped) != cudaSuccess ||
+        cudaHostGetDevicePointer((void**)&fault_d, c->fault, 0) != cudaSuccess) {
+      set_reason("context creation: status word setup failed");
+      rc = Z0P_ERR_CUDA;
+    } else {
+      *c->fault = 0u;
+      c->tb.fault = fault_d;
+    }
+  }
+  if (rc == Z0P_OK) {
     c->slot = take_slots(1);
     c->nslots = c->slot < 0 ? 0 : 1;
     if (c->slot < 0) {
@@ -2712,6 +2730,7 @@ void z0p_gpu_ctx_destroy(z0p_gpu_ctx* c) {
     release(c, *b);
   if (c->stream) cudaStreamSynchronize(c->stream);
   if (c->hio) cudaFreeHost(c->hio);
+  if (c->fault) cudaFreeHost(c->fault);
   if (c->consts) cudaFreeHost(c->consts);
   give_slots(c->slot, c->nslots);
   if (c->stream) cudaStreamDestroy(c->stream);
@@ -3514,7 +3533,8 @@ static int autotune_locked(z0p_gpu_ctx* c, uint32_t max_log_n, launch::Schedule*
     float t_def = 0.f, t_best = 0.f;
     uint32_t pick = 0, pick_r32 = 0;
     for (uint32_t s1 = (def > lo + 2 ? def - 2 : lo); s1 <= hi && s1 <= def + 2; s1++)
-      for (uint32_t r32 = 0; r32 < 2; r32++) {
+      for (uint32_t r32 = 0; r32 < 3; r32++) {
+        if (r32 == 2 && !(launch::reg_split_ok(s1) && launch::reg_split_ok(l - s1))) continue;
         launch::Schedule s = base;
         s.ntt_log_n1[l] = (uint8_t)s1;
         s.ntt_radix32[l] = (uint8_t)r32;

@@ -1,8 +1,9 @@
 """Launch schedules and their autotuner (no counterpart in the reference).
 
-A schedule picks, per device, the four-step NTT split and register-group
-radix (16 or 32) for each transform size, the Merkle level where one top
-kernel takes over, and the proof-of-work grid. Every schedule gives byte-identical proofs.
+A schedule picks, per device, the four-step NTT split and pass variant
+(shared-memory passes in register groups of 16 or 32, or register passes
+with TMA-loaded tiles) for each transform size, the Merkle level where one
+top kernel takes over, and the proof-of-work grid. Every schedule gives byte-identical proofs.
 
     sched, report = tune.autotune(ctx)        # measure and install
     tune.save("gb300.schedule.json", sched)   # later: tune.set(tune.load(...))
@@ -33,7 +34,8 @@ def set(schedule: Schedule, device: int = 0) -> None:  # noqa: A001 - module-lev
 
 def to_dict(s: Schedule) -> dict:
     return {"ntt_log_n1": {str(l): int(s.ntt_log_n1[l]) for l in range(32) if s.ntt_log_n1[l]},
-            "ntt_radix32": sorted(l for l in range(32) if s.ntt_radix32[l]),
+            "ntt_radix32": sorted(l for l in range(32) if s.ntt_radix32[l] == 1),
+            "ntt_regpass": sorted(l for l in range(32) if s.ntt_radix32[l] == 2),
             "merkle_top_log": int(s.merkle_top_log), "grind_ctas_per_sm": int(s.grind_ctas_per_sm)}
 
 
@@ -43,6 +45,8 @@ def from_dict(d: dict) -> Schedule:
         s.ntt_log_n1[int(l)] = int(v)
     for l in d.get("ntt_radix32", []):
         s.ntt_radix32[int(l)] = 1
+    for l in d.get("ntt_regpass", []):  # register passes (pass variant 2)
+        s.ntt_radix32[int(l)] = 2
     s.merkle_top_log = int(d.get("merkle_top_log", s.merkle_top_log))
     s.grind_ctas_per_sm = int(d.get("grind_ctas_per_sm", s.grind_ctas_per_sm))
     return s
