@@ -194,6 +194,65 @@ def stage_work(n, params):
     return work
 
 
+class UtilSampler:
+    """nvidia-smi utilization.gpu every 20 ms (the percent of the driver's
+    sample window in which a kernel was running; read-only query)."""
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", "--query-gpu=utilization.gpu",
+                 "--format=csv,noheader,nounits", "-lms", "20"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=lambda: [self.lines.append(x.strip()) for x in self.proc.stdout],
+                                      daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        v = []
+        for x in self.lines:
+            try:
+                v.append(float(x))
+            except ValueError:
+                pass
+        if not v:
+            return None
+        return {"samples": len(v), "mean_pct": round(statistics.mean(v), 1),
+                "median_pct": statistics.median(v), "p10_pct": _pct(v, 0.1)}
+
+
+def _device_work_ms(Z, ctx, specs):
+    """Device time of each proof of specs proved alone: the sum of its kernel
+    stages, timed by the library's CUDA events (profiling mode)."""
+    out = []
+    ctx.set_profiling(True)
+    try:
+        for params, _, label in specs:
+            mod = Z.air if isinstance(params, Z.air.Params) else Z.range
+            mod.prove(params, Z.Transcript(label), ctx)
+            prof = ctx.profile()
+            prof.pop("host", None)
+            out.append(sum(v["ms"] for v in prof.values()))
+    finally:
+        ctx.set_profiling(False)
+    return out
+
+
 # ------------------------------------------------- batched / served configs --
 def _mix_params(Z, seed, n_air, n_range, air_logs, range_logs):
     """Seeded job mix: Fibonacci AIRs (log2 steps uniform in air_logs) and
@@ -706,6 +765,7 @@ def run_served(Z, ctx, rates=(100, 200, 400, None), requests=120, workers=16, bu
                 if rate:
                     time.sleep(rng.expovariate(rate))
 
+        util = UtilSampler(ctx.device).start() if rate is None else None
         t0 = pool.clock()
         th = threading.Thread(target=arrive)
         th.start()
@@ -713,6 +773,8 @@ def run_served(Z, ctx, rates=(100, 200, 400, None), requests=120, workers=16, bu
         for t in tickets:
             pool.wait(t)
         t1 = max(j.end_s for j in jobs)
+        if util:
+            sat_util, sat_wall = util.stop(), t1 - t0
         lat = [j.end_s - j.submit_s for j in jobs]
         out.append({"rate_per_s": rate if rate else "saturate", "requests": len(jobs), "steps": steps,
                     "steps_per_s": steps / (t1 - t0),
@@ -721,16 +783,34 @@ def run_served(Z, ctx, rates=(100, 200, 400, None), requests=120, workers=16, bu
     # the same request set proved one at a time on the plain path
     specs = _mix_params(Z, 0x5EED000000000004, (3 * requests) // 4, requests - (3 * requests) // 4,
                         list(range(10, 23)), list(range(12, 19)))
+    util = UtilSampler(ctx.device).start()
     t0 = time.perf_counter()
     _, lat = _prove_plain(Z, ctx, specs)
     t_plain = time.perf_counter() - t0
+    plain_util = util.stop()
+    # Device work of the same set: each proof alone, its kernel stages summed.
+    work = _device_work_ms(Z, ctx, specs)
+    work_ms = sum(work)
+    big = sorted(work, reverse=True)[:len(work) // 10]
     steps = sum(n for _, n, _ in specs)
     sat = [r for r in out if r["rate_per_s"] == "saturate"]
     return {"workload": "poisson arrivals; 75% fibonacci 2^10..2^22, 25% range-16 2^12..2^18",
             "workers": workers, "hbm_budget_gb": budget / 2**30, "by_rate": out,
             "plain_one_at_a_time": {"steps_per_s": steps / t_plain,
                                     "latency_ms": {"p50": 1e3 * _pct(lat, 0.5), "p99": 1e3 * _pct(lat, 0.99)}},
-            "saturated_vs_plain": (sat[0]["steps_per_s"] / (steps / t_plain)) if sat else None}
+            "saturated_vs_plain": (sat[0]["steps_per_s"] / (steps / t_plain)) if sat else None,
+            "device_busy": {
+                "how": "work = sum over the request set of each proof's kernel-stage time alone (CUDA events); "
+                       "busy = work / wall; util = nvidia-smi utilization.gpu every 20 ms",
+                "work_ms": round(work_ms, 2),
+                "work_ms_largest_tenth_of_requests": round(sum(big), 2),
+                "plain": {"wall_ms": round(1e3 * t_plain, 2), "busy_pct": round(100 * work_ms / (1e3 * t_plain), 1),
+                          "util": plain_util},
+                "saturated": ({"wall_ms": round(1e3 * sat_wall, 2),
+                               "busy_pct": round(100 * work_ms / (1e3 * sat_wall), 1), "util": sat_util}
+                              if sat else None),
+                "plain_wall_over_work": round(t_plain * 1e3 / work_ms, 2),
+            }}
 
 
 # -------------------------------------------------------------------- arms --
@@ -1015,8 +1095,11 @@ def summary(line):
                          "by_rate": {str(r["rate_per_s"]): [r2(r["steps_per_s"] / 1e6), r2(r["latency_ms"]["p50"]),
                                                             r2(r["latency_ms"]["p99"])] for r in sv["by_rate"]},
                          "by_rate_fields": "M steps/s, p50 ms, p99 ms"}
-        if "device_busy" in sv:
-            out["served"]["device_busy_pct"] = sv["device_busy"]
+        if sv.get("device_busy"):
+            d = sv["device_busy"]
+            out["served"]["busy_pct_plain_sat"] = [d["plain"]["busy_pct"],
+                                                   d["saturated"]["busy_pct"] if d["saturated"] else None]
+            out["served"]["plain_wall_over_work"] = d["plain_wall_over_work"]
     st = line.get("stages")
     if st:
         out["stages_ms_frac"] = {k: [v["ms_per_proof"], v.get("frac_hbm"), v.get("frac_hash_ceiling")]
