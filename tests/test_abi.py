@@ -207,7 +207,10 @@ def test_schedule_get_set_validation(z0p):
     t = z0p.tune
     d = t.default()
     assert (d.merkle_top_log, d.grind_ctas_per_sm) == (16, 4)
-    assert all(v == 0 for v in d.ntt_log_n1) and all(v == 0 for v in d.ntt_radix32)
+    assert all(v == 0 for v in d.ntt_log_n1)
+    # register passes (variant 2) where the balanced split has two even halves
+    assert [l for l in range(32) if d.ntt_radix32[l]] == [16, 20, 24]
+    assert all(d.ntt_radix32[l] == 2 for l in (16, 20, 24))
     dev = 5
     before = t.to_dict(t.get(dev))
     good = t.from_dict({"ntt_log_n1": {"20": 9, "26": 13, "13": 7}, "ntt_radix32": [13, 20, 26],
@@ -217,11 +220,16 @@ def test_schedule_get_set_validation(z0p):
     for bad in [{"ntt_log_n1": {"20": 14}}, {"ntt_log_n1": {"20": 6}}, {"ntt_log_n1": {"12": 6}},
                 {"ntt_log_n1": {"27": 13}}, {"ntt_log_n1": {"14": 9}}, {"merkle_top_log": 9},
                 {"merkle_top_log": 19}, {"grind_ctas_per_sm": 0}, {"grind_ctas_per_sm": 17},
-                {"ntt_radix32": [12]}, {"ntt_radix32": [27]}]:
+                {"ntt_radix32": [12]}, {"ntt_radix32": [27]}, {"ntt_regpass": [12]},
+                {"ntt_regpass": [27]}]:
         with pytest.raises(z0p.Z0pError) as e:
             t.set(t.from_dict(bad), dev)
         assert e.value.code == 106, bad
         assert t.to_dict(t.get(dev)) == t.to_dict(good)
+    three = t.from_dict({})
+    three.ntt_radix32[20] = 3  # no such variant
+    with pytest.raises(z0p.Z0pError):
+        t.set(three, dev)
     with pytest.raises(z0p.Z0pError):
         t.get(64)
     t.set(t.from_dict(before), dev)

@@ -1701,7 +1701,7 @@ std::mutex g_sched_mu;
 Schedule g_sched[kMaxDevices];
 
 // Allows the pass-`pass` kernel `func` for half-length 2^L `smem` bytes of
-// dynamic shared memory on the current device. Each kernel's need is fixed by
+// dynamic shared memory, with the largest carveout, on the current device. Each kernel's need is fixed by
 // L, so the attribute is set once per kernel and device, not per launch.
 // cudaFuncSetAttribute acts on the current device only, so what has been
 // raised is recorded per device, and only after the call has succeeded (a
@@ -1717,6 +1717,11 @@ cudaError_t raise_smem(K* func, int pass, uint32_t L, size_t smem) {
   std::lock_guard<std::mutex> lk(mu);
   if (done[dev][pass][L] >= smem) return cudaSuccess;
   e = cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  // The largest shared-memory carveout (a hint): several CTAs of 40-50 KB
+  // fit beside one another on an SM only with it.
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(func, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             (int)cudaSharedmemCarveoutMaxShared);
   if (e == cudaSuccess) done[dev][pass][L] = smem;
   return e;
 }

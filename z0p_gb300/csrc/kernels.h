@@ -231,6 +231,15 @@ namespace launch {
 // CTAs and passes but never a result. One per device, process-wide; the
 // launchers read the current device's on every call.
 struct Schedule {
+  // The default: register passes (variant 2) wherever the balanced split has
+  // two even halves within 2^6..2^12 (2^16, 2^20 and 2^24 points), the
+  // shared-memory passes in groups of 16 elsewhere.
+  Schedule() {
+    for (uint32_t l = 13; l <= 26; l++) {
+      const uint32_t s = (l + 1) / 2;
+      if ((s & 1u) == 0 && ((l - s) & 1u) == 0 && s <= 12 && l - s >= 6) ntt_radix32[l] = 2;
+    }
+  }
   // Four-step NTT of length 2^logn (13 <= logn <= 26): log2 of the pass-1
   // transform length; 0 = the balanced default ceil(logn / 2).
   uint8_t ntt_log_n1[32] = {};

@@ -188,7 +188,7 @@ __host__ __device__ constexpr size_t pass2_smem(uint32_t L) {
 // [n1][n2] (the tensor map's x = i2, y = i1, z = input block b / in_div),
 // twisted by w^(j i) on load; writes yt[k1][i2] times the four-step twiddle.
 template <int L, bool INV>
-__global__ void __launch_bounds__(reg_ntt::kC << (L / 2))
+__global__ void __launch_bounds__(reg_ntt::kC << (L / 2), L == 10 ? 4 : 1)
     ntt_reg1_kernel(const __grid_constant__ CUtensorMap tmap, uint32_t* __restrict__ yt, NttArgs a) {
   using namespace reg_ntt;
   constexpr int H = L / 2;
@@ -240,13 +240,18 @@ __global__ void __launch_bounds__(reg_ntt::kC << (L / 2))
   const uint32_t i2 = c0 + c;
   const uint32_t shift = kRootBits - a.logn;
   const uint32_t hb = brev_bits(l, H);
-  uint32_t w = root_pow(a.tb, i2 * (tw_exp(hb, shift, INV) + (j << a.twist_shift)));
-  const uint32_t q = root_pow(a.tb, i2 * tw_exp(R, shift, INV));
+  // Four interleaved chains (e = 4 t + u) keep the products independent.
+  const uint32_t e_base = i2 * (tw_exp(hb, shift, INV) + (j << a.twist_shift));
+  const uint32_t e_q = i2 * tw_exp(R, shift, INV);
+  uint32_t w[4];
+#pragma unroll
+  for (int u = 0; u < 4; u++) w[u] = root_pow(a.tb, e_base + (uint32_t)u * e_q);
+  const uint32_t q4 = root_pow(a.tb, 4u * e_q);
   uint32_t* dst = yt + (size_t)b * n + i2;
 #pragma unroll
   for (int e = 0; e < (int)R; e++) {
-    dst[(size_t)(((uint32_t)e << H) | hb) << logn2] = mmul(x[brev_c<H>(e)], w);
-    w = mmul(w, q);
+    dst[(size_t)(((uint32_t)e << H) | hb) << logn2] = mmul(x[brev_c<H>(e)], w[e & 3]);
+    w[e & 3] = mmul(w[e & 3], q4);
   }
 }
 
@@ -291,12 +296,16 @@ __global__ void __launch_bounds__(reg_ntt::kC << (L / 2))
   const uint32_t hb = brev_bits(l, H);
   uint32_t* dst = out + (size_t)b * n + r0 + rho;
   if (a.post_gamma) {
-    uint32_t g = mmul(gamma_pow(a.tb, r0 + rho + (hb << logn1)), a.ninv_m);
-    const uint32_t gq = gamma_pow(a.tb, R << logn1);
+    // 31^k / n for k = r0 + rho + n1 k2, k2 = (e << H) | hb: four chains in e.
+    const uint32_t k0 = r0 + rho + (hb << logn1);
+    uint32_t g[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) g[u] = mmul(gamma_pow(a.tb, k0 + ((uint32_t)u * R << logn1)), a.ninv_m);
+    const uint32_t g4 = gamma_pow(a.tb, 4u * R << logn1);
 #pragma unroll
     for (int e = 0; e < (int)R; e++) {
-      dst[(size_t)(((uint32_t)e << H) | hb) << logn1] = mmul(x[brev_c<H>(e)], g);
-      g = mmul(g, gq);
+      dst[(size_t)(((uint32_t)e << H) | hb) << logn1] = mmul(x[brev_c<H>(e)], g[e & 3]);
+      g[e & 3] = mmul(g[e & 3], g4);
     }
   } else {
 #pragma unroll

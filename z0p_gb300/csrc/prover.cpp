@@ -3530,6 +3530,7 @@ static int autotune_locked(z0p_gpu_ctx* c, uint32_t max_log_n, launch::Schedule*
     uint32_t lo, hi;
     launch::ntt_split_range(l, &lo, &hi);
     const uint32_t def = launch::ntt_default_split(l);
+    const uint32_t def_r = base.ntt_radix32[l];  // the default schedule's variant
     float t_def = 0.f, t_best = 0.f;
     uint32_t pick = 0, pick_r32 = 0;
     for (uint32_t s1 = (def > lo + 2 ? def - 2 : lo); s1 <= hi && s1 <= def + 2; s1++)
@@ -3541,16 +3542,16 @@ static int autotune_locked(z0p_gpu_ctx* c, uint32_t max_log_n, launch::Schedule*
         use(s);
         float t = 0.f;
         CK(time_best(c, e0, e1, 3, run, &t));
-        if (s1 == def && !r32) t_def = t;
+        if (s1 == def && r32 == def_r) t_def = t;
         if (pick == 0 || t < t_best) {
           t_best = t;
           pick = s1;
           pick_r32 = r32;
         }
       }
-    if ((pick != def || pick_r32) && t_best > kKeep * t_def) {
+    if ((pick != def || pick_r32 != def_r) && t_best > kKeep * t_def) {
       pick = def;
-      pick_r32 = 0;
+      pick_r32 = def_r;
       t_best = t_def;
     }
     best->ntt_log_n1[l] = pick == def ? 0 : (uint8_t)pick;
