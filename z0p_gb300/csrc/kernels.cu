@@ -687,6 +687,34 @@ __global__ void merkle_level_kernel(const uint32_t* __restrict__ prev, uint32_t*
   if (cap) store_digest(cap + 8 * i, d);
 }
 
+// Two tree levels in one launch: thread i hashes nodes 2i and 2i+1 of level
+// l+1 from nodes 4i..4i+3 of level l (two independent node hashes the
+// scheduler interleaves), then their parent, node i of level l+2, without
+// reading level l+1 back. `count` = nodes at level l+2; `cap` (may be null)
+// receives level l+2 when it is the tree's cap level.
+__global__ void merkle_level2_kernel(const uint32_t* __restrict__ prev, uint32_t* __restrict__ mid,
+                                     uint32_t* __restrict__ next, uint64_t count,
+                                     uint32_t* __restrict__ cap, uint64_t stride, uint64_t cap_stride) {
+  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  prev += blockIdx.y * stride;
+  mid += blockIdx.y * stride;
+  next += blockIdx.y * stride;
+  if (cap) cap += blockIdx.y * cap_stride;
+  uint32_t a[8], b[8], c[8], e[8], d0[8], d1[8], d[8];
+  load_digest(prev + 32 * i, a);
+  load_digest(prev + 32 * i + 8, b);
+  load_digest(prev + 32 * i + 16, c);
+  load_digest(prev + 32 * i + 24, e);
+  blake3_node(a, b, d0);
+  blake3_node(c, e, d1);
+  store_digest(mid + 16 * i, d0);
+  store_digest(mid + 16 * i + 8, d1);
+  blake3_node(d0, d1, d);
+  store_digest(next + 8 * i, d);
+  if (cap) store_digest(cap + 8 * i, d);
+}
+
 __global__ void copy_words_kernel(const uint32_t* __restrict__ src, uint32_t* __restrict__ dst,
                                   uint64_t n, uint64_t src_stride, uint64_t dst_stride) {
   uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -2010,6 +2038,19 @@ cudaError_t merkle_build(cudaStream_t st, uint32_t* tree, uint64_t leaves, uint3
   // nodes measured within 7% on a 2^21-leaf tree; 2^16 was the fastest.)
   uint32_t level = from;
   const uint32_t top_log = current_schedule().merkle_top_log;
+  // Pairs of levels while both source levels are above the top kernel's.
+  while (level + 2 <= top && (leaves >> (level + 1)) > (1ull << top_log)) {
+    uint64_t cnt = leaves >> (level + 2);
+    const uint32_t* prev = tree + 8 * (2 * leaves - 2 * (leaves >> level));
+    uint32_t* mid = tree + 8 * (2 * leaves - 2 * (leaves >> (level + 1)));
+    uint32_t* next = tree + 8 * (2 * leaves - 2 * (leaves >> (level + 2)));
+    stg.launched();
+    merkle_level2_kernel<<<dim3(grid_for(cnt), nproofs), kThreads, 0, st>>>(
+        prev, mid, next, cnt, level + 2 == top ? cap : nullptr, stride, cap_stride);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    level += 2;
+  }
   while (level < top && (leaves >> level) > (1ull << top_log)) {
     uint64_t cnt = leaves >> (level + 1);
     const uint32_t* prev = tree + 8 * (2 * leaves - 2 * (leaves >> level));
