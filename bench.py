@@ -150,10 +150,11 @@ def measured_peaks():
 
 
 def measured_traffic():
-    """Per-stage DRAM bytes per proof from the committed ncu capture of this
-    workload (profiles/dram_traffic_air_prove_2p20.json), or {}."""
+    """Per stage, one captured launch of its main kernel in this workload
+    (profiles/traffic_air_prove_2p20.json, ncu with -k <kernel> -c 1): its
+    DRAM bytes, its algorithmic bytes and its ALU-pipe %, or {}."""
     try:
-        with open(os.path.join(ROOT, "profiles", "dram_traffic_air_prove_2p20.json")) as f:
+        with open(os.path.join(ROOT, "profiles", "traffic_air_prove_2p20.json")) as f:
             return json.load(f)["stages"]
     except (OSError, KeyError, ValueError):
         return {}
@@ -663,6 +664,39 @@ def run_sweep(Z, ctx):
             "fold": stage(t_fold, by_fold), "blake3_compressions": compressions, "groups": rows}
 
 
+def run_rare(Z, ctx, reps=5):
+    """The shapes that reach the kernels no production shape reaches: a FRI
+    commitment whose final layer has fewer than four values (its last fold is
+    fri_fold_plain, and the final layer's one-value leaves are leaf16,
+    fri::commit_layer_values, src/fri.rs:1422-1428), and a range proof of an
+    out-of-range value whose final layer is below the blowup (the row-by-row
+    path, whose constant columns fill_columns writes). Median wall time of
+    the public call and the proof size (bytes against the oracle: the GPU
+    tests)."""
+    vals = [(7 * i + 3) % P for i in range(1 << 10)]
+    fz = Z.fri.Params.new(8, 8, 2).with_grinding_bits(0).with_cap_height(0)
+    rz = Z.range.Params.new(1 << 10, 4, 16, 8, 4, 300)
+
+    def fri():
+        t = Z.Transcript(b"bench/rare-fri")
+        st = Z.fri.commit(vals, fz, t, ctx)
+        return st.commitment + Z.fri.open(st, t)[0]
+
+    def rng():
+        return Z.range.prove(rz, Z.Transcript(b"bench/rare-range"), ctx)
+    rows = []
+    for name, fn in [("fri 2^10 coefficients B8 Q8 final 2 (fri_fold_plain, leaf16)", fri),
+                     ("range 2^10 rows 4 bits B16 final 4, value 300 (fill_columns)", rng)]:
+        out = fn()
+        times = []
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            fn()
+            times.append(time.perf_counter() - t0)
+        rows.append({"row": name, "ms": round(1e3 * statistics.median(times), 4), "bytes": len(out)})
+    return {"rows": rows}
+
+
 def run_table(Z, ctx, reps=5):
     """Table membership (table::prove): the reference's `table 4-entry` row
     (docs/benchmarks.md:125; workload of benches/speed_size.rs:301-305) and a
@@ -894,7 +928,7 @@ def run_gpu(args):
     if args.only:
         # One section alone (for profilers and quick checks): no headline line.
         fn = {"published": run_published, "scale": run_scale, "sweep": run_sweep, "fri_pcs": run_fri_pcs,
-              "fold_ivc": run_fold_ivc,
+              "fold_ivc": run_fold_ivc, "rare": run_rare,
               "table": run_table, "batched": run_batched, "served": run_served}[args.only]
         print(json.dumps({"section": args.only, "result": fn(Z, ctx)}), flush=True)
         return 0
@@ -1013,13 +1047,17 @@ def run_gpu(args):
         per_launch_ms = d["ms_per_proof"] / max(d["launches_per_proof"], 1)
         alg = d.get("alg_bytes", 0) / max(d["launches_per_proof"], 1)
         achieved = alg / (per_launch_ms / 1e3) / 1e9 if per_launch_ms > 0 else 0.0
-        traffic = measured_traffic().get(dominant, {}).get("dram_bytes_per_proof")
+        # DRAM bytes per launch: the captured launch's ratio of DRAM to
+        # algorithmic bytes, applied to this stage's average launch.
+        cap = measured_traffic().get(dominant, {})
+        traffic = (cap["dram_bytes"] / cap["alg_bytes"] * alg) if cap.get("alg_bytes") else None
         # BLAKE3 stages are bound by integer issue (ALU pipe), not by HBM.
         bound = "int32" if "blake3_compressions" in d else "hbm"
         roof = {"kernel": dominant, "bound": bound, "achieved": round(achieved, 1), "peak": peak,
                 "unit": "GB/s", "frac": round(achieved / peak, 4),
                 # ncu dram__bytes_read.sum + dram__bytes_write.sum, per launch like achieved
-                "traffic": (round(traffic / max(d["launches_per_proof"], 1)) if traffic else None),
+                "traffic": round(traffic) if traffic else None,
+                "traffic_source": cap.get("launch"),
                 "alg_bytes_per_launch": round(alg),
                 "peak_source": peak_kind}
         if "blake3_compressions" in d:
@@ -1122,7 +1160,7 @@ def main():
                     help="launch schedule file written by z0p_gb300.tune.save (default: autotune live)")
     ap.add_argument("--only", default=None,
                     choices=["published", "scale", "sweep", "fri_pcs", "fold_ivc", "table", "batched",
-                             "served"],
+                             "served", "rare"],
                     help="run one secondary section alone and print its JSON (no headline line)")
     args = ap.parse_args()
     if args.impl == "reference":

@@ -2302,12 +2302,23 @@ int fold_add(z0p_gpu_fold* f, const uint32_t* col_a, const uint32_t* col_b,
   RC(ensure(c, step.tree, 32 * tree_digests(m)));
   const uint32_t depth = logm, drop = p.cap_height < depth ? (uint32_t)p.cap_height : depth;
   const size_t cap_bytes = 32ull << drop;
-  RC(ensure_hio(c, 64 + cap_bytes));
+  // Segments of up to 2^12 rows are interpolated by the one-CTA transform,
+  // which reads the two columns straight from the mapped buffer: no copy
+  // operation is queued for them. Larger ones are copied to the device.
+  const bool mapped_cols = logN <= 12;
+  const size_t cols_at = 64 + cap_bytes;
+  RC(ensure_hio(c, cols_at + (mapped_cols ? 8 * S : 0)));
   unsigned int* bad_h = reinterpret_cast<unsigned int*>(c->hio);
   *bad_h = 0;
   uint32_t* cols = (uint32_t*)c->cols.p;
-  CK(cudaMemcpyAsync(cols, col_a, 4 * S, cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(cols + S, col_b, 4 * S, cudaMemcpyHostToDevice, st));
+  if (mapped_cols) {
+    std::memcpy(c->hio + cols_at, col_a, 4 * S);
+    std::memcpy(c->hio + cols_at + 4 * S, col_b, 4 * S);
+    cols = hio_dev<uint32_t>(c, cols_at);
+  } else {
+    CK(cudaMemcpyAsync(cols, col_a, 4 * S, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(cols + S, col_b, 4 * S, cudaMemcpyHostToDevice, st));
+  }
   c->h2d += 8 * S;
   NttPlan ip;  // interpolate (src/ntt.rs:316-321), outputs times 31^i / S
   ip.logn = logN; ip.batch = 2; ip.inverse = 1; ip.post_gamma = 1;
@@ -2390,16 +2401,22 @@ int fold_finalize(z0p_gpu_fold* f, z0p_transcript_state* ts, uint8_t* out) {
     zinv[j] = to_mont(finv(fsub(fmul(g_s, fpow(omega_m, j * S)), 1)));
   const size_t tbytes = (size_t)K * sizeof(FoldStepDev), zoff = (tbytes + 15) & ~(size_t)15;
   RC(ensure(c, f->table, zoff + 4 * B));
-  CK(cudaMemcpyAsync(f->table.p, table.data(), tbytes, cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync((char*)f->table.p + zoff, zinv.data(), 4 * B, cudaMemcpyHostToDevice, st));
-  c->h2d += tbytes + 4 * B;
-  RC(ensure(c, f->tinv, 4 * m));
-  CK(launch::row_inverses(st, c->tb, (uint32_t*)f->tinv.p, to_mont(w_last), logN, logB));
   FriBufs fb;
   RC(plan_fri_buffers(c, s, 1, &fb));
   const uint32_t stride = (4 + 16 * psteps + 3) & ~3u;
+  // The mapped buffer's extra region: the segments' opening blocks, then the
+  // step table and the coset inverses staged for one pinned (asynchronous)
+  // copy to the device.
+  const size_t open_bytes = 4ull * stride * fp.num_queries * K;
   HioPlan h;
-  RC(plan_hio(c, s, fp.num_queries, 0, 0, 1, &h, 4ull * stride * fp.num_queries * K));
+  RC(plan_hio(c, s, fp.num_queries, 0, 0, 1, &h, open_bytes + zoff + 4 * B));
+  uint8_t* staged = c->hio + h.extra + open_bytes;
+  std::memcpy(staged, table.data(), tbytes);
+  std::memcpy(staged + zoff, zinv.data(), 4 * B);
+  CK(cudaMemcpyAsync(f->table.p, staged, zoff + 4 * B, cudaMemcpyHostToDevice, st));
+  c->h2d += tbytes + 4 * B;
+  RC(ensure(c, f->tinv, 4 * m));
+  CK(launch::row_inverses(st, c->tb, (uint32_t*)f->tinv.p, to_mont(w_last), logN, logB));
   FoldCombineArgs ca;
   ca.steps = (const FoldStepDev*)f->table.p;
   ca.nsteps = K;
