@@ -1573,31 +1573,35 @@ __global__ void __launch_bounds__(256) hash_ceiling_kernel(const uint32_t* __res
 // device-resident layers and trees into the proof-order block of each query
 // (src/fri.rs:1229-1260 for FRI, src/air.rs:565-591 and src/range.rs:483-500
 // for the trace). One CTA per query; the block layout is OpenArgs'.
-__global__ void __launch_bounds__(128) openings_kernel(OpenArgs a) {
+// The argument block stays in parameter space (__grid_constant__): the
+// layer table is indexed at run time without a per-thread local copy.
+__global__ void __launch_bounds__(128) openings_kernel(const __grid_constant__ OpenArgs a) {
   const uint32_t qi = blockIdx.x, pk = blockIdx.y;  // query, proof of the group
   uint32_t* out = a.out + ((size_t)pk * a.nq + qi) * a.stride;
   const uint64_t leaf = a.indices[(size_t)pk * a.nq + qi];
   const uint64_t vo = pk * a.fri_val_stride, to = pk * a.fri_tree_stride;
-  a.lde += pk * a.lde_stride;
-  a.ttree += pk * a.ttree_stride;
-  if (a.cb) a.cb += (size_t)pk << a.logB;
-  if (a.tinv) a.tinv += (size_t)pk << (a.logN + a.logB);
-  // FRI layers: 16 words of values, then steps x 8 words of siblings.
-  for (uint32_t d = 0; d < a.nlayers; d++) {
+  const uint32_t* lde = a.lde + pk * a.lde_stride;
+  const uint32_t* ttree = a.ttree + pk * a.ttree_stride;
+  const uint32_t* cb = a.cb ? a.cb + ((size_t)pk << a.logB) : nullptr;
+  const uint32_t* tinv = a.tinv ? a.tinv + ((size_t)pk << (a.logN + a.logB)) : nullptr;
+  // FRI layers: 16 words of values, then steps x 8 words of siblings, the
+  // layers' blocks back to back from word 0. The words of all layers are one
+  // index range, so a CTA's loads are in flight together rather than one
+  // layer's latency after another's.
+  const uint32_t fri_words =
+      a.nlayers ? a.layer[a.nlayers - 1].off + 16 + 8 * a.layer[a.nlayers - 1].steps : 0u;
+  uint32_t d = 0;
+  for (uint32_t wi = threadIdx.x; wi < fri_words; wi += blockDim.x) {
+    while (d + 1 < a.nlayers && wi >= a.layer[d + 1].off) d++;
     const OpenLayer& L = a.layer[d];
+    const uint32_t t = wi - L.off;
     const uint64_t base = (leaf >> (2 * d)) & ~3ull;
-    const uint64_t Q = base >> 2;
-    uint32_t* o = out + L.off;
-    const uint32_t* values = L.values + vo;
-    const uint32_t* tree = L.tree + to;
-    for (uint32_t t = threadIdx.x; t < 16 + 8 * L.steps; t += blockDim.x) {
-      if (t < 16) {
-        o[t] = values[4 * base + t];
-      } else {
-        const uint32_t st = (t - 16) >> 3, w = (t - 16) & 7u;
-        const uint64_t sib = (Q >> st) ^ 1ull;
-        o[t] = tree[8 * (2 * L.leaves - 2 * (L.leaves >> st) + sib) + w];
-      }
+    if (t < 16) {
+      out[wi] = L.values[vo + 4 * base + t];
+    } else {
+      const uint32_t st = (t - 16) >> 3, w = (t - 16) & 7u;
+      const uint64_t sib = ((base >> 2) >> st) ^ 1ull;
+      out[wi] = L.tree[to + 8 * (2 * L.leaves - 2 * (L.leaves >> st) + sib) + w];
     }
   }
   if (a.no_trace) return;
@@ -1611,24 +1615,26 @@ __global__ void __launch_bounds__(128) openings_kernel(OpenArgs a) {
     // AIR: rows base..base+7 of `index` and of `index + B`, A || B each, with
     // B = A(q+1) + C_j * tinv[j][q] (the linked column).
     const uint64_t shift = a.shift ? a.shift : B;
-    for (uint32_t h = 0; h < 2; h++) {
+    const uint32_t per = 16 + 8 * a.tsteps;  // both rows' blocks in one index range
+    for (uint32_t ti = threadIdx.x; ti < 2 * per; ti += blockDim.x) {
+      const uint32_t h = ti >= per, t = ti - h * per;
       const uint64_t at = h ? (index + shift) % m : index;
       const uint64_t base = at & ~7ull;
-      uint32_t* oh = o + h * (16 + 8 * a.tsteps);
-      for (uint32_t t = threadIdx.x; t < 16 + 8 * a.tsteps; t += blockDim.x) {
+      uint32_t* oh = o + h * per;
+      {
         if (t < 16) {
           const uint32_t k = (uint32_t)base + (t >> 1);
           const uint32_t j = k & (B - 1u), q = k >> a.logB;
           const size_t cj = (size_t)j << a.logN;
-          uint32_t v = a.lde[cj + q];
+          uint32_t v = lde[cj + q];
           if (t & 1u)
             v = a.lde_b ? a.lde_b[cj + q]
-                        : fadd(a.lde[cj + ((q + 1u) & (N - 1u))], mmul(a.cb[j], a.tinv[cj + q]));
+                        : fadd(lde[cj + ((q + 1u) & (N - 1u))], mmul(cb[j], tinv[cj + q]));
           oh[t] = v;
         } else {
           const uint32_t st = (t - 16) >> 3, w = (t - 16) & 7u;
           const uint64_t sib = ((base >> 3) >> st) ^ 1ull;
-          oh[t] = a.ttree[8 * (2 * a.tleaves - 2 * (a.tleaves >> st) + sib) + w];
+          oh[t] = ttree[8 * (2 * a.tleaves - 2 * (a.tleaves >> st) + sib) + w];
         }
       }
     }
@@ -1637,11 +1643,11 @@ __global__ void __launch_bounds__(128) openings_kernel(OpenArgs a) {
     const uint32_t j = (uint32_t)index & (B - 1u), q = (uint32_t)(index >> a.logB);
     for (uint32_t t = threadIdx.x; t < a.ncol + 8 * a.tsteps; t += blockDim.x) {
       if (t < a.ncol) {
-        o[t] = a.lde[(size_t)t * m + ((size_t)j << a.logN) + q];
+        o[t] = lde[(size_t)t * m + ((size_t)j << a.logN) + q];
       } else {
         const uint32_t st = (t - a.ncol) >> 3, w = (t - a.ncol) & 7u;
         const uint64_t sib = (index >> st) ^ 1ull;
-        o[t] = a.ttree[8 * (2 * a.tleaves - 2 * (a.tleaves >> st) + sib) + w];
+        o[t] = ttree[8 * (2 * a.tleaves - 2 * (a.tleaves >> st) + sib) + w];
       }
     }
   }
