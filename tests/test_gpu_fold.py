@@ -40,6 +40,12 @@ CASES = [
     (64, 16, 20, 16, 8, 2, 5),
     (1 << 10, 8, 12, 8, 0, 3, 2),
     (1 << 12, 16, 30, 16, 6, 4, 3),
+    # one-launch segment commits (fold_segment: S B <= 256) at their edges:
+    # two-row segments, a cap at the leaves, 256 rows at two splits
+    (2, 16, 4, 8, 0, 0, 3),
+    (4, 8, 6, 8, 2, 5, 2),
+    (16, 16, 10, 4, 0, 2, 2),
+    (32, 8, 8, 4, 3, 1, 3),
 ]
 
 

@@ -608,6 +608,74 @@ __global__ void __launch_bounds__(kThreads) range_trace_leaves_kernel(
                 top, cap, counter);
 }
 
+// A small IVC segment's commit in one CTA (src/fold.rs:430-458): both
+// columns interpolated on <omega_S> with outputs times 31^i / S
+// (src/ntt.rs:316-321, 353-358), each extended to the B cosets of 2^logm
+// rows (src/ntt.rs:341-363, written coset-major per column like the
+// two-launch path), the 8-byte A || B row leaves hashed
+// (src/merkle.rs:63-80) and their tree built up to `top`, every level into
+// `tree` and level `top` into `cap`. One thread per LDE row (m = S B <=
+// kSegmentMaxRows); the 2 + 2B transforms of S = 2^L points share the
+// shared-memory DIF of the one-CTA NTT. The columns are read where the
+// caller left them (the mapped buffer) and checked as they load.
+constexpr uint32_t kSegmentMaxRows = 256;
+template <int L>
+__global__ void __launch_bounds__(kSegmentMaxRows) fold_segment_kernel(
+    const uint32_t* __restrict__ cols, unsigned int* bad, uint32_t* __restrict__ lde,
+    uint32_t* __restrict__ tree, uint32_t* __restrict__ cap, uint32_t logB, uint32_t top,
+    uint32_t ninv_m, Tables tb) {
+  constexpr uint32_t S = 1u << L;
+  constexpr uint32_t cs = (skewed_len(S) + 1u) & ~1u;  // column stride (words)
+  extern __shared__ uint32_t sm[];
+  const uint32_t B = 1u << logB, logm = L + logB, m = S << logB;
+  uint32_t* coef = sm;                                   // 2 columns
+  uint32_t* ext = coef + 2 * cs;                         // 2B cosets
+  uint2* tw_inv = reinterpret_cast<uint2*>(ext + 2 * B * cs);
+  uint2* tw_fwd = tw_inv + tw_entries(L);
+  uint32_t* buf = reinterpret_cast<uint32_t*>(tw_fwd + tw_entries(L));  // 2 * 9 * m words
+  const uint32_t t = threadIdx.x;
+  NttArgs a{};
+  a.tb = tb;
+  a.inverse = 1;
+  stage_twiddles<L>(tw_inv, a);
+  a.inverse = 0;
+  stage_twiddles<L>(tw_fwd, a);
+  for (uint32_t e = t; e < 2 * S; e += blockDim.x) {
+    const uint32_t c = e >> L, i = e & (S - 1u);
+    const uint32_t v = cols[e];
+    if (v >= kP) atomicOr(bad, 1u);
+    coef[c * cs + spos(i)] = v;
+  }
+  __syncthreads();
+  smem_dif_t<L>(coef, tw_inv, 2, cs);
+  // Coefficient i of column c times 31^i / S, then twisted by omega_m^(j i)
+  // into coset j's input.
+  for (uint32_t e = t; e < 2 * m; e += blockDim.x) {
+    const uint32_t b = e >> L, i = e & (S - 1u);  // b = c B + j
+    const uint32_t c = b >> logB, j = b & (B - 1u);
+    uint32_t v = mmul(mmul(coef[c * cs + spos(brev_bits(i, L))], gamma_pow(tb, i)), ninv_m);
+    if (j) v = mmul(v, root_pow(tb, (j * i) << (kRootBits - logm)));
+    ext[b * cs + spos(i)] = v;
+  }
+  __syncthreads();
+  smem_dif_t<L>(ext, tw_fwd, 2 * B, cs);
+  uint32_t d[8];
+  if (t < m) {
+    const uint32_t j = t & (B - 1u), q = t >> logB;  // row t = B q + j
+    const uint32_t p = spos(brev_bits(q, L));
+    uint32_t w[32];
+#pragma unroll
+    for (int k = 0; k < 32; k++) w[k] = 0u;
+    w[0] = ext[j * cs + p];
+    w[1] = ext[(B + j) * cs + p];
+    lde[(j << L) + q] = w[0];
+    lde[m + (j << L) + q] = w[1];
+    row_leaf_digest(w, 2, d);
+    store_digest(tree + 8 * t, d);
+  }
+  cta_subtree(d, buf, m, 0, tree, m, top, cap, nullptr);
+}
+
 // Merkle trees whose leaves repeat in runs (kernels.h, UniformTree): one CTA
 // per tree. Each group's chain is one thread's sequence of node hashes of a
 // digest with itself; the group roots then go up as an ordinary tree in
@@ -1241,20 +1309,43 @@ __global__ void row_inverses_kernel(uint32_t* __restrict__ tinv, uint32_t w_last
 //   1/z_trans = (x - w_last) / (x^s - 1)     (x^s constant on a coset)
 //   1/(x - w_last) = T(q),  1/(x - 1) = omega_s^-1 T(q-1)  (folded into ga[2], ga[3])
 // All arithmetic is exact, so the sum equals sum_k gamma_k C_k term by term.
+// kFused (small layer 0, a.counter): thread u makes leaf P = u and the launch
+// builds the layer-0 tree (cta_subtree); each thread inverts its four rows'
+// x - w_last and x omega_s^-1 - w_last (= x_{q-1} - w_last on a coset) in
+// one batch instead of reading T.
+template <bool kFused>
 __global__ void __launch_bounds__(kThreads) fold_combine_kernel(FoldCombineArgs a, Tables tb) {
+  __shared__ uint32_t buf[kFused ? 2 * kThreads * kTopStride : 1];
   const uint32_t logm = a.logN + a.logB;
   const uint32_t quarter = 1u << (logm - 2);
   const uint32_t u = blockIdx.x * blockDim.x + threadIdx.x;
-  if (u >= quarter) return;
+  if (!kFused && u >= quarter) return;
+  const uint32_t nt = quarter < kThreads ? quarter : kThreads;
+  uint32_t d[8];
+  if (u < quarter) {
   const uint32_t N = 1u << a.logN, B = 1u << a.logB;
-  uint32_t k0 = u;
-  if (a.logN >= 2) {
-    const uint32_t j = u >> (a.logN - 2), q0 = u & ((N >> 2) - 1u);
-    k0 = (q0 << a.logB) | j;
+  uint32_t k0 = u, P;
+  if (kFused) {
+    P = u;
+    k0 = brev_bits(u, logm - 2);
+  } else {
+    if (a.logN >= 2) {
+      const uint32_t j = u >> (a.logN - 2), q0 = u & ((N >> 2) - 1u);
+      k0 = (q0 << a.logB) | j;
+    }
+    P = brev_bits(k0, logm - 2);
   }
-  const uint32_t P = brev_bits(k0, logm - 2);
   uint32_t xs[4];
   quad_points(tb, k0, logm, xs);
+  uint32_t inv[8];  // kFused: T(q) of row s at s, T(q - 1) at 4 + s
+  if (kFused) {
+#pragma unroll
+    for (int s = 0; s < 4; s++) {
+      inv[s] = fsub(xs[s], a.w_last_m);
+      inv[4 + s] = fsub(mmul(xs[s], a.w_last_m), a.w_last_m);
+    }
+    batch_minv(inv);
+  }
   uint32_t leaf[16];
 #pragma unroll
   for (int s = 0; s < 4; s++) {
@@ -1262,8 +1353,8 @@ __global__ void __launch_bounds__(kThreads) fold_combine_kernel(FoldCombineArgs 
     const uint32_t j = k & (B - 1u), q = k >> a.logB;
     const size_t base = (size_t)j << a.logN;
     const size_t at = base + q, atn = base + ((q + 1u) & (N - 1u));
-    const uint32_t tm = __ldg(a.tinv + base + ((q - 1u) & (N - 1u)));
-    const uint32_t t0 = __ldg(a.tinv + at);
+    const uint32_t tm = kFused ? inv[4 + s] : __ldg(a.tinv + base + ((q - 1u) & (N - 1u)));
+    const uint32_t t0 = kFused ? inv[s] : __ldg(a.tinv + at);
     const uint32_t iz = mmul(fsub_lazy(xs[s], a.w_last_m), __ldg(a.zinv + j));
     uint32_t acc[4] = {0u, 0u, 0u, 0u};
     for (uint32_t st = 0; st < a.nsteps; st++) {
@@ -1291,9 +1382,12 @@ __global__ void __launch_bounds__(kThreads) fold_combine_kernel(FoldCombineArgs 
 #pragma unroll
   for (int t = 0; t < 4; t++)
     dst[t] = make_uint4(leaf[4 * t], leaf[4 * t + 1], leaf[4 * t + 2], leaf[4 * t + 3]);
-  uint32_t d[8];
   blake3_leaf64(leaf, d);
   store_digest(a.leaves + 8 * (size_t)P, d);
+  }
+  if constexpr (kFused)
+    cta_subtree(d, buf, nt, (uint64_t)blockIdx.x * kThreads, a.leaves, quarter, a.top, a.cap,
+                a.counter);
 }
 
 // CTA (query i, step k): 4 column words, then the two capped row paths.
@@ -2003,6 +2097,32 @@ cudaError_t air_trace_leaves(cudaStream_t st, const Tables& tb, const uint32_t* 
   return cudaGetLastError();
 }
 
+bool fold_segment_ok(uint32_t logN, uint32_t logB) {
+  return logN >= 1 && logN <= 8 && (1u << (logN + logB)) <= kSegmentMaxRows && logN + logB >= 5;
+}
+
+cudaError_t fold_segment(cudaStream_t st, const Tables& tb, const uint32_t* cols, unsigned int* bad,
+                         uint32_t* lde, uint32_t* tree, uint32_t* cap, uint32_t logN, uint32_t logB,
+                         uint32_t top) {
+  if (!fold_segment_ok(logN, logB) || !tb.stw) return cudaErrorInvalidValue;
+  const uint32_t S = 1u << logN, B = 1u << logB, m = S * B;
+  const uint32_t cs = (skewed_len(S) + 1u) & ~1u;
+  const size_t smem = 4 * ((size_t)2 * cs + 2ull * B * cs + 4ull * tw_entries(logN) + 18ull * m);
+  uint64_t inv2 = (kP + 1) / 2, v = 1;  // S^-1 in Montgomery form
+  for (uint32_t i = 0; i < logN; i++) v = v * inv2 % kP;
+  const uint32_t ninv_m = (uint32_t)((v << 32) % kP);
+  Stage stg("fold_segment", st);
+  stg.launched();
+  switch (logN) {
+#define Z0P_SEG(Lv) \
+  case Lv: fold_segment_kernel<Lv><<<1, m, smem, st>>>(cols, bad, lde, tree, cap, logB, top, ninv_m, tb); break;
+    Z0P_SEG(1) Z0P_SEG(2) Z0P_SEG(3) Z0P_SEG(4) Z0P_SEG(5) Z0P_SEG(6) Z0P_SEG(7) Z0P_SEG(8)
+#undef Z0P_SEG
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
 cudaError_t range_trace_leaves(cudaStream_t st, const uint32_t* lde, uint32_t* leaves,
                                uint32_t logN, uint32_t logB, uint32_t ncols, uint32_t nproofs,
                                uint64_t tree_stride, unsigned int* counter, uint32_t top,
@@ -2283,11 +2403,19 @@ cudaError_t row_inverses(cudaStream_t st, const Tables& tb, uint32_t* tinv, uint
 }
 
 
-cudaError_t fold_combine(cudaStream_t st, const Tables& tb, const FoldCombineArgs& a) {
+cudaError_t fold_combine(cudaStream_t st, const Tables& tb, const FoldCombineArgs& a,
+                         uint32_t* levels) {
   if (a.logN + a.logB < 3) return cudaErrorInvalidValue;
+  const uint64_t quarter = 1ull << (a.logN + a.logB - 2);
+  const bool fused = a.counter && quarter <= kFuseMaxLeaves;
+  if (!fused && !a.tinv) return cudaErrorInvalidValue;  // the unfused kernel reads T
+  if (levels) *levels = fused ? a.top : 0u;
   Stage stg("fold_combine", st);
   stg.launched();
-  fold_combine_kernel<<<grid_for(1ull << (a.logN + a.logB - 2)), kThreads, 0, st>>>(a, tb);
+  if (fused)
+    fold_combine_kernel<true><<<grid_for(quarter), kThreads, 0, st>>>(a, tb);
+  else
+    fold_combine_kernel<false><<<grid_for(quarter), kThreads, 0, st>>>(a, tb);
   return cudaGetLastError();
 }
 

@@ -194,6 +194,12 @@ struct FoldCombineArgs {
   uint32_t* leaves;      // its leaf digests
   uint32_t logN, logB;   // segment rows s = 2^logN, blowup 2^logB
   uint32_t w_last_m;     // omega_s^(s-1) (Montgomery)
+  // Non-null counter (layer 0 of at most kFuseMaxLeaves leaves): the launch
+  // computes its rows' 1/(x - w_last) itself (tinv unused) and builds the
+  // layer-0 tree up to `top`, that level also into `cap`.
+  unsigned int* counter = nullptr;
+  uint32_t top = 0;
+  uint32_t* cap = nullptr;
 };
 // Table membership composition inputs (src/table.rs:597-644).
 struct TableComposeArgs {
@@ -329,6 +335,16 @@ cudaError_t table_compose(cudaStream_t st, const Tables& tb, const TableComposeA
 // are alpha_0..alpha_4 with alpha_2, alpha_3 times omega_n^-1.
 cudaError_t air_compose_general(cudaStream_t st, const Tables& tb, const AirComposeArgs& a,
                                 const uint32_t* lde_b, uint32_t r);
+// A small IVC segment's commit in one launch (2 <= S = 2^logN <= 2^8,
+// 32 <= S B <= 256): interpolation of the two columns at `cols` (checked on
+// load, a non-canonical word sets *bad), their coset-major LDEs at `lde`
+// (column A, then column B), the 8-byte row leaves and the tree up to `top`,
+// level `top` also into `cap`. The same words as the two NTTs and the row
+// leaves of range_trace_leaves with two columns.
+bool fold_segment_ok(uint32_t logN, uint32_t logB);
+cudaError_t fold_segment(cudaStream_t st, const Tables& tb, const uint32_t* cols, unsigned int* bad,
+                         uint32_t* lde, uint32_t* tree, uint32_t* cap, uint32_t logN, uint32_t logB,
+                         uint32_t top);
 // With a counter (one zero word per proof) and at most kFuseMaxLeaves rows,
 // the launch also builds the tree up to `top` and writes that level to cap
 // (proof k at k * cap_stride); *levels receives the levels built (0:
@@ -385,7 +401,8 @@ cudaError_t row_inverses(cudaStream_t st, const Tables& tb, uint32_t* tinv, uint
                          uint32_t logN, uint32_t logB);
 // combined(x) = sum_k gamma_k C_k(x) over the accumulated segments, written
 // as FRI layer 0 with its leaf digests (src/fold.rs:494-517, 785-850).
-cudaError_t fold_combine(cudaStream_t st, const Tables& tb, const FoldCombineArgs& a);
+cudaError_t fold_combine(cudaStream_t st, const Tables& tb, const FoldCombineArgs& a,
+                         uint32_t* levels = nullptr);
 // Step openings (src/fold.rs:527-552): for step k and query i, at
 // out + (k nq + i) stride: A, B at index = brev(leaf) and at index + B
 // (mod m), then the capped paths of both rows (steps x 8 words each).

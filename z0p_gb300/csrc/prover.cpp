@@ -2320,22 +2320,28 @@ int fold_add(z0p_gpu_fold* f, const uint32_t* col_a, const uint32_t* col_b,
     CK(cudaMemcpyAsync(cols + S, col_b, 4 * S, cudaMemcpyHostToDevice, st));
   }
   c->h2d += 8 * S;
-  NttPlan ip;  // interpolate (src/ntt.rs:316-321), outputs times 31^i / S
-  ip.logn = logN; ip.batch = 2; ip.inverse = 1; ip.post_gamma = 1;
-  ip.bad = hio_dev<unsigned int>(c, 0);  // the columns are checked as they load
-  CK(launch::ntt(st, c->tb, ip, cols, (uint32_t*)c->coeffs.p, (uint32_t*)c->scratch.p));
-  NttPlan lp;  // evaluate_on_coset (src/ntt.rs:341-363), coset-major per column
-  lp.logn = logN; lp.batch = (uint32_t)(2 * B); lp.in_div = (uint32_t)B; lp.twist_mod = (uint32_t)B;
-  lp.twist_shift = 27 - logm;
   uint32_t* lde = (uint32_t*)step.lde.p;
-  CK(launch::ntt(st, c->tb, lp, (uint32_t*)c->coeffs.p, lde, (uint32_t*)c->scratch.p));
-  // Row tree over A || B (src/fold.rs:448-458: MerkleTree::from_flat, 8-byte rows).
   uint32_t* tree = (uint32_t*)step.tree.p;
-  uint32_t built = 0;  // small segment trees finished in the launch
-  CK(launch::range_trace_leaves(st, lde, tree, logN, logB, 2, 1, 0, merkle_counter(c), depth - drop,
-                                hio_dev<uint32_t>(c, 64), 0, &built));
-  if (built == 0)
-    CK(launch::merkle_build(st, tree, m, depth - drop, merkle_counter(c), hio_dev<uint32_t>(c, 64)));
+  if (mapped_cols && launch::fold_segment_ok(logN, logB)) {
+    // Small segments: interpolation, LDE, row leaves and tree in one launch.
+    CK(launch::fold_segment(st, c->tb, cols, hio_dev<unsigned int>(c, 0), lde, tree,
+                            hio_dev<uint32_t>(c, 64), logN, logB, depth - drop));
+  } else {
+    NttPlan ip;  // interpolate (src/ntt.rs:316-321), outputs times 31^i / S
+    ip.logn = logN; ip.batch = 2; ip.inverse = 1; ip.post_gamma = 1;
+    ip.bad = hio_dev<unsigned int>(c, 0);  // the columns are checked as they load
+    CK(launch::ntt(st, c->tb, ip, cols, (uint32_t*)c->coeffs.p, (uint32_t*)c->scratch.p));
+    NttPlan lp;  // evaluate_on_coset (src/ntt.rs:341-363), coset-major per column
+    lp.logn = logN; lp.batch = (uint32_t)(2 * B); lp.in_div = (uint32_t)B; lp.twist_mod = (uint32_t)B;
+    lp.twist_shift = 27 - logm;
+    CK(launch::ntt(st, c->tb, lp, (uint32_t*)c->coeffs.p, lde, (uint32_t*)c->scratch.p));
+    // Row tree over A || B (src/fold.rs:448-458: MerkleTree::from_flat, 8-byte rows).
+    uint32_t built = 0;  // small segment trees finished in the launch
+    CK(launch::range_trace_leaves(st, lde, tree, logN, logB, 2, 1, 0, merkle_counter(c), depth - drop,
+                                  hio_dev<uint32_t>(c, 64), 0, &built));
+    if (built == 0)
+      CK(launch::merkle_build(st, tree, m, depth - drop, merkle_counter(c), hio_dev<uint32_t>(c, 64)));
+  }
   CK(sync(c, "cap"));
   if (*reinterpret_cast<volatile unsigned int*>(bad_h)) {
     set_reason("field elements must be canonical (< p)");
@@ -2415,21 +2421,33 @@ int fold_finalize(z0p_gpu_fold* f, z0p_transcript_state* ts, uint8_t* out) {
   std::memcpy(staged + zoff, zinv.data(), 4 * B);
   CK(cudaMemcpyAsync(f->table.p, staged, zoff + 4 * B, cudaMemcpyHostToDevice, st));
   c->h2d += tbytes + 4 * B;
-  RC(ensure(c, f->tinv, 4 * m));
-  CK(launch::row_inverses(st, c->tb, (uint32_t*)f->tinv.p, to_mont(w_last), logN, logB));
+  // Small layers 0: the combination launch inverts its rows' denominators
+  // itself and builds the layer-0 tree; larger ones read a table of them.
+  const bool fused_combine = (m / 4) <= kFuseMaxLeaves;  // fold_combine's own test
+  if (!fused_combine) {
+    RC(ensure(c, f->tinv, 4 * m));
+    CK(launch::row_inverses(st, c->tb, (uint32_t*)f->tinv.p, to_mont(w_last), logN, logB));
+  }
   FoldCombineArgs ca;
   ca.steps = (const FoldStepDev*)f->table.p;
   ca.nsteps = K;
-  ca.tinv = (const uint32_t*)f->tinv.p;
+  ca.tinv = fused_combine ? nullptr : (const uint32_t*)f->tinv.p;
   ca.zinv = (const uint32_t*)((const char*)f->table.p + zoff);
   ca.layer0 = fb.layer[0];
   ca.leaves = fb.tree[0];
   ca.logN = logN; ca.logB = logB;
   ca.w_last_m = to_mont(w_last);
-  CK(launch::fold_combine(st, c->tb, ca));
-  CK(launch::merkle_build(st, fb.tree[0], s.leaves[0], s.depth[0] - s.drop[0], merkle_counter(c),
-                          hio_dev<uint32_t>(c, h.fri_cap[0]), 0, 1, fb.tree_stride,
-                          h.fri_cap_bytes[0] / 4));
+  if (fused_combine) {
+    ca.counter = merkle_counter(c);
+    ca.top = s.depth[0] - s.drop[0];
+    ca.cap = hio_dev<uint32_t>(c, h.fri_cap[0]);
+  }
+  uint32_t built0 = 0;
+  CK(launch::fold_combine(st, c->tb, ca, &built0));
+  if (built0 == 0)
+    CK(launch::merkle_build(st, fb.tree[0], s.leaves[0], s.depth[0] - s.drop[0], merkle_counter(c),
+                            hio_dev<uint32_t>(c, h.fri_cap[0]), 0, 1, fb.tree_stride,
+                            h.fri_cap_bytes[0] / 4));
   // fri::commit_ext_evals(combined, S - 1) and fri::open (src/fold.rs:517-520).
   Transcript* tp[1] = {&t};
   FriOut fo;
