@@ -1508,6 +1508,59 @@ __global__ void __launch_bounds__(kFoldThreads) fri_fold_leaf_kernel(FoldArgs a,
   cta_subtree(d, sm, avail, first, a.leaves, nleaf, a.top, a.cap, a.counter);
 }
 
+// The small-layer form of fri_fold_leaf_kernel<true> (trees of at most
+// kFuseMaxLeaves leaves, latency-bound launches of a few CTAs): four threads
+// per next leaf, one quad each, so a thread waits on one fold's loads and
+// products instead of four; the leaf's four values meet in its first lane by
+// warp shuffles, which hashes the leaf. 128 leaves per CTA as before, so the
+// subtree and the last CTA's levels are unchanged.
+constexpr int kFold4Threads = 4 * kFoldThreads;
+__global__ void __launch_bounds__(kFold4Threads) fri_fold_quad_kernel(FoldArgs a, Tables tb) {
+  __shared__ uint32_t sm[2 * kTopStride * (kFuseMaxLeaves / kFoldThreads)];
+  fold_for_proof(a);
+  const uint64_t nleaf = 1ull << (a.logn - 4);
+  const uint64_t first = (uint64_t)blockIdx.x * kFoldThreads;
+  const uint32_t avail = nleaf < (uint64_t)kFoldThreads ? (uint32_t)nleaf : (uint32_t)kFoldThreads;
+  const uint32_t tl = threadIdx.x >> 2, tq = threadIdx.x & 3u;  // leaf in the CTA, its quad
+  const uint64_t Pn = first + tl;
+  uint32_t r[4] = {0u, 0u, 0u, 0u};
+  if (tl < avail) {
+    const uint4* src = reinterpret_cast<const uint4*>(a.in) + Pn * 16 + 4 * tq;
+    E4 q[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+      uint4 v = __ldcs(src + i);
+      q[i].c[0] = v.x; q[i].c[1] = v.y; q[i].c[2] = v.z; q[i].c[3] = v.w;
+    }
+    const E4 f = fold_quad(q[0], q[1], q[2], q[3], quad_xinv(tb, a, (uint32_t)(4 * Pn + tq)), a);
+#pragma unroll
+    for (int c = 0; c < 4; c++) r[c] = f.c[c];
+    const uint4 o = make_uint4(r[0], r[1], r[2], r[3]);
+    reinterpret_cast<uint4*>(a.out + 16 * Pn)[tq] = o;
+    if (a.final_vals) reinterpret_cast<uint4*>(a.final_vals + 16 * Pn)[tq] = o;
+  }
+  // Lanes 4 tl .. 4 tl + 3 of a warp hold leaf tl's four values.
+  const uint32_t lane = threadIdx.x & 31u;
+  uint32_t leaf[16];
+#pragma unroll
+  for (int s2 = 0; s2 < 4; s2++)
+#pragma unroll
+    for (int c = 0; c < 4; c++) leaf[4 * s2 + c] = __shfl_sync(0xffffffffu, r[c], (lane & ~3u) | s2);
+  if (tl < avail && tq == 0) {
+    uint32_t d[8];
+    blake3_leaf64(leaf, d);
+    store_digest(a.leaves + 8 * Pn, d);
+#pragma unroll
+    for (int i = 0; i < 8; i++) sm[kTopStride * tl + i] = d[i];
+  }
+  __syncthreads();
+  uint32_t d[8];
+#pragma unroll
+  for (int i = 0; i < 8; i++) d[i] = threadIdx.x < avail ? sm[kTopStride * threadIdx.x + i] : 0u;
+  __syncthreads();
+  cta_subtree(d, sm, avail, first, a.leaves, nleaf, a.top, a.cap, a.counter);
+}
+
 // Thread per next-layer value (small layers; leaves hashed separately).
 __global__ void fri_fold_plain_kernel(FoldArgs a, Tables tb) {
   fold_for_proof(a);
@@ -2246,7 +2299,7 @@ cudaError_t fri_fold(cudaStream_t st, const Tables& tb, const FoldArgs& a, uint3
     stg.launched();
     const dim3 grid(grid_for(nleaf, kFoldThreads), nproofs);
     if (f.counter)
-      fri_fold_leaf_kernel<true><<<grid, kFoldThreads, 0, st>>>(f, tb);
+      fri_fold_quad_kernel<<<grid, kFold4Threads, 0, st>>>(f, tb);
     else
       fri_fold_leaf_kernel<false><<<grid, kFoldThreads, 0, st>>>(f, tb);
     return cudaGetLastError();
