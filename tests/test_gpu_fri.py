@@ -57,6 +57,9 @@ CASES = [
     (2, 1 << 12, 16, 10, 16, 5, 3, 255),
     (3, 256, 4, 8, 4, 0, 1, 63),
     (3, 1 << 14, 4, 24, 16, 0, 4, 1023),
+    # 256-digest caps and a 1024-value final layer: the device transcript
+    # absorbs about 16 KB per layer, crossing chunks and merging its stack.
+    (0, 1 << 12, 4, 8, 1024, 3, 8, 0),
 ]
 
 
@@ -98,6 +101,23 @@ def test_production_size_commitment(z0p, oracle, gpu_ctx):
     assert st.commitment == so.commitment
     proof, idx = z0p.fri.open(st, tg)
     assert (proof, idx) == oracle.fri_open(so, to)
+    assert tg.export() == to.export()
+
+
+def test_long_history_transcript(z0p, oracle, gpu_ctx):
+    """The commitment's transcript steps run on the device from a state with
+    chunks already pushed (stack, counters and block cache handed over)."""
+    values = _values(1 << 10, 5)
+    pz, po = _pair(z0p, oracle, 8, 12, 8, 4, 2)
+    tg, to = z0p.Transcript(b"pcs/long"), oracle.Transcript(b"pcs/long")
+    pad = bytes((7 * i + 3) % 251 for i in range(5000))
+    for t in (tg, to):
+        t.absorb(b"pad", pad)
+        t.absorb(b"pad2", pad[:77])
+    st = z0p.fri.commit(values, pz, tg, gpu_ctx)
+    so = oracle.fri_commit(po, 0, values, to)
+    assert tg.export() == to.export()
+    assert z0p.fri.open(st, tg) == oracle.fri_open(so, to)
     assert tg.export() == to.export()
 
 

@@ -371,6 +371,7 @@ __global__ void __launch_bounds__(512) ntt_pass2_kernel(const uint32_t* __restri
 }
 
 #include "ntt_reg.cuh"
+#include "transcript.cuh"
 
 // Per coset j: 1 / (x^N - 1) with x^N = 31^N * omega_B^j (constant on the
 // coset), in Montgomery form, the same value times 2^32 once more, and the
@@ -1421,8 +1422,9 @@ __global__ void __launch_bounds__(64) fold_openings_kernel(const FoldStepDev* st
 // fold_values (src/fri.rs:1311-1331): A + x^-1 (r0 B + x^-1 (r1 C + x^-1 r2 D))
 // with B, C, D the quarter-scaled differences; the 1/4 is folded into the
 // challenge tables (r_k / 4), so only the mean is halved twice here.
+using FoldTab = uint32_t[3][4][4];
 __device__ __forceinline__ E4 fold_quad(const E4& q0, const E4& q1, const E4& q2, const E4& q3,
-                                        uint32_t xinv_m, const FoldArgs& a) {
+                                        uint32_t xinv_m, const FoldArgs& a, const FoldTab& tab) {
   E4 s01 = e4_add(q0, q1), s23 = e4_add(q2, q3);
   E4 odd_diff = e4_sub(q0, q1);
   E4 skew_u = e4_mul_base(e4_sub_lazy(q2, q3), a.unit_m);
@@ -1430,11 +1432,10 @@ __device__ __forceinline__ E4 fold_quad(const E4& q0, const E4& q1, const E4& q2
   E4 odd4 = e4_sub(odd_diff, skew_u);
   E4 even4 = e4_sub(s01, s23);
   E4 skew4 = e4_add(odd_diff, skew_u);
-  const ProofConsts& pc = g_consts[a.slot];
   // The Horner sums only feed the next product by x^-1: left unreduced.
-  E4 acc = e4_add_lazy(e4_mul_base(e4_mul_tab(skew4, pc.tab[2]), xinv_m),
-                       e4_mul_tab(even4, pc.tab[1]));
-  acc = e4_add_lazy(e4_mul_base(acc, xinv_m), e4_mul_tab(odd4, pc.tab[0]));
+  E4 acc = e4_add_lazy(e4_mul_base(e4_mul_tab(skew4, tab[2]), xinv_m),
+                       e4_mul_tab(even4, tab[1]));
+  acc = e4_add_lazy(e4_mul_base(acc, xinv_m), e4_mul_tab(odd4, tab[0]));
   return e4_add(mean, e4_mul_base(acc, xinv_m));
 }
 
@@ -1457,7 +1458,15 @@ __device__ __forceinline__ void fold_for_proof(FoldArgs& a) {
   if (a.cap) a.cap += pk * a.cap_stride;
   if (a.counter) a.counter += pk;
   if (a.final_vals) a.final_vals += pk * a.final_stride;
-  a.slot += pk;
+  a.tab += pk * kFoldTabWords;
+}
+
+// The fold's challenge tables, staged once per CTA: every thread reads all
+// of them, and they were written by an earlier launch (device transcript or
+// host).
+__device__ __forceinline__ void stage_fold_tab(const FoldArgs& a, FoldTab& t) {
+  for (uint32_t i = threadIdx.x; i < kFoldTabWords; i += blockDim.x) (&t[0][0][0])[i] = a.tab[i];
+  __syncthreads();
 }
 
 // kFinish: the launch may finish a small tree in its last CTA (a.counter);
@@ -1467,7 +1476,9 @@ template <bool kFinish>
 __global__ void __launch_bounds__(kFoldThreads) fri_fold_leaf_kernel(FoldArgs a, Tables tb) {
   // The next layer's subtree (small trees), then the roots of all CTAs.
   __shared__ uint32_t sm[2 * kTopStride * (kFinish ? kFuseMaxLeaves / kFoldThreads : kFoldThreads)];
+  __shared__ FoldTab tab;
   fold_for_proof(a);
+  stage_fold_tab(a, tab);
   if (!kFinish) a.counter = nullptr;
   const uint64_t nleaf = 1ull << (a.logn - 4);
   const uint64_t first = (uint64_t)blockIdx.x * kFoldThreads;
@@ -1488,7 +1499,7 @@ __global__ void __launch_bounds__(kFoldThreads) fri_fold_leaf_kernel(FoldArgs a,
       q[i].c[0] = v.x; q[i].c[1] = v.y; q[i].c[2] = v.z; q[i].c[3] = v.w;
     }
     uint32_t P = (uint32_t)(4 * Pn + t);
-    E4 r = fold_quad(q[0], q[1], q[2], q[3], quad_xinv(tb, a, P), a);
+    E4 r = fold_quad(q[0], q[1], q[2], q[3], quad_xinv(tb, a, P), a, tab);
 #pragma unroll
     for (int c = 0; c < 4; c++) leaf[4 * t + c] = r.c[c];
   }
@@ -1517,7 +1528,9 @@ __global__ void __launch_bounds__(kFoldThreads) fri_fold_leaf_kernel(FoldArgs a,
 constexpr int kFold4Threads = 4 * kFoldThreads;
 __global__ void __launch_bounds__(kFold4Threads) fri_fold_quad_kernel(FoldArgs a, Tables tb) {
   __shared__ uint32_t sm[2 * kTopStride * (kFuseMaxLeaves / kFoldThreads)];
+  __shared__ FoldTab tab;
   fold_for_proof(a);
+  stage_fold_tab(a, tab);
   const uint64_t nleaf = 1ull << (a.logn - 4);
   const uint64_t first = (uint64_t)blockIdx.x * kFoldThreads;
   const uint32_t avail = nleaf < (uint64_t)kFoldThreads ? (uint32_t)nleaf : (uint32_t)kFoldThreads;
@@ -1532,7 +1545,7 @@ __global__ void __launch_bounds__(kFold4Threads) fri_fold_quad_kernel(FoldArgs a
       uint4 v = __ldcs(src + i);
       q[i].c[0] = v.x; q[i].c[1] = v.y; q[i].c[2] = v.z; q[i].c[3] = v.w;
     }
-    const E4 f = fold_quad(q[0], q[1], q[2], q[3], quad_xinv(tb, a, (uint32_t)(4 * Pn + tq)), a);
+    const E4 f = fold_quad(q[0], q[1], q[2], q[3], quad_xinv(tb, a, (uint32_t)(4 * Pn + tq)), a, tab);
 #pragma unroll
     for (int c = 0; c < 4; c++) r[c] = f.c[c];
     const uint4 o = make_uint4(r[0], r[1], r[2], r[3]);
@@ -1563,7 +1576,9 @@ __global__ void __launch_bounds__(kFold4Threads) fri_fold_quad_kernel(FoldArgs a
 
 // Thread per next-layer value (small layers; leaves hashed separately).
 __global__ void fri_fold_plain_kernel(FoldArgs a, Tables tb) {
+  __shared__ FoldTab tab;
   fold_for_proof(a);
+  stage_fold_tab(a, tab);
   uint32_t P = blockIdx.x * blockDim.x + threadIdx.x;
   if (P >= (1u << (a.logn - 2))) return;
   E4 q[4];
@@ -1572,7 +1587,7 @@ __global__ void fri_fold_plain_kernel(FoldArgs a, Tables tb) {
     uint4 v = reinterpret_cast<const uint4*>(a.in)[4 * P + i];
     q[i].c[0] = v.x; q[i].c[1] = v.y; q[i].c[2] = v.z; q[i].c[3] = v.w;
   }
-  E4 r = fold_quad(q[0], q[1], q[2], q[3], quad_xinv(tb, a, P), a);
+  E4 r = fold_quad(q[0], q[1], q[2], q[3], quad_xinv(tb, a, P), a, tab);
   reinterpret_cast<uint4*>(a.out)[P] = make_uint4(r.c[0], r.c[1], r.c[2], r.c[3]);
   if (a.final_vals)
     reinterpret_cast<uint4*>(a.final_vals)[P] = make_uint4(r.c[0], r.c[1], r.c[2], r.c[3]);
@@ -1594,7 +1609,7 @@ constexpr uint64_t kGrindChunk = (uint64_t)kGrindThreads * kGrindPerThread;
 // [3] CTAs finished. The last CTA to finish copies {best, status} to `out`
 // and puts the state back to {~0, 0, 0, 0} for the next launch.
 struct GrindArgs {
-  uint32_t slot;  // ProofConsts slot: the head
+  const uint32_t* head;  // proof k's head at head + k * kPowHeadWords
   uint32_t bits;
   unsigned long long* state;
   unsigned long long* out;
@@ -1619,13 +1634,19 @@ __device__ __forceinline__ void grind_finish(const GrindArgs& a) {
 constexpr uint32_t kPowHeadLen = 47;
 
 __global__ void __launch_bounds__(kGrindThreads) grind_kernel(GrindArgs a) {
-  a.slot += blockIdx.y;  // proof of the group: its head, search state and result
+  a.head += kPowHeadWords * blockIdx.y;  // proof of the group: its head, search state and result
   a.state += 4 * blockIdx.y;
   a.out += 2 * blockIdx.y;
   constexpr int W = kPowHeadLen / 4, SH = (kPowHeadLen % 4) * 8;
   static_assert(kPowHeadLen + 8 <= 64 && SH != 0, "head and nonce must fit one block");
   __shared__ unsigned long long s_chunk;
   __shared__ int s_stop;
+  __shared__ uint32_t s_head[W + 1];
+  if (threadIdx.x <= (unsigned)W) s_head[threadIdx.x] = a.head[threadIdx.x];
+  __syncthreads();
+  uint32_t head[W + 1];  // the head's words, kept in registers for every attempt
+#pragma unroll
+  for (int i = 0; i <= W; i++) head[i] = s_head[i];
   const volatile unsigned long long* best_p = a.state;
   for (;;) {
     if (threadIdx.x == 0) {
@@ -1654,8 +1675,8 @@ __global__ void __launch_bounds__(kGrindThreads) grind_kernel(GrindArgs a) {
       const uint32_t lo = (uint32_t)nonce, hi = (uint32_t)(nonce >> 32);
       uint32_t m[16];
 #pragma unroll
-      for (int i = 0; i < 16; i++) m[i] = i < W ? g_consts[a.slot].head[i] : 0u;
-      m[W] = g_consts[a.slot].head[W] | (lo << SH);
+      for (int i = 0; i < 16; i++) m[i] = i < W ? head[i] : 0u;
+      m[W] = head[W] | (lo << SH);
       m[W + 1] = (lo >> (32 - SH)) | (hi << SH);
       m[W + 2] = hi >> (32 - SH);
       uint32_t cv[8], o[8];
@@ -2341,13 +2362,31 @@ cudaError_t merkle_flat64_leaves(cudaStream_t st, const uint32_t* flat, uint64_t
 
 bool grind_supports(uint32_t head_len) { return head_len == kPowHeadLen; }
 
-cudaError_t grind(cudaStream_t st, uint32_t slot, uint32_t head_len, uint32_t bits,
+cudaError_t transcript(cudaStream_t st, const TranscriptArgs& a, uint32_t nproofs) {
+  if (!a.in || !a.out || nproofs == 0 || nproofs > 65535u || a.nops > kMaxTranscriptOps)
+    return cudaErrorInvalidValue;
+  for (uint32_t o = 0; o < a.nops; o++) {
+    const TranscriptOp& op = a.op[o];
+    if (op.label_len > kTrLabelMax) return cudaErrorInvalidValue;
+    if (op.kind == kTrAbsorb && (!op.src || op.len == 0 || op.len > kTrStage))
+      return cudaErrorInvalidValue;
+    if ((op.kind == kTrFoldTables || op.kind == kTrPowHead) && !op.dst) return cudaErrorInvalidValue;
+    if (op.kind == kTrPowHead && 40 + op.label_len > 4 * kPowHeadWords) return cudaErrorInvalidValue;
+    if (op.kind > kTrPowHead) return cudaErrorInvalidValue;
+  }
+  Stage stg("transcript", st);
+  stg.launched();
+  transcript_kernel<<<nproofs, 32, 0, st>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t grind(cudaStream_t st, const uint32_t* head, uint32_t head_len, uint32_t bits,
                   unsigned long long* state, unsigned long long* out, uint64_t max_nonces,
                   uint32_t nproofs) {
-  if (!grind_supports(head_len) || bits > 32 || slot + nproofs > (uint32_t)kConstSlots)
+  if (!grind_supports(head_len) || bits > 32 || !head || nproofs == 0 || nproofs > 65535u)
     return cudaErrorInvalidValue;
   GrindArgs a;
-  a.slot = slot;
+  a.head = head;
   a.bits = bits;
   a.state = state;
   a.out = out;
