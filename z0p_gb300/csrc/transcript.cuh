@@ -4,11 +4,13 @@
 // drawn where its commitments are made and the launches after them need no
 // host round trip.
 //
-// One warp per proof. Lane 0 does the hashing (a BLAKE3 stream is one chain
-// of compressions); the warp moves records and absorbed data between global
-// and shared memory. The record evolves exactly as the host's Transcript
-// (host.cpp) evolves the same state: the tail bytes, the chaining-value stack,
-// the chunk and byte counts, the squeeze counter and the block cache.
+// One warp per proof. A BLAKE3 stream is one chain of compressions, so lane 0
+// does every compression, its chaining values and block cache in registers
+// and its message blocks read from shared memory in 16-byte words; the warp
+// writes the framed messages into the tail in parallel and moves records and
+// absorbed data between global and shared memory. The record evolves exactly
+// as the host's Transcript (host.cpp) evolves the same state: tail bytes,
+// chaining-value stack, chunk and byte counts, squeeze counter, block cache.
 #pragma once
 
 namespace dtr {
@@ -17,19 +19,25 @@ constexpr uint32_t kChunk = 1024;
 constexpr uint32_t kTail = 2 * kChunk;
 constexpr uint32_t kStackMax = 54;
 
-// Block i of a chunk whose first len bytes are at p (4-byte aligned, inside
-// a record's tail), zero padded past len.
-__device__ __forceinline__ void chunk_block(const uint8_t* p, uint32_t len, uint32_t i,
-                                            uint32_t w[16]) {
-  const uint32_t off = 64 * i;
-  const uint32_t n = len - off < 64 ? len - off : 64;
-  const uint32_t* q = reinterpret_cast<const uint32_t*>(p + off);
+// Block b of a tail chunk, all 64 bytes present (16-byte aligned in shared
+// memory).
+__device__ __forceinline__ void full_block(const uint8_t* chunk, uint32_t b, uint32_t w[16]) {
+  const uint4* q = reinterpret_cast<const uint4*>(chunk + 64 * b);
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    const uint4 v = q[i];
+    w[4 * i] = v.x; w[4 * i + 1] = v.y; w[4 * i + 2] = v.z; w[4 * i + 3] = v.w;
+  }
+}
+// The last block of a chunk holding len bytes (1..1024), zero padded.
+__device__ __forceinline__ void last_block(const uint8_t* chunk, uint32_t len, uint32_t w[16]) {
+  const uint32_t b = (len - 1) / 64, n = len - 64 * b;
+  full_block(chunk, b, w);  // reads stay inside the 2048-byte tail
 #pragma unroll
   for (int j = 0; j < 16; j++) {
     const int rem = (int)n - 4 * j;
-    uint32_t v = rem > 0 ? q[j] : 0u;
-    if (rem > 0 && rem < 4) v &= (1u << (8 * rem)) - 1u;
-    w[j] = v;
+    if (rem <= 0) w[j] = 0u;
+    else if (rem < 4) w[j] &= (1u << (8 * rem)) - 1u;
   }
 }
 
@@ -38,13 +46,15 @@ __device__ __forceinline__ void compress(const uint32_t cv[8], uint32_t w[16], u
   blake3_compress(cv, w, (uint32_t)counter, (uint32_t)(counter >> 32), len, flags, out);
 }
 
-__device__ __forceinline__ void load8(const uint8_t* p, uint32_t v[8]) {
-  const uint32_t* q = reinterpret_cast<const uint32_t*>(p);
+// Chaining values in a record are 4-byte aligned (the stack starts at byte
+// 2052 of the state).
+__device__ __forceinline__ void load8(const void* p, uint32_t v[8]) {
+  const uint32_t* q = static_cast<const uint32_t*>(p);
 #pragma unroll
   for (int i = 0; i < 8; i++) v[i] = q[i];
 }
-__device__ __forceinline__ void store8(uint8_t* p, const uint32_t v[8]) {
-  uint32_t* q = reinterpret_cast<uint32_t*>(p);
+__device__ __forceinline__ void store8(void* p, const uint32_t v[8]) {
+  uint32_t* q = static_cast<uint32_t*>(p);
 #pragma unroll
   for (int i = 0; i < 8; i++) q[i] = v[i];
 }
@@ -62,143 +72,189 @@ __device__ __forceinline__ void parent(const uint32_t l[8], const uint32_t r[8],
   compress(iv, w, 0ull, 64u, flags, out);
 }
 
-// Hasher::push_merged (src/hash.rs:305-318).
-__device__ void push_merged(DevTranscript& T, const uint32_t cv[8]) {
-  z0p_transcript_state& s = T.st;
-  store8(s.stack[s.stack_len++], cv);
-  s.next_index++;
-  for (uint64_t total = s.next_index; (total & 1ull) == 0; total >>= 1) {
-    uint32_t l[8], r[8], m[8];
-    load8(s.stack[s.stack_len - 2], l);
-    load8(s.stack[s.stack_len - 1], r);
-    parent(l, r, kParent, m);
-    s.stack_len--;
-    store8(s.stack[s.stack_len - 1], m);
+// The hasher's block cache in registers: cv[h] is tail chunk h after its
+// first nb[h] blocks.
+struct Cache {
+  uint32_t cv[2][8];
+  uint32_t nb[2];
+};
+__device__ __forceinline__ void load_cache(const DevTranscript& T, Cache& c) {
+#pragma unroll
+  for (int h = 0; h < 2; h++) {
+    load8(T.cv[h], c.cv[h]);
+    c.nb[h] = T.nblk[h];
+  }
+}
+__device__ __forceinline__ void store_cache(DevTranscript& T, const Cache& c) {
+#pragma unroll
+  for (int h = 0; h < 2; h++) {
+    store8(T.cv[h], c.cv[h]);
+    T.nblk[h] = c.nb[h];
   }
 }
 
-// Folds into cv[h] every block of tail chunk h that has a byte after it in
-// its chunk (such a block is never its chunk's last, so its compression is
-// final), as the host hasher's cache does.
-__device__ void advance(DevTranscript& T) {
-  for (uint32_t h = 0; h < 2; h++) {
+// Folds into the cache every block of the tail (tail_len bytes) that has a
+// byte after it in its chunk: such a block is never its chunk's last, so its
+// compression (CHUNK_START or no flag, counter = chunk index) is final.
+__device__ __forceinline__ void advance(const uint8_t* tail, uint32_t tail_len, uint64_t next_index,
+                                        Cache& c) {
+#pragma unroll
+  for (int h = 0; h < 2; h++) {
     const uint32_t base = kChunk * h;
-    if (T.st.tail_len <= base) break;
-    const uint32_t len = T.st.tail_len - base < kChunk ? T.st.tail_len - base : kChunk;
-    while (64 * (T.nblk[h] + 1) < len) {
+    if (tail_len <= base) break;
+    const uint32_t len = tail_len - base < kChunk ? tail_len - base : kChunk;
+    while (64 * (c.nb[h] + 1) < len) {
       uint32_t w[16];
-      chunk_block(T.st.tail + base, len, T.nblk[h], w);
-      compress(T.cv[h], w, T.st.next_index + h, 64u, T.nblk[h] == 0 ? kChunkStart : 0u, T.cv[h]);
-      T.nblk[h]++;
+      full_block(tail + base, c.nb[h], w);
+      compress(c.cv[h], w, next_index + h, 64u, c.nb[h] == 0 ? kChunkStart : 0u, c.cv[h]);
+      c.nb[h]++;
     }
   }
 }
 
-// Hasher::update (src/hash.rs:256-272); data in any address space.
-__device__ void update(DevTranscript& T, const uint8_t* data, uint32_t len) {
+// Hasher::push_merged (src/hash.rs:305-318) on the record's stack.
+__device__ __forceinline__ void push_merged(DevTranscript& T, uint32_t cv[8]) {
   z0p_transcript_state& s = T.st;
-  s.total_len += len;
-  while (len) {
-    const uint32_t room = kTail - s.tail_len;
-    const uint32_t take = len < room ? len : room;
-    for (uint32_t i = 0; i < take; i++) s.tail[s.tail_len + i] = data[i];
-    s.tail_len += take;
-    data += take;
-    len -= take;
-    advance(T);
-    if (s.tail_len == kTail) {
-      // Blocks 0..14 of the first chunk are folded; its last block ends it.
-      uint32_t w[16], out[8];
-      chunk_block(s.tail, kChunk, 15, w);
-      compress(T.cv[0], w, s.next_index, 64u, kChunkEnd, out);
-      push_merged(T, out);
-      uint32_t* tw = reinterpret_cast<uint32_t*>(s.tail);
-      for (uint32_t i = 0; i < kChunk / 4; i++) tw[i] = tw[kChunk / 4 + i];
-      s.tail_len = kChunk;
-#pragma unroll
-      for (int i = 0; i < 8; i++) {
-        T.cv[0][i] = T.cv[1][i];
-      }
-      T.nblk[0] = T.nblk[1];
-      iv_words(T.cv[1]);
-      T.nblk[1] = 0;
-    }
+  uint32_t sl = s.stack_len;
+  const uint64_t n = s.next_index + 1;
+  for (uint64_t total = n; (total & 1ull) == 0; total >>= 1) {
+    uint32_t l[8];
+    load8(s.stack[--sl], l);
+    parent(l, cv, kParent, cv);
   }
+  store8(s.stack[sl++], cv);
+  s.stack_len = sl;
+  s.next_index = n;
 }
 
-__device__ __forceinline__ void update_u64(DevTranscript& T, uint64_t v) {
-  uint8_t b[8];
-#pragma unroll
-  for (int i = 0; i < 8; i++) b[i] = (uint8_t)(v >> (8 * i));
-  update(T, b, 8);
-}
-
-// Hasher::finalize (src/hash.rs:276-302), leaving the record unchanged.
-__device__ void finalize(const DevTranscript& T, uint32_t out[8]) {
+// Hasher::finalize (src/hash.rs:276-302) of the record's stack with a tail of
+// tail_len bytes and the cache c, without changing either.
+__device__ __forceinline__ void finalize(const DevTranscript& T, uint32_t tail_len,
+                                         uint64_t total_len, const Cache& c, uint32_t out[8]) {
   const z0p_transcript_state& s = T.st;
-  uint32_t iv[8];
-  iv_words(iv);
-  if (s.total_len == 0) {
-    uint32_t w[16];
+  if (total_len == 0) {
+    uint32_t w[16], iv[8];
 #pragma unroll
     for (int i = 0; i < 16; i++) w[i] = 0u;
+    iv_words(iv);
     compress(iv, w, 0ull, 0u, kChunkStart | kChunkEnd | kRoot, out);
     return;
   }
-  const uint32_t tl = s.tail_len;
   uint32_t sl = s.stack_len;
   uint32_t top[8];
   bool have_top = false;  // virtual stack: stack[0..sl) and then top
-  uint32_t h = 0;
-  if (tl > kChunk) {
+  uint32_t cur[8];
+  if (tail_len > kChunk) {
+    // The first tail chunk ends here: merged as push_merged would, virtually.
     uint32_t w[16];
-    chunk_block(s.tail, kChunk, 15, w);
-    compress(T.cv[0], w, s.next_index, 64u, kChunkEnd, top);
+    full_block(s.tail, 15, w);
+    compress(c.cv[0], w, s.next_index, 64u, kChunkEnd, top);
     for (uint64_t total = s.next_index + 1; (total & 1ull) == 0; total >>= 1) {
       uint32_t l[8];
-      load8(s.stack[sl - 1], l);
+      load8(s.stack[--sl], l);
       parent(l, top, kParent, top);
-      sl--;
     }
     have_top = true;
-    h = 1;
+    const uint32_t len = tail_len - kChunk, last = (len - 1) / 64;
+    last_block(s.tail + kChunk, len, w);
+    compress(c.cv[1], w, s.next_index + 1, len - 64 * last,
+             (last == 0 ? kChunkStart : 0u) | kChunkEnd, cur);
+  } else {
+    uint32_t w[16];
+    const uint32_t len = tail_len, last = (len - 1) / 64;
+    last_block(s.tail, len, w);
+    compress(c.cv[0], w, s.next_index, len - 64 * last,
+             (last == 0 ? kChunkStart : 0u) | kChunkEnd | (sl == 0 ? kRoot : 0u), cur);
   }
-  const uint32_t len = tl - kChunk * h;
-  const uint32_t last = (len + 63) / 64 - 1;
   const uint32_t depth = sl + (have_top ? 1u : 0u);
-  uint32_t w[16], cur[8];
-  chunk_block(s.tail + kChunk * h, len, last, w);
-  const uint32_t flags =
-      (last == 0 ? kChunkStart : 0u) | kChunkEnd | (depth == 0 ? kRoot : 0u);
-  compress(T.cv[h], w, s.next_index + h, len - 64 * last, flags, cur);
   if (depth == 0) {
 #pragma unroll
     for (int i = 0; i < 8; i++) out[i] = cur[i];
     return;
   }
-  for (uint32_t i = depth - 1; i >= 1; i--) {
+  // Merge from the top of the virtual stack down; the bottom one is the root.
+  for (uint32_t i = depth - 1;; i--) {
     uint32_t l[8];
-    if (i < sl) load8(s.stack[i], l);
-    else
+    if (i < sl) {
+      load8(s.stack[i], l);
+    } else {
 #pragma unroll
       for (int j = 0; j < 8; j++) l[j] = top[j];
+    }
+    if (i == 0) {
+      parent(l, cur, kParent | kRoot, out);
+      return;
+    }
     parent(l, cur, kParent, cur);
   }
-  uint32_t l[8];
-  if (sl > 0) load8(s.stack[0], l);
-  else
-#pragma unroll
-    for (int j = 0; j < 8; j++) l[j] = top[j];
-  parent(l, cur, kParent | kRoot, out);
 }
 
-// Transcript::absorb (src/transcript.rs:72-77).
-__device__ void absorb(DevTranscript& T, const char* label, uint32_t llen, const uint8_t* data,
-                       uint32_t len) {
-  update_u64(T, llen);
-  update(T, reinterpret_cast<const uint8_t*>(label), llen);
-  update_u64(T, len);
-  update(T, data, len);
+// The bytes of framed messages, item after item: for each item,
+// LE64(|label|) || label || LE64(word) || data, where word = |data| for an
+// absorb (src/transcript.rs:72-77) and the squeeze counter, with no data, for
+// a squeeze's suffix (src/transcript.rs:162-171).
+struct Msg {
+  const char* label;
+  uint32_t llen;
+  uint64_t word;
+  const uint8_t* data;  // item j's bytes at data + j * dlen (shared memory)
+  uint32_t dlen;
+  uint32_t count;
+  __device__ __forceinline__ uint32_t size() const { return (16 + llen + dlen) * count; }
+  __device__ __forceinline__ uint8_t at(uint32_t i) const {
+    const uint32_t S = 16 + llen + dlen, j = i / S, o = i - j * S;
+    if (o < 8) return (uint8_t)((uint64_t)llen >> (8 * o));
+    if (o < 8 + llen) return (uint8_t)label[o - 8];
+    if (o < 16 + llen) return (uint8_t)(word >> (8 * (o - 8 - llen)));
+    return data[(size_t)j * dlen + (o - 16 - llen)];
+  }
+};
+
+// Hasher::update (src/hash.rs:256-272) of a message, with the warp. The tail
+// is filled in parallel up to two chunks; lane 0 then folds its finished
+// blocks, and when the tail is full, ends its first chunk and pushes it, and
+// the warp moves the second chunk down. Every lane must call it.
+__device__ void update(DevTranscript& T, const Msg& m) {
+  const uint32_t lane = threadIdx.x, n = m.size();
+  uint32_t done = 0;
+  while (done < n) {
+    __syncwarp();
+    const uint32_t tl = T.st.tail_len;
+    const uint32_t take = n - done < kTail - tl ? n - done : kTail - tl;
+    for (uint32_t i = lane; i < take; i += 32) T.st.tail[tl + i] = m.at(done + i);
+    __syncwarp();
+    int full = 0;
+    if (lane == 0) {
+      Cache c;
+      load_cache(T, c);
+      advance(T.st.tail, tl + take, T.st.next_index, c);
+      T.st.tail_len = tl + take;
+      T.st.total_len += take;
+      if (tl + take == kTail) {
+        // Blocks 0..14 of the first chunk are folded; its last block ends it.
+        uint32_t w[16], out[8];
+        full_block(T.st.tail, 15, w);
+        compress(c.cv[0], w, T.st.next_index, 64u, kChunkEnd, out);
+        push_merged(T, out);
+#pragma unroll
+        for (int i = 0; i < 8; i++) c.cv[0][i] = c.cv[1][i];
+        c.nb[0] = c.nb[1];
+        iv_words(c.cv[1]);
+        c.nb[1] = 0;
+        T.st.tail_len = kChunk;
+        full = 1;
+      }
+      store_cache(T, c);
+    }
+    full = __shfl_sync(0xffffffffu, full, 0);
+    if (full) {
+      __syncwarp();
+      uint4* t = reinterpret_cast<uint4*>(T.st.tail);
+      for (uint32_t i = lane; i < kChunk / 16; i += 32) t[i] = t[kChunk / 16 + i];
+    }
+    done += take;
+  }
+  __syncwarp();
 }
 
 // Copies `bytes` (a multiple of 16, both ends 16-byte aligned) with the warp.
@@ -218,26 +274,60 @@ __device__ __forceinline__ void warp_stage(uint8_t* dst, const uint8_t* src, uin
   }
 }
 
-// squeeze_raw (src/transcript.rs:162-171): the hash of a copy of the history
-// with the label and counter appended; the output is then absorbed. The warp
-// makes the copy; lane 0 hashes. Every lane must call it.
-__device__ void squeeze(DevTranscript& T, DevTranscript& C, const char* label, uint32_t llen,
-                        uint32_t out[8]) {
-  __syncwarp();
-  warp_copy16(&C, &T, sizeof(DevTranscript));
-  __syncwarp();
+// The meaningful part of a record (tail and stack in use, counters, cache).
+__device__ __forceinline__ void warp_clone(DevTranscript& C, const DevTranscript& T) {
+  const uint32_t tail16 = (T.st.tail_len + 15) / 16 * 16;
+  warp_copy16(C.st.tail, T.st.tail, tail16);
+  for (uint32_t i = threadIdx.x; i < 8 * T.st.stack_len; i += 32)
+    reinterpret_cast<uint32_t*>(C.st.stack)[i] = reinterpret_cast<const uint32_t*>(T.st.stack)[i];
   if (threadIdx.x == 0) {
-    update_u64(C, llen);
-    update(C, reinterpret_cast<const uint8_t*>(label), llen);
-    update_u64(C, T.st.counter);
+    C.st.tail_len = T.st.tail_len;
+    C.st.stack_len = T.st.stack_len;
+    C.st.next_index = T.st.next_index;
+    C.st.total_len = T.st.total_len;
+    C.st.counter = T.st.counter;
+  }
+  if (threadIdx.x < 16) (&C.cv[0][0])[threadIdx.x] = (&T.cv[0][0])[threadIdx.x];
+  if (threadIdx.x < 2) C.nblk[threadIdx.x] = T.nblk[threadIdx.x];
+  __syncwarp();
+}
+
+// squeeze_raw (src/transcript.rs:162-171): the hash of the history with the
+// label and counter appended, which is then absorbed. When the suffix fits
+// in the tail, it is written past the record's bytes and hashed from a copy
+// of the cache (the absorb that follows overwrites it); otherwise a copy of
+// the record is extended. Every lane must call it; lane 0 receives out.
+__device__ void squeeze(DevTranscript& T, DevTranscript& C, uint8_t* out_bytes, const char* label,
+                        uint32_t llen, uint32_t out[8]) {
+  const uint32_t lane = threadIdx.x;
+  __syncwarp();
+  const Msg suffix{label, llen, T.st.counter, nullptr, 0, 1};
+  const uint32_t S = suffix.size(), tl = T.st.tail_len;
+  if (tl + S < kTail) {
+    for (uint32_t i = lane; i < S; i += 32) T.st.tail[tl + i] = suffix.at(i);
+    __syncwarp();
+    if (lane == 0) {
+      Cache c;
+      load_cache(T, c);
+      advance(T.st.tail, tl + S, T.st.next_index, c);
+      finalize(T, tl + S, T.st.total_len + S, c, out);
+    }
+  } else {
+    warp_clone(C, T);
+    update(C, suffix);
+    if (lane == 0) {
+      Cache c;
+      load_cache(C, c);
+      finalize(C, C.st.tail_len, C.st.total_len, c, out);
+    }
+  }
+  if (lane == 0) {
     T.st.counter++;
-    finalize(C, out);
-    uint8_t b[32];
 #pragma unroll
-    for (int i = 0; i < 32; i++) b[i] = (uint8_t)(out[i / 4] >> (8 * (i % 4)));
-    absorb(T, label, llen, b, 32);
+    for (int i = 0; i < 8; i++) reinterpret_cast<uint32_t*>(out_bytes)[i] = out[i];
   }
   __syncwarp();
+  update(T, Msg{label, llen, 32, out_bytes, 32, 1});
 }
 
 }  // namespace dtr
@@ -247,12 +337,13 @@ __global__ void __launch_bounds__(32) transcript_kernel(const __grid_constant__ 
   __shared__ __align__(16) DevTranscript T;
   __shared__ __align__(16) DevTranscript C;
   __shared__ __align__(16) uint8_t stage[kTrStage];
+  __shared__ __align__(16) uint8_t sq[32];
   const uint32_t k = blockIdx.x, lane = threadIdx.x;
   dtr::warp_copy16(&T, a.in + k, sizeof(DevTranscript));
   __syncwarp();
-  // A record the hasher could run out of bounds on is left alone.
-  // (The stack holds one value per set bit of the chunk count, so it never
-  // outgrows a consistent record.)
+  // A record the hasher could run out of bounds on is left alone. (The stack
+  // holds one value per set bit of the chunk count, so it never outgrows a
+  // consistent record.)
   if (T.st.tail_len >= dtr::kTail || T.st.stack_len > dtr::kStackMax ||
       (uint32_t)__popcll(T.st.next_index) != T.st.stack_len || (T.st.next_index >> 53) != 0 ||
       T.nblk[0] > 15 || T.nblk[1] > 15) {
@@ -273,55 +364,59 @@ __global__ void __launch_bounds__(32) transcript_kernel(const __grid_constant__ 
         __syncwarp();
         dtr::warp_stage(stage, src + (size_t)i0 * op.len, n * op.len);
         __syncwarp();
-        if (lane == 0)
-          for (uint32_t i = 0; i < n; i++)
-            dtr::absorb(T, op.label, op.label_len, stage + (size_t)i * op.len, op.len);
+        dtr::update(T, dtr::Msg{op.label, op.label_len, op.len, stage, op.len, n});
       }
     } else if (op.kind == kTrFoldTables) {
       // challenge_ext x 3 (src/transcript.rs:136-141), then the tables of
-      // r_k / 4 for e4_mul_tab: T[c][i] holds the coefficient of input
-      // coordinate i in output coordinate c, times 2^32 (Montgomery).
+      // r_k / 4 for e4_mul_tab.
       uint32_t ch[3][4];
+#pragma unroll
       for (int r = 0; r < 3; r++) {
-        uint32_t d[8];
-        dtr::squeeze(T, C, op.label, op.label_len, d);
+        uint32_t d[8] = {};
+        dtr::squeeze(T, C, sq, op.label, op.label_len, d);
 #pragma unroll
-        for (int e = 0; e < 4; e++) ch[r][e] = d[e] % kP;
+        for (int e = 0; e < 4; e++) ch[r][e] = __shfl_sync(0xffffffffu, d[e] % kP, 0);
       }
-      // Lane 0 drew the challenges; the 48 table words are spread over the
-      // warp (lanes 0..15 each write table r's word for r = 0, 1, 2).
-#pragma unroll
-      for (int r = 0; r < 3; r++)
-#pragma unroll
-        for (int e = 0; e < 4; e++) ch[r][e] = __shfl_sync(0xffffffffu, ch[r][e], 0);
       if (lane < 16) {
         // Product by q in the tower (src/ext4.rs:106-117, u^2 = 11): output
         // coordinate c takes input coordinate i times q[kIdx], times 11
-        // where kW11 says so.
-        constexpr uint8_t kIdx[16] = {0, 1, 3, 2, 1, 0, 2, 3, 2, 3, 0, 1, 3, 2, 1, 0};
-        constexpr uint8_t kW11[16] = {0, 1, 1, 1, 0, 0, 0, 1, 0, 1, 0, 1, 0, 0, 0, 0};
+        // where kW11 says so; word 4c + i of each table.
+        const uint32_t e = (0x0123103232012310ull >> (4 * lane)) & 0xfu;  // kIdx[lane]
+        const bool w11 = (0x0a8eu >> lane) & 1u;                            // kW11[lane]
         const uint32_t inv4 = 1509949441u;  // 4^-1 mod p
 #pragma unroll
         for (int r = 0; r < 3; r++) {
-          uint64_t v = (uint64_t)ch[r][kIdx[lane]] * inv4 % kP;
-          if (kW11[lane]) v = 11ull * v % kP;
+          const uint32_t q = e == 0 ? ch[r][0] : e == 1 ? ch[r][1] : e == 2 ? ch[r][2] : ch[r][3];
+          uint64_t v = (uint64_t)q * inv4 % kP;
+          if (w11) v = 11ull * v % kP;
           op.dst[k * op.dst_stride + 16 * r + lane] = to_mont((uint32_t)v);
         }
       }
     } else if (op.kind == kTrPowHead) {
+      // H(history) || LE64(|label|) || label, as little-endian words.
+      uint32_t d[8] = {};
       if (lane == 0) {
-        uint32_t d[8];
-        dtr::finalize(T, d);
-        uint8_t head[64];
-        for (int i = 0; i < 64; i++) head[i] = 0;
-        for (int i = 0; i < 32; i++) head[i] = (uint8_t)(d[i / 4] >> (8 * (i % 4)));
-        for (int i = 0; i < 8; i++) head[32 + i] = (uint8_t)((uint64_t)op.label_len >> (8 * i));
-        for (uint32_t i = 0; i < op.label_len && 40 + i < 64; i++) head[40 + i] = (uint8_t)op.label[i];
-        uint32_t* dst = op.dst + k * op.dst_stride;
-        for (int i = 0; i < 16; i++)
-          dst[i] = (uint32_t)head[4 * i] | ((uint32_t)head[4 * i + 1] << 8) |
-                   ((uint32_t)head[4 * i + 2] << 16) | ((uint32_t)head[4 * i + 3] << 24);
+        dtr::Cache c;
+        dtr::load_cache(T, c);
+        dtr::finalize(T, T.st.tail_len, T.st.total_len, c, d);
       }
+      uint32_t v = 0;
+#pragma unroll
+      for (int i = 0; i < 8; i++) {
+        const uint32_t di = __shfl_sync(0xffffffffu, d[i], 0);
+        if ((uint32_t)i == lane) v = di;
+      }
+      if (lane >= 8 && lane < kPowHeadWords) {
+        v = 0;
+        for (uint32_t b = 0; b < 4; b++) {
+          const uint32_t at = 4 * lane + b;  // byte of the head, 32 and up
+          uint32_t x = 0;
+          if (at < 40) x = (uint32_t)((uint64_t)op.label_len >> (8 * (at - 32)));
+          else if (at < 40 + op.label_len) x = (uint8_t)op.label[at - 40];
+          v |= (x & 0xffu) << (8 * b);
+        }
+      }
+      if (lane < kPowHeadWords) op.dst[k * op.dst_stride + lane] = v;
     }
     __syncwarp();
   }
