@@ -1699,7 +1699,7 @@ __global__ void __launch_bounds__(256) coset_to_natural_kernel(const uint32_t* _
                                                                uint32_t* __restrict__ out,
                                                                uint32_t logN, uint32_t logB) {
   __shared__ uint32_t tile[32][kNatTileQ + 1];
-  const uint64_t n = 1ull << logN, B = 1ull << logB, m = n << logB;
+  const uint64_t n = 1ull << logN, m = n << logB;
   const uint64_t q0 = (uint64_t)blockIdx.x * kNatTileQ, j0 = (uint64_t)blockIdx.y * 32;
   const uint32_t ltj = logB < 5 ? logB : 5, tj = 1u << ltj;  // B - j0 >= 32 whenever B > 32
   const uint32_t tq = (uint32_t)(n - q0 < kNatTileQ ? n - q0 : kNatTileQ);

@@ -5,8 +5,8 @@
 // host round trip.
 //
 // One warp per proof. A BLAKE3 stream is one chain of compressions, so lane 0
-// does every compression, its chaining values and block cache in registers
-// and its message blocks read from shared memory in 16-byte words; the warp
+// does every compression, through one non-inlined routine reading its block
+// straight from the record's tail in shared memory; the warp
 // writes the framed messages into the tail in parallel and moves records and
 // absorbed data between global and shared memory. The record evolves exactly
 // as the host's Transcript (host.cpp) evolves the same state: tail bytes,
@@ -19,49 +19,26 @@ constexpr uint32_t kChunk = 1024;
 constexpr uint32_t kTail = 2 * kChunk;
 constexpr uint32_t kStackMax = 54;
 
-// Block b of a tail chunk, all 64 bytes present (16-byte aligned in shared
-// memory).
-__device__ __forceinline__ void full_block(const uint8_t* chunk, uint32_t b, uint32_t w[16]) {
-  const uint4* q = reinterpret_cast<const uint4*>(chunk + 64 * b);
+// The one copy of the compression in this kernel: a single warp runs through
+// the hasher's straight-line code once, so every inlined copy would be
+// fetched cold; this one stays in the instruction cache. Chaining values and
+// blocks come by pointer (shared or local memory, 4-byte aligned); out may
+// alias cv.
+__device__ __noinline__ void compress_at(const uint32_t* cv, const uint32_t* w, uint64_t counter,
+                                         uint32_t len, uint32_t flags, uint32_t* out) {
+  uint32_t c[8], m[16], o[8];
 #pragma unroll
-  for (int i = 0; i < 4; i++) {
-    const uint4 v = q[i];
-    w[4 * i] = v.x; w[4 * i + 1] = v.y; w[4 * i + 2] = v.z; w[4 * i + 3] = v.w;
-  }
-}
-// The last block of a chunk holding len bytes (1..1024), zero padded.
-__device__ __forceinline__ void last_block(const uint8_t* chunk, uint32_t len, uint32_t w[16]) {
-  const uint32_t b = (len - 1) / 64, n = len - 64 * b;
-  full_block(chunk, b, w);  // reads stay inside the 2048-byte tail
+  for (int i = 0; i < 8; i++) c[i] = cv[i];
 #pragma unroll
-  for (int j = 0; j < 16; j++) {
-    const int rem = (int)n - 4 * j;
-    if (rem <= 0) w[j] = 0u;
-    else if (rem < 4) w[j] &= (1u << (8 * rem)) - 1u;
-  }
-}
-
-__device__ __forceinline__ void compress(const uint32_t cv[8], uint32_t w[16], uint64_t counter,
-                                         uint32_t len, uint32_t flags, uint32_t out[8]) {
-  blake3_compress(cv, w, (uint32_t)counter, (uint32_t)(counter >> 32), len, flags, out);
-}
-
-// Chaining values in a record are 4-byte aligned (the stack starts at byte
-// 2052 of the state).
-__device__ __forceinline__ void load8(const void* p, uint32_t v[8]) {
-  const uint32_t* q = static_cast<const uint32_t*>(p);
+  for (int i = 0; i < 16; i++) m[i] = w[i];
+  blake3_compress(c, m, (uint32_t)counter, (uint32_t)(counter >> 32), len, flags, o);
 #pragma unroll
-  for (int i = 0; i < 8; i++) v[i] = q[i];
-}
-__device__ __forceinline__ void store8(void* p, const uint32_t v[8]) {
-  uint32_t* q = static_cast<uint32_t*>(p);
-#pragma unroll
-  for (int i = 0; i < 8; i++) q[i] = v[i];
+  for (int i = 0; i < 8; i++) out[i] = o[i];
 }
 
 // Parent node of two chaining values (src/hash.rs:161-176).
-__device__ __forceinline__ void parent(const uint32_t l[8], const uint32_t r[8], uint32_t flags,
-                                       uint32_t out[8]) {
+__device__ __noinline__ void parent_at(const uint32_t* l, const uint32_t* r, uint32_t flags,
+                                       uint32_t* out) {
   uint32_t w[16], iv[8];
 #pragma unroll
   for (int i = 0; i < 8; i++) {
@@ -69,123 +46,110 @@ __device__ __forceinline__ void parent(const uint32_t l[8], const uint32_t r[8],
     w[8 + i] = r[i];
   }
   iv_words(iv);
-  compress(iv, w, 0ull, 64u, flags, out);
+  compress_at(iv, w, 0ull, 64u, flags, out);
 }
 
-// The hasher's block cache in registers: cv[h] is tail chunk h after its
-// first nb[h] blocks.
+// The hasher's block cache: cv[h] is tail chunk h after its first nb[h]
+// blocks (laid out as DevTranscript's cv and nblk).
 struct Cache {
   uint32_t cv[2][8];
   uint32_t nb[2];
 };
-__device__ __forceinline__ void load_cache(const DevTranscript& T, Cache& c) {
-#pragma unroll
-  for (int h = 0; h < 2; h++) {
-    load8(T.cv[h], c.cv[h]);
-    c.nb[h] = T.nblk[h];
-  }
+__device__ __forceinline__ Cache& cache_of(DevTranscript& T) {
+  return *reinterpret_cast<Cache*>(&T.cv[0][0]);
 }
-__device__ __forceinline__ void store_cache(DevTranscript& T, const Cache& c) {
-#pragma unroll
-  for (int h = 0; h < 2; h++) {
-    store8(T.cv[h], c.cv[h]);
-    T.nblk[h] = c.nb[h];
-  }
-}
+static_assert(offsetof(DevTranscript, nblk) == offsetof(DevTranscript, cv) + offsetof(Cache, nb),
+              "the cache fields are laid out as Cache");
 
 // Folds into the cache every block of the tail (tail_len bytes) that has a
 // byte after it in its chunk: such a block is never its chunk's last, so its
 // compression (CHUNK_START or no flag, counter = chunk index) is final.
-__device__ __forceinline__ void advance(const uint8_t* tail, uint32_t tail_len, uint64_t next_index,
-                                        Cache& c) {
-#pragma unroll
-  for (int h = 0; h < 2; h++) {
+__device__ __noinline__ void advance(const uint8_t* tail, uint32_t tail_len, uint64_t next_index,
+                                     Cache& c) {
+  for (uint32_t h = 0; h < 2; h++) {
     const uint32_t base = kChunk * h;
     if (tail_len <= base) break;
     const uint32_t len = tail_len - base < kChunk ? tail_len - base : kChunk;
     while (64 * (c.nb[h] + 1) < len) {
-      uint32_t w[16];
-      full_block(tail + base, c.nb[h], w);
-      compress(c.cv[h], w, next_index + h, 64u, c.nb[h] == 0 ? kChunkStart : 0u, c.cv[h]);
+      const uint32_t* blk = reinterpret_cast<const uint32_t*>(tail + base + 64 * c.nb[h]);
+      compress_at(c.cv[h], blk, next_index + h, 64u, c.nb[h] == 0 ? kChunkStart : 0u, c.cv[h]);
       c.nb[h]++;
     }
   }
 }
 
 // Hasher::push_merged (src/hash.rs:305-318) on the record's stack.
-__device__ __forceinline__ void push_merged(DevTranscript& T, uint32_t cv[8]) {
+__device__ __noinline__ void push_merged(DevTranscript& T, uint32_t* cv) {
   z0p_transcript_state& s = T.st;
   uint32_t sl = s.stack_len;
   const uint64_t n = s.next_index + 1;
   for (uint64_t total = n; (total & 1ull) == 0; total >>= 1) {
-    uint32_t l[8];
-    load8(s.stack[--sl], l);
-    parent(l, cv, kParent, cv);
+    --sl;
+    parent_at(reinterpret_cast<const uint32_t*>(s.stack[sl]), cv, kParent, cv);
   }
-  store8(s.stack[sl++], cv);
+  uint32_t* dst = reinterpret_cast<uint32_t*>(s.stack[sl++]);
+  for (int i = 0; i < 8; i++) dst[i] = cv[i];
   s.stack_len = sl;
   s.next_index = n;
 }
 
+// The last block of a chunk holding len bytes (1..1024), zero padded.
+__device__ __forceinline__ void last_block(const uint8_t* chunk, uint32_t len, uint32_t w[16]) {
+  const uint32_t b = (len - 1) / 64, n = len - 64 * b;
+  const uint32_t* q = reinterpret_cast<const uint32_t*>(chunk + 64 * b);
+  for (int j = 0; j < 16; j++) {
+    const int rem = (int)n - 4 * j;
+    w[j] = rem <= 0 ? 0u : rem < 4 ? q[j] & ((1u << (8 * rem)) - 1u) : q[j];
+  }
+}
+
 // Hasher::finalize (src/hash.rs:276-302) of the record's stack with a tail of
 // tail_len bytes and the cache c, without changing either.
-__device__ __forceinline__ void finalize(const DevTranscript& T, uint32_t tail_len,
-                                         uint64_t total_len, const Cache& c, uint32_t out[8]) {
+__device__ __noinline__ void finalize(const DevTranscript& T, uint32_t tail_len,
+                                      uint64_t total_len, const Cache& c, uint32_t* out) {
   const z0p_transcript_state& s = T.st;
+  uint32_t w[16], iv[8];
+  iv_words(iv);
   if (total_len == 0) {
-    uint32_t w[16], iv[8];
-#pragma unroll
     for (int i = 0; i < 16; i++) w[i] = 0u;
-    iv_words(iv);
-    compress(iv, w, 0ull, 0u, kChunkStart | kChunkEnd | kRoot, out);
+    compress_at(iv, w, 0ull, 0u, kChunkStart | kChunkEnd | kRoot, out);
     return;
   }
   uint32_t sl = s.stack_len;
-  uint32_t top[8];
+  uint32_t top[8], cur[8];
   bool have_top = false;  // virtual stack: stack[0..sl) and then top
-  uint32_t cur[8];
   if (tail_len > kChunk) {
     // The first tail chunk ends here: merged as push_merged would, virtually.
-    uint32_t w[16];
-    full_block(s.tail, 15, w);
-    compress(c.cv[0], w, s.next_index, 64u, kChunkEnd, top);
+    compress_at(c.cv[0], reinterpret_cast<const uint32_t*>(s.tail + 64 * 15), s.next_index, 64u,
+                kChunkEnd, top);
     for (uint64_t total = s.next_index + 1; (total & 1ull) == 0; total >>= 1) {
-      uint32_t l[8];
-      load8(s.stack[--sl], l);
-      parent(l, top, kParent, top);
+      --sl;
+      parent_at(reinterpret_cast<const uint32_t*>(s.stack[sl]), top, kParent, top);
     }
     have_top = true;
     const uint32_t len = tail_len - kChunk, last = (len - 1) / 64;
     last_block(s.tail + kChunk, len, w);
-    compress(c.cv[1], w, s.next_index + 1, len - 64 * last,
-             (last == 0 ? kChunkStart : 0u) | kChunkEnd, cur);
+    compress_at(c.cv[1], w, s.next_index + 1, len - 64 * last,
+                (last == 0 ? kChunkStart : 0u) | kChunkEnd, cur);
   } else {
-    uint32_t w[16];
     const uint32_t len = tail_len, last = (len - 1) / 64;
     last_block(s.tail, len, w);
-    compress(c.cv[0], w, s.next_index, len - 64 * last,
-             (last == 0 ? kChunkStart : 0u) | kChunkEnd | (sl == 0 ? kRoot : 0u), cur);
+    compress_at(c.cv[0], w, s.next_index, len - 64 * last,
+                (last == 0 ? kChunkStart : 0u) | kChunkEnd | (sl == 0 ? kRoot : 0u), cur);
   }
   const uint32_t depth = sl + (have_top ? 1u : 0u);
   if (depth == 0) {
-#pragma unroll
     for (int i = 0; i < 8; i++) out[i] = cur[i];
     return;
   }
   // Merge from the top of the virtual stack down; the bottom one is the root.
   for (uint32_t i = depth - 1;; i--) {
-    uint32_t l[8];
-    if (i < sl) {
-      load8(s.stack[i], l);
-    } else {
-#pragma unroll
-      for (int j = 0; j < 8; j++) l[j] = top[j];
-    }
+    const uint32_t* l = i < sl ? reinterpret_cast<const uint32_t*>(s.stack[i]) : top;
     if (i == 0) {
-      parent(l, cur, kParent | kRoot, out);
+      parent_at(l, cur, kParent | kRoot, out);
       return;
     }
-    parent(l, cur, kParent, cur);
+    parent_at(l, cur, kParent, cur);
   }
 }
 
@@ -225,18 +189,16 @@ __device__ void update(DevTranscript& T, const Msg& m) {
     __syncwarp();
     int full = 0;
     if (lane == 0) {
-      Cache c;
-      load_cache(T, c);
+      Cache& c = cache_of(T);
       advance(T.st.tail, tl + take, T.st.next_index, c);
       T.st.tail_len = tl + take;
       T.st.total_len += take;
       if (tl + take == kTail) {
         // Blocks 0..14 of the first chunk are folded; its last block ends it.
-        uint32_t w[16], out[8];
-        full_block(T.st.tail, 15, w);
-        compress(c.cv[0], w, T.st.next_index, 64u, kChunkEnd, out);
+        uint32_t out[8];
+        compress_at(c.cv[0], reinterpret_cast<const uint32_t*>(T.st.tail + 64 * 15),
+                    T.st.next_index, 64u, kChunkEnd, out);
         push_merged(T, out);
-#pragma unroll
         for (int i = 0; i < 8; i++) c.cv[0][i] = c.cv[1][i];
         c.nb[0] = c.nb[1];
         iv_words(c.cv[1]);
@@ -244,7 +206,6 @@ __device__ void update(DevTranscript& T, const Msg& m) {
         T.st.tail_len = kChunk;
         full = 1;
       }
-      store_cache(T, c);
     }
     full = __shfl_sync(0xffffffffu, full, 0);
     if (full) {
@@ -307,19 +268,15 @@ __device__ void squeeze(DevTranscript& T, DevTranscript& C, uint8_t* out_bytes, 
     for (uint32_t i = lane; i < S; i += 32) T.st.tail[tl + i] = suffix.at(i);
     __syncwarp();
     if (lane == 0) {
-      Cache c;
-      load_cache(T, c);
+      Cache& c = cache_of(C);  // the copy's cache area is free here
+      c = cache_of(T);
       advance(T.st.tail, tl + S, T.st.next_index, c);
       finalize(T, tl + S, T.st.total_len + S, c, out);
     }
   } else {
     warp_clone(C, T);
     update(C, suffix);
-    if (lane == 0) {
-      Cache c;
-      load_cache(C, c);
-      finalize(C, C.st.tail_len, C.st.total_len, c, out);
-    }
+    if (lane == 0) finalize(C, C.st.tail_len, C.st.total_len, cache_of(C), out);
   }
   if (lane == 0) {
     T.st.counter++;
@@ -370,7 +327,7 @@ __global__ void __launch_bounds__(32) transcript_kernel(const __grid_constant__ 
       // challenge_ext x 3 (src/transcript.rs:136-141), then the tables of
       // r_k / 4 for e4_mul_tab.
       uint32_t ch[3][4];
-#pragma unroll
+#pragma unroll 1
       for (int r = 0; r < 3; r++) {
         uint32_t d[8] = {};
         dtr::squeeze(T, C, sq, op.label, op.label_len, d);
@@ -395,11 +352,7 @@ __global__ void __launch_bounds__(32) transcript_kernel(const __grid_constant__ 
     } else if (op.kind == kTrPowHead) {
       // H(history) || LE64(|label|) || label, as little-endian words.
       uint32_t d[8] = {};
-      if (lane == 0) {
-        dtr::Cache c;
-        dtr::load_cache(T, c);
-        dtr::finalize(T, T.st.tail_len, T.st.total_len, c, d);
-      }
+      if (lane == 0) dtr::finalize(T, T.st.tail_len, T.st.total_len, dtr::cache_of(T), d);
       uint32_t v = 0;
 #pragma unroll
       for (int i = 0; i < 8; i++) {
