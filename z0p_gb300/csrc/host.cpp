@@ -296,26 +296,6 @@ std::vector<uint8_t> Transcript::pow_head(const char* label) const {
   return head;
 }
 
-void Transcript::cache(uint32_t cv[2][8], uint32_t nblk[2]) const {
-  std::memcpy(cv, h_.cv, sizeof h_.cv);
-  nblk[0] = h_.nblk[0];
-  nblk[1] = h_.nblk[1];
-}
-void Transcript::restore(const z0p_transcript_state& st, const uint32_t cv[2][8],
-                         const uint32_t nblk[2]) {
-  *h_.st = st;
-  std::memcpy(h_.cv, cv, sizeof h_.cv);
-  h_.nblk[0] = nblk[0];
-  h_.nblk[1] = nblk[1];
-}
-
-bool transcript_state_ok(const z0p_transcript_state& st) {
-  return st.tail_len < 2 * CHUNK_LEN && st.next_index < (1ull << 53) &&
-         (uint32_t)__builtin_popcountll(st.next_index) == st.stack_len &&
-         st.total_len == st.next_index * CHUNK_LEN + st.tail_len &&
-         (st.next_index == 0 || st.tail_len >= 1);
-}
-
 void transcript_init(z0p_transcript_state* st, const uint8_t* label, size_t len) {
   std::memset(st, 0, sizeof *st);  // src/transcript.rs:62-69
   Transcript(st).absorb("domain", label, len);

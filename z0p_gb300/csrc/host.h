@@ -59,19 +59,10 @@ class Transcript {
   uint64_t challenge_index(const char* label, uint64_t domain);
   // pow_head (src/transcript.rs:182-189): H(history) || LE64(|label|) || label.
   std::vector<uint8_t> pow_head(const char* label) const;
-  // The state and the hasher's block cache, for moving the transcript to
-  // another memory and back (a record of the same bytes and cache).
-  const z0p_transcript_state& state() const { return *h_.st; }
-  void cache(uint32_t cv[2][8], uint32_t nblk[2]) const;
-  void restore(const z0p_transcript_state& st, const uint32_t cv[2][8], const uint32_t nblk[2]);
 
  private:
   Hasher h_;
 };
-
-// A state the hasher can run on: tail below two chunks, one stack value per
-// set bit of the chunk count, byte count consistent with both.
-bool transcript_state_ok(const z0p_transcript_state& st);
 
 void transcript_init(z0p_transcript_state* st, const uint8_t* label, size_t len);
 inline void transcript_absorb(Transcript& t, const char* label, const uint8_t* data, size_t len) {

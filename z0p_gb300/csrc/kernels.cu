@@ -371,7 +371,6 @@ __global__ void __launch_bounds__(512) ntt_pass2_kernel(const uint32_t* __restri
 }
 
 #include "ntt_reg.cuh"
-#include "transcript.cuh"
 
 // Per coset j: 1 / (x^N - 1) with x^N = 31^N * omega_B^j (constant on the
 // coset), in Montgomery form, the same value times 2^32 once more, and the
@@ -1458,28 +1457,23 @@ __device__ __forceinline__ void fold_for_proof(FoldArgs& a) {
   if (a.cap) a.cap += pk * a.cap_stride;
   if (a.counter) a.counter += pk;
   if (a.final_vals) a.final_vals += pk * a.final_stride;
-  a.tab += pk * kFoldTabWords;
+  if (a.tab) a.tab += pk * kFoldTabWords;
+  a.slot += pk;
 }
 
-// The fold's challenge tables, staged once per CTA: every thread reads all
-// of them, and they were written by an earlier launch (device transcript or
-// host).
+// A small fold's challenge tables, staged once per CTA from a.tab (every
+// thread reads all of them).
 __device__ __forceinline__ void stage_fold_tab(const FoldArgs& a, FoldTab& t) {
   for (uint32_t i = threadIdx.x; i < kFoldTabWords; i += blockDim.x) (&t[0][0][0])[i] = a.tab[i];
   __syncthreads();
 }
 
-// kFinish: the launch may finish a small tree in its last CTA (a.counter);
-// a separate instantiation keeps the large layers' kernel at its own
-// register count.
-template <bool kFinish>
+// Large layers (and folds that stop at their CTAs' subtrees): the tables are
+// constant-bank operands of the products.
 __global__ void __launch_bounds__(kFoldThreads) fri_fold_leaf_kernel(FoldArgs a, Tables tb) {
-  // The next layer's subtree (small trees), then the roots of all CTAs.
-  __shared__ uint32_t sm[2 * kTopStride * (kFinish ? kFuseMaxLeaves / kFoldThreads : kFoldThreads)];
-  __shared__ FoldTab tab;
+  __shared__ uint32_t sm[2 * kTopStride * kFoldThreads];  // the CTA's subtree levels
   fold_for_proof(a);
-  stage_fold_tab(a, tab);
-  if (!kFinish) a.counter = nullptr;
+  a.counter = nullptr;
   const uint64_t nleaf = 1ull << (a.logn - 4);
   const uint64_t first = (uint64_t)blockIdx.x * kFoldThreads;
   const uint32_t avail = nleaf < (uint64_t)kFoldThreads ? (uint32_t)nleaf : (uint32_t)kFoldThreads;
@@ -1499,7 +1493,7 @@ __global__ void __launch_bounds__(kFoldThreads) fri_fold_leaf_kernel(FoldArgs a,
       q[i].c[0] = v.x; q[i].c[1] = v.y; q[i].c[2] = v.z; q[i].c[3] = v.w;
     }
     uint32_t P = (uint32_t)(4 * Pn + t);
-    E4 r = fold_quad(q[0], q[1], q[2], q[3], quad_xinv(tb, a, P), a, tab);
+    E4 r = fold_quad(q[0], q[1], q[2], q[3], quad_xinv(tb, a, P), a, g_consts[a.slot].tab);
 #pragma unroll
     for (int c = 0; c < 4; c++) leaf[4 * t + c] = r.c[c];
   }
@@ -1519,12 +1513,12 @@ __global__ void __launch_bounds__(kFoldThreads) fri_fold_leaf_kernel(FoldArgs a,
   cta_subtree(d, sm, avail, first, a.leaves, nleaf, a.top, a.cap, a.counter);
 }
 
-// The small-layer form of fri_fold_leaf_kernel<true> (trees of at most
-// kFuseMaxLeaves leaves, latency-bound launches of a few CTAs): four threads
-// per next leaf, one quad each, so a thread waits on one fold's loads and
-// products instead of four; the leaf's four values meet in its first lane by
-// warp shuffles, which hashes the leaf. 128 leaves per CTA as before, so the
-// subtree and the last CTA's levels are unchanged.
+// The small-layer fold (trees of at most kFuseMaxLeaves leaves, latency-
+// bound launches of a few CTAs), which also finishes the tree in its last
+// CTA: four threads per next leaf, one quad each, so a thread waits on one
+// fold's loads and products instead of four; the leaf's four values meet in
+// its first lane by warp shuffles, which hashes the leaf. 128 leaves per CTA,
+// so each CTA hashes a subtree of 128 leaves.
 constexpr int kFold4Threads = 4 * kFoldThreads;
 __global__ void __launch_bounds__(kFold4Threads) fri_fold_quad_kernel(FoldArgs a, Tables tb) {
   __shared__ uint32_t sm[2 * kTopStride * (kFuseMaxLeaves / kFoldThreads)];
@@ -2300,6 +2294,10 @@ cudaError_t range_compose_leaves(cudaStream_t st, const Tables& tb, const RangeC
   return cudaGetLastError();
 }
 
+bool fri_fold_uses_slot(const FoldArgs& a) {
+  return a.logn >= 4 && (!a.counter || (1ull << (a.logn - 4)) > kFuseMaxLeaves);
+}
+
 cudaError_t fri_fold(cudaStream_t st, const Tables& tb, const FoldArgs& a, uint32_t* levels,
                      uint32_t nproofs) {
   *levels = 0;
@@ -2316,15 +2314,18 @@ cudaError_t fri_fold(cudaStream_t st, const Tables& tb, const FoldArgs& a, uint3
                         : subtree_levels(nleaf < (uint64_t)kFoldThreads ? (uint32_t)nleaf
                                                                         : kFoldThreads,
                                          f.top);
+    const bool slot = fri_fold_uses_slot(a);
+    if (slot ? a.slot + nproofs > (uint32_t)kConstSlots : !a.tab) return cudaErrorInvalidValue;
     Stage stg("fri_fold_leaves", st);
     stg.launched();
     const dim3 grid(grid_for(nleaf, kFoldThreads), nproofs);
-    if (f.counter)
-      fri_fold_quad_kernel<<<grid, kFold4Threads, 0, st>>>(f, tb);
+    if (slot)
+      fri_fold_leaf_kernel<<<grid, kFoldThreads, 0, st>>>(f, tb);
     else
-      fri_fold_leaf_kernel<false><<<grid, kFoldThreads, 0, st>>>(f, tb);
+      fri_fold_quad_kernel<<<grid, kFold4Threads, 0, st>>>(f, tb);
     return cudaGetLastError();
   }
+  if (!a.tab) return cudaErrorInvalidValue;
   {
     Stage stg("fri_fold_small", st);
     stg.launched();
@@ -2361,24 +2362,6 @@ cudaError_t merkle_flat64_leaves(cudaStream_t st, const uint32_t* flat, uint64_t
 }
 
 bool grind_supports(uint32_t head_len) { return head_len == kPowHeadLen; }
-
-cudaError_t transcript(cudaStream_t st, const TranscriptArgs& a, uint32_t nproofs) {
-  if (!a.in || !a.out || nproofs == 0 || nproofs > 65535u || a.nops > kMaxTranscriptOps)
-    return cudaErrorInvalidValue;
-  for (uint32_t o = 0; o < a.nops; o++) {
-    const TranscriptOp& op = a.op[o];
-    if (op.label_len > kTrLabelMax) return cudaErrorInvalidValue;
-    if (op.kind == kTrAbsorb && (!op.src || op.len == 0 || op.len > kTrStage))
-      return cudaErrorInvalidValue;
-    if ((op.kind == kTrFoldTables || op.kind == kTrPowHead) && !op.dst) return cudaErrorInvalidValue;
-    if (op.kind == kTrPowHead && 40 + op.label_len > 4 * kPowHeadWords) return cudaErrorInvalidValue;
-    if (op.kind > kTrPowHead) return cudaErrorInvalidValue;
-  }
-  Stage stg("transcript", st);
-  stg.launched();
-  transcript_kernel<<<nproofs, 32, 0, st>>>(a);
-  return cudaGetLastError();
-}
 
 cudaError_t grind(cudaStream_t st, const uint32_t* head, uint32_t head_len, uint32_t bits,
                   unsigned long long* state, unsigned long long* out, uint64_t max_nonces,

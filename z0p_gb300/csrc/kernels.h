@@ -6,8 +6,6 @@
 
 #include <cstdint>
 
-#include "../../include/z0p_gpu.h"
-
 namespace z0p {
 
 struct Tables {
@@ -51,9 +49,9 @@ struct NttPlan {
 // B(x) = A(omega_N x) + C_j / (x - w_last) with C_j constant on coset j
 // (src/air.rs:806-844, linked_lde), so kernels that need B derive it from A.
 // Values that change from one proof to the next on the same shape: the
-// statement and the composition's challenges in the forms the kernels use.
-// Each context owns one slot of them in constant memory, filled by a
-// stream-ordered copy before the kernels that read it, so a captured launch
+// statement, the Fiat-Shamir challenges in the forms the kernels use. Each
+// context owns one slot of them in constant memory, filled by a stream-
+// ordered copy before the kernels that read it, so a captured launch
 // sequence replays unchanged for every proof of its shape.
 struct ProofConsts {
   uint32_t a0, b0, b_last;  // AIR statement (canonical)
@@ -63,60 +61,17 @@ struct ProofConsts {
   // Composition weights, coordinate c at [c][k] (Montgomery): alpha_1,
   // alpha_2 and alpha_3 times omega_N^-1, alpha_4 ([c][0] unused).
   uint32_t alpha[4][5];
+  uint32_t tab[3][4][4];    // a large fold's e4_mul_tab tables of r_k / 4
 };
-constexpr int kConstSlots = 168;  // 168 x 116 bytes of the 64 KiB constant bank
-
-// Words of one fold's challenge tables (e4_mul_tab of r_k / 4, k < 3) and of
-// one PoW head (47 bytes, little-endian words, zero padded), per proof.
-constexpr uint32_t kFoldTabWords = 48;
-constexpr uint32_t kPowHeadWords = 16;
-
-// A Fiat-Shamir transcript as the device keeps it: the C-ABI state and the
-// host hasher's block cache (cv[h] = tail chunk h after its first nblk[h]
-// blocks, none of them its chunk's last), so a transcript moves between host
-// and device memory without re-hashing its tail.
-struct DevTranscript {
-  z0p_transcript_state st;
-  uint32_t cv[2][8];
-  uint32_t nblk[2];
-  uint32_t pad[2];
-};
-static_assert(sizeof(DevTranscript) % 16 == 0, "records are copied in 16-byte words");
-
-// One step of a device transcript program (src/transcript.rs:72-189), run
-// for every proof k of a group:
-//  kTrAbsorb: `count` items of `len` bytes from src + k * src_stride (device-
-//    visible memory), each absorbed under the label (Transcript::absorb);
-//  kTrFoldTables: three challenge_ext under the label (src/fri.rs:603-606),
-//    written as the fold's challenge tables to dst + k * dst_stride;
-//  kTrPowHead: the PoW head H(history) || LE64(|label|) || label
-//    (src/transcript.rs:182-189) to dst + k * dst_stride.
-enum : uint32_t { kTrAbsorb = 0, kTrFoldTables = 1, kTrPowHead = 2 };
-constexpr uint32_t kTrLabelMax = 24;
-constexpr uint32_t kTrStage = 16384;  // largest absorbed item, bytes
-struct TranscriptOp {
-  uint32_t kind = kTrAbsorb;
-  uint32_t label_len = 0;
-  char label[kTrLabelMax] = {};
-  const void* src = nullptr;
-  uint64_t src_stride = 0;  // bytes
-  uint32_t len = 0, count = 0;
-  uint32_t* dst = nullptr;
-  uint64_t dst_stride = 0;  // words
-};
-constexpr uint32_t kMaxTranscriptOps = 6;
-struct TranscriptArgs {
-  const DevTranscript* in = nullptr;  // proof k's record at in + k
-  DevTranscript* out = nullptr;       // proof k's record at out + k (may equal in)
-  TranscriptOp op[kMaxTranscriptOps];
-  uint32_t nops = 0;
-  // Device-mapped status word: set (bit 2) when a record is not a valid
-  // state, which the launch then leaves unwritten.
-  unsigned int* fault = nullptr;
-};
+constexpr int kConstSlots = 168;  // 168 x 308 bytes of the 64 KiB constant bank
 // Largest proof group one launch sequence covers (per-proof counters and PoW
 // states are sized for it).
 constexpr int kMaxGroup = 64;
+
+// Words of one fold's challenge tables (ProofConsts::tab) and of one PoW head
+// (47 bytes, little-endian words, zero padded), per proof.
+constexpr uint32_t kFoldTabWords = 48;
+constexpr uint32_t kPowHeadWords = 16;
 
 struct AirComposeArgs {
   const uint32_t* lde_a;  // coset-major [j][q]
@@ -162,8 +117,12 @@ struct FoldArgs {
   uint32_t logn;
   uint32_t ginv_m;     // (31^(4^depth))^-1 (Montgomery)
   uint32_t unit_m;     // two_adic_generator(2) (Montgomery)
-  // The fold's challenge tables (kFoldTabWords per proof, device-visible).
+  // The fold's challenge tables: small layers (the launches that finish their
+  // tree) read them from `tab` (kFoldTabWords per proof, device-visible, e.g.
+  // mapped host memory, so no copy is queued before a latency-bound fold);
+  // large layers from the constant slots, first proof's at `slot`.
   const uint32_t* tab = nullptr;
+  uint32_t slot = 0;
   // One zero device word per proof: with it, a small tree is finished up to
   // `top` by the fold's last CTA (nullptr: the fold stops at its subtrees).
   unsigned int* counter = nullptr;
@@ -430,6 +389,9 @@ cudaError_t range_compose_leaves(cudaStream_t st, const Tables& tb, const RangeC
 // set; *levels receives the levels done above the leaves.
 cudaError_t fri_fold(cudaStream_t st, const Tables& tb, const FoldArgs& a, uint32_t* levels,
                      uint32_t nproofs = 1);
+// Whether fri_fold reads the tables of `a` from the constant slots (true) or
+// from a.tab (false).
+bool fri_fold_uses_slot(const FoldArgs& a);
 // fri::commit input: out[c][i] = in[c-th coordinate of value i] * 31^i (one
 // coordinate, or four for Ext4 input interleaved 4 words per value); *bad
 // receives 1 when an input word is not a canonical field element.
@@ -474,9 +436,7 @@ cudaError_t merkle_flat64_leaves(cudaStream_t st, const uint32_t* flat, uint64_t
 cudaError_t grind(cudaStream_t st, const uint32_t* head, uint32_t head_len, uint32_t bits,
                   unsigned long long* state, unsigned long long* out, uint64_t max_nonces,
                   uint32_t nproofs = 1);
-// Runs a transcript program (TranscriptArgs) for `nproofs` proofs, one warp
-// each.
-cudaError_t transcript(cudaStream_t st, const TranscriptArgs& a, uint32_t nproofs = 1);
+
 bool grind_supports(uint32_t head_len);
 // Reorders `batch` coset-major LDEs ([j][q]) into natural order ([B q + j]).
 cudaError_t coset_to_natural(cudaStream_t st, const uint32_t* in, uint32_t* out, uint32_t logN,

@@ -394,40 +394,12 @@ inline uint64_t tree_digests(uint64_t leaves) { return 2 * leaves - 1; }
 
 // Device counters that kernels leave as they found them, set once when the
 // context is created, one per proof of a group: the Merkle last-CTA counters
-// (kMaxGroup words) and the PoW search states (kMaxGroup x 4 u64). After
-// them, scratch of the device transcripts: kMaxGroup records, then as many
-// fold challenge tables and PoW heads.
+// (kMaxGroup words) and the PoW search states (kMaxGroup x 4 u64).
 inline unsigned int* merkle_counter(z0p_gpu_ctx* c) { return (unsigned int*)c->state.p; }
 inline unsigned long long* grind_state(z0p_gpu_ctx* c) {
   return reinterpret_cast<unsigned long long*>((char*)c->state.p + 4 * kMaxGroup);
 }
-constexpr size_t kRecordsAt = 4 * kMaxGroup + 32 * kMaxGroup;  // 16-byte aligned
-constexpr size_t kStateBytes =
-    kRecordsAt + kMaxGroup * (sizeof(DevTranscript) + 4 * (kFoldTabWords + kPowHeadWords));
-inline DevTranscript* dev_records(z0p_gpu_ctx* c) {
-  return reinterpret_cast<DevTranscript*>((char*)c->state.p + kRecordsAt);
-}
-inline uint32_t* dev_fold_tabs(z0p_gpu_ctx* c) {
-  return reinterpret_cast<uint32_t*>(dev_records(c) + kMaxGroup);
-}
-inline uint32_t* dev_pow_heads(z0p_gpu_ctx* c) { return dev_fold_tabs(c) + kFoldTabWords * kMaxGroup; }
 constexpr uint32_t kPowHeadBytes = 40 + 7;  // H(history) || LE64(7) || "fri-pow"
-
-// One step of a device transcript program (kernels.h, TranscriptOp).
-void tr_op(TranscriptArgs& a, uint32_t kind, const char* label, const void* src = nullptr,
-           uint64_t src_stride = 0, uint32_t len = 0, uint32_t count = 0, uint32_t* dst = nullptr,
-           uint64_t dst_stride = 0) {
-  TranscriptOp& op = a.op[a.nops++];
-  op.kind = kind;
-  op.label_len = (uint32_t)std::strlen(label);
-  std::memcpy(op.label, label, op.label_len);
-  op.src = src;
-  op.src_stride = src_stride;
-  op.len = len;
-  op.count = count;
-  op.dst = dst;
-  op.dst_stride = dst_stride;
-}
 
 
 inline uint64_t level_off(uint64_t leaves, uint32_t l) { return 2 * leaves - 2 * (leaves >> l); }
@@ -438,7 +410,6 @@ struct FriOut {
   std::vector<std::vector<uint8_t>> caps;
   std::vector<uint32_t> final_vals;
   uint64_t nonce = 0;
-  bool pow_done = false;  // the nonce was found and absorbed with the commitment
   std::vector<uint64_t> indices;
 };
 
@@ -486,7 +457,7 @@ struct HioPlan {
   size_t trace_cap = 0, trace_cap_bytes = 0;
   std::vector<size_t> fri_cap, fri_cap_bytes;
   size_t final_vals = 0, final_bytes = 0, grind = 0, indices = 0, open = 0;
-  size_t records = 0, heads = 0;  // transcript records (DevTranscript), PoW heads
+  size_t tabs = 0, heads = 0;  // small folds' challenge tables, PoW heads (read in place)
   size_t extra = 0, extra_bytes = 0;
   uint32_t stride = 0, trace_off = 0;  // one opening block, in words
   std::vector<uint32_t> layer_off;     // per non-final FRI layer, in words
@@ -513,7 +484,7 @@ int plan_hio(z0p_gpu_ctx* c, const FriShape& s, uint64_t queries, uint32_t tdrop
   h->final_bytes = 16 * s.len.back();
   h->final_vals = take(h->final_bytes);
   h->grind = take(16);
-  h->records = take(sizeof(DevTranscript));
+  h->tabs = take(4 * kFoldTabWords);
   h->heads = take(4 * kPowHeadWords);
   h->indices = take(8 * queries);
   size_t L = s.len.size() - 1;
@@ -535,30 +506,8 @@ int plan_hio(z0p_gpu_ctx* c, const FriShape& s, uint64_t queries, uint32_t tdrop
   return ensure_hio(c, at);
 }
 
-// Hands the group's transcripts to the device: proof k's record at
-// at + k * sizeof(DevTranscript) in the mapped buffer.
-int export_transcripts(z0p_gpu_ctx* c, Transcript* const* ts, uint32_t K, size_t at) {
-  DevTranscript* r = reinterpret_cast<DevTranscript*>(c->hio + at);
-  for (uint32_t k = 0; k < K; k++) {
-    if (!transcript_state_ok(ts[k]->state())) {
-      set_reason("transcript state is not a state the hasher reaches");
-      return Z0P_ERR_MALFORMED_INPUT;
-    }
-    r[k].st = ts[k]->state();
-    ts[k]->cache(r[k].cv, r[k].nblk);
-  }
-  c->h2d += (uint64_t)K * sizeof(DevTranscript);
-  return Z0P_OK;
-}
-// Takes them back once the stream has drained.
-void import_transcripts(z0p_gpu_ctx* c, Transcript* const* ts, uint32_t K, size_t at) {
-  const DevTranscript* r = reinterpret_cast<const DevTranscript*>(c->hio + at);
-  for (uint32_t k = 0; k < K; k++) ts[k]->restore(r[k].st, r[k].cv, r[k].nblk);
-  c->d2h += (uint64_t)K * sizeof(DevTranscript);
-}
-
 // The PoW search of a group whose heads are at `heads` (device-visible,
-// kPowHeadWords per proof): results at h.grind.
+// kPowHeadWords per proof): results at res_at in the mapped buffer.
 cudaError_t queue_grind(z0p_gpu_ctx* c, const FriParams& fp, const uint32_t* heads, size_t res_at,
                         uint32_t K) {
   return launch::grind(c->stream, heads, kPowHeadBytes, fp.grinding_bits, grind_state(c),
@@ -577,15 +526,13 @@ int check_grind(z0p_gpu_ctx* c, size_t res_at, uint32_t k, uint64_t* nonce) {
 }
 
 // FRI commit of one group (src/fri.rs:551-633), layer 0 and its tree
-// already queued. The transcripts move to the device for the whole commit:
-// after each layer's tree, one launch absorbs its cap and draws the next
-// fold's challenges as the fold's tables, so the layers follow one another
-// with no host round trip; the host takes the transcripts back at the one
-// synchronisation at the end. With `with_pow` (fri::open following at once,
-// as in every prover), the PoW head, search and nonce absorb are queued too.
+// already queued: fold tables proof by proof on the host, the device work
+// of each round for the whole group. A small fold reads its tables from the
+// mapped buffer in place, so the host queues nothing before it but the
+// launch; a large one reads them from the constant slots.
 int run_fri_commit(z0p_gpu_ctx* c, const FriShape& s, const FriParams& fp, const FriBufs& fb,
                    uint64_t poly_len, uint64_t degree_bound, Transcript* const* ts, uint32_t K,
-                   const HioPlan& h, FriOut* outs, bool with_pow) {
+                   const HioPlan& h, FriOut* outs) {
   uint8_t dims[24];  // src/fri.rs:1450-1456
   for (int i = 0; i < 8; i++) {
     dims[i] = (uint8_t)(s.m >> (8 * i));
@@ -595,24 +542,14 @@ int run_fri_commit(z0p_gpu_ctx* c, const FriShape& s, const FriParams& fp, const
   for (uint32_t k = 0; k < K; k++) {
     transcript_absorb(*ts[k], "fri-dims", dims, 24);
     outs[k].caps.assign(s.len.size(), {});
-    outs[k].pow_done = false;
-    outs[k].nonce = 0;
   }
-  if (K > (uint32_t)kMaxGroup) {  // the device records are sized for kMaxGroup proofs
-    set_reason("proof group larger than the device transcripts");
-    return Z0P_ERR_INVALID_ARGUMENT;
-  }
-  RC(export_transcripts(c, ts, K, h.records));
-  const bool grind_here = with_pow && fp.grinding_bits > 0;
-  DevTranscript* rec = dev_records(c);
-  DevTranscript* rec_host = hio_dev<DevTranscript>(c, h.records);
-  uint32_t* tabs = dev_fold_tabs(c);
-  const DevTranscript* from = rec_host;
   const uint32_t unit_m = to_mont(two_adic_generator(2));
   const uint64_t fl = s.len.back();
+  uint32_t(*tabs)[3][4][4] = reinterpret_cast<uint32_t(*)[3][4][4]>(c->hio + h.tabs);
   for (size_t l = 0;; l++) {
     const bool last = l + 1 == s.len.size();
-    // The last layer's values (sent in the clear) are in the mapped buffer,
+    // A layer's caps are in the mapped buffer once its trees are done; the
+    // last layer's values (sent in the clear) come back in the same trip,
     // written there by the last fold (or copied, when there is no fold).
     if (last) {
       c->d2h += (uint64_t)K * h.final_bytes;
@@ -621,33 +558,39 @@ int run_fri_commit(z0p_gpu_ctx* c, const FriShape& s, const FriParams& fp, const
                              4 * fb.val_stride, h.final_bytes, K, cudaMemcpyDeviceToHost,
                              c->stream));
     }
-    // Absorb the layer's cap, one digest at a time (src/fri.rs:596-600), then
-    // draw the fold's challenges or absorb the final layer.
-    TranscriptArgs ta;
-    ta.in = from;
-    ta.out = rec;
-    ta.fault = c->tb.fault;
-    tr_op(ta, kTrAbsorb, "fri-layer-root", hio_dev<uint8_t>(c, h.fri_cap[l]), h.fri_cap_bytes[l],
-          32, (uint32_t)(h.fri_cap_bytes[l] / 32));
-    if (!last) {
-      tr_op(ta, kTrFoldTables, "fri-fold", nullptr, 0, 0, 0, tabs, kFoldTabWords);
-    } else {
-      tr_op(ta, kTrAbsorb, "fri-final", hio_dev<uint8_t>(c, h.final_vals), h.final_bytes,
-            (uint32_t)(16 * fl), 1);
-      if (grind_here)
-        tr_op(ta, kTrPowHead, "fri-pow", nullptr, 0, 0, 0, dev_pow_heads(c), kPowHeadWords);
-      else
-        ta.out = rec_host;
+    CK(sync(c, last ? "cap+final" : "cap"));
+    for (uint32_t k = 0; k < K; k++) {
+      const uint8_t* cap = c->hio + h.fri_cap[l] + k * h.fri_cap_bytes[l];
+      outs[k].caps[l].assign(cap, cap + h.fri_cap_bytes[l]);
+      c->d2h += h.fri_cap_bytes[l];  // written by the tree kernel into the mapped buffer
+      for (size_t i = 0; i < h.fri_cap_bytes[l] / 32; i++)
+        transcript_absorb(*ts[k], "fri-layer-root", cap + 32 * i, 32);
     }
-    CK(launch::transcript(c->stream, ta, K));
-    from = rec;
     if (last) break;
     FoldArgs fa;
-    fa.tab = tabs;
     fa.in = fb.layer[l];
     fa.out = fb.layer[l + 1];
     fa.leaves = fb.tree[l + 1];
     fa.logn = log2u(s.len[l]);
+    fa.counter = merkle_counter(c);
+    fa.slot = (uint32_t)c->slot;
+    fa.tab = hio_dev<uint32_t>(c, h.tabs);
+    const bool slot = launch::fri_fold_uses_slot(fa);
+    const uint32_t inv4 = finv(4);
+    for (uint32_t k = 0; k < K; k++) {
+      uint32_t ch[3][4];
+      for (int r = 0; r < 3; r++) challenge_ext(*ts[k], "fri-fold", ch[r]);
+      for (int r = 0; r < 3; r++) {
+        uint32_t q[4];
+        for (int e = 0; e < 4; e++) q[e] = fmul(ch[r][e], inv4);
+        e4_table(q, slot ? c->consts[k].tab[r] : tabs[k][r]);
+      }
+    }
+    if (slot) {
+      CK(push_consts(c, K));
+    } else {
+      c->h2d += 4ull * kFoldTabWords * K;  // read by the fold in place
+    }
     // layer-l domain is 31^(4^l) <omega_len>; its inverse shift:
     uint32_t g = GENERATOR;
     for (size_t i = 0; i < l; i++) g = fpow(g, 4);
@@ -659,7 +602,6 @@ int run_fri_commit(z0p_gpu_ctx* c, const FriShape& s, const FriParams& fp, const
     fa.in_stride = fa.out_stride = fb.val_stride;
     fa.tree_stride = fb.tree_stride;
     fa.cap_stride = h.fri_cap_bytes[l + 1] / 4;
-    fa.counter = merkle_counter(c);
     if (l + 2 == s.len.size()) {  // this fold makes the final layer
       fa.final_vals = hio_dev<uint32_t>(c, h.final_vals);
       fa.final_stride = h.final_bytes / 4;
@@ -674,39 +616,23 @@ int run_fri_commit(z0p_gpu_ctx* c, const FriShape& s, const FriParams& fp, const
       CK(launch::merkle_build(c->stream, fb.tree[l + 1], s.leaves[l + 1], top, merkle_counter(c),
                               fa.cap, built, K, fb.tree_stride, fa.cap_stride));
   }
-  if (grind_here) {  // src/fri.rs:645-650, src/transcript.rs:206-228
-    CK(queue_grind(c, fp, dev_pow_heads(c), h.grind, K));
-    TranscriptArgs ta;
-    ta.in = rec;
-    ta.out = rec_host;
-    ta.fault = c->tb.fault;
-    tr_op(ta, kTrAbsorb, "fri-pow", hio_dev<uint8_t>(c, h.grind), 16, 8, 1);
-    CK(launch::transcript(c->stream, ta, K));
-  }
-  CK(sync(c, grind_here ? "commit+grind" : "commit"));
-  import_transcripts(c, ts, K, h.records);
+  // Final layer in the clear (src/fri.rs:620-621).
   for (uint32_t k = 0; k < K; k++) {
-    for (size_t l = 0; l < s.len.size(); l++) {
-      const uint8_t* cap = c->hio + h.fri_cap[l] + k * h.fri_cap_bytes[l];
-      outs[k].caps[l].assign(cap, cap + h.fri_cap_bytes[l]);
-      c->d2h += h.fri_cap_bytes[l];  // written by the tree kernels into the mapped buffer
-    }
-    outs[k].final_vals.resize(4 * fl);  // src/fri.rs:620-621
+    outs[k].final_vals.resize(4 * fl);
     std::memcpy(outs[k].final_vals.data(), c->hio + h.final_vals + k * h.final_bytes, 16 * fl);
-    if (grind_here) {
-      RC(check_grind(c, h.grind, k, &outs[k].nonce));
-      outs[k].pow_done = true;
-    }
+    transcript_absorb(*ts[k], "fri-final", (const uint8_t*)outs[k].final_vals.data(), 16 * fl);
+    outs[k].nonce = 0;
   }
   return Z0P_OK;
 }
 
 // FRI open of one group up to the openings (src/fri.rs:645-666): the PoW
-// nonce (unless the commitment already found it), then the query indices.
+// nonce, then the query indices.
 int run_fri_open(z0p_gpu_ctx* c, const FriShape& s, const FriParams& fp, Transcript* const* ts,
                  uint32_t K, const HioPlan& h, FriOut* outs) {
-  // Proof of work (src/fri.rs:645-650, src/transcript.rs:206-228).
-  if (fp.grinding_bits > 0 && !outs[0].pow_done) {
+  // Proof of work (src/fri.rs:645-650, src/transcript.rs:206-228); the heads
+  // are read by the search in place.
+  if (fp.grinding_bits > 0) {
     uint32_t* heads = reinterpret_cast<uint32_t*>(c->hio + h.heads);
     for (uint32_t k = 0; k < K; k++) {
       std::vector<uint8_t> head = pow_head(*ts[k], "fri-pow");
@@ -717,7 +643,6 @@ int run_fri_open(z0p_gpu_ctx* c, const FriShape& s, const FriParams& fp, Transcr
     CK(sync(c, "grind"));
     for (uint32_t k = 0; k < K; k++) {
       RC(check_grind(c, h.grind, k, &outs[k].nonce));
-      outs[k].pow_done = true;
       uint8_t nb[8];
       for (int i = 0; i < 8; i++) nb[i] = (uint8_t)(outs[k].nonce >> (8 * i));
       transcript_absorb(*ts[k], "fri-pow", nb, 8);
@@ -734,7 +659,7 @@ int run_fri_open(z0p_gpu_ctx* c, const FriShape& s, const FriParams& fp, Transcr
 int run_fri(z0p_gpu_ctx* c, const FriShape& s, const FriParams& fp, const FriBufs& fb,
             uint64_t poly_len, uint64_t degree_bound, Transcript* const* ts, uint32_t K,
             const HioPlan& h, FriOut* outs) {
-  RC(run_fri_commit(c, s, fp, fb, poly_len, degree_bound, ts, K, h, outs, true));
+  RC(run_fri_commit(c, s, fp, fb, poly_len, degree_bound, ts, K, h, outs));
   return run_fri_open(c, s, fp, ts, K, h, outs);
 }
 
@@ -2262,7 +2187,7 @@ int fri_commit(z0p_gpu_ctx* c, const FriInput& in, const uint32_t* values,
   z0p_transcript_state work = *t;
   Transcript tr(&work);
   Transcript* ts[1] = {&tr};
-  RC(run_fri_commit(c, s, in.fp, f.fb, in.poly_len, in.bound, ts, 1, f.h, &f.out, false));
+  RC(run_fri_commit(c, s, in.fp, f.fb, in.poly_len, in.bound, ts, 1, f.h, &f.out));
   if (*reinterpret_cast<volatile unsigned int*>(bad_h)) {  // read after the stream drained
     set_reason("field elements must be canonical (< p)");
     return Z0P_ERR_MALFORMED_INPUT;
@@ -2542,7 +2467,7 @@ int fold_finalize(z0p_gpu_fold* f, z0p_transcript_state* ts, uint8_t* out) {
   // fri::commit_ext_evals(combined, S - 1) and fri::open (src/fold.rs:517-520).
   Transcript* tp[1] = {&t};
   FriOut fo;
-  RC(run_fri_commit(c, s, fp, fb, m, S - 1, tp, 1, h, &fo, true));
+  RC(run_fri_commit(c, s, fp, fb, m, S - 1, tp, 1, h, &fo));
   RC(run_fri_open(c, s, fp, tp, 1, h, &fo));
   OpenArgs oa{};
   oa.no_trace = 1;
@@ -2826,7 +2751,7 @@ int z0p_gpu_ctx_create(int device, z0p_gpu_ctx** out) {
       std::memset(c->consts, 0, kMaxGroup * sizeof(ProofConsts));
     }
   }
-  const size_t state_bytes = kStateBytes;
+  const size_t state_bytes = 4 * kMaxGroup + 32 * kMaxGroup;
   if (rc == Z0P_OK) rc = ensure(c, c->state, state_bytes);
   if (rc == Z0P_OK) {
     // Merkle counters 0; PoW states {best = ~0, next chunk 0, status 0, done 0}.
@@ -3515,14 +3440,18 @@ int z0p_gpu_fri_fold(z0p_gpu_ctx* c, const uint32_t* d_in, uint64_t n, uint64_t 
   fa.unit_m = to_mont(two_adic_generator(2));
   const uint32_t inv4 = finv(4);
   RC(ensure_hio(c, 4 * kFoldTabWords));
-  uint32_t(*tab)[4][4] = reinterpret_cast<uint32_t(*)[4][4]>(c->hio);  // read by the fold in place
+  // Without a tree counter the fold reads the slot (n >= 16), or, below 16
+  // values, the tables in the mapped buffer in place: both are filled.
+  uint32_t(*tab)[4][4] = reinterpret_cast<uint32_t(*)[4][4]>(c->hio);
   for (int k = 0; k < 3; k++) {
     uint32_t q[4];
     for (int e = 0; e < 4; e++) q[e] = fmul(ch[4 * k + e] % P, inv4);
-    e4_table(q, tab[k]);
+    e4_table(q, c->consts->tab[k]);
+    std::memcpy(tab[k], c->consts->tab[k], sizeof tab[k]);
   }
   fa.tab = hio_dev<uint32_t>(c, 0);
-  c->h2d += 4 * kFoldTabWords;
+  fa.slot = (uint32_t)c->slot;
+  CK(push_consts(c, 1));
   uint32_t built = 0;
   CK(launch::fri_fold(c->stream, c->tb, fa, &built));  // top 0, no cap: leaves only
   CK(sync(c));
