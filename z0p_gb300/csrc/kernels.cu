@@ -1462,9 +1462,28 @@ __device__ __forceinline__ void fold_for_proof(FoldArgs& a) {
 }
 
 // A small fold's challenge tables, staged once per CTA from a.tab (every
-// thread reads all of them).
-__device__ __forceinline__ void stage_fold_tab(const FoldArgs& a, FoldTab& t) {
-  for (uint32_t i = threadIdx.x; i < kFoldTabWords; i += blockDim.x) (&t[0][0][0])[i] = a.tab[i];
+// thread reads all of them). With a gate, thread 0 first waits for the host's
+// go word (acquire at system scope: the tables were written before it), the
+// wait bounded by about 2^31 cycles; the tables are then read past the L1.
+__device__ __forceinline__ void stage_fold_tab(const FoldArgs& a, const Tables& tb, FoldTab& t) {
+  if (a.go) {
+    if (threadIdx.x == 0) {
+      const long long t0 = clock64();
+      for (;;) {
+        unsigned int v;
+        asm volatile("ld.acquire.sys.global.u32 %0, [%1];" : "=r"(v) : "l"(a.go) : "memory");
+        if (v == a.go_epoch) break;
+        if (clock64() - t0 > (1ll << 31)) {
+          if (tb.fault) atomicOr(tb.fault, 8u);
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    __syncthreads();
+  }
+  const volatile uint32_t* src = a.tab;
+  for (uint32_t i = threadIdx.x; i < kFoldTabWords; i += blockDim.x) (&t[0][0][0])[i] = src[i];
   __syncthreads();
 }
 
@@ -1524,7 +1543,7 @@ __global__ void __launch_bounds__(kFold4Threads) fri_fold_quad_kernel(FoldArgs a
   __shared__ uint32_t sm[2 * kTopStride * (kFuseMaxLeaves / kFoldThreads)];
   __shared__ FoldTab tab;
   fold_for_proof(a);
-  stage_fold_tab(a, tab);
+  stage_fold_tab(a, tb, tab);
   const uint64_t nleaf = 1ull << (a.logn - 4);
   const uint64_t first = (uint64_t)blockIdx.x * kFoldThreads;
   const uint32_t avail = nleaf < (uint64_t)kFoldThreads ? (uint32_t)nleaf : (uint32_t)kFoldThreads;
@@ -1572,7 +1591,7 @@ __global__ void __launch_bounds__(kFold4Threads) fri_fold_quad_kernel(FoldArgs a
 __global__ void fri_fold_plain_kernel(FoldArgs a, Tables tb) {
   __shared__ FoldTab tab;
   fold_for_proof(a);
-  stage_fold_tab(a, tab);
+  stage_fold_tab(a, tb, tab);
   uint32_t P = blockIdx.x * blockDim.x + threadIdx.x;
   if (P >= (1u << (a.logn - 2))) return;
   E4 q[4];

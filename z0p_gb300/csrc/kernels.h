@@ -123,6 +123,12 @@ struct FoldArgs {
   // large layers from the constant slots, first proof's at `slot`.
   const uint32_t* tab = nullptr;
   uint32_t slot = 0;
+  // Optional gate for a fold queued before its challenges exist (small
+  // layers): every CTA first waits until *go == go_epoch (a device-mapped
+  // word the host writes after the tables), at most about a second, after
+  // which it sets bit 3 of Tables::fault and runs on.
+  const unsigned int* go = nullptr;
+  unsigned int go_epoch = 0;
   // One zero device word per proof: with it, a small tree is finished up to
   // `top` by the fold's last CTA (nullptr: the fold stops at its subtrees).
   unsigned int* counter = nullptr;

@@ -167,6 +167,10 @@ struct z0p_gpu_ctx {
   // FRI commitment stays openable only while no other such call came after it.
   uint64_t work_serial = 0;
   z0p::FriPending* fri = nullptr;
+  // Gated FRI tails (run_fri_commit): one event per layer, and the value the
+  // current commitment writes into its gate words.
+  std::vector<cudaEvent_t> gate_ev;
+  uint32_t go_epoch = 0;
 };
 using HostSite = z0p_gpu_ctx::HostSite;
 
@@ -177,14 +181,15 @@ uint64_t now_ns() {
              std::chrono::steady_clock::now().time_since_epoch())
       .count();
 }
-// Every stream synchronisation of a prove call goes through here. With
+// Every stream synchronisation of a prove call goes through here (with
+// `upto`, the wait ends at that event rather than at the stream's end). With
 // profiling on, it also records, per call site, the time blocked and the host
 // time since the previous synchronisation returned (the GPU is idle for part
 // of the latter, from the moment its queue drains until the next launch).
-cudaError_t sync(z0p_gpu_ctx* c, const char* site = "other") {
+cudaError_t sync(z0p_gpu_ctx* c, const char* site = "other", cudaEvent_t upto = nullptr) {
   c->syncs++;
   uint64_t t0 = now_ns();
-  cudaError_t e = cudaStreamSynchronize(c->stream);
+  cudaError_t e = upto ? cudaEventSynchronize(upto) : cudaStreamSynchronize(c->stream);
   uint64_t t1 = now_ns();
   if (e == cudaSuccess && c->fault && *reinterpret_cast<volatile unsigned int*>(c->fault)) {
     *c->fault = 0u;  // reported once; the context stays usable
@@ -457,7 +462,10 @@ struct HioPlan {
   size_t trace_cap = 0, trace_cap_bytes = 0;
   std::vector<size_t> fri_cap, fri_cap_bytes;
   size_t final_vals = 0, final_bytes = 0, grind = 0, indices = 0, open = 0;
-  size_t tabs = 0, heads = 0;  // small folds' challenge tables, PoW heads (read in place)
+  // Read by kernels in place: the small folds' challenge tables, per layer
+  // ([layer][proof][kFoldTabWords]), their gate words (one per layer) and
+  // the PoW heads.
+  size_t tabs = 0, gates = 0, heads = 0;
   size_t extra = 0, extra_bytes = 0;
   uint32_t stride = 0, trace_off = 0;  // one opening block, in words
   std::vector<uint32_t> layer_off;     // per non-final FRI layer, in words
@@ -484,7 +492,8 @@ int plan_hio(z0p_gpu_ctx* c, const FriShape& s, uint64_t queries, uint32_t tdrop
   h->final_bytes = 16 * s.len.back();
   h->final_vals = take(h->final_bytes);
   h->grind = take(16);
-  h->tabs = take(4 * kFoldTabWords);
+  h->tabs = take(4 * kFoldTabWords * s.len.size());
+  h->gates = take(4 * s.len.size());
   h->heads = take(4 * kPowHeadWords);
   h->indices = take(8 * queries);
   size_t L = s.len.size() - 1;
@@ -525,11 +534,35 @@ int check_grind(z0p_gpu_ctx* c, size_t res_at, uint32_t k, uint64_t* nonce) {
   return Z0P_OK;
 }
 
+// Whether folds l, l+1, ... to the final layer are all small folds (one
+// launch that also finishes the next layer's tree, tables read in place),
+// so that they can be queued ahead behind gates.
+bool gated_tail(const FriShape& s, size_t l) {
+  if (l + 1 >= s.len.size()) return false;
+  for (size_t j = l; j + 1 < s.len.size(); j++)
+    if (s.len[j] < 16 || s.leaves[j + 1] > kFuseMaxLeaves) return false;
+  return true;
+}
+
+// Writes the go value of every gate from `next` on when dropped early, so
+// that folds queued behind them never wait out their bound.
+struct GateRelease {
+  volatile unsigned int* gates;
+  size_t next, end;
+  uint32_t epoch;
+  ~GateRelease() {
+    for (; next < end; next++) __atomic_store_n(const_cast<unsigned int*>(gates + next), epoch, __ATOMIC_RELEASE);
+  }
+};
+
 // FRI commit of one group (src/fri.rs:551-633), layer 0 and its tree
 // already queued: fold tables proof by proof on the host, the device work
-// of each round for the whole group. A small fold reads its tables from the
-// mapped buffer in place, so the host queues nothing before it but the
-// launch; a large one reads them from the constant slots.
+// of each round for the whole group. A large fold reads its tables from the
+// constant slots, a small one from the mapped buffer in place. Once every
+// remaining fold is small, they are all queued at once, each behind a gate
+// word in the mapped buffer: the host then waits for a layer's event, absorbs
+// its cap, writes the next fold's tables and opens its gate, so no launch
+// stands between a challenge and its fold.
 int run_fri_commit(z0p_gpu_ctx* c, const FriShape& s, const FriParams& fp, const FriBufs& fb,
                    uint64_t poly_len, uint64_t degree_bound, Transcript* const* ts, uint32_t K,
                    const HioPlan& h, FriOut* outs) {
@@ -543,30 +576,13 @@ int run_fri_commit(z0p_gpu_ctx* c, const FriShape& s, const FriParams& fp, const
     transcript_absorb(*ts[k], "fri-dims", dims, 24);
     outs[k].caps.assign(s.len.size(), {});
   }
+  const size_t L = s.len.size();
   const uint32_t unit_m = to_mont(two_adic_generator(2));
   const uint64_t fl = s.len.back();
-  uint32_t(*tabs)[3][4][4] = reinterpret_cast<uint32_t(*)[3][4][4]>(c->hio + h.tabs);
-  for (size_t l = 0;; l++) {
-    const bool last = l + 1 == s.len.size();
-    // A layer's caps are in the mapped buffer once its trees are done; the
-    // last layer's values (sent in the clear) come back in the same trip,
-    // written there by the last fold (or copied, when there is no fold).
-    if (last) {
-      c->d2h += (uint64_t)K * h.final_bytes;
-      if (l == 0)
-        CK(cudaMemcpy2DAsync(c->hio + h.final_vals, h.final_bytes, fb.layer.back(),
-                             4 * fb.val_stride, h.final_bytes, K, cudaMemcpyDeviceToHost,
-                             c->stream));
-    }
-    CK(sync(c, last ? "cap+final" : "cap"));
-    for (uint32_t k = 0; k < K; k++) {
-      const uint8_t* cap = c->hio + h.fri_cap[l] + k * h.fri_cap_bytes[l];
-      outs[k].caps[l].assign(cap, cap + h.fri_cap_bytes[l]);
-      c->d2h += h.fri_cap_bytes[l];  // written by the tree kernel into the mapped buffer
-      for (size_t i = 0; i < h.fri_cap_bytes[l] / 32; i++)
-        transcript_absorb(*ts[k], "fri-layer-root", cap + 32 * i, 32);
-    }
-    if (last) break;
+  auto tabs = [&](size_t l) {  // layer l's fold tables, proof 0's
+    return reinterpret_cast<uint32_t(*)[3][4][4]>(c->hio + h.tabs + 4ull * kFoldTabWords * K * l);
+  };
+  auto fold_args = [&](size_t l) {
     FoldArgs fa;
     fa.in = fb.layer[l];
     fa.out = fb.layer[l + 1];
@@ -574,8 +590,35 @@ int run_fri_commit(z0p_gpu_ctx* c, const FriShape& s, const FriParams& fp, const
     fa.logn = log2u(s.len[l]);
     fa.counter = merkle_counter(c);
     fa.slot = (uint32_t)c->slot;
-    fa.tab = hio_dev<uint32_t>(c, h.tabs);
-    const bool slot = launch::fri_fold_uses_slot(fa);
+    fa.tab = hio_dev<uint32_t>(c, h.tabs + 4ull * kFoldTabWords * K * l);
+    // layer-l domain is 31^(4^l) <omega_len>; its inverse shift:
+    uint32_t g = GENERATOR;
+    for (size_t i = 0; i < l; i++) g = fpow(g, 4);
+    fa.ginv_m = to_mont(finv(g));
+    fa.unit_m = unit_m;
+    fa.top = s.depth[l + 1] - s.drop[l + 1];
+    fa.cap = hio_dev<uint32_t>(c, h.fri_cap[l + 1]);
+    fa.in_stride = fa.out_stride = fb.val_stride;
+    fa.tree_stride = fb.tree_stride;
+    fa.cap_stride = h.fri_cap_bytes[l + 1] / 4;
+    if (l + 2 == L) {  // this fold makes the final layer
+      fa.final_vals = hio_dev<uint32_t>(c, h.final_vals);
+      fa.final_stride = h.final_bytes / 4;
+    }
+    return fa;
+  };
+  auto absorb_cap = [&](size_t l) {
+    for (uint32_t k = 0; k < K; k++) {
+      const uint8_t* cap = c->hio + h.fri_cap[l] + k * h.fri_cap_bytes[l];
+      outs[k].caps[l].assign(cap, cap + h.fri_cap_bytes[l]);
+      c->d2h += h.fri_cap_bytes[l];  // written by the tree kernel into the mapped buffer
+      for (size_t i = 0; i < h.fri_cap_bytes[l] / 32; i++)
+        transcript_absorb(*ts[k], "fri-layer-root", cap + 32 * i, 32);
+    }
+  };
+  // Fold l's challenges into its tables (src/fri.rs:603-606): the constant
+  // slots for a large fold, the mapped buffer for a small one.
+  auto fold_tables = [&](size_t l, bool slot) {
     const uint32_t inv4 = finv(4);
     for (uint32_t k = 0; k < K; k++) {
       uint32_t ch[3][4];
@@ -583,38 +626,68 @@ int run_fri_commit(z0p_gpu_ctx* c, const FriShape& s, const FriParams& fp, const
       for (int r = 0; r < 3; r++) {
         uint32_t q[4];
         for (int e = 0; e < 4; e++) q[e] = fmul(ch[r][e], inv4);
-        e4_table(q, slot ? c->consts[k].tab[r] : tabs[k][r]);
+        e4_table(q, slot ? c->consts[k].tab[r] : tabs(l)[k][r]);
       }
     }
-    if (slot) {
-      CK(push_consts(c, K));
-    } else {
-      c->h2d += 4ull * kFoldTabWords * K;  // read by the fold in place
+    if (!slot) c->h2d += 4ull * kFoldTabWords * K;  // read by the fold in place
+  };
+  if (L == 1) {  // the final layer is layer 0: its values come back by copy
+    c->d2h += (uint64_t)K * h.final_bytes;
+    CK(cudaMemcpy2DAsync(c->hio + h.final_vals, h.final_bytes, fb.layer.back(), 4 * fb.val_stride,
+                         h.final_bytes, K, cudaMemcpyDeviceToHost, c->stream));
+  }
+  for (size_t l = 0;; l++) {
+    if (gated_tail(s, l)) {
+      while (c->gate_ev.size() < L) {
+        cudaEvent_t e;
+        CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        c->gate_ev.push_back(e);
+      }
+      const uint32_t epoch = ++c->go_epoch;
+      volatile unsigned int* gates = reinterpret_cast<volatile unsigned int*>(c->hio + h.gates);
+      GateRelease release{gates, l, L - 1, epoch};
+      CK(cudaEventRecord(c->gate_ev[l], c->stream));  // layer l's cap
+      for (size_t j = l; j + 1 < L; j++) {
+        FoldArgs fa = fold_args(j);
+        fa.go = hio_dev<unsigned int>(c, h.gates) + j;
+        fa.go_epoch = epoch;
+        uint32_t built = 0;
+        CK(launch::fri_fold(c->stream, c->tb, fa, &built, K));
+        CK(cudaEventRecord(c->gate_ev[j + 1], c->stream));  // layer j+1's cap
+      }
+      c->d2h += (uint64_t)K * h.final_bytes;  // written by the last fold
+      for (size_t j = l;; j++) {
+        const bool last = j + 1 == L;
+        CK(sync(c, last ? "cap+final" : "cap", c->gate_ev[j]));
+        absorb_cap(j);
+        if (last) break;
+        fold_tables(j, false);
+        __atomic_store_n(const_cast<unsigned int*>(gates + j), epoch, __ATOMIC_RELEASE);
+        release.next = j + 1;
+      }
+      break;
     }
-    // layer-l domain is 31^(4^l) <omega_len>; its inverse shift:
-    uint32_t g = GENERATOR;
-    for (size_t i = 0; i < l; i++) g = fpow(g, 4);
-    fa.ginv_m = to_mont(finv(g));
-    fa.unit_m = unit_m;
-    const uint32_t top = s.depth[l + 1] - s.drop[l + 1];
-    fa.top = top;
-    fa.cap = hio_dev<uint32_t>(c, h.fri_cap[l + 1]);
-    fa.in_stride = fa.out_stride = fb.val_stride;
-    fa.tree_stride = fb.tree_stride;
-    fa.cap_stride = h.fri_cap_bytes[l + 1] / 4;
-    if (l + 2 == s.len.size()) {  // this fold makes the final layer
-      fa.final_vals = hio_dev<uint32_t>(c, h.final_vals);
-      fa.final_stride = h.final_bytes / 4;
-    }
+    const bool last = l + 1 == L;
+    // A layer's caps are in the mapped buffer once its trees are done; the
+    // last layer's values (sent in the clear) come back in the same trip,
+    // written there by the last fold (or copied, when there is no fold).
+    if (last && l > 0) c->d2h += (uint64_t)K * h.final_bytes;
+    CK(sync(c, last ? "cap+final" : "cap"));
+    absorb_cap(l);
+    if (last) break;
+    FoldArgs fa = fold_args(l);
+    const bool slot = launch::fri_fold_uses_slot(fa);
+    fold_tables(l, slot);
+    if (slot) CK(push_consts(c, K));
     uint32_t built = 0;  // tree levels the fold kernel hashed itself
     CK(launch::fri_fold(c->stream, c->tb, fa, &built, K));
     // Levels above `built` remain, if any. A tree capped at its leaves has
     // its cap written by the fold only when the fold hashed its subtree (64-
     // byte leaves, small tree); otherwise merkle_build copies it.
     const bool fused = s.len[l] >= 16 && s.leaves[l + 1] <= kFuseMaxLeaves;
-    if (built < top || (top == 0 && !fused))
-      CK(launch::merkle_build(c->stream, fb.tree[l + 1], s.leaves[l + 1], top, merkle_counter(c),
-                              fa.cap, built, K, fb.tree_stride, fa.cap_stride));
+    if (built < fa.top || (fa.top == 0 && !fused))
+      CK(launch::merkle_build(c->stream, fb.tree[l + 1], s.leaves[l + 1], fa.top,
+                              merkle_counter(c), fa.cap, built, K, fb.tree_stride, fa.cap_stride));
   }
   // Final layer in the clear (src/fri.rs:620-621).
   for (uint32_t k = 0; k < K; k++) {
@@ -2783,6 +2856,7 @@ void z0p_gpu_ctx_destroy(z0p_gpu_ctx* c) {
   if (c->hio) cudaFreeHost(c->hio);
   if (c->fault) cudaFreeHost(c->fault);
   if (c->consts) cudaFreeHost(c->consts);
+  for (cudaEvent_t e : c->gate_ev) cudaEventDestroy(e);
   give_slots(c->slot, c->nslots);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c->fri;
