@@ -1417,6 +1417,29 @@ __global__ void __launch_bounds__(64) fold_openings_kernel(const FoldStepDev* st
   }
 }
 
+// ---------------------------------------------------------------- gates ----
+// A launch queued before the host has written its inputs waits here: thread 0
+// polls the device-mapped gate word until it holds `epoch` (acquire at system
+// scope, so the inputs the host wrote before it are visible), at most about
+// 2^31 cycles, after which it sets bit 3 of *fault and the CTA runs on.
+__device__ __noinline__ void wait_gate(const unsigned int* go, unsigned int epoch,
+                                       unsigned int* fault) {
+  if (threadIdx.x == 0) {
+    const long long t0 = clock64();
+    for (;;) {
+      unsigned int v;
+      asm volatile("ld.acquire.sys.global.u32 %0, [%1];" : "=r"(v) : "l"(go) : "memory");
+      if (v == epoch) break;
+      if (clock64() - t0 > (1ll << 31)) {
+        if (fault) atomicOr(fault, 8u);
+        break;
+      }
+      __nanosleep(64);
+    }
+  }
+  __syncthreads();
+}
+
 // ----------------------------------------------------------------- FRI ----
 // fold_values (src/fri.rs:1311-1331): A + x^-1 (r0 B + x^-1 (r1 C + x^-1 r2 D))
 // with B, C, D the quarter-scaled differences; the 1/4 is folded into the
@@ -1462,26 +1485,10 @@ __device__ __forceinline__ void fold_for_proof(FoldArgs& a) {
 }
 
 // A small fold's challenge tables, staged once per CTA from a.tab (every
-// thread reads all of them). With a gate, thread 0 first waits for the host's
-// go word (acquire at system scope: the tables were written before it), the
-// wait bounded by about 2^31 cycles; the tables are then read past the L1.
+// thread reads all of them), after the fold's gate when it has one; the
+// tables are read past the L1.
 __device__ __forceinline__ void stage_fold_tab(const FoldArgs& a, const Tables& tb, FoldTab& t) {
-  if (a.go) {
-    if (threadIdx.x == 0) {
-      const long long t0 = clock64();
-      for (;;) {
-        unsigned int v;
-        asm volatile("ld.acquire.sys.global.u32 %0, [%1];" : "=r"(v) : "l"(a.go) : "memory");
-        if (v == a.go_epoch) break;
-        if (clock64() - t0 > (1ll << 31)) {
-          if (tb.fault) atomicOr(tb.fault, 8u);
-          break;
-        }
-        __nanosleep(64);
-      }
-    }
-    __syncthreads();
-  }
+  if (a.go) wait_gate(a.go, a.go_epoch, tb.fault);
   const volatile uint32_t* src = a.tab;
   for (uint32_t i = threadIdx.x; i < kFoldTabWords; i += blockDim.x) (&t[0][0][0])[i] = src[i];
   __syncthreads();
@@ -1623,6 +1630,9 @@ constexpr uint64_t kGrindChunk = (uint64_t)kGrindThreads * kGrindPerThread;
 // and puts the state back to {~0, 0, 0, 0} for the next launch.
 struct GrindArgs {
   const uint32_t* head;  // proof k's head at head + k * kPowHeadWords
+  const unsigned int* go;  // optional gate (wait_gate) before the head is read
+  unsigned int go_epoch;
+  unsigned int* fault;
   uint32_t bits;
   unsigned long long* state;
   unsigned long long* out;
@@ -1655,7 +1665,9 @@ __global__ void __launch_bounds__(kGrindThreads) grind_kernel(GrindArgs a) {
   __shared__ unsigned long long s_chunk;
   __shared__ int s_stop;
   __shared__ uint32_t s_head[W + 1];
-  if (threadIdx.x <= (unsigned)W) s_head[threadIdx.x] = a.head[threadIdx.x];
+  if (a.go) wait_gate(a.go, a.go_epoch, a.fault);
+  if (threadIdx.x <= (unsigned)W)
+    s_head[threadIdx.x] = reinterpret_cast<const volatile uint32_t*>(a.head)[threadIdx.x];
   __syncthreads();
   uint32_t head[W + 1];  // the head's words, kept in registers for every attempt
 #pragma unroll
@@ -1758,8 +1770,9 @@ __global__ void __launch_bounds__(256) hash_ceiling_kernel(const uint32_t* __res
 // layer table is indexed at run time without a per-thread local copy.
 __global__ void __launch_bounds__(128) openings_kernel(const __grid_constant__ OpenArgs a) {
   const uint32_t qi = blockIdx.x, pk = blockIdx.y;  // query, proof of the group
+  if (a.go) wait_gate(a.go, a.go_epoch, a.fault);
   uint32_t* out = a.out + ((size_t)pk * a.nq + qi) * a.stride;
-  const uint64_t leaf = a.indices[(size_t)pk * a.nq + qi];
+  const uint64_t leaf = *reinterpret_cast<const volatile uint64_t*>(a.indices + (size_t)pk * a.nq + qi);
   const uint64_t vo = pk * a.fri_val_stride, to = pk * a.fri_tree_stride;
   const uint32_t* lde = a.lde + pk * a.lde_stride;
   const uint32_t* ttree = a.ttree + pk * a.ttree_stride;
@@ -2384,11 +2397,15 @@ bool grind_supports(uint32_t head_len) { return head_len == kPowHeadLen; }
 
 cudaError_t grind(cudaStream_t st, const uint32_t* head, uint32_t head_len, uint32_t bits,
                   unsigned long long* state, unsigned long long* out, uint64_t max_nonces,
-                  uint32_t nproofs) {
+                  uint32_t nproofs, const unsigned int* go, unsigned int go_epoch,
+                  unsigned int* fault) {
   if (!grind_supports(head_len) || bits > 32 || !head || nproofs == 0 || nproofs > 65535u)
     return cudaErrorInvalidValue;
   GrindArgs a;
   a.head = head;
+  a.go = go;
+  a.go_epoch = go_epoch;
+  a.fault = fault;
   a.bits = bits;
   a.state = state;
   a.out = out;

@@ -125,7 +125,7 @@ struct FoldArgs {
   uint32_t slot = 0;
   // Optional gate for a fold queued before its challenges exist (small
   // layers): every CTA first waits until *go == go_epoch (a device-mapped
-  // word the host writes after the tables), at most about a second, after
+  // word the host writes after the tables), at most about 2^31 cycles, after
   // which it sets bit 3 of Tables::fault and runs on.
   const unsigned int* go = nullptr;
   unsigned int go_epoch = 0;
@@ -175,6 +175,11 @@ struct OpenArgs {
   // Per-proof strides (words) for a proof group: FRI layer values and trees,
   // trace LDE and trace tree (cb and tinv follow from B and m).
   uint64_t fri_val_stride = 0, fri_tree_stride = 0, lde_stride = 0, ttree_stride = 0;
+  // Optional gate (as FoldArgs::go): the launch waits for *go == go_epoch
+  // before it reads the indices; a wait that runs out sets bit 3 of *fault.
+  const unsigned int* go = nullptr;
+  unsigned int go_epoch = 0;
+  unsigned int* fault = nullptr;
 };
 
 // Product table of the Fp4 constant r (canonical coordinates) in the layout
@@ -438,10 +443,12 @@ cudaError_t merkle_flat64_leaves(cudaStream_t st, const uint32_t* flat, uint64_t
 // {~0, 0, 0, 0} before the call and again after it; `out` (device-visible)
 // receives {best nonce, status}, status 1 when the nonce cap was reached.
 // Proof k's head (head_len bytes) is at head + k * kPowHeadWords
-// (device-visible).
+// (device-visible). With `go`, the launch first waits at that gate (as
+// FoldArgs::go) for go_epoch; a wait that runs out sets bit 3 of *fault.
 cudaError_t grind(cudaStream_t st, const uint32_t* head, uint32_t head_len, uint32_t bits,
                   unsigned long long* state, unsigned long long* out, uint64_t max_nonces,
-                  uint32_t nproofs = 1);
+                  uint32_t nproofs = 1, const unsigned int* go = nullptr,
+                  unsigned int go_epoch = 0, unsigned int* fault = nullptr);
 
 bool grind_supports(uint32_t head_len);
 // Reorders `batch` coset-major LDEs ([j][q]) into natural order ([B q + j]).

@@ -463,8 +463,8 @@ struct HioPlan {
   std::vector<size_t> fri_cap, fri_cap_bytes;
   size_t final_vals = 0, final_bytes = 0, grind = 0, indices = 0, open = 0;
   // Read by kernels in place: the small folds' challenge tables, per layer
-  // ([layer][proof][kFoldTabWords]), their gate words (one per layer) and
-  // the PoW heads.
+  // ([layer][proof][kFoldTabWords]), the gate words (one per fold, then the
+  // PoW search's and the gather's) and the PoW heads.
   size_t tabs = 0, gates = 0, heads = 0;
   size_t extra = 0, extra_bytes = 0;
   uint32_t stride = 0, trace_off = 0;  // one opening block, in words
@@ -493,7 +493,7 @@ int plan_hio(z0p_gpu_ctx* c, const FriShape& s, uint64_t queries, uint32_t tdrop
   h->final_vals = take(h->final_bytes);
   h->grind = take(16);
   h->tabs = take(4 * kFoldTabWords * s.len.size());
-  h->gates = take(4 * s.len.size());
+  h->gates = take(4 * (s.len.size() + 1));
   h->heads = take(4 * kPowHeadWords);
   h->indices = take(8 * queries);
   size_t L = s.len.size() - 1;
@@ -544,15 +544,31 @@ bool gated_tail(const FriShape& s, size_t l) {
   return true;
 }
 
-// Writes the go value of every gate from `next` on when dropped early, so
-// that folds queued behind them never wait out their bound.
+// The gate words of one gated tail, opened in order. Whatever is still
+// closed when it is dropped (an early return) is opened then, so that no
+// launch queued behind a gate waits out its bound.
 struct GateRelease {
-  volatile unsigned int* gates;
-  size_t next, end;
-  uint32_t epoch;
-  ~GateRelease() {
-    for (; next < end; next++) __atomic_store_n(const_cast<unsigned int*>(gates + next), epoch, __ATOMIC_RELEASE);
+  volatile unsigned int* gates = nullptr;
+  size_t next = 0, end = 0;
+  uint32_t epoch = 0;
+  void open_next() {  // after the host has written the inputs behind it
+    __atomic_store_n(const_cast<unsigned int*>(gates + next), epoch, __ATOMIC_RELEASE);
+    next++;
   }
+  ~GateRelease() {
+    while (next < end) open_next();
+  }
+};
+
+// What follows a FRI commitment in a prover: the PoW search and the openings
+// gather (prepared, kernels.h OpenArgs), then `after`. When the commitment's
+// tail is gated, run_fri_commit queues them behind two more gates: the PoW
+// search's (word L - 1, L the layer count) and the gather's (word L).
+struct FriTail {
+  OpenArgs* oa = nullptr;
+  std::function<cudaError_t()> after;
+  bool queued = false;
+  GateRelease gates;
 };
 
 // FRI commit of one group (src/fri.rs:551-633), layer 0 and its tree
@@ -565,7 +581,7 @@ struct GateRelease {
 // stands between a challenge and its fold.
 int run_fri_commit(z0p_gpu_ctx* c, const FriShape& s, const FriParams& fp, const FriBufs& fb,
                    uint64_t poly_len, uint64_t degree_bound, Transcript* const* ts, uint32_t K,
-                   const HioPlan& h, FriOut* outs) {
+                   const HioPlan& h, FriOut* outs, FriTail* tail = nullptr) {
   uint8_t dims[24];  // src/fri.rs:1450-1456
   for (int i = 0; i < 8; i++) {
     dims[i] = (uint8_t)(s.m >> (8 * i));
@@ -638,22 +654,41 @@ int run_fri_commit(z0p_gpu_ctx* c, const FriShape& s, const FriParams& fp, const
   }
   for (size_t l = 0;; l++) {
     if (gated_tail(s, l)) {
-      while (c->gate_ev.size() < L) {
+      while (c->gate_ev.size() < L + 1) {
         cudaEvent_t e;
         CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
         c->gate_ev.push_back(e);
       }
       const uint32_t epoch = ++c->go_epoch;
-      volatile unsigned int* gates = reinterpret_cast<volatile unsigned int*>(c->hio + h.gates);
-      GateRelease release{gates, l, L - 1, epoch};
+      unsigned int* gates_dev = hio_dev<unsigned int>(c, h.gates);
+      GateRelease local;
+      GateRelease& rel = tail ? tail->gates : local;
+      rel.gates = reinterpret_cast<volatile unsigned int*>(c->hio + h.gates);
+      rel.epoch = epoch;
+      rel.next = l;
+      rel.end = tail ? L + 1 : L - 1;
       CK(cudaEventRecord(c->gate_ev[l], c->stream));  // layer l's cap
       for (size_t j = l; j + 1 < L; j++) {
         FoldArgs fa = fold_args(j);
-        fa.go = hio_dev<unsigned int>(c, h.gates) + j;
+        fa.go = gates_dev + j;
         fa.go_epoch = epoch;
         uint32_t built = 0;
         CK(launch::fri_fold(c->stream, c->tb, fa, &built, K));
         CK(cudaEventRecord(c->gate_ev[j + 1], c->stream));  // layer j+1's cap
+      }
+      if (tail) {
+        if (fp.grinding_bits > 0)
+          CK(launch::grind(c->stream, hio_dev<uint32_t>(c, h.heads), kPowHeadBytes,
+                           fp.grinding_bits, grind_state(c),
+                           hio_dev<unsigned long long>(c, h.grind), 1ull << 40, K,
+                           gates_dev + (L - 1), epoch, c->tb.fault));
+        CK(cudaEventRecord(c->gate_ev[L], c->stream));  // the PoW results
+        tail->oa->go = gates_dev + L;
+        tail->oa->go_epoch = epoch;
+        tail->oa->fault = c->tb.fault;
+        CK(launch::openings(c->stream, *tail->oa, K));
+        if (tail->after) CK(tail->after());
+        tail->queued = true;
       }
       c->d2h += (uint64_t)K * h.final_bytes;  // written by the last fold
       for (size_t j = l;; j++) {
@@ -662,8 +697,7 @@ int run_fri_commit(z0p_gpu_ctx* c, const FriShape& s, const FriParams& fp, const
         absorb_cap(j);
         if (last) break;
         fold_tables(j, false);
-        __atomic_store_n(const_cast<unsigned int*>(gates + j), epoch, __ATOMIC_RELEASE);
-        release.next = j + 1;
+        rel.open_next();  // gate j
       }
       break;
     }
@@ -729,20 +763,12 @@ int run_fri_open(z0p_gpu_ctx* c, const FriShape& s, const FriParams& fp, Transcr
   return Z0P_OK;
 }
 
-int run_fri(z0p_gpu_ctx* c, const FriShape& s, const FriParams& fp, const FriBufs& fb,
-            uint64_t poly_len, uint64_t degree_bound, Transcript* const* ts, uint32_t K,
-            const HioPlan& h, FriOut* outs) {
-  RC(run_fri_commit(c, s, fp, fb, poly_len, degree_bound, ts, K, h, outs));
-  return run_fri_open(c, s, fp, ts, K, h, outs);
-}
-
-// Gathers every opening of the group on the device (kernels.h, OpenArgs)
-// into the mapped buffer; `oa` arrives with its trace fields and strides set.
-int run_openings(z0p_gpu_ctx* c, const FriShape& s, const FriBufs& fb, const HioPlan& h,
-                 const FriOut* outs, uint32_t K, OpenArgs& oa) {
+// The openings gather's arguments (kernels.h, OpenArgs) for a group: every
+// opening lands in the mapped buffer; `oa` arrives with its trace fields and
+// strides set.
+void prepare_openings(z0p_gpu_ctx* c, const FriShape& s, const FriBufs& fb, const HioPlan& h,
+                      OpenArgs& oa) {
   const uint64_t Q = h.queries;
-  for (uint32_t k = 0; k < K; k++)
-    std::memcpy(c->hio + h.indices + 8 * Q * k, outs[k].indices.data(), 8 * Q);
   oa.indices = hio_dev<uint64_t>(c, h.indices);
   oa.out = hio_dev<uint32_t>(c, h.open);
   oa.nq = (uint32_t)Q;
@@ -754,10 +780,75 @@ int run_openings(z0p_gpu_ctx* c, const FriShape& s, const FriBufs& fb, const Hio
   for (uint32_t d = 0; d < oa.nlayers; d++)
     oa.layer[d] = OpenLayer{fb.layer[d], fb.tree[d], s.leaves[d], s.depth[d] - s.drop[d],
                             h.layer_off[d]};
+}
+
+void write_indices(z0p_gpu_ctx* c, const HioPlan& h, const FriOut* outs, uint32_t K) {
+  const uint64_t Q = h.queries;
+  for (uint32_t k = 0; k < K; k++)
+    std::memcpy(c->hio + h.indices + 8 * Q * k, outs[k].indices.data(), 8 * Q);
+  c->h2d += 8 * Q * K;                  // indices read in place
+  c->d2h += 4ull * h.stride * Q * K;    // opening blocks
+}
+
+// Gathers every opening of the group on the device, the query indices known.
+int run_openings(z0p_gpu_ctx* c, const FriShape& s, const FriBufs& fb, const HioPlan& h,
+                 const FriOut* outs, uint32_t K, OpenArgs& oa) {
+  write_indices(c, h, outs, K);
+  prepare_openings(c, s, fb, h, oa);
   CK(launch::openings(c->stream, oa, K));
   CK(sync(c, "openings"));
-  c->h2d += 8 * Q * K;                      // indices read in place
-  c->d2h += 4ull * h.stride * Q * K;        // opening blocks
+  return Z0P_OK;
+}
+
+// A prover's FRI commitment, opening and openings gather (src/fri.rs:551-666
+// and the proof's query loop), `oa` carrying the trace fields, `after` any
+// kernels that read the query indices after the gather. With a gated tail
+// the PoW search and the gather are queued with the folds; the host then
+// fills their inputs and opens their gates in turn. Ends with the openings
+// in the mapped buffer.
+int run_fri_openings(z0p_gpu_ctx* c, const FriShape& s, const FriParams& fp, const FriBufs& fb,
+                     uint64_t poly_len, uint64_t degree_bound, Transcript* const* ts, uint32_t K,
+                     const HioPlan& h, FriOut* outs, OpenArgs& oa,
+                     std::function<cudaError_t()> after = {}) {
+  prepare_openings(c, s, fb, h, oa);
+  FriTail tail;
+  tail.oa = &oa;
+  tail.after = after;
+  RC(run_fri_commit(c, s, fp, fb, poly_len, degree_bound, ts, K, h, outs, &tail));
+  if (!tail.queued) {
+    RC(run_fri_open(c, s, fp, ts, K, h, outs));
+    write_indices(c, h, outs, K);
+    CK(launch::openings(c->stream, oa, K));
+    if (after) CK(after());
+    CK(sync(c, "openings"));
+    return Z0P_OK;
+  }
+  if (fp.grinding_bits > 0) {  // src/fri.rs:645-650, src/transcript.rs:206-228
+    uint32_t* heads = reinterpret_cast<uint32_t*>(c->hio + h.heads);
+    for (uint32_t k = 0; k < K; k++) {
+      std::vector<uint8_t> head = pow_head(*ts[k], "fri-pow");
+      set_head(heads + kPowHeadWords * k, head.data(), head.size());
+    }
+    c->h2d += 4ull * kPowHeadWords * K;
+    tail.gates.open_next();  // the PoW search's gate
+    CK(sync(c, "grind", c->gate_ev[s.len.size()]));
+    for (uint32_t k = 0; k < K; k++) {
+      RC(check_grind(c, h.grind, k, &outs[k].nonce));
+      uint8_t nb[8];
+      for (int i = 0; i < 8; i++) nb[i] = (uint8_t)(outs[k].nonce >> (8 * i));
+      transcript_absorb(*ts[k], "fri-pow", nb, 8);
+    }
+  } else {
+    tail.gates.open_next();  // nothing behind it
+  }
+  for (uint32_t k = 0; k < K; k++) {
+    outs[k].indices.resize(fp.num_queries);
+    for (uint64_t i = 0; i < fp.num_queries; i++)
+      outs[k].indices[i] = challenge_index(*ts[k], "fri-query", s.m);
+  }
+  write_indices(c, h, outs, K);
+  tail.gates.open_next();  // the gather's gate
+  CK(sync(c, "openings"));
   return Z0P_OK;
 }
 
@@ -1096,13 +1187,12 @@ int air_prove_general(z0p_gpu_ctx* c, const z0p_air_params& p, const GeneralAir&
                           h.fri_cap_bytes[0] / 4));
   Transcript* ts[1] = {&t};
   FriOut fo;
-  RC(run_fri(c, s, fp, fb, m, N + g.n_rand - 1, ts, 1, h, &fo));
   const uint64_t offset = m / N;
   OpenArgs oa{};
   oa.lde = lde_a; oa.lde_b = lde_b; oa.shift = offset;
   oa.ttree = ttree; oa.tleaves = tleaves; oa.tsteps = tsteps;
   oa.logN = logL; oa.logB = logB; oa.ncol = 0;
-  RC(run_openings(c, s, fb, h, &fo, 1, oa));
+  RC(run_fri_openings(c, s, fp, fb, m, N + g.n_rand - 1, ts, 1, h, &fo, oa));
   Writer w(out, need);  // air::Proof::to_bytes (src/air.rs:262-281)
   w.byte(6);
   w.u32((uint32_t)(column_cap.size() / 32));
@@ -1632,11 +1722,10 @@ int table_prove_dev(z0p_gpu_ctx* c, const z0p_table_params& p, const uint32_t* t
   Transcript* ts[1] = {&t};
   FriOut fo;
   const uint64_t bound = membership_bound(tlen, N, n_rand);
-  RC(run_fri(c, s, fp, fb, m, bound, ts, 1, h, &fo));
   OpenArgs oa{};  // src/table.rs:412-420
   oa.lde = lde; oa.ttree = ttree; oa.tleaves = m; oa.tsteps = tsteps;
   oa.logN = logL; oa.logB = logB; oa.ncol = 1;
-  RC(run_openings(c, s, fb, h, &fo, 1, oa));
+  RC(run_fri_openings(c, s, fp, fb, m, bound, ts, 1, h, &fo, oa));
   Writer w(out, need);  // table::Proof::to_bytes (src/table.rs:244-262)
   w.byte(6);
   w.u32((uint32_t)(column_cap.size() / 32));
@@ -1807,8 +1896,6 @@ int air_prove(z0p_gpu_ctx* c, const AirTask* tasks, uint32_t K) {
   std::vector<Transcript*> ts(K);
   for (uint32_t k = 0; k < K; k++) ts[k] = tasks[k].ts;
   std::vector<FriOut> fo(K);
-  RC(run_fri(c, s, fp, fb, m, N - 1, ts.data(), K, h, fo.data()));
-
   // Openings: FRI queries plus the two trace leaves per query (src/air.rs:565-591).
   OpenArgs oa{};
   oa.lde = lde_a; oa.cb = cb; oa.tinv = tinv;
@@ -1816,7 +1903,7 @@ int air_prove(z0p_gpu_ctx* c, const AirTask* tasks, uint32_t K) {
   oa.logN = logN; oa.logB = logB; oa.ncol = 0;
   oa.lde_stride = m;
   oa.ttree_stride = ttree_words;
-  RC(run_openings(c, s, fb, h, fo.data(), K, oa));
+  RC(run_fri_openings(c, s, fp, fb, m, N - 1, ts.data(), K, h, fo.data(), oa));
 
   for (uint32_t k = 0; k < K; k++) {
     Writer w(tasks[k].out, need);  // air::Proof::to_bytes (src/air.rs:262-281)
@@ -2085,14 +2172,12 @@ int range_prove_columns(z0p_gpu_ctx* c, const RangeTask* tasks, uint32_t K, cons
   std::vector<Transcript*> ts(K);
   for (uint32_t k = 0; k < K; k++) ts[k] = tasks[k].ts;
   std::vector<FriOut> fo(K);
-  RC(run_fri(c, s, fp, fb, m, bound, ts.data(), K, h, fo.data()));
-
   OpenArgs oa{};  // src/range.rs:483-500
   oa.lde = lde; oa.ttree = ttree; oa.tleaves = m; oa.tsteps = tsteps;
   oa.logN = logL; oa.logB = logB; oa.ncol = (uint32_t)ncol;
   oa.lde_stride = m * ncol;
   oa.ttree_stride = ttree_words;
-  RC(run_openings(c, s, fb, h, fo.data(), K, oa));
+  RC(run_fri_openings(c, s, fp, fb, m, bound, ts.data(), K, h, fo.data(), oa));
 
   for (uint32_t k = 0; k < K; k++) {
     const z0p_range_params& p = *tasks[k].p;
@@ -2540,15 +2625,15 @@ int fold_finalize(z0p_gpu_fold* f, z0p_transcript_state* ts, uint8_t* out) {
   // fri::commit_ext_evals(combined, S - 1) and fri::open (src/fold.rs:517-520).
   Transcript* tp[1] = {&t};
   FriOut fo;
-  RC(run_fri_commit(c, s, fp, fb, m, S - 1, tp, 1, h, &fo));
-  RC(run_fri_open(c, s, fp, tp, 1, h, &fo));
   OpenArgs oa{};
   oa.no_trace = 1;
-  RC(run_openings(c, s, fb, h, &fo, 1, oa));  // also leaves the indices in the mapped buffer
-  CK(launch::fold_openings(st, ca.steps, K, hio_dev<uint64_t>(c, h.indices),
-                           (uint32_t)fp.num_queries, logN, logB, psteps,
-                           hio_dev<uint32_t>(c, h.extra), stride));
-  CK(sync(c, "openings"));
+  // The step openings read the same indices after the gather (stream order):
+  // both gathers end at one synchronisation.
+  RC(run_fri_openings(c, s, fp, fb, m, S - 1, tp, 1, h, &fo, oa, [&]() {
+    return launch::fold_openings(st, ca.steps, K, hio_dev<uint64_t>(c, h.indices),
+                                 (uint32_t)fp.num_queries, logN, logB, psteps,
+                                 hio_dev<uint32_t>(c, h.extra), stride);
+  }));
   // IvcProof::to_bytes (src/fold.rs:281-309).
   Writer w(out, fold_proof_bytes(p, K, s));
   w.byte(6);
