@@ -312,3 +312,49 @@ def _history_digest(oracle, label):
         return len(l).to_bytes(8, "little") + l + len(d).to_bytes(8, "little") + d
 
     return oracle.blake3(frame(b"domain", label) + frame(b"stmt", b"hello"))
+
+
+_UNGATED = r"""
+import sys
+sys.path.insert(0, sys.argv[1])
+import z0p_gb300 as Z
+ctx = Z.default_context(0)
+out = []
+for n, (b, q, f, g, c) in [(64, (8, 12, 8, 0, 0)), (1024, (16, 40, 16, 20, 4)), (256, (4, 12, 4, 2, 1))]:
+    p = Z.air.Params.new(n, b, q, f, 1, 1, 0)
+    p.grinding_bits = g
+    p.cap_height = c
+    out.append(Z.air.prove(p, Z.Transcript(b"ungated/%d" % n), ctx).hex())
+fp = Z.fri.Params.new(4, 12, 4)
+vals = [(7 * i + 3) % 2013265921 for i in range(256)]
+st = Z.fri.commit(vals, fp, Z.Transcript(b"ungated/fri"), ctx)
+out.append(st.commitment.hex())
+print(" ".join(out))
+"""
+
+
+def test_ungated_folds_prove_the_same_bytes(z0p, oracle, gpu_ctx):
+    """Where launches are serialised (an injected tool, CUDA_LAUNCH_BLOCKING),
+    the small folds are launched after their tables instead of behind gates
+    (Z0P_GATES=0 forces the same): the proof bytes do not change."""
+    import subprocess
+    import sys
+    env = dict(os.environ, Z0P_GATES="0")
+    r = subprocess.run([sys.executable, "-c", _UNGATED, ROOT], capture_output=True, text=True,
+                       env=env, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    ungated = r.stdout.split()
+    gated = []
+    for n, (b, q, f, g, c) in [(64, (8, 12, 8, 0, 0)), (1024, (16, 40, 16, 20, 4)),
+                               (256, (4, 12, 4, 2, 1))]:
+        pz = z0p.air.Params.new(n, b, q, f, 1, 1, 0)
+        pz.grinding_bits = g
+        pz.cap_height = c
+        proof = z0p.air.prove(pz, z0p.Transcript(b"ungated/%d" % n), gpu_ctx)
+        po = oracle.air_params_new(n, b, q, f, 1, 1, 0, g, c)
+        assert proof == oracle.air_prove(po, oracle.Transcript(b"ungated/%d" % n))
+        gated.append(proof.hex())
+    fp = z0p.fri.Params.new(4, 12, 4)
+    vals = [(7 * i + 3) % 2013265921 for i in range(256)]
+    gated.append(z0p.fri.commit(vals, fp, z0p.Transcript(b"ungated/fri"), gpu_ctx).commitment.hex())
+    assert ungated == gated

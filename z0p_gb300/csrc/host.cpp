@@ -134,12 +134,50 @@ static void chunk_block(const uint8_t* p, size_t len, uint32_t i, uint32_t w[16]
   block_words(p + off, len - off < 64 ? len - off : 64, w);
 }
 
+// The block cache of the last transcript this thread finished with. A prove
+// call works on a copy of the caller's state and hands it back, so the next
+// call usually starts from the same tail: its chunks' cached chaining values
+// are taken over instead of re-hashing up to 2 KiB. Chunk h's entry is used
+// only for a state with the same chunk count whose tail repeats the cached
+// blocks byte for byte, with a byte after them inside the chunk (so none of
+// them is the chunk's last); its chaining value depends on nothing else.
+namespace {
+struct CacheMemo {
+  bool valid = false;
+  uint64_t next_index = 0;
+  uint32_t cv[2][8];
+  uint32_t nblk[2];
+  uint8_t blocks[2 * CHUNK_LEN];  // the cached blocks' bytes, at their tail offsets
+};
+thread_local CacheMemo g_memo;
+}  // namespace
+
 Hasher::Hasher(z0p_transcript_state* s) : st(s) {
+  const CacheMemo& m = g_memo;
+  const bool same_chunks = m.valid && m.next_index == st->next_index && st->tail_len < 2 * CHUNK_LEN;
   for (int h = 0; h < 2; h++) {
     std::memcpy(cv[h], IV, 32);
     nblk[h] = 0;
+    if (!same_chunks || m.nblk[h] == 0) continue;
+    const size_t base = CHUNK_LEN * h, covered = 64 * (size_t)m.nblk[h];
+    if (st->tail_len > base + covered && covered < CHUNK_LEN &&
+        std::memcmp(st->tail + base, m.blocks + base, covered) == 0) {
+      std::memcpy(cv[h], m.cv[h], 32);
+      nblk[h] = m.nblk[h];
+    }
   }
   advance();
+}
+
+void Hasher::remember() const {
+  CacheMemo& m = g_memo;
+  m.valid = true;
+  m.next_index = st->next_index;
+  for (int h = 0; h < 2; h++) {
+    std::memcpy(m.cv[h], cv[h], 32);
+    m.nblk[h] = nblk[h];
+    std::memcpy(m.blocks + CHUNK_LEN * h, st->tail + CHUNK_LEN * h, 64 * (size_t)nblk[h]);
+  }
 }
 
 // Folds into cv[h] every block of tail chunk h that has at least one byte

@@ -43,6 +43,9 @@ struct Hasher {
   explicit Hasher(z0p_transcript_state* s);  // builds the cache from the state
   void update(const uint8_t* data, size_t len);
   void finalize(uint8_t out[32]) const;
+  // Leaves this cache for the next Hasher this thread builds on the same
+  // tail (host.cpp, CacheMemo).
+  void remember() const;
 
  private:
   void advance();
@@ -52,6 +55,7 @@ struct Hasher {
 class Transcript {
  public:
   explicit Transcript(z0p_transcript_state* st) : h_(st) {}
+  ~Transcript() { h_.remember(); }
   void absorb_raw(const uint8_t* label, size_t llen, const uint8_t* data, size_t len);
   void absorb(const char* label, const uint8_t* data, size_t len);
   void squeeze(const uint8_t* label, size_t llen, uint8_t out[32]);

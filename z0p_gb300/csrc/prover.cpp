@@ -17,6 +17,7 @@
 #include <functional>
 #include <map>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -534,11 +535,29 @@ int check_grind(z0p_gpu_ctx* c, size_t res_at, uint32_t k, uint64_t* nonce) {
   return Z0P_OK;
 }
 
+// Gated launches need a host thread that queues ahead and opens the gates
+// while they wait. A process whose launches block (CUDA_LAUNCH_BLOCKING=1)
+// or run under an injected tool that serialises them (profilers and
+// checkers set CUDA_INJECTION64_PATH) would leave each gated launch waiting
+// out its bound, so there the folds are launched after their tables, as
+// the large ones are. Z0P_GATES=0 turns gates off as well.
+bool gates_enabled() {
+  static const bool on = [] {
+    const char* g = std::getenv("Z0P_GATES");
+    if (g && std::strcmp(g, "0") == 0) return false;
+    const char* b = std::getenv("CUDA_LAUNCH_BLOCKING");
+    if (b && std::strcmp(b, "1") == 0) return false;
+    const char* inj = std::getenv("CUDA_INJECTION64_PATH");
+    return !(inj && *inj);
+  }();
+  return on;
+}
+
 // Whether folds l, l+1, ... to the final layer are all small folds (one
 // launch that also finishes the next layer's tree, tables read in place),
 // so that they can be queued ahead behind gates.
 bool gated_tail(const FriShape& s, size_t l) {
-  if (l + 1 >= s.len.size()) return false;
+  if (!gates_enabled() || l + 1 >= s.len.size()) return false;
   for (size_t j = l; j + 1 < s.len.size(); j++)
     if (s.len[j] < 16 || s.leaves[j + 1] > kFuseMaxLeaves) return false;
   return true;
