@@ -158,7 +158,13 @@ int z0p_range_proof_size(const z0p_range_params *params, size_t *len);
 
 /* ---------------------------------------------------------- contexts ---- */
 /* Creates a prover context on CUDA device `device` (one stream, lazily grown
- * device workspace). */
+ * device workspace).
+ * A prove call queues the small folds at the end of a FRI commitment, the PoW
+ * search and the openings gather ahead of their inputs, each waiting on a
+ * gate word that the calling thread opens once it has written them. The
+ * gates are off (each such launch follows its inputs) when the environment
+ * sets Z0P_GATES=0 or CUDA_LAUNCH_BLOCKING=1, or when a tool is injected
+ * through CUDA_INJECTION64_PATH; proofs are the same bytes either way. */
 int z0p_gpu_ctx_create(int device, z0p_gpu_ctx **out);
 void z0p_gpu_ctx_destroy(z0p_gpu_ctx *ctx);
 /* The context's cudaStream_t (as void*), for callers that time or order work. */
