@@ -2431,11 +2431,14 @@ cudaError_t grind(cudaStream_t st, const uint32_t* head, uint32_t head_len, uint
   // that passes the best hit, so at most one nonce per thread is hashed past
   // the answer: the grid can fill the GPU (four CTAs per SM reach the hash
   // ceiling) without wasting much, but stays below the expected search.
+  // A search of a few bits (2^bits within a few chunks) takes that many CTAs,
+  // not a full grid: the answer is the same, the launch and the last-CTA
+  // handshake shorter.
   uint64_t want = (1ull << bits) / kGrindChunk;
   const int per_sm = (int)current_schedule().grind_ctas_per_sm;
   int ctas = want > (uint64_t)(per_sm * sms) ? per_sm * sms : (int)want;
   if (ctas > max_ctas) ctas = max_ctas;
-  if (ctas < sms) ctas = sms;
+  if (ctas < 1) ctas = 1;
   Stage stg("grind", st);
   stg.launched();
   grind_kernel<<<dim3(ctas, nproofs), kGrindThreads, 0, st>>>(a);

@@ -46,6 +46,24 @@ class Params(FoldParams):
         return self
 
 
+_U32P = C.POINTER(C.c_uint32)
+
+
+def _u32_column(col):
+    """A segment column as 32-bit words: a short list of Python ints becomes a
+    ctypes array directly (a few microseconds less per segment than through
+    numpy); anything else goes through numpy, which also raises for values
+    outside 32 bits (the C boundary then rejects values >= p)."""
+    if (isinstance(col, (list, tuple)) and len(col) <= 4096
+            and all(type(v) is int and 0 <= v < 2**32 for v in col)):
+        return (C.c_uint32 * len(col))(*col)
+    return np.ascontiguousarray(np.asarray(col, dtype=np.uint32))
+
+
+def _u32_ptr(col):
+    return col if isinstance(col, C.Array) else col.ctypes.data_as(_U32P)
+
+
 class Accumulator:
     """fold::Accumulator (src/fold.rs:362-561); segments stay on the context's device."""
 
@@ -70,13 +88,11 @@ class Accumulator:
         return lib().z0p_gpu_fold_len(self.h)
 
     def add_segment(self, col_a, col_b, transcript: Transcript) -> None:
-        a = np.ascontiguousarray(np.asarray(col_a, dtype=np.uint32))
-        b = np.ascontiguousarray(np.asarray(col_b, dtype=np.uint32))
+        a, b = _u32_column(col_a), _u32_column(col_b)
         if len(a) != len(b):
             raise ValueError("segment columns must have one length")
-        u32p = C.POINTER(C.c_uint32)
-        check(lib().z0p_gpu_fold_add_segment(self.h, a.ctypes.data_as(u32p), b.ctypes.data_as(u32p),
-                                             len(a), C.byref(transcript.state)))
+        check(lib().z0p_gpu_fold_add_segment(self.h, _u32_ptr(a), _u32_ptr(b), len(a),
+                                             C.byref(transcript.state)))
 
     def finalize(self, transcript: Transcript) -> bytes:
         n = C.c_size_t()
