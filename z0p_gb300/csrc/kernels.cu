@@ -1313,77 +1313,111 @@ __global__ void row_inverses_kernel(uint32_t* __restrict__ tinv, uint32_t w_last
 // builds the layer-0 tree (cta_subtree); each thread inverts its four rows'
 // x - w_last and x omega_s^-1 - w_last (= x_{q-1} - w_last on a coset) in
 // one batch instead of reading T.
+// The segments go by in the outer loop, their table entries staged in shared
+// memory kCombineStage at a time: per segment a thread issues the sixteen
+// column loads of its four rows together, so a segment costs one memory
+// latency rather than four dependent pairs of them.
+constexpr uint32_t kCombineStage = 32;
 template <bool kFused>
 __global__ void __launch_bounds__(kThreads) fold_combine_kernel(FoldCombineArgs a, Tables tb) {
   __shared__ uint32_t buf[kFused ? 2 * kThreads * kTopStride : 1];
+  __shared__ FoldStepDev stage[kCombineStage];
+  static_assert(sizeof(FoldStepDev) % 4 == 0, "staged as words");
   const uint32_t logm = a.logN + a.logB;
   const uint32_t quarter = 1u << (logm - 2);
   const uint32_t u = blockIdx.x * blockDim.x + threadIdx.x;
-  if (!kFused && u >= quarter) return;
+  const bool live = u < quarter;
   const uint32_t nt = quarter < kThreads ? quarter : kThreads;
-  uint32_t d[8];
-  if (u < quarter) {
   const uint32_t N = 1u << a.logN, B = 1u << a.logB;
-  uint32_t k0 = u, P;
-  if (kFused) {
-    P = u;
-    k0 = brev_bits(u, logm - 2);
-  } else {
-    if (a.logN >= 2) {
-      const uint32_t j = u >> (a.logN - 2), q0 = u & ((N >> 2) - 1u);
-      k0 = (q0 << a.logB) | j;
+  uint32_t k0 = u, P = 0;
+  size_t at[4] = {}, atn[4] = {};
+  uint32_t tm[4] = {}, t0[4] = {}, iz[4] = {};
+  if (live) {
+    if (kFused) {
+      P = u;
+      k0 = brev_bits(u, logm - 2);
+    } else {
+      if (a.logN >= 2) {
+        const uint32_t j = u >> (a.logN - 2), q0 = u & ((N >> 2) - 1u);
+        k0 = (q0 << a.logB) | j;
+      }
+      P = brev_bits(k0, logm - 2);
     }
-    P = brev_bits(k0, logm - 2);
-  }
-  uint32_t xs[4];
-  quad_points(tb, k0, logm, xs);
-  uint32_t inv[8];  // kFused: T(q) of row s at s, T(q - 1) at 4 + s
-  if (kFused) {
+    uint32_t xs[4];
+    quad_points(tb, k0, logm, xs);
+    uint32_t inv[8];  // kFused: T(q) of row s at s, T(q - 1) at 4 + s
+    if (kFused) {
+#pragma unroll
+      for (int s = 0; s < 4; s++) {
+        inv[s] = fsub(xs[s], a.w_last_m);
+        inv[4 + s] = fsub(mmul(xs[s], a.w_last_m), a.w_last_m);
+      }
+      batch_minv(inv);
+    }
 #pragma unroll
     for (int s = 0; s < 4; s++) {
-      inv[s] = fsub(xs[s], a.w_last_m);
-      inv[4 + s] = fsub(mmul(xs[s], a.w_last_m), a.w_last_m);
+      const uint32_t k = k0 + (uint32_t)s * quarter;
+      const uint32_t j = k & (B - 1u), q = k >> a.logB;
+      const size_t base = (size_t)j << a.logN;
+      at[s] = base + q;
+      atn[s] = base + ((q + 1u) & (N - 1u));
+      tm[s] = kFused ? inv[4 + s] : __ldg(a.tinv + base + ((q - 1u) & (N - 1u)));
+      t0[s] = kFused ? inv[s] : __ldg(a.tinv + at[s]);
+      iz[s] = mmul(fsub_lazy(xs[s], a.w_last_m), __ldg(a.zinv + j));
     }
-    batch_minv(inv);
   }
-  uint32_t leaf[16];
+  uint32_t acc[4][4] = {};
+  for (uint32_t c0 = 0; c0 < a.nsteps; c0 += kCombineStage) {
+    const uint32_t cn = a.nsteps - c0 < kCombineStage ? a.nsteps - c0 : kCombineStage;
+    __syncthreads();
+    const uint32_t* src = reinterpret_cast<const uint32_t*>(a.steps + c0);
+    for (uint32_t i = threadIdx.x; i < cn * (uint32_t)(sizeof(FoldStepDev) / 4); i += blockDim.x)
+      reinterpret_cast<uint32_t*>(stage)[i] = __ldg(src + i);
+    __syncthreads();
+    if (!live) continue;
+    for (uint32_t st = 0; st < cn; st++) {
+      const FoldStepDev& S = stage[st];
+      uint32_t av[4], bv[4], an[4], bn[4];
 #pragma unroll
-  for (int s = 0; s < 4; s++) {
-    const uint32_t k = k0 + (uint32_t)s * quarter;
-    const uint32_t j = k & (B - 1u), q = k >> a.logB;
-    const size_t base = (size_t)j << a.logN;
-    const size_t at = base + q, atn = base + ((q + 1u) & (N - 1u));
-    const uint32_t tm = kFused ? inv[4 + s] : __ldg(a.tinv + base + ((q - 1u) & (N - 1u)));
-    const uint32_t t0 = kFused ? inv[s] : __ldg(a.tinv + at);
-    const uint32_t iz = mmul(fsub_lazy(xs[s], a.w_last_m), __ldg(a.zinv + j));
-    uint32_t acc[4] = {0u, 0u, 0u, 0u};
-    for (uint32_t st = 0; st < a.nsteps; st++) {
-      const FoldStepDev& S = a.steps[st];
-      const uint32_t av = __ldg(S.a + at), bv = __ldg(S.b + at);
-      const uint32_t an = __ldg(S.a + atn), bn = __ldg(S.b + atn);
-      const uint32_t tr1 = mmul(fsub_lazy(an, bv), iz);
-      const uint32_t tr2 = mmul(fsub_lazy(bn, fadd(av, bv)), iz);
-      const uint32_t ia = mmul(fsub_lazy(av, S.in_a), tm);
-      const uint32_t ib = mmul(fsub_lazy(bv, S.in_b), tm);
-      const uint32_t oa = mmul(fsub_lazy(av, S.out_a), t0);
-      const uint32_t ob = mmul(fsub_lazy(bv, S.out_b), t0);
+      for (int s = 0; s < 4; s++) {
+        av[s] = __ldg(S.a + at[s]);
+        bv[s] = __ldg(S.b + at[s]);
+        an[s] = __ldg(S.a + atn[s]);
+        bn[s] = __ldg(S.b + atn[s]);
+      }
 #pragma unroll
-      for (int c = 0; c < 4; c++) {
-        const uint32_t v = fadd(mdot4(tr1, S.ga[0][c], tr2, S.ga[1][c], ia, S.ga[2][c], ib, S.ga[3][c]),
-                                mdot2(oa, S.ga[4][c], ob, S.ga[5][c]));
-        acc[c] = fadd(acc[c], v);
+      for (int s = 0; s < 4; s++) {
+        const uint32_t tr1 = mmul(fsub_lazy(an[s], bv[s]), iz[s]);
+        const uint32_t tr2 = mmul(fsub_lazy(bn[s], fadd(av[s], bv[s])), iz[s]);
+        const uint32_t ia = mmul(fsub_lazy(av[s], S.in_a), tm[s]);
+        const uint32_t ib = mmul(fsub_lazy(bv[s], S.in_b), tm[s]);
+        const uint32_t oa = mmul(fsub_lazy(av[s], S.out_a), t0[s]);
+        const uint32_t ob = mmul(fsub_lazy(bv[s], S.out_b), t0[s]);
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+          const uint32_t v = fadd(mdot4(tr1, S.ga[0][c], tr2, S.ga[1][c], ia, S.ga[2][c], ib,
+                                        S.ga[3][c]),
+                                  mdot2(oa, S.ga[4][c], ob, S.ga[5][c]));
+          acc[s][c] = fadd(acc[s][c], v);
+        }
       }
     }
-    const int t = (s == 1) ? 2 : (s == 2) ? 1 : s;  // position 4P + brev2(s)
-#pragma unroll
-    for (int c = 0; c < 4; c++) leaf[4 * t + c] = acc[c];
   }
-  uint4* dst = reinterpret_cast<uint4*>(a.layer0 + 16 * (size_t)P);
+  uint32_t d[8];
+  if (live) {
+    uint32_t leaf[16];
 #pragma unroll
-  for (int t = 0; t < 4; t++)
-    dst[t] = make_uint4(leaf[4 * t], leaf[4 * t + 1], leaf[4 * t + 2], leaf[4 * t + 3]);
-  blake3_leaf64(leaf, d);
-  store_digest(a.leaves + 8 * (size_t)P, d);
+    for (int s = 0; s < 4; s++) {
+      const int t = (s == 1) ? 2 : (s == 2) ? 1 : s;  // position 4P + brev2(s)
+#pragma unroll
+      for (int c = 0; c < 4; c++) leaf[4 * t + c] = acc[s][c];
+    }
+    uint4* dst = reinterpret_cast<uint4*>(a.layer0 + 16 * (size_t)P);
+#pragma unroll
+    for (int t = 0; t < 4; t++)
+      dst[t] = make_uint4(leaf[4 * t], leaf[4 * t + 1], leaf[4 * t + 2], leaf[4 * t + 3]);
+    blake3_leaf64(leaf, d);
+    store_digest(a.leaves + 8 * (size_t)P, d);
   }
   if constexpr (kFused)
     cta_subtree(d, buf, nt, (uint64_t)blockIdx.x * kThreads, a.leaves, quarter, a.top, a.cap,
