@@ -633,29 +633,39 @@ __global__ void __launch_bounds__(kSegmentMaxRows) fold_segment_kernel(
   uint2* tw_inv = reinterpret_cast<uint2*>(ext + 2 * B * cs);
   uint2* tw_fwd = tw_inv + tw_entries(L);
   uint32_t* buf = reinterpret_cast<uint32_t*>(tw_fwd + tw_entries(L));  // 2 * 9 * m words
-  const uint32_t t = threadIdx.x;
+  const uint32_t t = threadIdx.x;  // blockDim.x == m: two LDE inputs per thread
+  // The columns (mapped host memory) are requested first; the twiddles and
+  // each input's twist factor load while they arrive.
+  uint32_t v_in = 0u;
+  if (t < 2 * S) v_in = cols[t];
   NttArgs a{};
   a.tb = tb;
   a.inverse = 1;
   stage_twiddles<L>(tw_inv, a);
   a.inverse = 0;
   stage_twiddles<L>(tw_fwd, a);
-  for (uint32_t e = t; e < 2 * S; e += blockDim.x) {
-    const uint32_t c = e >> L, i = e & (S - 1u);
-    const uint32_t v = cols[e];
-    if (v >= kP) atomicOr(bad, 1u);
-    coef[c * cs + spos(i)] = v;
+  // Input e = b S + i of coset b = c B + j takes coefficient i of column c
+  // times 31^i / S, twisted by omega_m^(j i).
+  uint32_t fac[2];
+#pragma unroll
+  for (int h = 0; h < 2; h++) {
+    const uint32_t e = t + (uint32_t)h * m;
+    const uint32_t b = e >> L, i = e & (S - 1u), j = b & (B - 1u);
+    fac[h] = mmul(gamma_pow(tb, i), ninv_m);
+    if (j) fac[h] = mmul(fac[h], root_pow(tb, (j * i) << (kRootBits - logm)));
+  }
+  if (t < 2 * S) {
+    if (v_in >= kP) atomicOr(bad, 1u);
+    coef[(t >> L) * cs + spos(t & (S - 1u))] = v_in;
   }
   __syncthreads();
   smem_dif_t<L>(coef, tw_inv, 2, cs);
-  // Coefficient i of column c times 31^i / S, then twisted by omega_m^(j i)
-  // into coset j's input.
-  for (uint32_t e = t; e < 2 * m; e += blockDim.x) {
-    const uint32_t b = e >> L, i = e & (S - 1u);  // b = c B + j
-    const uint32_t c = b >> logB, j = b & (B - 1u);
-    uint32_t v = mmul(mmul(coef[c * cs + spos(brev_bits(i, L))], gamma_pow(tb, i)), ninv_m);
-    if (j) v = mmul(v, root_pow(tb, (j * i) << (kRootBits - logm)));
-    ext[b * cs + spos(i)] = v;
+#pragma unroll
+  for (int h = 0; h < 2; h++) {
+    const uint32_t e = t + (uint32_t)h * m;
+    const uint32_t b = e >> L, i = e & (S - 1u);
+    const uint32_t c = b >> logB;
+    ext[b * cs + spos(i)] = mmul(coef[c * cs + spos(brev_bits(i, L))], fac[h]);
   }
   __syncthreads();
   smem_dif_t<L>(ext, tw_fwd, 2 * B, cs);
