@@ -43,7 +43,6 @@ uint64_t brev(uint64_t x, uint32_t bits) {
 // ---------------------------------------------------------------- BLAKE3 ----
 static const uint32_t IV[8] = {0x6A09E667u, 0xBB67AE85u, 0x3C6EF372u, 0xA54FF53Au,
                                0x510E527Fu, 0x9B05688Cu, 0x1F83D9ABu, 0x5BE0CD19u};
-static const uint8_t MSG_PERM[16] = {2, 6, 3, 10, 7, 0, 4, 13, 1, 11, 12, 5, 9, 14, 15, 8};
 enum : uint32_t { CHUNK_START = 1, CHUNK_END = 2, PARENT = 4, ROOT = 8 };
 constexpr size_t CHUNK_LEN = 1024;
 
@@ -70,35 +69,62 @@ static inline void put64(uint8_t* p, uint64_t v) {
     b = rotr(b ^ c, 7);           \
   } while (0)
 
+// The message words each round reads (specification: the permutation applied
+// after every round), as compile-time indices, so the message stays in
+// registers instead of being permuted through memory seven times.
+struct MsgSchedule {
+  uint8_t at[7][16];
+};
+static constexpr MsgSchedule make_schedule() {
+  constexpr uint8_t perm[16] = {2, 6, 3, 10, 7, 0, 4, 13, 1, 11, 12, 5, 9, 14, 15, 8};
+  MsgSchedule r{};
+  for (int i = 0; i < 16; i++) r.at[0][i] = (uint8_t)i;
+  for (int k = 1; k < 7; k++)
+    for (int i = 0; i < 16; i++) r.at[k][i] = r.at[k - 1][perm[i]];
+  return r;
+}
+static constexpr MsgSchedule SCHEDULE = make_schedule();
+
+template <int R>
+static inline void blake3_round(uint32_t (&v)[16], const uint32_t (&m)[16]) {
+  constexpr const uint8_t* S = SCHEDULE.at[R];
+  Z0P_HG(v[0], v[4], v[8], v[12], m[S[0]], m[S[1]]);
+  Z0P_HG(v[1], v[5], v[9], v[13], m[S[2]], m[S[3]]);
+  Z0P_HG(v[2], v[6], v[10], v[14], m[S[4]], m[S[5]]);
+  Z0P_HG(v[3], v[7], v[11], v[15], m[S[6]], m[S[7]]);
+  Z0P_HG(v[0], v[5], v[10], v[15], m[S[8]], m[S[9]]);
+  Z0P_HG(v[1], v[6], v[11], v[12], m[S[10]], m[S[11]]);
+  Z0P_HG(v[2], v[7], v[8], v[13], m[S[12]], m[S[13]]);
+  Z0P_HG(v[3], v[4], v[9], v[14], m[S[14]], m[S[15]]);
+}
+
 // BLAKE3 compression (specification; src/hash.rs:93-133). Returns the
-// chaining value (first 8 output words). The state lives in locals so the
-// compiler keeps it in registers; the message schedule is applied by index.
+// chaining value (first 8 output words); out may alias cv.
 static void compress_cv(const uint32_t cv[8], const uint32_t block[16], uint64_t counter,
                         uint32_t len, uint32_t flags, uint32_t out[8]) {
-  uint32_t s0 = cv[0], s1 = cv[1], s2 = cv[2], s3 = cv[3];
-  uint32_t s4 = cv[4], s5 = cv[5], s6 = cv[6], s7 = cv[7];
-  uint32_t s8 = IV[0], s9 = IV[1], s10 = IV[2], s11 = IV[3];
-  uint32_t s12 = (uint32_t)counter, s13 = (uint32_t)(counter >> 32), s14 = len, s15 = flags;
-  uint32_t m[16], t[16];
+  uint32_t m[16];
   std::memcpy(m, block, 64);
-  for (int r = 0; r < 7; r++) {
-    Z0P_HG(s0, s4, s8, s12, m[0], m[1]);
-    Z0P_HG(s1, s5, s9, s13, m[2], m[3]);
-    Z0P_HG(s2, s6, s10, s14, m[4], m[5]);
-    Z0P_HG(s3, s7, s11, s15, m[6], m[7]);
-    Z0P_HG(s0, s5, s10, s15, m[8], m[9]);
-    Z0P_HG(s1, s6, s11, s12, m[10], m[11]);
-    Z0P_HG(s2, s7, s8, s13, m[12], m[13]);
-    Z0P_HG(s3, s4, s9, s14, m[14], m[15]);
-    for (int i = 0; i < 16; i++) t[i] = m[MSG_PERM[i]];
-    std::memcpy(m, t, 64);
-  }
-  out[0] = s0 ^ s8; out[1] = s1 ^ s9; out[2] = s2 ^ s10; out[3] = s3 ^ s11;
-  out[4] = s4 ^ s12; out[5] = s5 ^ s13; out[6] = s6 ^ s14; out[7] = s7 ^ s15;
+  uint32_t v[16] = {cv[0], cv[1], cv[2], cv[3], cv[4], cv[5], cv[6], cv[7],
+                    IV[0], IV[1], IV[2], IV[3], (uint32_t)counter, (uint32_t)(counter >> 32), len,
+                    flags};
+  blake3_round<0>(v, m);
+  blake3_round<1>(v, m);
+  blake3_round<2>(v, m);
+  blake3_round<3>(v, m);
+  blake3_round<4>(v, m);
+  blake3_round<5>(v, m);
+  blake3_round<6>(v, m);
+  for (int i = 0; i < 8; i++) out[i] = v[i] ^ v[8 + i];
 }
 #undef Z0P_HG
 
 static void block_words(const uint8_t* p, size_t len, uint32_t w[16]) {
+#if defined(__BYTE_ORDER__) && __BYTE_ORDER__ == __ORDER_LITTLE_ENDIAN__
+  if (len == 64) {  // a full block is its words' bytes in order
+    std::memcpy(w, p, 64);
+    return;
+  }
+#endif
   uint8_t b[64] = {0};
   std::memcpy(b, p, len);
   for (int i = 0; i < 16; i++) w[i] = le32(b + 4 * i);
@@ -288,27 +314,51 @@ void blake3(const uint8_t* data, size_t len, uint8_t out[32]) {
 // ------------------------------------------------------------- transcript ----
 void Transcript::absorb_raw(const uint8_t* label, size_t llen, const uint8_t* data,
                             size_t len) {  // src/transcript.rs:72-77
-  uint8_t b[8];
-  put64(b, llen);
-  h_.update(b, 8);
-  h_.update(label, llen);
-  put64(b, len);
-  h_.update(b, 8);
+  uint8_t hdr[16 + 64];
+  if (llen <= 64) {  // LE64(|label|) || label || LE64(|data|) in one update
+    put64(hdr, llen);
+    std::memcpy(hdr + 8, label, llen);
+    put64(hdr + 8 + llen, len);
+    h_.update(hdr, 16 + llen);
+  } else {
+    put64(hdr, llen);
+    h_.update(hdr, 8);
+    h_.update(label, llen);
+    put64(hdr, len);
+    h_.update(hdr, 8);
+  }
   h_.update(data, len);
 }
 void Transcript::absorb(const char* label, const uint8_t* data, size_t len) {
   absorb_raw((const uint8_t*)label, std::strlen(label), data, len);
 }
 void Transcript::squeeze(const uint8_t* label, size_t llen, uint8_t out[32]) {
-  z0p_transcript_state copy = *h_.st;  // src/transcript.rs:162-171
+  // src/transcript.rs:162-171 on a copy of the history: only the parts in
+  // use (tail bytes, stack entries, counts) are copied.
+  const z0p_transcript_state& s = *h_.st;
+  z0p_transcript_state copy;
+  copy.tail_len = s.tail_len;
+  std::memcpy(copy.tail, s.tail, s.tail_len);
+  copy.stack_len = s.stack_len;
+  std::memcpy(copy.stack, s.stack, 32 * (size_t)s.stack_len);
+  copy.next_index = s.next_index;
+  copy.total_len = s.total_len;
+  copy.counter = s.counter;
   Hasher hc = h_;
   hc.st = &copy;
-  uint8_t b[8];
-  put64(b, llen);
-  hc.update(b, 8);
-  hc.update(label, llen);
-  put64(b, h_.st->counter);
-  hc.update(b, 8);
+  uint8_t sfx[16 + 64];
+  if (llen <= 64) {  // LE64(|label|) || label || LE64(counter) in one update
+    put64(sfx, llen);
+    std::memcpy(sfx + 8, label, llen);
+    put64(sfx + 8 + llen, s.counter);
+    hc.update(sfx, 16 + llen);
+  } else {
+    put64(sfx, llen);
+    hc.update(sfx, 8);
+    hc.update(label, llen);
+    put64(sfx, s.counter);
+    hc.update(sfx, 8);
+  }
   h_.st->counter++;
   hc.finalize(out);
   absorb_raw(label, llen, out, 32);
