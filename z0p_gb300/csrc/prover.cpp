@@ -2448,7 +2448,10 @@ struct FoldStepHost {
   uint32_t claims[4];  // in_a, in_b, out_a, out_b
   uint32_t alpha[6][4];
   std::vector<uint8_t> cap;
-  DevBuf lde, tree;  // [A planes | B planes] coset-major; level-contiguous row tree
+  // In one of the accumulator's slabs: [A planes | B planes] coset-major,
+  // then the level-contiguous row tree.
+  uint32_t* lde = nullptr;
+  uint32_t* tree = nullptr;
 };
 
 }  // namespace
@@ -2458,6 +2461,11 @@ struct z0p_gpu_fold {
   z0p_fold_params p{};
   std::vector<FoldStepHost> steps;
   DevBuf tinv, table;  // row inverses; FoldStepDev table + per-coset 1/(x^s - 1)
+  // Segments' LDEs and trees, several segments to an allocation: slabs of 4,
+  // 8, 16, ... segments, each at most 16 MB (one segment where that is
+  // less), so a short chain makes one allocation, not two per segment.
+  std::vector<DevBuf> slabs;
+  size_t slab_cap = 0, slab_used = 0;
   bool finalized = false;
 };
 
@@ -2491,8 +2499,21 @@ int fold_add(z0p_gpu_fold* f, const uint32_t* col_a, const uint32_t* col_b,
   RC(ensure(c, c->coeffs, 8 * S));
   RC(ensure(c, c->scratch, 8 * m));
   FoldStepHost step;
-  RC(ensure(c, step.lde, 8 * m));
-  RC(ensure(c, step.tree, 32 * tree_digests(m)));
+  const size_t lde_bytes = (8 * m + 255) & ~(size_t)255;
+  const size_t seg_bytes = lde_bytes + ((32 * tree_digests(m) + 255) & ~(size_t)255);
+  if (f->slab_used == f->slab_cap) {
+    size_t n = f->steps.empty() ? 4 : 2 * f->steps.size();
+    const size_t fit = ((size_t)16 << 20) / seg_bytes;
+    if (n > fit) n = fit > 0 ? fit : 1;
+    DevBuf slab;
+    RC(ensure(c, slab, n * seg_bytes));
+    f->slabs.push_back(slab);
+    f->slab_cap = n;
+    f->slab_used = 0;
+  }
+  char* seg = static_cast<char*>(f->slabs.back().p) + f->slab_used * seg_bytes;
+  step.lde = reinterpret_cast<uint32_t*>(seg);
+  step.tree = reinterpret_cast<uint32_t*>(seg + lde_bytes);
   const uint32_t depth = logm, drop = p.cap_height < depth ? (uint32_t)p.cap_height : depth;
   const size_t cap_bytes = 32ull << drop;
   // Segments of up to 2^12 rows are interpolated by the one-CTA transform,
@@ -2513,8 +2534,8 @@ int fold_add(z0p_gpu_fold* f, const uint32_t* col_a, const uint32_t* col_b,
     CK(cudaMemcpyAsync(cols + S, col_b, 4 * S, cudaMemcpyHostToDevice, st));
   }
   c->h2d += 8 * S;
-  uint32_t* lde = (uint32_t*)step.lde.p;
-  uint32_t* tree = (uint32_t*)step.tree.p;
+  uint32_t* lde = step.lde;
+  uint32_t* tree = step.tree;
   if (mapped_cols && launch::fold_segment_ok(logN, logB)) {
     // Small segments: interpolation, LDE, row leaves and tree in one launch.
     CK(launch::fold_segment(st, c->tb, cols, hio_dev<unsigned int>(c, 0), lde, tree,
@@ -2554,6 +2575,7 @@ int fold_add(z0p_gpu_fold* f, const uint32_t* col_a, const uint32_t* col_b,
   for (int k = 0; k < 6; k++) challenge_ext(t, "fold/alpha", step.alpha[k]);
   *ts = work;
   f->steps.push_back(std::move(step));
+  f->slab_used++;  // the segment's slot stays taken only once it is added
   return Z0P_OK;
 }
 
@@ -2581,9 +2603,9 @@ int fold_finalize(z0p_gpu_fold* f, z0p_transcript_state* ts, uint8_t* out) {
     challenge_ext(t, "fold/gamma", g);
     FoldStepHost& h = f->steps[k];
     FoldStepDev& d = table[k];
-    d.a = (const uint32_t*)h.lde.p;
+    d.a = h.lde;
     d.b = d.a + m;
-    d.tree = (const uint32_t*)h.tree.p;
+    d.tree = h.tree;
     d.in_a = h.claims[0]; d.in_b = h.claims[1]; d.out_a = h.claims[2]; d.out_b = h.claims[3];
     for (int j = 0; j < 6; j++) {
       uint32_t ga[4];
@@ -3258,10 +3280,7 @@ void z0p_gpu_fold_destroy(z0p_gpu_fold* f) {
   {
     std::lock_guard<std::mutex> lk(f->ctx->mu);
     cudaSetDevice(f->ctx->device);
-    for (auto& s : f->steps) {
-      release(f->ctx, s.lde);
-      release(f->ctx, s.tree);
-    }
+    for (DevBuf& b : f->slabs) release(f->ctx, b);
     release(f->ctx, f->tinv);
     release(f->ctx, f->table);
   }

@@ -49,14 +49,23 @@ class Params(FoldParams):
 _U32P = C.POINTER(C.c_uint32)
 
 
+_ARRAY_TYPES = {}
+
+
 def _u32_column(col):
-    """A segment column as 32-bit words: a short list of Python ints becomes a
+    """A segment column as 32-bit words: a short list of integers becomes a
     ctypes array directly (a few microseconds less per segment than through
     numpy); anything else goes through numpy, which also raises for values
     outside 32 bits (the C boundary then rejects values >= p)."""
-    if (isinstance(col, (list, tuple)) and len(col) <= 4096
-            and all(type(v) is int and 0 <= v < 2**32 for v in col)):
-        return (C.c_uint32 * len(col))(*col)
+    if isinstance(col, (list, tuple)) and len(col) <= 4096:
+        try:
+            if not col or (min(col) >= 0 and max(col) < 4294967296):
+                t = _ARRAY_TYPES.get(len(col))
+                if t is None:
+                    t = _ARRAY_TYPES[len(col)] = C.c_uint32 * len(col)
+                return t(*col)
+        except TypeError:
+            pass
     return np.ascontiguousarray(np.asarray(col, dtype=np.uint32))
 
 
