@@ -2614,40 +2614,58 @@ int fold_finalize(z0p_gpu_fold* f, z0p_transcript_state* ts, uint8_t* out) {
         d.ga[j][e] = to_mont(j == 2 || j == 3 ? fmul(ga[e], omega_inv) : ga[e]);
     }
   }
-  // Per-coset 1/(x^S - 1), x^S = 31^S omega_m^(j S) (src/fold.rs:818-825).
-  std::vector<uint32_t> zinv(B);
-  const uint32_t omega_m = two_adic_generator(logm);
-  const uint32_t g_s = fpow(GENERATOR, S);
-  for (uint64_t j = 0; j < B; j++)
-    zinv[j] = to_mont(finv(fsub(fmul(g_s, fpow(omega_m, j * S)), 1)));
+  // Per-coset 1/(x^S - 1), x^S = 31^S omega_m^(j S) = 31^S omega_B^j
+  // (src/fold.rs:818-825), inverted together: one inversion and three
+  // products per coset (Montgomery's batch inversion).
+  std::vector<uint32_t> zinv(B), pre(B);
+  {
+    const uint32_t omega_b = two_adic_generator(logB);
+    uint32_t x = fpow(GENERATOR, S), run = 1;
+    for (uint64_t j = 0; j < B; j++) {
+      zinv[j] = fsub(x, 1);  // nonzero: 31^S is outside the subgroup of order B
+      pre[j] = run;
+      run = fmul(run, zinv[j]);
+      x = fmul(x, omega_b);
+    }
+    uint32_t inv = finv(run);
+    for (uint64_t j = B; j-- > 0;) {
+      const uint32_t d = zinv[j];
+      zinv[j] = to_mont(fmul(inv, pre[j]));
+      inv = fmul(inv, d);
+    }
+  }
   const size_t tbytes = (size_t)K * sizeof(FoldStepDev), zoff = (tbytes + 15) & ~(size_t)15;
-  RC(ensure(c, f->table, zoff + 4 * B));
   FriBufs fb;
   RC(plan_fri_buffers(c, s, 1, &fb));
   const uint32_t stride = (4 + 16 * psteps + 3) & ~3u;
   // The mapped buffer's extra region: the segments' opening blocks, then the
-  // step table and the coset inverses staged for one pinned (asynchronous)
-  // copy to the device.
+  // step table and the coset inverses (read there in place by a small
+  // combination, else staged for one pinned, asynchronous copy).
   const size_t open_bytes = 4ull * stride * fp.num_queries * K;
   HioPlan h;
   RC(plan_hio(c, s, fp.num_queries, 0, 0, 1, &h, open_bytes + zoff + 4 * B));
   uint8_t* staged = c->hio + h.extra + open_bytes;
   std::memcpy(staged, table.data(), tbytes);
   std::memcpy(staged + zoff, zinv.data(), 4 * B);
-  CK(cudaMemcpyAsync(f->table.p, staged, zoff + 4 * B, cudaMemcpyHostToDevice, st));
   c->h2d += tbytes + 4 * B;
   // Small layers 0: the combination launch inverts its rows' denominators
-  // itself and builds the layer-0 tree; larger ones read a table of them.
+  // itself and builds the layer-0 tree, and its few CTAs read the table in
+  // place (staged once per CTA), so no copy is queued before it. Larger ones
+  // read a table of inverses and a device copy of the step table.
   const bool fused_combine = (m / 4) <= kFuseMaxLeaves;  // fold_combine's own test
+  const FoldStepDev* steps_dev = hio_dev<const FoldStepDev>(c, h.extra + open_bytes);
   if (!fused_combine) {
+    RC(ensure(c, f->table, zoff + 4 * B));
+    CK(cudaMemcpyAsync(f->table.p, staged, zoff + 4 * B, cudaMemcpyHostToDevice, st));
+    steps_dev = (const FoldStepDev*)f->table.p;
     RC(ensure(c, f->tinv, 4 * m));
     CK(launch::row_inverses(st, c->tb, (uint32_t*)f->tinv.p, to_mont(w_last), logN, logB));
   }
   FoldCombineArgs ca;
-  ca.steps = (const FoldStepDev*)f->table.p;
+  ca.steps = steps_dev;
   ca.nsteps = K;
   ca.tinv = fused_combine ? nullptr : (const uint32_t*)f->tinv.p;
-  ca.zinv = (const uint32_t*)((const char*)f->table.p + zoff);
+  ca.zinv = (const uint32_t*)((const char*)steps_dev + zoff);
   ca.layer0 = fb.layer[0];
   ca.leaves = fb.tree[0];
   ca.logN = logN; ca.logB = logB;
