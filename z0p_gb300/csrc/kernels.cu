@@ -1816,7 +1816,12 @@ __global__ void __launch_bounds__(128) openings_kernel(const __grid_constant__ O
   const uint32_t qi = blockIdx.x, pk = blockIdx.y;  // query, proof of the group
   if (a.go) wait_gate(a.go, a.go_epoch, a.fault);
   uint32_t* out = a.out + ((size_t)pk * a.nq + qi) * a.stride;
-  const uint64_t leaf = *reinterpret_cast<const volatile uint64_t*>(a.indices + (size_t)pk * a.nq + qi);
+  // Indices are positions in layer 0 (a power of two); masking leaves valid
+  // ones unchanged and keeps every read inside the layers and trees, whatever
+  // the mapped buffer holds (a gate opened on an early return).
+  const uint64_t dom = a.nlayers ? 4ull * a.layer[0].leaves : 1ull << (a.logN + a.logB);
+  const uint64_t leaf =
+      *reinterpret_cast<const volatile uint64_t*>(a.indices + (size_t)pk * a.nq + qi) & (dom - 1);
   const uint64_t vo = pk * a.fri_val_stride, to = pk * a.fri_tree_stride;
   const uint32_t* lde = a.lde + pk * a.lde_stride;
   const uint32_t* ttree = a.ttree + pk * a.ttree_stride;
