@@ -358,3 +358,37 @@ def test_ungated_folds_prove_the_same_bytes(z0p, oracle, gpu_ctx):
     vals = [(7 * i + 3) % 2013265921 for i in range(256)]
     gated.append(z0p.fri.commit(vals, fp, z0p.Transcript(b"ungated/fri"), gpu_ctx).commitment.hex())
     assert ungated == gated
+
+
+_FRESH_SEQUENCE = r"""
+import json, sys
+sys.path.insert(0, sys.argv[1])
+import z0p_gb300 as Z
+cases = json.loads(sys.argv[2])
+ctx = Z.Context(0)
+out = []
+for c in cases:
+    p = Z.air.Params.new(c["n"], c["blowup"], c["queries"], c["final"], c["a0"], c["b0"], c["b_last"])
+    p.grinding_bits = c["grinding"]
+    p.cap_height = c["cap"]
+    out.append(Z.air.prove(p, Z.Transcript(c["label"].encode()), ctx).hex())
+print(" ".join(out))
+"""
+
+
+def test_fresh_context_sequence(z0p, oracle):
+    """A fresh context proves a proof without gated launches and then one
+    with them (its first gated tail uses the first epoch); the mapped buffer
+    still holds the first proof's values where the second's gate words go,
+    and the bytes must not depend on them."""
+    import subprocess
+    import sys
+    names = ["air n2 b4", "air fib16", "air n4 b8 f2", "air fib64 bench"]
+    cases = [next(c for c in GOLD if c["name"] == n) for n in names]
+    r = subprocess.run([sys.executable, "-c", _FRESH_SEQUENCE, ROOT, json.dumps(cases)],
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    got = [bytes.fromhex(x) for x in r.stdout.split()]
+    for c, proof in zip(cases, got):
+        po, _ = _air_pair(z0p, oracle, c)
+        assert proof == oracle.air_prove(po, oracle.Transcript(c["label"].encode())), c["name"]

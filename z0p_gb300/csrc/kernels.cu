@@ -915,45 +915,13 @@ __device__ __forceinline__ void quad_points(const Tables& tb, uint32_t k0, uint3
 // With a.counter (small trees), thread u makes leaf P = u, so a CTA's leaves
 // are consecutive and it hashes their subtree (cta_subtree); otherwise
 // consecutive threads read consecutive LDE rows and leaf P is bit-reversed.
-template <bool kFused>
-__global__ void __launch_bounds__(kThreads) air_compose_leaves_kernel(AirComposeArgs a, Tables tb) {
-  // >= 2 * 9 * (kFuseMaxLeaves / 256) roots when fused
-  __shared__ uint32_t buf[kFused ? 2 * kThreads * kTopStride : 1];
-  if (!kFused) a.counter = nullptr;
-  const uint32_t logm = a.logN + a.logB;
-  const uint32_t quarter = 1u << (logm - 2);
-  const uint32_t u = blockIdx.x * blockDim.x + threadIdx.x;
-  {
-    const uint32_t pk = blockIdx.y;  // proof of the group
-    a.lde_a += (size_t)pk << logm;
-    a.tinv += (size_t)pk << logm;
-    a.cb += (size_t)pk << a.logB;
-    a.layer0 += pk * a.layer_stride;
-    a.leaves += pk * a.tree_stride;
-    a.slot += pk;
-    if (a.counter) a.counter += pk;
-    if (a.cap) a.cap += pk * a.cap_stride;
-  }
-  const uint32_t nt = quarter < kThreads ? quarter : kThreads;
-  uint32_t d[8];
-  if (u < quarter) {
-  const uint32_t N = 1u << a.logN, B = 1u << a.logB;
-  uint32_t k0, P;
-  if (a.counter) {
-    P = u;
-    k0 = brev_bits(u, logm - 2);
-  } else {
-    if (a.logN >= 2) {
-      uint32_t j = u >> (a.logN - 2), q0 = u & ((N >> 2) - 1u);
-      k0 = (q0 << a.logB) | j;
-    } else {
-      k0 = u;
-    }
-    P = brev_bits(k0, logm - 2);
-  }
+// The four composition values of layer-0 quad k0 (rows k0 + s quarter), each
+// at its leaf position 4P + brev2(s); `a` already offset to its proof.
+__device__ __forceinline__ void compose_quad(const AirComposeArgs& a, const Tables& tb, uint32_t k0,
+                                             uint32_t logm, uint32_t (&leaf)[16]) {
+  const uint32_t N = 1u << a.logN, B = 1u << a.logB, quarter = 1u << (logm - 2);
   uint32_t xs[4];
   quad_points(tb, k0, logm, xs);
-  uint32_t leaf[16];
 #pragma unroll
   for (int s = 0; s < 4; s++) {
     const uint32_t k = k0 + (uint32_t)s * quarter;
@@ -984,12 +952,59 @@ __global__ void __launch_bounds__(kThreads) air_compose_leaves_kernel(AirCompose
                              pc.kc[c]);
     }
   }
+}
+
+__device__ __forceinline__ void compose_for_proof(AirComposeArgs& a, uint32_t logm) {
+  const uint32_t pk = blockIdx.y;  // proof of the group
+  a.lde_a += (size_t)pk << logm;
+  a.tinv += (size_t)pk << logm;
+  a.cb += (size_t)pk << a.logB;
+  a.layer0 += pk * a.layer_stride;
+  a.leaves += pk * a.tree_stride;
+  a.slot += pk;
+  if (a.counter) a.counter += pk;
+  if (a.cap) a.cap += pk * a.cap_stride;
+}
+
+__device__ __forceinline__ void store_leaf_values(const AirComposeArgs& a, uint32_t P,
+                                                  const uint32_t (&leaf)[16]) {
   uint4* dst = reinterpret_cast<uint4*>(a.layer0 + 16 * (size_t)P);
 #pragma unroll
   for (int t = 0; t < 4; t++)
     dst[t] = make_uint4(leaf[4 * t], leaf[4 * t + 1], leaf[4 * t + 2], leaf[4 * t + 3]);
-  blake3_leaf64(leaf, d);
-  store_digest(a.leaves + 8 * (size_t)P, d);
+}
+
+template <bool kFused>
+__global__ void __launch_bounds__(kThreads) air_compose_leaves_kernel(AirComposeArgs a, Tables tb) {
+  // >= 2 * 9 * (kFuseMaxLeaves / 256) roots when fused
+  __shared__ uint32_t buf[kFused ? 2 * kThreads * kTopStride : 1];
+  if (!kFused) a.counter = nullptr;
+  const uint32_t logm = a.logN + a.logB;
+  const uint32_t quarter = 1u << (logm - 2);
+  const uint32_t u = blockIdx.x * blockDim.x + threadIdx.x;
+  compose_for_proof(a, logm);
+  const uint32_t nt = quarter < kThreads ? quarter : kThreads;
+  uint32_t d[8];
+  if (u < quarter) {
+    const uint32_t N = 1u << a.logN;
+    uint32_t k0, P;
+    if (a.counter) {
+      P = u;
+      k0 = brev_bits(u, logm - 2);
+    } else {
+      if (a.logN >= 2) {
+        uint32_t j = u >> (a.logN - 2), q0 = u & ((N >> 2) - 1u);
+        k0 = (q0 << a.logB) | j;
+      } else {
+        k0 = u;
+      }
+      P = brev_bits(k0, logm - 2);
+    }
+    uint32_t leaf[16];
+    compose_quad(a, tb, k0, logm, leaf);
+    store_leaf_values(a, P, leaf);
+    blake3_leaf64(leaf, d);
+    store_digest(a.leaves + 8 * (size_t)P, d);
   }
   if constexpr (kFused)
     cta_subtree(d, buf, nt, (uint64_t)blockIdx.x * kThreads, a.leaves, quarter, a.top, a.cap,

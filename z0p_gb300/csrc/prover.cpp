@@ -686,6 +686,12 @@ int run_fri_commit(z0p_gpu_ctx* c, const FriShape& s, const FriParams& fp, const
       rel.epoch = epoch;
       rel.next = l;
       rel.end = tail ? L + 1 : L - 1;
+      // Close every gate of this tail before anything is queued behind it: the
+      // mapped buffer is shared by all calls and shapes, so a word left there
+      // could otherwise already hold this epoch.
+      for (size_t g = l; g < rel.end; g++)
+        __atomic_store_n(const_cast<unsigned int*>(rel.gates + g), epoch - 1u, __ATOMIC_RELAXED);
+      __atomic_thread_fence(__ATOMIC_SEQ_CST);
       CK(cudaEventRecord(c->gate_ev[l], c->stream));  // layer l's cap
       for (size_t j = l; j + 1 < L; j++) {
         FoldArgs fa = fold_args(j);
