@@ -570,6 +570,9 @@ struct GateRelease {
   volatile unsigned int* gates = nullptr;
   size_t next = 0, end = 0;
   uint32_t epoch = 0;
+  GateRelease() = default;
+  GateRelease(const GateRelease&) = delete;  // one owner opens each gate once
+  GateRelease& operator=(const GateRelease&) = delete;
   void open_next() {  // after the host has written the inputs behind it
     __atomic_store_n(const_cast<unsigned int*>(gates + next), epoch, __ATOMIC_RELEASE);
     next++;
