@@ -166,6 +166,13 @@ int z0p_range_proof_size(const z0p_range_params *params, size_t *len);
  * sets Z0P_GATES=0 or CUDA_LAUNCH_BLOCKING=1, or when a tool is injected
  * through CUDA_INJECTION64_PATH; proofs are the same bytes either way. */
 int z0p_gpu_ctx_create(int device, z0p_gpu_ctx **out);
+/* Gated launches on (nonzero, the default) or off for this context. On, a
+ * single proof's latency is lower; off, the launches wait for their inputs
+ * on the host instead of on the GPU, which suits contexts proving side by
+ * side (a pool of more than one worker turns them off on its own contexts:
+ * launches waiting at their gates hold SM slots the other streams could
+ * use). Proofs are the same bytes either way. */
+int z0p_gpu_ctx_set_gates(z0p_gpu_ctx *ctx, int on);
 void z0p_gpu_ctx_destroy(z0p_gpu_ctx *ctx);
 /* The context's cudaStream_t (as void*), for callers that time or order work. */
 void *z0p_gpu_ctx_stream(z0p_gpu_ctx *ctx);

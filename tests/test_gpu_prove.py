@@ -392,3 +392,17 @@ def test_fresh_context_sequence(z0p, oracle):
     for c, proof in zip(cases, got):
         po, _ = _air_pair(z0p, oracle, c)
         assert proof == oracle.air_prove(po, oracle.Transcript(c["label"].encode())), c["name"]
+
+
+def test_context_without_gates_proves_the_same_bytes(z0p, oracle):
+    """z0p_gpu_ctx_set_gates(ctx, 0), as a pool of several workers sets on its
+    contexts: the small folds, the PoW search and the gather wait for their
+    inputs on the host; the bytes equal the gated context's and the oracle's."""
+    gated, ungated = z0p.Context(0), z0p.Context(0)
+    ungated.set_gates(False)
+    for name in ["air fib64 bench", "air n256 b4 grind8 cap3", "air prod 1024"]:
+        c = next(x for x in GOLD if x["name"] == name)
+        po, pz = _air_pair(z0p, oracle, c)
+        a = z0p.air.prove(pz, z0p.Transcript(c["label"].encode()), gated)
+        b = z0p.air.prove(pz, z0p.Transcript(c["label"].encode()), ungated)
+        assert a == b == oracle.air_prove(po, oracle.Transcript(c["label"].encode())), name

@@ -140,6 +140,7 @@ def lib():
             "z0p_gpu_ctx_stream": (vp, [vp]),
             "z0p_gpu_ctx_device_bytes": (sz, [vp]),
             "z0p_gpu_ctx_trim": (C.c_int, [vp]),
+            "z0p_gpu_ctx_set_gates": (C.c_int, [vp, C.c_int]),
             "z0p_gpu_ctx_reserve_group": (C.c_int, [vp, C.c_uint32]),
             "z0p_gpu_blake3_ceiling": (C.c_int, [vp, P(C.c_double)]),
             "z0p_range_proof_size_zk": (C.c_int, [P(RangeParams), sz, P(sz)]),

@@ -46,6 +46,11 @@ class Context:
         """Hand the proof workspace back to the library's device memory pool."""
         check(lib().z0p_gpu_ctx_trim(self.handle))
 
+    def set_gates(self, on: bool) -> None:
+        """Gated launches on (the default: lower single-proof latency) or off
+        (contexts proving side by side); the proof bytes do not change."""
+        check(lib().z0p_gpu_ctx_set_gates(self.handle, 1 if on else 0))
+
     def reserve_group(self, max_group: int) -> None:
         """Reserve constant slots for proof groups of up to max_group statements."""
         check(lib().z0p_gpu_ctx_reserve_group(self.handle, max_group))

@@ -199,6 +199,9 @@ int z0p_gpu_pool_create(int device, int workers, size_t hbm_budget, z0p_gpu_pool
       delete p;
       return rc;
     }
+    // Side by side, a worker's proofs overlap the others' latency-bound
+    // stages; launches waiting at gates would only hold SM slots.
+    if (workers > 1) z0p_gpu_ctx_set_gates(c, 0);
     p->ctxs.push_back(c);
   }
   // Each worker reserves constant slots for its groups: an equal share of

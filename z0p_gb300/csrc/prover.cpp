@@ -172,6 +172,7 @@ struct z0p_gpu_ctx {
   // current commitment writes into its gate words.
   std::vector<cudaEvent_t> gate_ev;
   uint32_t go_epoch = 0;
+  bool gates = true;  // z0p_gpu_ctx_set_gates
 };
 using HostSite = z0p_gpu_ctx::HostSite;
 
@@ -556,8 +557,8 @@ bool gates_enabled() {
 // Whether folds l, l+1, ... to the final layer are all small folds (one
 // launch that also finishes the next layer's tree, tables read in place),
 // so that they can be queued ahead behind gates.
-bool gated_tail(const FriShape& s, size_t l) {
-  if (!gates_enabled() || l + 1 >= s.len.size()) return false;
+bool gated_tail(const z0p_gpu_ctx* c, const FriShape& s, size_t l) {
+  if (!c->gates || !gates_enabled() || l + 1 >= s.len.size()) return false;
   for (size_t j = l; j + 1 < s.len.size(); j++)
     if (s.len[j] < 16 || s.leaves[j + 1] > kFuseMaxLeaves) return false;
   return true;
@@ -675,7 +676,7 @@ int run_fri_commit(z0p_gpu_ctx* c, const FriShape& s, const FriParams& fp, const
                          h.final_bytes, K, cudaMemcpyDeviceToHost, c->stream));
   }
   for (size_t l = 0;; l++) {
-    if (gated_tail(s, l)) {
+    if (gated_tail(c, s, l)) {
       while (c->gate_ev.size() < L + 1) {
         cudaEvent_t e;
         CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
@@ -3014,6 +3015,13 @@ void z0p_gpu_ctx_destroy(z0p_gpu_ctx* c) {
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c->fri;
   delete c;
+}
+
+int z0p_gpu_ctx_set_gates(z0p_gpu_ctx* c, int on) {
+  if (!c) return Z0P_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lk(c->mu);
+  c->gates = on != 0;
+  return Z0P_OK;
 }
 
 int z0p_gpu_ctx_trim(z0p_gpu_ctx* c) {
