@@ -516,7 +516,10 @@ int z0p_gpu_fri_fold(z0p_gpu_ctx *ctx, const uint32_t *d_in, uint64_t n, uint64_
  *    threads); 2: register passes (each half of 2^L points as two register
  *    passes of radix 2^(L/2) with one shared-memory transpose, tiles loaded
  *    by TMA), used when both halves are even and within 2^6..2^12 and the
- *    input is 16-byte aligned, variant 0 otherwise. The default schedule
+ *    input is 16-byte aligned, variant 0 otherwise; 3: the register passes
+ *    streamed (a resident grid, each CTA walking many tiles through two
+ *    buffers so the next tile's copy overlaps the current transform; a half
+ *    above 2^10 takes variant 2's kernel), same conditions. The default schedule
  *    (z0p_schedule_default) has variant 2 at 2^16, 2^20 and 2^24, whose
  *    balanced splits have two even halves, and 0 elsewhere.
  *  - merkle_top_log: a Merkle tree's levels are one launch each while they

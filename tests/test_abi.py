@@ -221,15 +221,18 @@ def test_schedule_get_set_validation(z0p):
                 {"ntt_log_n1": {"27": 13}}, {"ntt_log_n1": {"14": 9}}, {"merkle_top_log": 9},
                 {"merkle_top_log": 19}, {"grind_ctas_per_sm": 0}, {"grind_ctas_per_sm": 17},
                 {"ntt_radix32": [12]}, {"ntt_radix32": [27]}, {"ntt_regpass": [12]},
-                {"ntt_regpass": [27]}]:
+                {"ntt_regpass": [27]}, {"ntt_regstream": [12]}, {"ntt_regstream": [27]}]:
         with pytest.raises(z0p.Z0pError) as e:
             t.set(t.from_dict(bad), dev)
         assert e.value.code == 106, bad
         assert t.to_dict(t.get(dev)) == t.to_dict(good)
-    three = t.from_dict({})
-    three.ntt_radix32[20] = 3  # no such variant
+    streamed = t.from_dict({"ntt_regstream": [20]})
+    assert streamed.ntt_radix32[20] == 3 and t.to_dict(streamed)["ntt_regstream"] == [20]
+    t.set(streamed, dev)
+    four = t.from_dict({})
+    four.ntt_radix32[20] = 4  # no such variant
     with pytest.raises(z0p.Z0pError):
-        t.set(three, dev)
+        t.set(four, dev)
     with pytest.raises(z0p.Z0pError):
         t.get(64)
     t.set(t.from_dict(before), dev)

@@ -1,6 +1,7 @@
-"""The register-pass NTT variant (launch schedule variant 2: two register
+"""The register-pass NTT variants (launch schedule variant 2: two register
 passes per half with one shared-memory transpose, pass-1 tiles by TMA tensor
-copies and pass-2 rows by bulk copies) against the oracle on every path that
+copies and pass-2 rows by bulk copies; variant 3: the same tiles streamed
+through a resident grid) against the oracle on every path that
 reaches it: the interpolation (inverse, 31^k / n scaling) and the coset LDE
 of z0p_gpu_rs_extend for every half size 2^6..2^12 and batched inputs, the
 FRI commitment of base coefficients (31^i applied on load), the caller
@@ -16,13 +17,15 @@ pytestmark = pytest.mark.gpu
 P = 2**31 - 2**27 + 1
 
 
-@pytest.fixture
-def regpass(z0p):
+@pytest.fixture(params=["ntt_regpass", "ntt_regstream"])
+def regpass(z0p, request):
+    # Variant 2 (one tile per CTA) and variant 3 (streamed: a resident grid,
+    # two tile buffers per CTA; 2^12 halves take variant 2's kernel).
     before = z0p.tune.to_dict(z0p.tune.get(0))
 
     def use(splits):
         z0p.tune.set(z0p.tune.from_dict({"ntt_log_n1": {str(l): s for l, s in splits.items()},
-                                         "ntt_regpass": sorted(splits)}), 0)
+                                         request.param: sorted(splits)}), 0)
     yield use
     z0p.tune.set(z0p.tune.from_dict(before), 0)
 

@@ -45,6 +45,7 @@ def test_every_ntt_split_matches_oracle(z0p, oracle, gpu_ctx, restore_schedule, 
         variants = [{}, {"ntt_radix32": [logn]}]  # register groups of 16 and of 32
         if split % 2 == 0 and (logn - split) % 2 == 0 and 6 <= logn - split <= 12 and split <= 12:
             variants.append({"ntt_regpass": [logn]})  # register passes
+            variants.append({"ntt_regstream": [logn]})  # streamed through a resident grid
         for v in variants:
             z0p.tune.set(z0p.tune.from_dict({"ntt_log_n1": {str(logn): split}, **v}), 0)
             assert np.array_equal(_lde(z0p, gpu_ctx, vals, 16), ref), (logn, split, v)
@@ -55,6 +56,7 @@ SCHEDULES = [
     {"ntt_log_n1": {"16": 10, "14": 7}, "ntt_radix32": [14, 16, 20], "merkle_top_log": 18,
      "grind_ctas_per_sm": 8},
     {"ntt_log_n1": {"16": 8, "14": 8}, "ntt_regpass": [14, 16], "merkle_top_log": 14},
+    {"ntt_log_n1": {"16": 8, "14": 8}, "ntt_regstream": [14, 16], "merkle_top_log": 14},
     {"merkle_top_log": 12, "grind_ctas_per_sm": 16},
 ]
 

@@ -1011,6 +1011,7 @@ __global__ void __launch_bounds__(kThreads) air_compose_leaves_kernel(AirCompose
                 a.counter);
 }
 
+
 // Range-check composition (src/range.rs:678-741 == composition_at :746-774).
 __global__ void __launch_bounds__(kThreads) range_compose_leaves_kernel(RangeComposeArgs a,
                                                                         Tables tb) {
@@ -2001,7 +2002,7 @@ Schedule g_sched[kMaxDevices];
 template <typename K>
 cudaError_t raise_smem(K* func, int pass, uint32_t L, size_t smem) {
   static std::mutex mu;
-  static size_t done[kMaxDevices][10][32] = {};
+  static size_t done[kMaxDevices][14][32] = {};
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
@@ -2043,7 +2044,7 @@ bool schedule_valid(const Schedule& s) {
   for (uint32_t l = 0; l < 32; l++) {
     uint32_t lo, hi;
     ntt_split_range(l, &lo, &hi);
-    if (s.ntt_radix32[l] > 2 || (s.ntt_radix32[l] && lo > hi)) return false;
+    if (s.ntt_radix32[l] > 3 || (s.ntt_radix32[l] && lo > hi)) return false;
     if (!s.ntt_log_n1[l]) continue;
     if (s.ntt_log_n1[l] < lo || s.ntt_log_n1[l] > hi) return false;
   }
@@ -2079,18 +2080,61 @@ PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
   return fn;
 }
 
+// CTAs of `func` (threads, smem) resident on the current device at once:
+// the grid of a streamed kernel. Cached per kernel slot and device.
+template <typename K>
+uint32_t resident_ctas(K* func, int slot, uint32_t L, int threads, size_t smem) {
+  static std::mutex mu;
+  static uint32_t cached[kMaxDevices][4][32] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) dev = 0;
+  std::lock_guard<std::mutex> lk(mu);
+  uint32_t& c = cached[dev][slot][L];
+  if (!c) {
+    int sms = 0, per = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, func, threads, smem);
+    c = (uint32_t)((sms > 0 ? sms : 1) * (per > 0 ? per : 1));
+  }
+  return c;
+}
+
 template <int L, bool INV>
-cudaError_t reg_pass1(cudaStream_t st, const CUtensorMap& map, uint32_t* yt, const NttArgs& a, dim3 g) {
+cudaError_t reg_pass1(cudaStream_t st, const CUtensorMap& map, uint32_t* yt, const NttArgs& a, dim3 g,
+                      bool streamed) {
+  constexpr int threads = reg_ntt::kC << (L / 2);
+  if constexpr (reg_ntt::streamed_ok(L)) {
+    if (streamed) {
+      constexpr size_t smem = reg_ntt::pass1s_smem(L);
+      if (cudaError_t e = raise_smem(ntt_reg1s_kernel<L, INV>, 10 + INV, L, smem)) return e;
+      const uint32_t tiles = g.x * g.y;
+      const uint32_t res = resident_ctas(ntt_reg1s_kernel<L, INV>, INV, L, threads, smem);
+      ntt_reg1s_kernel<L, INV><<<tiles < res ? tiles : res, threads, smem, st>>>(map, yt, a, tiles);
+      return cudaGetLastError();
+    }
+  }
   constexpr size_t smem = reg_ntt::pass1_smem(L);
   if (cudaError_t e = raise_smem(ntt_reg1_kernel<L, INV>, 6 + INV, L, smem)) return e;
-  ntt_reg1_kernel<L, INV><<<g, reg_ntt::kC << (L / 2), smem, st>>>(map, yt, a);
+  ntt_reg1_kernel<L, INV><<<g, threads, smem, st>>>(map, yt, a);
   return cudaGetLastError();
 }
 template <int L, bool INV>
-cudaError_t reg_pass2(cudaStream_t st, const uint32_t* yt, uint32_t* out, const NttArgs& a, dim3 g) {
+cudaError_t reg_pass2(cudaStream_t st, const uint32_t* yt, uint32_t* out, const NttArgs& a, dim3 g,
+                      bool streamed) {
+  constexpr int threads = reg_ntt::kC << (L / 2);
+  if constexpr (reg_ntt::streamed_ok(L)) {
+    if (streamed) {
+      constexpr size_t smem = reg_ntt::pass2s_smem(L);
+      if (cudaError_t e = raise_smem(ntt_reg2s_kernel<L, INV>, 12 + INV, L, smem)) return e;
+      const uint32_t tiles = g.x * g.y;
+      const uint32_t res = resident_ctas(ntt_reg2s_kernel<L, INV>, 2 + INV, L, threads, smem);
+      ntt_reg2s_kernel<L, INV><<<tiles < res ? tiles : res, threads, smem, st>>>(yt, out, a, tiles);
+      return cudaGetLastError();
+    }
+  }
   constexpr size_t smem = reg_ntt::pass2_smem(L);
   if (cudaError_t e = raise_smem(ntt_reg2_kernel<L, INV>, 8 + INV, L, smem)) return e;
-  ntt_reg2_kernel<L, INV><<<g, reg_ntt::kC << (L / 2), smem, st>>>(yt, out, a);
+  ntt_reg2_kernel<L, INV><<<g, threads, smem, st>>>(yt, out, a);
   return cudaGetLastError();
 }
 }  // namespace
@@ -2098,7 +2142,7 @@ cudaError_t reg_pass2(cudaStream_t st, const uint32_t* yt, uint32_t* out, const 
 // Register-pass four-step transform (ntt_reg.cuh): pass 1 reads its column
 // tiles through a tensor map over `in`, viewed as [in blocks][n1][n2] words.
 cudaError_t ntt_reg(cudaStream_t st, const NttArgs& a, const NttPlan& plan, const uint32_t* in,
-                    uint32_t* out, uint32_t* scratch, uint32_t logn1, uint32_t logn2) {
+                    uint32_t* out, uint32_t* scratch, uint32_t logn1, uint32_t logn2, bool streamed) {
   PFN_cuTensorMapEncodeTiled_v12000 encode = tensor_map_encoder();
   if (!encode) return cudaErrorNotSupported;
   const uint32_t in_div = plan.in_div ? plan.in_div : 1;
@@ -2118,7 +2162,10 @@ cudaError_t ntt_reg(cudaStream_t st, const NttArgs& a, const NttPlan& plan, cons
   const bool inv = plan.inverse != 0;
   switch (logn1) {
 #define Z0P_R1(Lv) \
-  case Lv: e = inv ? reg_pass1<Lv, true>(st, map, scratch, a, g1) : reg_pass1<Lv, false>(st, map, scratch, a, g1); break;
+  case Lv:                                                                                         \
+    e = inv ? reg_pass1<Lv, true>(st, map, scratch, a, g1, streamed)                               \
+            : reg_pass1<Lv, false>(st, map, scratch, a, g1, streamed);                             \
+    break;
     Z0P_R1(8) Z0P_R1(10) Z0P_R1(12)  // pass 1 is at least 2^7 points
 #undef Z0P_R1
   }
@@ -2126,7 +2173,10 @@ cudaError_t ntt_reg(cudaStream_t st, const NttArgs& a, const NttPlan& plan, cons
   e = cudaErrorInvalidValue;
   switch (logn2) {
 #define Z0P_R2(Lv) \
-  case Lv: e = inv ? reg_pass2<Lv, true>(st, scratch, out, a, g2) : reg_pass2<Lv, false>(st, scratch, out, a, g2); break;
+  case Lv:                                                                                         \
+    e = inv ? reg_pass2<Lv, true>(st, scratch, out, a, g2, streamed)                               \
+            : reg_pass2<Lv, false>(st, scratch, out, a, g2, streamed);                             \
+    break;
     Z0P_R2(6) Z0P_R2(8) Z0P_R2(10) Z0P_R2(12)
 #undef Z0P_R2
   }
@@ -2178,9 +2228,10 @@ cudaError_t ntt(cudaStream_t st, const Tables& tb, const NttPlan& plan, const ui
   }
   const uint32_t logn2 = plan.logn - logn1;
   const uint32_t n1 = 1u << logn1, n2 = 1u << logn2;
-  if (plan.logn < 32 && sched.ntt_radix32[plan.logn] == 2 && reg_split_ok(logn1) &&
-      reg_split_ok(logn2) && tb.stw && (reinterpret_cast<uintptr_t>(in) & 15u) == 0)
-    return ntt_reg(st, a, plan, in, out, scratch, logn1, logn2);
+  const uint32_t variant = plan.logn < 32 ? sched.ntt_radix32[plan.logn] : 0u;
+  if (variant >= 2 && reg_split_ok(logn1) && reg_split_ok(logn2) && tb.stw &&
+      (reinterpret_cast<uintptr_t>(in) & 15u) == 0)
+    return ntt_reg(st, a, plan, in, out, scratch, logn1, logn2, variant == 3);
   // C = R = 8 columns per CTA (32-byte global segments), 4 for the largest halves.
   const int logc = logn1 > 12 ? 2 : 3;
   const int logr = logn2 > 12 ? 2 : 3;

@@ -273,7 +273,10 @@ struct Schedule {
   // groups of 16 elements (512 threads a CTA), 1 = the same in groups of 32
   // (256 threads), 2 = register passes (two register passes of radix
   // 2^(L/2) per half of 2^L points, one shared-memory transpose, the tiles
-  // loaded by TMA; both halves even and within 2^6..2^12, else variant 0).
+  // loaded by TMA; both halves even and within 2^6..2^12, else variant 0),
+  // 3 = the register passes streamed: a resident grid whose CTAs each walk
+  // many tiles through two buffers (halves up to 2^10; a 2^12 half takes
+  // variant 2's kernel).
   uint8_t ntt_radix32[32] = {};
   // A Merkle tree's levels go one launch each while they have more than
   // 2^merkle_top_log nodes; the rest go to one top kernel (10..18).

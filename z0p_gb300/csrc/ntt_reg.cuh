@@ -25,6 +25,10 @@
 //  * Pass 2 takes its eight contiguous rows with cp.async.bulk, one copy per
 //    row into a padded row slot, and stores eight consecutive output words
 //    per lane group (natural order).
+//  * The streamed kernels (schedule variant 3, halves up to 2^10) run the
+//    same tiles from a resident grid, each CTA walking its tiles through two
+//    buffers: the next tile's copy is in flight while the current one is
+//    transformed, and the pass-A twiddles are loaded once per CTA.
 // Every mbarrier wait is bounded: a CTA that gives up sets Tables::fault
 // (read by the host after its next synchronisation) and returns.
 
@@ -116,17 +120,18 @@ __device__ __forceinline__ void mbar_expect(uint64_t* bar, uint32_t bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(saddr(bar)), "r"(bytes)
                : "memory");
 }
-// Waits for phase 0 of bar, giving up after about 2^31 cycles (about a
-// second at full clock).
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar) {
+// Waits for the phase of bar with parity `par` (0 for its first use, 1 for
+// its second, ...), giving up after about 2^31 cycles (about a second at
+// full clock).
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t par = 0) {
   const long long t0 = clock64();
   for (;;) {
     uint32_t ok;
     asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n"
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
         " selp.u32 %0, 1, 0, p;\n}\n"
         : "=r"(ok)
-        : "r"(saddr(bar))
+        : "r"(saddr(bar)), "r"(par)
         : "memory");
     if (ok) return true;
     if (clock64() - t0 > (1ll << 31)) return false;
@@ -148,17 +153,25 @@ __device__ __forceinline__ void tensor_load_3d(void* dst, const CUtensorMap* map
       : "memory");
 }
 
-// Every thread waits on bar; the CTA goes on only if all of them saw the
-// copies land. Otherwise the host learns of it through fault, and the CTA
-// gives its copies a second bounded wait before it leaves.
-__device__ __forceinline__ bool cta_wait(uint64_t* bar, unsigned int* fault) {
-  const bool ok = mbar_wait(bar);
+// Every thread waits on bar (phase parity par); the CTA goes on only if all
+// of them saw the copies land. Otherwise the host learns of it through
+// fault, and the CTA gives its copies a second bounded wait (and those of
+// `other`, a prefetch in flight on another barrier, one) before it leaves.
+__device__ __forceinline__ bool cta_wait(uint64_t* bar, unsigned int* fault, uint32_t par = 0,
+                                         uint64_t* other = nullptr, uint32_t other_par = 0) {
+  const bool ok = mbar_wait(bar, par);
   if (__syncthreads_or(!ok)) {
     if (threadIdx.x == 0 && fault) atomicOr(fault, 1u);
-    if (!ok) mbar_wait(bar);
+    if (!ok) mbar_wait(bar, par);
+    if (other) mbar_wait(other, other_par);
     return false;
   }
   return true;
+}
+// Orders this thread's generic-proxy accesses of shared memory before the
+// async-proxy (TMA / bulk copy) writes that a later barrier lets start.
+__device__ __forceinline__ void fence_proxy_async() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 
 // Pass-A stage twiddles: entry 2^s - R + x = omega_{2^(s+1)}^(+-x), s = H..L-1,
@@ -181,39 +194,34 @@ __host__ __device__ constexpr size_t pass1_smem(uint32_t L) {
 __host__ __device__ constexpr size_t pass2_smem(uint32_t L) {
   return 128 + 4 * (size_t)kC * stride(L) + 8 * ((1u << L) - (1u << (L / 2))) + 16;
 }
+// The streamed kernels hold two tile buffers and two barriers.
+__host__ __device__ constexpr size_t pass1s_smem(uint32_t L) {
+  return 128 + 8 * (size_t)pass1_words(L) + 8 * ((1u << L) - (1u << (L / 2))) + 4 * (1u << L) + 16;
+}
+__host__ __device__ constexpr size_t pass2s_smem(uint32_t L) {
+  return 128 + 8 * (size_t)kC * stride(L) + 8 * ((1u << L) - (1u << (L / 2))) + 16;
+}
+// Halves the streamed kernels take: two buffers fit in shared memory up to
+// 2^10 points (80 KB for pass 1), not at 2^12 (266 KB).
+__host__ __device__ constexpr bool streamed_ok(uint32_t L) { return L <= 10; }
 
 }  // namespace reg_ntt
 
-// Pass 1: n1 = 2^L point columns i2 = c0 .. c0+7 of the input viewed as
-// [n1][n2] (the tensor map's x = i2, y = i1, z = input block b / in_div),
-// twisted by w^(j i) on load; writes yt[k1][i2] times the four-step twiddle.
+// Pass 1 on one tile: n1 = 2^L point columns i2 = c0 .. c0+7 of block b,
+// whose copy (kC words per row, rows i1 = 0 .. n1-1) has landed in `data`;
+// twisted by w^(j i) on load (twist[i1], filled when j != 0); writes
+// yt[k1][i2] times the four-step twiddle. Ends with `data` read (the
+// transpose's barriers are inside): a caller that reuses it adds a barrier.
 template <int L, bool INV>
-__global__ void __launch_bounds__(reg_ntt::kC << (L / 2), L == 10 ? 4 : 1)
-    ntt_reg1_kernel(const __grid_constant__ CUtensorMap tmap, uint32_t* __restrict__ yt, NttArgs a) {
+__device__ __forceinline__ void reg1_tile(uint32_t* data, const uint2* tw, const uint32_t* twist,
+                                          uint32_t* __restrict__ yt, const NttArgs& a, uint32_t b,
+                                          uint32_t c0, uint32_t j) {
   using namespace reg_ntt;
   constexpr int H = L / 2;
-  constexpr uint32_t R = 1u << H, n1 = 1u << L, CS = stride(L), T = kC * R;
-  constexpr uint32_t BOX = n1 < 256 ? n1 : 256;  // rows per tensor copy
-  extern __shared__ uint32_t sm_raw[];
-  uint32_t* data = reinterpret_cast<uint32_t*>((reinterpret_cast<uintptr_t>(sm_raw) + 127) & ~uintptr_t(127));
-  uint2* tw = reinterpret_cast<uint2*>(data + pass1_words(L));
-  uint32_t* twist = reinterpret_cast<uint32_t*>(tw + (n1 - R));
-  uint64_t* bar = reinterpret_cast<uint64_t*>(twist + n1);
+  constexpr uint32_t R = 1u << H, CS = stride(L);
   const uint32_t tid = threadIdx.x;
   const uint32_t logn2 = a.logn - L;
   const uint32_t n = 1u << a.logn;
-  const uint32_t b = blockIdx.y, c0 = blockIdx.x * kC;
-  const uint32_t j = b % a.twist_mod;
-  if (tid == 0) mbar_init(bar);
-  __syncthreads();
-  if (tid == 0) {
-    mbar_expect(bar, kC * n1 * 4u);
-    for (uint32_t y = 0; y < n1; y += BOX) tensor_load_3d(data + y * kC, &tmap, c0, y, b / a.in_div, bar);
-  }
-  load_pass_a_twiddles<L>(tw, a);
-  if (j)
-    for (uint32_t i1 = tid; i1 < n1; i1 += T) twist[i1] = root_pow(a.tb, ((j * i1) << logn2) << a.twist_shift);
-  if (!cta_wait(bar, a.tb.fault)) return;  // (also orders the tables above)
   const uint32_t c = tid & (kC - 1), l = tid / kC;
   uint32_t x[R];
 #pragma unroll
@@ -255,31 +263,18 @@ __global__ void __launch_bounds__(reg_ntt::kC << (L / 2), L == 10 ? 4 : 1)
   }
 }
 
-// Pass 2: rows k1 = r0 .. r0+7 of yt, n2 = 2^L points each, one bulk copy
-// per row; output k = k1 + n1 k2 (natural order), optionally times 31^k / n.
+// Pass 2 on one tile: rows k1 = r0 .. r0+7 of block b of yt, n2 = 2^L
+// points each, landed in `data` (row stride stride(L)); output k = k1 + n1
+// k2 (natural order), optionally times 31^k / n. Same reuse rule as pass 1.
 template <int L, bool INV>
-__global__ void __launch_bounds__(reg_ntt::kC << (L / 2))
-    ntt_reg2_kernel(const uint32_t* __restrict__ yt, uint32_t* __restrict__ out, NttArgs a) {
+__device__ __forceinline__ void reg2_tile(uint32_t* data, const uint2* tw, uint32_t* __restrict__ out,
+                                          const NttArgs& a, uint32_t b, uint32_t r0) {
   using namespace reg_ntt;
   constexpr int H = L / 2;
-  constexpr uint32_t R = 1u << H, n2 = 1u << L, RS = stride(L);
-  extern __shared__ uint32_t sm_raw[];
-  uint32_t* data = reinterpret_cast<uint32_t*>((reinterpret_cast<uintptr_t>(sm_raw) + 127) & ~uintptr_t(127));
-  uint2* tw = reinterpret_cast<uint2*>(data + kC * RS);
-  uint64_t* bar = reinterpret_cast<uint64_t*>(tw + (n2 - R));
+  constexpr uint32_t R = 1u << H, RS = stride(L);
   const uint32_t tid = threadIdx.x;
   const uint32_t logn1 = a.logn - L;
   const uint32_t n = 1u << a.logn;
-  const uint32_t b = blockIdx.y, r0 = blockIdx.x * kC;
-  if (tid == 0) mbar_init(bar);
-  __syncthreads();
-  if (tid == 0) {
-    mbar_expect(bar, kC * n2 * 4u);
-    const uint32_t* src = yt + (size_t)b * n + ((size_t)r0 << L);
-    for (uint32_t rho = 0; rho < kC; rho++) bulk_load(data + rho * RS, src + ((size_t)rho << L), n2 * 4u, bar);
-  }
-  load_pass_a_twiddles<L>(tw, a);
-  if (!cta_wait(bar, a.tb.fault)) return;
   const uint32_t rho = tid & (kC - 1), l = tid / kC;
   uint32_t* row = data + rho * RS;
   uint32_t x[R];
@@ -310,5 +305,157 @@ __global__ void __launch_bounds__(reg_ntt::kC << (L / 2))
   } else {
 #pragma unroll
     for (int e = 0; e < (int)R; e++) dst[(size_t)(((uint32_t)e << H) | hb) << logn1] = x[brev_c<H>(e)];
+  }
+}
+
+namespace reg_ntt {
+__device__ __forceinline__ uint32_t* align128(uint32_t* p) {
+  return reinterpret_cast<uint32_t*>((reinterpret_cast<uintptr_t>(p) + 127) & ~uintptr_t(127));
+}
+// The twist w^(j i1 n2) of pass-1 rows i1 for coset j != 0.
+template <int L>
+__device__ __forceinline__ void fill_twist(uint32_t* twist, const NttArgs& a, uint32_t j, uint32_t logn2) {
+  for (uint32_t i1 = threadIdx.x; i1 < (1u << L); i1 += blockDim.x)
+    twist[i1] = root_pow(a.tb, ((j * i1) << logn2) << a.twist_shift);
+}
+// Issues the tensor copies of pass-1 tile (b, c0) into dst (one thread).
+template <int L>
+__device__ __forceinline__ void fetch1(uint32_t* dst, const CUtensorMap* tmap, uint32_t b, uint32_t c0,
+                                       const NttArgs& a, uint64_t* bar) {
+  constexpr uint32_t n1 = 1u << L, BOX = n1 < 256 ? n1 : 256;  // rows per tensor copy
+  mbar_expect(bar, kC * n1 * 4u);
+  for (uint32_t y = 0; y < n1; y += BOX) tensor_load_3d(dst + y * kC, tmap, c0, y, b / a.in_div, bar);
+}
+// Issues the row copies of pass-2 tile (b, r0) into dst (one thread).
+template <int L>
+__device__ __forceinline__ void fetch2(uint32_t* dst, const uint32_t* yt, uint32_t b, uint32_t r0,
+                                       const NttArgs& a, uint64_t* bar) {
+  constexpr uint32_t n2 = 1u << L;
+  mbar_expect(bar, kC * n2 * 4u);
+  const uint32_t* src = yt + ((size_t)b << a.logn) + ((size_t)r0 << L);
+  for (uint32_t rho = 0; rho < kC; rho++) bulk_load(dst + rho * stride(L), src + ((size_t)rho << L), n2 * 4u, bar);
+}
+}  // namespace reg_ntt
+
+// Pass 1, one tile per CTA: columns c0 = blockIdx.x * 8 .. of the input
+// viewed as [n1][n2] (the tensor map's x = i2, y = i1, z = input block
+// b / in_div), block b = blockIdx.y.
+template <int L, bool INV>
+__global__ void __launch_bounds__(reg_ntt::kC << (L / 2), L == 10 ? 4 : 1)
+    ntt_reg1_kernel(const __grid_constant__ CUtensorMap tmap, uint32_t* __restrict__ yt, NttArgs a) {
+  using namespace reg_ntt;
+  constexpr uint32_t R = 1u << (L / 2), n1 = 1u << L;
+  extern __shared__ uint32_t sm_raw[];
+  uint32_t* data = align128(sm_raw);
+  uint2* tw = reinterpret_cast<uint2*>(data + pass1_words(L));
+  uint32_t* twist = reinterpret_cast<uint32_t*>(tw + (n1 - R));
+  uint64_t* bar = reinterpret_cast<uint64_t*>(twist + n1);
+  const uint32_t b = blockIdx.y, c0 = blockIdx.x * kC;
+  const uint32_t j = b % a.twist_mod;
+  if (threadIdx.x == 0) mbar_init(bar);
+  __syncthreads();
+  if (threadIdx.x == 0) fetch1<L>(data, &tmap, b, c0, a, bar);
+  load_pass_a_twiddles<L>(tw, a);
+  if (j) fill_twist<L>(twist, a, j, a.logn - L);
+  if (!cta_wait(bar, a.tb.fault)) return;  // (also orders the tables above)
+  reg1_tile<L, INV>(data, tw, twist, yt, a, b, c0, j);
+}
+
+// Pass 2, one tile per CTA: rows r0 = blockIdx.x * 8 .. of block b =
+// blockIdx.y, one bulk copy per row.
+template <int L, bool INV>
+__global__ void __launch_bounds__(reg_ntt::kC << (L / 2))
+    ntt_reg2_kernel(const uint32_t* __restrict__ yt, uint32_t* __restrict__ out, NttArgs a) {
+  using namespace reg_ntt;
+  constexpr uint32_t R = 1u << (L / 2), n2 = 1u << L;
+  extern __shared__ uint32_t sm_raw[];
+  uint32_t* data = align128(sm_raw);
+  uint2* tw = reinterpret_cast<uint2*>(data + kC * stride(L));
+  uint64_t* bar = reinterpret_cast<uint64_t*>(tw + (n2 - R));
+  const uint32_t b = blockIdx.y, r0 = blockIdx.x * kC;
+  if (threadIdx.x == 0) mbar_init(bar);
+  __syncthreads();
+  if (threadIdx.x == 0) fetch2<L>(data, yt, b, r0, a, bar);
+  load_pass_a_twiddles<L>(tw, a);
+  if (!cta_wait(bar, a.tb.fault)) return;
+  reg2_tile<L, INV>(data, tw, out, a, b, r0);
+}
+
+// Streamed pass 1: a resident grid whose CTAs walk the tiles t = blockIdx.x,
+// blockIdx.x + gridDim.x, ... < tiles (tile t: block t / (n2/8), columns
+// 8 (t mod n2/8) ..) through two tile buffers, so that the copy of a CTA's
+// next tile is in flight while it transforms the current one, and the
+// pass-A twiddles are loaded once per CTA rather than once per tile.
+// Buffer s = k mod 2 of a CTA's k-th tile completes its barrier's phase
+// k / 2, waited for with parity (k / 2) mod 2.
+template <int L, bool INV>
+__global__ void __launch_bounds__(reg_ntt::kC << (L / 2), L == 10 ? 2 : 4)
+    ntt_reg1s_kernel(const __grid_constant__ CUtensorMap tmap, uint32_t* __restrict__ yt, NttArgs a,
+                     uint32_t tiles) {
+  using namespace reg_ntt;
+  constexpr uint32_t R = 1u << (L / 2), n1 = 1u << L, W = pass1_words(L);
+  extern __shared__ uint32_t sm_raw[];
+  uint32_t* buf = align128(sm_raw);
+  uint2* tw = reinterpret_cast<uint2*>(buf + 2 * W);
+  uint32_t* twist = reinterpret_cast<uint32_t*>(tw + (n1 - R));
+  uint64_t* bar = reinterpret_cast<uint64_t*>(twist + n1);
+  const uint32_t logn2 = a.logn - L;
+  const uint32_t per_b = (1u << logn2) / kC;
+  if (threadIdx.x == 0) {
+    mbar_init(bar);
+    mbar_init(bar + 1);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && blockIdx.x < tiles)
+    fetch1<L>(buf, &tmap, blockIdx.x / per_b, (blockIdx.x % per_b) * kC, a, bar);
+  load_pass_a_twiddles<L>(tw, a);
+  uint32_t k = 0;
+  for (uint32_t t = blockIdx.x; t < tiles; t += gridDim.x, k++) {
+    const uint32_t s = k & 1u, tn = t + gridDim.x;
+    // The other buffer was last read before the barrier that ended the
+    // previous tile (and its proxy fences).
+    if (threadIdx.x == 0 && tn < tiles) fetch1<L>(buf + (s ^ 1u) * W, &tmap, tn / per_b, (tn % per_b) * kC, a, bar + (s ^ 1u));
+    const uint32_t b = t / per_b, c0 = (t % per_b) * kC;
+    const uint32_t j = b % a.twist_mod;
+    if (j) fill_twist<L>(twist, a, j, logn2);
+    if (!cta_wait(bar + s, a.tb.fault, (k >> 1) & 1u, tn < tiles ? bar + (s ^ 1u) : nullptr,
+                  ((k + 1) >> 1) & 1u))
+      return;
+    reg1_tile<L, INV>(buf + s * W, tw, twist, yt, a, b, c0, j);
+    fence_proxy_async();
+    __syncthreads();  // buffer s and the twist table are free
+  }
+}
+
+// Streamed pass 2: the same walk over the row tiles (tile t: block
+// t / (n1/8), rows 8 (t mod n1/8) ..).
+template <int L, bool INV>
+__global__ void __launch_bounds__(reg_ntt::kC << (L / 2), L == 10 ? 2 : 4)
+    ntt_reg2s_kernel(const uint32_t* __restrict__ yt, uint32_t* __restrict__ out, NttArgs a, uint32_t tiles) {
+  using namespace reg_ntt;
+  constexpr uint32_t R = 1u << (L / 2), n2 = 1u << L, W = kC * stride(L);
+  extern __shared__ uint32_t sm_raw[];
+  uint32_t* buf = align128(sm_raw);
+  uint2* tw = reinterpret_cast<uint2*>(buf + 2 * W);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(tw + (n2 - R));
+  const uint32_t per_b = (1u << (a.logn - L)) / kC;
+  if (threadIdx.x == 0) {
+    mbar_init(bar);
+    mbar_init(bar + 1);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && blockIdx.x < tiles)
+    fetch2<L>(buf, yt, blockIdx.x / per_b, (blockIdx.x % per_b) * kC, a, bar);
+  load_pass_a_twiddles<L>(tw, a);
+  uint32_t k = 0;
+  for (uint32_t t = blockIdx.x; t < tiles; t += gridDim.x, k++) {
+    const uint32_t s = k & 1u, tn = t + gridDim.x;
+    if (threadIdx.x == 0 && tn < tiles) fetch2<L>(buf + (s ^ 1u) * W, yt, tn / per_b, (tn % per_b) * kC, a, bar + (s ^ 1u));
+    if (!cta_wait(bar + s, a.tb.fault, (k >> 1) & 1u, tn < tiles ? bar + (s ^ 1u) : nullptr,
+                  ((k + 1) >> 1) & 1u))
+      return;
+    reg2_tile<L, INV>(buf + s * W, tw, out, a, t / per_b, (t % per_b) * kC);
+    fence_proxy_async();
+    __syncthreads();
   }
 }

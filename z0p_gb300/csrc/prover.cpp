@@ -3823,8 +3823,8 @@ static int autotune_locked(z0p_gpu_ctx* c, uint32_t max_log_n, launch::Schedule*
     float t_def = 0.f, t_best = 0.f;
     uint32_t pick = 0, pick_r32 = 0;
     for (uint32_t s1 = (def > lo + 2 ? def - 2 : lo); s1 <= hi && s1 <= def + 2; s1++)
-      for (uint32_t r32 = 0; r32 < 3; r32++) {
-        if (r32 == 2 && !(launch::reg_split_ok(s1) && launch::reg_split_ok(l - s1))) continue;
+      for (uint32_t r32 = 0; r32 < 4; r32++) {
+        if (r32 >= 2 && !(launch::reg_split_ok(s1) && launch::reg_split_ok(l - s1))) continue;
         launch::Schedule s = base;
         s.ntt_log_n1[l] = (uint8_t)s1;
         s.ntt_radix32[l] = (uint8_t)r32;

@@ -2,7 +2,8 @@
 
 A schedule picks, per device, the four-step NTT split and pass variant
 (shared-memory passes in register groups of 16 or 32, or register passes
-with TMA-loaded tiles) for each transform size, the Merkle level where one
+with TMA-loaded tiles, one tile per CTA or streamed through a resident
+grid) for each transform size, the Merkle level where one
 top kernel takes over, and the proof-of-work grid. Every schedule gives byte-identical proofs.
 
     sched, report = tune.autotune(ctx)        # measure and install
@@ -36,6 +37,7 @@ def to_dict(s: Schedule) -> dict:
     return {"ntt_log_n1": {str(l): int(s.ntt_log_n1[l]) for l in range(32) if s.ntt_log_n1[l]},
             "ntt_radix32": sorted(l for l in range(32) if s.ntt_radix32[l] == 1),
             "ntt_regpass": sorted(l for l in range(32) if s.ntt_radix32[l] == 2),
+            "ntt_regstream": sorted(l for l in range(32) if s.ntt_radix32[l] == 3),
             "merkle_top_log": int(s.merkle_top_log), "grind_ctas_per_sm": int(s.grind_ctas_per_sm)}
 
 
@@ -47,6 +49,8 @@ def from_dict(d: dict) -> Schedule:
         s.ntt_radix32[int(l)] = 1
     for l in d.get("ntt_regpass", []):  # register passes (pass variant 2)
         s.ntt_radix32[int(l)] = 2
+    for l in d.get("ntt_regstream", []):  # streamed register passes (variant 3)
+        s.ntt_radix32[int(l)] = 3
     s.merkle_top_log = int(d.get("merkle_top_log", s.merkle_top_log))
     s.grind_ctas_per_sm = int(d.get("grind_ctas_per_sm", s.grind_ctas_per_sm))
     return s
