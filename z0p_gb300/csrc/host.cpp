@@ -255,6 +255,30 @@ void Hasher::update(const uint8_t* data, size_t len) {
   }
 }
 
+// The first of two tail chunks ends with block 15 (flags CHUNK_END, counter
+// next_index); push_merged of its output on a virtual copy of the stack
+// leaves stack[0..top_sl) and top_cv. Kept for this next_index.
+void Hasher::first_chunk_top() const {
+  if (top_ok && top_index == st->next_index) return;
+  uint32_t w[16], o[8];
+  chunk_block(st->tail, CHUNK_LEN, 15, w);
+  compress_cv(cv[0], w, st->next_index, 64, CHUNK_END, o);
+  for (int i = 0; i < 8; i++) put32(top_cv + 4 * i, o[i]);
+  uint32_t sl = st->stack_len;
+  uint64_t total = st->next_index + 1;
+  while (total % 2 == 0) {
+    parent(st->stack[sl - 1], top_cv, PARENT, top_cv);
+    sl--;
+    total /= 2;
+  }
+  top_sl = sl;
+  top_index = st->next_index;
+  top_ok = true;
+}
+void Hasher::prime() const {
+  if (st->total_len && st->tail_len > CHUNK_LEN) first_chunk_top();
+}
+
 // Hasher::finalize (src/hash.rs:276-302) without touching the state: the
 // first chunk's output, when the tail holds two, is merged into a virtual
 // copy of the stack top; the last chunk needs only its last block.
@@ -267,20 +291,13 @@ void Hasher::finalize(uint8_t out[32]) const {
   }
   size_t tl = st->tail_len;
   uint32_t sl = st->stack_len;
-  uint8_t top[32];
+  const uint8_t* top = nullptr;
   bool have_top = false;  // virtual stack = stack[0..sl) (+ top)
   uint32_t h = 0;
   if (tl > CHUNK_LEN) {
-    uint32_t w[16], o[8];
-    chunk_block(st->tail, CHUNK_LEN, 15, w);
-    compress_cv(cv[0], w, st->next_index, 64, CHUNK_END, o);
-    for (int i = 0; i < 8; i++) put32(top + 4 * i, o[i]);
-    uint64_t total = st->next_index + 1;  // push_merged on the virtual stack
-    while (total % 2 == 0) {
-      parent(st->stack[sl - 1], top, PARENT, top);
-      sl--;
-      total /= 2;
-    }
+    first_chunk_top();
+    top = top_cv;
+    sl = top_sl;
     have_top = true;
     h = 1;
   }
@@ -344,6 +361,7 @@ void Transcript::squeeze(const uint8_t* label, size_t llen, uint8_t out[32]) {
   copy.next_index = s.next_index;
   copy.total_len = s.total_len;
   copy.counter = s.counter;
+  h_.prime();  // the copy inherits the first chunk's merged entry
   Hasher hc = h_;
   hc.st = &copy;
   uint8_t sfx[16 + 64];

@@ -46,9 +46,20 @@ struct Hasher {
   // Leaves this cache for the next Hasher this thread builds on the same
   // tail (host.cpp, CacheMemo).
   void remember() const;
+  // Computes the merged first-chunk entry finalize needs (below) now, so
+  // that copies of this hasher start with it.
+  void prime() const;
 
  private:
   void advance();
+  void first_chunk_top() const;
+  // While the tail holds two chunks, finalize merges the first chunk's
+  // output into the stack: the result (stack[0..top_sl) then top_cv) is
+  // fixed until the first chunk is pushed, i.e. for one next_index.
+  mutable bool top_ok = false;
+  mutable uint64_t top_index = 0;
+  mutable uint32_t top_sl = 0;
+  mutable uint8_t top_cv[32];
 };
 
 // Fiat-Shamir transcript (src/transcript.rs:54-189) over the C-ABI state.

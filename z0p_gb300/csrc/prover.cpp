@@ -883,10 +883,15 @@ int run_fri_openings(z0p_gpu_ctx* c, const FriShape& s, const FriParams& fp, con
 
 void write_path(Writer& w, const uint8_t* digests, uint64_t leaf, uint32_t steps) {
   w.u32(steps);  // src/codec.rs:95-101: digest then direction byte (1 = left)
-  for (uint32_t s = 0; s < steps; s++) {
-    w.bytes(digests + 32 * s, 32);
-    w.byte(((leaf >> s) & 1) == 0 ? 1 : 0);
+  const size_t len = 33ull * steps;
+  if (w.n + len <= w.cap) {  // one capacity check for the whole path
+    uint8_t* o = w.p + w.n;
+    for (uint32_t s = 0; s < steps; s++, o += 33) {
+      std::memcpy(o, digests + 32 * s, 32);
+      o[32] = (uint8_t)(((leaf >> s) & 1u) ^ 1u);
+    }
   }
+  w.n += len;
 }
 
 // Opening block of query qi of proof k.
