@@ -59,12 +59,32 @@ __device__ __forceinline__ void store_digest(uint32_t* p, const uint32_t d[8]) {
 __constant__ ProofConsts g_consts[kConstSlots];
 
 struct FibMats {
-  uint32_t m[32][4];  // M^(2^k), canonical
+  uint32_t m[32][4];  // M^(2^k), Montgomery form
 };
 
+// Coset j's constants (ZinvArgs) for proof blockIdx.y: zinv is shared by
+// the group, cb is per proof.
+__device__ __forceinline__ void coset_constants(const ZinvArgs& z, const Tables& tb, uint32_t j) {
+  const uint32_t pk = blockIdx.y;
+  if (j >= (1u << z.logB)) return;
+  uint32_t xn = mmul(z.gamma_n_m, root_pow(tb, j << (kRootBits - z.logB)));
+  uint32_t xn1 = fsub(xn, kR);
+  if (pk == 0) {
+    uint32_t inv = minv(xn1);
+    z.zinv[j] = inv;
+    z.zinv2[j] = mmul(inv, kR2);
+  }
+  if (z.cb) z.cb[((size_t)pk << z.logB) + j] = mmul(g_consts[z.slot + pk].coeff, xn1);
+}
+
+// CTAs from trace_ctas on compute the per-coset constants (when z.zinv).
 __global__ void fib_trace_kernel(uint32_t* __restrict__ col_a, uint32_t* __restrict__ col_b,
                                  uint32_t n, uint32_t slot, FibMats mats,
-                                 uint32_t per_lane) {
+                                 uint32_t per_lane, uint32_t trace_ctas, ZinvArgs z, Tables tb) {
+  if (blockIdx.x >= trace_ctas) {
+    coset_constants(z, tb, (blockIdx.x - trace_ctas) * blockDim.x + threadIdx.x);
+    return;
+  }
   const uint32_t pk = blockIdx.y;  // proof of the group
   col_a += (size_t)pk * n;
   col_b += (size_t)pk * n;
@@ -72,21 +92,24 @@ __global__ void fib_trace_kernel(uint32_t* __restrict__ col_a, uint32_t* __restr
   const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const uint64_t start = (t >> 5) * 32 * per_lane + (t & 31);
   if (start >= n) return;
-  uint32_t r00 = 1, r01 = 0, r10 = 0, r11 = 1;
+  // R = M^start in Montgomery form (the powers of M commute), one reduction
+  // per entry of each product.
+  uint32_t r00 = kR, r01 = 0, r10 = 0, r11 = kR;
   for (int k = 0; k < 32; k++) {
     if ((start >> k) & 1u) {
       const uint32_t* q = mats.m[k];
-      uint32_t n00 = fadd(fmul(r00, q[0]), fmul(r01, q[2]));
-      uint32_t n01 = fadd(fmul(r00, q[1]), fmul(r01, q[3]));
-      uint32_t n10 = fadd(fmul(r10, q[0]), fmul(r11, q[2]));
-      uint32_t n11 = fadd(fmul(r10, q[1]), fmul(r11, q[3]));
+      const uint32_t n00 = mdot2(r00, q[0], r01, q[2]);
+      const uint32_t n01 = mdot2(r00, q[1], r01, q[3]);
+      const uint32_t n10 = mdot2(r10, q[0], r11, q[2]);
+      const uint32_t n11 = mdot2(r10, q[1], r11, q[3]);
       r00 = n00; r01 = n01; r10 = n10; r11 = n11;
     }
   }
-  uint32_t a = fadd(fmul(r00, a0), fmul(r01, b0));
-  uint32_t b = fadd(fmul(r10, a0), fmul(r11, b0));
-  const uint32_t s00 = to_mont(mats.m[5][0]), s01 = to_mont(mats.m[5][1]);
-  const uint32_t s10 = to_mont(mats.m[5][2]), s11 = to_mont(mats.m[5][3]);
+  // Montgomery R times canonical (a0, b0): canonical rows.
+  uint32_t a = mdot2(r00, a0, r01, b0);
+  uint32_t b = mdot2(r10, a0, r11, b0);
+  const uint32_t s00 = mats.m[5][0], s01 = mats.m[5][1];
+  const uint32_t s10 = mats.m[5][2], s11 = mats.m[5][3];
   for (uint32_t j = 0; j < per_lane; j++) {
     const uint64_t i = start + 32ull * j;
     if (i >= n) break;
@@ -375,19 +398,8 @@ __global__ void __launch_bounds__(512) ntt_pass2_kernel(const uint32_t* __restri
 // Per coset j: 1 / (x^N - 1) with x^N = 31^N * omega_B^j (constant on the
 // coset), in Montgomery form, the same value times 2^32 once more, and the
 // linked-column constant C_j = coeff * (x^N - 1) (canonical).
-__global__ void coset_zinv_kernel(uint32_t* zinv, uint32_t* zinv2, uint32_t logB,
-                                  uint32_t gamma_n_m, uint32_t* cb, uint32_t slot, Tables tb) {
-  const uint32_t pk = blockIdx.y;  // zinv is shared by the group; cb is per proof
-  uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= (1u << logB)) return;
-  uint32_t xn = mmul(gamma_n_m, root_pow(tb, j << (kRootBits - logB)));
-  uint32_t xn1 = fsub(xn, kR);
-  if (pk == 0) {
-    uint32_t inv = minv(xn1);
-    zinv[j] = inv;
-    zinv2[j] = mmul(inv, kR2);
-  }
-  if (cb) cb[((size_t)pk << logB) + j] = mmul(g_consts[slot + pk].coeff, xn1);
+__global__ void coset_zinv_kernel(ZinvArgs z, Tables tb) {
+  coset_constants(z, tb, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // B at row k = B q + j of the LDE from A: A[j][q+1] + C_j / (x_k - w_last),
@@ -1958,16 +1970,21 @@ cudaError_t const_slot_address(int slot, void** ptr) {
 }
 
 cudaError_t fib_trace(cudaStream_t st, uint32_t* col_a, uint32_t* col_b, uint32_t n, uint32_t slot,
-                      const uint32_t mats[32][4], uint32_t nproofs) {
-  FibMats fm;
+                      const uint32_t mats[32][4], uint32_t nproofs, const ZinvArgs* zinv,
+                      const Tables* tb) {
+  if (zinv && !tb) return cudaErrorInvalidValue;
+  FibMats fm;  // M^(2^k) in Montgomery form
   for (int k = 0; k < 32; k++)
-    for (int i = 0; i < 4; i++) fm.m[k][i] = mats[k][i];
+    for (int i = 0; i < 4; i++) fm.m[k][i] = (uint32_t)(((uint64_t)mats[k][i] << 32) % kP);
   const uint32_t per_lane = 16;  // rows per lane; a warp covers 512 consecutive rows
   const uint64_t threads = 32 * ((n + 32 * per_lane - 1) / (32 * per_lane));
+  const uint32_t trace_ctas = (uint32_t)grid_for(threads);
+  const ZinvArgs z = zinv ? *zinv : ZinvArgs{};
+  const uint32_t extra = zinv ? (uint32_t)grid_for(1ull << zinv->logB) : 0u;
   Stage stg("trace", st);
   stg.launched();
-  fib_trace_kernel<<<dim3(grid_for(threads), nproofs), kThreads, 0, st>>>(col_a, col_b, n, slot, fm,
-                                                                          per_lane);
+  fib_trace_kernel<<<dim3(trace_ctas + extra, nproofs), kThreads, 0, st>>>(
+      col_a, col_b, n, slot, fm, per_lane, trace_ctas, z, tb ? *tb : Tables{});
   return cudaGetLastError();
 }
 
@@ -2285,8 +2302,8 @@ cudaError_t coset_zinv(cudaStream_t st, const Tables& tb, uint32_t* zinv, uint32
                        uint32_t nproofs) {
   Stage stg("coset_zinv", st);
   stg.launched();
-  coset_zinv_kernel<<<dim3(grid_for(1ull << logB), nproofs), kThreads, 0, st>>>(
-      zinv, zinv2, logB, gamma_n_m, cb, slot, tb);
+  const ZinvArgs z{zinv, zinv2, logB, gamma_n_m, cb, slot};
+  coset_zinv_kernel<<<dim3(grid_for(1ull << logB), nproofs), kThreads, 0, st>>>(z, tb);
   return cudaGetLastError();
 }
 

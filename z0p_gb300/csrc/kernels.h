@@ -73,6 +73,19 @@ constexpr int kMaxGroup = 64;
 constexpr uint32_t kFoldTabWords = 48;
 constexpr uint32_t kPowHeadWords = 16;
 
+// Per coset j of an LDE of 2^logB cosets (x^N = 31^N omega_B^j, gamma_n_m =
+// 31^N in Montgomery form): zinv = 1/(x^N - 1) (Montgomery), zinv2 = zinv *
+// 2^32, and, when cb is non-null, cb = coeff * (x^N - 1) (canonical; coeff
+// from the slot), the linked-column constant.
+struct ZinvArgs {
+  uint32_t* zinv;
+  uint32_t* zinv2;
+  uint32_t logB;
+  uint32_t gamma_n_m;
+  uint32_t* cb;
+  uint32_t slot;
+};
+
 struct AirComposeArgs {
   const uint32_t* lde_a;  // coset-major [j][q]
   const uint32_t* cb;     // per coset C_j (canonical)
@@ -320,16 +333,17 @@ cudaError_t const_slot_address(int slot, void** ptr);
 // once (grid y = proof). Proof k's buffers sit at the given per-proof strides
 // from proof 0's, its ProofConsts in slot + k, and its counters and search
 // state at index k.
+// With `zinv` the launch also computes the per-coset constants (extra CTAs
+// beside the trace's, as coset_zinv would).
 cudaError_t fib_trace(cudaStream_t st, uint32_t* col_a, uint32_t* col_b, uint32_t n, uint32_t slot,
-                      const uint32_t mats[32][4], uint32_t nproofs = 1);
+                      const uint32_t mats[32][4], uint32_t nproofs = 1, const ZinvArgs* zinv = nullptr,
+                      const Tables* tb = nullptr);
 // Proof k: cols + k n ncols, values + k ncols.
 cudaError_t fill_constant_columns(cudaStream_t st, uint32_t* cols, uint32_t n, uint32_t ncols,
                                   const uint32_t* d_values, uint32_t nproofs = 1);
 cudaError_t ntt(cudaStream_t st, const Tables& tb, const NttPlan& plan, const uint32_t* in,
                 uint32_t* out, uint32_t* scratch);
-// Per coset j (x^N = 31^N omega_B^j): zinv = 1/(x^N - 1) (Montgomery),
-// zinv2 = zinv * 2^32, and, when cb is non-null, cb = coeff * (x^N - 1)
-// (canonical; coeff from the slot), the linked-column constant.
+// The per-coset constants of ZinvArgs in a launch of their own.
 cudaError_t coset_zinv(cudaStream_t st, const Tables& tb, uint32_t* zinv, uint32_t* zinv2,
                        uint32_t logB, uint32_t gamma_n_m, uint32_t* cb, uint32_t slot,
                        uint32_t nproofs = 1);

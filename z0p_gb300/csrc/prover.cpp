@@ -1854,7 +1854,9 @@ int air_prove(z0p_gpu_ctx* c, const AirTask* tasks, uint32_t K) {
   // Column B is derived from A wherever it is needed (linked_lde,
   // src/air.rs:806-844): B(x) = A(omega_N x) + C_j / (x - w_last).
   CK(push_consts(c, K));
-  CK(launch::fib_trace(st, cols, cols + N * K, (uint32_t)N, slot, mats, K));
+  // The per-coset constants come from extra CTAs of the trace launch.
+  const ZinvArgs za{zinv, zinv2, logB, to_mont(fpow(GENERATOR, N)), cb, slot};
+  CK(launch::fib_trace(st, cols, cols + N * K, (uint32_t)N, slot, mats, K, &za, &c->tb));
   NttPlan ip;
   ip.logn = logN; ip.batch = K; ip.inverse = 1; ip.post_gamma = 1;
   CK(launch::ntt(st, c->tb, ip, cols, coeffs, (uint32_t*)c->scratch.p));
@@ -1863,7 +1865,6 @@ int air_prove(z0p_gpu_ctx* c, const AirTask* tasks, uint32_t K) {
   lp.twist_shift = 27 - logm;
   CK(launch::ntt(st, c->tb, lp, coeffs, lde, (uint32_t*)c->scratch.p));
   const uint32_t* lde_a = lde;
-  CK(launch::coset_zinv(st, c->tb, zinv, zinv2, logB, to_mont(fpow(GENERATOR, N)), cb, slot, K));
   const uint32_t w_last_m = to_mont(w_last);
 
   // Joint trace tree over 8-row 64-byte leaves (src/air.rs:520-537).
