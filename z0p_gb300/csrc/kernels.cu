@@ -35,6 +35,33 @@ inline unsigned grid_for(uint64_t n, int threads = kThreads) {
   return (unsigned)((n + threads - 1) / threads);
 }
 
+// Programmatic dependent launch. Every kernel of this file starts with
+// pdl_wait(): it returns once the stream's preceding kernel has completed and
+// its writes are visible (at once for a kernel launched without the
+// attribute). launch_dep launches with programmatic stream serialization, so
+// the kernel is scheduled as its predecessor's CTAs exit instead of after the
+// predecessor's completion has been processed: about 2 µs less between two
+// dependent kernels on a GB300.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+template <typename... KArgs, typename... Args>
+void launch_dep(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                Args&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  // A failed launch is left in the runtime's last error, which every
+  // launcher reads next (cudaGetLastError), as after <<< >>>.
+  (void)cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
+
 __device__ __forceinline__ uint32_t tw_exp(uint32_t e, uint32_t shift, uint32_t inverse) {
   uint32_t x = e << shift;
   return inverse ? 0u - x : x;
@@ -81,6 +108,7 @@ __device__ __forceinline__ void coset_constants(const ZinvArgs& z, const Tables&
 __global__ void fib_trace_kernel(uint32_t* __restrict__ col_a, uint32_t* __restrict__ col_b,
                                  uint32_t n, uint32_t slot, FibMats mats,
                                  uint32_t per_lane, uint32_t trace_ctas, ZinvArgs z, Tables tb) {
+  pdl_wait();
   if (blockIdx.x >= trace_ctas) {
     coset_constants(z, tb, (blockIdx.x - trace_ctas) * blockDim.x + threadIdx.x);
     return;
@@ -123,6 +151,7 @@ __global__ void fib_trace_kernel(uint32_t* __restrict__ col_a, uint32_t* __restr
 
 __global__ void fill_columns_kernel(uint32_t* cols, uint32_t n, uint32_t ncols,
                                     const uint32_t* __restrict__ values) {
+  pdl_wait();
   const uint32_t pk = blockIdx.y;
   uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= (uint64_t)n * ncols) return;
@@ -234,6 +263,7 @@ __host__ __device__ constexpr uint32_t tw_offset(uint32_t words) { return (words
 template <int L>
 __global__ void __launch_bounds__(512) ntt_small_kernel(const uint32_t* __restrict__ in,
                                                         uint32_t* __restrict__ out, NttArgs a) {
+  pdl_wait();
   extern __shared__ uint32_t sm[];
   constexpr uint32_t n = 1u << L;
   uint32_t* s = sm;
@@ -291,6 +321,7 @@ __host__ __device__ constexpr uint32_t col_stride(uint32_t L, uint32_t C) {
 template <int L1, int LOGC, int KM>
 __global__ void __launch_bounds__(512) ntt_pass1_kernel(const uint32_t* __restrict__ in,
                                                         uint32_t* __restrict__ yt, NttArgs a) {
+  pdl_wait();
   constexpr uint32_t C = 1u << LOGC;
   constexpr uint32_t n1 = 1u << L1;
   constexpr uint32_t cstride = col_stride(L1, C);
@@ -346,6 +377,7 @@ __global__ void __launch_bounds__(512) ntt_pass1_kernel(const uint32_t* __restri
 template <int L2, int LOGR, int KM>
 __global__ void __launch_bounds__(512) ntt_pass2_kernel(const uint32_t* __restrict__ yt,
                                                         uint32_t* __restrict__ out, NttArgs a) {
+  pdl_wait();
   constexpr uint32_t R = 1u << LOGR;
   constexpr uint32_t n2 = 1u << L2;
   constexpr uint32_t rstride = col_stride(L2, R);
@@ -399,6 +431,7 @@ __global__ void __launch_bounds__(512) ntt_pass2_kernel(const uint32_t* __restri
 // coset), in Montgomery form, the same value times 2^32 once more, and the
 // linked-column constant C_j = coeff * (x^N - 1) (canonical).
 __global__ void coset_zinv_kernel(ZinvArgs z, Tables tb) {
+  pdl_wait();
   coset_constants(z, tb, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
@@ -530,6 +563,7 @@ __global__ void __launch_bounds__(kTraceLeafThreads) air_trace_leaves_kernel(
     uint32_t* __restrict__ leaves, uint32_t* __restrict__ tinv, uint32_t logN, uint32_t logB,
     uint32_t nleaves, uint32_t top, uint32_t* cap, unsigned int* counter, uint64_t tree_stride,
     uint64_t cap_stride, const uint32_t* __restrict__ lde_b, Tables tb) {
+  pdl_wait();
   __shared__ uint32_t buf[2 * kTraceLeafThreads * 9];  // >= 2 * 9 * (kFuseMaxLeaves / 256) roots
   {
     const uint32_t pk = blockIdx.y;  // proof of the group
@@ -584,6 +618,7 @@ __global__ void __launch_bounds__(kThreads) range_trace_leaves_kernel(
     const uint32_t* __restrict__ lde, uint32_t* __restrict__ leaves, uint32_t logN, uint32_t logB,
     uint32_t ncols, uint64_t tree_stride, unsigned int* counter, uint32_t top, uint32_t* cap,
     uint64_t cap_stride) {
+  pdl_wait();
   __shared__ uint32_t buf[kFused ? 2 * kThreads * kTopStride : 1];
   const uint32_t u = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t m = 1u << (logN + logB);
@@ -636,6 +671,7 @@ __global__ void __launch_bounds__(kSegmentMaxRows) fold_segment_kernel(
     const uint32_t* __restrict__ cols, unsigned int* bad, uint32_t* __restrict__ lde,
     uint32_t* __restrict__ tree, uint32_t* __restrict__ cap, uint32_t logB, uint32_t top,
     uint32_t ninv_m, Tables tb) {
+  pdl_wait();
   constexpr uint32_t S = 1u << L;
   constexpr uint32_t cs = (skewed_len(S) + 1u) & ~1u;  // column stride (words)
   extern __shared__ uint32_t sm[];
@@ -704,6 +740,7 @@ __global__ void __launch_bounds__(kSegmentMaxRows) fold_segment_kernel(
 // shared memory.
 constexpr uint32_t kUniformMaxGroups = 512;
 __global__ void __launch_bounds__(128) uniform_trees_kernel(const UniformTree* trees) {
+  pdl_wait();
   __shared__ uint32_t top[2 * kUniformMaxGroups * 8];
   const UniformTree t = trees[blockIdx.x];
   if (t.G == 0 || t.G > kUniformMaxGroups || (t.G & (t.G - 1u)) || t.logS > 31 ||
@@ -764,6 +801,7 @@ __global__ void __launch_bounds__(128) uniform_trees_kernel(const UniformTree* t
 __global__ void merkle_level_kernel(const uint32_t* __restrict__ prev, uint32_t* __restrict__ next,
                                     uint64_t count, uint32_t* __restrict__ cap, uint64_t stride,
                                     uint64_t cap_stride) {
+  pdl_wait();
   uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= count) return;
   prev += blockIdx.y * stride;
@@ -785,6 +823,7 @@ __global__ void merkle_level_kernel(const uint32_t* __restrict__ prev, uint32_t*
 __global__ void merkle_level2_kernel(const uint32_t* __restrict__ prev, uint32_t* __restrict__ mid,
                                      uint32_t* __restrict__ next, uint64_t count,
                                      uint32_t* __restrict__ cap, uint64_t stride, uint64_t cap_stride) {
+  pdl_wait();
   uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= count) return;
   prev += blockIdx.y * stride;
@@ -807,6 +846,7 @@ __global__ void merkle_level2_kernel(const uint32_t* __restrict__ prev, uint32_t
 
 __global__ void copy_words_kernel(const uint32_t* __restrict__ src, uint32_t* __restrict__ dst,
                                   uint64_t n, uint64_t src_stride, uint64_t dst_stride) {
+  pdl_wait();
   uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) dst[blockIdx.y * dst_stride + i] = src[blockIdx.y * src_stride + i];
 }
@@ -825,6 +865,7 @@ __global__ void __launch_bounds__(kTopThreads) merkle_top_kernel(uint32_t* tree,
                                                                  unsigned int* counter,
                                                                  uint32_t* cap, uint64_t stride,
                                                                  uint64_t cap_stride) {
+  pdl_wait();
   __shared__ uint32_t sm[2][kTopMaxRoots * kTopStride];
   tree += blockIdx.y * stride;  // proof of the group: its tree, counter and cap
   counter += blockIdx.y;
@@ -870,6 +911,7 @@ __global__ void __launch_bounds__(kTopThreads) merkle_top_kernel(uint32_t* tree,
 __global__ void leaf64_kernel(const uint32_t* __restrict__ flat, uint32_t* __restrict__ leaves,
                               uint64_t count, uint64_t npad, uint64_t in_stride,
                               uint64_t out_stride) {
+  pdl_wait();
   uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= npad) return;
   flat += blockIdx.y * in_stride;
@@ -890,6 +932,7 @@ __global__ void leaf64_kernel(const uint32_t* __restrict__ flat, uint32_t* __res
 // four (src/fri.rs:1422-1428).
 __global__ void leaf16_kernel(const uint32_t* __restrict__ values, uint32_t* __restrict__ leaves,
                               uint64_t n, uint64_t in_stride, uint64_t out_stride) {
+  pdl_wait();
   uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   values += blockIdx.y * in_stride;
@@ -988,6 +1031,7 @@ __device__ __forceinline__ void store_leaf_values(const AirComposeArgs& a, uint3
 
 template <bool kFused>
 __global__ void __launch_bounds__(kThreads) air_compose_leaves_kernel(AirComposeArgs a, Tables tb) {
+  pdl_wait();
   // >= 2 * 9 * (kFuseMaxLeaves / 256) roots when fused
   __shared__ uint32_t buf[kFused ? 2 * kThreads * kTopStride : 1];
   if (!kFused) a.counter = nullptr;
@@ -1027,6 +1071,7 @@ __global__ void __launch_bounds__(kThreads) air_compose_leaves_kernel(AirCompose
 // Range-check composition (src/range.rs:678-741 == composition_at :746-774).
 __global__ void __launch_bounds__(kThreads) range_compose_leaves_kernel(RangeComposeArgs a,
                                                                         Tables tb) {
+  pdl_wait();
   const uint32_t logm = a.logN + a.logB;
   const uint32_t quarter = 1u << (logm - 2);
   uint32_t u = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1124,6 +1169,7 @@ __global__ void __launch_bounds__(kThreads) range_compose_leaves_kernel(RangeCom
 __global__ void mask_pad_kernel(const uint32_t* __restrict__ coeffs, const uint32_t* __restrict__ r,
                                 uint32_t* __restrict__ out, uint32_t n, uint32_t n_rand,
                                 uint32_t padded, Tables tb) {
+  pdl_wait();
   const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x, c = blockIdx.y;
   if (k >= padded) return;
   uint32_t v = k < n ? coeffs[(size_t)c * n + k] : 0u;
@@ -1142,6 +1188,7 @@ __global__ void mask_pad_kernel(const uint32_t* __restrict__ coeffs, const uint3
 __global__ void __launch_bounds__(kThreads) air_compose_general_kernel(AirComposeArgs a,
                                                                        const uint32_t* lde_b,
                                                                        uint32_t r, Tables tb) {
+  pdl_wait();
   const uint32_t logm = a.logN + a.logB;
   const uint32_t quarter = 1u << (logm - 2);
   const uint32_t u = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1196,6 +1243,7 @@ __global__ void __launch_bounds__(kThreads) air_compose_general_kernel(AirCompos
 // chain of Montgomery products of canonical factors and is brought back to
 // canonical by one product with R^len.
 __global__ void __launch_bounds__(kThreads) table_compose_kernel(TableComposeArgs a, Tables tb) {
+  pdl_wait();
   const uint32_t logm = a.logN + a.logB;
   const uint32_t quarter = 1u << (logm - 2);
   const uint32_t u = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1240,6 +1288,7 @@ __global__ void __launch_bounds__(kThreads) table_compose_kernel(TableComposeArg
 // value. Values >= p raise *bad (the C boundary takes canonical elements).
 __global__ void gamma_scale_kernel(const uint32_t* __restrict__ in, uint32_t* __restrict__ out,
                                    uint32_t n, uint32_t ext, unsigned int* bad, Tables tb) {
+  pdl_wait();
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x, c = blockIdx.y;
   if (i >= n) return;
   const uint32_t v = in[ext ? 4 * (size_t)i + c : i];
@@ -1267,6 +1316,7 @@ struct Layer0Args {
 // the launch hashes the tree up to `top`, as air_compose_leaves does.
 template <bool kFused>
 __global__ void __launch_bounds__(kThreads) layer0_leaves_kernel(Layer0Args a) {
+  pdl_wait();
   __shared__ uint32_t buf[kFused ? 2 * kThreads * kTopStride : 1];
   const uint32_t quarter = 1u << (a.logm - 2);
   const uint32_t u = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1322,6 +1372,7 @@ __global__ void __launch_bounds__(kThreads) layer0_leaves_kernel(Layer0Args a) {
 // batched inversion per thread, stored coset-major at [j][q], k = B q + j.
 __global__ void row_inverses_kernel(uint32_t* __restrict__ tinv, uint32_t w_last_m, uint32_t logN,
                                     uint32_t logB, Tables tb) {
+  pdl_wait();
   const uint32_t logm = logN + logB;
   const uint32_t L = blockIdx.x * blockDim.x + threadIdx.x;
   if (L >= (1u << (logm - 3))) return;
@@ -1358,6 +1409,7 @@ __global__ void row_inverses_kernel(uint32_t* __restrict__ tinv, uint32_t w_last
 constexpr uint32_t kCombineStage = 32;
 template <bool kFused>
 __global__ void __launch_bounds__(kThreads) fold_combine_kernel(FoldCombineArgs a, Tables tb) {
+  pdl_wait();
   __shared__ uint32_t buf[kFused ? 2 * kThreads * kTopStride : 1];
   __shared__ FoldStepDev stage[kCombineStage];
   static_assert(sizeof(FoldStepDev) % 4 == 0, "staged as words");
@@ -1468,6 +1520,7 @@ __global__ void __launch_bounds__(64) fold_openings_kernel(const FoldStepDev* st
                                                           uint32_t logN, uint32_t logB,
                                                           uint32_t path_steps, uint32_t* out,
                                                           uint32_t stride) {
+  pdl_wait();
   const uint32_t qi = blockIdx.x, k = blockIdx.y;
   const FoldStepDev& S = steps[k];
   const uint32_t logm = logN + logB;
@@ -1569,6 +1622,7 @@ __device__ __forceinline__ void stage_fold_tab(const FoldArgs& a, const Tables& 
 // Large layers (and folds that stop at their CTAs' subtrees): the tables are
 // constant-bank operands of the products.
 __global__ void __launch_bounds__(kFoldThreads) fri_fold_leaf_kernel(FoldArgs a, Tables tb) {
+  pdl_wait();
   __shared__ uint32_t sm[2 * kTopStride * kFoldThreads];  // the CTA's subtree levels
   fold_for_proof(a);
   a.counter = nullptr;
@@ -1619,6 +1673,7 @@ __global__ void __launch_bounds__(kFoldThreads) fri_fold_leaf_kernel(FoldArgs a,
 // so each CTA hashes a subtree of 128 leaves.
 constexpr int kFold4Threads = 4 * kFoldThreads;
 __global__ void __launch_bounds__(kFold4Threads) fri_fold_quad_kernel(FoldArgs a, Tables tb) {
+  pdl_wait();
   __shared__ uint32_t sm[2 * kTopStride * (kFuseMaxLeaves / kFoldThreads)];
   __shared__ FoldTab tab;
   fold_for_proof(a);
@@ -1668,6 +1723,7 @@ __global__ void __launch_bounds__(kFold4Threads) fri_fold_quad_kernel(FoldArgs a
 
 // Thread per next-layer value (small layers; leaves hashed separately).
 __global__ void fri_fold_plain_kernel(FoldArgs a, Tables tb) {
+  pdl_wait();
   __shared__ FoldTab tab;
   fold_for_proof(a);
   stage_fold_tab(a, tb, tab);
@@ -1729,6 +1785,7 @@ __device__ __forceinline__ void grind_finish(const GrindArgs& a) {
 constexpr uint32_t kPowHeadLen = 47;
 
 __global__ void __launch_bounds__(kGrindThreads) grind_kernel(GrindArgs a) {
+  pdl_wait();
   a.head += kPowHeadWords * blockIdx.y;  // proof of the group: its head, search state and result
   a.state += 4 * blockIdx.y;
   a.out += 2 * blockIdx.y;
@@ -1795,6 +1852,7 @@ constexpr uint32_t kNatTileQ = 64;
 __global__ void __launch_bounds__(256) coset_to_natural_kernel(const uint32_t* __restrict__ in,
                                                                uint32_t* __restrict__ out,
                                                                uint32_t logN, uint32_t logB) {
+  pdl_wait();
   __shared__ uint32_t tile[32][kNatTileQ + 1];
   const uint64_t n = 1ull << logN, m = n << logB;
   const uint64_t q0 = (uint64_t)blockIdx.x * kNatTileQ, j0 = (uint64_t)blockIdx.y * 32;
@@ -1819,6 +1877,7 @@ __global__ void __launch_bounds__(256) coset_to_natural_kernel(const uint32_t* _
 // bound by the BLAKE3 arithmetic alone, with no memory traffic.
 __global__ void __launch_bounds__(256) hash_ceiling_kernel(const uint32_t* __restrict__ in,
                                                            uint32_t* __restrict__ out, int iters) {
+  pdl_wait();
   const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   uint32_t l[8], r[8];
   load_digest(in + 16 * t, l);
@@ -1841,6 +1900,7 @@ __global__ void __launch_bounds__(256) hash_ceiling_kernel(const uint32_t* __res
 // The argument block stays in parameter space (__grid_constant__): the
 // layer table is indexed at run time without a per-thread local copy.
 __global__ void __launch_bounds__(128) openings_kernel(const __grid_constant__ OpenArgs a) {
+  pdl_wait();
   const uint32_t qi = blockIdx.x, pk = blockIdx.y;  // query, proof of the group
   if (a.go) wait_gate(a.go, a.go_epoch, a.fault);
   uint32_t* out = a.out + ((size_t)pk * a.nq + qi) * a.stride;
@@ -1983,7 +2043,7 @@ cudaError_t fib_trace(cudaStream_t st, uint32_t* col_a, uint32_t* col_b, uint32_
   const uint32_t extra = zinv ? (uint32_t)grid_for(1ull << zinv->logB) : 0u;
   Stage stg("trace", st);
   stg.launched();
-  fib_trace_kernel<<<dim3(trace_ctas + extra, nproofs), kThreads, 0, st>>>(
+  launch_dep(fib_trace_kernel, dim3(trace_ctas + extra, nproofs), kThreads, 0, st,
       col_a, col_b, n, slot, fm, per_lane, trace_ctas, z, tb ? *tb : Tables{});
   return cudaGetLastError();
 }
@@ -1992,7 +2052,7 @@ cudaError_t fill_constant_columns(cudaStream_t st, uint32_t* cols, uint32_t n, u
                                   const uint32_t* d_values, uint32_t nproofs) {
   Stage stg("fill_columns", st);
   stg.launched();
-  fill_columns_kernel<<<dim3(grid_for((uint64_t)n * ncols), nproofs), kThreads, 0, st>>>(cols, n, ncols,
+  launch_dep(fill_columns_kernel, dim3(grid_for((uint64_t)n * ncols), nproofs), kThreads, 0, st, cols, n, ncols,
                                                                                        d_values);
   return cudaGetLastError();
 }
@@ -2126,13 +2186,14 @@ cudaError_t reg_pass1(cudaStream_t st, const CUtensorMap& map, uint32_t* yt, con
       if (cudaError_t e = raise_smem(ntt_reg1s_kernel<L, INV>, 10 + INV, L, smem)) return e;
       const uint32_t tiles = g.x * g.y;
       const uint32_t res = resident_ctas(ntt_reg1s_kernel<L, INV>, INV, L, threads, smem);
-      ntt_reg1s_kernel<L, INV><<<tiles < res ? tiles : res, threads, smem, st>>>(map, yt, a, tiles);
+      const uint32_t ctas = tiles < res ? tiles : res;
+      launch_dep(ntt_reg1s_kernel<L, INV>, ctas, threads, smem, st, map, yt, a, tiles);
       return cudaGetLastError();
     }
   }
   constexpr size_t smem = reg_ntt::pass1_smem(L);
   if (cudaError_t e = raise_smem(ntt_reg1_kernel<L, INV>, 6 + INV, L, smem)) return e;
-  ntt_reg1_kernel<L, INV><<<g, threads, smem, st>>>(map, yt, a);
+  launch_dep(ntt_reg1_kernel<L, INV>, g, threads, smem, st, map, yt, a);
   return cudaGetLastError();
 }
 template <int L, bool INV>
@@ -2145,13 +2206,14 @@ cudaError_t reg_pass2(cudaStream_t st, const uint32_t* yt, uint32_t* out, const 
       if (cudaError_t e = raise_smem(ntt_reg2s_kernel<L, INV>, 12 + INV, L, smem)) return e;
       const uint32_t tiles = g.x * g.y;
       const uint32_t res = resident_ctas(ntt_reg2s_kernel<L, INV>, 2 + INV, L, threads, smem);
-      ntt_reg2s_kernel<L, INV><<<tiles < res ? tiles : res, threads, smem, st>>>(yt, out, a, tiles);
+      const uint32_t ctas = tiles < res ? tiles : res;
+      launch_dep(ntt_reg2s_kernel<L, INV>, ctas, threads, smem, st, yt, out, a, tiles);
       return cudaGetLastError();
     }
   }
   constexpr size_t smem = reg_ntt::pass2_smem(L);
   if (cudaError_t e = raise_smem(ntt_reg2_kernel<L, INV>, 8 + INV, L, smem)) return e;
-  ntt_reg2_kernel<L, INV><<<g, threads, smem, st>>>(yt, out, a);
+  launch_dep(ntt_reg2_kernel<L, INV>, g, threads, smem, st, yt, out, a);
   return cudaGetLastError();
 }
 }  // namespace
@@ -2227,7 +2289,7 @@ cudaError_t ntt(cudaStream_t st, const Tables& tb, const NttPlan& plan, const ui
     stg.launched();
     switch (plan.logn) {
 #define Z0P_SMALL(Lv) \
-  case Lv: ntt_small_kernel<Lv><<<plan.batch, threads, smem, st>>>(in, out, a); break;
+  case Lv: launch_dep(ntt_small_kernel<Lv>, plan.batch, threads, smem, st, in, out, a); break;
       Z0P_SMALL(0) Z0P_SMALL(1) Z0P_SMALL(2) Z0P_SMALL(3) Z0P_SMALL(4) Z0P_SMALL(5)
       Z0P_SMALL(6) Z0P_SMALL(7) Z0P_SMALL(8) Z0P_SMALL(9) Z0P_SMALL(10) Z0P_SMALL(11)
       Z0P_SMALL(12)
@@ -2266,7 +2328,7 @@ cudaError_t ntt(cudaStream_t st, const Tables& tb, const NttPlan& plan, const ui
 #define Z0P_P1K(Lv, LC, KM)                                                                      \
     if (cudaError_t re = raise_smem(ntt_pass1_kernel<Lv, LC, KM>, 1 + slot, Lv, smem1))          \
       return re;                                                                                 \
-    ntt_pass1_kernel<Lv, LC, KM><<<g1, threads, smem1, st>>>(in, scratch, a);
+    launch_dep(ntt_pass1_kernel<Lv, LC, KM>, g1, threads, smem1, st, in, scratch, a);
 #define Z0P_P1(Lv, LC)                                                                           \
   case Lv:                                                                                       \
     if (r32) { Z0P_P1K(Lv, LC, 5) } else { Z0P_P1K(Lv, LC, 4) }                                  \
@@ -2282,7 +2344,7 @@ cudaError_t ntt(cudaStream_t st, const Tables& tb, const NttPlan& plan, const ui
 #define Z0P_P2K(Lv, LR, KM)                                                                      \
     if (cudaError_t re = raise_smem(ntt_pass2_kernel<Lv, LR, KM>, 2 + slot, Lv, smem2))          \
       return re;                                                                                 \
-    ntt_pass2_kernel<Lv, LR, KM><<<g2, threads, smem2, st>>>(scratch, out, a);
+    launch_dep(ntt_pass2_kernel<Lv, LR, KM>, g2, threads, smem2, st, scratch, out, a);
 #define Z0P_P2(Lv, LR)                                                                           \
   case Lv:                                                                                       \
     if (r32) { Z0P_P2K(Lv, LR, 5) } else { Z0P_P2K(Lv, LR, 4) }                                  \
@@ -2303,7 +2365,7 @@ cudaError_t coset_zinv(cudaStream_t st, const Tables& tb, uint32_t* zinv, uint32
   Stage stg("coset_zinv", st);
   stg.launched();
   const ZinvArgs z{zinv, zinv2, logB, gamma_n_m, cb, slot};
-  coset_zinv_kernel<<<dim3(grid_for(1ull << logB), nproofs), kThreads, 0, st>>>(z, tb);
+  launch_dep(coset_zinv_kernel, dim3(grid_for(1ull << logB), nproofs), kThreads, 0, st, z, tb);
   return cudaGetLastError();
 }
 
@@ -2323,8 +2385,8 @@ cudaError_t air_trace_leaves(cudaStream_t st, const Tables& tb, const uint32_t* 
                     : subtree_levels(nleaves < kTraceLeafThreads ? nleaves : kTraceLeafThreads, top);
   Stage stg("trace_leaves", st);
   stg.launched();
-  air_trace_leaves_kernel<<<dim3(grid_for(nleaves, kTraceLeafThreads), nproofs), kTraceLeafThreads,
-                            0, st>>>(lde_a, cb, w_last_m, leaves, tinv, logN, logB, nleaves, top, cap,
+  launch_dep(air_trace_leaves_kernel, dim3(grid_for(nleaves, kTraceLeafThreads), nproofs), kTraceLeafThreads,
+                            0, st, lde_a, cb, w_last_m, leaves, tinv, logN, logB, nleaves, top, cap,
                                      counter, tree_stride, cap_stride, lde_b, tb);
   return cudaGetLastError();
 }
@@ -2347,7 +2409,7 @@ cudaError_t fold_segment(cudaStream_t st, const Tables& tb, const uint32_t* cols
   stg.launched();
   switch (logN) {
 #define Z0P_SEG(Lv) \
-  case Lv: fold_segment_kernel<Lv><<<1, m, smem, st>>>(cols, bad, lde, tree, cap, logB, top, ninv_m, tb); break;
+  case Lv: launch_dep(fold_segment_kernel<Lv>, 1, m, smem, st, cols, bad, lde, tree, cap, logB, top, ninv_m, tb); break;
     Z0P_SEG(1) Z0P_SEG(2) Z0P_SEG(3) Z0P_SEG(4) Z0P_SEG(5) Z0P_SEG(6) Z0P_SEG(7) Z0P_SEG(8)
 #undef Z0P_SEG
     default: return cudaErrorInvalidValue;
@@ -2367,11 +2429,11 @@ cudaError_t range_trace_leaves(cudaStream_t st, const uint32_t* lde, uint32_t* l
   stg.launched();
   const dim3 grid(grid_for(m), nproofs);
   if (fused)
-    range_trace_leaves_kernel<true><<<grid, kThreads, 0, st>>>(lde, leaves, logN, logB, ncols,
+    launch_dep(range_trace_leaves_kernel<true>, grid, kThreads, 0, st, lde, leaves, logN, logB, ncols,
                                                                tree_stride, counter, top, cap,
                                                                cap_stride);
   else
-    range_trace_leaves_kernel<false><<<grid, kThreads, 0, st>>>(lde, leaves, logN, logB, ncols,
+    launch_dep(range_trace_leaves_kernel<false>, grid, kThreads, 0, st, lde, leaves, logN, logB, ncols,
                                                                 tree_stride, nullptr, 0, nullptr,
                                                                 0);
   return cudaGetLastError();
@@ -2385,7 +2447,7 @@ cudaError_t merkle_build(cudaStream_t st, uint32_t* tree, uint64_t leaves, uint3
   if (top == 0) {  // the cap is the leaf level itself
     if (!cap) return cudaSuccess;
     stg.launched();
-    copy_words_kernel<<<dim3(grid_for(8 * leaves), nproofs), kThreads, 0, st>>>(tree, cap, 8 * leaves,
+    launch_dep(copy_words_kernel, dim3(grid_for(8 * leaves), nproofs), kThreads, 0, st, tree, cap, 8 * leaves,
                                                                                stride, cap_stride);
     return cudaGetLastError();
   }
@@ -2403,7 +2465,7 @@ cudaError_t merkle_build(cudaStream_t st, uint32_t* tree, uint64_t leaves, uint3
     uint32_t* mid = tree + 8 * (2 * leaves - 2 * (leaves >> (level + 1)));
     uint32_t* next = tree + 8 * (2 * leaves - 2 * (leaves >> (level + 2)));
     stg.launched();
-    merkle_level2_kernel<<<dim3(grid_for(cnt), nproofs), kThreads, 0, st>>>(
+    launch_dep(merkle_level2_kernel, dim3(grid_for(cnt), nproofs), kThreads, 0, st,
         prev, mid, next, cnt, level + 2 == top ? cap : nullptr, stride, cap_stride);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
@@ -2414,7 +2476,7 @@ cudaError_t merkle_build(cudaStream_t st, uint32_t* tree, uint64_t leaves, uint3
     const uint32_t* prev = tree + 8 * (2 * leaves - 2 * (leaves >> level));
     uint32_t* next = tree + 8 * (2 * leaves - 2 * (leaves >> (level + 1)));
     stg.launched();
-    merkle_level_kernel<<<dim3(grid_for(cnt), nproofs), kThreads, 0, st>>>(
+    launch_dep(merkle_level_kernel, dim3(grid_for(cnt), nproofs), kThreads, 0, st,
         prev, next, cnt, level + 1 == top ? cap : nullptr, stride, cap_stride);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
@@ -2425,7 +2487,7 @@ cudaError_t merkle_build(cudaStream_t st, uint32_t* tree, uint64_t leaves, uint3
   const uint64_t per_cta_children = 2ull << (lsub - level - 1);  // level-l0 nodes per CTA
   const uint64_t blocks = ((leaves >> level) + per_cta_children - 1) / per_cta_children;
   stg.launched();
-  merkle_top_kernel<<<dim3((unsigned)blocks, nproofs), kTopThreads, 0, st>>>(
+  launch_dep(merkle_top_kernel, dim3((unsigned)blocks, nproofs), kTopThreads, 0, st,
       tree, leaves, level, top, counter, cap, stride, cap_stride);
   return cudaGetLastError();
 }
@@ -2443,9 +2505,9 @@ cudaError_t air_compose_leaves(cudaStream_t st, const Tables& tb, const AirCompo
   Stage stg("air_compose_leaves", st);
   stg.launched();
   if (f.counter)
-    air_compose_leaves_kernel<true><<<dim3(grid_for(quarter), nproofs), kThreads, 0, st>>>(f, tb);
+    launch_dep(air_compose_leaves_kernel<true>, dim3(grid_for(quarter), nproofs), kThreads, 0, st, f, tb);
   else
-    air_compose_leaves_kernel<false><<<dim3(grid_for(quarter), nproofs), kThreads, 0, st>>>(f, tb);
+    launch_dep(air_compose_leaves_kernel<false>, dim3(grid_for(quarter), nproofs), kThreads, 0, st, f, tb);
   return cudaGetLastError();
 }
 
@@ -2454,7 +2516,7 @@ cudaError_t range_compose_leaves(cudaStream_t st, const Tables& tb, const RangeC
   uint32_t quarter = 1u << (a.logN + a.logB - 2);
   Stage stg("range_compose_leaves", st);
   stg.launched();
-  range_compose_leaves_kernel<<<dim3(grid_for(quarter), nproofs), kThreads, 0, st>>>(a, tb);
+  launch_dep(range_compose_leaves_kernel, dim3(grid_for(quarter), nproofs), kThreads, 0, st, a, tb);
   return cudaGetLastError();
 }
 
@@ -2484,16 +2546,16 @@ cudaError_t fri_fold(cudaStream_t st, const Tables& tb, const FoldArgs& a, uint3
     stg.launched();
     const dim3 grid(grid_for(nleaf, kFoldThreads), nproofs);
     if (slot)
-      fri_fold_leaf_kernel<<<grid, kFoldThreads, 0, st>>>(f, tb);
+      launch_dep(fri_fold_leaf_kernel, grid, kFoldThreads, 0, st, f, tb);
     else
-      fri_fold_quad_kernel<<<grid, kFold4Threads, 0, st>>>(f, tb);
+      launch_dep(fri_fold_quad_kernel, grid, kFold4Threads, 0, st, f, tb);
     return cudaGetLastError();
   }
   if (!a.tab) return cudaErrorInvalidValue;
   {
     Stage stg("fri_fold_small", st);
     stg.launched();
-    fri_fold_plain_kernel<<<dim3(1, nproofs), 32, 0, st>>>(a, tb);
+    launch_dep(fri_fold_plain_kernel, dim3(1, nproofs), 32, 0, st, a, tb);
   }
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
@@ -2506,11 +2568,11 @@ cudaError_t layer_leaves(cudaStream_t st, const uint32_t* values, uint64_t len, 
   Stage stg("layer_leaves", st);
   stg.launched();
   if (len % 4 == 0) {
-    leaf64_kernel<<<dim3(grid_for(len / 4), nproofs), kThreads, 0, st>>>(values, leaves, len / 4,
+    launch_dep(leaf64_kernel, dim3(grid_for(len / 4), nproofs), kThreads, 0, st, values, leaves, len / 4,
                                                                         len / 4, in_stride,
                                                                         out_stride);
   } else {
-    leaf16_kernel<<<dim3(grid_for(len), nproofs), kThreads, 0, st>>>(values, leaves, len, in_stride,
+    launch_dep(leaf16_kernel, dim3(grid_for(len), nproofs), kThreads, 0, st, values, leaves, len, in_stride,
                                                                     out_stride);
   }
   return cudaGetLastError();
@@ -2521,7 +2583,7 @@ cudaError_t merkle_flat64_leaves(cudaStream_t st, const uint32_t* flat, uint64_t
   if (!count || npad < count) return cudaErrorInvalidValue;
   Stage stg("leaf64", st);
   stg.launched();
-  leaf64_kernel<<<grid_for(npad), kThreads, 0, st>>>(flat, leaves, count, npad, 0, 0);
+  launch_dep(leaf64_kernel, grid_for(npad), kThreads, 0, st, flat, leaves, count, npad, 0, 0);
   return cudaGetLastError();
 }
 
@@ -2573,7 +2635,7 @@ cudaError_t grind(cudaStream_t st, const uint32_t* head, uint32_t head_len, uint
   if (ctas < 1) ctas = 1;
   Stage stg("grind", st);
   stg.launched();
-  grind_kernel<<<dim3(ctas, nproofs), kGrindThreads, 0, st>>>(a);
+  launch_dep(grind_kernel, dim3(ctas, nproofs), kGrindThreads, 0, st, a);
   return cudaGetLastError();
 }
 
@@ -2581,7 +2643,7 @@ cudaError_t uniform_trees(cudaStream_t st, const UniformTree* trees, uint32_t nt
   if (ntrees == 0) return cudaSuccess;
   Stage stg("uniform_trees", st);
   stg.launched();
-  uniform_trees_kernel<<<ntrees, 128, 0, st>>>(trees);
+  launch_dep(uniform_trees_kernel, ntrees, 128, 0, st, trees);
   return cudaGetLastError();
 }
 
@@ -2589,7 +2651,7 @@ cudaError_t mask_pad(cudaStream_t st, const Tables& tb, const uint32_t* coeffs, 
                      uint32_t* out, uint32_t n, uint32_t n_rand, uint32_t padded, uint32_t ncols) {
   Stage stg("mask_pad", st);
   stg.launched();
-  mask_pad_kernel<<<dim3(grid_for(padded), ncols), kThreads, 0, st>>>(coeffs, r, out, n, n_rand, padded,
+  launch_dep(mask_pad_kernel, dim3(grid_for(padded), ncols), kThreads, 0, st, coeffs, r, out, n, n_rand, padded,
                                                                       tb);
   return cudaGetLastError();
 }
@@ -2597,7 +2659,7 @@ cudaError_t mask_pad(cudaStream_t st, const Tables& tb, const uint32_t* coeffs, 
 cudaError_t table_compose(cudaStream_t st, const Tables& tb, const TableComposeArgs& a) {
   Stage stg("table_compose", st);
   stg.launched();
-  table_compose_kernel<<<grid_for(1ull << (a.logN + a.logB - 2)), kThreads, 0, st>>>(a, tb);
+  launch_dep(table_compose_kernel, grid_for(1ull << (a.logN + a.logB - 2)), kThreads, 0, st, a, tb);
   return cudaGetLastError();
 }
 
@@ -2605,7 +2667,7 @@ cudaError_t air_compose_general(cudaStream_t st, const Tables& tb, const AirComp
                                 const uint32_t* lde_b, uint32_t r) {
   Stage stg("air_compose_leaves", st);
   stg.launched();
-  air_compose_general_kernel<<<grid_for(1ull << (a.logN + a.logB - 2)), kThreads, 0, st>>>(a, lde_b, r,
+  launch_dep(air_compose_general_kernel, grid_for(1ull << (a.logN + a.logB - 2)), kThreads, 0, st, a, lde_b, r,
                                                                                         tb);
   return cudaGetLastError();
 }
@@ -2614,7 +2676,7 @@ cudaError_t gamma_scale(cudaStream_t st, const Tables& tb, const uint32_t* in, u
                         uint32_t n, uint32_t ext, unsigned int* bad) {
   Stage stg("fri_input", st);
   stg.launched();
-  gamma_scale_kernel<<<dim3(grid_for(n), ext ? 4 : 1), kThreads, 0, st>>>(in, out, n, ext, bad, tb);
+  launch_dep(gamma_scale_kernel, dim3(grid_for(n), ext ? 4 : 1), kThreads, 0, st, in, out, n, ext, bad, tb);
   return cudaGetLastError();
 }
 
@@ -2632,9 +2694,9 @@ cudaError_t layer0_leaves(cudaStream_t st, const uint32_t* src, uint32_t* layer0
   Stage stg("layer0_leaves", st);
   stg.launched();
   if (fused)
-    layer0_leaves_kernel<true><<<grid_for(quarter), kThreads, 0, st>>>(a);
+    launch_dep(layer0_leaves_kernel<true>, grid_for(quarter), kThreads, 0, st, a);
   else
-    layer0_leaves_kernel<false><<<grid_for(quarter), kThreads, 0, st>>>(a);
+    launch_dep(layer0_leaves_kernel<false>, grid_for(quarter), kThreads, 0, st, a);
   return cudaGetLastError();
 }
 
@@ -2643,7 +2705,7 @@ cudaError_t row_inverses(cudaStream_t st, const Tables& tb, uint32_t* tinv, uint
   if (logN + logB < 3) return cudaErrorInvalidValue;
   Stage stg("row_inverses", st);
   stg.launched();
-  row_inverses_kernel<<<grid_for(1ull << (logN + logB - 3)), kThreads, 0, st>>>(tinv, w_last_m, logN,
+  launch_dep(row_inverses_kernel, grid_for(1ull << (logN + logB - 3)), kThreads, 0, st, tinv, w_last_m, logN,
                                                                              logB, tb);
   return cudaGetLastError();
 }
@@ -2659,9 +2721,9 @@ cudaError_t fold_combine(cudaStream_t st, const Tables& tb, const FoldCombineArg
   Stage stg("fold_combine", st);
   stg.launched();
   if (fused)
-    fold_combine_kernel<true><<<grid_for(quarter), kThreads, 0, st>>>(a, tb);
+    launch_dep(fold_combine_kernel<true>, grid_for(quarter), kThreads, 0, st, a, tb);
   else
-    fold_combine_kernel<false><<<grid_for(quarter), kThreads, 0, st>>>(a, tb);
+    launch_dep(fold_combine_kernel<false>, grid_for(quarter), kThreads, 0, st, a, tb);
   return cudaGetLastError();
 }
 
@@ -2670,14 +2732,14 @@ cudaError_t fold_openings(cudaStream_t st, const FoldStepDev* steps, uint32_t ns
                           uint32_t path_steps, uint32_t* out, uint32_t stride) {
   Stage stg("fold_openings", st);
   stg.launched();
-  fold_openings_kernel<<<dim3(nq, nsteps), 64, 0, st>>>(steps, leaves, nq, logN, logB, path_steps,
+  launch_dep(fold_openings_kernel, dim3(nq, nsteps), 64, 0, st, steps, leaves, nq, logN, logB, path_steps,
                                                        out, stride);
   return cudaGetLastError();
 }
 
 cudaError_t hash_ceiling(cudaStream_t st, const uint32_t* in, uint32_t* out, uint32_t blocks,
                          int iters) {
-  hash_ceiling_kernel<<<blocks, 256, 0, st>>>(in, out, iters);
+  launch_dep(hash_ceiling_kernel, blocks, 256, 0, st, in, out, iters);
   return cudaGetLastError();
 }
 
@@ -2686,7 +2748,7 @@ cudaError_t openings(cudaStream_t st, const OpenArgs& a, uint32_t nproofs) {
   if (!a.nq) return cudaSuccess;
   Stage stg("gather", st);
   stg.launched();
-  openings_kernel<<<dim3(a.nq, nproofs), 128, 0, st>>>(a);
+  launch_dep(openings_kernel, dim3(a.nq, nproofs), 128, 0, st, a);
   return cudaGetLastError();
 }
 
@@ -2699,7 +2761,7 @@ cudaError_t coset_to_natural(cudaStream_t st, const uint32_t* in, uint32_t* out,
   if (qt > 0x7fffffffull) return cudaErrorInvalidValue;
   Stage stg("coset_to_natural", st);
   stg.launched();
-  coset_to_natural_kernel<<<dim3((unsigned)qt, jt, (unsigned)batch), 256, 0, st>>>(in, out, logN, logB);
+  launch_dep(coset_to_natural_kernel, dim3((unsigned)qt, jt, (unsigned)batch), 256, 0, st, in, out, logN, logB);
   return cudaGetLastError();
 }
 

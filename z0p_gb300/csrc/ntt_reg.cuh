@@ -343,6 +343,7 @@ __device__ __forceinline__ void fetch2(uint32_t* dst, const uint32_t* yt, uint32
 template <int L, bool INV>
 __global__ void __launch_bounds__(reg_ntt::kC << (L / 2), L == 10 ? 4 : 1)
     ntt_reg1_kernel(const __grid_constant__ CUtensorMap tmap, uint32_t* __restrict__ yt, NttArgs a) {
+  pdl_wait();
   using namespace reg_ntt;
   constexpr uint32_t R = 1u << (L / 2), n1 = 1u << L;
   extern __shared__ uint32_t sm_raw[];
@@ -366,6 +367,7 @@ __global__ void __launch_bounds__(reg_ntt::kC << (L / 2), L == 10 ? 4 : 1)
 template <int L, bool INV>
 __global__ void __launch_bounds__(reg_ntt::kC << (L / 2))
     ntt_reg2_kernel(const uint32_t* __restrict__ yt, uint32_t* __restrict__ out, NttArgs a) {
+  pdl_wait();
   using namespace reg_ntt;
   constexpr uint32_t R = 1u << (L / 2), n2 = 1u << L;
   extern __shared__ uint32_t sm_raw[];
@@ -392,6 +394,7 @@ template <int L, bool INV>
 __global__ void __launch_bounds__(reg_ntt::kC << (L / 2), L == 10 ? 2 : 4)
     ntt_reg1s_kernel(const __grid_constant__ CUtensorMap tmap, uint32_t* __restrict__ yt, NttArgs a,
                      uint32_t tiles) {
+  pdl_wait();
   using namespace reg_ntt;
   constexpr uint32_t R = 1u << (L / 2), n1 = 1u << L, W = pass1_words(L);
   extern __shared__ uint32_t sm_raw[];
@@ -432,6 +435,7 @@ __global__ void __launch_bounds__(reg_ntt::kC << (L / 2), L == 10 ? 2 : 4)
 template <int L, bool INV>
 __global__ void __launch_bounds__(reg_ntt::kC << (L / 2), L == 10 ? 2 : 4)
     ntt_reg2s_kernel(const uint32_t* __restrict__ yt, uint32_t* __restrict__ out, NttArgs a, uint32_t tiles) {
+  pdl_wait();
   using namespace reg_ntt;
   constexpr uint32_t R = 1u << (L / 2), n2 = 1u << L, W = kC * stride(L);
   extern __shared__ uint32_t sm_raw[];
