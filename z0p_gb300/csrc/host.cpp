@@ -349,6 +349,27 @@ void Transcript::absorb_raw(const uint8_t* label, size_t llen, const uint8_t* da
 void Transcript::absorb(const char* label, const uint8_t* data, size_t len) {
   absorb_raw((const uint8_t*)label, std::strlen(label), data, len);
 }
+void Transcript::absorb_each(const char* label, const uint8_t* data, size_t count, size_t len) {
+  const size_t llen = std::strlen(label), item = 16 + llen + len;
+  if (llen > 64 || item > 1024) {
+    for (size_t i = 0; i < count; i++) absorb_raw((const uint8_t*)label, llen, data + i * len, len);
+    return;
+  }
+  uint8_t buf[2048];  // whole framed items, LE64(|label|) || label || LE64(len) || item
+  size_t n = 0;
+  for (size_t i = 0; i < count; i++) {
+    if (n + item > sizeof buf) {
+      h_.update(buf, n);
+      n = 0;
+    }
+    put64(buf + n, llen);
+    std::memcpy(buf + n + 8, label, llen);
+    put64(buf + n + 8 + llen, len);
+    std::memcpy(buf + n + 16 + llen, data + i * len, len);
+    n += item;
+  }
+  if (n) h_.update(buf, n);
+}
 void Transcript::squeeze(const uint8_t* label, size_t llen, uint8_t out[32]) {
   // src/transcript.rs:162-171 on a copy of the history: only the parts in
   // use (tail bytes, stack entries, counts) are copied.

@@ -69,6 +69,9 @@ class Transcript {
   ~Transcript() { h_.remember(); }
   void absorb_raw(const uint8_t* label, size_t llen, const uint8_t* data, size_t len);
   void absorb(const char* label, const uint8_t* data, size_t len);
+  // `count` absorbs under one label of consecutive `len`-byte items: the same
+  // bytes as that many absorb calls, hashed in a few large updates.
+  void absorb_each(const char* label, const uint8_t* data, size_t count, size_t len);
   void squeeze(const uint8_t* label, size_t llen, uint8_t out[32]);
   void challenge_ext(const char* label, uint32_t out[4]);
   uint64_t challenge_index(const char* label, uint64_t domain);

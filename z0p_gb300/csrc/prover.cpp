@@ -651,8 +651,7 @@ int run_fri_commit(z0p_gpu_ctx* c, const FriShape& s, const FriParams& fp, const
       const uint8_t* cap = c->hio + h.fri_cap[l] + k * h.fri_cap_bytes[l];
       outs[k].caps[l].assign(cap, cap + h.fri_cap_bytes[l]);
       c->d2h += h.fri_cap_bytes[l];  // written by the tree kernel into the mapped buffer
-      for (size_t i = 0; i < h.fri_cap_bytes[l] / 32; i++)
-        transcript_absorb(*ts[k], "fri-layer-root", cap + 32 * i, 32);
+      ts[k]->absorb_each("fri-layer-root", cap, h.fri_cap_bytes[l] / 32, 32);
     }
   };
   // Fold l's challenges into its tables (src/fri.rs:603-606): the constant
@@ -1480,7 +1479,7 @@ int const_fri(z0p_gpu_ctx* c, const FriShape& s, const FriParams& fp, uint64_t p
       std::vector<uint8_t>& cap = f.fo.caps[l];
       cap.resize(32ull << s.drop[l]);
       for (uint64_t i = 0; i < (1ull << s.drop[l]); i++) std::memcpy(&cap[32 * i], tr.node(steps, i), 32);
-      for (size_t i = 0; i < cap.size() / 32; i++) transcript_absorb(t, "fri-layer-root", &cap[32 * i], 32);
+      t.absorb_each("fri-layer-root", cap.data(), cap.size() / 32, 32);
       if (l + 1 == nl) break;
       uint32_t ch[4];
       for (int r = 0; r < 3; r++) challenge_ext(t, "fri-fold", ch);  // the values do not depend on them
