@@ -208,6 +208,57 @@ cudaError_t sync(z0p_gpu_ctx* c, const char* site = "other", cudaEvent_t upto = 
   return e;
 }
 
+// A Merkle cap the device writes into the mapped buffer can be read as soon
+// as its last word lands, before the kernel that wrote it has retired and
+// the stream's completion has reached the host. arm_cap fills the cap's
+// region with kCapSentinel; it must run before the kernels that write the
+// cap are queued (after them, it could overwrite digests already written).
+// wait_cap then spins until no word of the region holds the sentinel,
+// querying the event (or the stream) every 64 passes, so that a launch that
+// failed, or a digest word equal to the sentinel (one chance in 2^32 a
+// word), ends the wait at the work's completion instead.
+constexpr uint32_t kCapSentinel = 0x6A09E667u;
+
+void arm_cap(z0p_gpu_ctx* c, size_t off, size_t bytes) {
+  uint32_t* w = reinterpret_cast<uint32_t*>(c->hio + off);
+  for (size_t i = 0; i < bytes / 4; i++) w[i] = kCapSentinel;
+  __atomic_thread_fence(__ATOMIC_SEQ_CST);
+}
+
+cudaError_t wait_cap(z0p_gpu_ctx* c, const char* site, size_t off, size_t bytes,
+                     cudaEvent_t upto = nullptr) {
+  c->syncs++;
+  const uint64_t t0 = now_ns();
+  const volatile uint32_t* w = reinterpret_cast<const volatile uint32_t*>(c->hio + off);
+  const size_t n = bytes / 4;
+  size_t i = 0;  // words before i are written (each is written once)
+  cudaError_t e = cudaSuccess;
+  for (uint32_t pass = 0;; pass++) {
+    while (i < n && w[i] != kCapSentinel) i++;
+    if (i == n) break;
+    if ((pass & 63u) == 63u) {
+      e = upto ? cudaEventQuery(upto) : cudaStreamQuery(c->stream);
+      if (e != cudaErrorNotReady) break;
+      e = cudaSuccess;
+    }
+  }
+  __atomic_thread_fence(__ATOMIC_ACQUIRE);
+  const uint64_t t1 = now_ns();
+  if (e == cudaSuccess && c->fault && *reinterpret_cast<volatile unsigned int*>(c->fault)) {
+    *c->fault = 0u;
+    e = cudaErrorLaunchTimeout;
+  }
+  c->sync_ns += t1 - t0;
+  if (c->profiling) {
+    HostSite& hs = c->sites[site];
+    hs.calls++;
+    hs.wait_ns += t1 - t0;
+    if (c->last_sync_ns) hs.before_ns += t0 - c->last_sync_ns;
+  }
+  c->last_sync_ns = t1;
+  return e;
+}
+
 // Workspace comes from one stream-ordered memory pool per device that keeps
 // freed memory for reuse: growing or releasing a context's buffers is queued
 // on its own stream and never synchronises the device, so contexts proving
@@ -602,9 +653,11 @@ struct FriTail {
 // word in the mapped buffer: the host then waits for a layer's event, absorbs
 // its cap, writes the next fold's tables and opens its gate, so no launch
 // stands between a challenge and its fold.
+// cap0_armed: layer 0's cap region was armed (arm_cap) before the kernels
+// that write it were queued, so its wait can end as soon as it lands.
 int run_fri_commit(z0p_gpu_ctx* c, const FriShape& s, const FriParams& fp, const FriBufs& fb,
                    uint64_t poly_len, uint64_t degree_bound, Transcript* const* ts, uint32_t K,
-                   const HioPlan& h, FriOut* outs, FriTail* tail = nullptr) {
+                   const HioPlan& h, FriOut* outs, FriTail* tail = nullptr, bool cap0_armed = false) {
   uint8_t dims[24];  // src/fri.rs:1450-1456
   for (int i = 0; i < 8; i++) {
     dims[i] = (uint8_t)(s.m >> (8 * i));
@@ -616,6 +669,19 @@ int run_fri_commit(z0p_gpu_ctx* c, const FriShape& s, const FriParams& fp, const
     outs[k].caps.assign(s.len.size(), {});
   }
   const size_t L = s.len.size();
+  std::vector<bool> armed(L, false);  // cap regions armed before their writers were queued
+  armed[0] = cap0_armed;
+  auto arm = [&](size_t l) {
+    arm_cap(c, h.fri_cap[l], (size_t)h.fri_cap_bytes[l] * K);
+    armed[l] = true;
+  };
+  // Waits for layer l's cap (and, for the last layer, the values in the
+  // clear) in the mapped buffer.
+  auto wait_layer = [&](size_t l, cudaEvent_t upto) -> cudaError_t {
+    if (l + 1 == L) return sync(c, "cap+final", upto);
+    if (armed[l]) return wait_cap(c, "cap", h.fri_cap[l], (size_t)h.fri_cap_bytes[l] * K, upto);
+    return sync(c, "cap", upto);
+  };
   const uint32_t unit_m = to_mont(two_adic_generator(2));
   const uint64_t fl = s.len.back();
   auto tabs = [&](size_t l) {  // layer l's fold tables, proof 0's
@@ -695,6 +761,7 @@ int run_fri_commit(z0p_gpu_ctx* c, const FriShape& s, const FriParams& fp, const
       for (size_t g = l; g < rel.end; g++)
         __atomic_store_n(const_cast<unsigned int*>(rel.gates + g), epoch - 1u, __ATOMIC_RELAXED);
       __atomic_thread_fence(__ATOMIC_SEQ_CST);
+      for (size_t j = l + 1; j + 1 < L; j++) arm(j);  // written by the folds queued below
       CK(cudaEventRecord(c->gate_ev[l], c->stream));  // layer l's cap
       for (size_t j = l; j + 1 < L; j++) {
         FoldArgs fa = fold_args(j);
@@ -721,7 +788,7 @@ int run_fri_commit(z0p_gpu_ctx* c, const FriShape& s, const FriParams& fp, const
       c->d2h += (uint64_t)K * h.final_bytes;  // written by the last fold
       for (size_t j = l;; j++) {
         const bool last = j + 1 == L;
-        CK(sync(c, last ? "cap+final" : "cap", c->gate_ev[j]));
+        CK(wait_layer(j, c->gate_ev[j]));
         absorb_cap(j);
         if (last) break;
         fold_tables(j, false);
@@ -734,9 +801,10 @@ int run_fri_commit(z0p_gpu_ctx* c, const FriShape& s, const FriParams& fp, const
     // last layer's values (sent in the clear) come back in the same trip,
     // written there by the last fold (or copied, when there is no fold).
     if (last && l > 0) c->d2h += (uint64_t)K * h.final_bytes;
-    CK(sync(c, last ? "cap+final" : "cap"));
+    CK(wait_layer(l, nullptr));
     absorb_cap(l);
     if (last) break;
+    if (l + 2 < L) arm(l + 1);  // written by this fold or the tree launches after it
     FoldArgs fa = fold_args(l);
     const bool slot = launch::fri_fold_uses_slot(fa);
     fold_tables(l, slot);
@@ -837,12 +905,12 @@ int run_openings(z0p_gpu_ctx* c, const FriShape& s, const FriBufs& fb, const Hio
 int run_fri_openings(z0p_gpu_ctx* c, const FriShape& s, const FriParams& fp, const FriBufs& fb,
                      uint64_t poly_len, uint64_t degree_bound, Transcript* const* ts, uint32_t K,
                      const HioPlan& h, FriOut* outs, OpenArgs& oa,
-                     std::function<cudaError_t()> after = {}) {
+                     std::function<cudaError_t()> after = {}, bool cap0_armed = false) {
   prepare_openings(c, s, fb, h, oa);
   FriTail tail;
   tail.oa = &oa;
   tail.after = after;
-  RC(run_fri_commit(c, s, fp, fb, poly_len, degree_bound, ts, K, h, outs, &tail));
+  RC(run_fri_commit(c, s, fp, fb, poly_len, degree_bound, ts, K, h, outs, &tail, cap0_armed));
   if (!tail.queued) {
     RC(run_fri_open(c, s, fp, ts, K, h, outs));
     write_indices(c, h, outs, K);
@@ -1870,13 +1938,14 @@ int air_prove(z0p_gpu_ctx* c, const AirTask* tasks, uint32_t K) {
   uint32_t* tinv = (uint32_t*)c->scratch.p;  // the NTT's scratch is free from here on
   uint32_t built = 0;  // subtree levels the leaf kernel hashed itself
   const uint64_t tcap_stride = h.trace_cap_bytes / 4;
+  arm_cap(c, h.trace_cap, (size_t)h.trace_cap_bytes * K);
   CK(launch::air_trace_leaves(st, c->tb, lde_a, cb, w_last_m, ttree, tinv, logN, logB, tsteps,
                               hio_dev<uint32_t>(c, h.trace_cap), merkle_counter(c), &built, K,
                               ttree_words, tcap_stride));
   if (built < tsteps || (tsteps == 0 && tleaves > kFuseMaxLeaves))
     CK(launch::merkle_build(st, ttree, tleaves, tsteps, merkle_counter(c),
                             hio_dev<uint32_t>(c, h.trace_cap), built, K, ttree_words, tcap_stride));
-  CK(sync(c, "cap"));
+  CK(wait_cap(c, "cap", h.trace_cap, (size_t)h.trace_cap_bytes * K));
   std::vector<std::vector<uint8_t>> column_cap(K);
   const uint32_t omega_inv = finv(omega_n);
   for (uint32_t k = 0; k < K; k++) {
@@ -1916,6 +1985,7 @@ int air_prove(z0p_gpu_ctx* c, const AirTask* tasks, uint32_t K) {
   ca.cap = hio_dev<uint32_t>(c, h.fri_cap[0]);
   ca.cap_stride = h.fri_cap_bytes[0] / 4;
   uint32_t built0 = 0;
+  arm_cap(c, h.fri_cap[0], (size_t)h.fri_cap_bytes[0] * K);
   CK(launch::air_compose_leaves(st, c->tb, ca, K, &built0));
   if (built0 == 0)
     CK(launch::merkle_build(st, fb.tree[0], s.leaves[0], s.depth[0] - s.drop[0], merkle_counter(c),
@@ -1937,7 +2007,7 @@ int air_prove(z0p_gpu_ctx* c, const AirTask* tasks, uint32_t K) {
   oa.logN = logN; oa.logB = logB; oa.ncol = 0;
   oa.lde_stride = m;
   oa.ttree_stride = ttree_words;
-  RC(run_fri_openings(c, s, fp, fb, m, N - 1, ts.data(), K, h, fo.data(), oa));
+  RC(run_fri_openings(c, s, fp, fb, m, N - 1, ts.data(), K, h, fo.data(), oa, {}, true));
 
   for (uint32_t k = 0; k < K; k++) {
     Writer w(tasks[k].out, need);  // air::Proof::to_bytes (src/air.rs:262-281)
