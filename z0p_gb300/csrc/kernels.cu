@@ -607,6 +607,54 @@ __global__ void __launch_bounds__(kTraceLeafThreads) air_trace_leaves_kernel(
               counter);
 }
 
+// The same leaves for trees that are not finished in the launch (more than
+// kFuseMaxLeaves leaves): thread t makes leaves 2t and 2t + 1, rows 16t ..
+// 16t + 15, with one batch inversion of their sixteen (x - w_last) (one
+// field inversion per sixteen rows instead of eight). With 16 cosets, the
+// warp's loads of one row index r read 32 consecutive q of coset r.
+__global__ void __launch_bounds__(kTraceLeafThreads) air_trace_leaves2_kernel(
+    const uint32_t* __restrict__ lde_a, const uint32_t* __restrict__ cb, uint32_t w_last_m,
+    uint32_t* __restrict__ leaves, uint32_t* __restrict__ tinv, uint32_t logN, uint32_t logB,
+    uint32_t nleaves, uint64_t tree_stride, const uint32_t* __restrict__ lde_b, Tables tb) {
+  pdl_wait();
+  {
+    const uint32_t pk = blockIdx.y;  // proof of the group
+    const size_t m = (size_t)nleaves * 8;
+    lde_a += pk * m;
+    cb += (size_t)pk << logB;
+    tinv += pk * m;
+    leaves += pk * tree_stride;
+  }
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (2 * t >= nleaves) return;
+  const uint32_t logm = logN + logB;
+  // Rows 16t .. 16t+15 are consecutive powers of omega_m: x_{k+1} = x_k omega_m.
+  const uint32_t step = root_pow(tb, 1u << (kRootBits - logm));
+  uint32_t x = mmul(to_mont(31u), root_pow(tb, (16u * t) << (kRootBits - logm)));
+  uint32_t den[16];
+#pragma unroll
+  for (int r = 0; r < 16; r++) {
+    den[r] = fsub(x, w_last_m);
+    x = mmul(x, step);
+  }
+  batch_minv(den);
+#pragma unroll
+  for (int h = 0; h < 2; h++) {
+    uint32_t msg[16], d[8];
+#pragma unroll
+    for (int r = 0; r < 8; r++) {
+      const uint32_t k = 16u * t + 8u * h + r;
+      const uint32_t j = k & ((1u << logB) - 1u), q = k >> logB;
+      msg[2 * r] = __ldg(lde_a + ((size_t)j << logN) + q);
+      msg[2 * r + 1] = lde_b ? __ldg(lde_b + ((size_t)j << logN) + q)
+                             : linked_b(lde_a, logN, j, q, __ldg(cb + j), den[8 * h + r]);
+      tinv[((size_t)j << logN) + q] = den[8 * h + r];
+    }
+    blake3_leaf64(msg, d);
+    store_digest(leaves + 8 * (2 * (size_t)t + h), d);
+  }
+}
+
 // Range tree leaf k = BLAKE3(0x00 || row k) with the row = ncols LE words
 // (src/range.rs:452-460, src/hash.rs:351-381). Threads walk rows in
 // coset-major order so column reads coalesce; digests land at index k.
@@ -1902,7 +1950,7 @@ __global__ void __launch_bounds__(256) hash_ceiling_kernel(const uint32_t* __res
 __global__ void __launch_bounds__(128) openings_kernel(const __grid_constant__ OpenArgs a) {
   pdl_wait();
   const uint32_t qi = blockIdx.x, pk = blockIdx.y;  // query, proof of the group
-  if (a.go) wait_gate(a.go, a.go_epoch, a.fault);
+  if (a.go) wait_gate(a.go_per_query ? a.go + qi : a.go, a.go_epoch, a.fault);
   uint32_t* out = a.out + ((size_t)pk * a.nq + qi) * a.stride;
   // Indices are positions in layer 0 (a power of two); masking leaves valid
   // ones unchanged and keeps every read inside the layers and trees, whatever
@@ -2385,9 +2433,14 @@ cudaError_t air_trace_leaves(cudaStream_t st, const Tables& tb, const uint32_t* 
                     : subtree_levels(nleaves < kTraceLeafThreads ? nleaves : kTraceLeafThreads, top);
   Stage stg("trace_leaves", st);
   stg.launched();
-  launch_dep(air_trace_leaves_kernel, dim3(grid_for(nleaves, kTraceLeafThreads), nproofs), kTraceLeafThreads,
-                            0, st, lde_a, cb, w_last_m, leaves, tinv, logN, logB, nleaves, top, cap,
-                                     counter, tree_stride, cap_stride, lde_b, tb);
+  if (nleaves > kFuseMaxLeaves)  // two leaves a thread, no subtree
+    launch_dep(air_trace_leaves2_kernel, dim3(grid_for(nleaves / 2, kTraceLeafThreads), nproofs),
+               kTraceLeafThreads, 0, st, lde_a, cb, w_last_m, leaves, tinv, logN, logB, nleaves,
+               tree_stride, lde_b, tb);
+  else
+    launch_dep(air_trace_leaves_kernel, dim3(grid_for(nleaves, kTraceLeafThreads), nproofs),
+               kTraceLeafThreads, 0, st, lde_a, cb, w_last_m, leaves, tinv, logN, logB, nleaves, top,
+               cap, counter, tree_stride, cap_stride, lde_b, tb);
   return cudaGetLastError();
 }
 

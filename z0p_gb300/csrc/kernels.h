@@ -190,8 +190,11 @@ struct OpenArgs {
   uint64_t fri_val_stride = 0, fri_tree_stride = 0, lde_stride = 0, ttree_stride = 0;
   // Optional gate (as FoldArgs::go): the launch waits for *go == go_epoch
   // before it reads the indices; a wait that runs out sets bit 3 of *fault.
+  // With go_per_query, query qi's CTAs wait on go[qi] instead, so that each
+  // gathers as soon as its own index is written.
   const unsigned int* go = nullptr;
   unsigned int go_epoch = 0;
+  unsigned int go_per_query = 0;
   unsigned int* fault = nullptr;
 };
 

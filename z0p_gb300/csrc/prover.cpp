@@ -517,7 +517,7 @@ struct HioPlan {
   size_t final_vals = 0, final_bytes = 0, grind = 0, indices = 0, open = 0;
   // Read by kernels in place: the small folds' challenge tables, per layer
   // ([layer][proof][kFoldTabWords]), the gate words (one per fold, then the
-  // PoW search's and the gather's) and the PoW heads.
+  // PoW search's, then one per query for the gather) and the PoW heads.
   size_t tabs = 0, gates = 0, heads = 0;
   size_t extra = 0, extra_bytes = 0;
   uint32_t stride = 0, trace_off = 0;  // one opening block, in words
@@ -546,7 +546,7 @@ int plan_hio(z0p_gpu_ctx* c, const FriShape& s, uint64_t queries, uint32_t tdrop
   h->final_vals = take(h->final_bytes);
   h->grind = take(16);
   h->tabs = take(4 * kFoldTabWords * s.len.size());
-  h->gates = take(4 * (s.len.size() + 1));
+  h->gates = take(4 * (s.len.size() + (queries ? queries : 1)));
   h->heads = take(4 * kPowHeadWords);
   h->indices = take(8 * queries);
   size_t L = s.len.size() - 1;
@@ -636,8 +636,9 @@ struct GateRelease {
 
 // What follows a FRI commitment in a prover: the PoW search and the openings
 // gather (prepared, kernels.h OpenArgs), then `after`. When the commitment's
-// tail is gated, run_fri_commit queues them behind two more gates: the PoW
-// search's (word L - 1, L the layer count) and the gather's (word L).
+// tail is gated, run_fri_commit queues them behind more gates: the PoW
+// search's (word L - 1, L the layer count) and one per query for the gather
+// (words L .. L + Q - 1), opened as the host draws each query's index.
 struct FriTail {
   OpenArgs* oa = nullptr;
   std::function<cudaError_t()> after;
@@ -754,7 +755,7 @@ int run_fri_commit(z0p_gpu_ctx* c, const FriShape& s, const FriParams& fp, const
       rel.gates = reinterpret_cast<volatile unsigned int*>(c->hio + h.gates);
       rel.epoch = epoch;
       rel.next = l;
-      rel.end = tail ? L + 1 : L - 1;
+      rel.end = tail ? L + (h.queries ? h.queries : 1) : L - 1;
       // Close every gate of this tail before anything is queued behind it: the
       // mapped buffer is shared by all calls and shapes, so a word left there
       // could otherwise already hold this epoch.
@@ -779,6 +780,7 @@ int run_fri_commit(z0p_gpu_ctx* c, const FriShape& s, const FriParams& fp, const
                            gates_dev + (L - 1), epoch, c->tb.fault));
         CK(cudaEventRecord(c->gate_ev[L], c->stream));  // the PoW results
         tail->oa->go = gates_dev + L;
+        tail->oa->go_per_query = 1;
         tail->oa->go_epoch = epoch;
         tail->oa->fault = c->tb.fault;
         CK(launch::openings(c->stream, *tail->oa, K));
@@ -937,13 +939,21 @@ int run_fri_openings(z0p_gpu_ctx* c, const FriShape& s, const FriParams& fp, con
   } else {
     tail.gates.open_next();  // nothing behind it
   }
-  for (uint32_t k = 0; k < K; k++) {
-    outs[k].indices.resize(fp.num_queries);
-    for (uint64_t i = 0; i < fp.num_queries; i++)
-      outs[k].indices[i] = challenge_index(*ts[k], "fri-query", s.m);
+  // Query i's gather starts once index i of every proof is in the mapped
+  // buffer, while the host draws the next ones.
+  for (uint32_t k = 0; k < K; k++) outs[k].indices.resize(fp.num_queries);
+  const uint64_t Q = h.queries;
+  for (uint64_t i = 0; i < fp.num_queries; i++) {
+    for (uint32_t k = 0; k < K; k++) {
+      const uint64_t v = challenge_index(*ts[k], "fri-query", s.m);
+      outs[k].indices[i] = v;
+      std::memcpy(c->hio + h.indices + 8 * (Q * k + i), &v, 8);
+    }
+    tail.gates.open_next();  // query i's gate
   }
-  write_indices(c, h, outs, K);
-  tail.gates.open_next();  // the gather's gate
+  while (tail.gates.next < tail.gates.end) tail.gates.open_next();  // (none left: Q queries)
+  c->h2d += 8 * Q * K;                // indices read in place
+  c->d2h += 4ull * h.stride * Q * K;  // opening blocks
   CK(sync(c, "openings"));
   return Z0P_OK;
 }
