@@ -751,7 +751,12 @@ __global__ void __launch_bounds__(kSegmentMaxRows) fold_segment_kernel(
     if (j) fac[h] = mmul(fac[h], root_pow(tb, (j * i) << (kRootBits - logm)));
   }
   if (t < 2 * S) {
-    if (v_in >= kP) atomicOr(bad, 1u);
+    if (v_in >= kP) {
+      // Visible to the host before any word of the cap (written after the
+      // barrier below), which the host may read before the launch retires.
+      atomicOr_system(bad, 1u);
+      __threadfence_system();
+    }
     coef[(t >> L) * cs + spos(t & (S - 1u))] = v_in;
   }
   __syncthreads();

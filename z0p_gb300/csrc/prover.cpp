@@ -2449,6 +2449,7 @@ int fri_commit(z0p_gpu_ctx* c, const FriInput& in, const uint32_t* values,
   const uint32_t top0 = s.depth[0] - s.drop[0];
   uint32_t* cap0 = hio_dev<uint32_t>(c, f.h.fri_cap[0]);
   uint32_t built0 = 0;
+  arm_cap(c, f.h.fri_cap[0], f.h.fri_cap_bytes[0]);  // the bad flag is read after the last wait
   const bool from_lde = !in.evals;  // coefficients were extended (coset-major LDE)
   CK(launch::layer0_leaves(st, from_lde ? (const uint32_t*)c->lde.p : src, f.fb.layer[0],
                            f.fb.tree[0], bad, logm, from_lde ? logB : 0, ncomp, from_lde,
@@ -2459,7 +2460,7 @@ int fri_commit(z0p_gpu_ctx* c, const FriInput& in, const uint32_t* values,
   z0p_transcript_state work = *t;
   Transcript tr(&work);
   Transcript* ts[1] = {&tr};
-  RC(run_fri_commit(c, s, in.fp, f.fb, in.poly_len, in.bound, ts, 1, f.h, &f.out));
+  RC(run_fri_commit(c, s, in.fp, f.fb, in.poly_len, in.bound, ts, 1, f.h, &f.out, nullptr, true));
   if (*reinterpret_cast<volatile unsigned int*>(bad_h)) {  // read after the stream drained
     set_reason("field elements must be canonical (< p)");
     return Z0P_ERR_MALFORMED_INPUT;
@@ -2631,8 +2632,12 @@ int fold_add(z0p_gpu_fold* f, const uint32_t* col_a, const uint32_t* col_b,
   c->h2d += 8 * S;
   uint32_t* lde = step.lde;
   uint32_t* tree = step.tree;
-  if (mapped_cols && launch::fold_segment_ok(logN, logB)) {
-    // Small segments: interpolation, LDE, row leaves and tree in one launch.
+  const bool one_launch = mapped_cols && launch::fold_segment_ok(logN, logB);
+  if (one_launch) {
+    // Small segments: interpolation, LDE, row leaves and tree in one launch,
+    // which publishes a bad column word before any word of the cap: the cap
+    // is read as soon as it lands (arm_cap, wait_cap).
+    arm_cap(c, 64, cap_bytes);
     CK(launch::fold_segment(st, c->tb, cols, hio_dev<unsigned int>(c, 0), lde, tree,
                             hio_dev<uint32_t>(c, 64), logN, logB, depth - drop));
   } else {
@@ -2651,7 +2656,7 @@ int fold_add(z0p_gpu_fold* f, const uint32_t* col_a, const uint32_t* col_b,
     if (built == 0)
       CK(launch::merkle_build(st, tree, m, depth - drop, merkle_counter(c), hio_dev<uint32_t>(c, 64)));
   }
-  CK(sync(c, "cap"));
+  CK(one_launch ? wait_cap(c, "cap", 64, cap_bytes) : sync(c, "cap"));
   if (*reinterpret_cast<volatile unsigned int*>(bad_h)) {
     set_reason("field elements must be canonical (< p)");
     return Z0P_ERR_MALFORMED_INPUT;
@@ -2771,6 +2776,7 @@ int fold_finalize(z0p_gpu_fold* f, z0p_transcript_state* ts, uint8_t* out) {
     ca.cap = hio_dev<uint32_t>(c, h.fri_cap[0]);
   }
   uint32_t built0 = 0;
+  arm_cap(c, h.fri_cap[0], h.fri_cap_bytes[0]);
   CK(launch::fold_combine(st, c->tb, ca, &built0));
   if (built0 == 0)
     CK(launch::merkle_build(st, fb.tree[0], s.leaves[0], s.depth[0] - s.drop[0], merkle_counter(c),
@@ -2787,7 +2793,7 @@ int fold_finalize(z0p_gpu_fold* f, z0p_transcript_state* ts, uint8_t* out) {
     return launch::fold_openings(st, ca.steps, K, hio_dev<uint64_t>(c, h.indices),
                                  (uint32_t)fp.num_queries, logN, logB, psteps,
                                  hio_dev<uint32_t>(c, h.extra), stride);
-  }));
+  }, true));
   // IvcProof::to_bytes (src/fold.rs:281-309).
   Writer w(out, fold_proof_bytes(p, K, s));
   w.byte(6);
