@@ -1825,8 +1825,11 @@ __device__ __forceinline__ void grind_finish(const GrindArgs& a) {
   __threadfence();
   if (atomicAdd(a.state + 3, 1ull) != gridDim.x - 1) return;
   __threadfence();
-  a.out[0] = atomicAdd(a.state + 0, 0ull);
+  // The cap flag first: the host may read the nonce word as soon as it
+  // lands, and the flag with it.
   a.out[1] = atomicAdd(a.state + 2, 0ull);
+  __threadfence_system();
+  a.out[0] = atomicAdd(a.state + 0, 0ull);
   a.state[0] = ~0ull;
   a.state[1] = 0ull;
   a.state[2] = 0ull;

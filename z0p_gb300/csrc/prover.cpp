@@ -219,6 +219,46 @@ cudaError_t sync(z0p_gpu_ctx* c, const char* site = "other", cudaEvent_t upto = 
 // word), ends the wait at the work's completion instead.
 constexpr uint32_t kCapSentinel = 0x6A09E667u;
 
+// The same for the PoW results (nonce word, then the cap flag, per proof):
+// a nonce word is below 2^40 or all ones, never kPowSentinel.
+constexpr uint64_t kPowSentinel = ~1ull;
+
+void arm_pow(z0p_gpu_ctx* c, size_t off, uint32_t K) {
+  for (uint32_t k = 0; k < K; k++) std::memcpy(c->hio + off + 16 * k, &kPowSentinel, 8);
+  __atomic_thread_fence(__ATOMIC_SEQ_CST);
+}
+
+cudaError_t wait_pow(z0p_gpu_ctx* c, size_t off, uint32_t K, cudaEvent_t upto) {
+  c->syncs++;
+  const uint64_t t0 = now_ns();
+  cudaError_t e = cudaSuccess;
+  uint32_t k = 0;
+  for (uint32_t pass = 0;; pass++) {
+    while (k < K && *reinterpret_cast<const volatile uint64_t*>(c->hio + off + 16 * k) != kPowSentinel) k++;
+    if (k == K) break;
+    if ((pass & 63u) == 63u) {
+      e = cudaEventQuery(upto);
+      if (e != cudaErrorNotReady) break;
+      e = cudaSuccess;
+    }
+  }
+  __atomic_thread_fence(__ATOMIC_ACQUIRE);
+  const uint64_t t1 = now_ns();
+  if (e == cudaSuccess && c->fault && *reinterpret_cast<volatile unsigned int*>(c->fault)) {
+    *c->fault = 0u;
+    e = cudaErrorLaunchTimeout;
+  }
+  c->sync_ns += t1 - t0;
+  if (c->profiling) {
+    HostSite& hs = c->sites["grind"];
+    hs.calls++;
+    hs.wait_ns += t1 - t0;
+    if (c->last_sync_ns) hs.before_ns += t0 - c->last_sync_ns;
+  }
+  c->last_sync_ns = t1;
+  return e;
+}
+
 void arm_cap(z0p_gpu_ctx* c, size_t off, size_t bytes) {
   uint32_t* w = reinterpret_cast<uint32_t*>(c->hio + off);
   for (size_t i = 0; i < bytes / 4; i++) w[i] = kCapSentinel;
@@ -773,6 +813,7 @@ int run_fri_commit(z0p_gpu_ctx* c, const FriShape& s, const FriParams& fp, const
         CK(cudaEventRecord(c->gate_ev[j + 1], c->stream));  // layer j+1's cap
       }
       if (tail) {
+        if (fp.grinding_bits > 0) arm_pow(c, h.grind, K);
         if (fp.grinding_bits > 0)
           CK(launch::grind(c->stream, hio_dev<uint32_t>(c, h.heads), kPowHeadBytes,
                            fp.grinding_bits, grind_state(c),
@@ -929,7 +970,7 @@ int run_fri_openings(z0p_gpu_ctx* c, const FriShape& s, const FriParams& fp, con
     }
     c->h2d += 4ull * kPowHeadWords * K;
     tail.gates.open_next();  // the PoW search's gate
-    CK(sync(c, "grind", c->gate_ev[s.len.size()]));
+    CK(wait_pow(c, h.grind, K, c->gate_ev[s.len.size()]));
     for (uint32_t k = 0; k < K; k++) {
       RC(check_grind(c, h.grind, k, &outs[k].nonce));
       uint8_t nb[8];
