@@ -1955,10 +1955,29 @@ __global__ void __launch_bounds__(256) hash_ceiling_kernel(const uint32_t* __res
 // for the trace). One CTA per query; the block layout is OpenArgs'.
 // The argument block stays in parameter space (__grid_constant__): the
 // layer table is indexed at run time without a per-thread local copy.
+__device__ __forceinline__ void gather_query(const OpenArgs& a);
+
 __global__ void __launch_bounds__(128) openings_kernel(const __grid_constant__ OpenArgs a) {
   pdl_wait();
   const uint32_t qi = blockIdx.x, pk = blockIdx.y;  // query, proof of the group
   if (a.go) wait_gate(a.go_per_query ? a.go + qi : a.go, a.go_epoch, a.fault);
+  gather_query(a);
+  // The block is written: its done word, for a host that reads blocks as
+  // they land.
+  if (a.done) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      __threadfence_system();
+      asm volatile("st.release.sys.global.u32 [%0], %1;" ::"l"(a.done + (size_t)pk * a.nq + qi),
+                   "r"(a.go_epoch)
+                   : "memory");
+    }
+  }
+}
+
+// Query blockIdx.x of proof blockIdx.y: its opening block.
+__device__ __forceinline__ void gather_query(const OpenArgs& a) {
+  const uint32_t qi = blockIdx.x, pk = blockIdx.y;
   uint32_t* out = a.out + ((size_t)pk * a.nq + qi) * a.stride;
   // Indices are positions in layer 0 (a power of two); masking leaves valid
   // ones unchanged and keeps every read inside the layers and trees, whatever

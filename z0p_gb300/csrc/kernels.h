@@ -196,6 +196,9 @@ struct OpenArgs {
   unsigned int go_epoch = 0;
   unsigned int go_per_query = 0;
   unsigned int* fault = nullptr;
+  // Optional: word pk * nq + qi is set to go_epoch (store-release, system
+  // scope) once the block of query qi of proof pk is written.
+  unsigned int* done = nullptr;
 };
 
 // Product table of the Fp4 constant r (canonical coordinates) in the layout

@@ -173,6 +173,11 @@ struct z0p_gpu_ctx {
   std::vector<cudaEvent_t> gate_ev;
   uint32_t go_epoch = 0;
   bool gates = true;  // z0p_gpu_ctx_set_gates
+  // Openings read as they land (run_fri_openings with `defer`): while
+  // open_epoch is non-zero, open_block waits for the query's done word in
+  // the mapped buffer (at open_done) to hold it.
+  uint32_t open_epoch = 0;
+  size_t open_done = 0;
 };
 using HostSite = z0p_gpu_ctx::HostSite;
 
@@ -559,6 +564,7 @@ struct HioPlan {
   // ([layer][proof][kFoldTabWords]), the gate words (one per fold, then the
   // PoW search's, then one per query for the gather) and the PoW heads.
   size_t tabs = 0, gates = 0, heads = 0;
+  size_t done = 0;  // the gather's done word per (proof, query)
   size_t extra = 0, extra_bytes = 0;
   uint32_t stride = 0, trace_off = 0;  // one opening block, in words
   std::vector<uint32_t> layer_off;     // per non-final FRI layer, in words
@@ -589,6 +595,7 @@ int plan_hio(z0p_gpu_ctx* c, const FriShape& s, uint64_t queries, uint32_t tdrop
   h->gates = take(4 * (s.len.size() + (queries ? queries : 1)));
   h->heads = take(4 * kPowHeadWords);
   h->indices = take(8 * queries);
+  h->done = take(4 * (queries ? queries : 1));
   size_t L = s.len.size() - 1;
   if (L > kMaxOpenLayers) {
     set_reason("more FRI layers than the openings kernel supports");
@@ -801,6 +808,11 @@ int run_fri_commit(z0p_gpu_ctx* c, const FriShape& s, const FriParams& fp, const
       // could otherwise already hold this epoch.
       for (size_t g = l; g < rel.end; g++)
         __atomic_store_n(const_cast<unsigned int*>(rel.gates + g), epoch - 1u, __ATOMIC_RELAXED);
+      if (tail) {  // the gather's done words too (open_block reads a block once its word is `epoch`)
+        unsigned int* done = reinterpret_cast<unsigned int*>(c->hio + h.done);
+        for (size_t i = 0; i < (size_t)K * h.queries; i++)
+          __atomic_store_n(done + i, epoch - 1u, __ATOMIC_RELAXED);
+      }
       __atomic_thread_fence(__ATOMIC_SEQ_CST);
       for (size_t j = l + 1; j + 1 < L; j++) arm(j);  // written by the folds queued below
       CK(cudaEventRecord(c->gate_ev[l], c->stream));  // layer l's cap
@@ -823,6 +835,7 @@ int run_fri_commit(z0p_gpu_ctx* c, const FriShape& s, const FriParams& fp, const
         tail->oa->go = gates_dev + L;
         tail->oa->go_per_query = 1;
         tail->oa->go_epoch = epoch;
+        tail->oa->done = hio_dev<unsigned int>(c, h.done);
         tail->oa->fault = c->tb.fault;
         CK(launch::openings(c->stream, *tail->oa, K));
         if (tail->after) CK(tail->after());
@@ -945,10 +958,15 @@ int run_openings(z0p_gpu_ctx* c, const FriShape& s, const FriBufs& fb, const Hio
 // the PoW search and the gather are queued with the folds; the host then
 // fills their inputs and opens their gates in turn. Ends with the openings
 // in the mapped buffer.
+// With `defer` (no `after` kernels), a gated gather is not waited for here:
+// the caller reads the blocks through open_block as they land and then calls
+// finish_openings; otherwise the openings are complete on return.
 int run_fri_openings(z0p_gpu_ctx* c, const FriShape& s, const FriParams& fp, const FriBufs& fb,
                      uint64_t poly_len, uint64_t degree_bound, Transcript* const* ts, uint32_t K,
                      const HioPlan& h, FriOut* outs, OpenArgs& oa,
-                     std::function<cudaError_t()> after = {}, bool cap0_armed = false) {
+                     std::function<cudaError_t()> after = {}, bool cap0_armed = false,
+                     bool defer = false) {
+  c->open_epoch = 0;
   prepare_openings(c, s, fb, h, oa);
   FriTail tail;
   tail.oa = &oa;
@@ -995,6 +1013,11 @@ int run_fri_openings(z0p_gpu_ctx* c, const FriShape& s, const FriParams& fp, con
   while (tail.gates.next < tail.gates.end) tail.gates.open_next();  // (none left: Q queries)
   c->h2d += 8 * Q * K;                // indices read in place
   c->d2h += 4ull * h.stride * Q * K;  // opening blocks
+  if (defer && !after) {
+    c->open_done = h.done;
+    c->open_epoch = tail.gates.epoch;
+    return Z0P_OK;
+  }
   CK(sync(c, "openings"));
   return Z0P_OK;
 }
@@ -1013,9 +1036,26 @@ void write_path(Writer& w, const uint8_t* digests, uint64_t leaf, uint32_t steps
 }
 
 // Opening block of query qi of proof k.
+// With openings read as they land, first waits for the block's done word
+// (querying the stream every 64 passes: a stream that has drained, or
+// failed, ends the wait; the failure is reported by finish_openings).
 const uint32_t* open_block(z0p_gpu_ctx* c, const HioPlan& h, uint32_t k, size_t qi) {
+  if (c->open_epoch) {
+    const volatile uint32_t* w =
+        reinterpret_cast<const volatile uint32_t*>(c->hio + c->open_done) + (size_t)k * h.queries + qi;
+    for (uint32_t pass = 0; *w != c->open_epoch; pass++)
+      if ((pass & 63u) == 63u && cudaStreamQuery(c->stream) != cudaErrorNotReady) break;
+    __atomic_thread_fence(__ATOMIC_ACQUIRE);
+  }
   return reinterpret_cast<const uint32_t*>(c->hio + h.open) +
          (size_t)h.stride * ((size_t)k * h.queries + qi);
+}
+
+// Ends openings read as they land: the stream's synchronisation, after the
+// proof bytes are written.
+cudaError_t finish_openings(z0p_gpu_ctx* c) {
+  c->open_epoch = 0;
+  return sync(c, "openings");
 }
 
 // Commitment::write_body (src/fri.rs:896-904).
@@ -2058,7 +2098,12 @@ int air_prove(z0p_gpu_ctx* c, const AirTask* tasks, uint32_t K) {
   oa.logN = logN; oa.logB = logB; oa.ncol = 0;
   oa.lde_stride = m;
   oa.ttree_stride = ttree_words;
-  RC(run_fri_openings(c, s, fp, fb, m, N - 1, ts.data(), K, h, fo.data(), oa, {}, true));
+  RC(run_fri_openings(c, s, fp, fb, m, N - 1, ts.data(), K, h, fo.data(), oa, {}, true, true));
+  // The proof bytes are written as the opening blocks land.
+  struct OpenGuard {
+    z0p_gpu_ctx* c;
+    ~OpenGuard() { c->open_epoch = 0; }
+  } open_guard{c};
 
   for (uint32_t k = 0; k < K; k++) {
     Writer w(tasks[k].out, need);  // air::Proof::to_bytes (src/air.rs:262-281)
@@ -2087,6 +2132,7 @@ int air_prove(z0p_gpu_ctx* c, const AirTask* tasks, uint32_t K) {
       return Z0P_ERR_CUDA;
     }
   }
+  CK(finish_openings(c));
   return Z0P_OK;
 }
 
