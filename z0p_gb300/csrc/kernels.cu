@@ -1674,6 +1674,9 @@ __device__ __forceinline__ void stage_fold_tab(const FoldArgs& a, const Tables& 
 
 // Large layers (and folds that stop at their CTAs' subtrees): the tables are
 // constant-bank operands of the products.
+// kWide: the input (and its per-proof stride) is 32-byte aligned, and each
+// thread reads its 256 bytes as eight 32-byte loads.
+template <bool kWide>
 __global__ void __launch_bounds__(kFoldThreads) fri_fold_leaf_kernel(FoldArgs a, Tables tb) {
   pdl_wait();
   __shared__ uint32_t sm[2 * kTopStride * kFoldThreads];  // the CTA's subtree levels
@@ -1685,17 +1688,30 @@ __global__ void __launch_bounds__(kFoldThreads) fri_fold_leaf_kernel(FoldArgs a,
   uint64_t Pn = first + threadIdx.x;
   uint32_t d[8];
   if (threadIdx.x < avail) {
-  // The thread's 256 input bytes are contiguous; each 16-byte load of a warp
-  // touches 32 lines that its next loads reuse from L1.
-  const uint4* src = reinterpret_cast<const uint4*>(a.in) + Pn * 16;
+  // The thread's 256 input bytes are contiguous. With kWide, eight 32-byte
+  // loads: every lane of a warp load takes a whole sector (a 16-byte load
+  // leaves half of each sector to the next load, which finds it evicted from
+  // L1 often enough to read it again from L2).
+  const uint32_t* src = a.in + Pn * 64;
   uint32_t leaf[16];
 #pragma unroll
   for (int t = 0; t < 4; t++) {
     E4 q[4];
 #pragma unroll
-    for (int i = 0; i < 4; i++) {
-      uint4 v = __ldcs(src + 4 * t + i);
-      q[i].c[0] = v.x; q[i].c[1] = v.y; q[i].c[2] = v.z; q[i].c[3] = v.w;
+    for (int i = 0; i < 4; i += 2) {
+      if constexpr (kWide) {
+        asm volatile(
+            "ld.global.nc.L1::no_allocate.v8.u32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+            : "=r"(q[i].c[0]), "=r"(q[i].c[1]), "=r"(q[i].c[2]), "=r"(q[i].c[3]),
+              "=r"(q[i + 1].c[0]), "=r"(q[i + 1].c[1]), "=r"(q[i + 1].c[2]), "=r"(q[i + 1].c[3])
+            : "l"(src + 16 * t + 4 * i));
+      } else {
+#pragma unroll
+        for (int u = 0; u < 2; u++) {
+          const uint4 v = __ldcs(reinterpret_cast<const uint4*>(src + 16 * t + 4 * (i + u)));
+          q[i + u].c[0] = v.x; q[i + u].c[1] = v.y; q[i + u].c[2] = v.z; q[i + u].c[3] = v.w;
+        }
+      }
     }
     uint32_t P = (uint32_t)(4 * Pn + t);
     E4 r = fold_quad(q[0], q[1], q[2], q[3], quad_xinv(tb, a, P), a, g_consts[a.slot].tab);
@@ -2625,8 +2641,11 @@ cudaError_t fri_fold(cudaStream_t st, const Tables& tb, const FoldArgs& a, uint3
     Stage stg("fri_fold_leaves", st);
     stg.launched();
     const dim3 grid(grid_for(nleaf, kFoldThreads), nproofs);
-    if (slot)
-      launch_dep(fri_fold_leaf_kernel, grid, kFoldThreads, 0, st, f, tb);
+    const bool wide = (reinterpret_cast<uintptr_t>(f.in) & 31u) == 0 && (f.in_stride & 7u) == 0;
+    if (slot && wide)
+      launch_dep(fri_fold_leaf_kernel<true>, grid, kFoldThreads, 0, st, f, tb);
+    else if (slot)
+      launch_dep(fri_fold_leaf_kernel<false>, grid, kFoldThreads, 0, st, f, tb);
     else
       launch_dep(fri_fold_quad_kernel, grid, kFold4Threads, 0, st, f, tb);
     return cudaGetLastError();
