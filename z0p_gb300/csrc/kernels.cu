@@ -2170,7 +2170,7 @@ Schedule g_sched[kMaxDevices];
 template <typename K>
 cudaError_t raise_smem(K* func, int pass, uint32_t L, size_t smem) {
   static std::mutex mu;
-  static size_t done[kMaxDevices][14][32] = {};
+  static size_t done[kMaxDevices][16][32] = {};
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
@@ -2283,8 +2283,13 @@ cudaError_t reg_pass1(cudaStream_t st, const CUtensorMap& map, uint32_t* yt, con
     }
   }
   constexpr size_t smem = reg_ntt::pass1_smem(L);
-  if (cudaError_t e = raise_smem(ntt_reg1_kernel<L, INV>, 6 + INV, L, smem)) return e;
-  launch_dep(ntt_reg1_kernel<L, INV>, g, threads, smem, st, map, yt, a);
+  if (!a.bad && !a.pre_gamma) {  // the LDE: no word check, no 31^i scaling
+    if (cudaError_t e = raise_smem(ntt_reg1_kernel<L, INV, true>, 14 + INV, L, smem)) return e;
+    launch_dep(ntt_reg1_kernel<L, INV, true>, g, threads, smem, st, map, yt, a);
+    return cudaGetLastError();
+  }
+  if (cudaError_t e = raise_smem(ntt_reg1_kernel<L, INV, false>, 6 + INV, L, smem)) return e;
+  launch_dep(ntt_reg1_kernel<L, INV, false>, g, threads, smem, st, map, yt, a);
   return cudaGetLastError();
 }
 template <int L, bool INV>

@@ -212,7 +212,9 @@ __host__ __device__ constexpr bool streamed_ok(uint32_t L) { return L <= 10; }
 // twisted by w^(j i) on load (twist[i1], filled when j != 0); writes
 // yt[k1][i2] times the four-step twiddle. Ends with `data` read (the
 // transpose's barriers are inside): a caller that reuses it adds a barrier.
-template <int L, bool INV>
+// PLAIN: a.bad is null and a.pre_gamma is 0 (the LDE), so the per-element
+// word check and scaling are compiled out.
+template <int L, bool INV, bool PLAIN = false>
 __device__ __forceinline__ void reg1_tile(uint32_t* data, const uint2* tw, const uint32_t* twist,
                                           uint32_t* __restrict__ yt, const NttArgs& a, uint32_t b,
                                           uint32_t c0, uint32_t j) {
@@ -224,14 +226,25 @@ __device__ __forceinline__ void reg1_tile(uint32_t* data, const uint2* tw, const
   const uint32_t n = 1u << a.logn;
   const uint32_t c = tid & (kC - 1), l = tid / kC;
   uint32_t x[R];
+  if constexpr (PLAIN) {
+    // Coset 0 of an LDE has no twist; the others twist every element.
+    if (j) {
 #pragma unroll
-  for (uint32_t r = 0; r < R; r++) {
-    const uint32_t i1 = l + R * r;
-    uint32_t v = data[i1 * kC + c];
-    if (a.bad && v >= kP) atomicOr(a.bad, 1u);
-    if (a.pre_gamma) v = mmul(v < kP ? v : 0u, gamma_pow(a.tb, (i1 << logn2) + c0 + c));
-    if (j) v = mmul(v, twist[i1]);
-    x[r] = v;
+      for (uint32_t r = 0; r < R; r++) x[r] = mmul(data[(l + R * r) * kC + c], twist[l + R * r]);
+    } else {
+#pragma unroll
+      for (uint32_t r = 0; r < R; r++) x[r] = data[(l + R * r) * kC + c];
+    }
+  } else {
+#pragma unroll
+    for (uint32_t r = 0; r < R; r++) {
+      const uint32_t i1 = l + R * r;
+      uint32_t v = data[i1 * kC + c];
+      if (a.bad && v >= kP) atomicOr(a.bad, 1u);
+      if (a.pre_gamma) v = mmul(v < kP ? v : 0u, gamma_pow(a.tb, (i1 << logn2) + c0 + c));
+      if (j) v = mmul(v, twist[i1]);
+      x[r] = v;
+    }
   }
   pass_a<H>(x, tw, l);
   __syncthreads();  // the tile has been read: its space takes the skewed columns
@@ -255,10 +268,13 @@ __device__ __forceinline__ void reg1_tile(uint32_t* data, const uint2* tw, const
 #pragma unroll
   for (int u = 0; u < 4; u++) w[u] = root_pow(a.tb, e_base + (uint32_t)u * e_q);
   const uint32_t q4 = root_pow(a.tb, 4u * e_q);
-  uint32_t* dst = yt + (size_t)b * n + i2;
+  // Row k1 = (e << H) | hb at dst + k1 n2: a base for hb, then e rows of
+  // 2^H n2 words apart.
+  uint32_t* dst = yt + (size_t)b * n + i2 + ((size_t)hb << logn2);
+  const size_t step = (size_t)1 << (H + logn2);
 #pragma unroll
   for (int e = 0; e < (int)R; e++) {
-    dst[(size_t)(((uint32_t)e << H) | hb) << logn2] = mmul(x[brev_c<H>(e)], w[e & 3]);
+    dst[(size_t)e * step] = mmul(x[brev_c<H>(e)], w[e & 3]);
     w[e & 3] = mmul(w[e & 3], q4);
   }
 }
@@ -289,7 +305,10 @@ __device__ __forceinline__ void reg2_tile(uint32_t* data, const uint2* tw, uint3
   for (uint32_t r = 0; r < R; r++) x[r] = row[(R + 1) * l + r];
   pass_b<H - 1, INV, (int)R>(x);
   const uint32_t hb = brev_bits(l, H);
-  uint32_t* dst = out + (size_t)b * n + r0 + rho;
+  // Output k = r0 + rho + n1 k2 for k2 = (e << H) | hb: a base for hb, then e
+  // steps of 2^H n1 words.
+  uint32_t* dst = out + (size_t)b * n + r0 + rho + ((size_t)hb << logn1);
+  const size_t step = (size_t)1 << (H + logn1);
   if (a.post_gamma) {
     // 31^k / n for k = r0 + rho + n1 k2, k2 = (e << H) | hb: four chains in e.
     const uint32_t k0 = r0 + rho + (hb << logn1);
@@ -299,12 +318,12 @@ __device__ __forceinline__ void reg2_tile(uint32_t* data, const uint2* tw, uint3
     const uint32_t g4 = gamma_pow(a.tb, 4u * R << logn1);
 #pragma unroll
     for (int e = 0; e < (int)R; e++) {
-      dst[(size_t)(((uint32_t)e << H) | hb) << logn1] = mmul(x[brev_c<H>(e)], g[e & 3]);
+      dst[(size_t)e * step] = mmul(x[brev_c<H>(e)], g[e & 3]);
       g[e & 3] = mmul(g[e & 3], g4);
     }
   } else {
 #pragma unroll
-    for (int e = 0; e < (int)R; e++) dst[(size_t)(((uint32_t)e << H) | hb) << logn1] = x[brev_c<H>(e)];
+    for (int e = 0; e < (int)R; e++) dst[(size_t)e * step] = x[brev_c<H>(e)];
   }
 }
 
@@ -340,7 +359,7 @@ __device__ __forceinline__ void fetch2(uint32_t* dst, const uint32_t* yt, uint32
 // Pass 1, one tile per CTA: columns c0 = blockIdx.x * 8 .. of the input
 // viewed as [n1][n2] (the tensor map's x = i2, y = i1, z = input block
 // b / in_div), block b = blockIdx.y.
-template <int L, bool INV>
+template <int L, bool INV, bool PLAIN>
 __global__ void __launch_bounds__(reg_ntt::kC << (L / 2), L == 10 ? 4 : 1)
     ntt_reg1_kernel(const __grid_constant__ CUtensorMap tmap, uint32_t* __restrict__ yt, NttArgs a) {
   pdl_wait();
@@ -359,7 +378,7 @@ __global__ void __launch_bounds__(reg_ntt::kC << (L / 2), L == 10 ? 4 : 1)
   load_pass_a_twiddles<L>(tw, a);
   if (j) fill_twist<L>(twist, a, j, a.logn - L);
   if (!cta_wait(bar, a.tb.fault)) return;  // (also orders the tables above)
-  reg1_tile<L, INV>(data, tw, twist, yt, a, b, c0, j);
+  reg1_tile<L, INV, PLAIN>(data, tw, twist, yt, a, b, c0, j);
 }
 
 // Pass 2, one tile per CTA: rows r0 = blockIdx.x * 8 .. of block b =
