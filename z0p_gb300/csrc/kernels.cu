@@ -612,6 +612,8 @@ __global__ void __launch_bounds__(kTraceLeafThreads) air_trace_leaves_kernel(
 // 16t + 15, with one batch inversion of their sixteen (x - w_last) (one
 // field inversion per sixteen rows instead of eight). With 16 cosets, the
 // warp's loads of one row index r read 32 consecutive q of coset r.
+// kLinked: B is derived from A (lde_b is null), decided once per launch.
+template <bool kLinked>
 __global__ void __launch_bounds__(kTraceLeafThreads) air_trace_leaves2_kernel(
     const uint32_t* __restrict__ lde_a, const uint32_t* __restrict__ cb, uint32_t w_last_m,
     uint32_t* __restrict__ leaves, uint32_t* __restrict__ tinv, uint32_t logN, uint32_t logB,
@@ -646,8 +648,10 @@ __global__ void __launch_bounds__(kTraceLeafThreads) air_trace_leaves2_kernel(
       const uint32_t k = 16u * t + 8u * h + r;
       const uint32_t j = k & ((1u << logB) - 1u), q = k >> logB;
       msg[2 * r] = __ldg(lde_a + ((size_t)j << logN) + q);
-      msg[2 * r + 1] = lde_b ? __ldg(lde_b + ((size_t)j << logN) + q)
-                             : linked_b(lde_a, logN, j, q, __ldg(cb + j), den[8 * h + r]);
+      if constexpr (kLinked)
+        msg[2 * r + 1] = linked_b(lde_a, logN, j, q, __ldg(cb + j), den[8 * h + r]);
+      else
+        msg[2 * r + 1] = __ldg(lde_b + ((size_t)j << logN) + q);
       tinv[((size_t)j << logN) + q] = den[8 * h + r];
     }
     blake3_leaf64(msg, d);
@@ -2481,8 +2485,12 @@ cudaError_t air_trace_leaves(cudaStream_t st, const Tables& tb, const uint32_t* 
                     : subtree_levels(nleaves < kTraceLeafThreads ? nleaves : kTraceLeafThreads, top);
   Stage stg("trace_leaves", st);
   stg.launched();
-  if (nleaves > kFuseMaxLeaves)  // two leaves a thread, no subtree
-    launch_dep(air_trace_leaves2_kernel, dim3(grid_for(nleaves / 2, kTraceLeafThreads), nproofs),
+  if (nleaves > kFuseMaxLeaves && !lde_b)  // two leaves a thread, no subtree
+    launch_dep(air_trace_leaves2_kernel<true>, dim3(grid_for(nleaves / 2, kTraceLeafThreads), nproofs),
+               kTraceLeafThreads, 0, st, lde_a, cb, w_last_m, leaves, tinv, logN, logB, nleaves,
+               tree_stride, lde_b, tb);
+  else if (nleaves > kFuseMaxLeaves)
+    launch_dep(air_trace_leaves2_kernel<false>, dim3(grid_for(nleaves / 2, kTraceLeafThreads), nproofs),
                kTraceLeafThreads, 0, st, lde_a, cb, w_last_m, leaves, tinv, logN, logB, nleaves,
                tree_stride, lde_b, tb);
   else
