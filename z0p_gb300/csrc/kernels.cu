@@ -1029,6 +1029,9 @@ __device__ __forceinline__ void quad_points(const Tables& tb, uint32_t k0, uint3
 // consecutive threads read consecutive LDE rows and leaf P is bit-reversed.
 // The four composition values of layer-0 quad k0 (rows k0 + s quarter), each
 // at its leaf position 4P + brev2(s); `a` already offset to its proof.
+// kParams: the statement and weights come from a (one proof a launch),
+// otherwise from the proof's constant slot.
+template <bool kParams>
 __device__ __forceinline__ void compose_quad(const AirComposeArgs& a, const Tables& tb, uint32_t k0,
                                              uint32_t logm, uint32_t (&leaf)[16]) {
   const uint32_t N = 1u << a.logN, B = 1u << a.logB, quarter = 1u << (logm - 2);
@@ -1052,16 +1055,18 @@ __device__ __forceinline__ void compose_quad(const AirComposeArgs& a, const Tabl
     const uint32_t bv = fadd(avn, mmul(cbj, t0));
     const uint32_t bvn = fadd(avnn, mmul(cbj, tn));
     const uint32_t t2 = mmul(fsub_lazy(bvn, fadd(av, bv)), zt);
-    const ProofConsts& pc = g_consts[a.slot];
-    const uint32_t ba = mmul(fsub_lazy(av, pc.a0), tm);
-    const uint32_t bb = mmul(fsub_lazy(bv, pc.b0), tm);
-    const uint32_t bo = mmul(fsub_lazy(bv, pc.b_last), t0);
+    const uint32_t a0 = kParams ? a.a0 : g_consts[a.slot].a0;
+    const uint32_t b0 = kParams ? a.b0 : g_consts[a.slot].b0;
+    const uint32_t b_last = kParams ? a.b_last : g_consts[a.slot].b_last;
+    const uint32_t ba = mmul(fsub_lazy(av, a0), tm);
+    const uint32_t bb = mmul(fsub_lazy(bv, b0), tm);
+    const uint32_t bo = mmul(fsub_lazy(bv, b_last), t0);
     const int t = (s == 1) ? 2 : (s == 2) ? 1 : s;  // position 4P + brev2(s)
 #pragma unroll
     for (int c = 0; c < 4; c++) {
-      leaf[4 * t + c] = fadd(mdot4(t2, pc.alpha[c][1], ba, pc.alpha[c][2], bb, pc.alpha[c][3], bo,
-                                   pc.alpha[c][4]),
-                             pc.kc[c]);
+      const uint32_t* al = kParams ? a.alpha[c] : g_consts[a.slot].alpha[c];
+      const uint32_t kc = kParams ? a.kc[c] : g_consts[a.slot].kc[c];
+      leaf[4 * t + c] = fadd(mdot4(t2, al[1], ba, al[2], bb, al[3], bo, al[4]), kc);
     }
   }
 }
@@ -1086,7 +1091,7 @@ __device__ __forceinline__ void store_leaf_values(const AirComposeArgs& a, uint3
     dst[t] = make_uint4(leaf[4 * t], leaf[4 * t + 1], leaf[4 * t + 2], leaf[4 * t + 3]);
 }
 
-template <bool kFused>
+template <bool kFused, bool kParams>
 __global__ void __launch_bounds__(kThreads) air_compose_leaves_kernel(AirComposeArgs a, Tables tb) {
   pdl_wait();
   // >= 2 * 9 * (kFuseMaxLeaves / 256) roots when fused
@@ -1114,7 +1119,7 @@ __global__ void __launch_bounds__(kThreads) air_compose_leaves_kernel(AirCompose
       P = brev_bits(k0, logm - 2);
     }
     uint32_t leaf[16];
-    compose_quad(a, tb, k0, logm, leaf);
+    compose_quad<kParams>(a, tb, k0, logm, leaf);
     store_leaf_values(a, P, leaf);
     blake3_leaf64(leaf, d);
     store_digest(a.leaves + 8 * (size_t)P, d);
@@ -2613,10 +2618,15 @@ cudaError_t air_compose_leaves(cudaStream_t st, const Tables& tb, const AirCompo
   if (levels) *levels = f.counter ? f.top : 0;
   Stage stg("air_compose_leaves", st);
   stg.launched();
-  if (f.counter)
-    launch_dep(air_compose_leaves_kernel<true>, dim3(grid_for(quarter), nproofs), kThreads, 0, st, f, tb);
+  const bool params = nproofs == 1;  // one proof: the weights travel as kernel parameters
+  if (f.counter && params)
+    launch_dep(air_compose_leaves_kernel<true, true>, dim3(grid_for(quarter), nproofs), kThreads, 0, st, f, tb);
+  else if (f.counter)
+    launch_dep(air_compose_leaves_kernel<true, false>, dim3(grid_for(quarter), nproofs), kThreads, 0, st, f, tb);
+  else if (params)
+    launch_dep(air_compose_leaves_kernel<false, true>, dim3(grid_for(quarter), nproofs), kThreads, 0, st, f, tb);
   else
-    launch_dep(air_compose_leaves_kernel<false>, dim3(grid_for(quarter), nproofs), kThreads, 0, st, f, tb);
+    launch_dep(air_compose_leaves_kernel<false, false>, dim3(grid_for(quarter), nproofs), kThreads, 0, st, f, tb);
   return cudaGetLastError();
 }
 

@@ -104,6 +104,12 @@ struct AirComposeArgs {
   uint32_t top = 0;
   uint32_t* cap = nullptr;
   uint64_t cap_stride = 0;
+  // A launch of one proof reads its statement and weights from here (kernel
+  // parameters, fixed offsets) rather than from its constant slot, which is
+  // indexed at run time; groups read the slots.
+  uint32_t a0 = 0, b0 = 0, b_last = 0;
+  uint32_t kc[4] = {};
+  uint32_t alpha[4][5] = {};
 };
 
 struct RangeComposeArgs {

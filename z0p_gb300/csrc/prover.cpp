@@ -2071,6 +2071,12 @@ int air_prove(z0p_gpu_ctx* c, const AirTask* tasks, uint32_t K) {
   ca.layer_stride = fb.val_stride;
   ca.tree_stride = fb.tree_stride;
   CK(push_consts(c, K));
+  if (K == 1) {  // one proof: its statement and weights as kernel parameters
+    const ProofConsts& p0 = c->consts[0];
+    ca.a0 = p0.a0; ca.b0 = p0.b0; ca.b_last = p0.b_last;
+    std::memcpy(ca.kc, p0.kc, sizeof ca.kc);
+    std::memcpy(ca.alpha, p0.alpha, sizeof ca.alpha);
+  }
   ca.counter = merkle_counter(c);  // small layer-0 trees are finished inside the launch
   ca.top = s.depth[0] - s.drop[0];
   ca.cap = hio_dev<uint32_t>(c, h.fri_cap[0]);
