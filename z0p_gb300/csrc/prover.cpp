@@ -233,7 +233,7 @@ void arm_pow(z0p_gpu_ctx* c, size_t off, uint32_t K) {
   __atomic_thread_fence(__ATOMIC_SEQ_CST);
 }
 
-cudaError_t wait_pow(z0p_gpu_ctx* c, size_t off, uint32_t K, cudaEvent_t upto) {
+cudaError_t wait_pow(z0p_gpu_ctx* c, size_t off, uint32_t K, cudaEvent_t upto = nullptr) {
   c->syncs++;
   const uint64_t t0 = now_ns();
   cudaError_t e = cudaSuccess;
@@ -242,7 +242,7 @@ cudaError_t wait_pow(z0p_gpu_ctx* c, size_t off, uint32_t K, cudaEvent_t upto) {
     while (k < K && *reinterpret_cast<const volatile uint64_t*>(c->hio + off + 16 * k) != kPowSentinel) k++;
     if (k == K) break;
     if ((pass & 63u) == 63u) {
-      e = cudaEventQuery(upto);
+      e = upto ? cudaEventQuery(upto) : cudaStreamQuery(c->stream);
       if (e != cudaErrorNotReady) break;
       e = cudaSuccess;
     }
@@ -898,8 +898,9 @@ int run_fri_open(z0p_gpu_ctx* c, const FriShape& s, const FriParams& fp, Transcr
       set_head(heads + kPowHeadWords * k, head.data(), head.size());
     }
     c->h2d += 4ull * kPowHeadWords * K;
+    arm_pow(c, h.grind, K);
     CK(queue_grind(c, fp, hio_dev<uint32_t>(c, h.heads), h.grind, K));
-    CK(sync(c, "grind"));
+    CK(wait_pow(c, h.grind, K));
     for (uint32_t k = 0; k < K; k++) {
       RC(check_grind(c, h.grind, k, &outs[k].nonce));
       uint8_t nb[8];
@@ -1658,8 +1659,9 @@ int const_fri(z0p_gpu_ctx* c, const FriShape& s, const FriParams& fp, uint64_t p
       set_head(heads + kPowHeadWords * k, head.data(), head.size());
     }
     c->h2d += 4ull * kPowHeadWords * K;
+    arm_pow(c, 0, K);
     CK(queue_grind(c, fp, hio_dev<uint32_t>(c, heads_at), 0, K));
-    CK(sync(c, "grind"));
+    CK(wait_pow(c, 0, K));
     for (uint32_t k = 0; k < K; k++) {
       RC(check_grind(c, 0, k, &fr[k].fo.nonce));
       uint8_t nb[8];
