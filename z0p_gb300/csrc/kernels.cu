@@ -558,6 +558,7 @@ __device__ __forceinline__ void cta_subtree(const uint32_t d[8], uint32_t* buf, 
 // eight (x - w_last) inverses per thread in one batch, also stored coset-major
 // in tinv for the composition.
 constexpr uint32_t kTraceLeafThreads = 256;
+template <bool kLinked>  // B derived from A (lde_b null), decided once per launch
 __global__ void __launch_bounds__(kTraceLeafThreads) air_trace_leaves_kernel(
     const uint32_t* __restrict__ lde_a, const uint32_t* __restrict__ cb, uint32_t w_last_m,
     uint32_t* __restrict__ leaves, uint32_t* __restrict__ tinv, uint32_t logN, uint32_t logB,
@@ -596,8 +597,10 @@ __global__ void __launch_bounds__(kTraceLeafThreads) air_trace_leaves_kernel(
     uint32_t k = 8u * L + r;
     uint32_t j = k & ((1u << logB) - 1u), q = k >> logB;
     m[2 * r] = __ldg(lde_a + ((size_t)j << logN) + q);
-    m[2 * r + 1] = lde_b ? __ldg(lde_b + ((size_t)j << logN) + q)
-                         : linked_b(lde_a, logN, j, q, __ldg(cb + j), den[r]);
+    if constexpr (kLinked)
+      m[2 * r + 1] = linked_b(lde_a, logN, j, q, __ldg(cb + j), den[r]);
+    else
+      m[2 * r + 1] = __ldg(lde_b + ((size_t)j << logN) + q);
     tinv[((size_t)j << logN) + q] = den[r];
   }
   blake3_leaf64(m, d);
@@ -2498,8 +2501,12 @@ cudaError_t air_trace_leaves(cudaStream_t st, const Tables& tb, const uint32_t* 
     launch_dep(air_trace_leaves2_kernel<false>, dim3(grid_for(nleaves / 2, kTraceLeafThreads), nproofs),
                kTraceLeafThreads, 0, st, lde_a, cb, w_last_m, leaves, tinv, logN, logB, nleaves,
                tree_stride, lde_b, tb);
+  else if (!lde_b)
+    launch_dep(air_trace_leaves_kernel<true>, dim3(grid_for(nleaves, kTraceLeafThreads), nproofs),
+               kTraceLeafThreads, 0, st, lde_a, cb, w_last_m, leaves, tinv, logN, logB, nleaves, top,
+               cap, counter, tree_stride, cap_stride, lde_b, tb);
   else
-    launch_dep(air_trace_leaves_kernel, dim3(grid_for(nleaves, kTraceLeafThreads), nproofs),
+    launch_dep(air_trace_leaves_kernel<false>, dim3(grid_for(nleaves, kTraceLeafThreads), nproofs),
                kTraceLeafThreads, 0, st, lde_a, cb, w_last_m, leaves, tinv, logN, logB, nleaves, top,
                cap, counter, tree_stride, cap_stride, lde_b, tb);
   return cudaGetLastError();
