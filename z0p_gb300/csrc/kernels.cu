@@ -2146,8 +2146,8 @@ cudaError_t fib_trace(cudaStream_t st, uint32_t* col_a, uint32_t* col_b, uint32_
   const uint32_t extra = zinv ? (uint32_t)grid_for(1ull << zinv->logB) : 0u;
   Stage stg("trace", st);
   stg.launched();
-  launch_dep(fib_trace_kernel, dim3(trace_ctas + extra, nproofs), kThreads, 0, st,
-      col_a, col_b, n, slot, fm, per_lane, trace_ctas, z, tb ? *tb : Tables{});
+  launch_dep(fib_trace_kernel, dim3(trace_ctas + extra, nproofs), kThreads, 0, st, col_a, col_b, n,
+             slot, fm, per_lane, trace_ctas, z, tb ? *tb : Tables{});
   return cudaGetLastError();
 }
 
@@ -2155,8 +2155,8 @@ cudaError_t fill_constant_columns(cudaStream_t st, uint32_t* cols, uint32_t n, u
                                   const uint32_t* d_values, uint32_t nproofs) {
   Stage stg("fill_columns", st);
   stg.launched();
-  launch_dep(fill_columns_kernel, dim3(grid_for((uint64_t)n * ncols), nproofs), kThreads, 0, st, cols, n, ncols,
-                                                                                       d_values);
+  launch_dep(fill_columns_kernel, dim3(grid_for((uint64_t)n * ncols), nproofs), kThreads, 0, st,
+             cols, n, ncols, d_values);
   return cudaGetLastError();
 }
 
@@ -2494,21 +2494,21 @@ cudaError_t air_trace_leaves(cudaStream_t st, const Tables& tb, const uint32_t* 
   Stage stg("trace_leaves", st);
   stg.launched();
   if (nleaves > kFuseMaxLeaves && !lde_b)  // two leaves a thread, no subtree
-    launch_dep(air_trace_leaves2_kernel<true>, dim3(grid_for(nleaves / 2, kTraceLeafThreads), nproofs),
-               kTraceLeafThreads, 0, st, lde_a, cb, w_last_m, leaves, tinv, logN, logB, nleaves,
-               tree_stride, lde_b, tb);
+    launch_dep(air_trace_leaves2_kernel<true>,
+               dim3(grid_for(nleaves / 2, kTraceLeafThreads), nproofs), kTraceLeafThreads, 0, st,
+               lde_a, cb, w_last_m, leaves, tinv, logN, logB, nleaves, tree_stride, lde_b, tb);
   else if (nleaves > kFuseMaxLeaves)
-    launch_dep(air_trace_leaves2_kernel<false>, dim3(grid_for(nleaves / 2, kTraceLeafThreads), nproofs),
-               kTraceLeafThreads, 0, st, lde_a, cb, w_last_m, leaves, tinv, logN, logB, nleaves,
-               tree_stride, lde_b, tb);
+    launch_dep(air_trace_leaves2_kernel<false>,
+               dim3(grid_for(nleaves / 2, kTraceLeafThreads), nproofs), kTraceLeafThreads, 0, st,
+               lde_a, cb, w_last_m, leaves, tinv, logN, logB, nleaves, tree_stride, lde_b, tb);
   else if (!lde_b)
     launch_dep(air_trace_leaves_kernel<true>, dim3(grid_for(nleaves, kTraceLeafThreads), nproofs),
-               kTraceLeafThreads, 0, st, lde_a, cb, w_last_m, leaves, tinv, logN, logB, nleaves, top,
-               cap, counter, tree_stride, cap_stride, lde_b, tb);
+               kTraceLeafThreads, 0, st, lde_a, cb, w_last_m, leaves, tinv, logN, logB, nleaves,
+               top, cap, counter, tree_stride, cap_stride, lde_b, tb);
   else
     launch_dep(air_trace_leaves_kernel<false>, dim3(grid_for(nleaves, kTraceLeafThreads), nproofs),
-               kTraceLeafThreads, 0, st, lde_a, cb, w_last_m, leaves, tinv, logN, logB, nleaves, top,
-               cap, counter, tree_stride, cap_stride, lde_b, tb);
+               kTraceLeafThreads, 0, st, lde_a, cb, w_last_m, leaves, tinv, logN, logB, nleaves,
+               top, cap, counter, tree_stride, cap_stride, lde_b, tb);
   return cudaGetLastError();
 }
 
@@ -2529,8 +2529,11 @@ cudaError_t fold_segment(cudaStream_t st, const Tables& tb, const uint32_t* cols
   Stage stg("fold_segment", st);
   stg.launched();
   switch (logN) {
-#define Z0P_SEG(Lv) \
-  case Lv: launch_dep(fold_segment_kernel<Lv>, 1, m, smem, st, cols, bad, lde, tree, cap, logB, top, ninv_m, tb); break;
+#define Z0P_SEG(Lv)                                                                              \
+  case Lv:                                                                                         \
+    launch_dep(fold_segment_kernel<Lv>, 1, m, smem, st, cols, bad, lde, tree, cap, logB, top,     \
+               ninv_m, tb);                                                                      \
+    break;
     Z0P_SEG(1) Z0P_SEG(2) Z0P_SEG(3) Z0P_SEG(4) Z0P_SEG(5) Z0P_SEG(6) Z0P_SEG(7) Z0P_SEG(8)
 #undef Z0P_SEG
     default: return cudaErrorInvalidValue;
@@ -2550,13 +2553,11 @@ cudaError_t range_trace_leaves(cudaStream_t st, const uint32_t* lde, uint32_t* l
   stg.launched();
   const dim3 grid(grid_for(m), nproofs);
   if (fused)
-    launch_dep(range_trace_leaves_kernel<true>, grid, kThreads, 0, st, lde, leaves, logN, logB, ncols,
-                                                               tree_stride, counter, top, cap,
-                                                               cap_stride);
+    launch_dep(range_trace_leaves_kernel<true>, grid, kThreads, 0, st, lde, leaves, logN, logB,
+               ncols, tree_stride, counter, top, cap, cap_stride);
   else
-    launch_dep(range_trace_leaves_kernel<false>, grid, kThreads, 0, st, lde, leaves, logN, logB, ncols,
-                                                                tree_stride, nullptr, 0, nullptr,
-                                                                0);
+    launch_dep(range_trace_leaves_kernel<false>, grid, kThreads, 0, st, lde, leaves, logN, logB,
+               ncols, tree_stride, nullptr, 0, nullptr, 0);
   return cudaGetLastError();
 }
 
@@ -2568,8 +2569,8 @@ cudaError_t merkle_build(cudaStream_t st, uint32_t* tree, uint64_t leaves, uint3
   if (top == 0) {  // the cap is the leaf level itself
     if (!cap) return cudaSuccess;
     stg.launched();
-    launch_dep(copy_words_kernel, dim3(grid_for(8 * leaves), nproofs), kThreads, 0, st, tree, cap, 8 * leaves,
-                                                                               stride, cap_stride);
+    launch_dep(copy_words_kernel, dim3(grid_for(8 * leaves), nproofs), kThreads, 0, st, tree, cap,
+               8 * leaves, stride, cap_stride);
     return cudaGetLastError();
   }
   // Levels with more than 2^16 nodes fill the GPU on their own: one launch
@@ -2586,8 +2587,8 @@ cudaError_t merkle_build(cudaStream_t st, uint32_t* tree, uint64_t leaves, uint3
     uint32_t* mid = tree + 8 * (2 * leaves - 2 * (leaves >> (level + 1)));
     uint32_t* next = tree + 8 * (2 * leaves - 2 * (leaves >> (level + 2)));
     stg.launched();
-    launch_dep(merkle_level2_kernel, dim3(grid_for(cnt), nproofs), kThreads, 0, st,
-        prev, mid, next, cnt, level + 2 == top ? cap : nullptr, stride, cap_stride);
+    launch_dep(merkle_level2_kernel, dim3(grid_for(cnt), nproofs), kThreads, 0, st, prev, mid, next,
+               cnt, level + 2 == top ? cap : nullptr, stride, cap_stride);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     level += 2;
@@ -2597,8 +2598,8 @@ cudaError_t merkle_build(cudaStream_t st, uint32_t* tree, uint64_t leaves, uint3
     const uint32_t* prev = tree + 8 * (2 * leaves - 2 * (leaves >> level));
     uint32_t* next = tree + 8 * (2 * leaves - 2 * (leaves >> (level + 1)));
     stg.launched();
-    launch_dep(merkle_level_kernel, dim3(grid_for(cnt), nproofs), kThreads, 0, st,
-        prev, next, cnt, level + 1 == top ? cap : nullptr, stride, cap_stride);
+    launch_dep(merkle_level_kernel, dim3(grid_for(cnt), nproofs), kThreads, 0, st, prev, next, cnt,
+               level + 1 == top ? cap : nullptr, stride, cap_stride);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     level++;
@@ -2608,8 +2609,8 @@ cudaError_t merkle_build(cudaStream_t st, uint32_t* tree, uint64_t leaves, uint3
   const uint64_t per_cta_children = 2ull << (lsub - level - 1);  // level-l0 nodes per CTA
   const uint64_t blocks = ((leaves >> level) + per_cta_children - 1) / per_cta_children;
   stg.launched();
-  launch_dep(merkle_top_kernel, dim3((unsigned)blocks, nproofs), kTopThreads, 0, st,
-      tree, leaves, level, top, counter, cap, stride, cap_stride);
+  launch_dep(merkle_top_kernel, dim3((unsigned)blocks, nproofs), kTopThreads, 0, st, tree, leaves,
+             level, top, counter, cap, stride, cap_stride);
   return cudaGetLastError();
 }
 
@@ -2627,13 +2628,17 @@ cudaError_t air_compose_leaves(cudaStream_t st, const Tables& tb, const AirCompo
   stg.launched();
   const bool params = nproofs == 1;  // one proof: the weights travel as kernel parameters
   if (f.counter && params)
-    launch_dep(air_compose_leaves_kernel<true, true>, dim3(grid_for(quarter), nproofs), kThreads, 0, st, f, tb);
+    launch_dep(air_compose_leaves_kernel<true, true>, dim3(grid_for(quarter), nproofs), kThreads, 0,
+               st, f, tb);
   else if (f.counter)
-    launch_dep(air_compose_leaves_kernel<true, false>, dim3(grid_for(quarter), nproofs), kThreads, 0, st, f, tb);
+    launch_dep(air_compose_leaves_kernel<true, false>, dim3(grid_for(quarter), nproofs), kThreads,
+               0, st, f, tb);
   else if (params)
-    launch_dep(air_compose_leaves_kernel<false, true>, dim3(grid_for(quarter), nproofs), kThreads, 0, st, f, tb);
+    launch_dep(air_compose_leaves_kernel<false, true>, dim3(grid_for(quarter), nproofs), kThreads,
+               0, st, f, tb);
   else
-    launch_dep(air_compose_leaves_kernel<false, false>, dim3(grid_for(quarter), nproofs), kThreads, 0, st, f, tb);
+    launch_dep(air_compose_leaves_kernel<false, false>, dim3(grid_for(quarter), nproofs), kThreads,
+               0, st, f, tb);
   return cudaGetLastError();
 }
 
@@ -2697,12 +2702,11 @@ cudaError_t layer_leaves(cudaStream_t st, const uint32_t* values, uint64_t len, 
   Stage stg("layer_leaves", st);
   stg.launched();
   if (len % 4 == 0) {
-    launch_dep(leaf64_kernel, dim3(grid_for(len / 4), nproofs), kThreads, 0, st, values, leaves, len / 4,
-                                                                        len / 4, in_stride,
-                                                                        out_stride);
+    launch_dep(leaf64_kernel, dim3(grid_for(len / 4), nproofs), kThreads, 0, st, values, leaves,
+               len / 4, len / 4, in_stride, out_stride);
   } else {
-    launch_dep(leaf16_kernel, dim3(grid_for(len), nproofs), kThreads, 0, st, values, leaves, len, in_stride,
-                                                                    out_stride);
+    launch_dep(leaf16_kernel, dim3(grid_for(len), nproofs), kThreads, 0, st, values, leaves, len,
+               in_stride, out_stride);
   }
   return cudaGetLastError();
 }
@@ -2780,8 +2784,8 @@ cudaError_t mask_pad(cudaStream_t st, const Tables& tb, const uint32_t* coeffs, 
                      uint32_t* out, uint32_t n, uint32_t n_rand, uint32_t padded, uint32_t ncols) {
   Stage stg("mask_pad", st);
   stg.launched();
-  launch_dep(mask_pad_kernel, dim3(grid_for(padded), ncols), kThreads, 0, st, coeffs, r, out, n, n_rand, padded,
-                                                                      tb);
+  launch_dep(mask_pad_kernel, dim3(grid_for(padded), ncols), kThreads, 0, st, coeffs, r, out, n,
+             n_rand, padded, tb);
   return cudaGetLastError();
 }
 
@@ -2796,8 +2800,8 @@ cudaError_t air_compose_general(cudaStream_t st, const Tables& tb, const AirComp
                                 const uint32_t* lde_b, uint32_t r) {
   Stage stg("air_compose_leaves", st);
   stg.launched();
-  launch_dep(air_compose_general_kernel, grid_for(1ull << (a.logN + a.logB - 2)), kThreads, 0, st, a, lde_b, r,
-                                                                                        tb);
+  launch_dep(air_compose_general_kernel,
+             grid_for(1ull << (a.logN + a.logB - 2)), kThreads, 0, st, a, lde_b, r, tb);
   return cudaGetLastError();
 }
 
@@ -2805,7 +2809,8 @@ cudaError_t gamma_scale(cudaStream_t st, const Tables& tb, const uint32_t* in, u
                         uint32_t n, uint32_t ext, unsigned int* bad) {
   Stage stg("fri_input", st);
   stg.launched();
-  launch_dep(gamma_scale_kernel, dim3(grid_for(n), ext ? 4 : 1), kThreads, 0, st, in, out, n, ext, bad, tb);
+  launch_dep(gamma_scale_kernel, dim3(grid_for(n), ext ? 4 : 1), kThreads, 0, st, in, out, n, ext,
+             bad, tb);
   return cudaGetLastError();
 }
 
@@ -2834,8 +2839,8 @@ cudaError_t row_inverses(cudaStream_t st, const Tables& tb, uint32_t* tinv, uint
   if (logN + logB < 3) return cudaErrorInvalidValue;
   Stage stg("row_inverses", st);
   stg.launched();
-  launch_dep(row_inverses_kernel, grid_for(1ull << (logN + logB - 3)), kThreads, 0, st, tinv, w_last_m, logN,
-                                                                             logB, tb);
+  launch_dep(row_inverses_kernel,
+             grid_for(1ull << (logN + logB - 3)), kThreads, 0, st, tinv, w_last_m, logN, logB, tb);
   return cudaGetLastError();
 }
 
@@ -2861,8 +2866,8 @@ cudaError_t fold_openings(cudaStream_t st, const FoldStepDev* steps, uint32_t ns
                           uint32_t path_steps, uint32_t* out, uint32_t stride) {
   Stage stg("fold_openings", st);
   stg.launched();
-  launch_dep(fold_openings_kernel, dim3(nq, nsteps), 64, 0, st, steps, leaves, nq, logN, logB, path_steps,
-                                                       out, stride);
+  launch_dep(fold_openings_kernel, dim3(nq, nsteps), 64, 0, st, steps, leaves, nq, logN, logB,
+             path_steps, out, stride);
   return cudaGetLastError();
 }
 
@@ -2890,7 +2895,8 @@ cudaError_t coset_to_natural(cudaStream_t st, const uint32_t* in, uint32_t* out,
   if (qt > 0x7fffffffull) return cudaErrorInvalidValue;
   Stage stg("coset_to_natural", st);
   stg.launched();
-  launch_dep(coset_to_natural_kernel, dim3((unsigned)qt, jt, (unsigned)batch), 256, 0, st, in, out, logN, logB);
+  launch_dep(coset_to_natural_kernel, dim3((unsigned)qt, jt, (unsigned)batch), 256, 0, st, in, out,
+             logN, logB);
   return cudaGetLastError();
 }
 
