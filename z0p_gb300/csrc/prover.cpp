@@ -213,84 +213,24 @@ cudaError_t sync(z0p_gpu_ctx* c, const char* site = "other", cudaEvent_t upto = 
   return e;
 }
 
-// A Merkle cap the device writes into the mapped buffer can be read as soon
-// as its last word lands, before the kernel that wrote it has retired and
-// the stream's completion has reached the host. arm_cap fills the cap's
-// region with kCapSentinel; it must run before the kernels that write the
-// cap are queued (after them, it could overwrite digests already written).
-// wait_cap then spins until no word of the region holds the sentinel,
-// querying the event (or the stream) every 64 passes, so that a launch that
-// failed, or a digest word equal to the sentinel (one chance in 2^32 a
-// word), ends the wait at the work's completion instead.
-constexpr uint32_t kCapSentinel = 0x6A09E667u;
-
-// The same for the PoW results (nonce word, then the cap flag, per proof):
-// a nonce word is below 2^40 or all ones, never kPowSentinel.
-constexpr uint64_t kPowSentinel = ~1ull;
-
-void arm_pow(z0p_gpu_ctx* c, size_t off, uint32_t K) {
-  for (uint32_t k = 0; k < K; k++) std::memcpy(c->hio + off + 16 * k, &kPowSentinel, 8);
-  __atomic_thread_fence(__ATOMIC_SEQ_CST);
-}
-
-cudaError_t wait_pow(z0p_gpu_ctx* c, size_t off, uint32_t K, cudaEvent_t upto = nullptr) {
+// Spins until done() holds, querying `upto` (or the stream) every 64
+// passes so that a launch that failed, or a word that legitimately equals
+// its sentinel, ends the wait at the work's completion; accounted like sync.
+template <class Done>
+cudaError_t wait_mapped(z0p_gpu_ctx* c, const char* site, cudaEvent_t upto, Done done) {
   c->syncs++;
   const uint64_t t0 = now_ns();
   cudaError_t e = cudaSuccess;
-  uint32_t k = 0;
-  for (uint32_t pass = 0;; pass++) {
-    while (k < K && *reinterpret_cast<const volatile uint64_t*>(c->hio + off + 16 * k) != kPowSentinel) k++;
-    if (k == K) break;
-    if ((pass & 63u) == 63u) {
-      e = upto ? cudaEventQuery(upto) : cudaStreamQuery(c->stream);
-      if (e != cudaErrorNotReady) break;
-      e = cudaSuccess;
-    }
+  for (uint32_t pass = 0; !done(); pass++) {
+    if ((pass & 63u) != 63u) continue;
+    e = upto ? cudaEventQuery(upto) : cudaStreamQuery(c->stream);
+    if (e != cudaErrorNotReady) break;
+    e = cudaSuccess;
   }
   __atomic_thread_fence(__ATOMIC_ACQUIRE);
   const uint64_t t1 = now_ns();
   if (e == cudaSuccess && c->fault && *reinterpret_cast<volatile unsigned int*>(c->fault)) {
-    *c->fault = 0u;
-    e = cudaErrorLaunchTimeout;
-  }
-  c->sync_ns += t1 - t0;
-  if (c->profiling) {
-    HostSite& hs = c->sites["grind"];
-    hs.calls++;
-    hs.wait_ns += t1 - t0;
-    if (c->last_sync_ns) hs.before_ns += t0 - c->last_sync_ns;
-  }
-  c->last_sync_ns = t1;
-  return e;
-}
-
-void arm_cap(z0p_gpu_ctx* c, size_t off, size_t bytes) {
-  uint32_t* w = reinterpret_cast<uint32_t*>(c->hio + off);
-  for (size_t i = 0; i < bytes / 4; i++) w[i] = kCapSentinel;
-  __atomic_thread_fence(__ATOMIC_SEQ_CST);
-}
-
-cudaError_t wait_cap(z0p_gpu_ctx* c, const char* site, size_t off, size_t bytes,
-                     cudaEvent_t upto = nullptr) {
-  c->syncs++;
-  const uint64_t t0 = now_ns();
-  const volatile uint32_t* w = reinterpret_cast<const volatile uint32_t*>(c->hio + off);
-  const size_t n = bytes / 4;
-  size_t i = 0;  // words before i are written (each is written once)
-  cudaError_t e = cudaSuccess;
-  for (uint32_t pass = 0;; pass++) {
-    while (i < n && w[i] != kCapSentinel) i++;
-    if (i == n) break;
-    if ((pass & 63u) == 63u) {
-      e = upto ? cudaEventQuery(upto) : cudaStreamQuery(c->stream);
-      if (e != cudaErrorNotReady) break;
-      e = cudaSuccess;
-    }
-  }
-  __atomic_thread_fence(__ATOMIC_ACQUIRE);
-  const uint64_t t1 = now_ns();
-  if (e == cudaSuccess && c->fault && *reinterpret_cast<volatile unsigned int*>(c->fault)) {
-    *c->fault = 0u;
+    *c->fault = 0u;  // reported once; the context stays usable
     e = cudaErrorLaunchTimeout;
   }
   c->sync_ns += t1 - t0;
@@ -302,6 +242,51 @@ cudaError_t wait_cap(z0p_gpu_ctx* c, const char* site, size_t off, size_t bytes,
   }
   c->last_sync_ns = t1;
   return e;
+}
+
+// A Merkle cap the device writes into the mapped buffer can be read as soon
+// as its last word lands, before the kernel that wrote it has retired and
+// the stream's completion has reached the host. arm_cap fills the cap's
+// region with kCapSentinel; it must run before the kernels that write the
+// cap are queued (after them, it could overwrite digests already written).
+// wait_cap then waits until no word of the region holds the sentinel (a
+// digest word equal to it, one chance in 2^32 a word, only sends the wait
+// on to the work's completion).
+constexpr uint32_t kCapSentinel = 0x6A09E667u;
+
+void arm_cap(z0p_gpu_ctx* c, size_t off, size_t bytes) {
+  uint32_t* w = reinterpret_cast<uint32_t*>(c->hio + off);
+  for (size_t i = 0; i < bytes / 4; i++) w[i] = kCapSentinel;
+  __atomic_thread_fence(__ATOMIC_SEQ_CST);
+}
+
+cudaError_t wait_cap(z0p_gpu_ctx* c, const char* site, size_t off, size_t bytes,
+                     cudaEvent_t upto = nullptr) {
+  const volatile uint32_t* w = reinterpret_cast<const volatile uint32_t*>(c->hio + off);
+  const size_t n = bytes / 4;
+  size_t i = 0;  // words before i are written (each is written once)
+  return wait_mapped(c, site, upto, [&] {
+    while (i < n && w[i] != kCapSentinel) i++;
+    return i == n;
+  });
+}
+
+// The same for the PoW results (per proof the nonce word, then the cap
+// flag, which the search writes first): a nonce word is below 2^40 or all
+// ones, never kPowSentinel.
+constexpr uint64_t kPowSentinel = ~1ull;
+
+void arm_pow(z0p_gpu_ctx* c, size_t off, uint32_t K) {
+  for (uint32_t k = 0; k < K; k++) std::memcpy(c->hio + off + 16 * k, &kPowSentinel, 8);
+  __atomic_thread_fence(__ATOMIC_SEQ_CST);
+}
+
+cudaError_t wait_pow(z0p_gpu_ctx* c, size_t off, uint32_t K, cudaEvent_t upto = nullptr) {
+  uint32_t k = 0;
+  return wait_mapped(c, "grind", upto, [&] {
+    while (k < K && *reinterpret_cast<const volatile uint64_t*>(c->hio + off + 16 * k) != kPowSentinel) k++;
+    return k == K;
+  });
 }
 
 // Workspace comes from one stream-ordered memory pool per device that keeps
