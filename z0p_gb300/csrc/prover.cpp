@@ -1502,70 +1502,8 @@ struct ConstTree {
   CompactTree view() const { return CompactTree{bytes.data(), G, logS}; }
 };
 
-// Few enough hashes for the host: the same digests without a launch and its
-// round trip (a chain of node hashes costs about 1.1 µs a level in one GPU
-// thread, a few tenths of a µs on a host core, against a 10 µs round trip).
-constexpr uint64_t kHostTreeHashes = 24;
-
-// Tree t's digests on the host, in the layout uniform_trees_kernel writes:
-// per seed g its leaf and the logS levels above it (g (logS + 1) ..), then
-// the G roots and the levels combining them.
-void host_const_tree(ConstTree& t) {
-  const uint32_t G = t.G, L = t.logS + 1;
-  t.bytes.assign(32ull * ((uint64_t)G * L + 2 * G - 1), 0);
-  uint8_t* out = t.bytes.data();
-  auto node = [](const uint8_t* l, const uint8_t* r, uint8_t* o) {  // BLAKE3(0x01 || l || r)
-    uint8_t b[65];
-    b[0] = 0x01;
-    std::memcpy(b + 1, l, 32);
-    std::memcpy(b + 33, r, 32);
-    blake3(b, 65, o);
-  };
-  std::vector<uint8_t> top(32ull * (2 * G - 1));
-  for (uint32_t g = 0; g < G; g++) {
-    const uint32_t* sd = t.seeds.data() + (size_t)g * t.words;
-    uint8_t* o = out + 32ull * ((uint64_t)g * L);
-    if (!t.row) {  // a 64-byte block leaf (16 words)
-      uint8_t b[64];
-      for (int i = 0; i < 16; i++)
-        for (int k = 0; k < 4; k++) b[4 * i + k] = (uint8_t)(sd[i] >> (8 * k));
-      blake3(b, 64, o);
-    } else {  // BLAKE3(0x00 || row)
-      std::vector<uint8_t> b(1 + 4ull * t.words);
-      b[0] = 0x00;
-      for (uint32_t i = 0; i < t.words; i++)
-        for (int k = 0; k < 4; k++) b[1 + 4 * i + k] = (uint8_t)(sd[i] >> (8 * k));
-      blake3(b.data(), b.size(), o);
-    }
-    for (uint32_t l = 1; l < L; l++) node(o + 32 * (l - 1), o + 32 * (l - 1), o + 32 * l);
-    std::memcpy(top.data() + 32ull * g, o + 32ull * (L - 1), 32);
-  }
-  uint8_t* dst = out + 32ull * ((uint64_t)G * L);
-  std::memcpy(dst, top.data(), 32ull * G);
-  for (uint32_t off = 0, cnt = G; cnt > 1; off += cnt, cnt >>= 1)
-    for (uint32_t i = 0; i < cnt / 2; i++) {
-      uint8_t* n = top.data() + 32ull * (off + cnt + i);
-      node(top.data() + 32ull * (off + 2 * i), top.data() + 32ull * (off + 2 * i + 1), n);
-      std::memcpy(dst + 32ull * (off + cnt + i), n, 32);
-    }
-}
-
-// Builds every tree in one launch through the mapped buffer and waits, or
-// on the host when they need few hashes.
+// Builds every tree in one launch through the mapped buffer and waits.
 int build_const_trees(z0p_gpu_ctx* c, std::vector<ConstTree*>& trees, const char* site) {
-  {
-    uint64_t hashes = 0;
-    bool shapes_ok = true;
-    for (const ConstTree* t : trees) {
-      shapes_ok = shapes_ok && t->G && t->G <= 512 && !(t->G & (t->G - 1)) &&
-                  t->seeds.size() == (size_t)t->G * t->words && (!t->row || t->words <= 31);
-      hashes += (uint64_t)t->G * (t->logS + 1) + t->G - 1;
-    }
-    if (shapes_ok && hashes <= kHostTreeHashes) {
-      for (ConstTree* t : trees) host_const_tree(*t);
-      return Z0P_OK;
-    }
-  }
   size_t at = 0;
   auto take = [&](size_t bytes) {
     size_t r = at;
