@@ -246,15 +246,30 @@ __device__ __forceinline__ uint32_t rotr8(uint32_t x) { return __byte_perm(x, 0,
 __device__ __forceinline__ uint32_t rotr12(uint32_t x) { return __funnelshift_r(x, x, 12); }
 __device__ __forceinline__ uint32_t rotr7(uint32_t x) { return __funnelshift_r(x, x, 7); }
 
+// A one the compiler cannot fold, so that x * k_unit + y stays a multiply-add.
+// The G function is bound by the integer ALU pipe (additions, XORs, byte
+// permutes and funnel shifts all issue there). Issuing three of its four
+// additions as multiply-adds by one moves them to the FMA pipe. A GB300
+// probe of 2^20 chained node-hash pairs measured 35.9 -> 38.6 G
+// compressions/s with this mix and identical digests. Moving all four
+// measured 37.5; moving only the c-additions measured 34.8.
+static __constant__ uint32_t k_unit = 1u;
+
+__device__ __forceinline__ uint32_t mad_unit(uint32_t x, uint32_t y) {
+  uint32_t r;
+  asm("mad.lo.u32 %0, %1, %2, %3;" : "=r"(r) : "r"(x), "r"(k_unit), "r"(y));
+  return r;
+}
+
 #define Z0P_G(a, b, c, d, x, y)    \
   do {                             \
-    a = a + b + (x);               \
+    a = mad_unit(b, a + (x));      \
     d = rotr16(d ^ a);             \
     c = c + d;                     \
     b = rotr12(b ^ c);             \
-    a = a + b + (y);               \
+    a = mad_unit(b, a + (y));      \
     d = rotr8(d ^ a);              \
-    c = c + d;                     \
+    c = mad_unit(d, c);            \
     b = rotr7(b ^ c);              \
   } while (0)
 
