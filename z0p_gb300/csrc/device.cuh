@@ -252,7 +252,8 @@ __device__ __forceinline__ uint32_t rotr7(uint32_t x) { return __funnelshift_r(x
 // additions as multiply-adds by one moves them to the FMA pipe. A GB300
 // probe of 2^20 chained node-hash pairs measured 35.9 -> 38.6 G
 // compressions/s with this mix and identical digests. Moving all four
-// measured 37.5; moving only the c-additions measured 34.8.
+// measured 37.5; moving only the c-additions measured 34.8. Z0P_G_ALU keeps
+// every addition on the ALU pipe (the tree-top kernel measured faster so).
 static __constant__ uint32_t k_unit = 1u;
 
 __device__ __forceinline__ uint32_t mad_unit(uint32_t x, uint32_t y) {
@@ -273,8 +274,23 @@ __device__ __forceinline__ uint32_t mad_unit(uint32_t x, uint32_t y) {
     b = rotr7(b ^ c);              \
   } while (0)
 
+#define Z0P_G_ALU(a, b, c, d, x, y) \
+  do {                              \
+    a = a + b + (x);                \
+    d = rotr16(d ^ a);              \
+    c = c + d;                      \
+    b = rotr12(b ^ c);              \
+    a = a + b + (y);                \
+    d = rotr8(d ^ a);               \
+    c = c + d;                      \
+    b = rotr7(b ^ c);               \
+  } while (0)
+
 // out[0..8] = first 8 words of the compression output (the chaining value /
-// root digest). m is consumed (permuted in place).
+// root digest). m is consumed (permuted in place). kMad selects the G step
+// with multiply-adds (true) or all additions on the ALU pipe (false); both
+// compute the same function.
+template <bool kMad = true>
 __device__ __forceinline__ void blake3_compress(const uint32_t cv[8], uint32_t m[16],
                                                 uint32_t counter_lo, uint32_t counter_hi,
                                                 uint32_t block_len, uint32_t flags,
@@ -285,14 +301,25 @@ __device__ __forceinline__ void blake3_compress(const uint32_t cv[8], uint32_t m
   uint32_t s12 = counter_lo, s13 = counter_hi, s14 = block_len, s15 = flags;
 #pragma unroll
   for (int r = 0; r < 7; r++) {
-    Z0P_G(s0, s4, s8, s12, m[0], m[1]);
-    Z0P_G(s1, s5, s9, s13, m[2], m[3]);
-    Z0P_G(s2, s6, s10, s14, m[4], m[5]);
-    Z0P_G(s3, s7, s11, s15, m[6], m[7]);
-    Z0P_G(s0, s5, s10, s15, m[8], m[9]);
-    Z0P_G(s1, s6, s11, s12, m[10], m[11]);
-    Z0P_G(s2, s7, s8, s13, m[12], m[13]);
-    Z0P_G(s3, s4, s9, s14, m[14], m[15]);
+    if (kMad) {
+      Z0P_G(s0, s4, s8, s12, m[0], m[1]);
+      Z0P_G(s1, s5, s9, s13, m[2], m[3]);
+      Z0P_G(s2, s6, s10, s14, m[4], m[5]);
+      Z0P_G(s3, s7, s11, s15, m[6], m[7]);
+      Z0P_G(s0, s5, s10, s15, m[8], m[9]);
+      Z0P_G(s1, s6, s11, s12, m[10], m[11]);
+      Z0P_G(s2, s7, s8, s13, m[12], m[13]);
+      Z0P_G(s3, s4, s9, s14, m[14], m[15]);
+    } else {
+      Z0P_G_ALU(s0, s4, s8, s12, m[0], m[1]);
+      Z0P_G_ALU(s1, s5, s9, s13, m[2], m[3]);
+      Z0P_G_ALU(s2, s6, s10, s14, m[4], m[5]);
+      Z0P_G_ALU(s3, s7, s11, s15, m[6], m[7]);
+      Z0P_G_ALU(s0, s5, s10, s15, m[8], m[9]);
+      Z0P_G_ALU(s1, s6, s11, s12, m[10], m[11]);
+      Z0P_G_ALU(s2, s7, s8, s13, m[12], m[13]);
+      Z0P_G_ALU(s3, s4, s9, s14, m[14], m[15]);
+    }
     if (r < 6) {  // message permutation (src/hash.rs:30)
       uint32_t t0 = m[2], t1 = m[6], t2 = m[3], t3 = m[10], t4 = m[7], t5 = m[0], t6 = m[4],
                t7 = m[13], t8 = m[1], t9 = m[11], t10 = m[12], t11 = m[5], t12 = m[9],
@@ -319,6 +346,7 @@ __device__ __forceinline__ void blake3_leaf64(uint32_t m[16], uint32_t out[8]) {
 }
 
 // BLAKE3(0x01 || l || r): 65 bytes, two compressions (src/hash.rs:417-443).
+template <bool kMad = true>
 __device__ __forceinline__ void blake3_node(const uint32_t l[8], const uint32_t r[8],
                                             uint32_t out[8]) {
   uint32_t m[16];
@@ -330,12 +358,12 @@ __device__ __forceinline__ void blake3_node(const uint32_t l[8], const uint32_t 
   for (int i = 1; i < 8; i++) m[8 + i] = __funnelshift_l(r[i - 1], r[i], 8);
   uint32_t cv[8], mid[8];
   iv_words(cv);
-  blake3_compress(cv, m, 0u, 0u, 64u, kChunkStart, mid);
+  blake3_compress<kMad>(cv, m, 0u, 0u, 64u, kChunkStart, mid);
   uint32_t m2[16];
   m2[0] = r[7] >> 24;
 #pragma unroll
   for (int i = 1; i < 16; i++) m2[i] = 0u;
-  blake3_compress(mid, m2, 0u, 0u, 1u, kChunkEnd | kRoot, out);
+  blake3_compress<kMad>(mid, m2, 0u, 0u, 1u, kChunkEnd | kRoot, out);
 }
 
 // BLAKE3(0x00 || data) for data of `nwords` 32-bit words (<= 25, i.e. at most

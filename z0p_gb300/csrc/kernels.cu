@@ -453,12 +453,13 @@ __device__ __forceinline__ uint64_t level_offset(uint64_t leaves, uint32_t level
 // at most when a thread reads its two children).
 constexpr int kTopStride = 9;
 
+template <bool kMad = true>
 __device__ __forceinline__ void hash_pair_smem(const uint32_t* pair, uint32_t* out_s,
                                                uint32_t* out_g, uint32_t* out_cap) {
   uint32_t a[8], b[8], d[8];
 #pragma unroll
   for (int i = 0; i < 8; i++) { a[i] = pair[i]; b[i] = pair[kTopStride + i]; }
-  blake3_node(a, b, d);
+  blake3_node<kMad>(a, b, d);
 #pragma unroll
   for (int i = 0; i < 8; i++) out_s[i] = d[i];
   store_digest(out_g, d);
@@ -472,6 +473,7 @@ __device__ __forceinline__ void hash_pair_smem(const uint32_t* pair, uint32_t* o
 // shared memory (buf: 2 * 9 * gridDim.x words) and hashes the remaining
 // levels there, each node to the tree and level `top` also to `cap`. It puts
 // the counter back to zero for the next launch. Every thread calls it.
+template <bool kMad = true>
 __device__ __forceinline__ void last_cta_levels(uint32_t* tree, uint64_t leaves, uint32_t lsub,
                                                 uint32_t top, unsigned int* counter,
                                                 uint32_t* cap, uint32_t* buf) {
@@ -499,7 +501,7 @@ __device__ __forceinline__ void last_cta_levels(uint32_t* tree, uint64_t leaves,
     n >>= 1;
     uint32_t* next = tree + 8 * level_offset(leaves, l + 1);
     for (uint64_t i = threadIdx.x; i < n; i += blockDim.x)
-      hash_pair_smem(cur + 2 * kTopStride * i, nxt + kTopStride * i, next + 8 * i,
+      hash_pair_smem<kMad>(cur + 2 * kTopStride * i, nxt + kTopStride * i, next + 8 * i,
                      (cap && l + 1 == top) ? cap + 8 * i : nullptr);
     uint32_t* tmp = cur;
     cur = nxt;
@@ -919,7 +921,9 @@ constexpr int kTopThreads = 256;
 constexpr int kTopMaxRoots = 512;  // level-l0 nodes <= 2^18, 512 per CTA
 
 // `cap` (may be null) receives a copy of level `top`. The CTA that finishes
-// the tree puts `counter` back to zero for the next launch.
+// the tree puts `counter` back to zero for the next launch. Its node hashes
+// keep every G addition on the ALU pipe: with the multiply-add G step this
+// kernel measured about 8% slower on a GB300 (24.5 -> 26.5 us a launch).
 __global__ void __launch_bounds__(kTopThreads) merkle_top_kernel(uint32_t* tree, uint64_t leaves,
                                                                  uint32_t l0, uint32_t top,
                                                                  unsigned int* counter,
@@ -942,7 +946,7 @@ __global__ void __launch_bounds__(kTopThreads) merkle_top_kernel(uint32_t* tree,
     uint32_t a[8], b[8];
     load_digest(prev + 16 * node, a);
     load_digest(prev + 16 * node + 8, b);
-    blake3_node(a, b, d);
+    blake3_node<false>(a, b, d);
     store_digest(tree + 8 * (level_offset(leaves, l0 + 1) + node), d);
     if (cap && l0 + 1 == top) store_digest(cap + 8 * node, d);
 #pragma unroll
@@ -953,7 +957,7 @@ __global__ void __launch_bounds__(kTopThreads) merkle_top_kernel(uint32_t* tree,
     per >>= 1;
     if (threadIdx.x < per) {
       uint64_t n = (uint64_t)blockIdx.x * per + threadIdx.x;
-      hash_pair_smem(sm[cur] + 2 * kTopStride * threadIdx.x, sm[cur ^ 1] + kTopStride * threadIdx.x,
+      hash_pair_smem<false>(sm[cur] + 2 * kTopStride * threadIdx.x, sm[cur ^ 1] + kTopStride * threadIdx.x,
                      tree + 8 * (level_offset(leaves, l + 1) + n),
                      (cap && l + 1 == top) ? cap + 8 * n : nullptr);
     }
@@ -961,7 +965,7 @@ __global__ void __launch_bounds__(kTopThreads) merkle_top_kernel(uint32_t* tree,
     __syncthreads();
   }
   if (lsub == top) return;
-  last_cta_levels(tree, leaves, lsub, top, counter, cap, &sm[0][0]);
+  last_cta_levels<false>(tree, leaves, lsub, top, counter, cap, &sm[0][0]);
 }
 
 // 64-byte leaves (four Ext4 values) of an in-memory FRI layer
