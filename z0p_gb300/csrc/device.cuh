@@ -250,8 +250,8 @@ __device__ __forceinline__ uint32_t rotr7(uint32_t x) { return __funnelshift_r(x
 // The G function is bound by the integer ALU pipe (additions, XORs, byte
 // permutes and funnel shifts all issue there). Issuing three of its four
 // additions as multiply-adds by one moves them to the FMA pipe. A GB300
-// probe of 2^20 chained node-hash pairs measured 35.9 -> 38.6 G
-// compressions/s with this mix and identical digests. Moving all four
+// probe (311,296 threads, each hashing two chains of 64 nodes) measured
+// 35.9 -> 38.6 G compressions/s with this mix and identical digests. Moving all four
 // measured 37.5; moving only the c-additions measured 34.8. Z0P_G_ALU keeps
 // every addition on the ALU pipe (the tree-top kernel measured faster so).
 static __constant__ uint32_t k_unit = 1u;
